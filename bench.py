@@ -1,0 +1,325 @@
+"""Benchmark: warm rows/s and % of HBM peak per query on the 1B-row table (one GB300).
+
+A step runs the query suite of the 1B-row configuration once over a warm, device-resident table:
+  q1 SELECT SUM(amount), MIN(amount), MAX(amount)                  aggregate_global_native
+  q2 SELECT COUNT(*) WHERE flag < 2                                scan_simple (count only)
+  q3 SELECT region, SUM(amount), COUNT(*) GROUP BY region         aggregate_dense_native, 50 groups
+  q4 SELECT amount, COUNT(*), SUM(region) GROUP BY amount         aggregate_dense_native, 10k groups
+  q5 SELECT id, ... WHERE id = k (a random k)                      scan_simple on the id sequence
+value = (queries x rows) / suite time, on the device (CUDA events around the step, inputs larger
+than L2). `e2e` runs the same suite through the C ABI from pinned HOST buffers: every step uploads the
+columns the queries read and reads the results back. `roofline` is the dominant kernel's algorithmic
+bytes per launch over its CUDA-event duration. `cpu_baseline` times the oracle's CPU restatement of
+the reference's operators on a bounded sample with all host cores.
+
+--impl reference times that CPU restatement alone (the reference's own CPU operator path does not
+build on Linux: it is a Win32-only unity build).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "warm rows/s and % HBM peak per query at 1B rows"
+UNIT = "rows/s"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+CPU_SAMPLE_ROWS = 100_000_000
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+
+    def stop(self, device_index=0):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9 or p[0] != str(device_index):
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    mx = float(p[2])
+                except ValueError:
+                    continue
+                for name, v in zip(names, p[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_queries(ops, t, rng_key):
+    """The suite as (name, algorithmic bytes, callable)."""
+    n = t.rows
+    k = int(rng_key)
+
+    def q1():
+        return ops.aggregate_global([t.amount])
+
+    def q2():
+        return ops.scan_simple([t.flag], [(0, ops.CMP_LT, 2)])
+
+    def q3():
+        return ops.group_dense(t.region, [ops.FUNC_SUM, ops.FUNC_COUNT], [t.amount, None])
+
+    def q4():
+        return ops.group_dense(t.amount, [ops.FUNC_COUNT, ops.FUNC_SUM], [None, t.region])
+
+    def q5():
+        return ops.scan_simple([t.id], [(0, ops.CMP_EQ, k)], want_rows=True, max_rows=16)
+
+    return [("sum_min_max_amount", 4 * n, q1), ("count_flag_lt_2", 4 * n, q2), ("group_by_region", 8 * n, q3),
+            ("group_by_amount_10k", 8 * n, q4), ("point_lookup_id", 4 * n, q5)]
+
+
+def profile_entries(native):
+    lib = native.load_cuda()
+    import ctypes as C
+    out = {}
+    i = 0
+    while True:
+        name = C.c_char_p()
+        ns = C.c_uint64()
+        cnt = C.c_uint64()
+        if not lib.cqlcuda_kernel_profile_entry(i, C.byref(name), C.byref(ns), C.byref(cnt)):
+            break
+        if cnt.value:
+            out[name.value.decode()] = (ns.value, cnt.value)
+        i += 1
+    return out
+
+
+def cpu_baseline(rows, threads=0):
+    """The oracle (CPU restatement of the reference's operators) on a bounded sample: rows/s over the suite."""
+    import numpy as np
+    import oracle
+    from computeql_gb300 import workloads
+    oracle.set_threads(threads)
+    h = workloads.fact_numpy(rows, gen=oracle.splitmix_u32)
+    ids = np.arange(rows, dtype=np.uint32)
+    t0 = time.perf_counter()
+    oracle.aggregate_global_cpu(h["amount"])
+    oracle.scan_and([(h["flag"], 1, 2)], rows)
+    oracle.group_cpu_reduce(h["region"], [h["amount"]], 64)
+    oracle.group_cpu_reduce(h["amount"], [h["region"]], 16384)
+    oracle.scan_and([(ids, 0, rows // 3)], rows, want_rows=True)
+    dt = time.perf_counter() - t0
+    return {"value": 5 * rows / dt, "unit": UNIT, "cores": oracle.lib().orc_threads(), "kind": "port",
+            "sample": f"the 5-query suite on the first {rows} rows of the seed-0 table ({dt:.2f} s)"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    rows = args.cpu_rows
+    samples = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(rows)
+        if i >= args.warmup:
+            samples.append(r)
+    value = statistics.median(s["value"] for s in samples)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 5 * rows / value * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic (splitmix64 seed 0)",
+            "config": {"workload": f"1B-row 4 x u32 table query suite (CPU sample of {rows} rows)", "rows": rows, "queries": 5},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": samples[0]["cores"], "kind": "port", "sample": samples[0]["sample"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--rows", type=int, default=1_000_000_000)
+    ap.add_argument("--cpu-rows", type=int, default=CPU_SAMPLE_ROWS)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    # one GPU per rank: replicas of the whole workload (weak scaling, no data-path collective)
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+
+    from computeql_gb300 import build, native, ops, workloads
+    build.build()
+    native.init()
+    lib = native.load_cuda()
+
+    t = workloads.fact_table(args.rows)
+    import numpy as np
+    key = np.random.default_rng(1234 + rank).integers(0, args.rows)
+    queries = make_queries(ops, t, key)
+
+    for _ in range(args.warmup):
+        for _, _, q in queries:
+            q()
+
+    clocks = Clocks()
+    clocks.start()
+    if dist:
+        dist.barrier()
+    lib.cqlcuda_kernel_profile_reset()
+    lib.cqlcuda_kernel_profile_enable(1)
+    launches0 = lib.cqlcuda_kernel_launch_count()
+    per_query = {name: [] for name, _, _ in queries}
+    step_ms = []
+    for _ in range(args.steps):
+        lib.cqlcuda_timer_begin()
+        for name, _, q in queries:
+            t0 = time.perf_counter()
+            q()
+            per_query[name].append((time.perf_counter() - t0) * 1e3)
+        step_ms.append(lib.cqlcuda_timer_end_ms())
+    launches = lib.cqlcuda_kernel_launch_count() - launches0
+    lib.cqlcuda_kernel_profile_enable(0)
+    clk = clocks.stop()
+    prof = profile_entries(native)
+
+    total_ms = sum(step_ms)
+    if dist:
+        import torch
+        tt = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    ms_per_step = total_ms / args.steps
+    nq = len(queries)
+    value = world * nq * args.rows / (ms_per_step / 1e3)
+
+    peak, peak_kind = hbm_peak()
+    # per-kernel CUDA-event time; the dominant kernel gives the roofline
+    kernel_bytes = {"aggregate_global_native": 4 * args.rows, "scan_simple": 4 * args.rows, "aggregate_dense_native": 8 * args.rows}
+    kernel_units = {"aggregate_global_native": "1 column x rows x 4 B", "scan_simple": "1 column x rows x 4 B",
+                    "aggregate_dense_native": "key + argument column x rows x 4 B"}
+    top = max((k for k in prof if k in kernel_bytes), key=lambda k: prof[k][0], default=None)
+    roofline = None
+    if top:
+        ns, cnt = prof[top]
+        avg_s = ns / cnt / 1e9
+        # scan_simple runs twice per step (the filter and the id lookup); the lookup reads no column
+        achieved = kernel_bytes[top] / avg_s / 1e9
+        roofline = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                    "frac": achieved / peak, "traffic": None, "bytes_per_launch": kernel_bytes[top],
+                    "per_unit": kernel_units[top], "avg_launch_ms": avg_s * 1e3, "launches": cnt}
+    qstats = {}
+    for name, nbytes, _ in queries:
+        ms = statistics.median(per_query[name])
+        qstats[name] = {"ms": ms, "rows_per_s": args.rows / (ms / 1e3), "GBps": nbytes / (ms / 1e3) / 1e9,
+                        "hbm_frac": nbytes / (ms / 1e3) / 1e9 / peak}
+    kernels = {k: {"ms_avg": ns / c / 1e6, "launches": c} for k, (ns, c) in prof.items()}
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, native, ops, t, queries, lib)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(args.cpu_rows)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+                "data": "synthetic (splitmix64 seed 0, generated on the device)",
+                "config": {"workload": "1B-row 4 x u32 table (id sequence, region, amount, flag), warm in HBM: 5-query suite",
+                           "rows": args.rows, "queries": [q[0] for q in queries], "l2": "inputs larger than L2 (4 GB columns)",
+                           "parallelism": f"replicas x{world}"},
+                "gpu_launches": launches, "queries": qstats, "kernels": kernels, "roofline": roofline, "clocks": clk,
+                "e2e": e2e, "cpu_baseline": cpu}
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_e2e(args, native, ops, t, queries, lib):
+    """The suite from pinned host buffers: upload region/amount/flag, run, read results, every step."""
+    import ctypes as C
+    import torch
+    n = args.rows
+    host = {}
+    for name in ("region", "amount", "flag"):
+        col = getattr(t, name)
+        h = torch.empty(n, dtype=torch.int32, pin_memory=True)
+        lib.cqlcuda_buffer_read(col.buffer.handle, C.c_void_p(h.data_ptr()), n * 4)
+        host[name] = h
+    h2d = 3 * n * 4
+    times = []
+    for i in range(args.warmup + max(2, args.steps // 2)):
+        t0 = time.perf_counter()
+        batch = lib.cqlcuda_batch_begin(h2d, 0)
+        for name in ("region", "amount", "flag"):
+            lib.cqlcuda_batch_buffer_write(batch, getattr(t, name).buffer.handle, C.c_void_p(host[name].data_ptr()), n * 4)
+        if not lib.cqlcuda_batch_end(batch):
+            raise RuntimeError("e2e upload failed: " + native.last_error())
+        for _, _, q in queries:
+            q()
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    ms = statistics.median(times) * 1e3
+    # results read back per step: partials/counters/group arrays of the 5 queries (a few hundred KB)
+    d2h = 2048 * 3 * 8 + 8 + 50 * 4 * 8 + 10000 * 4 * 8 + 8
+    return {"value": len(queries) * n / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

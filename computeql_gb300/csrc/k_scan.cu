@@ -1,0 +1,323 @@
+// Scan + filter kernels.
+//
+//  scan_simple - contract of src/gpu/vulkan/shaders/scan_simple.comp:1-383: an AND of up to 8 numeric
+//                comparisons, 8 rows per thread, leaf words laid out by qe_simple_leaf_words
+//                (src/query_exec/query_exec.c:1443-1460) and qe_scan_int_leaf_words (:1407-1440).
+//
+// GB300 design: a persistent grid; every thread evaluates 8 consecutive rows with 16-byte loads
+// (32 bytes of a u32 column in flight per thread), the match bits are compacted with a warp
+// prefix sum of popc() and one global atomic per CTA and pass. When the output binding has no room
+// for a single row (a COUNT(*) with no row list) every CTA counts privately and adds once at the end.
+#include "cql_internal.cuh"
+#include <algorithm>
+
+#define COLTYPE_U32 1u
+#define COLTYPE_F32 3u
+#define COLTYPE_F64 4u
+#define COLTYPE_I32 7u
+
+#define CMP_EQ 0u
+#define CMP_LT 1u
+#define CMP_LE 2u
+#define CMP_GT 3u
+#define CMP_GE 4u
+
+#define SCAN_INT_FLAG  0x10000u
+#define SCAN_INT_NEVER 0x20000u
+#define SCAN_INT_BIAS  0x40000u
+
+#define SCAN_THREADS 256
+#define ROWS_PER_THREAD 8u
+
+struct Leaf
+{
+  uint32_t slot, coltype, width, flags, op, w3, w4, enc_base;
+};
+
+__device__ __forceinline__ double widen_word(uint32_t coltype, uint32_t word)
+{
+  if (coltype == COLTYPE_U32) return (double)word;
+  if (coltype == COLTYPE_I32) return (double)(int)word;
+  return (double)__uint_as_float(word);
+}
+
+__device__ __forceinline__ bool cmp(uint32_t op, double v, double t)
+{
+  switch (op)
+  {
+    case CMP_EQ: return v == t;
+    case CMP_LT: return v < t;
+    case CMP_LE: return v <= t;
+    case CMP_GT: return v > t;
+    default: return v >= t;
+  }
+}
+
+// Bits of `valid` rows starting at first_row (a multiple of 8) for one integer-interval leaf.
+__device__ __forceinline__ uint32_t leaf_int_bits(const Leaf& L, const uint32_t* col, uint64_t first_row, uint32_t valid, uint32_t chunk_start)
+{
+  uint32_t lo = L.w3, span = L.w4;
+  uint32_t bias = (L.flags & SCAN_INT_BIAS) ? 0x80000000u : 0u;
+  uint32_t bits = 0;
+  if (L.width == 3)
+  {
+    for (uint32_t k = 0; k < valid; k++) bits |= ((chunk_start + (uint32_t)first_row + k - lo) <= span ? 1u : 0u) << k;
+    return bits;
+  }
+  if (valid == ROWS_PER_THREAD)
+  {
+    if (L.width == 1)
+    {
+      uint2 w = *(const uint2*)(col + first_row / 4);
+#pragma unroll
+      for (uint32_t k = 0; k < 4; k++)
+      {
+        bits |= ((((w.x >> (k * 8)) & 0xffu) - lo) <= span ? 1u : 0u) << k;
+        bits |= ((((w.y >> (k * 8)) & 0xffu) - lo) <= span ? 1u : 0u) << (k + 4);
+      }
+      return bits;
+    }
+    if (L.width == 2)
+    {
+      uint4 w = __ldcs((const uint4*)(col + first_row / 2));
+      uint32_t ws[4] = { w.x, w.y, w.z, w.w };
+#pragma unroll
+      for (uint32_t k = 0; k < 4; k++)
+      {
+        bits |= (((ws[k] & 0xffffu) - lo) <= span ? 1u : 0u) << (2 * k);
+        bits |= (((ws[k] >> 16) - lo) <= span ? 1u : 0u) << (2 * k + 1);
+      }
+      return bits;
+    }
+    const uint4* v = (const uint4*)(col + first_row);
+    uint4 a = __ldcs(v), b = __ldcs(v + 1);
+    uint32_t ws[8] = { a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w };
+#pragma unroll
+    for (uint32_t k = 0; k < 8; k++) bits |= (((ws[k] ^ bias) - lo) <= span ? 1u : 0u) << k;
+    return bits;
+  }
+  for (uint32_t k = 0; k < valid; k++)
+  {
+    uint64_t row = first_row + k;
+    uint32_t code;
+    if (L.width == 1) code = (col[row >> 2] >> ((row & 3) * 8)) & 0xffu;
+    else if (L.width == 2) code = (col[row >> 1] >> ((row & 1) * 16)) & 0xffffu;
+    else code = col[row] ^ bias;
+    bits |= ((code - lo) <= span ? 1u : 0u) << k;
+  }
+  return bits;
+}
+
+// Bits for a leaf compared in double, as compare_rows in scan_simple.comp does.
+__device__ __forceinline__ uint32_t leaf_f64_bits(const Leaf& L, const uint32_t* col, uint64_t first_row, uint32_t valid)
+{
+  double target = __hiloint2double((int)L.w4, (int)L.w3);
+  uint32_t bits = 0;
+  uint32_t op = L.op;
+  if (valid == ROWS_PER_THREAD && L.width == 1)
+  {
+    uint2 w = *(const uint2*)(col + first_row / 4);
+#pragma unroll
+    for (uint32_t k = 0; k < 4; k++)
+    {
+      bits |= (cmp(op, widen_word(L.coltype, L.enc_base + ((w.x >> (k * 8)) & 0xffu)), target) ? 1u : 0u) << k;
+      bits |= (cmp(op, widen_word(L.coltype, L.enc_base + ((w.y >> (k * 8)) & 0xffu)), target) ? 1u : 0u) << (k + 4);
+    }
+    return bits;
+  }
+  if (valid == ROWS_PER_THREAD && L.width == 2)
+  {
+    uint4 w = __ldcs((const uint4*)(col + first_row / 2));
+    uint32_t ws[4] = { w.x, w.y, w.z, w.w };
+#pragma unroll
+    for (uint32_t k = 0; k < 4; k++)
+    {
+      bits |= (cmp(op, widen_word(L.coltype, L.enc_base + (ws[k] & 0xffffu)), target) ? 1u : 0u) << (2 * k);
+      bits |= (cmp(op, widen_word(L.coltype, L.enc_base + (ws[k] >> 16)), target) ? 1u : 0u) << (2 * k + 1);
+    }
+    return bits;
+  }
+  if (valid == ROWS_PER_THREAD)
+  {
+    if (L.coltype == COLTYPE_F64)
+    {
+      const uint4* v = (const uint4*)(col + first_row * 2);
+#pragma unroll
+      for (uint32_t q = 0; q < 4; q++)
+      {
+        uint4 w = __ldcs(v + q);
+        double a = __hiloint2double((int)w.y, (int)w.x);
+        double b = __hiloint2double((int)w.w, (int)w.z);
+        bits |= (cmp(op, a, target) ? 1u : 0u) << (2 * q);
+        bits |= (cmp(op, b, target) ? 1u : 0u) << (2 * q + 1);
+      }
+      return bits;
+    }
+    const uint4* v = (const uint4*)(col + first_row);
+    uint4 a = __ldcs(v), b = __ldcs(v + 1);
+    uint32_t ws[8] = { a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w };
+#pragma unroll
+    for (uint32_t k = 0; k < 8; k++) bits |= (cmp(op, widen_word(L.coltype, ws[k]), target) ? 1u : 0u) << k;
+    return bits;
+  }
+  for (uint32_t k = 0; k < valid; k++)
+  {
+    uint64_t row = first_row + k;
+    double value;
+    if (L.width == 1) value = widen_word(L.coltype, L.enc_base + ((col[row >> 2] >> ((row & 3) * 8)) & 0xffu));
+    else if (L.width == 2) value = widen_word(L.coltype, L.enc_base + ((col[row >> 1] >> ((row & 1) * 16)) & 0xffffu));
+    else if (L.coltype == COLTYPE_F64) value = ((const double*)col)[row];
+    else value = widen_word(L.coltype, col[row]);
+    bits |= (cmp(op, value, target) ? 1u : 0u) << k;
+  }
+  return bits;
+}
+
+template <bool COUNT_ONLY>
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_simple(CqlLaunch a, uint64_t rows)
+{
+  __shared__ Leaf s_leaf[8];
+  __shared__ uint32_t s_leaf_count;
+  __shared__ uint32_t s_warp_total[SCAN_THREADS / 32];
+  __shared__ uint32_t s_base;
+
+  const uint32_t* leaf_words = (const uint32_t*)a.buf[0];
+  if (threadIdx.x == 0)
+  {
+    uint32_t n = leaf_words[0];
+    s_leaf_count = n > 8 ? 8 : n;
+  }
+  __syncthreads();
+  if (threadIdx.x < s_leaf_count)
+  {
+    const uint32_t* w = leaf_words + 1 + threadIdx.x * 6;
+    Leaf L;
+    L.slot = w[0];
+    L.coltype = w[1] & 0xffu;
+    L.width = (w[1] >> 8) & 0xffu;
+    L.flags = w[1] & 0x70000u;
+    L.op = w[2];
+    L.w3 = w[3];
+    L.w4 = w[4];
+    L.enc_base = w[5];
+    s_leaf[threadIdx.x] = L;
+  }
+  __syncthreads();
+
+  uint32_t* out = (uint32_t*)a.buf[3];
+  uint32_t* out_count = (uint32_t*)a.buf[4];
+  const uint32_t* skip = (const uint32_t*)a.buf[5];
+  uint64_t capacity = a.bytes[3] / 8;
+  uint32_t skip_shift = cql_word(a, 6);
+  bool skip_on = cql_word(a, 8) != 0;
+  uint32_t chunk_start = cql_word(a, 10);
+  uint32_t leaf_count = s_leaf_count;
+
+  uint64_t groups = (rows + ROWS_PER_THREAD - 1) / ROWS_PER_THREAD;
+  uint64_t per_pass = (uint64_t)gridDim.x * SCAN_THREADS;
+  uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t private_count = 0;
+
+  for (uint64_t base_group = (uint64_t)blockIdx.x * SCAN_THREADS; base_group < groups; base_group += per_pass)
+  {
+    uint64_t g = base_group + threadIdx.x;
+    uint64_t first_row = g * ROWS_PER_THREAD;
+    uint32_t valid = first_row < rows ? (uint32_t)min((uint64_t)ROWS_PER_THREAD, rows - first_row) : 0u;
+    uint32_t live = valid == 0 ? 0u : ((1u << valid) - 1u);
+    if (live && skip_on)
+    {
+      uint64_t chunk = first_row >> skip_shift;
+      if (skip[chunk >> 5] & (1u << (chunk & 31))) live = 0;
+    }
+    for (uint32_t l = 0; l < leaf_count && live; l++)
+    {
+      const Leaf& L = s_leaf[l];
+      const uint32_t* col = (const uint32_t*)a.buf[6 + (L.slot < 10 ? L.slot : 0)];
+      if (L.flags & SCAN_INT_FLAG)
+      {
+        if (L.flags & SCAN_INT_NEVER) live = 0;
+        else live &= leaf_int_bits(L, col, first_row, valid, chunk_start);
+      }
+      else
+      {
+        live &= leaf_f64_bits(L, col, first_row, valid);
+      }
+    }
+    uint32_t n = __popc(live);
+    if (COUNT_ONLY)
+    {
+      private_count += n;
+      continue;
+    }
+    // warp inclusive scan of the match counts
+    uint32_t incl = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31) s_warp_total[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+      uint32_t run = 0;
+      for (int w = 0; w < SCAN_THREADS / 32; w++)
+      {
+        uint32_t t = s_warp_total[w];
+        s_warp_total[w] = run;
+        run += t;
+      }
+      s_base = run ? atomicAdd(out_count, run) : 0u;
+    }
+    __syncthreads();
+    uint64_t pos = (uint64_t)s_base + s_warp_total[warp] + (incl - n);
+    while (live)
+    {
+      uint32_t k = __ffs(live) - 1;
+      live &= live - 1;
+      if (pos < capacity)
+      {
+        uint2 pair = make_uint2((uint32_t)(first_row + k), 0u);
+        *(uint2*)(out + pos * 2) = pair;
+      }
+      pos++;
+    }
+    __syncthreads();
+  }
+  if (COUNT_ONLY)
+  {
+    uint32_t w = private_count;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+    if (lane == 0) s_warp_total[warp] = w;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+      uint32_t total = 0;
+      for (int i = 0; i < SCAN_THREADS / 32; i++) total += s_warp_total[i];
+      if (total) atomicAdd(out_count, total);
+    }
+  }
+}
+
+static int launch_scan_simple(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t rows = cql_word(a, 0);
+  if (rows == 0) return 0;
+  uint64_t groups = (rows + ROWS_PER_THREAD - 1) / ROWS_PER_THREAD;
+  uint64_t ctas = (groups + SCAN_THREADS - 1) / SCAN_THREADS;
+  uint32_t grid = cql_stream_grid(ctas, 6);
+  bool count_only = a.bytes[3] < 8;
+  if (count_only) k_scan_simple<true><<<grid, SCAN_THREADS, 0, stream>>>(a, rows);
+  else k_scan_simple<false><<<grid, SCAN_THREADS, 0, stream>>>(a, rows);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+const CqlKernelDesc cql_kernels_scan[] = {
+  { "scan_simple", launch_scan_simple },
+  { nullptr, nullptr },
+};

@@ -1,0 +1,1471 @@
+// GB300 runtime behind the cqlcuda C ABI: device, buffers, pooled buffers with epochs and
+// eviction, host import, kernels by shader name, NVRTC-built kernels, batches, multi-slot
+// streams, kernel profile, failure injection.
+//
+// It replaces the Vulkan backend (src/gpu/vulkan/gpu_vulkan.c) behind the same vtable
+// (src/gpu/gpu_backend.h:179-233). Design differences, GB300-first:
+//  - device memory is plain cudaMalloc, one allocation per buffer (no sub-allocated blocks, no
+//    ReBAR heap): 280 GB of HBM makes block sub-allocation unnecessary;
+//  - a batch is the runtime's stream plus a pinned staging area for reads, finished by one
+//    bounded synchronise (gpu_vulkan.c:2864-3116 records a command buffer and waits on a fence);
+//  - each stream slot is a CUDA stream with its own pinned readback staging; submit records an
+//    event, wait polls it with a time limit instead of aborting (gpu_vulkan.c:1106-1135, 1390-1480);
+//  - kernel time comes from CUDA event pairs (gpu_vulkan.c:2976-2993 uses timestamp queries).
+#include "cql_internal.cuh"
+#include "../../include/cqlcuda.h"
+
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+int g_cql_sm_count = 152;
+int g_cql_max_smem_optin = 227 * 1024;
+
+// ---------------------------------------------------------------------------------------------
+// state
+
+struct CqlBuffer
+{
+  void* dptr;
+  uint64_t size;       // bound range seen by kernels
+  uint64_t capacity;   // bytes allocated
+  uint32_t flags;
+  int imported;        // host memory registered (or directly addressable), not owned
+  const void* host_ptr;
+  uint64_t charge;     // device bytes charged to the memory stats
+};
+
+struct CqlPooled
+{
+  std::string name;
+  CqlBuffer* buffer;
+  uint64_t capacity;
+  uint64_t last_epoch;
+  const void* imported_host_ptr;
+};
+
+struct CqlKernel
+{
+  std::string name;
+  CqlLauncher builtin;        // precompiled kernel family
+  cudaKernel_t generated;     // NVRTC-built kernel, launched with CqlLaunch by value
+  uint32_t gen_block;         // block size a generated kernel declares (256 unless its source says otherwise)
+  uint32_t gen_smem;          // dynamic shared memory a generated kernel asks for
+  uint32_t gen_per_sm;        // resident CTAs per SM the grid is sized for
+  CqlLaunch args;
+  uint32_t spec[16];
+  uint32_t spec_count;
+  uint32_t profile_index;
+};
+
+struct CqlPendingRead
+{
+  void* dst;
+  uint64_t staging_offset;
+  uint64_t size;
+};
+
+struct CqlTiming
+{
+  uint32_t profile_index;
+  cudaEvent_t start;
+  cudaEvent_t stop;
+};
+
+struct CqlStaging
+{
+  unsigned char* host;   // pinned
+  uint64_t capacity;
+  uint64_t used;
+  std::vector<CqlPendingRead> reads;
+};
+
+struct CqlBatch
+{
+  int active;
+  int failed;
+  CqlStaging staging;
+};
+
+struct CqlStreamSlot
+{
+  cudaStream_t stream;
+  cudaEvent_t done;
+  int submitted;
+  int failed;
+  CqlStaging staging;
+  std::vector<CqlTiming> timings;
+};
+
+struct CqlStream
+{
+  uint32_t slot_count;
+  CqlStreamSlot slots[8];
+  CqlStreamStats stats;
+};
+
+struct CqlProfileEntry
+{
+  std::string name;
+  uint64_t total_ns;
+  uint64_t dispatches;
+};
+
+struct CqlState
+{
+  int initialized;
+  int device;
+  int device_lost;
+  cudaStream_t stream;
+  cudaEvent_t exec_start, exec_stop, timer_start, timer_stop;
+  int pageable_access;
+
+  CqlMemoryStats mem;
+  uint64_t pool_epoch;
+  std::vector<CqlPooled> pool;
+  std::unordered_map<std::string, size_t> pool_index;
+  CqlEvictHook evict_hook;
+  uint64_t fault_alloc_at;
+
+  std::unordered_map<std::string, CqlKernel*> kernels;
+  uint64_t generated_compiles;
+  uint64_t generated_evictions;
+  std::string cache_dir;
+  uint32_t fail_compile_every;
+  uint64_t compile_attempts;
+  std::string compile_log;
+
+  CqlBatch batch;
+  std::vector<CqlTiming> batch_timings;
+
+  int profile_enabled;
+  std::vector<CqlProfileEntry> profile;
+  std::unordered_map<std::string, uint32_t> profile_index;
+
+  uint64_t last_kernel_us;
+  uint32_t launches;
+  uint32_t wait_timeout_ms;
+
+  void* flush_buf;
+  uint64_t flush_bytes;
+
+  std::string last_error;
+  std::recursive_mutex lock;
+};
+
+static CqlState* g_state = nullptr;
+
+static CqlState& S()
+{
+  if (!g_state)
+  {
+    g_state = new CqlState();
+    g_state->initialized = 0;
+    g_state->device_lost = 0;
+    g_state->pool_epoch = 1;
+    g_state->evict_hook = nullptr;
+    g_state->fault_alloc_at = 0;
+    g_state->generated_compiles = 0;
+    g_state->generated_evictions = 0;
+    g_state->fail_compile_every = 0;
+    g_state->compile_attempts = 0;
+    g_state->profile_enabled = 0;
+    g_state->last_kernel_us = 0;
+    g_state->launches = 0;
+    g_state->wait_timeout_ms = 30000;
+    g_state->flush_buf = nullptr;
+    g_state->flush_bytes = 0;
+    memset(&g_state->mem, 0, sizeof(g_state->mem));
+    g_state->batch.active = 0;
+    g_state->batch.failed = 0;
+    g_state->batch.staging.host = nullptr;
+    g_state->batch.staging.capacity = 0;
+    g_state->batch.staging.used = 0;
+  }
+  return *g_state;
+}
+
+void cql_note_launch(void) { S().launches += 1; }
+
+static void set_error(const char* fmt, ...)
+{
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  S().last_error = buf;
+}
+
+// A CUDA error that leaves the context unusable makes device_lost sticky, as
+// gpu_vulkan_note_result does for VK_ERROR_DEVICE_LOST (gpu_vulkan.c:1523-1535).
+static int note_cuda(cudaError_t e, const char* what)
+{
+  if (e == cudaSuccess) return 1;
+  set_error("%s: %s (%d)", what, cudaGetErrorString(e), (int)e);
+  switch (e)
+  {
+    case cudaErrorIllegalAddress:
+    case cudaErrorLaunchFailure:
+    case cudaErrorIllegalInstruction:
+    case cudaErrorMisalignedAddress:
+    case cudaErrorInvalidAddressSpace:
+    case cudaErrorInvalidPc:
+    case cudaErrorHardwareStackError:
+    case cudaErrorAssert:
+    case cudaErrorLaunchTimeout:
+    case cudaErrorECCUncorrectable:
+      S().device_lost = 1;
+      break;
+    default:
+      break;
+  }
+  return 0;
+}
+
+// Bounded wait on a stream: polls until done or the wait limit, never blocks forever.
+static int wait_stream(cudaStream_t stream, const char* what)
+{
+  auto t0 = std::chrono::steady_clock::now();
+  uint64_t spins = 0;
+  for (;;)
+  {
+    cudaError_t e = cudaStreamQuery(stream);
+    if (e == cudaSuccess) return 1;
+    if (e != cudaErrorNotReady) return note_cuda(e, what);
+    auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+    if ((uint64_t)ms > S().wait_timeout_ms)
+    {
+      set_error("%s: GPU work did not complete within %u ms", what, S().wait_timeout_ms);
+      return 0;
+    }
+    spins += 1;
+    if (spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+}
+
+static int wait_event(cudaEvent_t ev, const char* what)
+{
+  auto t0 = std::chrono::steady_clock::now();
+  uint64_t spins = 0;
+  for (;;)
+  {
+    cudaError_t e = cudaEventQuery(ev);
+    if (e == cudaSuccess) return 1;
+    if (e != cudaErrorNotReady) return note_cuda(e, what);
+    auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+    if ((uint64_t)ms > S().wait_timeout_ms)
+    {
+      set_error("%s: GPU work did not complete within %u ms", what, S().wait_timeout_ms);
+      return 0;
+    }
+    spins += 1;
+    if (spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// profile
+
+static uint32_t profile_slot(const std::string& name)
+{
+  CqlState& s = S();
+  auto it = s.profile_index.find(name);
+  if (it != s.profile_index.end()) return it->second;
+  uint32_t idx = (uint32_t)s.profile.size();
+  s.profile.push_back(CqlProfileEntry{name, 0, 0});
+  s.profile_index[name] = idx;
+  return idx;
+}
+
+static void timings_collect(std::vector<CqlTiming>& timings)
+{
+  CqlState& s = S();
+  for (auto& t : timings)
+  {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, t.start, t.stop) == cudaSuccess)
+    {
+      s.profile[t.profile_index].total_ns += (uint64_t)((double)ms * 1e6);
+      s.profile[t.profile_index].dispatches += 1;
+      s.last_kernel_us = (uint64_t)((double)ms * 1e3);
+    }
+    cudaEventDestroy(t.start);
+    cudaEventDestroy(t.stop);
+  }
+  timings.clear();
+}
+
+// ---------------------------------------------------------------------------------------------
+// device
+
+extern "C" int cqlcuda_init(void)
+{
+  CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
+  if (s.initialized) return !s.device_lost;
+  int count = 0;
+  if (!note_cuda(cudaGetDeviceCount(&count), "cudaGetDeviceCount")) return 0;
+  if (count <= 0)
+  {
+    set_error("cqlcuda_init: no CUDA device");
+    return 0;
+  }
+  s.device = 0;
+  if (!note_cuda(cudaSetDevice(s.device), "cudaSetDevice")) return 0;
+  cudaDeviceProp prop;
+  if (!note_cuda(cudaGetDeviceProperties(&prop, s.device), "cudaGetDeviceProperties")) return 0;
+  if (prop.major < 10)
+  {
+    set_error("cqlcuda_init: device %s is sm_%d%d, this library is built for sm_103a", prop.name, prop.major, prop.minor);
+    return 0;
+  }
+  g_cql_sm_count = prop.multiProcessorCount;
+  g_cql_max_smem_optin = (int)prop.sharedMemPerBlockOptin;
+  int pageable = 0;
+  cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, s.device);
+  s.pageable_access = pageable;
+  if (!note_cuda(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "cudaStreamCreate")) return 0;
+  cudaEventCreate(&s.exec_start);
+  cudaEventCreate(&s.exec_stop);
+  cudaEventCreate(&s.timer_start);
+  cudaEventCreate(&s.timer_stop);
+  s.initialized = 1;
+  return 1;
+}
+
+static int ensure_init(void)
+{
+  if (S().initialized) return !S().device_lost;
+  return cqlcuda_init();
+}
+
+static void staging_release(CqlStaging& st)
+{
+  if (st.host) cudaFreeHost(st.host);
+  st.host = nullptr;
+  st.capacity = 0;
+  st.used = 0;
+  st.reads.clear();
+}
+
+extern "C" void cqlcuda_release(void)
+{
+  CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
+  if (!s.initialized) return;
+  cudaStreamSynchronize(s.stream);
+  for (auto& p : s.pool)
+  {
+    if (p.buffer) cqlcuda_buffer_release(p.buffer);
+    p.buffer = nullptr;
+  }
+  s.pool.clear();
+  s.pool_index.clear();
+  for (auto& kv : s.kernels) delete kv.second;
+  s.kernels.clear();
+  staging_release(s.batch.staging);
+  if (s.flush_buf) cudaFree(s.flush_buf);
+  s.flush_buf = nullptr;
+  cudaStreamDestroy(s.stream);
+  s.initialized = 0;
+}
+
+extern "C" void cqlcuda_wait(void)
+{
+  if (!S().initialized) return;
+  wait_stream(S().stream, "cqlcuda_wait");
+}
+
+extern "C" uint64_t cqlcuda_get_executed_kernel_time_microseconds(void) { return S().last_kernel_us; }
+
+extern "C" uint64_t cqlcuda_device_total_memory(void)
+{
+  if (!ensure_init()) return 0;
+  size_t f = 0, t = 0;
+  cudaMemGetInfo(&f, &t);
+  return t;
+}
+
+extern "C" uint64_t cqlcuda_device_free_memory(void)
+{
+  if (!ensure_init()) return 0;
+  size_t f = 0, t = 0;
+  cudaMemGetInfo(&f, &t);
+  return f;
+}
+
+// No binding-range limit applies to a CUDA pointer; report the device memory so the operator
+// layer's GPU_MAX_BUFFER_SIZE-style chunking (src/main.c:7) never has to split a resident column.
+extern "C" uint64_t cqlcuda_device_max_storage_buffer_range(void) { return cqlcuda_device_total_memory(); }
+extern "C" int cqlcuda_device_lost(void) { return S().device_lost; }
+extern "C" void cqlcuda_pool_begin_epoch(void) { S().pool_epoch += 1; }
+extern "C" CqlMemoryStats cqlcuda_memory_stats(void) { return S().mem; }
+extern "C" uint32_t cqlcuda_sm_count(void) { ensure_init(); return (uint32_t)g_cql_sm_count; }
+
+// ---------------------------------------------------------------------------------------------
+// buffers
+
+// Pooled buffers no running query looked up in this epoch are freed, oldest first
+// (gpu_vulkan_pool_evict, gpu_vulkan.c:1577-1617).
+static uint64_t pool_evict(uint64_t bytes_wanted)
+{
+  CqlState& s = S();
+  if (s.batch.active) return 0;
+  uint64_t freed = 0;
+  while (freed < bytes_wanted)
+  {
+    CqlPooled* victim = nullptr;
+    for (auto& p : s.pool)
+    {
+      if (!p.buffer || p.buffer->charge == 0 || p.last_epoch >= s.pool_epoch) continue;
+      if (!victim || p.last_epoch < victim->last_epoch) victim = &p;
+    }
+    if (!victim) break;
+    uint64_t charge = victim->buffer->charge;
+    cqlcuda_buffer_release(victim->buffer);
+    victim->buffer = nullptr;
+    victim->capacity = 0;
+    victim->imported_host_ptr = nullptr;
+    freed += charge;
+    s.mem.pool_evictions += 1;
+    s.mem.pool_evicted_bytes += charge;
+  }
+  return freed;
+}
+
+// The k-th allocation call fails when fault_alloc_at == k (gpu_vulkan_fault_injected, gpu_vulkan.c:1619-1631).
+static int fault_injected(const char* what, uint64_t size)
+{
+  CqlState& s = S();
+  s.mem.alloc_calls += 1;
+  if (s.fault_alloc_at == 0 || s.mem.alloc_calls != s.fault_alloc_at) return 0;
+  s.mem.alloc_failures += 1;
+  set_error("cqlcuda: injected failure of allocation %llu (%s, %llu bytes)", (unsigned long long)s.mem.alloc_calls, what,
+            (unsigned long long)size);
+  return 1;
+}
+
+static void* device_alloc(uint64_t size)
+{
+  CqlState& s = S();
+  void* p = nullptr;
+  uint64_t bytes = size ? size : 16;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e == cudaErrorMemoryAllocation)
+  {
+    cudaGetLastError();
+    uint64_t freed = pool_evict(bytes);
+    if (freed < bytes && s.evict_hook) freed += s.evict_hook(bytes - freed);
+    if (freed > 0)
+    {
+      e = cudaMalloc(&p, bytes);
+      if (e == cudaSuccess) s.mem.alloc_retry_successes += 1;
+      else cudaGetLastError();
+    }
+  }
+  if (e != cudaSuccess)
+  {
+    s.mem.alloc_failures += 1;
+    s.mem.unrecovered_alloc_failures += 1;
+    set_error("cqlcuda: cudaMalloc of %llu bytes failed: %s", (unsigned long long)bytes, cudaGetErrorString(e));
+    return nullptr;
+  }
+  s.mem.bytes_in_use += bytes;
+  s.mem.bytes_peak = std::max(s.mem.bytes_peak, s.mem.bytes_in_use);
+  return p;
+}
+
+extern "C" CqlBuffer* cqlcuda_buffer_alloc(uint64_t size, uint32_t flags, const void* data)
+{
+  CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
+  if (!ensure_init()) return nullptr;
+  if (fault_injected("buffer", size)) return nullptr;
+  void* p = device_alloc(size);
+  if (!p) return nullptr;
+  CqlBuffer* b = new CqlBuffer();
+  b->dptr = p;
+  b->size = size;
+  b->capacity = size ? size : 16;
+  b->flags = flags;
+  b->imported = 0;
+  b->host_ptr = nullptr;
+  b->charge = b->capacity;
+  if (data && size)
+  {
+    if (!note_cuda(cudaMemcpyAsync(p, data, size, cudaMemcpyHostToDevice, s.stream), "buffer_alloc upload") ||
+        !wait_stream(s.stream, "buffer_alloc upload"))
+    {
+      cqlcuda_buffer_release(b);
+      return nullptr;
+    }
+  }
+  return b;
+}
+
+static CqlPooled* pool_find(const std::string& name)
+{
+  auto it = S().pool_index.find(name);
+  return it == S().pool_index.end() ? nullptr : &S().pool[it->second];
+}
+
+// Reused while its capacity covers the request; a bigger request replaces it
+// (gpu_vulkan_buffer_alloc_pooled, gpu_vulkan.c:2167-2211).
+extern "C" CqlBuffer* cqlcuda_buffer_alloc_pooled(const char* name, uint64_t name_len, uint64_t size, uint32_t flags, const void* data)
+{
+  CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
+  std::string key(name, name_len);
+  CqlPooled* slot = pool_find(key);
+  if (slot)
+  {
+    slot->last_epoch = s.pool_epoch;
+    if (size > slot->capacity || !slot->buffer || slot->imported_host_ptr)
+    {
+      cqlcuda_buffer_release(slot->buffer);
+      slot->buffer = cqlcuda_buffer_alloc(size, flags, data);
+      slot->capacity = slot->buffer ? size : 0;
+      slot->imported_host_ptr = nullptr;
+    }
+    else
+    {
+      slot->buffer->size = size;
+      if (data) cqlcuda_buffer_write(slot->buffer, data, size);
+    }
+    return slot->buffer;
+  }
+  CqlBuffer* b = cqlcuda_buffer_alloc(size, flags, data);
+  s.pool.push_back(CqlPooled{key, b, b ? size : 0, s.pool_epoch, nullptr});
+  s.pool_index[key] = s.pool.size() - 1;
+  return b;
+}
+
+// Host memory is pinned and mapped read-only; on a GB300 node (NVLink-C2C, ATS) the GPU could also
+// read pageable memory directly, which is the fallback when registration is refused.
+extern "C" CqlBuffer* cqlcuda_buffer_import_host_readonly(const void* host_ptr, uint64_t size)
+{
+  CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
+  if (!ensure_init() || !host_ptr || size == 0) return nullptr;
+  if (fault_injected("import", size)) return nullptr;
+  void* dptr = nullptr;
+  int registered = 0;
+  cudaError_t e = cudaHostRegister(const_cast<void*>(host_ptr), size, cudaHostRegisterMapped | cudaHostRegisterReadOnly);
+  if (e == cudaSuccess)
+  {
+    registered = 1;
+    if (cudaHostGetDevicePointer(&dptr, const_cast<void*>(host_ptr), 0) != cudaSuccess)
+    {
+      cudaHostUnregister(const_cast<void*>(host_ptr));
+      registered = 0;
+      dptr = nullptr;
+    }
+  }
+  else
+  {
+    cudaGetLastError();
+  }
+  if (!dptr && s.pageable_access) dptr = const_cast<void*>(host_ptr);
+  if (!dptr)
+  {
+    set_error("cqlcuda_buffer_import_host_readonly: host memory at %p (%llu bytes) cannot be mapped", host_ptr, (unsigned long long)size);
+    return nullptr;
+  }
+  CqlBuffer* b = new CqlBuffer();
+  b->dptr = dptr;
+  b->size = size;
+  b->capacity = size;
+  b->flags = CQLCUDA_BUFFER_READ;
+  b->imported = registered ? 1 : 2;
+  b->host_ptr = host_ptr;
+  b->charge = 0;
+  return b;
+}
+
+extern "C" CqlBuffer* cqlcuda_buffer_import_host_readonly_pooled(const char* name, uint64_t name_len, const void* host_ptr, uint64_t size)
+{
+  CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
+  std::string key(name, name_len);
+  CqlPooled* slot = pool_find(key);
+  if (slot && slot->buffer && slot->imported_host_ptr == host_ptr && slot->capacity == size)
+  {
+    slot->last_epoch = s.pool_epoch;
+    return slot->buffer;
+  }
+  CqlBuffer* b = cqlcuda_buffer_import_host_readonly(host_ptr, size);
+  if (slot)
+  {
+    cqlcuda_buffer_release(slot->buffer);
+    slot->buffer = b;
+    slot->capacity = b ? size : 0;
+    slot->imported_host_ptr = b ? host_ptr : nullptr;
+    slot->last_epoch = s.pool_epoch;
+    return b;
+  }
+  s.pool.push_back(CqlPooled{key, b, b ? size : 0, s.pool_epoch, b ? host_ptr : nullptr});
+  s.pool_index[key] = s.pool.size() - 1;
+  return b;
+}
+
+extern "C" void cqlcuda_buffer_release(CqlBuffer* b)
+{
+  if (!b) return;
+  CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
+  // a pooled slot that still points at this buffer forgets it
+  for (auto& p : s.pool)
+  {
+    if (p.buffer == b)
+    {
+      p.buffer = nullptr;
+      p.capacity = 0;
+      p.imported_host_ptr = nullptr;
+    }
+  }
+  if (b->imported == 1) cudaHostUnregister(const_cast<void*>(b->host_ptr));
+  else if (!b->imported && b->dptr)
+  {
+    // work already queued on the runtime stream may still read the buffer
+    cudaStreamSynchronize(s.stream);
+    cudaFree(b->dptr);
+    s.mem.bytes_in_use -= std::min(b->charge, s.mem.bytes_in_use);
+  }
+  delete b;
+}
+
+extern "C" void cqlcuda_buffer_write(CqlBuffer* b, const void* data, uint64_t size)
+{
+  if (!b || !data) return;
+  if (size > b->size)
+  {
+    set_error("cqlcuda_buffer_write: write size exceeds buffer size");
+    return;
+  }
+  if (b->imported)
+  {
+    set_error("cqlcuda_buffer_write: an imported host buffer is read-only");
+    return;
+  }
+  CqlState& s = S();
+  if (note_cuda(cudaMemcpyAsync(b->dptr, data, size, cudaMemcpyHostToDevice, s.stream), "buffer_write"))
+    wait_stream(s.stream, "buffer_write");
+}
+
+extern "C" void cqlcuda_buffer_read(CqlBuffer* b, void* data, uint64_t size)
+{
+  if (!b || !data) return;
+  if (size > b->size)
+  {
+    set_error("cqlcuda_buffer_read: read size exceeds buffer size");
+    return;
+  }
+  CqlState& s = S();
+  if (!note_cuda(cudaMemcpyAsync(data, b->dptr, size, cudaMemcpyDeviceToHost, s.stream), "buffer_read") ||
+      !wait_stream(s.stream, "buffer_read"))
+  {
+    memset(data, 0, size);
+  }
+}
+
+extern "C" uint64_t cqlcuda_buffer_size(const CqlBuffer* b) { return b ? b->size : 0; }
+extern "C" void* cqlcuda_buffer_device_pointer(const CqlBuffer* b) { return b ? b->dptr : nullptr; }
+
+// ---------------------------------------------------------------------------------------------
+// kernels
+
+static const CqlKernelDesc* find_builtin(const std::string& name)
+{
+  const CqlKernelDesc* tables[] = { cql_kernels_aggregate, cql_kernels_scan, cql_kernels_hash, cql_kernels_join, cql_kernels_sort };
+  for (const CqlKernelDesc* t : tables)
+  {
+    for (const CqlKernelDesc* d = t; d->name; d++)
+    {
+      if (name == d->name) return d;
+    }
+  }
+  return nullptr;
+}
+
+static CqlKernel* kernel_new(const std::string& name)
+{
+  CqlKernel* k = new CqlKernel();
+  k->name = name;
+  k->builtin = nullptr;
+  k->generated = nullptr;
+  k->gen_block = 256;
+  k->gen_smem = 0;
+  k->gen_per_sm = 4;
+  memset(&k->args, 0, sizeof(k->args));
+  memset(k->spec, 0, sizeof(k->spec));
+  k->spec_count = 0;
+  k->profile_index = profile_slot(name);
+  return k;
+}
+
+extern "C" CqlKernel* cqlcuda_kernel_alloc(const char* name, uint64_t name_len)
+{
+  CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
+  if (!ensure_init()) return nullptr;
+  std::string key(name, name_len);
+  auto it = s.kernels.find(key);
+  if (it != s.kernels.end()) return it->second;
+  const CqlKernelDesc* d = find_builtin(key);
+  if (!d)
+  {
+    set_error("cqlcuda_kernel_alloc: no kernel named '%s'", key.c_str());
+    return nullptr;
+  }
+  CqlKernel* k = kernel_new(key);
+  k->builtin = d->launch;
+  s.kernels[key] = k;
+  return k;
+}
+
+// A generated source may declare its launch shape in a first-line comment:
+//   // cql: block=256 smem=0 per_sm=4
+static void parse_generated_policy(const std::string& src, CqlKernel* k)
+{
+  size_t at = src.find("// cql:");
+  if (at == std::string::npos) return;
+  size_t end = src.find('\n', at);
+  std::string line = src.substr(at, end == std::string::npos ? std::string::npos : end - at);
+  unsigned v = 0;
+  size_t p;
+  if ((p = line.find("block=")) != std::string::npos && sscanf(line.c_str() + p, "block=%u", &v) == 1 && v >= 32 && v <= 1024) k->gen_block = v;
+  if ((p = line.find("smem=")) != std::string::npos && sscanf(line.c_str() + p, "smem=%u", &v) == 1) k->gen_smem = v;
+  if ((p = line.find("per_sm=")) != std::string::npos && sscanf(line.c_str() + p, "per_sm=%u", &v) == 1 && v >= 1 && v <= 32) k->gen_per_sm = v;
+}
+
+static uint64_t fnv1a(const void* data, uint64_t n)
+{
+  const unsigned char* p = (const unsigned char*)data;
+  uint64_t h = 1469598103934665603ull;
+  for (uint64_t i = 0; i < n; i++)
+  {
+    h ^= p[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+static std::vector<char> compile_nvrtc(const std::string& src, const std::string& name, int* ok)
+{
+  CqlState& s = S();
+  std::vector<char> cubin;
+  *ok = 0;
+  s.compile_attempts += 1;
+  if (s.fail_compile_every && (s.compile_attempts % s.fail_compile_every) == 0)
+  {
+    s.compile_log = "injected compile failure";
+    set_error("cqlcuda: injected NVRTC failure for '%s'", name.c_str());
+    return cubin;
+  }
+  // disk cache: key = source hash + a check hash + target + NVRTC version
+  int maj = 0, min = 0;
+  nvrtcVersion(&maj, &min);
+  uint64_t h1 = fnv1a(src.data(), src.size());
+  uint64_t h2 = 0;
+  for (size_t i = 0; i < src.size(); i++) h2 = h2 * 131 + (unsigned char)src[i];
+  char fname[512];
+  if (!s.cache_dir.empty())
+  {
+    snprintf(fname, sizeof(fname), "%s/cql_%016llx%016llx_sm103a_nvrtc%d.%d.cubin", s.cache_dir.c_str(), (unsigned long long)h1,
+             (unsigned long long)h2, maj, min);
+    FILE* f = fopen(fname, "rb");
+    if (f)
+    {
+      fseek(f, 0, SEEK_END);
+      long n = ftell(f);
+      fseek(f, 0, SEEK_SET);
+      if (n > 0)
+      {
+        cubin.resize((size_t)n);
+        if (fread(cubin.data(), 1, (size_t)n, f) == (size_t)n)
+        {
+          fclose(f);
+          *ok = 1;
+          return cubin;
+        }
+      }
+      fclose(f);
+      cubin.clear();
+    }
+  }
+  nvrtcProgram prog;
+  if (nvrtcCreateProgram(&prog, src.c_str(), (name + ".cu").c_str(), 0, nullptr, nullptr) != NVRTC_SUCCESS)
+  {
+    set_error("cqlcuda: nvrtcCreateProgram failed for '%s'", name.c_str());
+    return cubin;
+  }
+  const char* opts[] = { "--gpu-architecture=sm_103a", "--std=c++17", "-default-device", "--use_fast_math=false", "-lineinfo" };
+  nvrtcResult r = nvrtcCompileProgram(prog, 4, opts);
+  size_t log_size = 0;
+  nvrtcGetProgramLogSize(prog, &log_size);
+  s.compile_log.assign(log_size, '\0');
+  if (log_size) nvrtcGetProgramLog(prog, &s.compile_log[0]);
+  if (r != NVRTC_SUCCESS)
+  {
+    set_error("cqlcuda: NVRTC failed for '%s': %s", name.c_str(), nvrtcGetErrorString(r));
+    nvrtcDestroyProgram(&prog);
+    return cubin;
+  }
+  size_t n = 0;
+  nvrtcGetCUBINSize(prog, &n);
+  cubin.resize(n);
+  nvrtcGetCUBIN(prog, cubin.data());
+  nvrtcDestroyProgram(&prog);
+  s.generated_compiles += 1;
+  if (!s.cache_dir.empty())
+  {
+    FILE* f = fopen(fname, "wb");
+    if (f)
+    {
+      fwrite(cubin.data(), 1, cubin.size(), f);
+      fclose(f);
+    }
+  }
+  *ok = 1;
+  return cubin;
+}
+
+extern "C" CqlKernel* cqlcuda_kernel_alloc_from_image_spec(const char* name, uint64_t name_len, const void* image, uint64_t image_len,
+                                                          const uint32_t* spec_values, uint32_t spec_count)
+{
+  CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
+  if (!ensure_init()) return nullptr;
+  std::string key(name, name_len);
+  if (spec_count)
+  {
+    // a specialisation is its own kernel object
+    char suffix[32];
+    for (uint32_t i = 0; i < spec_count; i++)
+    {
+      snprintf(suffix, sizeof(suffix), ":%u", spec_values[i]);
+      key += suffix;
+    }
+  }
+  auto it = s.kernels.find(key);
+  if (it != s.kernels.end()) return it->second;
+  if (!image || image_len == 0)
+  {
+    return nullptr;  // lookup only (src/gpu/gpu.h:129-130)
+  }
+  const unsigned char* bytes = (const unsigned char*)image;
+  std::vector<char> cubin;
+  int is_elf = image_len >= 4 && bytes[0] == 0x7f && bytes[1] == 'E' && bytes[2] == 'L' && bytes[3] == 'F';
+  std::string src;
+  if (is_elf) cubin.assign((const char*)image, (const char*)image + image_len);
+  else
+  {
+    src.assign((const char*)image, image_len);
+    if (spec_count)
+    {
+      // specialisation constants become preprocessor definitions CQL_SPEC_<i>
+      std::string defs;
+      char line[64];
+      for (uint32_t i = 0; i < spec_count; i++)
+      {
+        snprintf(line, sizeof(line), "#define CQL_SPEC_%u %uu\n", i, spec_values[i]);
+        defs += line;
+      }
+      src = defs + src;
+    }
+    int ok = 0;
+    cubin = compile_nvrtc(src, key, &ok);
+    if (!ok) return nullptr;
+  }
+  cudaLibrary_t lib = nullptr;
+  if (!note_cuda(cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0), "cudaLibraryLoadData")) return nullptr;
+  cudaKernel_t kfn = nullptr;
+  if (!note_cuda(cudaLibraryGetKernel(&kfn, lib, "cql_main"), "cudaLibraryGetKernel(cql_main)")) return nullptr;
+  CqlKernel* k = kernel_new(key);
+  k->generated = kfn;
+  if (!src.empty()) parse_generated_policy(src, k);
+  if (k->gen_smem > 48 * 1024)
+  {
+    cudaFuncSetAttribute((const void*)kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k->gen_smem);
+  }
+  if (spec_count)
+  {
+    memcpy(k->spec, spec_values, sizeof(uint32_t) * std::min<uint32_t>(spec_count, 16));
+    k->spec_count = spec_count;
+  }
+  s.kernels[key] = k;
+  return k;
+}
+
+extern "C" CqlKernel* cqlcuda_kernel_alloc_from_image(const char* name, uint64_t name_len, const void* image, uint64_t image_len)
+{
+  return cqlcuda_kernel_alloc_from_image_spec(name, name_len, image, image_len, nullptr, 0);
+}
+
+extern "C" void cqlcuda_generated_kernel_stats(uint64_t* out_compiles, uint64_t* out_evictions)
+{
+  if (out_compiles) *out_compiles = S().generated_compiles;
+  if (out_evictions) *out_evictions = S().generated_evictions;
+}
+
+extern "C" void cqlcuda_kernel_release(CqlKernel*) {}
+
+extern "C" void cqlcuda_kernel_set_arg_buffer(CqlKernel* k, uint32_t index, CqlBuffer* b)
+{
+  if (!k) return;
+  if (index >= CQL_MAX_BINDINGS)
+  {
+    set_error("cqlcuda_kernel_set_arg_buffer: index %u exceeds %u", index, CQL_MAX_BINDINGS);
+    return;
+  }
+  if (!b)
+  {
+    set_error("cqlcuda_kernel_set_arg_buffer: buffer argument for index %u is NULL - a prior GPU buffer allocation failed", index);
+    return;
+  }
+  k->args.buf[index] = b->dptr;
+  k->args.bytes[index] = b->size;
+}
+
+extern "C" void cqlcuda_kernel_set_arg_buffer_range(CqlKernel* k, uint32_t index, CqlBuffer* b, uint64_t offset, uint64_t size)
+{
+  if (!k || !b || index >= CQL_MAX_BINDINGS) return;
+  if (offset > b->size || size > b->size - offset)
+  {
+    set_error("cqlcuda_kernel_set_arg_buffer_range: range [%llu, +%llu) outside a %llu byte buffer", (unsigned long long)offset,
+              (unsigned long long)size, (unsigned long long)b->size);
+    return;
+  }
+  k->args.buf[index] = (char*)b->dptr + offset;
+  k->args.bytes[index] = size;
+}
+
+extern "C" void cqlcuda_kernel_set_arg_u64(CqlKernel* k, uint32_t index, uint64_t value)
+{
+  if (!k) return;
+  if (index >= CQL_PUSH_SLOTS)
+  {
+    set_error("cqlcuda_kernel_set_arg_u64: index %u exceeds %u", index, CQL_PUSH_SLOTS);
+    return;
+  }
+  k->args.push[index] = value;
+}
+
+// Enqueues one dispatch on `stream`, bracketed by events when the profile is on.
+static int dispatch(CqlKernel* k, uint32_t gws, uint32_t lws, cudaStream_t stream, std::vector<CqlTiming>* timings)
+{
+  CqlState& s = S();
+  if (s.device_lost)
+  {
+    set_error("cqlcuda: device lost, dispatch of '%s' skipped", k->name.c_str());
+    return 0;
+  }
+  CqlTiming t;
+  int timed = s.profile_enabled && timings;
+  if (timed)
+  {
+    t.profile_index = k->profile_index;
+    cudaEventCreate(&t.start);
+    cudaEventCreate(&t.stop);
+    cudaEventRecord(t.start, stream);
+  }
+  int rc = 0;
+  if (k->builtin)
+  {
+    rc = k->builtin(k->args, gws, lws, stream);
+  }
+  else if (k->generated)
+  {
+    uint32_t block = k->gen_block;
+    uint64_t want = lws ? ((uint64_t)gws + lws - 1) / lws : 1;
+    uint32_t grid = cql_stream_grid(want ? want : 1, (int)k->gen_per_sm);
+    CqlLaunch a = k->args;
+    void* params[] = { &a };
+    cudaError_t e = cudaLaunchKernel((const void*)k->generated, dim3(grid), dim3(block), params, k->gen_smem, stream);
+    rc = (int)e;
+    if (e == cudaSuccess) cql_note_launch();
+  }
+  if (timed)
+  {
+    cudaEventRecord(t.stop, stream);
+    timings->push_back(t);
+  }
+  if (rc != 0)
+  {
+    note_cuda((cudaError_t)rc, k->name.c_str());
+    return 0;
+  }
+  return 1;
+}
+
+extern "C" void cqlcuda_kernel_execute(CqlKernel* k, uint32_t gws, uint32_t lws)
+{
+  if (!k) return;
+  CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
+  cudaEventRecord(s.exec_start, s.stream);
+  std::vector<CqlTiming> timings;
+  int ok = dispatch(k, gws, lws, s.stream, &timings);
+  cudaEventRecord(s.exec_stop, s.stream);
+  if (ok && wait_stream(s.stream, k->name.c_str()))
+  {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, s.exec_start, s.exec_stop) == cudaSuccess) s.last_kernel_us = (uint64_t)(ms * 1000.0f);
+    timings_collect(timings);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// pinned staging for reads
+
+static unsigned char* staging_reserve(CqlStaging& st, uint64_t size, uint64_t* out_offset)
+{
+  uint64_t offset = (st.used + 15) & ~15ull;
+  if (offset + size > st.capacity)
+  {
+    // growing while reads are pending would move them: callers size the staging at begin
+    if (!st.reads.empty()) return nullptr;
+    uint64_t cap = std::max<uint64_t>(offset + size, std::max<uint64_t>(st.capacity * 2, 1 << 16));
+    unsigned char* p = nullptr;
+    if (cudaHostAlloc((void**)&p, cap, cudaHostAllocDefault) != cudaSuccess)
+    {
+      cudaGetLastError();
+      return nullptr;
+    }
+    if (st.host) cudaFreeHost(st.host);
+    st.host = p;
+    st.capacity = cap;
+  }
+  st.used = offset + size;
+  *out_offset = offset;
+  return st.host + offset;
+}
+
+static void staging_prepare(CqlStaging& st, uint64_t bytes)
+{
+  st.used = 0;
+  st.reads.clear();
+  if (bytes + 4096 > st.capacity)
+  {
+    uint64_t unused;
+    staging_reserve(st, bytes + 4096, &unused);
+    st.used = 0;
+  }
+}
+
+static void staging_finish(CqlStaging& st, int ok)
+{
+  for (auto& r : st.reads)
+  {
+    if (ok) memcpy(r.dst, st.host + r.staging_offset, r.size);
+    else memset(r.dst, 0, r.size);
+  }
+  st.reads.clear();
+  st.used = 0;
+}
+
+static int enqueue_read(CqlStaging& st, CqlBuffer* b, void* out, uint64_t size, cudaStream_t stream)
+{
+  if (!b || !out) return 0;
+  if (size > b->size)
+  {
+    set_error("cqlcuda: read of %llu bytes from a %llu byte buffer", (unsigned long long)size, (unsigned long long)b->size);
+    return 0;
+  }
+  uint64_t off = 0;
+  unsigned char* dst = staging_reserve(st, size, &off);
+  if (!dst)
+  {
+    // the staging area could not hold it: read synchronously into the caller's memory
+    if (!note_cuda(cudaMemcpyAsync(out, b->dptr, size, cudaMemcpyDeviceToHost, stream), "read")) return 0;
+    return wait_stream(stream, "read");
+  }
+  if (!note_cuda(cudaMemcpyAsync(dst, b->dptr, size, cudaMemcpyDeviceToHost, stream), "read")) return 0;
+  st.reads.push_back(CqlPendingRead{out, off, size});
+  return 1;
+}
+
+// ---------------------------------------------------------------------------------------------
+// batches: one active at a time (src/gpu/vulkan/gpu_vulkan.h:215)
+
+extern "C" CqlBatch* cqlcuda_batch_begin(uint64_t upload_bytes_needed, uint64_t download_bytes_needed)
+{
+  CqlState& s = S();
+  s.lock.lock();
+  if (!ensure_init())
+  {
+    s.lock.unlock();
+    return nullptr;
+  }
+  (void)upload_bytes_needed;
+  CqlBatch* b = &s.batch;
+  b->active = 1;
+  b->failed = 0;
+  staging_prepare(b->staging, download_bytes_needed);
+  return b;
+}
+
+extern "C" void cqlcuda_batch_buffer_write(CqlBatch* batch, CqlBuffer* buffer, const void* data, uint64_t size)
+{
+  if (!batch || !buffer || !data) return;
+  if (size > buffer->size || buffer->imported)
+  {
+    set_error("cqlcuda_batch_buffer_write: bad destination");
+    batch->failed = 1;
+    return;
+  }
+  if (!note_cuda(cudaMemcpyAsync(buffer->dptr, data, size, cudaMemcpyHostToDevice, S().stream), "batch write")) batch->failed = 1;
+}
+
+extern "C" void cqlcuda_batch_buffer_zero(CqlBatch* batch, CqlBuffer* buffer, uint64_t size)
+{
+  if (!batch || !buffer) return;
+  if (!note_cuda(cudaMemsetAsync(buffer->dptr, 0, std::min(size, buffer->size), S().stream), "batch zero")) batch->failed = 1;
+}
+
+__global__ void k_fill_u32(uint32_t* p, uint64_t words, uint32_t value)
+{
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (; i < words; i += stride) p[i] = value;
+}
+
+static int fill_words(CqlBuffer* buffer, uint64_t size, uint32_t value, cudaStream_t stream)
+{
+  uint64_t bytes = std::min(size, buffer->size);
+  if (value == 0 || value == 0xffffffffu || ((value & 0xff) * 0x01010101u) == value)
+  {
+    return note_cuda(cudaMemsetAsync(buffer->dptr, (int)(value & 0xff), bytes, stream), "fill");
+  }
+  uint64_t words = bytes / 4;
+  if (words == 0) return 1;
+  uint32_t grid = cql_stream_grid((words + 255) / 256, 8);
+  k_fill_u32<<<grid, 256, 0, stream>>>((uint32_t*)buffer->dptr, words, value);
+  cql_note_launch();
+  return note_cuda(cudaGetLastError(), "fill");
+}
+
+extern "C" void cqlcuda_batch_buffer_fill(CqlBatch* batch, CqlBuffer* buffer, uint64_t size, uint32_t value)
+{
+  if (!batch || !buffer) return;
+  if (!fill_words(buffer, size, value, S().stream)) batch->failed = 1;
+}
+
+extern "C" void cqlcuda_batch_kernel_execute(CqlBatch* batch, CqlKernel* kernel, uint32_t gws, uint32_t lws)
+{
+  if (!batch || !kernel) return;
+  if (!dispatch(kernel, gws, lws, S().stream, &S().batch_timings)) batch->failed = 1;
+}
+
+extern "C" void cqlcuda_batch_buffer_read(CqlBatch* batch, CqlBuffer* buffer, void* out_data, uint64_t size)
+{
+  if (!batch) return;
+  if (!buffer)
+  {
+    if (out_data) memset(out_data, 0, size);
+    return;
+  }
+  if (!enqueue_read(batch->staging, buffer, out_data, size, S().stream)) batch->failed = 1;
+}
+
+extern "C" int cqlcuda_batch_end(CqlBatch* batch)
+{
+  CqlState& s = S();
+  if (!batch)
+  {
+    return 0;
+  }
+  int ok = !batch->failed && wait_stream(s.stream, "batch_end");
+  staging_finish(batch->staging, ok);
+  if (ok) timings_collect(s.batch_timings);
+  else
+  {
+    for (auto& t : s.batch_timings)
+    {
+      cudaEventDestroy(t.start);
+      cudaEventDestroy(t.stop);
+    }
+    s.batch_timings.clear();
+  }
+  batch->active = 0;
+  s.lock.unlock();
+  return ok;
+}
+
+// ---------------------------------------------------------------------------------------------
+// streams
+
+extern "C" CqlStream* cqlcuda_stream_alloc(uint32_t slot_count)
+{
+  if (!ensure_init()) return nullptr;
+  if (slot_count == 0 || slot_count > 8)
+  {
+    set_error("cqlcuda_stream_alloc: %u slots, 1 to 8 allowed", slot_count);
+    return nullptr;
+  }
+  CqlStream* st = new CqlStream();
+  st->slot_count = slot_count;
+  memset(&st->stats, 0, sizeof(st->stats));
+  st->stats.separate_copy_queue = 1;
+  for (uint32_t i = 0; i < slot_count; i++)
+  {
+    CqlStreamSlot& sl = st->slots[i];
+    if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess || cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess)
+    {
+      set_error("cqlcuda_stream_alloc: stream creation failed");
+      for (uint32_t j = 0; j < i; j++)
+      {
+        cudaStreamDestroy(st->slots[j].stream);
+        cudaEventDestroy(st->slots[j].done);
+      }
+      delete st;
+      return nullptr;
+    }
+    sl.submitted = 0;
+    sl.failed = 0;
+    sl.staging.host = nullptr;
+    sl.staging.capacity = 0;
+    sl.staging.used = 0;
+  }
+  // slots run after everything already queued on the runtime stream
+  cudaEvent_t ev;
+  cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+  cudaEventRecord(ev, S().stream);
+  for (uint32_t i = 0; i < slot_count; i++) cudaStreamWaitEvent(st->slots[i].stream, ev, 0);
+  cudaEventDestroy(ev);
+  return st;
+}
+
+extern "C" void cqlcuda_stream_release(CqlStream* st)
+{
+  if (!st) return;
+  for (uint32_t i = 0; i < st->slot_count; i++)
+  {
+    CqlStreamSlot& sl = st->slots[i];
+    wait_stream(sl.stream, "stream_release");
+    for (auto& t : sl.timings)
+    {
+      cudaEventDestroy(t.start);
+      cudaEventDestroy(t.stop);
+    }
+    cudaStreamDestroy(sl.stream);
+    cudaEventDestroy(sl.done);
+    staging_release(sl.staging);
+  }
+  delete st;
+}
+
+extern "C" int cqlcuda_stream_slot_begin(CqlStream* st, uint32_t slot, uint64_t upload_bytes, uint64_t readback_bytes)
+{
+  if (!st || slot >= st->slot_count) return 0;
+  CqlStreamSlot& sl = st->slots[slot];
+  (void)upload_bytes;
+  if (!sl.staging.reads.empty())
+  {
+    // the previous use of the slot was never waited for
+    if (!wait_stream(sl.stream, "stream_slot_begin")) return 0;
+    staging_finish(sl.staging, 1);
+  }
+  sl.submitted = 0;
+  sl.failed = 0;
+  staging_prepare(sl.staging, readback_bytes);
+  return 1;
+}
+
+extern "C" int cqlcuda_stream_copy(CqlStream* st, uint32_t slot, CqlBuffer* dst, const void* host_ptr, uint64_t size)
+{
+  if (!st || slot >= st->slot_count || !dst || !host_ptr) return 0;
+  if (size > dst->size || dst->imported)
+  {
+    set_error("cqlcuda_stream_copy: bad destination");
+    return 0;
+  }
+  CqlStreamSlot& sl = st->slots[slot];
+  if (!note_cuda(cudaMemcpyAsync(dst->dptr, host_ptr, size, cudaMemcpyHostToDevice, sl.stream), "stream_copy"))
+  {
+    sl.failed = 1;
+    return 0;
+  }
+  st->stats.bytes_copied += size;
+  return 1;
+}
+
+extern "C" void cqlcuda_stream_zero(CqlStream* st, uint32_t slot, CqlBuffer* b, uint64_t size)
+{
+  if (!st || slot >= st->slot_count || !b) return;
+  if (!note_cuda(cudaMemsetAsync(b->dptr, 0, std::min(size, b->size), st->slots[slot].stream), "stream_zero")) st->slots[slot].failed = 1;
+}
+
+extern "C" void cqlcuda_stream_fill(CqlStream* st, uint32_t slot, CqlBuffer* b, uint64_t size, uint32_t value)
+{
+  if (!st || slot >= st->slot_count || !b) return;
+  if (!fill_words(b, size, value, st->slots[slot].stream)) st->slots[slot].failed = 1;
+}
+
+extern "C" void cqlcuda_stream_dispatch(CqlStream* st, uint32_t slot, CqlKernel* k, uint32_t gws, uint32_t lws)
+{
+  if (!st || slot >= st->slot_count || !k) return;
+  if (!dispatch(k, gws, lws, st->slots[slot].stream, &st->slots[slot].timings)) st->slots[slot].failed = 1;
+}
+
+extern "C" void cqlcuda_stream_read(CqlStream* st, uint32_t slot, CqlBuffer* b, void* out, uint64_t size)
+{
+  if (!st || slot >= st->slot_count) return;
+  if (!enqueue_read(st->slots[slot].staging, b, out, size, st->slots[slot].stream)) st->slots[slot].failed = 1;
+}
+
+extern "C" int cqlcuda_stream_submit(CqlStream* st, uint32_t slot)
+{
+  if (!st || slot >= st->slot_count) return 0;
+  CqlStreamSlot& sl = st->slots[slot];
+  if (!note_cuda(cudaEventRecord(sl.done, sl.stream), "stream_submit")) return 0;
+  sl.submitted = 1;
+  return !sl.failed;
+}
+
+extern "C" int cqlcuda_stream_wait(CqlStream* st, uint32_t slot)
+{
+  if (!st || slot >= st->slot_count) return 0;
+  CqlStreamSlot& sl = st->slots[slot];
+  int ok = !sl.failed;
+  if (sl.submitted) ok = wait_event(sl.done, "stream_wait") && ok;
+  else ok = wait_stream(sl.stream, "stream_wait") && ok;
+  staging_finish(sl.staging, ok);
+  if (ok) timings_collect(sl.timings);
+  sl.submitted = 0;
+  return ok;
+}
+
+extern "C" CqlStreamStats cqlcuda_stream_get_stats(CqlStream* st)
+{
+  CqlStreamStats z;
+  memset(&z, 0, sizeof(z));
+  return st ? st->stats : z;
+}
+
+// ---------------------------------------------------------------------------------------------
+// hooks and diagnostics
+
+extern "C" void cqlcuda_set_fault_alloc_at(uint64_t call_index) { S().fault_alloc_at = call_index; }
+extern "C" void cqlcuda_set_evict_hook(CqlEvictHook hook) { S().evict_hook = hook; }
+extern "C" void cqlcuda_kernel_profile_enable(int enabled) { S().profile_enabled = enabled; }
+extern "C" void cqlcuda_kernel_profile_reset(void)
+{
+  for (auto& p : S().profile)
+  {
+    p.total_ns = 0;
+    p.dispatches = 0;
+  }
+}
+extern "C" int cqlcuda_kernel_profile_entry(uint32_t index, const char** out_name, uint64_t* out_total_ns, uint64_t* out_dispatches)
+{
+  CqlState& s = S();
+  if (index >= s.profile.size()) return 0;
+  if (out_name) *out_name = s.profile[index].name.c_str();
+  if (out_total_ns) *out_total_ns = s.profile[index].total_ns;
+  if (out_dispatches) *out_dispatches = s.profile[index].dispatches;
+  return 1;
+}
+extern "C" uint32_t cqlcuda_kernel_launch_count(void) { return S().launches; }
+extern "C" const char* cqlcuda_last_error(void) { return S().last_error.c_str(); }
+extern "C" void cqlcuda_clear_error(void) { S().last_error.clear(); }
+extern "C" void cqlcuda_set_wait_timeout_ms(uint32_t ms) { S().wait_timeout_ms = ms ? ms : 1; }
+extern "C" void cqlcuda_set_module_cache_dir(const char* path) { S().cache_dir = path ? path : ""; }
+extern "C" void cqlcuda_set_fail_compile_every(uint32_t n) { S().fail_compile_every = n; }
+extern "C" const char* cqlcuda_last_compile_log(void) { return S().compile_log.c_str(); }
+
+// ---------------------------------------------------------------------------------------------
+// data generation and timing helpers
+
+// splitmix64 (src/tests/bench_common.h:30-37): draw k (0-based) of the stream seeded `seed` is
+// mix(seed + (k + 1) * golden), so any draw can be computed on its own.
+__device__ __forceinline__ uint64_t splitmix_draw(uint64_t seed, uint64_t k)
+{
+  uint64_t z = seed + (k + 1) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__global__ void k_fill_splitmix(uint32_t* out, uint64_t rows, uint64_t seed, uint32_t per_row, uint32_t index, uint64_t range)
+{
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (; i < rows; i += stride)
+  {
+    uint64_t v = splitmix_draw(seed, i * per_row + index);
+    out[i] = (uint32_t)(range ? v % range : v);
+  }
+}
+
+__global__ void k_fill_sequence(uint32_t* out, uint64_t rows, uint32_t first)
+{
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (; i < rows; i += stride) out[i] = first + (uint32_t)i;
+}
+
+extern "C" int cqlcuda_fill_splitmix_u32(CqlBuffer* b, uint64_t rows, uint64_t seed, uint32_t per_row, uint32_t index, uint64_t range)
+{
+  if (!b || rows * 4 > b->size || b->imported) return 0;
+  CqlState& s = S();
+  uint32_t grid = cql_stream_grid((rows + 255) / 256, 8);
+  k_fill_splitmix<<<grid, 256, 0, s.stream>>>((uint32_t*)b->dptr, rows, seed, per_row, index, range);
+  if (!note_cuda(cudaGetLastError(), "fill_splitmix")) return 0;
+  return wait_stream(s.stream, "fill_splitmix");
+}
+
+extern "C" int cqlcuda_fill_sequence_u32(CqlBuffer* b, uint64_t rows, uint32_t first)
+{
+  if (!b || rows * 4 > b->size || b->imported) return 0;
+  CqlState& s = S();
+  uint32_t grid = cql_stream_grid((rows + 255) / 256, 8);
+  k_fill_sequence<<<grid, 256, 0, s.stream>>>((uint32_t*)b->dptr, rows, first);
+  if (!note_cuda(cudaGetLastError(), "fill_sequence")) return 0;
+  return wait_stream(s.stream, "fill_sequence");
+}
+
+extern "C" int cqlcuda_flush_l2(uint64_t bytes)
+{
+  CqlState& s = S();
+  if (!ensure_init()) return 0;
+  if (s.flush_bytes < bytes)
+  {
+    if (s.flush_buf) cudaFree(s.flush_buf);
+    s.flush_buf = nullptr;
+    s.flush_bytes = 0;
+    if (cudaMalloc(&s.flush_buf, bytes) != cudaSuccess)
+    {
+      cudaGetLastError();
+      return 0;
+    }
+    s.flush_bytes = bytes;
+  }
+  return note_cuda(cudaMemsetAsync(s.flush_buf, 0x5a, bytes, s.stream), "flush_l2");
+}
+
+extern "C" void cqlcuda_timer_begin(void)
+{
+  if (!ensure_init()) return;
+  cudaEventRecord(S().timer_start, S().stream);
+}
+
+extern "C" double cqlcuda_timer_end_ms(void)
+{
+  CqlState& s = S();
+  cudaEventRecord(s.timer_stop, s.stream);
+  if (!wait_event(s.timer_stop, "timer")) return -1.0;
+  float ms = 0;
+  cudaEventElapsedTime(&ms, s.timer_start, s.timer_stop);
+  return ms;
+}

@@ -1,0 +1,551 @@
+/*
+ * cql_ops.c - C99 operator layer: drives the cqlcuda backend with the reference operator layer's
+ * kernels, bindings, push-constant words and host folds (src/query_exec/query_exec.c), on whole
+ * device-resident columns.
+ */
+#include "cqlops.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define QE_GPU_WORKGROUP_SIZE 256
+#define QE_AGG_STREAM_DEFAULT_GROUPS 2048
+#define QE_AGG_STREAM_MAX_COLUMNS 4
+#define QE_SIMPLE_SCAN_MAX_LEAVES 8
+#define QE_SIMPLE_SCAN_ROWS_PER_THREAD 8
+#define QE_MAX_COLUMN_BINDINGS 10
+#define QE_DENSE_STREAM_MAX_ARGS 4
+#define QE_DENSE_STREAM_MAX_GROUPS 65536
+#define QE_DENSE_STREAM_ACC_WORDS 2048
+#define QE_DENSE_STREAM_MM_WORDS 1024
+#define QE_DENSE_STREAM_MAX_TILES 256
+#define QE_AGG_MAX_EXPRS 8
+#define QE_F64_MAX 1.7976931348623157e308
+
+#define QE_SCAN_INT_FLAG  0x10000u
+#define QE_SCAN_INT_NEVER 0x20000u
+#define QE_SCAN_INT_BIAS  0x40000u
+
+static uint32_t g_launch_mark = 0;
+
+uint32_t cqlops_last_launches(void)
+{
+  return cqlcuda_kernel_launch_count() - g_launch_mark;
+}
+
+static void launches_begin(void)
+{
+  g_launch_mark = cqlcuda_kernel_launch_count();
+}
+
+static CqlKernel* kernel_named(const char* name)
+{
+  return cqlcuda_kernel_alloc(name, (uint64_t)strlen(name));
+}
+
+static CqlBuffer* pooled(const char* name, uint64_t size, uint32_t flags)
+{
+  return cqlcuda_buffer_alloc_pooled(name, (uint64_t)strlen(name), size, flags, NULL);
+}
+
+/* A column the kernels read as `width` bytes per row (qe_encoding_shader_width, query_exec.c:1593-1601). */
+static uint32_t shader_width(const CqlColumn* c)
+{
+  return c->width == 4 ? 0u : c->width;
+}
+
+/* ------------------------------------------------------------------------------------------------
+ * SUM / MIN / MAX of whole columns: qe_aggregate_global_streamed (query_exec.c:8842-9112) */
+
+int cqlops_aggregate_global(const CqlColumn* columns, uint32_t column_count, double* out_sum, double* out_min, double* out_max)
+{
+  launches_begin();
+  if (column_count == 0 || column_count > QE_AGG_STREAM_MAX_COLUMNS)
+  {
+    return 0;
+  }
+  uint64_t rows = columns[0].rows;
+  double sum[QE_AGG_STREAM_MAX_COLUMNS], mn[QE_AGG_STREAM_MAX_COLUMNS], mx[QE_AGG_STREAM_MAX_COLUMNS];
+  const CqlColumn* gpu_cols[QE_AGG_STREAM_MAX_COLUMNS];
+  uint32_t gpu_to_col[QE_AGG_STREAM_MAX_COLUMNS];
+  uint32_t gpu_count = 0;
+  for (uint32_t c = 0; c < column_count; c++)
+  {
+    const CqlColumn* col = &columns[c];
+    uint32_t t = col->type;
+    if (col->rows != rows || !(t == CQLOPS_TYPE_U32 || t == CQLOPS_TYPE_I32 || t == CQLOPS_TYPE_F32 || t == CQLOPS_TYPE_F64))
+    {
+      return 0;
+    }
+    sum[c] = 0.0;
+    mn[c] = QE_F64_MAX;
+    mx[c] = -QE_F64_MAX;
+    if (col->width == 3)
+    {
+      /* base + row number: n * first + n * (n - 1) / 2 in 64-bit whole numbers, rounded once (:8906-8916) */
+      int64_t first = t == CQLOPS_TYPE_I32 ? (int64_t)(int32_t)col->base : (int64_t)col->base;
+      uint64_t n = rows;
+      if (n > 0)
+      {
+        int64_t total = first * (int64_t)n + (int64_t)(n * (n - 1) / 2);
+        sum[c] = (double)total;
+        mn[c] = (double)first;
+        mx[c] = (double)first + (double)(n - 1);
+      }
+    }
+    else
+    {
+      if (!col->buffer)
+      {
+        return 0;
+      }
+      gpu_cols[gpu_count] = col;
+      gpu_to_col[gpu_count] = c;
+      gpu_count++;
+    }
+  }
+  if (gpu_count > 0 && rows > 0)
+  {
+    CqlKernel* k = kernel_named("aggregate_global_native");
+    if (!k)
+    {
+      return 0;
+    }
+    uint64_t group_count = QE_AGG_STREAM_DEFAULT_GROUPS;
+    uint64_t partial_count = group_count * gpu_count * 3;
+    CqlBuffer* partials_buf = pooled("cqlops_agg_global_partials", partial_count * sizeof(double), CQLCUDA_BUFFER_READ);
+    double* partials = (double*)malloc(partial_count * sizeof(double));
+    if (!partials_buf || !partials)
+    {
+      free(partials);
+      return 0;
+    }
+    /* a binding with no column behind it is bound to the first column; the kernel never reads it */
+    for (uint32_t b = 0; b < QE_AGG_STREAM_MAX_COLUMNS; b++)
+    {
+      cqlcuda_kernel_set_arg_buffer(k, b, gpu_cols[b < gpu_count ? b : 0]->buffer);
+    }
+    cqlcuda_kernel_set_arg_buffer(k, QE_AGG_STREAM_MAX_COLUMNS, partials_buf);
+    cqlcuda_kernel_set_arg_u64(k, 0, rows);
+    cqlcuda_kernel_set_arg_u64(k, 1, gpu_count);
+    cqlcuda_kernel_set_arg_u64(k, 2, group_count);
+    for (uint32_t c = 0; c < QE_AGG_STREAM_MAX_COLUMNS; c++)
+    {
+      uint64_t type_word = 0;
+      if (c < gpu_count)
+      {
+        type_word = (uint64_t)gpu_cols[c]->type | ((uint64_t)shader_width(gpu_cols[c]) << 8) | ((uint64_t)gpu_cols[c]->base << 32);
+      }
+      cqlcuda_kernel_set_arg_u64(k, 3 + c, type_word);
+    }
+    CqlBatch* batch = cqlcuda_batch_begin(0, partial_count * sizeof(double));
+    cqlcuda_batch_kernel_execute(batch, k, (uint32_t)(group_count * QE_GPU_WORKGROUP_SIZE), QE_GPU_WORKGROUP_SIZE);
+    cqlcuda_batch_buffer_read(batch, partials_buf, partials, partial_count * sizeof(double));
+    if (!cqlcuda_batch_end(batch))
+    {
+      free(partials);
+      return 0;
+    }
+    /* folded in workgroup order (qe_agg_stream_retire, :8812-8841) */
+    for (uint64_t g = 0; g < group_count; g++)
+    {
+      for (uint32_t c = 0; c < gpu_count; c++)
+      {
+        const double* triple = &partials[(g * gpu_count + c) * 3];
+        uint32_t dst = gpu_to_col[c];
+        sum[dst] += triple[0];
+        mn[dst] = triple[1] < mn[dst] ? triple[1] : mn[dst];
+        mx[dst] = triple[2] > mx[dst] ? triple[2] : mx[dst];
+      }
+    }
+    free(partials);
+  }
+  for (uint32_t c = 0; c < column_count; c++)
+  {
+    if (out_sum) out_sum[c] = sum[c];
+    if (out_min) out_min[c] = mn[c];
+    if (out_max) out_max[c] = mx[c];
+  }
+  return 1;
+}
+
+/* ------------------------------------------------------------------------------------------------
+ * scan_simple leaves: qe_scan_int_interval / qe_scan_int_leaf_words / qe_simple_leaf_words
+ * (query_exec.c:1378-1460), and the narrow rewrite of qe_scan_filter_streamed (:2294-2321). */
+
+static int scan_int_interval(uint32_t op, double target, double code_offset, double max_code, uint32_t* out_lo, uint32_t* out_span)
+{
+  if (target != target)
+  {
+    return 0;
+  }
+  double low = -1e18;
+  double high = 1e18;
+  switch (op)
+  {
+    case 0:
+      if (floor(target) != target) return 0;
+      low = target;
+      high = target;
+      break;
+    case 1: high = ceil(target) - 1.0; break;
+    case 2: high = floor(target); break;
+    case 3: low = floor(target) + 1.0; break;
+    case 4: low = ceil(target); break;
+    default: return 0;
+  }
+  low = low - code_offset;
+  if (low < 0.0) low = 0.0;
+  high = high - code_offset;
+  if (high > max_code) high = max_code;
+  if (low > high)
+  {
+    return 0;
+  }
+  *out_lo = (uint32_t)low;
+  *out_span = (uint32_t)(high - low);
+  return 1;
+}
+
+static void scan_int_leaf_words(uint32_t* words, uint32_t type, uint32_t op, double target, uint32_t width, uint32_t base)
+{
+  double code_offset = 0.0;
+  double max_code = 4294967295.0;
+  uint32_t flags = QE_SCAN_INT_FLAG;
+  if (width == 3)
+  {
+    code_offset = type == CQLOPS_TYPE_I32 ? (double)(int32_t)base : (double)base;
+  }
+  else if (width == 1 || width == 2)
+  {
+    max_code = width == 1 ? 255.0 : 65535.0;
+    code_offset = type == CQLOPS_TYPE_I32 ? (double)(int32_t)base : (double)base;
+  }
+  else if (type == CQLOPS_TYPE_I32)
+  {
+    code_offset = -2147483648.0;
+    flags |= QE_SCAN_INT_BIAS;
+  }
+  uint32_t lo = 0, span = 0;
+  if (!scan_int_interval(op, target, code_offset, max_code, &lo, &span))
+  {
+    flags |= QE_SCAN_INT_NEVER;
+  }
+  words[1] = type | (width << 8) | flags;
+  words[3] = lo;
+  words[4] = span;
+  words[5] = 0;
+}
+
+static int simple_leaf_words(uint32_t* words, uint32_t slot, const CqlColumn* col, uint32_t op, double target)
+{
+  uint64_t bits;
+  memcpy(&bits, &target, sizeof(bits));
+  words[0] = slot;
+  words[1] = col->type;
+  words[2] = op;
+  words[3] = (uint32_t)(bits & 0xffffffffu);
+  words[4] = (uint32_t)(bits >> 32);
+  words[5] = 0;
+  uint32_t w = shader_width(col);
+  if (col->type == CQLOPS_TYPE_U32 || col->type == CQLOPS_TYPE_I32)
+  {
+    scan_int_leaf_words(words, col->type, op, target, w, col->base);
+  }
+  else if (w != 0)
+  {
+    return 0; /* narrow or sequence encodings exist only for whole-number columns */
+  }
+  return 1;
+}
+
+static int cmp_u32(const void* a, const void* b)
+{
+  uint32_t x = *(const uint32_t*)a, y = *(const uint32_t*)b;
+  return x < y ? -1 : (x > y);
+}
+
+int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const CqlLeaf* leaves, uint32_t leaf_count, uint64_t* out_count,
+                       uint32_t* out_rows, uint64_t out_capacity)
+{
+  launches_begin();
+  if (leaf_count == 0 || leaf_count > QE_SIMPLE_SCAN_MAX_LEAVES || column_count == 0 || column_count > QE_MAX_COLUMN_BINDINGS)
+  {
+    return 0;
+  }
+  uint64_t rows = columns[0].rows;
+  uint32_t words[1 + QE_SIMPLE_SCAN_MAX_LEAVES * 6];
+  memset(words, 0, sizeof(words));
+  words[0] = leaf_count;
+  for (uint32_t l = 0; l < leaf_count; l++)
+  {
+    if (leaves[l].column >= column_count)
+    {
+      return 0;
+    }
+    const CqlColumn* col = &columns[leaves[l].column];
+    uint32_t t = col->type;
+    if (col->rows != rows || !(t == CQLOPS_TYPE_U32 || t == CQLOPS_TYPE_I32 || t == CQLOPS_TYPE_F32 || t == CQLOPS_TYPE_F64))
+    {
+      return 0;
+    }
+    if (!simple_leaf_words(&words[1 + l * 6], leaves[l].column, col, leaves[l].op, leaves[l].target))
+    {
+      return 0;
+    }
+  }
+  CqlKernel* k = kernel_named("scan_simple");
+  if (!k)
+  {
+    return 0;
+  }
+  CqlBuffer* leaf_buf = pooled("cqlops_scan_leaves", sizeof(words), CQLCUDA_BUFFER_WRITE);
+  CqlBuffer* counter = pooled("scan_filter_result_counter", 2 * sizeof(uint32_t), CQLCUDA_BUFFER_READ_WRITE);
+  if (!leaf_buf || !counter)
+  {
+    return 0;
+  }
+  /* the output list: none for a count, else sized like the reference (:3084-3090) and grown once */
+  int want_rows = out_rows != NULL;
+  uint64_t cap_rows = 0;
+  if (want_rows)
+  {
+    uint64_t default_cap = rows / 32 > 65536 ? rows / 32 : 65536;
+    cap_rows = default_cap < rows ? default_cap : rows;
+    if (cap_rows == 0) cap_rows = 1;
+  }
+  for (uint32_t c = 0; c < QE_MAX_COLUMN_BINDINGS; c++)
+  {
+    const CqlColumn* col = &columns[c < column_count ? c : 0];
+    CqlBuffer* b = col->buffer ? col->buffer : leaf_buf; /* a sequence column is never read */
+    cqlcuda_kernel_set_arg_buffer(k, 6 + c, b);
+  }
+  cqlcuda_kernel_set_arg_buffer(k, 0, leaf_buf);
+  cqlcuda_kernel_set_arg_buffer(k, 4, counter);
+  cqlcuda_kernel_set_arg_buffer(k, 5, counter); /* skip bitmap off */
+  cqlcuda_kernel_set_arg_u64(k, 0, rows);
+  cqlcuda_kernel_set_arg_u64(k, 3, 0);
+  cqlcuda_kernel_set_arg_u64(k, 4, 0);
+  cqlcuda_kernel_set_arg_u64(k, 5, 0);
+  uint64_t result_count = 0;
+  CqlBuffer* output = NULL;
+  for (int attempt = 0; attempt < 2; attempt++)
+  {
+    if (want_rows)
+    {
+      output = pooled("scan_filter_output", cap_rows * 2 * sizeof(uint32_t), CQLCUDA_BUFFER_READ);
+      if (!output) return 0;
+      cqlcuda_kernel_set_arg_buffer(k, 3, output);
+    }
+    else
+    {
+      /* no room for a row: the kernel counts only */
+      CqlBuffer* none = pooled("cqlops_scan_no_output", 0, CQLCUDA_BUFFER_READ);
+      if (!none) return 0;
+      cqlcuda_kernel_set_arg_buffer(k, 3, none);
+    }
+    uint32_t count32[2] = { 0, 0 };
+    CqlBatch* batch = cqlcuda_batch_begin(sizeof(words), sizeof(count32));
+    cqlcuda_batch_buffer_write(batch, leaf_buf, words, sizeof(words));
+    cqlcuda_batch_buffer_zero(batch, counter, sizeof(count32));
+    uint64_t threads = (rows + QE_SIMPLE_SCAN_ROWS_PER_THREAD - 1) / QE_SIMPLE_SCAN_ROWS_PER_THREAD;
+    cqlcuda_batch_kernel_execute(batch, k, (uint32_t)threads, QE_GPU_WORKGROUP_SIZE);
+    cqlcuda_batch_buffer_read(batch, counter, count32, sizeof(count32));
+    if (!cqlcuda_batch_end(batch))
+    {
+      return 0;
+    }
+    result_count = count32[0];
+    if (!want_rows || result_count <= cap_rows)
+    {
+      break;
+    }
+    cap_rows = result_count;
+  }
+  if (want_rows && result_count > cap_rows)
+  {
+    return 0;
+  }
+  if (want_rows && result_count > 0 && out_capacity > 0)
+  {
+    uint32_t* pairs = (uint32_t*)malloc(result_count * 2 * sizeof(uint32_t));
+    if (!pairs) return 0;
+    cqlcuda_buffer_read(output, pairs, result_count * 2 * sizeof(uint32_t));
+    uint32_t* list = (uint32_t*)malloc(result_count * sizeof(uint32_t));
+    if (!list)
+    {
+      free(pairs);
+      return 0;
+    }
+    for (uint64_t i = 0; i < result_count; i++) list[i] = pairs[i * 2];
+    qsort(list, result_count, sizeof(uint32_t), cmp_u32);
+    uint64_t n = result_count < out_capacity ? result_count : out_capacity;
+    memcpy(out_rows, list, n * sizeof(uint32_t));
+    free(list);
+    free(pairs);
+  }
+  if (out_count) *out_count = result_count;
+  return 1;
+}
+
+/* ------------------------------------------------------------------------------------------------
+ * Dense GROUP BY: qe_dense_stream_core (query_exec.c:7632-7983) on one chunk */
+
+int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* arg_cols,
+                       uint64_t max_groups, uint64_t* out_group_count, int64_t* out_min_key, uint64_t* out_counts, int64_t* out_sums,
+                       int64_t* out_mins, int64_t* out_maxs)
+{
+  launches_begin();
+  if (!key || !key->has_range || !(key->type == CQLOPS_TYPE_U32 || key->type == CQLOPS_TYPE_I32) || key->rows != rows || !key->buffer ||
+      key->width == 3 || key->zone_min < -2147483648.0 || key->zone_max > 2147483647.0 ||
+      key->zone_max - key->zone_min + 1.0 > (double)QE_DENSE_STREAM_MAX_GROUPS)
+  {
+    return 0;
+  }
+  int64_t min_key = (int64_t)key->zone_min;
+  uint64_t group_count = (uint64_t)((int64_t)key->zone_max - min_key) + 1;
+  if (group_count > max_groups || expr_count == 0 || expr_count > QE_AGG_MAX_EXPRS)
+  {
+    return 0;
+  }
+  const CqlColumn* arg_columns[QE_DENSE_STREAM_MAX_ARGS] = { 0 };
+  uint32_t arg_count = 0, func_codes = 0, arg_index_codes = 0, arg_signed_bits = 0;
+  double largest_sum_arg = 0.0;
+  int has_min_max = 0;
+  for (uint32_t e = 0; e < expr_count; e++)
+  {
+    uint32_t f = funcs[e];
+    if (f > CQLOPS_FUNC_MAX)
+    {
+      return 0;
+    }
+    func_codes |= (f & 0xfu) << (e * 4u);
+    if (f == CQLOPS_FUNC_COUNT)
+    {
+      continue;
+    }
+    const CqlColumn* col = arg_cols[e];
+    if (!col || !(col->type == CQLOPS_TYPE_U32 || col->type == CQLOPS_TYPE_I32) || col->rows != rows || (!col->buffer && col->width != 3))
+    {
+      return 0;
+    }
+    /* MIN and MAX are signed 32-bit atomics, so the values have to fit (:7712-7718) */
+    if ((f == CQLOPS_FUNC_MIN || f == CQLOPS_FUNC_MAX) && (!col->has_range || col->zone_min < -2147483648.0 || col->zone_max > 2147483647.0))
+    {
+      return 0;
+    }
+    if (f == CQLOPS_FUNC_MIN || f == CQLOPS_FUNC_MAX) has_min_max = 1;
+    if (f == CQLOPS_FUNC_SUM || f == CQLOPS_FUNC_AVG)
+    {
+      double m = col->has_range ? (col->zone_max > -col->zone_min ? col->zone_max : -col->zone_min) : 4294967296.0;
+      if (m > largest_sum_arg) largest_sum_arg = m;
+    }
+    uint32_t index = 0;
+    while (index < arg_count && arg_columns[index] != col) index++;
+    if (index == arg_count)
+    {
+      if (arg_count == QE_DENSE_STREAM_MAX_ARGS) return 0;
+      arg_columns[arg_count++] = col;
+    }
+    arg_index_codes |= (index & 0xfu) << (e * 4u);
+    if (col->type == CQLOPS_TYPE_I32) arg_signed_bits |= 1u << index;
+  }
+  uint64_t slice_rows = 16384;
+  int narrow_sums = largest_sum_arg * (double)slice_rows < 1073741824.0;
+  uint64_t acc_stride = (1 + (narrow_sums ? 1 : 2) * (uint64_t)expr_count) | 1;
+  uint64_t mm_stride = has_min_max ? (2 * (uint64_t)expr_count) | 1 : 0;
+  uint64_t tile_groups = QE_DENSE_STREAM_ACC_WORDS / acc_stride;
+  if (mm_stride && QE_DENSE_STREAM_MM_WORDS / mm_stride < tile_groups) tile_groups = QE_DENSE_STREAM_MM_WORDS / mm_stride;
+  if (tile_groups > group_count) tile_groups = group_count;
+  uint64_t tile_count = (group_count + tile_groups - 1) / tile_groups;
+  if (tile_count > QE_DENSE_STREAM_MAX_TILES)
+  {
+    return 0;
+  }
+  CqlKernel* k = kernel_named("aggregate_dense_native");
+  if (!k)
+  {
+    return 0;
+  }
+  /* the key's encoding base must be the smallest key (:7778-7781) */
+  uint64_t key_width = shader_width(key);
+  if ((key_width == 1 || key_width == 2) && key->base != (uint32_t)(int32_t)min_key)
+  {
+    return 0;
+  }
+  uint64_t shader_widths = key_width;
+  uint32_t arg_bases[QE_DENSE_STREAM_MAX_ARGS] = { 0 };
+  for (uint32_t i = 0; i < arg_count; i++)
+  {
+    shader_widths |= (uint64_t)shader_width(arg_columns[i]) << (4 + 4 * i);
+    arg_bases[i] = arg_columns[i]->base;
+  }
+  uint64_t info_bytes = group_count * 2 * sizeof(uint32_t);
+  uint64_t sum_bytes = group_count * expr_count * 2 * sizeof(uint32_t);
+  uint64_t mm_bytes = group_count * expr_count * sizeof(uint32_t);
+  CqlBuffer* info_buf = pooled("cqlops_dense_info", info_bytes, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* sum_buf = pooled("cqlops_dense_sums", sum_bytes, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* min_buf = pooled("cqlops_dense_mins", mm_bytes, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* max_buf = pooled("cqlops_dense_maxs", mm_bytes, CQLCUDA_BUFFER_READ_WRITE);
+  uint32_t* info = (uint32_t*)malloc(info_bytes);
+  uint32_t* sums = (uint32_t*)malloc(sum_bytes);
+  uint32_t* mins = (uint32_t*)malloc(mm_bytes);
+  uint32_t* maxs = (uint32_t*)malloc(mm_bytes);
+  int ok = info_buf && sum_buf && min_buf && max_buf && info && sums && mins && maxs;
+  if (ok)
+  {
+    cqlcuda_kernel_set_arg_buffer(k, 0, key->buffer);
+    for (uint32_t b = 0; b < QE_DENSE_STREAM_MAX_ARGS; b++)
+    {
+      const CqlColumn* col = b < arg_count ? arg_columns[b] : key;
+      cqlcuda_kernel_set_arg_buffer(k, 1 + b, col->buffer ? col->buffer : key->buffer);
+    }
+    cqlcuda_kernel_set_arg_buffer(k, 5, info_buf);
+    cqlcuda_kernel_set_arg_buffer(k, 6, sum_buf);
+    cqlcuda_kernel_set_arg_buffer(k, 7, min_buf);
+    cqlcuda_kernel_set_arg_buffer(k, 8, max_buf);
+    cqlcuda_kernel_set_arg_u64(k, 0, rows | (shader_widths << 32));
+    cqlcuda_kernel_set_arg_u64(k, 1, (uint64_t)expr_count | ((uint64_t)arg_bases[0] << 32));
+    cqlcuda_kernel_set_arg_u64(k, 2, (uint64_t)func_codes | ((uint64_t)arg_bases[1] << 32));
+    cqlcuda_kernel_set_arg_u64(k, 3, (uint64_t)arg_index_codes | ((uint64_t)(arg_signed_bits | (narrow_sums ? 0x80000000u : 0u)) << 32));
+    cqlcuda_kernel_set_arg_u64(k, 4, group_count | ((uint64_t)arg_bases[2] << 32));
+    cqlcuda_kernel_set_arg_u64(k, 5, (uint64_t)(uint32_t)(int32_t)min_key | ((uint64_t)arg_bases[3] << 32));
+    cqlcuda_kernel_set_arg_u64(k, 6, tile_groups | (slice_rows << 32));
+    cqlcuda_kernel_set_arg_u64(k, 7, tile_count);
+    CqlBatch* batch = cqlcuda_batch_begin(0, info_bytes + sum_bytes + 2 * mm_bytes);
+    cqlcuda_batch_buffer_fill(batch, info_buf, info_bytes, 0);
+    cqlcuda_batch_buffer_fill(batch, sum_buf, sum_bytes, 0);
+    cqlcuda_batch_buffer_fill(batch, min_buf, mm_bytes, 0x7fffffffu);
+    cqlcuda_batch_buffer_fill(batch, max_buf, mm_bytes, 0x80000000u);
+    uint64_t workgroups = (rows + slice_rows - 1) / slice_rows;
+    cqlcuda_batch_kernel_execute(batch, k, (uint32_t)(workgroups * QE_GPU_WORKGROUP_SIZE), QE_GPU_WORKGROUP_SIZE);
+    cqlcuda_batch_buffer_read(batch, info_buf, info, info_bytes);
+    cqlcuda_batch_buffer_read(batch, sum_buf, sums, sum_bytes);
+    cqlcuda_batch_buffer_read(batch, min_buf, mins, mm_bytes);
+    cqlcuda_batch_buffer_read(batch, max_buf, maxs, mm_bytes);
+    ok = cqlcuda_batch_end(batch);
+  }
+  if (ok)
+  {
+    /* qe_dense_stream_retire (:7600-7628) */
+    for (uint64_t g = 0; g < group_count; g++)
+    {
+      out_counts[g] = info[g * 2 + 1];
+      for (uint32_t e = 0; e < expr_count; e++)
+      {
+        uint64_t i = g * expr_count + e;
+        out_sums[i] = (int64_t)(((uint64_t)sums[i * 2 + 1] << 32) | (uint64_t)sums[i * 2]);
+        out_mins[i] = (int64_t)(int32_t)mins[i];
+        out_maxs[i] = (int64_t)(int32_t)maxs[i];
+      }
+    }
+    *out_group_count = group_count;
+    *out_min_key = min_key;
+  }
+  free(info);
+  free(sums);
+  free(mins);
+  free(maxs);
+  return ok;
+}

@@ -1,0 +1,166 @@
+"""ctypes bindings of the two native libraries.
+
+libcqlcuda.so is the backend (include/cqlcuda.h); libcqlops.so is the C99 operator layer over it
+(include/cqlops.h). Nothing here computes: every result comes from the CUDA kernels. Loading
+fails loudly when a library is missing; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_CUDA = os.path.join(PKG, "libcqlcuda.so")
+LIB_OPS = os.path.join(PKG, "libcqlops.so")
+
+P, u32, u64, i64, dbl, cstr = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int64, C.c_double, C.c_char_p
+
+
+class CqlMemoryStats(C.Structure):
+    _fields_ = [(n, u64) for n in ("bytes_in_use", "bytes_peak", "alloc_failures", "alloc_retry_successes", "pool_evictions",
+                                   "pool_evicted_bytes", "alloc_calls", "unrecovered_alloc_failures")]
+
+
+class CqlStreamStats(C.Structure):
+    _fields_ = [("bytes_copied", u64), ("imports_created", u64), ("import_microseconds", u64), ("staged_bytes", u64),
+                ("separate_copy_queue", u32)]
+
+
+class CqlColumn(C.Structure):
+    _fields_ = [("type", u32), ("width", u32), ("base", u32), ("has_range", u32), ("rows", u64), ("buffer", P),
+                ("zone_min", dbl), ("zone_max", dbl)]
+
+
+class CqlLeaf(C.Structure):
+    _fields_ = [("column", u32), ("op", u32), ("target", dbl)]
+
+
+# (name, restype, argtypes) of every entry point include/cqlcuda.h declares
+CUDA_API = [
+    ("cqlcuda_init", C.c_int, []),
+    ("cqlcuda_release", None, []),
+    ("cqlcuda_wait", None, []),
+    ("cqlcuda_get_executed_kernel_time_microseconds", u64, []),
+    ("cqlcuda_device_total_memory", u64, []),
+    ("cqlcuda_device_free_memory", u64, []),
+    ("cqlcuda_device_max_storage_buffer_range", u64, []),
+    ("cqlcuda_device_lost", C.c_int, []),
+    ("cqlcuda_pool_begin_epoch", None, []),
+    ("cqlcuda_memory_stats", CqlMemoryStats, []),
+    ("cqlcuda_sm_count", u32, []),
+    ("cqlcuda_buffer_alloc", P, [u64, u32, P]),
+    ("cqlcuda_buffer_alloc_pooled", P, [cstr, u64, u64, u32, P]),
+    ("cqlcuda_buffer_import_host_readonly", P, [P, u64]),
+    ("cqlcuda_buffer_import_host_readonly_pooled", P, [cstr, u64, P, u64]),
+    ("cqlcuda_buffer_release", None, [P]),
+    ("cqlcuda_buffer_write", None, [P, P, u64]),
+    ("cqlcuda_buffer_read", None, [P, P, u64]),
+    ("cqlcuda_buffer_size", u64, [P]),
+    ("cqlcuda_buffer_device_pointer", P, [P]),
+    ("cqlcuda_kernel_alloc", P, [cstr, u64]),
+    ("cqlcuda_kernel_alloc_from_image", P, [cstr, u64, P, u64]),
+    ("cqlcuda_kernel_alloc_from_image_spec", P, [cstr, u64, P, u64, P, u32]),
+    ("cqlcuda_generated_kernel_stats", None, [P, P]),
+    ("cqlcuda_kernel_release", None, [P]),
+    ("cqlcuda_kernel_execute", None, [P, u32, u32]),
+    ("cqlcuda_kernel_set_arg_buffer", None, [P, u32, P]),
+    ("cqlcuda_kernel_set_arg_u64", None, [P, u32, u64]),
+    ("cqlcuda_kernel_set_arg_buffer_range", None, [P, u32, P, u64, u64]),
+    ("cqlcuda_batch_begin", P, [u64, u64]),
+    ("cqlcuda_batch_buffer_write", None, [P, P, P, u64]),
+    ("cqlcuda_batch_buffer_zero", None, [P, P, u64]),
+    ("cqlcuda_batch_buffer_fill", None, [P, P, u64, u32]),
+    ("cqlcuda_batch_kernel_execute", None, [P, P, u32, u32]),
+    ("cqlcuda_batch_buffer_read", None, [P, P, P, u64]),
+    ("cqlcuda_batch_end", C.c_int, [P]),
+    ("cqlcuda_stream_alloc", P, [u32]),
+    ("cqlcuda_stream_release", None, [P]),
+    ("cqlcuda_stream_slot_begin", C.c_int, [P, u32, u64, u64]),
+    ("cqlcuda_stream_copy", C.c_int, [P, u32, P, P, u64]),
+    ("cqlcuda_stream_zero", None, [P, u32, P, u64]),
+    ("cqlcuda_stream_fill", None, [P, u32, P, u64, u32]),
+    ("cqlcuda_stream_dispatch", None, [P, u32, P, u32, u32]),
+    ("cqlcuda_stream_read", None, [P, u32, P, P, u64]),
+    ("cqlcuda_stream_submit", C.c_int, [P, u32]),
+    ("cqlcuda_stream_wait", C.c_int, [P, u32]),
+    ("cqlcuda_stream_get_stats", CqlStreamStats, [P]),
+    ("cqlcuda_set_fault_alloc_at", None, [u64]),
+    ("cqlcuda_set_evict_hook", None, [P]),
+    ("cqlcuda_kernel_profile_enable", None, [C.c_int]),
+    ("cqlcuda_kernel_profile_reset", None, []),
+    ("cqlcuda_kernel_profile_entry", C.c_int, [u32, P, P, P]),
+    ("cqlcuda_kernel_launch_count", u32, []),
+    ("cqlcuda_last_error", cstr, []),
+    ("cqlcuda_clear_error", None, []),
+    ("cqlcuda_set_wait_timeout_ms", None, [u32]),
+    ("cqlcuda_set_module_cache_dir", None, [cstr]),
+    ("cqlcuda_set_fail_compile_every", None, [u32]),
+    ("cqlcuda_last_compile_log", cstr, []),
+    ("cqlcuda_fill_splitmix_u32", C.c_int, [P, u64, u64, u32, u32, u64]),
+    ("cqlcuda_fill_sequence_u32", C.c_int, [P, u64, u32]),
+    ("cqlcuda_flush_l2", C.c_int, [u64]),
+    ("cqlcuda_timer_begin", None, []),
+    ("cqlcuda_timer_end_ms", dbl, []),
+]
+
+OPS_API = [
+    ("cqlops_aggregate_global", C.c_int, [P, u32, P, P, P]),
+    ("cqlops_scan_simple", C.c_int, [P, u32, P, u32, P, P, u64]),
+    ("cqlops_group_dense", C.c_int, [P, u64, u32, P, P, u64, P, P, P, P, P, P]),
+    ("cqlops_last_launches", u32, []),
+]
+
+_cuda = None
+_ops = None
+
+
+def _bind(lib, api):
+    for name, res, args in api:
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+
+
+def load_cuda():
+    global _cuda
+    if _cuda is None:
+        if not os.path.exists(LIB_CUDA):
+            raise RuntimeError(f"{LIB_CUDA} is not built: run computeql_gb300.build.build() (or __graft_entry__.build())")
+        lib = C.CDLL(LIB_CUDA, mode=C.RTLD_GLOBAL)
+        _bind(lib, CUDA_API)
+        _cuda = lib
+    return _cuda
+
+
+def load_ops():
+    global _ops
+    if _ops is None:
+        load_cuda()
+        if not os.path.exists(LIB_OPS):
+            raise RuntimeError(f"{LIB_OPS} is not built")
+        lib = C.CDLL(LIB_OPS)
+        _bind(lib, OPS_API)
+        _ops = lib
+    return _ops
+
+
+class CudaError(RuntimeError):
+    pass
+
+
+def last_error():
+    e = load_cuda().cqlcuda_last_error()
+    return e.decode() if e else ""
+
+
+def init():
+    lib = load_cuda()
+    if not lib.cqlcuda_init():
+        raise CudaError("cqlcuda_init failed: " + last_error())
+    return lib
+
+
+def ptr(a):
+    return C.c_void_p(a.ctypes.data)

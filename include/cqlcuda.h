@@ -1,0 +1,182 @@
+/*
+ * cqlcuda.h - C ABI of the GB300 (sm_103a) execution backend for ComputeQL's GPU operators.
+ *
+ * Every entry point here replaces one function pointer of the reference's backend vtable
+ * `GPU_Backend` (src/gpu/gpu_backend.h:179-233) or one forwarder of the backend-neutral API
+ * (src/gpu/gpu.h:95-159). The reference's operator layer (src/query_exec) keeps calling
+ * gpu_* functions; a C99 adapter (gpu_cuda.c, listed in INTEGRATION.md) fills the vtable with
+ * these functions. Types are plain C: opaque handles, pointers and sizes, no CUDA or torch types.
+ *
+ * Kernels are looked up by the names of the reference's shaders (src/gpu/vulkan/shaders/<name>.comp)
+ * and honour the same binding contract: up to 16 buffer bindings and 8 U64 push-constant slots,
+ * seen by the kernel as 16 32-bit words, low word first (src/gpu/vulkan/gpu_vulkan.h:6-9).
+ * A kernel is free to pick its own grid: `global_work_size`/`local_work_size` are accepted for
+ * contract compatibility, and each kernel writes exactly the outputs its shader writes, with
+ * entries the shader would leave for workgroups it did not launch filled with neutral values.
+ *
+ * Errors follow the reference: allocation failure returns NULL, a failed batch or stream wait
+ * returns 0, a sticky device-lost flag is raised on unrecoverable CUDA errors, and the text of
+ * the last error is available from cqlcuda_last_error().
+ */
+#ifndef CQLCUDA_H
+#define CQLCUDA_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CQLCUDA_MAX_BINDINGS 16
+#define CQLCUDA_PUSH_SLOTS   8
+
+/* Buffer flags, bit-for-bit the reference's GPU_BufferFlags (src/gpu/gpu.h:8-22). */
+enum
+{
+  CQLCUDA_BUFFER_READ              = 1u << 0,
+  CQLCUDA_BUFFER_WRITE             = 1u << 1,
+  CQLCUDA_BUFFER_READ_WRITE        = 1u << 2,
+  CQLCUDA_BUFFER_HOST_VISIBLE      = 1u << 3,
+  CQLCUDA_BUFFER_DEVICE_LOCAL      = 1u << 4,
+  CQLCUDA_BUFFER_HOST_CACHED       = 1u << 5,
+  CQLCUDA_BUFFER_ZERO_COPY         = 1u << 6,
+  CQLCUDA_BUFFER_COPY_HOST_POINTER = 1u << 7,
+  CQLCUDA_BUFFER_DYNAMIC           = 1u << 8,
+  CQLCUDA_BUFFER_SHARED            = 1u << 9,
+};
+
+typedef struct CqlBuffer CqlBuffer;
+typedef struct CqlKernel CqlKernel;
+typedef struct CqlBatch  CqlBatch;
+typedef struct CqlStream CqlStream;
+
+/* Same fields and order as GPU_MemoryStats (src/gpu/gpu.h:24-35). */
+typedef struct CqlMemoryStats
+{
+  uint64_t bytes_in_use;
+  uint64_t bytes_peak;
+  uint64_t alloc_failures;
+  uint64_t alloc_retry_successes;
+  uint64_t pool_evictions;
+  uint64_t pool_evicted_bytes;
+  uint64_t alloc_calls;
+  uint64_t unrecovered_alloc_failures;
+} CqlMemoryStats;
+
+/* Same fields and order as GPU_StreamStats (src/gpu/gpu.h:87-94). */
+typedef struct CqlStreamStats
+{
+  uint64_t bytes_copied;
+  uint64_t imports_created;
+  uint64_t import_microseconds;
+  uint64_t staged_bytes;
+  uint32_t separate_copy_queue;
+} CqlStreamStats;
+
+/* Eviction hook: GPU_EvictHook (src/gpu/gpu.h:111-113). Called with the bytes still wanted after
+   pooled buffers were evicted; returns the bytes it freed. */
+typedef uint64_t (*CqlEvictHook)(uint64_t bytes_wanted);
+
+/* ---- device (GPU_Backend init/release/wait/... gpu_backend.h:183-192) ---- */
+int      cqlcuda_init(void);                                   /* gpu_backend.h:183 init; returns 1 on success */
+void     cqlcuda_release(void);                                /* gpu_backend.h:184 release */
+void     cqlcuda_wait(void);                                   /* gpu_backend.h:185 wait */
+uint64_t cqlcuda_get_executed_kernel_time_microseconds(void);  /* gpu_backend.h:186 */
+uint64_t cqlcuda_device_total_memory(void);                    /* gpu_backend.h:187 */
+uint64_t cqlcuda_device_free_memory(void);                     /* gpu_backend.h:188 */
+uint64_t cqlcuda_device_max_storage_buffer_range(void);        /* gpu_backend.h:189 */
+int      cqlcuda_device_lost(void);                            /* gpu_backend.h:190 */
+void     cqlcuda_pool_begin_epoch(void);                       /* gpu_backend.h:191 */
+CqlMemoryStats cqlcuda_memory_stats(void);                     /* gpu_backend.h:192 */
+uint32_t cqlcuda_sm_count(void);                               /* device property the kernels size grids by */
+
+/* ---- buffers (gpu_backend.h:194-200) ---- */
+CqlBuffer* cqlcuda_buffer_alloc(uint64_t size, uint32_t flags, const void* data);                       /* :194 */
+CqlBuffer* cqlcuda_buffer_alloc_pooled(const char* name, uint64_t name_len, uint64_t size,
+                                       uint32_t flags, const void* data);                             /* :195 */
+CqlBuffer* cqlcuda_buffer_import_host_readonly(const void* host_ptr, uint64_t size);                   /* :196 */
+CqlBuffer* cqlcuda_buffer_import_host_readonly_pooled(const char* name, uint64_t name_len,
+                                                      const void* host_ptr, uint64_t size);           /* :197 */
+void       cqlcuda_buffer_release(CqlBuffer* buffer);                                                  /* :198 */
+void       cqlcuda_buffer_write(CqlBuffer* buffer, const void* data, uint64_t size);                   /* :199 */
+void       cqlcuda_buffer_read(CqlBuffer* buffer, void* data, uint64_t size);                          /* :200 */
+uint64_t   cqlcuda_buffer_size(const CqlBuffer* buffer);       /* the bound range a kernel sees (VkDescriptorBufferInfo.range, gpu_vulkan.c:2797) */
+void*      cqlcuda_buffer_device_pointer(const CqlBuffer* buffer); /* for zero-copy interop (DLPack/torch) by host code */
+
+/* ---- kernels (gpu_backend.h:202-209) ---- */
+CqlKernel* cqlcuda_kernel_alloc(const char* name, uint64_t name_len);                                  /* :202, by shader name */
+/* :203 kernel_alloc_from_spirv. The reference hands over SPIR-V; here `image` is CUDA C++ source
+   (compiled with NVRTC for sm_103a) or a cubin. An empty image only looks the name up. */
+CqlKernel* cqlcuda_kernel_alloc_from_image(const char* name, uint64_t name_len, const void* image, uint64_t image_len);
+CqlKernel* cqlcuda_kernel_alloc_from_image_spec(const char* name, uint64_t name_len, const void* image, uint64_t image_len,
+                                                const uint32_t* spec_values, uint32_t spec_count);    /* :204 */
+void       cqlcuda_generated_kernel_stats(uint64_t* out_compiles, uint64_t* out_evictions);            /* :205 */
+void       cqlcuda_kernel_release(CqlKernel* kernel);                                                  /* :206, kernels are cached: no-op */
+void       cqlcuda_kernel_execute(CqlKernel* kernel, uint32_t global_work_size, uint32_t local_work_size); /* :207, synchronous */
+void       cqlcuda_kernel_set_arg_buffer(CqlKernel* kernel, uint32_t index, CqlBuffer* buffer);        /* :208 */
+void       cqlcuda_kernel_set_arg_u64(CqlKernel* kernel, uint32_t index, uint64_t value);              /* :209 */
+/* Binding at a byte offset into a buffer: a chunk of a resident column without a copy. Not in the
+   reference vtable; the adapter uses offset 0. */
+void       cqlcuda_kernel_set_arg_buffer_range(CqlKernel* kernel, uint32_t index, CqlBuffer* buffer, uint64_t offset, uint64_t size);
+
+/* ---- batches (gpu_backend.h:211-217) ---- */
+CqlBatch* cqlcuda_batch_begin(uint64_t upload_bytes_needed, uint64_t download_bytes_needed);           /* :211 */
+void      cqlcuda_batch_buffer_write(CqlBatch* batch, CqlBuffer* buffer, const void* data, uint64_t size); /* :212 */
+void      cqlcuda_batch_buffer_zero(CqlBatch* batch, CqlBuffer* buffer, uint64_t size);                 /* :213 */
+void      cqlcuda_batch_buffer_fill(CqlBatch* batch, CqlBuffer* buffer, uint64_t size, uint32_t value);  /* :214 */
+void      cqlcuda_batch_kernel_execute(CqlBatch* batch, CqlKernel* kernel, uint32_t global_work_size, uint32_t local_work_size); /* :215 */
+void      cqlcuda_batch_buffer_read(CqlBatch* batch, CqlBuffer* buffer, void* out_data, uint64_t size);  /* :216 */
+int       cqlcuda_batch_end(CqlBatch* batch);                                                            /* :217, 0 on failure (reads zero-filled) */
+
+/* ---- streams (gpu_backend.h:219-229) ---- */
+CqlStream* cqlcuda_stream_alloc(uint32_t slot_count);                                                    /* :219, 1..8 slots */
+void       cqlcuda_stream_release(CqlStream* stream);                                                    /* :220 */
+int        cqlcuda_stream_slot_begin(CqlStream* stream, uint32_t slot, uint64_t upload_bytes, uint64_t readback_bytes); /* :221 */
+int        cqlcuda_stream_copy(CqlStream* stream, uint32_t slot, CqlBuffer* destination, const void* host_ptr, uint64_t size); /* :222 */
+void       cqlcuda_stream_zero(CqlStream* stream, uint32_t slot, CqlBuffer* buffer, uint64_t size);      /* :223 */
+void       cqlcuda_stream_fill(CqlStream* stream, uint32_t slot, CqlBuffer* buffer, uint64_t size, uint32_t value); /* :224 */
+void       cqlcuda_stream_dispatch(CqlStream* stream, uint32_t slot, CqlKernel* kernel, uint32_t global_work_size, uint32_t local_work_size); /* :225 */
+void       cqlcuda_stream_read(CqlStream* stream, uint32_t slot, CqlBuffer* buffer, void* out_data, uint64_t size); /* :226 */
+int        cqlcuda_stream_submit(CqlStream* stream, uint32_t slot);                                      /* :227 */
+int        cqlcuda_stream_wait(CqlStream* stream, uint32_t slot);                                        /* :228, bounded wait */
+CqlStreamStats cqlcuda_stream_get_stats(CqlStream* stream);                                              /* :229 */
+
+/* ---- failure injection, eviction hook, kernel log and profile (src/gpu/gpu.h:38-113) ---- */
+void     cqlcuda_set_fault_alloc_at(uint64_t call_index);     /* g_gpu_fault_alloc_at (gpu.h:68): the k-th allocation call fails, 0 = off */
+void     cqlcuda_set_evict_hook(CqlEvictHook hook);           /* g_gpu_evict_hook (gpu.h:111-113) */
+void     cqlcuda_kernel_profile_enable(int enabled);          /* g_gpu_kernel_profile.enabled (gpu.h:48-58) */
+void     cqlcuda_kernel_profile_reset(void);                  /* gpu_kernel_profile_reset (gpu.h:61) */
+/* Profile entry i: its kernel name, total GPU nanoseconds and dispatch count. Returns 0 past the end. */
+int      cqlcuda_kernel_profile_entry(uint32_t index, const char** out_name, uint64_t* out_total_ns, uint64_t* out_dispatches);
+uint32_t cqlcuda_kernel_launch_count(void);                   /* launches of this library's kernels since init */
+const char* cqlcuda_last_error(void);                         /* text of the last error, "" when none */
+void     cqlcuda_clear_error(void);
+/* Seconds a stream or batch wait polls before it gives up and reports failure (the reference's
+   30 s stream timeout, src/gpu/vulkan/gpu_vulkan.h:235). */
+void     cqlcuda_set_wait_timeout_ms(uint32_t milliseconds);
+
+/* ---- NVRTC (the shaderc replacement behind kernel_alloc_from_spirv, src/query_exec/query_kernel.c:294-457) ---- */
+/* Disk cache directory for compiled cubins (empty = memory only). */
+void     cqlcuda_set_module_cache_dir(const char* path);
+/* Test hook mirroring QE_TEST_FAIL_SHADERC (src/query_exec/query_kernel.h:21-24): every n-th compile fails, 0 = off. */
+void     cqlcuda_set_fail_compile_every(uint32_t n);
+const char* cqlcuda_last_compile_log(void);
+
+/* ---- raw device helpers used by the bench and tests (not in the reference vtable) ---- */
+/* Fills `rows` rows of a u32 column from the splitmix64 stream seeded `seed`: row r takes draw
+   r*draws_per_row + draw_index (0-based) and stores draw % range (range 0 = the full 32 bits). */
+int      cqlcuda_fill_splitmix_u32(CqlBuffer* buffer, uint64_t rows, uint64_t seed, uint32_t draws_per_row, uint32_t draw_index, uint64_t range);
+/* Fills value[r] = first + r for r < rows. */
+int      cqlcuda_fill_sequence_u32(CqlBuffer* buffer, uint64_t rows, uint32_t first);
+/* Writes `bytes` bytes of a scratch buffer, to evict the L2 between timed runs. */
+int      cqlcuda_flush_l2(uint64_t bytes);
+/* CUDA-event timing of everything the library enqueues between begin and end, on its own stream. */
+void     cqlcuda_timer_begin(void);
+double   cqlcuda_timer_end_ms(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CQLCUDA_H */

@@ -1,0 +1,147 @@
+"""CPU oracle: a C restatement of the reference's algorithms, loaded with ctypes.
+
+TEST INFRASTRUCTURE ONLY. Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg
+(and its --impl reference arm) may import this package; the product never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+SOURCES = [os.path.join(HERE, "oracle.c")]
+
+U32, U64, F32, F64, I32, I64 = 1, 2, 3, 4, 7, 8
+
+_lib = None
+
+
+def build():
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    deps = SOURCES + [os.path.join(HERE, "oracle.h")]
+    if os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
+        return LIB
+    cmd = ["gcc", "-std=c99", "-O2", "-fPIC", "-shared", "-Wall", "-o", LIB, *SOURCES, "-lpthread", "-lm"]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout)
+    return LIB
+
+
+class OrcLeaf(C.Structure):
+    _fields_ = [("values", C.c_void_p), ("type", C.c_uint32), ("op", C.c_uint32), ("target", C.c_double)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        P, u32, u64, dbl = C.c_void_p, C.c_uint32, C.c_uint64, C.c_double
+        L.orc_set_threads.argtypes = [u32]
+        L.orc_threads.restype = u32
+        L.orc_splitmix_draw.argtypes = [u64, u64]
+        L.orc_splitmix_draw.restype = u64
+        L.orc_fill_splitmix_u32.argtypes = [P, u64, u64, u32, u32, u64]
+        L.orc_fill_closed_form.argtypes = [P, P, P, P, u64]
+        L.orc_aggregate_global_cpu.argtypes = [P, u32, u64, u32, P, P, P]
+        L.orc_aggregate_global_gpu_order.argtypes = [P, u32, u64, P, P, P]
+        L.orc_compensated_sum.argtypes = [P, u32, u64]
+        L.orc_compensated_sum.restype = dbl
+        L.orc_scan_and.argtypes = [P, u32, u64, P, u64]
+        L.orc_scan_and.restype = u64
+        L.orc_group_dense.argtypes = [P, u32, u64, C.c_int64, u64, u32, P, P, P, P, P, P, P]
+        L.orc_group_cpu_reduce.argtypes = [P, u64, u32, P, u64, P, P, P, P, P]
+        L.orc_group_cpu_reduce.restype = u64
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def set_threads(n):
+    lib().orc_set_threads(n)
+
+
+def splitmix_u32(rows, seed, per_row, index, rng):
+    out = np.empty(rows, dtype=np.uint32)
+    lib().orc_fill_splitmix_u32(_p(out), rows, seed, per_row, index, rng)
+    return out
+
+
+def closed_form(rows):
+    cols = [np.empty(rows, dtype=np.uint32) for _ in range(4)]
+    lib().orc_fill_closed_form(*[_p(c) for c in cols], rows)
+    return cols
+
+
+_NP_TYPE = {np.dtype(np.uint32): U32, np.dtype(np.int32): I32, np.dtype(np.float32): F32, np.dtype(np.float64): F64,
+            np.dtype(np.uint64): U64, np.dtype(np.int64): I64}
+
+
+def type_of(arr):
+    return _NP_TYPE[arr.dtype]
+
+
+def aggregate_global_cpu(values, tasks=0):
+    s, mn, mx = C.c_double(), C.c_double(), C.c_double()
+    lib().orc_aggregate_global_cpu(_p(values), type_of(values), len(values), tasks, C.byref(s), C.byref(mn), C.byref(mx))
+    return s.value, mn.value, mx.value
+
+
+def aggregate_global_gpu_order(values):
+    s, mn, mx = C.c_double(), C.c_double(), C.c_double()
+    lib().orc_aggregate_global_gpu_order(_p(values), type_of(values), len(values), C.byref(s), C.byref(mn), C.byref(mx))
+    return s.value, mn.value, mx.value
+
+
+def compensated_sum(values):
+    return lib().orc_compensated_sum(_p(values), type_of(values), len(values))
+
+
+def scan_and(leaves, rows, want_rows=False):
+    """leaves: list of (array, op, target). Returns (count, rows or None)."""
+    arr = (OrcLeaf * len(leaves))()
+    for i, (a, op, t) in enumerate(leaves):
+        arr[i] = OrcLeaf(a.ctypes.data, type_of(a), op, float(t))
+    out = None
+    cap = 0
+    if want_rows:
+        out = np.empty(rows, dtype=np.uint32)
+        cap = rows
+    n = lib().orc_scan_and(arr, len(leaves), rows, _p(out) if out is not None else None, cap)
+    return n, (out[:n].copy() if out is not None else None)
+
+
+def group_dense(key, min_key, groups, funcs, args):
+    """funcs: list of codes; args: list of arrays (or None for COUNT). Returns counts, sums, mins, maxs."""
+    e = len(funcs)
+    counts = np.zeros(groups, dtype=np.uint64)
+    sums = np.zeros(groups * e, dtype=np.int64)
+    mins = np.zeros(groups * e, dtype=np.int64)
+    maxs = np.zeros(groups * e, dtype=np.int64)
+    fa = np.array(funcs, dtype=np.uint32)
+    keep = [a if a is not None else key for a in args]
+    ptrs = (C.c_void_p * e)(*[a.ctypes.data for a in keep])
+    types = np.array([type_of(a) for a in keep], dtype=np.uint32)
+    lib().orc_group_dense(_p(key), type_of(key), len(key), int(min_key), groups, e, _p(fa), ptrs, _p(types), _p(counts), _p(sums),
+                          _p(mins), _p(maxs))
+    return counts, sums.reshape(groups, e), mins.reshape(groups, e), maxs.reshape(groups, e)
+
+
+def group_cpu_reduce(key, args, max_groups):
+    e = len(args)
+    keys = np.zeros(max_groups, dtype=np.uint32)
+    counts = np.zeros(max_groups, dtype=np.uint64)
+    sums = np.zeros(max_groups * max(e, 1), dtype=np.float64)
+    mins = np.zeros(max_groups * max(e, 1), dtype=np.float64)
+    maxs = np.zeros(max_groups * max(e, 1), dtype=np.float64)
+    ptrs = (C.c_void_p * max(e, 1))(*[a.ctypes.data for a in args] if e else [None])
+    n = lib().orc_group_cpu_reduce(_p(key), len(key), e, ptrs, max_groups, _p(keys), _p(counts), _p(sums), _p(mins), _p(maxs))
+    return keys[:n], counts[:n], sums[: n * e].reshape(n, e), mins[: n * e].reshape(n, e), maxs[: n * e].reshape(n, e)

@@ -1,0 +1,481 @@
+/*
+ * oracle.c - CPU restatement of the reference's algorithms (TEST INFRASTRUCTURE ONLY: the checker
+ * used by tests/, the smoke check and the bench's CPU-baseline leg; never part of the product).
+ * Each function cites the reference source it restates.
+ */
+#include "oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+#define ORC_F64_MAX 1.7976931348623157e308
+
+static uint32_t g_threads = 0;
+
+void orc_set_threads(uint32_t n) { g_threads = n; }
+
+uint32_t orc_threads(void)
+{
+  if (g_threads) return g_threads;
+  long n = sysconf(_SC_NPROCESSORS_ONLN);
+  return n > 0 ? (uint32_t)n : 1u;
+}
+
+/* ---- a small parallel-for over task ids ---- */
+typedef void (*orc_task_fn)(void* ctx, uint32_t task_id);
+typedef struct
+{
+  orc_task_fn fn;
+  void* ctx;
+  uint32_t tasks;
+  uint32_t next;
+  pthread_mutex_t lock;
+} orc_pool;
+
+static void* orc_worker(void* p)
+{
+  orc_pool* pool = (orc_pool*)p;
+  for (;;)
+  {
+    pthread_mutex_lock(&pool->lock);
+    uint32_t id = pool->next++;
+    pthread_mutex_unlock(&pool->lock);
+    if (id >= pool->tasks) break;
+    pool->fn(pool->ctx, id);
+  }
+  return NULL;
+}
+
+static void orc_parallel(uint32_t tasks, orc_task_fn fn, void* ctx)
+{
+  uint32_t workers = orc_threads();
+  if (workers > tasks) workers = tasks;
+  if (workers <= 1)
+  {
+    for (uint32_t i = 0; i < tasks; i++) fn(ctx, i);
+    return;
+  }
+  orc_pool pool;
+  pool.fn = fn;
+  pool.ctx = ctx;
+  pool.tasks = tasks;
+  pool.next = 0;
+  pthread_mutex_init(&pool.lock, NULL);
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * workers);
+  for (uint32_t i = 0; i < workers; i++) pthread_create(&th[i], NULL, orc_worker, &pool);
+  for (uint32_t i = 0; i < workers; i++) pthread_join(th[i], NULL);
+  free(th);
+  pthread_mutex_destroy(&pool.lock);
+}
+
+/* ---- data ---- */
+
+uint64_t orc_splitmix_draw(uint64_t seed, uint64_t k)
+{
+  uint64_t z = seed + (k + 1) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+typedef struct
+{
+  uint32_t* out;
+  uint64_t rows, seed, range;
+  uint32_t per_row, index, tasks;
+} fill_ctx;
+
+static void fill_task(void* p, uint32_t id)
+{
+  fill_ctx* c = (fill_ctx*)p;
+  uint64_t per = (c->rows + c->tasks - 1) / c->tasks;
+  uint64_t lo = (uint64_t)id * per, hi = lo + per;
+  if (hi > c->rows) hi = c->rows;
+  for (uint64_t r = lo; r < hi; r++)
+  {
+    uint64_t v = orc_splitmix_draw(c->seed, r * c->per_row + c->index);
+    c->out[r] = (uint32_t)(c->range ? v % c->range : v);
+  }
+}
+
+void orc_fill_splitmix_u32(uint32_t* out, uint64_t rows, uint64_t seed, uint32_t per_row, uint32_t index, uint64_t range)
+{
+  fill_ctx c = { out, rows, seed, range, per_row, index, 64 };
+  if (rows < 65536) c.tasks = 1;
+  orc_parallel(c.tasks, fill_task, &c);
+}
+
+void orc_fill_closed_form(uint32_t* id, uint32_t* region, uint32_t* amount, uint32_t* needle_key, uint64_t rows)
+{
+  for (uint64_t i = 0; i < rows; i++)
+  {
+    if (id) id[i] = (uint32_t)(i + 1);
+    if (region) region[i] = (uint32_t)(i % 50);
+    if (amount) amount[i] = (uint32_t)(i % 10000);
+    if (needle_key) needle_key[i] = (uint32_t)(i * 2654435761ull);
+  }
+}
+
+/* ---- whole-column aggregates ---- */
+
+static double widen(const void* values, uint32_t type, uint64_t i)
+{
+  switch (type)
+  {
+    case ORC_U32: return (double)((const uint32_t*)values)[i];
+    case ORC_I32: return (double)((const int32_t*)values)[i];
+    case ORC_U64: return (double)((const uint64_t*)values)[i];
+    case ORC_I64: return (double)((const int64_t*)values)[i];
+    case ORC_F32: return (double)((const float*)values)[i];
+    default: return ((const double*)values)[i];
+  }
+}
+
+typedef struct
+{
+  const void* values;
+  uint32_t type;
+  uint64_t base, rows, per;
+  double* sum;
+  double* mn;
+  double* mx;
+} agg_ctx;
+
+/* QE_CHUNK_REDUCE_LOOP (query_exec.c:7472-7482) over one tp_divide_work range */
+static void agg_task(void* p, uint32_t id)
+{
+  agg_ctx* c = (agg_ctx*)p;
+  uint64_t lo = (uint64_t)id * c->per, hi = lo + c->per;
+  if (lo > c->rows) lo = c->rows;
+  if (hi > c->rows) hi = c->rows;
+  double sum = 0.0, mn = ORC_F64_MAX, mx = -ORC_F64_MAX;
+  for (uint64_t i = lo; i < hi; i++)
+  {
+    double v = widen(c->values, c->type, c->base + i);
+    sum += v;
+    if (v < mn) mn = v;
+    if (v > mx) mx = v;
+  }
+  c->sum[id] = sum;
+  c->mn[id] = mn;
+  c->mx[id] = mx;
+}
+
+void orc_aggregate_global_cpu(const void* values, uint32_t type, uint64_t rows, uint32_t tasks_hint, double* out_sum, double* out_min,
+                              double* out_max)
+{
+  double sum = 0.0, mn = ORC_F64_MAX, mx = -ORC_F64_MAX;
+  const uint64_t chunk_rows = 67108864; /* QE_AGG_CHUNK_ROWS default (:9162) */
+  uint32_t workers = tasks_hint ? tasks_hint : orc_threads();
+  for (uint64_t start = 0; start < rows; start += chunk_rows)
+  {
+    uint64_t n = rows - start < chunk_rows ? rows - start : chunk_rows;
+    uint64_t task_count = n / 65536;
+    if (task_count > workers) task_count = workers;
+    if (task_count < 1) task_count = 1;
+    double* ts = (double*)malloc(sizeof(double) * task_count * 3);
+    agg_ctx c = { values, type, start, n, (n + task_count - 1) / task_count, ts, ts + task_count, ts + 2 * task_count };
+    orc_parallel((uint32_t)task_count, agg_task, &c);
+    for (uint64_t t = 0; t < task_count; t++)
+    {
+      sum += c.sum[t];
+      if (c.mn[t] < mn) mn = c.mn[t];
+      if (c.mx[t] > mx) mx = c.mx[t];
+    }
+    free(ts);
+  }
+  *out_sum = sum;
+  *out_min = mn;
+  *out_max = mx;
+}
+
+void orc_aggregate_global_gpu_order(const void* values, uint32_t type, uint64_t rows, double* out_sum, double* out_min, double* out_max)
+{
+  const uint64_t chunk_rows = 16777216; /* qe_stream_chunk_rows (:2096-2099) */
+  const uint32_t groups = 2048, wg = 256;
+  const uint64_t stride = (uint64_t)groups * wg;
+  double total = 0.0, tmin = ORC_F64_MAX, tmax = -ORC_F64_MAX;
+  double* sh_sum = (double*)malloc(sizeof(double) * wg);
+  double* sh_min = (double*)malloc(sizeof(double) * wg);
+  double* sh_max = (double*)malloc(sizeof(double) * wg);
+  uint32_t width = type == ORC_F64 ? 2 : 1;
+  for (uint64_t start = 0; start < rows; start += chunk_rows)
+  {
+    uint64_t n = rows - start < chunk_rows ? rows - start : chunk_rows;
+    uint64_t total_words = n * width, vec_count = total_words / 4, tail_start = vec_count * 4;
+    for (uint32_t g = 0; g < groups; g++)
+    {
+      for (uint32_t tid = 0; tid < wg; tid++)
+      {
+        uint64_t t = (uint64_t)g * wg + tid;
+        double acc = 0.0, mn = ORC_F64_MAX, mx = -ORC_F64_MAX;
+        for (uint64_t i = t; i < vec_count; i += stride)
+        {
+          if (width == 1)
+          {
+            double v0 = widen(values, type, start + i * 4 + 0), v1 = widen(values, type, start + i * 4 + 1);
+            double v2 = widen(values, type, start + i * 4 + 2), v3 = widen(values, type, start + i * 4 + 3);
+            acc += (v0 + v1) + (v2 + v3);
+            double a = v0 < v1 ? v0 : v1, b = v2 < v3 ? v2 : v3;
+            double m = a < b ? a : b;
+            mn = m < mn ? m : mn;
+            a = v0 > v1 ? v0 : v1;
+            b = v2 > v3 ? v2 : v3;
+            m = a > b ? a : b;
+            mx = m > mx ? m : mx;
+          }
+          else
+          {
+            double v0 = widen(values, type, start + i * 2 + 0), v1 = widen(values, type, start + i * 2 + 1);
+            acc += v0 + v1;
+            double a = v0 < v1 ? v0 : v1;
+            mn = a < mn ? a : mn;
+            a = v0 > v1 ? v0 : v1;
+            mx = a > mx ? a : mx;
+          }
+        }
+        if (width == 1)
+        {
+          if (t < total_words - tail_start)
+          {
+            double x = widen(values, type, start + tail_start + t);
+            acc += x;
+            mn = x < mn ? x : mn;
+            mx = x > mx ? x : mx;
+          }
+        }
+        else if (t == 0 && total_words > tail_start)
+        {
+          double x = widen(values, type, start + tail_start / 2);
+          acc += x;
+          mn = x < mn ? x : mn;
+          mx = x > mx ? x : mx;
+        }
+        sh_sum[tid] = acc;
+        sh_min[tid] = mn;
+        sh_max[tid] = mx;
+      }
+      for (uint32_t step = 128; step > 0; step >>= 1)
+      {
+        for (uint32_t tid = 0; tid < step; tid++)
+        {
+          sh_sum[tid] += sh_sum[tid + step];
+          sh_min[tid] = sh_min[tid + step] < sh_min[tid] ? sh_min[tid + step] : sh_min[tid];
+          sh_max[tid] = sh_max[tid + step] > sh_max[tid] ? sh_max[tid + step] : sh_max[tid];
+        }
+      }
+      total += sh_sum[0];
+      tmin = sh_min[0] < tmin ? sh_min[0] : tmin;
+      tmax = sh_max[0] > tmax ? sh_max[0] : tmax;
+    }
+  }
+  free(sh_sum);
+  free(sh_min);
+  free(sh_max);
+  *out_sum = total;
+  *out_min = tmin;
+  *out_max = tmax;
+}
+
+double orc_compensated_sum(const void* values, uint32_t type, uint64_t rows)
+{
+  double s = 0.0, c = 0.0;
+  for (uint64_t i = 0; i < rows; i++)
+  {
+    double x = widen(values, type, i);
+    double t = s + x;
+    if (fabs(s) >= fabs(x)) c += (s - t) + x;
+    else c += (x - t) + s;
+    s = t;
+  }
+  return s + c;
+}
+
+/* ---- scan + filter ---- */
+
+static int leaf_match(const OrcLeaf* l, uint64_t row)
+{
+  double v = widen(l->values, l->type, row);
+  switch (l->op)
+  {
+    case 0: return v == l->target;
+    case 1: return v < l->target;
+    case 2: return v <= l->target;
+    case 3: return v > l->target;
+    default: return v >= l->target;
+  }
+}
+
+typedef struct
+{
+  const OrcLeaf* leaves;
+  uint32_t leaf_count;
+  uint64_t rows, per;
+  uint64_t* counts;
+  uint32_t** lists;
+} scan_ctx;
+
+static void scan_task(void* p, uint32_t id)
+{
+  scan_ctx* c = (scan_ctx*)p;
+  uint64_t lo = (uint64_t)id * c->per, hi = lo + c->per;
+  if (lo > c->rows) lo = c->rows;
+  if (hi > c->rows) hi = c->rows;
+  uint64_t n = 0;
+  for (uint64_t r = lo; r < hi; r++)
+  {
+    int ok = 1;
+    for (uint32_t l = 0; l < c->leaf_count && ok; l++) ok = leaf_match(&c->leaves[l], r);
+    if (ok)
+    {
+      if (c->lists && c->lists[id]) c->lists[id][n] = (uint32_t)r;
+      n++;
+    }
+  }
+  c->counts[id] = n;
+}
+
+uint64_t orc_scan_and(const OrcLeaf* leaves, uint32_t leaf_count, uint64_t rows, uint32_t* out_rows, uint64_t cap)
+{
+  uint32_t tasks = orc_threads();
+  if (rows < 65536) tasks = 1;
+  scan_ctx c;
+  c.leaves = leaves;
+  c.leaf_count = leaf_count;
+  c.rows = rows;
+  c.per = (rows + tasks - 1) / tasks;
+  c.counts = (uint64_t*)calloc(tasks, sizeof(uint64_t));
+  c.lists = NULL;
+  if (out_rows && cap)
+  {
+    c.lists = (uint32_t**)calloc(tasks, sizeof(uint32_t*));
+    for (uint32_t t = 0; t < tasks; t++) c.lists[t] = (uint32_t*)malloc(sizeof(uint32_t) * (c.per ? c.per : 1));
+  }
+  orc_parallel(tasks, scan_task, &c);
+  uint64_t total = 0;
+  for (uint32_t t = 0; t < tasks; t++)
+  {
+    if (c.lists)
+    {
+      for (uint64_t i = 0; i < c.counts[t] && total + i < cap; i++) out_rows[total + i] = c.lists[t][i];
+      free(c.lists[t]);
+    }
+    total += c.counts[t];
+  }
+  free(c.lists);
+  free(c.counts);
+  return total;
+}
+
+/* ---- dense GROUP BY ---- */
+
+void orc_group_dense(const uint32_t* key, uint32_t key_type, uint64_t rows, int64_t min_key, uint64_t groups, uint32_t expr_count,
+                     const uint32_t* funcs, const uint32_t* const* args, const uint32_t* arg_types, uint64_t* out_counts,
+                     int64_t* out_sums, int64_t* out_mins, int64_t* out_maxs)
+{
+  for (uint64_t g = 0; g < groups; g++)
+  {
+    out_counts[g] = 0;
+    for (uint32_t e = 0; e < expr_count; e++)
+    {
+      out_sums[g * expr_count + e] = 0;
+      out_mins[g * expr_count + e] = 2147483647;
+      out_maxs[g * expr_count + e] = -2147483648ll;
+    }
+  }
+  for (uint64_t r = 0; r < rows; r++)
+  {
+    int64_t k = key_type == ORC_I32 ? (int64_t)(int32_t)key[r] : (int64_t)key[r];
+    int64_t g = k - min_key;
+    if (g < 0 || (uint64_t)g >= groups) continue;
+    out_counts[g] += 1;
+    for (uint32_t e = 0; e < expr_count; e++)
+    {
+      uint32_t f = funcs[e];
+      if (f == 0) continue;
+      uint32_t w = args[e][r];
+      int64_t* s = &out_sums[g * expr_count + e];
+      if (f == 1 || f == 2)
+      {
+        uint64_t add = arg_types[e] == ORC_I32 ? (uint64_t)(int64_t)(int32_t)w : (uint64_t)w;
+        *s = (int64_t)((uint64_t)*s + add);
+      }
+      else if (f == 3)
+      {
+        int64_t v = (int64_t)(int32_t)w;
+        if (v < out_mins[g * expr_count + e]) out_mins[g * expr_count + e] = v;
+      }
+      else if (f == 4)
+      {
+        int64_t v = (int64_t)(int32_t)w;
+        if (v > out_maxs[g * expr_count + e]) out_maxs[g * expr_count + e] = v;
+      }
+    }
+  }
+}
+
+/* The reference hashes its keys with qe_aggregate_hash_key; the table order only affects speed,
+   the groups come out in first-appearance order either way. This restatement hashes the key word. */
+static uint64_t key_hash(uint32_t k)
+{
+  uint64_t h = (uint64_t)k * 0x9E3779B97F4A7C15ull;
+  return h ^ (h >> 29);
+}
+
+uint64_t orc_group_cpu_reduce(const uint32_t* key, uint64_t rows, uint32_t expr_count, const uint32_t* const* args, uint64_t max_groups,
+                              uint32_t* out_keys, uint64_t* out_counts, double* out_sums, double* out_mins, double* out_maxs)
+{
+  uint64_t table_size = 16;
+  while (table_size < max_groups * 2) table_size <<= 1;
+  uint32_t* table = (uint32_t*)malloc(sizeof(uint32_t) * table_size);
+  for (uint64_t i = 0; i < table_size; i++) table[i] = 0xffffffffu;
+  uint64_t group_count = 0;
+  for (uint64_t r = 0; r < rows; r++)
+  {
+    uint64_t slot = key_hash(key[r]) & (table_size - 1);
+    uint64_t g;
+    for (;;)
+    {
+      uint32_t occ = table[slot];
+      if (occ == 0xffffffffu)
+      {
+        if (group_count >= max_groups)
+        {
+          free(table);
+          return 0;
+        }
+        g = group_count++;
+        table[slot] = (uint32_t)g;
+        out_keys[g] = key[r];
+        out_counts[g] = 0;
+        for (uint32_t e = 0; e < expr_count; e++)
+        {
+          out_sums[g * expr_count + e] = 0.0;
+          out_mins[g * expr_count + e] = 1.0e300;
+          out_maxs[g * expr_count + e] = -1.0e300;
+        }
+        break;
+      }
+      if (out_keys[occ] == key[r])
+      {
+        g = occ;
+        break;
+      }
+      slot = (slot + 1) & (table_size - 1);
+    }
+    out_counts[g] += 1;
+    for (uint32_t e = 0; e < expr_count; e++)
+    {
+      double v = args[e] ? (double)args[e][r] : 0.0;
+      out_sums[g * expr_count + e] += v;
+      if (v < out_mins[g * expr_count + e]) out_mins[g * expr_count + e] = v;
+      if (v > out_maxs[g * expr_count + e]) out_maxs[g * expr_count + e] = v;
+    }
+  }
+  free(table);
+  return group_count;
+}

@@ -1,0 +1,21 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a) and the built native libraries")
+
+
+@pytest.fixture(scope="session")
+def gpu():
+    """Builds the native libraries (quick when up to date) and initialises the backend."""
+    from computeql_gb300 import build, native
+    build.build()
+    native.init()
+    return native

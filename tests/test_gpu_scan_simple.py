@@ -1,0 +1,115 @@
+"""scan_simple through the C ABI against the oracle (counts and row sets bit-exact)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from tests import closed_form as cf
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+EQ, LT, LE, GT, GE = 0, 1, 2, 3, 4
+
+
+@pytest.fixture(scope="module")
+def ops(gpu):
+    from computeql_gb300 import ops as o
+    return o
+
+
+def test_c1_count_flag_lt_2_matches_golden(ops):
+    from computeql_gb300 import workloads
+    fx = json.load(open(os.path.join(GOLDEN, "c1_oracle.json")))
+    t = workloads.fact_table(fx["rows"])
+    cnt, _ = ops.scan_simple([t.flag], [(0, LT, 2)])
+    assert cnt == fx["count_flag_lt_2"]
+
+
+@pytest.mark.parametrize("n", [1, 7, 8, 9, 10001, 1000003, 5_000_000])
+def test_closed_form_filters(ops, n):
+    idc, region, amount, _ = oracle.closed_form(n)
+    exp = cf.expected(n)
+    a = ops.Column.from_numpy(amount)
+    r = ops.Column.from_numpy(region)
+    assert ops.scan_simple([a], [(0, GT, cf.HIGH_AMOUNT)])[0] == exp["count_amount_gt_9990"]
+    assert ops.scan_simple([r], [(0, EQ, 7)])[0] == exp["count_region_eq_7"]
+    # id is its row number plus one: stored, and as a sequence the kernel computes
+    for idcol in (ops.Column.from_numpy(idc), ops.Column.sequence(n, 1)):
+        assert ops.scan_simple([idcol], [(0, GT, 1000), (0, LE, 900000000)])[0] == exp["count_id_range"]
+    # narrow encodings of the same columns
+    an = ops.Column.from_numpy(amount, narrow=True)
+    rn = ops.Column.from_numpy(region, narrow=True)
+    assert ops.scan_simple([an], [(0, GT, cf.HIGH_AMOUNT)])[0] == exp["count_amount_gt_9990"]
+    assert ops.scan_simple([rn], [(0, EQ, 7)])[0] == exp["count_region_eq_7"]
+    zc, zrows = ops.scan_simple([rn], [(0, GE, 20), (0, LE, 29)], want_rows=True)
+    assert [zc, float(amount[zrows].astype(np.float64).sum())] == list(exp["join_zone2"])
+
+
+def _column(dtype, n, rng):
+    if dtype == np.uint32:
+        return rng.integers(0, 1000, n).astype(np.uint32)
+    if dtype == np.int32:
+        return rng.integers(-500, 500, n).astype(np.int32)
+    if dtype == np.float32:
+        return (rng.integers(-500, 500, n) / 4.0).astype(np.float32)
+    return (rng.integers(-500, 500, n) / 8.0).astype(np.float64)
+
+
+@pytest.mark.parametrize("dtype", [np.uint32, np.int32, np.float32, np.float64])
+@pytest.mark.parametrize("op", [EQ, LT, LE, GT, GE])
+@pytest.mark.parametrize("target", [-3.5, 0.0, 17.0, 17.25, 499.0, 1e12, -1e12, float("nan")])
+def test_single_leaf_matches_oracle(ops, dtype, op, target):
+    n = 20011
+    rng = np.random.default_rng(abs(hash((str(dtype), op))) % 1000)
+    a = _column(dtype, n, rng)
+    cnt, rows = ops.scan_simple([ops.Column.from_numpy(a)], [(0, op, target)], want_rows=True)
+    ecnt, erows = oracle.scan_and([(a, op, target)], n, want_rows=True)
+    assert cnt == ecnt
+    assert np.array_equal(rows, erows)
+
+
+@pytest.mark.parametrize("n", [1, 2, 7, 8, 9, 15, 16, 17, 255, 256, 2047, 2048, 2049, 100000])
+def test_ragged_sizes_and_multi_leaf(ops, n):
+    rng = np.random.default_rng(n)
+    cols = [_column(np.uint32, n, rng), _column(np.int32, n, rng), _column(np.float64, n, rng), _column(np.float32, n, rng)]
+    leaves = [(0, GE, 100), (1, LT, 300), (2, GT, -40.0), (3, LE, 100.0), (0, LT, 950), (1, GE, -480)]
+    dev = [ops.Column.from_numpy(c) for c in cols]
+    cnt, rows = ops.scan_simple(dev, leaves, want_rows=True)
+    ecnt, erows = oracle.scan_and([(cols[c], op, t) for c, op, t in leaves], n, want_rows=True)
+    assert cnt == ecnt
+    assert np.array_equal(rows, erows)
+
+
+def test_eight_leaves_narrow_and_wide_mix(ops):
+    n = 333_333
+    rng = np.random.default_rng(5)
+    a = rng.integers(1000, 1200, n).astype(np.uint32)
+    b = rng.integers(-30000, 30000, n).astype(np.int32)
+    cols = [ops.Column.from_numpy(a, narrow=True), ops.Column.from_numpy(b, narrow=True), ops.Column.from_numpy(a), ops.Column.from_numpy(b)]
+    assert cols[0].width == 1 and cols[1].width == 2
+    leaves = [(0, GE, 1010), (1, LT, 20000), (2, LE, 1190), (3, GT, -25000), (0, LT, 1195.5), (1, GE, -29999.5), (2, GT, 1011), (3, LE, 19999)]
+    cnt, rows = ops.scan_simple(cols, leaves, want_rows=True)
+    srcs = [a, b, a, b]
+    ecnt, erows = oracle.scan_and([(srcs[c], op, t) for c, op, t in leaves], n, want_rows=True)
+    assert cnt == ecnt
+    assert np.array_equal(rows, erows)
+
+
+def test_output_grows_when_over_the_default_cap(ops):
+    # 50 % selective: more than the max(65536, rows/32) first guess, so the second attempt runs
+    n = 1_000_000
+    a = np.arange(n, dtype=np.uint32) % 2
+    cnt, rows = ops.scan_simple([ops.Column.from_numpy(a)], [(0, EQ, 1)], want_rows=True)
+    assert cnt == n // 2
+    assert np.array_equal(rows, np.arange(1, n, 2, dtype=np.uint32))
+
+
+def test_no_match_and_all_match(ops):
+    n = 100_000
+    a = np.full(n, 5, dtype=np.uint32)
+    col = ops.Column.from_numpy(a)
+    assert ops.scan_simple([col], [(0, EQ, 6)])[0] == 0
+    assert ops.scan_simple([col], [(0, EQ, 5)])[0] == n
+    assert ops.scan_simple([col], [(0, LT, -1)])[0] == 0
