@@ -623,6 +623,238 @@ __global__ void __launch_bounds__(1024) k_aggregate_dense(CqlLaunch a, DenseLayo
   }
 }
 
+
+// Fast path for whole-word keys and argument columns (the full-width u32/i32 case): per-expression
+// metadata unrolled into registers, key and argument vectors loaded together (16 bytes each), 32-bit
+// shared atomics with a carry into the high word as aggregate_dense_native.comp:184-200 does, one
+// private table per warp when the groups are few.
+template <int NE, int NA>
+__global__ void __launch_bounds__(1024) k_aggregate_dense_wide(CqlLaunch a, uint32_t G, uint32_t group_base, uint64_t rows,
+                                                               uint32_t copies, uint32_t copy_words, uint32_t nsum)
+{
+  extern __shared__ __align__(16) uint32_t smem[];
+  uint32_t func_codes = cql_word(a, 4);
+  uint32_t arg_index = cql_word(a, 6);
+  uint32_t arg_signed = cql_word(a, 7);
+  int min_key = (int)cql_word(a, 10);
+  uint32_t f[NE], ai[NE], sg[NE], slot[NE];
+  uint32_t ns = 0, nm = 0;
+#pragma unroll
+  for (int e = 0; e < NE; e++)
+  {
+    f[e] = (func_codes >> (4 * e)) & 0xfu;
+    ai[e] = (arg_index >> (4 * e)) & 0x3u;
+    sg[e] = (arg_signed >> ai[e]) & 1u;
+    slot[e] = 0;
+    if (f[e] == FUNC_SUM || f[e] == FUNC_AVG) slot[e] = ns++;
+    else if (f[e] == FUNC_MIN || f[e] == FUNC_MAX) slot[e] = nm++;
+  }
+  uint32_t mm_off = G + 2 * G * nsum;
+  for (uint32_t i = threadIdx.x; i < copies * copy_words; i += blockDim.x)
+  {
+    uint32_t in_copy = i % copy_words;
+    uint32_t v = 0;
+    if (in_copy >= mm_off)
+    {
+      uint32_t k = in_copy - mm_off;          // [slot][min G | max G]
+      v = ((k / G) & 1u) ? 0x80000000u : 0x7fffffffu;
+    }
+    smem[i] = v;
+  }
+  __syncthreads();
+  uint32_t copy = (threadIdx.x >> 5) % copies;
+  uint32_t* cnt = smem + copy * copy_words;
+  uint32_t* sums = cnt + G;
+  int* mm = (int*)(cnt + mm_off);
+
+  auto row = [&](uint32_t key, const uint32_t* v) {
+    uint32_t id = (uint32_t)((int)key - min_key - (int)group_base);
+    if (id >= G) return;
+    atomicAdd(&cnt[id], 1u);
+#pragma unroll
+    for (int e = 0; e < NE; e++)
+    {
+      if (f[e] == FUNC_COUNT) continue;
+      uint32_t x = v[0];
+#pragma unroll
+      for (int c = 1; c < NA; c++)
+        if (ai[e] == (uint32_t)c) x = v[c];
+      if (f[e] == FUNC_SUM || f[e] == FUNC_AVG)
+      {
+        uint32_t* lo = sums + slot[e] * 2 * G;
+        uint32_t old = atomicAdd(&lo[id], x);
+        uint32_t hi_add = ((sg[e] && (int)x < 0) ? 0xffffffffu : 0u) + ((old + x < old) ? 1u : 0u);
+        if (hi_add) atomicAdd(&lo[G + id], hi_add);
+      }
+      else if (f[e] == FUNC_MIN)
+        atomicMin(&mm[slot[e] * 2 * G + id], (int)x);
+      else if (f[e] == FUNC_MAX)
+        atomicMax(&mm[slot[e] * 2 * G + G + id], (int)x);
+    }
+  };
+
+  const uint4* kv = (const uint4*)a.buf[0];
+  uint64_t vec_count = rows / 4;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr int NC = NA > 0 ? NA : 1;
+  uint64_t i = t;
+  // two key vectors and two vectors of every argument column in flight per thread
+  for (; i + stride < vec_count; i += 2 * stride)
+  {
+    uint4 k0 = __ldcs(kv + i), k1 = __ldcs(kv + i + stride);
+    uint4 q0[NC], q1[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++)
+    {
+      if (c < NA)
+      {
+        q0[c] = __ldcs((const uint4*)a.buf[1 + c] + i);
+        q1[c] = __ldcs((const uint4*)a.buf[1 + c] + i + stride);
+      }
+      else
+      {
+        q0[c] = make_uint4(0, 0, 0, 0);
+        q1[c] = q0[c];
+      }
+    }
+    uint32_t v[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) v[c] = q0[c].x;
+    row(k0.x, v);
+#pragma unroll
+    for (int c = 0; c < NC; c++) v[c] = q0[c].y;
+    row(k0.y, v);
+#pragma unroll
+    for (int c = 0; c < NC; c++) v[c] = q0[c].z;
+    row(k0.z, v);
+#pragma unroll
+    for (int c = 0; c < NC; c++) v[c] = q0[c].w;
+    row(k0.w, v);
+#pragma unroll
+    for (int c = 0; c < NC; c++) v[c] = q1[c].x;
+    row(k1.x, v);
+#pragma unroll
+    for (int c = 0; c < NC; c++) v[c] = q1[c].y;
+    row(k1.y, v);
+#pragma unroll
+    for (int c = 0; c < NC; c++) v[c] = q1[c].z;
+    row(k1.z, v);
+#pragma unroll
+    for (int c = 0; c < NC; c++) v[c] = q1[c].w;
+    row(k1.w, v);
+  }
+  for (; i < vec_count; i += stride)
+  {
+    uint4 k0 = __ldcs(kv + i);
+    uint4 q0[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) q0[c] = c < NA ? __ldcs((const uint4*)a.buf[1 + c] + i) : make_uint4(0, 0, 0, 0);
+    uint32_t v[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) v[c] = q0[c].x;
+    row(k0.x, v);
+#pragma unroll
+    for (int c = 0; c < NC; c++) v[c] = q0[c].y;
+    row(k0.y, v);
+#pragma unroll
+    for (int c = 0; c < NC; c++) v[c] = q0[c].z;
+    row(k0.z, v);
+#pragma unroll
+    for (int c = 0; c < NC; c++) v[c] = q0[c].w;
+    row(k0.w, v);
+  }
+  uint64_t tail = vec_count * 4;
+  if (t < rows - tail)
+  {
+    uint64_t r = tail + t;
+    uint32_t v[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) v[c] = c < NA ? ((const uint32_t*)a.buf[1 + c])[r] : 0u;
+    row(((const uint32_t*)a.buf[0])[r], v);
+  }
+  __syncthreads();
+
+  uint32_t* info = (uint32_t*)a.buf[5];
+  unsigned long long* gsum = (unsigned long long*)a.buf[6];
+  int* gmin = (int*)a.buf[7];
+  int* gmax = (int*)a.buf[8];
+  uint64_t info_cap = a.bytes[5] / 4, sum_cap = a.bytes[6] / 8, min_cap = a.bytes[7] / 4, max_cap = a.bytes[8] / 4;
+  for (uint32_t g = threadIdx.x; g < G; g += blockDim.x)
+  {
+    uint32_t count = 0;
+    for (uint32_t c = 0; c < copies; c++) count += smem[c * copy_words + g];
+    if (count == 0) continue;
+    uint64_t gg = (uint64_t)group_base + g;
+    if (gg * 2 + 1 < info_cap) atomicAdd(&info[gg * 2 + 1], count);
+#pragma unroll
+    for (int e = 0; e < NE; e++)
+    {
+      uint64_t index = gg * NE + e;
+      if (f[e] == FUNC_SUM || f[e] == FUNC_AVG)
+      {
+        unsigned long long total = 0;
+        for (uint32_t c = 0; c < copies; c++)
+        {
+          const uint32_t* lo = smem + c * copy_words + G + slot[e] * 2 * G;
+          total += ((unsigned long long)lo[G + g] << 32) | lo[g];
+        }
+        if (index < sum_cap) atomicAdd(&gsum[index], total);
+      }
+      else if (f[e] == FUNC_MIN || f[e] == FUNC_MAX)
+      {
+        int best = f[e] == FUNC_MIN ? 0x7fffffff : (int)0x80000000;
+        for (uint32_t c = 0; c < copies; c++)
+        {
+          const int* m = (const int*)(smem + c * copy_words + mm_off) + slot[e] * 2 * G;
+          best = f[e] == FUNC_MIN ? min(best, m[g]) : max(best, m[G + g]);
+        }
+        if (f[e] == FUNC_MIN && index < min_cap) atomicMin(&gmin[index], best);
+        if (f[e] == FUNC_MAX && index < max_cap) atomicMax(&gmax[index], best);
+      }
+    }
+  }
+}
+
+typedef void (*DenseWideFn)(CqlLaunch, uint32_t, uint32_t, uint64_t, uint32_t, uint32_t, uint32_t);
+#define DW_ROW(NE) { k_aggregate_dense_wide<NE, 0>, k_aggregate_dense_wide<NE, 1>, k_aggregate_dense_wide<NE, 2>, k_aggregate_dense_wide<NE, 4> }
+static const DenseWideFn k_dense_wide_table[8][4] = { DW_ROW(1), DW_ROW(2), DW_ROW(3), DW_ROW(4), DW_ROW(5), DW_ROW(6), DW_ROW(7), DW_ROW(8) };
+#undef DW_ROW
+
+// Whole-word key and arguments: one pass per tile of groups that fits shared memory.
+static int launch_dense_wide(const CqlLaunch& a, uint64_t rows, uint32_t exprs, uint32_t groups, uint32_t nsum, uint32_t nmm, cudaStream_t stream)
+{
+  uint32_t per_group = 1 + 2 * nsum + 2 * nmm;
+  uint32_t budget_words = (uint32_t)(std::min(g_cql_max_smem_optin, 200 * 1024) / 4);
+  uint32_t tile = std::min<uint32_t>(groups, budget_words / per_group);
+  if (tile == 0) return (int)cudaErrorInvalidValue;
+  // distinct argument columns are bound at 1..n in order (qe_dense_stream_core, query_exec.c:7863-7867)
+  uint32_t funcs = cql_word(a, 4), arg_index = cql_word(a, 6), na = 0;
+  for (uint32_t e = 0; e < exprs; e++)
+  {
+    uint32_t f = (funcs >> (4 * e)) & 0xfu;
+    if (f != FUNC_COUNT) na = std::max(na, ((arg_index >> (4 * e)) & 0x3u) + 1);
+  }
+  DenseWideFn fn = k_dense_wide_table[exprs - 1][na <= 2 ? na : 3];
+  for (uint32_t base = 0; base < groups; base += tile)
+  {
+    uint32_t G = std::min(tile, groups - base);
+    uint32_t copy_words = (G * per_group + 3) & ~3u;
+    uint32_t threads = copy_words * 4 > 48 * 1024 ? 1024 : 512;
+    uint32_t copies = 1;
+    while (copies < threads / 32 && (uint64_t)copy_words * 4 * copies * 2 <= 32 * 1024) copies *= 2;
+    size_t smem = (size_t)copy_words * 4 * copies;
+    if (smem > 48 * 1024) cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)threads, smem) != cudaSuccess || per_sm < 1) per_sm = 1;
+    uint64_t need = (rows / 4 + threads - 1) / threads;
+    uint32_t grid = cql_stream_grid(need ? need : 1, per_sm);
+    fn<<<grid, threads, smem, stream>>>(a, G, base, rows, copies, copy_words, nsum);
+    CQL_LAUNCH_CHECK();
+  }
+  return 0;
+}
+
 static int launch_aggregate_dense(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
 {
   (void)gws;
@@ -649,6 +881,15 @@ static int launch_aggregate_dense(const CqlLaunch& a, uint32_t gws, uint32_t lws
     if (f == FUNC_SUM || f == FUNC_AVG) L.sum_slot[e] = L.nsum++;
     if (f == FUNC_MIN || f == FUNC_MAX) L.mm_slot[e] = L.nmm++;
   }
+  // whole-word key and arguments take the fast path
+  bool all_wide = true;
+  for (uint32_t c = 0; c < 5; c++)
+  {
+    uint32_t w = (widths >> (4 * c)) & 0xfu;
+    if (!(w == 0 || w == 4)) all_wide = false;
+  }
+  if (all_wide) return launch_dense_wide(a, rows, exprs, groups, L.nsum, L.nmm, stream);
+
   uint32_t per_group_words = dense_group_words(L.nsum, L.nmm);
   uint32_t budget_words = (uint32_t)(std::min(g_cql_max_smem_optin, 200 * 1024) / 4);
   uint32_t tile = groups;

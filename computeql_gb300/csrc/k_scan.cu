@@ -317,7 +317,217 @@ static int launch_scan_simple(const CqlLaunch& a, uint32_t gws, uint32_t lws, cu
   return 0;
 }
 
+// ---------------------------------------------------------------------------------------------
+// scan_filter - the bytecode interpreter (contract of src/gpu/vulkan/shaders/scan_filter.comp:1-559):
+// opcodes of src/query_exec/query_exec.h:58-81 over a double stack of 8, one row per thread, the
+// instruction pointer and the step count bounded by the program length. It runs only for shapes a
+// per-query kernel could not be built for. Trigram similarity and edit distance are not evaluated
+// (the operator layer keeps scored programs off the GPU path).
+
+#define IOP_PUSH_TRUE 0
+#define IOP_LOAD_NUM_COL 1
+#define IOP_PUSH_CONST 2
+#define IOP_CMP_EQ 3
+#define IOP_CMP_NE 4
+#define IOP_CMP_LT 5
+#define IOP_CMP_GT 6
+#define IOP_CMP_LE 7
+#define IOP_CMP_GE 8
+#define IOP_AND 9
+#define IOP_OR 10
+#define IOP_STR_EQ 11
+#define IOP_STR_CONTAINS 12
+#define IOP_HALT 13
+#define IOP_PUSH_FALSE 14
+#define IOP_STR_NE 17
+#define IOP_STR_LT 18
+#define IOP_STR_GT 19
+#define IOP_STR_LE 20
+#define IOP_STR_GE 21
+#define INTERP_MAX_STACK 8
+
+__device__ __forceinline__ const uint32_t* slot_words(const CqlLaunch& a, uint32_t slot) { return (const uint32_t*)a.buf[6 + (slot < 10 ? slot : 0)]; }
+
+__device__ double interp_load(const CqlLaunch& a, uint32_t slot, uint32_t coltype, uint64_t row)
+{
+  const uint32_t* w = slot_words(a, slot);
+  switch (coltype)
+  {
+    case 1: case 12: return (double)w[row];
+    case 2: return (double)w[row * 2 + 1] * 4294967296.0 + (double)w[row * 2];
+    case 3: return (double)__uint_as_float(w[row]);
+    case 4: return __hiloint2double((int)w[row * 2 + 1], (int)w[row * 2]);
+    case 6: return (double)((const unsigned char*)w)[row];
+    case 7: case 9: return (double)(int)w[row];
+    default:
+    {
+      uint32_t lo = w[row * 2], hi = w[row * 2 + 1];
+      double u = (double)hi * 4294967296.0 + (double)lo;
+      return (hi & 0x80000000u) ? u - 18446744073709551616.0 : u;
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t str_off(const CqlLaunch& a, uint32_t slot, uint64_t row) { return slot_words(a, slot + 1)[row * 2]; }
+__device__ __forceinline__ uint32_t str_byte(const CqlLaunch& a, uint32_t slot, uint64_t i) { return ((const unsigned char*)slot_words(a, slot))[i]; }
+__device__ __forceinline__ uint32_t const_byte(const CqlLaunch& a, uint32_t wo, uint32_t i) { return ((const unsigned char*)a.buf[2])[wo * 4u + i]; }
+
+__device__ int interp_str_cmp3(const CqlLaunch& a, uint32_t slot, uint64_t row, uint32_t wo, uint32_t len)
+{
+  uint32_t s = str_off(a, slot, row), e = str_off(a, slot, row + 1), n = e - s, m = n < len ? n : len;
+  for (uint32_t i = 0; i < m; i++)
+  {
+    uint32_t x = str_byte(a, slot, s + i), y = const_byte(a, wo, i);
+    if (x != y) return x < y ? -1 : 1;
+  }
+  return n < len ? -1 : (n > len ? 1 : 0);
+}
+
+__device__ bool interp_str_contains(const CqlLaunch& a, uint32_t slot, uint64_t row, uint32_t wo, uint32_t len)
+{
+  uint32_t s = str_off(a, slot, row), e = str_off(a, slot, row + 1), n = e - s;
+  if (len == 0) return true;
+  if (n < len) return false;
+  for (uint32_t i = 0; i + len <= n; i++)
+  {
+    uint32_t j = 0;
+    while (j < len && str_byte(a, slot, s + i + j) == const_byte(a, wo, j)) j++;
+    if (j == len) return true;
+  }
+  return false;
+}
+
+__device__ bool interp_row(const CqlLaunch& a, const uint32_t* code, uint32_t words, uint64_t row)
+{
+  const uint32_t* consts = (const uint32_t*)a.buf[1];
+  double stack[INTERP_MAX_STACK];
+  int sp = 0;
+  uint32_t ip = 0, steps = 0;
+  while (ip < words && steps < words + 64u)
+  {
+    steps++;
+    uint32_t op = code[ip++];
+    if (op == IOP_HALT) break;
+    if (op == IOP_PUSH_TRUE || op == IOP_PUSH_FALSE)
+    {
+      if (sp >= INTERP_MAX_STACK) return false;
+      stack[sp++] = op == IOP_PUSH_TRUE ? 1.0 : 0.0;
+    }
+    else if (op == IOP_LOAD_NUM_COL)
+    {
+      if (sp >= INTERP_MAX_STACK || ip >= words) return false;
+      uint32_t operand = code[ip++];
+      stack[sp++] = interp_load(a, operand & 0xffu, (operand >> 8) & 0xffu, row);
+    }
+    else if (op == IOP_PUSH_CONST)
+    {
+      if (sp >= INTERP_MAX_STACK || ip >= words) return false;
+      uint32_t k = code[ip++];
+      stack[sp++] = __hiloint2double((int)consts[k * 2 + 1], (int)consts[k * 2]);
+    }
+    else if (op >= IOP_CMP_EQ && op <= IOP_OR)
+    {
+      if (sp < 2) return false;
+      double b = stack[--sp], x = stack[--sp];
+      bool r;
+      switch (op)
+      {
+        case IOP_CMP_EQ: r = x == b; break;
+        case IOP_CMP_NE: r = x != b; break;
+        case IOP_CMP_LT: r = x < b; break;
+        case IOP_CMP_GT: r = x > b; break;
+        case IOP_CMP_LE: r = x <= b; break;
+        case IOP_CMP_GE: r = x >= b; break;
+        case IOP_AND: r = x != 0.0 && b != 0.0; break;
+        default: r = x != 0.0 || b != 0.0; break;
+      }
+      stack[sp++] = r ? 1.0 : 0.0;
+    }
+    else if (op == IOP_STR_EQ || op == IOP_STR_NE || op == IOP_STR_CONTAINS || (op >= IOP_STR_LT && op <= IOP_STR_GE))
+    {
+      if (sp >= INTERP_MAX_STACK || ip + 3 > words) return false;
+      uint32_t slot = code[ip], wo = code[ip + 1], len = code[ip + 2];
+      ip += 3;
+      if (slot + 1 >= 10) return false;
+      bool r;
+      if (op == IOP_STR_CONTAINS) r = interp_str_contains(a, slot, row, wo, len);
+      else
+      {
+        int c = interp_str_cmp3(a, slot, row, wo, len);
+        r = op == IOP_STR_EQ ? c == 0 : op == IOP_STR_NE ? c != 0 : op == IOP_STR_LT ? c < 0 : op == IOP_STR_GT ? c > 0 : op == IOP_STR_LE ? c <= 0 : c >= 0;
+      }
+      stack[sp++] = r ? 1.0 : 0.0;
+    }
+    else
+    {
+      // an opcode this kernel does not evaluate ends the program
+      break;
+    }
+  }
+  return sp > 0 && stack[sp - 1] != 0.0;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_filter(CqlLaunch a, uint64_t rows)
+{
+  __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+  __shared__ uint32_t s_base;
+  const uint32_t* code = (const uint32_t*)a.buf[0];
+  uint32_t words = (uint32_t)(a.bytes[0] / 4);
+  uint32_t* out = (uint32_t*)a.buf[3];
+  uint32_t* out_count = (uint32_t*)a.buf[4];
+  const uint32_t* skip = (const uint32_t*)a.buf[5];
+  uint64_t capacity = a.bytes[3] / 8;
+  uint32_t skip_shift = cql_word(a, 6);
+  bool skip_on = cql_word(a, 8) != 0;
+  uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (uint64_t base = (uint64_t)blockIdx.x * SCAN_THREADS; base < rows; base += (uint64_t)gridDim.x * SCAN_THREADS)
+  {
+    uint64_t row = base + threadIdx.x;
+    bool in_range = row < rows;
+    if (in_range && skip_on)
+    {
+      uint64_t ch = row >> skip_shift;
+      in_range = ((skip[ch >> 5] >> (ch & 31)) & 1u) == 0u;
+    }
+    bool matched = in_range && interp_row(a, code, words, row);
+    uint32_t ballot = __ballot_sync(0xffffffffu, matched);
+    if (lane == 0) s_warp[warp] = __popc(ballot);
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+      uint32_t run = 0;
+      for (int w = 0; w < SCAN_THREADS / 32; w++)
+      {
+        uint32_t t = s_warp[w];
+        s_warp[w] = run;
+        run += t;
+      }
+      s_base = run ? atomicAdd(out_count, run) : 0u;
+    }
+    __syncthreads();
+    if (matched)
+    {
+      uint64_t pos = (uint64_t)s_base + s_warp[warp] + __popc(ballot & ((1u << lane) - 1u));
+      if (pos < capacity) *(uint2*)(out + pos * 2) = make_uint2((uint32_t)row, 0u);
+    }
+    __syncthreads();
+  }
+}
+
+static int launch_scan_filter(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t rows = cql_word(a, 0);
+  if (rows == 0) return 0;
+  uint32_t grid = cql_stream_grid((rows + SCAN_THREADS - 1) / SCAN_THREADS, 8);
+  k_scan_filter<<<grid, SCAN_THREADS, 0, stream>>>(a, rows);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
 const CqlKernelDesc cql_kernels_scan[] = {
   { "scan_simple", launch_scan_simple },
+  { "scan_filter", launch_scan_filter },
   { nullptr, nullptr },
 };

@@ -809,7 +809,7 @@ static std::vector<char> compile_nvrtc(const std::string& src, const std::string
     set_error("cqlcuda: nvrtcCreateProgram failed for '%s'", name.c_str());
     return cubin;
   }
-  const char* opts[] = { "--gpu-architecture=sm_103a", "--std=c++17", "-default-device", "--use_fast_math=false", "-lineinfo" };
+  const char* opts[] = { "--gpu-architecture=sm_103a", "--std=c++17", "-default-device", "-lineinfo" };
   nvrtcResult r = nvrtcCompileProgram(prog, 4, opts);
   size_t log_size = 0;
   nvrtcGetProgramLogSize(prog, &log_size);
@@ -1383,6 +1383,22 @@ extern "C" void cqlcuda_set_wait_timeout_ms(uint32_t ms) { S().wait_timeout_ms =
 extern "C" void cqlcuda_set_module_cache_dir(const char* path) { S().cache_dir = path ? path : ""; }
 extern "C" void cqlcuda_set_fail_compile_every(uint32_t n) { S().fail_compile_every = n; }
 extern "C" const char* cqlcuda_last_compile_log(void) { return S().compile_log.c_str(); }
+
+extern "C" int cqlcuda_compile_check(const char* source, uint64_t source_len)
+{
+  CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
+  std::string src(source, source_len);
+  std::string saved = s.cache_dir;
+  s.cache_dir.clear();
+  uint32_t fail_every = s.fail_compile_every;
+  s.fail_compile_every = 0;
+  int ok = 0;
+  compile_nvrtc(src, "compile_check", &ok);
+  s.cache_dir = saved;
+  s.fail_compile_every = fail_every;
+  return ok;
+}
 
 // ---------------------------------------------------------------------------------------------
 // data generation and timing helpers

@@ -6,6 +6,7 @@
 #include "cqlops.h"
 
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -28,6 +29,24 @@
 #define QE_SCAN_INT_BIAS  0x40000u
 
 static uint32_t g_launch_mark = 0;
+static char g_error[256] = "";
+
+const char* cqlops_last_error(void)
+{
+  return g_error;
+}
+
+/* Records why a request is refused (the reference logs and returns 0 at the same points). */
+void cqlops_note_error(const char* why)
+{
+  snprintf(g_error, sizeof(g_error), "%s", why);
+}
+
+static int refuse(const char* why)
+{
+  cqlops_note_error(why);
+  return 0;
+}
 
 uint32_t cqlops_last_launches(void)
 {
@@ -37,6 +56,7 @@ uint32_t cqlops_last_launches(void)
 static void launches_begin(void)
 {
   g_launch_mark = cqlcuda_kernel_launch_count();
+  g_error[0] = 0;
 }
 
 static CqlKernel* kernel_named(const char* name)
@@ -401,7 +421,7 @@ int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count,
       key->width == 3 || key->zone_min < -2147483648.0 || key->zone_max > 2147483647.0 ||
       key->zone_max - key->zone_min + 1.0 > (double)QE_DENSE_STREAM_MAX_GROUPS)
   {
-    return 0;
+    return refuse("dense group-by: the key must be a whole-number column with a zone range of at most 65536 values");
   }
   int64_t min_key = (int64_t)key->zone_min;
   uint64_t group_count = (uint64_t)((int64_t)key->zone_max - min_key) + 1;
@@ -433,7 +453,7 @@ int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count,
     /* MIN and MAX are signed 32-bit atomics, so the values have to fit (:7712-7718) */
     if ((f == CQLOPS_FUNC_MIN || f == CQLOPS_FUNC_MAX) && (!col->has_range || col->zone_min < -2147483648.0 || col->zone_max > 2147483647.0))
     {
-      return 0;
+      return refuse("dense group-by: MIN/MAX values must fit a signed 32-bit word");
     }
     if (f == CQLOPS_FUNC_MIN || f == CQLOPS_FUNC_MAX) has_min_max = 1;
     if (f == CQLOPS_FUNC_SUM || f == CQLOPS_FUNC_AVG)
@@ -461,7 +481,7 @@ int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count,
   uint64_t tile_count = (group_count + tile_groups - 1) / tile_groups;
   if (tile_count > QE_DENSE_STREAM_MAX_TILES)
   {
-    return 0;
+    return refuse("dense group-by: more than 256 tiles of the reference's shared-memory slices");
   }
   CqlKernel* k = kernel_named("aggregate_dense_native");
   if (!k)

@@ -28,13 +28,33 @@ class CqlStreamStats(C.Structure):
                 ("separate_copy_queue", u32)]
 
 
+class CqlDict(C.Structure):
+    _fields_ = [("count", u32), ("offsets", P), ("bytes", P)]
+
+
 class CqlColumn(C.Structure):
     _fields_ = [("type", u32), ("width", u32), ("base", u32), ("has_range", u32), ("rows", u64), ("buffer", P),
-                ("zone_min", dbl), ("zone_max", dbl)]
+                ("zone_min", dbl), ("zone_max", dbl), ("offsets", P), ("dict", P)]
 
 
 class CqlLeaf(C.Structure):
     _fields_ = [("column", u32), ("op", u32), ("target", dbl)]
+
+
+MAX_WORDS, MAX_CONSTS, MAX_STR_POOL, MAX_BINDINGS = 4096, 256, 65536, 10
+
+
+class CqlProgram(C.Structure):
+    _fields_ = [("words", u32 * MAX_WORDS), ("word_count", u32), ("consts", u32 * (2 * MAX_CONSTS)), ("const_count", u32),
+                ("str_pool", C.c_uint8 * MAX_STR_POOL), ("str_pool_size", u32), ("binding_count", u32),
+                ("binding_column", u32 * MAX_BINDINGS), ("binding_type", u32 * MAX_BINDINGS), ("binding_slot", u32 * MAX_BINDINGS),
+                ("binding_dict", u32 * MAX_BINDINGS), ("next_slot", u32), ("requires_cpu_scan", u32), ("has_score_output", u32),
+                ("error", C.c_char * 128)]
+
+
+class CqlFusedAgg(C.Structure):
+    _fields_ = [("column_count", u32), ("slots", u32 * 4), ("coltypes", u32 * 4), ("grouped", u32), ("key_count", u32),
+                ("key_slots", u32 * 3), ("key_types", u32 * 3), ("key_ranges", u32 * 3), ("group_count", u32)]
 
 
 # (name, restype, argtypes) of every entry point include/cqlcuda.h declares
@@ -98,6 +118,7 @@ CUDA_API = [
     ("cqlcuda_set_module_cache_dir", None, [cstr]),
     ("cqlcuda_set_fail_compile_every", None, [u32]),
     ("cqlcuda_last_compile_log", cstr, []),
+    ("cqlcuda_compile_check", C.c_int, [cstr, u64]),
     ("cqlcuda_fill_splitmix_u32", C.c_int, [P, u64, u64, u32, u32, u64]),
     ("cqlcuda_fill_sequence_u32", C.c_int, [P, u64, u32]),
     ("cqlcuda_flush_l2", C.c_int, [u64]),
@@ -110,6 +131,15 @@ OPS_API = [
     ("cqlops_scan_simple", C.c_int, [P, u32, P, u32, P, P, u64]),
     ("cqlops_group_dense", C.c_int, [P, u64, u32, P, P, u64, P, P, P, P, P, P]),
     ("cqlops_last_launches", u32, []),
+    ("cqlops_last_error", cstr, []),
+    ("cqlops_program_build", C.c_int, [cstr, P, P, u32, P]),
+    ("cqlops_program_bind", C.c_int, [P, P, u32]),
+    ("cqlops_program_max_stack_depth", u32, [P]),
+    ("cqlops_program_simple_leaves", u32, [P, P, u32]),
+    ("cqlops_program_source", C.c_int, [P, u32, P, P, u64, P]),
+    ("cqlops_scan_filter", C.c_int, [P, P, u32, P, P, u64, P]),
+    ("cqlops_fused_filter_aggregate", C.c_int, [P, P, P, u32, P, P, P, P]),
+    ("cqlops_fused_filter_group", C.c_int, [P, P, P, u32, P, u32, u64, P, P, P, P, P, P, P, P]),
 ]
 
 _cuda = None
@@ -151,8 +181,15 @@ class CudaError(RuntimeError):
 
 
 def last_error():
+    msgs = []
+    if _ops is not None:
+        e = _ops.cqlops_last_error()
+        if e:
+            msgs.append(e.decode())
     e = load_cuda().cqlcuda_last_error()
-    return e.decode() if e else ""
+    if e:
+        msgs.append(e.decode())
+    return "; ".join(msgs)
 
 
 def init():

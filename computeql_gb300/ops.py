@@ -177,3 +177,150 @@ def group_dense(key, funcs, args):
 
 def launches():
     return N.load_ops().cqlops_last_launches()
+
+
+# ---------------------------------------------------------------------------------------------
+# WHERE programs, per-query kernels and fused operators
+
+SCAN_AUTO, SCAN_INTERPRETER, SCAN_GENERATED, SCAN_SIMPLE = 0, 1, 2, 3
+KERNEL_SCAN, KERNEL_FUSED_AGG, KERNEL_FUSED_GROUP = 0, 1, 2
+TYPE_STRING8 = 5
+
+
+class StringColumn(Column):
+    """A STRING8 column: raw bytes + u64 offsets on the device, and optionally dictionary codes."""
+
+    def __init__(self, values, dictionary=False):
+        raw = [v.encode() if isinstance(v, str) else bytes(v) for v in values]
+        n = len(raw)
+        self.values = raw
+        self.dict_struct = None
+        if dictionary:
+            uniq = {}
+            codes = np.empty(n, dtype=np.uint32)
+            for i, v in enumerate(raw):
+                codes[i] = uniq.setdefault(v, len(uniq))
+            items = sorted(uniq.items(), key=lambda kv: kv[1])
+            offs = np.zeros(len(items) + 1, dtype=np.uint32)
+            for i, (v, _) in enumerate(items):
+                offs[i + 1] = offs[i] + len(v)
+            blob = b"".join(v for v, _ in items) or b"\0"
+            self._dict_offsets = offs
+            self._dict_bytes = C.create_string_buffer(blob, len(blob))
+            self.dict_struct = N.CqlDict(len(items), offs.ctypes.data, C.addressof(self._dict_bytes))
+            self.codes = codes
+            super().__init__(TYPE_STRING8, n, DeviceBuffer(codes.nbytes, codes) if n else DeviceBuffer(4), zone=(0.0, float(max(len(items) - 1, 0))))
+            self.offsets_buf = None
+        else:
+            offs = np.zeros(n + 1, dtype=np.uint64)
+            for i, v in enumerate(raw):
+                offs[i + 1] = offs[i] + len(v)
+            blob = np.frombuffer(b"".join(raw) + b"\0" * 16, dtype=np.uint8)
+            super().__init__(TYPE_STRING8, n, DeviceBuffer(blob.nbytes, blob), zone=None)
+            self.offsets_buf = DeviceBuffer(offs.nbytes, offs)
+
+    def c(self):
+        col = super().c()
+        col.offsets = self.offsets_buf.handle if self.offsets_buf else None
+        col.dict = C.addressof(self.dict_struct) if self.dict_struct else None
+        return col
+
+
+class Program:
+    """A compiled WHERE condition over named columns (s-expression syntax, see cql_program.c)."""
+
+    def __init__(self, where, columns):
+        self.names = list(columns.keys())
+        self.columns = [columns[n] for n in self.names]
+        self._name_bufs = [C.create_string_buffer(n.encode()) for n in self.names]
+        self._names = (C.c_char_p * len(self.names))(*[C.cast(b, C.c_char_p) for b in self._name_bufs])
+        self._cols = (N.CqlColumn * len(self.columns))(*[c.c() for c in self.columns])
+        self.prog = N.CqlProgram()
+        ok = N.load_ops().cqlops_program_build(where.encode(), self._cols, self._names, len(self.names), C.byref(self.prog))
+        if not ok:
+            raise OpError("cqlops_program_build failed: " + self.prog.error.decode())
+
+    @property
+    def words(self):
+        return list(self.prog.words[: self.prog.word_count])
+
+    @property
+    def consts(self):
+        raw = np.array(self.prog.consts[: 2 * self.prog.const_count], dtype=np.uint32)
+        return raw.view(np.float64).tolist()
+
+    def stack_depth(self):
+        return N.load_ops().cqlops_program_max_stack_depth(C.byref(self.prog))
+
+    def source(self, kind=KERNEL_SCAN, fuse=None):
+        lib = N.load_ops()
+        n = C.c_uint64()
+        f = C.byref(fuse) if fuse is not None else None
+        if not lib.cqlops_program_source(C.byref(self.prog), kind, f, None, 0, C.byref(n)):
+            why = C.create_string_buffer(256)
+            lib.cqlops_program_source(C.byref(self.prog), kind, f, why, 256, None)
+            raise OpError("no generated kernel: " + why.value.decode())
+        buf = C.create_string_buffer(n.value + 1)
+        lib.cqlops_program_source(C.byref(self.prog), kind, f, buf, n.value + 1, None)
+        return buf.value.decode()
+
+    def index(self, name):
+        return self.names.index(name)
+
+
+def scan_filter(program, strategy=SCAN_AUTO, want_rows=False, max_rows=None):
+    """-> (count, sorted rows or None, strategy that ran)."""
+    count = C.c_uint64()
+    ran = C.c_uint32()
+    rows_arr = None
+    cap = 0
+    if want_rows:
+        n = program.columns[0].rows if program.columns else 0
+        cap = n if max_rows is None else min(max_rows, n)
+        rows_arr = np.empty(max(cap, 1), dtype=np.uint32)
+    ok = N.load_ops().cqlops_scan_filter(C.byref(program.prog), program._cols, strategy, C.byref(count),
+                                         N.ptr(rows_arr) if want_rows else None, cap, C.byref(ran))
+    _check(ok, "cqlops_scan_filter")
+    rows = rows_arr[: min(count.value, cap)].copy() if want_rows else None
+    return count.value, rows, ran.value
+
+
+def fused_aggregate(program, agg_names):
+    k = len(agg_names)
+    idx = (C.c_uint32 * max(k, 1))(*[program.index(n) for n in agg_names])
+    cnt = C.c_double()
+    s = (C.c_double * max(k, 1))()
+    mn = (C.c_double * max(k, 1))()
+    mx = (C.c_double * max(k, 1))()
+    _check(N.load_ops().cqlops_fused_filter_aggregate(C.byref(program.prog), program._cols, idx, k, C.byref(cnt), s, mn, mx),
+           "cqlops_fused_filter_aggregate")
+    return cnt.value, list(s)[:k], list(mn)[:k], list(mx)[:k]
+
+
+def fused_group(program, key_names, agg_names, max_groups=1 << 16):
+    kc, ac = len(key_names), len(agg_names)
+    keys = (C.c_uint32 * 3)(*[program.index(n) for n in key_names])
+    aggs = (C.c_uint32 * 4)(*[program.index(n) for n in agg_names])
+    total = C.c_uint64()
+    kmin = (C.c_int64 * 3)()
+    krange = (C.c_uint32 * 3)()
+    counts = np.zeros(max_groups, dtype=np.uint64)
+    minrow = np.zeros(max_groups, dtype=np.uint64)
+    sums = np.zeros(max_groups * max(ac, 1), dtype=np.int64)
+    mins = np.zeros(max_groups * max(ac, 1), dtype=np.int64)
+    maxs = np.zeros(max_groups * max(ac, 1), dtype=np.int64)
+    _check(N.load_ops().cqlops_fused_filter_group(C.byref(program.prog), program._cols, keys, kc, aggs, ac, max_groups, C.byref(total), kmin,
+                                                  krange, N.ptr(counts), N.ptr(minrow), N.ptr(sums), N.ptr(mins), N.ptr(maxs)),
+           "cqlops_fused_filter_group")
+    G = total.value
+    return {"groups": G, "key_min": list(kmin)[:kc], "key_range": list(krange)[:kc], "counts": counts[:G], "min_row": minrow[:G],
+            "sums": sums[: G * ac].reshape(G, ac), "mins": mins[: G * ac].reshape(G, ac), "maxs": maxs[: G * ac].reshape(G, ac)}
+
+
+def compile_check(source):
+    """NVRTC compile of a generated source for sm_103a, no device needed -> (ok, log)."""
+    lib = N.load_cuda()
+    b = source.encode()
+    ok = lib.cqlcuda_compile_check(b, len(b))
+    log = lib.cqlcuda_last_compile_log()
+    return bool(ok), (log.decode() if log else "")

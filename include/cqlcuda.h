@@ -162,6 +162,9 @@ void     cqlcuda_set_module_cache_dir(const char* path);
 /* Test hook mirroring QE_TEST_FAIL_SHADERC (src/query_exec/query_kernel.h:21-24): every n-th compile fails, 0 = off. */
 void     cqlcuda_set_fail_compile_every(uint32_t n);
 const char* cqlcuda_last_compile_log(void);
+/* Compiles CUDA C++ source with NVRTC for sm_103a without loading it (no device needed): 1 when it
+   compiles. The log goes to cqlcuda_last_compile_log(). */
+int      cqlcuda_compile_check(const char* source, uint64_t source_len);
 
 /* ---- raw device helpers used by the bench and tests (not in the reference vtable) ---- */
 /* Fills `rows` rows of a u32 column from the splitmix64 stream seeded `seed`: row r takes draw

@@ -56,10 +56,20 @@ enum
   CQLOPS_CMP_GE = 4,
 };
 
+/* A string dictionary: value i is bytes[offsets[i] .. offsets[i+1]) (CQL_StringDict, src/cql/cql.h:146-153). */
+typedef struct CqlDict
+{
+  uint32_t count;
+  const uint32_t* offsets;
+  const char* bytes;
+} CqlDict;
+
 /* A device-resident column. `width` is the encoding the kernels are told
    (qe_encoding_shader_width, query_exec.c:1593-1601): 0 = stored as is, 1/2 = narrow codes of that
    many bytes with value = base + code, 3 = a sequence (value = base + row number, nothing stored).
-   zone_min/zone_max stand in for the zone map range (qe_column_range_from_zone_map). */
+   zone_min/zone_max stand in for the zone map range (qe_column_range_from_zone_map).
+   A STRING8 column holds its bytes in `buffer` and (rows + 1) u64 offsets in `offsets`; with a
+   dictionary, `buffer` holds the u32 codes instead and `dict` the values (host side). */
 typedef struct CqlColumn
 {
   uint32_t type;
@@ -70,6 +80,8 @@ typedef struct CqlColumn
   CqlBuffer* buffer;
   double zone_min;
   double zone_max;
+  CqlBuffer* offsets;
+  const CqlDict* dict;
 } CqlColumn;
 
 /* One comparison `column op target` of an AND-only filter (the leaves qe_scan_filter_selected
@@ -80,6 +92,102 @@ typedef struct CqlLeaf
   uint32_t op;        /* CQLOPS_CMP_* */
   double target;
 } CqlLeaf;
+
+/* ---- WHERE bytecode (QE_BytecodeProgram, src/query_exec/query_exec.h:96-126) ---- */
+#define CQLOPS_MAX_WORDS 4096
+#define CQLOPS_MAX_CONSTS 256
+#define CQLOPS_MAX_STR_POOL 65536
+#define CQLOPS_MAX_BINDINGS 10
+
+typedef struct CqlProgram
+{
+  uint32_t words[CQLOPS_MAX_WORDS];
+  uint32_t word_count;
+  uint32_t consts[CQLOPS_MAX_CONSTS * 2];     /* f64 constants as (lo, hi) words */
+  uint32_t const_count;
+  uint8_t str_pool[CQLOPS_MAX_STR_POOL];
+  uint32_t str_pool_size;
+  uint32_t binding_count;
+  uint32_t binding_column[CQLOPS_MAX_BINDINGS];  /* index into the caller's column array */
+  uint32_t binding_type[CQLOPS_MAX_BINDINGS];    /* the type it is read as (U32 for dictionary codes) */
+  uint32_t binding_slot[CQLOPS_MAX_BINDINGS];    /* first column slot: binding 6 + slot */
+  uint32_t binding_dict[CQLOPS_MAX_BINDINGS];    /* 1 when the binding is dictionary codes */
+  uint32_t next_slot;
+  uint32_t requires_cpu_scan;
+  uint32_t has_score_output;
+  char error[128];
+} CqlProgram;
+
+/* Compiles a WHERE condition given as an s-expression over the named columns (qe_bytecode_program_build,
+   query_exec.c:510-530; grammar in computeql_gb300/host/cql_program.c). An empty condition is TRUE.
+   Returns 0 and sets prog->error on a malformed or unsupported condition. */
+int cqlops_program_build(const char* where, const CqlColumn* columns, const char* const* names, uint32_t column_count, CqlProgram* prog);
+/* Binds one more column to the program (the fused aggregates' argument and key columns); returns its slot or -1. */
+int cqlops_program_bind(CqlProgram* prog, const CqlColumn* columns, uint32_t column_index);
+/* qe_bytecode_program_max_stack_depth (query_exec.c:552-612). */
+uint32_t cqlops_program_max_stack_depth(const CqlProgram* prog);
+/* The leaves of an AND-only tree of numeric comparisons with literals, the shape scan_simple runs;
+   0 when the program has another shape. */
+uint32_t cqlops_program_simple_leaves(const CqlProgram* prog, CqlLeaf* out, uint32_t cap);
+
+/* ---- per-query kernels (qk_* of src/query_exec/query_kernel.h:198-240, emitted as CUDA C++) ---- */
+enum
+{
+  CQLOPS_KERNEL_SCAN = 0,        /* scan_filter.comp's bindings: matching rows compacted */
+  CQLOPS_KERNEL_FUSED_AGG = 1,   /* WHERE + COUNT and SUM/MIN/MAX per column, partials per workgroup */
+  CQLOPS_KERNEL_FUSED_GROUP = 2, /* WHERE + GROUP BY up to 3 small-range keys */
+};
+
+/* QK_FusedAgg (src/query_exec/query_kernel.h:171-196). */
+typedef struct CqlFusedAgg
+{
+  uint32_t column_count;
+  uint32_t slots[4];
+  uint32_t coltypes[4];
+  uint32_t grouped;
+  uint32_t key_count;
+  uint32_t key_slots[3];
+  uint32_t key_types[3];
+  uint32_t key_ranges[3];
+  uint32_t group_count;
+} CqlFusedAgg;
+
+/* The CUDA C++ source of a program's kernel of the given kind (qk_scan_source_build,
+   query_kernel.c:971-1672). Writes at most cap bytes (NUL-terminated) and the length to out_len.
+   Returns 0 when the program has an opcode the generated kernel does not take (the reason is
+   written to out then). */
+int cqlops_program_source(const CqlProgram* prog, uint32_t kind, const CqlFusedAgg* fuse, char* out, uint64_t cap, uint64_t* out_len);
+
+/* Scan strategies of cqlops_scan_filter (the kernel choice cascade of qe_scan_filter_selected,
+   query_exec.c:2566-2680). */
+enum
+{
+  CQLOPS_SCAN_AUTO = 0,         /* scan_simple for numeric AND leaves, else the per-query kernel, else the interpreter */
+  CQLOPS_SCAN_INTERPRETER = 1,  /* scan_filter: the bytecode interpreter */
+  CQLOPS_SCAN_GENERATED = 2,    /* the per-query NVRTC kernel only */
+  CQLOPS_SCAN_SIMPLE = 3,       /* scan_simple only */
+};
+
+/* Runs a WHERE program over the columns: the count of matching rows and, when out_rows is not NULL,
+   up to out_capacity of them in ascending order. out_strategy (may be NULL) receives the strategy
+   that ran. */
+int cqlops_scan_filter(const CqlProgram* prog, const CqlColumn* columns, uint32_t strategy, uint64_t* out_count, uint32_t* out_rows,
+                       uint64_t out_capacity, uint32_t* out_strategy);
+
+/* WHERE + COUNT(*) and SUM/MIN/MAX of up to 4 numeric columns in one pass (qe_fused_filter_aggregate,
+   query_exec.c:9888-10254). agg_columns index the column array. Partials are folded in workgroup order. */
+int cqlops_fused_filter_aggregate(const CqlProgram* prog, const CqlColumn* columns, const uint32_t* agg_columns, uint32_t agg_count,
+                                  double* out_count, double* out_sum, double* out_min, double* out_max);
+
+/* WHERE + GROUP BY up to 3 small-range whole-number (or dictionary-coded) keys with COUNT and
+   SUM/MIN/MAX of up to 4 U32/I32 columns (qe_fused_filter_group_aggregate, query_exec.c:9442-9886).
+   Per group g (the keys as digits, key 0 most significant): out_counts[g], out_min_row[g] (the
+   smallest matching row), out_sums/out_mins/out_maxs[g*agg_count + c]. out_group_total receives the
+   number of groups (the product of the key ranges); the arrays must hold max_groups groups. */
+int cqlops_fused_filter_group(const CqlProgram* prog, const CqlColumn* columns, const uint32_t* key_columns, uint32_t key_count,
+                              const uint32_t* agg_columns, uint32_t agg_count, uint64_t max_groups, uint64_t* out_group_total,
+                              int64_t* out_key_min, uint32_t* out_key_range, uint64_t* out_counts, uint64_t* out_min_row, int64_t* out_sums,
+                              int64_t* out_mins, int64_t* out_maxs);
 
 /* SUM/MIN/MAX of up to 4 whole columns (qe_aggregate_global_streamed, query_exec.c:8842-9112, one
    chunk). Partials are folded in workgroup order. Sequence columns are summed in closed form. */
@@ -102,6 +210,10 @@ int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const Cq
 int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* arg_cols,
                        uint64_t max_groups, uint64_t* out_group_count, int64_t* out_min_key, uint64_t* out_counts, int64_t* out_sums,
                        int64_t* out_mins, int64_t* out_maxs);
+
+/* Why the last operator call returned 0 when it refused the request itself ("" otherwise; GPU
+   failures are in cqlcuda_last_error()). */
+const char* cqlops_last_error(void);
 
 /* Count of kernel launches of the last operator call (for the bench's gpu_launches figure). */
 uint32_t cqlops_last_launches(void);

@@ -57,6 +57,8 @@ def lib():
         L.orc_group_dense.argtypes = [P, u32, u64, C.c_int64, u64, u32, P, P, P, P, P, P, P]
         L.orc_group_cpu_reduce.argtypes = [P, u64, u32, P, u64, P, P, P, P, P]
         L.orc_group_cpu_reduce.restype = u64
+        L.orc_eval_program.argtypes = [P, u32, P, P, P, P, u64, P]
+        L.orc_eval_program.restype = u64
         _lib = L
     return _lib
 
@@ -145,3 +147,18 @@ def group_cpu_reduce(key, args, max_groups):
     ptrs = (C.c_void_p * max(e, 1))(*[a.ctypes.data for a in args] if e else [None])
     n = lib().orc_group_cpu_reduce(_p(key), len(key), e, ptrs, max_groups, _p(keys), _p(counts), _p(sums), _p(mins), _p(maxs))
     return keys[:n], counts[:n], sums[: n * e].reshape(n, e), mins[: n * e].reshape(n, e), maxs[: n * e].reshape(n, e)
+
+
+def eval_program(words, consts, str_pool, slot_arrays, slot_types, rows):
+    """The scan bytecode evaluated per row (orc_eval_program). slot_arrays[s]: the column bound at
+    slot s (raw strings: bytes at s, u64 offsets at s + 1), or None. Returns the match mask (uint8)."""
+    w = np.ascontiguousarray(words, dtype=np.uint32)
+    k = np.ascontiguousarray(consts if len(consts) else [0, 0], dtype=np.uint32)
+    sp = np.frombuffer(bytes(str_pool) + b"\0" * 8, dtype=np.uint8).copy()
+    keep = [np.ascontiguousarray(a) if a is not None else np.zeros(1, dtype=np.uint64) for a in slot_arrays]
+    ptrs = (C.c_void_p * 10)(*[keep[i].ctypes.data if i < len(keep) else None for i in range(10)])
+    types = np.zeros(10, dtype=np.uint32)
+    types[: len(slot_types)] = slot_types
+    mask = np.zeros(max(rows, 1), dtype=np.uint8)
+    lib().orc_eval_program(_p(w), len(w), _p(k), _p(sp), ptrs, _p(types), rows, _p(mask))
+    return mask[:rows]

@@ -479,3 +479,126 @@ uint64_t orc_group_cpu_reduce(const uint32_t* key, uint64_t rows, uint32_t expr_
   free(table);
   return group_count;
 }
+
+/* ---- scan bytecode ---- */
+
+static double slot_value(const void* const* data, const uint32_t* types, uint32_t slot, uint64_t row)
+{
+  const void* p = data[slot];
+  switch (types[slot])
+  {
+    case 1: case 12: return (double)((const uint32_t*)p)[row];
+    case 2:
+    {
+      uint64_t v = ((const uint64_t*)p)[row];
+      return (double)(uint32_t)(v >> 32) * 4294967296.0 + (double)(uint32_t)v;
+    }
+    case 3: return (double)((const float*)p)[row];
+    case 4: return ((const double*)p)[row];
+    case 6: return (double)((const uint8_t*)p)[row];
+    case 7: case 9: return (double)((const int32_t*)p)[row];
+    default:
+    {
+      uint64_t v = ((const uint64_t*)p)[row];
+      double u = (double)(uint32_t)(v >> 32) * 4294967296.0 + (double)(uint32_t)v;
+      return (v >> 63) ? u - 18446744073709551616.0 : u;
+    }
+  }
+}
+
+/* qe_str8_compare-style three-way compare of a row's string with a constant (scan_filter.comp:185-207) */
+static int str_cmp3(const void* const* data, uint32_t slot, uint64_t row, const uint8_t* c, uint32_t len)
+{
+  const uint8_t* bytes = (const uint8_t*)data[slot];
+  const uint64_t* offs = (const uint64_t*)data[slot + 1];
+  uint64_t s = offs[row], e = offs[row + 1], n = e - s, m = n < len ? n : len;
+  for (uint64_t i = 0; i < m; i++)
+  {
+    if (bytes[s + i] != c[i]) return bytes[s + i] < c[i] ? -1 : 1;
+  }
+  return n < len ? -1 : (n > len ? 1 : 0);
+}
+
+static int str_contains(const void* const* data, uint32_t slot, uint64_t row, const uint8_t* c, uint32_t len)
+{
+  const uint8_t* bytes = (const uint8_t*)data[slot];
+  const uint64_t* offs = (const uint64_t*)data[slot + 1];
+  uint64_t s = offs[row], n = offs[row + 1] - s;
+  if (len == 0) return 1;
+  for (uint64_t i = 0; i + len <= n; i++)
+    if (memcmp(bytes + s + i, c, len) == 0) return 1;
+  return 0;
+}
+
+uint64_t orc_eval_program(const uint32_t* words, uint32_t word_count, const uint32_t* consts, const uint8_t* str_pool,
+                          const void* const* slot_data, const uint32_t* slot_types, uint64_t rows, uint8_t* out_match)
+{
+  uint64_t count = 0;
+  double stack[64];
+  for (uint64_t row = 0; row < rows; row++)
+  {
+    int sp = 0;
+    uint32_t ip = 0;
+    int ok = 1;
+    while (ok && ip < word_count)
+    {
+      uint32_t op = words[ip++];
+      if (op == 13) break;
+      switch (op)
+      {
+        case 0: stack[sp++] = 1.0; break;
+        case 14: stack[sp++] = 0.0; break;
+        case 1:
+        {
+          uint32_t operand = words[ip++];
+          uint32_t slot = operand & 0xffu;
+          uint32_t saved = slot_types[slot];
+          uint32_t types_local[10];
+          memcpy(types_local, slot_types, sizeof(types_local));
+          types_local[slot] = (operand >> 8) & 0xffu;
+          (void)saved;
+          stack[sp++] = slot_value(slot_data, types_local, slot, row);
+          break;
+        }
+        case 2:
+        {
+          uint32_t k = words[ip++];
+          uint64_t bits = ((uint64_t)consts[2 * k + 1] << 32) | consts[2 * k];
+          double v;
+          memcpy(&v, &bits, sizeof(v));
+          stack[sp++] = v;
+          break;
+        }
+        case 3: case 4: case 5: case 6: case 7: case 8: case 9: case 10:
+        {
+          double b = stack[--sp], a = stack[--sp];
+          int r = op == 3 ? a == b : op == 4 ? a != b : op == 5 ? a < b : op == 6 ? a > b : op == 7 ? a <= b : op == 8 ? a >= b
+                : op == 9 ? (a != 0.0 && b != 0.0) : (a != 0.0 || b != 0.0);
+          stack[sp++] = r ? 1.0 : 0.0;
+          break;
+        }
+        case 11: case 12: case 17: case 18: case 19: case 20: case 21:
+        {
+          uint32_t slot = words[ip], wo = words[ip + 1], len = words[ip + 2];
+          ip += 3;
+          const uint8_t* c = str_pool + (uint64_t)wo * 4;
+          int r;
+          if (op == 12) r = str_contains(slot_data, slot, row, c, len);
+          else
+          {
+            int t = str_cmp3(slot_data, slot, row, c, len);
+            r = op == 11 ? t == 0 : op == 17 ? t != 0 : op == 18 ? t < 0 : op == 19 ? t > 0 : op == 20 ? t <= 0 : t >= 0;
+          }
+          stack[sp++] = r ? 1.0 : 0.0;
+          break;
+        }
+        default: ok = 0; break;
+      }
+      if (sp >= 63) ok = 0;
+    }
+    int m = sp > 0 && stack[sp - 1] != 0.0;
+    if (out_match) out_match[row] = (uint8_t)m;
+    count += (uint64_t)m;
+  }
+  return count;
+}

@@ -66,6 +66,13 @@ typedef struct OrcLeaf
    scan_simple.comp:214-300). Returns the match count; writes up to `cap` matching rows ascending. */
 uint64_t orc_scan_and(const OrcLeaf* leaves, uint32_t leaf_count, uint64_t rows, uint32_t* out_rows, uint64_t cap);
 
+/* The scan bytecode (opcodes of src/query_exec/query_exec.h:58-81) evaluated row by row with a double
+   stack, as the reference's interpreter scan_filter.comp:325-559 and its CPU scan compute a WHERE
+   clause. slot_data[s] is the column of slot s (a raw string column: bytes at s, u64 offsets at
+   s + 1), slot_types[s] its CQL type. Writes out_match[r] = 1 for a matching row; returns the count. */
+uint64_t orc_eval_program(const uint32_t* words, uint32_t word_count, const uint32_t* consts, const uint8_t* str_pool,
+                          const void* const* slot_data, const uint32_t* slot_types, uint64_t rows, uint8_t* out_match);
+
 /* ---- dense GROUP BY ---- */
 /* Per group g = key - min_key over [0, groups): the count, and per expression the 64-bit
    two's-complement sum, the min and the max of the argument column (as the reference's dense path

@@ -88,7 +88,7 @@ def test_narrow_columns(ops, width, span, n):
     base = 123456
     a = (base + rng.integers(0, span, n)).astype(np.uint32)
     col = ops.Column.from_numpy(a, narrow=True)
-    assert col.width == width
+    assert col.width == (1 if a.max() - a.min() < 256 else 2)
     s, mn, mx = ops.aggregate_global([col])
     assert s[0] == float(a.astype(np.int64).sum())
     assert (mn[0], mx[0]) == (float(a.min()), float(a.max()))

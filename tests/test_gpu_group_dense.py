@@ -74,6 +74,16 @@ def test_group_counts_and_all_functions(ops, groups):
     else:
         # the reference caps a dense group-by at 256 tiles of its 2048-word slices (query_exec.c:7739-7743)
         _check(ops, key, [COUNT, SUM], [None, v])
+        if groups <= 10000:
+            _check(ops, key, [MIN, MAX], [w, w])
+
+
+def test_refuses_what_the_reference_refuses(ops):
+    n = 1000
+    key = (np.arange(n) % 65536).astype(np.uint32)
+    key[-1] = 65535
+    w = np.arange(n, dtype=np.int32)
+    with pytest.raises(ops.OpError, match="256 tiles"):
         _check(ops, key, [MIN, MAX], [w, w])
 
 
