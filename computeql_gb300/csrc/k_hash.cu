@@ -1,6 +1,551 @@
-// Kernel family placeholder: filled in as the hash kernels are built.
+// Hash GROUP BY: slot assignment, compaction, atomic reduce, member lists, member reduce with the
+// HyperLogLog and t-digest sketches, and the selection gather.
+//
+//  aggregate_assign            src/gpu/vulkan/shaders/aggregate_assign.comp:1-186
+//  aggregate_compact           src/gpu/vulkan/shaders/aggregate_compact.comp:1-111
+//  aggregate_hash_reduce_fixed src/gpu/vulkan/shaders/aggregate_hash_reduce_fixed.comp:1-122
+//  csr_scatter / _tiled        src/gpu/vulkan/shaders/csr_scatter.comp:1-31, csr_scatter_tiled.comp:1-77
+//  aggregate_reduce            src/gpu/vulkan/shaders/aggregate_reduce.comp:1-222
+//  selection_gather            src/gpu/vulkan/shaders/selection_gather.comp:1-78
+//
+// The slot table is buckets x K slots whose owner row is claimed with a compare-and-swap, keys are
+// compared as f64 values (or string bytes) and hashed from their bit patterns; the HyperLogLog
+// register update hashes the f64 bit pattern of each value the same way (hash_u32(lo ^ hash_u32(hi)),
+// bucket = top p bits, rho = position of the leading one of the rest), so the registers are
+// identical to the reference's for the same values. GB300 design: persistent grid-stride launches
+// instead of one thread per row, and the member reduce runs one warp per chunk (eight of the
+// reference's 256 lanes per warp lane) so groups of a few rows do not idle 256 threads each, while
+// the per-lane t-digest centroid (first sample, weight) is computed for the same 256 lane positions.
 #include "cql_internal.cuh"
+#include <algorithm>
+#include <float.h>
+
+#define HASH_THREADS 256
+#define EMPTY_SLOT 0xffffffffu
+
+__device__ __forceinline__ uint32_t hash_u32(uint32_t x)
+{
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+// ---------------------------------------------------------------------------------------------
+// aggregate_assign: binding 0 owner row per slot, 1 rows per slot, 2 slot per row, 3 overflow count,
+// 4 + 2c / 5 + 2c key column c (f64 values, or string bytes + u64 offsets);
+// words 0 rows, 2 buckets, 4 K, 6 key columns, 8 string mask
+
+struct KeyCols
+{
+  const uint32_t* data[4];
+  const uint32_t* off[4];
+};
+
+__device__ __forceinline__ uint32_t key_str_off(const KeyCols& k, uint32_t c, uint64_t row) { return k.off[c][row * 2]; }
+__device__ __forceinline__ uint32_t key_byte(const KeyCols& k, uint32_t c, uint64_t i) { return ((const unsigned char*)k.data[c])[i]; }
+
+__device__ uint32_t key_hash(const KeyCols& k, uint32_t ncols, uint32_t string_mask, uint64_t row)
+{
+  uint32_t h = 2166136261u;
+  for (uint32_t c = 0; c < ncols; c++)
+  {
+    uint32_t hh;
+    if ((string_mask >> c) & 1u)
+    {
+      uint32_t s = key_str_off(k, c, row), e = key_str_off(k, c, row + 1);
+      hh = 2166136261u;
+      for (uint32_t i = s; i < e; i++) hh = (hh ^ key_byte(k, c, i)) * 16777619u;
+    }
+    else
+    {
+      uint32_t lo = k.data[c][row * 2], hi = k.data[c][row * 2 + 1];
+      hh = hash_u32(lo ^ hash_u32(hi));
+    }
+    h = hash_u32(h ^ hh);
+  }
+  return h;
+}
+
+__device__ bool keys_equal(const KeyCols& k, uint32_t ncols, uint32_t string_mask, uint64_t a, uint64_t b)
+{
+  for (uint32_t c = 0; c < ncols; c++)
+  {
+    if ((string_mask >> c) & 1u)
+    {
+      uint32_t sa = key_str_off(k, c, a), ea = key_str_off(k, c, a + 1);
+      uint32_t sb = key_str_off(k, c, b), eb = key_str_off(k, c, b + 1);
+      if (ea - sa != eb - sb) return false;
+      for (uint32_t i = 0; i < ea - sa; i++)
+        if (key_byte(k, c, sa + i) != key_byte(k, c, sb + i)) return false;
+    }
+    else
+    {
+      double x = __hiloint2double((int)k.data[c][a * 2 + 1], (int)k.data[c][a * 2]);
+      double y = __hiloint2double((int)k.data[c][b * 2 + 1], (int)k.data[c][b * 2]);
+      if (!(x == y)) return false;
+    }
+  }
+  return true;
+}
+
+__global__ void __launch_bounds__(HASH_THREADS) k_aggregate_assign(CqlLaunch a, uint64_t rows)
+{
+  uint32_t* owner = (uint32_t*)a.buf[0];
+  uint32_t* counts = (uint32_t*)a.buf[1];
+  uint32_t* row_slot = (uint32_t*)a.buf[2];
+  uint32_t* overflow = (uint32_t*)a.buf[3];
+  uint32_t buckets = cql_word(a, 2), K = cql_word(a, 4), ncols = cql_word(a, 6), string_mask = cql_word(a, 8);
+  if (ncols > 4) ncols = 4;
+  KeyCols k;
+  for (int c = 0; c < 4; c++)
+  {
+    k.data[c] = (const uint32_t*)a.buf[4 + 2 * c];
+    k.off[c] = (const uint32_t*)a.buf[5 + 2 * c];
+  }
+  uint64_t slots = a.bytes[0] / 4;
+  for (uint64_t row = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; row < rows; row += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint32_t h = ncols ? key_hash(k, ncols, string_mask, row) : 0u;
+    uint64_t start = (uint64_t)(h % (buckets ? buckets : 1u)) * K;
+    uint32_t claimed = EMPTY_SLOT;
+    for (uint32_t p = 0; p < K; p++)
+    {
+      uint64_t slot = start + p;
+      if (slot >= slots) break;
+      uint32_t prev = atomicCAS(&owner[slot], EMPTY_SLOT, (uint32_t)row);
+      if (prev == EMPTY_SLOT || keys_equal(k, ncols, string_mask, row, prev))
+      {
+        claimed = (uint32_t)slot;
+        break;
+      }
+    }
+    if (claimed == EMPTY_SLOT)
+    {
+      atomicAdd(overflow, 1u);
+      continue;
+    }
+    row_slot[row] = claimed;
+    atomicAdd(&counts[claimed], 1u);
+  }
+}
+
+static int launch_aggregate_assign(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t rows = cql_word(a, 0);
+  if (rows == 0) return 0;
+  k_aggregate_assign<<<cql_stream_grid((rows + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, rows);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// aggregate_compact: three modes over blocks of 256 slots (the block sums index is index / 256)
+
+__device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* sh, uint32_t* total)
+{
+  uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= (uint32_t)o) incl += y;
+  }
+  if (lane == 31) sh[warp] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    uint32_t run = 0;
+    for (int w = 0; w < HASH_THREADS / 32; w++)
+    {
+      uint32_t t = sh[w];
+      sh[w] = run;
+      run += t;
+    }
+    sh[HASH_THREADS / 32] = run;
+  }
+  __syncthreads();
+  uint32_t ex = sh[warp] + incl - v;
+  *total = sh[HASH_THREADS / 32];
+  __syncthreads();
+  return ex;
+}
+
+__global__ void __launch_bounds__(HASH_THREADS) k_aggregate_compact(CqlLaunch a, uint32_t mode, uint32_t n)
+{
+  __shared__ uint32_t sh[HASH_THREADS / 32 + 1];
+  const uint32_t* counts = (const uint32_t*)a.buf[0];
+  const uint32_t* owner = (const uint32_t*)a.buf[1];
+  uint32_t* offsets = (uint32_t*)a.buf[2];
+  uint32_t* block_sums = (uint32_t*)a.buf[3];
+  uint32_t* out_owner = (uint32_t*)a.buf[4];
+  uint32_t* out_count = (uint32_t*)a.buf[5];
+  uint32_t* total_out = (uint32_t*)a.buf[6];
+  uint32_t blocks = (n + 255) / 256;
+  uint32_t total;
+  if (mode == 0)
+  {
+    for (uint32_t b = blockIdx.x; b < blocks; b += gridDim.x)
+    {
+      uint32_t index = b * 256 + threadIdx.x;
+      uint32_t v = (index < n && counts[index] != 0) ? 1u : 0u;
+      uint32_t ex = block_exclusive_scan(v, sh, &total);
+      if (index < n) offsets[index] = ex;
+      if (threadIdx.x == 0) block_sums[b] = total;
+    }
+  }
+  else if (mode == 1)
+  {
+    if (blockIdx.x != 0) return;
+    uint32_t chunk = (blocks + 255) / 256;
+    uint32_t start = min(threadIdx.x * chunk, blocks), end = min(start + chunk, blocks);
+    uint32_t sum = 0;
+    for (uint32_t i = start; i < end; i++) sum += block_sums[i];
+    uint32_t running = block_exclusive_scan(sum, sh, &total);
+    for (uint32_t i = start; i < end; i++)
+    {
+      uint32_t t = block_sums[i];
+      block_sums[i] = running;
+      running += t;
+    }
+    if (threadIdx.x == 0)
+    {
+      offsets[n] = total;
+      total_out[0] = total;
+    }
+  }
+  else
+  {
+    for (uint64_t index = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; index < n; index += (uint64_t)gridDim.x * blockDim.x)
+    {
+      uint32_t id = offsets[index] + block_sums[index / 256];
+      offsets[index] = id;
+      uint32_t c = counts[index];
+      if (c != 0)
+      {
+        out_owner[id] = owner[index];
+        out_count[id] = c;
+      }
+    }
+  }
+}
+
+static int launch_aggregate_compact(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint32_t n = cql_word(a, 0), mode = cql_word(a, 2);
+  uint32_t blocks = (n + 255) / 256;
+  if (mode == 1) k_aggregate_compact<<<1, HASH_THREADS, 0, stream>>>(a, mode, n);
+  else k_aggregate_compact<<<cql_stream_grid(blocks ? blocks : 1, 8), HASH_THREADS, 0, stream>>>(a, mode, n);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// aggregate_hash_reduce_fixed: binding 0 slot per row, 1 group per slot, 2 sums (lo, hi), 3 counts,
+// 4 mins, 5 maxs, 6..13 f64 arguments; words 0 rows, 2 exprs, 4 funcs, 6 power-of-ten exponents
+
+#define FUNC_COUNT 0u
+#define FUNC_SUM 1u
+#define FUNC_AVG 2u
+#define FUNC_MIN 3u
+#define FUNC_MAX 4u
+#define FUNC_ACD 5u
+#define FUNC_PCT 6u
+
+__constant__ double c_pow10[7] = { 1.0, 10.0, 100.0, 1000.0, 10000.0, 100000.0, 1000000.0 };
+
+__global__ void __launch_bounds__(HASH_THREADS) k_hash_reduce_fixed(CqlLaunch a, uint64_t rows)
+{
+  const uint32_t* row_slot = (const uint32_t*)a.buf[0];
+  const uint32_t* slot_group = (const uint32_t*)a.buf[1];
+  unsigned long long* sums = (unsigned long long*)a.buf[2];
+  uint32_t* counts = (uint32_t*)a.buf[3];
+  int* mins = (int*)a.buf[4];
+  int* maxs = (int*)a.buf[5];
+  uint32_t exprs = min(cql_word(a, 2), 8u), funcs = cql_word(a, 4), scales = cql_word(a, 6);
+  for (uint64_t row = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; row < rows; row += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint32_t slot = row_slot[row];
+    if (slot == EMPTY_SLOT) continue;
+    uint32_t g = slot_group[slot];
+    if (g == EMPTY_SLOT) continue;
+    for (uint32_t e = 0; e < exprs; e++)
+    {
+      uint32_t f = (funcs >> (e * 4)) & 0xfu;
+      uint64_t index = (uint64_t)g * exprs + e;
+      atomicAdd(&counts[index], 1u);
+      if (f == FUNC_COUNT) continue;
+      double scaled = ((const double*)a.buf[6 + e])[row] * c_pow10[min((scales >> (e * 4)) & 0xfu, 6u)];
+      int q = (int)floor(scaled + 0.5);
+      if (f == FUNC_SUM || f == FUNC_AVG) atomicAdd(&sums[index], (unsigned long long)(long long)q);
+      else if (f == FUNC_MIN) atomicMin(&mins[index], q);
+      else if (f == FUNC_MAX) atomicMax(&maxs[index], q);
+    }
+  }
+}
+
+static int launch_hash_reduce_fixed(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t rows = cql_word(a, 0);
+  if (rows == 0) return 0;
+  k_hash_reduce_fixed<<<cql_stream_grid((rows + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, rows);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// csr_scatter (and the tiled variant, same bindings plus the slot count in slot 1): every row takes
+// the next place of its slot's member list through the slot's cursor
+
+__global__ void __launch_bounds__(HASH_THREADS) k_csr_scatter(CqlLaunch a, uint64_t rows)
+{
+  const uint32_t* row_slot = (const uint32_t*)a.buf[0];
+  uint32_t* cursor = (uint32_t*)a.buf[1];
+  uint32_t* out_rows = (uint32_t*)a.buf[2];
+  uint64_t cap = a.bytes[2] / 4;
+  for (uint64_t row = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; row < rows; row += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint32_t slot = row_slot[row];
+    if (slot == EMPTY_SLOT) continue;
+    uint32_t pos = atomicAdd(&cursor[slot], 1u);
+    if (pos < cap) out_rows[pos] = (uint32_t)row;
+  }
+}
+
+static int launch_csr_scatter(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t rows = cql_word(a, 0);
+  if (rows == 0) return 0;
+  k_csr_scatter<<<cql_stream_grid((rows + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, rows);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// aggregate_reduce: chunk c covers members [range[2c], range[2c+1]) of group chunk_group[c].
+// binding 0 members, 1 chunk ranges, 2 chunk groups, 3 representative per group, 4 partials
+// [chunk][expr][acc, count, min, max], 5..12 f64 arguments, 13 HLL registers
+// [group][hll expr][2^p], 14/15 t-digest centroid mean/weight [chunk][pct expr][256].
+// words 0 chunks, 2 exprs, 4 funcs, 6 identity mode, 8 HLL precision, 10 HLL slot per expr,
+// 12 HLL exprs, 14 percentile exprs, 15 percentile slot per expr
+
+__device__ __forceinline__ void hll_add(uint32_t* sketch, uint64_t sketch_words, uint32_t slot, uint32_t g, uint32_t nhll, uint32_t p, double value)
+{
+  unsigned long long bits = (unsigned long long)__double_as_longlong(value);
+  uint32_t lo = (uint32_t)bits, hi = (uint32_t)(bits >> 32);
+  uint32_t h = hash_u32(lo ^ hash_u32(hi));
+  uint32_t rest_bits = 32u - p;
+  uint32_t bucket = h >> rest_bits;
+  uint32_t rest = h & ((1u << rest_bits) - 1u);
+  // findMSB: the index of the highest set bit, -1 for zero
+  int msb = rest ? 31 - __clz(rest) : -1;
+  uint32_t rho = msb < 0 ? rest_bits + 1u : rest_bits - (uint32_t)msb;
+  uint64_t idx = ((uint64_t)g * nhll + slot) * (1ull << p) + bucket;
+  if (idx < sketch_words) atomicMax(&sketch[idx], rho);
+}
+
+__global__ void __launch_bounds__(HASH_THREADS) k_aggregate_reduce(CqlLaunch a, uint32_t chunks)
+{
+  const uint32_t* members = (const uint32_t*)a.buf[0];
+  const uint32_t* range = (const uint32_t*)a.buf[1];
+  const uint32_t* chunk_group = (const uint32_t*)a.buf[2];
+  uint32_t* repr = (uint32_t*)a.buf[3];
+  double* partials = (double*)a.buf[4];
+  uint32_t* sketch = (uint32_t*)a.buf[13];
+  float* dmean = (float*)a.buf[14];
+  float* dweight = (float*)a.buf[15];
+  uint64_t sketch_words = a.bytes[13] / 4, digest_cap = a.bytes[14] / 4, partial_cap = a.bytes[4] / 8;
+  uint32_t exprs = min(cql_word(a, 2), 8u), funcs = cql_word(a, 4);
+  bool identity = cql_word(a, 6) != 0;
+  uint32_t p = cql_word(a, 8), hll_slots = cql_word(a, 10), nhll = cql_word(a, 12);
+  uint32_t npct = cql_word(a, 14), pct_slots = cql_word(a, 15);
+  if (p > 16) p = 16;
+  uint32_t lane = threadIdx.x & 31;
+  uint32_t warps_total = gridDim.x * (blockDim.x / 32);
+  for (uint32_t c = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); c < chunks; c += warps_total)
+  {
+    uint32_t start = range[c * 2], end = range[c * 2 + 1];
+    uint32_t g = chunk_group[c];
+    if (lane == 0) repr[g] = identity ? start : members[start];
+    for (uint32_t e = 0; e < exprs; e++)
+    {
+      uint32_t f = (funcs >> (e * 4)) & 0xfu;
+      const double* arg = (const double*)a.buf[5 + e];
+      double acc = 0.0, mn = 1.0e300, mx = -1.0e300;
+      uint32_t count = 0;
+      // this lane stands for reference lanes t = lane + 32 j, j = 0..7
+      for (uint32_t j = 0; j < 8; j++)
+      {
+        uint32_t t = lane + 32 * j;
+        double first = 0.0;
+        uint32_t tcount = 0;
+        for (uint32_t m = start + t; m < end; m += 256)
+        {
+          uint32_t row = identity ? m : members[m];
+          tcount++;
+          if (f == FUNC_SUM || f == FUNC_AVG) acc += arg[row];
+          else if (f == FUNC_MIN) { double v = arg[row]; if (v < mn) mn = v; }
+          else if (f == FUNC_MAX) { double v = arg[row]; if (v > mx) mx = v; }
+          else if (f == FUNC_ACD) hll_add(sketch, sketch_words, (hll_slots >> (e * 4)) & 0xfu, g, nhll, p, arg[row]);
+          else if (f == FUNC_PCT && tcount == 1) first = arg[row];
+        }
+        count += tcount;
+        if (f == FUNC_PCT)
+        {
+          uint64_t di = ((uint64_t)c * npct + ((pct_slots >> (e * 4)) & 0xfu)) * 256u + t;
+          if (di < digest_cap)
+          {
+            dmean[di] = (float)first;
+            dweight[di] = (float)tcount;
+          }
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+      {
+        acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        double omn = __shfl_xor_sync(0xffffffffu, mn, o);
+        double omx = __shfl_xor_sync(0xffffffffu, mx, o);
+        mn = omn < mn ? omn : mn;
+        mx = omx > mx ? omx : mx;
+        count += __shfl_xor_sync(0xffffffffu, count, o);
+      }
+      if (lane == 0)
+      {
+        uint64_t base = ((uint64_t)c * exprs + e) * 4;
+        if (base + 3 < partial_cap)
+        {
+          partials[base + 0] = acc;
+          partials[base + 1] = (double)count;
+          partials[base + 2] = mn;
+          partials[base + 3] = mx;
+        }
+      }
+    }
+  }
+}
+
+static int launch_aggregate_reduce(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint32_t chunks = cql_word(a, 0);
+  if (chunks == 0) return 0;
+  uint32_t warps = HASH_THREADS / 32;
+  k_aggregate_reduce<<<cql_stream_grid((chunks + warps - 1) / warps, 8), HASH_THREADS, 0, stream>>>(a, chunks);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// selection_gather: binding 0 rows (one index every `stride` words), 1 source, 2 destination,
+// 3 positions; words 0 count, 2 stride, 4 row offset, 6 mode, 8 map stride, 10 word offset, 12 map offset
+
+__global__ void __launch_bounds__(HASH_THREADS) k_selection_gather(CqlLaunch a, uint64_t count)
+{
+  const uint32_t* rows = (const uint32_t*)a.buf[0];
+  const uint32_t* source = (const uint32_t*)a.buf[1];
+  uint32_t* dest = (uint32_t*)a.buf[2];
+  const uint32_t* positions = (const uint32_t*)a.buf[3];
+  uint32_t stride = cql_word(a, 2), row_offset = cql_word(a, 4), mode = cql_word(a, 6);
+  uint32_t map_stride = cql_word(a, 8), word_offset = cql_word(a, 10), map_offset = cql_word(a, 12);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x)
+  {
+    if (mode == 2)
+    {
+      uint32_t index = rows[(uint64_t)positions[i] * stride + word_offset];
+      dest[i] = index == EMPTY_SLOT ? EMPTY_SLOT : index + row_offset;
+      continue;
+    }
+    uint32_t index = rows[i * stride + word_offset];
+    if (mode == 4)
+    {
+      dest[i] = index == EMPTY_SLOT ? EMPTY_SLOT : index + row_offset;
+      continue;
+    }
+    if (mode == 3)
+    {
+      uint32_t mapped = index == EMPTY_SLOT ? EMPTY_SLOT : source[(uint64_t)index * map_stride];
+      dest[i] = mapped == EMPTY_SLOT ? EMPTY_SLOT : mapped + map_offset;
+      continue;
+    }
+    bool has = index != EMPTY_SLOT;
+    uint64_t row = (uint64_t)index + row_offset;
+    if (mode == 0)
+    {
+      uint2 v = has ? *(const uint2*)(source + row * 2) : make_uint2(0, 0);
+      *(uint2*)(dest + i * 2) = v;
+    }
+    else dest[i] = has ? source[row] : 0u;
+  }
+}
+
+static int launch_selection_gather(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t count = cql_word(a, 0);
+  if (count == 0) return 0;
+  k_selection_gather<<<cql_stream_grid((count + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, count);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Widening of a device column to dense f64 (the gather the operator layer does on the host before
+// a hash GROUP BY, query_exec.c:10454-10690): binding 0 source, 1 destination; word 0 rows, word 2
+// the source CQL type. Not a reference kernel: the reference uploads the f64 copy it builds on the host.
+
+__global__ void __launch_bounds__(HASH_THREADS) k_widen_f64(CqlLaunch a, uint64_t rows, uint32_t type)
+{
+  const uint32_t* s = (const uint32_t*)a.buf[0];
+  double* d = (double*)a.buf[1];
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (uint64_t)gridDim.x * blockDim.x)
+  {
+    double v;
+    switch (type)
+    {
+      case 1: v = (double)s[i]; break;
+      case 7: v = (double)(int)s[i]; break;
+      case 3: v = (double)__uint_as_float(s[i]); break;
+      case 4: v = ((const double*)s)[i]; break;
+      case 2: v = (double)((const unsigned long long*)s)[i]; break;
+      default: v = (double)((const long long*)s)[i]; break;
+    }
+    d[i] = v;
+  }
+}
+
+static int launch_widen_f64(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t rows = a.push[0];
+  if (rows == 0) return 0;
+  k_widen_f64<<<cql_stream_grid((rows + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, rows, cql_word(a, 2));
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
 
 const CqlKernelDesc cql_kernels_hash[] = {
+  { "aggregate_assign", launch_aggregate_assign },
+  { "aggregate_compact", launch_aggregate_compact },
+  { "aggregate_hash_reduce_fixed", launch_hash_reduce_fixed },
+  { "csr_scatter", launch_csr_scatter },
+  { "csr_scatter_tiled", launch_csr_scatter },
+  { "aggregate_reduce", launch_aggregate_reduce },
+  { "selection_gather", launch_selection_gather },
+  { "cql_widen_f64", launch_widen_f64 },
   { nullptr, nullptr },
 };

@@ -136,9 +136,12 @@ static int bind_columns(CqlKernel* k, const CqlProgram* prog, const CqlColumn* c
   return 1;
 }
 
+/* the table's row count: a program that reads no column (a folded TRUE/FALSE) still runs over the
+   rows of the table its columns belong to */
 static uint64_t program_rows(const CqlProgram* prog, const CqlColumn* columns, uint64_t fallback)
 {
-  return prog->binding_count ? columns[prog->binding_column[0]].rows : fallback;
+  (void)fallback;
+  return prog->binding_count ? columns[prog->binding_column[0]].rows : columns[0].rows;
 }
 
 static int cmp_u32(const void* a, const void* b)
@@ -201,7 +204,6 @@ int cqlops_scan_filter(const CqlProgram* prog, const CqlColumn* columns, uint32_
 {
   cqlops_note_error("");
   if (prog->requires_cpu_scan || prog->has_score_output) return refuse("the program needs the CPU scan, which this backend does not have");
-  if (prog->binding_count == 0) return refuse("a filter with no column has no row count");
   uint64_t rows = program_rows(prog, columns, 0);
 
   if (strategy == CQLOPS_SCAN_AUTO || strategy == CQLOPS_SCAN_SIMPLE)
@@ -323,7 +325,7 @@ int cqlops_fused_filter_aggregate(const CqlProgram* prog_in, const CqlColumn* co
       fuse.coltypes[c] = col->type;
     }
   }
-  if (ok && prog->binding_count == 0) ok = refuse("a fused aggregate needs a column for its row count");
+
   CqlKernel* k = ok ? generated_kernel(prog, CQLOPS_KERNEL_FUSED_AGG, &fuse) : NULL;
   CqlBuffer *code = NULL, *consts = NULL, *strs = NULL;
   if (k) ok = upload_program(prog, &code, &consts, &strs);

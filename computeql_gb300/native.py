@@ -140,6 +140,9 @@ OPS_API = [
     ("cqlops_scan_filter", C.c_int, [P, P, u32, P, P, u64, P]),
     ("cqlops_fused_filter_aggregate", C.c_int, [P, P, P, u32, P, P, P, P]),
     ("cqlops_fused_filter_group", C.c_int, [P, P, P, u32, P, u32, u64, P, P, P, P, P, P, P, P]),
+    ("cqlops_group_hash", C.c_int, [P, u32, u32, P, P, P, u64, u32, u64, P, P, P, P, P]),
+    ("cqlops_hll_estimate", dbl, [P, u64]),
+    ("cqlops_tdigest_percentile", dbl, [P, P, u64, dbl]),
 ]
 
 _cuda = None

@@ -317,6 +317,33 @@ def fused_group(program, key_names, agg_names, max_groups=1 << 16):
             "sums": sums[: G * ac].reshape(G, ac), "mins": mins[: G * ac].reshape(G, ac), "maxs": maxs[: G * ac].reshape(G, ac)}
 
 
+FUNC_ACD, FUNC_PCT = 5, 6
+
+
+def group_hash(keys, funcs, args, params=None, group_hint=0, path=0, max_groups=None):
+    """Hash GROUP BY -> dict(groups, repr_row[G], counts[G], results[G, E], path)."""
+    kc, e = len(keys), len(funcs)
+    kcols = (N.CqlColumn * max(kc, 1))(*[k.c() for k in keys])
+    structs = {}
+    for a in args:
+        if a is not None and id(a) not in structs:
+            structs[id(a)] = a.c()
+    arg_ptrs = (C.c_void_p * e)(*[C.addressof(structs[id(a)]) if a is not None else None for a in args])
+    fa = np.array(funcs, dtype=np.uint32)
+    pa = np.array(params if params is not None else [0.5] * e, dtype=np.float64)
+    rows = keys[0].rows if keys else next(a.rows for a in args if a is not None)
+    mg = max_groups if max_groups is not None else rows
+    repr_row = np.zeros(max(mg, 1), dtype=np.uint64)
+    counts = np.zeros(max(mg, 1), dtype=np.uint64)
+    results = np.zeros(max(mg, 1) * e, dtype=np.float64)
+    g = C.c_uint64()
+    used = C.c_uint32()
+    _check(N.load_ops().cqlops_group_hash(kcols, kc, e, N.ptr(fa), arg_ptrs, N.ptr(pa), group_hint, path, mg, C.byref(g), N.ptr(repr_row),
+                                          N.ptr(counts), N.ptr(results), C.byref(used)), "cqlops_group_hash")
+    G = g.value
+    return {"groups": G, "repr_row": repr_row[:G], "counts": counts[:G], "results": results[: G * e].reshape(G, e), "path": used.value}
+
+
 def compile_check(source):
     """NVRTC compile of a generated source for sm_103a, no device needed -> (ok, log)."""
     lib = N.load_cuda()

@@ -211,6 +211,21 @@ int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count,
                        uint64_t max_groups, uint64_t* out_group_count, int64_t* out_min_key, uint64_t* out_counts, int64_t* out_sums,
                        int64_t* out_mins, int64_t* out_maxs);
 
+/* Hash GROUP BY of up to 4 keys (numeric, widened to f64, or raw strings) with up to 8 aggregates:
+   COUNT/SUM/AVG/MIN/MAX, APPROX_COUNT_DISTINCT (HyperLogLog, precision 10) and APPROX_PERCENTILE
+   (t-digest, params[e] is the fraction) - qe_aggregate_impl's GPU hash path,
+   src/query_exec/query_exec.c:10258-12300. group_hint > 0 sizes the table for that many groups.
+   path: 0 automatic, 1 member lists + aggregate_reduce, 2 the fixed-point atomic reduce. Per dense
+   group g: out_repr_row[g] (a row of the group), out_counts[g], out_results[g*expr_count + e].
+   out_path receives the path taken (1 or 2). */
+int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* args,
+                      const double* params, uint64_t group_hint, uint32_t path, uint64_t max_groups, uint64_t* out_group_count,
+                      uint64_t* out_repr_row, uint64_t* out_counts, double* out_results, uint32_t* out_path);
+/* qe_hll_estimate_cardinality (query_exec.c:6711-6737) over m registers. */
+double cqlops_hll_estimate(const uint32_t* registers, uint64_t m);
+/* qe_tdigest_estimate_percentile (query_exec.c:6748-6790); sorts the centroids in place. */
+double cqlops_tdigest_percentile(float* means, float* weights, uint64_t count, double fraction);
+
 /* Why the last operator call returned 0 when it refused the request itself ("" otherwise; GPU
    failures are in cqlcuda_last_error()). */
 const char* cqlops_last_error(void);

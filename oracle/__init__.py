@@ -13,7 +13,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
-SOURCES = [os.path.join(HERE, "oracle.c")]
+SOURCES = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "oracle_sketch.c")]
 
 U32, U64, F32, F64, I32, I64 = 1, 2, 3, 4, 7, 8
 
@@ -59,6 +59,11 @@ def lib():
         L.orc_group_cpu_reduce.restype = u64
         L.orc_eval_program.argtypes = [P, u32, P, P, P, P, u64, P]
         L.orc_eval_program.restype = u64
+        L.orc_hll_add.argtypes = [P, u64, u32, P]
+        L.orc_hll_estimate.argtypes = [P, u64]
+        L.orc_hll_estimate.restype = dbl
+        L.orc_tdigest_percentile.argtypes = [P, P, u64, dbl]
+        L.orc_tdigest_percentile.restype = dbl
         _lib = L
     return _lib
 
@@ -162,3 +167,21 @@ def eval_program(words, consts, str_pool, slot_arrays, slot_types, rows):
     mask = np.zeros(max(rows, 1), dtype=np.uint8)
     lib().orc_eval_program(_p(w), len(w), _p(k), _p(sp), ptrs, _p(types), rows, _p(mask))
     return mask[:rows]
+
+
+def hll_registers(values, p=10):
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    regs = np.zeros(1 << p, dtype=np.uint32)
+    lib().orc_hll_add(_p(v), len(v), p, _p(regs))
+    return regs
+
+
+def hll_estimate(regs):
+    r = np.ascontiguousarray(regs, dtype=np.uint32)
+    return lib().orc_hll_estimate(_p(r), len(r))
+
+
+def tdigest_percentile(means, weights, fraction):
+    m = np.ascontiguousarray(means, dtype=np.float32)
+    w = np.ascontiguousarray(weights, dtype=np.float32)
+    return lib().orc_tdigest_percentile(_p(m), _p(w), len(m), fraction)

@@ -73,6 +73,16 @@ uint64_t orc_scan_and(const OrcLeaf* leaves, uint32_t leaf_count, uint64_t rows,
 uint64_t orc_eval_program(const uint32_t* words, uint32_t word_count, const uint32_t* consts, const uint8_t* str_pool,
                           const void* const* slot_data, const uint32_t* slot_types, uint64_t rows, uint8_t* out_match);
 
+/* ---- sketches ---- */
+/* HyperLogLog registers of a set of values (hll_add, src/gpu/vulkan/shaders/aggregate_reduce.comp:66-92):
+   h = hash_u32(lo ^ hash_u32(hi)) of the value's f64 bits, bucket = top p bits, rho from the leading
+   one of the rest; regs[bucket] = max(regs, rho). regs has 2^p entries and is not cleared here. */
+void orc_hll_add(const double* values, uint64_t n, uint32_t p, uint32_t* regs);
+/* qe_hll_estimate_cardinality (src/query_exec/query_exec.c:6711-6737), not rounded. */
+double orc_hll_estimate(const uint32_t* regs, uint64_t m);
+/* qe_tdigest_estimate_percentile (src/query_exec/query_exec.c:6748-6790) over (mean, weight) centroids; sorts them. */
+double orc_tdigest_percentile(float* means, float* weights, uint64_t count, double fraction);
+
 /* ---- dense GROUP BY ---- */
 /* Per group g = key - min_key over [0, groups): the count, and per expression the 64-bit
    two's-complement sum, the min and the max of the argument column (as the reference's dense path

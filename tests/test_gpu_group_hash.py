@@ -1,0 +1,178 @@
+"""Hash GROUP BY, HyperLogLog and t-digest through the C ABI against the oracle.
+
+Counts, whole-number sums, minimums, maximums and group membership are bit-exact; f64 sums within
+1e-12 relative; HyperLogLog estimates equal the oracle's estimate from its own registers (so the
+registers agree) and stay within the reference's 3 x 1.04 / sqrt(2^10) bound
+(src/tests/bench_query_approx_agg.c:174-179); t-digest percentiles within the reference's 5 %
+(:265-270); the exact edge cases 1 row -> 1 and all-identical -> 1 (:428-478).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+COUNT, SUM, AVG, MIN, MAX, ACD, PCT = 0, 1, 2, 3, 4, 5, 6
+HLL_BOUND = 3 * 1.04 / math.sqrt(1024)
+
+
+@pytest.fixture(scope="module")
+def ops(gpu):
+    from computeql_gb300 import ops as o
+    return o
+
+
+def by_key(res, key_arrays):
+    """group results keyed by the key values of each group's representative row"""
+    out = {}
+    for g in range(res["groups"]):
+        r = int(res["repr_row"][g])
+        out[tuple(k[r].item() for k in key_arrays)] = (int(res["counts"][g]), res["results"][g])
+    return out
+
+
+@pytest.mark.parametrize("path", [0, 1])
+@pytest.mark.parametrize("groups", [1, 7, 1000, 100_000])
+def test_integer_aggregates_per_group(ops, path, groups):
+    n = 1_000_003
+    rng = np.random.default_rng(groups)
+    key = rng.integers(0, groups, n).astype(np.uint32)
+    v = rng.integers(0, 1 << 20, n).astype(np.uint32)
+    w = rng.integers(-(1 << 20), 1 << 20, n).astype(np.int32)
+    kc, vc, wc = ops.Column.from_numpy(key), ops.Column.from_numpy(v), ops.Column.from_numpy(w)
+    res = ops.group_hash([kc], [COUNT, SUM, MIN, MAX, SUM, AVG], [None, vc, vc, vc, wc, wc], path=path)
+    assert res["path"] == (2 if path == 0 else 1)
+    got = by_key(res, [key])
+    uniq = np.unique(key)
+    assert len(got) == len(uniq)
+    order = np.argsort(key, kind="stable")
+    ks = key[order]
+    starts = np.searchsorted(ks, uniq)
+    ends = np.searchsorted(ks, uniq, side="right")
+    for u, s, e in zip(uniq, starts, ends):
+        rows = order[s:e]
+        cnt, r = got[(int(u),)]
+        assert cnt == e - s
+        assert r[0] == e - s
+        assert r[1] == float(v[rows].astype(np.int64).sum())
+        assert (r[2], r[3]) == (float(v[rows].min()), float(v[rows].max()))
+        ws = float(w[rows].astype(np.int64).sum())
+        assert r[4] == ws
+        assert r[5] == ws / (e - s)
+
+
+def test_two_keys_and_f64_arguments(ops):
+    n = 400_001
+    rng = np.random.default_rng(5)
+    k1 = rng.integers(0, 30, n).astype(np.uint32)
+    k2 = rng.integers(-5, 5, n).astype(np.int32)
+    d = rng.lognormal(3.0, 1.0, n)
+    res = ops.group_hash([ops.Column.from_numpy(k1), ops.Column.from_numpy(k2)], [SUM, MIN, MAX, COUNT], [ops.Column.from_numpy(d)] * 3 + [None])
+    dcol_res = by_key(res, [k1, k2])
+    assert len(dcol_res) == len(set(zip(k1.tolist(), k2.tolist())))
+    for (a, b), (cnt, r) in dcol_res.items():
+        sel = d[(k1 == a) & (k2 == b)]
+        assert cnt == len(sel) and r[3] == len(sel)
+        exact = math.fsum(sel)
+        assert abs(r[0] - exact) <= 1e-12 * abs(exact)
+        assert (r[1], r[2]) == (sel.min(), sel.max())
+
+
+def test_string_keys(ops):
+    n = 200_000
+    rng = np.random.default_rng(8)
+    words = ["north", "south", "east", "west", "centre", "", "x" * 40]
+    vals = [words[i] for i in rng.integers(0, len(words), n)]
+    v = rng.integers(0, 100, n).astype(np.uint32)
+    sc = ops.StringColumn(vals)
+    res = ops.group_hash([sc], [COUNT, SUM], [None, ops.Column.from_numpy(v)])
+    assert res["groups"] == len(set(vals))
+    arr = np.array(vals, dtype=object)
+    for g in range(res["groups"]):
+        name = vals[int(res["repr_row"][g])]
+        sel = arr == name
+        assert res["counts"][g] == sel.sum()
+        assert res["results"][g, 1] == float(v[sel].astype(np.int64).sum())
+
+
+@pytest.mark.parametrize("distinct", [1, 2, 100, 5000, 4_000_000])
+def test_hll_global_matches_oracle_registers(ops, distinct):
+    n = 2_000_000 if distinct < 4_000_000 else 10_000_000
+    rng = np.random.default_rng(distinct)
+    session = rng.integers(0, distinct, n).astype(np.uint32)
+    res = ops.group_hash([], [ACD], [ops.Column.from_numpy(session)])
+    assert res["groups"] == 1
+    est = res["results"][0, 0]
+    want = round(oracle.hll_estimate(oracle.hll_registers(session.astype(np.float64))))
+    assert est == want
+    true = len(np.unique(session))
+    assert abs(est - true) <= HLL_BOUND * true
+
+
+def test_hll_per_group_matches_oracle(ops):
+    n = 1_000_000
+    rng = np.random.default_rng(77)
+    key = rng.integers(0, 10, n).astype(np.uint32)
+    val = rng.integers(0, 50_000, n).astype(np.uint32)
+    res = ops.group_hash([ops.Column.from_numpy(key)], [ACD, COUNT], [ops.Column.from_numpy(val), None])
+    for g in range(res["groups"]):
+        k = key[int(res["repr_row"][g])]
+        sel = val[key == k].astype(np.float64)
+        assert res["results"][g, 0] == round(oracle.hll_estimate(oracle.hll_registers(sel)))
+        assert res["results"][g, 1] == len(sel)
+
+
+def test_hll_exact_edge_cases(ops):
+    one = ops.Column.from_numpy(np.array([42], dtype=np.uint32))
+    assert ops.group_hash([], [ACD], [one])["results"][0, 0] == 1
+    same = ops.Column.from_numpy(np.full(100_000, 7, dtype=np.uint32))
+    assert ops.group_hash([], [ACD], [same])["results"][0, 0] == 1
+    empty = ops.Column.from_numpy(np.zeros(0, dtype=np.uint32))
+    assert ops.group_hash([], [ACD], [empty])["groups"] == 0
+
+
+@pytest.mark.parametrize("fraction", [0.1, 0.5, 0.9, 0.99])
+def test_tdigest_within_five_percent(ops, fraction):
+    n = 1_000_000
+    rng = np.random.default_rng(int(fraction * 100))
+    d = rng.lognormal(3.0, 1.0, n)
+    res = ops.group_hash([], [PCT], [ops.Column.from_numpy(d)], params=[fraction])
+    exact = float(np.quantile(d, fraction))
+    assert abs(res["results"][0, 0] - exact) <= 0.05 * exact
+
+
+def test_tdigest_single_row_and_grouped(ops):
+    one = ops.Column.from_numpy(np.array([3.25]))
+    assert ops.group_hash([], [PCT], [one], params=[0.5])["results"][0, 0] == 3.25
+    n = 500_000
+    rng = np.random.default_rng(3)
+    key = rng.integers(0, 5, n).astype(np.uint32)
+    d = rng.random(n) * 100
+    res = ops.group_hash([ops.Column.from_numpy(key)], [PCT, COUNT], [ops.Column.from_numpy(d), None], params=[0.5, 0.5])
+    for g in range(res["groups"]):
+        k = key[int(res["repr_row"][g])]
+        exact = float(np.median(d[key == k]))
+        assert abs(res["results"][g, 0] - exact) <= 0.05 * exact
+
+
+def test_tdigest_estimator_matches_the_oracle_on_fixed_centroids():
+    from computeql_gb300 import native
+    import ctypes as C
+    rng = np.random.default_rng(1)
+    m = rng.random(1000).astype(np.float32)
+    w = rng.integers(1, 20, 1000).astype(np.float32)
+    for f in (0.0, 0.01, 0.5, 0.77, 1.0):
+        a, b = m.copy(), w.copy()
+        got = native.load_ops().cqlops_tdigest_percentile(a.ctypes.data, b.ctypes.data, len(a), f)
+        assert got == oracle.tdigest_percentile(m, w, f)
+
+
+def test_small_table_grows_buckets_on_overflow(ops):
+    # 200k distinct keys in 400k rows: the first table (rows/64 buckets) overflows and is grown
+    n = 400_000
+    key = (np.arange(n) % 200_000).astype(np.uint32)
+    res = ops.group_hash([ops.Column.from_numpy(key)], [COUNT], [None])
+    assert res["groups"] == 200_000
+    assert np.all(res["counts"] == 2)
