@@ -40,6 +40,8 @@ const char* cqlops_last_error(void)
 void cqlops_note_error(const char* why)
 {
   snprintf(g_error, sizeof(g_error), "%s", why);
+  /* an operator starting afresh also drops the backend's text of an earlier failure */
+  if (!why[0]) cqlcuda_clear_error();
 }
 
 static int refuse(const char* why)
@@ -56,7 +58,7 @@ uint32_t cqlops_last_launches(void)
 static void launches_begin(void)
 {
   g_launch_mark = cqlcuda_kernel_launch_count();
-  g_error[0] = 0;
+  cqlops_note_error("");
 }
 
 static CqlKernel* kernel_named(const char* name)

@@ -27,6 +27,7 @@ def env(gpu):
     arrays["i"] = rng.integers(-1000, 1000, N).astype(np.int32)
     arrays["f"] = (rng.standard_normal(N) * 10).astype(np.float32)
     arrays["region"] = rng.integers(0, 50, N).astype(np.uint32)
+    arrays["status"] = rng.integers(0, 5, N).astype(np.uint32)
     words = ["alpha", "bravo", "charlie", "delta", "echo", "foxtrot", "golf", "hotel"]
     svals = [words[int(x)] + str(int(y)) for x, y in zip(rng.integers(0, 8, N), rng.integers(0, 5, N))]
     arrays["s"] = string_arrays(svals)
@@ -188,14 +189,16 @@ def test_fused_count_where_matches_scan(env):
 @pytest.mark.parametrize("where", ["", "(< u0 20000)", "(or (> d0 0.9) (= region 3))"])
 def test_fused_filter_group(env, where):
     ops, arrays, cols, svals = env
-    use = {"u0": cols["u0"], "d0": cols["d0"], "region": cols["region"], "i": cols["i"], "sd": cols["sd"], "u1": cols["u1"]}
+    use = {"u0": cols["u0"], "d0": cols["d0"], "region": cols["region"], "i": cols["i"], "sd": cols["sd"], "u1": cols["u1"],
+           "status": cols["status"]}
     p = ops.Program(where, use)
     mask = oracle_mask(p, arrays).astype(bool) if where else np.ones(N, dtype=bool)
-    res = ops.fused_group(p, ["region", "sd"], ["u1", "i"])
+    # 5 x 40 groups x (2 + 4 x 2) words: inside the reference's 4096-word table
+    res = ops.fused_group(p, ["status", "sd"], ["u1", "i"])
     codes = cols["sd"].codes
     ndict = int(codes.max()) + 1
-    assert res["key_range"] == [50, ndict]
-    g = arrays["region"].astype(np.int64) * ndict + codes
+    assert res["key_range"] == [5, ndict]
+    g = arrays["status"].astype(np.int64) * ndict + codes
     for gi in range(res["groups"]):
         sel = mask & (g == gi)
         assert res["counts"][gi] == sel.sum()
