@@ -19,6 +19,7 @@
 #include "cql_internal.cuh"
 #include <algorithm>
 #include <float.h>
+#include <string.h>
 
 #define HASH_THREADS 256
 #define EMPTY_SLOT 0xffffffffu
@@ -245,6 +246,77 @@ static int launch_aggregate_compact(const CqlLaunch& a, uint32_t gws, uint32_t l
   else k_aggregate_compact<<<cql_stream_grid(blocks ? blocks : 1, 8), HASH_THREADS, 0, stream>>>(a, mode, n);
   CQL_LAUNCH_CHECK();
   return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Slot compaction that allocates nothing.
+//
+// Some callers cannot allocate device memory while they run a query. One example is a serving loop
+// that reserves all of HBM ahead of time: it gives most of it to resident tables and sets aside a
+// fixed budget for each admitted query. There, a cudaMalloc on the query path can fail, or can force
+// an eviction halfway through a query. For those callers, this entry point runs the same three
+// aggregate_compact passes with the block totals (the kernel's only scratch) in a static device
+// array. Every GPU that loads this library holds that array until the process exits.
+//
+// Limit: CQL_NOALLOC_COMPACT_MAX_SLOTS slots (2^24, i.e. 65536 blocks of 256; 256 KB of scratch).
+// The first call on a device looks up the array's device address with cudaGetSymbolAddress, with
+// that device current, and keeps it for later calls. Make that first call before any stream capture.
+// All calls share the array. Calls whose work overlaps on the GPU race on it: serialise them, for
+// example by issuing them on one stream. Nothing in the array has to start at zero: every block
+// total is written before it is read, and so is the group total.
+
+#define CQL_NOALLOC_COMPACT_MAX_SLOTS (1u << 24)
+#define CQL_NOALLOC_COMPACT_BLOCKS (CQL_NOALLOC_COMPACT_MAX_SLOTS / 256u)
+#define CQL_NOALLOC_MAX_DEVICES 64
+
+static __device__ __align__(256) uint32_t g_noalloc_compact_scratch[CQL_NOALLOC_COMPACT_BLOCKS + 64];
+
+static uint32_t* g_noalloc_scratch_ptr[CQL_NOALLOC_MAX_DEVICES];
+
+extern "C" int cqlcuda_compact_slots_noalloc(const uint32_t* slot_counts, const uint32_t* slot_owner, uint32_t slot_count,
+                                             uint32_t* slot_group, uint32_t* group_owner, uint32_t* group_count, uint32_t* out_group_total,
+                                             void* stream)
+{
+  if (slot_count == 0 || slot_count > CQL_NOALLOC_COMPACT_MAX_SLOTS) return -1;
+  if (!slot_counts || !slot_owner || !slot_group || !group_owner || !group_count || !out_group_total) return -2;
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= CQL_NOALLOC_MAX_DEVICES) return -3;
+  if (!g_noalloc_scratch_ptr[device])
+  {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_compact_scratch) != cudaSuccess || !p) return -3;
+    g_noalloc_scratch_ptr[device] = (uint32_t*)p;
+  }
+  uint32_t* scratch = g_noalloc_scratch_ptr[device];
+  cudaStream_t s = (cudaStream_t)stream;
+  CqlLaunch a;
+  memset(&a, 0, sizeof(a));
+  uint32_t blocks = (slot_count + 255u) / 256u;
+  a.buf[0] = (void*)slot_counts;
+  a.bytes[0] = (uint64_t)slot_count * 4;
+  a.buf[1] = (void*)slot_owner;
+  a.bytes[1] = (uint64_t)slot_count * 4;
+  a.buf[2] = slot_group;
+  a.bytes[2] = ((uint64_t)slot_count + 1) * 4;
+  a.buf[3] = scratch;                                  // block totals
+  a.bytes[3] = (uint64_t)blocks * 4;
+  a.buf[4] = group_owner;
+  a.bytes[4] = (uint64_t)slot_count * 4;
+  a.buf[5] = group_count;
+  a.bytes[5] = (uint64_t)slot_count * 4;
+  a.buf[6] = scratch + CQL_NOALLOC_COMPACT_BLOCKS;     // group total
+  a.bytes[6] = 4;
+  a.push[0] = slot_count;
+  for (uint32_t mode = 0; mode < 3; mode++)
+  {
+    a.push[1] = mode;
+    if (mode == 1) k_aggregate_compact<<<1, HASH_THREADS, 0, s>>>(a, mode, slot_count);
+    else k_aggregate_compact<<<cql_stream_grid(blocks, 8), HASH_THREADS, 0, s>>>(a, mode, slot_count);
+    if (cudaGetLastError() != cudaSuccess) return -4;
+  }
+  if (cudaMemcpyAsync(out_group_total, scratch + CQL_NOALLOC_COMPACT_BLOCKS, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return -4;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return -4;
+  return 1;
 }
 
 // ---------------------------------------------------------------------------------------------

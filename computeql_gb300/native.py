@@ -119,6 +119,7 @@ CUDA_API = [
     ("cqlcuda_set_fail_compile_every", None, [u32]),
     ("cqlcuda_last_compile_log", cstr, []),
     ("cqlcuda_compile_check", C.c_int, [cstr, u64]),
+    ("cqlcuda_compact_slots_noalloc", C.c_int, [P, P, u32, P, P, P, P, P]),
     ("cqlcuda_fill_splitmix_u32", C.c_int, [P, u64, u64, u32, u32, u64]),
     ("cqlcuda_fill_sequence_u32", C.c_int, [P, u64, u32]),
     ("cqlcuda_flush_l2", C.c_int, [u64]),

@@ -166,6 +166,25 @@ const char* cqlcuda_last_compile_log(void);
    compiles. The log goes to cqlcuda_last_compile_log(). */
 int      cqlcuda_compile_check(const char* source, uint64_t source_len);
 
+/* ---- slot compaction without allocation (no counterpart in the reference) ----
+   For callers that cannot allocate device memory while they run a query, e.g. a serving loop that
+   reserves all of HBM ahead of time for resident tables and per-query budgets, where a cudaMalloc on
+   the query path can fail or force an eviction mid-query. It runs the three aggregate_compact passes
+   over caller-owned device buffers and keeps the kernel's scratch (the block totals) in a static
+   device array, so it calls no cudaMalloc, cudaFree or allocating library routine.
+   Inputs: slot_counts/slot_owner, slot_count entries each. Outputs: slot_group (slot_count + 1
+   entries: the dense group id of every occupied slot, the group total last), group_owner and
+   group_count (up to slot_count entries), and *out_group_total on the host.
+   Limit: slot_count <= 2^24 (256 KB of scratch, held by every GPU that loads the library until exit).
+   The first call on a device looks the scratch address up with that device current: make it
+   before any stream capture. All calls share the scratch; calls whose work overlaps on the GPU race.
+   `stream` is a cudaStream_t (NULL = the legacy default stream); the call returns once it is done.
+   Returns 1, or -1 slot_count is 0 or over the limit, -2 a NULL pointer, -3 no usable device,
+   -4 a launch or copy failed. */
+int      cqlcuda_compact_slots_noalloc(const uint32_t* slot_counts, const uint32_t* slot_owner, uint32_t slot_count,
+                                       uint32_t* slot_group, uint32_t* group_owner, uint32_t* group_count, uint32_t* out_group_total,
+                                       void* stream);
+
 /* ---- raw device helpers used by the bench and tests (not in the reference vtable) ---- */
 /* Fills `rows` rows of a u32 column from the splitmix64 stream seeded `seed`: row r takes draw
    r*draws_per_row + draw_index (0-based) and stores draw % range (range 0 = the full 32 bits). */
