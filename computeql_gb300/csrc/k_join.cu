@@ -1,6 +1,411 @@
-// Kernel family placeholder: filled in as the join kernels are built.
+// Hash joins.
+//
+//  hash_join_build_count  src/gpu/vulkan/shaders/hash_join_build_count.comp:1-81  bucket histogram of the build keys
+//  prefix_sum / _sum2     src/gpu/vulkan/shaders/prefix_sum.comp:1-103            exclusive scan in three modes, seeds the cursor
+//  hash_join_probe        src/gpu/vulkan/shaders/hash_join_probe.comp:1-137       probe rows emit (probe, build) pairs, LEFT JOIN unmatched
+//  join_pack_key          src/gpu/vulkan/shaders/join_pack_key.comp:1-52          two whole-number keys folded into one f64 key
+//  join_probe_native      src/gpu/vulkan/shaders/join_probe_native.comp:1-238     fact-side probe fused with per-dim-row aggregates
+//
+// Keys are f64 values (or raw strings) hashed from their bit patterns exactly as the reference does, so a
+// build row lands in the same bucket. GB300 design: persistent grid-stride launches; the fused probe keeps
+// eight keys and their Bloom words in flight per thread and bounds every open-addressing walk by the
+// table size (the reference's walk assumes an empty slot exists).
 #include "cql_internal.cuh"
+#include <algorithm>
+
+#define JOIN_THREADS 256
+#define BUILD_NULL 0xffffffffu
+
+__device__ __forceinline__ uint32_t jhash_u32(uint32_t x)
+{
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+__device__ __forceinline__ uint32_t num_hash(const uint32_t* data, uint64_t row)
+{
+  uint32_t lo = data[row * 2], hi = data[row * 2 + 1];
+  return jhash_u32(lo ^ jhash_u32(hi));
+}
+
+// ---------------------------------------------------------------------------------------------
+// hash_join_build_count: binding 0 build keys, 1 build offsets, 2 bucket counts, 3 bucket per row;
+// words 0 rows, 2 buckets, 4 string key
+
+__global__ void __launch_bounds__(JOIN_THREADS) k_join_build_count(CqlLaunch a, uint64_t rows)
+{
+  const uint32_t* data = (const uint32_t*)a.buf[0];
+  const uint32_t* off = (const uint32_t*)a.buf[1];
+  uint32_t* counts = (uint32_t*)a.buf[2];
+  uint32_t* row_bucket = (uint32_t*)a.buf[3];
+  uint32_t buckets = cql_word(a, 2);
+  bool is_str = cql_word(a, 4) != 0;
+  if (!buckets) return;
+  for (uint64_t row = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; row < rows; row += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint32_t h;
+    if (is_str)
+    {
+      uint32_t s = off[row * 2], e = off[(row + 1) * 2];
+      h = 2166136261u;
+      const unsigned char* b = (const unsigned char*)data;
+      for (uint32_t i = s; i < e; i++) h = (h ^ b[i]) * 16777619u;
+    }
+    else h = num_hash(data, row);
+    uint32_t bucket = h % buckets;
+    row_bucket[row] = bucket;
+    atomicAdd(&counts[bucket], 1u);
+  }
+}
+
+static int launch_join_build_count(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t rows = cql_word(a, 0);
+  if (rows == 0) return 0;
+  k_join_build_count<<<cql_stream_grid((rows + JOIN_THREADS - 1) / JOIN_THREADS, 8), JOIN_THREADS, 0, stream>>>(a, rows);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// prefix_sum: binding 0 counts, 1 offsets (n + 1), 2 cursor, 3 block totals; word 0 n, word 2 mode
+
+__device__ uint32_t join_block_scan(uint32_t v, uint32_t* sh, uint32_t* total)
+{
+  uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= (uint32_t)o) incl += y;
+  }
+  if (lane == 31) sh[warp] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    uint32_t run = 0;
+    for (int w = 0; w < JOIN_THREADS / 32; w++)
+    {
+      uint32_t t = sh[w];
+      sh[w] = run;
+      run += t;
+    }
+    sh[JOIN_THREADS / 32] = run;
+  }
+  __syncthreads();
+  uint32_t ex = sh[warp] + incl - v;
+  *total = sh[JOIN_THREADS / 32];
+  __syncthreads();
+  return ex;
+}
+
+__global__ void __launch_bounds__(JOIN_THREADS) k_prefix_sum(CqlLaunch a, uint32_t mode, uint32_t n)
+{
+  __shared__ uint32_t sh[JOIN_THREADS / 32 + 1];
+  const uint32_t* counts = (const uint32_t*)a.buf[0];
+  uint32_t* offsets = (uint32_t*)a.buf[1];
+  uint32_t* cursor = (uint32_t*)a.buf[2];
+  uint32_t* block_sums = (uint32_t*)a.buf[3];
+  uint32_t blocks = (n + 255) / 256;
+  uint32_t total;
+  if (mode == 0)
+  {
+    for (uint32_t b = blockIdx.x; b < blocks; b += gridDim.x)
+    {
+      uint32_t index = b * 256 + threadIdx.x;
+      uint32_t v = index < n ? counts[index] : 0u;
+      uint32_t ex = join_block_scan(v, sh, &total);
+      if (index < n) offsets[index] = ex;
+      if (threadIdx.x == 0) block_sums[b] = total;
+    }
+  }
+  else if (mode == 1)
+  {
+    if (blockIdx.x != 0) return;
+    uint32_t chunk = (blocks + 255) / 256;
+    uint32_t start = min(threadIdx.x * chunk, blocks), end = min(start + chunk, blocks);
+    uint32_t sum = 0;
+    for (uint32_t i = start; i < end; i++) sum += block_sums[i];
+    uint32_t running = join_block_scan(sum, sh, &total);
+    for (uint32_t i = start; i < end; i++)
+    {
+      uint32_t t = block_sums[i];
+      block_sums[i] = running;
+      running += t;
+    }
+    if (threadIdx.x == 0) offsets[n] = total;
+  }
+  else
+  {
+    for (uint64_t index = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; index < n; index += (uint64_t)gridDim.x * blockDim.x)
+    {
+      uint32_t t = offsets[index] + block_sums[index / 256];
+      offsets[index] = t;
+      cursor[index] = t;
+    }
+  }
+}
+
+static int launch_prefix_sum(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint32_t n = cql_word(a, 0), mode = cql_word(a, 2);
+  uint32_t blocks = (n + 255) / 256;
+  if (mode == 1) k_prefix_sum<<<1, JOIN_THREADS, 0, stream>>>(a, mode, n);
+  else k_prefix_sum<<<cql_stream_grid(blocks ? blocks : 1, 8), JOIN_THREADS, 0, stream>>>(a, mode, n);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// hash_join_probe: binding 0/1 build keys + offsets, 2 bucket offsets (buckets + 1), 3 bucket rows,
+// 4/5 probe keys + offsets, 6 pairs (probe, 0, build, 0) x capacity, 7 pair count;
+// words 0 probe rows, 2 buckets, 4 left join, 6 string key, 8 capacity
+
+__device__ bool str_equal(const uint32_t* bd, const uint32_t* bo, uint64_t brow, const uint32_t* pd, const uint32_t* po, uint64_t prow)
+{
+  uint32_t bs = bo[brow * 2], be = bo[(brow + 1) * 2], ps = po[prow * 2], pe = po[(prow + 1) * 2];
+  if (be - bs != pe - ps) return false;
+  const unsigned char* b = (const unsigned char*)bd;
+  const unsigned char* p = (const unsigned char*)pd;
+  for (uint32_t i = 0; i < be - bs; i++)
+    if (b[bs + i] != p[ps + i]) return false;
+  return true;
+}
+
+__global__ void __launch_bounds__(JOIN_THREADS) k_join_probe(CqlLaunch a, uint64_t probe_rows)
+{
+  const uint32_t* bd = (const uint32_t*)a.buf[0];
+  const uint32_t* bo = (const uint32_t*)a.buf[1];
+  const uint32_t* bucket_off = (const uint32_t*)a.buf[2];
+  const uint32_t* bucket_rows = (const uint32_t*)a.buf[3];
+  const uint32_t* pd = (const uint32_t*)a.buf[4];
+  const uint32_t* po = (const uint32_t*)a.buf[5];
+  uint32_t* pairs = (uint32_t*)a.buf[6];
+  uint32_t* count = (uint32_t*)a.buf[7];
+  uint32_t buckets = cql_word(a, 2), capacity = cql_word(a, 8);
+  bool left = cql_word(a, 4) != 0, is_str = cql_word(a, 6) != 0;
+  uint64_t cap_words = a.bytes[6] / 16;
+  if (cap_words < capacity) capacity = (uint32_t)cap_words;
+  if (!buckets) return;
+  for (uint64_t row = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; row < probe_rows; row += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint32_t h;
+    if (is_str)
+    {
+      uint32_t s = po[row * 2], e = po[(row + 1) * 2];
+      h = 2166136261u;
+      const unsigned char* b = (const unsigned char*)pd;
+      for (uint32_t i = s; i < e; i++) h = (h ^ b[i]) * 16777619u;
+    }
+    else h = num_hash(pd, row);
+    uint32_t bucket = h % buckets;
+    uint32_t start = bucket_off[bucket], end = bucket_off[bucket + 1];
+    bool found = false;
+    double pv = is_str ? 0.0 : __hiloint2double((int)pd[row * 2 + 1], (int)pd[row * 2]);
+    for (uint32_t m = start; m < end; m++)
+    {
+      uint32_t brow = bucket_rows[m];
+      bool eq = is_str ? str_equal(bd, bo, brow, pd, po, row) : (__hiloint2double((int)bd[brow * 2 + 1], (int)bd[brow * 2]) == pv);
+      if (eq)
+      {
+        found = true;
+        uint32_t pos = atomicAdd(count, 1u);
+        if (pos < capacity) *(uint4*)(pairs + (uint64_t)pos * 4) = make_uint4((uint32_t)row, 0u, brow, 0u);
+      }
+    }
+    if (!found && left)
+    {
+      uint32_t pos = atomicAdd(count, 1u);
+      if (pos < capacity) *(uint4*)(pairs + (uint64_t)pos * 4) = make_uint4((uint32_t)row, 0u, BUILD_NULL, BUILD_NULL);
+    }
+  }
+}
+
+static int launch_join_probe(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t rows = cql_word(a, 0);
+  if (rows == 0) return 0;
+  k_join_probe<<<cql_stream_grid((rows + JOIN_THREADS - 1) / JOIN_THREADS, 8), JOIN_THREADS, 0, stream>>>(a, rows);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// join_pack_key: binding 0/1 the two f64 keys, 2 the packed f64 key; word 0 count, slots 1-4 the
+// f64 min of each key and their spans (from the build side)
+
+__global__ void __launch_bounds__(JOIN_THREADS) k_join_pack_key(CqlLaunch a, uint64_t count)
+{
+  const double* first = (const double*)a.buf[0];
+  const double* second = (const double*)a.buf[1];
+  double* dest = (double*)a.buf[2];
+  double min_first = __longlong_as_double((long long)a.push[1]), min_second = __longlong_as_double((long long)a.push[2]);
+  double span_first = __longlong_as_double((long long)a.push[3]), span_second = __longlong_as_double((long long)a.push[4]);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x)
+  {
+    double x = first[i] - min_first, y = second[i] - min_second;
+    double key = -1.0;
+    if (x >= 0.0 && x < span_first && y >= 0.0 && y < span_second) key = x * span_second + y;
+    dest[i] = key;
+  }
+}
+
+static int launch_join_pack_key(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t count = cql_word(a, 0);
+  if (count == 0) return 0;
+  k_join_pack_key<<<cql_stream_grid((count + JOIN_THREADS - 1) / JOIN_THREADS, 8), JOIN_THREADS, 0, stream>>>(a, count);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// join_probe_native: binding 0 fact key, 1..4 arguments, 5 table keys, 6 table row + 1 (0 empty),
+// 7 counts per dim row, 8 sums (lo, hi), 9 mins, 10 maxs, 11 Bloom words.
+// word 0 rows, 1 widths (key bits 0-3, arg a bits 4+4a), 2 exprs, 3 base of arg 0, 4 funcs, 5 base of
+// arg 1, 6 arg index per expr, 7 signed bits, 8 table mask, 9 base of arg 2, 10 key base, 11 base of
+// arg 3, 12 log2 table size, 13 log2 Bloom words
+
+#define JFUNC_COUNT 0u
+#define JFUNC_SUM 1u
+#define JFUNC_AVG 2u
+#define JFUNC_MIN 3u
+#define JFUNC_MAX 4u
+
+struct JoinDecode
+{
+  const uint32_t* col[5];
+  uint32_t log2w[5], bits[5], mask[5], base[5];
+};
+
+__device__ __forceinline__ uint32_t join_read(const JoinDecode& d, int c, uint64_t row)
+{
+  uint32_t l = d.log2w[c];
+  uint32_t w = d.col[c][row >> l];
+  uint32_t sh = (uint32_t)((row & ((1u << l) - 1u)) * d.bits[c]) & 31u;
+  return d.base[c] + ((w >> sh) & d.mask[c]);
+}
+
+__global__ void __launch_bounds__(JOIN_THREADS) k_join_probe_native(CqlLaunch a, uint64_t rows)
+{
+  JoinDecode d;
+  uint32_t widths = cql_word(a, 1);
+  uint32_t arg_base[4] = { cql_word(a, 3), cql_word(a, 5), cql_word(a, 9), cql_word(a, 11) };
+#pragma unroll
+  for (int c = 0; c < 5; c++)
+  {
+    uint32_t w = (widths >> (4 * c)) & 0xfu;
+    d.col[c] = (const uint32_t*)a.buf[c];
+    d.log2w[c] = w == 1 ? 2 : (w == 2 ? 1 : 0);
+    d.bits[c] = w == 1 ? 8 : (w == 2 ? 16 : 32);
+    d.mask[c] = w == 1 ? 0xffu : (w == 2 ? 0xffffu : 0xffffffffu);
+    d.base[c] = (w == 1 || w == 2) ? (c == 0 ? cql_word(a, 10) : arg_base[c - 1]) : 0u;
+  }
+  const uint32_t* tkeys = (const uint32_t*)a.buf[5];
+  const uint32_t* trows = (const uint32_t*)a.buf[6];
+  uint32_t* counts = (uint32_t*)a.buf[7];
+  unsigned long long* sums = (unsigned long long*)a.buf[8];
+  int* mins = (int*)a.buf[9];
+  int* maxs = (int*)a.buf[10];
+  const uint32_t* bloom = (const uint32_t*)a.buf[11];
+  uint32_t exprs = min(cql_word(a, 2), 8u), funcs = cql_word(a, 4), arg_index = cql_word(a, 6), arg_signed = cql_word(a, 7);
+  uint32_t mask = cql_word(a, 8), log2_size = cql_word(a, 12), bloom_log2 = cql_word(a, 13);
+  uint32_t table_size = mask + 1;
+  uint64_t count_cap = a.bytes[7] / 4;
+  const uint32_t UNROLL = 8;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; base < rows; base += stride * UNROLL)
+  {
+    uint32_t key[UNROLL];
+    bool maybe[UNROLL];
+#pragma unroll
+    for (uint32_t u = 0; u < UNROLL; u++)
+    {
+      uint64_t at = base + u * stride;
+      key[u] = at < rows ? join_read(d, 0, at) : 0u;
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < UNROLL; u++)
+    {
+      uint64_t at = base + u * stride;
+      uint32_t h = key[u] * 0x9E3779B1u, h2 = key[u] * 0x85EBCA6Bu;
+      uint32_t bits = (1u << ((h2 >> 27) & 31u)) | (1u << ((h2 >> 22) & 31u));
+      maybe[u] = at < rows && (bloom[h >> (32u - bloom_log2)] & bits) == bits;
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < UNROLL; u++)
+    {
+      if (!maybe[u]) continue;
+      uint64_t row = base + u * stride;
+      uint32_t slot = (key[u] * 0x9E3779B1u) >> (32u - log2_size);
+      uint32_t found = 0;
+      for (uint32_t probe = 0; probe < table_size; probe++)
+      {
+        uint32_t r1 = trows[slot];
+        if (r1 == 0u) break;
+        if (tkeys[slot] == key[u])
+        {
+          found = r1;
+          break;
+        }
+        slot = (slot + 1u) & mask;
+      }
+      if (!found) continue;
+      uint32_t dim_row = found - 1u;
+      if (dim_row >= count_cap) continue;
+      atomicAdd(&counts[dim_row], 1u);
+      for (uint32_t e = 0; e < exprs; e++)
+      {
+        uint32_t f = (funcs >> (e * 4)) & 0xfu;
+        if (f == JFUNC_COUNT) continue;
+        uint32_t ai = (arg_index >> (e * 4)) & 0x3u;
+        uint32_t w = join_read(d, 1 + (int)ai, row);
+        uint64_t index = (uint64_t)dim_row * exprs + e;
+        if (f == JFUNC_SUM || f == JFUNC_AVG)
+        {
+          bool sg = ((arg_signed >> ai) & 1u) != 0;
+          atomicAdd(&sums[index], sg ? (unsigned long long)(long long)(int)w : (unsigned long long)w);
+        }
+        else if (f == JFUNC_MIN) atomicMin(&mins[index], (int)w);
+        else if (f == JFUNC_MAX) atomicMax(&maxs[index], (int)w);
+      }
+    }
+  }
+}
+
+static int launch_join_probe_native(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t rows = cql_word(a, 0);
+  uint32_t log2_size = cql_word(a, 12), bloom_log2 = cql_word(a, 13);
+  if (rows == 0) return 0;
+  if (log2_size == 0 || log2_size > 31 || bloom_log2 == 0 || bloom_log2 > 31) return (int)cudaErrorInvalidValue;
+  if ((uint64_t)(cql_word(a, 8)) + 1 != (1ull << log2_size)) return (int)cudaErrorInvalidValue;
+  k_join_probe_native<<<cql_stream_grid((rows + JOIN_THREADS * 8 - 1) / (JOIN_THREADS * 8), 8), JOIN_THREADS, 0, stream>>>(a, rows);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
 
 const CqlKernelDesc cql_kernels_join[] = {
+  { "hash_join_build_count", launch_join_build_count },
+  { "prefix_sum", launch_prefix_sum },
+  { "prefix_sum2", launch_prefix_sum },
+  { "hash_join_probe", launch_join_probe },
+  { "join_pack_key", launch_join_pack_key },
+  { "join_probe_native", launch_join_probe_native },
   { nullptr, nullptr },
 };

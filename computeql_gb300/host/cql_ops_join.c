@@ -1,0 +1,529 @@
+/*
+ * cql_ops_join.c - hash joins and the join-aggregate pushdown, driven through the cqlcuda C ABI.
+ *
+ *  cqlops_hash_join       qe_hash_join_impl (src/query_exec/query_exec.c:14541-15358): build-side bucket
+ *                         histogram, three-pass prefix sum, scatter into bucket lists, probe emitting
+ *                         (probe row, build row) pairs, LEFT JOIN unmatched rows, output capacity
+ *                         max(probe, build) + probe (qe_join_output_capacity :14368-14381) grown once
+ *  cqlops_join_aggregate  qe_aggregate_join_pushdown (:8442-8776): the fact table reduced to totals per
+ *                         join key - densely when the fact key's range is small (qe_dense_stream_core),
+ *                         else by probing a CPU-built linear-probing table of the dim keys behind a Bloom
+ *                         filter (qe_join_probe_stream_core :8080-8420) - then every (filtered) dim row
+ *                         meets its key's totals and is folded into a group of its group columns on the host
+ */
+#include "cqlops.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define QE_GPU_WORKGROUP_SIZE 256
+#define PROBE_STREAM_MAX_DIM_ROWS (1ull << 26)
+
+void cqlops_note_error(const char* why);
+
+static int refuse(const char* why)
+{
+  cqlops_note_error(why);
+  return 0;
+}
+
+static CqlBuffer* pooled(const char* name, uint64_t size, uint32_t flags)
+{
+  return cqlcuda_buffer_alloc_pooled(name, (uint64_t)strlen(name), size ? size : 4, flags, NULL);
+}
+
+static CqlKernel* kernel(const char* name)
+{
+  return cqlcuda_kernel_alloc(name, (uint64_t)strlen(name));
+}
+
+/* a join key as the join kernels read it: f64 values (widened on the device) or raw strings */
+static int join_key(const CqlColumn* col, const char* name, CqlBuffer** data, CqlBuffer** off, int* is_str)
+{
+  if (col->type == CQLOPS_TYPE_STRING8)
+  {
+    if (!col->offsets || col->dict) return refuse("a string join key is read as raw bytes and offsets");
+    *data = col->buffer;
+    *off = col->offsets;
+    *is_str = 1;
+    return 1;
+  }
+  if (col->width != 0 || !col->buffer) return refuse("a join key must be stored at full width");
+  CqlBuffer* out = pooled(name, col->rows * 8, CQLCUDA_BUFFER_READ_WRITE);
+  CqlKernel* k = kernel("cql_widen_f64");
+  if (!out || !k) return 0;
+  cqlcuda_kernel_set_arg_buffer(k, 0, col->buffer);
+  cqlcuda_kernel_set_arg_buffer(k, 1, out);
+  cqlcuda_kernel_set_arg_u64(k, 0, col->rows);
+  cqlcuda_kernel_set_arg_u64(k, 1, col->type);
+  CqlBatch* b = cqlcuda_batch_begin(0, 0);
+  cqlcuda_batch_kernel_execute(b, k, (uint32_t)col->rows, QE_GPU_WORKGROUP_SIZE);
+  if (!cqlcuda_batch_end(b)) return 0;
+  *data = out;
+  *off = out;
+  *is_str = 0;
+  return 1;
+}
+
+static int pair_cmp(const void* a, const void* b)
+{
+  const uint32_t* x = (const uint32_t*)a;
+  const uint32_t* y = (const uint32_t*)b;
+  if (x[0] != y[0]) return x[0] < y[0] ? -1 : 1;
+  if (x[1] != y[1]) return x[1] < y[1] ? -1 : 1;
+  return 0;
+}
+
+int cqlops_hash_join(const CqlColumn* build_key, const CqlColumn* probe_key, int left_join, uint64_t hint_pairs, uint64_t* out_count,
+                     uint32_t* out_pairs, uint64_t out_capacity)
+{
+  cqlops_note_error("");
+  uint64_t brows = build_key->rows, prows = probe_key->rows;
+  if (brows >= 0xffffffffull || prows >= 0xffffffffull) return refuse("row count out of range");
+  CqlBuffer *bd, *bo, *pd, *po;
+  int bstr, pstr;
+  if (!join_key(build_key, "hj_build_f64", &bd, &bo, &bstr) || !join_key(probe_key, "hj_probe_f64", &pd, &po, &pstr)) return 0;
+  if (bstr != pstr) return refuse("the two join keys must both be strings or both numeric");
+  uint64_t buckets = 1;
+  while (buckets < brows) buckets <<= 1;
+  uint64_t blocks = (buckets + 255) / 256;
+  CqlBuffer* counts = pooled("hj_bucket_count_buf", buckets * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* row_bucket = pooled("hj_row_bucket_buf", (brows ? brows : 1) * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* offsets = pooled("hj_bucket_offsets_buf", (buckets + 1) * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* cursor = pooled("hj_cursor_buf", buckets * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* block_sums = pooled("hj_block_sum_buf", blocks * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* bucket_rows = pooled("hj_bucket_rows_buf", (brows ? brows : 1) * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* pair_count = pooled("hj_out_count_buf", 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlKernel* build = kernel("hash_join_build_count");
+  CqlKernel* scan = kernel("prefix_sum");
+  CqlKernel* scatter = kernel("csr_scatter");
+  CqlKernel* probe = kernel("hash_join_probe");
+  if (!counts || !row_bucket || !offsets || !cursor || !block_sums || !bucket_rows || !pair_count || !build || !scan || !scatter || !probe) return 0;
+  cqlcuda_kernel_set_arg_buffer(build, 0, bd);
+  cqlcuda_kernel_set_arg_buffer(build, 1, bo);
+  cqlcuda_kernel_set_arg_buffer(build, 2, counts);
+  cqlcuda_kernel_set_arg_buffer(build, 3, row_bucket);
+  cqlcuda_kernel_set_arg_u64(build, 0, brows);
+  cqlcuda_kernel_set_arg_u64(build, 1, buckets);
+  cqlcuda_kernel_set_arg_u64(build, 2, (uint64_t)bstr);
+  cqlcuda_kernel_set_arg_buffer(scan, 0, counts);
+  cqlcuda_kernel_set_arg_buffer(scan, 1, offsets);
+  cqlcuda_kernel_set_arg_buffer(scan, 2, cursor);
+  cqlcuda_kernel_set_arg_buffer(scan, 3, block_sums);
+  cqlcuda_kernel_set_arg_u64(scan, 0, buckets);
+  cqlcuda_kernel_set_arg_buffer(scatter, 0, row_bucket);
+  cqlcuda_kernel_set_arg_buffer(scatter, 1, cursor);
+  cqlcuda_kernel_set_arg_buffer(scatter, 2, bucket_rows);
+  cqlcuda_kernel_set_arg_u64(scatter, 0, brows);
+  {
+    CqlBatch* b = cqlcuda_batch_begin(0, 0);
+    cqlcuda_batch_buffer_zero(b, counts, buckets * 4);
+    cqlcuda_batch_kernel_execute(b, build, (uint32_t)brows, QE_GPU_WORKGROUP_SIZE);
+    for (uint32_t mode = 0; mode < 3; mode++)
+    {
+      cqlcuda_kernel_set_arg_u64(scan, 1, mode);
+      cqlcuda_batch_kernel_execute(b, scan, mode == 1 ? 256u : (uint32_t)(blocks * 256), 256);
+    }
+    cqlcuda_batch_kernel_execute(b, scatter, (uint32_t)brows, QE_GPU_WORKGROUP_SIZE);
+    if (!cqlcuda_batch_end(b)) return 0;
+  }
+  uint64_t capacity = (prows > brows ? prows : brows) + prows;
+  if (hint_pairs > 0)
+  {
+    uint64_t hinted = hint_pairs + hint_pairs / 4 + 16;
+    if (hinted > capacity) capacity = hinted;
+  }
+  if (capacity > 0xffffffffull) capacity = 0xffffffffull;
+  if (capacity < 1) capacity = 1;
+  uint32_t produced = 0;
+  CqlBuffer* pairs = NULL;
+  for (int attempt = 0; attempt < 2; attempt++)
+  {
+    pairs = pooled("hj_out_pairs_buf", capacity * 16, CQLCUDA_BUFFER_READ_WRITE);
+    if (!pairs) return 0;
+    cqlcuda_kernel_set_arg_buffer(probe, 0, bd);
+    cqlcuda_kernel_set_arg_buffer(probe, 1, bo);
+    cqlcuda_kernel_set_arg_buffer(probe, 2, offsets);
+    cqlcuda_kernel_set_arg_buffer(probe, 3, bucket_rows);
+    cqlcuda_kernel_set_arg_buffer(probe, 4, pd);
+    cqlcuda_kernel_set_arg_buffer(probe, 5, po);
+    cqlcuda_kernel_set_arg_buffer(probe, 6, pairs);
+    cqlcuda_kernel_set_arg_buffer(probe, 7, pair_count);
+    cqlcuda_kernel_set_arg_u64(probe, 0, prows);
+    cqlcuda_kernel_set_arg_u64(probe, 1, buckets);
+    cqlcuda_kernel_set_arg_u64(probe, 2, (uint64_t)(left_join != 0));
+    cqlcuda_kernel_set_arg_u64(probe, 3, (uint64_t)pstr);
+    cqlcuda_kernel_set_arg_u64(probe, 4, capacity);
+    CqlBatch* b = cqlcuda_batch_begin(0, 4);
+    cqlcuda_batch_buffer_zero(b, pair_count, 4);
+    cqlcuda_batch_kernel_execute(b, probe, (uint32_t)prows, QE_GPU_WORKGROUP_SIZE);
+    cqlcuda_batch_buffer_read(b, pair_count, &produced, 4);
+    if (!cqlcuda_batch_end(b)) return 0;
+    if (produced <= capacity) break;
+    capacity = produced;
+  }
+  if (produced > capacity) return refuse("the join produced more pairs than its output could hold");
+  if (out_pairs && produced)
+  {
+    uint32_t* raw = (uint32_t*)malloc((uint64_t)produced * 16);
+    if (!raw) return 0;
+    cqlcuda_buffer_read(pairs, raw, (uint64_t)produced * 16);
+    for (uint64_t i = 0; i < produced; i++)
+    {
+      raw[i * 2] = raw[i * 4];
+      raw[i * 2 + 1] = raw[i * 4 + 2];
+    }
+    qsort(raw, produced, 8, pair_cmp);
+    uint64_t n = produced < out_capacity ? produced : out_capacity;
+    memcpy(out_pairs, raw, n * 8);
+    free(raw);
+  }
+  *out_count = produced;
+  return 1;
+}
+
+int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* arg_cols,
+                       uint64_t max_groups, uint64_t* out_group_count, int64_t* out_min_key, uint64_t* out_counts, int64_t* out_sums,
+                       int64_t* out_mins, int64_t* out_maxs);
+
+/* totals per dim row by probing a table of the dim keys (qe_join_probe_stream_core) */
+static int probe_totals(const CqlJoinAgg* q, uint32_t core_count, const uint32_t* core_funcs, const CqlColumn* const* core_cols,
+                        uint64_t* counts, int64_t* sums, int64_t* mins, int64_t* maxs)
+{
+  const CqlColumn* fk = q->fact_key;
+  uint64_t rows = fk->rows;
+  uint64_t table_rows = q->dim_rows ? q->dim_count : q->dim_table_rows;
+  if (q->dim_table_rows == 0 || q->dim_table_rows > PROBE_STREAM_MAX_DIM_ROWS) return refuse("dim table size out of range");
+  const CqlColumn* arg_columns[4] = { 0 };
+  uint32_t arg_count = 0, func_codes = 0, arg_index_codes = 0, arg_signed_bits = 0;
+  for (uint32_t e = 0; e < core_count; e++)
+  {
+    func_codes |= (core_funcs[e] & 0xfu) << (4 * e);
+    if (core_funcs[e] == CQLOPS_FUNC_COUNT) continue;
+    const CqlColumn* c = core_cols[e];
+    if (!c || !(c->type == CQLOPS_TYPE_U32 || c->type == CQLOPS_TYPE_I32) || c->rows != rows || c->width == 3)
+      return refuse("probe aggregates take U32/I32 fact columns");
+    if ((core_funcs[e] == CQLOPS_FUNC_MIN || core_funcs[e] == CQLOPS_FUNC_MAX) &&
+        (!c->has_range || c->zone_min < -2147483648.0 || c->zone_max > 2147483647.0))
+      return refuse("MIN/MAX values must fit a signed 32-bit word");
+    uint32_t idx = 0;
+    while (idx < arg_count && arg_columns[idx] != c) idx++;
+    if (idx == arg_count)
+    {
+      if (arg_count == 4) return refuse("at most 4 argument columns");
+      arg_columns[arg_count++] = c;
+    }
+    arg_index_codes |= (idx & 0xfu) << (4 * e);
+    if (c->type == CQLOPS_TYPE_I32) arg_signed_bits |= 1u << idx;
+  }
+  /* the table: twice the keys, a power of two; a duplicate dim key refuses, as the reference does */
+  uint32_t log2_size = 4;
+  while ((1ull << log2_size) < table_rows * 2) log2_size++;
+  uint64_t size = 1ull << log2_size;
+  uint32_t* tkeys = (uint32_t*)calloc(size, 4);
+  uint32_t* trows = (uint32_t*)calloc(size, 4);
+  uint32_t bloom_log2 = 4;
+  while ((1ull << bloom_log2) * 2 < table_rows) bloom_log2++;
+  uint32_t* bloom = (uint32_t*)calloc(1ull << bloom_log2, 4);
+  int ok = tkeys && trows && bloom;
+  for (uint64_t v = 0; ok && v < table_rows; v++)
+  {
+    uint64_t dim_row = q->dim_rows ? q->dim_rows[v] : v;
+    uint32_t key = q->dim_keys[dim_row];
+    uint64_t slot = (uint32_t)(key * 0x9E3779B1u) >> (32 - log2_size);
+    while (trows[slot] != 0)
+    {
+      if (tkeys[slot] == key)
+      {
+        ok = refuse("a dim key appears twice");
+        break;
+      }
+      slot = (slot + 1) & (size - 1);
+    }
+    if (!ok) break;
+    tkeys[slot] = key;
+    trows[slot] = (uint32_t)dim_row + 1;
+    uint32_t h = key * 0x9E3779B1u, h2 = key * 0x85EBCA6Bu;
+    bloom[h >> (32 - bloom_log2)] |= (1u << ((h2 >> 27) & 31)) | (1u << ((h2 >> 22) & 31));
+  }
+  uint64_t D = q->dim_table_rows;
+  CqlBuffer* kb = ok ? pooled("jp_table_keys", size * 4, CQLCUDA_BUFFER_WRITE) : NULL;
+  CqlBuffer* rb = ok ? pooled("jp_table_rows", size * 4, CQLCUDA_BUFFER_WRITE) : NULL;
+  CqlBuffer* bb = ok ? pooled("jp_bloom", (1ull << bloom_log2) * 4, CQLCUDA_BUFFER_WRITE) : NULL;
+  CqlBuffer* cb = ok ? pooled("jp_counts", D * 4, CQLCUDA_BUFFER_READ_WRITE) : NULL;
+  CqlBuffer* sb = ok ? pooled("jp_sums", D * core_count * 8, CQLCUDA_BUFFER_READ_WRITE) : NULL;
+  CqlBuffer* nb = ok ? pooled("jp_mins", D * core_count * 4, CQLCUDA_BUFFER_READ_WRITE) : NULL;
+  CqlBuffer* xb = ok ? pooled("jp_maxs", D * core_count * 4, CQLCUDA_BUFFER_READ_WRITE) : NULL;
+  CqlKernel* k = ok ? kernel("join_probe_native") : NULL;
+  uint32_t* hc = ok ? (uint32_t*)malloc(D * 4) : NULL;
+  uint32_t* hn = ok ? (uint32_t*)malloc(D * core_count * 4) : NULL;
+  uint32_t* hx = ok ? (uint32_t*)malloc(D * core_count * 4) : NULL;
+  ok = ok && kb && rb && bb && cb && sb && nb && xb && k && hc && hn && hx;
+  if (ok)
+  {
+    uint64_t widths = fk->width == 4 ? 0 : fk->width;
+    uint32_t bases[4] = { 0, 0, 0, 0 };
+    for (uint32_t i = 0; i < arg_count; i++)
+    {
+      widths |= (uint64_t)(arg_columns[i]->width == 4 ? 0 : arg_columns[i]->width) << (4 + 4 * i);
+      bases[i] = arg_columns[i]->base;
+    }
+    cqlcuda_kernel_set_arg_buffer(k, 0, fk->buffer);
+    for (uint32_t i = 0; i < 4; i++) cqlcuda_kernel_set_arg_buffer(k, 1 + i, i < arg_count ? arg_columns[i]->buffer : fk->buffer);
+    cqlcuda_kernel_set_arg_buffer(k, 5, kb);
+    cqlcuda_kernel_set_arg_buffer(k, 6, rb);
+    cqlcuda_kernel_set_arg_buffer(k, 7, cb);
+    cqlcuda_kernel_set_arg_buffer(k, 8, sb);
+    cqlcuda_kernel_set_arg_buffer(k, 9, nb);
+    cqlcuda_kernel_set_arg_buffer(k, 10, xb);
+    cqlcuda_kernel_set_arg_buffer(k, 11, bb);
+    cqlcuda_kernel_set_arg_u64(k, 0, rows | (widths << 32));
+    cqlcuda_kernel_set_arg_u64(k, 1, core_count | ((uint64_t)bases[0] << 32));
+    cqlcuda_kernel_set_arg_u64(k, 2, func_codes | ((uint64_t)bases[1] << 32));
+    cqlcuda_kernel_set_arg_u64(k, 3, arg_index_codes | ((uint64_t)arg_signed_bits << 32));
+    cqlcuda_kernel_set_arg_u64(k, 4, (size - 1) | ((uint64_t)bases[2] << 32));
+    cqlcuda_kernel_set_arg_u64(k, 5, (uint64_t)fk->base | ((uint64_t)bases[3] << 32));
+    cqlcuda_kernel_set_arg_u64(k, 6, log2_size | ((uint64_t)bloom_log2 << 32));
+    CqlBatch* b = cqlcuda_batch_begin(size * 8, D * (4 + core_count * 16));
+    cqlcuda_batch_buffer_write(b, kb, tkeys, size * 4);
+    cqlcuda_batch_buffer_write(b, rb, trows, size * 4);
+    cqlcuda_batch_buffer_write(b, bb, bloom, (1ull << bloom_log2) * 4);
+    cqlcuda_batch_buffer_zero(b, cb, D * 4);
+    cqlcuda_batch_buffer_zero(b, sb, D * core_count * 8);
+    cqlcuda_batch_buffer_fill(b, nb, D * core_count * 4, 0x7fffffffu);
+    cqlcuda_batch_buffer_fill(b, xb, D * core_count * 4, 0x80000000u);
+    cqlcuda_batch_kernel_execute(b, k, (uint32_t)((rows + 8191) / 8192 * 256), QE_GPU_WORKGROUP_SIZE);
+    cqlcuda_batch_buffer_read(b, cb, hc, D * 4);
+    cqlcuda_batch_buffer_read(b, sb, sums, D * core_count * 8);
+    cqlcuda_batch_buffer_read(b, nb, hn, D * core_count * 4);
+    cqlcuda_batch_buffer_read(b, xb, hx, D * core_count * 4);
+    ok = cqlcuda_batch_end(b);
+  }
+  if (ok)
+  {
+    for (uint64_t r = 0; r < D; r++)
+    {
+      counts[r] = hc[r];
+      for (uint32_t e = 0; e < core_count; e++)
+      {
+        mins[r * core_count + e] = (int32_t)hn[r * core_count + e];
+        maxs[r * core_count + e] = (int32_t)hx[r * core_count + e];
+      }
+    }
+  }
+  free(tkeys);
+  free(trows);
+  free(bloom);
+  free(hc);
+  free(hn);
+  free(hx);
+  return ok;
+}
+
+int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* out_groups, uint64_t* out_group_dim_row, double* out_results,
+                          uint32_t* out_strategy)
+{
+  cqlops_note_error("");
+  const CqlColumn* fk = q->fact_key;
+  if (!fk || !(fk->type == CQLOPS_TYPE_U32 || fk->type == CQLOPS_TYPE_I32) || !q->dim_keys || q->expr_count == 0 || q->expr_count > 8)
+    return refuse("a U32/I32 fact key, the dim keys and 1 to 8 aggregates");
+  /* the fact-side totals each expression needs: AVG is a SUM and the count (:8558-8583) */
+  uint32_t core_funcs[8];
+  const CqlColumn* core_cols[8];
+  uint32_t core_count = 0, core_of_expr[8];
+  for (uint32_t e = 0; e < q->expr_count; e++)
+  {
+    uint32_t f = q->funcs[e];
+    if (f > CQLOPS_FUNC_MAX) return refuse("unsupported aggregate function");
+    core_of_expr[e] = 0;
+    if (f == CQLOPS_FUNC_COUNT || (q->dim_args && q->dim_args[e])) continue;
+    uint32_t cf = f == CQLOPS_FUNC_AVG ? CQLOPS_FUNC_SUM : f;
+    const CqlColumn* col = q->fact_args[e];
+    uint32_t i = 0;
+    while (i < core_count && !(core_funcs[i] == cf && core_cols[i] == col)) i++;
+    if (i == core_count)
+    {
+      core_funcs[core_count] = cf;
+      core_cols[core_count] = col;
+      core_count++;
+    }
+    core_of_expr[e] = i;
+  }
+  if (core_count == 0)
+  {
+    core_funcs[0] = CQLOPS_FUNC_COUNT;
+    core_cols[0] = NULL;
+    core_count = 1;
+  }
+  uint64_t rows = fk->rows;
+  /* totals per key: dense over a small key range, else per dim row by probing (:8607-8617) */
+  uint64_t groups_cap = fk->has_range ? (uint64_t)(fk->zone_max - fk->zone_min) + 1 : 0;
+  int by_dim_row = 0;
+  uint64_t total_groups = 0;
+  int64_t min_key = 0;
+  uint64_t* counts = NULL;
+  int64_t *sums = NULL, *mins = NULL, *maxs = NULL;
+  int ok = 0;
+  if (q->strategy != 2 && fk->has_range && groups_cap <= 65536)
+  {
+    counts = (uint64_t*)malloc(groups_cap * 8);
+    sums = (int64_t*)malloc(groups_cap * core_count * 8);
+    mins = (int64_t*)malloc(groups_cap * core_count * 8);
+    maxs = (int64_t*)malloc(groups_cap * core_count * 8);
+    ok = counts && sums && mins && maxs &&
+         cqlops_group_dense(fk, rows, core_count, core_funcs, core_cols, groups_cap, &total_groups, &min_key, counts, sums, mins, maxs);
+    if (!ok)
+    {
+      free(counts);
+      free(sums);
+      free(mins);
+      free(maxs);
+      counts = NULL;
+      sums = mins = maxs = NULL;
+    }
+  }
+  if (!ok)
+  {
+    if (q->strategy == 1) return refuse("the fact key's range is not small enough for the dense path");
+    by_dim_row = 1;
+    uint64_t D = q->dim_table_rows;
+    counts = (uint64_t*)malloc(D * 8);
+    sums = (int64_t*)malloc(D * core_count * 8);
+    mins = (int64_t*)malloc(D * core_count * 8);
+    maxs = (int64_t*)malloc(D * core_count * 8);
+    ok = counts && sums && mins && maxs && probe_totals(q, core_count, core_funcs, core_cols, counts, sums, mins, maxs);
+    total_groups = D;
+  }
+  if (!ok)
+  {
+    free(counts);
+    free(sums);
+    free(mins);
+    free(maxs);
+    return 0;
+  }
+  /* each (filtered) dim row meets its key's totals and joins the group of its group values (:8619-8720) */
+  uint64_t visits = q->dim_rows ? q->dim_count : q->dim_table_rows;
+  uint64_t cap = 64;
+  while (cap < visits * 2 + 2) cap *= 2;
+  uint32_t* slots = (uint32_t*)calloc(cap, 4);
+  typedef struct
+  {
+    uint64_t count;
+    double sum, mn, mx;
+    int seen;
+  } Acc;
+  Acc* acc = (Acc*)calloc((visits ? visits : 1) * q->expr_count, sizeof(Acc));
+  uint64_t* rep = (uint64_t*)malloc((visits ? visits : 1) * 8);
+  uint64_t groups = 0;
+  ok = slots && acc && rep;
+  for (uint64_t v = 0; ok && v < visits; v++)
+  {
+    uint64_t dim_row = q->dim_rows ? q->dim_rows[v] : v;
+    uint32_t kw = q->dim_keys[dim_row];
+    int64_t key_value = fk->type == CQLOPS_TYPE_I32 ? (int64_t)(int32_t)kw : (int64_t)kw;
+    int64_t id = by_dim_row ? (int64_t)dim_row : key_value - min_key;
+    if (id < 0 || (uint64_t)id >= total_groups || counts[id] == 0) continue;
+    uint64_t g = 0;
+    if (q->group_count == 0)
+    {
+      if (groups == 0)
+      {
+        groups = 1;
+        rep[0] = dim_row;
+      }
+    }
+    else
+    {
+      uint64_t h = 1469598103934665603ull;
+      for (uint32_t c = 0; c < q->group_count; c++)
+      {
+        uint64_t bits;
+        memcpy(&bits, &q->dim_group_values[c][dim_row], 8);
+        h = (h ^ bits) * 1099511628211ull;
+        h ^= h >> 29;
+      }
+      uint64_t pos = h & (cap - 1);
+      for (;;)
+      {
+        uint32_t stored = slots[pos];
+        if (stored == 0)
+        {
+          g = groups++;
+          slots[pos] = (uint32_t)g + 1;
+          rep[g] = dim_row;
+          break;
+        }
+        uint64_t cand = rep[stored - 1];
+        int same = 1;
+        for (uint32_t c = 0; c < q->group_count && same; c++) same = q->dim_group_values[c][cand] == q->dim_group_values[c][dim_row];
+        if (same)
+        {
+          g = stored - 1;
+          break;
+        }
+        pos = (pos + 1) & (cap - 1);
+      }
+    }
+    uint64_t matches = counts[id];
+    for (uint32_t e = 0; e < q->expr_count; e++)
+    {
+      Acc* a = &acc[g * q->expr_count + e];
+      a->count += matches;
+      uint32_t f = q->funcs[e];
+      if (f == CQLOPS_FUNC_COUNT) continue;
+      double value_sum, value_min, value_max;
+      if (q->dim_args && q->dim_args[e])
+      {
+        double value = q->dim_args[e][dim_row];
+        value_sum = value * (double)matches;
+        value_min = value_max = value;
+      }
+      else
+      {
+        uint64_t slot = (uint64_t)id * core_count + core_of_expr[e];
+        value_sum = (double)sums[slot];
+        value_min = (double)mins[slot];
+        value_max = (double)maxs[slot];
+      }
+      a->sum += value_sum;
+      a->mn = a->seen ? (value_min < a->mn ? value_min : a->mn) : value_min;
+      a->mx = a->seen ? (value_max > a->mx ? value_max : a->mx) : value_max;
+      a->seen = 1;
+    }
+  }
+  if (ok && groups > max_groups) ok = refuse("more groups than the output arrays hold");
+  if (ok)
+  {
+    for (uint64_t g = 0; g < groups; g++)
+    {
+      out_group_dim_row[g] = rep[g];
+      for (uint32_t e = 0; e < q->expr_count; e++)
+      {
+        Acc* a = &acc[g * q->expr_count + e];
+        double r;
+        switch (q->funcs[e])
+        {
+          case CQLOPS_FUNC_COUNT: r = (double)a->count; break;
+          case CQLOPS_FUNC_SUM: r = a->sum; break;
+          case CQLOPS_FUNC_AVG: r = a->count ? a->sum / (double)a->count : 0.0; break;
+          case CQLOPS_FUNC_MIN: r = a->mn; break;
+          default: r = a->mx; break;
+        }
+        out_results[g * q->expr_count + e] = r;
+      }
+    }
+    *out_groups = groups;
+    if (out_strategy) *out_strategy = by_dim_row ? 2u : 1u;
+  }
+  free(slots);
+  free(acc);
+  free(rep);
+  free(counts);
+  free(sums);
+  free(mins);
+  free(maxs);
+  return ok;
+}

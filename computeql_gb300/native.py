@@ -52,6 +52,12 @@ class CqlProgram(C.Structure):
                 ("error", C.c_char * 128)]
 
 
+class CqlJoinAgg(C.Structure):
+    _fields_ = [("fact_key", P), ("expr_count", u32), ("funcs", P), ("fact_args", P), ("dim_args", P), ("dim_keys", P),
+                ("dim_table_rows", u64), ("dim_rows", P), ("dim_count", u64), ("group_count", u32), ("dim_group_values", P),
+                ("strategy", u32)]
+
+
 class CqlFusedAgg(C.Structure):
     _fields_ = [("column_count", u32), ("slots", u32 * 4), ("coltypes", u32 * 4), ("grouped", u32), ("key_count", u32),
                 ("key_slots", u32 * 3), ("key_types", u32 * 3), ("key_ranges", u32 * 3), ("group_count", u32)]
@@ -142,6 +148,8 @@ OPS_API = [
     ("cqlops_fused_filter_aggregate", C.c_int, [P, P, P, u32, P, P, P, P]),
     ("cqlops_fused_filter_group", C.c_int, [P, P, P, u32, P, u32, u64, P, P, P, P, P, P, P, P]),
     ("cqlops_group_hash", C.c_int, [P, u32, u32, P, P, P, u64, u32, u64, P, P, P, P, P]),
+    ("cqlops_hash_join", C.c_int, [P, P, C.c_int, u64, P, P, u64]),
+    ("cqlops_join_aggregate", C.c_int, [P, u64, P, P, P, P]),
     ("cqlops_hll_estimate", dbl, [P, u64]),
     ("cqlops_tdigest_percentile", dbl, [P, P, u64, dbl]),
 ]

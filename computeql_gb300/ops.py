@@ -344,6 +344,49 @@ def group_hash(keys, funcs, args, params=None, group_hint=0, path=0, max_groups=
     return {"groups": G, "repr_row": repr_row[:G], "counts": counts[:G], "results": results[: G * e].reshape(G, e), "path": used.value}
 
 
+def hash_join(build_key, probe_key, left=False, hint_pairs=0, want_pairs=True):
+    """-> (pair count, pairs as an (n, 2) array of (probe row, build row) sorted, or None)."""
+    bc, pc_ = build_key.c(), probe_key.c()
+    count = C.c_uint64()
+    cap = (max(probe_key.rows, build_key.rows) + probe_key.rows) * 4 if want_pairs else 0
+    out = np.zeros(max(cap, 1) * 2, dtype=np.uint32) if want_pairs else None
+    _check(N.load_ops().cqlops_hash_join(C.byref(bc), C.byref(pc_), 1 if left else 0, hint_pairs, C.byref(count),
+                                         N.ptr(out) if want_pairs else None, cap), "cqlops_hash_join")
+    n = count.value
+    return n, (out[: 2 * min(n, cap)].reshape(-1, 2) if want_pairs else None)
+
+
+def join_aggregate(fact_key, funcs, fact_args, dim_keys, dim_rows=None, group_values=(), dim_args=None, strategy=0):
+    """Join-aggregate pushdown -> dict(groups, dim_row[G], results[G, E], strategy)."""
+    e = len(funcs)
+    fk = fact_key.c()
+    structs = {}
+    for a in fact_args:
+        if a is not None and id(a) not in structs:
+            structs[id(a)] = a.c()
+    fargs = (C.c_void_p * e)(*[C.addressof(structs[id(a)]) if a is not None else None for a in fact_args])
+    dargs_keep = [np.ascontiguousarray(d, dtype=np.float64) if d is not None else None for d in (dim_args or [None] * e)]
+    dargs = (C.c_void_p * e)(*[d.ctypes.data if d is not None else None for d in dargs_keep])
+    dk = np.ascontiguousarray(dim_keys, dtype=np.uint32)
+    dr = np.ascontiguousarray(dim_rows, dtype=np.uint64) if dim_rows is not None else None
+    gv_keep = [np.ascontiguousarray(g, dtype=np.float64) for g in group_values]
+    gv = (C.c_void_p * max(len(gv_keep), 1))(*[g.ctypes.data for g in gv_keep])
+    fa = np.array(funcs, dtype=np.uint32)
+    q = N.CqlJoinAgg(C.addressof(fk), e, fa.ctypes.data, C.addressof(fargs), C.addressof(dargs), dk.ctypes.data, len(dk),
+                     dr.ctypes.data if dr is not None else None, len(dr) if dr is not None else 0, len(gv_keep),
+                     C.addressof(gv) if gv_keep else None, strategy)
+    visits = len(dr) if dr is not None else len(dk)
+    mg = max(visits, 1)
+    dim_row = np.zeros(mg, dtype=np.uint64)
+    results = np.zeros(mg * e, dtype=np.float64)
+    groups = C.c_uint64()
+    used = C.c_uint32()
+    _check(N.load_ops().cqlops_join_aggregate(C.byref(q), mg, C.byref(groups), N.ptr(dim_row), N.ptr(results), C.byref(used)),
+           "cqlops_join_aggregate")
+    G = groups.value
+    return {"groups": G, "dim_row": dim_row[:G], "results": results[: G * e].reshape(G, e), "strategy": used.value}
+
+
 def compile_check(source):
     """NVRTC compile of a generated source for sm_103a, no device needed -> (ok, log)."""
     lib = N.load_cuda()

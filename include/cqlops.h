@@ -226,6 +226,38 @@ double cqlops_hll_estimate(const uint32_t* registers, uint64_t m);
 /* qe_tdigest_estimate_percentile (query_exec.c:6748-6790); sorts the centroids in place. */
 double cqlops_tdigest_percentile(float* means, float* weights, uint64_t count, double fraction);
 
+/* Equi-join of two key columns (numeric, compared as f64 values, or raw strings) - qe_hash_join_impl's
+   GPU path, src/query_exec/query_exec.c:14541-15358: the build side hashed into buckets (a power of
+   two >= its rows), bucket lists by prefix sum and scatter, every probe row emitting its
+   (probe row, build row) pairs; a LEFT join also emits (probe row, 0xffffffff) for an unmatched row.
+   hint_pairs > 0 sizes the output for that many pairs. Writes the pair count and up to
+   out_capacity pairs, sorted, as (probe, build) u32 pairs. */
+int cqlops_hash_join(const CqlColumn* build_key, const CqlColumn* probe_key, int left_join, uint64_t hint_pairs, uint64_t* out_count,
+                     uint32_t* out_pairs, uint64_t out_capacity);
+
+/* A join of a fact table to a dim table aggregated by dim columns (qe_aggregate_join_pushdown,
+   query_exec.c:8442-8776). */
+typedef struct CqlJoinAgg
+{
+  const CqlColumn* fact_key;          /* device, U32 or I32 */
+  uint32_t expr_count;
+  const uint32_t* funcs;              /* COUNT/SUM/AVG/MIN/MAX */
+  const CqlColumn* const* fact_args;  /* per expression: a fact column (device), or NULL */
+  const double* const* dim_args;      /* per expression: a dim column as f64 (host), or NULL; may itself be NULL */
+  const uint32_t* dim_keys;           /* host, the dim key column (dim_table_rows entries, same type as fact_key) */
+  uint64_t dim_table_rows;
+  const uint64_t* dim_rows;           /* the dim rows that pass the dim-side filter, NULL = all */
+  uint64_t dim_count;
+  uint32_t group_count;               /* GROUP BY dim columns */
+  const double* const* dim_group_values; /* host, f64 per dim row */
+  uint32_t strategy;                  /* 0 automatic, 1 dense over the fact key's range, 2 probe a hash table of the dim keys */
+} CqlJoinAgg;
+
+/* Groups come out in the order their first dim row is met; out_group_dim_row[g] is that row,
+   out_results[g*expr_count + e] the aggregate. out_strategy receives 1 (dense) or 2 (probe). */
+int cqlops_join_aggregate(const CqlJoinAgg* query, uint64_t max_groups, uint64_t* out_groups, uint64_t* out_group_dim_row, double* out_results,
+                          uint32_t* out_strategy);
+
 /* Why the last operator call returned 0 when it refused the request itself ("" otherwise; GPU
    failures are in cqlcuda_last_error()). */
 const char* cqlops_last_error(void);

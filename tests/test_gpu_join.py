@@ -1,0 +1,145 @@
+"""Hash joins and the join-aggregate pushdown through the C ABI.
+
+Join output is compared as sorted (probe, build) pairs with a join computed independently on the
+host; the pushdown against the reference's own closed-form answers (the joins of
+src/tests/scale/bench_select_scale.c:1158-1170: the 50-row table filtered on its zone, the 1M-row
+table on the needle key) and against numpy on the 1B-row configuration's tables at 10M rows.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from tests import closed_form as cf
+
+pytestmark = pytest.mark.gpu
+COUNT, SUM, AVG, MIN, MAX = 0, 1, 2, 3, 4
+
+
+@pytest.fixture(scope="module")
+def ops(gpu):
+    from computeql_gb300 import ops as o
+    return o
+
+
+def host_join(build, probe, left=False):
+    order = np.argsort(build, kind="stable")
+    sb = build[order]
+    lo = np.searchsorted(sb, probe, side="left")
+    hi = np.searchsorted(sb, probe, side="right")
+    pairs = []
+    for p in range(len(probe)):
+        if hi[p] > lo[p]:
+            for j in range(lo[p], hi[p]):
+                pairs.append((p, order[j]))
+        elif left:
+            pairs.append((p, 0xFFFFFFFF))
+    return np.array(sorted(pairs), dtype=np.uint32).reshape(-1, 2)
+
+
+@pytest.mark.parametrize("left", [False, True])
+@pytest.mark.parametrize("dtype", [np.uint32, np.int32, np.float64])
+def test_numeric_join_pairs(ops, left, dtype):
+    rng = np.random.default_rng(3)
+    build = rng.integers(-50, 2000, 5000).astype(dtype)   # duplicates included
+    probe = rng.integers(-100, 2500, 20000).astype(dtype)
+    n, pairs = ops.hash_join(ops.Column.from_numpy(build), ops.Column.from_numpy(probe), left=left)
+    want = host_join(build, probe, left)
+    assert n == len(want)
+    assert np.array_equal(pairs, want)
+
+
+def test_string_join_pairs(ops):
+    rng = np.random.default_rng(4)
+    words = [f"k{i:04d}" for i in range(300)] + ["", "a" * 30]
+    build = [words[i] for i in rng.integers(0, len(words), 400)]
+    probe = [words[i] for i in rng.integers(0, len(words), 3000)] + ["missing"]
+    n, pairs = ops.hash_join(ops.StringColumn(build), ops.StringColumn(probe), left=True)
+    b = np.array(build, dtype=object)
+    want = []
+    for p, key in enumerate(probe):
+        hits = np.nonzero(b == key)[0]
+        if len(hits):
+            want += [(p, int(h)) for h in hits]
+        else:
+            want.append((p, 0xFFFFFFFF))
+    assert n == len(want)
+    assert np.array_equal(pairs, np.array(sorted(want), dtype=np.uint32))
+
+
+def test_output_grows_past_the_first_guess(ops):
+    # every probe row matches 10 build rows: 10x the max(probe, build) + probe first guess
+    build = np.repeat(np.arange(100, dtype=np.uint32), 10)
+    probe = np.tile(np.arange(100, dtype=np.uint32), 50)
+    n, pairs = ops.hash_join(ops.Column.from_numpy(build), ops.Column.from_numpy(probe))
+    assert n == 5000 * 10
+    assert np.array_equal(pairs, host_join(build, probe))
+
+
+@pytest.mark.parametrize("n", [1_000_000, 3_000_017])
+def test_closed_form_filtered_join_to_the_50_row_table(ops, n):
+    _, region, amount, _ = oracle.closed_form(n)
+    regions_k = np.arange(50, dtype=np.uint32)
+    zone = regions_k // 10
+    dim_rows = np.nonzero(zone == 2)[0]
+    res = ops.join_aggregate(ops.Column.from_numpy(region), [COUNT, SUM], [None, ops.Column.from_numpy(amount)], regions_k,
+                             dim_rows=dim_rows)
+    assert res["strategy"] == 1  # region has a small range: the dense path
+    assert res["groups"] == 1
+    assert [res["results"][0, 0], res["results"][0, 1]] == [float(x) for x in cf.join_zone_expected(n)]
+
+
+def test_closed_form_join_to_the_1m_row_table(ops):
+    n = 2_000_000
+    _, _, _, needle = oracle.closed_form(n)
+    j = np.arange(1_000_000, dtype=np.uint64)
+    big_key = ((j * (n // 1_000_000)) * cf.KEY_MULTIPLIER & 0xFFFFFFFF).astype(np.uint32)
+    weight = (j % 100).astype(np.float64)
+    res = ops.join_aggregate(ops.Column.from_numpy(needle), [COUNT, SUM], [None, None], big_key, dim_args=[None, weight])
+    assert res["strategy"] == 2  # needle_key spans the 32-bit range: the probe path
+    assert [res["results"][0, 0], res["results"][0, 1]] == [1_000_000.0, cf.weight_sum(1_000_000)]
+
+
+def test_c2_joins_at_10m_rows(ops):
+    from computeql_gb300 import workloads
+    n = 10_000_000
+    t = workloads.fact_table(n)
+    h = workloads.fact_numpy(n, gen=oracle.splitmix_u32)
+    # dim50: k = 0..49, name_id = draw % 10, val = draw (seed 1); dim1M: k = 0..999999, seg = draw % 20 (seed 2)
+    name_id = oracle.splitmix_u32(50, 1, 2, 0, 10)
+    seg = oracle.splitmix_u32(1_000_000, 2, 1, 0, 20)
+    # SELECT COUNT(*), SUM(amount) FROM fact JOIN dim50 ON region = k WHERE name_id = 3
+    rows3 = np.nonzero(name_id == 3)[0]
+    res = ops.join_aggregate(t.region, [COUNT, SUM], [None, t.amount], np.arange(50, dtype=np.uint32), dim_rows=rows3)
+    sel = np.isin(h["region"], rows3)
+    assert res["results"][0, 0] == sel.sum()
+    assert res["results"][0, 1] == float(h["amount"][sel].astype(np.int64).sum())
+    # SELECT seg, SUM(amount) FROM fact JOIN dim1M ON amount = k GROUP BY seg
+    res = ops.join_aggregate(t.amount, [SUM, COUNT], [t.amount, None], np.arange(1_000_000, dtype=np.uint32),
+                             group_values=[seg.astype(np.float64)])
+    got = {int(seg[r]): (res["results"][g, 0], res["results"][g, 1]) for g, r in enumerate(res["dim_row"])}
+    s = seg[h["amount"]]
+    for v in range(20):
+        m = s == v
+        if m.any():
+            assert got[v] == (float(h["amount"][m].astype(np.int64).sum()), float(m.sum()))
+
+
+def test_dense_and_probe_paths_agree(ops):
+    rng = np.random.default_rng(9)
+    n = 1_000_000
+    key = rng.integers(0, 5000, n).astype(np.uint32)
+    v = rng.integers(-1000, 1000, n).astype(np.int32)
+    dim_keys = rng.permutation(6000).astype(np.uint32)
+    grp = (np.arange(6000) % 7).astype(np.float64)
+    kc, vc = ops.Column.from_numpy(key), ops.Column.from_numpy(v)
+    a = ops.join_aggregate(kc, [COUNT, SUM, MIN, MAX, AVG], [None, vc, vc, vc, vc], dim_keys, group_values=[grp], strategy=1)
+    b = ops.join_aggregate(kc, [COUNT, SUM, MIN, MAX, AVG], [None, vc, vc, vc, vc], dim_keys, group_values=[grp], strategy=2)
+    assert (a["strategy"], b["strategy"]) == (1, 2)
+    ga = {grp[r]: tuple(a["results"][g]) for g, r in enumerate(a["dim_row"])}
+    gb = {grp[r]: tuple(b["results"][g]) for g, r in enumerate(b["dim_row"])}
+    assert ga == gb
+    for gval, r in ga.items():
+        keys_in = dim_keys[grp == gval]
+        m = np.isin(key, keys_in)
+        assert r[0] == m.sum() and r[1] == float(v[m].astype(np.int64).sum())
+        assert (r[2], r[3]) == (float(v[m].min()), float(v[m].max()))
