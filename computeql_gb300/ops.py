@@ -387,6 +387,25 @@ def join_aggregate(fact_key, funcs, fact_args, dim_keys, dim_rows=None, group_va
     return {"groups": G, "dim_row": dim_row[:G], "results": results[: G * e].reshape(G, e), "strategy": used.value}
 
 
+def sort_rows(keys, desc=None, selection=None, count=None):
+    """ORDER BY -> row numbers in sorted order (keys compared as F64, ties by input position).
+
+    `selection` is an optional DeviceBuffer of u32 row numbers (a filter's row set, `count` of them, all
+    by default); the sort then orders those rows and returns their row numbers.
+    """
+    kc = len(keys)
+    arr = (N.CqlColumn * kc)(*[k.c() for k in keys])
+    d = np.array(desc if desc is not None else [0] * kc, dtype=np.uint32)
+    if selection is not None:
+        n = selection.nbytes // 4 if count is None else count
+        sel = selection.handle
+    else:
+        n, sel = keys[0].rows, None
+    out = np.zeros(max(n, 1), dtype=np.uint32)
+    _check(N.load_ops().cqlops_sort_rows(arr, kc, N.ptr(d), sel, n, N.ptr(out), n), "cqlops_sort_rows")
+    return out[:n]
+
+
 def compile_check(source):
     """NVRTC compile of a generated source for sm_103a, no device needed -> (ok, log)."""
     lib = N.load_cuda()

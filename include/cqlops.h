@@ -258,6 +258,15 @@ typedef struct CqlJoinAgg
 int cqlops_join_aggregate(const CqlJoinAgg* query, uint64_t max_groups, uint64_t* out_groups, uint64_t* out_group_dim_row, double* out_results,
                           uint32_t* out_strategy);
 
+/* ORDER BY up to 4 numeric keys (desc[k] != 0 for DESC), keys compared as F64 values with ties broken
+   by input position - qe_sort_rows (src/query_exec/query_exec.c:5376-6155, compare :4859-4882) with a
+   stable LSD radix sort in place of the bitonic sorts. Without a selection the input is the columns' rows
+   and the output their row numbers; with one (selection_count u32 row numbers in a device buffer, the
+   row set of a filter) the input is those rows in selection order and the output is their row numbers.
+   Writes up to out_capacity row numbers in sorted order. */
+int cqlops_sort_rows(const CqlColumn* keys, uint32_t key_count, const uint32_t* desc, CqlBuffer* selection,
+                     uint64_t selection_count, uint32_t* out_rows, uint64_t out_capacity);
+
 /* Why the last operator call returned 0 when it refused the request itself ("" otherwise; GPU
    failures are in cqlcuda_last_error()). */
 const char* cqlops_last_error(void);

@@ -13,7 +13,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
-SOURCES = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "oracle_sketch.c")]
+SOURCES = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "oracle_sketch.c"), os.path.join(HERE, "oracle_sort.c")]
 
 U32, U64, F32, F64, I32, I64 = 1, 2, 3, 4, 7, 8
 
@@ -64,6 +64,8 @@ def lib():
         L.orc_hll_estimate.restype = dbl
         L.orc_tdigest_percentile.argtypes = [P, P, u64, dbl]
         L.orc_tdigest_percentile.restype = dbl
+        L.orc_sort_rows.argtypes = [P, u32, P, u64, P]
+        L.orc_sort_rows.restype = C.c_int
         _lib = L
     return _lib
 
@@ -185,3 +187,14 @@ def tdigest_percentile(means, weights, fraction):
     m = np.ascontiguousarray(means, dtype=np.float32)
     w = np.ascontiguousarray(weights, dtype=np.float32)
     return lib().orc_tdigest_percentile(_p(m), _p(w), len(m), fraction)
+
+
+def sort_rows(keys, desc=None):
+    """Row numbers in ORDER BY order: keys compared as F64, DESC per key, ties by position."""
+    rows = len(keys[0])
+    k = np.ascontiguousarray(np.stack([np.asarray(x).astype(np.float64) for x in keys]))
+    d = np.array(desc if desc is not None else [0] * len(keys), dtype=np.uint32)
+    out = np.empty(max(rows, 1), dtype=np.uint64)
+    if not lib().orc_sort_rows(_p(k), len(keys), _p(d), rows, _p(out)):
+        raise MemoryError("orc_sort_rows")
+    return out[:rows]

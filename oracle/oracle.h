@@ -101,4 +101,8 @@ uint64_t orc_group_cpu_reduce(const uint32_t* key, uint64_t rows, uint32_t expr_
 }
 #endif
 
+
+/* ORDER BY over key_count F64 key columns laid out key-major (keys[k * rows + i]); desc[k] != 0 for DESC.
+   Writes the row numbers in order, ties by position (query_exec.c:4859-4940). */
+int orc_sort_rows(const double* keys, uint32_t key_count, const uint32_t* desc, uint64_t rows, uint64_t* out);
 #endif
