@@ -6,6 +6,10 @@ A step runs the query suite of the 1B-row configuration once over a warm, device
   q3 SELECT region, SUM(amount), COUNT(*) GROUP BY region         aggregate_dense_native, 50 groups
   q4 SELECT amount, COUNT(*), SUM(region) GROUP BY amount         aggregate_dense_native, 10k groups
   q5 SELECT id, ... WHERE id = k (a random k)                      scan_simple on the id sequence
+  q6 SELECT COUNT(*), SUM(amount) FROM fact JOIN dim50 ON region = dim50.k WHERE dim50.name_id = 3
+                                                                    join_probe_native (dense core)
+  q7 SELECT seg, SUM(amount), COUNT(*) FROM fact JOIN dim1M ON amount % 1000000 = dim1M.k GROUP BY seg
+                                                                    join_probe_native (dense core)
 value = (queries x rows) / suite time, on the device (CUDA events around the step, inputs larger
 than L2). `e2e` runs the same suite through the C ABI from pinned HOST buffers: every step uploads the
 columns the queries read and reads the results back. `roofline` is the dominant kernel's algorithmic
@@ -34,6 +38,7 @@ UNIT = "rows/s"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 CPU_SAMPLE_ROWS = 100_000_000
+N_QUERIES = 7
 
 
 def hbm_peak():
@@ -92,10 +97,13 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_queries(ops, t, rng_key):
+def make_queries(ops, t, rng_key, dims):
     """The suite as (name, algorithmic bytes, callable)."""
+    import numpy as np
     n = t.rows
     k = int(rng_key)
+    d50, d1m = dims
+    seg_values = d1m["seg"].astype(np.float64)
 
     def q1():
         return ops.aggregate_global([t.amount])
@@ -112,8 +120,18 @@ def make_queries(ops, t, rng_key):
     def q5():
         return ops.scan_simple([t.id], [(0, ops.CMP_EQ, k)], want_rows=True, max_rows=16)
 
+    def q6():
+        kept = np.nonzero(d50["name_id"] == 3)[0]          # the dimension filter (50 rows)
+        return ops.join_aggregate(t.region, [ops.FUNC_COUNT, ops.FUNC_SUM], [None, t.amount], d50["k"], dim_rows=kept)
+
+    def q7():
+        # amount < 10000, so amount % 1000000 is amount itself
+        return ops.join_aggregate(t.amount, [ops.FUNC_SUM, ops.FUNC_COUNT], [t.amount, None], d1m["k"],
+                                  group_values=[seg_values])
+
     return [("sum_min_max_amount", 4 * n, q1), ("count_flag_lt_2", 4 * n, q2), ("group_by_region", 8 * n, q3),
-            ("group_by_amount_10k", 8 * n, q4), ("point_lookup_id", 4 * n, q5)]
+            ("group_by_amount_10k", 8 * n, q4), ("point_lookup_id", 4 * n, q5), ("join_dim50_filtered", 8 * n, q6),
+            ("join_dim1m_group_by_seg", 4 * n, q7)]
 
 
 def profile_entries(native):
@@ -141,15 +159,20 @@ def cpu_baseline(rows, threads=0):
     oracle.set_threads(threads)
     h = workloads.fact_numpy(rows, gen=oracle.splitmix_u32)
     ids = np.arange(rows, dtype=np.uint32)
+    d50 = {"k": np.arange(50, dtype=np.uint32), "name_id": oracle.splitmix_u32(50, workloads.DIM50_SEED, 2, 0, 10)}
+    d1m = {"k": np.arange(1_000_000, dtype=np.uint32), "seg": oracle.splitmix_u32(1_000_000, workloads.DIM1M_SEED, 1, 0, 20)}
     t0 = time.perf_counter()
     oracle.aggregate_global_cpu(h["amount"])
     oracle.scan_and([(h["flag"], 1, 2)], rows)
     oracle.group_cpu_reduce(h["region"], [h["amount"]], 64)
     oracle.group_cpu_reduce(h["amount"], [h["region"]], 16384)
     oracle.scan_and([(ids, 0, rows // 3)], rows, want_rows=True)
+    keep = np.where(d50["name_id"] == 3, 0, 0xFFFFFFFF).astype(np.uint32)
+    oracle.join_aggregate(h["region"], h["amount"], d50["k"], keep, 1)
+    oracle.join_aggregate(h["amount"], h["amount"], d1m["k"], d1m["seg"], 20)
     dt = time.perf_counter() - t0
-    return {"value": 5 * rows / dt, "unit": UNIT, "cores": oracle.lib().orc_threads(), "kind": "port",
-            "sample": f"the 5-query suite on the first {rows} rows of the seed-0 table ({dt:.2f} s)"}
+    return {"value": N_QUERIES * rows / dt, "unit": UNIT, "cores": oracle.lib().orc_threads(), "kind": "port",
+            "sample": f"the {N_QUERIES}-query suite on the first {rows} rows of the seed-0 table ({dt:.2f} s)"}
 
 
 def run_reference(args, rank, world):
@@ -163,9 +186,10 @@ def run_reference(args, rank, world):
             samples.append(r)
     value = statistics.median(s["value"] for s in samples)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 5 * rows / value * 1e3, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": N_QUERIES * rows / value * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32", "data": "synthetic (splitmix64 seed 0)",
-            "config": {"workload": f"1B-row 4 x u32 table query suite (CPU sample of {rows} rows)", "rows": rows, "queries": 5},
+            "config": {"workload": f"1B-row 4 x u32 table + dim50 + dim1M query suite (CPU sample of {rows} rows)", "rows": rows,
+                       "queries": N_QUERIES},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": samples[0]["cores"], "kind": "port", "sample": samples[0]["sample"]},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -207,7 +231,7 @@ def main():
     t = workloads.fact_table(args.rows)
     import numpy as np
     key = np.random.default_rng(1234 + rank).integers(0, args.rows)
-    queries = make_queries(ops, t, key)
+    queries = make_queries(ops, t, key, workloads.dim_tables())
 
     for _ in range(args.warmup):
         for _, _, q in queries:
@@ -246,9 +270,11 @@ def main():
 
     peak, peak_kind = hbm_peak()
     # per-kernel CUDA-event time; the dominant kernel gives the roofline
-    kernel_bytes = {"aggregate_global_native": 4 * args.rows, "scan_simple": 4 * args.rows, "aggregate_dense_native": 8 * args.rows}
+    kernel_bytes = {"aggregate_global_native": 4 * args.rows, "scan_simple": 4 * args.rows, "aggregate_dense_native": 8 * args.rows,
+                    "join_probe_native": 6 * args.rows}
     kernel_units = {"aggregate_global_native": "1 column x rows x 4 B", "scan_simple": "1 column x rows x 4 B",
-                    "aggregate_dense_native": "key + argument column x rows x 4 B"}
+                    "aggregate_dense_native": "key + argument column x rows x 4 B",
+                    "join_probe_native": "two launches a step: key + argument (8 B/row) and one shared column (4 B/row)"}
     top = max((k for k in prof if k in kernel_bytes), key=lambda k: prof[k][0], default=None)
     roofline = None
     if top:
@@ -278,7 +304,8 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
                 "data": "synthetic (splitmix64 seed 0, generated on the device)",
-                "config": {"workload": "1B-row 4 x u32 table (id sequence, region, amount, flag), warm in HBM: 5-query suite",
+                "config": {"workload": "1B-row 4 x u32 table (id sequence, region, amount, flag) + dim50 + dim1M, warm in HBM: "
+                                       f"{len(queries)}-query suite",
                            "rows": args.rows, "queries": [q[0] for q in queries], "l2": "inputs larger than L2 (4 GB columns)",
                            "parallelism": f"replicas x{world}"},
                 "gpu_launches": launches, "queries": qstats, "kernels": kernels, "roofline": roofline, "clocks": clk,
@@ -315,8 +342,8 @@ def run_e2e(args, native, ops, t, queries, lib):
         if i >= args.warmup:
             times.append(dt)
     ms = statistics.median(times) * 1e3
-    # results read back per step: partials/counters/group arrays of the 5 queries (a few hundred KB)
-    d2h = 2048 * 3 * 8 + 8 + 50 * 4 * 8 + 10000 * 4 * 8 + 8
+    # results read back per step: partials/counters/group arrays of the queries (a few hundred KB)
+    d2h = 2048 * 3 * 8 + 8 + 50 * 4 * 8 + 10000 * 4 * 8 + 8 + 2 * 8 + 20 * 2 * 8
     return {"value": len(queries) * n / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h}
 

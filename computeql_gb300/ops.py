@@ -349,11 +349,15 @@ def hash_join(build_key, probe_key, left=False, hint_pairs=0, want_pairs=True):
     bc, pc_ = build_key.c(), probe_key.c()
     count = C.c_uint64()
     cap = (max(probe_key.rows, build_key.rows) + probe_key.rows) * 4 if want_pairs else 0
-    out = np.zeros(max(cap, 1) * 2, dtype=np.uint32) if want_pairs else None
-    _check(N.load_ops().cqlops_hash_join(C.byref(bc), C.byref(pc_), 1 if left else 0, hint_pairs, C.byref(count),
-                                         N.ptr(out) if want_pairs else None, cap), "cqlops_hash_join")
-    n = count.value
-    return n, (out[: 2 * min(n, cap)].reshape(-1, 2) if want_pairs else None)
+    while True:
+        out = np.zeros(max(cap, 1) * 2, dtype=np.uint32) if want_pairs else None
+        _check(N.load_ops().cqlops_hash_join(C.byref(bc), C.byref(pc_), 1 if left else 0, hint_pairs, C.byref(count),
+                                             N.ptr(out) if want_pairs else None, cap), "cqlops_hash_join")
+        n = count.value
+        if not want_pairs or n <= cap:
+            break
+        cap = hint_pairs = n          # the host array was too small: once more with room for every pair
+    return n, (out[: 2 * n].reshape(-1, 2) if want_pairs else None)
 
 
 def join_aggregate(fact_key, funcs, fact_args, dim_keys, dim_rows=None, group_values=(), dim_args=None, strategy=0):

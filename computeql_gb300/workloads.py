@@ -41,3 +41,15 @@ def fact_numpy(rows, seed=FACT_SEED, gen=None):
     for name, idx, rng in FACT_DRAWN:
         out[name] = gen(rows, seed, len(FACT_DRAWN), idx, rng)
     return out
+
+
+def dim_tables():
+    """dim50 (k, name_id, val) and dim1M (k, seg) as host arrays, drawn on the device like the fact table."""
+    import numpy as np
+    from .ops import Column
+    n50, n1m = 50, 1_000_000
+    d50 = {name: Column.splitmix(n50, DIM50_SEED, len(DIM50_DRAWN), idx, rng).buffer.read(np.uint32) for name, idx, rng in DIM50_DRAWN}
+    d1m = {name: Column.splitmix(n1m, DIM1M_SEED, len(DIM1M_DRAWN), idx, rng).buffer.read(np.uint32) for name, idx, rng in DIM1M_DRAWN}
+    d50["k"] = np.arange(n50, dtype=np.uint32)
+    d1m["k"] = np.arange(n1m, dtype=np.uint32)
+    return d50, d1m

@@ -13,7 +13,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
-SOURCES = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "oracle_sketch.c"), os.path.join(HERE, "oracle_sort.c")]
+SOURCES = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "oracle_sketch.c"), os.path.join(HERE, "oracle_sort.c"),
+           os.path.join(HERE, "oracle_join.c")]
 
 U32, U64, F32, F64, I32, I64 = 1, 2, 3, 4, 7, 8
 
@@ -66,6 +67,8 @@ def lib():
         L.orc_tdigest_percentile.restype = dbl
         L.orc_sort_rows.argtypes = [P, u32, P, u64, P]
         L.orc_sort_rows.restype = C.c_int
+        L.orc_join_aggregate.argtypes = [P, P, u64, P, P, u64, u32, P, P]
+        L.orc_join_aggregate.restype = C.c_int
         _lib = L
     return _lib
 
@@ -198,3 +201,18 @@ def sort_rows(keys, desc=None):
     if not lib().orc_sort_rows(_p(k), len(keys), _p(d), rows, _p(out)):
         raise MemoryError("orc_sort_rows")
     return out[:rows]
+
+
+def join_aggregate(fact_key, fact_arg, dim_key, dim_group, groups):
+    """COUNT(*) and SUM(fact_arg) per group over fact JOIN dim (dim_group 0xffffffff = filtered out)."""
+    fk = np.ascontiguousarray(fact_key, dtype=np.uint32)
+    fa = np.ascontiguousarray(fact_arg, dtype=np.uint32) if fact_arg is not None else None
+    dk = np.ascontiguousarray(dim_key, dtype=np.uint32)
+    dg = np.ascontiguousarray(dim_group, dtype=np.uint32)
+    counts = np.zeros(groups, dtype=np.uint64)
+    sums = np.zeros(groups, dtype=np.int64)
+    ok = lib().orc_join_aggregate(_p(fk), _p(fa) if fa is not None else None, len(fk), _p(dk), _p(dg), len(dk), groups,
+                                  _p(counts), _p(sums))
+    if not ok:
+        raise MemoryError("orc_join_aggregate")
+    return counts, sums

@@ -72,6 +72,8 @@ static void orc_parallel(uint32_t tasks, orc_task_fn fn, void* ctx)
   pthread_mutex_destroy(&pool.lock);
 }
 
+void orc_parallel_for(uint32_t tasks, orc_task_fn fn, void* ctx) { orc_parallel(tasks, fn, ctx); }
+
 /* ---- data ---- */
 
 uint64_t orc_splitmix_draw(uint64_t seed, uint64_t k)

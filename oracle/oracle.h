@@ -105,4 +105,9 @@ uint64_t orc_group_cpu_reduce(const uint32_t* key, uint64_t rows, uint32_t expr_
 /* ORDER BY over key_count F64 key columns laid out key-major (keys[k * rows + i]); desc[k] != 0 for DESC.
    Writes the row numbers in order, ties by position (query_exec.c:4859-4940). */
 int orc_sort_rows(const double* keys, uint32_t key_count, const uint32_t* desc, uint64_t rows, uint64_t* out);
+
+/* SELECT group, COUNT(*), SUM(fact_arg) over fact JOIN dim ON fact_key = dim_key, dim_group[d] the
+   group of dimension row d (0xffffffff = the row is filtered out); fact_arg may be NULL. */
+int orc_join_aggregate(const uint32_t* fact_key, const uint32_t* fact_arg, uint64_t rows, const uint32_t* dim_key,
+                       const uint32_t* dim_group, uint64_t dim_count, uint32_t groups, uint64_t* out_counts, int64_t* out_sums);
 #endif
