@@ -151,6 +151,11 @@ def profile_entries(native):
     return out
 
 
+def device_ns(native):
+    """Total CUDA-event time of every kernel launched so far (the profile must be on)."""
+    return sum(ns for ns, _ in profile_entries(native).values())
+
+
 def cpu_baseline(rows, threads=0):
     """The oracle (CPU restatement of the reference's operators) on a bounded sample: rows/s over the suite."""
     import numpy as np
@@ -245,13 +250,16 @@ def main():
     lib.cqlcuda_kernel_profile_enable(1)
     launches0 = lib.cqlcuda_kernel_launch_count()
     per_query = {name: [] for name, _, _ in queries}
+    per_query_device = {name: [] for name, _, _ in queries}
     step_ms = []
     for _ in range(args.steps):
         lib.cqlcuda_timer_begin()
         for name, _, q in queries:
+            d0 = device_ns(native)
             t0 = time.perf_counter()
             q()
             per_query[name].append((time.perf_counter() - t0) * 1e3)
+            per_query_device[name].append((device_ns(native) - d0) / 1e6)
         step_ms.append(lib.cqlcuda_timer_end_ms())
     launches = lib.cqlcuda_kernel_launch_count() - launches0
     lib.cqlcuda_kernel_profile_enable(0)
@@ -288,8 +296,10 @@ def main():
     qstats = {}
     for name, nbytes, _ in queries:
         ms = statistics.median(per_query[name])
+        dms = statistics.median(per_query_device[name])
         qstats[name] = {"ms": ms, "rows_per_s": args.rows / (ms / 1e3), "GBps": nbytes / (ms / 1e3) / 1e9,
-                        "hbm_frac": nbytes / (ms / 1e3) / 1e9 / peak}
+                        "hbm_frac": nbytes / (ms / 1e3) / 1e9 / peak, "kernel_ms": dms,
+                        "kernel_hbm_frac": nbytes / (dms / 1e3) / 1e9 / peak if dms > 0 else None}
     kernels = {k: {"ms_avg": ns / c / 1e6, "launches": c} for k, (ns, c) in prof.items()}
 
     e2e = None

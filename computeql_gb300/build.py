@@ -26,8 +26,8 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["runtime.cu", "k_aggregate.cu", "k_scan.cu", "k_hash.cu", "k_join.cu", "k_sort.cu"]
-C_SOURCES = ["cql_ops.c", "cql_program.c", "cql_codegen.c", "cql_ops_filter.c", "cql_ops_hash.c", "cql_ops_join.c", "cql_ops_sort.c"]
+CU_SOURCES = ["runtime.cu", "k_aggregate.cu", "k_scan.cu", "k_hash.cu", "k_join.cu", "k_sort.cu", "k_fixed.cu"]
+C_SOURCES = ["cql_ops.c", "cql_program.c", "cql_codegen.c", "cql_ops_filter.c", "cql_ops_hash.c", "cql_ops_join.c", "cql_ops_sort.c", "cql_ops_fixed.c"]
 
 LIB_CUDA = os.path.join(PKG, "libcqlcuda.so")
 LIB_OPS = os.path.join(PKG, "libcqlops.so")
@@ -70,7 +70,7 @@ def _compile_c(src):
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     if not _stale(obj, [src] + _headers()):
         return obj
-    _run(["gcc", "-std=c99", "-O2", "-fPIC", "-Wall", "-Wno-unused-function", "-I", INCLUDE, "-I", HOST, "-c", src, "-o", obj])
+    _run(["gcc", "-std=c99", "-O2", "-ffp-contract=off", "-fPIC", "-Wall", "-Wno-unused-function", "-I", INCLUDE, "-I", HOST, "-c", src, "-o", obj])
     return obj
 
 

@@ -698,6 +698,10 @@ __global__ void __launch_bounds__(1024) k_aggregate_dense_wide(CqlLaunch a, uint
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   constexpr int NC = NA > 0 ? NA : 1;
+  // an argument that is the key column itself (GROUP BY amount ... SUM(amount)) is not read twice
+  bool is_key[NC];
+#pragma unroll
+  for (int c = 0; c < NC; c++) is_key[c] = c < NA && a.buf[1 + c] == a.buf[0];
   uint64_t i = t;
   // two key vectors and two vectors of every argument column in flight per thread
   for (; i + stride < vec_count; i += 2 * stride)
@@ -707,7 +711,12 @@ __global__ void __launch_bounds__(1024) k_aggregate_dense_wide(CqlLaunch a, uint
 #pragma unroll
     for (int c = 0; c < NC; c++)
     {
-      if (c < NA)
+      if (c < NA && is_key[c])
+      {
+        q0[c] = k0;
+        q1[c] = k1;
+      }
+      else if (c < NA)
       {
         q0[c] = __ldcs((const uint4*)a.buf[1 + c] + i);
         q1[c] = __ldcs((const uint4*)a.buf[1 + c] + i + stride);
@@ -749,7 +758,7 @@ __global__ void __launch_bounds__(1024) k_aggregate_dense_wide(CqlLaunch a, uint
     uint4 k0 = __ldcs(kv + i);
     uint4 q0[NC];
 #pragma unroll
-    for (int c = 0; c < NC; c++) q0[c] = c < NA ? __ldcs((const uint4*)a.buf[1 + c] + i) : make_uint4(0, 0, 0, 0);
+    for (int c = 0; c < NC; c++) q0[c] = c < NA ? (is_key[c] ? k0 : __ldcs((const uint4*)a.buf[1 + c] + i)) : make_uint4(0, 0, 0, 0);
     uint32_t v[NC];
 #pragma unroll
     for (int c = 0; c < NC; c++) v[c] = q0[c].x;

@@ -151,6 +151,8 @@ OPS_API = [
     ("cqlops_hash_join", C.c_int, [P, P, C.c_int, u64, P, P, u64]),
     ("cqlops_join_aggregate", C.c_int, [P, u64, P, P, P, P]),
     ("cqlops_sort_rows", C.c_int, [P, u32, P, P, u64, P, u64]),
+    ("cqlops_fixed_scale", C.c_int, [P, P, u64, P, P]),
+    ("cqlops_group_dense_fixed", C.c_int, [P, u32, P, P, P, u64, u64, P, P, P, P, P, P]),
     ("cqlops_hll_estimate", dbl, [P, u64]),
     ("cqlops_tdigest_percentile", dbl, [P, P, u64, dbl]),
 ]

@@ -410,6 +410,42 @@ def sort_rows(keys, desc=None, selection=None, count=None):
     return out[:n]
 
 
+def fixed_scale(column, selection=None, count=None):
+    """-> (scale or -1, largest magnitude): the decimal places every value needs (at most 6)."""
+    n = column.rows if selection is None else (selection.nbytes // 4 if count is None else count)
+    c = column.c()
+    scale = C.c_int32()
+    largest = C.c_double()
+    _check(N.load_ops().cqlops_fixed_scale(C.byref(c), selection.handle if selection is not None else None, n, C.byref(scale),
+                                           C.byref(largest)), "cqlops_fixed_scale")
+    return scale.value, largest.value
+
+
+def group_dense_fixed(key, funcs, args, selection=None, count=None, max_groups=65536):
+    """GROUP BY key with COUNT/SUM/AVG/MIN/MAX over decimal f64/f32 columns, exact as scaled integers.
+
+    -> dict(keys, first_rows, counts, results[G, E], scales) for the present groups in key order.
+    """
+    e = len(funcs)
+    kc = key.c()
+    structs = [a.c() if a is not None else None for a in args]
+    arr = (C.c_void_p * e)(*[C.addressof(s) if s is not None else None for s in structs])
+    fa = np.array(funcs, dtype=np.uint32)
+    n = key.rows if selection is None else (selection.nbytes // 4 if count is None else count)
+    keys = np.zeros(max_groups, dtype=np.int64)
+    first = np.zeros(max_groups, dtype=np.uint64)
+    counts = np.zeros(max_groups, dtype=np.uint64)
+    results = np.zeros(max_groups * e, dtype=np.float64)
+    scales = np.zeros(e, dtype=np.int32)
+    groups = C.c_uint64()
+    _check(N.load_ops().cqlops_group_dense_fixed(C.byref(kc), e, N.ptr(fa), arr, selection.handle if selection is not None else None,
+                                                 n, max_groups, C.byref(groups), N.ptr(keys), N.ptr(first), N.ptr(counts),
+                                                 N.ptr(results), N.ptr(scales)), "cqlops_group_dense_fixed")
+    G = groups.value
+    return {"keys": keys[:G], "first_rows": first[:G], "counts": counts[:G], "results": results[: G * e].reshape(G, e),
+            "scales": list(scales)}
+
+
 def compile_check(source):
     """NVRTC compile of a generated source for sm_103a, no device needed -> (ok, log)."""
     lib = N.load_cuda()

@@ -258,6 +258,26 @@ typedef struct CqlJoinAgg
 int cqlops_join_aggregate(const CqlJoinAgg* query, uint64_t max_groups, uint64_t* out_groups, uint64_t* out_group_dim_row, double* out_results,
                           uint32_t* out_strategy);
 
+/* qe_values_fixed_point (src/query_exec/query_exec.c:3893-3983) over a device column (or the rows of
+   a selection): the smallest scale s <= 6 at which every value v is whole, that is (S64)(v*10^s +- 0.5)
+   / 10^s == v, with every |v| < 2^31 and the largest |v| * 10^s < 2^31; -1 when there is none.
+   U32/I32 columns have scale 0 while their magnitudes stay below 2^31. Returns 1 when it ran. */
+int cqlops_fixed_scale(const CqlColumn* column, CqlBuffer* selection, uint64_t selection_count, int32_t* out_scale, double* out_largest);
+
+/* GROUP BY one small-range whole-number key (U32/I32, or F64 holding whole numbers) with
+   COUNT/SUM/AVG/MIN/MAX over F64/F32 arguments that are decimals of at most 6 places - the dense
+   branch of qe_aggregate_impl with fixed-point arguments (query_exec.c:10896-11083, kernels
+   aggregate_dense_f64/_f32). Each argument is scaled by 10^s and summed exactly as an integer; the
+   values are finalized as there: SUM = (F64)sum / 10^s, AVG = (F64)sum / 10^s / count, MIN/MAX =
+   (F64)(S32)q / 10^s, COUNT = count. Optional selection: selection_count u32 row numbers in a device
+   buffer. Writes the present groups in key order: out_keys, out_first_rows (the smallest row of the
+   group), out_counts and out_results[g * expr_count + e], at most max_groups of them; out_scales[e]
+   (optional) receives each argument's scale. Refuses (returns 0 with cqlops_last_error set) when an
+   argument is not fixed-point or the key range is too wide, as the reference then takes another path. */
+int cqlops_group_dense_fixed(const CqlColumn* key, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* args,
+                             CqlBuffer* selection, uint64_t selection_count, uint64_t max_groups, uint64_t* out_groups,
+                             int64_t* out_keys, uint64_t* out_first_rows, uint64_t* out_counts, double* out_results, int32_t* out_scales);
+
 /* ORDER BY up to 4 numeric keys (desc[k] != 0 for DESC), keys compared as F64 values with ties broken
    by input position - qe_sort_rows (src/query_exec/query_exec.c:5376-6155, compare :4859-4882) with a
    stable LSD radix sort in place of the bitonic sorts. Without a selection the input is the columns' rows

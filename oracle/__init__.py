@@ -14,7 +14,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 SOURCES = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "oracle_sketch.c"), os.path.join(HERE, "oracle_sort.c"),
-           os.path.join(HERE, "oracle_join.c")]
+           os.path.join(HERE, "oracle_join.c"), os.path.join(HERE, "oracle_fixed.c")]
 
 U32, U64, F32, F64, I32, I64 = 1, 2, 3, 4, 7, 8
 
@@ -26,7 +26,7 @@ def build():
     deps = SOURCES + [os.path.join(HERE, "oracle.h")]
     if os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
         return LIB
-    cmd = ["gcc", "-std=c99", "-O2", "-fPIC", "-shared", "-Wall", "-o", LIB, *SOURCES, "-lpthread", "-lm"]
+    cmd = ["gcc", "-std=c99", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", "-o", LIB, *SOURCES, "-lpthread", "-lm"]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + r.stdout)
@@ -69,6 +69,11 @@ def lib():
         L.orc_sort_rows.restype = C.c_int
         L.orc_join_aggregate.argtypes = [P, P, u64, P, P, u64, u32, P, P]
         L.orc_join_aggregate.restype = C.c_int
+        L.orc_fixed_scale.argtypes = [P, u64, P, P]
+        L.orc_fixed_scale.restype = C.c_int
+        L.orc_fixed_scale_each.argtypes = [P, u64, P]
+        L.orc_dense_fixed.argtypes = [P, u64, u32, P, P, P, C.c_int64, u64, P, P, P, P]
+        L.orc_dense_fixed.restype = u64
         _lib = L
     return _lib
 
@@ -216,3 +221,37 @@ def join_aggregate(fact_key, fact_arg, dim_key, dim_group, groups):
     if not ok:
         raise MemoryError("orc_join_aggregate")
     return counts, sums
+
+
+def fixed_scale(values):
+    """qe_values_fixed_point over f64 values -> (scale or -1, largest magnitude)."""
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    scale = C.c_int32()
+    largest = C.c_double()
+    lib().orc_fixed_scale(_p(v), len(v), C.byref(scale), C.byref(largest))
+    return scale.value, largest.value
+
+
+def fixed_scale_each(values):
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    out = np.empty(len(v), dtype=np.int8)
+    lib().orc_fixed_scale_each(_p(v), len(v), _p(out))
+    return out
+
+
+def dense_fixed(keys, funcs, args, scales):
+    """The dense fixed-point GROUP BY -> dict(keys, first_rows, counts, results[G, E]) of the present groups."""
+    k = np.ascontiguousarray(keys, dtype=np.float64)
+    e = len(funcs)
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else np.zeros(1) for a in args]
+    ptrs = (C.c_void_p * e)(*[a.ctypes.data for a in arrs])
+    fa = np.array(funcs, dtype=np.uint32)
+    sc = np.array(scales, dtype=np.int32)
+    lo, hi = (int(k.min()), int(k.max())) if len(k) else (0, 0)
+    groups = hi - lo + 1
+    ok = np.zeros(groups, dtype=np.int64)
+    of = np.zeros(groups, dtype=np.uint64)
+    oc = np.zeros(groups, dtype=np.uint64)
+    res = np.zeros(groups * e, dtype=np.float64)
+    G = lib().orc_dense_fixed(_p(k), len(k), e, _p(fa), ptrs, _p(sc), lo, groups, _p(ok), _p(of), _p(oc), _p(res))
+    return {"keys": ok[:G], "first_rows": of[:G], "counts": oc[:G], "results": res[: G * e].reshape(G, e)}

@@ -110,4 +110,14 @@ int orc_sort_rows(const double* keys, uint32_t key_count, const uint32_t* desc, 
    group of dimension row d (0xffffffff = the row is filtered out); fact_arg may be NULL. */
 int orc_join_aggregate(const uint32_t* fact_key, const uint32_t* fact_arg, uint64_t rows, const uint32_t* dim_key,
                        const uint32_t* dim_group, uint64_t dim_count, uint32_t groups, uint64_t* out_counts, int64_t* out_sums);
+
+/* qe_values_fixed_point for one task (query_exec.c:3893-3983): the scale (or -1) and the largest |v|. */
+int orc_fixed_scale(const double* values, uint64_t count, int32_t* out_scale, double* out_largest);
+/* the smallest scale at which each value alone is whole (-1: none up to 6, or |v| >= 2^31) */
+void orc_fixed_scale_each(const double* values, uint64_t count, int8_t* out);
+/* the dense fixed-point reduce and finalize (aggregate_dense_f64.comp:73-145, query_exec.c:11011-11060);
+   keys as f64 whole numbers; returns the present groups, written in key order */
+uint64_t orc_dense_fixed(const double* keys, uint64_t rows, uint32_t expr_count, const uint32_t* funcs, const double* const* args,
+                         const int32_t* scales, int64_t min_key, uint64_t groups, int64_t* out_keys, uint64_t* out_first_rows,
+                         uint64_t* out_counts, double* out_results);
 #endif

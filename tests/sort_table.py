@@ -8,22 +8,12 @@ SORT_CASES are the test's ORDER BY clauses (bench_query_sort.c:256-268) as (colu
 """
 import numpy as np
 
-GAMMA = np.uint64(0x9E3779B97F4A7C15)
-
-
-def _mix(z):
-    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
-    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
-    return z ^ (z >> np.uint64(31))
+from tests.bench_rng import GAMMA, mix as _mix, rows as _rows
 
 
 def pq_table(rows, narrow=False):
-    with np.errstate(over="ignore"):
-        j = np.arange(rows, dtype=np.uint64) * np.uint64(3)
-        # draw k (k = 1, 2, ...) mixes the state GAMMA * (k + 1)
-        r0 = _mix(GAMMA * (j + np.uint64(2)))
-        r1 = _mix(GAMMA * (j + np.uint64(3)))
-        r2 = _mix(GAMMA * (j + np.uint64(4)))
+    r = _rows(int(GAMMA), rows, 3)
+    r0, r1, r2 = r[:, 0], r[:, 1], r[:, 2]
     hi0 = (r0 >> np.uint64(32))
     if narrow:
         a = (r0 % np.uint64(60000)).astype(np.uint32)
