@@ -627,8 +627,9 @@ __global__ void __launch_bounds__(1024) k_aggregate_dense(CqlLaunch a, DenseLayo
 // Fast path for whole-word keys and argument columns (the full-width u32/i32 case): per-expression
 // metadata unrolled into registers, key and argument vectors loaded together (16 bytes each), 32-bit
 // shared atomics with a carry into the high word as aggregate_dense_native.comp:184-200 does, one
-// private table per warp when the groups are few.
-template <int NE, int NA>
+// private table per warp when the groups are few. KEYARG: the one argument column is the key column
+// itself (GROUP BY amount ... SUM(amount)), read once.
+template <int NE, int NA, bool KEYARG = false>
 __global__ void __launch_bounds__(1024) k_aggregate_dense_wide(CqlLaunch a, uint32_t G, uint32_t group_base, uint64_t rows,
                                                                uint32_t copies, uint32_t copy_words, uint32_t nsum)
 {
@@ -671,25 +672,29 @@ __global__ void __launch_bounds__(1024) k_aggregate_dense_wide(CqlLaunch a, uint
     uint32_t id = (uint32_t)((int)key - min_key - (int)group_base);
     if (id >= G) return;
     atomicAdd(&cnt[id], 1u);
-#pragma unroll
-    for (int e = 0; e < NE; e++)
+    // the argument is the key: its SUM is key x count and its MIN and MAX the key, set at the fold
+    if constexpr (!KEYARG)
     {
-      if (f[e] == FUNC_COUNT) continue;
-      uint32_t x = v[0];
 #pragma unroll
-      for (int c = 1; c < NA; c++)
-        if (ai[e] == (uint32_t)c) x = v[c];
-      if (f[e] == FUNC_SUM || f[e] == FUNC_AVG)
+      for (int e = 0; e < NE; e++)
       {
-        uint32_t* lo = sums + slot[e] * 2 * G;
-        uint32_t old = atomicAdd(&lo[id], x);
-        uint32_t hi_add = ((sg[e] && (int)x < 0) ? 0xffffffffu : 0u) + ((old + x < old) ? 1u : 0u);
-        if (hi_add) atomicAdd(&lo[G + id], hi_add);
+        if (f[e] == FUNC_COUNT) continue;
+        uint32_t x = v[0];
+#pragma unroll
+        for (int c = 1; c < NA; c++)
+          if (ai[e] == (uint32_t)c) x = v[c];
+        if (f[e] == FUNC_SUM || f[e] == FUNC_AVG)
+        {
+          uint32_t* lo = sums + slot[e] * 2 * G;
+          uint32_t old = atomicAdd(&lo[id], x);
+          uint32_t hi_add = ((sg[e] && (int)x < 0) ? 0xffffffffu : 0u) + ((old + x < old) ? 1u : 0u);
+          if (hi_add) atomicAdd(&lo[G + id], hi_add);
+        }
+        else if (f[e] == FUNC_MIN)
+          atomicMin(&mm[slot[e] * 2 * G + id], (int)x);
+        else if (f[e] == FUNC_MAX)
+          atomicMax(&mm[slot[e] * 2 * G + G + id], (int)x);
       }
-      else if (f[e] == FUNC_MIN)
-        atomicMin(&mm[slot[e] * 2 * G + id], (int)x);
-      else if (f[e] == FUNC_MAX)
-        atomicMax(&mm[slot[e] * 2 * G + G + id], (int)x);
     }
   };
 
@@ -698,10 +703,6 @@ __global__ void __launch_bounds__(1024) k_aggregate_dense_wide(CqlLaunch a, uint
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   constexpr int NC = NA > 0 ? NA : 1;
-  // an argument that is the key column itself (GROUP BY amount ... SUM(amount)) is not read twice
-  bool is_key[NC];
-#pragma unroll
-  for (int c = 0; c < NC; c++) is_key[c] = c < NA && a.buf[1 + c] == a.buf[0];
   uint64_t i = t;
   // two key vectors and two vectors of every argument column in flight per thread
   for (; i + stride < vec_count; i += 2 * stride)
@@ -711,7 +712,7 @@ __global__ void __launch_bounds__(1024) k_aggregate_dense_wide(CqlLaunch a, uint
 #pragma unroll
     for (int c = 0; c < NC; c++)
     {
-      if (c < NA && is_key[c])
+      if (KEYARG)
       {
         q0[c] = k0;
         q1[c] = k1;
@@ -758,7 +759,7 @@ __global__ void __launch_bounds__(1024) k_aggregate_dense_wide(CqlLaunch a, uint
     uint4 k0 = __ldcs(kv + i);
     uint4 q0[NC];
 #pragma unroll
-    for (int c = 0; c < NC; c++) q0[c] = c < NA ? (is_key[c] ? k0 : __ldcs((const uint4*)a.buf[1 + c] + i)) : make_uint4(0, 0, 0, 0);
+    for (int c = 0; c < NC; c++) q0[c] = c < NA ? (KEYARG ? k0 : __ldcs((const uint4*)a.buf[1 + c] + i)) : make_uint4(0, 0, 0, 0);
     uint32_t v[NC];
 #pragma unroll
     for (int c = 0; c < NC; c++) v[c] = q0[c].x;
@@ -800,6 +801,15 @@ __global__ void __launch_bounds__(1024) k_aggregate_dense_wide(CqlLaunch a, uint
     for (int e = 0; e < NE; e++)
     {
       uint64_t index = gg * NE + e;
+      if (KEYARG && f[e] != FUNC_COUNT)
+      {
+        uint32_t key = (uint32_t)(min_key + (int)gg);
+        unsigned long long value = sg[e] ? (unsigned long long)(long long)(int)key : (unsigned long long)key;
+        if ((f[e] == FUNC_SUM || f[e] == FUNC_AVG) && index < sum_cap) atomicAdd(&gsum[index], value * count);
+        if (f[e] == FUNC_MIN && index < min_cap) atomicMin(&gmin[index], (int)key);
+        if (f[e] == FUNC_MAX && index < max_cap) atomicMax(&gmax[index], (int)key);
+        continue;
+      }
       if (f[e] == FUNC_SUM || f[e] == FUNC_AVG)
       {
         unsigned long long total = 0;
@@ -828,6 +838,10 @@ __global__ void __launch_bounds__(1024) k_aggregate_dense_wide(CqlLaunch a, uint
 typedef void (*DenseWideFn)(CqlLaunch, uint32_t, uint32_t, uint64_t, uint32_t, uint32_t, uint32_t);
 #define DW_ROW(NE) { k_aggregate_dense_wide<NE, 0>, k_aggregate_dense_wide<NE, 1>, k_aggregate_dense_wide<NE, 2>, k_aggregate_dense_wide<NE, 4> }
 static const DenseWideFn k_dense_wide_table[8][4] = { DW_ROW(1), DW_ROW(2), DW_ROW(3), DW_ROW(4), DW_ROW(5), DW_ROW(6), DW_ROW(7), DW_ROW(8) };
+static const DenseWideFn k_dense_keyarg_table[8] = { k_aggregate_dense_wide<1, 1, true>, k_aggregate_dense_wide<2, 1, true>,
+                                                     k_aggregate_dense_wide<3, 1, true>, k_aggregate_dense_wide<4, 1, true>,
+                                                     k_aggregate_dense_wide<5, 1, true>, k_aggregate_dense_wide<6, 1, true>,
+                                                     k_aggregate_dense_wide<7, 1, true>, k_aggregate_dense_wide<8, 1, true> };
 #undef DW_ROW
 
 // Whole-word key and arguments: one pass per tile of groups that fits shared memory.
@@ -845,6 +859,7 @@ static int launch_dense_wide(const CqlLaunch& a, uint64_t rows, uint32_t exprs, 
     if (f != FUNC_COUNT) na = std::max(na, ((arg_index >> (4 * e)) & 0x3u) + 1);
   }
   DenseWideFn fn = k_dense_wide_table[exprs - 1][na <= 2 ? na : 3];
+  if (na == 1 && a.buf[1] == a.buf[0]) fn = k_dense_keyarg_table[exprs - 1];
   for (uint32_t base = 0; base < groups; base += tile)
   {
     uint32_t G = std::min(tile, groups - base);

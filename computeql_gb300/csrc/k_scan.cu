@@ -9,6 +9,7 @@
 // prefix sum of popc() and one global atomic per CTA and pass. When the output binding has no room
 // for a single row (a COUNT(*) with no row list) every CTA counts privately and adds once at the end.
 #include "cql_internal.cuh"
+#include <math_constants.h>
 #include <algorithm>
 
 #define COLTYPE_U32 1u
@@ -211,6 +212,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_simple(CqlLaunch a, uint6
   uint32_t skip_shift = cql_word(a, 6);
   bool skip_on = cql_word(a, 8) != 0;
   uint32_t chunk_start = cql_word(a, 10);
+  uint32_t row_offset = cql_word(a, 12);   // added to every row written (a dispatch over one range of the table)
   uint32_t leaf_count = s_leaf_count;
 
   uint64_t groups = (rows + ROWS_PER_THREAD - 1) / ROWS_PER_THREAD;
@@ -278,7 +280,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_simple(CqlLaunch a, uint6
       live &= live - 1;
       if (pos < capacity)
       {
-        uint2 pair = make_uint2((uint32_t)(first_row + k), 0u);
+        uint2 pair = make_uint2(row_offset + (uint32_t)(first_row + k), 0u);
         *(uint2*)(out + pos * 2) = pair;
       }
       pos++;
@@ -526,7 +528,90 @@ static int launch_scan_filter(const CqlLaunch& a, uint32_t gws, uint32_t lws, cu
   return 0;
 }
 
+// ---------------------------------------------------------------------------------------------
+// cql_zone_map: the per-chunk min/max of a column (cql_column_ensure_zone_map, the zone maps
+// qe_scan_build_dispatch_ranges prunes with, src/query_exec/query_exec.c:13294-13540). Binding 0 the
+// column, 1 out: f64 (min, max) per chunk, min > max for a chunk without values (all NaN);
+// words 0 rows, 2 type (U32/I32/F32/F64), 3 width (0 stored, 1/2 narrow codes), 4 narrow base,
+// 6 log2 of the chunk rows. One CTA per chunk at a time.
+
+__device__ __forceinline__ double zone_value(const void* col, uint32_t type, uint32_t width, uint32_t base, uint64_t r)
+{
+  if (width == 1 || width == 2)
+  {
+    uint32_t code = width == 1 ? ((const uint8_t*)col)[r] : ((const uint16_t*)col)[r];
+    uint32_t v = base + code;
+    return type == COLTYPE_I32 ? (double)(int)v : (double)v;
+  }
+  if (type == COLTYPE_F64) return ((const double*)col)[r];
+  return widen_word(type, ((const uint32_t*)col)[r]);
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_zone_map(CqlLaunch a, uint64_t rows, uint64_t chunks)
+{
+  __shared__ double s_min[SCAN_THREADS / 32], s_max[SCAN_THREADS / 32];
+  const void* col = a.buf[0];
+  double* out = (double*)a.buf[1];
+  uint32_t type = cql_word(a, 2), width = cql_word(a, 3), base = cql_word(a, 4), log2_rows = cql_word(a, 6);
+  uint64_t chunk_rows = 1ull << log2_rows;
+  for (uint64_t z = blockIdx.x; z < chunks; z += gridDim.x)
+  {
+    uint64_t start = z * chunk_rows, end = min(start + chunk_rows, rows);
+    double lo = CUDART_INF, hi = -CUDART_INF;
+    for (uint64_t r = start + threadIdx.x; r < end; r += SCAN_THREADS)
+    {
+      double v = zone_value(col, type, width, base, r);
+      if (v == v)
+      {
+        lo = fmin(lo, v);
+        hi = fmax(hi, v);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+      lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+      hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31u) == 0)
+    {
+      s_min[threadIdx.x >> 5] = lo;
+      s_max[threadIdx.x >> 5] = hi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+      for (int w = 1; w < SCAN_THREADS / 32; w++)
+      {
+        lo = fmin(lo, s_min[w]);
+        hi = fmax(hi, s_max[w]);
+      }
+      out[z * 2] = lo;
+      out[z * 2 + 1] = hi;
+    }
+    __syncthreads();
+  }
+}
+
+static int launch_zone_map(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t rows = cql_word(a, 0);
+  uint32_t type = cql_word(a, 2), width = cql_word(a, 3), log2_rows = cql_word(a, 6);
+  if (rows == 0) return 0;
+  if (log2_rows < 3 || log2_rows > 30 || width > 2 || (width && type != COLTYPE_U32 && type != COLTYPE_I32)) return (int)cudaErrorInvalidValue;
+  if (type != COLTYPE_U32 && type != COLTYPE_I32 && type != COLTYPE_F32 && type != COLTYPE_F64) return (int)cudaErrorInvalidValue;
+  uint64_t elem = width ? width : (type == COLTYPE_F64 ? 8 : 4);
+  uint64_t chunks = (rows + (1ull << log2_rows) - 1) >> log2_rows;
+  if (a.bytes[0] < rows * elem || a.bytes[1] < chunks * 16) return (int)cudaErrorInvalidValue;
+  k_zone_map<<<cql_stream_grid(chunks, 8), SCAN_THREADS, 0, stream>>>(a, rows, chunks);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
 const CqlKernelDesc cql_kernels_scan[] = {
+  { "cql_zone_map", launch_zone_map },
   { "scan_simple", launch_scan_simple },
   { "scan_filter", launch_scan_filter },
   { nullptr, nullptr },

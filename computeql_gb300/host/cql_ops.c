@@ -14,6 +14,7 @@
 #define QE_AGG_STREAM_DEFAULT_GROUPS 2048
 #define QE_AGG_STREAM_MAX_COLUMNS 4
 #define QE_SIMPLE_SCAN_MAX_LEAVES 8
+#define SCAN_MAX_RANGES 64
 #define QE_SIMPLE_SCAN_ROWS_PER_THREAD 8
 #define QE_MAX_COLUMN_BINDINGS 10
 #define QE_DENSE_STREAM_MAX_ARGS 4
@@ -337,19 +338,31 @@ int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const Cq
     cap_rows = default_cap < rows ? default_cap : rows;
     if (cap_rows == 0) cap_rows = 1;
   }
-  for (uint32_t c = 0; c < QE_MAX_COLUMN_BINDINGS; c++)
+  /* zone-map pruning: the ranges of the table the leaves can match, or one pass with a skip bitmap
+     (qe_scan_build_dispatch_ranges, :13307-13540) */
+  uint64_t chunks = (rows + CQLOPS_ZONEMAP_CHUNK_ROWS - 1) / CQLOPS_ZONEMAP_CHUNK_ROWS;
+  uint64_t ranges[2 * SCAN_MAX_RANGES];
+  uint32_t* skip_bits = (uint32_t*)malloc(((chunks + 31) / 32 + 1) * sizeof(uint32_t));
+  int use_skip = 0;
+  uint64_t pruned_rows = 0;
+  if (!skip_bits) return 0;
+  uint64_t range_count = cqlops_scan_ranges(columns, column_count, leaves, leaf_count, ranges, SCAN_MAX_RANGES, skip_bits, &use_skip,
+                                            &pruned_rows);
+  CqlBuffer* skip_buf = counter; /* the skip binding always holds a buffer; it only counts when enabled */
+  if (use_skip)
   {
-    const CqlColumn* col = &columns[c < column_count ? c : 0];
-    CqlBuffer* b = col->buffer ? col->buffer : leaf_buf; /* a sequence column is never read */
-    cqlcuda_kernel_set_arg_buffer(k, 6 + c, b);
+    skip_buf = pooled("scan_filter_skip", ((chunks + 31) / 32) * sizeof(uint32_t), CQLCUDA_BUFFER_WRITE);
+    if (!skip_buf)
+    {
+      free(skip_bits);
+      return 0;
+    }
   }
   cqlcuda_kernel_set_arg_buffer(k, 0, leaf_buf);
   cqlcuda_kernel_set_arg_buffer(k, 4, counter);
-  cqlcuda_kernel_set_arg_buffer(k, 5, counter); /* skip bitmap off */
-  cqlcuda_kernel_set_arg_u64(k, 0, rows);
-  cqlcuda_kernel_set_arg_u64(k, 3, 0);
-  cqlcuda_kernel_set_arg_u64(k, 4, 0);
-  cqlcuda_kernel_set_arg_u64(k, 5, 0);
+  cqlcuda_kernel_set_arg_buffer(k, 5, skip_buf);
+  cqlcuda_kernel_set_arg_u64(k, 3, use_skip ? 13 : 0);
+  cqlcuda_kernel_set_arg_u64(k, 4, use_skip ? 1 : 0);
   uint64_t result_count = 0;
   CqlBuffer* output = NULL;
   for (int attempt = 0; attempt < 2; attempt++)
@@ -368,14 +381,38 @@ int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const Cq
       cqlcuda_kernel_set_arg_buffer(k, 3, none);
     }
     uint32_t count32[2] = { 0, 0 };
-    CqlBatch* batch = cqlcuda_batch_begin(sizeof(words), sizeof(count32));
+    CqlBatch* batch = cqlcuda_batch_begin(sizeof(words) + (use_skip ? ((chunks + 31) / 32) * 4 : 0), sizeof(count32));
     cqlcuda_batch_buffer_write(batch, leaf_buf, words, sizeof(words));
+    if (use_skip) cqlcuda_batch_buffer_write(batch, skip_buf, skip_bits, ((chunks + 31) / 32) * sizeof(uint32_t));
     cqlcuda_batch_buffer_zero(batch, counter, sizeof(count32));
-    uint64_t threads = (rows + QE_SIMPLE_SCAN_ROWS_PER_THREAD - 1) / QE_SIMPLE_SCAN_ROWS_PER_THREAD;
-    cqlcuda_batch_kernel_execute(batch, k, (uint32_t)threads, QE_GPU_WORKGROUP_SIZE);
+    for (uint64_t r = 0; r < range_count; r++)
+    {
+      /* one dispatch per range: the columns bound from the range's first row, row numbers written
+         from there (a sequence column's values from chunk_start) */
+      uint64_t start = ranges[2 * r], end = ranges[2 * r + 1];
+      for (uint32_t c = 0; c < QE_MAX_COLUMN_BINDINGS; c++)
+      {
+        const CqlColumn* col = &columns[c < column_count ? c : 0];
+        if (!col->buffer)
+        {
+          cqlcuda_kernel_set_arg_buffer(k, 6 + c, leaf_buf); /* a sequence column is never read */
+          continue;
+        }
+        uint64_t elem = col->width == 1 ? 1 : col->width == 2 ? 2 : col->type == CQLOPS_TYPE_F64 ? 8 : 4;
+        uint64_t size = cqlcuda_buffer_size(col->buffer);
+        uint64_t offset = start * elem;
+        cqlcuda_kernel_set_arg_buffer_range(k, 6 + c, col->buffer, offset, size > offset ? size - offset : 0);
+      }
+      cqlcuda_kernel_set_arg_u64(k, 0, end - start);
+      cqlcuda_kernel_set_arg_u64(k, 5, start);
+      cqlcuda_kernel_set_arg_u64(k, 6, start);
+      uint64_t threads = (end - start + QE_SIMPLE_SCAN_ROWS_PER_THREAD - 1) / QE_SIMPLE_SCAN_ROWS_PER_THREAD;
+      cqlcuda_batch_kernel_execute(batch, k, (uint32_t)threads, QE_GPU_WORKGROUP_SIZE);
+    }
     cqlcuda_batch_buffer_read(batch, counter, count32, sizeof(count32));
     if (!cqlcuda_batch_end(batch))
     {
+      free(skip_bits);
       return 0;
     }
     result_count = count32[0];
@@ -385,6 +422,7 @@ int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const Cq
     }
     cap_rows = result_count;
   }
+  free(skip_bits);
   if (want_rows && result_count > cap_rows)
   {
     return 0;

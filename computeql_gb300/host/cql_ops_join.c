@@ -322,6 +322,20 @@ static int probe_totals(const CqlJoinAgg* q, uint32_t core_count, const uint32_t
   return ok;
 }
 
+/* FNV-style hash of a dim row's group values (their f64 bits) */
+static uint64_t group_hash(const CqlJoinAgg* q, uint64_t dim_row)
+{
+  uint64_t h = 1469598103934665603ull;
+  for (uint32_t c = 0; c < q->group_count; c++)
+  {
+    uint64_t bits;
+    memcpy(&bits, &q->dim_group_values[c][dim_row], 8);
+    h = (h ^ bits) * 1099511628211ull;
+    h ^= h >> 29;
+  }
+  return h;
+}
+
 int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* out_groups, uint64_t* out_group_dim_row, double* out_results,
                           uint32_t* out_strategy)
 {
@@ -404,28 +418,43 @@ int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* ou
     free(maxs);
     return 0;
   }
-  /* each (filtered) dim row meets its key's totals and joins the group of its group values (:8619-8720) */
+  /* each (filtered) dim row meets its key's totals and joins the group of its group values (:8619-8720);
+     the group tables start small and grow with the groups found */
   uint64_t visits = q->dim_rows ? q->dim_count : q->dim_table_rows;
-  uint64_t cap = 64;
-  while (cap < visits * 2 + 2) cap *= 2;
-  uint32_t* slots = (uint32_t*)calloc(cap, 4);
+  uint64_t cap = 1024, acc_cap = 256;
   typedef struct
   {
     uint64_t count;
     double sum, mn, mx;
     int seen;
   } Acc;
-  Acc* acc = (Acc*)calloc((visits ? visits : 1) * q->expr_count, sizeof(Acc));
-  uint64_t* rep = (uint64_t*)malloc((visits ? visits : 1) * 8);
+  uint32_t* slots = (uint32_t*)calloc(cap, 4);
+  Acc* acc = (Acc*)calloc(acc_cap * q->expr_count, sizeof(Acc));
+  uint64_t* rep = (uint64_t*)malloc(acc_cap * 8);
   uint64_t groups = 0;
   ok = slots && acc && rep;
-  for (uint64_t v = 0; ok && v < visits; v++)
+  int signed_key = fk->type == CQLOPS_TYPE_I32;
+  uint64_t cand[1024];
+  for (uint64_t v0 = 0; ok && v0 < visits; v0 += 1024)
   {
-    uint64_t dim_row = q->dim_rows ? q->dim_rows[v] : v;
+    /* a branch-free pass keeps the dim rows whose key falls inside the totals */
+    uint64_t vn = visits - v0 < 1024 ? visits - v0 : 1024, nc = 0;
+    for (uint64_t v = v0; v < v0 + vn; v++)
+    {
+      uint64_t dim_row = q->dim_rows ? q->dim_rows[v] : v;
+      uint32_t kw = q->dim_keys[dim_row];
+      int64_t key_value = signed_key ? (int64_t)(int32_t)kw : (int64_t)kw;
+      uint64_t id = by_dim_row ? dim_row : (uint64_t)(key_value - min_key);
+      cand[nc] = dim_row;
+      nc += id < total_groups;
+    }
+    for (uint64_t ci = 0; ok && ci < nc; ci++)
+    {
+    uint64_t dim_row = cand[ci];
     uint32_t kw = q->dim_keys[dim_row];
-    int64_t key_value = fk->type == CQLOPS_TYPE_I32 ? (int64_t)(int32_t)kw : (int64_t)kw;
-    int64_t id = by_dim_row ? (int64_t)dim_row : key_value - min_key;
-    if (id < 0 || (uint64_t)id >= total_groups || counts[id] == 0) continue;
+    int64_t key_value = signed_key ? (int64_t)(int32_t)kw : (int64_t)kw;
+    uint64_t id = by_dim_row ? dim_row : (uint64_t)(key_value - min_key);
+    if (counts[id] == 0) continue;
     uint64_t g = 0;
     if (q->group_count == 0)
     {
@@ -437,28 +466,54 @@ int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* ou
     }
     else
     {
-      uint64_t h = 1469598103934665603ull;
-      for (uint32_t c = 0; c < q->group_count; c++)
-      {
-        uint64_t bits;
-        memcpy(&bits, &q->dim_group_values[c][dim_row], 8);
-        h = (h ^ bits) * 1099511628211ull;
-        h ^= h >> 29;
-      }
-      uint64_t pos = h & (cap - 1);
+      uint64_t pos = group_hash(q, dim_row) & (cap - 1);
       for (;;)
       {
         uint32_t stored = slots[pos];
         if (stored == 0)
         {
+          if (groups == acc_cap)
+          {
+            Acc* a2 = (Acc*)realloc(acc, acc_cap * 2 * q->expr_count * sizeof(Acc));
+            uint64_t* r2 = (uint64_t*)realloc(rep, acc_cap * 2 * 8);
+            if (a2) acc = a2;
+            if (r2) rep = r2;
+            if (!a2 || !r2)
+            {
+              ok = 0;
+              break;
+            }
+            memset(acc + acc_cap * q->expr_count, 0, acc_cap * q->expr_count * sizeof(Acc));
+            acc_cap *= 2;
+          }
           g = groups++;
-          slots[pos] = (uint32_t)g + 1;
           rep[g] = dim_row;
+          if (groups * 2 > cap)
+          {
+            /* rehash into twice the slots */
+            uint32_t* s2 = (uint32_t*)calloc(cap * 2, 4);
+            if (!s2)
+            {
+              ok = 0;
+              break;
+            }
+            free(slots);
+            slots = s2;
+            cap *= 2;
+            for (uint64_t gg = 0; gg < groups; gg++)
+            {
+              uint64_t p2 = group_hash(q, rep[gg]) & (cap - 1);
+              while (slots[p2]) p2 = (p2 + 1) & (cap - 1);
+              slots[p2] = (uint32_t)gg + 1;
+            }
+          }
+          else
+            slots[pos] = (uint32_t)g + 1;
           break;
         }
-        uint64_t cand = rep[stored - 1];
+        uint64_t other = rep[stored - 1];
         int same = 1;
-        for (uint32_t c = 0; c < q->group_count && same; c++) same = q->dim_group_values[c][cand] == q->dim_group_values[c][dim_row];
+        for (uint32_t c = 0; c < q->group_count && same; c++) same = q->dim_group_values[c][other] == q->dim_group_values[c][dim_row];
         if (same)
         {
           g = stored - 1;
@@ -466,6 +521,7 @@ int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* ou
         }
         pos = (pos + 1) & (cap - 1);
       }
+      if (!ok) break;
     }
     uint64_t matches = counts[id];
     for (uint32_t e = 0; e < q->expr_count; e++)
@@ -492,6 +548,7 @@ int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* ou
       a->mn = a->seen ? (value_min < a->mn ? value_min : a->mn) : value_min;
       a->mx = a->seen ? (value_max > a->mx ? value_max : a->mx) : value_max;
       a->seen = 1;
+    }
     }
   }
   if (ok && groups > max_groups) ok = refuse("more groups than the output arrays hold");

@@ -34,7 +34,7 @@ class CqlDict(C.Structure):
 
 class CqlColumn(C.Structure):
     _fields_ = [("type", u32), ("width", u32), ("base", u32), ("has_range", u32), ("rows", u64), ("buffer", P),
-                ("zone_min", dbl), ("zone_max", dbl), ("offsets", P), ("dict", P)]
+                ("zone_min", dbl), ("zone_max", dbl), ("offsets", P), ("dict", P), ("zone_map", P), ("zone_map_chunks", u64)]
 
 
 class CqlLeaf(C.Structure):
@@ -152,6 +152,8 @@ OPS_API = [
     ("cqlops_join_aggregate", C.c_int, [P, u64, P, P, P, P]),
     ("cqlops_sort_rows", C.c_int, [P, u32, P, P, u64, P, u64]),
     ("cqlops_fixed_scale", C.c_int, [P, P, u64, P, P]),
+    ("cqlops_zone_map_build", C.c_int, [P, P, u64]),
+    ("cqlops_scan_ranges", u64, [P, u32, P, u32, P, u64, P, P, P]),
     ("cqlops_group_dense_fixed", C.c_int, [P, u32, P, P, P, u64, u64, P, P, P, P, P, P]),
     ("cqlops_hll_estimate", dbl, [P, u64]),
     ("cqlops_tdigest_percentile", dbl, [P, P, u64, dbl]),

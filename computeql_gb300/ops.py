@@ -14,6 +14,7 @@ from . import native as N
 TYPE_U32, TYPE_U64, TYPE_F32, TYPE_F64, TYPE_I32, TYPE_I64 = 1, 2, 3, 4, 7, 8
 FUNC_COUNT, FUNC_SUM, FUNC_AVG, FUNC_MIN, FUNC_MAX = 0, 1, 2, 3, 4
 CMP_EQ, CMP_LT, CMP_LE, CMP_GT, CMP_GE = 0, 1, 2, 3, 4
+ZONEMAP_CHUNK_ROWS = 8192
 
 _NP_TYPES = {np.dtype(np.uint32): TYPE_U32, np.dtype(np.int32): TYPE_I32, np.dtype(np.float32): TYPE_F32,
              np.dtype(np.float64): TYPE_F64, np.dtype(np.uint64): TYPE_U64, np.dtype(np.int64): TYPE_I64}
@@ -70,13 +71,26 @@ class DeviceBuffer:
 class Column:
     """A device-resident column: its buffer, CQL type, encoding and zone range."""
 
-    def __init__(self, ctype, rows, buffer=None, width=0, base=0, zone=None):
+    def __init__(self, ctype, rows, buffer=None, width=0, base=0, zone=None, zone_map=True):
         self.ctype = ctype
         self.rows = rows
         self.buffer = buffer
         self.width = width
         self.base = base
         self.zone = zone
+        self.zone_map = None
+        if zone_map and buffer is not None and rows and ctype in (TYPE_U32, TYPE_I32, TYPE_F32, TYPE_F64) and width in (0, 1, 2):
+            self.build_zone_map()
+
+    def build_zone_map(self):
+        """The per-chunk min/max scans prune with (8192-row chunks), computed on the GPU."""
+        chunks = (self.rows + ZONEMAP_CHUNK_ROWS - 1) // ZONEMAP_CHUNK_ROWS
+        zm = np.zeros(2 * max(chunks, 1), dtype=np.float64)
+        self.zone_map = None
+        c = self.c()
+        _check(N.load_ops().cqlops_zone_map_build(C.byref(c), N.ptr(zm), chunks), "cqlops_zone_map_build")
+        self.zone_map = zm
+        return zm
 
     @classmethod
     def from_numpy(cls, arr, zone=True, narrow=False):
@@ -117,6 +131,9 @@ class Column:
         col.buffer = self.buffer.handle if self.buffer else None
         if self.zone:
             col.zone_min, col.zone_max = self.zone
+        if self.zone_map is not None:
+            col.zone_map = self.zone_map.ctypes.data
+            col.zone_map_chunks = len(self.zone_map) // 2
         return col
 
 

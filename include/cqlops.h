@@ -69,7 +69,11 @@ typedef struct CqlDict
    many bytes with value = base + code, 3 = a sequence (value = base + row number, nothing stored).
    zone_min/zone_max stand in for the zone map range (qe_column_range_from_zone_map).
    A STRING8 column holds its bytes in `buffer` and (rows + 1) u64 offsets in `offsets`; with a
-   dictionary, `buffer` holds the u32 codes instead and `dict` the values (host side). */
+   dictionary, `buffer` holds the u32 codes instead and `dict` the values (host side).
+   zone_map (optional, host memory) holds the column's zone map: (min, max) as f64 for each chunk of
+   CQLOPS_ZONEMAP_CHUNK_ROWS rows, zone_map_chunks of them (cqlops_zone_map_build fills one); scans
+   prune chunks with it. A sequence column needs none. */
+#define CQLOPS_ZONEMAP_CHUNK_ROWS 8192
 typedef struct CqlColumn
 {
   uint32_t type;
@@ -82,6 +86,8 @@ typedef struct CqlColumn
   double zone_max;
   CqlBuffer* offsets;
   const CqlDict* dict;
+  const double* zone_map;
+  uint64_t zone_map_chunks;
 } CqlColumn;
 
 /* One comparison `column op target` of an AND-only filter (the leaves qe_scan_filter_selected
@@ -257,6 +263,24 @@ typedef struct CqlJoinAgg
    out_results[g*expr_count + e] the aggregate. out_strategy receives 1 (dense) or 2 (probe). */
 int cqlops_join_aggregate(const CqlJoinAgg* query, uint64_t max_groups, uint64_t* out_groups, uint64_t* out_group_dim_row, double* out_results,
                           uint32_t* out_strategy);
+
+/* The zone map of a numeric column (cql_column_ensure_zone_map; the CQL_ZoneMapChunk ranges scans
+   prune with, src/query_exec/query_exec.c:13294-13540): for each chunk of CQLOPS_ZONEMAP_CHUNK_ROWS
+   rows its smallest and largest value as f64 (min > max: a chunk with no values, all NaN) into
+   out_zone_map[2 * chunk], out_chunks = ceil(rows / chunk rows) entries. Computed on the GPU. */
+int cqlops_zone_map_build(const CqlColumn* column, double* out_zone_map, uint64_t out_chunks);
+
+/* The zone-map pruning of an AND of leaves over a table held in one buffer
+   (qe_scan_build_dispatch_ranges, query_exec.c:13307-13540): a chunk is skipped when a leaf proves it
+   empty (qe_zonemap_chunk_is_prunable, :13294-13304); short interior gaps (< 1M rows) are scanned
+   anyway; nothing is pruned unless 10% of the rows go; the kept chunks merge into ranges, or - when
+   the ranges would cost more than one pass (4M rows each) - one range with a skip bitmap. Writes at
+   most max_ranges ranges as (first row, end row) pairs; out_skip_bits (optional, one bit per chunk,
+   ceil(chunks / 32) words) is filled and *out_use_skip set when the bitmap form is chosen. Returns the
+   number of ranges (0 for an empty table). */
+uint64_t cqlops_scan_ranges(const CqlColumn* columns, uint32_t column_count, const CqlLeaf* leaves, uint32_t leaf_count,
+                            uint64_t* out_ranges, uint64_t max_ranges, uint32_t* out_skip_bits, int* out_use_skip,
+                            uint64_t* out_pruned_rows);
 
 /* qe_values_fixed_point (src/query_exec/query_exec.c:3893-3983) over a device column (or the rows of
    a selection): the smallest scale s <= 6 at which every value v is whole, that is (S64)(v*10^s +- 0.5)

@@ -137,7 +137,7 @@ def test_group_by_large_sums_and_scale_6(ops):
     rng = np.random.default_rng(10)
     n = 4_000_000
     key = rng.integers(0, 3, n).astype(np.uint32)
-    v = rng.integers(-2147, 2147, n) + rng.integers(0, 10**6, n) / 1e6      # 6 places, |v * 10^6| < 2^31
+    v = rng.integers(-2**31 + 1, 2**31, n) / 1e6       # the doubles nearest 6-place decimals, |v * 10^6| < 2^31
     _check_group(ops, key, [SUM, AVG, MIN, MAX], [v, v, v, v])
 
 

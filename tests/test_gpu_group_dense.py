@@ -129,3 +129,12 @@ def test_large_sums_wrap_like_two_words(ops):
     key = np.zeros(n, dtype=np.uint32)
     v = np.full(n, 0xFFFFFFF0, dtype=np.uint32)
     _check(ops, key, [SUM], [v])
+
+
+@pytest.mark.parametrize("dtype,lo,hi", [(np.uint32, 0, 10000), (np.int32, -3000, 3000), (np.uint32, 2**31 - 600, 2**31 - 1)])
+def test_key_as_its_own_argument(ops, dtype, lo, hi):
+    # GROUP BY amount ... SUM(amount): the argument column is the key column (read once, SUM = key x count)
+    rng = np.random.default_rng(17)
+    key = rng.integers(lo, hi, 2_000_003).astype(dtype)
+    funcs = [SUM, COUNT, MIN, MAX, AVG]
+    _check(ops, key, funcs, [key if f != COUNT else None for f in funcs])

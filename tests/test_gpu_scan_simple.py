@@ -113,3 +113,63 @@ def test_no_match_and_all_match(ops):
     assert ops.scan_simple([col], [(0, EQ, 6)])[0] == 0
     assert ops.scan_simple([col], [(0, EQ, 5)])[0] == n
     assert ops.scan_simple([col], [(0, LT, -1)])[0] == 0
+
+
+# ---- zone maps and zone-map pruning (cql_zone_map, cqlops_scan_ranges) ----
+
+@pytest.mark.parametrize("dtype,narrow", [(np.uint32, False), (np.int32, True), (np.uint32, True), (np.float32, False), (np.float64, False)])
+def test_zone_map_matches_numpy(ops, dtype, narrow):
+    rng = np.random.default_rng(3)
+    n = 8192 * 37 + 1234
+    if dtype == np.float64:
+        v = rng.normal(size=n)
+        v[8192 * 3: 8192 * 4] = np.nan               # a chunk with no values
+        v[5] = np.nan
+    elif dtype == np.float32:
+        v = rng.normal(size=n).astype(np.float32)
+    else:
+        v = (rng.integers(-100, 100, n) if dtype == np.int32 else rng.integers(0, 60000 if narrow else 2**32, n)).astype(dtype)
+    c = ops.Column.from_numpy(v, narrow=narrow)
+    if narrow:
+        assert c.width in (1, 2)
+    zm = c.zone_map.reshape(-1, 2)
+    for z in range(len(zm)):
+        part = v[z * 8192:(z + 1) * 8192].astype(np.float64)
+        part = part[~np.isnan(part)]
+        if len(part) == 0:
+            assert zm[z, 0] > zm[z, 1]
+        else:
+            assert (zm[z, 0], zm[z, 1]) == (part.min(), part.max())
+
+
+@pytest.mark.parametrize("n", [1_000_000_007, 30_000_000])
+def test_point_lookup_on_sequence_scans_one_chunk(ops, n):
+    ids = ops.Column.sequence(n, 0)
+    for k in (0, 8191, 8192, n // 3, n - 1, n + 5):
+        cnt, rows = ops.scan_simple([ids], [(0, EQ, k)], want_rows=True, max_rows=16)
+        assert cnt == (1 if k < n else 0)
+        assert list(rows) == ([k] if k < n else [])
+    cnt, rows = ops.scan_simple([ids], [(0, GE, n - 20000), (0, LT, n - 100)], want_rows=True)
+    assert cnt == 19900 and np.array_equal(rows, np.arange(n - 20000, n - 100, dtype=np.uint32))
+
+
+def test_pruning_on_a_clustered_column(ops):
+    # a column sorted in blocks: zone maps prune most chunks; results equal the unpruned oracle
+    rng = np.random.default_rng(7)
+    n = 50_000_000
+    ts = np.sort(rng.integers(0, 10**9, n)).astype(np.uint32)
+    val = rng.integers(0, 100, n).astype(np.uint32)
+    tcol, vcol = ops.Column.from_numpy(ts), ops.Column.from_numpy(val)
+    for lo, hi in [(10**8, 10**8 + 10**6), (5 * 10**8, 6 * 10**8), (0, 3000)]:
+        leaves = [(0, GE, lo), (0, LT, hi), (1, LT, 30)]
+        cnt, rows = ops.scan_simple([tcol, vcol], leaves, want_rows=True)
+        m = (ts >= lo) & (ts < hi) & (val < 30)
+        assert cnt == m.sum()
+        assert np.array_equal(rows, np.nonzero(m)[0].astype(np.uint32))
+    # many scattered hits: the skip-bitmap form
+    ts2 = ts.copy()
+    ts2[::400_000] = 7
+    c2 = ops.Column.from_numpy(ts2)
+    cnt, rows = ops.scan_simple([c2], [(0, LE, 7)], want_rows=True)
+    m = ts2 <= 7
+    assert cnt == m.sum() and np.array_equal(rows, np.nonzero(m)[0].astype(np.uint32))
