@@ -338,7 +338,7 @@ def run_e2e(args, native, ops, t, queries, lib):
         lib.cqlcuda_buffer_read(col.buffer.handle, C.c_void_p(h.data_ptr()), n * 4)
         host[name] = h
     h2d = 3 * n * 4
-    times = []
+    times, uploads = [], []
     for i in range(args.warmup + max(2, args.steps // 2)):
         t0 = time.perf_counter()
         batch = lib.cqlcuda_batch_begin(h2d, 0)
@@ -346,16 +346,19 @@ def run_e2e(args, native, ops, t, queries, lib):
             lib.cqlcuda_batch_buffer_write(batch, getattr(t, name).buffer.handle, C.c_void_p(host[name].data_ptr()), n * 4)
         if not lib.cqlcuda_batch_end(batch):
             raise RuntimeError("e2e upload failed: " + native.last_error())
+        t1 = time.perf_counter()
         for _, _, q in queries:
             q()
         dt = time.perf_counter() - t0
         if i >= args.warmup:
             times.append(dt)
+            uploads.append(t1 - t0)
     ms = statistics.median(times) * 1e3
+    upload_ms = statistics.median(uploads) * 1e3
     # results read back per step: partials/counters/group arrays of the queries (a few hundred KB)
     d2h = 2048 * 3 * 8 + 8 + 50 * 4 * 8 + 10000 * 4 * 8 + 8 + 2 * 8 + 20 * 2 * 8
     return {"value": len(queries) * n / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h}
+            "d2h_bytes_per_step": d2h, "upload_ms": upload_ms, "h2d_GBps": h2d / (upload_ms / 1e3) / 1e9}
 
 
 if __name__ == "__main__":

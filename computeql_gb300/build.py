@@ -27,7 +27,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["runtime.cu", "k_aggregate.cu", "k_scan.cu", "k_hash.cu", "k_join.cu", "k_sort.cu", "k_fixed.cu"]
-C_SOURCES = ["cql_ops.c", "cql_program.c", "cql_codegen.c", "cql_ops_filter.c", "cql_ops_hash.c", "cql_ops_join.c", "cql_ops_sort.c", "cql_ops_fixed.c", "cql_zonemap.c"]
+C_SOURCES = ["cql_ops.c", "cql_program.c", "cql_codegen.c", "cql_ops_filter.c", "cql_ops_hash.c", "cql_ops_join.c", "cql_ops_sort.c", "cql_ops_fixed.c", "cql_zonemap.c", "cql_pool.c"]
 
 LIB_CUDA = os.path.join(PKG, "libcqlcuda.so")
 LIB_OPS = os.path.join(PKG, "libcqlops.so")
@@ -95,7 +95,7 @@ def build(verbose=False, ptxas_verbose=False):
               "-Xlinker", "-rpath=" + cudart_dir])
     cobjs = [_compile_c(os.path.join(HOST, f)) for f in C_SOURCES]
     if _stale(LIB_OPS, cobjs + [LIB_CUDA]):
-        _run(["gcc", "-shared", "-o", LIB_OPS, *cobjs, "-L", PKG, "-lcqlcuda", "-Wl,-rpath,$ORIGIN", "-lm"])
+        _run(["gcc", "-shared", "-o", LIB_OPS, *cobjs, "-L", PKG, "-lcqlcuda", "-Wl,-rpath,$ORIGIN", "-lm", "-lpthread"])
     return LIB_CUDA, LIB_OPS
 
 

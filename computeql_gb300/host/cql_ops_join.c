@@ -12,6 +12,7 @@
  *                         meets its key's totals and is folded into a group of its group columns on the host
  */
 #include "cqlops.h"
+#include "cql_pool.h"
 
 #include <math.h>
 #include <stdio.h>
@@ -322,6 +323,40 @@ static int probe_totals(const CqlJoinAgg* q, uint32_t core_count, const uint32_t
   return ok;
 }
 
+/* the visit pre-pass: one slice of dim rows per task, the kept ones written at the slice's start */
+#define VISIT_SLICE 32768u
+typedef struct
+{
+  const CqlJoinAgg* q;
+  int signed_key, by_dim_row;
+  int64_t min_key;
+  uint64_t total_groups;
+  const uint64_t* counts;
+  uint64_t visits;
+  uint32_t tasks;
+  uint32_t* cand;
+  uint64_t* found;
+} VisitCtx;
+
+static void visit_task(void* p, uint32_t task)
+{
+  VisitCtx* c = (VisitCtx*)p;
+  uint64_t v0 = (uint64_t)task * VISIT_SLICE;
+  uint64_t v1 = v0 + VISIT_SLICE < c->visits ? v0 + VISIT_SLICE : c->visits;
+  uint32_t* out = c->cand + v0;
+  uint64_t n = 0;
+  for (uint64_t v = v0; v < v1; v++)
+  {
+    uint64_t dim_row = c->q->dim_rows ? c->q->dim_rows[v] : v;
+    uint32_t kw = c->q->dim_keys[dim_row];
+    int64_t key_value = c->signed_key ? (int64_t)(int32_t)kw : (int64_t)kw;
+    uint64_t id = c->by_dim_row ? dim_row : (uint64_t)(key_value - c->min_key);
+    out[n] = (uint32_t)dim_row;
+    n += id < c->total_groups && c->counts[id < c->total_groups ? id : 0] != 0;
+  }
+  c->found[task] = n;
+}
+
 /* FNV-style hash of a dim row's group values (their f64 bits) */
 static uint64_t group_hash(const CqlJoinAgg* q, uint64_t dim_row)
 {
@@ -434,121 +469,117 @@ int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* ou
   uint64_t groups = 0;
   ok = slots && acc && rep;
   int signed_key = fk->type == CQLOPS_TYPE_I32;
-  uint64_t cand[1024];
-  for (uint64_t v0 = 0; ok && v0 < visits; v0 += 1024)
+  /* the dim rows whose key falls inside the totals, found in parallel slices and kept in dim-row order */
+  VisitCtx vc = { q, signed_key, by_dim_row, min_key, total_groups, counts, visits, 0, NULL, NULL };
+  vc.tasks = (uint32_t)((visits + VISIT_SLICE - 1) / VISIT_SLICE);
+  vc.cand = (uint32_t*)malloc((visits ? visits : 1) * sizeof(uint32_t));
+  vc.found = (uint64_t*)malloc((vc.tasks ? vc.tasks : 1) * sizeof(uint64_t));
+  ok = ok && vc.cand && vc.found;
+  if (ok) cql_parallel_for(vc.tasks, visit_task, &vc);
+  for (uint32_t task = 0; ok && task < vc.tasks; task++)
   {
-    /* a branch-free pass keeps the dim rows whose key falls inside the totals */
-    uint64_t vn = visits - v0 < 1024 ? visits - v0 : 1024, nc = 0;
-    for (uint64_t v = v0; v < v0 + vn; v++)
+    const uint32_t* cand = vc.cand + (uint64_t)task * VISIT_SLICE;
+    uint64_t nc = vc.found[task];
+    for (uint64_t ci = 0; ok && ci < nc; ci++)
     {
-      uint64_t dim_row = q->dim_rows ? q->dim_rows[v] : v;
+      uint64_t dim_row = cand[ci];
       uint32_t kw = q->dim_keys[dim_row];
       int64_t key_value = signed_key ? (int64_t)(int32_t)kw : (int64_t)kw;
       uint64_t id = by_dim_row ? dim_row : (uint64_t)(key_value - min_key);
-      cand[nc] = dim_row;
-      nc += id < total_groups;
-    }
-    for (uint64_t ci = 0; ok && ci < nc; ci++)
-    {
-    uint64_t dim_row = cand[ci];
-    uint32_t kw = q->dim_keys[dim_row];
-    int64_t key_value = signed_key ? (int64_t)(int32_t)kw : (int64_t)kw;
-    uint64_t id = by_dim_row ? dim_row : (uint64_t)(key_value - min_key);
-    if (counts[id] == 0) continue;
-    uint64_t g = 0;
-    if (q->group_count == 0)
-    {
-      if (groups == 0)
+      uint64_t g = 0;
+      if (q->group_count == 0)
       {
-        groups = 1;
-        rep[0] = dim_row;
-      }
-    }
-    else
-    {
-      uint64_t pos = group_hash(q, dim_row) & (cap - 1);
-      for (;;)
-      {
-        uint32_t stored = slots[pos];
-        if (stored == 0)
+        if (groups == 0)
         {
-          if (groups == acc_cap)
-          {
-            Acc* a2 = (Acc*)realloc(acc, acc_cap * 2 * q->expr_count * sizeof(Acc));
-            uint64_t* r2 = (uint64_t*)realloc(rep, acc_cap * 2 * 8);
-            if (a2) acc = a2;
-            if (r2) rep = r2;
-            if (!a2 || !r2)
-            {
-              ok = 0;
-              break;
-            }
-            memset(acc + acc_cap * q->expr_count, 0, acc_cap * q->expr_count * sizeof(Acc));
-            acc_cap *= 2;
-          }
-          g = groups++;
-          rep[g] = dim_row;
-          if (groups * 2 > cap)
-          {
-            /* rehash into twice the slots */
-            uint32_t* s2 = (uint32_t*)calloc(cap * 2, 4);
-            if (!s2)
-            {
-              ok = 0;
-              break;
-            }
-            free(slots);
-            slots = s2;
-            cap *= 2;
-            for (uint64_t gg = 0; gg < groups; gg++)
-            {
-              uint64_t p2 = group_hash(q, rep[gg]) & (cap - 1);
-              while (slots[p2]) p2 = (p2 + 1) & (cap - 1);
-              slots[p2] = (uint32_t)gg + 1;
-            }
-          }
-          else
-            slots[pos] = (uint32_t)g + 1;
-          break;
+          groups = 1;
+          rep[0] = dim_row;
         }
-        uint64_t other = rep[stored - 1];
-        int same = 1;
-        for (uint32_t c = 0; c < q->group_count && same; c++) same = q->dim_group_values[c][other] == q->dim_group_values[c][dim_row];
-        if (same)
-        {
-          g = stored - 1;
-          break;
-        }
-        pos = (pos + 1) & (cap - 1);
-      }
-      if (!ok) break;
-    }
-    uint64_t matches = counts[id];
-    for (uint32_t e = 0; e < q->expr_count; e++)
-    {
-      Acc* a = &acc[g * q->expr_count + e];
-      a->count += matches;
-      uint32_t f = q->funcs[e];
-      if (f == CQLOPS_FUNC_COUNT) continue;
-      double value_sum, value_min, value_max;
-      if (q->dim_args && q->dim_args[e])
-      {
-        double value = q->dim_args[e][dim_row];
-        value_sum = value * (double)matches;
-        value_min = value_max = value;
       }
       else
       {
-        uint64_t slot = (uint64_t)id * core_count + core_of_expr[e];
-        value_sum = (double)sums[slot];
-        value_min = (double)mins[slot];
-        value_max = (double)maxs[slot];
+        uint64_t pos = group_hash(q, dim_row) & (cap - 1);
+        for (;;)
+        {
+          uint32_t stored = slots[pos];
+          if (stored == 0)
+          {
+            if (groups == acc_cap)
+            {
+              Acc* a2 = (Acc*)realloc(acc, acc_cap * 2 * q->expr_count * sizeof(Acc));
+              uint64_t* r2 = (uint64_t*)realloc(rep, acc_cap * 2 * 8);
+              if (a2) acc = a2;
+              if (r2) rep = r2;
+              if (!a2 || !r2)
+              {
+                ok = 0;
+                break;
+              }
+              memset(acc + acc_cap * q->expr_count, 0, acc_cap * q->expr_count * sizeof(Acc));
+              acc_cap *= 2;
+            }
+            g = groups++;
+            rep[g] = dim_row;
+            if (groups * 2 > cap)
+            {
+              /* rehash into twice the slots */
+              uint32_t* s2 = (uint32_t*)calloc(cap * 2, 4);
+              if (!s2)
+              {
+                ok = 0;
+                break;
+              }
+              free(slots);
+              slots = s2;
+              cap *= 2;
+              for (uint64_t gg = 0; gg < groups; gg++)
+              {
+                uint64_t p2 = group_hash(q, rep[gg]) & (cap - 1);
+                while (slots[p2]) p2 = (p2 + 1) & (cap - 1);
+                slots[p2] = (uint32_t)gg + 1;
+              }
+            }
+            else
+              slots[pos] = (uint32_t)g + 1;
+            break;
+          }
+          uint64_t other = rep[stored - 1];
+          int same = 1;
+          for (uint32_t c = 0; c < q->group_count && same; c++) same = q->dim_group_values[c][other] == q->dim_group_values[c][dim_row];
+          if (same)
+          {
+            g = stored - 1;
+            break;
+          }
+          pos = (pos + 1) & (cap - 1);
+        }
+        if (!ok) break;
       }
-      a->sum += value_sum;
-      a->mn = a->seen ? (value_min < a->mn ? value_min : a->mn) : value_min;
-      a->mx = a->seen ? (value_max > a->mx ? value_max : a->mx) : value_max;
-      a->seen = 1;
-    }
+      uint64_t matches = counts[id];
+      for (uint32_t e = 0; e < q->expr_count; e++)
+      {
+        Acc* a = &acc[g * q->expr_count + e];
+        a->count += matches;
+        uint32_t f = q->funcs[e];
+        if (f == CQLOPS_FUNC_COUNT) continue;
+        double value_sum, value_min, value_max;
+        if (q->dim_args && q->dim_args[e])
+        {
+          double value = q->dim_args[e][dim_row];
+          value_sum = value * (double)matches;
+          value_min = value_max = value;
+        }
+        else
+        {
+          uint64_t slot = (uint64_t)id * core_count + core_of_expr[e];
+          value_sum = (double)sums[slot];
+          value_min = (double)mins[slot];
+          value_max = (double)maxs[slot];
+        }
+        a->sum += value_sum;
+        a->mn = a->seen ? (value_min < a->mn ? value_min : a->mn) : value_min;
+        a->mx = a->seen ? (value_max > a->mx ? value_max : a->mx) : value_max;
+        a->seen = 1;
+      }
     }
   }
   if (ok && groups > max_groups) ok = refuse("more groups than the output arrays hold");
@@ -575,6 +606,8 @@ int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* ou
     *out_groups = groups;
     if (out_strategy) *out_strategy = by_dim_row ? 2u : 1u;
   }
+  free(vc.cand);
+  free(vc.found);
   free(slots);
   free(acc);
   free(rep);

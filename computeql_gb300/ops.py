@@ -85,10 +85,10 @@ class Column:
     def build_zone_map(self):
         """The per-chunk min/max scans prune with (8192-row chunks), computed on the GPU."""
         chunks = (self.rows + ZONEMAP_CHUNK_ROWS - 1) // ZONEMAP_CHUNK_ROWS
-        zm = np.zeros(2 * max(chunks, 1), dtype=np.float64)
+        zm = np.zeros(2 * (chunks + 1), dtype=np.float64)      # the chunks, then the summary pair
         self.zone_map = None
         c = self.c()
-        _check(N.load_ops().cqlops_zone_map_build(C.byref(c), N.ptr(zm), chunks), "cqlops_zone_map_build")
+        _check(N.load_ops().cqlops_zone_map_build(C.byref(c), N.ptr(zm), chunks + 1), "cqlops_zone_map_build")
         self.zone_map = zm
         return zm
 
@@ -133,7 +133,7 @@ class Column:
             col.zone_min, col.zone_max = self.zone
         if self.zone_map is not None:
             col.zone_map = self.zone_map.ctypes.data
-            col.zone_map_chunks = len(self.zone_map) // 2
+            col.zone_map_chunks = len(self.zone_map) // 2 - 1
         return col
 
 
@@ -172,10 +172,10 @@ def group_dense(key, funcs, args):
     e = len(funcs)
     lo, hi = key.zone
     max_groups = int(hi - lo) + 1
-    counts = np.zeros(max_groups, dtype=np.uint64)
-    sums = np.zeros(max_groups * e, dtype=np.int64)
-    mins = np.zeros(max_groups * e, dtype=np.int64)
-    maxs = np.zeros(max_groups * e, dtype=np.int64)
+    counts = np.empty(max_groups, dtype=np.uint64)
+    sums = np.empty(max_groups * e, dtype=np.int64)
+    mins = np.empty(max_groups * e, dtype=np.int64)
+    maxs = np.empty(max_groups * e, dtype=np.int64)
     kc = key.c()
     # the operator layer tells argument columns apart by identity: one descriptor per distinct column
     structs = {}
@@ -321,11 +321,11 @@ def fused_group(program, key_names, agg_names, max_groups=1 << 16):
     total = C.c_uint64()
     kmin = (C.c_int64 * 3)()
     krange = (C.c_uint32 * 3)()
-    counts = np.zeros(max_groups, dtype=np.uint64)
-    minrow = np.zeros(max_groups, dtype=np.uint64)
-    sums = np.zeros(max_groups * max(ac, 1), dtype=np.int64)
-    mins = np.zeros(max_groups * max(ac, 1), dtype=np.int64)
-    maxs = np.zeros(max_groups * max(ac, 1), dtype=np.int64)
+    counts = np.empty(max_groups, dtype=np.uint64)
+    minrow = np.empty(max_groups, dtype=np.uint64)
+    sums = np.empty(max_groups * max(ac, 1), dtype=np.int64)
+    mins = np.empty(max_groups * max(ac, 1), dtype=np.int64)
+    maxs = np.empty(max_groups * max(ac, 1), dtype=np.int64)
     _check(N.load_ops().cqlops_fused_filter_group(C.byref(program.prog), program._cols, keys, kc, aggs, ac, max_groups, C.byref(total), kmin,
                                                   krange, N.ptr(counts), N.ptr(minrow), N.ptr(sums), N.ptr(mins), N.ptr(maxs)),
            "cqlops_fused_filter_group")
@@ -350,9 +350,9 @@ def group_hash(keys, funcs, args, params=None, group_hint=0, path=0, max_groups=
     pa = np.array(params if params is not None else [0.5] * e, dtype=np.float64)
     rows = keys[0].rows if keys else next(a.rows for a in args if a is not None)
     mg = max_groups if max_groups is not None else rows
-    repr_row = np.zeros(max(mg, 1), dtype=np.uint64)
-    counts = np.zeros(max(mg, 1), dtype=np.uint64)
-    results = np.zeros(max(mg, 1) * e, dtype=np.float64)
+    repr_row = np.empty(max(mg, 1), dtype=np.uint64)
+    counts = np.empty(max(mg, 1), dtype=np.uint64)
+    results = np.empty(max(mg, 1) * e, dtype=np.float64)
     g = C.c_uint64()
     used = C.c_uint32()
     _check(N.load_ops().cqlops_group_hash(kcols, kc, e, N.ptr(fa), arg_ptrs, N.ptr(pa), group_hint, path, mg, C.byref(g), N.ptr(repr_row),
@@ -367,7 +367,7 @@ def hash_join(build_key, probe_key, left=False, hint_pairs=0, want_pairs=True):
     count = C.c_uint64()
     cap = (max(probe_key.rows, build_key.rows) + probe_key.rows) * 4 if want_pairs else 0
     while True:
-        out = np.zeros(max(cap, 1) * 2, dtype=np.uint32) if want_pairs else None
+        out = np.empty(max(cap, 1) * 2, dtype=np.uint32) if want_pairs else None
         _check(N.load_ops().cqlops_hash_join(C.byref(bc), C.byref(pc_), 1 if left else 0, hint_pairs, C.byref(count),
                                              N.ptr(out) if want_pairs else None, cap), "cqlops_hash_join")
         n = count.value
@@ -398,8 +398,8 @@ def join_aggregate(fact_key, funcs, fact_args, dim_keys, dim_rows=None, group_va
                      C.addressof(gv) if gv_keep else None, strategy)
     visits = len(dr) if dr is not None else len(dk)
     mg = max(visits, 1)
-    dim_row = np.zeros(mg, dtype=np.uint64)
-    results = np.zeros(mg * e, dtype=np.float64)
+    dim_row = np.empty(mg, dtype=np.uint64)
+    results = np.empty(mg * e, dtype=np.float64)
     groups = C.c_uint64()
     used = C.c_uint32()
     _check(N.load_ops().cqlops_join_aggregate(C.byref(q), mg, C.byref(groups), N.ptr(dim_row), N.ptr(results), C.byref(used)),
@@ -422,7 +422,7 @@ def sort_rows(keys, desc=None, selection=None, count=None):
         sel = selection.handle
     else:
         n, sel = keys[0].rows, None
-    out = np.zeros(max(n, 1), dtype=np.uint32)
+    out = np.empty(max(n, 1), dtype=np.uint32)
     _check(N.load_ops().cqlops_sort_rows(arr, kc, N.ptr(d), sel, n, N.ptr(out), n), "cqlops_sort_rows")
     return out[:n]
 
@@ -449,10 +449,10 @@ def group_dense_fixed(key, funcs, args, selection=None, count=None, max_groups=6
     arr = (C.c_void_p * e)(*[C.addressof(s) if s is not None else None for s in structs])
     fa = np.array(funcs, dtype=np.uint32)
     n = key.rows if selection is None else (selection.nbytes // 4 if count is None else count)
-    keys = np.zeros(max_groups, dtype=np.int64)
-    first = np.zeros(max_groups, dtype=np.uint64)
-    counts = np.zeros(max_groups, dtype=np.uint64)
-    results = np.zeros(max_groups * e, dtype=np.float64)
+    keys = np.empty(max_groups, dtype=np.int64)
+    first = np.empty(max_groups, dtype=np.uint64)
+    counts = np.empty(max_groups, dtype=np.uint64)
+    results = np.empty(max_groups * e, dtype=np.float64)
     scales = np.zeros(e, dtype=np.int32)
     groups = C.c_uint64()
     _check(N.load_ops().cqlops_group_dense_fixed(C.byref(kc), e, N.ptr(fa), arr, selection.handle if selection is not None else None,

@@ -71,8 +71,9 @@ typedef struct CqlDict
    A STRING8 column holds its bytes in `buffer` and (rows + 1) u64 offsets in `offsets`; with a
    dictionary, `buffer` holds the u32 codes instead and `dict` the values (host side).
    zone_map (optional, host memory) holds the column's zone map: (min, max) as f64 for each chunk of
-   CQLOPS_ZONEMAP_CHUNK_ROWS rows, zone_map_chunks of them (cqlops_zone_map_build fills one); scans
-   prune chunks with it. A sequence column needs none. */
+   CQLOPS_ZONEMAP_CHUNK_ROWS rows, zone_map_chunks of them, then one more pair: the largest chunk min
+   and the smallest chunk max (cqlops_zone_map_build fills it); scans prune chunks with it. A
+   sequence column needs none. */
 #define CQLOPS_ZONEMAP_CHUNK_ROWS 8192
 typedef struct CqlColumn
 {
@@ -267,7 +268,8 @@ int cqlops_join_aggregate(const CqlJoinAgg* query, uint64_t max_groups, uint64_t
 /* The zone map of a numeric column (cql_column_ensure_zone_map; the CQL_ZoneMapChunk ranges scans
    prune with, src/query_exec/query_exec.c:13294-13540): for each chunk of CQLOPS_ZONEMAP_CHUNK_ROWS
    rows its smallest and largest value as f64 (min > max: a chunk with no values, all NaN) into
-   out_zone_map[2 * chunk], out_chunks = ceil(rows / chunk rows) entries. Computed on the GPU. */
+   out_zone_map[2 * chunk], then the largest min and the smallest max over the chunks with values;
+   out_chunks >= ceil(rows / chunk rows) + 1 entries. Computed on the GPU. */
 int cqlops_zone_map_build(const CqlColumn* column, double* out_zone_map, uint64_t out_chunks);
 
 /* The zone-map pruning of an AND of leaves over a table held in one buffer

@@ -138,3 +138,15 @@ def test_key_as_its_own_argument(ops, dtype, lo, hi):
     key = rng.integers(lo, hi, 2_000_003).astype(dtype)
     funcs = [SUM, COUNT, MIN, MAX, AVG]
     _check(ops, key, funcs, [key if f != COUNT else None for f in funcs])
+
+
+@pytest.mark.parametrize("arg_range", [(0, 50), (-1000, 1000), (0, 100_000), (0, 2**31 - 1)])
+@pytest.mark.parametrize("groups", [7, 10000])
+def test_count_and_sum_of_one_argument(ops, arg_range, groups):
+    # COUNT/SUM/AVG of one column: packed into one shared word per group when a CTA cannot carry past 2^31
+    rng = np.random.default_rng(groups + arg_range[1])
+    n = 20_000_003
+    key = rng.integers(0, groups, n).astype(np.uint32)
+    arg = rng.integers(arg_range[0], arg_range[1], n)
+    arg = arg.astype(np.int32 if arg_range[0] < 0 else np.uint32)
+    _check(ops, key, [COUNT, SUM, AVG, SUM], [None, arg, arg, arg])

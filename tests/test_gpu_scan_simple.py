@@ -132,7 +132,10 @@ def test_zone_map_matches_numpy(ops, dtype, narrow):
     c = ops.Column.from_numpy(v, narrow=narrow)
     if narrow:
         assert c.width in (1, 2)
-    zm = c.zone_map.reshape(-1, 2)
+    zm = c.zone_map.reshape(-1, 2)[:-1]
+    summary = c.zone_map[-2:]
+    has = zm[:, 0] <= zm[:, 1]
+    assert (summary[0], summary[1]) == (zm[has, 0].max(), zm[has, 1].min())
     for z in range(len(zm)):
         part = v[z * 8192:(z + 1) * 8192].astype(np.float64)
         part = part[~np.isnan(part)]

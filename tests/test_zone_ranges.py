@@ -27,9 +27,13 @@ def col(N, rows, ctype=1, width=0, base=0, zone_map=None, keep=None):
     c.type, c.width, c.base, c.rows = ctype, width, base, rows
     c.buffer = None if width == 3 else 1   # never dereferenced on the host
     if zone_map is not None:
+        pairs = zone_map.reshape(-1, 2)
+        has = pairs[:, 0] <= pairs[:, 1]
+        summary = [pairs[has, 0].max(), pairs[has, 1].min()] if has.any() else [-np.inf, np.inf]
+        zone_map = np.concatenate([zone_map, summary])      # the chunks, then (largest min, smallest max)
         keep.append(zone_map)
         c.zone_map = zone_map.ctypes.data
-        c.zone_map_chunks = len(zone_map) // 2
+        c.zone_map_chunks = len(zone_map) // 2 - 1
     return c
 
 
@@ -113,6 +117,15 @@ def test_many_ranges_become_a_skip_bitmap(N):
     assert skip == 1 and r == [(0, rows)]
     for z in range(chunks):
         assert bool(bits[z >> 5] & (1 << (z & 31))) == (z not in kept)
+
+
+def test_summary_short_cuts_a_leaf_that_prunes_nothing(N):
+    keep = []
+    rows = 1_000_000
+    chunks = (rows + CHUNK - 1) // CHUNK
+    zm = np.tile([0.0, 99.0], chunks)
+    r, skip, pruned, _ = ranges(N, [col(N, rows, zone_map=zm, keep=keep)], [(0, LT, 2.0)])
+    assert r == [(0, rows)] and pruned == 0
 
 
 def test_everything_pruned(N):
