@@ -835,80 +835,6 @@ __global__ void __launch_bounds__(1024) k_aggregate_dense_wide(CqlLaunch a, uint
   }
 }
 
-// COUNT and SUM of one argument column packed in one 64-bit shared word per group: the count in the
-// low half, the argument's running sum in the high half, one shared atomic per row. Taken only when a
-// CTA can never carry its high half past 2^31 (its rows x the largest |argument| < 2^31), so the
-// high half is the exact sum of the CTA's rows, sign-extended for an i32 argument.
-template <bool SIGNED>
-__global__ void __launch_bounds__(1024) k_aggregate_dense_packed(CqlLaunch a, uint32_t G, uint32_t group_base, uint64_t rows,
-                                                                 uint32_t copies, uint32_t copy_words, uint32_t exprs)
-{
-  extern __shared__ __align__(16) unsigned long long smem64[];
-  uint32_t func_codes = cql_word(a, 4);
-  int min_key = (int)cql_word(a, 10);
-  for (uint32_t i = threadIdx.x; i < copies * copy_words; i += blockDim.x) smem64[i] = 0ull;
-  __syncthreads();
-  unsigned long long* packed = smem64 + ((threadIdx.x >> 5) % copies) * copy_words;
-  auto row = [&](uint32_t key, uint32_t x) {
-    uint32_t id = (uint32_t)((int)key - min_key - (int)group_base);
-    if (id < G) atomicAdd(&packed[id], ((unsigned long long)x << 32) | 1ull);
-  };
-  const uint4* kv = (const uint4*)a.buf[0];
-  const uint4* av = (const uint4*)a.buf[1];
-  uint64_t vec_count = rows / 4;
-  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  uint64_t i = t;
-  for (; i + stride < vec_count; i += 2 * stride)
-  {
-    uint4 k0 = __ldcs(kv + i), k1 = __ldcs(kv + i + stride);
-    uint4 q0 = __ldcs(av + i), q1 = __ldcs(av + i + stride);
-    row(k0.x, q0.x);
-    row(k0.y, q0.y);
-    row(k0.z, q0.z);
-    row(k0.w, q0.w);
-    row(k1.x, q1.x);
-    row(k1.y, q1.y);
-    row(k1.z, q1.z);
-    row(k1.w, q1.w);
-  }
-  for (; i < vec_count; i += stride)
-  {
-    uint4 k0 = __ldcs(kv + i), q0 = __ldcs(av + i);
-    row(k0.x, q0.x);
-    row(k0.y, q0.y);
-    row(k0.z, q0.z);
-    row(k0.w, q0.w);
-  }
-  uint64_t tail = vec_count * 4;
-  if (t < rows - tail) row(((const uint32_t*)a.buf[0])[tail + t], ((const uint32_t*)a.buf[1])[tail + t]);
-  __syncthreads();
-  uint32_t* info = (uint32_t*)a.buf[5];
-  unsigned long long* gsum = (unsigned long long*)a.buf[6];
-  uint64_t info_cap = a.bytes[5] / 4, sum_cap = a.bytes[6] / 8;
-  for (uint32_t g = threadIdx.x; g < G; g += blockDim.x)
-  {
-    uint32_t count = 0;
-    unsigned long long total = 0;
-    for (uint32_t c = 0; c < copies; c++)
-    {
-      unsigned long long w = smem64[c * copy_words + g];
-      count += (uint32_t)w;
-      uint32_t hi = (uint32_t)(w >> 32);
-      total += SIGNED ? (unsigned long long)(long long)(int)hi : (unsigned long long)hi;
-    }
-    if (count == 0) continue;
-    uint64_t gg = (uint64_t)group_base + g;
-    if (gg * 2 + 1 < info_cap) atomicAdd(&info[gg * 2 + 1], count);
-    for (uint32_t e = 0; e < exprs; e++)
-    {
-      uint32_t f = (func_codes >> (4 * e)) & 0xfu;
-      uint64_t index = gg * exprs + e;
-      if ((f == FUNC_SUM || f == FUNC_AVG) && index < sum_cap) atomicAdd(&gsum[index], total);
-    }
-  }
-}
-
 typedef void (*DenseWideFn)(CqlLaunch, uint32_t, uint32_t, uint64_t, uint32_t, uint32_t, uint32_t);
 #define DW_ROW(NE) { k_aggregate_dense_wide<NE, 0>, k_aggregate_dense_wide<NE, 1>, k_aggregate_dense_wide<NE, 2>, k_aggregate_dense_wide<NE, 4> }
 static const DenseWideFn k_dense_wide_table[8][4] = { DW_ROW(1), DW_ROW(2), DW_ROW(3), DW_ROW(4), DW_ROW(5), DW_ROW(6), DW_ROW(7), DW_ROW(8) };
@@ -1039,58 +965,7 @@ static int launch_aggregate_global_f32(const CqlLaunch& a, uint32_t gws, uint32_
   return launch_aggregate_global(b, gws, lws, stream);
 }
 
-// cql_dense_count_sum: aggregate_dense_native's bindings and words, for a full-width key and ONE
-// distinct full-width argument column under COUNT/SUM/AVG only, with word 15 (the native kernel's
-// chunk start, which such an argument never needs) holding the argument's largest magnitude. Runs the
-// packed kernel when no CTA can carry past 2^31, else the native kernel.
-static int launch_dense_count_sum(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
-{
-  uint64_t rows = cql_word(a, 0);
-  uint32_t exprs = cql_word(a, 2);
-  uint32_t groups = cql_word(a, 8);
-  uint32_t funcs = cql_word(a, 4);
-  uint32_t widths = cql_word(a, 1);
-  if (exprs == 0 || exprs > 8 || groups == 0 || rows == 0) return 0;
-  bool ok = ((widths & 0xfu) == 0 || (widths & 0xfu) == 4) && (((widths >> 4) & 0xfu) == 0 || ((widths >> 4) & 0xfu) == 4);
-  for (uint32_t e = 0; e < exprs; e++)
-  {
-    uint32_t f = (funcs >> (4 * e)) & 0xfu;
-    if (f != FUNC_COUNT && f != FUNC_SUM && f != FUNC_AVG) ok = false;
-    if (f != FUNC_COUNT && ((cql_word(a, 6) >> (4 * e)) & 0xfu) != 0) ok = false;
-  }
-  uint32_t largest = cql_word(a, 15);
-  uint64_t budget = (uint64_t)std::min(g_cql_max_smem_optin, 200 * 1024) / 8;
-  if (ok && largest != 0 && groups <= budget && a.buf[1] != a.buf[0] && a.bytes[0] >= rows * 4 && a.bytes[1] >= rows * 4)
-  {
-    bool is_signed = (cql_word(a, 7) & 1u) != 0;
-    DenseWideFn pf = is_signed ? k_aggregate_dense_packed<true> : k_aggregate_dense_packed<false>;
-    uint32_t copy_words = (groups + 1) & ~1u;
-    uint32_t threads = 1024;
-    uint32_t copies = 1;
-    while (copies < threads / 32 && (uint64_t)copy_words * 8 * copies * 2 <= 32 * 1024) copies *= 2;
-    size_t smem = (size_t)copy_words * 8 * copies;
-    if (smem > 48 * 1024) cudaFuncSetAttribute((const void*)pf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int per_sm = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pf, (int)threads, smem) != cudaSuccess || per_sm < 1) per_sm = 1;
-    uint64_t need = (rows / 4 + threads - 1) / threads;
-    uint32_t grid = cql_stream_grid(need ? need : 1, per_sm);
-    // rows one CTA reads: its share of the 4-row vectors, rounded up, and the tail
-    uint64_t stride_vec = (uint64_t)grid * threads;
-    uint64_t per_cta = ((rows / 4 + stride_vec - 1) / stride_vec) * 4 * threads + threads;
-    if ((double)per_cta * (double)largest < 2147483648.0)
-    {
-      pf<<<grid, threads, smem, stream>>>(a, groups, 0, rows, copies, copy_words, exprs);
-      CQL_LAUNCH_CHECK();
-      return 0;
-    }
-  }
-  CqlLaunch b = a;
-  b.push[7] &= 0xffffffffull;   // the native kernel reads word 15 as the chunk start
-  return launch_aggregate_dense(b, gws, lws, stream);
-}
-
 const CqlKernelDesc cql_kernels_aggregate[] = {
-  { "cql_dense_count_sum", launch_dense_count_sum },
   { "aggregate_global_native", launch_aggregate_global },
   { "aggregate_global_f32", launch_aggregate_global_f32 },
   { "aggregate_dense_native", launch_aggregate_dense },

@@ -23,7 +23,6 @@
 #include <climits>
 
 #define FIX_THREADS 256
-#define FIXED_MAX_SCALE 6
 #define FUNC_COUNT 0u
 #define FUNC_SUM 1u
 #define FUNC_AVG 2u
@@ -34,103 +33,7 @@
 #define TYPE_F64 4u
 #define TYPE_I32 7u
 
-__constant__ unsigned long long c_fix_pow10[FIXED_MAX_SCALE + 1] = { 1ull, 10ull, 100ull, 1000ull, 10000ull, 100000ull, 1000000ull };
-
-// |v| = m * 2^-sh; `big` when !(|v| < 2^31), which includes infinities and NaN
-struct FixVal
-{
-  unsigned long long m;
-  int sh;
-  bool neg;
-  bool big;
-  unsigned long long mag_bits;   // |v| as f64 bits
-};
-
-__device__ __forceinline__ FixVal fix_decode_f64(unsigned long long bits)
-{
-  FixVal f;
-  uint32_t e = (uint32_t)(bits >> 52) & 0x7ffu;
-  unsigned long long frac = bits & 0xfffffffffffffull;
-  f.neg = (bits >> 63) != 0;
-  f.m = e ? (frac | (1ull << 52)) : frac;
-  f.sh = e ? 1075 - (int)e : 1074;
-  f.big = e >= 1023u + 31u;
-  f.mag_bits = bits & 0x7fffffffffffffffull;
-  return f;
-}
-
-// a float as the double it converts to exactly
-__device__ __forceinline__ FixVal fix_decode_f32(uint32_t bits)
-{
-  FixVal f;
-  uint32_t e = (bits >> 23) & 0xffu;
-  uint32_t frac = bits & 0x7fffffu;
-  f.neg = (bits >> 31) != 0;
-  if (e)
-  {
-    f.m = ((unsigned long long)(frac | 0x800000u)) << 29;
-    f.sh = 1075 - (int)(e + 896u);
-    f.mag_bits = ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)frac << 29);
-  }
-  else
-  {
-    f.m = (unsigned long long)frac << 29;   // zero, or a subnormal float: |v| < 2^-126, never whole
-    f.sh = 1075 - 896 + 29;
-    f.mag_bits = 0;
-  }
-  f.big = e >= 127u + 31u;
-  return f;
-}
-
-// The nearest integer W to |v| * 10^s; returns whether W / 10^s rounds back to |v|.
-__device__ __forceinline__ bool fix_whole(const FixVal& f, int s, unsigned long long* out_w)
-{
-  unsigned long long p = c_fix_pow10[s];
-  *out_w = 0;
-  if (f.m == 0) return true;
-  if (f.sh >= 75) return false;   // |v| * 10^s < 1/4 rounds to 0, which is not v
-  if (f.sh <= 21) return false;   // |v| >= 2^31: outside the fixed-point range
-  bool pow2 = f.m == (1ull << 52);
-  bool even = (f.m & 1ull) == 0;
-  if (s <= 3 && f.sh <= 63)
-  {
-    // m * p < 2^63: everything fits 64 bits
-    unsigned long long P = f.m * p;
-    unsigned long long W = (P + (1ull << (f.sh - 1))) >> f.sh;
-    *out_w = W;
-    if (W == 0) return false;
-    unsigned long long Ws = W << f.sh;
-    if (Ws >= P)
-    {
-      unsigned long long d2 = (Ws - P) << 1;
-      return d2 < p || (d2 == p && even);
-    }
-    unsigned long long d = P - Ws;
-    if (pow2) return (d << 2) <= p;
-    return (d << 1) < p || ((d << 1) == p && even);
-  }
-  unsigned __int128 P = (unsigned __int128)f.m * p;
-  unsigned __int128 W = (P + ((unsigned __int128)1 << (f.sh - 1))) >> f.sh;
-  *out_w = (unsigned long long)W;
-  if (W == 0) return false;
-  unsigned __int128 Ws = W << f.sh;
-  if (Ws >= P)
-  {
-    unsigned __int128 d2 = (Ws - P) << 1;
-    return d2 < p || (d2 == p && even);
-  }
-  unsigned __int128 d = P - Ws;
-  if (pow2) return (d << 2) <= p;
-  return (d << 1) < p || ((d << 1) == p && even);
-}
-
-// floor(v * 10^s + 0.5) of a value known to be whole at scale s
-__device__ __forceinline__ int fix_scaled(const FixVal& f, int s)
-{
-  unsigned long long w;
-  fix_whole(f, s, &w);
-  return f.neg ? -(int)w : (int)w;
-}
+#include "cql_fixed.cuh"
 
 // ---------------------------------------------------------------------------------------------
 // cql_fixed_scale: binding 0 values, 1 result (u32 max scale, u32 failed, u64 max |v| f64 bits; zeroed
@@ -310,30 +213,43 @@ struct DenseFixedArgs
   uint64_t row_limit;   // rows every bound column holds (a selected row at or past it is skipped)
 };
 
+// One row into the shared table. owner[e] is the first expression reading the same argument at the
+// same scale, whose scaled value expression e reuses (SUM, MIN and MAX of one column decode it once).
 __device__ __forceinline__ void fixed_row(const CqlLaunch& a, const DenseFixedArgs& p, uint32_t* acc, int* mm, uint32_t key_type,
-                                          const void* keys, uint64_t r, uint32_t row_number)
+                                          const void* keys, uint64_t r, uint32_t row_number, const uint32_t* owner)
 {
   long long kv;
-  if (key_type == TYPE_F64)
-  {
-    // int(keys[row]) of the reference: truncation toward zero of a whole number
-    if (!key_value(TYPE_F64, keys, r, &kv)) return;
-  }
-  else if (!key_value(key_type, keys, r, &kv)) return;
+  if (!key_value(key_type, keys, r, &kv)) return;   // an f64 key is int(keys[row]) of a whole number
   long long id = kv - (long long)p.min_key;
   if (id < 0 || id >= (long long)p.groups) return;
   uint32_t* g = acc + (uint32_t)id * p.acc_stride;
   int* gm = mm + (uint32_t)id * 2 * p.exprs;
   atomicMin(&g[0], row_number);
   atomicAdd(&g[1], 1u);
-  for (uint32_t e = 0; e < p.exprs; e++)
+  int qv[8];
+#pragma unroll
+  for (uint32_t e = 0; e < 8; e++)
   {
+    qv[e] = 0;
+    if (e >= p.exprs) continue;
     uint32_t f = (p.funcs >> (4 * e)) & 0xfu;
     if (f == FUNC_COUNT) continue;
-    int s = (int)min((p.scales >> (4 * e)) & 0xfu, (uint32_t)FIXED_MAX_SCALE);
-    const void* arg = a.buf[5 + e];
-    FixVal fv = ((p.arg_f32 >> e) & 1u) ? fix_decode_f32(((const uint32_t*)arg)[r]) : fix_decode_f64(((const unsigned long long*)arg)[r]);
-    int q = fix_scaled(fv, s);
+    int q;
+    if (owner[e] == e)
+    {
+      int s = (int)min((p.scales >> (4 * e)) & 0xfu, (uint32_t)FIXED_MAX_SCALE);
+      const void* arg = a.buf[5 + e];
+      FixVal fv = ((p.arg_f32 >> e) & 1u) ? fix_decode_f32(((const uint32_t*)arg)[r]) : fix_decode_f64(((const unsigned long long*)arg)[r]);
+      q = fix_scaled(fv, s);
+    }
+    else
+    {
+      q = 0;
+#pragma unroll
+      for (uint32_t o = 0; o < e; o++)
+        if (owner[e] == o) q = qv[o];
+    }
+    qv[e] = q;
     if (f == FUNC_SUM || f == FUNC_AVG)
     {
       uint32_t low = (uint32_t)q;
@@ -366,10 +282,31 @@ __global__ void __launch_bounds__(FIX_THREADS) k_dense_fixed(CqlLaunch a, DenseF
   int* mm = (int*)(acc + acc_words);
   const void* keys = a.buf[0];
   const uint32_t* sel = (const uint32_t*)a.buf[13];
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (uint64_t)gridDim.x * blockDim.x)
+  uint32_t owner[8];
+#pragma unroll
+  for (uint32_t e = 0; e < 8; e++)
   {
-    uint64_t r = selected ? sel[i] : i;
-    if (r < p.row_limit) fixed_row(a, p, acc, mm, key_type, keys, r, (uint32_t)r);
+    owner[e] = e;
+    for (uint32_t o = 0; o < e && e < p.exprs; o++)
+    {
+      uint32_t fo = (p.funcs >> (4 * o)) & 0xfu;
+      if (owner[e] == e && fo != FUNC_COUNT && a.buf[5 + o] == a.buf[5 + e] && ((p.arg_f32 >> o) & 1u) == ((p.arg_f32 >> e) & 1u) &&
+          ((p.scales >> (4 * o)) & 0xfu) == ((p.scales >> (4 * e)) & 0xfu))
+        owner[e] = o;
+    }
+  }
+  // four consecutive rows per thread and step: their loads are in flight together
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x * 4;
+  for (uint64_t i0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4; i0 < rows; i0 += stride)
+  {
+#pragma unroll
+    for (uint32_t j = 0; j < 4; j++)
+    {
+      uint64_t i = i0 + j;
+      if (i >= rows) break;
+      uint64_t r = selected ? sel[i] : i;
+      if (r < p.row_limit) fixed_row(a, p, acc, mm, key_type, keys, r, (uint32_t)r, owner);
+    }
   }
   __syncthreads();
   uint32_t* info = (uint32_t*)a.buf[1];

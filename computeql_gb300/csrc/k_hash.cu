@@ -17,12 +17,14 @@
 // reference's 256 lanes per warp lane) so groups of a few rows do not idle 256 threads each, while
 // the per-lane t-digest centroid (first sample, weight) is computed for the same 256 lane positions.
 #include "cql_internal.cuh"
+#include "cql_fixed.cuh"
 #include <algorithm>
 #include <float.h>
 #include <string.h>
 
 #define HASH_THREADS 256
 #define EMPTY_SLOT 0xffffffffu
+#define PAST_END 0xfffffffeu
 
 __device__ __forceinline__ uint32_t hash_u32(uint32_t x)
 {
@@ -107,29 +109,36 @@ __global__ void __launch_bounds__(HASH_THREADS) k_aggregate_assign(CqlLaunch a, 
     k.off[c] = (const uint32_t*)a.buf[5 + 2 * c];
   }
   uint64_t slots = a.bytes[0] / 4;
-  for (uint64_t row = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; row < rows; row += (uint64_t)gridDim.x * blockDim.x)
+  uint32_t lane = threadIdx.x & 31u;
+  // the loop runs while the warp's first row is in range, so whole warps take every iteration together
+  for (uint64_t row = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; row - lane < rows; row += (uint64_t)gridDim.x * blockDim.x)
   {
-    uint32_t h = ncols ? key_hash(k, ncols, string_mask, row) : 0u;
+    bool valid = row < rows;
+    uint32_t h = (valid && ncols) ? key_hash(k, ncols, string_mask, row) : 0u;
     uint64_t start = (uint64_t)(h % (buckets ? buckets : 1u)) * K;
     uint32_t claimed = EMPTY_SLOT;
-    for (uint32_t p = 0; p < K; p++)
+    for (uint32_t p = 0; valid && p < K; p++)
     {
       uint64_t slot = start + p;
       if (slot >= slots) break;
-      uint32_t prev = atomicCAS(&owner[slot], EMPTY_SLOT, (uint32_t)row);
+      // a slot's owner only ever goes from empty to a row: read it first, claim it only when empty
+      uint32_t prev = *((volatile uint32_t*)&owner[slot]);
+      if (prev == EMPTY_SLOT) prev = atomicCAS(&owner[slot], EMPTY_SLOT, (uint32_t)row);
       if (prev == EMPTY_SLOT || keys_equal(k, ncols, string_mask, row, prev))
       {
         claimed = (uint32_t)slot;
         break;
       }
     }
-    if (claimed == EMPTY_SLOT)
+    if (valid && claimed != EMPTY_SLOT) row_slot[row] = claimed;
+    // one count atomic per distinct slot of the warp (few groups would otherwise serialise on them)
+    uint32_t tag = valid ? claimed : PAST_END;
+    uint32_t peers = __match_any_sync(0xffffffffu, tag);
+    if (lane == (uint32_t)(__ffs(peers) - 1) && tag != PAST_END)
     {
-      atomicAdd(overflow, 1u);
-      continue;
+      if (claimed == EMPTY_SLOT) atomicAdd(overflow, (uint32_t)__popc(peers));
+      else atomicAdd(&counts[claimed], (uint32_t)__popc(peers));
     }
-    row_slot[row] = claimed;
-    atomicAdd(&counts[claimed], 1u);
   }
 }
 
@@ -331,7 +340,6 @@ extern "C" int cqlcuda_compact_slots_noalloc(const uint32_t* slot_counts, const 
 #define FUNC_ACD 5u
 #define FUNC_PCT 6u
 
-__constant__ double c_pow10[7] = { 1.0, 10.0, 100.0, 1000.0, 10000.0, 100000.0, 1000000.0 };
 
 __global__ void __launch_bounds__(HASH_THREADS) k_hash_reduce_fixed(CqlLaunch a, uint64_t rows)
 {
@@ -342,23 +350,50 @@ __global__ void __launch_bounds__(HASH_THREADS) k_hash_reduce_fixed(CqlLaunch a,
   int* mins = (int*)a.buf[4];
   int* maxs = (int*)a.buf[5];
   uint32_t exprs = min(cql_word(a, 2), 8u), funcs = cql_word(a, 4), scales = cql_word(a, 6);
-  for (uint64_t row = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; row < rows; row += (uint64_t)gridDim.x * blockDim.x)
+  uint64_t nslots = a.bytes[1] / 4;
+  uint32_t lane = threadIdx.x & 31u;
+  // whole warps take every iteration, so the lanes of one group combine before a single atomic
+  for (uint64_t row = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; row - lane < rows; row += (uint64_t)gridDim.x * blockDim.x)
   {
-    uint32_t slot = row_slot[row];
-    if (slot == EMPTY_SLOT) continue;
-    uint32_t g = slot_group[slot];
-    if (g == EMPTY_SLOT) continue;
+    uint32_t g = PAST_END;
+    if (row < rows)
+    {
+      uint32_t slot = row_slot[row];
+      if (slot < nslots)
+      {
+        uint32_t gg = slot_group[slot];
+        if (gg != EMPTY_SLOT) g = gg;
+      }
+    }
+    uint32_t peers = __match_any_sync(0xffffffffu, g);
+    bool leader = lane == (uint32_t)(__ffs(peers) - 1) && g != PAST_END;
     for (uint32_t e = 0; e < exprs; e++)
     {
       uint32_t f = (funcs >> (e * 4)) & 0xfu;
       uint64_t index = (uint64_t)g * exprs + e;
-      atomicAdd(&counts[index], 1u);
+      if (leader) atomicAdd(&counts[index], (uint32_t)__popc(peers));
       if (f == FUNC_COUNT) continue;
-      double scaled = ((const double*)a.buf[6 + e])[row] * c_pow10[min((scales >> (e * 4)) & 0xfu, 6u)];
-      int q = (int)floor(scaled + 0.5);
-      if (f == FUNC_SUM || f == FUNC_AVG) atomicAdd(&sums[index], (unsigned long long)(long long)q);
-      else if (f == FUNC_MIN) atomicMin(&mins[index], q);
-      else if (f == FUNC_MAX) atomicMax(&maxs[index], q);
+      // floor(v * 10^s + 0.5) of the argument, in integer arithmetic (exact for decimals of scale s)
+      int q = 0;
+      if (g != PAST_END)
+        q = fix_scaled(fix_decode_f64(((const unsigned long long*)a.buf[6 + e])[row]), (int)min((scales >> (e * 4)) & 0xfu, 6u));
+      long long acc = 0;
+      int mn = 0x7fffffff, mx = (int)0x80000000;
+#pragma unroll 8
+      for (int src = 0; src < 32; src++)
+      {
+        int v = __shfl_sync(0xffffffffu, q, src);
+        if ((peers >> src) & 1u)
+        {
+          acc += v;
+          mn = min(mn, v);
+          mx = max(mx, v);
+        }
+      }
+      if (!leader) continue;
+      if (f == FUNC_SUM || f == FUNC_AVG) atomicAdd(&sums[index], (unsigned long long)acc);
+      else if (f == FUNC_MIN) atomicMin(&mins[index], mn);
+      else if (f == FUNC_MAX) atomicMax(&maxs[index], mx);
     }
   }
 }
@@ -383,13 +418,20 @@ __global__ void __launch_bounds__(HASH_THREADS) k_csr_scatter(CqlLaunch a, uint6
   const uint32_t* row_slot = (const uint32_t*)a.buf[0];
   uint32_t* cursor = (uint32_t*)a.buf[1];
   uint32_t* out_rows = (uint32_t*)a.buf[2];
-  uint64_t cap = a.bytes[2] / 4;
-  for (uint64_t row = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; row < rows; row += (uint64_t)gridDim.x * blockDim.x)
+  uint64_t cap = a.bytes[2] / 4, slots = a.bytes[1] / 4;
+  uint32_t lane = threadIdx.x & 31u;
+  for (uint64_t row = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; row - lane < rows; row += (uint64_t)gridDim.x * blockDim.x)
   {
-    uint32_t slot = row_slot[row];
-    if (slot == EMPTY_SLOT) continue;
-    uint32_t pos = atomicAdd(&cursor[slot], 1u);
-    if (pos < cap) out_rows[pos] = (uint32_t)row;
+    uint32_t slot = row < rows ? row_slot[row] : EMPTY_SLOT;
+    if (slot >= slots) slot = EMPTY_SLOT;
+    // lanes of one slot take consecutive places with one atomic
+    uint32_t peers = __match_any_sync(0xffffffffu, slot);
+    uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+    uint32_t base = 0;
+    if (lane == leader && slot != EMPTY_SLOT) base = atomicAdd(&cursor[slot], (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    uint32_t pos = base + __popc(peers & ((1u << lane) - 1u));
+    if (slot != EMPTY_SLOT && pos < cap) out_rows[pos] = (uint32_t)row;
   }
 }
 
@@ -610,7 +652,151 @@ static int launch_widen_f64(const CqlLaunch& a, uint32_t gws, uint32_t lws, cuda
   return 0;
 }
 
+// ---------------------------------------------------------------------------------------------
+// The member-list layout of the CSR reduce, built on the device (the reference builds it on the host,
+// query_exec.c:11826-11990): group starts and chunk bases are prefix sums (prefix_sum), these kernels
+// fill the rest and fold each group's chunk partials in chunk order.
+//
+//  cql_group_chunks  binding 0 rows per group (u32), 1 chunks per group (u32 out); word 0 groups,
+//                    word 2 rows per chunk. A group of no rows still has one chunk.
+//  cql_slot_cursor   binding 0 rows per slot, 1 slot -> group (compact offsets), 2 group starts,
+//                    3 cursor per slot (out); word 0 slots
+//  cql_chunk_ranges  binding 0 group starts, 1 rows per group, 2 chunk bases, 3 chunk (first, end) row
+//                    pairs (out), 4 chunk group (out); word 0 groups, word 2 rows per chunk
+//  cql_group_fold    binding 0 partials (chunk, expr) x (sum, count, min, max) f64, 1 chunk bases
+//                    (groups + 1), 2 results (group, expr) f64 (out); word 0 groups, 2 exprs, 4 codes
+
+__global__ void __launch_bounds__(HASH_THREADS) k_group_chunks(CqlLaunch a, uint32_t groups, uint32_t per_chunk)
+{
+  const uint32_t* count = (const uint32_t*)a.buf[0];
+  uint32_t* chunks = (uint32_t*)a.buf[1];
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < groups; g += gridDim.x * blockDim.x)
+    chunks[g] = count[g] ? (count[g] + per_chunk - 1) / per_chunk : 1u;
+}
+
+__global__ void __launch_bounds__(HASH_THREADS) k_slot_cursor(CqlLaunch a, uint64_t slots, uint32_t groups)
+{
+  const uint32_t* count = (const uint32_t*)a.buf[0];
+  const uint32_t* group_of = (const uint32_t*)a.buf[1];
+  const uint32_t* start = (const uint32_t*)a.buf[2];
+  uint32_t* cursor = (uint32_t*)a.buf[3];
+  for (uint64_t sl = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; sl < slots; sl += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint32_t g = group_of[sl];
+    cursor[sl] = (count[sl] && g < groups) ? start[g] : 0u;
+  }
+}
+
+__global__ void __launch_bounds__(HASH_THREADS) k_chunk_ranges(CqlLaunch a, uint32_t groups, uint32_t per_chunk, uint64_t chunk_cap)
+{
+  const uint32_t* start = (const uint32_t*)a.buf[0];
+  const uint32_t* count = (const uint32_t*)a.buf[1];
+  const uint32_t* base = (const uint32_t*)a.buf[2];
+  uint32_t* range = (uint32_t*)a.buf[3];
+  uint32_t* group = (uint32_t*)a.buf[4];
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < groups; g += gridDim.x * blockDim.x)
+  {
+    uint32_t n = base[g + 1] - base[g], s = start[g], e = start[g] + count[g];
+    for (uint32_t k = 0; k < n; k++)
+    {
+      uint64_t c = (uint64_t)base[g] + k;
+      if (c >= chunk_cap) break;
+      uint32_t first = s + k * per_chunk;
+      range[c * 2] = first;
+      range[c * 2 + 1] = min(first + per_chunk, e);
+      group[c] = g;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(HASH_THREADS) k_group_fold(CqlLaunch a, uint32_t groups, uint32_t exprs, uint32_t codes)
+{
+  const double* partials = (const double*)a.buf[0];
+  const uint32_t* base = (const uint32_t*)a.buf[1];
+  double* results = (double*)a.buf[2];
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < groups; g += gridDim.x * blockDim.x)
+  {
+    for (uint32_t e = 0; e < exprs; e++)
+    {
+      // the host fold of the reference, chunk after chunk (query_exec.c:12180-12215)
+      double acc = 0.0, mn = 1.0e300, mx = -1.0e300, cnt = 0.0;
+      uint64_t limit = a.bytes[0] / 32 / exprs;
+      for (uint32_t c = base[g]; c < base[g + 1] && c < limit; c++)
+      {
+        const double* pp = &partials[((uint64_t)c * exprs + e) * 4];
+        acc = __dadd_rn(acc, pp[0]);
+        cnt = __dadd_rn(cnt, pp[1]);
+        mn = pp[2] < mn ? pp[2] : mn;
+        mx = pp[3] > mx ? pp[3] : mx;
+      }
+      uint32_t f = (codes >> (4 * e)) & 0xfu;
+      double r = 0.0;
+      if (f == 0) r = cnt;
+      else if (f == 1) r = acc;
+      else if (f == 2) r = cnt > 0.0 ? __ddiv_rn(acc, cnt) : 0.0;
+      else if (f == 3) r = mn;
+      else if (f == 4) r = mx;
+      results[(uint64_t)g * exprs + e] = r;
+    }
+  }
+}
+
+static int launch_group_chunks(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint32_t groups = cql_word(a, 0), per_chunk = cql_word(a, 2);
+  if (groups == 0) return 0;
+  if (per_chunk == 0 || a.bytes[0] < (uint64_t)groups * 4 || a.bytes[1] < (uint64_t)groups * 4) return (int)cudaErrorInvalidValue;
+  k_group_chunks<<<cql_stream_grid((groups + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, groups, per_chunk);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+static int launch_slot_cursor(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t slots = cql_word(a, 0);
+  if (slots == 0) return 0;
+  uint32_t groups = (uint32_t)(a.bytes[2] / 4);
+  if (a.bytes[0] < slots * 4 || a.bytes[1] < slots * 4 || a.bytes[3] < slots * 4) return (int)cudaErrorInvalidValue;
+  k_slot_cursor<<<cql_stream_grid((slots + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, slots, groups);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+static int launch_chunk_ranges(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint32_t groups = cql_word(a, 0), per_chunk = cql_word(a, 2);
+  if (groups == 0) return 0;
+  uint64_t cap = std::min(a.bytes[3] / 8, a.bytes[4] / 4);
+  if (per_chunk == 0 || a.bytes[0] < (uint64_t)groups * 4 || a.bytes[1] < (uint64_t)groups * 4 || a.bytes[2] < ((uint64_t)groups + 1) * 4)
+    return (int)cudaErrorInvalidValue;
+  k_chunk_ranges<<<cql_stream_grid((groups + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, groups, per_chunk, cap);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+static int launch_group_fold(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint32_t groups = cql_word(a, 0), exprs = cql_word(a, 2), codes = cql_word(a, 4);
+  if (groups == 0) return 0;
+  if (exprs == 0 || exprs > 8 || a.bytes[1] < ((uint64_t)groups + 1) * 4 || a.bytes[2] < (uint64_t)groups * exprs * 8) return (int)cudaErrorInvalidValue;
+  k_group_fold<<<cql_stream_grid((groups + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, groups, exprs, codes);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
 const CqlKernelDesc cql_kernels_hash[] = {
+  { "cql_group_chunks", launch_group_chunks },
+  { "cql_slot_cursor", launch_slot_cursor },
+  { "cql_chunk_ranges", launch_chunk_ranges },
+  { "cql_group_fold", launch_group_fold },
   { "aggregate_assign", launch_aggregate_assign },
   { "aggregate_compact", launch_aggregate_compact },
   { "aggregate_hash_reduce_fixed", launch_hash_reduce_fixed },

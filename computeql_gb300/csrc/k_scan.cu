@@ -10,6 +10,7 @@
 // for a single row (a COUNT(*) with no row list) every CTA counts privately and adds once at the end.
 #include "cql_internal.cuh"
 #include <math_constants.h>
+#include <climits>
 #include <algorithm>
 
 #define COLTYPE_U32 1u
@@ -535,43 +536,73 @@ static int launch_scan_filter(const CqlLaunch& a, uint32_t gws, uint32_t lws, cu
 // words 0 rows, 2 type (U32/I32/F32/F64), 3 width (0 stored, 1/2 narrow codes), 4 narrow base,
 // 6 log2 of the chunk rows. One CTA per chunk at a time.
 
-__device__ __forceinline__ double zone_value(const void* col, uint32_t type, uint32_t width, uint32_t base, uint64_t r)
-{
-  if (width == 1 || width == 2)
-  {
-    uint32_t code = width == 1 ? ((const uint8_t*)col)[r] : ((const uint16_t*)col)[r];
-    uint32_t v = base + code;
-    return type == COLTYPE_I32 ? (double)(int)v : (double)v;
-  }
-  if (type == COLTYPE_F64) return ((const double*)col)[r];
-  return widen_word(type, ((const uint32_t*)col)[r]);
-}
-
+// integer columns (stored, or narrow codes: value = base + code) compare as 64-bit integers, floats as
+// floats: no FP64 arithmetic per row
+template <int KIND>  // 0 u32, 1 i32, 2 f32, 3 f64
 __global__ void __launch_bounds__(SCAN_THREADS) k_zone_map(CqlLaunch a, uint64_t rows, uint64_t chunks)
 {
   __shared__ double s_min[SCAN_THREADS / 32], s_max[SCAN_THREADS / 32];
   const void* col = a.buf[0];
   double* out = (double*)a.buf[1];
-  uint32_t type = cql_word(a, 2), width = cql_word(a, 3), base = cql_word(a, 4), log2_rows = cql_word(a, 6);
+  uint32_t width = cql_word(a, 3), base = cql_word(a, 4), log2_rows = cql_word(a, 6);
   uint64_t chunk_rows = 1ull << log2_rows;
   for (uint64_t z = blockIdx.x; z < chunks; z += gridDim.x)
   {
     uint64_t start = z * chunk_rows, end = min(start + chunk_rows, rows);
-    double lo = CUDART_INF, hi = -CUDART_INF;
-    for (uint64_t r = start + threadIdx.x; r < end; r += SCAN_THREADS)
+    double lo, hi;
+    if (KIND <= 1)
     {
-      double v = zone_value(col, type, width, base, r);
-      if (v == v)
+      long long ilo = LLONG_MAX, ihi = LLONG_MIN;
+      for (uint64_t r = start + threadIdx.x; r < end; r += SCAN_THREADS)
       {
+        uint32_t w = width == 1 ? base + ((const uint8_t*)col)[r] : width == 2 ? base + ((const uint16_t*)col)[r] : ((const uint32_t*)col)[r];
+        long long v = KIND == 1 ? (long long)(int)w : (long long)w;
+        ilo = min(ilo, v);
+        ihi = max(ihi, v);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+      {
+        ilo = min(ilo, __shfl_xor_sync(0xffffffffu, ilo, o));
+        ihi = max(ihi, __shfl_xor_sync(0xffffffffu, ihi, o));
+      }
+      lo = ilo == LLONG_MAX ? CUDART_INF : (double)ilo;
+      hi = ihi == LLONG_MIN ? -CUDART_INF : (double)ihi;
+    }
+    else if (KIND == 2)
+    {
+      float flo = CUDART_INF_F, fhi = -CUDART_INF_F;
+      for (uint64_t r = start + threadIdx.x; r < end; r += SCAN_THREADS)
+      {
+        float v = ((const float*)col)[r];
+        flo = fminf(flo, v);   // fminf/fmaxf pass over NaN
+        fhi = fmaxf(fhi, v);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+      {
+        flo = fminf(flo, __shfl_xor_sync(0xffffffffu, flo, o));
+        fhi = fmaxf(fhi, __shfl_xor_sync(0xffffffffu, fhi, o));
+      }
+      lo = flo;
+      hi = fhi;
+    }
+    else
+    {
+      lo = CUDART_INF;
+      hi = -CUDART_INF;
+      for (uint64_t r = start + threadIdx.x; r < end; r += SCAN_THREADS)
+      {
+        double v = ((const double*)col)[r];
         lo = fmin(lo, v);
         hi = fmax(hi, v);
       }
-    }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-    {
-      lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-      hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+      for (int o = 16; o > 0; o >>= 1)
+      {
+        lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+      }
     }
     if ((threadIdx.x & 31u) == 0)
     {
@@ -605,7 +636,11 @@ static int launch_zone_map(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaS
   uint64_t elem = width ? width : (type == COLTYPE_F64 ? 8 : 4);
   uint64_t chunks = (rows + (1ull << log2_rows) - 1) >> log2_rows;
   if (a.bytes[0] < rows * elem || a.bytes[1] < chunks * 16) return (int)cudaErrorInvalidValue;
-  k_zone_map<<<cql_stream_grid(chunks, 8), SCAN_THREADS, 0, stream>>>(a, rows, chunks);
+  uint32_t grid = cql_stream_grid(chunks, 8);
+  if (type == COLTYPE_U32) k_zone_map<0><<<grid, SCAN_THREADS, 0, stream>>>(a, rows, chunks);
+  else if (type == COLTYPE_I32) k_zone_map<1><<<grid, SCAN_THREADS, 0, stream>>>(a, rows, chunks);
+  else if (type == COLTYPE_F32) k_zone_map<2><<<grid, SCAN_THREADS, 0, stream>>>(a, rows, chunks);
+  else k_zone_map<3><<<grid, SCAN_THREADS, 0, stream>>>(a, rows, chunks);
   CQL_LAUNCH_CHECK();
   return 0;
 }

@@ -93,23 +93,38 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_keys(CqlLaunch a, uint64_
 template <typename K>
 __global__ void __launch_bounds__(SORT_THREADS) k_radix_count(CqlLaunch a, uint64_t n, uint32_t tiles)
 {
-  __shared__ uint32_t hist[RADIX];
+  // one histogram per warp (fewer lanes on one shared counter), summed at the end of the tile
+  __shared__ uint32_t hist[SORT_WARPS][RADIX];
   const K* keys = (const K*)a.buf[0];
   uint32_t* out = (uint32_t*)a.buf[1];
   uint32_t shift = cql_word(a, 2);
+  uint32_t warp = threadIdx.x >> 5;
   for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x)
   {
-    for (uint32_t i = threadIdx.x; i < RADIX; i += SORT_THREADS) hist[i] = 0;
+    for (uint32_t i = threadIdx.x; i < SORT_WARPS * RADIX; i += SORT_THREADS) (&hist[0][0])[i] = 0;
     __syncthreads();
     uint64_t base = (uint64_t)tile * SORT_TILE;
-#pragma unroll 4
-    for (uint32_t j = threadIdx.x; j < SORT_TILE; j += SORT_THREADS)
+    K k[SORT_ROUNDS];
+#pragma unroll
+    for (uint32_t j = 0; j < SORT_ROUNDS; j++)
     {
-      uint64_t i = base + j;
-      if (i < n) atomicAdd(&hist[(uint32_t)(keys[i] >> shift) & 0xffu], 1u);
+      uint64_t i = base + (uint64_t)j * SORT_THREADS + threadIdx.x;
+      k[j] = i < n ? keys[i] : (K)0;
+    }
+#pragma unroll
+    for (uint32_t j = 0; j < SORT_ROUNDS; j++)
+    {
+      uint64_t i = base + (uint64_t)j * SORT_THREADS + threadIdx.x;
+      if (i < n) atomicAdd(&hist[warp][(uint32_t)(k[j] >> shift) & 0xffu], 1u);
     }
     __syncthreads();
-    for (uint32_t d = threadIdx.x; d < RADIX; d += SORT_THREADS) out[(uint64_t)d * tiles + tile] = hist[d];
+    for (uint32_t d = threadIdx.x; d < RADIX; d += SORT_THREADS)
+    {
+      uint32_t total = 0;
+#pragma unroll
+      for (uint32_t w = 0; w < SORT_WARPS; w++) total += hist[w][d];
+      out[(uint64_t)d * tiles + tile] = total;
+    }
     __syncthreads();
   }
 }
@@ -118,6 +133,7 @@ template <typename K>
 __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(CqlLaunch a, uint64_t n, uint32_t tiles)
 {
   __shared__ uint32_t warp_count[SORT_WARPS][RADIX];
+  __shared__ uint32_t s_base[RADIX];
   const K* keys_in = (const K*)a.buf[0];
   const uint32_t* pos_in = (const uint32_t*)a.buf[1];
   K* keys_out = (K*)a.buf[2];
@@ -131,17 +147,22 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(CqlLaunch a, uin
   for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x)
   {
     for (uint32_t i = threadIdx.x; i < SORT_WARPS * RADIX; i += SORT_THREADS) (&warp_count[0][0])[i] = 0;
-    __syncthreads();
-    // each warp owns 16 rounds of 32 consecutive rows; rank within the warp in input order
+    // the tile's global base of every digit, once (one load per thread)
+    for (uint32_t d = threadIdx.x; d < RADIX; d += SORT_THREADS) s_base[d] = base_of[(uint64_t)d * tiles + tile];
+    // each warp owns 16 rounds of 32 consecutive rows; all its keys and positions are loaded up front
     uint64_t warp_base = (uint64_t)tile * SORT_TILE + (uint64_t)warp * 32 * SORT_ROUNDS;
     K key[SORT_ROUNDS];
-    uint32_t local[SORT_ROUNDS];
+    uint32_t pos[SORT_ROUNDS];
 #pragma unroll
     for (uint32_t r = 0; r < SORT_ROUNDS; r++)
     {
       uint64_t i = warp_base + (uint64_t)r * 32 + lane;
       key[r] = i < n ? keys_in[i] : (K)0;
+      pos[r] = i < n ? pos_in[i] : 0u;
     }
+    __syncthreads();
+    // rank within the warp in input order
+    uint32_t local[SORT_ROUNDS];
 #pragma unroll
     for (uint32_t r = 0; r < SORT_ROUNDS; r++)
     {
@@ -155,10 +176,10 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(CqlLaunch a, uin
       __syncwarp();
     }
     __syncthreads();
-    // warps before this one, per digit
+    // per digit: the tile's base plus the warps before this one
     for (uint32_t d = threadIdx.x; d < RADIX; d += SORT_THREADS)
     {
-      uint32_t run = 0;
+      uint32_t run = s_base[d];
 #pragma unroll
       for (uint32_t w = 0; w < SORT_WARPS; w++)
       {
@@ -174,12 +195,11 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(CqlLaunch a, uin
       uint64_t i = warp_base + (uint64_t)r * 32 + lane;
       if (i >= n) continue;
       uint32_t d = (uint32_t)(key[r] >> shift) & 0xffu;
-      uint64_t pos = (uint64_t)base_of[(uint64_t)d * tiles + tile] + warp_count[warp][d] + local[r];
-      if (pos < n)
+      uint64_t dst = (uint64_t)warp_count[warp][d] + local[r];
+      if (dst < n)
       {
-        uint32_t p = pos_in[i];
-        if (write_keys) keys_out[pos] = key[r];
-        pos_out[pos] = map_rows ? sel[p] : p;
+        if (write_keys) keys_out[dst] = key[r];
+        pos_out[dst] = map_rows ? sel[pos[r]] : pos[r];
       }
     }
     __syncthreads();

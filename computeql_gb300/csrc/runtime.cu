@@ -1074,23 +1074,28 @@ static void staging_finish(CqlStaging& st, int ok)
   st.used = 0;
 }
 
-static int enqueue_read(CqlStaging& st, CqlBuffer* b, void* out, uint64_t size, cudaStream_t stream)
+#define CQL_DIRECT_READ_BYTES (8ull << 20)
+
+static int enqueue_read(CqlStaging& st, CqlBuffer* b, uint64_t offset, void* out, uint64_t size, cudaStream_t stream, bool allow_direct = true)
 {
   if (!b || !out) return 0;
-  if (size > b->size)
+  if (offset > b->size || size > b->size - offset)
   {
-    set_error("cqlcuda: read of %llu bytes from a %llu byte buffer", (unsigned long long)size, (unsigned long long)b->size);
+    set_error("cqlcuda: read of %llu bytes at %llu from a %llu byte buffer", (unsigned long long)size, (unsigned long long)offset,
+              (unsigned long long)b->size);
     return 0;
   }
+  const char* src = (const char*)b->dptr + offset;
   uint64_t off = 0;
-  unsigned char* dst = staging_reserve(st, size, &off);
+  // a large result goes straight to the caller's memory (the copy waits for the work before it):
+  // through a staging area it would cross host memory twice
+  unsigned char* dst = (allow_direct && size >= CQL_DIRECT_READ_BYTES) ? nullptr : staging_reserve(st, size, &off);
   if (!dst)
   {
-    // the staging area could not hold it: read synchronously into the caller's memory
-    if (!note_cuda(cudaMemcpyAsync(out, b->dptr, size, cudaMemcpyDeviceToHost, stream), "read")) return 0;
+    if (!note_cuda(cudaMemcpyAsync(out, src, size, cudaMemcpyDeviceToHost, stream), "read")) return 0;
     return wait_stream(stream, "read");
   }
-  if (!note_cuda(cudaMemcpyAsync(dst, b->dptr, size, cudaMemcpyDeviceToHost, stream), "read")) return 0;
+  if (!note_cuda(cudaMemcpyAsync(dst, src, size, cudaMemcpyDeviceToHost, stream), "read")) return 0;
   st.reads.push_back(CqlPendingRead{out, off, size});
   return 1;
 }
@@ -1175,7 +1180,18 @@ extern "C" void cqlcuda_batch_buffer_read(CqlBatch* batch, CqlBuffer* buffer, vo
     if (out_data) memset(out_data, 0, size);
     return;
   }
-  if (!enqueue_read(batch->staging, buffer, out_data, size, S().stream)) batch->failed = 1;
+  if (!enqueue_read(batch->staging, buffer, 0, out_data, size, S().stream)) batch->failed = 1;
+}
+
+extern "C" void cqlcuda_batch_buffer_read_at(CqlBatch* batch, CqlBuffer* buffer, uint64_t offset, void* out_data, uint64_t size)
+{
+  if (!batch) return;
+  if (!buffer)
+  {
+    if (out_data) memset(out_data, 0, size);
+    return;
+  }
+  if (!enqueue_read(batch->staging, buffer, offset, out_data, size, S().stream)) batch->failed = 1;
 }
 
 extern "C" int cqlcuda_batch_end(CqlBatch* batch)
@@ -1321,7 +1337,7 @@ extern "C" void cqlcuda_stream_dispatch(CqlStream* st, uint32_t slot, CqlKernel*
 extern "C" void cqlcuda_stream_read(CqlStream* st, uint32_t slot, CqlBuffer* b, void* out, uint64_t size)
 {
   if (!st || slot >= st->slot_count) return;
-  if (!enqueue_read(st->slots[slot].staging, b, out, size, st->slots[slot].stream)) st->slots[slot].failed = 1;
+  if (!enqueue_read(st->slots[slot].staging, b, 0, out, size, st->slots[slot].stream, false)) st->slots[slot].failed = 1;
 }
 
 extern "C" int cqlcuda_stream_submit(CqlStream* st, uint32_t slot)

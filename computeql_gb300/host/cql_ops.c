@@ -523,12 +523,7 @@ int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count,
   {
     return refuse("dense group-by: more than 256 tiles of the reference's shared-memory slices");
   }
-  /* one full-width argument under COUNT/SUM/AVG with a known largest magnitude: the packed count+sum
-     kernel (the same bindings and words), which falls back to the native one when a CTA could overflow */
-  int count_sum = arg_count == 1 && !has_min_max && arg_columns[0]->buffer && arg_columns[0]->buffer != key->buffer &&
-                  (shader_width(key) == 0 || shader_width(key) == 4) && (shader_width(arg_columns[0]) == 0 || shader_width(arg_columns[0]) == 4) &&
-                  largest_sum_arg > 0.0 && largest_sum_arg < 4294967295.0;
-  CqlKernel* k = kernel_named(count_sum ? "cql_dense_count_sum" : "aggregate_dense_native");
+  CqlKernel* k = kernel_named("aggregate_dense_native");
   if (!k)
   {
     return 0;
@@ -577,9 +572,7 @@ int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count,
     cqlcuda_kernel_set_arg_u64(k, 4, group_count | ((uint64_t)arg_bases[2] << 32));
     cqlcuda_kernel_set_arg_u64(k, 5, (uint64_t)(uint32_t)(int32_t)min_key | ((uint64_t)arg_bases[3] << 32));
     cqlcuda_kernel_set_arg_u64(k, 6, tile_groups | (slice_rows << 32));
-    /* cql_dense_count_sum reads word 15 as the argument's largest magnitude (the native kernel's
-       chunk start, 0 here: no sequence argument is read through it) */
-    cqlcuda_kernel_set_arg_u64(k, 7, tile_count | (count_sum ? (uint64_t)largest_sum_arg << 32 : 0));
+    cqlcuda_kernel_set_arg_u64(k, 7, tile_count);
     CqlBatch* batch = cqlcuda_batch_begin(0, info_bytes + sum_bytes + 2 * mm_bytes);
     cqlcuda_batch_buffer_fill(batch, info_buf, info_bytes, 0);
     cqlcuda_batch_buffer_fill(batch, sum_buf, sum_bytes, 0);

@@ -25,6 +25,8 @@
 #define HLL_PRECISION 10
 #define HLL_SKETCH_MAX_BYTES (64ull << 20)
 
+static const double g_pow10[7] = { 1.0, 10.0, 100.0, 1000.0, 10000.0, 100000.0, 1000000.0 };
+
 void cqlops_note_error(const char* why);
 
 static int refuse(const char* why)
@@ -136,6 +138,191 @@ static int whole_number_arg(const CqlColumn* col)
          col->zone_max <= 2147483647.0;
 }
 
+/* The CSR member reduce of the groups found by assign/compact: slot_counts/slot_group (compact
+   offsets) per slot, group_counts per group, row_slot per row. Writes out_results[g * exprs + e].
+   With row_slot NULL there is one group of every row in order (no key). */
+static int csr_reduce(uint64_t rows, uint64_t slots, uint64_t groups, CqlBuffer* slot_counts, CqlBuffer* slot_group,
+                      CqlBuffer* group_counts, CqlBuffer* row_slot, uint32_t expr_count, const uint32_t* funcs, uint32_t func_codes,
+                      CqlBuffer* const* arg_f64, const double* params, double* out_results)
+{
+  uint64_t gb = (groups + 255) / 256;
+  CqlBuffer* g_start = pooled("agg_group_start_buf", (groups + 1) * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* g_chunks = pooled("agg_group_chunks_buf", groups * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* c_base = pooled("agg_chunk_base_buf", (groups + 1) * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* scratch = pooled("agg_scan_scratch_buf", groups * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* block_sums = pooled("agg_scan_block_buf", gb * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlKernel* kchunks = kernel("cql_group_chunks");
+  CqlKernel* scan = kernel("prefix_sum");
+  if (!g_start || !g_chunks || !c_base || !scratch || !block_sums || !kchunks || !scan) return 0;
+  uint32_t total_chunks32 = 0;
+  {
+    CqlBatch* b = cqlcuda_batch_begin(0, 4);
+    cqlcuda_kernel_set_arg_buffer(kchunks, 0, group_counts);
+    cqlcuda_kernel_set_arg_buffer(kchunks, 1, g_chunks);
+    cqlcuda_kernel_set_arg_u64(kchunks, 0, groups);
+    cqlcuda_kernel_set_arg_u64(kchunks, 1, AGG_ROWS_PER_CHUNK);
+    cqlcuda_batch_kernel_execute(b, kchunks, (uint32_t)groups, QE_GPU_WORKGROUP_SIZE);
+    for (int pass = 0; pass < 2; pass++)
+    {
+      cqlcuda_kernel_set_arg_buffer(scan, 0, pass ? g_chunks : group_counts);
+      cqlcuda_kernel_set_arg_buffer(scan, 1, pass ? c_base : g_start);
+      cqlcuda_kernel_set_arg_buffer(scan, 2, scratch);
+      cqlcuda_kernel_set_arg_buffer(scan, 3, block_sums);
+      cqlcuda_kernel_set_arg_u64(scan, 0, groups);
+      for (uint32_t mode = 0; mode < 3; mode++)
+      {
+        cqlcuda_kernel_set_arg_u64(scan, 1, mode);
+        cqlcuda_batch_kernel_execute(b, scan, mode == 1 ? 256u : (uint32_t)(gb * 256), 256);
+      }
+    }
+    /* the chunk count: the scan's total, after the last chunk base */
+    cqlcuda_batch_buffer_read_at(b, c_base, groups * 4, &total_chunks32, 4);
+    if (!cqlcuda_batch_end(b)) return 0;
+  }
+  uint64_t total_chunks = total_chunks32;
+  uint32_t num_hll = 0, num_pct = 0, hll_slot_packed = 0, pct_slot_packed = 0;
+  for (uint32_t e = 0; e < expr_count; e++)
+  {
+    if (funcs[e] == CQLOPS_FUNC_APPROX_COUNT_DISTINCT) hll_slot_packed |= (num_hll++) << (4 * e);
+    if (funcs[e] == CQLOPS_FUNC_APPROX_PERCENTILE) pct_slot_packed |= (num_pct++) << (4 * e);
+  }
+  uint64_t hll_words = 1ull << HLL_PRECISION;
+  uint64_t sketch_bytes = (groups ? groups : 1) * (num_hll ? num_hll : 1) * hll_words * 4;
+  uint64_t digest_words = total_chunks * (num_pct ? num_pct : 1) * 256;
+  if (num_hll && sketch_bytes > HLL_SKETCH_MAX_BYTES) return refuse("the HyperLogLog sketches exceed QE_HLL_SKETCH_MAX_TOTAL_BYTES (64 MB)");
+  CqlBuffer* cursor_buf = pooled("agg_cursor_buf", slots * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* members = pooled("agg_members_buf", rows * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* range_buf = pooled("agg_chunk_range_buf", total_chunks * 8, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* group_buf = pooled("agg_chunk_group_buf", total_chunks * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* repr_buf = pooled("agg_repr_buf", groups * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* partials_buf = pooled("agg_partials_buf", total_chunks * expr_count * 32, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* results_buf = pooled("agg_results_buf", groups * expr_count * 8, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* sketch_buf = pooled("agg_sketch_buf", sketch_bytes, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* dmean_buf = pooled("agg_digest_mean_buf", digest_words * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* dweight_buf = pooled("agg_digest_weight_buf", digest_words * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlKernel* kcursor = kernel("cql_slot_cursor");
+  CqlKernel* kranges = kernel("cql_chunk_ranges");
+  CqlKernel* scatter = kernel("csr_scatter");
+  CqlKernel* reduce = kernel("aggregate_reduce");
+  CqlKernel* fold = kernel("cql_group_fold");
+  uint32_t* sketch = num_hll ? (uint32_t*)malloc(sketch_bytes) : NULL;
+  float* dmean = num_pct ? (float*)malloc(digest_words * 4) : NULL;
+  float* dweight = num_pct ? (float*)malloc(digest_words * 4) : NULL;
+  uint32_t* h_base = num_pct ? (uint32_t*)malloc((groups + 1) * 4) : NULL;
+  int ok = cursor_buf && members && range_buf && group_buf && repr_buf && partials_buf && results_buf && sketch_buf && dmean_buf &&
+           dweight_buf && kcursor && kranges && scatter && reduce && fold && (!num_hll || sketch) && (!num_pct || (dmean && dweight && h_base));
+  if (ok)
+  {
+    if (!row_slot)
+    {
+      /* one group of all rows in order: the members are the row numbers */
+      ok = cqlcuda_fill_sequence_u32(members, rows, 0);
+    }
+    cqlcuda_kernel_set_arg_buffer(kcursor, 0, slot_counts ? slot_counts : group_counts);
+    cqlcuda_kernel_set_arg_buffer(kcursor, 1, slot_group ? slot_group : group_counts);
+    cqlcuda_kernel_set_arg_buffer_range(kcursor, 2, g_start, 0, groups * 4);
+    cqlcuda_kernel_set_arg_buffer(kcursor, 3, cursor_buf);
+    cqlcuda_kernel_set_arg_u64(kcursor, 0, slots);
+    cqlcuda_kernel_set_arg_buffer(kranges, 0, g_start);
+    cqlcuda_kernel_set_arg_buffer(kranges, 1, group_counts);
+    cqlcuda_kernel_set_arg_buffer(kranges, 2, c_base);
+    cqlcuda_kernel_set_arg_buffer(kranges, 3, range_buf);
+    cqlcuda_kernel_set_arg_buffer(kranges, 4, group_buf);
+    cqlcuda_kernel_set_arg_u64(kranges, 0, groups);
+    cqlcuda_kernel_set_arg_u64(kranges, 1, AGG_ROWS_PER_CHUNK);
+    cqlcuda_kernel_set_arg_buffer(scatter, 0, row_slot ? row_slot : members);
+    cqlcuda_kernel_set_arg_buffer(scatter, 1, cursor_buf);
+    cqlcuda_kernel_set_arg_buffer(scatter, 2, members);
+    cqlcuda_kernel_set_arg_u64(scatter, 0, rows);
+    cqlcuda_kernel_set_arg_buffer(reduce, 0, members);
+    cqlcuda_kernel_set_arg_buffer(reduce, 1, range_buf);
+    cqlcuda_kernel_set_arg_buffer(reduce, 2, group_buf);
+    cqlcuda_kernel_set_arg_buffer(reduce, 3, repr_buf);
+    cqlcuda_kernel_set_arg_buffer(reduce, 4, partials_buf);
+    for (uint32_t e = 0; e < 8; e++) cqlcuda_kernel_set_arg_buffer(reduce, 5 + e, arg_f64[e] ? arg_f64[e] : members);
+    cqlcuda_kernel_set_arg_buffer(reduce, 13, sketch_buf);
+    cqlcuda_kernel_set_arg_buffer(reduce, 14, dmean_buf);
+    cqlcuda_kernel_set_arg_buffer(reduce, 15, dweight_buf);
+    cqlcuda_kernel_set_arg_u64(reduce, 0, total_chunks);
+    cqlcuda_kernel_set_arg_u64(reduce, 1, expr_count);
+    cqlcuda_kernel_set_arg_u64(reduce, 2, func_codes);
+    cqlcuda_kernel_set_arg_u64(reduce, 3, 0);
+    cqlcuda_kernel_set_arg_u64(reduce, 4, HLL_PRECISION);
+    cqlcuda_kernel_set_arg_u64(reduce, 5, hll_slot_packed);
+    cqlcuda_kernel_set_arg_u64(reduce, 6, num_hll);
+    cqlcuda_kernel_set_arg_u64(reduce, 7, num_pct | ((uint64_t)pct_slot_packed << 32));
+    cqlcuda_kernel_set_arg_buffer(fold, 0, partials_buf);
+    cqlcuda_kernel_set_arg_buffer(fold, 1, c_base);
+    cqlcuda_kernel_set_arg_buffer(fold, 2, results_buf);
+    cqlcuda_kernel_set_arg_u64(fold, 0, groups);
+    cqlcuda_kernel_set_arg_u64(fold, 1, expr_count);
+    cqlcuda_kernel_set_arg_u64(fold, 2, func_codes);
+    CqlBatch* b = cqlcuda_batch_begin(0, groups * expr_count * 8 + sketch_bytes + 2 * digest_words * 4 + (groups + 1) * 4);
+    if (num_hll) cqlcuda_batch_buffer_zero(b, sketch_buf, sketch_bytes);
+    if (row_slot) cqlcuda_batch_kernel_execute(b, kcursor, (uint32_t)slots, QE_GPU_WORKGROUP_SIZE);
+    cqlcuda_batch_kernel_execute(b, kranges, (uint32_t)groups, QE_GPU_WORKGROUP_SIZE);
+    if (row_slot) cqlcuda_batch_kernel_execute(b, scatter, (uint32_t)rows, QE_GPU_WORKGROUP_SIZE);
+    cqlcuda_batch_kernel_execute(b, reduce, (uint32_t)(total_chunks * QE_GPU_WORKGROUP_SIZE), QE_GPU_WORKGROUP_SIZE);
+    cqlcuda_batch_kernel_execute(b, fold, (uint32_t)groups, QE_GPU_WORKGROUP_SIZE);
+    cqlcuda_batch_buffer_read(b, results_buf, out_results, groups * expr_count * 8);
+    if (num_hll) cqlcuda_batch_buffer_read(b, sketch_buf, sketch, sketch_bytes);
+    if (num_pct)
+    {
+      cqlcuda_batch_buffer_read(b, dmean_buf, dmean, digest_words * 4);
+      cqlcuda_batch_buffer_read(b, dweight_buf, dweight, digest_words * 4);
+      cqlcuda_batch_buffer_read(b, c_base, h_base, (groups + 1) * 4);
+    }
+    ok = cqlcuda_batch_end(b);
+  }
+  if (ok && (num_hll || num_pct))
+  {
+    /* the sketches are finished on the host: qe_hll_estimate_cardinality, rounded (:12230), and the
+       t-digest percentile over a group's centroids in chunk order (:6748-6790) */
+    float* cm = NULL;
+    float* cw = NULL;
+    for (uint64_t g = 0; g < groups && ok; g++)
+      for (uint32_t e = 0; e < expr_count && ok; e++)
+      {
+        if (funcs[e] == CQLOPS_FUNC_APPROX_COUNT_DISTINCT)
+          out_results[g * expr_count + e] =
+            round(cqlops_hll_estimate(&sketch[(g * num_hll + ((hll_slot_packed >> (4 * e)) & 0xfu)) * hll_words], hll_words));
+        else if (funcs[e] == CQLOPS_FUNC_APPROX_PERCENTILE)
+        {
+          uint64_t n = h_base[g + 1] - h_base[g], cap = n * 256, v = 0;
+          float* m2 = (float*)realloc(cm, (cap ? cap : 1) * 4);
+          float* w2 = (float*)realloc(cw, (cap ? cap : 1) * 4);
+          if (m2) cm = m2;
+          if (w2) cw = w2;
+          if (!m2 || !w2)
+          {
+            ok = 0;
+            break;
+          }
+          uint32_t ps = (pct_slot_packed >> (4 * e)) & 0xfu;
+          for (uint64_t k = 0; k < n; k++)
+          {
+            uint64_t base = ((h_base[g] + k) * num_pct + ps) * 256;
+            for (uint32_t t = 0; t < 256; t++)
+              if (dweight[base + t] > 0.0f)
+              {
+                cm[v] = dmean[base + t];
+                cw[v] = dweight[base + t];
+                v++;
+              }
+          }
+          out_results[g * expr_count + e] = cqlops_tdigest_percentile(cm, cw, v, params ? params[e] : 0.5);
+        }
+      }
+    free(cm);
+    free(cw);
+  }
+  free(sketch);
+  free(dmean);
+  free(dweight);
+  free(h_base);
+  return ok;
+}
+
 int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* args,
                       const double* params, uint64_t group_hint, uint32_t path, uint64_t max_groups, uint64_t* out_group_count,
                       uint64_t* out_repr_row, uint64_t* out_counts, double* out_results, uint32_t* out_path)
@@ -177,6 +364,7 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
     }
   }
   int has_sketch = 0, all_whole = 1;
+  uint32_t fixed_scales = 0;
   uint32_t func_codes = 0;
   for (uint32_t e = 0; e < expr_count; e++)
   {
@@ -186,10 +374,20 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
     if (funcs[e] != CQLOPS_FUNC_COUNT)
     {
       if (!args[e] || args[e]->rows != rows) return refuse("an aggregate needs an argument column of the table's length");
-      if (!whole_number_arg(args[e])) all_whole = 0;
+      if (whole_number_arg(args[e]))
+        continue;
+      /* an f64 argument of decimals with at most 6 places reduces as scaled integers too (:10896-10913) */
+      int32_t scale = -1;
+      double largest = 0.0;
+      if (args[e]->type == CQLOPS_TYPE_F64 && funcs[e] <= CQLOPS_FUNC_MAX && args[e]->width == 0 &&
+          !cqlops_fixed_scale(args[e], NULL, 0, &scale, &largest))
+        return 0;
+      cqlops_note_error("");
+      if (scale < 0) all_whole = 0;
+      else fixed_scales |= (uint32_t)scale << (4 * e);
     }
   }
-  int use_fixed = !has_sketch && all_whole;
+  int use_fixed = !has_sketch && all_whole && key_count > 0;
   if (path == 1) use_fixed = 0;
   if (path == 2 && (!use_fixed)) return refuse("the fixed-point reduce takes whole-number COUNT/SUM/AVG/MIN/MAX only");
   CqlBuffer* arg_f64[8] = { 0 };
@@ -199,6 +397,23 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
     snprintf(name, sizeof(name), "cqlops_hash_arg_f64_%u", e);
     arg_f64[e] = widen(args[e], name);
     if (!arg_f64[e]) return refuse("an argument column could not be widened to f64");
+  }
+
+  if (key_count == 0)
+  {
+    /* no key: one group of every row, its members the rows in order - no hash table, no scatter */
+    CqlBuffer* one = pooled("agg_single_group_count_buf", 4, CQLCUDA_BUFFER_READ_WRITE);
+    if (!one || max_groups < 1) return one ? refuse("more groups than the output arrays hold") : 0;
+    uint32_t n32 = (uint32_t)rows;
+    CqlBatch* b = cqlcuda_batch_begin(4, 0);
+    cqlcuda_batch_buffer_write(b, one, &n32, 4);
+    if (!cqlcuda_batch_end(b)) return 0;
+    out_repr_row[0] = 0;
+    out_counts[0] = rows;
+    if (!csr_reduce(rows, 1, 1, NULL, NULL, one, NULL, expr_count, funcs, func_codes, arg_f64, params, out_results)) return 0;
+    *out_group_count = 1;
+    if (out_path) *out_path = 1u;
+    return 1;
   }
 
   /* buckets: ~64 rows per group unless the caller knows better (:10792-10826) */
@@ -348,7 +563,7 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
       cqlcuda_kernel_set_arg_u64(hr, 0, rows);
       cqlcuda_kernel_set_arg_u64(hr, 1, expr_count);
       cqlcuda_kernel_set_arg_u64(hr, 2, func_codes);
-      cqlcuda_kernel_set_arg_u64(hr, 3, 0); /* whole numbers: every scale exponent 0 */
+      cqlcuda_kernel_set_arg_u64(hr, 3, fixed_scales);
       CqlBatch* b = cqlcuda_batch_begin(0, cells * 16);
       cqlcuda_batch_buffer_zero(b, sums, cells * 8);
       cqlcuda_batch_buffer_zero(b, cnts, cells * 4);
@@ -365,15 +580,17 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
       for (uint64_t g = 0; g < groups; g++)
         for (uint32_t e = 0; e < expr_count; e++)
         {
+          /* back out of the scaled integers (:11750-11773) */
           uint64_t i = g * expr_count + e;
-          double r;
+          double divisor = g_pow10[(fixed_scales >> (4 * e)) & 0xfu];
+          double count = (double)g_count[g], r;
           switch (funcs[e])
           {
-            case CQLOPS_FUNC_COUNT: r = (double)g_count[g]; break;
-            case CQLOPS_FUNC_SUM: r = (double)hs[i]; break;
-            case CQLOPS_FUNC_AVG: r = (double)hs[i] / (double)g_count[g]; break;
-            case CQLOPS_FUNC_MIN: r = (double)hmn[i]; break;
-            default: r = (double)hmx[i]; break;
+            case CQLOPS_FUNC_COUNT: r = count; break;
+            case CQLOPS_FUNC_SUM: r = (double)hs[i] / divisor; break;
+            case CQLOPS_FUNC_AVG: r = count > 0 ? (double)hs[i] / divisor / count : 0.0; break;
+            case CQLOPS_FUNC_MIN: r = (double)hmn[i] / divisor; break;
+            default: r = (double)hmx[i] / divisor; break;
           }
           out_results[i] = r;
         }
@@ -384,188 +601,11 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
   }
   else
   {
-    /* 4b: member lists, group g's members at [start[g], start[g] + count[g]) */
-    uint32_t* g_start = (uint32_t*)malloc((groups + 1) * 4);
-    uint32_t* h_offsets = (uint32_t*)malloc((slots + 1) * 4);
-    uint32_t* h_counts = (uint32_t*)malloc(slots * 4);
-    uint32_t* cursor = (uint32_t*)malloc(slots * 4);
-    ok = g_start && h_offsets && h_counts && cursor;
-    if (ok)
-    {
-      CqlBatch* b = cqlcuda_batch_begin(0, slots * 8);
-      cqlcuda_batch_buffer_read(b, offsets, h_offsets, slots * 4);
-      cqlcuda_batch_buffer_read(b, count, h_counts, slots * 4);
-      ok = cqlcuda_batch_end(b);
-    }
-    if (ok)
-    {
-      uint32_t run = 0;
-      for (uint64_t g = 0; g < groups; g++)
-      {
-        g_start[g] = run;
-        run += g_count[g];
-      }
-      g_start[groups] = run;
-      for (uint64_t s = 0; s < slots; s++) cursor[s] = h_counts[s] ? g_start[h_offsets[s]] : 0u;
-      uint64_t total_chunks = 0;
-      for (uint64_t g = 0; g < groups; g++) total_chunks += g_count[g] ? (g_count[g] + AGG_ROWS_PER_CHUNK - 1) / AGG_ROWS_PER_CHUNK : 1;
-      uint32_t* chunk_range = (uint32_t*)malloc(total_chunks * 8 + 8);
-      uint32_t* chunk_group = (uint32_t*)malloc(total_chunks * 4 + 4);
-      uint64_t* chunk_base = (uint64_t*)malloc((groups + 1) * 8);
-      uint32_t num_hll = 0, num_pct = 0, hll_slot_packed = 0, pct_slot_packed = 0;
-      for (uint32_t e = 0; e < expr_count; e++)
-      {
-        if (funcs[e] == CQLOPS_FUNC_APPROX_COUNT_DISTINCT) hll_slot_packed |= (num_hll++) << (4 * e);
-        if (funcs[e] == CQLOPS_FUNC_APPROX_PERCENTILE) pct_slot_packed |= (num_pct++) << (4 * e);
-      }
-      uint64_t hll_words = 1ull << HLL_PRECISION;
-      uint64_t sketch_bytes = (groups ? groups : 1) * (num_hll ? num_hll : 1) * hll_words * 4;
-      uint64_t digest_words = total_chunks * (num_pct ? num_pct : 1) * 256;
-      if (num_hll && sketch_bytes > HLL_SKETCH_MAX_BYTES) ok = refuse("the HyperLogLog sketches exceed QE_HLL_SKETCH_MAX_TOTAL_BYTES (64 MB)");
-      uint64_t c = 0;
-      for (uint64_t g = 0; g < groups && ok; g++)
-      {
-        uint64_t n = g_count[g] ? (g_count[g] + AGG_ROWS_PER_CHUNK - 1) / AGG_ROWS_PER_CHUNK : 1;
-        chunk_base[g] = c;
-        for (uint64_t k = 0; k < n; k++, c++)
-        {
-          uint32_t s = g_start[g] + (uint32_t)(k * AGG_ROWS_PER_CHUNK);
-          uint32_t e2 = s + AGG_ROWS_PER_CHUNK < g_start[g] + g_count[g] ? s + AGG_ROWS_PER_CHUNK : g_start[g] + g_count[g];
-          chunk_range[c * 2] = s;
-          chunk_range[c * 2 + 1] = e2;
-          chunk_group[c] = (uint32_t)g;
-        }
-      }
-      CqlBuffer* cursor_buf = pooled("agg_cursor_buf", slots * 4, CQLCUDA_BUFFER_READ_WRITE);
-      CqlBuffer* members = pooled("agg_members_buf", rows * 4, CQLCUDA_BUFFER_READ_WRITE);
-      CqlBuffer* range_buf = pooled("agg_chunk_range_buf", total_chunks * 8, CQLCUDA_BUFFER_WRITE);
-      CqlBuffer* group_buf = pooled("agg_chunk_group_buf", total_chunks * 4, CQLCUDA_BUFFER_WRITE);
-      CqlBuffer* repr_buf = pooled("agg_repr_buf", groups * 4, CQLCUDA_BUFFER_READ_WRITE);
-      CqlBuffer* partials_buf = pooled("agg_partials_buf", total_chunks * expr_count * 32, CQLCUDA_BUFFER_READ_WRITE);
-      CqlBuffer* sketch_buf = pooled("agg_sketch_buf", sketch_bytes, CQLCUDA_BUFFER_READ_WRITE);
-      CqlBuffer* dmean_buf = pooled("agg_digest_mean_buf", digest_words * 4, CQLCUDA_BUFFER_READ_WRITE);
-      CqlBuffer* dweight_buf = pooled("agg_digest_weight_buf", digest_words * 4, CQLCUDA_BUFFER_READ_WRITE);
-      CqlKernel* scatter = kernel("csr_scatter");
-      CqlKernel* reduce = kernel("aggregate_reduce");
-      double* partials = (double*)malloc(total_chunks * expr_count * 32 + 8);
-      uint32_t* sketch = num_hll ? (uint32_t*)malloc(sketch_bytes) : NULL;
-      float* dmean = num_pct ? (float*)malloc(digest_words * 4) : NULL;
-      float* dweight = num_pct ? (float*)malloc(digest_words * 4) : NULL;
-      ok = ok && chunk_range && chunk_group && chunk_base && cursor_buf && members && range_buf && group_buf && repr_buf && partials_buf &&
-           sketch_buf && dmean_buf && dweight_buf && scatter && reduce && partials && (!num_hll || sketch) && (!num_pct || (dmean && dweight));
-      if (ok)
-      {
-        cqlcuda_kernel_set_arg_buffer(scatter, 0, row_slot);
-        cqlcuda_kernel_set_arg_buffer(scatter, 1, cursor_buf);
-        cqlcuda_kernel_set_arg_buffer(scatter, 2, members);
-        cqlcuda_kernel_set_arg_u64(scatter, 0, rows);
-        cqlcuda_kernel_set_arg_buffer(reduce, 0, members);
-        cqlcuda_kernel_set_arg_buffer(reduce, 1, range_buf);
-        cqlcuda_kernel_set_arg_buffer(reduce, 2, group_buf);
-        cqlcuda_kernel_set_arg_buffer(reduce, 3, repr_buf);
-        cqlcuda_kernel_set_arg_buffer(reduce, 4, partials_buf);
-        for (uint32_t e = 0; e < 8; e++) cqlcuda_kernel_set_arg_buffer(reduce, 5 + e, arg_f64[e] ? arg_f64[e] : members);
-        cqlcuda_kernel_set_arg_buffer(reduce, 13, sketch_buf);
-        cqlcuda_kernel_set_arg_buffer(reduce, 14, dmean_buf);
-        cqlcuda_kernel_set_arg_buffer(reduce, 15, dweight_buf);
-        cqlcuda_kernel_set_arg_u64(reduce, 0, total_chunks);
-        cqlcuda_kernel_set_arg_u64(reduce, 1, expr_count);
-        cqlcuda_kernel_set_arg_u64(reduce, 2, func_codes);
-        cqlcuda_kernel_set_arg_u64(reduce, 3, 0);
-        cqlcuda_kernel_set_arg_u64(reduce, 4, HLL_PRECISION);
-        cqlcuda_kernel_set_arg_u64(reduce, 5, hll_slot_packed);
-        cqlcuda_kernel_set_arg_u64(reduce, 6, num_hll);
-        cqlcuda_kernel_set_arg_u64(reduce, 7, num_pct | ((uint64_t)pct_slot_packed << 32));
-        CqlBatch* b = cqlcuda_batch_begin(slots * 4 + total_chunks * 12, total_chunks * expr_count * 32 + sketch_bytes + 2 * digest_words * 4);
-        cqlcuda_batch_buffer_write(b, cursor_buf, cursor, slots * 4);
-        cqlcuda_batch_buffer_write(b, range_buf, chunk_range, total_chunks * 8);
-        cqlcuda_batch_buffer_write(b, group_buf, chunk_group, total_chunks * 4);
-        if (num_hll) cqlcuda_batch_buffer_zero(b, sketch_buf, sketch_bytes);
-        cqlcuda_batch_kernel_execute(b, scatter, (uint32_t)rows, QE_GPU_WORKGROUP_SIZE);
-        cqlcuda_batch_kernel_execute(b, reduce, (uint32_t)(total_chunks * QE_GPU_WORKGROUP_SIZE), QE_GPU_WORKGROUP_SIZE);
-        cqlcuda_batch_buffer_read(b, partials_buf, partials, total_chunks * expr_count * 32);
-        if (num_hll) cqlcuda_batch_buffer_read(b, sketch_buf, sketch, sketch_bytes);
-        if (num_pct)
-        {
-          cqlcuda_batch_buffer_read(b, dmean_buf, dmean, digest_words * 4);
-          cqlcuda_batch_buffer_read(b, dweight_buf, dweight, digest_words * 4);
-        }
-        ok = cqlcuda_batch_end(b);
-      }
-      if (ok)
-      {
-        /* fold each group's chunks in chunk order (:12180-12215) */
-        float* cm = NULL;
-        float* cw = NULL;
-        for (uint64_t g = 0; g < groups && ok; g++)
-        {
-          uint64_t n = g_count[g] ? (g_count[g] + AGG_ROWS_PER_CHUNK - 1) / AGG_ROWS_PER_CHUNK : 1;
-          for (uint32_t e = 0; e < expr_count; e++)
-          {
-            double acc = 0.0, mn = 1.0e300, mx = -1.0e300, cnt = 0.0;
-            for (uint64_t k = 0; k < n; k++)
-            {
-              const double* pp = &partials[((chunk_base[g] + k) * expr_count + e) * 4];
-              acc += pp[0];
-              cnt += pp[1];
-              mn = pp[2] < mn ? pp[2] : mn;
-              mx = pp[3] > mx ? pp[3] : mx;
-            }
-            double r;
-            switch (funcs[e])
-            {
-              case CQLOPS_FUNC_COUNT: r = cnt; break;
-              case CQLOPS_FUNC_SUM: r = acc; break;
-              case CQLOPS_FUNC_AVG: r = cnt > 0 ? acc / cnt : 0.0; break;
-              case CQLOPS_FUNC_MIN: r = mn; break;
-              case CQLOPS_FUNC_MAX: r = mx; break;
-              case CQLOPS_FUNC_APPROX_COUNT_DISTINCT:
-                r = round(cqlops_hll_estimate(&sketch[(g * num_hll + ((hll_slot_packed >> (4 * e)) & 0xfu)) * hll_words], hll_words));
-                break;
-              default:
-              {
-                uint64_t cap = n * 256, v = 0;
-                cm = (float*)realloc(cm, cap * 4);
-                cw = (float*)realloc(cw, cap * 4);
-                if (!cm || !cw)
-                {
-                  ok = 0;
-                  r = 0.0;
-                  break;
-                }
-                uint32_t ps = (pct_slot_packed >> (4 * e)) & 0xfu;
-                for (uint64_t k = 0; k < n; k++)
-                {
-                  uint64_t base = ((chunk_base[g] + k) * num_pct + ps) * 256;
-                  for (uint32_t t = 0; t < 256; t++)
-                    if (dweight[base + t] > 0.0f)
-                    {
-                      cm[v] = dmean[base + t];
-                      cw[v] = dweight[base + t];
-                      v++;
-                    }
-                }
-                r = cqlops_tdigest_percentile(cm, cw, v, params ? params[e] : 0.5);
-              }
-            }
-            out_results[g * expr_count + e] = r;
-          }
-        }
-        free(cm);
-        free(cw);
-      }
-      free(chunk_range);
-      free(chunk_group);
-      free(chunk_base);
-      free(partials);
-      free(sketch);
-      free(dmean);
-      free(dweight);
-    }
-    free(g_start);
-    free(h_offsets);
-    free(h_counts);
-    free(cursor);
+    /* 4b: member lists, group g's members at [start[g], start[g] + count[g]), laid out on the device:
+       group starts and chunk bases by prefix sums, cursors and chunk ranges by kernels, the member
+       reduce per 4096-row chunk, and each group's chunks folded in chunk order (:11826-12215) */
+    ok = csr_reduce(rows, slots, groups, count, offsets, out_count, row_slot, expr_count, funcs, func_codes, arg_f64, params,
+                    out_results);
   }
   free(g_owner);
   free(g_count);

@@ -1,0 +1,138 @@
+"""Per-operator timing: rows/s, GB/s and the kernels behind each operator, on device-resident tables.
+
+    python -m computeql_gb300.opbench [--op NAME ...] [--rows N] [--reps R]
+
+Each operator runs `reps` times after two warm-up calls; the figures are the median wall time of a call
+(through the C ABI, inputs resident, results read back) and the CUDA-event time of its kernels. One
+JSON line per operator. Inputs are synthetic and seeded (splitmix64 on the device, or numpy), shaped
+like the configurations the operators serve:
+
+  sort          ORDER BY one u32 key over `rows` rows
+  sort_f64_2    ORDER BY an f64 measure DESC, then a u32 key, over `rows` rows
+  sort_subset   ORDER BY an f64 measure over the ~200k rows a filter keeps of a 10M-row table
+  fixed         GROUP BY region (50) with SUM/MIN/MAX of a 2-place decimal f64 column
+  hash_group    GROUP BY user_id (1M groups) with COUNT and SUM of an f64 measure over 10M rows
+  hll           APPROX_COUNT_DISTINCT(session) over 10M rows (4M distinct)
+  hash_join     a 1M-row build side (unique keys) probed by 10M rows, pairs counted
+  zone_map      the zone map of one u32 column
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import statistics
+import time
+
+import numpy as np
+
+from . import build, native, ops
+
+OPS = ["sort", "sort_f64_2", "sort_subset", "fixed", "hash_group", "hll", "hash_join", "zone_map"]
+
+
+def _profile():
+    import ctypes as C
+    lib = native.load_cuda()
+    out = {}
+    i = 0
+    while True:
+        name = C.c_char_p()
+        ns = C.c_uint64()
+        cnt = C.c_uint64()
+        if not lib.cqlcuda_kernel_profile_entry(i, C.byref(name), C.byref(ns), C.byref(cnt)):
+            break
+        if cnt.value:
+            out[name.value.decode()] = (ns.value, cnt.value)
+        i += 1
+    return out
+
+
+def _time(fn, reps):
+    lib = native.load_cuda()
+    fn()
+    fn()
+    lib.cqlcuda_kernel_profile_reset()
+    lib.cqlcuda_kernel_profile_enable(1)
+    walls = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn()
+        walls.append((time.perf_counter() - t0) * 1e3)
+    lib.cqlcuda_kernel_profile_enable(0)
+    prof = _profile()
+    kernel_ms = sum(ns for ns, _ in prof.values()) / reps / 1e6
+    kernels = {k: {"ms_per_call": ns / reps / 1e6, "launches_per_call": c / reps} for k, (ns, c) in prof.items()}
+    return statistics.median(walls), kernel_ms, kernels
+
+
+def _lognormal_f64(n, seed):
+    rng = np.random.default_rng(seed)
+    return rng.lognormal(3.0, 1.0, n)
+
+
+def run(op, rows, reps):
+    rng = np.random.default_rng(0)
+    if op == "sort":
+        key = ops.Column.splitmix(rows, 0, 1, 0, 0)
+        fn = lambda: ops.sort_rows([key])
+        n, nbytes = rows, rows * 4
+    elif op == "sort_f64_2":
+        m = ops.Column.from_numpy(_lognormal_f64(rows, 1))
+        k = ops.Column.splitmix(rows, 0, 1, 0, 1000)
+        fn = lambda: ops.sort_rows([m, k], [1, 0])
+        n, nbytes = rows, rows * 12
+    elif op == "sort_subset":
+        total = 10_000_000
+        measure = ops.Column.from_numpy(_lognormal_f64(total, 2))
+        status = rng.integers(0, 50, total).astype(np.uint32)
+        sel_rows = np.nonzero(status == 17)[0].astype(np.uint32)
+        sel = ops.DeviceBuffer(sel_rows.nbytes, sel_rows)
+        fn = lambda: ops.sort_rows([measure], [0], selection=sel)
+        n, nbytes = len(sel_rows), len(sel_rows) * 12
+    elif op == "fixed":
+        region = ops.Column.splitmix(rows, 0, 3, 0, 50)
+        price = ops.Column.from_numpy(rng.integers(0, 10**6, rows) / 100.0)
+        fn = lambda: ops.group_dense_fixed(region, [1, 3, 4], [price, price, price])
+        n, nbytes = rows, rows * 12
+    elif op == "hash_group":
+        total = 10_000_000
+        user = ops.Column.splitmix(total, 0, 2, 0, 1_000_000)
+        measure = ops.Column.from_numpy(_lognormal_f64(total, 3))
+        fn = lambda: ops.group_hash([user], [0, 1], [None, measure], group_hint=1_000_000)
+        n, nbytes = total, total * 12
+    elif op == "hll":
+        total = 10_000_000
+        session = ops.Column.splitmix(total, 0, 2, 1, 4_000_000)
+        fn = lambda: ops.group_hash([], [5], [session])
+        n, nbytes = total, total * 4
+    elif op == "hash_join":
+        build_rows, probe_rows = 1_000_000, 10_000_000
+        bk = ops.Column.from_numpy(rng.permutation(build_rows).astype(np.uint32))
+        pk = ops.Column.splitmix(probe_rows, 0, 1, 0, 1_000_000)
+        fn = lambda: ops.hash_join(bk, pk, want_pairs=False)
+        n, nbytes = probe_rows, (build_rows + probe_rows) * 4
+    elif op == "zone_map":
+        col = ops.Column.splitmix(rows, 0, 1, 0, 100)
+        fn = col.build_zone_map
+        n, nbytes = rows, rows * 4
+    else:
+        raise ValueError(op)
+    wall, kernel_ms, kernels = _time(fn, reps)
+    return {"op": op, "rows": n, "reps": reps, "wall_ms": wall, "kernel_ms": kernel_ms, "rows_per_s": n / (wall / 1e3),
+            "kernel_GBps": nbytes / (kernel_ms / 1e3) / 1e9 if kernel_ms > 0 else None, "bytes": nbytes, "kernels": kernels}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--op", action="append", choices=OPS)
+    ap.add_argument("--rows", type=int, default=100_000_000)
+    ap.add_argument("--reps", type=int, default=5)
+    args = ap.parse_args(argv)
+    build.build()
+    native.init()
+    for op in args.op or OPS:
+        print(json.dumps(run(op, args.rows, args.reps)), flush=True)
+
+
+if __name__ == "__main__":
+    main()

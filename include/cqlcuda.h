@@ -127,6 +127,9 @@ void      cqlcuda_batch_buffer_zero(CqlBatch* batch, CqlBuffer* buffer, uint64_t
 void      cqlcuda_batch_buffer_fill(CqlBatch* batch, CqlBuffer* buffer, uint64_t size, uint32_t value);  /* :214 */
 void      cqlcuda_batch_kernel_execute(CqlBatch* batch, CqlKernel* kernel, uint32_t global_work_size, uint32_t local_work_size); /* :215 */
 void      cqlcuda_batch_buffer_read(CqlBatch* batch, CqlBuffer* buffer, void* out_data, uint64_t size);  /* :216 */
+/* The same from byte `offset` of the buffer (no reference counterpart: a read of one word of a device
+   array, such as the total a prefix sum leaves after its last element). */
+void      cqlcuda_batch_buffer_read_at(CqlBatch* batch, CqlBuffer* buffer, uint64_t offset, void* out_data, uint64_t size);
 int       cqlcuda_batch_end(CqlBatch* batch);                                                            /* :217, 0 on failure (reads zero-filled) */
 
 /* ---- streams (gpu_backend.h:219-229) ---- */

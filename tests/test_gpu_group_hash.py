@@ -176,3 +176,65 @@ def test_small_table_grows_buckets_on_overflow(ops):
     res = ops.group_hash([ops.Column.from_numpy(key)], [COUNT], [None])
     assert res["groups"] == 200_000
     assert np.all(res["counts"] == 2)
+
+
+def test_decimal_arguments_take_the_fixed_path(ops):
+    # f64 decimals of at most 6 places reduce as scaled integers (aggregate_hash_reduce_fixed with the
+    # found scale), finalized as the reference does: bit for bit what the fixed-point oracle gives
+    n = 1_000_003
+    rng = np.random.default_rng(31)
+    key = rng.integers(0, 1000, n).astype(np.uint32)
+    price = rng.integers(-10**7, 10**7, n) / 100.0
+    qty = rng.integers(0, 10**4, n) / 1000.0
+    pc, qc = ops.Column.from_numpy(price), ops.Column.from_numpy(qty)
+    funcs = [COUNT, SUM, AVG, MIN, MAX, SUM]
+    res = ops.group_hash([ops.Column.from_numpy(key)], funcs, [None, pc, pc, pc, pc, qc])
+    assert res["path"] == 2
+    want = oracle.dense_fixed(key.astype(np.float64), funcs, [None, price, price, price, price, qty], [0, 2, 2, 2, 2, 3])
+    got = {int(key[int(res["repr_row"][g])]): res["results"][g] for g in range(res["groups"])}
+    assert len(got) == len(want["keys"])
+    for i, k in enumerate(want["keys"]):
+        assert np.array_equal(got[int(k)].view(np.uint64), want["results"][i].view(np.uint64))
+
+
+def test_million_groups(ops):
+    # GROUP BY user_id over 10M rows (the 30-column event table's 1M-group query)
+    n = 10_000_000
+    rng = np.random.default_rng(41)
+    user = rng.integers(0, 1_000_000, n).astype(np.uint32)
+    measure = rng.lognormal(3.0, 1.0, n)
+    res = ops.group_hash([ops.Column.from_numpy(user)], [COUNT, SUM], [None, ops.Column.from_numpy(measure)], group_hint=1_000_000)
+    assert res["path"] == 1
+    keys = user[res["repr_row"].astype(np.int64)]
+    assert len(np.unique(keys)) == res["groups"] == len(np.unique(user))
+    counts = np.bincount(user, minlength=1_000_000)
+    sums = np.bincount(user, weights=measure, minlength=1_000_000)
+    assert np.array_equal(res["results"][:, 0], counts[keys].astype(np.float64))
+    assert np.array_equal(res["counts"], counts[keys].astype(np.uint64))
+    assert np.all(np.abs(res["results"][:, 1] - sums[keys]) <= 1e-11 * sums[keys])
+    for g in range(0, res["groups"], 99991):
+        exact = math.fsum(measure[user == keys[g]])
+        assert abs(res["results"][g, 1] - exact) <= 1e-12 * exact
+
+
+@pytest.mark.parametrize("groups", [1, 3, 5])
+def test_few_groups_many_rows(ops, groups):
+    # every lane of a warp on a handful of groups: warp-aggregated counts, cursors and sums
+    n = 5_000_000
+    rng = np.random.default_rng(groups)
+    key = rng.integers(0, groups, n).astype(np.uint32)
+    v = rng.integers(-1000, 1000, n).astype(np.int32)
+    d = rng.random(n)
+    kc, vc, dc = ops.Column.from_numpy(key), ops.Column.from_numpy(v), ops.Column.from_numpy(d)
+    fixed = ops.group_hash([kc], [COUNT, SUM, MIN, MAX], [None, vc, vc, vc])
+    assert fixed["path"] == 2
+    csr = ops.group_hash([kc], [COUNT, SUM], [None, dc])
+    assert csr["path"] == 1
+    for g in range(fixed["groups"]):
+        k = key[int(fixed["repr_row"][g])]
+        m = key == k
+        assert list(fixed["results"][g]) == [m.sum(), float(v[m].astype(np.int64).sum()), float(v[m].min()), float(v[m].max())]
+    for g in range(csr["groups"]):
+        k = key[int(csr["repr_row"][g])]
+        exact = math.fsum(d[key == k])
+        assert abs(csr["results"][g, 1] - exact) <= 1e-12 * exact
