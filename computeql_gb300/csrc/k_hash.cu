@@ -687,6 +687,7 @@ __global__ void __launch_bounds__(HASH_THREADS) k_slot_cursor(CqlLaunch a, uint6
   }
 }
 
+// one warp per group: a group of 10M rows has ~2400 chunks
 __global__ void __launch_bounds__(HASH_THREADS) k_chunk_ranges(CqlLaunch a, uint32_t groups, uint32_t per_chunk, uint64_t chunk_cap)
 {
   const uint32_t* start = (const uint32_t*)a.buf[0];
@@ -694,19 +695,35 @@ __global__ void __launch_bounds__(HASH_THREADS) k_chunk_ranges(CqlLaunch a, uint
   const uint32_t* base = (const uint32_t*)a.buf[2];
   uint32_t* range = (uint32_t*)a.buf[3];
   uint32_t* group = (uint32_t*)a.buf[4];
-  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < groups; g += gridDim.x * blockDim.x)
+  uint32_t lane = threadIdx.x & 31u;
+  uint64_t warps = (uint64_t)gridDim.x * (blockDim.x / 32);
+  for (uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; g < groups; g += warps)
   {
     uint32_t n = base[g + 1] - base[g], s = start[g], e = start[g] + count[g];
-    for (uint32_t k = 0; k < n; k++)
+    for (uint32_t k = lane; k < n; k += 32)
     {
       uint64_t c = (uint64_t)base[g] + k;
       if (c >= chunk_cap) break;
       uint32_t first = s + k * per_chunk;
       range[c * 2] = first;
       range[c * 2 + 1] = min(first + per_chunk, e);
-      group[c] = g;
+      group[c] = (uint32_t)g;
     }
   }
+}
+
+// The fold of each group's chunk partials, in chunk order for SUM/AVG (the same sequence of f64
+// additions as the reference's host fold); COUNT, MIN and MAX do not depend on the order (counts are
+// whole numbers far below 2^53). A warp takes 32 consecutive groups: a lane folds its own group when it
+// has few chunks, and the warp folds the groups of many chunks together, one after the other.
+__device__ __forceinline__ double fold_result(uint32_t f, double acc, double cnt, double mn, double mx)
+{
+  if (f == 0) return cnt;
+  if (f == 1) return acc;
+  if (f == 2) return cnt > 0.0 ? __ddiv_rn(acc, cnt) : 0.0;
+  if (f == 3) return mn;
+  if (f == 4) return mx;
+  return 0.0;   // sketches are finished on the host
 }
 
 __global__ void __launch_bounds__(HASH_THREADS) k_group_fold(CqlLaunch a, uint32_t groups, uint32_t exprs, uint32_t codes)
@@ -714,29 +731,75 @@ __global__ void __launch_bounds__(HASH_THREADS) k_group_fold(CqlLaunch a, uint32
   const double* partials = (const double*)a.buf[0];
   const uint32_t* base = (const uint32_t*)a.buf[1];
   double* results = (double*)a.buf[2];
-  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < groups; g += gridDim.x * blockDim.x)
+  uint64_t limit = a.bytes[0] / 32 / exprs;
+  uint32_t lane = threadIdx.x & 31u;
+  uint64_t warps = (uint64_t)gridDim.x * (blockDim.x / 32);
+  for (uint64_t g0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32 * 32; g0 < groups; g0 += warps * 32)
   {
-    for (uint32_t e = 0; e < exprs; e++)
-    {
-      // the host fold of the reference, chunk after chunk (query_exec.c:12180-12215)
-      double acc = 0.0, mn = 1.0e300, mx = -1.0e300, cnt = 0.0;
-      uint64_t limit = a.bytes[0] / 32 / exprs;
-      for (uint32_t c = base[g]; c < base[g + 1] && c < limit; c++)
+    uint64_t g = g0 + lane;
+    uint64_t first = g < groups ? base[g] : 0, end = g < groups ? min((uint64_t)base[g + 1], limit) : 0;
+    bool small = end - first <= 32;
+    if (g < groups && small)
+      for (uint32_t e = 0; e < exprs; e++)
       {
-        const double* pp = &partials[((uint64_t)c * exprs + e) * 4];
-        acc = __dadd_rn(acc, pp[0]);
-        cnt = __dadd_rn(cnt, pp[1]);
-        mn = pp[2] < mn ? pp[2] : mn;
-        mx = pp[3] > mx ? pp[3] : mx;
+        uint32_t f = (codes >> (4 * e)) & 0xfu;
+        if (f > 4) continue;
+        double acc = 0.0, mn = 1.0e300, mx = -1.0e300, cnt = 0.0;
+        for (uint64_t c = first; c < end; c++)
+        {
+          const double* pp = &partials[(c * exprs + e) * 4];
+          acc = __dadd_rn(acc, pp[0]);
+          cnt = __dadd_rn(cnt, pp[1]);
+          mn = pp[2] < mn ? pp[2] : mn;
+          mx = pp[3] > mx ? pp[3] : mx;
+        }
+        results[g * exprs + e] = fold_result(f, acc, cnt, mn, mx);
       }
-      uint32_t f = (codes >> (4 * e)) & 0xfu;
-      double r = 0.0;
-      if (f == 0) r = cnt;
-      else if (f == 1) r = acc;
-      else if (f == 2) r = cnt > 0.0 ? __ddiv_rn(acc, cnt) : 0.0;
-      else if (f == 3) r = mn;
-      else if (f == 4) r = mx;
-      results[(uint64_t)g * exprs + e] = r;
+    uint32_t big = __ballot_sync(0xffffffffu, g < groups && !small);
+    while (big)
+    {
+      uint32_t j = __ffs(big) - 1;
+      big &= big - 1;
+      uint64_t gb = g0 + j;
+      uint64_t bf = __shfl_sync(0xffffffffu, first, j), be = __shfl_sync(0xffffffffu, end, j);
+      for (uint32_t e = 0; e < exprs; e++)
+      {
+        uint32_t f = (codes >> (4 * e)) & 0xfu;
+        if (f > 4) continue;
+        double acc = 0.0, mn = 1.0e300, mx = -1.0e300, cnt = 0.0;
+        bool ordered = f == 1 || f == 2;
+        for (uint64_t c0 = bf; c0 < be; c0 += 32)
+        {
+          uint64_t c = c0 + lane;
+          double p0 = 0.0, p1 = 0.0, p2 = 1.0e300, p3 = -1.0e300;
+          if (c < be)
+          {
+            const double* pp = &partials[(c * exprs + e) * 4];
+            p0 = pp[0];
+            p1 = pp[1];
+            p2 = pp[2];
+            p3 = pp[3];
+          }
+          if (ordered)
+          {
+            uint32_t m = (uint32_t)min((uint64_t)32, be - c0);
+            for (uint32_t k = 0; k < m; k++) acc = __dadd_rn(acc, __shfl_sync(0xffffffffu, p0, k));
+          }
+          // counts (whole numbers), minima and maxima: any order
+          cnt = __dadd_rn(cnt, p1);
+          mn = p2 < mn ? p2 : mn;
+          mx = p3 > mx ? p3 : mx;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+        {
+          cnt = __dadd_rn(cnt, __shfl_xor_sync(0xffffffffu, cnt, o));
+          double lo = __shfl_xor_sync(0xffffffffu, mn, o), hi = __shfl_xor_sync(0xffffffffu, mx, o);
+          mn = lo < mn ? lo : mn;
+          mx = hi > mx ? hi : mx;
+        }
+        if (lane == 0) results[gb * exprs + e] = fold_result(f, acc, cnt, mn, mx);
+      }
     }
   }
 }
@@ -775,7 +838,7 @@ static int launch_chunk_ranges(const CqlLaunch& a, uint32_t gws, uint32_t lws, c
   uint64_t cap = std::min(a.bytes[3] / 8, a.bytes[4] / 4);
   if (per_chunk == 0 || a.bytes[0] < (uint64_t)groups * 4 || a.bytes[1] < (uint64_t)groups * 4 || a.bytes[2] < ((uint64_t)groups + 1) * 4)
     return (int)cudaErrorInvalidValue;
-  k_chunk_ranges<<<cql_stream_grid((groups + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, groups, per_chunk, cap);
+  k_chunk_ranges<<<cql_stream_grid(((uint64_t)groups * 32 + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, groups, per_chunk, cap);
   CQL_LAUNCH_CHECK();
   return 0;
 }
@@ -787,7 +850,7 @@ static int launch_group_fold(const CqlLaunch& a, uint32_t gws, uint32_t lws, cud
   uint32_t groups = cql_word(a, 0), exprs = cql_word(a, 2), codes = cql_word(a, 4);
   if (groups == 0) return 0;
   if (exprs == 0 || exprs > 8 || a.bytes[1] < ((uint64_t)groups + 1) * 4 || a.bytes[2] < (uint64_t)groups * exprs * 8) return (int)cudaErrorInvalidValue;
-  k_group_fold<<<cql_stream_grid((groups + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, groups, exprs, codes);
+  k_group_fold<<<cql_stream_grid(((uint64_t)groups + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, groups, exprs, codes);
   CQL_LAUNCH_CHECK();
   return 0;
 }

@@ -129,11 +129,19 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_count(CqlLaunch a, uint6
   }
 }
 
+// The scatter of one tile: rank every key within the tile in input order (per-warp counters, lanes of
+// one digit found with __match_any_sync), place the tile in shared memory in digit order, then write
+// it out in that order, so consecutive threads write consecutive places of each digit's run.
 template <typename K>
 __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(CqlLaunch a, uint64_t n, uint32_t tiles)
 {
   __shared__ uint32_t warp_count[SORT_WARPS][RADIX];
-  __shared__ uint32_t s_base[RADIX];
+  __shared__ uint32_t s_base[RADIX];     // global place of the tile's first key of each digit
+  __shared__ uint32_t s_start[RADIX];    // place of each digit's first key inside the tile
+  __shared__ uint32_t s_warp_total[SORT_WARPS];
+  extern __shared__ __align__(16) unsigned char s_tile[];
+  K* s_key = (K*)s_tile;
+  uint32_t* s_pos = (uint32_t*)(s_tile + sizeof(K) * SORT_TILE);
   const K* keys_in = (const K*)a.buf[0];
   const uint32_t* pos_in = (const uint32_t*)a.buf[1];
   K* keys_out = (K*)a.buf[2];
@@ -147,10 +155,11 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(CqlLaunch a, uin
   for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x)
   {
     for (uint32_t i = threadIdx.x; i < SORT_WARPS * RADIX; i += SORT_THREADS) (&warp_count[0][0])[i] = 0;
-    // the tile's global base of every digit, once (one load per thread)
     for (uint32_t d = threadIdx.x; d < RADIX; d += SORT_THREADS) s_base[d] = base_of[(uint64_t)d * tiles + tile];
-    // each warp owns 16 rounds of 32 consecutive rows; all its keys and positions are loaded up front
-    uint64_t warp_base = (uint64_t)tile * SORT_TILE + (uint64_t)warp * 32 * SORT_ROUNDS;
+    // each warp owns 16 rounds of 32 consecutive rows; its keys and positions are loaded up front
+    uint64_t tile_first = (uint64_t)tile * SORT_TILE;
+    uint32_t tile_rows = (uint32_t)min((uint64_t)SORT_TILE, n - tile_first);
+    uint64_t warp_base = tile_first + (uint64_t)warp * 32 * SORT_ROUNDS;
     K key[SORT_ROUNDS];
     uint32_t pos[SORT_ROUNDS];
 #pragma unroll
@@ -161,7 +170,6 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(CqlLaunch a, uin
       pos[r] = i < n ? pos_in[i] : 0u;
     }
     __syncthreads();
-    // rank within the warp in input order
     uint32_t local[SORT_ROUNDS];
 #pragma unroll
     for (uint32_t r = 0; r < SORT_ROUNDS; r++)
@@ -176,30 +184,53 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(CqlLaunch a, uin
       __syncwarp();
     }
     __syncthreads();
-    // per digit: the tile's base plus the warps before this one
-    for (uint32_t d = threadIdx.x; d < RADIX; d += SORT_THREADS)
-    {
-      uint32_t run = s_base[d];
+    // per digit (one per thread): the warps before each warp, and the digit's total in the tile
+    uint32_t d = threadIdx.x;
+    uint32_t run = 0;
 #pragma unroll
-      for (uint32_t w = 0; w < SORT_WARPS; w++)
-      {
-        uint32_t c = warp_count[w][d];
-        warp_count[w][d] = run;
-        run += c;
-      }
+    for (uint32_t w = 0; w < SORT_WARPS; w++)
+    {
+      uint32_t c = warp_count[w][d];
+      warp_count[w][d] = run;
+      run += c;
     }
+    // exclusive scan of the digit totals over the block: where each digit starts in the tile
+    uint32_t incl = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31) s_warp_total[warp] = incl;
     __syncthreads();
+    uint32_t warp_prefix = 0;
+    for (uint32_t w = 0; w < warp; w++) warp_prefix += s_warp_total[w];
+    s_start[d] = warp_prefix + incl - run;
+    __syncthreads();
+    // the tile in digit order, in shared memory
 #pragma unroll
     for (uint32_t r = 0; r < SORT_ROUNDS; r++)
     {
       uint64_t i = warp_base + (uint64_t)r * 32 + lane;
       if (i >= n) continue;
-      uint32_t d = (uint32_t)(key[r] >> shift) & 0xffu;
-      uint64_t dst = (uint64_t)warp_count[warp][d] + local[r];
+      uint32_t dd = (uint32_t)(key[r] >> shift) & 0xffu;
+      uint32_t at = s_start[dd] + warp_count[warp][dd] + local[r];
+      s_key[at] = key[r];
+      s_pos[at] = pos[r];
+    }
+    __syncthreads();
+    // out in order: place j of the tile goes to its digit's global base plus its place in the run
+    for (uint32_t j = threadIdx.x; j < tile_rows; j += SORT_THREADS)
+    {
+      K k = s_key[j];
+      uint32_t dd = (uint32_t)(k >> shift) & 0xffu;
+      uint64_t dst = (uint64_t)s_base[dd] + (j - s_start[dd]);
       if (dst < n)
       {
-        if (write_keys) keys_out[dst] = key[r];
-        pos_out[dst] = map_rows ? sel[pos[r]] : pos[r];
+        if (write_keys) keys_out[dst] = k;
+        uint32_t p = s_pos[j];
+        pos_out[dst] = map_rows ? sel[p] : p;
       }
     }
     __syncthreads();
@@ -270,9 +301,16 @@ static int launch_radix_scatter(const CqlLaunch& a, uint32_t gws, uint32_t lws, 
   if ((kb != 4 && kb != 8) || shift >= kb * 8 || a.bytes[0] < n * kb || a.bytes[1] < n * 4 || a.bytes[3] < n * 4 ||
       (write_keys && a.bytes[2] < n * kb) || (uint64_t)tiles * RADIX * 4 > a.bytes[4] || (cql_word(a, 6) && a.bytes[5] < n * 4))
     return (int)cudaErrorInvalidValue;
-  uint32_t grid = cql_stream_grid(tiles, 4);
-  if (kb == 4) k_radix_scatter<uint32_t><<<grid, SORT_THREADS, 0, stream>>>(a, n, tiles);
-  else k_radix_scatter<unsigned long long><<<grid, SORT_THREADS, 0, stream>>>(a, n, tiles);
+  // the tile's keys and positions staged in dynamic shared memory
+  size_t smem = (size_t)SORT_TILE * (kb + 4);
+  const void* fn = kb == 4 ? (const void*)k_radix_scatter<uint32_t> : (const void*)k_radix_scatter<unsigned long long>;
+  // dynamic plus static shared memory passes the default 48 KB for 8-byte keys: opt in
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, SORT_THREADS, smem) != cudaSuccess || per_sm < 1) per_sm = 1;
+  uint32_t grid = cql_stream_grid(tiles, per_sm);
+  if (kb == 4) k_radix_scatter<uint32_t><<<grid, SORT_THREADS, smem, stream>>>(a, n, tiles);
+  else k_radix_scatter<unsigned long long><<<grid, SORT_THREADS, smem, stream>>>(a, n, tiles);
   CQL_LAUNCH_CHECK();
   return 0;
 }
