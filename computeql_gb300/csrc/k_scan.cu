@@ -312,7 +312,7 @@ static int launch_scan_simple(const CqlLaunch& a, uint32_t gws, uint32_t lws, cu
   if (rows == 0) return 0;
   uint64_t groups = (rows + ROWS_PER_THREAD - 1) / ROWS_PER_THREAD;
   uint64_t ctas = (groups + SCAN_THREADS - 1) / SCAN_THREADS;
-  uint32_t grid = cql_stream_grid(ctas, 6);
+  uint32_t grid = cql_stream_grid(ctas, 8);
   bool count_only = a.bytes[3] < 8;
   if (count_only) k_scan_simple<true><<<grid, SCAN_THREADS, 0, stream>>>(a, rows);
   else k_scan_simple<false><<<grid, SCAN_THREADS, 0, stream>>>(a, rows);
