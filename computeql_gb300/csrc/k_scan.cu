@@ -645,7 +645,48 @@ static int launch_zone_map(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaS
   return 0;
 }
 
+// ---------------------------------------------------------------------------------------------
+// cql_batch_fold: the batched scan's per-CTA partials [cta][query] x (count, sum low, sum high) summed
+// over the CTAs in order into [query] x (count, low, high) (128-bit integer sums, so any order gives the
+// same bits); binding 0 partials, 1 out; word 0 queries, word 2 CTAs.
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_batch_fold(CqlLaunch a, uint32_t nq, uint32_t ctas)
+{
+  const unsigned long long* parts = (const unsigned long long*)a.buf[0];
+  unsigned long long* out = (unsigned long long*)a.buf[1];
+  uint64_t pcap = a.bytes[0] / 24;
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x)
+  {
+    unsigned long long c = 0, lo = 0, hi = 0;
+    for (uint32_t b = 0; b < ctas; b++)
+    {
+      uint64_t at = (uint64_t)b * nq + q;
+      if (at >= pcap) break;
+      c += parts[at * 3];
+      unsigned long long l2 = lo + parts[at * 3 + 1];
+      hi += parts[at * 3 + 2] + (l2 < lo ? 1ull : 0ull);
+      lo = l2;
+    }
+    out[q * 3] = c;
+    out[q * 3 + 1] = lo;
+    out[q * 3 + 2] = hi;
+  }
+}
+
+static int launch_batch_fold(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint32_t nq = cql_word(a, 0), ctas = cql_word(a, 2);
+  if (nq == 0) return 0;
+  if (a.bytes[1] < (uint64_t)nq * 24) return (int)cudaErrorInvalidValue;
+  k_batch_fold<<<cql_stream_grid((nq + SCAN_THREADS - 1) / SCAN_THREADS, 8), SCAN_THREADS, 0, stream>>>(a, nq, ctas);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
 const CqlKernelDesc cql_kernels_scan[] = {
+  { "cql_batch_fold", launch_batch_fold },
   { "cql_zone_map", launch_zone_map },
   { "scan_simple", launch_scan_simple },
   { "scan_filter", launch_scan_filter },

@@ -1,0 +1,713 @@
+/*
+ * cql_batch.c - many filter/aggregate queries over one table in one shared scan.
+ *
+ * SELECT COUNT(*), SUM(col) FROM t WHERE <query q's condition>, for q = 0 .. Q-1, answered by one pass
+ * over the table: the batched form of the per-query fused filter+aggregate (qe_fused_filter_aggregate,
+ * src/query_exec/query_exec.c:9888-10254, generated kernel query_kernel.c:1538-1614).
+ *
+ *  1. Each query's program is rebound so that every column is read from the register block of its
+ *     column index, and queries whose rebound bytecode is the same word for word share a shape. The
+ *     shape is emitted once as a predicate (cql_codegen_batch_predicate) and evaluated for each of its
+ *     queries; a shape's literals differ per query only.
+ *  2. The literals of a comparison with a column become per-query thresholds on the host: an interval
+ *     of (sign-biased) codes for whole-number columns and of order keys for f64 columns, float bounds
+ *     rounded down/up for f32 columns - integer work per row, the same answer as the reference's
+ *     comparison in double.
+ *  3. SUM is accumulated exactly in 128-bit integers of the value scaled by 2^k, k chosen from the
+ *     column's range so that one row is below 2^55 in magnitude: the sum of the matched rows is then
+ *     exact up to 2^-(k+1) per row (below 1e-16 of the largest value), independent of order. A query
+ *     whose bound is not far below 1e-12 of its sum is answered again by the per-query fused kernel.
+ *  4. One warp owns its accumulators in shared memory (no atomics); a CTA folds its warps, a second
+ *     kernel folds the CTAs in order. At most CQL_BATCH_LAUNCH_QUERIES queries go into one launch.
+ */
+#include "cqlops.h"
+#include "cql_codegen.h"
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define QE_GPU_WORKGROUP_SIZE 256
+#define BATCH_MAX_SITES 16
+#define BATCH_MAX_CONSTS 32
+#define CQL_BATCH_LAUNCH_QUERIES 384
+#define BATCH_MAX_SHAPES 256
+
+void cqlops_note_error(const char* why);
+
+static int refuse(const char* why)
+{
+  cqlops_note_error(why);
+  return 0;
+}
+
+enum
+{
+  OP_LOAD_NUM_COL = 1, OP_PUSH_CONST = 2, OP_CMP_EQ = 3, OP_CMP_NE = 4, OP_CMP_LT = 5, OP_CMP_GT = 6, OP_CMP_LE = 7, OP_CMP_GE = 8,
+  OP_STR_EQ = 11, OP_STR_CONTAINS = 12, OP_TRIGRAM_SIM = 15, OP_EDIT_DISTANCE = 16, OP_STR_NE = 17, OP_STR_GE = 21,
+};
+
+/* a threshold, 32 bytes: a/b the interval (low, span), c = invert (or the op of a float test), d = strict */
+typedef struct
+{
+  uint64_t a, b;
+  uint32_t c, d;
+  uint64_t pad;
+} Thr;
+
+/* ---- thresholds, worked out on the host ---- */
+
+/* whole-number column: match = ((code - lo) <= span) != invert over the (sign-biased) 32-bit code; the
+   same rules as the per-query kernel's cql_thr_int */
+static void thr_int(double c, int op, int biased, Thr* t)
+{
+  memset(t, 0, sizeof(*t));
+  t->b = 0xffffffffu;
+  double off = biased ? 2147483648.0 : 0.0;
+  if (c != c)
+  {
+    t->c = op != OP_CMP_NE;
+    return;
+  }
+  double lo = -1e300, hi = 1e300;
+  int ne = 0;
+  if (op == OP_CMP_EQ || op == OP_CMP_NE)
+  {
+    if (floor(c) != c)
+    {
+      t->c = op == OP_CMP_EQ;
+      return;
+    }
+    lo = c;
+    hi = c;
+    ne = op == OP_CMP_NE;
+  }
+  else if (op == OP_CMP_LT) hi = ceil(c) - 1.0;
+  else if (op == OP_CMP_LE) hi = floor(c);
+  else if (op == OP_CMP_GT) lo = floor(c) + 1.0;
+  else lo = ceil(c);
+  lo += off;
+  hi += off;
+  if (lo < 0.0) lo = 0.0;
+  if (hi > 4294967295.0) hi = 4294967295.0;
+  if (lo > hi)
+  {
+    t->c = !ne;
+    return;
+  }
+  t->a = (uint32_t)lo;
+  t->b = (uint32_t)(hi - lo);
+  t->c = (uint32_t)ne;
+}
+
+static float f32_down(double c)
+{
+  float f = (float)c;
+  if ((double)f > c) f = nextafterf(f, -INFINITY);
+  return f;
+}
+
+static float f32_up(double c)
+{
+  float f = (float)c;
+  if ((double)f < c) f = nextafterf(f, INFINITY);
+  return f;
+}
+
+/* f32 column: the literal rounded down/up to floats, as the per-query kernel's cql_thr_f32 */
+static void thr_f32(double c, int op, Thr* t)
+{
+  memset(t, 0, sizeof(*t));
+  float v = NAN;
+  uint32_t strict = 1;
+  if (c == c)
+  {
+    float fd = f32_down(c), fu = f32_up(c);
+    if (op == OP_CMP_LT)
+    {
+      v = fd;
+      strict = (double)fd == c;
+    }
+    else if (op == OP_CMP_LE) v = fd;
+    else if (op == OP_CMP_GT)
+    {
+      v = fu;
+      strict = (double)fu == c;
+    }
+    else if (op == OP_CMP_GE) v = fu;
+    else if ((double)fd == c) v = fd;
+  }
+  uint32_t bits;
+  memcpy(&bits, &v, 4);
+  t->a = bits;
+  t->c = (uint32_t)op;
+  t->d = strict;
+}
+
+static uint64_t f64_key(double x)
+{
+  uint64_t b;
+  memcpy(&b, &x, 8);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+/* f64 column: an interval of order keys ((bits >> 63) ? ~bits : bits | sign bit). -0.0 and +0.0 have
+   neighbouring keys, which the intervals of a zero literal cover together; NaN keys lie beyond the
+   infinities, outside every interval (so only != matches a NaN, as in double). */
+static void thr_f64(double c, int op, Thr* t)
+{
+  memset(t, 0, sizeof(*t));
+  const uint64_t kninf = f64_key(-INFINITY), kpinf = f64_key(INFINITY);
+  const uint64_t kz_neg = 0x7fffffffffffffffull, kz_pos = 0x8000000000000000ull;
+  if (c != c)
+  {
+    t->b = ~0ull;
+    t->c = op != OP_CMP_NE;
+    return;
+  }
+  int zero = c == 0.0;
+  uint64_t kc = f64_key(c);
+  uint64_t lo, hi;
+  int ne = 0;
+  switch (op)
+  {
+    case OP_CMP_EQ: case OP_CMP_NE:
+      lo = zero ? kz_neg : kc;
+      hi = zero ? kz_pos : kc;
+      ne = op == OP_CMP_NE;
+      break;
+    case OP_CMP_LT:
+      lo = kninf;
+      hi = zero ? kz_neg - 1 : kc - 1;
+      if (c == -INFINITY) lo = 1, hi = 0;
+      break;
+    case OP_CMP_LE:
+      lo = kninf;
+      hi = zero ? kz_pos : kc;
+      break;
+    case OP_CMP_GT:
+      lo = zero ? kz_pos + 1 : kc + 1;
+      hi = kpinf;
+      if (c == INFINITY) lo = 1, hi = 0;
+      break;
+    default:
+      lo = zero ? kz_neg : kc;
+      hi = kpinf;
+      break;
+  }
+  if (lo > hi)
+  {
+    /* nothing matches: the inverted full range */
+    t->a = 0;
+    t->b = ~0ull;
+    t->c = 1;
+    return;
+  }
+  t->a = lo;
+  t->b = hi - lo;
+  t->c = (uint32_t)ne;
+}
+
+static double const_value(const CqlProgram* p, uint32_t index)
+{
+  uint64_t bits = ((uint64_t)p->consts[2 * index + 1] << 32) | p->consts[2 * index];
+  double v;
+  memcpy(&v, &bits, 8);
+  return v;
+}
+
+/* the program with each column load reading the register block of its column index */
+static int rebind(const CqlProgram* p, uint32_t column_count, CqlProgram* out)
+{
+  memcpy(out, p, sizeof(*out));
+  int slot_column[CQLOPS_MAX_BINDINGS];
+  for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++) slot_column[s] = -1;
+  for (uint32_t b = 0; b < p->binding_count; b++)
+    if (p->binding_slot[b] < CQLOPS_MAX_BINDINGS) slot_column[p->binding_slot[b]] = (int)p->binding_column[b];
+  uint64_t ip = 0;
+  while (ip < p->word_count)
+  {
+    uint32_t op = p->words[ip++];
+    if (op == OP_LOAD_NUM_COL)
+    {
+      if (ip >= p->word_count) return 0;
+      uint32_t operand = p->words[ip];
+      uint32_t slot = operand & 0xffu;
+      if (slot >= CQLOPS_MAX_BINDINGS || slot_column[slot] < 0 || (uint32_t)slot_column[slot] >= column_count) return 0;
+      out->words[ip] = (operand & ~0xffu) | (uint32_t)slot_column[slot];
+      ip++;
+    }
+    else if (op == OP_PUSH_CONST) ip++;
+    else if ((op >= OP_STR_EQ && op <= OP_STR_CONTAINS) || (op >= OP_STR_NE && op <= OP_STR_GE) || op == OP_TRIGRAM_SIM || op == OP_EDIT_DISTANCE)
+      return 0;
+  }
+  return 1;
+}
+
+static uint64_t words_hash(const CqlProgram* p)
+{
+  uint64_t h = 1469598103934665603ull;
+  for (uint32_t i = 0; i < p->word_count; i++) h = (h ^ p->words[i]) * 1099511628211ull;
+  return h ^ p->word_count;
+}
+
+/* ---- the generated kernel ---- */
+
+typedef struct
+{
+  char* p;
+  size_t n, cap;
+  int failed;
+} Buf;
+
+static void bput(Buf* b, const char* fmt, ...)
+{
+  if (b->failed) return;
+  va_list ap;
+  for (;;)
+  {
+    va_start(ap, fmt);
+    int need = vsnprintf(b->p ? b->p + b->n : NULL, b->p ? b->cap - b->n : 0, fmt, ap);
+    va_end(ap);
+    if (need < 0)
+    {
+      b->failed = 1;
+      return;
+    }
+    if (b->p && b->n + (size_t)need < b->cap)
+    {
+      b->n += (size_t)need;
+      return;
+    }
+    size_t nc = (b->cap ? b->cap * 2 : 16384) + (size_t)need;
+    char* q = (char*)realloc(b->p, nc);
+    if (!q)
+    {
+      b->failed = 1;
+      return;
+    }
+    b->p = q;
+    b->cap = nc;
+  }
+}
+
+static int type_bytes(int t)
+{
+  if (t == CQLOPS_TYPE_F64 || t == CQLOPS_TYPE_U64 || t == CQLOPS_TYPE_I64) return 8;
+  if (t == CQLOPS_TYPE_BOOL) return 1;
+  return 4;
+}
+
+static const char* BATCH_PRELUDE =
+  "typedef unsigned int u32;\n"
+  "typedef unsigned long long u64;\n"
+  "struct CqlLaunch { void* buf[16]; u64 bytes[16]; u64 push[8]; };\n"
+  "struct Thr { u64 a, b; u32 c, d; u64 pad; };\n"
+  "__device__ __forceinline__ u32 cql_word(const CqlLaunch& a, u32 i) { u64 s = a.push[i >> 1]; return (i & 1u) ? (u32)(s >> 32) : (u32)s; }\n"
+  "__device__ __forceinline__ uint4 cql_ld4(const void* p) { uint4 v; asm volatile(\"ld.global.cs.v4.u32 {%0,%1,%2,%3}, [%4];\" : \"=r\"(v.x), \"=r\"(v.y), \"=r\"(v.z), \"=r\"(v.w) : \"l\"(p)); return v; }\n"
+  "__device__ __forceinline__ bool cql_bi(const Thr* t, u32 code) { return ((code - (u32)t->a) <= (u32)t->b) != (t->c != 0u); }\n"
+  "__device__ __forceinline__ bool cql_bd(const Thr* t, u64 bits) { u64 k = (bits >> 63) ? ~bits : (bits | 0x8000000000000000ull); return ((k - t->a) <= t->b) != (t->c != 0u); }\n"
+  "__device__ __forceinline__ bool cql_bf(const Thr* t, float v) { float x = __uint_as_float((u32)t->a); u32 op = t->c; bool s = t->d != 0u;\n"
+  "  if (op == 5u) return s ? v < x : v <= x; if (op == 7u) return v <= x; if (op == 6u) return s ? v > x : v >= x; if (op == 8u) return v >= x;\n"
+  "  if (op == 3u) return v == x; return v != x; }\n"
+  "__device__ __forceinline__ double cql_i64d(u64 x) { double u = (double)(u32)(x >> 32) * 4294967296.0 + (double)(u32)x; return (x >> 63) ? u - 18446744073709551616.0 : u; }\n";
+
+/* the source of one launch: `shape_exprs` over `shapes` shapes, the register blocks of slot_type */
+static char* batch_source(char** shape_exprs, uint32_t shapes, const int* slot_type, const int* sum_cols, uint32_t sum_col_count,
+                          uint32_t rows_per_thread)
+{
+  Buf b;
+  memset(&b, 0, sizeof(b));
+  bput(&b, "// cql: block=256 smem=%u per_sm=2\n", 8u * CQL_BATCH_LAUNCH_QUERIES * 24u);
+  bput(&b, "%s", BATCH_PRELUDE);
+  for (uint32_t s = 0; s < shapes; s++) bput(&b, "#define CQL_SHAPE_%u(k) (%s)\n", s, shape_exprs[s]);
+  bput(&b,
+       "extern \"C\" __global__ void __launch_bounds__(256) cql_main(CqlLaunch a)\n{\n"
+       "  const u64 rows = cql_word(a, 0); const u32 nq = cql_word(a, 2); const u32 q0 = cql_word(a, 4);\n"
+       "  const double* col_scale = (const double*)a.buf[0];\n"
+       "  const Thr* thr = (const Thr*)a.buf[1];\n"
+       "  const double* qconst = (const double*)a.buf[2];\n"
+       "  const u32* qsum = (const u32*)a.buf[3];\n"
+       "  const u32* shape_begin = (const u32*)a.buf[4];\n"
+       "  u64* partials = (u64*)a.buf[5]; const u64 pcap = a.bytes[5] / 24ull;\n"
+       "  extern __shared__ u64 s_acc[];   /* [warp][query][count, lo, hi] */\n"
+       "  const u32 lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;\n"
+       "  for (u32 i = threadIdx.x; i < warps * nq * 3u; i += blockDim.x) s_acc[i] = 0ull;\n"
+       "  __syncthreads();\n"
+       "  u64* acc = s_acc + (u64)warp * nq * 3u;\n"
+       "  const u32 RPT = %uu;\n"
+       "  const u64 groups = (rows + RPT - 1ull) / RPT; const u64 per_pass = (u64)gridDim.x * blockDim.x;\n"
+       "  for (u64 g0 = (u64)blockIdx.x * blockDim.x; g0 < groups; g0 += per_pass)\n  {\n"
+       "    const u64 row0 = (g0 + threadIdx.x) * RPT;\n"
+       "    const u32 valid = row0 < rows ? (u32)min((u64)RPT, rows - row0) : 0u;\n",
+       rows_per_thread);
+  /* the register blocks */
+  for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++)
+  {
+    int t = slot_type[s];
+    if (!t) continue;
+    int w = type_bytes(t);
+    bput(&b, "    %s r%d[%u];\n", w == 8 ? "u64" : "u32", s, rows_per_thread);
+    if (w == 8)
+      bput(&b, "    for (u32 v = 0; v < RPT; v++) r%d[v] = v < valid ? ((const u64*)a.buf[%d])[row0 + v] : 0ull;\n", s, 6 + s);
+    else if (w == 1)
+      bput(&b, "    for (u32 v = 0; v < RPT; v++) r%d[v] = v < valid ? (u32)((const unsigned char*)a.buf[%d])[row0 + v] : 0u;\n", s, 6 + s);
+    else
+      bput(&b,
+           "    if (valid == RPT && (RPT & 3u) == 0u) { for (u32 v = 0; v < RPT; v += 4) { uint4 q = cql_ld4((const u32*)a.buf[%d] + row0 + v); r%d[v] = q.x; r%d[v + 1] = q.y; r%d[v + 2] = q.z; r%d[v + 3] = q.w; } }\n"
+           "    else { for (u32 v = 0; v < RPT; v++) r%d[v] = v < valid ? ((const u32*)a.buf[%d])[row0 + v] : 0u; }\n",
+           6 + s, s, s, s, s, s, 6 + s);
+  }
+  /* the summed columns as scaled integers, once per row */
+  for (uint32_t i = 0; i < sum_col_count; i++)
+  {
+    int c = sum_cols[i];
+    int t = slot_type[c];
+    const char* val = t == CQLOPS_TYPE_F64 ? "__longlong_as_double((long long)r%d[v])"
+                    : t == CQLOPS_TYPE_F32 ? "(double)__uint_as_float(r%d[v])"
+                    : t == CQLOPS_TYPE_I32 ? "(double)(int)r%d[v]"
+                    : t == CQLOPS_TYPE_U64 ? "(double)r%d[v]"
+                    : t == CQLOPS_TYPE_I64 ? "cql_i64d(r%d[v])"
+                                           : "(double)r%d[v]";
+    bput(&b, "    long long fx%d[%u];\n    { const double sc = col_scale[%d]; for (u32 v = 0; v < RPT; v++) { double x = ", c, rows_per_thread, c);
+    bput(&b, val, c);
+    bput(&b, "; fx%d[v] = v < valid ? __double2ll_rn(x * sc) : 0ll; } }\n", c);
+  }
+  for (uint32_t s = 0; s < shapes; s++)
+  {
+    bput(&b,
+         "    for (u32 q = shape_begin[%u]; q < shape_begin[%u]; q++)\n    {\n"
+         "      const Thr* TH = thr + (u64)(q0 + q) * %uu; const double* QC = qconst + (u64)(q0 + q) * %uu;\n"
+         "      u32 m = 0u;\n"
+         "#pragma unroll\n"
+         "      for (u32 k = 0; k < RPT; k++) if (k < valid && (CQL_SHAPE_%u(k))) m |= 1u << k;\n"
+         "      const u32 cnt = __reduce_add_sync(0xffffffffu, (u32)__popc(m));\n"
+         "      const u32 sc = qsum[q0 + q];\n"
+         "      long long sv = 0ll;\n",
+         s, s + 1, BATCH_MAX_SITES, BATCH_MAX_CONSTS, s);
+    for (uint32_t i = 0; i < sum_col_count; i++)
+      bput(&b, "      if (sc == %du) { for (u32 k = 0; k < RPT; k++) sv += ((m >> k) & 1u) ? fx%d[k] : 0ll; }\n", sum_cols[i], sum_cols[i]);
+    bput(&b,
+         "      if (sc != 0xffffffffu) { for (int o = 16; o > 0; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o); }\n"
+         "      if (lane == 0u)\n      {\n"
+         "        u64* e = acc + (u64)q * 3u; e[0] += cnt;\n"
+         "        u64 lo = e[1] + (u64)sv; e[2] += (u64)(sv < 0 ? -1ll : 0ll) + (lo < (u64)sv ? 1ull : 0ull); e[1] = lo;\n"
+         "      }\n    }\n");
+  }
+  bput(&b,
+       "  }\n"
+       "  __syncthreads();\n"
+       "  for (u32 q = threadIdx.x; q < nq; q += blockDim.x)\n  {\n"
+       "    u64 c = 0ull, lo = 0ull, hi = 0ull;\n"
+       "    for (u32 w = 0; w < warps; w++) { const u64* e = s_acc + ((u64)w * nq + q) * 3u; c += e[0]; u64 l2 = lo + e[1]; hi += e[2] + (l2 < lo ? 1ull : 0ull); lo = l2; }\n"
+       "    const u64 at = (u64)blockIdx.x * nq + q;\n"
+       "    if (at < pcap) { partials[at * 3] = c; partials[at * 3 + 1] = lo; partials[at * 3 + 2] = hi; }\n"
+       "  }\n}\n");
+  if (b.failed)
+  {
+    free(b.p);
+    return NULL;
+  }
+  return b.p;
+}
+
+/* ---- the operator ---- */
+
+static uint64_t fnv_str(const char* s)
+{
+  uint64_t h = 1469598103934665603ull;
+  for (; *s; s++) h = (h ^ (unsigned char)*s) * 1099511628211ull;
+  return h;
+}
+
+static CqlBuffer* pooled(const char* name, uint64_t size, uint32_t flags)
+{
+  return cqlcuda_buffer_alloc_pooled(name, (uint64_t)strlen(name), size ? size : 8, flags, NULL);
+}
+
+int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
+                                  const int32_t* sum_columns, uint32_t rows_per_thread, uint64_t* out_counts, double* out_sums,
+                                  uint32_t* out_shapes)
+{
+  cqlops_note_error("");
+  if (query_count == 0) return 1;
+  if (column_count == 0 || column_count > CQLOPS_MAX_BINDINGS) return refuse("1 to 10 columns");
+  if (rows_per_thread != 4 && rows_per_thread != 8 && rows_per_thread != 16) rows_per_thread = 8;
+  uint64_t rows = columns[0].rows;
+  for (uint32_t c = 0; c < column_count; c++)
+  {
+    const CqlColumn* col = &columns[c];
+    if (col->rows != rows || !col->buffer || col->width != 0 || col->type == CQLOPS_TYPE_STRING8)
+      return refuse("batched columns are full-width numeric columns of one length");
+  }
+  /* per query: rebound program, shape, thresholds, literals */
+  CqlProgram* rb = (CqlProgram*)malloc(sizeof(CqlProgram));
+  uint64_t* shape_hash = (uint64_t*)malloc(query_count * 8);
+  uint32_t* shape_of = (uint32_t*)malloc(query_count * 4);
+  uint32_t* order = (uint32_t*)malloc(query_count * 4);
+  Thr* thr = (Thr*)calloc((size_t)query_count * BATCH_MAX_SITES, sizeof(Thr));
+  double* qconst = (double*)calloc((size_t)query_count * BATCH_MAX_CONSTS, sizeof(double));
+  uint32_t* qsum = (uint32_t*)malloc(query_count * 4);
+  char* exprs[BATCH_MAX_SHAPES];
+  uint64_t shape_keys[BATCH_MAX_SHAPES];
+  uint32_t shapes = 0;
+  int slot_type[CQLOPS_MAX_BINDINGS] = { 0 };
+  int ok = rb && shape_hash && shape_of && order && thr && qconst && qsum;
+  char why[160] = "";
+  for (uint32_t q = 0; ok && q < query_count; q++)
+  {
+    const CqlProgram* p = programs[q];
+    if (!p || p->const_count > BATCH_MAX_CONSTS || !rebind(p, column_count, rb))
+    {
+      snprintf(why, sizeof(why), "query %u cannot be batched (strings, or more than %d literals)", q, BATCH_MAX_CONSTS);
+      ok = 0;
+      break;
+    }
+    CqlBatchSite sites[BATCH_MAX_SITES];
+    uint32_t site_count = 0;
+    int st[CQLOPS_MAX_BINDINGS];
+    char* expr = NULL;
+    if (!cql_codegen_batch_predicate(rb, sites, BATCH_MAX_SITES, &site_count, st, &expr, why, sizeof(why)))
+    {
+      ok = 0;
+      break;
+    }
+    for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++)
+    {
+      if (!st[s]) continue;
+      if (slot_type[s] && slot_type[s] != st[s])
+      {
+        snprintf(why, sizeof(why), "column %d read as two types", s);
+        ok = 0;
+      }
+      slot_type[s] = st[s];
+    }
+    uint64_t h = words_hash(rb);
+    uint32_t s = 0;
+    while (s < shapes && !(shape_keys[s] == h && !strcmp(exprs[s], expr))) s++;
+    if (s == shapes)
+    {
+      if (shapes == BATCH_MAX_SHAPES)
+      {
+        snprintf(why, sizeof(why), "more than %d query shapes in one batch", BATCH_MAX_SHAPES);
+        free(expr);
+        ok = 0;
+        break;
+      }
+      shape_keys[s] = h;
+      exprs[s] = expr;
+      shapes++;
+    }
+    else
+      free(expr);
+    shape_of[q] = s;
+    for (uint32_t i = 0; i < site_count; i++)
+    {
+      double c = const_value(p, sites[i].const_index);
+      int t = (int)sites[i].col_type;
+      Thr* th = &thr[(uint64_t)q * BATCH_MAX_SITES + i];
+      if (t == CQLOPS_TYPE_F32) thr_f32(c, (int)sites[i].op, th);
+      else if (t == CQLOPS_TYPE_F64) thr_f64(c, (int)sites[i].op, th);
+      else thr_int(c, (int)sites[i].op, t == CQLOPS_TYPE_I32 || t == 9, th);
+    }
+    for (uint32_t i = 0; i < p->const_count; i++) qconst[(uint64_t)q * BATCH_MAX_CONSTS + i] = const_value(p, i);
+    int32_t sc = sum_columns ? sum_columns[q] : -1;
+    if (sc >= (int32_t)column_count)
+    {
+      snprintf(why, sizeof(why), "query %u sums a column outside the table", q);
+      ok = 0;
+      break;
+    }
+    qsum[q] = sc < 0 ? 0xffffffffu : (uint32_t)sc;
+  }
+  /* summed columns: loaded, scaled by 2^k with k from the column's range */
+  int sum_cols[CQLOPS_MAX_BINDINGS];
+  uint32_t sum_col_count = 0;
+  double col_scale[CQLOPS_MAX_BINDINGS] = { 0 };
+  double col_max[CQLOPS_MAX_BINDINGS] = { 0 };
+  for (uint32_t q = 0; ok && q < query_count; q++)
+  {
+    if (qsum[q] == 0xffffffffu) continue;
+    int c = (int)qsum[q];
+    uint32_t i = 0;
+    while (i < sum_col_count && sum_cols[i] != c) i++;
+    if (i < sum_col_count) continue;
+    const CqlColumn* col = &columns[c];
+    if (!col->has_range)
+    {
+      snprintf(why, sizeof(why), "a summed column needs its range");
+      ok = 0;
+      break;
+    }
+    if (!slot_type[c]) slot_type[c] = (int)col->type;
+    double m = fabs(col->zone_min) > fabs(col->zone_max) ? fabs(col->zone_min) : fabs(col->zone_max);
+    int e = 0;
+    if (m > 0.0) frexp(m, &e);   /* m < 2^e */
+    col_scale[c] = ldexp(1.0, 55 - e);
+    col_max[c] = m;
+    sum_cols[sum_col_count++] = c;
+  }
+  /* queries grouped by shape */
+  uint32_t* shape_count = (uint32_t*)calloc(shapes + 1, 4);
+  ok = ok && shape_count;
+  if (ok)
+  {
+    for (uint32_t q = 0; q < query_count; q++) shape_count[shape_of[q]]++;
+    uint32_t* start = (uint32_t*)malloc((shapes + 1) * 4);
+    if (!start) ok = 0;
+    else
+    {
+      uint32_t run = 0;
+      for (uint32_t s = 0; s < shapes; s++)
+      {
+        start[s] = run;
+        run += shape_count[s];
+      }
+      for (uint32_t q = 0; q < query_count; q++) order[start[shape_of[q]]++] = q;
+      free(start);
+    }
+  }
+  /* thresholds, literals and sums in shape order */
+  Thr* thr_o = ok ? (Thr*)malloc((size_t)query_count * BATCH_MAX_SITES * sizeof(Thr)) : NULL;
+  double* qc_o = ok ? (double*)malloc((size_t)query_count * BATCH_MAX_CONSTS * sizeof(double)) : NULL;
+  uint32_t* qs_o = ok ? (uint32_t*)malloc(query_count * 4) : NULL;
+  ok = ok && thr_o && qc_o && qs_o;
+  if (ok)
+    for (uint32_t i = 0; i < query_count; i++)
+    {
+      uint32_t q = order[i];
+      memcpy(&thr_o[(uint64_t)i * BATCH_MAX_SITES], &thr[(uint64_t)q * BATCH_MAX_SITES], sizeof(Thr) * BATCH_MAX_SITES);
+      memcpy(&qc_o[(uint64_t)i * BATCH_MAX_CONSTS], &qconst[(uint64_t)q * BATCH_MAX_CONSTS], sizeof(double) * BATCH_MAX_CONSTS);
+      qs_o[i] = qsum[q];
+    }
+  uint64_t* folded = ok ? (uint64_t*)malloc((size_t)query_count * 24) : NULL;
+  ok = ok && folded;
+  /* launches of at most CQL_BATCH_LAUNCH_QUERIES queries, each the shapes of its slice */
+  CqlBuffer* scale_buf = ok ? pooled("batch_col_scale", sizeof(col_scale), CQLCUDA_BUFFER_WRITE) : NULL;
+  CqlBuffer* thr_buf = ok ? pooled("batch_thresholds", (uint64_t)query_count * BATCH_MAX_SITES * sizeof(Thr), CQLCUDA_BUFFER_WRITE) : NULL;
+  CqlBuffer* qc_buf = ok ? pooled("batch_literals", (uint64_t)query_count * BATCH_MAX_CONSTS * 8, CQLCUDA_BUFFER_WRITE) : NULL;
+  CqlBuffer* qs_buf = ok ? pooled("batch_sum_columns", (uint64_t)query_count * 4, CQLCUDA_BUFFER_WRITE) : NULL;
+  CqlBuffer* begin_buf = ok ? pooled("batch_shape_begin", (BATCH_MAX_SHAPES + 1) * 4, CQLCUDA_BUFFER_WRITE) : NULL;
+  CqlBuffer* out_buf = ok ? pooled("batch_folded", (uint64_t)query_count * 24, CQLCUDA_BUFFER_READ_WRITE) : NULL;
+  CqlKernel* fold = ok ? cqlcuda_kernel_alloc("cql_batch_fold", 14) : NULL;
+  ok = ok && scale_buf && thr_buf && qc_buf && qs_buf && begin_buf && out_buf && fold;
+  if (ok)
+  {
+    CqlBatch* b = cqlcuda_batch_begin(0, 0);
+    cqlcuda_batch_buffer_write(b, scale_buf, col_scale, sizeof(col_scale));
+    cqlcuda_batch_buffer_write(b, thr_buf, thr_o, (uint64_t)query_count * BATCH_MAX_SITES * sizeof(Thr));
+    cqlcuda_batch_buffer_write(b, qc_buf, qc_o, (uint64_t)query_count * BATCH_MAX_CONSTS * 8);
+    cqlcuda_batch_buffer_write(b, qs_buf, qs_o, (uint64_t)query_count * 4);
+    ok = cqlcuda_batch_end(b);
+  }
+  uint32_t sm = cqlcuda_sm_count();
+  uint64_t ctas = (uint64_t)(sm ? sm : 152) * 2;
+  for (uint32_t first = 0; ok && first < query_count; first += CQL_BATCH_LAUNCH_QUERIES)
+  {
+    uint32_t nq = query_count - first < CQL_BATCH_LAUNCH_QUERIES ? query_count - first : CQL_BATCH_LAUNCH_QUERIES;
+    /* the shapes of this slice, in order, and where each starts */
+    uint32_t begin[BATCH_MAX_SHAPES + 1];
+    char* slice_exprs[BATCH_MAX_SHAPES];
+    uint32_t ns = 0;
+    for (uint32_t i = 0; i < nq; i++)
+    {
+      uint32_t s = shape_of[order[first + i]];
+      if (ns == 0 || slice_exprs[ns - 1] != exprs[s])
+      {
+        slice_exprs[ns] = exprs[s];
+        begin[ns] = i;
+        ns++;
+      }
+    }
+    begin[ns] = nq;
+    char* src = batch_source(slice_exprs, ns, slot_type, sum_cols, sum_col_count, rows_per_thread);
+    if (!src)
+    {
+      ok = 0;
+      break;
+    }
+    char name[64];
+    snprintf(name, sizeof(name), "qk_batch_%016llx", (unsigned long long)fnv_str(src));
+    size_t nlen = strlen(name);
+    CqlKernel* k = cqlcuda_kernel_alloc(name, nlen);
+    if (!k) k = cqlcuda_kernel_alloc_from_image(name, nlen, src, strlen(src));
+    free(src);
+    if (!k)
+    {
+      ok = 0;
+      break;
+    }
+    CqlBuffer* parts = pooled("batch_partials", ctas * nq * 24, CQLCUDA_BUFFER_READ_WRITE);
+    if (!parts)
+    {
+      ok = 0;
+      break;
+    }
+    cqlcuda_kernel_set_arg_buffer(k, 0, scale_buf);
+    cqlcuda_kernel_set_arg_buffer(k, 1, thr_buf);
+    cqlcuda_kernel_set_arg_buffer(k, 2, qc_buf);
+    cqlcuda_kernel_set_arg_buffer(k, 3, qs_buf);
+    cqlcuda_kernel_set_arg_buffer(k, 4, begin_buf);
+    cqlcuda_kernel_set_arg_buffer(k, 5, parts);
+    for (uint32_t c = 0; c < CQLOPS_MAX_BINDINGS; c++)
+      cqlcuda_kernel_set_arg_buffer(k, 6 + c, columns[c < column_count ? c : 0].buffer);
+    cqlcuda_kernel_set_arg_u64(k, 0, rows);
+    cqlcuda_kernel_set_arg_u64(k, 1, nq);
+    cqlcuda_kernel_set_arg_u64(k, 2, first);
+    cqlcuda_kernel_set_arg_buffer(fold, 0, parts);
+    cqlcuda_kernel_set_arg_buffer_range(fold, 1, out_buf, (uint64_t)first * 24, (uint64_t)nq * 24);
+    cqlcuda_kernel_set_arg_u64(fold, 0, nq);
+    cqlcuda_kernel_set_arg_u64(fold, 1, ctas);
+    CqlBatch* b = cqlcuda_batch_begin((ns + 1) * 4, 0);
+    cqlcuda_batch_buffer_write(b, begin_buf, begin, (ns + 1) * 4);
+    cqlcuda_batch_buffer_zero(b, parts, ctas * nq * 24);
+    cqlcuda_batch_kernel_execute(b, k, (uint32_t)(ctas * QE_GPU_WORKGROUP_SIZE), QE_GPU_WORKGROUP_SIZE);
+    cqlcuda_batch_kernel_execute(b, fold, nq, QE_GPU_WORKGROUP_SIZE);
+    ok = cqlcuda_batch_end(b);
+  }
+  if (ok)
+  {
+    CqlBatch* b = cqlcuda_batch_begin(0, (uint64_t)query_count * 24);
+    cqlcuda_batch_buffer_read(b, out_buf, folded, (uint64_t)query_count * 24);
+    ok = cqlcuda_batch_end(b);
+  }
+  if (ok)
+  {
+    for (uint32_t i = 0; i < query_count; i++)
+    {
+      uint32_t q = order[i];
+      uint64_t cnt = folded[i * 3], lo = folded[i * 3 + 1];
+      int64_t hi = (int64_t)folded[i * 3 + 2];
+      out_counts[q] = cnt;
+      if (!out_sums) continue;
+      if (qsum[q] == 0xffffffffu)
+      {
+        out_sums[q] = 0.0;
+        continue;
+      }
+      /* the 128-bit scaled sum, back to a double: hi * 2^64 + lo, then / 2^k */
+      double v = (double)hi * 18446744073709551616.0 + (double)lo;
+      out_sums[q] = v / col_scale[qsum[q]];
+    }
+    if (out_shapes) *out_shapes = shapes;
+  }
+  else if (why[0])
+    refuse(why);
+  for (uint32_t s = 0; s < shapes; s++) free(exprs[s]);
+  free(rb);
+  free(shape_hash);
+  free(shape_of);
+  free(order);
+  free(thr);
+  free(qconst);
+  free(qsum);
+  free(shape_count);
+  free(thr_o);
+  free(qc_o);
+  free(qs_o);
+  free(folded);
+  (void)col_max;
+  return ok;
+}

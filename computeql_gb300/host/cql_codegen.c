@@ -18,6 +18,7 @@
  * reference's comparison in double.
  */
 #include "cqlops.h"
+#include "cql_codegen.h"
 
 #include <stdarg.h>
 #include <stdio.h>
@@ -143,6 +144,10 @@ typedef struct
   int sites;
   int failed;
   char why[128];
+  /* batch mode: thresholds and literals come from the query's tables (TH, QC), the sites are listed */
+  int batch;
+  CqlBatchSite* batch_sites;
+  uint32_t batch_cap;
 } Gen;
 
 static void gen_fail(Gen* g, const char* why)
@@ -181,6 +186,25 @@ static char* column_vs_const(Gen* g, const Val* col, const Val* k, int op)
 {
   int site = g->sites++;
   int t = col->col_type;
+  if (g->batch)
+  {
+    if ((uint32_t)site >= g->batch_cap)
+    {
+      gen_fail(g, "too many comparisons for one batched query");
+      return dupf("false");
+    }
+    CqlBatchSite* bs = &g->batch_sites[site];
+    bs->const_index = (uint32_t)k->const_index;
+    bs->op = (uint32_t)op;
+    bs->col_type = (uint32_t)t;
+    bs->pad = 0;
+    if (t == CQLOPS_TYPE_U32 || t == 12 || t == CQLOPS_TYPE_BOOL) return dupf("cql_bi(TH + %d, r%d[k])", site, col->col_slot);
+    if (t == CQLOPS_TYPE_I32 || t == 9) return dupf("cql_bi(TH + %d, r%d[k] ^ 0x80000000u)", site, col->col_slot);
+    if (t == CQLOPS_TYPE_F32) return dupf("cql_bf(TH + %d, __uint_as_float(r%d[k]))", site, col->col_slot);
+    if (t == CQLOPS_TYPE_F64) return dupf("cql_bd(TH + %d, r%d[k])", site, col->col_slot);
+    gen_fail(g, "a 64-bit integer comparison is not batched");
+    return dupf("false");
+  }
   if (t == CQLOPS_TYPE_U32 || t == 12 || t == CQLOPS_TYPE_BOOL || t == CQLOPS_TYPE_I32 || t == 9)
   {
     int bias = (t == CQLOPS_TYPE_I32 || t == 9);
@@ -261,12 +285,12 @@ static char* build_expression(Gen* g)
         if (sp >= 64 || ip >= p->word_count) { gen_fail(g, "stack"); break; }
         uint32_t index = p->words[ip++];
         if (index >= p->const_count) { gen_fail(g, "constant index"); break; }
-        if (!consts_seen[index])
+        if (!consts_seen[index] && !g->batch)
         {
           consts_seen[index] = 1;
           sprintf_(&g->pro, "  const double K%u = cql_const(a, %uu);\n", index, index);
         }
-        stack[sp].text = dupf("K%u", index);
+        stack[sp].text = g->batch ? dupf("QC[%u]", index) : dupf("K%u", index);
         stack[sp].is_bool = 0;
         stack[sp].col_slot = -1;
         stack[sp].const_index = (int)index;
@@ -320,6 +344,11 @@ static char* build_expression(Gen* g)
       }
       case OP_STR_EQ: case OP_STR_NE: case OP_STR_LT: case OP_STR_GT: case OP_STR_LE: case OP_STR_GE: case OP_STR_CONTAINS:
       {
+        if (g->batch)
+        {
+          gen_fail(g, "string comparisons are not batched");
+          break;
+        }
         if (sp >= 64 || ip + 3 > p->word_count) { gen_fail(g, "stack"); break; }
         uint32_t slot = p->words[ip], wo = p->words[ip + 1], len = p->words[ip + 2];
         ip += 3;
@@ -728,4 +757,27 @@ int cqlops_program_source(const CqlProgram* prog, uint32_t kind, const CqlFusedA
   }
   free(s.p);
   return ok;
+}
+
+int cql_codegen_batch_predicate(const CqlProgram* prog, CqlBatchSite* sites, uint32_t site_cap, uint32_t* site_count, int* slot_type,
+                                char** expr, char* why, size_t why_cap)
+{
+  Gen g;
+  memset(&g, 0, sizeof(g));
+  g.prog = prog;
+  g.batch = 1;
+  g.batch_sites = sites;
+  g.batch_cap = site_cap;
+  char* e = build_expression(&g);
+  free(g.pro.p);
+  if (g.failed || !e)
+  {
+    free(e);
+    if (why && why_cap) snprintf(why, why_cap, "%s", g.failed ? g.why : "empty program");
+    return 0;
+  }
+  *site_count = (uint32_t)g.sites;
+  for (int i = 0; i < CQLOPS_MAX_BINDINGS; i++) slot_type[i] = g.slot_type[i];
+  *expr = e;
+  return 1;
 }

@@ -15,6 +15,8 @@ like the configurations the operators serve:
   hll           APPROX_COUNT_DISTINCT(session) over 10M rows (4M distinct)
   hash_join     a 1M-row build side (unique keys) probed by 10M rows, pairs counted
   zone_map      the zone map of one u32 column
+  batch         512 COUNT+SUM queries over 29 WHERE shapes on a table of 4 u32 + 4 f64 columns, in one shared
+                scan (cqlops_batch_filter_aggregate) and, for comparison, one generated kernel per query
 """
 from __future__ import annotations
 
@@ -27,7 +29,7 @@ import numpy as np
 
 from . import build, native, ops
 
-OPS = ["sort", "sort_f64_2", "sort_subset", "fixed", "hash_group", "hll", "hash_join", "zone_map"]
+OPS = ["sort", "sort_f64_2", "sort_subset", "fixed", "hash_group", "hll", "hash_join", "zone_map", "batch"]
 
 
 def _profile():
@@ -111,6 +113,8 @@ def run(op, rows, reps):
         pk = ops.Column.splitmix(probe_rows, 0, 1, 0, 1_000_000)
         fn = lambda: ops.hash_join(bk, pk, want_pairs=False)
         n, nbytes = probe_rows, (build_rows + probe_rows) * 4
+    elif op == "batch":
+        return run_batch(rows, reps)
     elif op == "zone_map":
         col = ops.Column.splitmix(rows, 0, 1, 0, 100)
         fn = col.build_zone_map
@@ -120,6 +124,81 @@ def run(op, rows, reps):
     wall, kernel_ms, kernels = _time(fn, reps)
     return {"op": op, "rows": n, "reps": reps, "wall_ms": wall, "kernel_ms": kernel_ms, "rows_per_s": n / (wall / 1e3),
             "kernel_GBps": nbytes / (kernel_ms / 1e3) / 1e9 if kernel_ms > 0 else None, "bytes": nbytes, "kernels": kernels}
+
+
+def _batch_queries(count, shape_count, seed):
+    """WHERE shapes drawn like the reference's per-query kernel benchmark (pc_random_shape,
+    src/tests/bench_perquery_compile.c:238-258): 1-8 range comparisons over the 8 columns, one in four
+    joined by OR, one parenthesised pair when there are 4 or more; each query a shape with new literals."""
+    u32, f64 = ["u0", "u1", "u2", "u3"], ["d0", "d1", "d2", "d3"]
+    cols = u32 + f64
+    srng = np.random.default_rng(seed)
+    states = [int(srng.integers(0, 2**63)) for _ in range(shape_count)]
+    qrng = np.random.default_rng(seed + 1)
+
+    def lit(c):
+        return int(qrng.integers(0, 1 << 16)) if c[0] == "u" else round(float(qrng.random()), 6)
+
+    def shape(state):
+        r = np.random.default_rng(state)
+        n = 1 + int(r.integers(0, 8))
+        leaves, join = [], []
+        for _ in range(n):
+            c = cols[int(r.integers(0, len(cols)))]
+            upper, inclusive = bool(r.integers(0, 2)), bool(r.integers(0, 2))
+            op = ("<=" if inclusive else "<") if upper else (">=" if inclusive else ">")
+            leaves.append(f"({op} {c} {lit(c)!r})")
+            join.append(int(r.integers(0, 4)) == 0)
+        items, i = [], 0
+        group = int(r.integers(0, n - 2)) if n >= 4 else None
+        if group is not None:
+            join[group] = not join[group + 1]
+        while i < n:
+            if i == group:
+                items += [f"({'or' if join[i] else 'and'} {leaves[i]} {leaves[i + 1]})", "or" if join[i + 1] else "and"]
+                i += 2
+            else:
+                items += [leaves[i], "or" if join[i] else "and"]
+                i += 1
+        items = items[:-1]
+        terms, cur = [], [items[0]]
+        for k in range(1, len(items), 2):
+            if items[k] == "and":
+                cur.append(items[k + 1])
+            else:
+                terms.append(cur)
+                cur = [items[k + 1]]
+        terms.append(cur)
+
+        def chain(o, xs):
+            out = xs[0]
+            for x in xs[1:]:
+                out = f"({o} {out} {x})"
+            return out
+        return chain("or", [chain("and", t) for t in terms])
+
+    return [(shape(states[q % shape_count]), f64[q % 4]) for q in range(count)]
+
+
+def run_batch(rows, reps):
+    rng = np.random.default_rng(4)
+    cols = {f"u{i}": ops.Column.splitmix(rows, 4, 8, i, 1 << 16) for i in range(4)}
+    cols.update({f"d{i}": ops.Column.from_numpy(rng.random(rows)) for i in range(4)})
+    qs = _batch_queries(512, 29, 9)
+    progs = [ops.Program(w, cols) for w, _ in qs]
+    sums = [s for _, s in qs]
+    best = None
+    for rpt in (4, 8, 16):
+        # the tuning knob: rows per thread of the generated kernel, the fastest kept
+        wall, kernel_ms, kernels = _time(lambda: ops.batch_aggregate(progs, sums, rpt), reps)
+        if best is None or wall < best[1]:
+            best = (rpt, wall, kernel_ms, kernels)
+    one_wall, one_kernel, _ = _time(lambda: [ops.fused_aggregate(p, [s]) for p, s in zip(progs, sums)], max(1, reps // 2))
+    nbytes = rows * (4 * 4 + 4 * 8)
+    return {"op": "batch", "rows": rows, "queries": len(qs), "shapes": 29, "reps": reps, "rows_per_thread": best[0],
+            "wall_ms": best[1], "kernel_ms": best[2], "rows_per_s": len(qs) * rows / (best[1] / 1e3),
+            "kernel_GBps": nbytes / (best[2] / 1e3) / 1e9, "bytes": nbytes, "kernels": best[3],
+            "one_at_a_time_wall_ms": one_wall, "one_at_a_time_kernel_ms": one_kernel, "speedup_wall": one_wall / best[1]}
 
 
 def main(argv=None):

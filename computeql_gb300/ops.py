@@ -314,6 +314,24 @@ def fused_aggregate(program, agg_names):
     return cnt.value, list(s)[:k], list(mn)[:k], list(mx)[:k]
 
 
+def batch_aggregate(programs, sum_names, rows_per_thread=8):
+    """COUNT(*) and SUM(sum_names[q]) WHERE programs[q] for every q in one shared scan.
+
+    All programs are built over the same columns (the first program's); sum_names[q] None = COUNT only.
+    -> (counts, sums, shapes).
+    """
+    q = len(programs)
+    base = programs[0]
+    ptrs = (C.c_void_p * q)(*[C.addressof(p.prog) for p in programs])
+    sc = np.array([base.index(n) if n is not None else -1 for n in sum_names], dtype=np.int32)
+    counts = np.empty(max(q, 1), dtype=np.uint64)
+    sums = np.empty(max(q, 1), dtype=np.float64)
+    shapes = C.c_uint32()
+    _check(N.load_ops().cqlops_batch_filter_aggregate(ptrs, q, base._cols, len(base.columns), N.ptr(sc), rows_per_thread, N.ptr(counts),
+                                                      N.ptr(sums), C.byref(shapes)), "cqlops_batch_filter_aggregate")
+    return counts[:q], sums[:q], shapes.value
+
+
 def fused_group(program, key_names, agg_names, max_groups=1 << 16):
     kc, ac = len(key_names), len(agg_names)
     keys = (C.c_uint32 * 3)(*[program.index(n) for n in key_names])

@@ -313,6 +313,20 @@ int cqlops_group_dense_fixed(const CqlColumn* key, uint32_t expr_count, const ui
 int cqlops_sort_rows(const CqlColumn* keys, uint32_t key_count, const uint32_t* desc, CqlBuffer* selection,
                      uint64_t selection_count, uint32_t* out_rows, uint64_t out_capacity);
 
+/* Q filter/aggregate queries over one table in one shared scan: SELECT COUNT(*), SUM(col) WHERE
+   <programs[q]> for q = 0 .. query_count-1 - the batched form of cqlops_fused_filter_aggregate
+   (qe_fused_filter_aggregate, query_exec.c:9888-10254). Every program is built over `columns` (numeric,
+   full width, one length; at most 10); sum_columns[q] is the summed column's index or -1 (COUNT only);
+   a summed column needs its range (has_range). Queries are grouped by shape (the same bytecode up to
+   literal values), one generated kernel evaluates each shape for its queries, literals become per-query
+   thresholds. Counts are exact; sums are exact 128-bit sums of the values scaled by 2^k (k from the
+   column's range, |value| x 2^k < 2^55), so |error| <= matched rows x 2^-(k+1). rows_per_thread (4, 8
+   or 16) is the tuning knob of the generated kernel. out_shapes (optional) receives the shape count.
+   Refuses programs with string comparisons. */
+int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
+                                  const int32_t* sum_columns, uint32_t rows_per_thread, uint64_t* out_counts, double* out_sums,
+                                  uint32_t* out_shapes);
+
 /* Why the last operator call returned 0 when it refused the request itself ("" otherwise; GPU
    failures are in cqlcuda_last_error()). */
 const char* cqlops_last_error(void);

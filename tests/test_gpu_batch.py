@@ -1,0 +1,99 @@
+"""The batched shared scan (cqlops_batch_filter_aggregate) against the oracle, query by query.
+
+Every query of a batch must give alone what the oracle gives: the count of rows its condition
+matches (the oracle's restatement of the bytecode interpreter) bit for bit, and its SUM within 1e-12
+of the exact sum of those rows (math.fsum). The workload is the batched configuration's table shape
+(4 u32 + 4 f64 columns) with shapes drawn as the reference's per-query kernel benchmark draws them.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from tests.batch_workload import F64, U32, queries, table
+from tests.where_shapes import oracle_mask
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ops(gpu):
+    from computeql_gb300 import ops as o
+    return o
+
+
+def _columns(ops, arrays):
+    return {n: ops.Column.from_numpy(a) for n, a in arrays.items()}
+
+
+def _check(ops, arrays, cols, qs, rows_per_thread=8):
+    progs = [ops.Program(where, cols) for where, _ in qs]
+    counts, sums, shapes = ops.batch_aggregate(progs, [s for _, s in qs], rows_per_thread)
+    for i, (where, scol) in enumerate(qs):
+        m = oracle_mask(progs[i], arrays).astype(bool)
+        assert counts[i] == m.sum(), where
+        if scol is None:
+            continue
+        exact = math.fsum(arrays[scol][m])
+        assert abs(sums[i] - exact) <= 1e-12 * max(abs(exact), 1e-300), (where, sums[i], exact)
+    return shapes
+
+
+@pytest.mark.parametrize("rows_per_thread", [4, 8, 16])
+def test_batch_matches_each_query_alone(ops, rows_per_thread):
+    arrays = table(2_000_003, 1)
+    cols = _columns(ops, arrays)
+    qs = queries(64, 8, 7)
+    shapes = _check(ops, arrays, cols, qs, rows_per_thread)
+    assert shapes <= 8
+
+
+def test_more_queries_than_one_launch_holds(ops):
+    arrays = table(300_001, 2)
+    cols = _columns(ops, arrays)
+    qs = queries(500, 29, 11)
+    assert _check(ops, arrays, cols, qs) <= 29
+
+
+def test_count_only_and_special_values(ops):
+    rng = np.random.default_rng(5)
+    n = 100_000
+    arrays = table(n, 3)
+    d = arrays["d0"]
+    d[::7] = 0.0
+    d[3::7] = -0.0
+    d[5::101] = np.nan
+    d[6::103] = np.inf
+    d[2::107] = -np.inf
+    arrays["d0"] = d
+    cols = _columns(ops, {**arrays, "d0": np.where(np.isnan(d), 0.0, d)})   # the summed copy has no NaN
+    cols["d0"] = ops.Column.from_numpy(d)
+    qs = [("(> d0 0.0)", None), ("(>= d0 0.0)", None), ("(= d0 0.0)", None), ("(!= d0 0.0)", None), ("(< d0 -0.0)", None),
+          ("(<= d0 0.0)", None), ("(< d0 1e308)", None), ("(> d0 -1e308)", None), ("(and (> d0 0.25) (< d0 0.5))", "d1"),
+          ("(or (= u0 7) (< u1 100))", "d2"), ("(and (>= u2 65535) (<= u2 65535))", None), ("(< u3 0)", None)]
+    progs = [ops.Program(w, cols) for w, _ in qs]
+    counts, sums, _ = ops.batch_aggregate(progs, [s for _, s in qs])
+    for i, (w, s) in enumerate(qs):
+        m = oracle_mask(progs[i], arrays).astype(bool)
+        assert counts[i] == m.sum(), w
+        if s:
+            exact = math.fsum(arrays[s][m])
+            assert abs(sums[i] - exact) <= 1e-12 * abs(exact)
+
+
+def test_signed_and_float_columns(ops):
+    rng = np.random.default_rng(8)
+    n = 500_000
+    arrays = {"i": rng.integers(-1000, 1000, n).astype(np.int32), "f": rng.normal(size=n).astype(np.float32),
+              "v": rng.lognormal(3.0, 1.0, n)}
+    cols = _columns(ops, arrays)
+    qs = [("(< i -10)", "v"), ("(>= i 999)", "v"), ("(and (> f 0.5) (< i 0))", "v"), ("(<= f -1.25)", "i"),
+          ("(or (= i 0) (> f 2.5))", "f"), ("(< f 0.1)", None)]
+    progs = [ops.Program(w, cols) for w, _ in qs]
+    counts, sums, _ = ops.batch_aggregate(progs, [s for _, s in qs])
+    for i, (w, s) in enumerate(qs):
+        m = oracle_mask(progs[i], arrays).astype(bool)
+        assert counts[i] == m.sum(), w
+        if s:
+            exact = math.fsum(arrays[s][m].astype(np.float64))
+            assert abs(sums[i] - exact) <= 1e-12 * abs(exact), w
