@@ -13,12 +13,13 @@
  *     of (sign-biased) codes for whole-number columns and of order keys for f64 columns, float bounds
  *     rounded down/up for f32 columns - integer work per row, the same answer as the reference's
  *     comparison in double.
- *  3. SUM is accumulated exactly in 128-bit integers of the value scaled by 2^k, k chosen from the
- *     column's range so that one row is below 2^55 in magnitude: the sum of the matched rows is then
- *     exact up to 2^-(k+1) per row (below 1e-16 of the largest value), independent of order. A query
- *     whose bound is not far below 1e-12 of its sum is answered again by the per-query fused kernel.
- *  4. One warp owns its accumulators in shared memory (no atomics); a CTA folds its warps, a second
- *     kernel folds the CTAs in order. At most CQL_BATCH_LAUNCH_QUERIES queries go into one launch.
+ *  3. SUM is accumulated exactly in integers of the value scaled by 2^k, k chosen from the column's range
+ *     and the rows one warp can see so that a warp's total stays below 2^62: the sum of the matched rows
+ *     is then exact up to 2^-(k+1) per row, independent of order (for the configured tables, far below
+ *     1e-16 of the largest value).
+ *  4. One warp owns its accumulators in shared memory (a 32-bit count and a 64-bit sum per query, no
+ *     atomics); a CTA folds its warps into 128-bit sums, a second kernel folds the CTAs in order. At
+ *     most CQL_BATCH_LAUNCH_QUERIES queries go into one launch.
  */
 #include "cqlops.h"
 #include "cql_codegen.h"
@@ -33,6 +34,7 @@
 #define BATCH_MAX_SITES 16
 #define BATCH_MAX_CONSTS 32
 #define CQL_BATCH_LAUNCH_QUERIES 384
+#define BATCH_CTAS_PER_SM 6
 #define BATCH_MAX_SHAPES 256
 
 void cqlops_note_error(const char* why);
@@ -315,12 +317,12 @@ static const char* BATCH_PRELUDE =
   "__device__ __forceinline__ double cql_i64d(u64 x) { double u = (double)(u32)(x >> 32) * 4294967296.0 + (double)(u32)x; return (x >> 63) ? u - 18446744073709551616.0 : u; }\n";
 
 /* the source of one launch: `shape_exprs` over `shapes` shapes, the register blocks of slot_type */
-static char* batch_source(char** shape_exprs, uint32_t shapes, const int* slot_type, const int* sum_cols, uint32_t sum_col_count,
-                          uint32_t rows_per_thread)
+static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint32_t shapes, const int* slot_type, const int* sum_cols,
+                          uint32_t sum_col_count, uint32_t rows_per_thread)
 {
   Buf b;
   memset(&b, 0, sizeof(b));
-  bput(&b, "// cql: block=256 smem=%u per_sm=2\n", 8u * CQL_BATCH_LAUNCH_QUERIES * 24u);
+  bput(&b, "// cql: block=256 smem=%u per_sm=%u\n", 8u * CQL_BATCH_LAUNCH_QUERIES * 12u, BATCH_CTAS_PER_SM);
   bput(&b, "%s", BATCH_PRELUDE);
   for (uint32_t s = 0; s < shapes; s++) bput(&b, "#define CQL_SHAPE_%u(k) (%s)\n", s, shape_exprs[s]);
   bput(&b,
@@ -332,11 +334,12 @@ static char* batch_source(char** shape_exprs, uint32_t shapes, const int* slot_t
        "  const u32* qsum = (const u32*)a.buf[3];\n"
        "  const u32* shape_begin = (const u32*)a.buf[4];\n"
        "  u64* partials = (u64*)a.buf[5]; const u64 pcap = a.bytes[5] / 24ull;\n"
-       "  extern __shared__ u64 s_acc[];   /* [warp][query][count, lo, hi] */\n"
+       "  extern __shared__ u64 s_acc[];   /* [warp][query] sums, then [warp][query] counts */\n"
        "  const u32 lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;\n"
-       "  for (u32 i = threadIdx.x; i < warps * nq * 3u; i += blockDim.x) s_acc[i] = 0ull;\n"
+       "  u32* s_cnt = (u32*)(s_acc + (u64)warps * nq);\n"
+       "  for (u32 i = threadIdx.x; i < warps * nq; i += blockDim.x) { s_acc[i] = 0ull; s_cnt[i] = 0u; }\n"
        "  __syncthreads();\n"
-       "  u64* acc = s_acc + (u64)warp * nq * 3u;\n"
+       "  long long* acc = (long long*)s_acc + (u64)warp * nq; u32* cacc = s_cnt + (u64)warp * nq;\n"
        "  const u32 RPT = %uu;\n"
        "  const u64 groups = (rows + RPT - 1ull) / RPT; const u64 per_pass = (u64)gridDim.x * blockDim.x;\n"
        "  for (u64 g0 = (u64)blockIdx.x * blockDim.x; g0 < groups; g0 += per_pass)\n  {\n"
@@ -377,31 +380,38 @@ static char* batch_source(char** shape_exprs, uint32_t shapes, const int* slot_t
   }
   for (uint32_t s = 0; s < shapes; s++)
   {
+    /* the query's thresholds into registers once, before its rows */
+    char decls[BATCH_MAX_SITES * 40 + 1];
+    size_t dn = 0;
+    decls[0] = 0;
+    for (uint32_t i = 0; i < shape_sites[s] && i < BATCH_MAX_SITES; i++)
+      dn += (size_t)snprintf(decls + dn, sizeof(decls) - dn, "      const Thr T%u = TH[%u];\n", i, i);
     bput(&b,
          "    for (u32 q = shape_begin[%u]; q < shape_begin[%u]; q++)\n    {\n"
          "      const Thr* TH = thr + (u64)(q0 + q) * %uu; const double* QC = qconst + (u64)(q0 + q) * %uu;\n"
+         "      (void)TH; (void)QC;\n"
+         "%s"
          "      u32 m = 0u;\n"
          "#pragma unroll\n"
          "      for (u32 k = 0; k < RPT; k++) if (k < valid && (CQL_SHAPE_%u(k))) m |= 1u << k;\n"
          "      const u32 cnt = __reduce_add_sync(0xffffffffu, (u32)__popc(m));\n"
          "      const u32 sc = qsum[q0 + q];\n"
          "      long long sv = 0ll;\n",
-         s, s + 1, BATCH_MAX_SITES, BATCH_MAX_CONSTS, s);
+         s, s + 1, BATCH_MAX_SITES, BATCH_MAX_CONSTS, decls, s);
     for (uint32_t i = 0; i < sum_col_count; i++)
       bput(&b, "      if (sc == %du) { for (u32 k = 0; k < RPT; k++) sv += ((m >> k) & 1u) ? fx%d[k] : 0ll; }\n", sum_cols[i], sum_cols[i]);
     bput(&b,
          "      if (sc != 0xffffffffu) { for (int o = 16; o > 0; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o); }\n"
-         "      if (lane == 0u)\n      {\n"
-         "        u64* e = acc + (u64)q * 3u; e[0] += cnt;\n"
-         "        u64 lo = e[1] + (u64)sv; e[2] += (u64)(sv < 0 ? -1ll : 0ll) + (lo < (u64)sv ? 1ull : 0ull); e[1] = lo;\n"
-         "      }\n    }\n");
+         "      if (lane == 0u) { cacc[q] += cnt; acc[q] += sv; }\n"
+         "    }\n");
   }
   bput(&b,
        "  }\n"
        "  __syncthreads();\n"
        "  for (u32 q = threadIdx.x; q < nq; q += blockDim.x)\n  {\n"
        "    u64 c = 0ull, lo = 0ull, hi = 0ull;\n"
-       "    for (u32 w = 0; w < warps; w++) { const u64* e = s_acc + ((u64)w * nq + q) * 3u; c += e[0]; u64 l2 = lo + e[1]; hi += e[2] + (l2 < lo ? 1ull : 0ull); lo = l2; }\n"
+       "    for (u32 w = 0; w < warps; w++) { long long v = (long long)s_acc[(u64)w * nq + q]; c += s_cnt[(u64)w * nq + q];\n"
+       "      u64 l2 = lo + (u64)v; hi += (u64)(v < 0 ? -1ll : 0ll) + (l2 < lo ? 1ull : 0ull); lo = l2; }\n"
        "    const u64 at = (u64)blockIdx.x * nq + q;\n"
        "    if (at < pcap) { partials[at * 3] = c; partials[at * 3 + 1] = lo; partials[at * 3 + 2] = hi; }\n"
        "  }\n}\n");
@@ -427,9 +437,10 @@ static CqlBuffer* pooled(const char* name, uint64_t size, uint32_t flags)
   return cqlcuda_buffer_alloc_pooled(name, (uint64_t)strlen(name), size ? size : 8, flags, NULL);
 }
 
-int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
-                                  const int32_t* sum_columns, uint32_t rows_per_thread, uint64_t* out_counts, double* out_sums,
-                                  uint32_t* out_shapes)
+/* the operator, or with source_only the source of its first launch (no device work) */
+static int batch_run(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
+                     const int32_t* sum_columns, uint32_t rows_per_thread, uint64_t* out_counts, double* out_sums, uint32_t* out_shapes,
+                     int source_only, char* src_out, uint64_t src_cap, uint64_t* src_len)
 {
   cqlops_note_error("");
   if (query_count == 0) return 1;
@@ -439,7 +450,7 @@ int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t qu
   for (uint32_t c = 0; c < column_count; c++)
   {
     const CqlColumn* col = &columns[c];
-    if (col->rows != rows || !col->buffer || col->width != 0 || col->type == CQLOPS_TYPE_STRING8)
+    if (col->rows != rows || (!col->buffer && !source_only) || col->width != 0 || col->type == CQLOPS_TYPE_STRING8)
       return refuse("batched columns are full-width numeric columns of one length");
   }
   /* per query: rebound program, shape, thresholds, literals */
@@ -451,6 +462,7 @@ int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t qu
   double* qconst = (double*)calloc((size_t)query_count * BATCH_MAX_CONSTS, sizeof(double));
   uint32_t* qsum = (uint32_t*)malloc(query_count * 4);
   char* exprs[BATCH_MAX_SHAPES];
+  uint32_t shape_sites[BATCH_MAX_SHAPES];
   uint64_t shape_keys[BATCH_MAX_SHAPES];
   uint32_t shapes = 0;
   int slot_type[CQLOPS_MAX_BINDINGS] = { 0 };
@@ -498,6 +510,7 @@ int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t qu
       }
       shape_keys[s] = h;
       exprs[s] = expr;
+      shape_sites[s] = site_count;
       shapes++;
     }
     else
@@ -523,6 +536,7 @@ int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t qu
     qsum[q] = sc < 0 ? 0xffffffffu : (uint32_t)sc;
   }
   /* summed columns: loaded, scaled by 2^k with k from the column's range */
+  uint32_t sm_count = cqlcuda_sm_count();
   int sum_cols[CQLOPS_MAX_BINDINGS];
   uint32_t sum_col_count = 0;
   double col_scale[CQLOPS_MAX_BINDINGS] = { 0 };
@@ -545,7 +559,13 @@ int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t qu
     double m = fabs(col->zone_min) > fabs(col->zone_max) ? fabs(col->zone_min) : fabs(col->zone_max);
     int e = 0;
     if (m > 0.0) frexp(m, &e);   /* m < 2^e */
-    col_scale[c] = ldexp(1.0, 55 - e);
+    /* the rows one warp accumulates: its passes over the grid, 32 lanes x rows_per_thread each */
+    uint64_t groups = (rows + rows_per_thread - 1) / rows_per_thread;
+    uint64_t per_pass = (uint64_t)(sm_count ? sm_count : 152) * BATCH_CTAS_PER_SM * QE_GPU_WORKGROUP_SIZE;
+    uint64_t warp_rows = ((groups + per_pass - 1) / per_pass) * 32 * rows_per_thread;
+    int wr = 0;
+    frexp((double)warp_rows, &wr);   /* warp_rows < 2^wr */
+    col_scale[c] = ldexp(1.0, 62 - e - wr);
     col_max[c] = m;
     sum_cols[sum_col_count++] = c;
   }
@@ -584,16 +604,52 @@ int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t qu
     }
   uint64_t* folded = ok ? (uint64_t*)malloc((size_t)query_count * 24) : NULL;
   ok = ok && folded;
+  if (source_only)
+  {
+    free(folded);
+  }
   /* launches of at most CQL_BATCH_LAUNCH_QUERIES queries, each the shapes of its slice */
-  CqlBuffer* scale_buf = ok ? pooled("batch_col_scale", sizeof(col_scale), CQLCUDA_BUFFER_WRITE) : NULL;
-  CqlBuffer* thr_buf = ok ? pooled("batch_thresholds", (uint64_t)query_count * BATCH_MAX_SITES * sizeof(Thr), CQLCUDA_BUFFER_WRITE) : NULL;
-  CqlBuffer* qc_buf = ok ? pooled("batch_literals", (uint64_t)query_count * BATCH_MAX_CONSTS * 8, CQLCUDA_BUFFER_WRITE) : NULL;
-  CqlBuffer* qs_buf = ok ? pooled("batch_sum_columns", (uint64_t)query_count * 4, CQLCUDA_BUFFER_WRITE) : NULL;
-  CqlBuffer* begin_buf = ok ? pooled("batch_shape_begin", (BATCH_MAX_SHAPES + 1) * 4, CQLCUDA_BUFFER_WRITE) : NULL;
-  CqlBuffer* out_buf = ok ? pooled("batch_folded", (uint64_t)query_count * 24, CQLCUDA_BUFFER_READ_WRITE) : NULL;
-  CqlKernel* fold = ok ? cqlcuda_kernel_alloc("cql_batch_fold", 14) : NULL;
-  ok = ok && scale_buf && thr_buf && qc_buf && qs_buf && begin_buf && out_buf && fold;
-  if (ok)
+  if (ok && source_only)
+  {
+    /* the first launch's slice: the shapes of its queries */
+    uint32_t nq = query_count < CQL_BATCH_LAUNCH_QUERIES ? query_count : CQL_BATCH_LAUNCH_QUERIES;
+    char* slice_exprs[BATCH_MAX_SHAPES];
+    uint32_t slice_sites[BATCH_MAX_SHAPES];
+    uint32_t ns = 0;
+    for (uint32_t i = 0; i < nq; i++)
+    {
+      uint32_t sh = shape_of[order[i]];
+      if (ns == 0 || slice_exprs[ns - 1] != exprs[sh])
+      {
+        slice_exprs[ns] = exprs[sh];
+        slice_sites[ns] = shape_sites[sh];
+        ns++;
+      }
+    }
+    char* src = batch_source(slice_exprs, slice_sites, ns, slot_type, sum_cols, sum_col_count, rows_per_thread);
+    ok = src != NULL;
+    if (ok)
+    {
+      uint64_t n = strlen(src);
+      if (src_len) *src_len = n;
+      if (src_out && src_cap) snprintf(src_out, src_cap, "%s", src);
+      if (src_out && n + 1 > src_cap) ok = 0;
+    }
+    free(src);
+    if (out_shapes) *out_shapes = shapes;
+    folded = NULL;
+  }
+  int launch = ok && !source_only;
+  CqlBuffer* scale_buf = launch ? pooled("batch_col_scale", sizeof(col_scale), CQLCUDA_BUFFER_WRITE) : NULL;
+  CqlBuffer* thr_buf = launch ? pooled("batch_thresholds", (uint64_t)query_count * BATCH_MAX_SITES * sizeof(Thr), CQLCUDA_BUFFER_WRITE) : NULL;
+  CqlBuffer* qc_buf = launch ? pooled("batch_literals", (uint64_t)query_count * BATCH_MAX_CONSTS * 8, CQLCUDA_BUFFER_WRITE) : NULL;
+  CqlBuffer* qs_buf = launch ? pooled("batch_sum_columns", (uint64_t)query_count * 4, CQLCUDA_BUFFER_WRITE) : NULL;
+  CqlBuffer* begin_buf = launch ? pooled("batch_shape_begin", (BATCH_MAX_SHAPES + 1) * 4, CQLCUDA_BUFFER_WRITE) : NULL;
+  CqlBuffer* out_buf = launch ? pooled("batch_folded", (uint64_t)query_count * 24, CQLCUDA_BUFFER_READ_WRITE) : NULL;
+  CqlKernel* fold = launch ? cqlcuda_kernel_alloc("cql_batch_fold", 14) : NULL;
+  if (launch) ok = scale_buf && thr_buf && qc_buf && qs_buf && begin_buf && out_buf && fold;
+  launch = launch && ok;
+  if (launch)
   {
     CqlBatch* b = cqlcuda_batch_begin(0, 0);
     cqlcuda_batch_buffer_write(b, scale_buf, col_scale, sizeof(col_scale));
@@ -602,14 +658,14 @@ int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t qu
     cqlcuda_batch_buffer_write(b, qs_buf, qs_o, (uint64_t)query_count * 4);
     ok = cqlcuda_batch_end(b);
   }
-  uint32_t sm = cqlcuda_sm_count();
-  uint64_t ctas = (uint64_t)(sm ? sm : 152) * 2;
-  for (uint32_t first = 0; ok && first < query_count; first += CQL_BATCH_LAUNCH_QUERIES)
+  uint64_t ctas = (uint64_t)(sm_count ? sm_count : 152) * BATCH_CTAS_PER_SM;
+  for (uint32_t first = 0; launch && ok && first < query_count; first += CQL_BATCH_LAUNCH_QUERIES)
   {
     uint32_t nq = query_count - first < CQL_BATCH_LAUNCH_QUERIES ? query_count - first : CQL_BATCH_LAUNCH_QUERIES;
     /* the shapes of this slice, in order, and where each starts */
     uint32_t begin[BATCH_MAX_SHAPES + 1];
     char* slice_exprs[BATCH_MAX_SHAPES];
+    uint32_t slice_sites[BATCH_MAX_SHAPES];
     uint32_t ns = 0;
     for (uint32_t i = 0; i < nq; i++)
     {
@@ -617,12 +673,13 @@ int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t qu
       if (ns == 0 || slice_exprs[ns - 1] != exprs[s])
       {
         slice_exprs[ns] = exprs[s];
+        slice_sites[ns] = shape_sites[s];
         begin[ns] = i;
         ns++;
       }
     }
     begin[ns] = nq;
-    char* src = batch_source(slice_exprs, ns, slot_type, sum_cols, sum_col_count, rows_per_thread);
+    char* src = batch_source(slice_exprs, slice_sites, ns, slot_type, sum_cols, sum_col_count, rows_per_thread);
     if (!src)
     {
       ok = 0;
@@ -667,13 +724,13 @@ int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t qu
     cqlcuda_batch_kernel_execute(b, fold, nq, QE_GPU_WORKGROUP_SIZE);
     ok = cqlcuda_batch_end(b);
   }
-  if (ok)
+  if (launch && ok)
   {
     CqlBatch* b = cqlcuda_batch_begin(0, (uint64_t)query_count * 24);
     cqlcuda_batch_buffer_read(b, out_buf, folded, (uint64_t)query_count * 24);
     ok = cqlcuda_batch_end(b);
   }
-  if (ok)
+  if (launch && ok)
   {
     for (uint32_t i = 0; i < query_count; i++)
     {
@@ -693,7 +750,7 @@ int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t qu
     }
     if (out_shapes) *out_shapes = shapes;
   }
-  else if (why[0])
+  else if (!ok && why[0])
     refuse(why);
   for (uint32_t s = 0; s < shapes; s++) free(exprs[s]);
   free(rb);
@@ -710,4 +767,18 @@ int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t qu
   free(folded);
   (void)col_max;
   return ok;
+}
+
+int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
+                                  const int32_t* sum_columns, uint32_t rows_per_thread, uint64_t* out_counts, double* out_sums,
+                                  uint32_t* out_shapes)
+{
+  return batch_run(programs, query_count, columns, column_count, sum_columns, rows_per_thread, out_counts, out_sums, out_shapes, 0, NULL,
+                   0, NULL);
+}
+
+int cqlops_batch_source(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
+                        const int32_t* sum_columns, uint32_t rows_per_thread, char* out, uint64_t cap, uint64_t* out_len, uint32_t* out_shapes)
+{
+  return batch_run(programs, query_count, columns, column_count, sum_columns, rows_per_thread, NULL, NULL, out_shapes, 1, out, cap, out_len);
 }

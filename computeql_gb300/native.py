@@ -155,6 +155,7 @@ OPS_API = [
     ("cqlops_fixed_scale", C.c_int, [P, P, u64, P, P]),
     ("cqlops_zone_map_build", C.c_int, [P, P, u64]),
     ("cqlops_batch_filter_aggregate", C.c_int, [P, u32, P, u32, P, u32, P, P, P]),
+    ("cqlops_batch_source", C.c_int, [P, u32, P, u32, P, u32, P, u64, P, P]),
     ("cqlops_scan_ranges", u64, [P, u32, P, u32, P, u64, P, P, P]),
     ("cqlops_group_dense_fixed", C.c_int, [P, u32, P, P, P, u64, u64, P, P, P, P, P, P]),
     ("cqlops_hll_estimate", dbl, [P, u64]),

@@ -332,6 +332,22 @@ def batch_aggregate(programs, sum_names, rows_per_thread=8):
     return counts[:q], sums[:q], shapes.value
 
 
+def batch_source(programs, sum_names, rows_per_thread=8):
+    """The generated source of the batched scan's first launch (no device work) -> (source, shapes)."""
+    q = len(programs)
+    base = programs[0]
+    ptrs = (C.c_void_p * q)(*[C.addressof(p.prog) for p in programs])
+    sc = np.array([base.index(n) if n is not None else -1 for n in sum_names], dtype=np.int32)
+    n = C.c_uint64()
+    shapes = C.c_uint32()
+    lib = N.load_ops()
+    lib.cqlops_batch_source(ptrs, q, base._cols, len(base.columns), N.ptr(sc), rows_per_thread, None, 0, C.byref(n), C.byref(shapes))
+    buf = C.create_string_buffer(n.value + 1)
+    _check(lib.cqlops_batch_source(ptrs, q, base._cols, len(base.columns), N.ptr(sc), rows_per_thread, buf, n.value + 1, None, None),
+           "cqlops_batch_source")
+    return buf.value.decode(), shapes.value
+
+
 def fused_group(program, key_names, agg_names, max_groups=1 << 16):
     kc, ac = len(key_names), len(agg_names)
     keys = (C.c_uint32 * 3)(*[program.index(n) for n in key_names])

@@ -327,6 +327,11 @@ int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t qu
                                   const int32_t* sum_columns, uint32_t rows_per_thread, uint64_t* out_counts, double* out_sums,
                                   uint32_t* out_shapes);
 
+/* The CUDA C++ source cqlops_batch_filter_aggregate would compile for its first launch (no device
+   work), up to cap bytes into out (out_len receives the length). */
+int cqlops_batch_source(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
+                        const int32_t* sum_columns, uint32_t rows_per_thread, char* out, uint64_t cap, uint64_t* out_len, uint32_t* out_shapes);
+
 /* Why the last operator call returned 0 when it refused the request itself ("" otherwise; GPU
    failures are in cqlcuda_last_error()). */
 const char* cqlops_last_error(void);

@@ -1,0 +1,48 @@
+"""The batched scan's generated kernel (cqlops_batch_source), built and NVRTC-compiled without a GPU."""
+import numpy as np
+import pytest
+
+from tests.batch_workload import F64, U32, queries
+
+
+@pytest.fixture(scope="module")
+def ops():
+    from computeql_gb300 import build, ops as o
+    build.build()
+    return o
+
+
+def columns(ops, rows=1000):
+    cols = {n: ops.Column(ops.TYPE_U32, rows, zone=(0.0, 65535.0)) for n in U32}
+    cols.update({n: ops.Column(ops.TYPE_F64, rows, zone=(0.0, 1.0)) for n in F64})
+    return cols
+
+
+@pytest.mark.parametrize("rows_per_thread", [4, 8, 16])
+def test_source_compiles(ops, rows_per_thread):
+    cols = columns(ops)
+    qs = queries(120, 29, 3)
+    progs = [ops.Program(w, cols) for w, _ in qs]
+    src, shapes = ops.batch_source(progs, [s for _, s in qs], rows_per_thread)
+    assert shapes == 29
+    assert src.count("#define CQL_SHAPE_") == 29
+    ok, log = ops.compile_check(src)
+    assert ok, log
+
+
+def test_queries_of_one_shape_share_its_predicate(ops):
+    cols = columns(ops)
+    qs = [(f"(and (< u0 {k}) (>= d1 0.{k}))", "d0") for k in range(1, 50)]
+    progs = [ops.Program(w, cols) for w, _ in qs]
+    src, shapes = ops.batch_source(progs, [s for _, s in qs])
+    assert shapes == 1
+    # the literals are per-query thresholds, not in the source
+    assert "#define CQL_SHAPE_0(k) ((cql_bi(&T0, r0[k]) & cql_bd(&T1, r5[k])))" in src
+
+
+def test_strings_are_refused(ops):
+    cols = columns(ops)
+    cols["s"] = ops.Column(ops.TYPE_STRING8, 1000)
+    progs = [ops.Program("(= s 'x')", cols)]
+    with pytest.raises(ops.OpError):
+        ops.batch_source(progs, [None])
