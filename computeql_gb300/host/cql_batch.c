@@ -310,7 +310,8 @@ static const char* BATCH_PRELUDE =
   "__device__ __forceinline__ u32 cql_word(const CqlLaunch& a, u32 i) { u64 s = a.push[i >> 1]; return (i & 1u) ? (u32)(s >> 32) : (u32)s; }\n"
   "__device__ __forceinline__ uint4 cql_ld4(const void* p) { uint4 v; asm volatile(\"ld.global.cs.v4.u32 {%0,%1,%2,%3}, [%4];\" : \"=r\"(v.x), \"=r\"(v.y), \"=r\"(v.z), \"=r\"(v.w) : \"l\"(p)); return v; }\n"
   "__device__ __forceinline__ bool cql_bi(const Thr* t, u32 code) { return ((code - (u32)t->a) <= (u32)t->b) != (t->c != 0u); }\n"
-  "__device__ __forceinline__ bool cql_bd(const Thr* t, u64 bits) { u64 k = (bits >> 63) ? ~bits : (bits | 0x8000000000000000ull); return ((k - t->a) <= t->b) != (t->c != 0u); }\n"
+  "__device__ __forceinline__ u64 cql_key(u64 bits) { return (bits >> 63) ? ~bits : (bits | 0x8000000000000000ull); }\n"
+  "__device__ __forceinline__ bool cql_bk(const Thr* t, u64 key) { return ((key - t->a) <= t->b) != (t->c != 0u); }\n"
   "__device__ __forceinline__ bool cql_bf(const Thr* t, float v) { float x = __uint_as_float((u32)t->a); u32 op = t->c; bool s = t->d != 0u;\n"
   "  if (op == 5u) return s ? v < x : v <= x; if (op == 7u) return v <= x; if (op == 6u) return s ? v > x : v >= x; if (op == 8u) return v >= x;\n"
   "  if (op == 3u) return v == x; return v != x; }\n"
@@ -344,7 +345,8 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
        "  const u64 groups = (rows + RPT - 1ull) / RPT; const u64 per_pass = (u64)gridDim.x * blockDim.x;\n"
        "  for (u64 g0 = (u64)blockIdx.x * blockDim.x; g0 < groups; g0 += per_pass)\n  {\n"
        "    const u64 row0 = (g0 + threadIdx.x) * RPT;\n"
-       "    const u32 valid = row0 < rows ? (u32)min((u64)RPT, rows - row0) : 0u;\n",
+       "    const u32 valid = row0 < rows ? (u32)min((u64)RPT, rows - row0) : 0u;\n"
+       "    const u32 valid_mask = valid >= 32u ? 0xffffffffu : ((1u << valid) - 1u);\n",
        rows_per_thread);
   /* the register blocks */
   for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++)
@@ -363,6 +365,9 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
            "    else { for (u32 v = 0; v < RPT; v++) r%d[v] = v < valid ? ((const u32*)a.buf[%d])[row0 + v] : 0u; }\n",
            6 + s, s, s, s, s, s, 6 + s);
   }
+  /* the order keys of the f64 columns, once per row (every query's comparisons read them) */
+  for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++)
+    if (slot_type[s] == CQLOPS_TYPE_F64) bput(&b, "    u64 kd%d[%u];\n    for (u32 v = 0; v < RPT; v++) kd%d[v] = cql_key(r%d[v]);\n", s, rows_per_thread, s, s);
   /* the summed columns as scaled integers, once per row */
   for (uint32_t i = 0; i < sum_col_count; i++)
   {
@@ -393,13 +398,15 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
          "%s"
          "      u32 m = 0u;\n"
          "#pragma unroll\n"
-         "      for (u32 k = 0; k < RPT; k++) if (k < valid && (CQL_SHAPE_%u(k))) m |= 1u << k;\n"
+         "      for (u32 k = 0; k < RPT; k++) m |= ((CQL_SHAPE_%u(k)) ? 1u : 0u) << k;\n"
+         "      m &= valid_mask;\n"
          "      const u32 cnt = __reduce_add_sync(0xffffffffu, (u32)__popc(m));\n"
          "      const u32 sc = qsum[q0 + q];\n"
          "      long long sv = 0ll;\n",
          s, s + 1, BATCH_MAX_SITES, BATCH_MAX_CONSTS, decls, s);
     for (uint32_t i = 0; i < sum_col_count; i++)
-      bput(&b, "      if (sc == %du) { for (u32 k = 0; k < RPT; k++) sv += ((m >> k) & 1u) ? fx%d[k] : 0ll; }\n", sum_cols[i], sum_cols[i]);
+      bput(&b, "      if (sc == %du && m) {\n#pragma unroll\n        for (u32 k = 0; k < RPT; k++) if ((m >> k) & 1u) sv += fx%d[k];\n      }\n", sum_cols[i],
+           sum_cols[i]);
     bput(&b,
          "      if (sc != 0xffffffffu) { for (int o = 16; o > 0; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o); }\n"
          "      if (lane == 0u) { cacc[q] += cnt; acc[q] += sv; }\n"

@@ -201,7 +201,7 @@ static char* column_vs_const(Gen* g, const Val* col, const Val* k, int op)
     if (t == CQLOPS_TYPE_U32 || t == 12 || t == CQLOPS_TYPE_BOOL) return dupf("cql_bi(&T%d, r%d[k])", site, col->col_slot);
     if (t == CQLOPS_TYPE_I32 || t == 9) return dupf("cql_bi(&T%d, r%d[k] ^ 0x80000000u)", site, col->col_slot);
     if (t == CQLOPS_TYPE_F32) return dupf("cql_bf(&T%d, __uint_as_float(r%d[k]))", site, col->col_slot);
-    if (t == CQLOPS_TYPE_F64) return dupf("cql_bd(&T%d, r%d[k])", site, col->col_slot);
+    if (t == CQLOPS_TYPE_F64) return dupf("cql_bk(&T%d, kd%d[k])", site, col->col_slot);
     gen_fail(g, "a 64-bit integer comparison is not batched");
     return dupf("false");
   }

@@ -18,7 +18,8 @@ typedef struct
 
 /* The program as one boolean expression over raw row k of the column registers r<slot>[k], its
    comparisons with literals reading the query's thresholds T<site> (copies of TH[site] the caller
-   declares; cql_bi / cql_bf / cql_bd) and any other literal QC[index]. Lists the sites and the slot types the expression reads. Returns 0 with
+   declares; cql_bi / cql_bf, and cql_bk over kd<slot>[k], the order keys of an f64 column the caller
+   computes once per row) and any other literal QC[index]. Lists the sites and the slot types the expression reads. Returns 0 with
    `why` when the program cannot be batched (strings, 64-bit integer comparisons). */
 int cql_codegen_batch_predicate(const CqlProgram* prog, CqlBatchSite* sites, uint32_t site_cap, uint32_t* site_count, int* slot_type,
                                 char** expr, char* why, size_t why_cap);

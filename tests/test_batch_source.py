@@ -37,7 +37,7 @@ def test_queries_of_one_shape_share_its_predicate(ops):
     src, shapes = ops.batch_source(progs, [s for _, s in qs])
     assert shapes == 1
     # the literals are per-query thresholds, not in the source
-    assert "#define CQL_SHAPE_0(k) ((cql_bi(&T0, r0[k]) & cql_bd(&T1, r5[k])))" in src
+    assert "#define CQL_SHAPE_0(k) ((cql_bi(&T0, r0[k]) & cql_bk(&T1, kd5[k])))" in src
 
 
 def test_strings_are_refused(ops):
