@@ -217,6 +217,12 @@ static char* column_vs_const(Gen* g, const Val* col, const Val* k, int op)
     sprintf_(&g->pro, "  const ThrF T%d = cql_thr_f32(K%d, %d);\n", site, k->const_index, op);
     return dupf("T%d.m(__uint_as_float(r%d[k]))", site, col->col_slot);
   }
+  if (t == CQLOPS_TYPE_F64)
+  {
+    /* an interval of order keys of the double: integer work per row, the same answer as comparing in double */
+    sprintf_(&g->pro, "  const ThrD T%d = cql_thr_f64(K%d, %d);\n", site, k->const_index, op);
+    return dupf("T%d.m(r%d[k])", site, col->col_slot);
+  }
   char* d = dbl_of(col->col_slot, t);
   char* r = dupf("(%s %s K%d)", d, op_text(op), k->const_index);
   free(d);
@@ -423,6 +429,24 @@ static const char* PRELUDE =
   "  else if (op == 8) r.t = fu;\n"
   "  else if ((double)fd == c) r.t = fd;\n"
   "  return r; }\n"
+  /* double comparison as an interval of order keys ((bits >> 63) ? ~bits : bits | sign bit): -0.0 and
+     +0.0 are neighbouring keys, NaN keys lie beyond the infinities (only != matches a NaN) */
+  "struct ThrD { u64 lo, span; bool invert; __device__ __forceinline__ bool m(u64 bits) const {\n"
+  "  u64 k = (bits >> 63) ? ~bits : (bits | 0x8000000000000000ull); return ((k - lo) <= span) != invert; } };\n"
+  "__device__ __forceinline__ u64 cql_dkey(double x) { u64 b = (u64)__double_as_longlong(x); return (b >> 63) ? ~b : (b | 0x8000000000000000ull); }\n"
+  "__device__ ThrD cql_thr_f64(double c, int op) {\n"
+  "  ThrD t; t.lo = 0ull; t.span = ~0ull; t.invert = false;\n"
+  "  if (c != c) { t.invert = (op != 4); return t; }\n"
+  "  const u64 kninf = cql_dkey(__longlong_as_double(0xfff0000000000000ll)), kpinf = cql_dkey(__longlong_as_double(0x7ff0000000000000ll));\n"
+  "  const u64 kzn = 0x7fffffffffffffffull, kzp = 0x8000000000000000ull;\n"
+  "  const bool zero = c == 0.0; const u64 kc = cql_dkey(c); u64 lo, hi; bool ne = false, empty = false;\n"
+  "  if (op == 3 || op == 4) { lo = zero ? kzn : kc; hi = zero ? kzp : kc; ne = (op == 4); }\n"
+  "  else if (op == 5) { lo = kninf; hi = zero ? kzn - 1ull : kc - 1ull; empty = (kc == kninf); }\n"
+  "  else if (op == 7) { lo = kninf; hi = zero ? kzp : kc; }\n"
+  "  else if (op == 6) { lo = zero ? kzp + 1ull : kc + 1ull; hi = kpinf; empty = (kc == kpinf); }\n"
+  "  else { lo = zero ? kzn : kc; hi = kpinf; }\n"
+  "  if (empty || lo > hi) { t.invert = true; return t; }\n"
+  "  t.lo = lo; t.span = hi - lo; t.invert = ne; return t; }\n"
   /* raw strings: the data slot holds bytes, the next slot the row's u64 offsets (scan_filter.comp:105-200) */
   "__device__ __forceinline__ u32 cql_byte(const CqlLaunch& a, u32 slot, u64 i) { const unsigned char* p = (const unsigned char*)a.buf[6 + slot]; return p[i]; }\n"
   "__device__ __forceinline__ u32 cql_cbyte(const CqlLaunch& a, u32 wo, u32 i) { const unsigned char* p = (const unsigned char*)a.buf[2]; return p[wo * 4u + i]; }\n"

@@ -217,3 +217,27 @@ def test_fused_group_refuses_what_the_reference_refuses(env):
         ops.fused_group(p, ["u0"], ["u1"], max_groups=1 << 17)
     with pytest.raises(ops.OpError, match="U32/I32"):
         ops.fused_group(p, ["u0"], ["d0"])
+
+
+@pytest.mark.parametrize("where", [
+    "(< x 0.0)", "(<= x 0.0)", "(= x 0.0)", "(!= x 0.0)", "(> x -0.0)", "(>= x -0.0)", "(< x -1e308)", "(> x 1e308)",
+    "(<= x -1e308)", "(>= x 1e308)", "(= x 2.5)", "(!= x 2.5)", "(< x 2.5)", "(> x -7.25)", "(and (> x -1.0) (< x 1.0))",
+])
+def test_f64_special_values(env, where):
+    # -0.0, +-inf, NaN and literals at them: the generated kernels compare order keys, not doubles
+    ops, _, _, _ = env
+    rng = np.random.default_rng(17)
+    x = rng.normal(size=50_003) * 3
+    x[::11] = 0.0
+    x[1::13] = -0.0
+    x[2::17] = np.inf
+    x[3::19] = -np.inf
+    x[4::23] = np.nan
+    x[5::29] = 2.5
+    x[6::31] = -7.25
+    x[7::37] = 1e308
+    x[8::41] = -1e308
+    arrays = {"x": x}
+    p = ops.Program(where, {"x": ops.Column.from_numpy(x)})
+    check_scan(ops, p, arrays, ops.SCAN_GENERATED)
+    check_scan(ops, p, arrays, ops.SCAN_INTERPRETER)
