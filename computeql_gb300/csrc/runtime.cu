@@ -12,6 +12,7 @@
 //    event, wait polls it with a time limit instead of aborting (gpu_vulkan.c:1106-1135, 1390-1480);
 //  - kernel time comes from CUDA event pairs (gpu_vulkan.c:2976-2993 uses timestamp queries).
 #include "cql_internal.cuh"
+#include <atomic>
 #include "../../include/cqlcuda.h"
 
 #include <nvrtc.h>
@@ -120,6 +121,21 @@ struct CqlProfileEntry
   uint64_t dispatches;
 };
 
+// A lane is where a thread's batches run: a stream, a batch with its staging area and timings, the
+// kernel arguments the thread has set, and the tag its pooled buffers are named under. The process
+// has one main lane (the reference's single queue: one batch at a time); a thread that opens its own
+// lane (cqlcuda_thread_lane_begin) runs its batches on its own stream, concurrently with the others.
+struct CqlLane
+{
+  cudaStream_t stream;
+  CqlBatch batch;
+  std::vector<CqlTiming> timings;
+  std::string pool_tag;
+  std::unordered_map<const CqlKernel*, CqlLaunch> args;
+  uint32_t launches;     // kernels this lane launched
+  int is_main;
+};
+
 struct CqlState
 {
   int initialized;
@@ -144,21 +160,20 @@ struct CqlState
   uint64_t compile_attempts;
   std::string compile_log;
 
-  CqlBatch batch;
-  std::vector<CqlTiming> batch_timings;
+  CqlLane main_lane;
+  uint32_t lanes_open;   // threads with a lane of their own (pool eviction waits until they close)
 
   int profile_enabled;
   std::vector<CqlProfileEntry> profile;
   std::unordered_map<std::string, uint32_t> profile_index;
 
   uint64_t last_kernel_us;
-  uint32_t launches;
+  std::atomic<uint32_t> launches;
   uint32_t wait_timeout_ms;
 
   void* flush_buf;
   uint64_t flush_bytes;
 
-  std::string last_error;
   std::recursive_mutex lock;
 };
 
@@ -185,16 +200,31 @@ static CqlState& S()
     g_state->flush_buf = nullptr;
     g_state->flush_bytes = 0;
     memset(&g_state->mem, 0, sizeof(g_state->mem));
-    g_state->batch.active = 0;
-    g_state->batch.failed = 0;
-    g_state->batch.staging.host = nullptr;
-    g_state->batch.staging.capacity = 0;
-    g_state->batch.staging.used = 0;
+    CqlLane& m = g_state->main_lane;
+    m.stream = nullptr;
+    m.batch.active = 0;
+    m.batch.failed = 0;
+    m.batch.staging.host = nullptr;
+    m.batch.staging.capacity = 0;
+    m.batch.staging.used = 0;
+    m.is_main = 1;
+    m.launches = 0;
+    g_state->lanes_open = 0;
   }
   return *g_state;
 }
 
-void cql_note_launch(void) { S().launches += 1; }
+static thread_local CqlLane* tl_lane = nullptr;
+static thread_local std::string tl_error;
+
+// the calling thread's lane
+static CqlLane& L() { return tl_lane ? *tl_lane : S().main_lane; }
+
+void cql_note_launch(void)
+{
+  S().launches.fetch_add(1, std::memory_order_relaxed);
+  if (tl_lane) tl_lane->launches += 1;
+}
 
 static void set_error(const char* fmt, ...)
 {
@@ -203,7 +233,7 @@ static void set_error(const char* fmt, ...)
   va_start(ap, fmt);
   vsnprintf(buf, sizeof(buf), fmt, ap);
   va_end(ap);
-  S().last_error = buf;
+  tl_error = buf;
 }
 
 // A CUDA error that leaves the context unusable makes device_lost sticky, as
@@ -290,6 +320,7 @@ static uint32_t profile_slot(const std::string& name)
 static void timings_collect(std::vector<CqlTiming>& timings)
 {
   CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
   for (auto& t : timings)
   {
     float ms = 0.0f;
@@ -335,6 +366,7 @@ extern "C" int cqlcuda_init(void)
   cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, s.device);
   s.pageable_access = pageable;
   if (!note_cuda(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "cudaStreamCreate")) return 0;
+  s.main_lane.stream = s.stream;
   cudaEventCreate(&s.exec_start);
   cudaEventCreate(&s.exec_stop);
   cudaEventCreate(&s.timer_start);
@@ -373,7 +405,7 @@ extern "C" void cqlcuda_release(void)
   s.pool_index.clear();
   for (auto& kv : s.kernels) delete kv.second;
   s.kernels.clear();
-  staging_release(s.batch.staging);
+  staging_release(s.main_lane.batch.staging);
   if (s.flush_buf) cudaFree(s.flush_buf);
   s.flush_buf = nullptr;
   cudaStreamDestroy(s.stream);
@@ -383,7 +415,7 @@ extern "C" void cqlcuda_release(void)
 extern "C" void cqlcuda_wait(void)
 {
   if (!S().initialized) return;
-  wait_stream(S().stream, "cqlcuda_wait");
+  wait_stream(L().stream ? L().stream : S().stream, "cqlcuda_wait");
 }
 
 extern "C" uint64_t cqlcuda_get_executed_kernel_time_microseconds(void) { return S().last_kernel_us; }
@@ -420,7 +452,8 @@ extern "C" uint32_t cqlcuda_sm_count(void) { ensure_init(); return (uint32_t)g_c
 static uint64_t pool_evict(uint64_t bytes_wanted)
 {
   CqlState& s = S();
-  if (s.batch.active) return 0;
+  // never while a batch is recording: its buffers are bound (any lane's batch)
+  if (s.main_lane.batch.active || s.lanes_open) return 0;
   uint64_t freed = 0;
   while (freed < bytes_wanted)
   {
@@ -525,7 +558,7 @@ extern "C" CqlBuffer* cqlcuda_buffer_alloc_pooled(const char* name, uint64_t nam
 {
   CqlState& s = S();
   std::lock_guard<std::recursive_mutex> g(s.lock);
-  std::string key(name, name_len);
+  std::string key = L().pool_tag + std::string(name, name_len);
   CqlPooled* slot = pool_find(key);
   if (slot)
   {
@@ -596,7 +629,7 @@ extern "C" CqlBuffer* cqlcuda_buffer_import_host_readonly_pooled(const char* nam
 {
   CqlState& s = S();
   std::lock_guard<std::recursive_mutex> g(s.lock);
-  std::string key(name, name_len);
+  std::string key = L().pool_tag + std::string(name, name_len);
   CqlPooled* slot = pool_find(key);
   if (slot && slot->buffer && slot->imported_host_ptr == host_ptr && slot->capacity == size)
   {
@@ -933,8 +966,9 @@ extern "C" void cqlcuda_kernel_set_arg_buffer(CqlKernel* k, uint32_t index, CqlB
     set_error("cqlcuda_kernel_set_arg_buffer: buffer argument for index %u is NULL - a prior GPU buffer allocation failed", index);
     return;
   }
-  k->args.buf[index] = b->dptr;
-  k->args.bytes[index] = b->size;
+  CqlLaunch& A = L().args[k];
+  A.buf[index] = b->dptr;
+  A.bytes[index] = b->size;
 }
 
 extern "C" void cqlcuda_kernel_set_arg_buffer_range(CqlKernel* k, uint32_t index, CqlBuffer* b, uint64_t offset, uint64_t size)
@@ -946,8 +980,9 @@ extern "C" void cqlcuda_kernel_set_arg_buffer_range(CqlKernel* k, uint32_t index
               (unsigned long long)size, (unsigned long long)b->size);
     return;
   }
-  k->args.buf[index] = (char*)b->dptr + offset;
-  k->args.bytes[index] = size;
+  CqlLaunch& A = L().args[k];
+  A.buf[index] = (char*)b->dptr + offset;
+  A.bytes[index] = size;
 }
 
 extern "C" void cqlcuda_kernel_set_arg_u64(CqlKernel* k, uint32_t index, uint64_t value)
@@ -958,7 +993,7 @@ extern "C" void cqlcuda_kernel_set_arg_u64(CqlKernel* k, uint32_t index, uint64_
     set_error("cqlcuda_kernel_set_arg_u64: index %u exceeds %u", index, CQL_PUSH_SLOTS);
     return;
   }
-  k->args.push[index] = value;
+  L().args[k].push[index] = value;
 }
 
 // Enqueues one dispatch on `stream`, bracketed by events when the profile is on.
@@ -982,14 +1017,14 @@ static int dispatch(CqlKernel* k, uint32_t gws, uint32_t lws, cudaStream_t strea
   int rc = 0;
   if (k->builtin)
   {
-    rc = k->builtin(k->args, gws, lws, stream);
+    rc = k->builtin(L().args[k], gws, lws, stream);
   }
   else if (k->generated)
   {
     uint32_t block = k->gen_block;
     uint64_t want = lws ? ((uint64_t)gws + lws - 1) / lws : 1;
     uint32_t grid = cql_stream_grid(want ? want : 1, (int)k->gen_per_sm);
-    CqlLaunch a = k->args;
+    CqlLaunch a = L().args[k];
     void* params[] = { &a };
     cudaError_t e = cudaLaunchKernel((const void*)k->generated, dim3(grid), dim3(block), params, k->gen_smem, stream);
     rc = (int)e;
@@ -1106,14 +1141,16 @@ static int enqueue_read(CqlStaging& st, CqlBuffer* b, uint64_t offset, void* out
 extern "C" CqlBatch* cqlcuda_batch_begin(uint64_t upload_bytes_needed, uint64_t download_bytes_needed)
 {
   CqlState& s = S();
-  s.lock.lock();
+  CqlLane& l = L();
+  // the main lane holds one batch at a time (src/gpu/vulkan/gpu_vulkan.h:215); a thread's own lane needs no lock
+  if (l.is_main) s.lock.lock();
   if (!ensure_init())
   {
-    s.lock.unlock();
+    if (l.is_main) s.lock.unlock();
     return nullptr;
   }
   (void)upload_bytes_needed;
-  CqlBatch* b = &s.batch;
+  CqlBatch* b = &l.batch;
   b->active = 1;
   b->failed = 0;
   staging_prepare(b->staging, download_bytes_needed);
@@ -1129,13 +1166,13 @@ extern "C" void cqlcuda_batch_buffer_write(CqlBatch* batch, CqlBuffer* buffer, c
     batch->failed = 1;
     return;
   }
-  if (!note_cuda(cudaMemcpyAsync(buffer->dptr, data, size, cudaMemcpyHostToDevice, S().stream), "batch write")) batch->failed = 1;
+  if (!note_cuda(cudaMemcpyAsync(buffer->dptr, data, size, cudaMemcpyHostToDevice, L().stream), "batch write")) batch->failed = 1;
 }
 
 extern "C" void cqlcuda_batch_buffer_zero(CqlBatch* batch, CqlBuffer* buffer, uint64_t size)
 {
   if (!batch || !buffer) return;
-  if (!note_cuda(cudaMemsetAsync(buffer->dptr, 0, std::min(size, buffer->size), S().stream), "batch zero")) batch->failed = 1;
+  if (!note_cuda(cudaMemsetAsync(buffer->dptr, 0, std::min(size, buffer->size), L().stream), "batch zero")) batch->failed = 1;
 }
 
 __global__ void k_fill_u32(uint32_t* p, uint64_t words, uint32_t value)
@@ -1163,13 +1200,13 @@ static int fill_words(CqlBuffer* buffer, uint64_t size, uint32_t value, cudaStre
 extern "C" void cqlcuda_batch_buffer_fill(CqlBatch* batch, CqlBuffer* buffer, uint64_t size, uint32_t value)
 {
   if (!batch || !buffer) return;
-  if (!fill_words(buffer, size, value, S().stream)) batch->failed = 1;
+  if (!fill_words(buffer, size, value, L().stream)) batch->failed = 1;
 }
 
 extern "C" void cqlcuda_batch_kernel_execute(CqlBatch* batch, CqlKernel* kernel, uint32_t gws, uint32_t lws)
 {
   if (!batch || !kernel) return;
-  if (!dispatch(kernel, gws, lws, S().stream, &S().batch_timings)) batch->failed = 1;
+  if (!dispatch(kernel, gws, lws, L().stream, &L().timings)) batch->failed = 1;
 }
 
 extern "C" void cqlcuda_batch_buffer_read(CqlBatch* batch, CqlBuffer* buffer, void* out_data, uint64_t size)
@@ -1180,7 +1217,7 @@ extern "C" void cqlcuda_batch_buffer_read(CqlBatch* batch, CqlBuffer* buffer, vo
     if (out_data) memset(out_data, 0, size);
     return;
   }
-  if (!enqueue_read(batch->staging, buffer, 0, out_data, size, S().stream)) batch->failed = 1;
+  if (!enqueue_read(batch->staging, buffer, 0, out_data, size, L().stream)) batch->failed = 1;
 }
 
 extern "C" void cqlcuda_batch_buffer_read_at(CqlBatch* batch, CqlBuffer* buffer, uint64_t offset, void* out_data, uint64_t size)
@@ -1191,7 +1228,7 @@ extern "C" void cqlcuda_batch_buffer_read_at(CqlBatch* batch, CqlBuffer* buffer,
     if (out_data) memset(out_data, 0, size);
     return;
   }
-  if (!enqueue_read(batch->staging, buffer, offset, out_data, size, S().stream)) batch->failed = 1;
+  if (!enqueue_read(batch->staging, buffer, offset, out_data, size, L().stream)) batch->failed = 1;
 }
 
 extern "C" int cqlcuda_batch_end(CqlBatch* batch)
@@ -1201,20 +1238,21 @@ extern "C" int cqlcuda_batch_end(CqlBatch* batch)
   {
     return 0;
   }
-  int ok = !batch->failed && wait_stream(s.stream, "batch_end");
+  CqlLane& l = L();
+  int ok = !batch->failed && wait_stream(l.stream, "batch_end");
   staging_finish(batch->staging, ok);
-  if (ok) timings_collect(s.batch_timings);
+  if (ok) timings_collect(l.timings);
   else
   {
-    for (auto& t : s.batch_timings)
+    for (auto& t : l.timings)
     {
       cudaEventDestroy(t.start);
       cudaEventDestroy(t.stop);
     }
-    s.batch_timings.clear();
+    l.timings.clear();
   }
   batch->active = 0;
-  s.lock.unlock();
+  if (l.is_main) s.lock.unlock();
   return ok;
 }
 
@@ -1392,9 +1430,10 @@ extern "C" int cqlcuda_kernel_profile_entry(uint32_t index, const char** out_nam
   if (out_dispatches) *out_dispatches = s.profile[index].dispatches;
   return 1;
 }
-extern "C" uint32_t cqlcuda_kernel_launch_count(void) { return S().launches; }
-extern "C" const char* cqlcuda_last_error(void) { return S().last_error.c_str(); }
-extern "C" void cqlcuda_clear_error(void) { S().last_error.clear(); }
+// a thread with its own lane counts its own launches; otherwise the process's
+extern "C" uint32_t cqlcuda_kernel_launch_count(void) { return tl_lane ? tl_lane->launches : S().launches.load(); }
+extern "C" const char* cqlcuda_last_error(void) { return tl_error.c_str(); }
+extern "C" void cqlcuda_clear_error(void) { tl_error.clear(); }
 extern "C" void cqlcuda_set_wait_timeout_ms(uint32_t ms) { S().wait_timeout_ms = ms ? ms : 1; }
 extern "C" void cqlcuda_set_module_cache_dir(const char* path) { S().cache_dir = path ? path : ""; }
 extern "C" void cqlcuda_set_fail_compile_every(uint32_t n) { S().fail_compile_every = n; }
@@ -1500,4 +1539,50 @@ extern "C" double cqlcuda_timer_end_ms(void)
   float ms = 0;
   cudaEventElapsedTime(&ms, s.timer_start, s.timer_stop);
   return ms;
+}
+
+// ---------------------------------------------------------------------------------------------
+// lanes: a thread's own stream, batch, kernel arguments and pooled-buffer names
+
+extern "C" int cqlcuda_thread_lane_begin(const char* pool_tag)
+{
+  CqlState& s = S();
+  if (tl_lane) return 1;
+  {
+    std::lock_guard<std::recursive_mutex> g(s.lock);
+    if (!ensure_init()) return 0;
+    s.lanes_open += 1;
+  }
+  CqlLane* l = new CqlLane();
+  l->is_main = 0;
+  l->launches = 0;
+  l->batch.active = 0;
+  l->batch.failed = 0;
+  l->batch.staging.host = nullptr;
+  l->batch.staging.capacity = 0;
+  l->batch.staging.used = 0;
+  l->pool_tag = std::string(pool_tag ? pool_tag : "") + "/";
+  if (!note_cuda(cudaStreamCreateWithFlags(&l->stream, cudaStreamNonBlocking), "cudaStreamCreate(lane)"))
+  {
+    delete l;
+    std::lock_guard<std::recursive_mutex> g(s.lock);
+    s.lanes_open -= 1;
+    return 0;
+  }
+  tl_lane = l;
+  return 1;
+}
+
+extern "C" void cqlcuda_thread_lane_end(void)
+{
+  CqlLane* l = tl_lane;
+  if (!l) return;
+  wait_stream(l->stream, "lane end");
+  staging_release(l->batch.staging);
+  cudaStreamDestroy(l->stream);
+  tl_lane = nullptr;
+  delete l;
+  CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
+  if (s.lanes_open) s.lanes_open -= 1;
 }

@@ -25,6 +25,7 @@
 #include "cql_codegen.h"
 
 #include <math.h>
+#include <pthread.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -36,6 +37,7 @@
 #define CQL_BATCH_LAUNCH_QUERIES 384
 #define BATCH_CTAS_PER_SM 6
 #define BATCH_MAX_SHAPES 256
+#define CQL_BATCH_CATALOG_SHAPES 64
 
 void cqlops_note_error(const char* why);
 
@@ -329,6 +331,8 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
   bput(&b,
        "extern \"C\" __global__ void __launch_bounds__(256) cql_main(CqlLaunch a)\n{\n"
        "  const u64 rows = cql_word(a, 0); const u32 nq = cql_word(a, 2); const u32 q0 = cql_word(a, 4);\n"
+       "  const u32 need = cql_word(a, 6), need_sum = cql_word(a, 7);   /* the columns this launch reads and sums */\n"
+       "  (void)need_sum;\n"
        "  const double* col_scale = (const double*)a.buf[0];\n"
        "  const Thr* thr = (const Thr*)a.buf[1];\n"
        "  const double* qconst = (const double*)a.buf[2];\n"
@@ -354,14 +358,16 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
     int t = slot_type[s];
     if (!t) continue;
     int w = type_bytes(t);
-    bput(&b, "    %s r%d[%u];\n", w == 8 ? "u64" : "u32", s, rows_per_thread);
+    /* a column no query of the launch reads is not loaded (a grid-uniform branch) */
+    bput(&b, "    %s r%d[%u];\n    if (!((need >> %d) & 1u)) { for (u32 v = 0; v < RPT; v++) r%d[v] = 0u; }\n", w == 8 ? "u64" : "u32", s,
+         rows_per_thread, s, s);
     if (w == 8)
-      bput(&b, "    for (u32 v = 0; v < RPT; v++) r%d[v] = v < valid ? ((const u64*)a.buf[%d])[row0 + v] : 0ull;\n", s, 6 + s);
+      bput(&b, "    else { for (u32 v = 0; v < RPT; v++) r%d[v] = v < valid ? ((const u64*)a.buf[%d])[row0 + v] : 0ull; }\n", s, 6 + s);
     else if (w == 1)
-      bput(&b, "    for (u32 v = 0; v < RPT; v++) r%d[v] = v < valid ? (u32)((const unsigned char*)a.buf[%d])[row0 + v] : 0u;\n", s, 6 + s);
+      bput(&b, "    else { for (u32 v = 0; v < RPT; v++) r%d[v] = v < valid ? (u32)((const unsigned char*)a.buf[%d])[row0 + v] : 0u; }\n", s, 6 + s);
     else
       bput(&b,
-           "    if (valid == RPT && (RPT & 3u) == 0u) { for (u32 v = 0; v < RPT; v += 4) { uint4 q = cql_ld4((const u32*)a.buf[%d] + row0 + v); r%d[v] = q.x; r%d[v + 1] = q.y; r%d[v + 2] = q.z; r%d[v + 3] = q.w; } }\n"
+           "    else if (valid == RPT && (RPT & 3u) == 0u) { for (u32 v = 0; v < RPT; v += 4) { uint4 q = cql_ld4((const u32*)a.buf[%d] + row0 + v); r%d[v] = q.x; r%d[v + 1] = q.y; r%d[v + 2] = q.z; r%d[v + 3] = q.w; } }\n"
            "    else { for (u32 v = 0; v < RPT; v++) r%d[v] = v < valid ? ((const u32*)a.buf[%d])[row0 + v] : 0u; }\n",
            6 + s, s, s, s, s, s, 6 + s);
   }
@@ -379,7 +385,8 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
                     : t == CQLOPS_TYPE_U64 ? "(double)r%d[v]"
                     : t == CQLOPS_TYPE_I64 ? "cql_i64d(r%d[v])"
                                            : "(double)r%d[v]";
-    bput(&b, "    long long fx%d[%u];\n    { const double sc = col_scale[%d]; for (u32 v = 0; v < RPT; v++) { double x = ", c, rows_per_thread, c);
+    bput(&b, "    long long fx%d[%u];\n    if (!((need_sum >> %d) & 1u)) { for (u32 v = 0; v < RPT; v++) fx%d[v] = 0ll; }\n", c, rows_per_thread, c, c);
+    bput(&b, "    else { const double sc = col_scale[%d]; for (u32 v = 0; v < RPT; v++) { double x = ", c);
     bput(&b, val, c);
     bput(&b, "; fx%d[v] = v < valid ? __double2ll_rn(x * sc) : 0ll; } }\n", c);
   }
@@ -444,10 +451,135 @@ static CqlBuffer* pooled(const char* name, uint64_t size, uint32_t flags)
   return cqlcuda_buffer_alloc_pooled(name, (uint64_t)strlen(name), size ? size : 8, flags, NULL);
 }
 
-/* the operator, or with source_only the source of its first launch (no device work) */
-static int batch_run(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
-                     const int32_t* sum_columns, uint32_t rows_per_thread, uint64_t* out_counts, double* out_sums, uint32_t* out_shapes,
-                     int source_only, char* src_out, uint64_t src_cap, uint64_t* src_len)
+/* ---- the shape catalog ---- */
+
+struct CqlBatchCatalog
+{
+  pthread_mutex_t lock;
+  uint32_t shapes;
+  uint64_t keys[CQL_BATCH_CATALOG_SHAPES];
+  char* exprs[CQL_BATCH_CATALOG_SHAPES];
+  uint32_t sites[CQL_BATCH_CATALOG_SHAPES];
+  int slot_type[CQLOPS_MAX_BINDINGS];
+  uint32_t sum_mask;     /* the columns any batch summed */
+  uint64_t version;      /* bumped when a shape, a column type or a summed column is added */
+};
+
+CqlBatchCatalog* cqlops_batch_catalog_create(void)
+{
+  CqlBatchCatalog* c = (CqlBatchCatalog*)calloc(1, sizeof(CqlBatchCatalog));
+  if (c) pthread_mutex_init(&c->lock, NULL);
+  return c;
+}
+
+void cqlops_batch_catalog_destroy(CqlBatchCatalog* c)
+{
+  if (!c) return;
+  for (uint32_t s = 0; s < c->shapes; s++) free(c->exprs[s]);
+  pthread_mutex_destroy(&c->lock);
+  free(c);
+}
+
+uint32_t cqlops_batch_catalog_shapes(CqlBatchCatalog* c)
+{
+  if (!c) return 0;
+  pthread_mutex_lock(&c->lock);
+  uint32_t n = c->shapes;
+  pthread_mutex_unlock(&c->lock);
+  return n;
+}
+
+/* What a launch over the catalog compiles: its shapes, column types and summed columns, as they stood. */
+typedef struct
+{
+  uint32_t shapes;
+  char* exprs[CQL_BATCH_CATALOG_SHAPES];
+  uint32_t sites[CQL_BATCH_CATALOG_SHAPES];
+  int slot_type[CQLOPS_MAX_BINDINGS];
+  uint32_t sum_mask;
+} CatalogView;
+
+/* Maps the batch's shapes to catalog entries (adding the new ones) and takes a view of the catalog.
+   0 when the catalog cannot take them (full, or a column read as another type): the batch then runs
+   without it. Entries are never removed, so the view's strings stay valid while the catalog lives. */
+static int catalog_map(CqlBatchCatalog* c, uint32_t shapes, char** exprs, const uint64_t* keys, const uint32_t* sites,
+                       const int* slot_type, uint32_t sum_mask, uint32_t* out_index, CatalogView* view)
+{
+  int ok = 1;
+  pthread_mutex_lock(&c->lock);
+  for (int t = 0; t < CQLOPS_MAX_BINDINGS; t++)
+    if (slot_type[t] && c->slot_type[t] && c->slot_type[t] != slot_type[t]) ok = 0;
+  uint32_t added = 0;
+  for (uint32_t s = 0; ok && s < shapes; s++)
+  {
+    uint32_t k = 0;
+    while (k < c->shapes && !(c->keys[k] == keys[s] && !strcmp(c->exprs[k], exprs[s]))) k++;
+    if (k == c->shapes)
+    {
+      if (k + added >= CQL_BATCH_CATALOG_SHAPES)
+      {
+        ok = 0;
+        break;
+      }
+      k = c->shapes + added;
+      added++;
+    }
+    out_index[s] = k;
+  }
+  if (ok)
+  {
+    /* the new shapes, in the order the batch met them */
+    for (uint32_t s = 0; s < shapes; s++)
+    {
+      if (out_index[s] < c->shapes) continue;
+      uint32_t k = out_index[s];
+      size_t n = strlen(exprs[s]) + 1;
+      char* e = (char*)malloc(n);
+      if (!e)
+      {
+        ok = 0;
+        break;
+      }
+      memcpy(e, exprs[s], n);
+      c->keys[k] = keys[s];
+      c->exprs[k] = e;
+      c->sites[k] = sites[s];
+      c->shapes = k + 1;
+      c->version++;
+    }
+  }
+  if (ok)
+  {
+    for (int t = 0; t < CQLOPS_MAX_BINDINGS; t++)
+      if (slot_type[t] && !c->slot_type[t])
+      {
+        c->slot_type[t] = slot_type[t];
+        c->version++;
+      }
+    if ((c->sum_mask | sum_mask) != c->sum_mask)
+    {
+      c->sum_mask |= sum_mask;
+      c->version++;
+    }
+    view->shapes = c->shapes;
+    memcpy(view->exprs, c->exprs, sizeof(c->exprs));
+    memcpy(view->sites, c->sites, sizeof(c->sites));
+    memcpy(view->slot_type, c->slot_type, sizeof(c->slot_type));
+    view->sum_mask = c->sum_mask;
+  }
+  pthread_mutex_unlock(&c->lock);
+  return ok;
+}
+
+/* ---- the operator ---- */
+
+enum { BATCH_RUN = 0, BATCH_SOURCE = 1, BATCH_PREPARE = 2 };
+
+/* The operator; with BATCH_SOURCE the source of its first launch, with BATCH_PREPARE its kernel compiled
+   and the shapes entered in the catalog (neither does device work on the table). */
+static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns,
+                     uint32_t column_count, const int32_t* sum_columns, uint32_t rows_per_thread, uint64_t* out_counts, double* out_sums,
+                     uint32_t* out_shapes, int mode, char* src_out, uint64_t src_cap, uint64_t* src_len)
 {
   cqlops_note_error("");
   if (query_count == 0) return 1;
@@ -457,12 +589,11 @@ static int batch_run(const CqlProgram* const* programs, uint32_t query_count, co
   for (uint32_t c = 0; c < column_count; c++)
   {
     const CqlColumn* col = &columns[c];
-    if (col->rows != rows || (!col->buffer && !source_only) || col->width != 0 || col->type == CQLOPS_TYPE_STRING8)
+    if (col->rows != rows || (!col->buffer && mode == BATCH_RUN) || col->width != 0 || col->type == CQLOPS_TYPE_STRING8)
       return refuse("batched columns are full-width numeric columns of one length");
   }
   /* per query: rebound program, shape, thresholds, literals */
   CqlProgram* rb = (CqlProgram*)malloc(sizeof(CqlProgram));
-  uint64_t* shape_hash = (uint64_t*)malloc(query_count * 8);
   uint32_t* shape_of = (uint32_t*)malloc(query_count * 4);
   uint32_t* order = (uint32_t*)malloc(query_count * 4);
   Thr* thr = (Thr*)calloc((size_t)query_count * BATCH_MAX_SITES, sizeof(Thr));
@@ -473,7 +604,7 @@ static int batch_run(const CqlProgram* const* programs, uint32_t query_count, co
   uint64_t shape_keys[BATCH_MAX_SHAPES];
   uint32_t shapes = 0;
   int slot_type[CQLOPS_MAX_BINDINGS] = { 0 };
-  int ok = rb && shape_hash && shape_of && order && thr && qconst && qsum;
+  int ok = rb && shape_of && order && thr && qconst && qsum;
   char why[160] = "";
   for (uint32_t q = 0; ok && q < query_count; q++)
   {
@@ -544,17 +675,13 @@ static int batch_run(const CqlProgram* const* programs, uint32_t query_count, co
   }
   /* summed columns: loaded, scaled by 2^k with k from the column's range */
   uint32_t sm_count = cqlcuda_sm_count();
-  int sum_cols[CQLOPS_MAX_BINDINGS];
-  uint32_t sum_col_count = 0;
   double col_scale[CQLOPS_MAX_BINDINGS] = { 0 };
-  double col_max[CQLOPS_MAX_BINDINGS] = { 0 };
+  uint32_t sum_mask = 0;
   for (uint32_t q = 0; ok && q < query_count; q++)
   {
     if (qsum[q] == 0xffffffffu) continue;
     int c = (int)qsum[q];
-    uint32_t i = 0;
-    while (i < sum_col_count && sum_cols[i] != c) i++;
-    if (i < sum_col_count) continue;
+    if ((sum_mask >> c) & 1u) continue;
     const CqlColumn* col = &columns[c];
     if (!col->has_range)
     {
@@ -573,21 +700,49 @@ static int batch_run(const CqlProgram* const* programs, uint32_t query_count, co
     int wr = 0;
     frexp((double)warp_rows, &wr);   /* warp_rows < 2^wr */
     col_scale[c] = ldexp(1.0, 62 - e - wr);
-    col_max[c] = m;
-    sum_cols[sum_col_count++] = c;
+    sum_mask |= 1u << c;
   }
-  /* queries grouped by shape */
-  uint32_t* shape_count = (uint32_t*)calloc(shapes + 1, 4);
+  /* the columns this batch loads */
+  uint32_t need = 0;
+  for (int c = 0; c < CQLOPS_MAX_BINDINGS; c++)
+    if (slot_type[c]) need |= 1u << c;
+  /* what the launches compile: this batch's shapes, or the catalog's */
+  uint32_t launch_shapes = shapes;
+  char** launch_exprs = exprs;
+  uint32_t* launch_sites = shape_sites;
+  int* launch_types = slot_type;
+  uint32_t launch_sums = sum_mask;
+  CatalogView* view = NULL;
+  if (ok && catalog)
+  {
+    view = (CatalogView*)malloc(sizeof(CatalogView));
+    uint32_t index[BATCH_MAX_SHAPES];
+    if (view && catalog_map(catalog, shapes, exprs, shape_keys, shape_sites, slot_type, sum_mask, index, view))
+    {
+      for (uint32_t q = 0; q < query_count; q++) shape_of[q] = index[shape_of[q]];
+      launch_shapes = view->shapes;
+      launch_exprs = view->exprs;
+      launch_sites = view->sites;
+      launch_types = view->slot_type;
+      launch_sums = view->sum_mask;
+    }
+  }
+  int sum_cols[CQLOPS_MAX_BINDINGS];
+  uint32_t sum_col_count = 0;
+  for (int c = 0; c < CQLOPS_MAX_BINDINGS; c++)
+    if ((launch_sums >> c) & 1u) sum_cols[sum_col_count++] = c;
+  /* queries grouped by (launch) shape */
+  uint32_t* shape_count = (uint32_t*)calloc(launch_shapes + 1, 4);
   ok = ok && shape_count;
   if (ok)
   {
     for (uint32_t q = 0; q < query_count; q++) shape_count[shape_of[q]]++;
-    uint32_t* start = (uint32_t*)malloc((shapes + 1) * 4);
+    uint32_t* start = (uint32_t*)malloc((launch_shapes + 1) * 4);
     if (!start) ok = 0;
     else
     {
       uint32_t run = 0;
-      for (uint32_t s = 0; s < shapes; s++)
+      for (uint32_t s = 0; s < launch_shapes; s++)
       {
         start[s] = run;
         run += shape_count[s];
@@ -609,44 +764,68 @@ static int batch_run(const CqlProgram* const* programs, uint32_t query_count, co
       memcpy(&qc_o[(uint64_t)i * BATCH_MAX_CONSTS], &qconst[(uint64_t)q * BATCH_MAX_CONSTS], sizeof(double) * BATCH_MAX_CONSTS);
       qs_o[i] = qsum[q];
     }
-  uint64_t* folded = ok ? (uint64_t*)malloc((size_t)query_count * 24) : NULL;
-  ok = ok && folded;
-  if (source_only)
+  uint64_t* folded = ok && mode == BATCH_RUN ? (uint64_t*)malloc((size_t)query_count * 24) : NULL;
+  ok = ok && (folded || mode != BATCH_RUN);
+  /* one launch per slice of at most CQL_BATCH_LAUNCH_QUERIES queries: its shapes (all of the catalog's,
+     with a catalog) and where each starts */
+  uint32_t begin[BATCH_MAX_SHAPES + 1];
+  char* slice_exprs[BATCH_MAX_SHAPES];
+  uint32_t slice_sites[BATCH_MAX_SHAPES];
+#define SLICE_SHAPES(first, nq, ns)                                                   \
+  do                                                                                  \
+  {                                                                                   \
+    ns = 0;                                                                           \
+    if (view && launch_exprs == view->exprs)                                          \
+    {                                                                                 \
+      uint32_t at_ = 0;                                                               \
+      for (uint32_t s_ = 0; s_ < launch_shapes; s_++)                                 \
+      {                                                                               \
+        while (at_ < (nq) && shape_of[order[(first) + at_]] < s_) at_++;              \
+        begin[s_] = at_;                                                              \
+        slice_exprs[s_] = launch_exprs[s_];                                           \
+        slice_sites[s_] = launch_sites[s_];                                           \
+      }                                                                               \
+      ns = launch_shapes;                                                             \
+    }                                                                                 \
+    else                                                                              \
+      for (uint32_t i_ = 0; i_ < (nq); i_++)                                          \
+      {                                                                               \
+        uint32_t s_ = shape_of[order[(first) + i_]];                                  \
+        if (ns == 0 || slice_exprs[ns - 1] != launch_exprs[s_])                       \
+        {                                                                             \
+          slice_exprs[ns] = launch_exprs[s_];                                         \
+          slice_sites[ns] = launch_sites[s_];                                         \
+          begin[ns] = i_;                                                             \
+          ns++;                                                                       \
+        }                                                                             \
+      }                                                                               \
+    begin[ns] = (nq);                                                                 \
+  } while (0)
+  if (ok && mode != BATCH_RUN)
   {
-    free(folded);
-  }
-  /* launches of at most CQL_BATCH_LAUNCH_QUERIES queries, each the shapes of its slice */
-  if (ok && source_only)
-  {
-    /* the first launch's slice: the shapes of its queries */
     uint32_t nq = query_count < CQL_BATCH_LAUNCH_QUERIES ? query_count : CQL_BATCH_LAUNCH_QUERIES;
-    char* slice_exprs[BATCH_MAX_SHAPES];
-    uint32_t slice_sites[BATCH_MAX_SHAPES];
-    uint32_t ns = 0;
-    for (uint32_t i = 0; i < nq; i++)
-    {
-      uint32_t sh = shape_of[order[i]];
-      if (ns == 0 || slice_exprs[ns - 1] != exprs[sh])
-      {
-        slice_exprs[ns] = exprs[sh];
-        slice_sites[ns] = shape_sites[sh];
-        ns++;
-      }
-    }
-    char* src = batch_source(slice_exprs, slice_sites, ns, slot_type, sum_cols, sum_col_count, rows_per_thread);
+    uint32_t ns;
+    SLICE_SHAPES(0, nq, ns);
+    char* src = batch_source(slice_exprs, slice_sites, ns, launch_types, sum_cols, sum_col_count, rows_per_thread);
     ok = src != NULL;
-    if (ok)
+    if (ok && mode == BATCH_SOURCE)
     {
       uint64_t n = strlen(src);
       if (src_len) *src_len = n;
       if (src_out && src_cap) snprintf(src_out, src_cap, "%s", src);
       if (src_out && n + 1 > src_cap) ok = 0;
     }
+    else if (ok)
+    {
+      char name[64];
+      snprintf(name, sizeof(name), "qk_batch_%016llx", (unsigned long long)fnv_str(src));
+      size_t nlen = strlen(name);
+      ok = cqlcuda_kernel_alloc(name, nlen) || cqlcuda_kernel_alloc_from_image(name, nlen, src, strlen(src));
+    }
     free(src);
     if (out_shapes) *out_shapes = shapes;
-    folded = NULL;
   }
-  int launch = ok && !source_only;
+  int launch = ok && mode == BATCH_RUN;
   CqlBuffer* scale_buf = launch ? pooled("batch_col_scale", sizeof(col_scale), CQLCUDA_BUFFER_WRITE) : NULL;
   CqlBuffer* thr_buf = launch ? pooled("batch_thresholds", (uint64_t)query_count * BATCH_MAX_SITES * sizeof(Thr), CQLCUDA_BUFFER_WRITE) : NULL;
   CqlBuffer* qc_buf = launch ? pooled("batch_literals", (uint64_t)query_count * BATCH_MAX_CONSTS * 8, CQLCUDA_BUFFER_WRITE) : NULL;
@@ -666,42 +845,33 @@ static int batch_run(const CqlProgram* const* programs, uint32_t query_count, co
     ok = cqlcuda_batch_end(b);
   }
   uint64_t ctas = (uint64_t)(sm_count ? sm_count : 152) * BATCH_CTAS_PER_SM;
+  CqlKernel* shared_k = NULL;   /* with a catalog every slice runs the same kernel */
   for (uint32_t first = 0; launch && ok && first < query_count; first += CQL_BATCH_LAUNCH_QUERIES)
   {
     uint32_t nq = query_count - first < CQL_BATCH_LAUNCH_QUERIES ? query_count - first : CQL_BATCH_LAUNCH_QUERIES;
-    /* the shapes of this slice, in order, and where each starts */
-    uint32_t begin[BATCH_MAX_SHAPES + 1];
-    char* slice_exprs[BATCH_MAX_SHAPES];
-    uint32_t slice_sites[BATCH_MAX_SHAPES];
-    uint32_t ns = 0;
-    for (uint32_t i = 0; i < nq; i++)
-    {
-      uint32_t s = shape_of[order[first + i]];
-      if (ns == 0 || slice_exprs[ns - 1] != exprs[s])
-      {
-        slice_exprs[ns] = exprs[s];
-        slice_sites[ns] = shape_sites[s];
-        begin[ns] = i;
-        ns++;
-      }
-    }
-    begin[ns] = nq;
-    char* src = batch_source(slice_exprs, slice_sites, ns, slot_type, sum_cols, sum_col_count, rows_per_thread);
-    if (!src)
-    {
-      ok = 0;
-      break;
-    }
-    char name[64];
-    snprintf(name, sizeof(name), "qk_batch_%016llx", (unsigned long long)fnv_str(src));
-    size_t nlen = strlen(name);
-    CqlKernel* k = cqlcuda_kernel_alloc(name, nlen);
-    if (!k) k = cqlcuda_kernel_alloc_from_image(name, nlen, src, strlen(src));
-    free(src);
+    uint32_t ns;
+    SLICE_SHAPES(first, nq, ns);
+    CqlKernel* k = shared_k;
     if (!k)
     {
-      ok = 0;
-      break;
+      char* src = batch_source(slice_exprs, slice_sites, ns, launch_types, sum_cols, sum_col_count, rows_per_thread);
+      if (!src)
+      {
+        ok = 0;
+        break;
+      }
+      char name[64];
+      snprintf(name, sizeof(name), "qk_batch_%016llx", (unsigned long long)fnv_str(src));
+      size_t nlen = strlen(name);
+      k = cqlcuda_kernel_alloc(name, nlen);
+      if (!k) k = cqlcuda_kernel_alloc_from_image(name, nlen, src, strlen(src));
+      free(src);
+      if (!k)
+      {
+        ok = 0;
+        break;
+      }
+      if (view && launch_exprs == view->exprs) shared_k = k;
     }
     CqlBuffer* parts = pooled("batch_partials", ctas * nq * 24, CQLCUDA_BUFFER_READ_WRITE);
     if (!parts)
@@ -720,6 +890,7 @@ static int batch_run(const CqlProgram* const* programs, uint32_t query_count, co
     cqlcuda_kernel_set_arg_u64(k, 0, rows);
     cqlcuda_kernel_set_arg_u64(k, 1, nq);
     cqlcuda_kernel_set_arg_u64(k, 2, first);
+    cqlcuda_kernel_set_arg_u64(k, 3, (uint64_t)need | (uint64_t)sum_mask << 32);
     cqlcuda_kernel_set_arg_buffer(fold, 0, parts);
     cqlcuda_kernel_set_arg_buffer_range(fold, 1, out_buf, (uint64_t)first * 24, (uint64_t)nq * 24);
     cqlcuda_kernel_set_arg_u64(fold, 0, nq);
@@ -731,6 +902,7 @@ static int batch_run(const CqlProgram* const* programs, uint32_t query_count, co
     cqlcuda_batch_kernel_execute(b, fold, nq, QE_GPU_WORKGROUP_SIZE);
     ok = cqlcuda_batch_end(b);
   }
+#undef SLICE_SHAPES
   if (launch && ok)
   {
     CqlBatch* b = cqlcuda_batch_begin(0, (uint64_t)query_count * 24);
@@ -760,8 +932,8 @@ static int batch_run(const CqlProgram* const* programs, uint32_t query_count, co
   else if (!ok && why[0])
     refuse(why);
   for (uint32_t s = 0; s < shapes; s++) free(exprs[s]);
+  free(view);
   free(rb);
-  free(shape_hash);
   free(shape_of);
   free(order);
   free(thr);
@@ -772,7 +944,6 @@ static int batch_run(const CqlProgram* const* programs, uint32_t query_count, co
   free(qc_o);
   free(qs_o);
   free(folded);
-  (void)col_max;
   return ok;
 }
 
@@ -780,12 +951,28 @@ int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t qu
                                   const int32_t* sum_columns, uint32_t rows_per_thread, uint64_t* out_counts, double* out_sums,
                                   uint32_t* out_shapes)
 {
-  return batch_run(programs, query_count, columns, column_count, sum_columns, rows_per_thread, out_counts, out_sums, out_shapes, 0, NULL,
-                   0, NULL);
+  return batch_run(NULL, programs, query_count, columns, column_count, sum_columns, rows_per_thread, out_counts, out_sums, out_shapes,
+                   BATCH_RUN, NULL, 0, NULL);
+}
+
+int cqlops_batch_filter_aggregate_cat(CqlBatchCatalog* catalog, const CqlProgram* const* programs, uint32_t query_count,
+                                      const CqlColumn* columns, uint32_t column_count, const int32_t* sum_columns, uint32_t rows_per_thread,
+                                      uint64_t* out_counts, double* out_sums, uint32_t* out_shapes)
+{
+  return batch_run(catalog, programs, query_count, columns, column_count, sum_columns, rows_per_thread, out_counts, out_sums, out_shapes,
+                   BATCH_RUN, NULL, 0, NULL);
+}
+
+int cqlops_batch_prepare(CqlBatchCatalog* catalog, const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns,
+                         uint32_t column_count, const int32_t* sum_columns, uint32_t rows_per_thread)
+{
+  return batch_run(catalog, programs, query_count, columns, column_count, sum_columns, rows_per_thread, NULL, NULL, NULL, BATCH_PREPARE,
+                   NULL, 0, NULL);
 }
 
 int cqlops_batch_source(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
                         const int32_t* sum_columns, uint32_t rows_per_thread, char* out, uint64_t cap, uint64_t* out_len, uint32_t* out_shapes)
 {
-  return batch_run(programs, query_count, columns, column_count, sum_columns, rows_per_thread, NULL, NULL, out_shapes, 1, out, cap, out_len);
+  return batch_run(NULL, programs, query_count, columns, column_count, sum_columns, rows_per_thread, NULL, NULL, out_shapes, BATCH_SOURCE, out,
+                   cap, out_len);
 }

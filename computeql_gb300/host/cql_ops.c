@@ -29,8 +29,9 @@
 #define QE_SCAN_INT_NEVER 0x20000u
 #define QE_SCAN_INT_BIAS  0x40000u
 
-static uint32_t g_launch_mark = 0;
-static char g_error[256] = "";
+/* per calling thread: operators run concurrently on threads with their own backend lanes */
+static __thread uint32_t g_launch_mark = 0;
+static __thread char g_error[256] = "";
 
 const char* cqlops_last_error(void)
 {

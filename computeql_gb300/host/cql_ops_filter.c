@@ -13,6 +13,7 @@
  */
 #include "cqlops.h"
 
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -25,6 +26,8 @@
 const char* cqlops_last_error(void);
 uint32_t cqlops_program_simple_leaves(const CqlProgram* prog, CqlLeaf* out, uint32_t cap);
 
+/* the failed-key memo and its counters, shared by every calling thread */
+static pthread_mutex_t g_failed_lock = PTHREAD_MUTEX_INITIALIZER;
 static uint64_t g_failed[FAILED_CAP];
 static uint32_t g_failed_count = 0;
 static uint64_t g_generated_requests = 0, g_generated_failures = 0;
@@ -32,8 +35,10 @@ void cqlops_note_error(const char* why);
 
 void cqlops_generated_stats(uint64_t* out_requests, uint64_t* out_failures)
 {
+  pthread_mutex_lock(&g_failed_lock);
   if (out_requests) *out_requests = g_generated_requests;
   if (out_failures) *out_failures = g_generated_failures;
+  pthread_mutex_unlock(&g_failed_lock);
 }
 
 static int refuse(const char* why)
@@ -68,9 +73,12 @@ static uint64_t hash_check(const char* s, uint64_t n)
 
 static int failed_before(uint64_t key)
 {
+  int found = 0;
+  pthread_mutex_lock(&g_failed_lock);
   for (uint32_t i = 0; i < g_failed_count && i < FAILED_CAP; i++)
-    if (g_failed[i] == key) return 1;
-  return 0;
+    if (g_failed[i] == key) found = 1;
+  pthread_mutex_unlock(&g_failed_lock);
+  return found;
 }
 
 /* the generated kernel of `kind` for the program, from the backend's cache or NVRTC; NULL on failure */
@@ -90,7 +98,9 @@ static CqlKernel* generated_kernel(const CqlProgram* prog, uint32_t kind, const 
     free(src);
     return NULL;
   }
+  pthread_mutex_lock(&g_failed_lock);
   g_generated_requests += 1;
+  pthread_mutex_unlock(&g_failed_lock);
   uint64_t key = hash_fnv(src, len), check = hash_check(src, len);
   char name[64];
   snprintf(name, sizeof(name), "qk_%s_%016llx%016llx", kind == CQLOPS_KERNEL_SCAN ? "scan" : (kind == CQLOPS_KERNEL_FUSED_AGG ? "fagg" : "fgrp"),
@@ -105,8 +115,10 @@ static CqlKernel* generated_kernel(const CqlProgram* prog, uint32_t kind, const 
   free(src);
   if (!k)
   {
+    pthread_mutex_lock(&g_failed_lock);
     g_generated_failures += 1;
     g_failed[g_failed_count++ % FAILED_CAP] = key ^ check;
+    pthread_mutex_unlock(&g_failed_lock);
     refuse("the generated kernel did not compile");
   }
   return k;

@@ -37,6 +37,23 @@ class CqlColumn(C.Structure):
                 ("zone_min", dbl), ("zone_max", dbl), ("offsets", P), ("dict", P), ("zone_map", P), ("zone_map_chunks", u64)]
 
 
+class CqlServeConfig(C.Structure):
+    _fields_ = [("workers", u32), ("fuse", u32), ("max_fuse", u32), ("rows_per_thread", u32), ("memory_budget", u64)]
+
+
+class CqlServeRequest(C.Structure):
+    _fields_ = [("kind", u32), ("table", u32), ("program", P), ("sum_column", C.c_int32), ("column_count", u32), ("columns", u32 * 4),
+                ("expr_count", u32), ("funcs", u32 * 8), ("args", C.c_int32 * 8), ("max_groups", u64), ("out_counts", P),
+                ("out_sums", P), ("out_mins", P), ("out_maxs", P), ("call", P), ("ctx", P), ("footprint", u64), ("count", u64),
+                ("min_key", i64), ("sum", dbl * 4), ("min", dbl * 4), ("max", dbl * 4), ("status", C.c_int32), ("fused", u32),
+                ("submit_ns", u64), ("start_ns", u64), ("done_ns", u64), ("error", C.c_char * 128), ("next", P)]
+
+
+class CqlServeStats(C.Structure):
+    _fields_ = [(n, u64) for n in ("submitted", "completed", "failed", "scans", "fused_requests", "max_fused", "in_flight_bytes",
+                                   "peak_in_flight_bytes", "memory_budget", "admission_waits")]
+
+
 class CqlLeaf(C.Structure):
     _fields_ = [("column", u32), ("op", u32), ("target", dbl)]
 
@@ -127,6 +144,8 @@ CUDA_API = [
     ("cqlcuda_last_compile_log", cstr, []),
     ("cqlcuda_compile_check", C.c_int, [cstr, u64]),
     ("cqlcuda_compact_slots_noalloc", C.c_int, [P, P, u32, P, P, P, P, P]),
+    ("cqlcuda_thread_lane_begin", C.c_int, [cstr]),
+    ("cqlcuda_thread_lane_end", None, []),
     ("cqlcuda_fill_splitmix_u32", C.c_int, [P, u64, u64, u32, u32, u64]),
     ("cqlcuda_fill_sequence_u32", C.c_int, [P, u64, u32]),
     ("cqlcuda_flush_l2", C.c_int, [u64]),
@@ -156,6 +175,19 @@ OPS_API = [
     ("cqlops_zone_map_build", C.c_int, [P, P, u64]),
     ("cqlops_batch_filter_aggregate", C.c_int, [P, u32, P, u32, P, u32, P, P, P]),
     ("cqlops_batch_source", C.c_int, [P, u32, P, u32, P, u32, P, u64, P, P]),
+    ("cqlops_batch_catalog_create", P, []),
+    ("cqlops_batch_catalog_destroy", None, [P]),
+    ("cqlops_batch_catalog_shapes", u32, [P]),
+    ("cqlops_batch_filter_aggregate_cat", C.c_int, [P, P, u32, P, u32, P, u32, P, P, P]),
+    ("cqlops_batch_prepare", C.c_int, [P, P, u32, P, u32, P, u32]),
+    ("cqlserve_create", P, [P]),
+    ("cqlserve_destroy", None, [P]),
+    ("cqlserve_add_table", C.c_int, [P, P, u32]),
+    ("cqlserve_prepare", C.c_int, [P, u32, P, u32, P]),
+    ("cqlserve_submit", C.c_int, [P, P]),
+    ("cqlserve_wait", C.c_int, [P, P, u32]),
+    ("cqlserve_drain", None, [P]),
+    ("cqlserve_stats", CqlServeStats, [P]),
     ("cqlops_scan_ranges", u64, [P, u32, P, u32, P, u64, P, P, P]),
     ("cqlops_group_dense_fixed", C.c_int, [P, u32, P, P, P, u64, u64, P, P, P, P, P, P]),
     ("cqlops_hll_estimate", dbl, [P, u64]),

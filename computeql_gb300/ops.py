@@ -504,3 +504,217 @@ def compile_check(source):
     ok = lib.cqlcuda_compile_check(b, len(b))
     log = lib.cqlcuda_last_compile_log()
     return bool(ok), (log.decode() if log else "")
+
+
+# ---------------------------------------------------------------------------------------------
+# the served form (include/cqlserve.h)
+
+SERVE_FILTER_AGG, SERVE_AGG_GLOBAL, SERVE_GROUP_DENSE, SERVE_CALL = 1, 2, 3, 4
+_SERVE_CALL = C.CFUNCTYPE(C.c_int, C.c_void_p)
+
+
+class BatchCatalog:
+    """A shape catalog for repeated shared scans over one table (cqlops_batch_catalog_*)."""
+
+    def __init__(self):
+        self.h = N.load_ops().cqlops_batch_catalog_create()
+        if not self.h:
+            raise OpError("cqlops_batch_catalog_create failed")
+
+    @property
+    def shapes(self):
+        return N.load_ops().cqlops_batch_catalog_shapes(self.h)
+
+    def aggregate(self, programs, sum_names, rows_per_thread=8):
+        """batch_aggregate through the catalog -> (counts, sums, shapes)."""
+        q = len(programs)
+        base = programs[0]
+        ptrs = (C.c_void_p * q)(*[C.addressof(p.prog) for p in programs])
+        sc = np.array([base.index(n) if n is not None else -1 for n in sum_names], dtype=np.int32)
+        counts = np.empty(max(q, 1), dtype=np.uint64)
+        sums = np.empty(max(q, 1), dtype=np.float64)
+        shapes = C.c_uint32()
+        _check(N.load_ops().cqlops_batch_filter_aggregate_cat(self.h, ptrs, q, base._cols, len(base.columns), N.ptr(sc), rows_per_thread,
+                                                              N.ptr(counts), N.ptr(sums), C.byref(shapes)), "cqlops_batch_filter_aggregate_cat")
+        return counts[:q], sums[:q], shapes.value
+
+    def close(self):
+        if self.h:
+            N.load_ops().cqlops_batch_catalog_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ServeTable:
+    """A table registered with a Server: its named columns, in the order programs over it must use."""
+
+    def __init__(self, index, columns):
+        self.index = index
+        self.names = list(columns.keys())
+        self.columns = columns
+
+    def col(self, name):
+        return self.names.index(name)
+
+    def program(self, where):
+        return Program(where, self.columns)
+
+
+class ServeRequest:
+    """A submitted request; wait() blocks until it is done, then the result fields are valid."""
+
+    def __init__(self, server, req, keep):
+        self.server = server
+        self.req = req
+        self._keep = keep
+
+    def wait(self, timeout_ms=0):
+        return bool(N.load_ops().cqlserve_wait(self.server.h, C.byref(self.req), timeout_ms))
+
+    @property
+    def status(self):
+        return self.req.status
+
+    @property
+    def ok(self):
+        return self.req.status == 1
+
+    @property
+    def error(self):
+        return self.req.error.decode()
+
+    @property
+    def count(self):
+        return self.req.count
+
+    @property
+    def sum(self):
+        return self.req.sum[0]
+
+    @property
+    def fused(self):
+        return self.req.fused
+
+    @property
+    def latency_ns(self):
+        return self.req.done_ns - self.req.submit_ns
+
+    def group_result(self):
+        g = self.req.count
+        e = self.req.expr_count
+        counts, sums, mins, maxs = self._keep[1:5]
+        return (self.req.min_key, counts[:g], sums[: g * e].reshape(g, e), mins[: g * e].reshape(g, e), maxs[: g * e].reshape(g, e))
+
+
+class Server:
+    """Concurrent serving over resident tables: worker threads on their own lanes, admission by planned
+    device footprint, and (fuse=True) continuous batching of filter/aggregate requests into shared scans."""
+
+    def __init__(self, workers=2, fuse=True, max_fuse=1024, rows_per_thread=8, memory_budget=0):
+        cfg = N.CqlServeConfig(workers, int(bool(fuse)), max_fuse, rows_per_thread, memory_budget)
+        self.h = N.load_ops().cqlserve_create(C.byref(cfg))
+        if not self.h:
+            raise OpError("cqlserve_create failed: " + N.last_error())
+        self._tables = []
+
+    def add_table(self, columns):
+        arr = (N.CqlColumn * len(columns))(*[c.c() for c in columns.values()])
+        idx = N.load_ops().cqlserve_add_table(self.h, arr, len(columns))
+        if idx < 0:
+            raise OpError("cqlserve_add_table failed")
+        t = ServeTable(idx, columns)
+        t._arr = arr
+        self._tables.append(t)
+        return t
+
+    def prepare(self, table, programs, sum_names):
+        q = len(programs)
+        ptrs = (C.c_void_p * q)(*[C.addressof(p.prog) for p in programs])
+        sc = np.array([table.col(n) if n is not None else -1 for n in sum_names], dtype=np.int32)
+        _check(N.load_ops().cqlserve_prepare(self.h, table.index, ptrs, q, N.ptr(sc)), "cqlserve_prepare")
+
+    def _submit(self, req, keep):
+        r = ServeRequest(self, req, keep)
+        N.load_ops().cqlserve_submit(self.h, C.byref(req))
+        return r
+
+    def filter_agg(self, table, program, sum_name=None):
+        """SELECT COUNT(*)[, SUM(sum_name)] WHERE program."""
+        if program.names != table.names:
+            raise OpError("the program is not built over the table's columns")
+        req = N.CqlServeRequest()
+        req.kind = SERVE_FILTER_AGG
+        req.table = table.index
+        req.program = C.addressof(program.prog)
+        req.sum_column = table.col(sum_name) if sum_name is not None else -1
+        return self._submit(req, (program,))
+
+    def agg_global(self, table, names):
+        """SUM/MIN/MAX of up to 4 columns."""
+        req = N.CqlServeRequest()
+        req.kind = SERVE_AGG_GLOBAL
+        req.table = table.index
+        req.column_count = len(names)
+        for i, n in enumerate(names):
+            req.columns[i] = table.col(n)
+        return self._submit(req, ())
+
+    def group_dense(self, table, key, funcs, args):
+        """GROUP BY key (small range) with funcs over args (None for COUNT)."""
+        e = len(funcs)
+        lo, hi = table.columns[key].zone
+        g = int(hi - lo) + 1
+        counts = np.empty(g, dtype=np.uint64)
+        sums = np.empty(g * e, dtype=np.int64)
+        mins = np.empty(g * e, dtype=np.int64)
+        maxs = np.empty(g * e, dtype=np.int64)
+        req = N.CqlServeRequest()
+        req.kind = SERVE_GROUP_DENSE
+        req.table = table.index
+        req.column_count = 1
+        req.columns[0] = table.col(key)
+        req.expr_count = e
+        for i, (f, a) in enumerate(zip(funcs, args)):
+            req.funcs[i] = f
+            req.args[i] = table.col(a) if a is not None else -1
+        req.max_groups = g
+        req.out_counts, req.out_sums, req.out_mins, req.out_maxs = (a.ctypes.data for a in (counts, sums, mins, maxs))
+        return self._submit(req, ((), counts, sums, mins, maxs))
+
+    def call(self, fn, footprint=0):
+        """Runs fn() (-> bool) on a worker, admitted with `footprint` planned device bytes."""
+        cb = _SERVE_CALL(lambda _ctx: 1 if fn() else 0)
+        req = N.CqlServeRequest()
+        req.kind = SERVE_CALL
+        req.call = C.cast(cb, C.c_void_p)
+        req.footprint = footprint
+        return self._submit(req, (cb,))
+
+    def drain(self):
+        N.load_ops().cqlserve_drain(self.h)
+
+    def stats(self):
+        s = N.load_ops().cqlserve_stats(self.h)
+        return {n: getattr(s, n) for n, _ in N.CqlServeStats._fields_}
+
+    def close(self):
+        if self.h:
+            N.load_ops().cqlserve_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -193,6 +193,12 @@ int      cqlcuda_compact_slots_noalloc(const uint32_t* slot_counts, const uint32
    r*draws_per_row + draw_index (0-based) and stores draw % range (range 0 = the full 32 bits). */
 int      cqlcuda_fill_splitmix_u32(CqlBuffer* buffer, uint64_t rows, uint64_t seed, uint32_t draws_per_row, uint32_t draw_index, uint64_t range);
 /* Fills value[r] = first + r for r < rows. */
+/* Lanes (no reference counterpart): the calling thread gets its own stream, batch, kernel arguments and
+   pooled-buffer namespace (pool_tag), so several threads can run operators on the device at once.
+   Without a lane a thread uses the main lane: one batch at a time, as the reference's single queue.
+   Pooled buffers are not evicted while any lane is open. */
+int      cqlcuda_thread_lane_begin(const char* pool_tag);
+void     cqlcuda_thread_lane_end(void);
 int      cqlcuda_fill_sequence_u32(CqlBuffer* buffer, uint64_t rows, uint32_t first);
 /* Writes `bytes` bytes of a scratch buffer, to evict the L2 between timed runs. */
 int      cqlcuda_flush_l2(uint64_t bytes);

@@ -327,6 +327,27 @@ int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t qu
                                   const int32_t* sum_columns, uint32_t rows_per_thread, uint64_t* out_counts, double* out_sums,
                                   uint32_t* out_shapes);
 
+/* A shape catalog for a stream of batches over one table: the WHERE shapes, column types and summed
+   columns its batches have met, in the order met (at most 64 shapes). A batch run with a catalog
+   compiles one kernel for all of the catalog's shapes - a shape absent from the batch has no queries -
+   so batches of varying mixes of known shapes reuse one kernel; columns no query of a launch reads are
+   not loaded. A batch the catalog cannot take (full, or a column read as another type) runs as without
+   it. Safe to share between threads. */
+typedef struct CqlBatchCatalog CqlBatchCatalog;
+CqlBatchCatalog* cqlops_batch_catalog_create(void);
+void cqlops_batch_catalog_destroy(CqlBatchCatalog* catalog);
+uint32_t cqlops_batch_catalog_shapes(CqlBatchCatalog* catalog);
+
+/* cqlops_batch_filter_aggregate through a catalog; the results are the same. */
+int cqlops_batch_filter_aggregate_cat(CqlBatchCatalog* catalog, const CqlProgram* const* programs, uint32_t query_count,
+                                      const CqlColumn* columns, uint32_t column_count, const int32_t* sum_columns, uint32_t rows_per_thread,
+                                      uint64_t* out_counts, double* out_sums, uint32_t* out_shapes);
+
+/* Enters the queries' shapes in the catalog and compiles its kernel, without running it (a prepared
+   statement's compile step). */
+int cqlops_batch_prepare(CqlBatchCatalog* catalog, const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns,
+                         uint32_t column_count, const int32_t* sum_columns, uint32_t rows_per_thread);
+
 /* The CUDA C++ source cqlops_batch_filter_aggregate would compile for its first launch (no device
    work), up to cap bytes into out (out_len receives the length). */
 int cqlops_batch_source(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
