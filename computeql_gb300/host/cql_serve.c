@@ -27,6 +27,7 @@
 #define SERVE_MAX_TABLES 64
 #define SERVE_DEFAULT_BUDGET (160ull << 30)
 #define SERVE_SMALL_FOOTPRINT (1ull << 20)
+#define TAKE_REJECTED 0xffffffffu
 
 typedef struct
 {
@@ -187,7 +188,8 @@ static void unlink_request(CqlServer* sv, CqlServeRequest* prev, CqlServeRequest
 }
 
 /* With the lock held: takes the head request (and, fusing, the requests that share its scan) when the
-   budget admits it. Returns the count taken, 0 when the head must wait. */
+   budget admits it. Returns the count taken, 0 when the head must wait, TAKE_REJECTED when the head can
+   never fit (it is failed and removed). */
 static uint32_t take(CqlServer* sv, CqlServeRequest** group, uint32_t cap, uint64_t* out_bytes)
 {
   CqlServeRequest* h = sv->head;
@@ -200,7 +202,7 @@ static uint32_t take(CqlServer* sv, CqlServeRequest** group, uint32_t cap, uint6
     h->done_ns = now_ns();
     sv->stats.failed++;
     pthread_cond_broadcast(&sv->done);
-    return (uint32_t)-1;
+    return TAKE_REJECTED;
   }
   if (sv->stats.in_flight_bytes + fp > budget)
   {
@@ -257,14 +259,20 @@ static void* worker_main(void* arg)
   {
     uint32_t n = 0;
     uint64_t bytes = 0;
-    while (!(sv->stopping && !sv->head))
+    for (;;)
     {
       if (sv->head)
       {
-        n = take(sv, group, cap, &bytes);
-        if (n == (uint32_t)-1) continue;
-        if (n) break;
+        uint32_t got = take(sv, group, cap, &bytes);
+        if (got == TAKE_REJECTED) continue;   /* the head failed admission for good: look again */
+        if (got)
+        {
+          n = got;
+          break;
+        }
       }
+      else if (sv->stopping)
+        break;
       pthread_cond_wait(&sv->work, &sv->lock);
     }
     if (!n) break;
