@@ -647,29 +647,55 @@ static int launch_zone_map(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaS
 
 // ---------------------------------------------------------------------------------------------
 // cql_batch_fold: the batched scan's per-CTA partials [cta][query] x (count, sum low, sum high) summed
-// over the CTAs in order into [query] x (count, low, high) (128-bit integer sums, so any order gives the
-// same bits); binding 0 partials, 1 out; word 0 queries, word 2 CTAs.
+// over the CTAs into [query] x (count, low, high). One CTA per query; its threads take the CTAs in turn and
+// the block combines them in a tree. The sums are 128-bit integers, so any order gives the same bits.
+// Binding 0 partials, 1 out; word 0 queries, word 2 CTAs.
+
+struct Fold128
+{
+  unsigned long long c, lo, hi;
+};
+
+__device__ __forceinline__ void fold_add(Fold128& a, unsigned long long c, unsigned long long lo, unsigned long long hi)
+{
+  unsigned long long l2 = a.lo + lo;
+  a.hi += hi + (l2 < a.lo ? 1ull : 0ull);
+  a.lo = l2;
+  a.c += c;
+}
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_batch_fold(CqlLaunch a, uint32_t nq, uint32_t ctas)
 {
   const unsigned long long* parts = (const unsigned long long*)a.buf[0];
   unsigned long long* out = (unsigned long long*)a.buf[1];
-  uint64_t pcap = a.bytes[0] / 24;
-  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x)
+  const uint64_t pcap = a.bytes[0] / 24;
+  __shared__ Fold128 s_warp[SCAN_THREADS / 32];
+  for (uint32_t q = blockIdx.x; q < nq; q += gridDim.x)
   {
-    unsigned long long c = 0, lo = 0, hi = 0;
-    for (uint32_t b = 0; b < ctas; b++)
+    Fold128 f = { 0ull, 0ull, 0ull };
+    for (uint32_t b = threadIdx.x; b < ctas; b += blockDim.x)
     {
-      uint64_t at = (uint64_t)b * nq + q;
-      if (at >= pcap) break;
-      c += parts[at * 3];
-      unsigned long long l2 = lo + parts[at * 3 + 1];
-      hi += parts[at * 3 + 2] + (l2 < lo ? 1ull : 0ull);
-      lo = l2;
+      const uint64_t at = (uint64_t)b * nq + q;
+      if (at < pcap) fold_add(f, parts[at * 3], parts[at * 3 + 1], parts[at * 3 + 2]);
     }
-    out[q * 3] = c;
-    out[q * 3 + 1] = lo;
-    out[q * 3 + 2] = hi;
+    for (int o = 16; o > 0; o >>= 1)
+    {
+      unsigned long long c = __shfl_xor_sync(0xffffffffu, f.c, o);
+      unsigned long long lo = __shfl_xor_sync(0xffffffffu, f.lo, o);
+      unsigned long long hi = __shfl_xor_sync(0xffffffffu, f.hi, o);
+      fold_add(f, c, lo, hi);
+    }
+    if ((threadIdx.x & 31u) == 0u) s_warp[threadIdx.x >> 5] = f;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+      Fold128 t = s_warp[0];
+      for (uint32_t w = 1; w < blockDim.x / 32u; w++) fold_add(t, s_warp[w].c, s_warp[w].lo, s_warp[w].hi);
+      out[(uint64_t)q * 3] = t.c;
+      out[(uint64_t)q * 3 + 1] = t.lo;
+      out[(uint64_t)q * 3 + 2] = t.hi;
+    }
+    __syncthreads();
   }
 }
 
@@ -680,7 +706,7 @@ static int launch_batch_fold(const CqlLaunch& a, uint32_t gws, uint32_t lws, cud
   uint32_t nq = cql_word(a, 0), ctas = cql_word(a, 2);
   if (nq == 0) return 0;
   if (a.bytes[1] < (uint64_t)nq * 24) return (int)cudaErrorInvalidValue;
-  k_batch_fold<<<cql_stream_grid((nq + SCAN_THREADS - 1) / SCAN_THREADS, 8), SCAN_THREADS, 0, stream>>>(a, nq, ctas);
+  k_batch_fold<<<std::min<uint32_t>(nq, 65535u), SCAN_THREADS, 0, stream>>>(a, nq, ctas);
   CQL_LAUNCH_CHECK();
   return 0;
 }

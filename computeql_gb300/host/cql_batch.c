@@ -317,7 +317,25 @@ static const char* BATCH_PRELUDE =
   "__device__ __forceinline__ bool cql_bf(const Thr* t, float v) { float x = __uint_as_float((u32)t->a); u32 op = t->c; bool s = t->d != 0u;\n"
   "  if (op == 5u) return s ? v < x : v <= x; if (op == 7u) return v <= x; if (op == 6u) return s ? v > x : v >= x; if (op == 8u) return v >= x;\n"
   "  if (op == 3u) return v == x; return v != x; }\n"
-  "__device__ __forceinline__ double cql_i64d(u64 x) { double u = (double)(u32)(x >> 32) * 4294967296.0 + (double)(u32)x; return (x >> 63) ? u - 18446744073709551616.0 : u; }\n";
+  "__device__ __forceinline__ double cql_i64d(u64 x) { double u = (double)(u32)(x >> 32) * 4294967296.0 + (double)(u32)x; return (x >> 63) ? u - 18446744073709551616.0 : u; }\n"
+  /* x * 2^sh rounded to the nearest integer (ties to even), from the bits of x in integer arithmetic:
+     x = m * 2^e, so x * 2^sh = m * 2^(e + sh). Exact, as the product of x by the power of two is; a
+     NaN, an infinity or a product past 2^62 takes the double multiply and conversion instead. */
+  "__device__ __forceinline__ long long cql_fx64(u64 bits, int sh, double sc)\n"
+  "{\n"
+  "  const u32 ex = (u32)(bits >> 52) & 0x7ffu;\n"
+  "  u64 m = bits & 0xfffffffffffffull;\n"
+  "  int e = -1074;\n"
+  "  if (ex) { m |= 1ull << 52; e = (int)ex - 1075; }\n"
+  "  const int s = e + sh;\n"
+  "  if (ex == 0x7ffu || s > 9) return __double2ll_rn(__longlong_as_double((long long)bits) * sc);\n"
+  "  u64 mag;\n"
+  "  if (s >= 0) mag = m << s;\n"
+  "  else if (s < -63) mag = 0ull;\n"
+  "  else { const u32 r = (u32)(-s); const u64 q = m >> r, rem = m & ((1ull << r) - 1ull), half = 1ull << (r - 1u);\n"
+  "         mag = q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull); }\n"
+  "  return (bits >> 63) ? -(long long)mag : (long long)mag;\n"
+  "}\n";
 
 /* the source of one launch: `shape_exprs` over `shapes` shapes, the register blocks of slot_type */
 static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint32_t shapes, const int* slot_type, const int* sum_cols,
@@ -333,7 +351,8 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
        "  const u64 rows = cql_word(a, 0); const u32 nq = cql_word(a, 2); const u32 q0 = cql_word(a, 4);\n"
        "  const u32 need = cql_word(a, 6), need_sum = cql_word(a, 7);   /* the columns this launch reads and sums */\n"
        "  (void)need_sum;\n"
-       "  const double* col_scale = (const double*)a.buf[0];\n"
+       "  const double* col_scale = (const double*)a.buf[0];   /* 2^k per summed column, then k at [16 + column] */\n"
+       "  const long long* col_shift = (const long long*)a.buf[0] + 16;\n"
        "  const Thr* thr = (const Thr*)a.buf[1];\n"
        "  const double* qconst = (const double*)a.buf[2];\n"
        "  const u32* qsum = (const u32*)a.buf[3];\n"
@@ -379,16 +398,19 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
   {
     int c = sum_cols[i];
     int t = slot_type[c];
-    const char* val = t == CQLOPS_TYPE_F64 ? "__longlong_as_double((long long)r%d[v])"
-                    : t == CQLOPS_TYPE_F32 ? "(double)__uint_as_float(r%d[v])"
-                    : t == CQLOPS_TYPE_I32 ? "(double)(int)r%d[v]"
-                    : t == CQLOPS_TYPE_U64 ? "(double)r%d[v]"
-                    : t == CQLOPS_TYPE_I64 ? "cql_i64d(r%d[v])"
-                                           : "(double)r%d[v]";
+    /* the value times 2^k as an integer: a shift for whole numbers, the bits of a float otherwise; FP64
+       arithmetic only for 64-bit integers (the GPU's FP64 rate is a small fraction of its integer rate) */
+    char expr[200];
+    if (t == CQLOPS_TYPE_F64) snprintf(expr, sizeof(expr), "cql_fx64(r%d[v], sh, sc)", c);
+    else if (t == CQLOPS_TYPE_F32) snprintf(expr, sizeof(expr), "cql_fx64((u64)__double_as_longlong((double)__uint_as_float(r%d[v])), sh, sc)", c);
+    else if (t == CQLOPS_TYPE_I32)
+      snprintf(expr, sizeof(expr), "(sh >= 0 ? (long long)(int)r%d[v] * (1ll << sh) : __double2ll_rn((double)(int)r%d[v] * sc))", c, c);
+    else if (t == CQLOPS_TYPE_U64) snprintf(expr, sizeof(expr), "__double2ll_rn((double)r%d[v] * sc)", c);
+    else if (t == CQLOPS_TYPE_I64) snprintf(expr, sizeof(expr), "__double2ll_rn(cql_i64d(r%d[v]) * sc)", c);
+    else snprintf(expr, sizeof(expr), "(sh >= 0 ? (long long)((u64)r%d[v] << sh) : __double2ll_rn((double)r%d[v] * sc))", c, c);
     bput(&b, "    long long fx%d[%u];\n    if (!((need_sum >> %d) & 1u)) { for (u32 v = 0; v < RPT; v++) fx%d[v] = 0ll; }\n", c, rows_per_thread, c, c);
-    bput(&b, "    else { const double sc = col_scale[%d]; for (u32 v = 0; v < RPT; v++) { double x = ", c);
-    bput(&b, val, c);
-    bput(&b, "; fx%d[v] = v < valid ? __double2ll_rn(x * sc) : 0ll; } }\n", c);
+    bput(&b, "    else { const double sc = col_scale[%d]; const int sh = (int)col_shift[%d]; (void)sh; (void)sc;\n", c, c);
+    bput(&b, "      for (u32 v = 0; v < RPT; v++) fx%d[v] = v < valid ? %s : 0ll; }\n", c, expr);
   }
   for (uint32_t s = 0; s < shapes; s++)
   {
@@ -676,6 +698,7 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
   /* summed columns: loaded, scaled by 2^k with k from the column's range */
   uint32_t sm_count = cqlcuda_sm_count();
   double col_scale[CQLOPS_MAX_BINDINGS] = { 0 };
+  int64_t col_shift[CQLOPS_MAX_BINDINGS] = { 0 };
   uint32_t sum_mask = 0;
   for (uint32_t q = 0; ok && q < query_count; q++)
   {
@@ -700,6 +723,7 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     int wr = 0;
     frexp((double)warp_rows, &wr);   /* warp_rows < 2^wr */
     col_scale[c] = ldexp(1.0, 62 - e - wr);
+    col_shift[c] = 62 - e - wr;
     sum_mask |= 1u << c;
   }
   /* the columns this batch loads */
@@ -826,31 +850,47 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     if (out_shapes) *out_shapes = shapes;
   }
   int launch = ok && mode == BATCH_RUN;
-  CqlBuffer* scale_buf = launch ? pooled("batch_col_scale", sizeof(col_scale), CQLCUDA_BUFFER_WRITE) : NULL;
-  CqlBuffer* thr_buf = launch ? pooled("batch_thresholds", (uint64_t)query_count * BATCH_MAX_SITES * sizeof(Thr), CQLCUDA_BUFFER_WRITE) : NULL;
-  CqlBuffer* qc_buf = launch ? pooled("batch_literals", (uint64_t)query_count * BATCH_MAX_CONSTS * 8, CQLCUDA_BUFFER_WRITE) : NULL;
-  CqlBuffer* qs_buf = launch ? pooled("batch_sum_columns", (uint64_t)query_count * 4, CQLCUDA_BUFFER_WRITE) : NULL;
-  CqlBuffer* begin_buf = launch ? pooled("batch_shape_begin", (BATCH_MAX_SHAPES + 1) * 4, CQLCUDA_BUFFER_WRITE) : NULL;
-  CqlBuffer* out_buf = launch ? pooled("batch_folded", (uint64_t)query_count * 24, CQLCUDA_BUFFER_READ_WRITE) : NULL;
-  CqlKernel* fold = launch ? cqlcuda_kernel_alloc("cql_batch_fold", 14) : NULL;
-  if (launch) ok = scale_buf && thr_buf && qc_buf && qs_buf && begin_buf && out_buf && fold;
-  launch = launch && ok;
-  if (launch)
+  /* one upload of every launch parameter: the scales (doubles at 0..), then their exponents (64-bit
+     integers at 16..), the thresholds, literals and summed columns in shape order, and each slice's shape
+     starts; each part on a 16-byte boundary */
+  uint32_t slices = (query_count + CQL_BATCH_LAUNCH_QUERIES - 1) / CQL_BATCH_LAUNCH_QUERIES;
+  const uint64_t off_thr = 256;
+  const uint64_t off_qc = off_thr + (uint64_t)query_count * BATCH_MAX_SITES * sizeof(Thr);
+  const uint64_t off_qs = off_qc + (uint64_t)query_count * BATCH_MAX_CONSTS * 8;
+  const uint64_t off_begin = off_qs + (((uint64_t)query_count * 4 + 15) & ~15ull);
+  const uint64_t begin_stride = ((BATCH_MAX_SHAPES + 1) * 4 + 15) & ~15ull;
+  const uint64_t param_bytes = off_begin + (uint64_t)slices * begin_stride;
+  unsigned char* params = launch ? (unsigned char*)calloc(1, param_bytes) : NULL;
+  if (launch && !params) ok = 0;
+  if (params)
   {
-    CqlBatch* b = cqlcuda_batch_begin(0, 0);
-    cqlcuda_batch_buffer_write(b, scale_buf, col_scale, sizeof(col_scale));
-    cqlcuda_batch_buffer_write(b, thr_buf, thr_o, (uint64_t)query_count * BATCH_MAX_SITES * sizeof(Thr));
-    cqlcuda_batch_buffer_write(b, qc_buf, qc_o, (uint64_t)query_count * BATCH_MAX_CONSTS * 8);
-    cqlcuda_batch_buffer_write(b, qs_buf, qs_o, (uint64_t)query_count * 4);
-    ok = cqlcuda_batch_end(b);
+    memcpy(params, col_scale, sizeof(col_scale));
+    memcpy(params + 128, col_shift, sizeof(col_shift));
+    memcpy(params + off_thr, thr_o, (size_t)query_count * BATCH_MAX_SITES * sizeof(Thr));
+    memcpy(params + off_qc, qc_o, (size_t)query_count * BATCH_MAX_CONSTS * 8);
+    memcpy(params + off_qs, qs_o, (size_t)query_count * 4);
   }
   uint64_t ctas = (uint64_t)(sm_count ? sm_count : 152) * BATCH_CTAS_PER_SM;
+  uint32_t widest = query_count < CQL_BATCH_LAUNCH_QUERIES ? query_count : CQL_BATCH_LAUNCH_QUERIES;
+  CqlBuffer* param_buf = launch && ok ? pooled("batch_params", param_bytes, CQLCUDA_BUFFER_WRITE) : NULL;
+  CqlBuffer* out_buf = launch && ok ? pooled("batch_folded", (uint64_t)query_count * 24, CQLCUDA_BUFFER_READ_WRITE) : NULL;
+  CqlBuffer* parts = launch && ok ? pooled("batch_partials", ctas * widest * 24, CQLCUDA_BUFFER_READ_WRITE) : NULL;
+  CqlKernel* fold = launch ? cqlcuda_kernel_alloc("cql_batch_fold", 14) : NULL;
+  if (launch) ok = ok && param_buf && out_buf && parts && fold;
+  launch = launch && ok;
+  /* each slice's kernel, compiled (or found) before anything is queued; with a catalog one for all */
+  CqlKernel** kernels = launch ? (CqlKernel**)calloc(slices, sizeof(CqlKernel*)) : NULL;
+  uint32_t* slice_ns = launch ? (uint32_t*)calloc(slices, 4) : NULL;
+  if (launch && (!kernels || !slice_ns)) ok = 0;
   CqlKernel* shared_k = NULL;   /* with a catalog every slice runs the same kernel */
-  for (uint32_t first = 0; launch && ok && first < query_count; first += CQL_BATCH_LAUNCH_QUERIES)
+  for (uint32_t sl = 0; launch && ok && sl < slices; sl++)
   {
+    uint32_t first = sl * CQL_BATCH_LAUNCH_QUERIES;
     uint32_t nq = query_count - first < CQL_BATCH_LAUNCH_QUERIES ? query_count - first : CQL_BATCH_LAUNCH_QUERIES;
     uint32_t ns;
     SLICE_SHAPES(first, nq, ns);
+    memcpy(params + off_begin + sl * begin_stride, begin, (ns + 1) * 4);
+    slice_ns[sl] = ns;
     CqlKernel* k = shared_k;
     if (!k)
     {
@@ -873,42 +913,45 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
       }
       if (view && launch_exprs == view->exprs) shared_k = k;
     }
-    CqlBuffer* parts = pooled("batch_partials", ctas * nq * 24, CQLCUDA_BUFFER_READ_WRITE);
-    if (!parts)
-    {
-      ok = 0;
-      break;
-    }
-    cqlcuda_kernel_set_arg_buffer(k, 0, scale_buf);
-    cqlcuda_kernel_set_arg_buffer(k, 1, thr_buf);
-    cqlcuda_kernel_set_arg_buffer(k, 2, qc_buf);
-    cqlcuda_kernel_set_arg_buffer(k, 3, qs_buf);
-    cqlcuda_kernel_set_arg_buffer(k, 4, begin_buf);
-    cqlcuda_kernel_set_arg_buffer(k, 5, parts);
-    for (uint32_t c = 0; c < CQLOPS_MAX_BINDINGS; c++)
-      cqlcuda_kernel_set_arg_buffer(k, 6 + c, columns[c < column_count ? c : 0].buffer);
-    cqlcuda_kernel_set_arg_u64(k, 0, rows);
-    cqlcuda_kernel_set_arg_u64(k, 1, nq);
-    cqlcuda_kernel_set_arg_u64(k, 2, first);
-    cqlcuda_kernel_set_arg_u64(k, 3, (uint64_t)need | (uint64_t)sum_mask << 32);
-    cqlcuda_kernel_set_arg_buffer(fold, 0, parts);
-    cqlcuda_kernel_set_arg_buffer_range(fold, 1, out_buf, (uint64_t)first * 24, (uint64_t)nq * 24);
-    cqlcuda_kernel_set_arg_u64(fold, 0, nq);
-    cqlcuda_kernel_set_arg_u64(fold, 1, ctas);
-    CqlBatch* b = cqlcuda_batch_begin((ns + 1) * 4, 0);
-    cqlcuda_batch_buffer_write(b, begin_buf, begin, (ns + 1) * 4);
-    cqlcuda_batch_buffer_zero(b, parts, ctas * nq * 24);
-    cqlcuda_batch_kernel_execute(b, k, (uint32_t)(ctas * QE_GPU_WORKGROUP_SIZE), QE_GPU_WORKGROUP_SIZE);
-    cqlcuda_batch_kernel_execute(b, fold, nq, QE_GPU_WORKGROUP_SIZE);
-    ok = cqlcuda_batch_end(b);
+    kernels[sl] = k;
   }
 #undef SLICE_SHAPES
+  /* one batch: the upload, every slice's scan and fold, the read-back; one wait */
   if (launch && ok)
   {
-    CqlBatch* b = cqlcuda_batch_begin(0, (uint64_t)query_count * 24);
+    CqlBatch* b = cqlcuda_batch_begin(param_bytes, (uint64_t)query_count * 24);
+    cqlcuda_batch_buffer_write(b, param_buf, params, param_bytes);
+    for (uint32_t sl = 0; sl < slices; sl++)
+    {
+      uint32_t first = sl * CQL_BATCH_LAUNCH_QUERIES;
+      uint32_t nq = query_count - first < CQL_BATCH_LAUNCH_QUERIES ? query_count - first : CQL_BATCH_LAUNCH_QUERIES;
+      CqlKernel* k = kernels[sl];
+      cqlcuda_kernel_set_arg_buffer_range(k, 0, param_buf, 0, 256);
+      cqlcuda_kernel_set_arg_buffer_range(k, 1, param_buf, off_thr, off_qc - off_thr);
+      cqlcuda_kernel_set_arg_buffer_range(k, 2, param_buf, off_qc, off_qs - off_qc);
+      cqlcuda_kernel_set_arg_buffer_range(k, 3, param_buf, off_qs, (uint64_t)query_count * 4);
+      cqlcuda_kernel_set_arg_buffer_range(k, 4, param_buf, off_begin + sl * begin_stride, (slice_ns[sl] + 1) * 4);
+      cqlcuda_kernel_set_arg_buffer_range(k, 5, parts, 0, ctas * nq * 24);
+      for (uint32_t c = 0; c < CQLOPS_MAX_BINDINGS; c++)
+        cqlcuda_kernel_set_arg_buffer(k, 6 + c, columns[c < column_count ? c : 0].buffer);
+      cqlcuda_kernel_set_arg_u64(k, 0, rows);
+      cqlcuda_kernel_set_arg_u64(k, 1, nq);
+      cqlcuda_kernel_set_arg_u64(k, 2, first);
+      cqlcuda_kernel_set_arg_u64(k, 3, (uint64_t)need | (uint64_t)sum_mask << 32);
+      cqlcuda_kernel_set_arg_buffer_range(fold, 0, parts, 0, ctas * nq * 24);
+      cqlcuda_kernel_set_arg_buffer_range(fold, 1, out_buf, (uint64_t)first * 24, (uint64_t)nq * 24);
+      cqlcuda_kernel_set_arg_u64(fold, 0, nq);
+      cqlcuda_kernel_set_arg_u64(fold, 1, ctas);
+      cqlcuda_batch_buffer_zero(b, parts, ctas * nq * 24);
+      cqlcuda_batch_kernel_execute(b, k, (uint32_t)(ctas * QE_GPU_WORKGROUP_SIZE), QE_GPU_WORKGROUP_SIZE);
+      cqlcuda_batch_kernel_execute(b, fold, nq, QE_GPU_WORKGROUP_SIZE);
+    }
     cqlcuda_batch_buffer_read(b, out_buf, folded, (uint64_t)query_count * 24);
     ok = cqlcuda_batch_end(b);
   }
+  free(params);
+  free(kernels);
+  free(slice_ns);
   if (launch && ok)
   {
     for (uint32_t i = 0; i < query_count; i++)
