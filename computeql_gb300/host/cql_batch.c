@@ -473,6 +473,239 @@ static CqlBuffer* pooled(const char* name, uint64_t size, uint32_t flags)
   return cqlcuda_buffer_alloc_pooled(name, (uint64_t)strlen(name), size ? size : 8, flags, NULL);
 }
 
+/* ---- the shared-memory tile form ---- */
+
+/* A CTA stages a tile of rows of every loaded column (32-bit values as they are, f64 columns as order
+   keys, 64-bit integers raw) and of every summed column (its fixed-point summands) in shared memory; its
+   warps then take (query, part of the tile) items, each lane walking the part's rows 32 apart with the
+   count and sum in registers, and a warp adds its totals to the CTA's accumulators once per item - not
+   once per few rows as the register form does. */
+typedef struct
+{
+  uint32_t tile;     /* rows per tile: 1024 or 512 */
+  uint32_t per_sm;   /* resident CTAs per SM the shared memory allows (at most 8) */
+  uint32_t smem;     /* dynamic shared memory per CTA */
+  uint32_t n32, n64; /* 32-bit and 64-bit tiles */
+} TiledLayout;
+
+#define TILED_SHAPE_SLOTS 260   /* the query-to-shape table in shared memory (u32 entries) */
+
+static TiledLayout tiled_layout(const int* slot_type, uint32_t sum_col_count)
+{
+  TiledLayout l;
+  l.n32 = 0;
+  l.n64 = sum_col_count;
+  for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++)
+    if (slot_type[s])
+    {
+      if (type_bytes(slot_type[s]) == 8) l.n64++;
+      else l.n32++;
+    }
+  uint32_t per_row = 4 * l.n32 + 8 * l.n64;
+  uint32_t fixed = 2u * CQL_BATCH_LAUNCH_QUERIES * 8u + (CQL_BATCH_LAUNCH_QUERIES + TILED_SHAPE_SLOTS) * 4u;
+  l.tile = per_row * 1024u + fixed <= 72u * 1024u ? 1024u : 512u;
+  l.smem = per_row * l.tile + fixed;
+  uint32_t per_sm = (227u * 1024u) / (l.smem + 1024u);
+  l.per_sm = per_sm > 8 ? 8 : (per_sm < 1 ? 1 : per_sm);
+  return l;
+}
+
+static char* batch_source_tiled(char** shape_exprs, const uint32_t* shape_sites, uint32_t shapes, const int* slot_type, const int* sum_cols,
+                                uint32_t sum_col_count)
+{
+  TiledLayout L = tiled_layout(slot_type, sum_col_count);
+  const uint32_t per_thread = L.tile / QE_GPU_WORKGROUP_SIZE;   /* rows a thread stages: 4 or 2 */
+  Buf b;
+  memset(&b, 0, sizeof(b));
+  bput(&b, "// cql: block=%u smem=%u per_sm=%u\n", QE_GPU_WORKGROUP_SIZE, L.smem, L.per_sm);
+  bput(&b, "%s", BATCH_PRELUDE);
+  bput(&b, "struct KeyBits { const u64* p; __device__ __forceinline__ u64 operator[](u32 i) const { const u64 k = p[i]; return (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k; } };\n");
+  for (uint32_t s = 0; s < shapes; s++) bput(&b, "#define CQL_SHAPE_%u(k) (%s)\n", s, shape_exprs[s]);
+  bput(&b,
+       "extern \"C\" __global__ void __launch_bounds__(%u) cql_main(CqlLaunch a)\n{\n"
+       "  const u32 TILE = %uu, PT = %uu;\n"
+       "  const u64 rows = cql_word(a, 0); const u32 nq = cql_word(a, 2); const u32 q0 = cql_word(a, 4);\n"
+       "  const u32 need = cql_word(a, 6), need_sum = cql_word(a, 7);   /* the columns this launch reads and sums */\n"
+       "  const double* col_scale = (const double*)a.buf[0];   /* 2^k per summed column, then k at [16 + column] */\n"
+       "  const long long* col_shift = (const long long*)a.buf[0] + 16;\n"
+       "  const Thr* thr = (const Thr*)a.buf[1];\n"
+       "  const double* qconst = (const double*)a.buf[2];\n"
+       "  const u32* qsum = (const u32*)a.buf[3];\n"
+       "  const u32* shape_begin = (const u32*)a.buf[4];\n"
+       "  u64* partials = (u64*)a.buf[5]; const u64 pcap = a.bytes[5] / 24ull;\n"
+       "  (void)col_scale; (void)col_shift; (void)need_sum;\n"
+       "  extern __shared__ u64 s_mem[];\n"
+       "  u64* s_cnt = s_mem; u64* s_sum = s_mem + %uu;\n"
+       "  u32* s_shape = (u32*)(s_mem + 2u * %uu);\n"
+       "  u64* t64 = s_mem + 2u * %uu + (%uu + 1u) / 2u;\n"
+       "  u32* t32 = (u32*)(t64 + (u64)%uu * TILE);\n"
+       "  const u32 lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;\n"
+       "  for (u32 i = threadIdx.x; i < 2u * %uu; i += blockDim.x) s_mem[i] = 0ull;\n"
+       "  for (u32 q = threadIdx.x; q < nq; q += blockDim.x) { u32 s = 0u; while (s + 1u < %uu && q >= shape_begin[s + 1u]) s++; s_shape[q] = s; }\n",
+       QE_GPU_WORKGROUP_SIZE, L.tile, per_thread, CQL_BATCH_LAUNCH_QUERIES, CQL_BATCH_LAUNCH_QUERIES, CQL_BATCH_LAUNCH_QUERIES,
+       CQL_BATCH_LAUNCH_QUERIES + TILED_SHAPE_SLOTS, L.n64, CQL_BATCH_LAUNCH_QUERIES, shapes + 1);
+  /* the tiles: 64-bit ones first (f64 keys, raw 64-bit integers, then the summands), then 32-bit ones */
+  uint32_t i64 = 0, i32 = 0;
+  for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++)
+  {
+    int t = slot_type[s];
+    if (!t) continue;
+    if (type_bytes(t) == 8)
+    {
+      if (t == CQLOPS_TYPE_F64) bput(&b, "  u64* kd%d = t64 + %uu * TILE; const KeyBits r%d = { kd%d };\n", s, i64, s, s);
+      else bput(&b, "  u64* r%d = t64 + %uu * TILE;\n", s, i64);
+      i64++;
+    }
+    else
+      bput(&b, "  u32* r%d = t32 + %uu * TILE;\n", s, i32++);
+  }
+  for (uint32_t i = 0; i < sum_col_count; i++) bput(&b, "  long long* fx%d = (long long*)(t64 + %uu * TILE);\n", sum_cols[i], i64++);
+  bput(&b,
+       "  const u32 parts = nq >= warps ? 1u : warps / nq;   /* few queries: each also split over the tile's rows */\n"
+       "  const u32 items = nq * parts;\n"
+       "  const u64 tiles = (rows + TILE - 1ull) / TILE;\n"
+       "  const u32 i0 = threadIdx.x * PT;\n");
+  /* each thread's PT consecutive rows of every needed column, fetched into registers one tile ahead: the
+     next tile's loads are in flight while the warps evaluate this one */
+  for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++)
+    if (slot_type[s]) bput(&b, "  %s v%d[%u];\n", type_bytes(slot_type[s]) == 8 ? "u64" : "u32", s, per_thread);
+  bput(&b, "  u64 tf = blockIdx.x;\n");
+  char* fetch = NULL;
+  {
+    Buf f;
+    memset(&f, 0, sizeof(f));
+    bput(&f, "  {\n    const u64 fb = tf * TILE; const u32 fn = tf < tiles ? (u32)min((u64)TILE, rows - fb) : 0u;\n");
+    for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++)
+    {
+      int t = slot_type[s];
+      if (!t) continue;
+      int w = type_bytes(t);
+      bput(&f, "    if ((need >> %d) & 1u)\n    {\n", s);
+      if (w == 8)
+        bput(&f,
+             "      if (fn == TILE) { for (u32 j = 0; j < PT; j += 2u) { uint4 x = cql_ld4((const u64*)a.buf[%d] + fb + i0 + j); v%d[j] = ((u64)x.y << 32) | x.x; v%d[j + 1] = ((u64)x.w << 32) | x.z; } }\n"
+             "      else { for (u32 j = 0; j < PT; j++) v%d[j] = i0 + j < fn ? ((const u64*)a.buf[%d])[fb + i0 + j] : 0ull; }\n",
+             6 + s, s, s, s, 6 + s);
+      else if (w == 1)
+        bput(&f, "      for (u32 j = 0; j < PT; j++) v%d[j] = i0 + j < fn ? (u32)((const unsigned char*)a.buf[%d])[fb + i0 + j] : 0u;\n", s, 6 + s);
+      else if (per_thread == 4)
+        bput(&f,
+             "      if (fn == TILE) { uint4 x = cql_ld4((const u32*)a.buf[%d] + fb + i0); v%d[0] = x.x; v%d[1] = x.y; v%d[2] = x.z; v%d[3] = x.w; }\n"
+             "      else { for (u32 j = 0; j < 4u; j++) v%d[j] = i0 + j < fn ? ((const u32*)a.buf[%d])[fb + i0 + j] : 0u; }\n",
+             6 + s, s, s, s, s, s, 6 + s);
+      else
+        bput(&f, "      for (u32 j = 0; j < PT; j++) v%d[j] = i0 + j < fn ? ((const u32*)a.buf[%d])[fb + i0 + j] : 0u;\n", s, 6 + s);
+      bput(&f, "    }\n");
+    }
+    bput(&f, "  }\n");
+    if (f.failed)
+    {
+      free(f.p);
+      b.failed = 1;
+    }
+    else
+      fetch = f.p;
+  }
+  if (fetch) bput(&b, "%s", fetch);
+  bput(&b,
+       "  __syncthreads();\n"
+       "  for (u64 t = blockIdx.x; t < tiles; t += gridDim.x)\n  {\n"
+       "    const u64 base = t * TILE;\n"
+       "    const u32 n = (u32)min((u64)TILE, rows - base);\n"
+       "    (void)base;\n");
+  /* staging: the fetched registers into the tiles (f64 columns as order keys, summed columns also as
+     their fixed-point summands) */
+  for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++)
+  {
+    int t = slot_type[s];
+    if (!t) continue;
+    int summed = 0;
+    for (uint32_t i = 0; i < sum_col_count; i++)
+      if (sum_cols[i] == s) summed = 1;
+    bput(&b, "    if ((need >> %d) & 1u)\n    {\n", s);
+    if (t == CQLOPS_TYPE_F64) bput(&b, "      for (u32 j = 0; j < PT; j++) kd%d[i0 + j] = cql_key(v%d[j]);\n", s, s);
+    else bput(&b, "      for (u32 j = 0; j < PT; j++) r%d[i0 + j] = v%d[j];\n", s, s);
+    if (summed)
+    {
+      char expr[220];
+      if (t == CQLOPS_TYPE_F64) snprintf(expr, sizeof(expr), "cql_fx64(v%d[j], sh, sc)", s);
+      else if (t == CQLOPS_TYPE_F32) snprintf(expr, sizeof(expr), "cql_fx64((u64)__double_as_longlong((double)__uint_as_float(v%d[j])), sh, sc)", s);
+      else if (t == CQLOPS_TYPE_I32)
+        snprintf(expr, sizeof(expr), "(sh >= 0 ? (long long)(int)v%d[j] * (1ll << sh) : __double2ll_rn((double)(int)v%d[j] * sc))", s, s);
+      else if (t == CQLOPS_TYPE_U64) snprintf(expr, sizeof(expr), "__double2ll_rn((double)v%d[j] * sc)", s);
+      else if (t == CQLOPS_TYPE_I64) snprintf(expr, sizeof(expr), "__double2ll_rn(cql_i64d(v%d[j]) * sc)", s);
+      else snprintf(expr, sizeof(expr), "(sh >= 0 ? (long long)((u64)v%d[j] << sh) : __double2ll_rn((double)v%d[j] * sc))", s, s);
+      bput(&b,
+           "      if ((need_sum >> %d) & 1u) { const double sc = col_scale[%d]; const int sh = (int)col_shift[%d]; (void)sc; (void)sh;\n"
+           "        for (u32 j = 0; j < PT; j++) fx%d[i0 + j] = i0 + j < n ? %s : 0ll; }\n",
+           s, s, s, s, expr);
+    }
+    bput(&b, "    }\n");
+  }
+  bput(&b, "    __syncthreads();\n    tf = t + gridDim.x;\n");
+  if (fetch) bput(&b, "%s", fetch);
+  free(fetch);
+  bput(&b,
+       "    for (u32 it = warp; it < items; it += warps)\n    {\n"
+       "      const u32 q = it / parts, part = it - q * parts;\n"
+       "      const u32 span = (n + parts - 1u) / parts;\n"
+       "      const u32 lo = min(n, part * span), hi = min(n, lo + span);\n"
+       "      const Thr* TH = thr + (u64)(q0 + q) * %uu; const double* QC = qconst + (u64)(q0 + q) * %uu;\n"
+       "      (void)TH; (void)QC;\n"
+       "      const u32 sc = qsum[q0 + q];\n"
+       "      const long long* fxp = ",
+       BATCH_MAX_SITES, BATCH_MAX_CONSTS);
+  for (uint32_t i = 0; i < sum_col_count; i++) bput(&b, "sc == %du ? fx%d : ", sum_cols[i], sum_cols[i]);
+  bput(&b,
+       "(const long long*)0;\n"
+       "      (void)fxp;\n"
+       "      u32 cnt = 0u; long long sv = 0ll;\n"
+       "      switch (s_shape[q])\n      {\n");
+  for (uint32_t s = 0; s < shapes; s++)
+  {
+    char decls[BATCH_MAX_SITES * 40 + 1];
+    size_t dn = 0;
+    decls[0] = 0;
+    for (uint32_t i = 0; i < shape_sites[s] && i < BATCH_MAX_SITES; i++)
+      dn += (size_t)snprintf(decls + dn, sizeof(decls) - dn, "        const Thr T%u = TH[%u];\n", i, i);
+    bput(&b,
+         "      case %uu:\n      {\n"
+         "%s"
+         "        if (!fxp) { for (u32 k = lo + lane; k < hi; k += 32u) cnt += (CQL_SHAPE_%u(k)) ? 1u : 0u; }\n"
+         "        else { for (u32 k = lo + lane; k < hi; k += 32u) { const bool m = CQL_SHAPE_%u(k); cnt += m ? 1u : 0u; sv += m ? fxp[k] : 0ll; } }\n"
+         "        break;\n      }\n",
+         s, decls, s, s);
+  }
+  bput(&b,
+       "      default: break;\n"
+       "      }\n"
+       "      cnt = __reduce_add_sync(0xffffffffu, cnt);\n"
+       "      if (fxp) { for (int o = 16; o > 0; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o); }\n"
+       "      if (lane == 0u) { atomicAdd(&s_cnt[q], (u64)cnt); if (sv) atomicAdd(&s_sum[q], (u64)sv); }\n"
+       "    }\n"
+       "    __syncthreads();\n"
+       "  }\n"
+       "  for (u32 q = threadIdx.x; q < nq; q += blockDim.x)\n  {\n"
+       "    const long long v = (long long)s_sum[q];\n"
+       "    const u64 at = (u64)blockIdx.x * nq + q;\n"
+       "    if (at < pcap) { partials[at * 3] = s_cnt[q]; partials[at * 3 + 1] = (u64)v; partials[at * 3 + 2] = v < 0 ? ~0ull : 0ull; }\n"
+       "  }\n}\n");
+  if (b.failed)
+  {
+    free(b.p);
+    return NULL;
+  }
+  return b.p;
+}
+
+/* the source of one launch in the form rows_per_thread asks for */
+static char* launch_source(char** shape_exprs, const uint32_t* shape_sites, uint32_t shapes, const int* slot_type, const int* sum_cols,
+                           uint32_t sum_col_count, uint32_t rows_per_thread)
+{
+  if (!rows_per_thread) return batch_source_tiled(shape_exprs, shape_sites, shapes, slot_type, sum_cols, sum_col_count);
+  return batch_source(shape_exprs, shape_sites, shapes, slot_type, sum_cols, sum_col_count, rows_per_thread);
+}
+
 /* ---- the shape catalog ---- */
 
 struct CqlBatchCatalog
@@ -606,7 +839,8 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
   cqlops_note_error("");
   if (query_count == 0) return 1;
   if (column_count == 0 || column_count > CQLOPS_MAX_BINDINGS) return refuse("1 to 10 columns");
-  if (rows_per_thread != 4 && rows_per_thread != 8 && rows_per_thread != 16) rows_per_thread = 8;
+  /* 0: the shared-memory tile form; 4, 8 or 16: the register form with that many rows per thread */
+  if (rows_per_thread != 0 && rows_per_thread != 4 && rows_per_thread != 8 && rows_per_thread != 16) rows_per_thread = 0;
   uint64_t rows = columns[0].rows;
   for (uint32_t c = 0; c < column_count; c++)
   {
@@ -716,10 +950,18 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     double m = fabs(col->zone_min) > fabs(col->zone_max) ? fabs(col->zone_min) : fabs(col->zone_max);
     int e = 0;
     if (m > 0.0) frexp(m, &e);   /* m < 2^e */
-    /* the rows one warp accumulates: its passes over the grid, 32 lanes x rows_per_thread each */
-    uint64_t groups = (rows + rows_per_thread - 1) / rows_per_thread;
-    uint64_t per_pass = (uint64_t)(sm_count ? sm_count : 152) * BATCH_CTAS_PER_SM * QE_GPU_WORKGROUP_SIZE;
-    uint64_t warp_rows = ((groups + per_pass - 1) / per_pass) * 32 * rows_per_thread;
+    /* the rows one accumulator takes: in the register form a warp's passes over the grid (32 lanes x
+       rows_per_thread each), in the tile form a CTA's tiles (at most one SM's share of the rows and two
+       tiles, whatever the CTAs per SM) */
+    uint64_t warp_rows;
+    if (rows_per_thread)
+    {
+      uint64_t groups = (rows + rows_per_thread - 1) / rows_per_thread;
+      uint64_t per_pass = (uint64_t)(sm_count ? sm_count : 152) * BATCH_CTAS_PER_SM * QE_GPU_WORKGROUP_SIZE;
+      warp_rows = ((groups + per_pass - 1) / per_pass) * 32 * rows_per_thread;
+    }
+    else
+      warp_rows = rows / (sm_count ? sm_count : 152) + 2048;
     int wr = 0;
     frexp((double)warp_rows, &wr);   /* warp_rows < 2^wr */
     col_scale[c] = ldexp(1.0, 62 - e - wr);
@@ -830,7 +1072,7 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     uint32_t nq = query_count < CQL_BATCH_LAUNCH_QUERIES ? query_count : CQL_BATCH_LAUNCH_QUERIES;
     uint32_t ns;
     SLICE_SHAPES(0, nq, ns);
-    char* src = batch_source(slice_exprs, slice_sites, ns, launch_types, sum_cols, sum_col_count, rows_per_thread);
+    char* src = launch_source(slice_exprs, slice_sites, ns, launch_types, sum_cols, sum_col_count, rows_per_thread);
     ok = src != NULL;
     if (ok && mode == BATCH_SOURCE)
     {
@@ -870,7 +1112,8 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     memcpy(params + off_qc, qc_o, (size_t)query_count * BATCH_MAX_CONSTS * 8);
     memcpy(params + off_qs, qs_o, (size_t)query_count * 4);
   }
-  uint64_t ctas = (uint64_t)(sm_count ? sm_count : 152) * BATCH_CTAS_PER_SM;
+  uint32_t per_sm = rows_per_thread ? BATCH_CTAS_PER_SM : tiled_layout(launch_types, sum_col_count).per_sm;
+  uint64_t ctas = (uint64_t)(sm_count ? sm_count : 152) * per_sm;
   uint32_t widest = query_count < CQL_BATCH_LAUNCH_QUERIES ? query_count : CQL_BATCH_LAUNCH_QUERIES;
   CqlBuffer* param_buf = launch && ok ? pooled("batch_params", param_bytes, CQLCUDA_BUFFER_WRITE) : NULL;
   CqlBuffer* out_buf = launch && ok ? pooled("batch_folded", (uint64_t)query_count * 24, CQLCUDA_BUFFER_READ_WRITE) : NULL;
@@ -894,7 +1137,7 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     CqlKernel* k = shared_k;
     if (!k)
     {
-      char* src = batch_source(slice_exprs, slice_sites, ns, launch_types, sum_cols, sum_col_count, rows_per_thread);
+      char* src = launch_source(slice_exprs, slice_sites, ns, launch_types, sum_cols, sum_col_count, rows_per_thread);
       if (!src)
       {
         ok = 0;

@@ -188,14 +188,17 @@ def run_batch(rows, reps):
     progs = [ops.Program(w, cols) for w, _ in qs]
     sums = [s for _, s in qs]
     best = None
-    for rpt in (4, 8, 16):
-        # the tuning knob: rows per thread of the generated kernel, the fastest kept
+    tuning = {}
+    for rpt in (0, 4, 8, 16):
+        # the tuning knob: the shared-memory tile form (0) or the register form with 4, 8 or 16 rows per
+        # thread; the fastest kept
         wall, kernel_ms, kernels = _time(lambda: ops.batch_aggregate(progs, sums, rpt), reps)
+        tuning["tile" if rpt == 0 else f"rows_per_thread_{rpt}"] = round(wall, 3)
         if best is None or wall < best[1]:
             best = (rpt, wall, kernel_ms, kernels)
     one_wall, one_kernel, _ = _time(lambda: [ops.fused_aggregate(p, [s]) for p, s in zip(progs, sums)], max(1, reps // 2))
     nbytes = rows * (4 * 4 + 4 * 8)
-    return {"op": "batch", "rows": rows, "queries": len(qs), "shapes": 29, "reps": reps, "rows_per_thread": best[0],
+    return {"op": "batch", "rows": rows, "queries": len(qs), "shapes": 29, "reps": reps, "rows_per_thread": best[0], "tuning_wall_ms": tuning,
             "wall_ms": best[1], "kernel_ms": best[2], "rows_per_s": len(qs) * rows / (best[1] / 1e3),
             "kernel_GBps": nbytes / (best[2] / 1e3) / 1e9, "bytes": nbytes, "kernels": best[3],
             "one_at_a_time_wall_ms": one_wall, "one_at_a_time_kernel_ms": one_kernel, "speedup_wall": one_wall / best[1]}

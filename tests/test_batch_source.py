@@ -18,7 +18,7 @@ def columns(ops, rows=1000):
     return cols
 
 
-@pytest.mark.parametrize("rows_per_thread", [4, 8, 16])
+@pytest.mark.parametrize("rows_per_thread", [0, 4, 8, 16])
 def test_source_compiles(ops, rows_per_thread):
     cols = columns(ops)
     qs = queries(120, 29, 3)
@@ -46,3 +46,18 @@ def test_strings_are_refused(ops):
     progs = [ops.Program("(= s 'x')", cols)]
     with pytest.raises(ops.OpError):
         ops.batch_source(progs, [None])
+
+
+def test_tile_form_sizes_its_shared_memory(ops):
+    """The tile form stages 1024 rows when they fit in 72 KB with the accumulators, else 512, and asks for
+    as many CTAs per SM as 227 KB holds (at most 8)."""
+    cols = columns(ops)
+    qs = queries(64, 8, 5)
+    progs = [ops.Program(w, cols) for w, _ in qs]
+    src, _ = ops.batch_source(progs, [s for _, s in qs], 0)
+    head = src.splitlines()[0]
+    assert head.startswith("// cql: block=256 smem=")
+    smem = int(head.split("smem=")[1].split()[0])
+    per_sm = int(head.split("per_sm=")[1].split()[0])
+    assert "const u32 TILE = 512u" in src or "const u32 TILE = 1024u" in src
+    assert smem <= 227 * 1024 and 1 <= per_sm <= 8 and per_sm * (smem + 1024) <= 227 * 1024

@@ -39,7 +39,7 @@ def _check(ops, arrays, cols, qs, rows_per_thread=8):
     return shapes
 
 
-@pytest.mark.parametrize("rows_per_thread", [4, 8, 16])
+@pytest.mark.parametrize("rows_per_thread", [0, 4, 8, 16])
 def test_batch_matches_each_query_alone(ops, rows_per_thread):
     arrays = table(2_000_003, 1)
     cols = _columns(ops, arrays)
@@ -48,14 +48,16 @@ def test_batch_matches_each_query_alone(ops, rows_per_thread):
     assert shapes <= 8
 
 
-def test_more_queries_than_one_launch_holds(ops):
+@pytest.mark.parametrize("rows_per_thread", [0, 8])
+def test_more_queries_than_one_launch_holds(ops, rows_per_thread):
     arrays = table(300_001, 2)
     cols = _columns(ops, arrays)
     qs = queries(500, 29, 11)
-    assert _check(ops, arrays, cols, qs) <= 29
+    assert _check(ops, arrays, cols, qs, rows_per_thread) <= 29
 
 
-def test_count_only_and_special_values(ops):
+@pytest.mark.parametrize("rows_per_thread", [0, 8])
+def test_count_only_and_special_values(ops, rows_per_thread):
     rng = np.random.default_rng(5)
     n = 100_000
     arrays = table(n, 3)
@@ -72,7 +74,7 @@ def test_count_only_and_special_values(ops):
           ("(<= d0 0.0)", None), ("(< d0 1e308)", None), ("(> d0 -1e308)", None), ("(and (> d0 0.25) (< d0 0.5))", "d1"),
           ("(or (= u0 7) (< u1 100))", "d2"), ("(and (>= u2 65535) (<= u2 65535))", None), ("(< u3 0)", None)]
     progs = [ops.Program(w, cols) for w, _ in qs]
-    counts, sums, _ = ops.batch_aggregate(progs, [s for _, s in qs])
+    counts, sums, _ = ops.batch_aggregate(progs, [s for _, s in qs], rows_per_thread)
     for i, (w, s) in enumerate(qs):
         m = oracle_mask(progs[i], arrays).astype(bool)
         assert counts[i] == m.sum(), w
@@ -81,7 +83,8 @@ def test_count_only_and_special_values(ops):
             assert abs(sums[i] - exact) <= 1e-12 * abs(exact)
 
 
-def test_signed_and_float_columns(ops):
+@pytest.mark.parametrize("rows_per_thread", [0, 8])
+def test_signed_and_float_columns(ops, rows_per_thread):
     rng = np.random.default_rng(8)
     n = 500_000
     arrays = {"i": rng.integers(-1000, 1000, n).astype(np.int32), "f": rng.normal(size=n).astype(np.float32),
@@ -90,10 +93,25 @@ def test_signed_and_float_columns(ops):
     qs = [("(< i -10)", "v"), ("(>= i 999)", "v"), ("(and (> f 0.5) (< i 0))", "v"), ("(<= f -1.25)", "i"),
           ("(or (= i 0) (> f 2.5))", "f"), ("(< f 0.1)", None)]
     progs = [ops.Program(w, cols) for w, _ in qs]
-    counts, sums, _ = ops.batch_aggregate(progs, [s for _, s in qs])
+    counts, sums, _ = ops.batch_aggregate(progs, [s for _, s in qs], rows_per_thread)
     for i, (w, s) in enumerate(qs):
         m = oracle_mask(progs[i], arrays).astype(bool)
         assert counts[i] == m.sum(), w
         if s:
             exact = math.fsum(arrays[s][m].astype(np.float64))
             assert abs(sums[i] - exact) <= 1e-12 * abs(exact), w
+
+
+def test_tile_and_register_forms_agree(ops):
+    """The two kernel forms give identical counts; their sums differ only by the rounding of each row's
+    summand at the scale each form chooses, far inside 1e-12."""
+    arrays = table(50_000, 4)
+    cols = _columns(ops, arrays)
+    qs = queries(96, 12, 21)
+    progs = [ops.Program(w, cols) for w, _ in qs]
+    c0, s0, _ = ops.batch_aggregate(progs, [s for _, s in qs], 0)
+    c8, s8, _ = ops.batch_aggregate(progs, [s for _, s in qs], 8)
+    assert np.array_equal(c0, c8)
+    for i, (w, scol) in enumerate(qs):
+        if scol:
+            assert abs(s0[i] - s8[i]) <= 1e-12 * max(abs(s8[i]), 1e-300), w
