@@ -263,44 +263,39 @@ static int note_cuda(cudaError_t e, const char* what)
 }
 
 // Bounded wait on a stream: polls until done or the wait limit, never blocks forever.
-static int wait_stream(cudaStream_t stream, const char* what)
+// Waits poll without sleeping for the first CQL_SPIN_US microseconds, so that a result is seen within a
+// microsecond or two of the GPU finishing (a sleep on Linux overshoots by tens of microseconds, which
+// short queries would pay at every wait); longer waits poll every 20 us and give the core back. Both end
+// with an error after the wait timeout instead of blocking for ever.
+#define CQL_SPIN_US 20000
+
+template <typename Query>
+static int wait_polled(Query done, const char* what)
 {
   auto t0 = std::chrono::steady_clock::now();
-  uint64_t spins = 0;
   for (;;)
   {
-    cudaError_t e = cudaStreamQuery(stream);
+    cudaError_t e = done();
     if (e == cudaSuccess) return 1;
     if (e != cudaErrorNotReady) return note_cuda(e, what);
-    auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
-    if ((uint64_t)ms > S().wait_timeout_ms)
+    auto us = std::chrono::duration_cast<std::chrono::microseconds>(std::chrono::steady_clock::now() - t0).count();
+    if ((uint64_t)us > (uint64_t)S().wait_timeout_ms * 1000ull)
     {
       set_error("%s: GPU work did not complete within %u ms", what, S().wait_timeout_ms);
       return 0;
     }
-    spins += 1;
-    if (spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(20));
+    if (us > CQL_SPIN_US) std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
+}
+
+static int wait_stream(cudaStream_t stream, const char* what)
+{
+  return wait_polled([stream]() { return cudaStreamQuery(stream); }, what);
 }
 
 static int wait_event(cudaEvent_t ev, const char* what)
 {
-  auto t0 = std::chrono::steady_clock::now();
-  uint64_t spins = 0;
-  for (;;)
-  {
-    cudaError_t e = cudaEventQuery(ev);
-    if (e == cudaSuccess) return 1;
-    if (e != cudaErrorNotReady) return note_cuda(e, what);
-    auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
-    if ((uint64_t)ms > S().wait_timeout_ms)
-    {
-      set_error("%s: GPU work did not complete within %u ms", what, S().wait_timeout_ms);
-      return 0;
-    }
-    spins += 1;
-    if (spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(20));
-  }
+  return wait_polled([ev]() { return cudaEventQuery(ev); }, what);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -317,6 +312,34 @@ static uint32_t profile_slot(const std::string& name)
   return idx;
 }
 
+// Timing events are reused: creating and destroying two events per dispatch would cost the profiled
+// run microseconds per kernel.
+static std::mutex g_event_pool_lock;
+static std::vector<cudaEvent_t> g_event_pool;
+
+static cudaEvent_t timing_event_get()
+{
+  {
+    std::lock_guard<std::mutex> g(g_event_pool_lock);
+    if (!g_event_pool.empty())
+    {
+      cudaEvent_t e = g_event_pool.back();
+      g_event_pool.pop_back();
+      return e;
+    }
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+static void timing_event_put(cudaEvent_t e)
+{
+  if (!e) return;
+  std::lock_guard<std::mutex> g(g_event_pool_lock);
+  g_event_pool.push_back(e);
+}
+
 static void timings_collect(std::vector<CqlTiming>& timings)
 {
   CqlState& s = S();
@@ -330,8 +353,8 @@ static void timings_collect(std::vector<CqlTiming>& timings)
       s.profile[t.profile_index].dispatches += 1;
       s.last_kernel_us = (uint64_t)((double)ms * 1e3);
     }
-    cudaEventDestroy(t.start);
-    cudaEventDestroy(t.stop);
+    timing_event_put(t.start);
+    timing_event_put(t.stop);
   }
   timings.clear();
 }
@@ -1010,8 +1033,8 @@ static int dispatch(CqlKernel* k, uint32_t gws, uint32_t lws, cudaStream_t strea
   if (timed)
   {
     t.profile_index = k->profile_index;
-    cudaEventCreate(&t.start);
-    cudaEventCreate(&t.stop);
+    t.start = timing_event_get();
+    t.stop = timing_event_get();
     cudaEventRecord(t.start, stream);
   }
   int rc = 0;
@@ -1182,17 +1205,19 @@ __global__ void k_fill_u32(uint32_t* p, uint64_t words, uint32_t value)
   for (; i < words; i += stride) p[i] = value;
 }
 
-static int fill_words(CqlBuffer* buffer, uint64_t size, uint32_t value, cudaStream_t stream)
+static int fill_words(CqlBuffer* buffer, uint64_t offset, uint64_t size, uint32_t value, cudaStream_t stream)
 {
-  uint64_t bytes = std::min(size, buffer->size);
+  if (offset > buffer->size || (offset & 3)) return 0;
+  uint64_t bytes = std::min(size, buffer->size - offset);
+  char* at = (char*)buffer->dptr + offset;
   if (value == 0 || value == 0xffffffffu || ((value & 0xff) * 0x01010101u) == value)
   {
-    return note_cuda(cudaMemsetAsync(buffer->dptr, (int)(value & 0xff), bytes, stream), "fill");
+    return note_cuda(cudaMemsetAsync(at, (int)(value & 0xff), bytes, stream), "fill");
   }
   uint64_t words = bytes / 4;
   if (words == 0) return 1;
   uint32_t grid = cql_stream_grid((words + 255) / 256, 8);
-  k_fill_u32<<<grid, 256, 0, stream>>>((uint32_t*)buffer->dptr, words, value);
+  k_fill_u32<<<grid, 256, 0, stream>>>((uint32_t*)at, words, value);
   cql_note_launch();
   return note_cuda(cudaGetLastError(), "fill");
 }
@@ -1200,7 +1225,17 @@ static int fill_words(CqlBuffer* buffer, uint64_t size, uint32_t value, cudaStre
 extern "C" void cqlcuda_batch_buffer_fill(CqlBatch* batch, CqlBuffer* buffer, uint64_t size, uint32_t value)
 {
   if (!batch || !buffer) return;
-  if (!fill_words(buffer, size, value, L().stream)) batch->failed = 1;
+  if (!fill_words(buffer, 0, size, value, L().stream)) batch->failed = 1;
+}
+
+extern "C" void cqlcuda_batch_fill_range(CqlBatch* batch, CqlBuffer* buffer, uint64_t offset, uint64_t size, uint32_t value)
+{
+  if (!batch || !buffer) return;
+  if (!fill_words(buffer, offset, size, value, L().stream))
+  {
+    set_error("cqlcuda_batch_fill_range: offset %llu of a %llu byte buffer", (unsigned long long)offset, (unsigned long long)buffer->size);
+    batch->failed = 1;
+  }
 }
 
 extern "C" void cqlcuda_batch_kernel_execute(CqlBatch* batch, CqlKernel* kernel, uint32_t gws, uint32_t lws)
@@ -1246,8 +1281,8 @@ extern "C" int cqlcuda_batch_end(CqlBatch* batch)
   {
     for (auto& t : l.timings)
     {
-      cudaEventDestroy(t.start);
-      cudaEventDestroy(t.stop);
+      timing_event_put(t.start);
+      timing_event_put(t.stop);
     }
     l.timings.clear();
   }
@@ -1309,8 +1344,8 @@ extern "C" void cqlcuda_stream_release(CqlStream* st)
     wait_stream(sl.stream, "stream_release");
     for (auto& t : sl.timings)
     {
-      cudaEventDestroy(t.start);
-      cudaEventDestroy(t.stop);
+      timing_event_put(t.start);
+      timing_event_put(t.stop);
     }
     cudaStreamDestroy(sl.stream);
     cudaEventDestroy(sl.done);
@@ -1363,7 +1398,7 @@ extern "C" void cqlcuda_stream_zero(CqlStream* st, uint32_t slot, CqlBuffer* b, 
 extern "C" void cqlcuda_stream_fill(CqlStream* st, uint32_t slot, CqlBuffer* b, uint64_t size, uint32_t value)
 {
   if (!st || slot >= st->slot_count || !b) return;
-  if (!fill_words(b, size, value, st->slots[slot].stream)) st->slots[slot].failed = 1;
+  if (!fill_words(b, 0, size, value, st->slots[slot].stream)) st->slots[slot].failed = 1;
 }
 
 extern "C" void cqlcuda_stream_dispatch(CqlStream* st, uint32_t slot, CqlKernel* k, uint32_t gws, uint32_t lws)

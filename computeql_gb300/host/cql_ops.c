@@ -545,15 +545,19 @@ int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count,
   uint64_t info_bytes = group_count * 2 * sizeof(uint32_t);
   uint64_t sum_bytes = group_count * expr_count * 2 * sizeof(uint32_t);
   uint64_t mm_bytes = group_count * expr_count * sizeof(uint32_t);
-  CqlBuffer* info_buf = pooled("cqlops_dense_info", info_bytes, CQLCUDA_BUFFER_READ_WRITE);
-  CqlBuffer* sum_buf = pooled("cqlops_dense_sums", sum_bytes, CQLCUDA_BUFFER_READ_WRITE);
-  CqlBuffer* min_buf = pooled("cqlops_dense_mins", mm_bytes, CQLCUDA_BUFFER_READ_WRITE);
-  CqlBuffer* max_buf = pooled("cqlops_dense_maxs", mm_bytes, CQLCUDA_BUFFER_READ_WRITE);
-  uint32_t* info = (uint32_t*)malloc(info_bytes);
-  uint32_t* sums = (uint32_t*)malloc(sum_bytes);
-  uint32_t* mins = (uint32_t*)malloc(mm_bytes);
-  uint32_t* maxs = (uint32_t*)malloc(mm_bytes);
-  int ok = info_buf && sum_buf && min_buf && max_buf && info && sums && mins && maxs;
+  /* the four outputs in one buffer (info, sums, then MIN and MAX words, each part 16-byte aligned), bound
+     as four ranges: one clear and one read-back for the counts and sums */
+  uint64_t sum_at = (info_bytes + 15) & ~15ull;
+  uint64_t min_at = (sum_at + sum_bytes + 15) & ~15ull;
+  uint64_t max_at = (min_at + mm_bytes + 15) & ~15ull;
+  uint64_t out_bytes = max_at + mm_bytes;
+  CqlBuffer* out_buf = pooled("cqlops_dense_out", out_bytes, CQLCUDA_BUFFER_READ_WRITE);
+  unsigned char* host_out = (unsigned char*)malloc(out_bytes);
+  uint32_t* info = (uint32_t*)host_out;
+  uint32_t* sums = host_out ? (uint32_t*)(host_out + sum_at) : NULL;
+  uint32_t* mins = host_out ? (uint32_t*)(host_out + min_at) : NULL;
+  uint32_t* maxs = host_out ? (uint32_t*)(host_out + max_at) : NULL;
+  int ok = out_buf && host_out;
   if (ok)
   {
     cqlcuda_kernel_set_arg_buffer(k, 0, key->buffer);
@@ -562,10 +566,10 @@ int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count,
       const CqlColumn* col = b < arg_count ? arg_columns[b] : key;
       cqlcuda_kernel_set_arg_buffer(k, 1 + b, col->buffer ? col->buffer : key->buffer);
     }
-    cqlcuda_kernel_set_arg_buffer(k, 5, info_buf);
-    cqlcuda_kernel_set_arg_buffer(k, 6, sum_buf);
-    cqlcuda_kernel_set_arg_buffer(k, 7, min_buf);
-    cqlcuda_kernel_set_arg_buffer(k, 8, max_buf);
+    cqlcuda_kernel_set_arg_buffer_range(k, 5, out_buf, 0, info_bytes);
+    cqlcuda_kernel_set_arg_buffer_range(k, 6, out_buf, sum_at, sum_bytes);
+    cqlcuda_kernel_set_arg_buffer_range(k, 7, out_buf, min_at, mm_bytes);
+    cqlcuda_kernel_set_arg_buffer_range(k, 8, out_buf, max_at, mm_bytes);
     cqlcuda_kernel_set_arg_u64(k, 0, rows | (shader_widths << 32));
     cqlcuda_kernel_set_arg_u64(k, 1, (uint64_t)expr_count | ((uint64_t)arg_bases[0] << 32));
     cqlcuda_kernel_set_arg_u64(k, 2, (uint64_t)func_codes | ((uint64_t)arg_bases[1] << 32));
@@ -574,17 +578,27 @@ int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count,
     cqlcuda_kernel_set_arg_u64(k, 5, (uint64_t)(uint32_t)(int32_t)min_key | ((uint64_t)arg_bases[3] << 32));
     cqlcuda_kernel_set_arg_u64(k, 6, tile_groups | (slice_rows << 32));
     cqlcuda_kernel_set_arg_u64(k, 7, tile_count);
-    CqlBatch* batch = cqlcuda_batch_begin(0, info_bytes + sum_bytes + 2 * mm_bytes);
-    cqlcuda_batch_buffer_fill(batch, info_buf, info_bytes, 0);
-    cqlcuda_batch_buffer_fill(batch, sum_buf, sum_bytes, 0);
-    cqlcuda_batch_buffer_fill(batch, min_buf, mm_bytes, 0x7fffffffu);
-    cqlcuda_batch_buffer_fill(batch, max_buf, mm_bytes, 0x80000000u);
+    /* the kernel touches the MIN/MAX arrays only for MIN/MAX expressions: without any, their initial
+       values are the results and neither array crosses the bus */
+    uint64_t counted = has_min_max ? out_bytes : min_at;
+    CqlBatch* batch = cqlcuda_batch_begin(0, counted);
+    cqlcuda_batch_buffer_zero(batch, out_buf, min_at);
+    if (has_min_max)
+    {
+      cqlcuda_batch_fill_range(batch, out_buf, min_at, mm_bytes, 0x7fffffffu);
+      cqlcuda_batch_fill_range(batch, out_buf, max_at, mm_bytes, 0x80000000u);
+    }
     uint64_t workgroups = (rows + slice_rows - 1) / slice_rows;
     cqlcuda_batch_kernel_execute(batch, k, (uint32_t)(workgroups * QE_GPU_WORKGROUP_SIZE), QE_GPU_WORKGROUP_SIZE);
-    cqlcuda_batch_buffer_read(batch, info_buf, info, info_bytes);
-    cqlcuda_batch_buffer_read(batch, sum_buf, sums, sum_bytes);
-    cqlcuda_batch_buffer_read(batch, min_buf, mins, mm_bytes);
-    cqlcuda_batch_buffer_read(batch, max_buf, maxs, mm_bytes);
+    cqlcuda_batch_buffer_read(batch, out_buf, host_out, counted);
+    if (!has_min_max)
+    {
+      for (uint64_t i = 0; i < group_count * expr_count; i++)
+      {
+        mins[i] = 0x7fffffffu;
+        maxs[i] = 0x80000000u;
+      }
+    }
     ok = cqlcuda_batch_end(batch);
   }
   if (ok)
@@ -604,9 +618,6 @@ int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count,
     *out_group_count = group_count;
     *out_min_key = min_key;
   }
-  free(info);
-  free(sums);
-  free(mins);
-  free(maxs);
+  free(host_out);
   return ok;
 }

@@ -323,39 +323,15 @@ static int probe_totals(const CqlJoinAgg* q, uint32_t core_count, const uint32_t
   return ok;
 }
 
-/* the visit pre-pass: one slice of dim rows per task, the kept ones written at the slice's start */
-#define VISIT_SLICE 32768u
+/* ---- the dim-row pass: groups of the kept dim rows and their accumulators ---- */
+
+/* one aggregate of one group */
 typedef struct
 {
-  const CqlJoinAgg* q;
-  int signed_key, by_dim_row;
-  int64_t min_key;
-  uint64_t total_groups;
-  const uint64_t* counts;
-  uint64_t visits;
-  uint32_t tasks;
-  uint32_t* cand;
-  uint64_t* found;
-} VisitCtx;
-
-static void visit_task(void* p, uint32_t task)
-{
-  VisitCtx* c = (VisitCtx*)p;
-  uint64_t v0 = (uint64_t)task * VISIT_SLICE;
-  uint64_t v1 = v0 + VISIT_SLICE < c->visits ? v0 + VISIT_SLICE : c->visits;
-  uint32_t* out = c->cand + v0;
-  uint64_t n = 0;
-  for (uint64_t v = v0; v < v1; v++)
-  {
-    uint64_t dim_row = c->q->dim_rows ? c->q->dim_rows[v] : v;
-    uint32_t kw = c->q->dim_keys[dim_row];
-    int64_t key_value = c->signed_key ? (int64_t)(int32_t)kw : (int64_t)kw;
-    uint64_t id = c->by_dim_row ? dim_row : (uint64_t)(key_value - c->min_key);
-    out[n] = (uint32_t)dim_row;
-    n += id < c->total_groups && c->counts[id < c->total_groups ? id : 0] != 0;
-  }
-  c->found[task] = n;
-}
+  uint64_t count;
+  double sum, mn, mx;
+  int seen;
+} JoinAcc;
 
 /* FNV-style hash of a dim row's group values (their f64 bits) */
 static uint64_t group_hash(const CqlJoinAgg* q, uint64_t dim_row)
@@ -369,6 +345,181 @@ static uint64_t group_hash(const CqlJoinAgg* q, uint64_t dim_row)
     h ^= h >> 29;
   }
   return h;
+}
+
+/* two dim rows are in one group when every group value compares equal */
+static int same_group(const CqlJoinAgg* q, uint64_t a, uint64_t b)
+{
+  for (uint32_t c = 0; c < q->group_count; c++)
+    if (!(q->dim_group_values[c][a] == q->dim_group_values[c][b])) return 0;
+  return 1;
+}
+
+/* groups in the order their first dim row was met, found through an open-addressing table of
+   (group + 1), each with expr_count accumulators */
+typedef struct
+{
+  uint32_t* slots;
+  uint64_t cap, groups, acc_cap;
+  uint64_t* rep;
+  JoinAcc* acc;
+  uint32_t exprs;
+} GroupTable;
+
+static int gt_init(GroupTable* t, uint32_t exprs)
+{
+  t->cap = 64;
+  t->acc_cap = 16;
+  t->groups = 0;
+  t->exprs = exprs;
+  t->slots = (uint32_t*)calloc(t->cap, 4);
+  t->rep = (uint64_t*)malloc(t->acc_cap * 8);
+  t->acc = (JoinAcc*)calloc(t->acc_cap * exprs, sizeof(JoinAcc));
+  return t->slots && t->rep && t->acc;
+}
+
+static void gt_free(GroupTable* t)
+{
+  free(t->slots);
+  free(t->rep);
+  free(t->acc);
+  t->slots = NULL;
+  t->rep = NULL;
+  t->acc = NULL;
+}
+
+/* the group of dim_row, a new one when none matches; -1 when memory runs out */
+static int64_t gt_find(GroupTable* t, const CqlJoinAgg* q, uint64_t dim_row)
+{
+  uint64_t pos = 0;
+  if (q->group_count == 0)
+  {
+    if (t->groups) return 0;
+  }
+  else
+  {
+    pos = group_hash(q, dim_row) & (t->cap - 1);
+    for (;;)
+    {
+      uint32_t stored = t->slots[pos];
+      if (!stored) break;
+      if (same_group(q, t->rep[stored - 1], dim_row)) return stored - 1;
+      pos = (pos + 1) & (t->cap - 1);
+    }
+  }
+  if (t->groups == t->acc_cap)
+  {
+    JoinAcc* a2 = (JoinAcc*)realloc(t->acc, t->acc_cap * 2 * t->exprs * sizeof(JoinAcc));
+    if (a2) t->acc = a2;
+    uint64_t* r2 = a2 ? (uint64_t*)realloc(t->rep, t->acc_cap * 2 * 8) : NULL;
+    if (r2) t->rep = r2;
+    if (!a2 || !r2) return -1;
+    memset(t->acc + t->acc_cap * t->exprs, 0, t->acc_cap * t->exprs * sizeof(JoinAcc));
+    t->acc_cap *= 2;
+  }
+  uint64_t g = t->groups++;
+  t->rep[g] = dim_row;
+  if (q->group_count == 0) return 0;
+  if (t->groups * 2 > t->cap)
+  {
+    uint32_t* s2 = (uint32_t*)calloc(t->cap * 2, 4);
+    if (!s2) return -1;
+    free(t->slots);
+    t->slots = s2;
+    t->cap *= 2;
+    for (uint64_t gg = 0; gg < t->groups; gg++)
+    {
+      uint64_t p2 = group_hash(q, t->rep[gg]) & (t->cap - 1);
+      while (t->slots[p2]) p2 = (p2 + 1) & (t->cap - 1);
+      t->slots[p2] = (uint32_t)gg + 1;
+    }
+  }
+  else
+    t->slots[pos] = (uint32_t)g + 1;
+  return (int64_t)g;
+}
+
+/* one slice of dim rows per task: its kept rows grouped and accumulated in dim-row order; the slices'
+   groups are merged afterwards in slice order, so groups keep the order of their first dim row */
+#define VISIT_SLICE 32768u
+typedef struct
+{
+  const CqlJoinAgg* q;
+  int signed_key, by_dim_row;
+  int64_t min_key;
+  uint64_t total_groups;
+  const uint64_t* counts;
+  const int64_t* sums;
+  const int64_t* mins;
+  const int64_t* maxs;
+  uint32_t core_count;
+  const uint32_t* core_of_expr;
+  uint64_t visits;
+  uint32_t tasks;
+  GroupTable* slices;
+  int* failed;
+} VisitCtx;
+
+/* a kept dim row's contribution: its key's totals, or its own value times the key's matches */
+static void accumulate(const VisitCtx* c, JoinAcc* a, uint64_t dim_row, uint64_t id)
+{
+  const CqlJoinAgg* q = c->q;
+  uint64_t matches = c->counts[id];
+  for (uint32_t e = 0; e < q->expr_count; e++)
+  {
+    JoinAcc* x = &a[e];
+    x->count += matches;
+    uint32_t f = q->funcs[e];
+    if (f == CQLOPS_FUNC_COUNT) continue;
+    double value_sum, value_min, value_max;
+    if (q->dim_args && q->dim_args[e])
+    {
+      double value = q->dim_args[e][dim_row];
+      value_sum = value * (double)matches;
+      value_min = value_max = value;
+    }
+    else
+    {
+      uint64_t slot = id * c->core_count + c->core_of_expr[e];
+      value_sum = (double)c->sums[slot];
+      value_min = (double)c->mins[slot];
+      value_max = (double)c->maxs[slot];
+    }
+    x->sum += value_sum;
+    x->mn = x->seen ? (value_min < x->mn ? value_min : x->mn) : value_min;
+    x->mx = x->seen ? (value_max > x->mx ? value_max : x->mx) : value_max;
+    x->seen = 1;
+  }
+}
+
+static void visit_task(void* p, uint32_t task)
+{
+  VisitCtx* c = (VisitCtx*)p;
+  GroupTable* t = &c->slices[task];
+  if (!gt_init(t, c->q->expr_count))
+  {
+    c->failed[task] = 1;
+    return;
+  }
+  uint64_t v0 = (uint64_t)task * VISIT_SLICE;
+  uint64_t v1 = v0 + VISIT_SLICE < c->visits ? v0 + VISIT_SLICE : c->visits;
+  const uint64_t* dim_rows = c->q->dim_rows;
+  const uint32_t* dim_keys = c->q->dim_keys;
+  for (uint64_t v = v0; v < v1; v++)
+  {
+    uint64_t dim_row = dim_rows ? dim_rows[v] : v;
+    uint32_t kw = dim_keys[dim_row];
+    int64_t key_value = c->signed_key ? (int64_t)(int32_t)kw : (int64_t)kw;
+    uint64_t id = c->by_dim_row ? dim_row : (uint64_t)(key_value - c->min_key);
+    if (id >= c->total_groups || c->counts[id] == 0) continue;
+    int64_t g = gt_find(t, c->q, dim_row);
+    if (g < 0)
+    {
+      c->failed[task] = 1;
+      return;
+    }
+    accumulate(c, &t->acc[(uint64_t)g * t->exprs], dim_row, id);
+  }
 }
 
 int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* out_groups, uint64_t* out_group_dim_row, double* out_results,
@@ -456,132 +607,54 @@ int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* ou
   /* each (filtered) dim row meets its key's totals and joins the group of its group values (:8619-8720);
      the group tables start small and grow with the groups found */
   uint64_t visits = q->dim_rows ? q->dim_count : q->dim_table_rows;
-  uint64_t cap = 1024, acc_cap = 256;
-  typedef struct
-  {
-    uint64_t count;
-    double sum, mn, mx;
-    int seen;
-  } Acc;
-  uint32_t* slots = (uint32_t*)calloc(cap, 4);
-  Acc* acc = (Acc*)calloc(acc_cap * q->expr_count, sizeof(Acc));
-  uint64_t* rep = (uint64_t*)malloc(acc_cap * 8);
-  uint64_t groups = 0;
-  ok = slots && acc && rep;
   int signed_key = fk->type == CQLOPS_TYPE_I32;
-  /* the dim rows whose key falls inside the totals, found in parallel slices and kept in dim-row order */
-  VisitCtx vc = { q, signed_key, by_dim_row, min_key, total_groups, counts, visits, 0, NULL, NULL };
+  VisitCtx vc = { q, signed_key, by_dim_row, min_key, total_groups, counts, sums, mins, maxs, core_count, core_of_expr, visits, 0, NULL, NULL };
   vc.tasks = (uint32_t)((visits + VISIT_SLICE - 1) / VISIT_SLICE);
-  vc.cand = (uint32_t*)malloc((visits ? visits : 1) * sizeof(uint32_t));
-  vc.found = (uint64_t*)malloc((vc.tasks ? vc.tasks : 1) * sizeof(uint64_t));
-  ok = ok && vc.cand && vc.found;
+  vc.slices = (GroupTable*)calloc(vc.tasks ? vc.tasks : 1, sizeof(GroupTable));
+  vc.failed = (int*)calloc(vc.tasks ? vc.tasks : 1, sizeof(int));
+  GroupTable all;
+  memset(&all, 0, sizeof(all));
+  ok = vc.slices && vc.failed && gt_init(&all, q->expr_count);
   if (ok) cql_parallel_for(vc.tasks, visit_task, &vc);
+  /* the slices' groups in slice order: a group's first dim row decides its place */
   for (uint32_t task = 0; ok && task < vc.tasks; task++)
   {
-    const uint32_t* cand = vc.cand + (uint64_t)task * VISIT_SLICE;
-    uint64_t nc = vc.found[task];
-    for (uint64_t ci = 0; ok && ci < nc; ci++)
+    const GroupTable* t = &vc.slices[task];
+    if (vc.failed[task])
     {
-      uint64_t dim_row = cand[ci];
-      uint32_t kw = q->dim_keys[dim_row];
-      int64_t key_value = signed_key ? (int64_t)(int32_t)kw : (int64_t)kw;
-      uint64_t id = by_dim_row ? dim_row : (uint64_t)(key_value - min_key);
-      uint64_t g = 0;
-      if (q->group_count == 0)
+      ok = 0;
+      break;
+    }
+    for (uint64_t lg = 0; ok && lg < t->groups; lg++)
+    {
+      int64_t g = gt_find(&all, q, t->rep[lg]);
+      if (g < 0)
       {
-        if (groups == 0)
-        {
-          groups = 1;
-          rep[0] = dim_row;
-        }
+        ok = 0;
+        break;
       }
-      else
-      {
-        uint64_t pos = group_hash(q, dim_row) & (cap - 1);
-        for (;;)
-        {
-          uint32_t stored = slots[pos];
-          if (stored == 0)
-          {
-            if (groups == acc_cap)
-            {
-              Acc* a2 = (Acc*)realloc(acc, acc_cap * 2 * q->expr_count * sizeof(Acc));
-              uint64_t* r2 = (uint64_t*)realloc(rep, acc_cap * 2 * 8);
-              if (a2) acc = a2;
-              if (r2) rep = r2;
-              if (!a2 || !r2)
-              {
-                ok = 0;
-                break;
-              }
-              memset(acc + acc_cap * q->expr_count, 0, acc_cap * q->expr_count * sizeof(Acc));
-              acc_cap *= 2;
-            }
-            g = groups++;
-            rep[g] = dim_row;
-            if (groups * 2 > cap)
-            {
-              /* rehash into twice the slots */
-              uint32_t* s2 = (uint32_t*)calloc(cap * 2, 4);
-              if (!s2)
-              {
-                ok = 0;
-                break;
-              }
-              free(slots);
-              slots = s2;
-              cap *= 2;
-              for (uint64_t gg = 0; gg < groups; gg++)
-              {
-                uint64_t p2 = group_hash(q, rep[gg]) & (cap - 1);
-                while (slots[p2]) p2 = (p2 + 1) & (cap - 1);
-                slots[p2] = (uint32_t)gg + 1;
-              }
-            }
-            else
-              slots[pos] = (uint32_t)g + 1;
-            break;
-          }
-          uint64_t other = rep[stored - 1];
-          int same = 1;
-          for (uint32_t c = 0; c < q->group_count && same; c++) same = q->dim_group_values[c][other] == q->dim_group_values[c][dim_row];
-          if (same)
-          {
-            g = stored - 1;
-            break;
-          }
-          pos = (pos + 1) & (cap - 1);
-        }
-        if (!ok) break;
-      }
-      uint64_t matches = counts[id];
       for (uint32_t e = 0; e < q->expr_count; e++)
       {
-        Acc* a = &acc[g * q->expr_count + e];
-        a->count += matches;
-        uint32_t f = q->funcs[e];
-        if (f == CQLOPS_FUNC_COUNT) continue;
-        double value_sum, value_min, value_max;
-        if (q->dim_args && q->dim_args[e])
+        JoinAcc* x = &all.acc[(uint64_t)g * q->expr_count + e];
+        const JoinAcc* y = &t->acc[lg * q->expr_count + e];
+        x->count += y->count;
+        x->sum += y->sum;
+        if (y->seen)
         {
-          double value = q->dim_args[e][dim_row];
-          value_sum = value * (double)matches;
-          value_min = value_max = value;
+          x->mn = x->seen ? (y->mn < x->mn ? y->mn : x->mn) : y->mn;
+          x->mx = x->seen ? (y->mx > x->mx ? y->mx : x->mx) : y->mx;
+          x->seen = 1;
         }
-        else
-        {
-          uint64_t slot = (uint64_t)id * core_count + core_of_expr[e];
-          value_sum = (double)sums[slot];
-          value_min = (double)mins[slot];
-          value_max = (double)maxs[slot];
-        }
-        a->sum += value_sum;
-        a->mn = a->seen ? (value_min < a->mn ? value_min : a->mn) : value_min;
-        a->mx = a->seen ? (value_max > a->mx ? value_max : a->mx) : value_max;
-        a->seen = 1;
       }
     }
   }
+  if (vc.slices)
+    for (uint32_t task = 0; task < vc.tasks; task++) gt_free(&vc.slices[task]);
+  free(vc.slices);
+  free(vc.failed);
+  uint64_t groups = ok ? all.groups : 0;
+  uint64_t* rep = all.rep;
+  JoinAcc* acc = all.acc;
   if (ok && groups > max_groups) ok = refuse("more groups than the output arrays hold");
   if (ok)
   {
@@ -590,7 +663,7 @@ int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* ou
       out_group_dim_row[g] = rep[g];
       for (uint32_t e = 0; e < q->expr_count; e++)
       {
-        Acc* a = &acc[g * q->expr_count + e];
+        JoinAcc* a = &acc[g * q->expr_count + e];
         double r;
         switch (q->funcs[e])
         {
@@ -606,11 +679,7 @@ int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* ou
     *out_groups = groups;
     if (out_strategy) *out_strategy = by_dim_row ? 2u : 1u;
   }
-  free(vc.cand);
-  free(vc.found);
-  free(slots);
-  free(acc);
-  free(rep);
+  gt_free(&all);
   free(counts);
   free(sums);
   free(mins);

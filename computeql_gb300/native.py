@@ -118,6 +118,7 @@ CUDA_API = [
     ("cqlcuda_batch_kernel_execute", None, [P, P, u32, u32]),
     ("cqlcuda_batch_buffer_read", None, [P, P, P, u64]),
     ("cqlcuda_batch_buffer_read_at", None, [P, P, u64, P, u64]),
+    ("cqlcuda_batch_fill_range", None, [P, P, u64, u64, u32]),
     ("cqlcuda_batch_end", C.c_int, [P]),
     ("cqlcuda_stream_alloc", P, [u32]),
     ("cqlcuda_stream_release", None, [P]),

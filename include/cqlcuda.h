@@ -130,6 +130,9 @@ void      cqlcuda_batch_buffer_read(CqlBatch* batch, CqlBuffer* buffer, void* ou
 /* The same from byte `offset` of the buffer (no reference counterpart: a read of one word of a device
    array, such as the total a prefix sum leaves after its last element). */
 void      cqlcuda_batch_buffer_read_at(CqlBatch* batch, CqlBuffer* buffer, uint64_t offset, void* out_data, uint64_t size);
+/* cqlcuda_batch_buffer_fill from byte `offset` (a multiple of 4) of the buffer (no reference counterpart:
+   several output arrays of one operator kept in one buffer). */
+void      cqlcuda_batch_fill_range(CqlBatch* batch, CqlBuffer* buffer, uint64_t offset, uint64_t size, uint32_t value);
 int       cqlcuda_batch_end(CqlBatch* batch);                                                            /* :217, 0 on failure (reads zero-filled) */
 
 /* ---- streams (gpu_backend.h:219-229) ---- */
