@@ -439,9 +439,12 @@ static int64_t gt_find(GroupTable* t, const CqlJoinAgg* q, uint64_t dim_row)
   return (int64_t)g;
 }
 
-/* one slice of dim rows per task: its kept rows grouped and accumulated in dim-row order; the slices'
-   groups are merged afterwards in slice order, so groups keep the order of their first dim row */
+/* The dim-row pass in two parallel steps: slices of dim rows find their kept rows (those whose key has
+   totals), then equal chunks of the kept rows, in dim-row order, are grouped and accumulated; the chunks'
+   groups are merged afterwards in chunk order, so groups keep the order of their first dim row and the
+   work does not depend on where in the dim table the kept rows lie. */
 #define VISIT_SLICE 32768u
+#define GROUP_CHUNK 1024u
 typedef struct
 {
   const CqlJoinAgg* q;
@@ -455,10 +458,22 @@ typedef struct
   uint32_t core_count;
   const uint32_t* core_of_expr;
   uint64_t visits;
-  uint32_t tasks;
-  GroupTable* slices;
+  uint32_t slices;
+  uint32_t* kept;          /* each slice's kept dim rows from the slice's start */
+  uint64_t* kept_count;    /* per slice */
+  uint64_t* kept_before;   /* kept rows of the slices before it */
+  uint64_t kept_total;
+  uint32_t chunks;
+  GroupTable* chunk_groups;
   int* failed;
 } VisitCtx;
+
+static uint64_t key_id(const VisitCtx* c, uint64_t dim_row)
+{
+  uint32_t kw = c->q->dim_keys[dim_row];
+  int64_t key_value = c->signed_key ? (int64_t)(int32_t)kw : (int64_t)kw;
+  return c->by_dim_row ? dim_row : (uint64_t)(key_value - c->min_key);
+}
 
 /* a kept dim row's contribution: its key's totals, or its own value times the key's matches */
 static void accumulate(const VisitCtx* c, JoinAcc* a, uint64_t dim_row, uint64_t id)
@@ -492,35 +507,60 @@ static void accumulate(const VisitCtx* c, JoinAcc* a, uint64_t dim_row, uint64_t
   }
 }
 
-static void visit_task(void* p, uint32_t task)
+static void scan_task(void* p, uint32_t task)
 {
   VisitCtx* c = (VisitCtx*)p;
-  GroupTable* t = &c->slices[task];
-  if (!gt_init(t, c->q->expr_count))
-  {
-    c->failed[task] = 1;
-    return;
-  }
   uint64_t v0 = (uint64_t)task * VISIT_SLICE;
   uint64_t v1 = v0 + VISIT_SLICE < c->visits ? v0 + VISIT_SLICE : c->visits;
   const uint64_t* dim_rows = c->q->dim_rows;
-  const uint32_t* dim_keys = c->q->dim_keys;
+  uint32_t* out = c->kept + v0;
+  uint64_t n = 0;
   for (uint64_t v = v0; v < v1; v++)
   {
     uint64_t dim_row = dim_rows ? dim_rows[v] : v;
-    uint32_t kw = dim_keys[dim_row];
-    int64_t key_value = c->signed_key ? (int64_t)(int32_t)kw : (int64_t)kw;
-    uint64_t id = c->by_dim_row ? dim_row : (uint64_t)(key_value - c->min_key);
-    if (id >= c->total_groups || c->counts[id] == 0) continue;
+    uint64_t id = key_id(c, dim_row);
+    /* written only when kept: a dim table much wider than the fact key's range touches little memory */
+    if (id < c->total_groups && c->counts[id] != 0) out[n++] = (uint32_t)dim_row;
+  }
+  c->kept_count[task] = n;
+}
+
+static void group_task(void* p, uint32_t chunk)
+{
+  VisitCtx* c = (VisitCtx*)p;
+  GroupTable* t = &c->chunk_groups[chunk];
+  if (!gt_init(t, c->q->expr_count))
+  {
+    c->failed[chunk] = 1;
+    return;
+  }
+  uint64_t k0 = (uint64_t)chunk * GROUP_CHUNK;
+  uint64_t k1 = k0 + GROUP_CHUNK < c->kept_total ? k0 + GROUP_CHUNK : c->kept_total;
+  /* the slice holding kept row k0 */
+  uint32_t lo = 0, hi = c->slices;
+  while (hi - lo > 1)
+  {
+    uint32_t mid = (lo + hi) / 2;
+    if (c->kept_before[mid] <= k0) lo = mid;
+    else hi = mid;
+  }
+  uint32_t slice = lo;
+  for (uint64_t k = k0; k < k1; k++)
+  {
+    while (k >= c->kept_before[slice] + c->kept_count[slice]) slice++;
+    uint64_t dim_row = c->kept[(uint64_t)slice * VISIT_SLICE + (k - c->kept_before[slice])];
     int64_t g = gt_find(t, c->q, dim_row);
     if (g < 0)
     {
-      c->failed[task] = 1;
+      c->failed[chunk] = 1;
       return;
     }
-    accumulate(c, &t->acc[(uint64_t)g * t->exprs], dim_row, id);
+    accumulate(c, &t->acc[(uint64_t)g * t->exprs], dim_row, key_id(c, dim_row));
   }
 }
+
+static __thread uint32_t* tl_kept = NULL;
+static __thread uint64_t tl_kept_cap = 0;
 
 int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* out_groups, uint64_t* out_group_dim_row, double* out_results,
                           uint32_t* out_strategy)
@@ -608,18 +648,49 @@ int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* ou
      the group tables start small and grow with the groups found */
   uint64_t visits = q->dim_rows ? q->dim_count : q->dim_table_rows;
   int signed_key = fk->type == CQLOPS_TYPE_I32;
-  VisitCtx vc = { q, signed_key, by_dim_row, min_key, total_groups, counts, sums, mins, maxs, core_count, core_of_expr, visits, 0, NULL, NULL };
-  vc.tasks = (uint32_t)((visits + VISIT_SLICE - 1) / VISIT_SLICE);
-  vc.slices = (GroupTable*)calloc(vc.tasks ? vc.tasks : 1, sizeof(GroupTable));
-  vc.failed = (int*)calloc(vc.tasks ? vc.tasks : 1, sizeof(int));
+  VisitCtx vc;
+  memset(&vc, 0, sizeof(vc));
+  vc.q = q;
+  vc.signed_key = signed_key;
+  vc.by_dim_row = by_dim_row;
+  vc.min_key = min_key;
+  vc.total_groups = total_groups;
+  vc.counts = counts;
+  vc.sums = sums;
+  vc.mins = mins;
+  vc.maxs = maxs;
+  vc.core_count = core_count;
+  vc.core_of_expr = core_of_expr;
+  vc.visits = visits;
+  vc.slices = (uint32_t)((visits + VISIT_SLICE - 1) / VISIT_SLICE);
+  /* the kept rows live in a buffer kept per calling thread: a fresh one each call would fault its pages in */
+  if (visits + 1 > tl_kept_cap)
+  {
+    uint32_t* grown = (uint32_t*)realloc(tl_kept, (visits + 1) * sizeof(uint32_t));
+    if (grown)
+    {
+      tl_kept = grown;
+      tl_kept_cap = visits + 1;
+    }
+  }
+  vc.kept = visits + 1 <= tl_kept_cap ? tl_kept : NULL;
+  vc.kept_count = (uint64_t*)calloc(vc.slices + 1, 8);
+  vc.kept_before = (uint64_t*)calloc(vc.slices + 1, 8);
   GroupTable all;
   memset(&all, 0, sizeof(all));
-  ok = vc.slices && vc.failed && gt_init(&all, q->expr_count);
-  if (ok) cql_parallel_for(vc.tasks, visit_task, &vc);
-  /* the slices' groups in slice order: a group's first dim row decides its place */
-  for (uint32_t task = 0; ok && task < vc.tasks; task++)
+  ok = vc.kept && vc.kept_count && vc.kept_before && gt_init(&all, q->expr_count);
+  if (ok) cql_parallel_for(vc.slices, scan_task, &vc);
+  for (uint32_t sl = 0; ok && sl < vc.slices; sl++) vc.kept_before[sl + 1] = vc.kept_before[sl] + vc.kept_count[sl];
+  vc.kept_total = ok ? vc.kept_before[vc.slices] : 0;
+  vc.chunks = (uint32_t)((vc.kept_total + GROUP_CHUNK - 1) / GROUP_CHUNK);
+  vc.chunk_groups = (GroupTable*)calloc(vc.chunks ? vc.chunks : 1, sizeof(GroupTable));
+  vc.failed = (int*)calloc(vc.chunks ? vc.chunks : 1, sizeof(int));
+  ok = ok && vc.chunk_groups && vc.failed;
+  if (ok && vc.chunks) cql_parallel_for(vc.chunks, group_task, &vc);
+  /* the chunks' groups in chunk order: a group's first dim row decides its place */
+  for (uint32_t task = 0; ok && task < vc.chunks; task++)
   {
-    const GroupTable* t = &vc.slices[task];
+    const GroupTable* t = &vc.chunk_groups[task];
     if (vc.failed[task])
     {
       ok = 0;
@@ -648,10 +719,12 @@ int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* ou
       }
     }
   }
-  if (vc.slices)
-    for (uint32_t task = 0; task < vc.tasks; task++) gt_free(&vc.slices[task]);
-  free(vc.slices);
+  if (vc.chunk_groups)
+    for (uint32_t task = 0; task < vc.chunks; task++) gt_free(&vc.chunk_groups[task]);
+  free(vc.chunk_groups);
   free(vc.failed);
+  free(vc.kept_count);
+  free(vc.kept_before);
   uint64_t groups = ok ? all.groups : 0;
   uint64_t* rep = all.rep;
   JoinAcc* acc = all.acc;
