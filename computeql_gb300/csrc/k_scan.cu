@@ -221,6 +221,28 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_simple(CqlLaunch a, uint6
   uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t private_count = 0;
 
+  // COUNT(*) of one whole-number comparison on a full-width column (the common count query): 16 rows
+  // per thread with all four 16-byte loads issued before the compares, twice the bytes in flight of the
+  // general loop. The condition is the same for every thread of the grid.
+  const Leaf& L0 = s_leaf[0];
+  if (COUNT_ONLY && leaf_count == 1 && (L0.flags & SCAN_INT_FLAG) && !(L0.flags & SCAN_INT_NEVER) && L0.width == 0 && !skip_on)
+  {
+    const uint32_t* col = (const uint32_t*)a.buf[6 + (L0.slot < 10 ? L0.slot : 0)];
+    const uint32_t lo = L0.w3, span = L0.w4, bias = (L0.flags & SCAN_INT_BIAS) ? 0x80000000u : 0u;
+    const uint64_t blocks16 = rows / 16;
+    for (uint64_t g = (uint64_t)blockIdx.x * SCAN_THREADS + threadIdx.x; g < blocks16; g += per_pass)
+    {
+      const uint4* v = (const uint4*)(col + g * 16);
+      uint4 q0 = __ldcs(v), q1 = __ldcs(v + 1), q2 = __ldcs(v + 2), q3 = __ldcs(v + 3);
+      uint32_t w[16] = { q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w };
+#pragma unroll
+      for (uint32_t k = 0; k < 16; k++) private_count += ((w[k] ^ bias) - lo) <= span ? 1u : 0u;
+    }
+    for (uint64_t r = blocks16 * 16 + (uint64_t)blockIdx.x * SCAN_THREADS + threadIdx.x; r < rows; r += per_pass)
+      private_count += ((col[r] ^ bias) - lo) <= span ? 1u : 0u;
+    groups = 0;   // the general loop below has nothing left to do
+  }
+
   for (uint64_t base_group = (uint64_t)blockIdx.x * SCAN_THREADS; base_group < groups; base_group += per_pass)
   {
     uint64_t g = base_group + threadIdx.x;
