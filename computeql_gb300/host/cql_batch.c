@@ -698,6 +698,419 @@ static char* batch_source_tiled(char** shape_exprs, const uint32_t* shape_sites,
   return b.p;
 }
 
+/* ---- the cube form: group once, answer many ---- */
+
+/* Queries whose WHERE reads only whole-number columns of small range are answered from a dense table of
+   the rows: for every combination of those columns' values (a cell) the count of rows and the
+   fixed-point sums of the summed columns, built in one pass over the table (shared-memory tables per CTA,
+   then 128-bit totals in global memory). A query then tests its predicate on each cell's values - the
+   values of the rows in that cell, so the test is the rows' test - and adds up the cells that pass.
+   Counts are exact and the sums are the same integers the scan adds, so the results are the scan's;
+   the table costs one pass whatever the number of queries, and a query costs a pass over the cells. */
+#define CUBE_MAX 8
+#define CUBE_MAX_DIMS 4
+#define CUBE_MAX_CELLS 65536u
+#define CUBE_SMEM_BYTES (200u * 1024u)
+#define CUBE_THREADS 1024u
+
+typedef struct
+{
+  uint32_t dims;
+  int slot[CUBE_MAX_DIMS];
+  uint32_t min[CUBE_MAX_DIMS];      /* the column's smallest value (bits of the i32 for I32 columns) */
+  uint32_t radix[CUBE_MAX_DIMS];
+  uint32_t stride[CUBE_MAX_DIMS];
+  int is_signed[CUBE_MAX_DIMS];
+  uint32_t cells;
+  uint32_t mask;                    /* the slots */
+  uint32_t nsum;
+  int sum_slot[CQLOPS_MAX_BINDINGS];
+  uint64_t word_off;                /* first word of the cube's global table: counts, then (lo, hi) sums */
+  uint32_t pass;                    /* the table pass that builds it */
+  uint32_t smem_off;                /* bytes into its pass's shared tables: u32 counts, then 128-bit sums [sum][cell] */
+} Cube;
+
+typedef struct
+{
+  uint32_t cubes;
+  Cube cube[CUBE_MAX];
+  uint64_t words;
+  uint32_t passes;                  /* table passes: each builds the cubes whose shared tables fit together */
+  uint32_t smem[CUBE_MAX];          /* one copy of a pass's shared tables */
+  uint32_t copies[CUBE_MAX];        /* copies of them per CTA (warps spread over them) */
+} CubePlan;
+
+static uint32_t cube_smem(const Cube* c)
+{
+  return ((c->cells * 4u + 7u) & ~7u) + c->cells * c->nsum * 16u;
+}
+
+/* whether column `slot` can be a dimension: a whole-number column of at most 65536 values */
+static int cube_dim_ok(const CqlColumn* columns, uint32_t column_count, int slot, int load_type)
+{
+  if (slot < 0 || (uint32_t)slot >= column_count) return 0;
+  const CqlColumn* c = &columns[slot];
+  if (!(load_type == CQLOPS_TYPE_U32 || load_type == CQLOPS_TYPE_I32) || c->type != (uint32_t)load_type || !c->has_range) return 0;
+  if (!(c->zone_max >= c->zone_min) || c->zone_max - c->zone_min > 65535.0) return 0;
+  if (load_type == CQLOPS_TYPE_U32 && (c->zone_min < 0.0 || c->zone_max > 4294967295.0)) return 0;
+  if (load_type == CQLOPS_TYPE_I32 && (c->zone_min < -2147483648.0 || c->zone_max > 2147483647.0)) return 0;
+  return 1;
+}
+
+/* Assigns shapes to cubes: each eligible shape's column set, merged into a cube over a superset when one
+   exists. When the shared tables do not fit, the largest cube's column set is excluded and the plan made
+   again (its shapes may then join other cubes or get their own; a shape over an excluded set goes to the
+   scan). cube_of[s] = -1 for a shape the scan answers. */
+static void cube_assign(uint32_t shapes, const uint32_t* shape_mask, const uint32_t* shape_sums, const int* eligible,
+                        const uint32_t* excluded, uint32_t excluded_count, const CqlColumn* columns, CubePlan* plan, int* cube_of)
+{
+  memset(plan, 0, sizeof(*plan));
+  uint32_t order[BATCH_MAX_SHAPES];
+  uint32_t n = 0;
+  for (uint32_t s = 0; s < shapes; s++)
+  {
+    cube_of[s] = -1;
+    int out = !eligible[s];
+    for (uint32_t e = 0; !out && e < excluded_count; e++) out = shape_mask[s] == excluded[e];
+    if (!out) order[n++] = s;
+  }
+  for (uint32_t i = 1; i < n; i++)
+    for (uint32_t j = i; j > 0 && __builtin_popcount(shape_mask[order[j]]) > __builtin_popcount(shape_mask[order[j - 1]]); j--)
+    {
+      uint32_t t = order[j];
+      order[j] = order[j - 1];
+      order[j - 1] = t;
+    }
+  for (uint32_t i = 0; i < n; i++)
+  {
+    uint32_t s = order[i], m = shape_mask[s];
+    int chosen = -1;
+    for (uint32_t c = 0; c < plan->cubes && chosen < 0; c++)
+      if ((plan->cube[c].mask & m) == m) chosen = (int)c;
+    if (chosen < 0 && plan->cubes < CUBE_MAX)
+    {
+      Cube* c = &plan->cube[plan->cubes];
+      memset(c, 0, sizeof(*c));
+      c->mask = m;
+      for (int d = 0; d < CQLOPS_MAX_BINDINGS; d++)
+        if ((m >> d) & 1u)
+        {
+          c->slot[c->dims] = d;
+          c->is_signed[c->dims] = columns[d].type == CQLOPS_TYPE_I32;
+          c->min[c->dims] = c->is_signed[c->dims] ? (uint32_t)(int32_t)columns[d].zone_min : (uint32_t)columns[d].zone_min;
+          c->radix[c->dims] = (uint32_t)(columns[d].zone_max - columns[d].zone_min) + 1u;
+          c->dims++;
+        }
+      /* row-major strides: the last dimension varies fastest */
+      uint32_t stride = 1;
+      for (int d = (int)c->dims - 1; d >= 0; d--)
+      {
+        c->stride[d] = stride;
+        stride *= c->radix[d];
+      }
+      c->cells = stride;
+      chosen = (int)plan->cubes++;
+    }
+    cube_of[s] = chosen;
+  }
+  /* summed columns of each cube: those its shapes' queries sum */
+  for (uint32_t s = 0; s < shapes; s++)
+  {
+    if (cube_of[s] < 0) continue;
+    Cube* c = &plan->cube[cube_of[s]];
+    for (int col = 0; col < CQLOPS_MAX_BINDINGS; col++)
+    {
+      if (!((shape_sums[s] >> col) & 1u)) continue;
+      uint32_t j = 0;
+      while (j < c->nsum && c->sum_slot[j] != col) j++;
+      if (j == c->nsum) c->sum_slot[c->nsum++] = col;
+    }
+  }
+  /* global tables one after another; passes by first fit, largest cube first */
+  uint64_t words = 0;
+  for (uint32_t c = 0; c < plan->cubes; c++)
+  {
+    plan->cube[c].word_off = words;
+    words += (uint64_t)plan->cube[c].cells * (1u + 2u * plan->cube[c].nsum);
+  }
+  plan->words = words;
+  uint32_t by_size[CUBE_MAX];
+  for (uint32_t c = 0; c < plan->cubes; c++) by_size[c] = c;
+  for (uint32_t i = 1; i < plan->cubes; i++)
+    for (uint32_t j = i; j > 0 && cube_smem(&plan->cube[by_size[j]]) > cube_smem(&plan->cube[by_size[j - 1]]); j--)
+    {
+      uint32_t t = by_size[j];
+      by_size[j] = by_size[j - 1];
+      by_size[j - 1] = t;
+    }
+  plan->passes = 0;
+  for (uint32_t i = 0; i < plan->cubes; i++)
+  {
+    Cube* cu = &plan->cube[by_size[i]];
+    uint32_t b = cube_smem(cu), p = 0;
+    while (p < plan->passes && plan->smem[p] + b > CUBE_SMEM_BYTES) p++;
+    if (p == plan->passes) plan->smem[plan->passes++] = 0;
+    cu->pass = p;
+    cu->smem_off = plan->smem[p];
+    plan->smem[p] += b;
+  }
+  for (uint32_t p = 0; p < plan->passes; p++)
+  {
+    uint32_t copies = plan->smem[p] ? CUBE_SMEM_BYTES / plan->smem[p] : 1;
+    plan->copies[p] = copies > 32 ? 32 : (copies < 1 ? 1 : copies);
+  }
+}
+
+static void cube_plan(uint32_t shapes, const uint32_t* shape_mask, const int* shape_types, const uint32_t* shape_sums,
+                      const CqlColumn* columns, uint32_t column_count, CubePlan* plan, int* cube_of)
+{
+  /* eligible: at most 4 whole-number columns of small range, at most CUBE_MAX_CELLS combinations */
+  int eligible[BATCH_MAX_SHAPES];
+  for (uint32_t s = 0; s < shapes; s++)
+  {
+    uint32_t m = shape_mask[s];
+    int ok = __builtin_popcount(m) <= CUBE_MAX_DIMS;
+    double cells = 1.0;
+    for (int d = 0; ok && d < CQLOPS_MAX_BINDINGS; d++)
+      if ((m >> d) & 1u)
+      {
+        ok = cube_dim_ok(columns, column_count, d, shape_types[s * CQLOPS_MAX_BINDINGS + d]);
+        if (ok) cells *= columns[d].zone_max - columns[d].zone_min + 1.0;
+      }
+    eligible[s] = ok && cells <= (double)CUBE_MAX_CELLS;
+  }
+  /* a cube whose shared table alone is too large is not built: its column set is excluded and the
+     shapes planned again (they may fit smaller cubes) */
+  uint32_t excluded[BATCH_MAX_SHAPES];
+  uint32_t excluded_count = 0;
+  for (;;)
+  {
+    cube_assign(shapes, shape_mask, shape_sums, eligible, excluded, excluded_count, columns, plan, cube_of);
+    int too_large = -1;
+    for (uint32_t c = 0; c < plan->cubes && too_large < 0; c++)
+      if (cube_smem(&plan->cube[c]) > CUBE_SMEM_BYTES) too_large = (int)c;
+    if (too_large < 0) break;
+    excluded[excluded_count++] = plan->cube[too_large].mask;
+  }
+}
+
+/* the summand of slot `c` of type t in the kernels' fixed point, from v (the loaded word(s)) */
+static void fx_expr(char* out, size_t cap, int t, const char* v)
+{
+  if (t == CQLOPS_TYPE_F64) snprintf(out, cap, "cql_fx64(%s, sh, sc)", v);
+  else if (t == CQLOPS_TYPE_F32) snprintf(out, cap, "cql_fx64((u64)__double_as_longlong((double)__uint_as_float(%s)), sh, sc)", v);
+  else if (t == CQLOPS_TYPE_I32) snprintf(out, cap, "(sh >= 0 ? (long long)(int)%s * (1ll << sh) : __double2ll_rn((double)(int)%s * sc))", v, v);
+  else if (t == CQLOPS_TYPE_U64) snprintf(out, cap, "__double2ll_rn((double)%s * sc)", v);
+  else if (t == CQLOPS_TYPE_I64) snprintf(out, cap, "__double2ll_rn(cql_i64d(%s) * sc)", v);
+  else snprintf(out, cap, "(sh >= 0 ? (long long)((u64)%s << sh) : __double2ll_rn((double)%s * sc))", v, v);
+}
+
+/* The table pass: bindings 0 the scales, 1 the global tables (zeroed), 2 an error word, 6.. the columns;
+   words 0 rows, 2 the summed columns this launch needs. */
+static char* cube_build_source(const CubePlan* P, uint32_t pass, const int* slot_type)
+{
+  Buf b;
+  memset(&b, 0, sizeof(b));
+  const uint32_t SMEM = P->smem[pass], COPIES = P->copies[pass];
+  uint32_t load = 0;   /* the columns the pass reads: dimensions and summed columns */
+  for (uint32_t c = 0; c < P->cubes; c++)
+  {
+    if (P->cube[c].pass != pass) continue;
+    load |= P->cube[c].mask;
+    for (uint32_t j = 0; j < P->cube[c].nsum; j++) load |= 1u << P->cube[c].sum_slot[j];
+  }
+  bput(&b, "// cql: block=%u smem=%u per_sm=1\n", CUBE_THREADS, SMEM * COPIES);
+  bput(&b, "%s", BATCH_PRELUDE);
+  bput(&b,
+       "extern \"C\" __global__ void __launch_bounds__(%u) cql_main(CqlLaunch a)\n{\n"
+       "  const u64 rows = cql_word(a, 0); const u32 need_sum = cql_word(a, 2); (void)need_sum;\n"
+       "  const double* col_scale = (const double*)a.buf[0]; const long long* col_shift = (const long long*)a.buf[0] + 16;\n"
+       "  (void)col_scale; (void)col_shift;\n"
+       "  u64* g = (u64*)a.buf[1]; u32* err = (u32*)a.buf[2];\n"
+       "  extern __shared__ u64 s_mem[];\n"
+       "  for (u32 i = threadIdx.x; i < %uu; i += blockDim.x) s_mem[i] = 0ull;\n"
+       "  __syncthreads();\n"
+       "  unsigned char* tab = (unsigned char*)s_mem + ((threadIdx.x >> 5) %% %uu) * %uu;   /* this warp's copy */\n"
+       "  u32 bad = 0u;\n"
+       "  const u64 per_pass = (u64)gridDim.x * blockDim.x * 4ull;\n"
+       "  for (u64 row0 = ((u64)blockIdx.x * blockDim.x + threadIdx.x) * 4ull; row0 < rows; row0 += per_pass)\n  {\n"
+       "    const u32 valid = (u32)min((u64)4, rows - row0);\n",
+       CUBE_THREADS, SMEM * COPIES / 8u, COPIES, SMEM);
+  for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++)
+  {
+    if (!((load >> s) & 1u)) continue;
+    int t = slot_type[s];
+    if (type_bytes(t) == 8)
+      bput(&b,
+           "    u64 v%d[4];\n"
+           "    if (valid == 4u) { uint4 x = cql_ld4((const u64*)a.buf[%d] + row0); uint4 y = cql_ld4((const u64*)a.buf[%d] + row0 + 2);\n"
+           "      v%d[0] = ((u64)x.y << 32) | x.x; v%d[1] = ((u64)x.w << 32) | x.z; v%d[2] = ((u64)y.y << 32) | y.x; v%d[3] = ((u64)y.w << 32) | y.z; }\n"
+           "    else { for (u32 j = 0; j < 4u; j++) v%d[j] = j < valid ? ((const u64*)a.buf[%d])[row0 + j] : 0ull; }\n",
+           s, 6 + s, 6 + s, s, s, s, s, s, 6 + s);
+    else if (type_bytes(t) == 1)
+      bput(&b, "    u32 v%d[4];\n    for (u32 j = 0; j < 4u; j++) v%d[j] = j < valid ? (u32)((const unsigned char*)a.buf[%d])[row0 + j] : 0u;\n", s, s,
+           6 + s);
+    else
+      bput(&b,
+           "    u32 v%d[4];\n"
+           "    if (valid == 4u) { uint4 x = cql_ld4((const u32*)a.buf[%d] + row0); v%d[0] = x.x; v%d[1] = x.y; v%d[2] = x.z; v%d[3] = x.w; }\n"
+           "    else { for (u32 j = 0; j < 4u; j++) v%d[j] = j < valid ? ((const u32*)a.buf[%d])[row0 + j] : 0u; }\n",
+           s, 6 + s, s, s, s, s, s, 6 + s);
+  }
+  /* the summands, once per row */
+  uint32_t summed = 0;
+  for (uint32_t c = 0; c < P->cubes; c++)
+    if (P->cube[c].pass == pass)
+      for (uint32_t j = 0; j < P->cube[c].nsum; j++) summed |= 1u << P->cube[c].sum_slot[j];
+  for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++)
+  {
+    if (!((summed >> s) & 1u)) continue;
+    char vj[16], ex[220];
+    snprintf(vj, sizeof(vj), "v%d[j]", s);
+    fx_expr(ex, sizeof(ex), slot_type[s], vj);
+    bput(&b,
+         "    long long fx%d[4];\n"
+         "    if ((need_sum >> %d) & 1u) { const double sc = col_scale[%d]; const int sh = (int)col_shift[%d]; (void)sc; (void)sh;\n"
+         "      for (u32 j = 0; j < 4u; j++) fx%d[j] = j < valid ? %s : 0ll; }\n"
+         "    else { for (u32 j = 0; j < 4u; j++) fx%d[j] = 0ll; }\n",
+         s, s, s, s, s, ex, s);
+  }
+  bput(&b, "    for (u32 j = 0; j < valid; j++)\n    {\n");
+  for (uint32_t c = 0; c < P->cubes; c++)
+  {
+    const Cube* cu = &P->cube[c];
+    if (cu->pass != pass) continue;
+    bput(&b, "      {\n        u32 cell = 0u; bool in = true;\n");
+    for (uint32_t d = 0; d < cu->dims; d++)
+    {
+      if (cu->is_signed[d]) bput(&b, "        { const u32 x = (u32)((int)v%d[j] - (int)%du); in = in && x < %uu; cell += x * %uu; }\n", cu->slot[d], cu->min[d], cu->radix[d], cu->stride[d]);
+      else bput(&b, "        { const u32 x = v%d[j] - %uu; in = in && x < %uu; cell += x * %uu; }\n", cu->slot[d], cu->min[d], cu->radix[d], cu->stride[d]);
+    }
+    bput(&b,
+         "        if (!in) bad = 1u;\n"
+         "        else\n        {\n"
+         "          atomicAdd((u32*)(tab + %uu) + cell, 1u);\n",
+         cu->smem_off);
+    uint32_t sums_at = cu->smem_off + ((cu->cells * 4u + 7u) & ~7u);
+    /* a cell's sum is a 128-bit (lo, hi) pair: the low word by atomic add, the high word when the add
+       carried or the summand is negative */
+    for (uint32_t jj = 0; jj < cu->nsum; jj++)
+      bput(&b,
+           "          if (fx%d[j]) { u64* w = (u64*)(tab + %uu) + 2u * (%uu + cell); const u64 v = (u64)fx%d[j]; const u64 old = atomicAdd(&w[0], v);\n"
+           "            const u64 h = (fx%d[j] < 0 ? ~0ull : 0ull) + (old + v < old ? 1ull : 0ull); if (h) atomicAdd(&w[1], h); }\n",
+           cu->sum_slot[jj], sums_at, jj * cu->cells, cu->sum_slot[jj], cu->sum_slot[jj]);
+    bput(&b, "        }\n      }\n");
+  }
+  bput(&b, "    }\n  }\n  if (bad) atomicOr(err, 1u);\n  __syncthreads();\n");
+  /* the copies folded into the global tables: counts added, sums as 128-bit totals */
+  for (uint32_t c = 0; c < P->cubes; c++)
+  {
+    const Cube* cu = &P->cube[c];
+    if (cu->pass != pass) continue;
+    uint32_t sums_at = cu->smem_off + ((cu->cells * 4u + 7u) & ~7u);
+    bput(&b,
+         "  for (u32 cell = threadIdx.x; cell < %uu; cell += blockDim.x)\n  {\n"
+         "    u64 n = 0ull;\n"
+         "    for (u32 k = 0; k < %uu; k++) n += ((const u32*)((const unsigned char*)s_mem + k * %uu + %uu))[cell];\n"
+         "    if (n) atomicAdd(&g[%lluull + cell], n);\n",
+         cu->cells, COPIES, SMEM, cu->smem_off, (unsigned long long)cu->word_off);
+    for (uint32_t jj = 0; jj < cu->nsum; jj++)
+      bput(&b,
+           "    {\n      u64 lo = 0ull, hi = 0ull;\n"
+           "      for (u32 k = 0; k < %uu; k++) { const u64* v = (const u64*)((const unsigned char*)s_mem + k * %uu + %uu) + 2u * (%uu + cell);\n"
+           "        const u64 l2 = lo + v[0]; hi += v[1] + (l2 < lo ? 1ull : 0ull); lo = l2; }\n"
+           "      if (lo | hi) { u64* w = &g[%lluull + 2ull * ((u64)%uu + cell)]; const u64 old = atomicAdd(&w[0], lo);\n"
+           "        const u64 carry = (old + lo < old) ? 1ull : 0ull; if (hi + carry) atomicAdd(&w[1], hi + carry); }\n"
+           "    }\n",
+           COPIES, SMEM, sums_at, jj * cu->cells, (unsigned long long)(cu->word_off + cu->cells), jj * cu->cells);
+    bput(&b, "  }\n");
+  }
+  bput(&b, "}\n");
+  if (b.failed)
+  {
+    free(b.p);
+    return NULL;
+  }
+  return b.p;
+}
+
+/* The answers: one CTA per query; bindings 1 the global tables, 3 thresholds, 4 literals, 5 per query
+   (shape | cube << 8 | (summed column's index in the cube + 1) << 16), 6 out (count, lo, hi) per query;
+   word 0 queries. */
+static char* cube_answer_source(const CubePlan* P, char** shape_exprs, const uint32_t* shape_sites, uint32_t shapes, const int* cube_of)
+{
+  Buf b;
+  memset(&b, 0, sizeof(b));
+  bput(&b, "// cql: block=256 smem=0 per_sm=8\n");
+  bput(&b, "%s", BATCH_PRELUDE);
+  bput(&b, "struct CubeDim { u32 min, radix, stride; __device__ __forceinline__ u32 operator[](u32 cell) const { return min + (cell / stride) %% radix; } };\n");
+  for (uint32_t s = 0; s < shapes; s++)
+    if (cube_of[s] >= 0) bput(&b, "#define CQL_SHAPE_%u(k) (%s)\n", s, shape_exprs[s]);
+  bput(&b,
+       "extern \"C\" __global__ void __launch_bounds__(256) cql_main(CqlLaunch a)\n{\n"
+       "  const u32 nq = cql_word(a, 0);\n"
+       "  const u64* g = (const u64*)a.buf[1];\n"
+       "  const Thr* thr = (const Thr*)a.buf[3]; const double* qconst = (const double*)a.buf[4];\n"
+       "  const u32* meta = (const u32*)a.buf[5]; u64* out = (u64*)a.buf[6];\n"
+       "  __shared__ u64 s_red[3 * 8];\n"
+       "  for (u32 q = blockIdx.x; q < nq; q += gridDim.x)\n  {\n"
+       "    const u32 m = meta[q]; const u32 shape = m & 0xffu, cube = (m >> 8) & 0xffu; const int sj = (int)(m >> 16) - 1;\n"
+       "    const Thr* TH = thr + (u64)q * %uu; const double* QC = qconst + (u64)q * %uu; (void)TH; (void)QC;\n"
+       "    u64 c = 0ull, lo = 0ull, hi = 0ull;\n"
+       "    switch (cube)\n    {\n",
+       BATCH_MAX_SITES, BATCH_MAX_CONSTS);
+  for (uint32_t c = 0; c < P->cubes; c++)
+  {
+    const Cube* cu = &P->cube[c];
+    bput(&b, "    case %uu:\n    {\n", c);
+    for (uint32_t d = 0; d < cu->dims; d++)
+      bput(&b, "      const CubeDim r%d = { %uu, %uu, %uu };\n", cu->slot[d], cu->min[d], cu->radix[d], cu->stride[d]);
+    bput(&b,
+         "      const u64* cnt = g + %lluull; const u64* sums = g + %lluull; (void)sums;\n"
+         "      const u32 cells = %uu;\n"
+         "      switch (shape)\n      {\n",
+         (unsigned long long)cu->word_off, (unsigned long long)(cu->word_off + cu->cells), cu->cells);
+    for (uint32_t s = 0; s < shapes; s++)
+    {
+      if (cube_of[s] != (int)c) continue;
+      char decls[BATCH_MAX_SITES * 40 + 1];
+      size_t dn = 0;
+      decls[0] = 0;
+      for (uint32_t i = 0; i < shape_sites[s] && i < BATCH_MAX_SITES; i++)
+        dn += (size_t)snprintf(decls + dn, sizeof(decls) - dn, "        const Thr T%u = TH[%u];\n", i, i);
+      bput(&b,
+           "      case %uu:\n      {\n"
+           "%s"
+           "        for (u32 k = threadIdx.x; k < cells; k += blockDim.x)\n"
+           "          if (CQL_SHAPE_%u(k)) { c += cnt[k]; if (sj >= 0) { const u64* w = sums + 2ull * ((u64)sj * cells + k); const u64 l2 = lo + w[0]; hi += w[1] + (l2 < lo ? 1ull : 0ull); lo = l2; } }\n"
+           "        break;\n      }\n",
+           s, decls, s);
+    }
+    bput(&b, "      default: break;\n      }\n      break;\n    }\n");
+  }
+  bput(&b,
+       "    default: break;\n    }\n"
+       "    for (int o = 16; o > 0; o >>= 1)\n    {\n"
+       "      const u64 c2 = __shfl_xor_sync(0xffffffffu, c, o), l2 = __shfl_xor_sync(0xffffffffu, lo, o), h2 = __shfl_xor_sync(0xffffffffu, hi, o);\n"
+       "      const u64 s = lo + l2; hi += h2 + (s < lo ? 1ull : 0ull); lo = s; c += c2;\n"
+       "    }\n"
+       "    if ((threadIdx.x & 31u) == 0u) { s_red[(threadIdx.x >> 5) * 3] = c; s_red[(threadIdx.x >> 5) * 3 + 1] = lo; s_red[(threadIdx.x >> 5) * 3 + 2] = hi; }\n"
+       "    __syncthreads();\n"
+       "    if (threadIdx.x == 0u)\n    {\n"
+       "      u64 tc = 0ull, tl = 0ull, th = 0ull;\n"
+       "      for (u32 w = 0; w < blockDim.x / 32u; w++) { const u64 s = tl + s_red[w * 3 + 1]; th += s_red[w * 3 + 2] + (s < tl ? 1ull : 0ull); tl = s; tc += s_red[w * 3]; }\n"
+       "      out[(u64)q * 3] = tc; out[(u64)q * 3 + 1] = tl; out[(u64)q * 3 + 2] = th;\n"
+       "    }\n"
+       "    __syncthreads();\n"
+       "  }\n}\n");
+  if (b.failed)
+  {
+    free(b.p);
+    return NULL;
+  }
+  return b.p;
+}
+
 /* the source of one launch in the form rows_per_thread asks for */
 static char* launch_source(char** shape_exprs, const uint32_t* shape_sites, uint32_t shapes, const int* slot_type, const int* sum_cols,
                            uint32_t sum_col_count, uint32_t rows_per_thread)
@@ -715,6 +1128,9 @@ struct CqlBatchCatalog
   uint64_t keys[CQL_BATCH_CATALOG_SHAPES];
   char* exprs[CQL_BATCH_CATALOG_SHAPES];
   uint32_t sites[CQL_BATCH_CATALOG_SHAPES];
+  uint32_t masks[CQL_BATCH_CATALOG_SHAPES];                       /* the columns each shape reads */
+  int types[CQL_BATCH_CATALOG_SHAPES * CQLOPS_MAX_BINDINGS];      /* and as what */
+  uint32_t sums[CQL_BATCH_CATALOG_SHAPES];                        /* the columns its queries have summed */
   int slot_type[CQLOPS_MAX_BINDINGS];
   uint32_t sum_mask;     /* the columns any batch summed */
   uint64_t version;      /* bumped when a shape, a column type or a summed column is added */
@@ -750,6 +1166,9 @@ typedef struct
   uint32_t shapes;
   char* exprs[CQL_BATCH_CATALOG_SHAPES];
   uint32_t sites[CQL_BATCH_CATALOG_SHAPES];
+  uint32_t masks[CQL_BATCH_CATALOG_SHAPES];
+  int types[CQL_BATCH_CATALOG_SHAPES * CQLOPS_MAX_BINDINGS];
+  uint32_t sums[CQL_BATCH_CATALOG_SHAPES];
   int slot_type[CQLOPS_MAX_BINDINGS];
   uint32_t sum_mask;
 } CatalogView;
@@ -758,7 +1177,8 @@ typedef struct
    0 when the catalog cannot take them (full, or a column read as another type): the batch then runs
    without it. Entries are never removed, so the view's strings stay valid while the catalog lives. */
 static int catalog_map(CqlBatchCatalog* c, uint32_t shapes, char** exprs, const uint64_t* keys, const uint32_t* sites,
-                       const int* slot_type, uint32_t sum_mask, uint32_t* out_index, CatalogView* view)
+                       const uint32_t* masks, const int* types, const uint32_t* sums, const int* slot_type, uint32_t sum_mask,
+                       uint32_t* out_index, CatalogView* view)
 {
   int ok = 1;
   pthread_mutex_lock(&c->lock);
@@ -799,8 +1219,20 @@ static int catalog_map(CqlBatchCatalog* c, uint32_t shapes, char** exprs, const 
       c->keys[k] = keys[s];
       c->exprs[k] = e;
       c->sites[k] = sites[s];
+      c->masks[k] = masks[s];
+      memcpy(&c->types[k * CQLOPS_MAX_BINDINGS], &types[s * CQLOPS_MAX_BINDINGS], sizeof(int) * CQLOPS_MAX_BINDINGS);
+      c->sums[k] = 0;
       c->shapes = k + 1;
       c->version++;
+    }
+    for (uint32_t s = 0; ok && s < shapes; s++)
+    {
+      uint32_t k = out_index[s];
+      if ((c->sums[k] | sums[s]) != c->sums[k])
+      {
+        c->sums[k] |= sums[s];
+        c->version++;
+      }
     }
   }
   if (ok)
@@ -819,6 +1251,9 @@ static int catalog_map(CqlBatchCatalog* c, uint32_t shapes, char** exprs, const 
     view->shapes = c->shapes;
     memcpy(view->exprs, c->exprs, sizeof(c->exprs));
     memcpy(view->sites, c->sites, sizeof(c->sites));
+    memcpy(view->masks, c->masks, sizeof(c->masks));
+    memcpy(view->types, c->types, sizeof(c->types));
+    memcpy(view->sums, c->sums, sizeof(c->sums));
     memcpy(view->slot_type, c->slot_type, sizeof(c->slot_type));
     view->sum_mask = c->sum_mask;
   }
@@ -828,19 +1263,21 @@ static int catalog_map(CqlBatchCatalog* c, uint32_t shapes, char** exprs, const 
 
 /* ---- the operator ---- */
 
-enum { BATCH_RUN = 0, BATCH_SOURCE = 1, BATCH_PREPARE = 2 };
+enum { BATCH_RUN = 0, BATCH_SOURCE = 1, BATCH_PREPARE = 2, BATCH_CUBE_BUILD_SOURCE = 3, BATCH_CUBE_ANSWER_SOURCE = 4 };
 
 /* The operator; with BATCH_SOURCE the source of its first launch, with BATCH_PREPARE its kernel compiled
    and the shapes entered in the catalog (neither does device work on the table). */
 static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns,
                      uint32_t column_count, const int32_t* sum_columns, uint32_t rows_per_thread, uint64_t* out_counts, double* out_sums,
-                     uint32_t* out_shapes, int mode, char* src_out, uint64_t src_cap, uint64_t* src_len)
+                     uint32_t* out_shapes, int mode, char* src_out, uint64_t src_cap, uint64_t* src_len, int allow_cubes)
 {
   cqlops_note_error("");
   if (query_count == 0) return 1;
   if (column_count == 0 || column_count > CQLOPS_MAX_BINDINGS) return refuse("1 to 10 columns");
-  /* 0: the shared-memory tile form; 4, 8 or 16: the register form with that many rows per thread */
-  if (rows_per_thread != 0 && rows_per_thread != 4 && rows_per_thread != 8 && rows_per_thread != 16) rows_per_thread = 0;
+  /* 0: the shared-memory tile form; 4, 8 or 16: the register form with that many rows per thread (the
+     cube-source modes carry the table pass here instead) */
+  uint32_t cube_pass = rows_per_thread;
+  if (rows_per_thread != 0 && rows_per_thread != 4 && rows_per_thread != 8 && rows_per_thread != 16) rows_per_thread = 8;
   uint64_t rows = columns[0].rows;
   for (uint32_t c = 0; c < column_count; c++)
   {
@@ -858,9 +1295,12 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
   char* exprs[BATCH_MAX_SHAPES];
   uint32_t shape_sites[BATCH_MAX_SHAPES];
   uint64_t shape_keys[BATCH_MAX_SHAPES];
+  uint32_t shape_mask[BATCH_MAX_SHAPES];
+  uint32_t shape_sums[BATCH_MAX_SHAPES];
+  int* shape_types = (int*)calloc(BATCH_MAX_SHAPES * CQLOPS_MAX_BINDINGS, sizeof(int));
   uint32_t shapes = 0;
   int slot_type[CQLOPS_MAX_BINDINGS] = { 0 };
-  int ok = rb && shape_of && order && thr && qconst && qsum;
+  int ok = rb && shape_of && order && thr && qconst && qsum && shape_types;
   char why[160] = "";
   for (uint32_t q = 0; ok && q < query_count; q++)
   {
@@ -905,6 +1345,13 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
       shape_keys[s] = h;
       exprs[s] = expr;
       shape_sites[s] = site_count;
+      shape_mask[s] = 0;
+      shape_sums[s] = 0;
+      for (int d = 0; d < CQLOPS_MAX_BINDINGS; d++)
+      {
+        shape_types[s * CQLOPS_MAX_BINDINGS + d] = st[d];
+        if (st[d]) shape_mask[s] |= 1u << d;
+      }
       shapes++;
     }
     else
@@ -928,6 +1375,7 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
       break;
     }
     qsum[q] = sc < 0 ? 0xffffffffu : (uint32_t)sc;
+    if (sc >= 0) shape_sums[s] |= 1u << sc;
   }
   /* summed columns: loaded, scaled by 2^k with k from the column's range */
   uint32_t sm_count = cqlcuda_sm_count();
@@ -953,6 +1401,8 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     /* the rows one accumulator takes: in the register form a warp's passes over the grid (32 lanes x
        rows_per_thread each), in the tile form a CTA's tiles (at most one SM's share of the rows and two
        tiles, whatever the CTAs per SM) */
+    /* (the cube form adds each row's summand to 128-bit cell totals, so any of these bounds serves it:
+       a query's sum is the same integer whether the cube or the register form answers it) */
     uint64_t warp_rows;
     if (rows_per_thread)
     {
@@ -968,14 +1418,13 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     col_shift[c] = 62 - e - wr;
     sum_mask |= 1u << c;
   }
-  /* the columns this batch loads */
-  uint32_t need = 0;
-  for (int c = 0; c < CQLOPS_MAX_BINDINGS; c++)
-    if (slot_type[c]) need |= 1u << c;
   /* what the launches compile: this batch's shapes, or the catalog's */
   uint32_t launch_shapes = shapes;
   char** launch_exprs = exprs;
   uint32_t* launch_sites = shape_sites;
+  uint32_t* launch_masks = shape_mask;
+  int* launch_shape_types = shape_types;
+  uint32_t* launch_shape_sums = shape_sums;
   int* launch_types = slot_type;
   uint32_t launch_sums = sum_mask;
   CatalogView* view = NULL;
@@ -983,12 +1432,16 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
   {
     view = (CatalogView*)malloc(sizeof(CatalogView));
     uint32_t index[BATCH_MAX_SHAPES];
-    if (view && catalog_map(catalog, shapes, exprs, shape_keys, shape_sites, slot_type, sum_mask, index, view))
+    if (view &&
+        catalog_map(catalog, shapes, exprs, shape_keys, shape_sites, shape_mask, shape_types, shape_sums, slot_type, sum_mask, index, view))
     {
       for (uint32_t q = 0; q < query_count; q++) shape_of[q] = index[shape_of[q]];
       launch_shapes = view->shapes;
       launch_exprs = view->exprs;
       launch_sites = view->sites;
+      launch_masks = view->masks;
+      launch_shape_types = view->types;
+      launch_shape_sums = view->sums;
       launch_types = view->slot_type;
       launch_sums = view->sum_mask;
     }
@@ -997,40 +1450,77 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
   uint32_t sum_col_count = 0;
   for (int c = 0; c < CQLOPS_MAX_BINDINGS; c++)
     if ((launch_sums >> c) & 1u) sum_cols[sum_col_count++] = c;
-  /* queries grouped by (launch) shape */
+  /* the cube plan over the launch shapes, and the queries it answers */
+  CubePlan* plan = NULL;
+  int cube_of[BATCH_MAX_SHAPES];
+  for (uint32_t sh = 0; sh < BATCH_MAX_SHAPES; sh++) cube_of[sh] = -1;
+  int cube_source_mode = mode == BATCH_CUBE_BUILD_SOURCE || mode == BATCH_CUBE_ANSWER_SOURCE;
+  if (ok && allow_cubes && (mode == BATCH_RUN || mode == BATCH_PREPARE || cube_source_mode))
+  {
+    plan = (CubePlan*)malloc(sizeof(CubePlan));
+    if (plan) cube_plan(launch_shapes, launch_masks, launch_shape_types, launch_shape_sums, columns, column_count, plan, cube_of);
+    if (plan && plan->cubes == 0)
+    {
+      free(plan);
+      plan = NULL;
+    }
+  }
+  uint32_t* cube_q = (uint32_t*)malloc(query_count * 4);
+  ok = ok && cube_q;
+  uint32_t cube_n = 0;
+  uint32_t need = 0, scan_sums = 0, cube_sums = 0;
+  for (uint32_t q = 0; ok && q < query_count; q++)
+  {
+    uint32_t bit = qsum[q] == 0xffffffffu ? 0u : 1u << qsum[q];
+    if (plan && cube_of[shape_of[q]] >= 0)
+    {
+      cube_q[cube_n++] = q;
+      cube_sums |= bit;
+    }
+    else
+    {
+      need |= launch_masks[shape_of[q]] | bit;
+      scan_sums |= bit;
+    }
+  }
+  uint32_t scan_n = query_count - cube_n;
+  /* the scan's queries grouped by (launch) shape */
   uint32_t* shape_count = (uint32_t*)calloc(launch_shapes + 1, 4);
   ok = ok && shape_count;
   if (ok)
   {
-    for (uint32_t q = 0; q < query_count; q++) shape_count[shape_of[q]]++;
+    for (uint32_t q = 0; q < query_count; q++)
+      if (!(plan && cube_of[shape_of[q]] >= 0)) shape_count[shape_of[q]]++;
     uint32_t* start = (uint32_t*)malloc((launch_shapes + 1) * 4);
     if (!start) ok = 0;
     else
     {
       uint32_t run = 0;
-      for (uint32_t s = 0; s < launch_shapes; s++)
+      for (uint32_t sh = 0; sh < launch_shapes; sh++)
       {
-        start[s] = run;
-        run += shape_count[s];
+        start[sh] = run;
+        run += shape_count[sh];
       }
-      for (uint32_t q = 0; q < query_count; q++) order[start[shape_of[q]]++] = q;
+      for (uint32_t q = 0; q < query_count; q++)
+        if (!(plan && cube_of[shape_of[q]] >= 0)) order[start[shape_of[q]]++] = q;
       free(start);
     }
   }
-  /* thresholds, literals and sums in shape order */
-  Thr* thr_o = ok ? (Thr*)malloc((size_t)query_count * BATCH_MAX_SITES * sizeof(Thr)) : NULL;
-  double* qc_o = ok ? (double*)malloc((size_t)query_count * BATCH_MAX_CONSTS * sizeof(double)) : NULL;
-  uint32_t* qs_o = ok ? (uint32_t*)malloc(query_count * 4) : NULL;
+  /* thresholds, literals and sums of the scan's queries in shape order */
+  uint32_t nalloc = scan_n ? scan_n : 1;
+  Thr* thr_o = ok ? (Thr*)malloc((size_t)nalloc * BATCH_MAX_SITES * sizeof(Thr)) : NULL;
+  double* qc_o = ok ? (double*)malloc((size_t)nalloc * BATCH_MAX_CONSTS * sizeof(double)) : NULL;
+  uint32_t* qs_o = ok ? (uint32_t*)malloc(nalloc * 4) : NULL;
   ok = ok && thr_o && qc_o && qs_o;
   if (ok)
-    for (uint32_t i = 0; i < query_count; i++)
+    for (uint32_t i = 0; i < scan_n; i++)
     {
       uint32_t q = order[i];
       memcpy(&thr_o[(uint64_t)i * BATCH_MAX_SITES], &thr[(uint64_t)q * BATCH_MAX_SITES], sizeof(Thr) * BATCH_MAX_SITES);
       memcpy(&qc_o[(uint64_t)i * BATCH_MAX_CONSTS], &qconst[(uint64_t)q * BATCH_MAX_CONSTS], sizeof(double) * BATCH_MAX_CONSTS);
       qs_o[i] = qsum[q];
     }
-  uint64_t* folded = ok && mode == BATCH_RUN ? (uint64_t*)malloc((size_t)query_count * 24) : NULL;
+  uint64_t* folded = ok && mode == BATCH_RUN ? (uint64_t*)malloc((size_t)nalloc * 24) : NULL;
   ok = ok && (folded || mode != BATCH_RUN);
   /* one launch per slice of at most CQL_BATCH_LAUNCH_QUERIES queries: its shapes (all of the catalog's,
      with a catalog) and where each starts */
@@ -1067,9 +1557,62 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
       }                                                                               \
     begin[ns] = (nq);                                                                 \
   } while (0)
-  if (ok && mode != BATCH_RUN)
+  /* the cube kernels (compiled or found in the cache) */
+  CqlKernel* cube_build[CUBE_MAX] = { NULL };
+  CqlKernel* cube_answer = NULL;
+  if (cube_source_mode)
   {
-    uint32_t nq = query_count < CQL_BATCH_LAUNCH_QUERIES ? query_count : CQL_BATCH_LAUNCH_QUERIES;
+    /* the cube kernels' sources, for a compile check (no device work) */
+    char* src = NULL;
+    if (ok && plan && mode == BATCH_CUBE_ANSWER_SOURCE) src = cube_answer_source(plan, launch_exprs, launch_sites, launch_shapes, cube_of);
+    else if (ok && plan && cube_pass < plan->passes) src = cube_build_source(plan, cube_pass, launch_types);
+    else if (ok && plan) refuse("no such table pass");
+    if (src)
+    {
+      uint64_t n = strlen(src);
+      if (src_len) *src_len = n;
+      if (src_out && src_cap) snprintf(src_out, src_cap, "%s", src);
+      ok = !(src_out && n + 1 > src_cap);
+    }
+    else
+    {
+      if (ok && !plan) refuse("no query of the batch can be answered from a cube");
+      ok = 0;
+    }
+    free(src);
+    if (out_shapes) *out_shapes = cube_n;
+    mode = BATCH_SOURCE + 100;   /* nothing below runs */
+    free(plan);
+    plan = NULL;
+  }
+  if (ok && plan)
+  {
+    char name[64];
+    for (uint32_t p = 0; ok && p < plan->passes; p++)
+    {
+      char* src = cube_build_source(plan, p, launch_types);
+      if (src)
+      {
+        snprintf(name, sizeof(name), "qk_cube_%016llx", (unsigned long long)fnv_str(src));
+        cube_build[p] = cqlcuda_kernel_alloc(name, strlen(name));
+        if (!cube_build[p]) cube_build[p] = cqlcuda_kernel_alloc_from_image(name, strlen(name), src, strlen(src));
+      }
+      free(src);
+      if (!cube_build[p]) ok = 0;
+    }
+    char* asrc = ok ? cube_answer_source(plan, launch_exprs, launch_sites, launch_shapes, cube_of) : NULL;
+    if (asrc)
+    {
+      snprintf(name, sizeof(name), "qk_cubea_%016llx", (unsigned long long)fnv_str(asrc));
+      cube_answer = cqlcuda_kernel_alloc(name, strlen(name));
+      if (!cube_answer) cube_answer = cqlcuda_kernel_alloc_from_image(name, strlen(name), asrc, strlen(asrc));
+    }
+    free(asrc);
+    if (!cube_answer) ok = 0;
+  }
+  if (ok && (mode == BATCH_SOURCE || mode == BATCH_PREPARE) && (scan_n || view))
+  {
+    uint32_t nq = scan_n < CQL_BATCH_LAUNCH_QUERIES ? scan_n : CQL_BATCH_LAUNCH_QUERIES;
     uint32_t ns;
     SLICE_SHAPES(0, nq, ns);
     char* src = launch_source(slice_exprs, slice_sites, ns, launch_types, sum_cols, sum_col_count, rows_per_thread);
@@ -1089,47 +1632,68 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
       ok = cqlcuda_kernel_alloc(name, nlen) || cqlcuda_kernel_alloc_from_image(name, nlen, src, strlen(src));
     }
     free(src);
-    if (out_shapes) *out_shapes = shapes;
   }
+  if (ok && (mode == BATCH_SOURCE || mode == BATCH_PREPARE) && out_shapes) *out_shapes = shapes;
   int launch = ok && mode == BATCH_RUN;
   /* one upload of every launch parameter: the scales (doubles at 0..), then their exponents (64-bit
-     integers at 16..), the thresholds, literals and summed columns in shape order, and each slice's shape
-     starts; each part on a 16-byte boundary */
-  uint32_t slices = (query_count + CQL_BATCH_LAUNCH_QUERIES - 1) / CQL_BATCH_LAUNCH_QUERIES;
+     integers at 16..), the scan's thresholds, literals and summed columns in shape order, each slice's shape
+     starts, then the cube queries' thresholds, literals and (shape, cube, summed column); each part on a
+     16-byte boundary */
+  uint32_t slices = (scan_n + CQL_BATCH_LAUNCH_QUERIES - 1) / CQL_BATCH_LAUNCH_QUERIES;
   const uint64_t off_thr = 256;
-  const uint64_t off_qc = off_thr + (uint64_t)query_count * BATCH_MAX_SITES * sizeof(Thr);
-  const uint64_t off_qs = off_qc + (uint64_t)query_count * BATCH_MAX_CONSTS * 8;
-  const uint64_t off_begin = off_qs + (((uint64_t)query_count * 4 + 15) & ~15ull);
+  const uint64_t off_qc = off_thr + (uint64_t)scan_n * BATCH_MAX_SITES * sizeof(Thr);
+  const uint64_t off_qs = off_qc + (uint64_t)scan_n * BATCH_MAX_CONSTS * 8;
+  const uint64_t off_begin = off_qs + (((uint64_t)scan_n * 4 + 15) & ~15ull);
   const uint64_t begin_stride = ((BATCH_MAX_SHAPES + 1) * 4 + 15) & ~15ull;
-  const uint64_t param_bytes = off_begin + (uint64_t)slices * begin_stride;
+  const uint64_t off_cthr = off_begin + (uint64_t)slices * begin_stride;
+  const uint64_t off_cqc = off_cthr + (uint64_t)cube_n * BATCH_MAX_SITES * sizeof(Thr);
+  const uint64_t off_cmeta = off_cqc + (uint64_t)cube_n * BATCH_MAX_CONSTS * 8;
+  const uint64_t param_bytes = off_cmeta + (((uint64_t)cube_n * 4 + 15) & ~15ull) + 16;
   unsigned char* params = launch ? (unsigned char*)calloc(1, param_bytes) : NULL;
   if (launch && !params) ok = 0;
   if (params)
   {
     memcpy(params, col_scale, sizeof(col_scale));
     memcpy(params + 128, col_shift, sizeof(col_shift));
-    memcpy(params + off_thr, thr_o, (size_t)query_count * BATCH_MAX_SITES * sizeof(Thr));
-    memcpy(params + off_qc, qc_o, (size_t)query_count * BATCH_MAX_CONSTS * 8);
-    memcpy(params + off_qs, qs_o, (size_t)query_count * 4);
+    memcpy(params + off_thr, thr_o, (size_t)scan_n * BATCH_MAX_SITES * sizeof(Thr));
+    memcpy(params + off_qc, qc_o, (size_t)scan_n * BATCH_MAX_CONSTS * 8);
+    memcpy(params + off_qs, qs_o, (size_t)scan_n * 4);
+    for (uint32_t i = 0; i < cube_n; i++)
+    {
+      uint32_t q = cube_q[i];
+      const Cube* cu = &plan->cube[cube_of[shape_of[q]]];
+      uint32_t j = 0;
+      while (j < cu->nsum && (uint32_t)cu->sum_slot[j] != qsum[q]) j++;
+      uint32_t meta = shape_of[q] | ((uint32_t)cube_of[shape_of[q]] << 8) | ((qsum[q] == 0xffffffffu || j == cu->nsum) ? 0u : (j + 1u) << 16);
+      memcpy(params + off_cthr + (uint64_t)i * BATCH_MAX_SITES * sizeof(Thr), &thr[(uint64_t)q * BATCH_MAX_SITES], BATCH_MAX_SITES * sizeof(Thr));
+      memcpy(params + off_cqc + (uint64_t)i * BATCH_MAX_CONSTS * 8, &qconst[(uint64_t)q * BATCH_MAX_CONSTS], BATCH_MAX_CONSTS * 8);
+      memcpy(params + off_cmeta + (uint64_t)i * 4, &meta, 4);
+    }
   }
   uint32_t per_sm = rows_per_thread ? BATCH_CTAS_PER_SM : tiled_layout(launch_types, sum_col_count).per_sm;
   uint64_t ctas = (uint64_t)(sm_count ? sm_count : 152) * per_sm;
-  uint32_t widest = query_count < CQL_BATCH_LAUNCH_QUERIES ? query_count : CQL_BATCH_LAUNCH_QUERIES;
+  uint32_t widest = scan_n < CQL_BATCH_LAUNCH_QUERIES ? scan_n : CQL_BATCH_LAUNCH_QUERIES;
+  const uint64_t cube_out_bytes = 16 + (uint64_t)cube_n * 24;   /* the error word, then (count, lo, hi) per cube query */
+  uint64_t* cube_out = launch && cube_n ? (uint64_t*)malloc(cube_out_bytes) : NULL;
+  if (launch && cube_n && !cube_out) ok = 0;
   CqlBuffer* param_buf = launch && ok ? pooled("batch_params", param_bytes, CQLCUDA_BUFFER_WRITE) : NULL;
-  CqlBuffer* out_buf = launch && ok ? pooled("batch_folded", (uint64_t)query_count * 24, CQLCUDA_BUFFER_READ_WRITE) : NULL;
-  CqlBuffer* parts = launch && ok ? pooled("batch_partials", ctas * widest * 24, CQLCUDA_BUFFER_READ_WRITE) : NULL;
-  CqlKernel* fold = launch ? cqlcuda_kernel_alloc("cql_batch_fold", 14) : NULL;
-  if (launch) ok = ok && param_buf && out_buf && parts && fold;
+  CqlBuffer* out_buf = launch && ok && scan_n ? pooled("batch_folded", (uint64_t)scan_n * 24, CQLCUDA_BUFFER_READ_WRITE) : NULL;
+  CqlBuffer* parts = launch && ok && scan_n ? pooled("batch_partials", ctas * widest * 24, CQLCUDA_BUFFER_READ_WRITE) : NULL;
+  CqlBuffer* tables = launch && ok && cube_n ? pooled("batch_cube_tables", plan->words * 8, CQLCUDA_BUFFER_READ_WRITE) : NULL;
+  CqlBuffer* cube_out_buf = launch && ok && cube_n ? pooled("batch_cube_out", cube_out_bytes, CQLCUDA_BUFFER_READ_WRITE) : NULL;
+  CqlKernel* fold = launch && scan_n ? cqlcuda_kernel_alloc("cql_batch_fold", 14) : NULL;
+  if (launch)
+    ok = ok && param_buf && (!scan_n || (out_buf && parts && fold)) && (!cube_n || (tables && cube_out_buf && cube_answer));
   launch = launch && ok;
   /* each slice's kernel, compiled (or found) before anything is queued; with a catalog one for all */
-  CqlKernel** kernels = launch ? (CqlKernel**)calloc(slices, sizeof(CqlKernel*)) : NULL;
-  uint32_t* slice_ns = launch ? (uint32_t*)calloc(slices, 4) : NULL;
+  CqlKernel** kernels = launch ? (CqlKernel**)calloc(slices ? slices : 1, sizeof(CqlKernel*)) : NULL;
+  uint32_t* slice_ns = launch ? (uint32_t*)calloc(slices ? slices : 1, 4) : NULL;
   if (launch && (!kernels || !slice_ns)) ok = 0;
-  CqlKernel* shared_k = NULL;   /* with a catalog every slice runs the same kernel */
+  CqlKernel* shared_k = NULL;
   for (uint32_t sl = 0; launch && ok && sl < slices; sl++)
   {
     uint32_t first = sl * CQL_BATCH_LAUNCH_QUERIES;
-    uint32_t nq = query_count - first < CQL_BATCH_LAUNCH_QUERIES ? query_count - first : CQL_BATCH_LAUNCH_QUERIES;
+    uint32_t nq = scan_n - first < CQL_BATCH_LAUNCH_QUERIES ? scan_n - first : CQL_BATCH_LAUNCH_QUERIES;
     uint32_t ns;
     SLICE_SHAPES(first, nq, ns);
     memcpy(params + off_begin + sl * begin_stride, begin, (ns + 1) * 4);
@@ -1159,20 +1723,44 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     kernels[sl] = k;
   }
 #undef SLICE_SHAPES
-  /* one batch: the upload, every slice's scan and fold, the read-back; one wait */
+  /* one batch: the upload, the cube pass and answers, every slice's scan and fold, the read-backs; one wait */
   if (launch && ok)
   {
-    CqlBatch* b = cqlcuda_batch_begin(param_bytes, (uint64_t)query_count * 24);
+    CqlBatch* b = cqlcuda_batch_begin(param_bytes, (uint64_t)scan_n * 24 + (cube_n ? cube_out_bytes : 0));
     cqlcuda_batch_buffer_write(b, param_buf, params, param_bytes);
+    if (cube_n)
+    {
+      cqlcuda_batch_buffer_zero(b, tables, plan->words * 8);
+      cqlcuda_batch_buffer_zero(b, cube_out_buf, 16);
+      for (uint32_t p = 0; p < plan->passes; p++)
+      {
+        CqlKernel* kb = cube_build[p];
+        cqlcuda_kernel_set_arg_buffer_range(kb, 0, param_buf, 0, 256);
+        cqlcuda_kernel_set_arg_buffer(kb, 1, tables);
+        cqlcuda_kernel_set_arg_buffer_range(kb, 2, cube_out_buf, 0, 16);
+        for (uint32_t c = 0; c < CQLOPS_MAX_BINDINGS; c++)
+          cqlcuda_kernel_set_arg_buffer(kb, 6 + c, columns[c < column_count ? c : 0].buffer);
+        cqlcuda_kernel_set_arg_u64(kb, 0, rows);
+        cqlcuda_kernel_set_arg_u64(kb, 1, cube_sums);
+        cqlcuda_batch_kernel_execute(b, kb, (uint32_t)((sm_count ? sm_count : 152) * CUBE_THREADS), CUBE_THREADS);
+      }
+      cqlcuda_kernel_set_arg_buffer(cube_answer, 1, tables);
+      cqlcuda_kernel_set_arg_buffer_range(cube_answer, 3, param_buf, off_cthr, off_cqc - off_cthr);
+      cqlcuda_kernel_set_arg_buffer_range(cube_answer, 4, param_buf, off_cqc, off_cmeta - off_cqc);
+      cqlcuda_kernel_set_arg_buffer_range(cube_answer, 5, param_buf, off_cmeta, (uint64_t)cube_n * 4);
+      cqlcuda_kernel_set_arg_buffer_range(cube_answer, 6, cube_out_buf, 16, (uint64_t)cube_n * 24);
+      cqlcuda_kernel_set_arg_u64(cube_answer, 0, cube_n);
+      cqlcuda_batch_kernel_execute(b, cube_answer, cube_n * 256u, 256u);
+    }
     for (uint32_t sl = 0; sl < slices; sl++)
     {
       uint32_t first = sl * CQL_BATCH_LAUNCH_QUERIES;
-      uint32_t nq = query_count - first < CQL_BATCH_LAUNCH_QUERIES ? query_count - first : CQL_BATCH_LAUNCH_QUERIES;
+      uint32_t nq = scan_n - first < CQL_BATCH_LAUNCH_QUERIES ? scan_n - first : CQL_BATCH_LAUNCH_QUERIES;
       CqlKernel* k = kernels[sl];
       cqlcuda_kernel_set_arg_buffer_range(k, 0, param_buf, 0, 256);
       cqlcuda_kernel_set_arg_buffer_range(k, 1, param_buf, off_thr, off_qc - off_thr);
       cqlcuda_kernel_set_arg_buffer_range(k, 2, param_buf, off_qc, off_qs - off_qc);
-      cqlcuda_kernel_set_arg_buffer_range(k, 3, param_buf, off_qs, (uint64_t)query_count * 4);
+      cqlcuda_kernel_set_arg_buffer_range(k, 3, param_buf, off_qs, (uint64_t)scan_n * 4);
       cqlcuda_kernel_set_arg_buffer_range(k, 4, param_buf, off_begin + sl * begin_stride, (slice_ns[sl] + 1) * 4);
       cqlcuda_kernel_set_arg_buffer_range(k, 5, parts, 0, ctas * nq * 24);
       for (uint32_t c = 0; c < CQLOPS_MAX_BINDINGS; c++)
@@ -1180,7 +1768,7 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
       cqlcuda_kernel_set_arg_u64(k, 0, rows);
       cqlcuda_kernel_set_arg_u64(k, 1, nq);
       cqlcuda_kernel_set_arg_u64(k, 2, first);
-      cqlcuda_kernel_set_arg_u64(k, 3, (uint64_t)need | (uint64_t)sum_mask << 32);
+      cqlcuda_kernel_set_arg_u64(k, 3, (uint64_t)need | (uint64_t)scan_sums << 32);
       cqlcuda_kernel_set_arg_buffer_range(fold, 0, parts, 0, ctas * nq * 24);
       cqlcuda_kernel_set_arg_buffer_range(fold, 1, out_buf, (uint64_t)first * 24, (uint64_t)nq * 24);
       cqlcuda_kernel_set_arg_u64(fold, 0, nq);
@@ -1189,7 +1777,8 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
       cqlcuda_batch_kernel_execute(b, k, (uint32_t)(ctas * QE_GPU_WORKGROUP_SIZE), QE_GPU_WORKGROUP_SIZE);
       cqlcuda_batch_kernel_execute(b, fold, nq, QE_GPU_WORKGROUP_SIZE);
     }
-    cqlcuda_batch_buffer_read(b, out_buf, folded, (uint64_t)query_count * 24);
+    if (scan_n) cqlcuda_batch_buffer_read(b, out_buf, folded, (uint64_t)scan_n * 24);
+    if (cube_n) cqlcuda_batch_buffer_read(b, cube_out_buf, cube_out, cube_out_bytes);
     ok = cqlcuda_batch_end(b);
   }
   free(params);
@@ -1197,11 +1786,26 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
   free(slice_ns);
   if (launch && ok)
   {
-    for (uint32_t i = 0; i < query_count; i++)
+    for (uint32_t i = 0; i < scan_n + cube_n; i++)
     {
-      uint32_t q = order[i];
-      uint64_t cnt = folded[i * 3], lo = folded[i * 3 + 1];
-      int64_t hi = (int64_t)folded[i * 3 + 2];
+      uint32_t q;
+      uint64_t cnt, lo;
+      int64_t hi;
+      if (i < scan_n)
+      {
+        q = order[i];
+        cnt = folded[i * 3];
+        lo = folded[i * 3 + 1];
+        hi = (int64_t)folded[i * 3 + 2];
+      }
+      else
+      {
+        uint32_t ci = i - scan_n;
+        q = cube_q[ci];
+        cnt = cube_out[2 + ci * 3];
+        lo = cube_out[2 + ci * 3 + 1];
+        hi = (int64_t)cube_out[2 + ci * 3 + 2];
+      }
       out_counts[q] = cnt;
       if (!out_sums) continue;
       if (qsum[q] == 0xffffffffu)
@@ -1214,11 +1818,41 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
       out_sums[q] = v / col_scale[qsum[q]];
     }
     if (out_shapes) *out_shapes = shapes;
+    /* a value outside its column's stated range left the cube pass: those queries run on the scan */
+    if (cube_n && (uint32_t)cube_out[0] != 0u)
+    {
+      const CqlProgram** sub = (const CqlProgram**)malloc(cube_n * sizeof(*sub));
+      int32_t* sub_sums = (int32_t*)malloc(cube_n * 4);
+      uint64_t* sub_counts = (uint64_t*)malloc(cube_n * 8);
+      double* sub_out = (double*)malloc(cube_n * 8);
+      ok = sub && sub_sums && sub_counts && sub_out;
+      for (uint32_t i = 0; ok && i < cube_n; i++)
+      {
+        sub[i] = programs[cube_q[i]];
+        sub_sums[i] = qsum[cube_q[i]] == 0xffffffffu ? -1 : (int32_t)qsum[cube_q[i]];
+      }
+      if (ok)
+        ok = batch_run(catalog, sub, cube_n, columns, column_count, sub_sums, rows_per_thread, sub_counts, sub_out, NULL, BATCH_RUN, NULL, 0,
+                       NULL, 0);
+      for (uint32_t i = 0; ok && i < cube_n; i++)
+      {
+        out_counts[cube_q[i]] = sub_counts[i];
+        if (out_sums) out_sums[cube_q[i]] = sub_out[i];
+      }
+      free(sub);
+      free(sub_sums);
+      free(sub_counts);
+      free(sub_out);
+    }
   }
   else if (!ok && why[0])
     refuse(why);
-  for (uint32_t s = 0; s < shapes; s++) free(exprs[s]);
+  for (uint32_t sh = 0; sh < shapes; sh++) free(exprs[sh]);
   free(view);
+  free(plan);
+  free(cube_q);
+  free(cube_out);
+  free(shape_types);
   free(rb);
   free(shape_of);
   free(order);
@@ -1238,7 +1872,7 @@ int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t qu
                                   uint32_t* out_shapes)
 {
   return batch_run(NULL, programs, query_count, columns, column_count, sum_columns, rows_per_thread, out_counts, out_sums, out_shapes,
-                   BATCH_RUN, NULL, 0, NULL);
+                   BATCH_RUN, NULL, 0, NULL, 1);
 }
 
 int cqlops_batch_filter_aggregate_cat(CqlBatchCatalog* catalog, const CqlProgram* const* programs, uint32_t query_count,
@@ -1246,19 +1880,26 @@ int cqlops_batch_filter_aggregate_cat(CqlBatchCatalog* catalog, const CqlProgram
                                       uint64_t* out_counts, double* out_sums, uint32_t* out_shapes)
 {
   return batch_run(catalog, programs, query_count, columns, column_count, sum_columns, rows_per_thread, out_counts, out_sums, out_shapes,
-                   BATCH_RUN, NULL, 0, NULL);
+                   BATCH_RUN, NULL, 0, NULL, 1);
 }
 
 int cqlops_batch_prepare(CqlBatchCatalog* catalog, const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns,
                          uint32_t column_count, const int32_t* sum_columns, uint32_t rows_per_thread)
 {
   return batch_run(catalog, programs, query_count, columns, column_count, sum_columns, rows_per_thread, NULL, NULL, NULL, BATCH_PREPARE,
-                   NULL, 0, NULL);
+                   NULL, 0, NULL, 1);
 }
 
 int cqlops_batch_source(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
                         const int32_t* sum_columns, uint32_t rows_per_thread, char* out, uint64_t cap, uint64_t* out_len, uint32_t* out_shapes)
 {
   return batch_run(NULL, programs, query_count, columns, column_count, sum_columns, rows_per_thread, NULL, NULL, out_shapes, BATCH_SOURCE, out,
-                   cap, out_len);
+                   cap, out_len, 0);
+}
+
+int cqlops_batch_cube_source(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
+                             const int32_t* sum_columns, uint32_t which, char* out, uint64_t cap, uint64_t* out_len, uint32_t* out_cube_queries)
+{
+  return batch_run(NULL, programs, query_count, columns, column_count, sum_columns, which ? which - 1 : 0, NULL, NULL, out_cube_queries,
+                   which ? BATCH_CUBE_BUILD_SOURCE : BATCH_CUBE_ANSWER_SOURCE, out, cap, out_len, 1);
 }

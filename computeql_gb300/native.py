@@ -176,6 +176,7 @@ OPS_API = [
     ("cqlops_zone_map_build", C.c_int, [P, P, u64]),
     ("cqlops_batch_filter_aggregate", C.c_int, [P, u32, P, u32, P, u32, P, P, P]),
     ("cqlops_batch_source", C.c_int, [P, u32, P, u32, P, u32, P, u64, P, P]),
+    ("cqlops_batch_cube_source", C.c_int, [P, u32, P, u32, P, u32, P, u64, P, P]),
     ("cqlops_batch_catalog_create", P, []),
     ("cqlops_batch_catalog_destroy", None, [P]),
     ("cqlops_batch_catalog_shapes", u32, [P]),

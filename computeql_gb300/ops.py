@@ -348,6 +348,25 @@ def batch_source(programs, sum_names, rows_per_thread=8):
     return buf.value.decode(), shapes.value
 
 
+def batch_cube_source(programs, sum_names, which):
+    """The cube kernels' source for these queries (which 0: the answers, 1 + p: table pass p), no device
+    work -> (source, queries the cube answers); raises when no query can be answered from a cube or there
+    is no such pass."""
+    q = len(programs)
+    base = programs[0]
+    ptrs = (C.c_void_p * q)(*[C.addressof(p.prog) for p in programs])
+    sc = np.array([base.index(n) if n is not None else -1 for n in sum_names], dtype=np.int32)
+    n = C.c_uint64()
+    nq = C.c_uint32()
+    lib = N.load_ops()
+    _check(lib.cqlops_batch_cube_source(ptrs, q, base._cols, len(base.columns), N.ptr(sc), which, None, 0, C.byref(n), C.byref(nq)),
+           "cqlops_batch_cube_source")
+    buf = C.create_string_buffer(n.value + 1)
+    _check(lib.cqlops_batch_cube_source(ptrs, q, base._cols, len(base.columns), N.ptr(sc), which, buf, n.value + 1, None, None),
+           "cqlops_batch_cube_source")
+    return buf.value.decode(), nq.value
+
+
 def fused_group(program, key_names, agg_names, max_groups=1 << 16):
     kc, ac = len(key_names), len(agg_names)
     keys = (C.c_uint32 * 3)(*[program.index(n) for n in key_names])

@@ -348,6 +348,16 @@ int cqlops_batch_filter_aggregate_cat(CqlBatchCatalog* catalog, const CqlProgram
 int cqlops_batch_prepare(CqlBatchCatalog* catalog, const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns,
                          uint32_t column_count, const int32_t* sum_columns, uint32_t rows_per_thread);
 
+/* The sources of the cube kernels cqlops_batch_filter_aggregate would compile for these queries (no
+   device work): which = 0 the answers, 1 + p table pass p (the cubes whose shared tables fit together
+   are built by one pass; 0 is returned past the last). Queries whose WHERE reads only whole-number
+   columns of small range (at most 4 columns, 65536 value combinations) are answered from a dense table of
+   the rows - per combination, the row count and the 128-bit fixed-point sums - built in one pass; each
+   such query tests its predicate on the combinations instead of the rows. out_cube_queries receives how
+   many queries the cube answers. Returns 0 when none can be. */
+int cqlops_batch_cube_source(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
+                             const int32_t* sum_columns, uint32_t which, char* out, uint64_t cap, uint64_t* out_len, uint32_t* out_cube_queries);
+
 /* The CUDA C++ source cqlops_batch_filter_aggregate would compile for its first launch (no device
    work), up to cap bytes into out (out_len receives the length). */
 int cqlops_batch_source(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,

@@ -61,3 +61,42 @@ def test_tile_form_sizes_its_shared_memory(ops):
     per_sm = int(head.split("per_sm=")[1].split()[0])
     assert "const u32 TILE = 512u" in src or "const u32 TILE = 1024u" in src
     assert smem <= 227 * 1024 and 1 <= per_sm <= 8 and per_sm * (smem + 1024) <= 227 * 1024
+
+
+def cube_columns(ops, rows=1000):
+    return {"region": ops.Column(ops.TYPE_U32, rows, zone=(0.0, 49.0)), "flag": ops.Column(ops.TYPE_U32, rows, zone=(0.0, 99.0)),
+            "status": ops.Column(ops.TYPE_I32, rows, zone=(-3.0, 5.0)), "amount": ops.Column(ops.TYPE_U32, rows, zone=(0.0, 9999.0)),
+            "v": ops.Column(ops.TYPE_F64, rows, zone=(0.0, 1e6))}
+
+
+def test_cube_sources_compile(ops):
+    """The cube kernels of a mixed batch NVRTC-compile for sm_103a: the answers and every table pass (the
+    {flag, region} table with two sums fills a pass of its own). Only the small-range integer shapes go to
+    the cube (the f64 comparison stays on the scan)."""
+    cols = cube_columns(ops)
+    qs = [("(< flag 7)", None), ("(= region 3)", "amount"), ("(and (< flag 9) (and (>= region 4) (< region 9)))", "v"),
+          ("(and (>= amount 100) (< amount 900))", None), ("(and (or (= region 1) (= region 2)) (>= flag 50))", "amount"),
+          ("(and (<= status 2) (> flag 10))", "status"), ("(> v 3.5)", "amount")]
+    progs = [ops.Program(w, cols) for w, _ in qs]
+    sums = [s for _, s in qs]
+    src, n = ops.batch_cube_source(progs, sums, 0)
+    assert n == 6
+    ok, log = ops.compile_check(src)
+    assert ok, log
+    passes = 0
+    while True:
+        try:
+            src, _ = ops.batch_cube_source(progs, sums, 1 + passes)
+        except ops.OpError:
+            break
+        ok, log = ops.compile_check(src)
+        assert ok, log
+        passes += 1
+    assert passes == 2
+
+
+def test_no_cube_for_wide_or_float_columns(ops):
+    cols = cube_columns(ops)
+    progs = [ops.Program(w, cols) for w in ("(> v 3.5)", "(< v 1.0)")]
+    with pytest.raises(ops.OpError):
+        ops.batch_cube_source(progs, [None, None], 0)
