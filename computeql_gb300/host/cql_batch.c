@@ -712,6 +712,7 @@ static char* batch_source_tiled(char** shape_exprs, const uint32_t* shape_sites,
 #define CUBE_MAX_CELLS 65536u
 #define CUBE_SMEM_BYTES (200u * 1024u)
 #define CUBE_THREADS 1024u
+#define CUBE_MIN_QUERIES 6u
 
 typedef struct
 {
@@ -924,6 +925,7 @@ static char* cube_build_source(const CubePlan* P, uint32_t pass, const int* slot
   bput(&b,
        "extern \"C\" __global__ void __launch_bounds__(%u) cql_main(CqlLaunch a)\n{\n"
        "  const u64 rows = cql_word(a, 0); const u32 need_sum = cql_word(a, 2); (void)need_sum;\n"
+       "  const u32 cube_need = cql_word(a, 4), load_need = cql_word(a, 6); (void)cube_need; (void)load_need;   /* the cubes this batch asks for, their columns */\n"
        "  const double* col_scale = (const double*)a.buf[0]; const long long* col_shift = (const long long*)a.buf[0] + 16;\n"
        "  (void)col_scale; (void)col_shift;\n"
        "  u64* g = (u64*)a.buf[1]; u32* err = (u32*)a.buf[2];\n"
@@ -943,19 +945,21 @@ static char* cube_build_source(const CubePlan* P, uint32_t pass, const int* slot
     if (type_bytes(t) == 8)
       bput(&b,
            "    u64 v%d[4];\n"
-           "    if (valid == 4u) { uint4 x = cql_ld4((const u64*)a.buf[%d] + row0); uint4 y = cql_ld4((const u64*)a.buf[%d] + row0 + 2);\n"
+           "    if (!((load_need >> %d) & 1u)) { for (u32 j = 0; j < 4u; j++) v%d[j] = 0ull; }\n"
+           "    else if (valid == 4u) { uint4 x = cql_ld4((const u64*)a.buf[%d] + row0); uint4 y = cql_ld4((const u64*)a.buf[%d] + row0 + 2);\n"
            "      v%d[0] = ((u64)x.y << 32) | x.x; v%d[1] = ((u64)x.w << 32) | x.z; v%d[2] = ((u64)y.y << 32) | y.x; v%d[3] = ((u64)y.w << 32) | y.z; }\n"
            "    else { for (u32 j = 0; j < 4u; j++) v%d[j] = j < valid ? ((const u64*)a.buf[%d])[row0 + j] : 0ull; }\n",
-           s, 6 + s, 6 + s, s, s, s, s, s, 6 + s);
+           s, s, s, 6 + s, 6 + s, s, s, s, s, s, 6 + s);
     else if (type_bytes(t) == 1)
-      bput(&b, "    u32 v%d[4];\n    for (u32 j = 0; j < 4u; j++) v%d[j] = j < valid ? (u32)((const unsigned char*)a.buf[%d])[row0 + j] : 0u;\n", s, s,
-           6 + s);
+      bput(&b, "    u32 v%d[4];\n    for (u32 j = 0; j < 4u; j++) v%d[j] = j < valid && ((load_need >> %d) & 1u) ? (u32)((const unsigned char*)a.buf[%d])[row0 + j] : 0u;\n",
+           s, s, s, 6 + s);
     else
       bput(&b,
            "    u32 v%d[4];\n"
-           "    if (valid == 4u) { uint4 x = cql_ld4((const u32*)a.buf[%d] + row0); v%d[0] = x.x; v%d[1] = x.y; v%d[2] = x.z; v%d[3] = x.w; }\n"
+           "    if (!((load_need >> %d) & 1u)) { for (u32 j = 0; j < 4u; j++) v%d[j] = 0u; }\n"
+           "    else if (valid == 4u) { uint4 x = cql_ld4((const u32*)a.buf[%d] + row0); v%d[0] = x.x; v%d[1] = x.y; v%d[2] = x.z; v%d[3] = x.w; }\n"
            "    else { for (u32 j = 0; j < 4u; j++) v%d[j] = j < valid ? ((const u32*)a.buf[%d])[row0 + j] : 0u; }\n",
-           s, 6 + s, s, s, s, s, s, 6 + s);
+           s, s, s, 6 + s, s, s, s, s, s, 6 + s);
   }
   /* the summands, once per row */
   uint32_t summed = 0;
@@ -980,7 +984,7 @@ static char* cube_build_source(const CubePlan* P, uint32_t pass, const int* slot
   {
     const Cube* cu = &P->cube[c];
     if (cu->pass != pass) continue;
-    bput(&b, "      {\n        u32 cell = 0u; bool in = true;\n");
+    bput(&b, "      if ((cube_need >> %uu) & 1u)\n      {\n        u32 cell = 0u; bool in = true;\n", c);
     for (uint32_t d = 0; d < cu->dims; d++)
     {
       if (cu->is_signed[d]) bput(&b, "        { const u32 x = (u32)((int)v%d[j] - (int)%du); in = in && x < %uu; cell += x * %uu; }\n", cu->slot[d], cu->min[d], cu->radix[d], cu->stride[d]);
@@ -1465,10 +1469,22 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
       plan = NULL;
     }
   }
+  /* a table pass costs about as much as a handful of queries on the scan (it reads the cubes' columns
+     and adds every row to each table): fewer cube-answerable queries than CUBE_MIN_QUERIES stay on the scan */
+  if (plan && mode == BATCH_RUN)
+  {
+    uint32_t answerable = 0;
+    for (uint32_t q = 0; q < query_count; q++) answerable += cube_of[shape_of[q]] >= 0;
+    if (answerable < CUBE_MIN_QUERIES)
+    {
+      free(plan);
+      plan = NULL;
+    }
+  }
   uint32_t* cube_q = (uint32_t*)malloc(query_count * 4);
   ok = ok && cube_q;
   uint32_t cube_n = 0;
-  uint32_t need = 0, scan_sums = 0, cube_sums = 0;
+  uint32_t need = 0, scan_sums = 0, cube_sums = 0, cube_need = 0, cube_load = 0;
   for (uint32_t q = 0; ok && q < query_count; q++)
   {
     uint32_t bit = qsum[q] == 0xffffffffu ? 0u : 1u << qsum[q];
@@ -1476,6 +1492,8 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     {
       cube_q[cube_n++] = q;
       cube_sums |= bit;
+      cube_need |= 1u << cube_of[shape_of[q]];
+      cube_load |= plan->cube[cube_of[shape_of[q]]].mask | bit;
     }
     else
     {
@@ -1734,6 +1752,9 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
       cqlcuda_batch_buffer_zero(b, cube_out_buf, 16);
       for (uint32_t p = 0; p < plan->passes; p++)
       {
+        int wanted = 0;
+        for (uint32_t c = 0; c < plan->cubes; c++) wanted |= plan->cube[c].pass == p && ((cube_need >> c) & 1u);
+        if (!wanted) continue;   /* no query of the batch reads this pass's cubes */
         CqlKernel* kb = cube_build[p];
         cqlcuda_kernel_set_arg_buffer_range(kb, 0, param_buf, 0, 256);
         cqlcuda_kernel_set_arg_buffer(kb, 1, tables);
@@ -1742,6 +1763,8 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
           cqlcuda_kernel_set_arg_buffer(kb, 6 + c, columns[c < column_count ? c : 0].buffer);
         cqlcuda_kernel_set_arg_u64(kb, 0, rows);
         cqlcuda_kernel_set_arg_u64(kb, 1, cube_sums);
+        cqlcuda_kernel_set_arg_u64(kb, 2, cube_need);
+        cqlcuda_kernel_set_arg_u64(kb, 3, cube_load);
         cqlcuda_batch_kernel_execute(b, kb, (uint32_t)((sm_count ? sm_count : 152) * CUBE_THREADS), CUBE_THREADS);
       }
       cqlcuda_kernel_set_arg_buffer(cube_answer, 1, tables);

@@ -120,6 +120,16 @@ def test_cube_and_scan_give_the_same_integers(env):
             assert abs(sums[i] - fs[0]) <= 1e-12 * max(abs(fs[0]), 1.0), w
 
 
+def test_few_queries_stay_on_the_scan(env):
+    """Below six cube-answerable queries a table pass would cost more than the scan: the scan answers."""
+    ops, arrays, cols = env
+    qs = [("(< flag 7)", None), ("(= region 3)", "amount"), ("(and (>= amount 10) (< amount 900))", None)]
+    progs = [ops.Program(w, cols) for w, _ in qs]
+    counts, sums, prof = _run(ops, progs, [s for _, s in qs])
+    assert not any(k.startswith("qk_cube") for k in prof), prof
+    _check(arrays, progs, qs, counts, sums)
+
+
 def test_catalog_batches_reuse_the_cube_kernels(env):
     ops, arrays, cols = env
     from computeql_gb300 import native
@@ -148,7 +158,7 @@ def test_values_outside_the_stated_range_fall_back_to_the_scan(env):
     narrow = ops.Column(ops.TYPE_U32, ROWS, cols["region"].buffer, zone=(0.0, 39.0), zone_map=False)   # the data reach 49
     table = dict(cols)
     table["region"] = narrow
-    qs = [(f"(= region {r})", None) for r in (3, 41, 47)] + [("(< region 45)", "amount")]
+    qs = [(f"(= region {r})", None) for r in (3, 41, 47, 12, 25, 39, 44)] + [("(< region 45)", "amount")]
     progs = [ops.Program(w, table) for w, _ in qs]
     counts, sums, prof = _run(ops, progs, [s for _, s in qs])
     assert any(k.startswith("qk_cube_") for k in prof)
