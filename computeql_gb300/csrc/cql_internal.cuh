@@ -42,6 +42,7 @@ extern const CqlKernelDesc cql_kernels_hash[];
 extern const CqlKernelDesc cql_kernels_join[];
 extern const CqlKernelDesc cql_kernels_sort[];
 extern const CqlKernelDesc cql_kernels_fixed[];
+extern const CqlKernelDesc cql_kernels_window[];
 
 // Device facts the launchers size grids by (set once by cqlcuda_init).
 extern int g_cql_sm_count;

@@ -753,7 +753,8 @@ extern "C" void* cqlcuda_buffer_device_pointer(const CqlBuffer* b) { return b ? 
 
 static const CqlKernelDesc* find_builtin(const std::string& name)
 {
-  const CqlKernelDesc* tables[] = { cql_kernels_aggregate, cql_kernels_scan, cql_kernels_hash, cql_kernels_join, cql_kernels_sort, cql_kernels_fixed };
+  const CqlKernelDesc* tables[] = { cql_kernels_aggregate, cql_kernels_scan, cql_kernels_hash, cql_kernels_join, cql_kernels_sort, cql_kernels_fixed,
+                                    cql_kernels_window };
   for (const CqlKernelDesc* t : tables)
   {
     for (const CqlKernelDesc* d = t; d->name; d++)

@@ -35,24 +35,32 @@ static int key_bytes(uint32_t type)
   }
 }
 
-int cqlops_sort_rows(const CqlColumn* keys, uint32_t key_count, const uint32_t* desc, CqlBuffer* selection,
-                     uint64_t selection_count, uint32_t* out_rows, uint64_t out_capacity)
+/* The sort's checks and scratch; 0 (with the reason noted) when the keys cannot be sorted. */
+static int sort_check(const CqlColumn* keys, uint32_t key_count, CqlBuffer* selection, uint64_t selection_count, uint64_t* out_n)
 {
-  cqlops_note_error("");
   if (key_count == 0 || key_count > 4) return refuse("1 to 4 sort keys");
   uint64_t rows = keys[0].rows;
   uint64_t n = selection ? selection_count : rows;
   if (rows >= 0xffffffffull || n >= 0xffffffffull) return refuse("row count out of range");
-  uint32_t widest = 4;
   for (uint32_t k = 0; k < key_count; k++)
   {
     int narrow_ok = keys[k].width == 0 || (keys[k].width <= 3 && key_bytes(keys[k].type) == 4 && keys[k].type != CQLOPS_TYPE_F32);
     if (keys[k].rows != rows || (!keys[k].buffer && keys[k].width != 3) || !narrow_ok || !key_bytes(keys[k].type))
       return refuse("sort keys are numeric columns of the same length (narrow encodings only for 32-bit integers)");
-    if (key_bytes(keys[k].type) > (int)widest) widest = 8;
   }
   if (selection && cqlcuda_buffer_size(selection) < n * 4) return refuse("selection buffer smaller than its count");
-  if (n == 0) return 1;
+  *out_n = n;
+  return 1;
+}
+
+/* Queues the stable LSD radix sort of n > 0 rows into batch b; *out_sorted receives the buffer that holds
+   the row numbers in sorted order when the batch has run. */
+static int sort_enqueue(CqlBatch* b, const CqlColumn* keys, uint32_t key_count, const uint32_t* desc, CqlBuffer* selection, uint64_t n,
+                        CqlBuffer** out_sorted)
+{
+  uint32_t widest = 4;
+  for (uint32_t k = 0; k < key_count; k++)
+    if (key_bytes(keys[k].type) > (int)widest) widest = 8;
   uint64_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
   uint64_t hist_n = tiles * 256;
   CqlBuffer* perm[2] = { pooled("sort_perm_a", n * 4, CQLCUDA_BUFFER_READ_WRITE), pooled("sort_perm_b", n * 4, CQLCUDA_BUFFER_READ_WRITE) };
@@ -69,7 +77,6 @@ int cqlops_sort_rows(const CqlColumn* keys, uint32_t key_count, const uint32_t* 
     return 0;
   CqlBuffer* sel = selection ? selection : perm[0];
   int cur = 0;
-  CqlBatch* b = cqlcuda_batch_begin(0, n * 4);
   for (int k = (int)key_count - 1; k >= 0; k--)
   {
     int kb = key_bytes(keys[k].type);
@@ -120,7 +127,97 @@ int cqlops_sort_rows(const CqlColumn* keys, uint32_t key_count, const uint32_t* 
       cur ^= 1;
     }
   }
+  *out_sorted = perm[cur];
+  return 1;
+}
+
+int cqlops_sort_rows(const CqlColumn* keys, uint32_t key_count, const uint32_t* desc, CqlBuffer* selection,
+                     uint64_t selection_count, uint32_t* out_rows, uint64_t out_capacity)
+{
+  cqlops_note_error("");
+  uint64_t n = 0;
+  if (!sort_check(keys, key_count, selection, selection_count, &n)) return 0;
+  if (n == 0) return 1;
+  CqlBatch* b = cqlcuda_batch_begin(0, n * 4);
+  CqlBuffer* sorted = NULL;
+  if (!sort_enqueue(b, keys, key_count, desc, selection, n, &sorted))
+  {
+    cqlcuda_batch_end(b);
+    return 0;
+  }
   uint64_t m = n < out_capacity ? n : out_capacity;
-  if (out_rows && m) cqlcuda_batch_buffer_read(b, perm[cur], out_rows, m * 4);
+  if (out_rows && m) cqlcuda_batch_buffer_read(b, sorted, out_rows, m * 4);
+  return cqlcuda_batch_end(b);
+}
+
+/* ROW_NUMBER, RANK and DENSE_RANK (qe_window_rank_gpu, src/query_exec/query_exec.c:6155-6540): the rows
+   sorted by (partition keys, order keys) with the sort above, then per sorted position whether it starts a
+   partition or a peer group (keys compared as F64 with !=, window_rank_flags.comp), then the three ranks by
+   one scan over the positions - all in one batch. */
+#define WIN_TILE 2048u
+#define WIN_AGG_BYTES 24u
+
+int cqlops_window_rank(const CqlColumn* keys, uint32_t key_count, const uint32_t* desc, uint32_t partition_key_count, CqlBuffer* selection,
+                       uint64_t selection_count, uint32_t* out_rows, uint32_t* out_row_number, uint32_t* out_rank, uint32_t* out_dense_rank,
+                       uint64_t out_capacity)
+{
+  cqlops_note_error("");
+  uint64_t n = 0;
+  if (partition_key_count > key_count) return refuse("more partition keys than keys");
+  if (!sort_check(keys, key_count, selection, selection_count, &n)) return 0;
+  if (n == 0) return 1;
+  if (out_capacity < n) return refuse("the outputs must hold every row");
+  uint64_t tiles = (n + WIN_TILE - 1) / WIN_TILE;
+  CqlBuffer* flags = pooled("window_flags", n, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* agg = pooled("window_tiles", tiles * WIN_AGG_BYTES, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* carry = pooled("window_carry", tiles * WIN_AGG_BYTES, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* ranks = pooled("window_ranks", n * 12, CQLCUDA_BUFFER_READ_WRITE);
+  CqlKernel* kflags = cqlcuda_kernel_alloc("cql_window_flags", 16);
+  CqlKernel* ktiles = cqlcuda_kernel_alloc("cql_window_tiles", 16);
+  CqlKernel* kcarry = cqlcuda_kernel_alloc("cql_window_carry", 16);
+  CqlKernel* kapply = cqlcuda_kernel_alloc("cql_window_apply", 16);
+  if (!flags || !agg || !carry || !ranks || !kflags || !ktiles || !kcarry || !kapply) return 0;
+  CqlBatch* b = cqlcuda_batch_begin(0, n * 16);
+  CqlBuffer* sorted = NULL;
+  if (!sort_enqueue(b, keys, key_count, desc, selection, n, &sorted))
+  {
+    cqlcuda_batch_end(b);
+    return 0;
+  }
+  uint32_t types = 0, widths = 0;
+  for (uint32_t k = 0; k < key_count; k++)
+  {
+    types |= (keys[k].type & 0xffu) << (8 * k);
+    widths |= (keys[k].width & 0xffu) << (8 * k);
+  }
+  cqlcuda_kernel_set_arg_buffer(kflags, 0, sorted);
+  cqlcuda_kernel_set_arg_buffer(kflags, 1, flags);
+  for (uint32_t k = 0; k < 4; k++)
+    cqlcuda_kernel_set_arg_buffer(kflags, 2 + k, k < key_count && keys[k].buffer ? keys[k].buffer : sorted);
+  cqlcuda_kernel_set_arg_u64(kflags, 0, n);
+  cqlcuda_kernel_set_arg_u64(kflags, 1, (uint64_t)key_count | (uint64_t)partition_key_count << 32);
+  cqlcuda_kernel_set_arg_u64(kflags, 2, (uint64_t)types | (uint64_t)widths << 32);
+  cqlcuda_kernel_set_arg_u64(kflags, 3, (uint64_t)(key_count > 0 ? keys[0].base : 0) | (uint64_t)(key_count > 1 ? keys[1].base : 0) << 32);
+  cqlcuda_kernel_set_arg_u64(kflags, 4, (uint64_t)(key_count > 2 ? keys[2].base : 0) | (uint64_t)(key_count > 3 ? keys[3].base : 0) << 32);
+  cqlcuda_batch_kernel_execute(b, kflags, (uint32_t)n, QE_GPU_WORKGROUP_SIZE);
+  cqlcuda_kernel_set_arg_buffer(ktiles, 0, flags);
+  cqlcuda_kernel_set_arg_buffer(ktiles, 1, agg);
+  cqlcuda_kernel_set_arg_u64(ktiles, 0, n);
+  cqlcuda_batch_kernel_execute(b, ktiles, (uint32_t)(tiles * QE_GPU_WORKGROUP_SIZE), QE_GPU_WORKGROUP_SIZE);
+  cqlcuda_kernel_set_arg_buffer(kcarry, 0, agg);
+  cqlcuda_kernel_set_arg_buffer(kcarry, 1, carry);
+  cqlcuda_kernel_set_arg_u64(kcarry, 0, tiles);
+  cqlcuda_batch_kernel_execute(b, kcarry, QE_GPU_WORKGROUP_SIZE, QE_GPU_WORKGROUP_SIZE);
+  cqlcuda_kernel_set_arg_buffer(kapply, 0, flags);
+  cqlcuda_kernel_set_arg_buffer(kapply, 1, carry);
+  cqlcuda_kernel_set_arg_buffer_range(kapply, 2, ranks, 0, n * 4);
+  cqlcuda_kernel_set_arg_buffer_range(kapply, 3, ranks, n * 4, n * 4);
+  cqlcuda_kernel_set_arg_buffer_range(kapply, 4, ranks, n * 8, n * 4);
+  cqlcuda_kernel_set_arg_u64(kapply, 0, n);
+  cqlcuda_batch_kernel_execute(b, kapply, (uint32_t)(tiles * QE_GPU_WORKGROUP_SIZE), QE_GPU_WORKGROUP_SIZE);
+  if (out_rows) cqlcuda_batch_buffer_read(b, sorted, out_rows, n * 4);
+  if (out_row_number) cqlcuda_batch_buffer_read_at(b, ranks, 0, out_row_number, n * 4);
+  if (out_rank) cqlcuda_batch_buffer_read_at(b, ranks, n * 4, out_rank, n * 4);
+  if (out_dense_rank) cqlcuda_batch_buffer_read_at(b, ranks, n * 8, out_dense_rank, n * 4);
   return cqlcuda_batch_end(b);
 }

@@ -172,6 +172,7 @@ OPS_API = [
     ("cqlops_hash_join", C.c_int, [P, P, C.c_int, u64, P, P, u64]),
     ("cqlops_join_aggregate", C.c_int, [P, u64, P, P, P, P]),
     ("cqlops_sort_rows", C.c_int, [P, u32, P, P, u64, P, u64]),
+    ("cqlops_window_rank", C.c_int, [P, u32, P, u32, P, u64, P, P, P, P, u64]),
     ("cqlops_fixed_scale", C.c_int, [P, P, u64, P, P]),
     ("cqlops_zone_map_build", C.c_int, [P, P, u64]),
     ("cqlops_batch_filter_aggregate", C.c_int, [P, u32, P, u32, P, u32, P, P, P]),

@@ -480,6 +480,23 @@ def sort_rows(keys, desc=None, selection=None, count=None):
     return out[:n]
 
 
+def window_rank(keys, desc=None, partitions=0, selection=None, count=None):
+    """ROW_NUMBER / RANK / DENSE_RANK over (PARTITION BY keys[:partitions] ORDER BY keys[partitions:])
+    -> dict of u32 arrays in window order: rows, row_number, rank, dense_rank."""
+    k = len(keys)
+    structs = (N.CqlColumn * k)(*[c.c() for c in keys])
+    d = np.array(desc if desc is not None else [0] * k, dtype=np.uint32)
+    if selection is not None:
+        n = selection.nbytes // 4 if count is None else count
+    else:
+        n = keys[0].rows
+    out = {name: np.empty(max(n, 1), dtype=np.uint32) for name in ("rows", "row_number", "rank", "dense_rank")}
+    _check(N.load_ops().cqlops_window_rank(structs, k, N.ptr(d), partitions, selection.handle if selection is not None else None, n,
+                                           N.ptr(out["rows"]), N.ptr(out["row_number"]), N.ptr(out["rank"]), N.ptr(out["dense_rank"]),
+                                           max(n, 1)), "cqlops_window_rank")
+    return {name: a[:n] for name, a in out.items()}
+
+
 def fixed_scale(column, selection=None, count=None):
     """-> (scale or -1, largest magnitude): the decimal places every value needs (at most 6)."""
     n = column.rows if selection is None else (selection.nbytes // 4 if count is None else count)

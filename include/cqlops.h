@@ -313,6 +313,18 @@ int cqlops_group_dense_fixed(const CqlColumn* key, uint32_t expr_count, const ui
 int cqlops_sort_rows(const CqlColumn* keys, uint32_t key_count, const uint32_t* desc, CqlBuffer* selection,
                      uint64_t selection_count, uint32_t* out_rows, uint64_t out_capacity);
 
+/* ROW_NUMBER, RANK and DENSE_RANK over (PARTITION BY the first partition_key_count keys ORDER BY the
+   rest) - qe_window_rank_gpu, src/query_exec/query_exec.c:6155-6540. The rows (or the selection's, as for
+   cqlops_sort_rows) are ordered by all the keys as cqlops_sort_rows orders them; a position starts a
+   partition when a partition key differs from the previous position's and a peer group when any key
+   differs (keys compared as F64 with !=, window_rank_flags.comp). Per sorted position: out_rows the row
+   number, out_row_number the position within its partition (from 1), out_rank 1 + the position of its
+   peer group's first row within the partition, out_dense_rank the count of peer groups up to it in the
+   partition. Every output (any may be NULL) must hold all the rows. */
+int cqlops_window_rank(const CqlColumn* keys, uint32_t key_count, const uint32_t* desc, uint32_t partition_key_count, CqlBuffer* selection,
+                       uint64_t selection_count, uint32_t* out_rows, uint32_t* out_row_number, uint32_t* out_rank, uint32_t* out_dense_rank,
+                       uint64_t out_capacity);
+
 /* Q filter/aggregate queries over one table in one shared scan: SELECT COUNT(*), SUM(col) WHERE
    <programs[q]> for q = 0 .. query_count-1 - the batched form of cqlops_fused_filter_aggregate
    (qe_fused_filter_aggregate, query_exec.c:9888-10254). Every program is built over `columns` (numeric,

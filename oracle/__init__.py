@@ -67,6 +67,8 @@ def lib():
         L.orc_tdigest_percentile.restype = dbl
         L.orc_sort_rows.argtypes = [P, u32, P, u64, P]
         L.orc_sort_rows.restype = C.c_int
+        L.orc_window_rank.argtypes = [P, u32, P, u32, u64, P, P, P, P]
+        L.orc_window_rank.restype = C.c_int
         L.orc_join_aggregate.argtypes = [P, P, u64, P, P, u64, u32, P, P]
         L.orc_join_aggregate.restype = C.c_int
         L.orc_fixed_scale.argtypes = [P, u64, P, P]
@@ -206,6 +208,18 @@ def sort_rows(keys, desc=None):
     if not lib().orc_sort_rows(_p(k), len(keys), _p(d), rows, _p(out)):
         raise MemoryError("orc_sort_rows")
     return out[:rows]
+
+
+def window_rank(keys, desc=None, partitions=0):
+    """ROW_NUMBER / RANK / DENSE_RANK in window order -> (rows, row_number, rank, dense_rank)."""
+    rows = len(keys[0])
+    k = np.ascontiguousarray(np.stack([np.asarray(x).astype(np.float64) for x in keys]))
+    d = np.array(desc if desc is not None else [0] * len(keys), dtype=np.uint32)
+    out = np.empty(max(rows, 1), dtype=np.uint64)
+    rn, rk, dr = (np.empty(max(rows, 1), dtype=np.uint32) for _ in range(3))
+    if not lib().orc_window_rank(_p(k), len(keys), _p(d), partitions, rows, _p(out), _p(rn), _p(rk), _p(dr)):
+        raise MemoryError("orc_window_rank")
+    return out[:rows], rn[:rows], rk[:rows], dr[:rows]
 
 
 def join_aggregate(fact_key, fact_arg, dim_key, dim_group, groups):

@@ -105,6 +105,8 @@ uint64_t orc_group_cpu_reduce(const uint32_t* key, uint64_t rows, uint32_t expr_
 /* ORDER BY over key_count F64 key columns laid out key-major (keys[k * rows + i]); desc[k] != 0 for DESC.
    Writes the row numbers in order, ties by position (query_exec.c:4859-4940). */
 int orc_sort_rows(const double* keys, uint32_t key_count, const uint32_t* desc, uint64_t rows, uint64_t* out);
+int orc_window_rank(const double* keys, uint32_t key_count, const uint32_t* desc, uint32_t partition_count, uint64_t rows, uint64_t* out_rows,
+                    uint32_t* row_number, uint32_t* rank, uint32_t* dense_rank);
 
 /* SELECT group, COUNT(*), SUM(fact_arg) over fact JOIN dim ON fact_key = dim_key, dim_group[d] the
    group of dimension row d (0xffffffff = the row is filtered out); fact_arg may be NULL. */

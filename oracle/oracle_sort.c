@@ -49,3 +49,44 @@ int orc_sort_rows(const double* keys, uint32_t key_count, const uint32_t* desc, 
   free(buf);
   return 1;
 }
+
+/* ROW_NUMBER / RANK / DENSE_RANK as the reference computes them (qe_window_rank_gpu,
+   src/query_exec/query_exec.c:6155-6216 and window_rank_flags.comp): the rows in the ORDER BY order
+   above, a position starting a partition when a partition key differs from the previous row's and a peer
+   group when any key differs (F64 !=), then one pass: row number from the partition start, rank from the
+   peer group's start, dense rank counting peer groups. */
+int orc_window_rank(const double* keys, uint32_t key_count, const uint32_t* desc, uint32_t partition_count, uint64_t rows, uint64_t* out_rows,
+                    uint32_t* row_number, uint32_t* rank, uint32_t* dense_rank)
+{
+  if (!orc_sort_rows(keys, key_count, desc, rows, out_rows)) return 0;
+  uint64_t part_start = 0, peer_start = 0;
+  uint32_t dense = 0;
+  for (uint64_t i = 0; i < rows; i++)
+  {
+    int new_part = i == 0, new_peer = i == 0;
+    for (uint32_t k = 0; i > 0 && k < key_count; k++)
+    {
+      double a = keys[(uint64_t)k * rows + out_rows[i - 1]], b = keys[(uint64_t)k * rows + out_rows[i]];
+      if (a != b)
+      {
+        new_peer = 1;
+        if (k < partition_count) new_part = 1;
+      }
+    }
+    if (new_part)
+    {
+      part_start = i;
+      peer_start = i;
+      dense = 1;
+    }
+    else if (new_peer)
+    {
+      peer_start = i;
+      dense += 1;
+    }
+    row_number[i] = (uint32_t)(i - part_start + 1);
+    rank[i] = (uint32_t)(peer_start - part_start + 1);
+    dense_rank[i] = dense;
+  }
+  return 1;
+}
