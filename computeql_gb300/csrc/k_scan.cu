@@ -347,7 +347,9 @@ static int launch_scan_simple(const CqlLaunch& a, uint32_t gws, uint32_t lws, cu
 // opcodes of src/query_exec/query_exec.h:58-81 over a double stack of 8, one row per thread, the
 // instruction pointer and the step count bounded by the program length. It runs only for shapes a
 // per-query kernel could not be built for. Trigram similarity and edit distance are not evaluated
-// (the operator layer keeps scored programs off the GPU path).
+// The fuzzy comparisons SIMILARITY (trigram similarity) and EDIT_DISTANCE (scan_filter.comp:236-323)
+// leave their score in the output pair's second word (an f32 similarity, an integer distance) when
+// word 2 has bit 0; word 4 is the gram length.
 
 #define IOP_PUSH_TRUE 0
 #define IOP_LOAD_NUM_COL 1
@@ -364,6 +366,8 @@ static int launch_scan_simple(const CqlLaunch& a, uint32_t gws, uint32_t lws, cu
 #define IOP_STR_CONTAINS 12
 #define IOP_HALT 13
 #define IOP_PUSH_FALSE 14
+#define IOP_TRIGRAM_SIM 15
+#define IOP_EDIT_DISTANCE 16
 #define IOP_STR_NE 17
 #define IOP_STR_LT 18
 #define IOP_STR_GT 19
@@ -422,7 +426,67 @@ __device__ bool interp_str_contains(const CqlLaunch& a, uint32_t slot, uint64_t 
   return false;
 }
 
-__device__ bool interp_row(const CqlLaunch& a, const uint32_t* code, uint32_t words, uint64_t row)
+#define FUZZY_MAX_NEEDLE 64u          // QE_FUZZY_MAX_NEEDLE_LEN, scan_filter.comp:35
+#define FUZZY_MAX_STRING 1048576u     // MAX_SANE_STRING_LEN, scan_filter.comp:205
+
+// the shared n-grams of the row and the needle (each needle gram used once, the first unused match taken)
+// over the union of the two gram counts
+__device__ double interp_trigram(const CqlLaunch& a, uint32_t slot, uint64_t row, uint32_t wo, uint32_t clen, uint32_t n)
+{
+  uint32_t s = str_off(a, slot, row), e = str_off(a, slot, row + 1), len = e - s;
+  if (len < n || clen < n)
+  {
+    if (len != clen) return 0.0;
+    for (uint32_t i = 0; i < len; i++)
+      if (str_byte(a, slot, s + i) != const_byte(a, wo, i)) return 0.0;
+    return 1.0;
+  }
+  if (len > FUZZY_MAX_STRING) return 0.0;
+  uint32_t needle_grams = min(clen - n + 1u, FUZZY_MAX_NEEDLE);
+  unsigned long long used = 0ull;   // one bit per needle gram (at most 64)
+  uint32_t shared = 0;
+  for (uint32_t i = 0; i + n <= len; i++)
+    for (uint32_t j = 0; j < needle_grams; j++)
+    {
+      if ((used >> j) & 1ull) continue;
+      uint32_t k = 0;
+      while (k < n && str_byte(a, slot, s + i + k) == const_byte(a, wo, j + k)) k++;
+      if (k == n)
+      {
+        used |= 1ull << j;
+        shared++;
+        break;
+      }
+    }
+  uint32_t uni = (len - n + 1u) + needle_grams - shared;
+  return uni == 0 ? 0.0 : (double)shared / (double)uni;
+}
+
+// the Levenshtein distance to the first 64 bytes of the needle, one rolling row
+__device__ double interp_edit_distance(const CqlLaunch& a, uint32_t slot, uint64_t row, uint32_t wo, uint32_t clen)
+{
+  uint32_t s = str_off(a, slot, row), e = str_off(a, slot, row + 1), len = e - s;
+  if (len > FUZZY_MAX_STRING) return (double)FUZZY_MAX_STRING;
+  uint32_t m = min(clen, FUZZY_MAX_NEEDLE);
+  uint32_t dp[FUZZY_MAX_NEEDLE + 1];
+  for (uint32_t j = 0; j <= m; j++) dp[j] = j;
+  for (uint32_t i = 1; i <= len; i++)
+  {
+    uint32_t diag = dp[0];
+    dp[0] = i;
+    uint32_t hb = str_byte(a, slot, s + i - 1);
+    for (uint32_t j = 1; j <= m; j++)
+    {
+      uint32_t keep = dp[j];
+      uint32_t cost = hb == const_byte(a, wo, j - 1) ? 0u : 1u;
+      dp[j] = min(min(dp[j] + 1u, dp[j - 1] + 1u), diag + cost);
+      diag = keep;
+    }
+  }
+  return (double)dp[m];
+}
+
+__device__ bool interp_row(const CqlLaunch& a, const uint32_t* code, uint32_t words, uint64_t row, uint32_t gram, uint32_t* aux)
 {
   const uint32_t* consts = (const uint32_t*)a.buf[1];
   double stack[INTERP_MAX_STACK];
@@ -483,6 +547,16 @@ __device__ bool interp_row(const CqlLaunch& a, const uint32_t* code, uint32_t wo
       }
       stack[sp++] = r ? 1.0 : 0.0;
     }
+    else if (op == IOP_TRIGRAM_SIM || op == IOP_EDIT_DISTANCE)
+    {
+      if (sp >= INTERP_MAX_STACK || ip + 3 > words) return false;
+      uint32_t slot = code[ip], wo = code[ip + 1], len = code[ip + 2];
+      ip += 3;
+      if (slot + 1 >= 10) return false;
+      double v = op == IOP_TRIGRAM_SIM ? interp_trigram(a, slot, row, wo, len, gram) : interp_edit_distance(a, slot, row, wo, len);
+      *aux = op == IOP_TRIGRAM_SIM ? __float_as_uint((float)v) : (uint32_t)v;
+      stack[sp++] = v;
+    }
     else
     {
       // an opcode this kernel does not evaluate ends the program
@@ -504,6 +578,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_filter(CqlLaunch a, uint6
   uint64_t capacity = a.bytes[3] / 8;
   uint32_t skip_shift = cql_word(a, 6);
   bool skip_on = cql_word(a, 8) != 0;
+  bool scored = (cql_word(a, 2) & 1u) != 0u;
+  uint32_t gram = max(cql_word(a, 4), 1u);
   uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (uint64_t base = (uint64_t)blockIdx.x * SCAN_THREADS; base < rows; base += (uint64_t)gridDim.x * SCAN_THREADS)
   {
@@ -514,7 +590,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_filter(CqlLaunch a, uint6
       uint64_t ch = row >> skip_shift;
       in_range = ((skip[ch >> 5] >> (ch & 31)) & 1u) == 0u;
     }
-    bool matched = in_range && interp_row(a, code, words, row);
+    uint32_t aux = 0u;
+    bool matched = in_range && interp_row(a, code, words, row, gram, &aux);
     uint32_t ballot = __ballot_sync(0xffffffffu, matched);
     if (lane == 0) s_warp[warp] = __popc(ballot);
     __syncthreads();
@@ -533,7 +610,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_filter(CqlLaunch a, uint6
     if (matched)
     {
       uint64_t pos = (uint64_t)s_base + s_warp[warp] + __popc(ballot & ((1u << lane) - 1u));
-      if (pos < capacity) *(uint2*)(out + pos * 2) = make_uint2((uint32_t)row, 0u);
+      if (pos < capacity) *(uint2*)(out + pos * 2) = make_uint2((uint32_t)row, scored ? aux : 0u);
     }
     __syncthreads();
   }

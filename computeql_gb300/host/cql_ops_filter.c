@@ -156,12 +156,6 @@ static uint64_t program_rows(const CqlProgram* prog, const CqlColumn* columns, u
   return prog->binding_count ? columns[prog->binding_column[0]].rows : columns[0].rows;
 }
 
-static int cmp_u32(const void* a, const void* b)
-{
-  uint32_t x = *(const uint32_t*)a, y = *(const uint32_t*)b;
-  return x < y ? -1 : (x > y);
-}
-
 /* bytecode, constants and string pool of a program into pooled buffers, written in one batch */
 static int upload_program(const CqlProgram* prog, CqlBuffer** out_code, CqlBuffer** out_consts, CqlBuffer** out_strs)
 {
@@ -211,11 +205,24 @@ static int run_simple(const CqlProgram* prog, const CqlColumn* columns, const Cq
   return cqlops_scan_simple(cols, used, local, n, out_count, out_rows, cap);
 }
 
-int cqlops_scan_filter(const CqlProgram* prog, const CqlColumn* columns, uint32_t strategy, uint64_t* out_count, uint32_t* out_rows,
-                       uint64_t out_capacity, uint32_t* out_strategy)
+static int pair_by_row(const void* a, const void* b)
+{
+  uint32_t x = ((const uint32_t*)a)[0], y = ((const uint32_t*)b)[0];
+  return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+static int scan_filter_run(const CqlProgram* prog, const CqlColumn* columns, uint32_t strategy, uint64_t* out_count, uint32_t* out_rows,
+                           double* out_scores, uint64_t out_capacity, uint32_t* out_strategy)
 {
   cqlops_note_error("");
-  if (prog->requires_cpu_scan || prog->has_score_output) return refuse("the program needs the CPU scan, which this backend does not have");
+  if (prog->requires_cpu_scan) return refuse("the program needs the CPU scan, which this backend does not have");
+  /* a fuzzy comparison runs on the interpreter only (qe_scan_filter_selected, :2532, :2641) */
+  uint32_t score_flags = prog->has_score_output ? (1u | (prog->has_score_output == 2u ? 2u : 0u)) : 0u;
+  if (score_flags)
+  {
+    if (strategy == CQLOPS_SCAN_SIMPLE || strategy == CQLOPS_SCAN_GENERATED) return refuse("a fuzzy comparison runs on the interpreter");
+    strategy = CQLOPS_SCAN_INTERPRETER;
+  }
   uint64_t rows = program_rows(prog, columns, 0);
 
   if (strategy == CQLOPS_SCAN_AUTO || strategy == CQLOPS_SCAN_SIMPLE)
@@ -256,13 +263,13 @@ int cqlops_scan_filter(const CqlProgram* prog, const CqlColumn* columns, uint32_
   cqlcuda_kernel_set_arg_buffer(k, 4, counter);
   cqlcuda_kernel_set_arg_buffer(k, 5, filler);
   cqlcuda_kernel_set_arg_u64(k, 0, rows);
-  cqlcuda_kernel_set_arg_u64(k, 1, 0);
-  cqlcuda_kernel_set_arg_u64(k, 2, 3);
+  cqlcuda_kernel_set_arg_u64(k, 1, score_flags);   /* word 2: bit 0 score output, bit 1 a distance */
+  cqlcuda_kernel_set_arg_u64(k, 2, 3);             /* word 4: the trigram length */
   cqlcuda_kernel_set_arg_u64(k, 3, 0);
   cqlcuda_kernel_set_arg_u64(k, 4, 0);
   cqlcuda_kernel_set_arg_u64(k, 5, 0);
 
-  int want_rows = out_rows != NULL;
+  int want_rows = out_rows != NULL || out_scores != NULL;
   uint64_t cap_rows = 0;
   if (want_rows)
   {
@@ -291,23 +298,39 @@ int cqlops_scan_filter(const CqlProgram* prog, const CqlColumn* columns, uint32_
   if (want_rows && result && out_capacity)
   {
     uint32_t* pairs = (uint32_t*)malloc(result * 8);
-    uint32_t* list = (uint32_t*)malloc(result * 4);
-    if (!pairs || !list)
-    {
-      free(pairs);
-      free(list);
-      return 0;
-    }
+    if (!pairs) return 0;
     cqlcuda_buffer_read(output, pairs, result * 8);
-    for (uint64_t i = 0; i < result; i++) list[i] = pairs[2 * i];
-    qsort(list, result, 4, cmp_u32);
-    memcpy(out_rows, list, (result < out_capacity ? result : out_capacity) * 4);
+    /* the kernel's order is not deterministic: rows ascending, each with its score */
+    qsort(pairs, result, 8, pair_by_row);
+    uint64_t m = result < out_capacity ? result : out_capacity;
+    for (uint64_t i = 0; i < m; i++)
+    {
+      if (out_rows) out_rows[i] = pairs[2 * i];
+      if (out_scores)
+      {
+        uint32_t aux = pairs[2 * i + 1];
+        float f;
+        memcpy(&f, &aux, 4);
+        out_scores[i] = !score_flags ? 0.0 : (score_flags & 2u) ? (double)aux : (double)f;
+      }
+    }
     free(pairs);
-    free(list);
   }
   if (out_count) *out_count = result;
   if (out_strategy) *out_strategy = ran;
   return 1;
+}
+
+int cqlops_scan_filter(const CqlProgram* prog, const CqlColumn* columns, uint32_t strategy, uint64_t* out_count, uint32_t* out_rows,
+                       uint64_t out_capacity, uint32_t* out_strategy)
+{
+  return scan_filter_run(prog, columns, strategy, out_count, out_rows, NULL, out_capacity, out_strategy);
+}
+
+int cqlops_scan_filter_scored(const CqlProgram* prog, const CqlColumn* columns, uint64_t* out_count, uint32_t* out_rows, double* out_scores,
+                              uint64_t out_capacity)
+{
+  return scan_filter_run(prog, columns, CQLOPS_SCAN_AUTO, out_count, out_rows, out_scores, out_capacity, NULL);
 }
 
 int cqlops_fused_filter_aggregate(const CqlProgram* prog_in, const CqlColumn* columns, const uint32_t* agg_columns, uint32_t agg_count,

@@ -10,6 +10,7 @@
  * The condition arrives as an s-expression over named columns instead of the reference's IR tree:
  *   (and A B) (or A B) (= a 5) (!= a 5) (< a 2.5) (<= ..) (> ..) (>= ..) (in a 1 2 3) (not_in a 1 2)
  *   (is_null a) (is_not_null a) (contains s 'text') true false
+ *   (> (similarity s 'text') 0.4) (<= (edit_distance s 'text') 2)   - fuzzy search, the score reported per row
  * Literals: numbers, or 'quoted' strings for string columns.
  */
 #include "cqlops.h"
@@ -286,9 +287,47 @@ static int dict_code(const CqlDict* d, const char* value, uint32_t* out)
 
 static void compile(Ctx* c, Node* n);
 
+#define FUZZY_MAX_NEEDLE_LEN 64
+
 static void compile_comparison(Ctx* c, const char* op, Node* left, Node* right)
 {
   CqlProgram* p = c->prog;
+  /* fuzzy search: (op (similarity col 'term') threshold), (op (edit_distance col 'term') threshold)
+     (:307-349): the score is compared, and also reported per matching row */
+  if (left->is_list && left->first && !left->first->is_list &&
+      (!strcmp(left->first->atom, "similarity") || !strcmp(left->first->atom, "edit_distance")))
+  {
+    int is_distance = !strcmp(left->first->atom, "edit_distance");
+    Node* col_arg = left->first->next;
+    Node* needle = col_arg ? col_arg->next : NULL;
+    int ci = col_arg && !col_arg->is_list && !col_arg->quoted ? find_column(c, col_arg->atom) : -1;
+    uint32_t cmp = cmp_opcode(op);
+    if (ci < 0 || c->columns[ci].type != CQLOPS_TYPE_STRING8 || !needle || !needle->quoted || !cmp || (c->columns[ci].dict && !c->columns[ci].offsets))
+    {
+      fail(p, "similarity() / edit_distance() take a raw string column, a string literal and a comparison");
+      emit(p, OP_PUSH_TRUE);
+      return;
+    }
+    int b = bind(c, (uint32_t)ci, 0);
+    if (b < 0)
+    {
+      emit(p, OP_PUSH_TRUE);
+      return;
+    }
+    /* a needle longer than the kernels' limit is cut to it (QE_*_MAX_NEEDLE_LEN, 64 bytes by default) */
+    char cut[FUZZY_MAX_NEEDLE_LEN + 1];
+    snprintf(cut, sizeof(cut), "%s", needle->atom);
+    uint32_t wo = 0, len = 0;
+    add_string(p, cut, &wo, &len);
+    emit(p, is_distance ? OP_EDIT_DISTANCE : OP_TRIGRAM_SIM);
+    emit(p, p->binding_slot[b]);
+    emit(p, wo);
+    emit(p, len);
+    p->has_score_output = is_distance ? 2u : 1u;
+    load_value(c, right);
+    emit(p, cmp);
+    return;
+  }
   /* string column op 'literal' (:358-455) */
   int li = (!left->is_list && !left->quoted) ? find_column(c, left->atom) : -1;
   if (li >= 0 && c->columns[li].type == CQLOPS_TYPE_STRING8 && right->quoted)

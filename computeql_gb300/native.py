@@ -166,6 +166,7 @@ OPS_API = [
     ("cqlops_program_simple_leaves", u32, [P, P, u32]),
     ("cqlops_program_source", C.c_int, [P, u32, P, P, u64, P]),
     ("cqlops_scan_filter", C.c_int, [P, P, u32, P, P, u64, P]),
+    ("cqlops_scan_filter_scored", C.c_int, [P, P, P, P, P, u64]),
     ("cqlops_fused_filter_aggregate", C.c_int, [P, P, P, u32, P, P, P, P]),
     ("cqlops_fused_filter_group", C.c_int, [P, P, P, u32, P, u32, u64, P, P, P, P, P, P, P, P]),
     ("cqlops_group_hash", C.c_int, [P, u32, u32, P, P, P, u64, u32, u64, P, P, P, P, P]),
@@ -173,6 +174,7 @@ OPS_API = [
     ("cqlops_join_aggregate", C.c_int, [P, u64, P, P, P, P]),
     ("cqlops_sort_rows", C.c_int, [P, u32, P, P, u64, P, u64]),
     ("cqlops_window_rank", C.c_int, [P, u32, P, u32, P, u64, P, P, P, P, u64]),
+    ("cqlops_having", C.c_int, [cstr, P, u32, P, u32, u64, P]),
     ("cqlops_fixed_scale", C.c_int, [P, P, u64, P, P]),
     ("cqlops_zone_map_build", C.c_int, [P, P, u64]),
     ("cqlops_batch_filter_aggregate", C.c_int, [P, u32, P, u32, P, u32, P, P, P]),

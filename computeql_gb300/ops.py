@@ -302,6 +302,19 @@ def scan_filter(program, strategy=SCAN_AUTO, want_rows=False, max_rows=None):
     return count.value, rows, ran.value
 
 
+def scan_scored(program, max_rows=None):
+    """A WHERE with a fuzzy comparison (similarity / edit_distance) -> (count, rows ascending, scores)."""
+    n = program.columns[0].rows if program.columns else 0
+    cap = n if max_rows is None else min(max_rows, n)
+    rows = np.empty(max(cap, 1), dtype=np.uint32)
+    scores = np.empty(max(cap, 1), dtype=np.float64)
+    count = C.c_uint64()
+    _check(N.load_ops().cqlops_scan_filter_scored(C.byref(program.prog), program._cols, C.byref(count), N.ptr(rows), N.ptr(scores), cap),
+           "cqlops_scan_filter_scored")
+    m = min(count.value, cap)
+    return count.value, rows[:m].copy(), scores[:m].copy()
+
+
 def fused_aggregate(program, agg_names):
     k = len(agg_names)
     idx = (C.c_uint32 * max(k, 1))(*[program.index(n) for n in agg_names])
@@ -478,6 +491,18 @@ def sort_rows(keys, desc=None, selection=None, count=None):
     out = np.empty(max(n, 1), dtype=np.uint32)
     _check(N.load_ops().cqlops_sort_rows(arr, kc, N.ptr(d), sel, n, N.ptr(out), n), "cqlops_sort_rows")
     return out[:n]
+
+
+def having(condition, columns, literals=()):
+    """HAVING over grouped results: `condition` over v0..v7 (the columns, float64 arrays of one length) and
+    lit[i] (the literals) -> u32 keep flags per group."""
+    cols = [np.ascontiguousarray(c, dtype=np.float64) for c in columns]
+    g = len(cols[0]) if cols else 0
+    ptrs = (C.c_void_p * max(len(cols), 1))(*[c.ctypes.data for c in cols])
+    lits = np.array(list(literals) + [0.0], dtype=np.float64)
+    keep = np.empty(max(g, 1), dtype=np.uint32)
+    _check(N.load_ops().cqlops_having(condition.encode(), N.ptr(lits), len(literals), ptrs, len(cols), g, N.ptr(keep)), "cqlops_having")
+    return keep[:g]
 
 
 def window_rank(keys, desc=None, partitions=0, selection=None, count=None):

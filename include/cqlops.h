@@ -121,7 +121,7 @@ typedef struct CqlProgram
   uint32_t binding_dict[CQLOPS_MAX_BINDINGS];    /* 1 when the binding is dictionary codes */
   uint32_t next_slot;
   uint32_t requires_cpu_scan;
-  uint32_t has_score_output;
+  uint32_t has_score_output;                     /* 1: a SIMILARITY score, 2: an EDIT_DISTANCE score per matching row */
   char error[128];
 } CqlProgram;
 
@@ -180,6 +180,13 @@ enum
    that ran. */
 int cqlops_scan_filter(const CqlProgram* prog, const CqlColumn* columns, uint32_t strategy, uint64_t* out_count, uint32_t* out_rows,
                        uint64_t out_capacity, uint32_t* out_strategy);
+
+/* cqlops_scan_filter for a program with a fuzzy comparison (has_score_output): it runs on the interpreter
+   (scan_filter, as in the reference) and writes, next to each of the first out_capacity matching rows in
+   ascending order, the row's score - the trigram similarity as the f32 the kernel reports, or the edit
+   distance (scan_filter.comp:510-527). Programs without a fuzzy comparison get score 0. */
+int cqlops_scan_filter_scored(const CqlProgram* prog, const CqlColumn* columns, uint64_t* out_count, uint32_t* out_rows, double* out_scores,
+                              uint64_t out_capacity);
 
 /* WHERE + COUNT(*) and SUM/MIN/MAX of up to 4 numeric columns in one pass (qe_fused_filter_aggregate,
    query_exec.c:9888-10254). agg_columns index the column array. Partials are folded in workgroup order. */
@@ -312,6 +319,14 @@ int cqlops_group_dense_fixed(const CqlColumn* key, uint32_t expr_count, const ui
    Writes up to out_capacity row numbers in sorted order. */
 int cqlops_sort_rows(const CqlColumn* keys, uint32_t key_count, const uint32_t* desc, CqlBuffer* selection,
                      uint64_t selection_count, uint32_t* out_rows, uint64_t out_capacity);
+
+/* A HAVING condition over the grouped result, evaluated for every group at once (qk_having_kernel,
+   src/query_exec/query_kernel.c:2530-2575): `condition` is an expression over v0..v7 (group i's values of
+   the result columns, as doubles) and lit[0..15] (the literals), in C syntax (&&, ||, !, comparisons,
+   arithmetic, fabs/fmin/fmax/floor/ceil/sqrt/isnan); out_keep[i] = 1 when group i passes. Conditions that
+   differ only in their literals share one compiled kernel. Refuses a condition with anything else. */
+int cqlops_having(const char* condition, const double* literals, uint32_t literal_count, const double* const* columns, uint32_t column_count,
+                  uint64_t group_count, uint32_t* out_keep);
 
 /* ROW_NUMBER, RANK and DENSE_RANK over (PARTITION BY the first partition_key_count keys ORDER BY the
    rest) - qe_window_rank_gpu, src/query_exec/query_exec.c:6155-6540. The rows (or the selection's, as for

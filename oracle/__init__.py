@@ -60,6 +60,8 @@ def lib():
         L.orc_group_cpu_reduce.restype = u64
         L.orc_eval_program.argtypes = [P, u32, P, P, P, P, u64, P]
         L.orc_eval_program.restype = u64
+        L.orc_eval_program_scored.argtypes = [P, u32, P, P, P, P, u64, P, P]
+        L.orc_eval_program_scored.restype = u64
         L.orc_hll_add.argtypes = [P, u64, u32, P]
         L.orc_hll_estimate.argtypes = [P, u64]
         L.orc_hll_estimate.restype = dbl
@@ -166,7 +168,7 @@ def group_cpu_reduce(key, args, max_groups):
     return keys[:n], counts[:n], sums[: n * e].reshape(n, e), mins[: n * e].reshape(n, e), maxs[: n * e].reshape(n, e)
 
 
-def eval_program(words, consts, str_pool, slot_arrays, slot_types, rows):
+def eval_program(words, consts, str_pool, slot_arrays, slot_types, rows, scores=False):
     """The scan bytecode evaluated per row (orc_eval_program). slot_arrays[s]: the column bound at
     slot s (raw strings: bytes at s, u64 offsets at s + 1), or None. Returns the match mask (uint8)."""
     w = np.ascontiguousarray(words, dtype=np.uint32)
@@ -177,6 +179,10 @@ def eval_program(words, consts, str_pool, slot_arrays, slot_types, rows):
     types = np.zeros(10, dtype=np.uint32)
     types[: len(slot_types)] = slot_types
     mask = np.zeros(max(rows, 1), dtype=np.uint8)
+    if scores:
+        sc = np.zeros(max(rows, 1), dtype=np.float64)
+        lib().orc_eval_program_scored(_p(w), len(w), _p(k), _p(sp), ptrs, _p(types), rows, _p(mask), _p(sc))
+        return mask[:rows], sc[:rows]
     lib().orc_eval_program(_p(w), len(w), _p(k), _p(sp), ptrs, _p(types), rows, _p(mask))
     return mask[:rows]
 

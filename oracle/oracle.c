@@ -532,8 +532,71 @@ static int str_contains(const void* const* data, uint32_t slot, uint64_t row, co
   return 0;
 }
 
-uint64_t orc_eval_program(const uint32_t* words, uint32_t word_count, const uint32_t* consts, const uint8_t* str_pool,
-                          const void* const* slot_data, const uint32_t* slot_types, uint64_t rows, uint8_t* out_match)
+#define FUZZY_MAX_NEEDLE 64u          /* QE_FUZZY_MAX_NEEDLE_LEN, scan_filter.comp:35 */
+#define FUZZY_MAX_STRING 1048576u     /* MAX_SANE_STRING_LEN, scan_filter.comp:205 */
+
+/* trigram_similarity (scan_filter.comp:236-290): the shared n-grams of the row and the needle, each needle
+   gram used once, the first unused match taken, over the union of the two gram counts */
+static double str_trigram(const void* const* data, uint32_t slot, uint64_t row, const uint8_t* c, uint32_t clen, uint32_t n)
+{
+  const uint8_t* bytes = (const uint8_t*)data[slot];
+  const uint64_t* offs = (const uint64_t*)data[slot + 1];
+  uint64_t s = offs[row], len = offs[row + 1] - s;
+  if (len < n || clen < n)
+  {
+    if (len != clen) return 0.0;
+    return memcmp(bytes + s, c, len) == 0 ? 1.0 : 0.0;
+  }
+  if (len > FUZZY_MAX_STRING) return 0.0;
+  uint32_t needle_grams = clen - n + 1 < FUZZY_MAX_NEEDLE ? clen - n + 1 : FUZZY_MAX_NEEDLE;
+  uint8_t used[FUZZY_MAX_NEEDLE] = { 0 };
+  uint64_t hay_grams = len - n + 1, shared = 0;
+  for (uint64_t i = 0; i < hay_grams; i++)
+    for (uint32_t j = 0; j < needle_grams; j++)
+    {
+      if (used[j]) continue;
+      if (memcmp(bytes + s + i, c + j, n) == 0)
+      {
+        used[j] = 1;
+        shared++;
+        break;
+      }
+    }
+  uint64_t uni = hay_grams + needle_grams - shared;
+  return uni == 0 ? 0.0 : (double)shared / (double)uni;
+}
+
+/* edit_distance (scan_filter.comp:292-323): the Levenshtein distance to the first 64 bytes of the needle,
+   one rolling row */
+static double str_edit_distance(const void* const* data, uint32_t slot, uint64_t row, const uint8_t* c, uint32_t clen)
+{
+  const uint8_t* bytes = (const uint8_t*)data[slot];
+  const uint64_t* offs = (const uint64_t*)data[slot + 1];
+  uint64_t s = offs[row], len = offs[row + 1] - s;
+  if (len > FUZZY_MAX_STRING) return (double)FUZZY_MAX_STRING;
+  uint32_t m = clen < FUZZY_MAX_NEEDLE ? clen : FUZZY_MAX_NEEDLE;
+  uint32_t dp[FUZZY_MAX_NEEDLE + 1];
+  for (uint32_t j = 0; j <= m; j++) dp[j] = j;
+  for (uint64_t i = 1; i <= len; i++)
+  {
+    uint32_t diag = dp[0];
+    dp[0] = (uint32_t)i;
+    for (uint32_t j = 1; j <= m; j++)
+    {
+      uint32_t keep = dp[j];
+      uint32_t cost = bytes[s + i - 1] == c[j - 1] ? 0u : 1u;
+      uint32_t best = dp[j] + 1u;
+      if (dp[j - 1] + 1u < best) best = dp[j - 1] + 1u;
+      if (diag + cost < best) best = diag + cost;
+      dp[j] = best;
+      diag = keep;
+    }
+  }
+  return (double)dp[m];
+}
+
+static uint64_t eval_program(const uint32_t* words, uint32_t word_count, const uint32_t* consts, const uint8_t* str_pool,
+                             const void* const* slot_data, const uint32_t* slot_types, uint64_t rows, uint8_t* out_match, double* out_score)
 {
   uint64_t count = 0;
   double stack[64];
@@ -542,6 +605,7 @@ uint64_t orc_eval_program(const uint32_t* words, uint32_t word_count, const uint
     int sp = 0;
     uint32_t ip = 0;
     int ok = 1;
+    double score = 0.0;   /* the last fuzzy score of the row, as the scan outputs it */
     while (ok && ip < word_count)
     {
       uint32_t op = words[ip++];
@@ -594,13 +658,37 @@ uint64_t orc_eval_program(const uint32_t* words, uint32_t word_count, const uint
           stack[sp++] = r ? 1.0 : 0.0;
           break;
         }
+        case 15: case 16:
+        {
+          uint32_t slot = words[ip], wo = words[ip + 1], len = words[ip + 2];
+          ip += 3;
+          const uint8_t* c = str_pool + (uint64_t)wo * 4;
+          double v = op == 15 ? str_trigram(slot_data, slot, row, c, len, 3) : str_edit_distance(slot_data, slot, row, c, len);
+          /* the scan reports a similarity as an f32 and a distance as an integer */
+          score = op == 15 ? (double)(float)v : (double)(uint32_t)v;
+          stack[sp++] = v;
+          break;
+        }
         default: ok = 0; break;
       }
       if (sp >= 63) ok = 0;
     }
     int m = sp > 0 && stack[sp - 1] != 0.0;
     if (out_match) out_match[row] = (uint8_t)m;
+    if (out_score) out_score[row] = score;
     count += (uint64_t)m;
   }
   return count;
+}
+
+uint64_t orc_eval_program(const uint32_t* words, uint32_t word_count, const uint32_t* consts, const uint8_t* str_pool,
+                          const void* const* slot_data, const uint32_t* slot_types, uint64_t rows, uint8_t* out_match)
+{
+  return eval_program(words, word_count, consts, str_pool, slot_data, slot_types, rows, out_match, NULL);
+}
+
+uint64_t orc_eval_program_scored(const uint32_t* words, uint32_t word_count, const uint32_t* consts, const uint8_t* str_pool,
+                                 const void* const* slot_data, const uint32_t* slot_types, uint64_t rows, uint8_t* out_match, double* out_score)
+{
+  return eval_program(words, word_count, consts, str_pool, slot_data, slot_types, rows, out_match, out_score);
 }

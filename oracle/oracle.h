@@ -72,6 +72,9 @@ uint64_t orc_scan_and(const OrcLeaf* leaves, uint32_t leaf_count, uint64_t rows,
    s + 1), slot_types[s] its CQL type. Writes out_match[r] = 1 for a matching row; returns the count. */
 uint64_t orc_eval_program(const uint32_t* words, uint32_t word_count, const uint32_t* consts, const uint8_t* str_pool,
                           const void* const* slot_data, const uint32_t* slot_types, uint64_t rows, uint8_t* out_match);
+/* the same with each row's last fuzzy score (SIMILARITY as its f32 value, EDIT_DISTANCE as an integer) */
+uint64_t orc_eval_program_scored(const uint32_t* words, uint32_t word_count, const uint32_t* consts, const uint8_t* str_pool,
+                                 const void* const* slot_data, const uint32_t* slot_types, uint64_t rows, uint8_t* out_match, double* out_score);
 
 /* ---- sketches ---- */
 /* HyperLogLog registers of a set of values (hll_add, src/gpu/vulkan/shaders/aggregate_reduce.comp:66-92):
