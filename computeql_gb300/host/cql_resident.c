@@ -1,0 +1,358 @@
+/*
+ * cql_resident.c - the resident chunk cache: device copies of host column chunks kept between queries
+ * (QE_ResidentCache, src/query_exec/query_exec.c:1679-1970).
+ *
+ * A chunk is found by (column, write generation, first row, rows, stored width). A hit hands back the
+ * cached buffer; a miss makes room within the budget and copies the rows in. Room is made the
+ * reference's way: first the entries used only once (a scan that passed through once), the most recent of
+ * them first, then the least recently used of the rest; pinned entries are never taken. A column written
+ * since (a new generation) makes its entries unusable, and they are freed on sight. The budget is a share
+ * of the device's memory, never more than the memory the driver reports reachable, less a reserve. The
+ * allocator's eviction hook frees entries when another allocation does not fit.
+ *
+ * The memory operations are callbacks, so the policy runs the same over device buffers (the default: the
+ * cqlcuda backend) and over any other allocator a caller provides. No callback runs under the cache's lock:
+ * the backend calls the eviction hook while it holds its own, so the cache takes its lock inside the
+ * backend's and never the other way round; freed buffers are collected under the lock and released after.
+ */
+#include "cqlops.h"
+
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define RESIDENT_MAX_ENTRIES 4096
+#define RESIDENT_RESERVE (512ull << 20)
+#define RESIDENT_BUDGET_PERCENT 70
+
+typedef struct
+{
+  int used, ready;
+  uint64_t column_uid, generation, row_start, rows;
+  uint32_t width;
+  void* buffer;
+  uint64_t bytes;
+  uint64_t last_use;
+  uint32_t uses, pins;
+} ResidentChunk;
+
+struct CqlResident
+{
+  pthread_mutex_t lock;
+  ResidentChunk entries[RESIDENT_MAX_ENTRIES];
+  uint64_t tick, bytes_in_use, entry_count, hit_bytes, miss_bytes, evicted_bytes;
+  uint64_t budget_bytes;   /* 0: the share of device memory */
+  CqlResidentOps ops;
+};
+
+static CqlResident* g_hooked = NULL;   /* the cache the backend's eviction hook frees from */
+
+static uint64_t budget(CqlResident* r)
+{
+  uint64_t total = r->ops.total_memory ? r->ops.total_memory(r->ops.ctx) : 0;
+  uint64_t b = total / 100 * RESIDENT_BUDGET_PERCENT;
+  if (r->budget_bytes && (r->budget_bytes < b || !total)) b = r->budget_bytes;
+  /* other buffers, the driver and other processes use device memory too */
+  if (r->ops.free_memory)
+  {
+    uint64_t reachable = r->bytes_in_use + r->ops.free_memory(r->ops.ctx);
+    reachable = reachable > RESIDENT_RESERVE ? reachable - RESIDENT_RESERVE : 0;
+    if (reachable < b) b = reachable;
+  }
+  return b;
+}
+
+/* buffers taken out of the cache under its lock, released after it */
+typedef struct
+{
+  void* items[64];
+  uint32_t n;
+} Doomed;
+
+static void doom_release(CqlResident* r, Doomed* d)
+{
+  for (uint32_t i = 0; i < d->n; i++) r->ops.release(r->ops.ctx, d->items[i]);
+  d->n = 0;
+}
+
+/* unlinks an entry; its buffer goes to `d` (released at once when `d` is full, which only the
+   unlocked paths allow) */
+static void unlink_entry(CqlResident* r, ResidentChunk* e, Doomed* d)
+{
+  if (e->buffer) d->items[d->n++] = e->buffer;
+  r->bytes_in_use -= e->bytes < r->bytes_in_use ? e->bytes : r->bytes_in_use;
+  r->entry_count -= 1;
+  memset(e, 0, sizeof(*e));
+}
+
+/* entries used once go first (the most recent of them), then the least recently used */
+static ResidentChunk* pick_victim(CqlResident* r)
+{
+  ResidentChunk *probation = NULL, *lru = NULL;
+  for (int i = 0; i < RESIDENT_MAX_ENTRIES; i++)
+  {
+    ResidentChunk* e = &r->entries[i];
+    if (!e->used || e->pins > 0 || !e->ready) continue;
+    if (e->uses <= 1)
+    {
+      if (!probation || e->last_use > probation->last_use) probation = e;
+    }
+    else if (!lru || e->last_use < lru->last_use)
+      lru = e;
+  }
+  return probation ? probation : lru;
+}
+
+/* evicts until `wanted` bytes are freed, none can be or `d` is full; returns the bytes freed */
+static uint64_t evict_locked(CqlResident* r, uint64_t wanted, Doomed* d)
+{
+  uint64_t freed = 0;
+  while (freed < wanted && d->n < 64)
+  {
+    ResidentChunk* v = pick_victim(r);
+    if (!v) break;
+    freed += v->bytes;
+    r->evicted_bytes += v->bytes;
+    unlink_entry(r, v, d);
+  }
+  return freed;
+}
+
+static uint64_t evict(CqlResident* r, uint64_t wanted)
+{
+  uint64_t freed = 0;
+  for (;;)
+  {
+    Doomed d = { { 0 }, 0 };
+    pthread_mutex_lock(&r->lock);
+    uint64_t got = evict_locked(r, wanted - freed, &d);
+    pthread_mutex_unlock(&r->lock);
+    doom_release(r, &d);
+    freed += got;
+    if (!got || freed >= wanted) return freed;
+  }
+}
+
+/* the backend calls this when an allocation does not fit (g_gpu_evict_hook) */
+static uint64_t backend_evict_hook(uint64_t wanted)
+{
+  CqlResident* r = g_hooked;
+  return r ? evict(r, wanted) : 0;
+}
+
+/* ---- the cqlcuda backend as the allocator ---- */
+
+static void* dev_alloc(void* ctx, uint64_t bytes)
+{
+  (void)ctx;
+  return cqlcuda_buffer_alloc(bytes, CQLCUDA_BUFFER_READ_WRITE, NULL);
+}
+
+static int dev_copy(void* ctx, void* buffer, const void* host, uint64_t bytes)
+{
+  (void)ctx;
+  CqlBatch* b = cqlcuda_batch_begin(bytes, 0);
+  cqlcuda_batch_buffer_write(b, (CqlBuffer*)buffer, host, bytes);
+  return cqlcuda_batch_end(b);
+}
+
+static void dev_release(void* ctx, void* buffer)
+{
+  (void)ctx;
+  cqlcuda_buffer_release((CqlBuffer*)buffer);
+}
+
+static uint64_t dev_total(void* ctx)
+{
+  (void)ctx;
+  return cqlcuda_device_total_memory();
+}
+
+static uint64_t dev_free(void* ctx)
+{
+  (void)ctx;
+  return cqlcuda_device_free_memory();
+}
+
+CqlResident* cqlops_resident_create(uint64_t budget_bytes, const CqlResidentOps* ops)
+{
+  CqlResident* r = (CqlResident*)calloc(1, sizeof(CqlResident));
+  if (!r) return NULL;
+  pthread_mutex_init(&r->lock, NULL);
+  r->budget_bytes = budget_bytes;
+  if (ops) r->ops = *ops;
+  else
+  {
+    r->ops.alloc = dev_alloc;
+    r->ops.copy = dev_copy;
+    r->ops.release = dev_release;
+    r->ops.total_memory = dev_total;
+    r->ops.free_memory = dev_free;
+    r->ops.ctx = NULL;
+    /* the backend frees from this cache when an allocation does not fit (qe_resident_acquire sets
+       g_gpu_evict_hook the same way) */
+    g_hooked = r;
+    cqlcuda_set_evict_hook(backend_evict_hook);
+  }
+  return r;
+}
+
+void cqlops_resident_destroy(CqlResident* r)
+{
+  if (!r) return;
+  if (g_hooked == r)
+  {
+    cqlcuda_set_evict_hook(NULL);
+    g_hooked = NULL;
+  }
+  for (int i = 0; i < RESIDENT_MAX_ENTRIES; i++)
+    if (r->entries[i].used && r->entries[i].buffer) r->ops.release(r->ops.ctx, r->entries[i].buffer);
+  pthread_mutex_destroy(&r->lock);
+  free(r);
+}
+
+void* cqlops_resident_acquire(CqlResident* r, uint64_t column_uid, uint64_t generation, const void* host_rows, uint64_t row_start, uint64_t rows,
+                              uint32_t width, int* out_hit)
+{
+  if (out_hit) *out_hit = 0;
+  if (!r) return NULL;
+  uint64_t bytes = rows * width;
+  uint64_t b = budget(r);   /* asks the allocator for free memory: outside the lock */
+  Doomed d = { { 0 }, 0 };
+  pthread_mutex_lock(&r->lock);
+  ResidentChunk* free_slot = NULL;
+  for (int i = 0; i < RESIDENT_MAX_ENTRIES; i++)
+  {
+    ResidentChunk* e = &r->entries[i];
+    if (!e->used)
+    {
+      if (!free_slot) free_slot = e;
+      continue;
+    }
+    if (e->column_uid != column_uid) continue;
+    if (e->generation != generation)
+    {
+      /* the column has been written since: nothing in this entry can be used again */
+      if (e->pins == 0 && e->ready && d.n < 64)
+      {
+        unlink_entry(r, e, &d);
+        if (!free_slot) free_slot = e;
+      }
+      continue;
+    }
+    if (e->ready && e->row_start == row_start && e->rows == rows && e->width == width)
+    {
+      r->tick++;
+      e->last_use = r->tick;
+      e->uses++;
+      e->pins++;
+      r->hit_bytes += bytes;
+      void* buf = e->buffer;
+      pthread_mutex_unlock(&r->lock);
+      doom_release(r, &d);
+      if (out_hit) *out_hit = 1;
+      return buf;
+    }
+  }
+  int fits = free_slot && bytes && bytes <= b && host_rows;
+  if (fits && r->bytes_in_use + bytes > b)
+  {
+    uint64_t over = r->bytes_in_use + bytes - b;
+    fits = evict_locked(r, over, &d) >= over;
+  }
+  if (!fits)
+  {
+    pthread_mutex_unlock(&r->lock);
+    doom_release(r, &d);
+    return NULL;
+  }
+  /* the slot is held (pinned, not ready: no one finds it, no one evicts it) while the buffer is made */
+  r->tick++;
+  free_slot->used = 1;
+  free_slot->ready = 0;
+  free_slot->column_uid = column_uid;
+  free_slot->generation = generation;
+  free_slot->row_start = row_start;
+  free_slot->rows = rows;
+  free_slot->width = width;
+  free_slot->buffer = NULL;
+  free_slot->bytes = bytes;
+  free_slot->last_use = r->tick;
+  free_slot->uses = 1;
+  free_slot->pins = 1;
+  r->bytes_in_use += bytes;
+  r->entry_count++;
+  r->miss_bytes += bytes;
+  pthread_mutex_unlock(&r->lock);
+  doom_release(r, &d);
+  void* buf = r->ops.alloc(r->ops.ctx, bytes);
+  int copied = buf && r->ops.copy(r->ops.ctx, buf, host_rows, bytes);
+  pthread_mutex_lock(&r->lock);
+  if (copied)
+  {
+    free_slot->buffer = buf;
+    free_slot->ready = 1;
+  }
+  else
+  {
+    free_slot->buffer = NULL;
+    unlink_entry(r, free_slot, &d);
+  }
+  pthread_mutex_unlock(&r->lock);
+  if (!copied && buf) r->ops.release(r->ops.ctx, buf);
+  return copied ? buf : NULL;
+}
+
+void cqlops_resident_release(CqlResident* r, const void* buffer)
+{
+  if (!r || !buffer) return;
+  pthread_mutex_lock(&r->lock);
+  for (int i = 0; i < RESIDENT_MAX_ENTRIES; i++)
+  {
+    ResidentChunk* e = &r->entries[i];
+    if (e->used && e->buffer == buffer)
+    {
+      if (e->pins) e->pins--;
+      break;
+    }
+  }
+  pthread_mutex_unlock(&r->lock);
+}
+
+uint64_t cqlops_resident_evict(CqlResident* r, uint64_t bytes_wanted)
+{
+  return r ? evict(r, bytes_wanted) : 0;
+}
+
+void cqlops_resident_clear(CqlResident* r)
+{
+  if (!r) return;
+  for (;;)
+  {
+    Doomed d = { { 0 }, 0 };
+    pthread_mutex_lock(&r->lock);
+    for (int i = 0; i < RESIDENT_MAX_ENTRIES && d.n < 64; i++)
+      if (r->entries[i].used && r->entries[i].pins == 0 && r->entries[i].ready) unlink_entry(r, &r->entries[i], &d);
+    pthread_mutex_unlock(&r->lock);
+    uint32_t n = d.n;
+    doom_release(r, &d);
+    if (n < 64) return;
+  }
+}
+
+CqlResidentStats cqlops_resident_stats(CqlResident* r)
+{
+  CqlResidentStats s;
+  memset(&s, 0, sizeof(s));
+  if (!r) return s;
+  uint64_t b = budget(r);
+  pthread_mutex_lock(&r->lock);
+  s.hit_bytes = r->hit_bytes;
+  s.miss_bytes = r->miss_bytes;
+  s.evicted_bytes = r->evicted_bytes;
+  s.bytes_in_use = r->bytes_in_use;
+  s.entries = r->entry_count;
+  s.budget_bytes = b;
+  pthread_mutex_unlock(&r->lock);
+  return s;
+}

@@ -54,6 +54,21 @@ class CqlServeStats(C.Structure):
                                    "peak_in_flight_bytes", "memory_budget", "admission_waits")]
 
 
+RESIDENT_ALLOC = C.CFUNCTYPE(C.c_void_p, C.c_void_p, u64)
+RESIDENT_COPY = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, u64)
+RESIDENT_RELEASE = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p)
+RESIDENT_MEMORY = C.CFUNCTYPE(u64, C.c_void_p)
+
+
+class CqlResidentOps(C.Structure):
+    _fields_ = [("alloc", RESIDENT_ALLOC), ("copy", RESIDENT_COPY), ("release", RESIDENT_RELEASE), ("total_memory", RESIDENT_MEMORY),
+                ("free_memory", RESIDENT_MEMORY), ("ctx", P)]
+
+
+class CqlResidentStats(C.Structure):
+    _fields_ = [(n, u64) for n in ("hit_bytes", "miss_bytes", "evicted_bytes", "bytes_in_use", "entries", "budget_bytes")]
+
+
 class CqlLeaf(C.Structure):
     _fields_ = [("column", u32), ("op", u32), ("target", dbl)]
 
@@ -185,6 +200,13 @@ OPS_API = [
     ("cqlops_batch_catalog_shapes", u32, [P]),
     ("cqlops_batch_filter_aggregate_cat", C.c_int, [P, P, u32, P, u32, P, u32, P, P, P]),
     ("cqlops_batch_prepare", C.c_int, [P, P, u32, P, u32, P, u32]),
+    ("cqlops_resident_create", P, [u64, P]),
+    ("cqlops_resident_destroy", None, [P]),
+    ("cqlops_resident_acquire", P, [P, u64, u64, P, u64, u64, u32, P]),
+    ("cqlops_resident_release", None, [P, P]),
+    ("cqlops_resident_evict", u64, [P, u64]),
+    ("cqlops_resident_clear", None, [P]),
+    ("cqlops_resident_stats", CqlResidentStats, [P]),
     ("cqlserve_create", P, [P]),
     ("cqlserve_destroy", None, [P]),
     ("cqlserve_add_table", C.c_int, [P, P, u32]),

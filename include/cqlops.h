@@ -390,6 +390,43 @@ int cqlops_batch_cube_source(const CqlProgram* const* programs, uint32_t query_c
 int cqlops_batch_source(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
                         const int32_t* sum_columns, uint32_t rows_per_thread, char* out, uint64_t cap, uint64_t* out_len, uint32_t* out_shapes);
 
+/* ---- the resident chunk cache (QE_ResidentCache, src/query_exec/query_exec.c:1679-1970) ----
+   Device copies of host column chunks kept between queries, found by (column, write generation, first
+   row, rows, stored width). A miss makes room within the budget (the entries used only once first, the
+   most recent of them first, then the least recently used; pinned entries are never taken) and copies
+   the rows in; a chunk of a column written since (another generation) is never handed out and is freed
+   when met. The budget is budget_bytes (0: 70 % of the device's memory), never more than the memory the
+   allocator reports reachable less 512 MB. With ops NULL the buffers are cqlcuda buffers (acquire returns
+   a CqlBuffer*) and the backend's eviction hook frees entries when another allocation does not fit;
+   other ops put the same policy over any allocator. Safe to share between threads. */
+typedef struct CqlResidentOps
+{
+  void* (*alloc)(void* ctx, uint64_t bytes);
+  int (*copy)(void* ctx, void* buffer, const void* host, uint64_t bytes);   /* 1 on success */
+  void (*release)(void* ctx, void* buffer);
+  uint64_t (*total_memory)(void* ctx);   /* may be NULL */
+  uint64_t (*free_memory)(void* ctx);    /* may be NULL */
+  void* ctx;
+} CqlResidentOps;
+
+typedef struct CqlResidentStats
+{
+  uint64_t hit_bytes, miss_bytes, evicted_bytes, bytes_in_use, entries, budget_bytes;
+} CqlResidentStats;
+
+typedef struct CqlResident CqlResident;
+CqlResident* cqlops_resident_create(uint64_t budget_bytes, const CqlResidentOps* ops);
+void cqlops_resident_destroy(CqlResident* cache);
+/* The chunk's buffer, pinned until cqlops_resident_release; *out_hit says whether it was cached. NULL
+   when it cannot be held (the caller then streams the rows through a buffer of its own). */
+void* cqlops_resident_acquire(CqlResident* cache, uint64_t column_uid, uint64_t generation, const void* host_rows, uint64_t row_start,
+                              uint64_t rows, uint32_t width, int* out_hit);
+void cqlops_resident_release(CqlResident* cache, const void* buffer);
+/* Frees unpinned entries until bytes_wanted are freed or none is left; returns the bytes freed. */
+uint64_t cqlops_resident_evict(CqlResident* cache, uint64_t bytes_wanted);
+void cqlops_resident_clear(CqlResident* cache);
+CqlResidentStats cqlops_resident_stats(CqlResident* cache);
+
 /* Why the last operator call returned 0 when it refused the request itself ("" otherwise; GPU
    failures are in cqlcuda_last_error()). */
 const char* cqlops_last_error(void);
