@@ -225,7 +225,23 @@ static double const_value(const CqlProgram* p, uint32_t index)
 /* the program with each column load reading the register block of its column index */
 static int rebind(const CqlProgram* p, uint32_t column_count, CqlProgram* out)
 {
-  memcpy(out, p, sizeof(*out));
+  /* only what the batched predicate reads: the words and the constants (a program is ~80 KB with its
+     string pool, which a batched program never uses) */
+  if (p->word_count > CQLOPS_MAX_WORDS || p->const_count > CQLOPS_MAX_CONSTS) return 0;
+  memcpy(out->words, p->words, p->word_count * sizeof(uint32_t));
+  memcpy(out->consts, p->consts, p->const_count * 2 * sizeof(uint32_t));
+  out->word_count = p->word_count;
+  out->const_count = p->const_count;
+  out->str_pool_size = 0;
+  out->binding_count = p->binding_count;
+  memcpy(out->binding_column, p->binding_column, sizeof(p->binding_column));
+  memcpy(out->binding_type, p->binding_type, sizeof(p->binding_type));
+  memcpy(out->binding_slot, p->binding_slot, sizeof(p->binding_slot));
+  memcpy(out->binding_dict, p->binding_dict, sizeof(p->binding_dict));
+  out->next_slot = p->next_slot;
+  out->requires_cpu_scan = p->requires_cpu_scan;
+  out->has_score_output = p->has_score_output;
+  out->error[0] = 0;
   int slot_column[CQLOPS_MAX_BINDINGS];
   for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++) slot_column[s] = -1;
   for (uint32_t b = 0; b < p->binding_count; b++)
@@ -969,6 +985,7 @@ static char* cube_build_source(const CubePlan* P, uint32_t pass, const int* slot
   for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++)
   {
     if (!((summed >> s) & 1u)) continue;
+    if (slot_type[s] == CQLOPS_TYPE_U32 || slot_type[s] == CQLOPS_TYPE_I32) continue;   /* whole numbers: their raw sum is kept */
     char vj[16], ex[220];
     snprintf(vj, sizeof(vj), "v%d[j]", s);
     fx_expr(ex, sizeof(ex), slot_type[s], vj);
@@ -997,12 +1014,23 @@ static char* cube_build_source(const CubePlan* P, uint32_t pass, const int* slot
          cu->smem_off);
     uint32_t sums_at = cu->smem_off + ((cu->cells * 4u + 7u) & ~7u);
     /* a cell's sum is a 128-bit (lo, hi) pair: the low word by atomic add, the high word when the add
-       carried or the summand is negative */
+       carried or the summand is negative. A whole-number column adds its raw value into a 64-bit (lo, hi)
+       pair of 32-bit words instead (one 32-bit atomic a row), scaled by 2^k when the tables are folded:
+       the same integer as the sum of the scaled summands */
     for (uint32_t jj = 0; jj < cu->nsum; jj++)
-      bput(&b,
-           "          if (fx%d[j]) { u64* w = (u64*)(tab + %uu) + 2u * (%uu + cell); const u64 v = (u64)fx%d[j]; const u64 old = atomicAdd(&w[0], v);\n"
-           "            const u64 h = (fx%d[j] < 0 ? ~0ull : 0ull) + (old + v < old ? 1ull : 0ull); if (h) atomicAdd(&w[1], h); }\n",
-           cu->sum_slot[jj], sums_at, jj * cu->cells, cu->sum_slot[jj], cu->sum_slot[jj]);
+    {
+      int sl = cu->sum_slot[jj], t = slot_type[sl];
+      if (t == CQLOPS_TYPE_U32 || t == CQLOPS_TYPE_I32)
+        bput(&b,
+             "          if (((need_sum >> %d) & 1u) && v%d[j]) { u32* w = (u32*)(tab + %uu) + 4u * (%uu + cell); const u32 v = v%d[j]; const u32 old = atomicAdd(&w[0], v);\n"
+             "            const u32 h = (%s ? 0xffffffffu : 0u) + (old + v < old ? 1u : 0u); if (h) atomicAdd(&w[1], h); }\n",
+             sl, sl, sums_at, jj * cu->cells, sl, t == CQLOPS_TYPE_I32 ? "(int)v < 0" : "false");
+      else
+        bput(&b,
+             "          if (fx%d[j]) { u64* w = (u64*)(tab + %uu) + 2u * (%uu + cell); const u64 v = (u64)fx%d[j]; const u64 old = atomicAdd(&w[0], v);\n"
+             "            const u64 h = (fx%d[j] < 0 ? ~0ull : 0ull) + (old + v < old ? 1ull : 0ull); if (h) atomicAdd(&w[1], h); }\n",
+             sl, sums_at, jj * cu->cells, sl, sl);
+    }
     bput(&b, "        }\n      }\n");
   }
   bput(&b, "    }\n  }\n  if (bad) atomicOr(err, 1u);\n  __syncthreads();\n");
@@ -1019,14 +1047,32 @@ static char* cube_build_source(const CubePlan* P, uint32_t pass, const int* slot
          "    if (n) atomicAdd(&g[%lluull + cell], n);\n",
          cu->cells, COPIES, SMEM, cu->smem_off, (unsigned long long)cu->word_off);
     for (uint32_t jj = 0; jj < cu->nsum; jj++)
-      bput(&b,
-           "    {\n      u64 lo = 0ull, hi = 0ull;\n"
-           "      for (u32 k = 0; k < %uu; k++) { const u64* v = (const u64*)((const unsigned char*)s_mem + k * %uu + %uu) + 2u * (%uu + cell);\n"
-           "        const u64 l2 = lo + v[0]; hi += v[1] + (l2 < lo ? 1ull : 0ull); lo = l2; }\n"
-           "      if (lo | hi) { u64* w = &g[%lluull + 2ull * ((u64)%uu + cell)]; const u64 old = atomicAdd(&w[0], lo);\n"
-           "        const u64 carry = (old + lo < old) ? 1ull : 0ull; if (hi + carry) atomicAdd(&w[1], hi + carry); }\n"
-           "    }\n",
-           COPIES, SMEM, sums_at, jj * cu->cells, (unsigned long long)(cu->word_off + cu->cells), jj * cu->cells);
+    {
+      int sl = cu->sum_slot[jj], t = slot_type[sl];
+      if (t == CQLOPS_TYPE_U32 || t == CQLOPS_TYPE_I32)
+        /* the raw 64-bit sum over the copies, then times 2^k as a 128-bit pair (k >= 0 for columns of this
+           range; otherwise the queries go back to the scan) */
+        bput(&b,
+             "    {\n      long long tot = 0;\n"
+             "      for (u32 k = 0; k < %uu; k++) { const u32* v = (const u32*)((const unsigned char*)s_mem + k * %uu + %uu) + 4u * (%uu + cell);\n"
+             "        tot += (long long)(((u64)v[1] << 32) | v[0]); }\n"
+             "      const int sh = (int)col_shift[%d];\n"
+             "      if (sh < 0 || sh > 62) { if (tot) atomicOr(err, 2u); }\n"
+             "      else if (tot) { const u64 lo = (u64)tot << sh; const u64 hi = sh ? (u64)(tot >> (64 - sh)) : (tot < 0 ? ~0ull : 0ull);\n"
+             "        u64* w = &g[%lluull + 2ull * ((u64)%uu + cell)]; const u64 old = atomicAdd(&w[0], lo);\n"
+             "        const u64 carry = (old + lo < old) ? 1ull : 0ull; if (hi + carry) atomicAdd(&w[1], hi + carry); }\n"
+             "    }\n",
+             COPIES, SMEM, sums_at, jj * cu->cells, sl, (unsigned long long)(cu->word_off + cu->cells), jj * cu->cells);
+      else
+        bput(&b,
+             "    {\n      u64 lo = 0ull, hi = 0ull;\n"
+             "      for (u32 k = 0; k < %uu; k++) { const u64* v = (const u64*)((const unsigned char*)s_mem + k * %uu + %uu) + 2u * (%uu + cell);\n"
+             "        const u64 l2 = lo + v[0]; hi += v[1] + (l2 < lo ? 1ull : 0ull); lo = l2; }\n"
+             "      if (lo | hi) { u64* w = &g[%lluull + 2ull * ((u64)%uu + cell)]; const u64 old = atomicAdd(&w[0], lo);\n"
+             "        const u64 carry = (old + lo < old) ? 1ull : 0ull; if (hi + carry) atomicAdd(&w[1], hi + carry); }\n"
+             "    }\n",
+             COPIES, SMEM, sums_at, jj * cu->cells, (unsigned long long)(cu->word_off + cu->cells), jj * cu->cells);
+    }
     bput(&b, "  }\n");
   }
   bput(&b, "}\n");
@@ -1302,9 +1348,15 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
   uint32_t shape_mask[BATCH_MAX_SHAPES];
   uint32_t shape_sums[BATCH_MAX_SHAPES];
   int* shape_types = (int*)calloc(BATCH_MAX_SHAPES * CQLOPS_MAX_BINDINGS, sizeof(int));
+  CqlBatchSite* shape_site_list = (CqlBatchSite*)malloc((size_t)BATCH_MAX_SHAPES * BATCH_MAX_SITES * sizeof(CqlBatchSite));
+  struct
+  {
+    uint32_t* w;
+    uint32_t n;
+  } shape_words[BATCH_MAX_SHAPES];
   uint32_t shapes = 0;
   int slot_type[CQLOPS_MAX_BINDINGS] = { 0 };
-  int ok = rb && shape_of && order && thr && qconst && qsum && shape_types;
+  int ok = rb && shape_of && order && thr && qconst && qsum && shape_types && shape_site_list;
   char why[160] = "";
   for (uint32_t q = 0; ok && q < query_count; q++)
   {
@@ -1315,37 +1367,39 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
       ok = 0;
       break;
     }
-    CqlBatchSite sites[BATCH_MAX_SITES];
-    uint32_t site_count = 0;
-    int st[CQLOPS_MAX_BINDINGS];
-    char* expr = NULL;
-    if (!cql_codegen_batch_predicate(rb, sites, BATCH_MAX_SITES, &site_count, st, &expr, why, sizeof(why)))
-    {
-      ok = 0;
-      break;
-    }
-    for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++)
-    {
-      if (!st[s]) continue;
-      if (slot_type[s] && slot_type[s] != st[s])
-      {
-        snprintf(why, sizeof(why), "column %d read as two types", s);
-        ok = 0;
-      }
-      slot_type[s] = st[s];
-    }
+    /* a shape is its rebound bytecode: a query whose words match a shape's takes its predicate, sites
+       and column types without generating them again */
     uint64_t h = words_hash(rb);
     uint32_t s = 0;
-    while (s < shapes && !(shape_keys[s] == h && !strcmp(exprs[s], expr))) s++;
+    while (s < shapes && !(shape_keys[s] == h && shape_words[s].n == rb->word_count &&
+                           !memcmp(shape_words[s].w, rb->words, rb->word_count * sizeof(uint32_t))))
+      s++;
     if (s == shapes)
     {
       if (shapes == BATCH_MAX_SHAPES)
       {
         snprintf(why, sizeof(why), "more than %d query shapes in one batch", BATCH_MAX_SHAPES);
+        ok = 0;
+        break;
+      }
+      uint32_t site_count = 0;
+      int st[CQLOPS_MAX_BINDINGS];
+      char* expr = NULL;
+      if (!cql_codegen_batch_predicate(rb, &shape_site_list[(uint64_t)s * BATCH_MAX_SITES], BATCH_MAX_SITES, &site_count, st, &expr, why,
+                                       sizeof(why)))
+      {
+        ok = 0;
+        break;
+      }
+      shape_words[s].w = (uint32_t*)malloc(rb->word_count * sizeof(uint32_t) + 4);
+      if (!shape_words[s].w)
+      {
         free(expr);
         ok = 0;
         break;
       }
+      memcpy(shape_words[s].w, rb->words, rb->word_count * sizeof(uint32_t));
+      shape_words[s].n = rb->word_count;
       shape_keys[s] = h;
       exprs[s] = expr;
       shape_sites[s] = site_count;
@@ -1356,11 +1410,21 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
         shape_types[s * CQLOPS_MAX_BINDINGS + d] = st[d];
         if (st[d]) shape_mask[s] |= 1u << d;
       }
+      for (int d = 0; d < CQLOPS_MAX_BINDINGS; d++)
+      {
+        if (!st[d]) continue;
+        if (slot_type[d] && slot_type[d] != st[d])
+        {
+          snprintf(why, sizeof(why), "column %d read as two types", d);
+          ok = 0;
+        }
+        slot_type[d] = st[d];
+      }
       shapes++;
     }
-    else
-      free(expr);
     shape_of[q] = s;
+    const CqlBatchSite* sites = &shape_site_list[(uint64_t)s * BATCH_MAX_SITES];
+    uint32_t site_count = shape_sites[s];
     for (uint32_t i = 0; i < site_count; i++)
     {
       double c = const_value(p, sites[i].const_index);
@@ -1870,7 +1934,12 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
   }
   else if (!ok && why[0])
     refuse(why);
-  for (uint32_t sh = 0; sh < shapes; sh++) free(exprs[sh]);
+  for (uint32_t sh = 0; sh < shapes; sh++)
+  {
+    free(exprs[sh]);
+    free(shape_words[sh].w);
+  }
+  free(shape_site_list);
   free(view);
   free(plan);
   free(cube_q);
