@@ -699,12 +699,18 @@ class Server:
         sc = np.array([table.col(n) if n is not None else -1 for n in sum_names], dtype=np.int32)
         _check(N.load_ops().cqlserve_prepare(self.h, table.index, ptrs, q, N.ptr(sc)), "cqlserve_prepare")
 
-    def _submit(self, req, keep):
+    def _submit(self, req, keep, submit=True):
         r = ServeRequest(self, req, keep)
-        N.load_ops().cqlserve_submit(self.h, C.byref(req))
+        if submit:
+            N.load_ops().cqlserve_submit(self.h, C.byref(req))
         return r
 
-    def filter_agg(self, table, program, sum_name=None):
+    def submit(self, request):
+        """Queues a request built with submit=False."""
+        N.load_ops().cqlserve_submit(self.h, C.byref(request.req))
+        return request
+
+    def filter_agg(self, table, program, sum_name=None, submit=True):
         """SELECT COUNT(*)[, SUM(sum_name)] WHERE program."""
         if program.names != table.names:
             raise OpError("the program is not built over the table's columns")
@@ -713,9 +719,9 @@ class Server:
         req.table = table.index
         req.program = C.addressof(program.prog)
         req.sum_column = table.col(sum_name) if sum_name is not None else -1
-        return self._submit(req, (program,))
+        return self._submit(req, (program,), submit)
 
-    def agg_global(self, table, names):
+    def agg_global(self, table, names, submit=True):
         """SUM/MIN/MAX of up to 4 columns."""
         req = N.CqlServeRequest()
         req.kind = SERVE_AGG_GLOBAL
@@ -723,9 +729,9 @@ class Server:
         req.column_count = len(names)
         for i, n in enumerate(names):
             req.columns[i] = table.col(n)
-        return self._submit(req, ())
+        return self._submit(req, (), submit)
 
-    def group_dense(self, table, key, funcs, args):
+    def group_dense(self, table, key, funcs, args, submit=True):
         """GROUP BY key (small range) with funcs over args (None for COUNT)."""
         e = len(funcs)
         lo, hi = table.columns[key].zone
@@ -745,7 +751,7 @@ class Server:
             req.args[i] = table.col(a) if a is not None else -1
         req.max_groups = g
         req.out_counts, req.out_sums, req.out_mins, req.out_maxs = (a.ctypes.data for a in (counts, sums, mins, maxs))
-        return self._submit(req, ((), counts, sums, mins, maxs))
+        return self._submit(req, ((), counts, sums, mins, maxs), submit)
 
     def call(self, fn, footprint=0):
         """Runs fn() (-> bool) on a worker, admitted with `footprint` planned device bytes."""
