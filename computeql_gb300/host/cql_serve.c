@@ -10,7 +10,9 @@
  *     request to finish (a request larger than the whole budget fails at once);
  *   - a filter/aggregate request, with fusing on, takes with it every other filter/aggregate request
  *     queued on the same table (up to max_fuse, within the budget): one shared scan answers them all;
- *   - anything else runs alone.
+ *   - any other request takes with it the identical requests queued (same operator, table, columns and
+ *     functions): one run answers them all, its results copied to each;
+ *   - a call request runs alone.
  * The worker runs its work on its own lane, publishes the results and wakes the waiters. Requests that
  * arrive while the scans run queue up and form the next batch.
  */
@@ -177,6 +179,45 @@ static void run_shared(CqlServer* sv, CqlServeRequest** group, uint32_t n)
   free(sumv);
 }
 
+/* two requests that ask the same thing: one run answers both (filter/aggregate requests are fused
+   instead; a call request is never merged) */
+static int same_request(const CqlServeRequest* a, const CqlServeRequest* b)
+{
+  if (a->kind != b->kind || a->table != b->table) return 0;
+  if (a->kind == CQLSERVE_AGG_GLOBAL)
+    return a->column_count == b->column_count && !memcmp(a->columns, b->columns, a->column_count * sizeof(uint32_t));
+  if (a->kind == CQLSERVE_GROUP_DENSE)
+    return a->columns[0] == b->columns[0] && a->expr_count == b->expr_count && a->max_groups == b->max_groups &&
+           !memcmp(a->funcs, b->funcs, a->expr_count * sizeof(uint32_t)) && !memcmp(a->args, b->args, a->expr_count * sizeof(int32_t));
+  return 0;
+}
+
+/* the first request's results, copied to the others that asked the same */
+static void share_results(CqlServeRequest** group, uint32_t n)
+{
+  const CqlServeRequest* h = group[0];
+  for (uint32_t i = 1; i < n; i++)
+  {
+    CqlServeRequest* r = group[i];
+    r->status = h->status;
+    memcpy(r->error, h->error, sizeof(r->error));
+    r->count = h->count;
+    r->min_key = h->min_key;
+    memcpy(r->sum, h->sum, sizeof(r->sum));
+    memcpy(r->min, h->min, sizeof(r->min));
+    memcpy(r->max, h->max, sizeof(r->max));
+    if (h->kind == CQLSERVE_GROUP_DENSE && h->status == 1)
+    {
+      uint64_t g = h->count, e = h->expr_count;
+      memcpy(r->out_counts, h->out_counts, g * sizeof(uint64_t));
+      memcpy(r->out_sums, h->out_sums, g * e * sizeof(int64_t));
+      memcpy(r->out_mins, h->out_mins, g * e * sizeof(int64_t));
+      memcpy(r->out_maxs, h->out_maxs, g * e * sizeof(int64_t));
+    }
+  }
+  for (uint32_t i = 0; i < n; i++) group[i]->fused = n;
+}
+
 /* ---- the queue ---- */
 
 static void unlink_request(CqlServer* sv, CqlServeRequest* prev, CqlServeRequest* r)
@@ -213,15 +254,18 @@ static uint32_t take(CqlServer* sv, CqlServeRequest** group, uint32_t cap, uint6
   group[0] = h;
   uint32_t n = 1;
   uint64_t bytes = fp;
-  if (sv->cfg.fuse && h->kind == CQLSERVE_FILTER_AGG)
+  if (sv->cfg.fuse && h->kind != CQLSERVE_CALL)
   {
+    /* a filter/aggregate request takes the others queued on its table into one shared scan; any other
+       request takes the identical ones queued, which its one run answers */
     CqlServeRequest* prev = NULL;
     CqlServeRequest* r = sv->head;
     while (r && n < cap)
     {
       CqlServeRequest* next = r->next;
-      uint64_t f = footprint(r);
-      if (r->kind == CQLSERVE_FILTER_AGG && r->table == h->table && sv->stats.in_flight_bytes + bytes + f <= budget)
+      uint64_t f = h->kind == CQLSERVE_FILTER_AGG ? footprint(r) : 0;
+      int joins = h->kind == CQLSERVE_FILTER_AGG ? (r->kind == CQLSERVE_FILTER_AGG && r->table == h->table) : same_request(h, r);
+      if (joins && sv->stats.in_flight_bytes + bytes + f <= budget)
       {
         unlink_request(sv, prev, r);
         group[n++] = r;
@@ -283,8 +327,12 @@ static void* worker_main(void* arg)
 
     uint64_t t0 = now_ns();
     for (uint32_t i = 0; i < n; i++) group[i]->start_ns = t0;
-    if (n > 1 || (sv->cfg.fuse && group[0]->kind == CQLSERVE_FILTER_AGG)) run_shared(sv, group, n);
-    else run_alone(sv, group[0]);
+    if (group[0]->kind == CQLSERVE_FILTER_AGG && (n > 1 || sv->cfg.fuse)) run_shared(sv, group, n);
+    else
+    {
+      run_alone(sv, group[0]);
+      if (n > 1) share_results(group, n);
+    }
     uint64_t t1 = now_ns();
 
     pthread_mutex_lock(&sv->lock);
@@ -300,6 +348,8 @@ static void* worker_main(void* arg)
       sv->stats.fused_requests += n;
       if (n > sv->stats.max_fused) sv->stats.max_fused = n;
     }
+    else if (n > 1)
+      sv->stats.merged_requests += n - 1;
     sv->running -= n;
     sv->stats.in_flight_bytes -= bytes;
     pthread_cond_broadcast(&sv->done);

@@ -51,7 +51,7 @@ class CqlServeRequest(C.Structure):
 
 class CqlServeStats(C.Structure):
     _fields_ = [(n, u64) for n in ("submitted", "completed", "failed", "scans", "fused_requests", "max_fused", "in_flight_bytes",
-                                   "peak_in_flight_bytes", "memory_budget", "admission_waits")]
+                                   "peak_in_flight_bytes", "memory_budget", "admission_waits", "merged_requests")]
 
 
 RESIDENT_ALLOC = C.CFUNCTYPE(C.c_void_p, C.c_void_p, u64)

@@ -15,8 +15,9 @@
  *     whole budget fails);
  *   - continuous batching: a free worker takes every filter/aggregate request queued on the same table
  *     (up to max_fuse) and answers them with one shared scan (cqlops_batch_filter_aggregate_cat), so
- *     under load the table is read once per batch rather than once per query. Requests that arrive
- *     while a scan runs form the next batch.
+ *     under load the table is read once per batch rather than once per query; a whole-column aggregate
+ *     or group-by takes the identical requests queued behind it and answers them with one run. Requests
+ *     that arrive while a scan runs form the next batch.
  *
  * Results do not depend on what a request was batched with: counts are exact and the shared scan's sums
  * are exact sums of scaled integers, independent of order and of the other queries.
@@ -37,7 +38,8 @@ typedef struct CqlServer CqlServer;
 typedef struct CqlServeConfig
 {
   uint32_t workers;          /* worker threads, each on its own lane; 0 = 2 */
-  uint32_t fuse;             /* 1: filter/aggregate requests queued on one table run in one shared scan */
+  uint32_t fuse;             /* 1: filter/aggregate requests queued on one table run in one shared scan, and
+                                identical queued requests are answered by one run */
   uint32_t max_fuse;         /* most requests in one shared scan; 0 = 1024 */
   uint32_t rows_per_thread;  /* of the shared scan (4, 8 or 16); 0 = 8 */
   uint64_t memory_budget;    /* planned device bytes the running requests may hold together; 0 = 160 GB,
@@ -81,7 +83,8 @@ typedef struct CqlServeRequest
   double min[4];
   double max[4];
   int32_t status;                 /* 0 queued or running, 1 done, -1 failed (error says why) */
-  uint32_t fused;                 /* requests answered by the shared scan that answered this one (1: alone) */
+  uint32_t fused;                 /* requests answered by the run that answered this one: a shared scan, or
+                                     identical requests merged (1: alone) */
   uint64_t submit_ns;             /* CLOCK_MONOTONIC: submitted, started, finished */
   uint64_t start_ns;
   uint64_t done_ns;
@@ -99,6 +102,7 @@ typedef struct CqlServeStats
   uint64_t peak_in_flight_bytes;
   uint64_t memory_budget;
   uint64_t admission_waits;       /* times the head request waited for memory */
+  uint64_t merged_requests;       /* requests answered by an identical request's run */
 } CqlServeStats;
 
 /* Starts the workers; NULL when a worker's lane cannot be opened (cqlcuda_last_error says why). */

@@ -253,3 +253,29 @@ def test_bad_requests_fail_at_submit(env):
         req2.column_count = 1
         assert native.load_ops().cqlserve_submit(sv.h, native.C.byref(req2)) == 0
         assert b"no such table" in req2.error
+
+
+def test_identical_requests_share_one_run(env):
+    ops, arrays, cols = env
+    with ops.Server(workers=1, fuse=True) as sv:
+        t = sv.add_table(cols)
+        gate = threading.Event()
+        hold = sv.call(lambda: gate.wait(30) or True)
+        groups = [sv.group_dense(t, "k", [ops.FUNC_COUNT, ops.FUNC_SUM, ops.FUNC_MAX], [None, "u1", "u2"]) for _ in range(5)]
+        globs = [sv.agg_global(t, ["u0", "d1"]) for _ in range(3)]
+        other = sv.agg_global(t, ["u3"])
+        gate.set()
+        for r in [hold] + groups + globs + [other]:
+            assert r.wait(60000) and r.ok, r.error
+        stats = sv.stats()
+    d_ref = ops.group_dense(cols["k"], [ops.FUNC_COUNT, ops.FUNC_SUM, ops.FUNC_MAX], [None, cols["u1"], cols["u2"]])
+    for r in groups:
+        got = r.group_result()
+        assert got[0] == d_ref[0] and r.fused == 5
+        for a, b in zip(got[1:], d_ref[1:]):
+            assert np.array_equal(a, b)
+    g_ref = ops.aggregate_global([cols["u0"], cols["d1"]])
+    for r in globs:
+        assert (list(r.req.sum[:2]), list(r.req.min[:2]), list(r.req.max[:2])) == g_ref and r.fused == 3
+    assert other.fused == 1 and other.req.sum[0] == ops.aggregate_global([cols["u3"]])[0][0]
+    assert stats["merged_requests"] == 4 + 2
