@@ -39,7 +39,7 @@ __device__ __forceinline__ uint32_t hash_u32(uint32_t x)
 // ---------------------------------------------------------------------------------------------
 // aggregate_assign: binding 0 owner row per slot, 1 rows per slot, 2 slot per row, 3 overflow count,
 // 4 + 2c / 5 + 2c key column c (f64 values, or string bytes + u64 offsets);
-// words 0 rows, 2 buckets, 4 K, 6 key columns, 8 string mask
+// words 0 rows, 2 buckets, 4 K, 6 key columns, 8 string mask, 10 1 = count atomics per lane (many groups)
 
 struct KeyCols
 {
@@ -94,6 +94,14 @@ __device__ bool keys_equal(const KeyCols& k, uint32_t ncols, uint32_t string_mas
   return true;
 }
 
+// The lanes of the warp that share this lane's tag, for one atomic per distinct tag. With many groups
+// (alone: the host knows or was told there are thousands) a warp's lanes almost never share one, and a
+// lane's own atomic costs less than the match instruction that would find its peers.
+__device__ __forceinline__ uint32_t combine_peers(uint32_t tag, bool alone, uint32_t lane)
+{
+  return alone ? (1u << lane) : __match_any_sync(0xffffffffu, tag);
+}
+
 __global__ void __launch_bounds__(HASH_THREADS) k_aggregate_assign(CqlLaunch a, uint64_t rows)
 {
   uint32_t* owner = (uint32_t*)a.buf[0];
@@ -101,6 +109,7 @@ __global__ void __launch_bounds__(HASH_THREADS) k_aggregate_assign(CqlLaunch a, 
   uint32_t* row_slot = (uint32_t*)a.buf[2];
   uint32_t* overflow = (uint32_t*)a.buf[3];
   uint32_t buckets = cql_word(a, 2), K = cql_word(a, 4), ncols = cql_word(a, 6), string_mask = cql_word(a, 8);
+  bool alone = cql_word(a, 10) != 0;
   if (ncols > 4) ncols = 4;
   KeyCols k;
   for (int c = 0; c < 4; c++)
@@ -133,7 +142,7 @@ __global__ void __launch_bounds__(HASH_THREADS) k_aggregate_assign(CqlLaunch a, 
     if (valid && claimed != EMPTY_SLOT) row_slot[row] = claimed;
     // one count atomic per distinct slot of the warp (few groups would otherwise serialise on them)
     uint32_t tag = valid ? claimed : PAST_END;
-    uint32_t peers = __match_any_sync(0xffffffffu, tag);
+    uint32_t peers = combine_peers(tag, alone, lane);
     if (lane == (uint32_t)(__ffs(peers) - 1) && tag != PAST_END)
     {
       if (claimed == EMPTY_SLOT) atomicAdd(overflow, (uint32_t)__popc(peers));
@@ -330,7 +339,8 @@ extern "C" int cqlcuda_compact_slots_noalloc(const uint32_t* slot_counts, const 
 
 // ---------------------------------------------------------------------------------------------
 // aggregate_hash_reduce_fixed: binding 0 slot per row, 1 group per slot, 2 sums (lo, hi), 3 counts,
-// 4 mins, 5 maxs, 6..13 f64 arguments; words 0 rows, 2 exprs, 4 funcs, 6 power-of-ten exponents
+// 4 mins, 5 maxs, 6..13 f64 arguments; words 0 rows, 2 exprs, 4 funcs, 6 power-of-ten exponents,
+// 8 1 = atomics per lane (many groups)
 
 #define FUNC_COUNT 0u
 #define FUNC_SUM 1u
@@ -350,6 +360,7 @@ __global__ void __launch_bounds__(HASH_THREADS) k_hash_reduce_fixed(CqlLaunch a,
   int* mins = (int*)a.buf[4];
   int* maxs = (int*)a.buf[5];
   uint32_t exprs = min(cql_word(a, 2), 8u), funcs = cql_word(a, 4), scales = cql_word(a, 6);
+  bool alone = cql_word(a, 8) != 0;
   uint64_t nslots = a.bytes[1] / 4;
   uint32_t lane = threadIdx.x & 31u;
   // whole warps take every iteration, so the lanes of one group combine before a single atomic
@@ -365,7 +376,7 @@ __global__ void __launch_bounds__(HASH_THREADS) k_hash_reduce_fixed(CqlLaunch a,
         if (gg != EMPTY_SLOT) g = gg;
       }
     }
-    uint32_t peers = __match_any_sync(0xffffffffu, g);
+    uint32_t peers = combine_peers(g, alone, lane);
     bool leader = lane == (uint32_t)(__ffs(peers) - 1) && g != PAST_END;
     for (uint32_t e = 0; e < exprs; e++)
     {
@@ -377,17 +388,23 @@ __global__ void __launch_bounds__(HASH_THREADS) k_hash_reduce_fixed(CqlLaunch a,
       int q = 0;
       if (g != PAST_END)
         q = fix_scaled(fix_decode_f64(((const unsigned long long*)a.buf[6 + e])[row]), (int)min((scales >> (e * 4)) & 0xfu, 6u));
-      long long acc = 0;
-      int mn = 0x7fffffff, mx = (int)0x80000000;
-#pragma unroll 8
-      for (int src = 0; src < 32; src++)
+      long long acc = q;
+      int mn = q, mx = q;
+      if (!alone)
       {
-        int v = __shfl_sync(0xffffffffu, q, src);
-        if ((peers >> src) & 1u)
+        acc = 0;
+        mn = 0x7fffffff;
+        mx = (int)0x80000000;
+#pragma unroll 8
+        for (int src = 0; src < 32; src++)
         {
-          acc += v;
-          mn = min(mn, v);
-          mx = max(mx, v);
+          int v = __shfl_sync(0xffffffffu, q, src);
+          if ((peers >> src) & 1u)
+          {
+            acc += v;
+            mn = min(mn, v);
+            mx = max(mx, v);
+          }
         }
       }
       if (!leader) continue;
@@ -411,7 +428,8 @@ static int launch_hash_reduce_fixed(const CqlLaunch& a, uint32_t gws, uint32_t l
 
 // ---------------------------------------------------------------------------------------------
 // csr_scatter (and the tiled variant, same bindings plus the slot count in slot 1): every row takes
-// the next place of its slot's member list through the slot's cursor
+// the next place of its slot's member list through the slot's cursor; word 0 rows, word 2 1 = one
+// atomic per lane (many slots)
 
 __global__ void __launch_bounds__(HASH_THREADS) k_csr_scatter(CqlLaunch a, uint64_t rows)
 {
@@ -419,13 +437,14 @@ __global__ void __launch_bounds__(HASH_THREADS) k_csr_scatter(CqlLaunch a, uint6
   uint32_t* cursor = (uint32_t*)a.buf[1];
   uint32_t* out_rows = (uint32_t*)a.buf[2];
   uint64_t cap = a.bytes[2] / 4, slots = a.bytes[1] / 4;
+  bool alone = cql_word(a, 2) != 0;
   uint32_t lane = threadIdx.x & 31u;
   for (uint64_t row = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; row - lane < rows; row += (uint64_t)gridDim.x * blockDim.x)
   {
     uint32_t slot = row < rows ? row_slot[row] : EMPTY_SLOT;
     if (slot >= slots) slot = EMPTY_SLOT;
     // lanes of one slot take consecutive places with one atomic
-    uint32_t peers = __match_any_sync(0xffffffffu, slot);
+    uint32_t peers = combine_peers(slot, alone, lane);
     uint32_t leader = (uint32_t)(__ffs(peers) - 1);
     uint32_t base = 0;
     if (lane == leader && slot != EMPTY_SLOT) base = atomicAdd(&cursor[slot], (uint32_t)__popc(peers));
@@ -469,83 +488,158 @@ __device__ __forceinline__ void hll_add(uint32_t* sketch, uint64_t sketch_words,
   if (idx < sketch_words) atomicMax(&sketch[idx], rho);
 }
 
+struct ReduceArgs
+{
+  const uint32_t* members;
+  uint32_t* repr;
+  double* partials;
+  uint32_t* sketch;
+  float* dmean;
+  float* dweight;
+  uint64_t sketch_words, digest_cap, partial_cap;
+  uint32_t exprs, funcs, p, hll_slots, nhll, npct, pct_slots;
+  bool identity;
+};
+
+__device__ __forceinline__ void reduce_store(const ReduceArgs& r, uint32_t c, uint32_t e, double acc, uint32_t count, double mn, double mx)
+{
+  uint64_t base = ((uint64_t)c * r.exprs + e) * 4;
+  if (base + 3 < r.partial_cap)
+  {
+    r.partials[base + 0] = acc;
+    r.partials[base + 1] = (double)count;
+    r.partials[base + 2] = mn;
+    r.partials[base + 3] = mx;
+  }
+}
+
+// One chunk by the whole warp, in the reference's layout: this lane stands for reference lanes
+// t = lane + 32 j, j = 0..7, each taking members start + t, start + t + 256, ...; the t-digest's
+// per-lane centroids (the first value and the count of each reference lane) need exactly this layout.
+__device__ __forceinline__ void reduce_chunk_warp(const CqlLaunch& a, const ReduceArgs& r, uint32_t c, uint32_t start, uint32_t end, uint32_t g, uint32_t lane)
+{
+  if (lane == 0 && (r.identity || end > start)) r.repr[g] = r.identity ? start : r.members[start];
+  for (uint32_t e = 0; e < r.exprs; e++)
+  {
+    uint32_t f = (r.funcs >> (e * 4)) & 0xfu;
+    const double* arg = (const double*)a.buf[5 + e];
+    double acc = 0.0, mn = 1.0e300, mx = -1.0e300;
+    uint32_t count = 0;
+    for (uint32_t j = 0; j < 8; j++)
+    {
+      uint32_t t = lane + 32 * j;
+      double first = 0.0;
+      uint32_t tcount = 0;
+      for (uint32_t m = start + t; m < end; m += 256)
+      {
+        uint32_t row = r.identity ? m : r.members[m];
+        tcount++;
+        if (f == FUNC_SUM || f == FUNC_AVG) acc += arg[row];
+        else if (f == FUNC_MIN) { double v = arg[row]; if (v < mn) mn = v; }
+        else if (f == FUNC_MAX) { double v = arg[row]; if (v > mx) mx = v; }
+        else if (f == FUNC_ACD) hll_add(r.sketch, r.sketch_words, (r.hll_slots >> (e * 4)) & 0xfu, g, r.nhll, r.p, arg[row]);
+        else if (f == FUNC_PCT && tcount == 1) first = arg[row];
+      }
+      count += tcount;
+      if (f == FUNC_PCT)
+      {
+        uint64_t di = ((uint64_t)c * r.npct + ((r.pct_slots >> (e * 4)) & 0xfu)) * 256u + t;
+        if (di < r.digest_cap)
+        {
+          r.dmean[di] = (float)first;
+          r.dweight[di] = (float)tcount;
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+      acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      double omn = __shfl_xor_sync(0xffffffffu, mn, o);
+      double omx = __shfl_xor_sync(0xffffffffu, mx, o);
+      mn = omn < mn ? omn : mn;
+      mx = omx > mx ? omx : mx;
+      count += __shfl_xor_sync(0xffffffffu, count, o);
+    }
+    if (lane == 0) reduce_store(r, c, e, acc, count, mn, mx);
+  }
+}
+
+// One small chunk by one lane, its members in order: the same partials (sums in another order, within
+// rounding of the warp's), for chunks of a few members, where the warp form spends most of its
+// instructions on empty reference lanes and cross-lane reductions.
+__device__ __forceinline__ void reduce_chunk_lane(const CqlLaunch& a, const ReduceArgs& r, uint32_t c, uint32_t start, uint32_t end, uint32_t g)
+{
+  if (r.identity || end > start) r.repr[g] = r.identity ? start : r.members[start];
+  for (uint32_t e = 0; e < r.exprs; e++)
+  {
+    uint32_t f = (r.funcs >> (e * 4)) & 0xfu;
+    const double* arg = (const double*)a.buf[5 + e];
+    double acc = 0.0, mn = 1.0e300, mx = -1.0e300;
+    if (f == FUNC_SUM || f == FUNC_AVG || f == FUNC_MIN || f == FUNC_MAX || f == FUNC_ACD)
+      for (uint32_t m = start; m < end; m++)
+      {
+        uint32_t row = r.identity ? m : r.members[m];
+        double v = arg[row];
+        if (f == FUNC_SUM || f == FUNC_AVG) acc += v;
+        else if (f == FUNC_MIN) { if (v < mn) mn = v; }
+        else if (f == FUNC_MAX) { if (v > mx) mx = v; }
+        else hll_add(r.sketch, r.sketch_words, (r.hll_slots >> (e * 4)) & 0xfu, g, r.nhll, r.p, v);
+      }
+    reduce_store(r, c, e, acc, end - start, mn, mx);
+  }
+}
+
+#define REDUCE_LANE_CHUNK 64   // chunks of at most this many members are reduced by one lane
+
 __global__ void __launch_bounds__(HASH_THREADS) k_aggregate_reduce(CqlLaunch a, uint32_t chunks)
 {
-  const uint32_t* members = (const uint32_t*)a.buf[0];
   const uint32_t* range = (const uint32_t*)a.buf[1];
   const uint32_t* chunk_group = (const uint32_t*)a.buf[2];
-  uint32_t* repr = (uint32_t*)a.buf[3];
-  double* partials = (double*)a.buf[4];
-  uint32_t* sketch = (uint32_t*)a.buf[13];
-  float* dmean = (float*)a.buf[14];
-  float* dweight = (float*)a.buf[15];
-  uint64_t sketch_words = a.bytes[13] / 4, digest_cap = a.bytes[14] / 4, partial_cap = a.bytes[4] / 8;
-  uint32_t exprs = min(cql_word(a, 2), 8u), funcs = cql_word(a, 4);
-  bool identity = cql_word(a, 6) != 0;
-  uint32_t p = cql_word(a, 8), hll_slots = cql_word(a, 10), nhll = cql_word(a, 12);
-  uint32_t npct = cql_word(a, 14), pct_slots = cql_word(a, 15);
-  if (p > 16) p = 16;
+  ReduceArgs r;
+  r.members = (const uint32_t*)a.buf[0];
+  r.repr = (uint32_t*)a.buf[3];
+  r.partials = (double*)a.buf[4];
+  r.sketch = (uint32_t*)a.buf[13];
+  r.dmean = (float*)a.buf[14];
+  r.dweight = (float*)a.buf[15];
+  r.sketch_words = a.bytes[13] / 4;
+  r.digest_cap = a.bytes[14] / 4;
+  r.partial_cap = a.bytes[4] / 8;
+  r.exprs = min(cql_word(a, 2), 8u);
+  r.funcs = cql_word(a, 4);
+  r.identity = cql_word(a, 6) != 0;
+  r.p = min(cql_word(a, 8), 16u);
+  r.hll_slots = cql_word(a, 10);
+  r.nhll = cql_word(a, 12);
+  r.npct = cql_word(a, 14);
+  r.pct_slots = cql_word(a, 15);
   uint32_t lane = threadIdx.x & 31;
   uint32_t warps_total = gridDim.x * (blockDim.x / 32);
-  for (uint32_t c = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); c < chunks; c += warps_total)
+  uint32_t warp_id = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  // a warp takes 32 chunks spaced the grid's warp count apart: each lane reduces a small one alone,
+  // then the warp reduces the large ones together (all of them when a percentile needs the reference's
+  // lane layout); the spacing spreads a run of large chunks (one large group's) over many warps
+  for (uint64_t first = warp_id; first < chunks; first += 32ull * warps_total)
   {
-    uint32_t start = range[c * 2], end = range[c * 2 + 1];
-    uint32_t g = chunk_group[c];
-    if (lane == 0) repr[g] = identity ? start : members[start];
-    for (uint32_t e = 0; e < exprs; e++)
+    uint64_t c = first + (uint64_t)lane * warps_total;
+    uint32_t start = 0, end = 0, g = 0;
+    bool have = c < chunks;
+    if (have)
     {
-      uint32_t f = (funcs >> (e * 4)) & 0xfu;
-      const double* arg = (const double*)a.buf[5 + e];
-      double acc = 0.0, mn = 1.0e300, mx = -1.0e300;
-      uint32_t count = 0;
-      // this lane stands for reference lanes t = lane + 32 j, j = 0..7
-      for (uint32_t j = 0; j < 8; j++)
-      {
-        uint32_t t = lane + 32 * j;
-        double first = 0.0;
-        uint32_t tcount = 0;
-        for (uint32_t m = start + t; m < end; m += 256)
-        {
-          uint32_t row = identity ? m : members[m];
-          tcount++;
-          if (f == FUNC_SUM || f == FUNC_AVG) acc += arg[row];
-          else if (f == FUNC_MIN) { double v = arg[row]; if (v < mn) mn = v; }
-          else if (f == FUNC_MAX) { double v = arg[row]; if (v > mx) mx = v; }
-          else if (f == FUNC_ACD) hll_add(sketch, sketch_words, (hll_slots >> (e * 4)) & 0xfu, g, nhll, p, arg[row]);
-          else if (f == FUNC_PCT && tcount == 1) first = arg[row];
-        }
-        count += tcount;
-        if (f == FUNC_PCT)
-        {
-          uint64_t di = ((uint64_t)c * npct + ((pct_slots >> (e * 4)) & 0xfu)) * 256u + t;
-          if (di < digest_cap)
-          {
-            dmean[di] = (float)first;
-            dweight[di] = (float)tcount;
-          }
-        }
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1)
-      {
-        acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        double omn = __shfl_xor_sync(0xffffffffu, mn, o);
-        double omx = __shfl_xor_sync(0xffffffffu, mx, o);
-        mn = omn < mn ? omn : mn;
-        mx = omx > mx ? omx : mx;
-        count += __shfl_xor_sync(0xffffffffu, count, o);
-      }
-      if (lane == 0)
-      {
-        uint64_t base = ((uint64_t)c * exprs + e) * 4;
-        if (base + 3 < partial_cap)
-        {
-          partials[base + 0] = acc;
-          partials[base + 1] = (double)count;
-          partials[base + 2] = mn;
-          partials[base + 3] = mx;
-        }
-      }
+      start = range[c * 2];
+      end = range[c * 2 + 1];
+      g = chunk_group[c];
+    }
+    bool alone = have && r.npct == 0 && end - start <= REDUCE_LANE_CHUNK;
+    if (alone) reduce_chunk_lane(a, r, (uint32_t)c, start, end, g);
+    uint32_t big = __ballot_sync(0xffffffffu, have && !alone);
+    while (big)
+    {
+      uint32_t src = (uint32_t)(__ffs(big) - 1);
+      big &= big - 1;
+      uint32_t bs = __shfl_sync(0xffffffffu, start, src), be = __shfl_sync(0xffffffffu, end, src), bg = __shfl_sync(0xffffffffu, g, src);
+      reduce_chunk_warp(a, r, (uint32_t)(first + (uint64_t)src * warps_total), bs, be, bg, lane);
     }
   }
 }
@@ -556,6 +650,7 @@ static int launch_aggregate_reduce(const CqlLaunch& a, uint32_t gws, uint32_t lw
   (void)lws;
   uint32_t chunks = cql_word(a, 0);
   if (chunks == 0) return 0;
+  // a warp per chunk up to the resident grid (the large chunks' parallelism), 32 chunks a warp beyond
   uint32_t warps = HASH_THREADS / 32;
   k_aggregate_reduce<<<cql_stream_grid((chunks + warps - 1) / warps, 8), HASH_THREADS, 0, stream>>>(a, chunks);
   CQL_LAUNCH_CHECK();

@@ -19,7 +19,7 @@
 //                     selection's row instead of the position, word 8 1 = write no keys (the last pass)
 //
 // A tile is 8 warps x 16 rounds x 32 rows = 4096 rows. The scatter ranks a row within its tile in input
-// order: __match_any_sync finds the lanes of a round with the same digit, per-warp digit counters carry
+// order: eight ballots find the lanes of a round with the same digit, per-warp digit counters carry
 // the rounds, and a prefix over the warps orders the warps; the global base of (digit, tile) comes from
 // an exclusive scan of the digit-major histogram (the prefix_sum kernel).
 #include "cql_internal.cuh"
@@ -130,14 +130,41 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_count(CqlLaunch a, uint6
 }
 
 // The scatter of one tile: rank every key within the tile in input order (per-warp counters, lanes of
-// one digit found with __match_any_sync), place the tile in shared memory in digit order, then write
+// one digit found by ballots), place the tile in shared memory in digit order, then write
 // it out in that order, so consecutive threads write consecutive places of each digit's run.
+//
+// The kernel is bound by the latency of the ranking's shared-memory chain, so it is built for several
+// resident CTAs per SM: only the keys and their ranks live in registers while a tile is ranked (the
+// positions are read once the ranks are known), within the register budget of 4 CTAs (3 for 8-byte keys).
+#define SORT_SCATTER_CTAS(K) (sizeof(K) == 4 ? 4 : 3)
+
+// The lanes of the warp whose digit equals this lane's, from one ballot per digit bit (the match
+// instruction is far slower); a ninth bit marks the lanes past the end in the last, partial tile.
+__device__ __forceinline__ uint32_t same_digit_lanes(uint32_t dg, bool partial)
+{
+  uint32_t peers = 0xffffffffu;
+#pragma unroll
+  for (uint32_t b = 0; b < 8; b++)
+  {
+    uint32_t bit = (dg >> b) & 1u;
+    uint32_t m = __ballot_sync(0xffffffffu, bit);
+    peers &= bit ? m : ~m;
+  }
+  if (partial)
+  {
+    uint32_t bit = (dg >> 8) & 1u;
+    uint32_t m = __ballot_sync(0xffffffffu, bit);
+    peers &= bit ? m : ~m;
+  }
+  return peers;
+}
+
 template <typename K>
-__global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(CqlLaunch a, uint64_t n, uint32_t tiles)
+__global__ void __launch_bounds__(SORT_THREADS, SORT_SCATTER_CTAS(K)) k_radix_scatter(CqlLaunch a, uint64_t n, uint32_t tiles)
 {
   __shared__ uint32_t warp_count[SORT_WARPS][RADIX];
-  __shared__ uint32_t s_base[RADIX];     // global place of the tile's first key of each digit
   __shared__ uint32_t s_start[RADIX];    // place of each digit's first key inside the tile
+  __shared__ uint32_t s_off[RADIX];      // global place of a tile place j of the digit: s_off + j (mod 2^32)
   __shared__ uint32_t s_warp_total[SORT_WARPS];
   extern __shared__ __align__(16) unsigned char s_tile[];
   K* s_key = (K*)s_tile;
@@ -155,37 +182,36 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(CqlLaunch a, uin
   for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x)
   {
     for (uint32_t i = threadIdx.x; i < SORT_WARPS * RADIX; i += SORT_THREADS) (&warp_count[0][0])[i] = 0;
-    for (uint32_t d = threadIdx.x; d < RADIX; d += SORT_THREADS) s_base[d] = base_of[(uint64_t)d * tiles + tile];
-    // each warp owns 16 rounds of 32 consecutive rows; its keys and positions are loaded up front
+    // each warp owns 16 rounds of 32 consecutive rows; its keys are loaded up front
     uint64_t tile_first = (uint64_t)tile * SORT_TILE;
     uint32_t tile_rows = (uint32_t)min((uint64_t)SORT_TILE, n - tile_first);
+    bool partial = tile_rows != SORT_TILE;
     uint64_t warp_base = tile_first + (uint64_t)warp * 32 * SORT_ROUNDS;
     K key[SORT_ROUNDS];
-    uint32_t pos[SORT_ROUNDS];
 #pragma unroll
     for (uint32_t r = 0; r < SORT_ROUNDS; r++)
     {
       uint64_t i = warp_base + (uint64_t)r * 32 + lane;
       key[r] = i < n ? keys_in[i] : (K)0;
-      pos[r] = i < n ? pos_in[i] : 0u;
     }
+    uint32_t d = threadIdx.x;
+    uint32_t tile_base = base_of[(uint64_t)d * tiles + tile];
     __syncthreads();
     uint32_t local[SORT_ROUNDS];
 #pragma unroll
     for (uint32_t r = 0; r < SORT_ROUNDS; r++)
     {
       uint64_t i = warp_base + (uint64_t)r * 32 + lane;
-      uint32_t d = i < n ? ((uint32_t)(key[r] >> shift) & 0xffu) : RADIX;  // RADIX: past the end
-      uint32_t peers = __match_any_sync(0xffffffffu, d);
-      uint32_t before = d < RADIX ? warp_count[warp][d] : 0u;
+      uint32_t dg = i < n ? ((uint32_t)(key[r] >> shift) & 0xffu) : RADIX;  // RADIX: past the end
+      uint32_t peers = same_digit_lanes(dg, partial);
+      uint32_t before = dg < RADIX ? warp_count[warp][dg] : 0u;
       local[r] = before + __popc(peers & lt);
       __syncwarp();
-      if (d < RADIX && (peers & lt) == 0) warp_count[warp][d] = before + __popc(peers);
+      if (dg < RADIX && (peers & lt) == 0) warp_count[warp][dg] = before + __popc(peers);
       __syncwarp();
     }
     __syncthreads();
     // per digit (one per thread): the warps before each warp, and the digit's total in the tile
-    uint32_t d = threadIdx.x;
     uint32_t run = 0;
 #pragma unroll
     for (uint32_t w = 0; w < SORT_WARPS; w++)
@@ -206,18 +232,31 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(CqlLaunch a, uin
     __syncthreads();
     uint32_t warp_prefix = 0;
     for (uint32_t w = 0; w < warp; w++) warp_prefix += s_warp_total[w];
-    s_start[d] = warp_prefix + incl - run;
+    uint32_t start = warp_prefix + incl - run;
+    s_start[d] = start;
+    s_off[d] = tile_base - start;
     __syncthreads();
-    // the tile in digit order, in shared memory
+    // the tile in digit order, in shared memory: the keys, then the positions read now
 #pragma unroll
     for (uint32_t r = 0; r < SORT_ROUNDS; r++)
     {
       uint64_t i = warp_base + (uint64_t)r * 32 + lane;
-      if (i >= n) continue;
-      uint32_t dd = (uint32_t)(key[r] >> shift) & 0xffu;
-      uint32_t at = s_start[dd] + warp_count[warp][dd] + local[r];
-      s_key[at] = key[r];
-      s_pos[at] = pos[r];
+      uint32_t dg = (uint32_t)(key[r] >> shift) & 0xffu;
+      local[r] += s_start[dg] + warp_count[warp][dg];
+      if (i < n) s_key[local[r]] = key[r];
+    }
+    uint32_t pos[SORT_ROUNDS];
+#pragma unroll
+    for (uint32_t r = 0; r < SORT_ROUNDS; r++)
+    {
+      uint64_t i = warp_base + (uint64_t)r * 32 + lane;
+      pos[r] = i < n ? pos_in[i] : 0u;
+    }
+#pragma unroll
+    for (uint32_t r = 0; r < SORT_ROUNDS; r++)
+    {
+      uint64_t i = warp_base + (uint64_t)r * 32 + lane;
+      if (i < n) s_pos[local[r]] = pos[r];
     }
     __syncthreads();
     // out in order: place j of the tile goes to its digit's global base plus its place in the run
@@ -225,7 +264,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(CqlLaunch a, uin
     {
       K k = s_key[j];
       uint32_t dd = (uint32_t)(k >> shift) & 0xffu;
-      uint64_t dst = (uint64_t)s_base[dd] + (j - s_start[dd]);
+      uint64_t dst = (uint32_t)(s_off[dd] + j);
       if (dst < n)
       {
         if (write_keys) keys_out[dst] = k;
@@ -306,6 +345,7 @@ static int launch_radix_scatter(const CqlLaunch& a, uint32_t gws, uint32_t lws, 
   const void* fn = kb == 4 ? (const void*)k_radix_scatter<uint32_t> : (const void*)k_radix_scatter<unsigned long long>;
   // dynamic plus static shared memory passes the default 48 KB for 8-byte keys: opt in
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   int per_sm = 1;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, SORT_THREADS, smem) != cudaSuccess || per_sm < 1) per_sm = 1;
   uint32_t grid = cql_stream_grid(tiles, per_sm);

@@ -22,6 +22,9 @@
 #define QE_GPU_WORKGROUP_SIZE 256
 #define EMPTY 0xffffffffu
 #define AGG_ROWS_PER_CHUNK 4096
+/* from this many groups on, a warp's rows rarely share a group: per-row atomics instead of combining
+   the warp's lanes of one group first */
+#define AGG_MANY_GROUPS 4096
 #define HLL_PRECISION 10
 #define HLL_SKETCH_MAX_BYTES (64ull << 20)
 
@@ -234,6 +237,7 @@ static int csr_reduce(uint64_t rows, uint64_t slots, uint64_t groups, CqlBuffer*
     cqlcuda_kernel_set_arg_buffer(scatter, 1, cursor_buf);
     cqlcuda_kernel_set_arg_buffer(scatter, 2, members);
     cqlcuda_kernel_set_arg_u64(scatter, 0, rows);
+    cqlcuda_kernel_set_arg_u64(scatter, 1, groups >= AGG_MANY_GROUPS);
     cqlcuda_kernel_set_arg_buffer(reduce, 0, members);
     cqlcuda_kernel_set_arg_buffer(reduce, 1, range_buf);
     cqlcuda_kernel_set_arg_buffer(reduce, 2, group_buf);
@@ -460,6 +464,7 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
     cqlcuda_kernel_set_arg_u64(assign, 2, K);
     cqlcuda_kernel_set_arg_u64(assign, 3, key_count);
     cqlcuda_kernel_set_arg_u64(assign, 4, string_mask);
+    cqlcuda_kernel_set_arg_u64(assign, 5, group_hint >= AGG_MANY_GROUPS);
     uint32_t over = 0;
     CqlBatch* b = cqlcuda_batch_begin(0, 4);
     cqlcuda_batch_buffer_fill(b, owner, slots * 4, EMPTY);
@@ -564,6 +569,7 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
       cqlcuda_kernel_set_arg_u64(hr, 1, expr_count);
       cqlcuda_kernel_set_arg_u64(hr, 2, func_codes);
       cqlcuda_kernel_set_arg_u64(hr, 3, fixed_scales);
+      cqlcuda_kernel_set_arg_u64(hr, 4, groups >= AGG_MANY_GROUPS);
       CqlBatch* b = cqlcuda_batch_begin(0, cells * 16);
       cqlcuda_batch_buffer_zero(b, sums, cells * 8);
       cqlcuda_batch_buffer_zero(b, cnts, cells * 4);

@@ -118,6 +118,7 @@ int cqlops_hash_join(const CqlColumn* build_key, const CqlColumn* probe_key, int
   cqlcuda_kernel_set_arg_buffer(scatter, 1, cursor);
   cqlcuda_kernel_set_arg_buffer(scatter, 2, bucket_rows);
   cqlcuda_kernel_set_arg_u64(scatter, 0, brows);
+  cqlcuda_kernel_set_arg_u64(scatter, 1, 0);   /* build keys may repeat: combine a warp's rows of one bucket */
   {
     CqlBatch* b = cqlcuda_batch_begin(0, 0);
     cqlcuda_batch_buffer_zero(b, counts, buckets * 4);
