@@ -196,37 +196,65 @@ __global__ void __launch_bounds__(JOIN_THREADS) k_join_probe(CqlLaunch a, uint64
   uint64_t cap_words = a.bytes[6] / 16;
   if (cap_words < capacity) capacity = (uint32_t)cap_words;
   if (!buckets) return;
-  for (uint64_t row = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; row < probe_rows; row += (uint64_t)gridDim.x * blockDim.x)
+  uint32_t lane = threadIdx.x & 31u;
+  // whole warps take every iteration: a warp counts its lanes' pairs, takes their places with one
+  // atomic on the pair count (one per pair serialised on that counter), then writes them
+  for (uint64_t row = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; row - lane < probe_rows; row += (uint64_t)gridDim.x * blockDim.x)
   {
-    uint32_t h;
-    if (is_str)
+    bool valid = row < probe_rows;
+    uint32_t start = 0, end = 0;
+    double pv = 0.0;
+    if (valid)
     {
-      uint32_t s = po[row * 2], e = po[(row + 1) * 2];
-      h = 2166136261u;
-      const unsigned char* b = (const unsigned char*)pd;
-      for (uint32_t i = s; i < e; i++) h = (h ^ b[i]) * 16777619u;
+      uint32_t h;
+      if (is_str)
+      {
+        uint32_t s = po[row * 2], e = po[(row + 1) * 2];
+        h = 2166136261u;
+        const unsigned char* b = (const unsigned char*)pd;
+        for (uint32_t i = s; i < e; i++) h = (h ^ b[i]) * 16777619u;
+      }
+      else
+      {
+        h = num_hash(pd, row);
+        pv = __hiloint2double((int)pd[row * 2 + 1], (int)pd[row * 2]);
+      }
+      uint32_t bucket = h % buckets;
+      start = bucket_off[bucket];
+      end = bucket_off[bucket + 1];
     }
-    else h = num_hash(pd, row);
-    uint32_t bucket = h % buckets;
-    uint32_t start = bucket_off[bucket], end = bucket_off[bucket + 1];
-    bool found = false;
-    double pv = is_str ? 0.0 : __hiloint2double((int)pd[row * 2 + 1], (int)pd[row * 2]);
+    uint32_t matches = 0;
     for (uint32_t m = start; m < end; m++)
     {
       uint32_t brow = bucket_rows[m];
-      bool eq = is_str ? str_equal(bd, bo, brow, pd, po, row) : (__hiloint2double((int)bd[brow * 2 + 1], (int)bd[brow * 2]) == pv);
-      if (eq)
+      if (is_str ? str_equal(bd, bo, brow, pd, po, row) : (__hiloint2double((int)bd[brow * 2 + 1], (int)bd[brow * 2]) == pv)) matches++;
+    }
+    uint32_t out = matches ? matches : (valid && left ? 1u : 0u);
+    uint32_t incl = out;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += y;
+    }
+    uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t base = 0;
+    if (lane == 0 && total) base = atomicAdd(count, total);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    uint64_t pos = (uint64_t)base + incl - out;
+    if (matches)
+    {
+      for (uint32_t m = start; m < end; m++)
       {
-        found = true;
-        uint32_t pos = atomicAdd(count, 1u);
-        if (pos < capacity) *(uint4*)(pairs + (uint64_t)pos * 4) = make_uint4((uint32_t)row, 0u, brow, 0u);
+        uint32_t brow = bucket_rows[m];
+        if (is_str ? str_equal(bd, bo, brow, pd, po, row) : (__hiloint2double((int)bd[brow * 2 + 1], (int)bd[brow * 2]) == pv))
+        {
+          if (pos < capacity) *(uint4*)(pairs + pos * 4) = make_uint4((uint32_t)row, 0u, brow, 0u);
+          pos++;
+        }
       }
     }
-    if (!found && left)
-    {
-      uint32_t pos = atomicAdd(count, 1u);
-      if (pos < capacity) *(uint4*)(pairs + (uint64_t)pos * 4) = make_uint4((uint32_t)row, 0u, BUILD_NULL, BUILD_NULL);
-    }
+    else if (out && pos < capacity) *(uint4*)(pairs + pos * 4) = make_uint4((uint32_t)row, 0u, BUILD_NULL, BUILD_NULL);
   }
 }
 
