@@ -27,7 +27,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["runtime.cu", "k_aggregate.cu", "k_scan.cu", "k_hash.cu", "k_join.cu", "k_sort.cu", "k_fixed.cu", "k_window.cu"]
-C_SOURCES = ["cql_ops.c", "cql_program.c", "cql_codegen.c", "cql_ops_filter.c", "cql_ops_hash.c", "cql_ops_join.c", "cql_ops_sort.c", "cql_ops_fixed.c", "cql_zonemap.c", "cql_pool.c", "cql_batch.c", "cql_serve.c", "cql_having.c", "cql_resident.c"]
+C_SOURCES = ["cql_ops.c", "cql_program.c", "cql_codegen.c", "cql_ops_filter.c", "cql_ops_hash.c", "cql_ops_join.c", "cql_ops_sort.c", "cql_ops_fixed.c", "cql_zonemap.c", "cql_pool.c", "cql_batch.c", "cql_serve.c", "cql_having.c", "cql_resident.c", "cql_gather.c"]
 
 LIB_CUDA = os.path.join(PKG, "libcqlcuda.so")
 LIB_OPS = os.path.join(PKG, "libcqlops.so")

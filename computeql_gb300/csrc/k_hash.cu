@@ -712,6 +712,131 @@ static int launch_selection_gather(const CqlLaunch& a, uint32_t gws, uint32_t lw
 }
 
 // ---------------------------------------------------------------------------------------------
+// Row materialization: the values of the selected rows of many columns, the multi-column form of the
+// reference's per-column gathers (selection_gather.comp modes 0 and 1, qe_selection_gather_column
+// query_exec.c:4371-4410). One launch covers up to GATHER_COLUMNS columns, column j on blockIdx.y,
+// so the selected row numbers are read once per column from L2 and every store is coalesced.
+//
+//  cql_gather_columns  binding 0 selected rows (u32), 1 per-column params (u32 x 4: kind, base,
+//                      destination byte offset lo, hi), 2 destination, 3.. the columns' buffers;
+//                      word 0 count, word 2 1 = rows given (else rows 0..count-1), word 4 columns.
+//                      kind 0 4-byte values, 1 u8 codes (base + code), 2 u16 codes, 3 a sequence
+//                      (base + row, nothing read), 4 8-byte values, 5 1-byte values (BOOL)
+//  cql_gather_string_lengths  binding 0 rows, 1 the column's (rows + 1) u64 offsets, 2 lengths (u32);
+//                      word 0 count, word 2 rows given
+//  cql_gather_string_bytes    binding 0 rows, 1 offsets (u64), 2 the column's bytes, 3 output offsets
+//                      (u32, the exclusive scan of the lengths), 4 output bytes; word 0 count, word 2
+//                      rows given. A warp per selected row, its lanes over the row's bytes.
+// A row past a column's buffer reads as zero (the host checks the selection first).
+
+#define GATHER_COLUMNS 13
+
+__global__ void __launch_bounds__(HASH_THREADS) k_gather_columns(CqlLaunch a, uint64_t count)
+{
+  const uint32_t* rows = (const uint32_t*)a.buf[0];
+  const uint32_t* params = (const uint32_t*)a.buf[1];
+  unsigned char* dest = (unsigned char*)a.buf[2];
+  bool given = cql_word(a, 2) != 0;
+  uint32_t j = blockIdx.y;
+  const uint32_t* pj = params + j * 4;
+  uint32_t kind = pj[0], base = pj[1];
+  uint64_t off = (uint64_t)pj[2] | ((uint64_t)pj[3] << 32);
+  const void* src = a.buf[3 + j];
+  uint64_t src_bytes = a.bytes[3 + j];
+  // the column's section must lie inside the destination
+  uint64_t size = kind == 4 ? 8 : kind == 5 ? 1 : 4;
+  if (off % size != 0 || off > a.bytes[2] || count > (a.bytes[2] - off) / size) return;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint64_t r = given ? rows[i] : i;
+    switch (kind)
+    {
+      case 0: ((uint32_t*)(dest + off))[i] = (r + 1) * 4 <= src_bytes ? ((const uint32_t*)src)[r] : 0u; break;
+      case 1: ((uint32_t*)(dest + off))[i] = base + (r < src_bytes ? (uint32_t)((const uint8_t*)src)[r] : 0u); break;
+      case 2: ((uint32_t*)(dest + off))[i] = base + ((r + 1) * 2 <= src_bytes ? (uint32_t)((const uint16_t*)src)[r] : 0u); break;
+      case 3: ((uint32_t*)(dest + off))[i] = base + (uint32_t)r; break;
+      case 4: ((unsigned long long*)(dest + off))[i] = (r + 1) * 8 <= src_bytes ? ((const unsigned long long*)src)[r] : 0ull; break;
+      default: (dest + off)[i] = r < src_bytes ? ((const uint8_t*)src)[r] : (uint8_t)0; break;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(HASH_THREADS) k_gather_string_lengths(CqlLaunch a, uint64_t count)
+{
+  const uint32_t* rows = (const uint32_t*)a.buf[0];
+  const unsigned long long* offsets = (const unsigned long long*)a.buf[1];
+  uint32_t* lengths = (uint32_t*)a.buf[2];
+  bool given = cql_word(a, 2) != 0;
+  uint64_t n_off = a.bytes[1] / 8;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint64_t r = given ? rows[i] : i;
+    lengths[i] = r + 1 < n_off ? (uint32_t)(offsets[r + 1] - offsets[r]) : 0u;
+  }
+}
+
+__global__ void __launch_bounds__(HASH_THREADS) k_gather_string_bytes(CqlLaunch a, uint64_t count)
+{
+  const uint32_t* rows = (const uint32_t*)a.buf[0];
+  const unsigned long long* offsets = (const unsigned long long*)a.buf[1];
+  const unsigned char* bytes = (const unsigned char*)a.buf[2];
+  const uint32_t* out_off = (const uint32_t*)a.buf[3];
+  unsigned char* out = (unsigned char*)a.buf[4];
+  bool given = cql_word(a, 2) != 0;
+  uint64_t n_off = a.bytes[1] / 8, n_bytes = a.bytes[2], out_cap = a.bytes[4];
+  uint32_t lane = threadIdx.x & 31u;
+  uint64_t warps = (uint64_t)gridDim.x * (blockDim.x / 32);
+  for (uint64_t i = (uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); i < count; i += warps)
+  {
+    uint64_t r = given ? rows[i] : i;
+    if (r + 1 >= n_off) continue;
+    uint64_t s = offsets[r], e = offsets[r + 1], d = out_off[i];
+    if (e > n_bytes || s > e || d + (e - s) > out_cap) continue;
+    for (uint64_t b = lane; b < e - s; b += 32) out[d + b] = bytes[s + b];
+  }
+}
+
+static int launch_gather_columns(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t count = cql_word(a, 0);
+  uint32_t cols = cql_word(a, 4);
+  if (count == 0 || cols == 0) return 0;
+  if (cols > GATHER_COLUMNS || a.bytes[1] < cols * 16ull || (cql_word(a, 2) && a.bytes[0] < count * 4)) return (int)cudaErrorInvalidValue;
+  uint32_t blocks = cql_stream_grid((count + HASH_THREADS - 1) / HASH_THREADS, 8);
+  uint32_t x = (blocks + cols - 1) / cols;
+  k_gather_columns<<<dim3(x ? x : 1, cols), HASH_THREADS, 0, stream>>>(a, count);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+static int launch_gather_string_lengths(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t count = cql_word(a, 0);
+  if (count == 0) return 0;
+  if (a.bytes[2] < count * 4 || (cql_word(a, 2) && a.bytes[0] < count * 4)) return (int)cudaErrorInvalidValue;
+  k_gather_string_lengths<<<cql_stream_grid((count + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, count);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+static int launch_gather_string_bytes(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t count = cql_word(a, 0);
+  if (count == 0) return 0;
+  if (a.bytes[3] < count * 4 || (cql_word(a, 2) && a.bytes[0] < count * 4)) return (int)cudaErrorInvalidValue;
+  uint32_t warps = HASH_THREADS / 32;
+  k_gather_string_bytes<<<cql_stream_grid((count + warps - 1) / warps, 8), HASH_THREADS, 0, stream>>>(a, count);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
 // Widening of a device column to dense f64 (the gather the operator layer does on the host before
 // a hash GROUP BY, query_exec.c:10454-10690): binding 0 source, 1 destination; word 0 rows, word 2
 // the source CQL type. Not a reference kernel: the reference uploads the f64 copy it builds on the host.
@@ -961,6 +1086,9 @@ const CqlKernelDesc cql_kernels_hash[] = {
   { "csr_scatter", launch_csr_scatter },
   { "csr_scatter_tiled", launch_csr_scatter },
   { "aggregate_reduce", launch_aggregate_reduce },
+  { "cql_gather_columns", launch_gather_columns },
+  { "cql_gather_string_lengths", launch_gather_string_lengths },
+  { "cql_gather_string_bytes", launch_gather_string_bytes },
   { "selection_gather", launch_selection_gather },
   { "cql_widen_f64", launch_widen_f64 },
   { nullptr, nullptr },

@@ -29,7 +29,7 @@ import numpy as np
 
 from . import build, native, ops
 
-OPS = ["sort", "sort_f64_2", "sort_subset", "fixed", "hash_group", "hll", "hash_join", "zone_map", "batch"]
+OPS = ["sort", "sort_f64_2", "sort_subset", "fixed", "hash_group", "hll", "hash_join", "zone_map", "batch", "materialize"]
 
 
 def _profile():
@@ -113,6 +113,14 @@ def run(op, rows, reps):
         pk = ops.Column.splitmix(probe_rows, 0, 1, 0, 1_000_000)
         fn = lambda: ops.hash_join(bk, pk, want_pairs=False)
         n, nbytes = probe_rows, (build_rows + probe_rows) * 4
+    elif op == "materialize":
+        # 30 columns of a 10M-row table (20 u32, 10 f64) for the rows of a 1 % filter, read back to the host
+        total = 10_000_000
+        cols = [ops.Column.splitmix(total, 5, 30, i, 1 << 20) for i in range(20)]
+        cols += [ops.Column.from_numpy(rng.random(total)) for _ in range(10)]
+        sel_rows = np.sort(rng.choice(total, total // 100, replace=False)).astype(np.uint32)
+        fn = lambda: ops.gather_rows(cols, rows=sel_rows)
+        n, nbytes = len(sel_rows), len(sel_rows) * (20 * 4 + 10 * 8)
     elif op == "batch":
         return run_batch(rows, reps)
     elif op == "zone_map":

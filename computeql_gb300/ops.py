@@ -522,6 +522,55 @@ def window_rank(keys, desc=None, partitions=0, selection=None, count=None):
     return {name: a[:n] for name, a in out.items()}
 
 
+_GATHER_DTYPES = {TYPE_U32: np.uint32, 12: np.uint32, TYPE_I32: np.int32, 9: np.int32, TYPE_F32: np.float32, TYPE_U64: np.uint64,
+                  TYPE_I64: np.int64, 10: np.int64, 11: np.int64, TYPE_F64: np.float64, 6: np.uint8, TYPE_STRING8: np.uint32}
+
+
+def _gather_selection(rows, selection, count, default):
+    if rows is not None:
+        r = np.ascontiguousarray(rows, dtype=np.uint32)
+        return r, None, len(r)
+    if selection is not None:
+        return None, selection, (selection.nbytes // 4 if count is None else count)
+    return None, None, (default if count is None else count)
+
+
+def gather_rows(columns, rows=None, selection=None, count=None):
+    """Row materialization: the selected rows' values of each column, in selection order -> a list of
+    arrays (narrow and sequence columns decoded, dictionary strings as their codes). The selection is
+    `rows` (host row numbers), else the device buffer `selection`, else rows 0..count-1."""
+    k = len(columns)
+    r, sel, n = _gather_selection(rows, selection, count, min((c.rows for c in columns), default=0))
+    outs = [np.empty(max(n, 1), dtype=_GATHER_DTYPES[c.ctype]) for c in columns]
+    structs = (N.CqlColumn * k)(*[c.c() for c in columns])
+    ptrs = (C.c_void_p * k)(*[o.ctypes.data for o in outs])
+    _check(N.load_ops().cqlops_gather_rows(structs, k, N.ptr(r) if r is not None else None, sel.handle if sel is not None else None, n, ptrs),
+           "cqlops_gather_rows")
+    return [o[:n] for o in outs]
+
+
+def gather_strings(column, rows=None, selection=None, count=None):
+    """The selected rows of a raw string column -> a list of bytes objects, in selection order."""
+    r, sel, n = _gather_selection(rows, selection, count, column.rows)
+    offs = np.zeros(n + 1, dtype=np.uint64)
+    lib = N.load_ops()
+    c = column.c()
+    need = C.c_uint64()
+    cap = 0
+    buf = C.create_string_buffer(1)
+    for _ in range(2):
+        ok = lib.cqlops_gather_strings(C.byref(c), N.ptr(r) if r is not None else None, sel.handle if sel is not None else None, n,
+                                       N.ptr(offs), buf, cap, C.byref(need))
+        if ok:
+            data = buf.raw
+            return [data[int(offs[i]):int(offs[i + 1])] for i in range(n)]
+        if need.value <= cap:
+            break
+        cap = need.value
+        buf = C.create_string_buffer(max(cap, 1))
+    _check(0, "cqlops_gather_strings")
+
+
 def fixed_scale(column, selection=None, count=None):
     """-> (scale or -1, largest magnitude): the decimal places every value needs (at most 6)."""
     n = column.rows if selection is None else (selection.nbytes // 4 if count is None else count)

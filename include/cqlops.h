@@ -320,6 +320,24 @@ int cqlops_group_dense_fixed(const CqlColumn* key, uint32_t expr_count, const ui
 int cqlops_sort_rows(const CqlColumn* keys, uint32_t key_count, const uint32_t* desc, CqlBuffer* selection,
                      uint64_t selection_count, uint32_t* out_rows, uint64_t out_capacity);
 
+/* Row materialization (selection_gather.comp modes 0/1, qe_selection_gather_column,
+   src/query_exec/query_exec.c:4371-4410): the values of `count` selected rows of each column, in
+   selection order, written to host memory. The selection is `rows` (host memory, e.g. a scan's out_rows),
+   else the device buffer `selection` (count u32 row numbers), else rows 0..count-1. out_values[c] receives
+   count values of column c: 4 bytes each for U32/I32/F32/DATE/ENUM columns, for narrow and sequence
+   encodings (the value base + code or base + row) and for dictionary strings (the code); 8 bytes for
+   U64/I64/F64/TIMESTAMP/DECIMAL; 1 byte for BOOL. Raw strings go through cqlops_gather_strings. Host rows
+   are checked against the columns' length; a device selection's rows past a column read as zero. */
+int cqlops_gather_rows(const CqlColumn* columns, uint32_t column_count, const uint32_t* rows, CqlBuffer* selection, uint64_t count,
+                       void* const* out_values);
+
+/* The selected rows of a raw STRING8 column (bytes and u64 offsets), selection as cqlops_gather_rows:
+   row i's bytes are out_bytes[out_offsets[i] .. out_offsets[i + 1]), out_offsets holding count + 1 values.
+   *out_bytes_needed receives the selected bytes; when they exceed bytes_capacity nothing is written past
+   the offsets' first entry and 0 is returned (call again with room). At most 4 GB of selected bytes. */
+int cqlops_gather_strings(const CqlColumn* column, const uint32_t* rows, CqlBuffer* selection, uint64_t count, uint64_t* out_offsets,
+                          char* out_bytes, uint64_t bytes_capacity, uint64_t* out_bytes_needed);
+
 /* A HAVING condition over the grouped result, evaluated for every group at once (qk_having_kernel,
    src/query_exec/query_kernel.c:2530-2575): `condition` is an expression over v0..v7 (group i's values of
    the result columns, as doubles) and lit[0..15] (the literals), in C syntax (&&, ||, !, comparisons,

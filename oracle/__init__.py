@@ -228,6 +228,25 @@ def window_rank(keys, desc=None, partitions=0):
     return out[:rows], rn[:rows], rk[:rows], dr[:rows]
 
 
+def gather_column(stored, rows, width=0, base=0):
+    """The selected rows of one column (selection_gather.comp:64-78, modes 0/1: dest[i] = source[row i]),
+    with the encodings decoded as the scans read them (qe_encoding_shader_width, query_exec.c:1593-1601):
+    width 1/2 narrow codes -> base + code, width 3 -> base + row, both in 32-bit arithmetic.
+    `stored` is what the column holds (codes for narrow widths, None for a sequence)."""
+    r = np.asarray(rows, dtype=np.int64)
+    if width == 3:
+        return ((base + r) & 0xFFFFFFFF).astype(np.uint32)
+    v = np.asarray(stored)[r]
+    if width in (1, 2):
+        return ((base + v.astype(np.int64)) & 0xFFFFFFFF).astype(np.uint32)
+    return v
+
+
+def gather_strings(values, rows):
+    """The selected rows of a string column, as bytes."""
+    return [values[int(i)] for i in rows]
+
+
 def join_aggregate(fact_key, fact_arg, dim_key, dim_group, groups):
     """COUNT(*) and SUM(fact_arg) per group over fact JOIN dim (dim_group 0xffffffff = filtered out)."""
     fk = np.ascontiguousarray(fact_key, dtype=np.uint32)
