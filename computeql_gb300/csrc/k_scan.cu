@@ -8,6 +8,10 @@
 // (32 bytes of a u32 column in flight per thread), the match bits are compacted with a warp
 // prefix sum of popc() and one global atomic per CTA and pass. When the output binding has no room
 // for a single row (a COUNT(*) with no row list) every CTA counts privately and adds once at the end.
+// When rows are wanted, the scans write a bitmap of the table's rows instead (bitmap mode): every
+// 32-row word is stored once by the lanes that evaluated it, with no atomics and no capacity, and the
+// bitmap becomes ascending rows on the device (cql_bitmap_popc, prefix_sum, cql_bitmap_emit) - the
+// reference's list, unordered across workgroups, had to be sorted on the host.
 #include "cql_internal.cuh"
 #include <math_constants.h>
 #include <climits>
@@ -214,6 +218,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_simple(CqlLaunch a, uint6
   bool skip_on = cql_word(a, 8) != 0;
   uint32_t chunk_start = cql_word(a, 10);
   uint32_t row_offset = cql_word(a, 12);   // added to every row written (a dispatch over one range of the table)
+  // word 14: 1 = the matches as a bitmap of the table's rows (binding 3, one bit a row, each 32-row word
+  // written by the four lanes that own it; the dispatch's first row is a multiple of 32)
+  const bool bitmap_mode = !COUNT_ONLY && cql_word(a, 14) != 0;
+  const uint64_t bitmap_words = a.bytes[3] / 4;
   uint32_t leaf_count = s_leaf_count;
 
   uint64_t groups = (rows + ROWS_PER_THREAD - 1) / ROWS_PER_THREAD;
@@ -274,6 +282,17 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_simple(CqlLaunch a, uint6
       private_count += n;
       continue;
     }
+    if (bitmap_mode)
+    {
+      // eight rows a lane, four lanes a 32-row word; every word of the dispatch written once
+      uint32_t m = live << (8u * (lane & 3u));
+      m |= __shfl_xor_sync(0xffffffffu, m, 1);
+      m |= __shfl_xor_sync(0xffffffffu, m, 2);
+      uint64_t word = ((uint64_t)row_offset >> 5) + (g >> 2);
+      if ((lane & 3u) == 0u && word < bitmap_words) out[word] = m;
+      private_count += n;
+      continue;
+    }
     // warp inclusive scan of the match counts
     uint32_t incl = n;
 #pragma unroll
@@ -310,7 +329,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_simple(CqlLaunch a, uint6
     }
     __syncthreads();
   }
-  if (COUNT_ONLY)
+  if (COUNT_ONLY || bitmap_mode)
   {
     uint32_t w = private_count;
 #pragma unroll
@@ -335,7 +354,8 @@ static int launch_scan_simple(const CqlLaunch& a, uint32_t gws, uint32_t lws, cu
   uint64_t groups = (rows + ROWS_PER_THREAD - 1) / ROWS_PER_THREAD;
   uint64_t ctas = (groups + SCAN_THREADS - 1) / SCAN_THREADS;
   uint32_t grid = cql_stream_grid(ctas, 8);
-  bool count_only = a.bytes[3] < 8;
+  // no room for one row pair and no bitmap: count only (a bitmap of at most 32 rows is one 4-byte word)
+  bool count_only = a.bytes[3] < 8 && cql_word(a, 14) == 0;
   if (count_only) k_scan_simple<true><<<grid, SCAN_THREADS, 0, stream>>>(a, rows);
   else k_scan_simple<false><<<grid, SCAN_THREADS, 0, stream>>>(a, rows);
   CQL_LAUNCH_CHECK();
@@ -580,7 +600,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_filter(CqlLaunch a, uint6
   bool skip_on = cql_word(a, 8) != 0;
   bool scored = (cql_word(a, 2) & 1u) != 0u;
   uint32_t gram = max(cql_word(a, 4), 1u);
+  // word 10: 1 = the matches as a bitmap of the rows (binding 3): a warp's 32 rows are one word, its ballot
+  const bool bitmap_mode = cql_word(a, 10) != 0 && !scored;
+  const uint64_t bitmap_words = a.bytes[3] / 4;
   uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t bitmap_count = 0;
   for (uint64_t base = (uint64_t)blockIdx.x * SCAN_THREADS; base < rows; base += (uint64_t)gridDim.x * SCAN_THREADS)
   {
     uint64_t row = base + threadIdx.x;
@@ -593,6 +617,13 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_filter(CqlLaunch a, uint6
     uint32_t aux = 0u;
     bool matched = in_range && interp_row(a, code, words, row, gram, &aux);
     uint32_t ballot = __ballot_sync(0xffffffffu, matched);
+    if (bitmap_mode)
+    {
+      uint64_t word = (base >> 5) + warp;
+      if (lane == 0 && word < bitmap_words) out[word] = ballot;
+      bitmap_count += __popc(ballot);
+      continue;
+    }
     if (lane == 0) s_warp[warp] = __popc(ballot);
     __syncthreads();
     if (threadIdx.x == 0)
@@ -614,6 +645,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_filter(CqlLaunch a, uint6
     }
     __syncthreads();
   }
+  if (bitmap_mode && lane == 0 && bitmap_count) atomicAdd(out_count, bitmap_count);
 }
 
 static int launch_scan_filter(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
@@ -624,6 +656,65 @@ static int launch_scan_filter(const CqlLaunch& a, uint32_t gws, uint32_t lws, cu
   if (rows == 0) return 0;
   uint32_t grid = cql_stream_grid((rows + SCAN_THREADS - 1) / SCAN_THREADS, 8);
   k_scan_filter<<<grid, SCAN_THREADS, 0, stream>>>(a, rows);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// A selection bitmap (one bit a row, as the scans write it in bitmap mode) to its rows in ascending
+// order: cql_bitmap_popc counts each word's rows (binding 0 bitmap, 1 counts; word 0 words), the
+// prefix_sum kernel turns the counts into offsets, and cql_bitmap_emit writes each word's rows from its
+// offset (binding 0 bitmap, 1 offsets, 2 rows; word 0 words). No atomics and no sort: the order is the
+// bitmap's.
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_bitmap_popc(CqlLaunch a, uint64_t words)
+{
+  const uint32_t* bits = (const uint32_t*)a.buf[0];
+  uint32_t* counts = (uint32_t*)a.buf[1];
+  for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += (uint64_t)gridDim.x * blockDim.x)
+    counts[w] = __popc(bits[w]);
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_bitmap_emit(CqlLaunch a, uint64_t words)
+{
+  const uint32_t* bits = (const uint32_t*)a.buf[0];
+  const uint32_t* offsets = (const uint32_t*)a.buf[1];
+  uint32_t* rows = (uint32_t*)a.buf[2];
+  uint64_t cap = a.bytes[2] / 4;
+  for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint32_t m = bits[w];
+    uint64_t pos = offsets[w];
+    while (m)
+    {
+      uint32_t b = (uint32_t)(__ffs(m) - 1);
+      m &= m - 1u;
+      if (pos < cap) rows[pos] = (uint32_t)(w * 32 + b);
+      pos++;
+    }
+  }
+}
+
+static int launch_bitmap_popc(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t words = cql_word(a, 0);
+  if (words == 0) return 0;
+  if (a.bytes[0] < words * 4 || a.bytes[1] < words * 4) return (int)cudaErrorInvalidValue;
+  k_bitmap_popc<<<cql_stream_grid((words + SCAN_THREADS - 1) / SCAN_THREADS, 8), SCAN_THREADS, 0, stream>>>(a, words);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+static int launch_bitmap_emit(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t words = cql_word(a, 0);
+  if (words == 0) return 0;
+  if (a.bytes[0] < words * 4 || a.bytes[1] < words * 4) return (int)cudaErrorInvalidValue;
+  k_bitmap_emit<<<cql_stream_grid((words + SCAN_THREADS - 1) / SCAN_THREADS, 8), SCAN_THREADS, 0, stream>>>(a, words);
   CQL_LAUNCH_CHECK();
   return 0;
 }
@@ -815,5 +906,7 @@ const CqlKernelDesc cql_kernels_scan[] = {
   { "cql_zone_map", launch_zone_map },
   { "scan_simple", launch_scan_simple },
   { "scan_filter", launch_scan_filter },
+  { "cql_bitmap_popc", launch_bitmap_popc },
+  { "cql_bitmap_emit", launch_bitmap_emit },
   { nullptr, nullptr },
 };

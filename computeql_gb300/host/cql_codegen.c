@@ -6,7 +6,9 @@
  * constant buffer (binding 1) so queries that differ only in literal values share one kernel, and
  * the kernel keeps the binding contract of the kernel it replaces:
  *   CQLOPS_KERNEL_SCAN        scan_filter.comp's bindings: row ids + aux word into binding 3, count
- *                             in binding 4, zone skip bits in binding 5 (query_kernel.c:1616-1670)
+ *                             in binding 4, zone skip bits in binding 5 (query_kernel.c:1616-1670);
+ *                             with word 10 set, binding 3 receives a bitmap of the rows instead (each
+ *                             32-row word from the four lanes that own it)
  *   CQLOPS_KERNEL_FUSED_AGG   partials [workgroup][1 + 3k] doubles in binding 3 (:1538-1614)
  *   CQLOPS_KERNEL_FUSED_GROUP [group][2 + 4k] words in binding 3 (:1433-1537)
  *
@@ -589,6 +591,7 @@ int cqlops_program_source(const CqlProgram* prog, uint32_t kind, const CqlFusedA
           "  __shared__ u32 s_warp[8]; __shared__ u32 s_base;\n"
           "  u32* out = (u32*)a.buf[3]; u32* out_count = (u32*)a.buf[4]; const u32* skip = (const u32*)a.buf[5];\n"
           "  const u64 capacity = a.bytes[3] / 8ull; const u32 skip_shift = cql_word(a, 6); const bool skip_on = cql_word(a, 8) != 0u;\n"
+          "  const bool bitmap_mode = cql_word(a, 10) != 0u; const u64 bitmap_words = a.bytes[3] / 4ull; u32 bitmap_count = 0u;\n"
           "  for (u64 base = (u64)blockIdx.x * 256ull; base < groups8; base += per_pass)\n  {\n"
           "    const u64 row0 = (base + threadIdx.x) * 8ull;\n"
           "    const u32 valid = row0 < rows ? (u32)min((u64)8, rows - row0) : 0u;\n"
@@ -600,6 +603,12 @@ int cqlops_program_source(const CqlProgram* prog, uint32_t kind, const CqlFusedA
     sprintf_(&s, "#pragma unroll\n      for (u32 k = 0; k < 8u; k++) { if (k < valid) { bool m = %s; live |= (m ? 1u : 0u) << k; } }\n", expr);
     sputs(&s,
           "    }\n"
+          "    if (bitmap_mode)\n    {\n"
+          "      u32 m = live << (8u * (lane & 3u)); m |= __shfl_xor_sync(0xffffffffu, m, 1); m |= __shfl_xor_sync(0xffffffffu, m, 2);\n"
+          "      const u64 word = (base + threadIdx.x) >> 2;\n"
+          "      if ((lane & 3u) == 0u && word < bitmap_words) out[word] = m;\n"
+          "      bitmap_count += __popc(live);\n"
+          "      continue;\n    }\n"
           "    const u32 n = __popc(live); u32 incl = n;\n"
           "#pragma unroll\n    for (int o = 1; o < 32; o <<= 1) { u32 y = __shfl_up_sync(0xffffffffu, incl, o); if (lane >= (u32)o) incl += y; }\n"
           "    if (lane == 31u) s_warp[warp] = incl;\n"
@@ -609,7 +618,10 @@ int cqlops_program_source(const CqlProgram* prog, uint32_t kind, const CqlFusedA
           "    u64 pos = (u64)s_base + s_warp[warp] + (incl - n);\n"
           "    while (live) { u32 k = __ffs(live) - 1u; live &= live - 1u; if (pos < capacity) { uint2 pr = make_uint2((u32)(row0 + k), 0u); *((uint2*)(out + pos * 2ull)) = pr; } pos++; }\n"
           "    __syncthreads();\n"
-          "  }\n}\n");
+          "  }\n"
+          "  if (bitmap_mode)\n  {\n"
+          "#pragma unroll\n    for (int o = 16; o > 0; o >>= 1) bitmap_count += __shfl_xor_sync(0xffffffffu, bitmap_count, o);\n"
+          "    if (lane == 0u && bitmap_count) atomicAdd(out_count, bitmap_count);\n  }\n}\n");
   }
   else if (kind == CQLOPS_KERNEL_FUSED_AGG)
   {

@@ -284,10 +284,45 @@ static int simple_leaf_words(uint32_t* words, uint32_t slot, const CqlColumn* co
   return 1;
 }
 
-static int cmp_u32(const void* a, const void* b)
+/* The rows of a selection bitmap (one bit a row, as the scans write it in bitmap mode) in ascending
+   order, on the device: each word's population, an exclusive scan of them, then every word's rows written
+   from its offset. The first min(count, cap) rows land in out_rows; count is the bitmap's population. */
+int cqlops_bitmap_rows(CqlBuffer* bitmap, uint64_t rows, uint64_t count, uint32_t* out_rows, uint64_t cap)
 {
-  uint32_t x = *(const uint32_t*)a, y = *(const uint32_t*)b;
-  return x < y ? -1 : (x > y);
+  if (!count || !cap || !out_rows) return 1;
+  uint64_t words = (rows + 31) / 32, blocks = (words + 255) / 256;
+  uint64_t n = count < cap ? count : cap;
+  CqlBuffer* counts = pooled("bitmap_word_counts", words * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* offsets = pooled("bitmap_word_offsets", (words + 1) * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* cursor = pooled("bitmap_word_cursor", words * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* block_sums = pooled("bitmap_block_sums", blocks * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* list = pooled("bitmap_rows", count * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlKernel* popc = kernel_named("cql_bitmap_popc");
+  CqlKernel* scan = kernel_named("prefix_sum");
+  CqlKernel* emit = kernel_named("cql_bitmap_emit");
+  if (!counts || !offsets || !cursor || !block_sums || !list || !popc || !scan || !emit) return 0;
+  cqlcuda_kernel_set_arg_buffer(popc, 0, bitmap);
+  cqlcuda_kernel_set_arg_buffer(popc, 1, counts);
+  cqlcuda_kernel_set_arg_u64(popc, 0, words);
+  cqlcuda_kernel_set_arg_buffer(scan, 0, counts);
+  cqlcuda_kernel_set_arg_buffer(scan, 1, offsets);
+  cqlcuda_kernel_set_arg_buffer(scan, 2, cursor);
+  cqlcuda_kernel_set_arg_buffer(scan, 3, block_sums);
+  cqlcuda_kernel_set_arg_u64(scan, 0, words);
+  cqlcuda_kernel_set_arg_buffer(emit, 0, bitmap);
+  cqlcuda_kernel_set_arg_buffer(emit, 1, offsets);
+  cqlcuda_kernel_set_arg_buffer(emit, 2, list);
+  cqlcuda_kernel_set_arg_u64(emit, 0, words);
+  CqlBatch* b = cqlcuda_batch_begin(0, n * 4);
+  cqlcuda_batch_kernel_execute(b, popc, (uint32_t)words, QE_GPU_WORKGROUP_SIZE);
+  for (uint32_t mode = 0; mode < 3; mode++)
+  {
+    cqlcuda_kernel_set_arg_u64(scan, 1, mode);
+    cqlcuda_batch_kernel_execute(b, scan, mode == 1 ? 256u : (uint32_t)(blocks * 256), 256);
+  }
+  cqlcuda_batch_kernel_execute(b, emit, (uint32_t)words, QE_GPU_WORKGROUP_SIZE);
+  cqlcuda_batch_buffer_read(b, list, out_rows, n * 4);
+  return cqlcuda_batch_end(b);
 }
 
 int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const CqlLeaf* leaves, uint32_t leaf_count, uint64_t* out_count,
@@ -330,15 +365,9 @@ int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const Cq
   {
     return 0;
   }
-  /* the output list: none for a count, else sized like the reference (:3084-3090) and grown once */
+  /* the output: none for a count, else a bitmap of the rows (no capacity to outgrow, unlike the
+     reference's list sized at :3084-3090) */
   int want_rows = out_rows != NULL;
-  uint64_t cap_rows = 0;
-  if (want_rows)
-  {
-    uint64_t default_cap = rows / 32 > 65536 ? rows / 32 : 65536;
-    cap_rows = default_cap < rows ? default_cap : rows;
-    if (cap_rows == 0) cap_rows = 1;
-  }
   /* zone-map pruning: the ranges of the table the leaves can match, or one pass with a skip bitmap
      (qe_scan_build_dispatch_ranges, :13307-13540) */
   uint64_t chunks = (rows + CQLOPS_ZONEMAP_CHUNK_ROWS - 1) / CQLOPS_ZONEMAP_CHUNK_ROWS;
@@ -364,88 +393,58 @@ int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const Cq
   cqlcuda_kernel_set_arg_buffer(k, 5, skip_buf);
   cqlcuda_kernel_set_arg_u64(k, 3, use_skip ? 13 : 0);
   cqlcuda_kernel_set_arg_u64(k, 4, use_skip ? 1 : 0);
-  uint64_t result_count = 0;
-  CqlBuffer* output = NULL;
-  for (int attempt = 0; attempt < 2; attempt++)
+  /* the matches as a bitmap of the table's rows (word 14), turned into ascending rows on the device */
+  uint64_t bitmap_words = (rows + 31) / 32;
+  CqlBuffer* output = want_rows ? pooled("scan_bitmap", bitmap_words * 4, CQLCUDA_BUFFER_READ_WRITE)
+                                : pooled("cqlops_scan_no_output", 0, CQLCUDA_BUFFER_READ);   /* count only */
+  if (!output)
   {
-    if (want_rows)
-    {
-      output = pooled("scan_filter_output", cap_rows * 2 * sizeof(uint32_t), CQLCUDA_BUFFER_READ);
-      if (!output) return 0;
-      cqlcuda_kernel_set_arg_buffer(k, 3, output);
-    }
-    else
-    {
-      /* no room for a row: the kernel counts only */
-      CqlBuffer* none = pooled("cqlops_scan_no_output", 0, CQLCUDA_BUFFER_READ);
-      if (!none) return 0;
-      cqlcuda_kernel_set_arg_buffer(k, 3, none);
-    }
-    uint32_t count32[2] = { 0, 0 };
-    CqlBatch* batch = cqlcuda_batch_begin(sizeof(words) + (use_skip ? ((chunks + 31) / 32) * 4 : 0), sizeof(count32));
-    cqlcuda_batch_buffer_write(batch, leaf_buf, words, sizeof(words));
-    if (use_skip) cqlcuda_batch_buffer_write(batch, skip_buf, skip_bits, ((chunks + 31) / 32) * sizeof(uint32_t));
-    cqlcuda_batch_buffer_zero(batch, counter, sizeof(count32));
-    for (uint64_t r = 0; r < range_count; r++)
-    {
-      /* one dispatch per range: the columns bound from the range's first row, row numbers written
-         from there (a sequence column's values from chunk_start) */
-      uint64_t start = ranges[2 * r], end = ranges[2 * r + 1];
-      for (uint32_t c = 0; c < QE_MAX_COLUMN_BINDINGS; c++)
-      {
-        const CqlColumn* col = &columns[c < column_count ? c : 0];
-        if (!col->buffer)
-        {
-          cqlcuda_kernel_set_arg_buffer(k, 6 + c, leaf_buf); /* a sequence column is never read */
-          continue;
-        }
-        uint64_t elem = col->width == 1 ? 1 : col->width == 2 ? 2 : col->type == CQLOPS_TYPE_F64 ? 8 : 4;
-        uint64_t size = cqlcuda_buffer_size(col->buffer);
-        uint64_t offset = start * elem;
-        cqlcuda_kernel_set_arg_buffer_range(k, 6 + c, col->buffer, offset, size > offset ? size - offset : 0);
-      }
-      cqlcuda_kernel_set_arg_u64(k, 0, end - start);
-      cqlcuda_kernel_set_arg_u64(k, 5, start);
-      cqlcuda_kernel_set_arg_u64(k, 6, start);
-      uint64_t threads = (end - start + QE_SIMPLE_SCAN_ROWS_PER_THREAD - 1) / QE_SIMPLE_SCAN_ROWS_PER_THREAD;
-      cqlcuda_batch_kernel_execute(batch, k, (uint32_t)threads, QE_GPU_WORKGROUP_SIZE);
-    }
-    cqlcuda_batch_buffer_read(batch, counter, count32, sizeof(count32));
-    if (!cqlcuda_batch_end(batch))
-    {
-      free(skip_bits);
-      return 0;
-    }
-    result_count = count32[0];
-    if (!want_rows || result_count <= cap_rows)
-    {
-      break;
-    }
-    cap_rows = result_count;
-  }
-  free(skip_bits);
-  if (want_rows && result_count > cap_rows)
-  {
+    free(skip_bits);
     return 0;
   }
-  if (want_rows && result_count > 0 && out_capacity > 0)
+  cqlcuda_kernel_set_arg_buffer(k, 3, output);
+  cqlcuda_kernel_set_arg_u64(k, 7, want_rows ? 1 : 0);
+  uint32_t count32[2] = { 0, 0 };
+  CqlBatch* batch = cqlcuda_batch_begin(sizeof(words) + (use_skip ? ((chunks + 31) / 32) * 4 : 0), sizeof(count32));
+  cqlcuda_batch_buffer_write(batch, leaf_buf, words, sizeof(words));
+  if (use_skip) cqlcuda_batch_buffer_write(batch, skip_buf, skip_bits, ((chunks + 31) / 32) * sizeof(uint32_t));
+  cqlcuda_batch_buffer_zero(batch, counter, sizeof(count32));
+  /* ranges a zone map keeps leave the other words unwritten: they must read as no match */
+  int whole = range_count == 1 && ranges[0] == 0 && ranges[1] == rows;
+  if (want_rows && !whole) cqlcuda_batch_buffer_zero(batch, output, bitmap_words * 4);
+  for (uint64_t r = 0; r < range_count; r++)
   {
-    uint32_t* pairs = (uint32_t*)malloc(result_count * 2 * sizeof(uint32_t));
-    if (!pairs) return 0;
-    cqlcuda_buffer_read(output, pairs, result_count * 2 * sizeof(uint32_t));
-    uint32_t* list = (uint32_t*)malloc(result_count * sizeof(uint32_t));
-    if (!list)
+    /* one dispatch per range: the columns bound from the range's first row, row numbers written
+       from there (a sequence column's values from chunk_start) */
+    uint64_t start = ranges[2 * r], end = ranges[2 * r + 1];
+    for (uint32_t c = 0; c < QE_MAX_COLUMN_BINDINGS; c++)
     {
-      free(pairs);
-      return 0;
+      const CqlColumn* col = &columns[c < column_count ? c : 0];
+      if (!col->buffer)
+      {
+        cqlcuda_kernel_set_arg_buffer(k, 6 + c, leaf_buf); /* a sequence column is never read */
+        continue;
+      }
+      uint64_t elem = col->width == 1 ? 1 : col->width == 2 ? 2 : col->type == CQLOPS_TYPE_F64 ? 8 : 4;
+      uint64_t size = cqlcuda_buffer_size(col->buffer);
+      uint64_t offset = start * elem;
+      cqlcuda_kernel_set_arg_buffer_range(k, 6 + c, col->buffer, offset, size > offset ? size - offset : 0);
     }
-    for (uint64_t i = 0; i < result_count; i++) list[i] = pairs[i * 2];
-    qsort(list, result_count, sizeof(uint32_t), cmp_u32);
-    uint64_t n = result_count < out_capacity ? result_count : out_capacity;
-    memcpy(out_rows, list, n * sizeof(uint32_t));
-    free(list);
-    free(pairs);
+    cqlcuda_kernel_set_arg_u64(k, 0, end - start);
+    cqlcuda_kernel_set_arg_u64(k, 5, start);
+    cqlcuda_kernel_set_arg_u64(k, 6, start);
+    uint64_t threads = (end - start + QE_SIMPLE_SCAN_ROWS_PER_THREAD - 1) / QE_SIMPLE_SCAN_ROWS_PER_THREAD;
+    cqlcuda_batch_kernel_execute(batch, k, (uint32_t)threads, QE_GPU_WORKGROUP_SIZE);
   }
+  cqlcuda_batch_buffer_read(batch, counter, count32, sizeof(count32));
+  if (!cqlcuda_batch_end(batch))
+  {
+    free(skip_bits);
+    return 0;
+  }
+  uint64_t result_count = count32[0];
+  free(skip_bits);
+  if (want_rows && !cqlops_bitmap_rows(output, rows, result_count, out_rows, out_capacity)) return 0;
   if (out_count) *out_count = result_count;
   return 1;
 }
@@ -458,11 +457,13 @@ int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count,
                        int64_t* out_mins, int64_t* out_maxs)
 {
   launches_begin();
-  if (!key || !key->has_range || !(key->type == CQLOPS_TYPE_U32 || key->type == CQLOPS_TYPE_I32) || key->rows != rows || !key->buffer ||
+  /* a dictionary string column groups by its codes, as the reference's dictionary GROUP BY does */
+  int dict_key = key && key->type == CQLOPS_TYPE_STRING8 && key->dict && key->width == 0;
+  if (!key || !key->has_range || !(key->type == CQLOPS_TYPE_U32 || key->type == CQLOPS_TYPE_I32 || dict_key) || key->rows != rows || !key->buffer ||
       key->width == 3 || key->zone_min < -2147483648.0 || key->zone_max > 2147483647.0 ||
       key->zone_max - key->zone_min + 1.0 > (double)QE_DENSE_STREAM_MAX_GROUPS)
   {
-    return refuse("dense group-by: the key must be a whole-number column with a zone range of at most 65536 values");
+    return refuse("dense group-by: the key must be a whole-number or dictionary string column with a zone range of at most 65536 values");
   }
   int64_t min_key = (int64_t)key->zone_min;
   uint64_t group_count = (uint64_t)((int64_t)key->zone_max - min_key) + 1;

@@ -32,6 +32,7 @@ static uint64_t g_failed[FAILED_CAP];
 static uint32_t g_failed_count = 0;
 static uint64_t g_generated_requests = 0, g_generated_failures = 0;
 void cqlops_note_error(const char* why);
+int cqlops_bitmap_rows(CqlBuffer* bitmap, uint64_t rows, uint64_t count, uint32_t* out_rows, uint64_t cap);
 
 void cqlops_generated_stats(uint64_t* out_requests, uint64_t* out_failures)
 {
@@ -267,9 +268,29 @@ static int scan_filter_run(const CqlProgram* prog, const CqlColumn* columns, uin
   cqlcuda_kernel_set_arg_u64(k, 2, 3);             /* word 4: the trigram length */
   cqlcuda_kernel_set_arg_u64(k, 3, 0);
   cqlcuda_kernel_set_arg_u64(k, 4, 0);
-  cqlcuda_kernel_set_arg_u64(k, 5, 0);
 
   int want_rows = out_rows != NULL || out_scores != NULL;
+  /* rows without scores: the kernel writes a bitmap of the rows (word 10), which becomes ascending rows
+     on the device; no output capacity, no second run, no host sort */
+  int bitmap = want_rows && !score_flags && out_scores == NULL;
+  cqlcuda_kernel_set_arg_u64(k, 5, bitmap ? 1 : 0);
+  if (bitmap)
+  {
+    uint64_t words = (rows + 31) / 32;
+    CqlBuffer* bits = pooled("scan_bitmap", words * 4, CQLCUDA_BUFFER_READ_WRITE);
+    if (!bits) return 0;
+    cqlcuda_kernel_set_arg_buffer(k, 3, bits);
+    uint32_t c32[2] = { 0, 0 };
+    CqlBatch* batch = cqlcuda_batch_begin(0, 8);
+    cqlcuda_batch_buffer_zero(batch, counter, 8);
+    cqlcuda_batch_kernel_execute(batch, k, (uint32_t)(rows < 0xffffffffull ? rows : 0xffffffffull), QE_GPU_WORKGROUP_SIZE);
+    cqlcuda_batch_buffer_read(batch, counter, c32, 8);
+    if (!cqlcuda_batch_end(batch)) return 0;
+    if (!cqlops_bitmap_rows(bits, rows, c32[0], out_rows, out_capacity)) return 0;
+    if (out_count) *out_count = c32[0];
+    if (out_strategy) *out_strategy = ran;
+    return 1;
+  }
   uint64_t cap_rows = 0;
   if (want_rows)
   {

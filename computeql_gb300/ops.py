@@ -236,6 +236,26 @@ class StringColumn(Column):
             super().__init__(TYPE_STRING8, n, DeviceBuffer(blob.nbytes, blob), zone=None)
             self.offsets_buf = DeviceBuffer(offs.nbytes, offs)
 
+    @classmethod
+    def from_codes(cls, codes, words):
+        """A dictionary-coded column from its codes (code j is words[j]), built without a pass over the rows."""
+        obj = cls.__new__(cls)
+        codes = np.ascontiguousarray(codes, dtype=np.uint32)
+        raw = [w.encode() if isinstance(w, str) else bytes(w) for w in words]
+        offs = np.zeros(len(raw) + 1, dtype=np.uint32)
+        for i, v in enumerate(raw):
+            offs[i + 1] = offs[i] + len(v)
+        blob = b"".join(raw) or b"\0"
+        obj.values = None
+        obj.codes = codes
+        obj._dict_offsets = offs
+        obj._dict_bytes = C.create_string_buffer(blob, len(blob))
+        obj.dict_struct = N.CqlDict(len(raw), offs.ctypes.data, C.addressof(obj._dict_bytes))
+        obj.offsets_buf = None
+        Column.__init__(obj, TYPE_STRING8, len(codes), DeviceBuffer(codes.nbytes, codes) if len(codes) else DeviceBuffer(4),
+                        zone=(0.0, float(max(len(raw) - 1, 0))))
+        return obj
+
     def c(self):
         col = super().c()
         col.offsets = self.offsets_buf.handle if self.offsets_buf else None

@@ -215,8 +215,9 @@ int cqlops_aggregate_global(const CqlColumn* columns, uint32_t column_count, dou
 int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const CqlLeaf* leaves, uint32_t leaf_count,
                        uint64_t* out_count, uint32_t* out_rows, uint64_t out_capacity);
 
-/* GROUP BY one small-range whole-number key with COUNT/SUM/AVG/MIN/MAX over whole-number
-   columns (qe_dense_stream_core, query_exec.c:7632-7983, one chunk). funcs[e]/arg_cols[e] describe
+/* GROUP BY one small-range whole-number key (or a dictionary string column, by its codes) with
+   COUNT/SUM/AVG/MIN/MAX over whole-number columns (qe_dense_stream_core, query_exec.c:7632-7983, one
+   chunk). funcs[e]/arg_cols[e] describe
    expression e (arg_cols[e] is ignored for COUNT). Outputs, per group g = key - min_key:
    out_counts[g], out_sums[g*exprs+e] (64-bit two's complement), out_mins/out_maxs[g*exprs+e]
    (INT32_MAX / INT32_MIN when the group has no rows). out_group_count receives the group count;
