@@ -428,6 +428,129 @@ static int launch_join_probe_native(const CqlLaunch& a, uint32_t gws, uint32_t l
   return 0;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Join-aggregate through a lookup table over the fact key's range (not a reference kernel: the
+// reference probes a hash table of the dim keys and visits every dim row on the host,
+// qe_aggregate_join_pushdown query_exec.c:8442-8776). With unique dim keys, each fact key value maps to
+// at most one dim row and so to one group: the table turns the fact key column into a column of group
+// ids that the dense group-by aggregates, and the first kept dim row of each group (its place in the
+// output) is found on the device too. Key offsets are taken in 32-bit arithmetic (key - min mod 2^32),
+// right for U32 and I32 keys alike; a key outside [min, min + range) matches nothing.
+//
+//  cql_join_lut_build  binding 0 visits (u32 dim rows; unbound: rows 0..visits-1), 1 dim keys (u32), 2 dim
+//                      group values (f64), 3 table (u32 group id per key value, all EMPTY before),
+//                      4 visit per key value (u32), 5 error word; word 0 visits, word 2 1 = visit list
+//                      given, word 4 min key bits, word 6 range, word 8/9 the smallest group value (f64
+//                      bits), word 10 group values given (else every row is group 0).
+//                      Error bit 0: a key met twice (the table cannot stand for the join).
+//  cql_join_lut_map    binding 0 fact keys, 1 table, 2 group ids out (u32), 3 key-present bitmap (all 0
+//                      before); word 0 rows, word 4 min key bits, word 6 range, word 8 the id of no group
+//  cql_join_lut_first  binding 0 key-present bitmap, 1 table, 2 visit per key value, 3 first visit per
+//                      group (u32, all EMPTY before); word 6 range
+
+#define LUT_EMPTY 0xffffffffu
+
+__global__ void __launch_bounds__(JOIN_THREADS) k_join_lut_build(CqlLaunch a, uint64_t visits)
+{
+  const uint32_t* visit_rows = (const uint32_t*)a.buf[0];
+  const uint32_t* dim_keys = (const uint32_t*)a.buf[1];
+  const double* group_values = (const double*)a.buf[2];
+  uint32_t* table = (uint32_t*)a.buf[3];
+  uint32_t* visit_of = (uint32_t*)a.buf[4];
+  uint32_t* error = (uint32_t*)a.buf[5];
+  bool listed = cql_word(a, 2) != 0, grouped = cql_word(a, 10) != 0;
+  uint32_t min_key = cql_word(a, 4), range = cql_word(a, 6);
+  double group_min = __longlong_as_double((long long)a.push[4]);
+  uint64_t dim_rows = a.bytes[1] / 4, value_rows = a.bytes[2] / 8;
+  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < visits; v += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint64_t row = listed ? visit_rows[v] : v;
+    if (row >= dim_rows || (grouped && row >= value_rows)) continue;
+    uint32_t k = dim_keys[row] - min_key;
+    if (k >= range) continue;
+    uint32_t gid = grouped ? (uint32_t)(group_values[row] - group_min) : 0u;
+    uint32_t prev = atomicCAS(&table[k], LUT_EMPTY, gid);
+    if (prev != LUT_EMPTY) atomicOr(error, 1u);
+    else visit_of[k] = (uint32_t)v;
+  }
+}
+
+__global__ void __launch_bounds__(JOIN_THREADS) k_join_lut_map(CqlLaunch a, uint64_t rows)
+{
+  const uint32_t* keys = (const uint32_t*)a.buf[0];
+  const uint32_t* table = (const uint32_t*)a.buf[1];
+  uint32_t* ids = (uint32_t*)a.buf[2];
+  uint32_t* present = (uint32_t*)a.buf[3];
+  uint32_t min_key = cql_word(a, 4), range = cql_word(a, 6), none = cql_word(a, 8);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint32_t k = keys[i] - min_key;
+    uint32_t gid = k < range ? table[k] : LUT_EMPTY;
+    ids[i] = gid == LUT_EMPTY ? none : gid;
+    if (gid != LUT_EMPTY)
+    {
+      // most keys repeat: read the word first, write it only the first time
+      uint32_t bit = 1u << (k & 31u);
+      if (!(present[k >> 5] & bit)) atomicOr(&present[k >> 5], bit);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(JOIN_THREADS) k_join_lut_first(CqlLaunch a, uint64_t range)
+{
+  const uint32_t* present = (const uint32_t*)a.buf[0];
+  const uint32_t* table = (const uint32_t*)a.buf[1];
+  const uint32_t* visit_of = (const uint32_t*)a.buf[2];
+  uint32_t* first = (uint32_t*)a.buf[3];
+  uint64_t groups = a.bytes[3] / 4;
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < range; k += (uint64_t)gridDim.x * blockDim.x)
+  {
+    if (!((present[k >> 5] >> (k & 31)) & 1u)) continue;
+    uint32_t gid = table[k];
+    if (gid < groups) atomicMin(&first[gid], visit_of[k]);
+  }
+}
+
+static int launch_join_lut_build(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t visits = cql_word(a, 0);
+  uint64_t range = cql_word(a, 6);
+  if (visits == 0) return 0;
+  if (a.bytes[3] < range * 4 || a.bytes[4] < range * 4 || a.bytes[5] < 4 || (cql_word(a, 2) && a.bytes[0] < visits * 4))
+    return (int)cudaErrorInvalidValue;
+  k_join_lut_build<<<cql_stream_grid((visits + JOIN_THREADS - 1) / JOIN_THREADS, 8), JOIN_THREADS, 0, stream>>>(a, visits);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+static int launch_join_lut_map(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t rows = cql_word(a, 0);
+  uint64_t range = cql_word(a, 6);
+  if (rows == 0) return 0;
+  if (a.bytes[0] < rows * 4 || a.bytes[1] < range * 4 || a.bytes[2] < rows * 4 || a.bytes[3] < ((range + 31) / 32) * 4)
+    return (int)cudaErrorInvalidValue;
+  k_join_lut_map<<<cql_stream_grid((rows + JOIN_THREADS - 1) / JOIN_THREADS, 8), JOIN_THREADS, 0, stream>>>(a, rows);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+static int launch_join_lut_first(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t range = cql_word(a, 6);
+  if (range == 0) return 0;
+  if (a.bytes[0] < ((range + 31) / 32) * 4 || a.bytes[1] < range * 4 || a.bytes[2] < range * 4) return (int)cudaErrorInvalidValue;
+  k_join_lut_first<<<cql_stream_grid((range + JOIN_THREADS - 1) / JOIN_THREADS, 8), JOIN_THREADS, 0, stream>>>(a, range);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
 const CqlKernelDesc cql_kernels_join[] = {
   { "hash_join_build_count", launch_join_build_count },
   { "prefix_sum", launch_prefix_sum },
@@ -435,5 +558,8 @@ const CqlKernelDesc cql_kernels_join[] = {
   { "hash_join_probe", launch_join_probe },
   { "join_pack_key", launch_join_pack_key },
   { "join_probe_native", launch_join_probe_native },
+  { "cql_join_lut_build", launch_join_lut_build },
+  { "cql_join_lut_map", launch_join_lut_map },
+  { "cql_join_lut_first", launch_join_lut_first },
   { nullptr, nullptr },
 };

@@ -563,6 +563,207 @@ static void group_task(void* p, uint32_t chunk)
 static __thread uint32_t* tl_kept = NULL;
 static __thread uint64_t tl_kept_cap = 0;
 
+/* ---- strategy 3: a lookup table over the fact key's range ----
+   With unique dim keys and one whole-number GROUP BY value of small range (or none), every fact key value
+   maps to at most one group: the device builds that table from the dim rows, turns the fact keys into
+   group ids (cql_join_lut_map) and the dense group-by aggregates them; the first kept dim row of every
+   group comes from the device as well. The host passes over the visited dim rows once (their group
+   values' range) and never over the fact rows. Gives way (-1) when the dim keys repeat, the group values
+   are not small whole numbers, there are dim-side aggregates or the key range passes 2^24. */
+#define LUT_MAX_RANGE (1ull << 24)
+#define LUT_MAX_GROUPS 65535u
+
+typedef struct
+{
+  uint32_t first, gid;
+} LutGroup;
+
+static int lut_group_by_first(const void* a, const void* b)
+{
+  uint32_t x = ((const LutGroup*)a)->first, y = ((const LutGroup*)b)->first;
+  return x < y ? -1 : (x > y);
+}
+
+static int lut_join_aggregate(const CqlJoinAgg* q, uint32_t core_count, const uint32_t* core_funcs, const CqlColumn* const* core_cols,
+                              const uint32_t* core_of_expr, uint64_t max_groups, uint64_t* out_groups, uint64_t* out_group_dim_row,
+                              double* out_results)
+{
+  const CqlColumn* fk = q->fact_key;
+  if (!fk->has_range || !fk->buffer || fk->width != 0 || q->group_count > 1) return -1;
+  for (uint32_t e = 0; q->dim_args && e < q->expr_count; e++)
+    if (q->dim_args[e]) return -1;
+  double span = fk->zone_max - fk->zone_min;
+  if (!(span >= 0.0) || span + 1.0 > (double)LUT_MAX_RANGE) return -1;
+  uint64_t range = (uint64_t)span + 1;
+  uint32_t min_bits = (uint32_t)(int64_t)fk->zone_min;
+  uint64_t visits = q->dim_rows ? q->dim_count : q->dim_table_rows;
+  uint64_t D = q->dim_table_rows;
+  if (visits == 0 || D == 0 || D >= 0xffffffffull || visits >= 0xffffffffull) return -1;
+  /* the group values of the visited rows: whole numbers within LUT_MAX_GROUPS of each other */
+  const double* gv = q->group_count ? q->dim_group_values[0] : NULL;
+  double vmin = 0.0, vmax = 0.0;
+  if (gv)
+  {
+    vmin = HUGE_VAL;
+    vmax = -HUGE_VAL;
+    for (uint64_t v = 0; v < visits; v++)
+    {
+      uint64_t row = q->dim_rows ? q->dim_rows[v] : v;
+      if (row >= D) return -1;
+      double x = gv[row];
+      if (!(x == (double)(int64_t)x) || x > 9.0e15 || x < -9.0e15) return -1;
+      if (x < vmin) vmin = x;
+      if (x > vmax) vmax = x;
+    }
+    if (vmax - vmin > (double)(LUT_MAX_GROUPS - 1)) return -1;
+  }
+  uint32_t ngroups = gv ? (uint32_t)(vmax - vmin) + 1u : 1u;
+  uint64_t rows = fk->rows;
+  uint32_t* visit_list = NULL;
+  if (q->dim_rows)
+  {
+    visit_list = (uint32_t*)malloc(visits * 4);
+    if (!visit_list) return refuse("out of host memory");
+    for (uint64_t v = 0; v < visits; v++)
+    {
+      if (q->dim_rows[v] >= D)
+      {
+        free(visit_list);
+        return -1;
+      }
+      visit_list[v] = (uint32_t)q->dim_rows[v];
+    }
+  }
+  CqlBuffer* vbuf = pooled("join_lut_visits", visit_list ? visits * 4 : 4, CQLCUDA_BUFFER_WRITE);
+  CqlBuffer* kbuf = pooled("join_lut_dim_keys", D * 4, CQLCUDA_BUFFER_WRITE);
+  CqlBuffer* gbuf = pooled("join_lut_group_values", gv ? D * 8 : 8, CQLCUDA_BUFFER_WRITE);
+  CqlBuffer* table = pooled("join_lut_table", range * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* visit_of = pooled("join_lut_visit_of", range * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* err = pooled("join_lut_error", 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* ids = pooled("join_lut_group_ids", rows * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* present = pooled("join_lut_present", ((range + 31) / 32) * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* first = pooled("join_lut_first", (uint64_t)ngroups * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlKernel* kb = kernel("cql_join_lut_build");
+  CqlKernel* km = kernel("cql_join_lut_map");
+  CqlKernel* kf = kernel("cql_join_lut_first");
+  uint32_t* h_first = (uint32_t*)malloc((uint64_t)ngroups * 4);
+  if (!vbuf || !kbuf || !gbuf || !table || !visit_of || !err || !ids || !present || !first || !kb || !km || !kf || !h_first)
+  {
+    free(visit_list);
+    free(h_first);
+    return 0;
+  }
+  uint64_t group_min_bits;
+  memcpy(&group_min_bits, &vmin, 8);
+  cqlcuda_kernel_set_arg_buffer(kb, 0, vbuf);
+  cqlcuda_kernel_set_arg_buffer(kb, 1, kbuf);
+  cqlcuda_kernel_set_arg_buffer(kb, 2, gbuf);
+  cqlcuda_kernel_set_arg_buffer(kb, 3, table);
+  cqlcuda_kernel_set_arg_buffer(kb, 4, visit_of);
+  cqlcuda_kernel_set_arg_buffer(kb, 5, err);
+  cqlcuda_kernel_set_arg_u64(kb, 0, visits);
+  cqlcuda_kernel_set_arg_u64(kb, 1, visit_list ? 1 : 0);
+  cqlcuda_kernel_set_arg_u64(kb, 2, min_bits);
+  cqlcuda_kernel_set_arg_u64(kb, 3, range);
+  cqlcuda_kernel_set_arg_u64(kb, 4, group_min_bits);
+  cqlcuda_kernel_set_arg_u64(kb, 5, gv ? 1 : 0);
+  cqlcuda_kernel_set_arg_buffer(km, 0, fk->buffer);
+  cqlcuda_kernel_set_arg_buffer(km, 1, table);
+  cqlcuda_kernel_set_arg_buffer(km, 2, ids);
+  cqlcuda_kernel_set_arg_buffer(km, 3, present);
+  cqlcuda_kernel_set_arg_u64(km, 0, rows);
+  cqlcuda_kernel_set_arg_u64(km, 2, min_bits);
+  cqlcuda_kernel_set_arg_u64(km, 3, range);
+  cqlcuda_kernel_set_arg_u64(km, 4, ngroups);
+  cqlcuda_kernel_set_arg_buffer(kf, 0, present);
+  cqlcuda_kernel_set_arg_buffer(kf, 1, table);
+  cqlcuda_kernel_set_arg_buffer(kf, 2, visit_of);
+  cqlcuda_kernel_set_arg_buffer(kf, 3, first);
+  cqlcuda_kernel_set_arg_u64(kf, 3, range);
+  uint32_t error = 0;
+  CqlBatch* b = cqlcuda_batch_begin((visit_list ? visits * 4 : 0) + D * 4 + (gv ? D * 8 : 0), 4 + (uint64_t)ngroups * 4);
+  if (visit_list) cqlcuda_batch_buffer_write(b, vbuf, visit_list, visits * 4);
+  cqlcuda_batch_buffer_write(b, kbuf, q->dim_keys, D * 4);
+  if (gv) cqlcuda_batch_buffer_write(b, gbuf, gv, D * 8);
+  cqlcuda_batch_buffer_fill(b, table, range * 4, 0xffffffffu);
+  cqlcuda_batch_buffer_fill(b, first, (uint64_t)ngroups * 4, 0xffffffffu);
+  cqlcuda_batch_buffer_zero(b, present, ((range + 31) / 32) * 4);
+  cqlcuda_batch_buffer_zero(b, err, 4);
+  cqlcuda_batch_kernel_execute(b, kb, (uint32_t)visits, QE_GPU_WORKGROUP_SIZE);
+  cqlcuda_batch_kernel_execute(b, km, (uint32_t)(rows < 0xffffffffull ? rows : 0xffffffffull), QE_GPU_WORKGROUP_SIZE);
+  cqlcuda_batch_kernel_execute(b, kf, (uint32_t)range, QE_GPU_WORKGROUP_SIZE);
+  cqlcuda_batch_buffer_read(b, err, &error, 4);
+  cqlcuda_batch_buffer_read(b, first, h_first, (uint64_t)ngroups * 4);
+  int ok = cqlcuda_batch_end(b);
+  free(visit_list);
+  if (ok && error)
+  {
+    free(h_first);
+    return -1;   /* a dim key repeats */
+  }
+  /* the aggregates per group id (the last id collects the fact rows that join nothing) */
+  CqlColumn idcol;
+  memset(&idcol, 0, sizeof(idcol));
+  idcol.type = CQLOPS_TYPE_U32;
+  idcol.rows = rows;
+  idcol.buffer = ids;
+  idcol.has_range = 1;
+  idcol.zone_min = 0.0;
+  idcol.zone_max = (double)ngroups;
+  uint64_t slots = (uint64_t)ngroups + 1;
+  uint64_t* counts = (uint64_t*)malloc(slots * 8);
+  int64_t* sums = (int64_t*)malloc(slots * core_count * 8);
+  int64_t* mins = (int64_t*)malloc(slots * core_count * 8);
+  int64_t* maxs = (int64_t*)malloc(slots * core_count * 8);
+  LutGroup* order = (LutGroup*)malloc((uint64_t)ngroups * sizeof(LutGroup));
+  uint64_t got_groups = 0;
+  int64_t got_min = 0;
+  ok = ok && counts && sums && mins && maxs && order &&
+       cqlops_group_dense(&idcol, rows, core_count, core_funcs, core_cols, slots, &got_groups, &got_min, counts, sums, mins, maxs);
+  int result = ok ? 1 : -1;
+  if (ok)
+  {
+    uint64_t groups = 0;
+    for (uint32_t gid = 0; gid < ngroups; gid++)
+      if (h_first[gid] != 0xffffffffu && gid < got_groups)
+      {
+        order[groups].first = h_first[gid];
+        order[groups].gid = gid;
+        groups++;
+      }
+    qsort(order, groups, sizeof(LutGroup), lut_group_by_first);
+    if (groups > max_groups) result = refuse("more groups than the output arrays hold");
+    for (uint64_t g = 0; result == 1 && g < groups; g++)
+    {
+      uint32_t gid = order[g].gid;
+      uint64_t visit = order[g].first;
+      out_group_dim_row[g] = q->dim_rows ? q->dim_rows[visit] : visit;
+      for (uint32_t e = 0; e < q->expr_count; e++)
+      {
+        uint64_t slot = (uint64_t)gid * core_count + core_of_expr[e];
+        double count = (double)counts[gid], r;
+        switch (q->funcs[e])
+        {
+          case CQLOPS_FUNC_COUNT: r = count; break;
+          case CQLOPS_FUNC_SUM: r = (double)sums[slot]; break;
+          case CQLOPS_FUNC_AVG: r = counts[gid] ? (double)sums[slot] / count : 0.0; break;
+          case CQLOPS_FUNC_MIN: r = (double)mins[slot]; break;
+          default: r = (double)maxs[slot]; break;
+        }
+        out_results[g * q->expr_count + e] = r;
+      }
+    }
+    if (result == 1) *out_groups = groups;
+  }
+  free(counts);
+  free(sums);
+  free(mins);
+  free(maxs);
+  free(order);
+  free(h_first);
+  return result;
+}
+
 int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* out_groups, uint64_t* out_group_dim_row, double* out_results,
                           uint32_t* out_strategy)
 {
@@ -601,6 +802,18 @@ int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* ou
   uint64_t rows = fk->rows;
   /* totals per key: dense over a small key range, else per dim row by probing (:8607-8617) */
   uint64_t groups_cap = fk->has_range ? (uint64_t)(fk->zone_max - fk->zone_min) + 1 : 0;
+  /* a mid-sized key range: through a lookup table on the device when the dim side allows it */
+  if (q->strategy == 3 || (q->strategy == 0 && fk->has_range && groups_cap > 65536))
+  {
+    int r = lut_join_aggregate(q, core_count, core_funcs, core_cols, core_of_expr, max_groups, out_groups, out_group_dim_row, out_results);
+    if (r >= 0)
+    {
+      if (r == 1 && out_strategy) *out_strategy = 3u;
+      return r;
+    }
+    if (q->strategy == 3) return refuse("the lookup-table join needs unique dim keys, one small whole-number GROUP BY value and no dim-side aggregates");
+    cqlops_note_error("");
+  }
   int by_dim_row = 0;
   uint64_t total_groups = 0;
   int64_t min_key = 0;

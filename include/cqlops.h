@@ -265,11 +265,14 @@ typedef struct CqlJoinAgg
   uint64_t dim_count;
   uint32_t group_count;               /* GROUP BY dim columns */
   const double* const* dim_group_values; /* host, f64 per dim row */
-  uint32_t strategy;                  /* 0 automatic, 1 dense over the fact key's range, 2 probe a hash table of the dim keys */
+  uint32_t strategy;                  /* 0 automatic, 1 dense over the fact key's range, 2 probe a hash table of the dim keys,
+                                         3 a lookup table over the fact key's range (unique dim keys, at most one
+                                         whole-number GROUP BY value spanning < 65536, no dim-side aggregates, a key
+                                         range up to 2^24; automatic picks it for ranges above 65536 when it applies) */
 } CqlJoinAgg;
 
 /* Groups come out in the order their first dim row is met; out_group_dim_row[g] is that row,
-   out_results[g*expr_count + e] the aggregate. out_strategy receives 1 (dense) or 2 (probe). */
+   out_results[g*expr_count + e] the aggregate. out_strategy receives 1 (dense), 2 (probe) or 3 (lookup table). */
 int cqlops_join_aggregate(const CqlJoinAgg* query, uint64_t max_groups, uint64_t* out_groups, uint64_t* out_group_dim_row, double* out_results,
                           uint32_t* out_strategy);
 

@@ -143,3 +143,82 @@ def test_dense_and_probe_paths_agree(ops):
         m = np.isin(key, keys_in)
         assert r[0] == m.sum() and r[1] == float(v[m].astype(np.int64).sum())
         assert (r[2], r[3]) == (float(v[m].min()), float(v[m].max()))
+
+
+def _join_reference(ops, kc, funcs, args, dim_keys, **kw):
+    """The probe path's answer (strategy 2) as {dim_row: results} in output order."""
+    r = ops.join_aggregate(kc, funcs, args, dim_keys, strategy=2, **kw)
+    return list(r["dim_row"]), r["results"]
+
+
+@pytest.mark.parametrize("signed", [False, True])
+def test_lookup_table_join_equals_the_probe(ops, signed):
+    """Strategy 3 (a lookup table over a 1M-value key range) against the probe path: the same groups in
+    the same order (their first kept dim row), the same COUNT/SUM/AVG/MIN/MAX."""
+    rng = np.random.default_rng(21 + signed)
+    n, d = 3_000_000, 1_000_000
+    base = -500_000 if signed else 0
+    key = (rng.integers(0, d, n) + base).astype(np.int32 if signed else np.uint32)
+    v = rng.integers(-2000, 2000, n).astype(np.int32)
+    dim_keys = (rng.permutation(d) + base).astype(np.int32 if signed else np.uint32).view(np.uint32)
+    seg = rng.integers(0, 20, d).astype(np.float64)
+    kc, vc = ops.Column.from_numpy(key), ops.Column.from_numpy(v)
+    funcs, args = [COUNT, SUM, AVG, MIN, MAX], [None, vc, vc, vc, vc]
+    auto = ops.join_aggregate(kc, funcs, args, dim_keys, group_values=[seg])
+    assert auto["strategy"] == 3
+    rows, res = _join_reference(ops, kc, funcs, args, dim_keys, group_values=[seg])
+    assert list(auto["dim_row"]) == rows
+    np.testing.assert_array_equal(auto["results"], res)
+    # against the oracle: the joined rows per segment; and each segment's SUM from the fact side
+    counts, _ = oracle.join_aggregate(key.view(np.uint32), None, dim_keys, seg.astype(np.uint32), 20)
+    seg_of_key = np.empty(d, dtype=np.int64)
+    seg_of_key[dim_keys.view(key.dtype).astype(np.int64) - base] = seg.astype(np.int64)
+    fact_seg = seg_of_key[key.astype(np.int64) - base]
+    for g, r in enumerate(auto["dim_row"]):
+        s = int(seg[r])
+        m = fact_seg == s
+        assert auto["results"][g, 0] == counts[s] == m.sum()
+        assert auto["results"][g, 1] == float(v[m].astype(np.int64).sum())
+
+
+def test_lookup_table_join_with_a_dim_filter_and_no_group(ops):
+    rng = np.random.default_rng(33)
+    n, d = 2_000_000, 400_000
+    key = rng.integers(0, d, n).astype(np.uint32)
+    dim_keys = rng.permutation(d).astype(np.uint32)
+    kept = np.sort(rng.choice(d, d // 3, replace=False)).astype(np.uint64)
+    kc = ops.Column.from_numpy(key)
+    a = ops.join_aggregate(kc, [COUNT], [None], dim_keys, dim_rows=kept, strategy=3)
+    b = ops.join_aggregate(kc, [COUNT], [None], dim_keys, dim_rows=kept, strategy=2)
+    assert a["strategy"] == 3 and a["groups"] == b["groups"] == 1
+    assert list(a["dim_row"]) == list(b["dim_row"])
+    assert a["results"][0, 0] == np.isin(key, dim_keys[kept.astype(np.int64)]).sum()
+    seg = (np.arange(d) % 11).astype(np.float64)
+    a = ops.join_aggregate(kc, [COUNT], [None], dim_keys, dim_rows=kept, group_values=[seg], strategy=3)
+    b = ops.join_aggregate(kc, [COUNT], [None], dim_keys, dim_rows=kept, group_values=[seg], strategy=2)
+    assert list(a["dim_row"]) == list(b["dim_row"])
+    np.testing.assert_array_equal(a["results"], b["results"])
+
+
+def test_lookup_table_gives_way_to_repeated_dim_keys(ops):
+    """Repeated dim keys: the lookup table gives way; past the dense range the probe path refuses them as
+    it did before (each key must name one dim row), and a forced lookup table refuses too."""
+    rng = np.random.default_rng(44)
+    n, d = 1_000_000, 200_000
+    key = rng.integers(0, d, n).astype(np.uint32)
+    dim_keys = rng.integers(0, d, d).astype(np.uint32)
+    seg = (np.arange(d) % 5).astype(np.float64)
+    kc = ops.Column.from_numpy(key)
+    for strategy in (0, 2, 3):
+        with pytest.raises(ops.OpError):
+            ops.join_aggregate(kc, [COUNT], [None], dim_keys, group_values=[seg], strategy=strategy)
+    # within the dense range the repeats are joined once per dim row
+    small = (key % 1000).astype(np.uint32)
+    dk = rng.integers(0, 1000, 3000).astype(np.uint32)
+    sg = (np.arange(3000) % 5).astype(np.float64)
+    r = ops.join_aggregate(ops.Column.from_numpy(small), [COUNT], [None], dk, group_values=[sg])
+    assert r["strategy"] == 1
+    per_key = np.bincount(small, minlength=1000)
+    for g, row in enumerate(r["dim_row"]):
+        want = sum(int(per_key[k]) for k in dk[sg == sg[row]])
+        assert r["results"][g, 0] == want
