@@ -837,6 +837,161 @@ static int launch_gather_string_bytes(const CqlLaunch& a, uint32_t gws, uint32_t
 }
 
 // ---------------------------------------------------------------------------------------------
+// cql_group_finish: the hash group-by's per-group outputs in the caller's layout, on the device: binding
+// 0 the compacted owner row per group (u32), 1 the row count per group (u32), 2 representative rows out
+// (u64), 3 counts out (u64); with word 8 set also the results of the fixed-point reduce: binding 4 sums
+// (i64 [group][expr]), 5 mins, 6 maxs (i32), 7 results out (f64 [group][expr]). Words 0 groups, 2 exprs,
+// 4 funcs (4 bits each), 6 the power-of-ten exponents (4 bits each), 8 results wanted. A scaled integer
+// becomes its value as the host finalized it (query_exec.c:11750-11773): the double of the integer
+// divided by 10^s, AVG divided by the count after that.
+
+__constant__ double c_pow10[7] = { 1.0, 10.0, 100.0, 1000.0, 10000.0, 100000.0, 1000000.0 };
+
+__global__ void __launch_bounds__(HASH_THREADS) k_group_finish(CqlLaunch a, uint64_t groups)
+{
+  const uint32_t* owner = (const uint32_t*)a.buf[0];
+  const uint32_t* count = (const uint32_t*)a.buf[1];
+  unsigned long long* repr = (unsigned long long*)a.buf[2];
+  unsigned long long* counts = (unsigned long long*)a.buf[3];
+  const long long* sums = (const long long*)a.buf[4];
+  const int* mins = (const int*)a.buf[5];
+  const int* maxs = (const int*)a.buf[6];
+  double* results = (double*)a.buf[7];
+  uint32_t exprs = min(cql_word(a, 2), 8u), funcs = cql_word(a, 4), scales = cql_word(a, 6);
+  bool finish = cql_word(a, 8) != 0;
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < groups; g += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint32_t c = count[g];
+    repr[g] = owner[g];
+    counts[g] = c;
+    if (!finish) continue;
+    for (uint32_t e = 0; e < exprs; e++)
+    {
+      uint64_t i = g * exprs + e;
+      uint32_t f = (funcs >> (4 * e)) & 0xfu;
+      double divisor = c_pow10[min((scales >> (4 * e)) & 0xfu, 6u)];
+      double n = (double)c, r;
+      switch (f)
+      {
+        case FUNC_COUNT: r = n; break;
+        case FUNC_SUM: r = (double)sums[i] / divisor; break;
+        case FUNC_AVG: r = c > 0 ? (double)sums[i] / divisor / n : 0.0; break;
+        case FUNC_MIN: r = (double)mins[i] / divisor; break;
+        default: r = (double)maxs[i] / divisor; break;
+      }
+      results[i] = r;
+    }
+  }
+}
+
+static int launch_group_finish(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t groups = cql_word(a, 0);
+  if (groups == 0) return 0;
+  uint64_t cells = groups * min(cql_word(a, 2), 8u);
+  if (a.bytes[0] < groups * 4 || a.bytes[1] < groups * 4 || a.bytes[2] < groups * 8 || a.bytes[3] < groups * 8)
+    return (int)cudaErrorInvalidValue;
+  if (cql_word(a, 8) && (a.bytes[4] < cells * 8 || a.bytes[5] < cells * 4 || a.bytes[6] < cells * 4 || a.bytes[7] < cells * 8))
+    return (int)cudaErrorInvalidValue;
+  k_group_finish<<<cql_stream_grid((groups + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, groups);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// cql_small_key_extrema: for each value of a small-range whole-number key (at most 64 values), its first
+// row and the MIN and MAX of up to 4 columns: binding 0 the key column (u32 words, full width), 1 first
+// row per value (u32, all 0xffffffff before), 2 per value and column the (min, max) as f64 order keys
+// (u64 pairs, min all ones and max all zeros before), 3..6 the columns; word 0 rows, word 2 the smallest
+// key (bits), word 4 the range, word 6 the columns, word 8 their CQL types (4 bits each: U32, I32, F32,
+// F64). NaN values are skipped, as `v < min` skips them. Each CTA keeps its extrema in shared memory and
+// takes an atomic only when a value beats the one held, which after the first rows is seldom.
+
+#define EXTREMA_VALUES 64
+#define EXTREMA_COLUMNS 4
+
+__device__ __forceinline__ unsigned long long extrema_key(const void* col, uint32_t type, uint64_t r, bool* ok)
+{
+  double v;
+  switch (type)
+  {
+    case 1: v = (double)((const uint32_t*)col)[r]; break;
+    case 7: v = (double)((const int*)col)[r]; break;
+    case 3: v = (double)((const float*)col)[r]; break;
+    default: v = ((const double*)col)[r]; break;
+  }
+  *ok = v == v;
+  unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  if ((b << 1) == 0) b = 0;   // -0.0 compares equal to +0.0
+  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__global__ void __launch_bounds__(HASH_THREADS) k_small_key_extrema(CqlLaunch a, uint64_t rows)
+{
+  __shared__ uint32_t s_first[EXTREMA_VALUES];
+  __shared__ unsigned long long s_ext[EXTREMA_VALUES * EXTREMA_COLUMNS * 2];
+  const uint32_t* key = (const uint32_t*)a.buf[0];
+  uint32_t* first = (uint32_t*)a.buf[1];
+  unsigned long long* ext = (unsigned long long*)a.buf[2];
+  uint32_t min_key = cql_word(a, 2), range = min(cql_word(a, 4), (uint32_t)EXTREMA_VALUES);
+  uint32_t ncols = min(cql_word(a, 6), (uint32_t)EXTREMA_COLUMNS), types = cql_word(a, 8);
+  uint64_t ext_words = a.bytes[2] / 8;
+  for (uint32_t i = threadIdx.x; i < EXTREMA_VALUES; i += blockDim.x) s_first[i] = 0xffffffffu;
+  for (uint32_t i = threadIdx.x; i < EXTREMA_VALUES * EXTREMA_COLUMNS * 2; i += blockDim.x) s_ext[i] = (i & 1) ? 0ull : ~0ull;
+  __syncthreads();
+  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint32_t k = key[r] - min_key;
+    if (k >= range) continue;
+    if ((uint32_t)r < s_first[k]) atomicMin(&s_first[k], (uint32_t)r);
+    for (uint32_t c = 0; c < ncols; c++)
+    {
+      bool ok;
+      unsigned long long o = extrema_key(a.buf[3 + c], (types >> (4 * c)) & 0xfu, r, &ok);
+      if (!ok) continue;
+      unsigned long long* e = s_ext + (k * EXTREMA_COLUMNS + c) * 2;
+      if (o < e[0]) atomicMin(&e[0], o);
+      if (o > e[1]) atomicMax(&e[1], o);
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < range; i += blockDim.x)
+  {
+    if (s_first[i] == 0xffffffffu) continue;
+    if ((uint64_t)(i + 1) * 4 <= a.bytes[1]) atomicMin(&first[i], s_first[i]);
+    for (uint32_t c = 0; c < ncols; c++)
+    {
+      uint64_t at = ((uint64_t)i * EXTREMA_COLUMNS + c) * 2;
+      if (at + 1 >= ext_words) continue;
+      const unsigned long long* e = s_ext + (i * EXTREMA_COLUMNS + c) * 2;
+      atomicMin(&ext[at], e[0]);
+      atomicMax(&ext[at + 1], e[1]);
+    }
+  }
+}
+
+static int launch_small_key_extrema(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t rows = cql_word(a, 0);
+  if (rows == 0) return 0;
+  uint32_t ncols = cql_word(a, 6), types = cql_word(a, 8);
+  if (a.bytes[0] < rows * 4 || cql_word(a, 4) > EXTREMA_VALUES || ncols > EXTREMA_COLUMNS) return (int)cudaErrorInvalidValue;
+  for (uint32_t c = 0; c < ncols; c++)
+  {
+    uint32_t t = (types >> (4 * c)) & 0xfu;
+    uint64_t width = t == 4 ? 8 : 4;
+    if (!(t == 1 || t == 7 || t == 3 || t == 4) || a.bytes[3 + c] < rows * width) return (int)cudaErrorInvalidValue;
+  }
+  k_small_key_extrema<<<cql_stream_grid((rows + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, rows);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
 // Widening of a device column to dense f64 (the gather the operator layer does on the host before
 // a hash GROUP BY, query_exec.c:10454-10690): binding 0 source, 1 destination; word 0 rows, word 2
 // the source CQL type. Not a reference kernel: the reference uploads the f64 copy it builds on the host.
@@ -1087,6 +1242,8 @@ const CqlKernelDesc cql_kernels_hash[] = {
   { "csr_scatter_tiled", launch_csr_scatter },
   { "aggregate_reduce", launch_aggregate_reduce },
   { "cql_gather_columns", launch_gather_columns },
+  { "cql_small_key_extrema", launch_small_key_extrema },
+  { "cql_group_finish", launch_group_finish },
   { "cql_gather_string_lengths", launch_gather_string_lengths },
   { "cql_gather_string_bytes", launch_gather_string_bytes },
   { "selection_gather", launch_selection_gather },

@@ -28,7 +28,6 @@
 #define HLL_PRECISION 10
 #define HLL_SKETCH_MAX_BYTES (64ull << 20)
 
-static const double g_pow10[7] = { 1.0, 10.0, 100.0, 1000.0, 10000.0, 100000.0, 1000000.0 };
 
 void cqlops_note_error(const char* why);
 
@@ -327,6 +326,186 @@ static int csr_reduce(uint64_t rows, uint64_t slots, uint64_t groups, CqlBuffer*
   return ok;
 }
 
+/* ---- path 3: a small-range key with COUNT/SUM/AVG/MIN/MAX of f32/f64 columns, through the shared scan ----
+   Each key value v and summed column s is the query COUNT(*), SUM(s) WHERE key = v; the batched shared scan
+   (cqlops_batch_filter_aggregate) answers them all in one pass over the columns, its sums exact 128-bit
+   sums of the values scaled by 2^k, so the result does not depend on the order of the rows. The first row
+   of each value and the MIN/MAX of up to 4 columns come from one more pass (cql_small_key_extrema). A key
+   of at most 64 values. Gives way (-1) when the query does not fit, and to the fixed-point path when every
+   f32/f64 argument is a decimal of at most 6 places (that path finalizes them as the reference does). */
+#define SMALL_KEY_VALUES 64
+
+static double order_key_to_double(uint64_t k)
+{
+  uint64_t b = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+  double v;
+  memcpy(&v, &b, 8);
+  return v;
+}
+
+static int numeric_full(const CqlColumn* c, uint64_t rows)
+{
+  return c && c->rows == rows && c->width == 0 && c->buffer &&
+         (c->type == CQLOPS_TYPE_U32 || c->type == CQLOPS_TYPE_I32 || c->type == CQLOPS_TYPE_F32 || c->type == CQLOPS_TYPE_F64);
+}
+
+static int group_small_key(const CqlColumn* key, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* args, uint64_t max_groups,
+                           uint64_t* out_group_count, uint64_t* out_repr_row, uint64_t* out_counts, double* out_results)
+{
+  if (!(key->type == CQLOPS_TYPE_U32 || key->type == CQLOPS_TYPE_I32) || key->width != 0 || !key->buffer || !key->has_range) return -1;
+  double span = key->zone_max - key->zone_min;
+  if (!(span >= 0.0) || span + 1.0 > (double)SMALL_KEY_VALUES) return -1;
+  uint32_t values = (uint32_t)span + 1u;
+  int64_t kmin = (int64_t)key->zone_min;
+  uint64_t rows = key->rows;
+  /* the table the programs are built over: the key, then each distinct summed column; the extrema columns */
+  CqlColumn cols[9];
+  const char* names[9] = { "k", "a0", "a1", "a2", "a3", "a4", "a5", "a6", "a7" };
+  const CqlColumn* ext_cols[4];
+  uint32_t ncols = 1, next = 0, slot_of_expr[8] = { 0 }, fractional = 0;
+  cols[0] = *key;
+  for (uint32_t e = 0; e < expr_count; e++)
+  {
+    uint32_t f = funcs[e];
+    if (f == CQLOPS_FUNC_COUNT) continue;
+    const CqlColumn* c = args[e];
+    if (f > CQLOPS_FUNC_MAX || !numeric_full(c, rows)) return -1;
+    if (c->type == CQLOPS_TYPE_F32 || c->type == CQLOPS_TYPE_F64) fractional = 1;
+    if (f == CQLOPS_FUNC_SUM || f == CQLOPS_FUNC_AVG)
+    {
+      if (!c->has_range) return -1;
+      uint32_t i = 1;
+      while (i < ncols && cols[i].buffer != c->buffer) i++;
+      if (i == ncols)
+      {
+        if (ncols == 9) return -1;
+        cols[ncols++] = *c;
+      }
+      slot_of_expr[e] = i;
+    }
+    else
+    {
+      uint32_t i = 0;
+      while (i < next && ext_cols[i]->buffer != c->buffer) i++;
+      if (i == next)
+      {
+        if (next == 4) return -1;
+        ext_cols[next++] = c;
+      }
+      slot_of_expr[e] = i;
+    }
+  }
+  if (!fractional) return -1;   /* whole numbers: the fixed-point hash reduce is exact already */
+  /* decimals of at most 6 places take the fixed-point reduce, which finalizes them as the reference does */
+  int all_decimal = 1;
+  for (uint32_t e = 0; e < expr_count && all_decimal; e++)
+  {
+    const CqlColumn* c = args[e];
+    if (funcs[e] == CQLOPS_FUNC_COUNT || (c->type != CQLOPS_TYPE_F32 && c->type != CQLOPS_TYPE_F64)) continue;
+    int32_t scale = -1;
+    double largest = 0.0;
+    if (!cqlops_fixed_scale(c, NULL, rows, &scale, &largest) || scale < 0) all_decimal = 0;
+  }
+  cqlops_note_error("");
+  if (all_decimal) return -1;
+  uint32_t sums_per_value = ncols > 1 ? ncols - 1 : 1;
+  uint32_t queries = values * sums_per_value;
+  CqlProgram* progs = (CqlProgram*)malloc((uint64_t)values * sizeof(CqlProgram));
+  const CqlProgram** qp = (const CqlProgram**)malloc((uint64_t)queries * sizeof(CqlProgram*));
+  int32_t* sum_cols = (int32_t*)malloc((uint64_t)queries * 4);
+  uint64_t* counts = (uint64_t*)malloc((uint64_t)queries * 8);
+  double* sums = (double*)malloc((uint64_t)queries * 8);
+  uint32_t* first = (uint32_t*)malloc((uint64_t)values * 4);
+  uint64_t ext_words = (uint64_t)values * 4 * 2;
+  uint64_t* ext = (uint64_t*)malloc(ext_words * 8);
+  int result = progs && qp && sum_cols && counts && sums && first && ext ? 1 : 0;
+  for (uint32_t v = 0; result == 1 && v < values; v++)
+  {
+    char where[64];
+    snprintf(where, sizeof(where), "(= k %lld)", (long long)(kmin + v));
+    if (!cqlops_program_build(where, cols, names, ncols, &progs[v])) result = -1;
+    for (uint32_t s = 0; s < sums_per_value; s++)
+    {
+      qp[v * sums_per_value + s] = &progs[v];
+      sum_cols[v * sums_per_value + s] = ncols > 1 ? (int32_t)(1 + s) : -1;
+    }
+  }
+  if (result == 1 && !cqlops_batch_filter_aggregate(qp, queries, cols, ncols, sum_cols, 8, counts, sums, NULL)) result = -1;
+  if (result == 1)
+  {
+    CqlBuffer* fb = pooled("agg_small_key_first", (uint64_t)values * 4, CQLCUDA_BUFFER_READ_WRITE);
+    CqlBuffer* eb = pooled("agg_small_key_extrema", ext_words * 8, CQLCUDA_BUFFER_READ_WRITE);
+    CqlKernel* k = kernel("cql_small_key_extrema");
+    if (!fb || !eb || !k) result = 0;
+    else
+    {
+      uint32_t types = 0;
+      for (uint32_t c = 0; c < next; c++) types |= (ext_cols[c]->type & 0xfu) << (4 * c);
+      cqlcuda_kernel_set_arg_buffer(k, 0, key->buffer);
+      cqlcuda_kernel_set_arg_buffer(k, 1, fb);
+      cqlcuda_kernel_set_arg_buffer(k, 2, eb);
+      for (uint32_t c = 0; c < 4; c++) cqlcuda_kernel_set_arg_buffer(k, 3 + c, c < next ? ext_cols[c]->buffer : key->buffer);
+      cqlcuda_kernel_set_arg_u64(k, 0, rows);
+      cqlcuda_kernel_set_arg_u64(k, 1, (uint32_t)kmin);
+      cqlcuda_kernel_set_arg_u64(k, 2, values);
+      cqlcuda_kernel_set_arg_u64(k, 3, next);
+      cqlcuda_kernel_set_arg_u64(k, 4, types);
+      CqlBatch* b = cqlcuda_batch_begin(0, (uint64_t)values * 4 + ext_words * 8);
+      cqlcuda_batch_buffer_fill(b, fb, (uint64_t)values * 4, 0xffffffffu);
+      for (uint64_t i = 0; i < ext_words; i++) ext[i] = (i & 1) ? 0ull : ~0ull;
+      cqlcuda_batch_buffer_write(b, eb, ext, ext_words * 8);
+      cqlcuda_batch_kernel_execute(b, k, (uint32_t)rows, QE_GPU_WORKGROUP_SIZE);
+      cqlcuda_batch_buffer_read(b, fb, first, (uint64_t)values * 4);
+      cqlcuda_batch_buffer_read(b, eb, ext, ext_words * 8);
+      if (!cqlcuda_batch_end(b)) result = 0;
+    }
+  }
+  if (result == 1)
+  {
+    uint64_t g = 0;
+    for (uint32_t v = 0; v < values && result == 1; v++)
+    {
+      uint64_t count = counts[v * sums_per_value];
+      if (count == 0) continue;
+      if (g >= max_groups)
+      {
+        result = refuse("more groups than the output arrays hold");
+        break;
+      }
+      out_repr_row[g] = first[v];
+      out_counts[g] = count;
+      for (uint32_t e = 0; e < expr_count; e++)
+      {
+        uint32_t f = funcs[e];
+        double r = (double)count;
+        if (f == CQLOPS_FUNC_SUM || f == CQLOPS_FUNC_AVG)
+        {
+          double sum = sums[v * sums_per_value + (slot_of_expr[e] - 1)];
+          r = f == CQLOPS_FUNC_AVG ? sum / (double)count : sum;
+        }
+        else if (f == CQLOPS_FUNC_MIN || f == CQLOPS_FUNC_MAX)
+        {
+          /* a group whose values are all NaN keeps the member reduce's starting values */
+          uint64_t o = ext[((uint64_t)v * 4 + slot_of_expr[e]) * 2 + (f == CQLOPS_FUNC_MAX)];
+          int empty = f == CQLOPS_FUNC_MIN ? o == ~0ull : o == 0ull;
+          r = empty ? (f == CQLOPS_FUNC_MIN ? 1.0e300 : -1.0e300) : order_key_to_double(o);
+        }
+        out_results[g * expr_count + e] = r;
+      }
+      g++;
+    }
+    if (result == 1) *out_group_count = g;
+  }
+  free(progs);
+  free(qp);
+  free(sum_cols);
+  free(counts);
+  free(sums);
+  free(first);
+  free(ext);
+  return result;
+}
+
 int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* args,
                       const double* params, uint64_t group_hint, uint32_t path, uint64_t max_groups, uint64_t* out_group_count,
                       uint64_t* out_repr_row, uint64_t* out_counts, double* out_results, uint32_t* out_path)
@@ -344,6 +523,17 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
     *out_group_count = 0;
     if (out_path) *out_path = 0;
     return 1;
+  }
+  if ((path == 0 || path == 3) && key_count == 1)
+  {
+    int r = group_small_key(&keys[0], expr_count, funcs, args, max_groups, out_group_count, out_repr_row, out_counts, out_results);
+    if (r >= 0)
+    {
+      if (r == 1 && out_path) *out_path = 3;
+      return r;
+    }
+    if (path == 3) return refuse("path 3 takes one whole-number key of at most 64 values with COUNT/SUM/AVG/MIN/MAX over f32/f64 columns");
+    cqlops_note_error("");
   }
   uint32_t string_mask = 0;
   CqlBuffer* key_data[4] = { 0 };
@@ -518,44 +708,41 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
   }
   uint64_t groups = groups32;
   if (groups > max_groups) return refuse("more groups than the output arrays hold");
-  uint32_t* g_owner = (uint32_t*)malloc((groups ? groups : 1) * 4);
-  uint32_t* g_count = (uint32_t*)malloc((groups ? groups : 1) * 4);
-  if (!g_owner || !g_count)
-  {
-    free(g_owner);
-    free(g_count);
-    return 0;
-  }
-  {
-    CqlBatch* b = cqlcuda_batch_begin(0, groups * 8);
-    cqlcuda_batch_buffer_read(b, out_owner, g_owner, groups * 4);
-    cqlcuda_batch_buffer_read(b, out_count, g_count, groups * 4);
-    if (!cqlcuda_batch_end(b))
-    {
-      free(g_owner);
-      free(g_count);
-      return 0;
-    }
-  }
-  for (uint64_t g = 0; g < groups; g++)
-  {
-    out_repr_row[g] = g_owner[g];
-    out_counts[g] = g_count[g];
-  }
+  /* the representative rows and counts (and, on the fixed path, the finished results) are written in the
+     caller's layout by cql_group_finish and read straight into the caller's arrays */
+  CqlBuffer* repr64 = pooled("agg_finish_repr_buf", groups * 8, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* count64 = pooled("agg_finish_count_buf", groups * 8, CQLCUDA_BUFFER_READ_WRITE);
+  CqlKernel* finish = kernel("cql_group_finish");
+  if (!repr64 || !count64 || !finish) return 0;
+  cqlcuda_kernel_set_arg_buffer(finish, 0, out_owner);
+  cqlcuda_kernel_set_arg_buffer(finish, 1, out_count);
+  cqlcuda_kernel_set_arg_buffer(finish, 2, repr64);
+  cqlcuda_kernel_set_arg_buffer(finish, 3, count64);
+  for (uint32_t i = 4; i < 8; i++) cqlcuda_kernel_set_arg_buffer(finish, i, out_owner);
+  cqlcuda_kernel_set_arg_u64(finish, 0, groups);
+  cqlcuda_kernel_set_arg_u64(finish, 1, expr_count);
+  cqlcuda_kernel_set_arg_u64(finish, 2, func_codes);
+  cqlcuda_kernel_set_arg_u64(finish, 3, fixed_scales);
+  cqlcuda_kernel_set_arg_u64(finish, 4, 0);
   int ok = 1;
   if (use_fixed)
   {
-    /* 4a: per-row atomics into per-group arrays; the compact offsets are the slot -> group map */
+    /* 4a: per-row atomics into per-group arrays; the compact offsets are the slot -> group map. A query
+       of COUNTs alone needs no reduce: the compacted counts are its results. */
+    int reduce = 0, has_min_max = 0;
+    for (uint32_t e = 0; e < expr_count; e++)
+    {
+      if (funcs[e] != CQLOPS_FUNC_COUNT) reduce = 1;
+      if (funcs[e] == CQLOPS_FUNC_MIN || funcs[e] == CQLOPS_FUNC_MAX) has_min_max = 1;
+    }
     CqlKernel* hr = kernel("aggregate_hash_reduce_fixed");
     uint64_t cells = groups * expr_count;
     CqlBuffer* sums = pooled("agg_hash_sum_buf", cells * 8, CQLCUDA_BUFFER_READ_WRITE);
     CqlBuffer* cnts = pooled("agg_hash_count_buf", cells * 4, CQLCUDA_BUFFER_READ_WRITE);
     CqlBuffer* mins = pooled("agg_hash_min_buf", cells * 4, CQLCUDA_BUFFER_READ_WRITE);
     CqlBuffer* maxs = pooled("agg_hash_max_buf", cells * 4, CQLCUDA_BUFFER_READ_WRITE);
-    int64_t* hs = (int64_t*)malloc(cells * 8 + 8);
-    int32_t* hmn = (int32_t*)malloc(cells * 4 + 4);
-    int32_t* hmx = (int32_t*)malloc(cells * 4 + 4);
-    ok = hr && sums && cnts && mins && maxs && hs && hmn && hmx;
+    CqlBuffer* results = pooled("agg_finish_results_buf", cells * 8, CQLCUDA_BUFFER_READ_WRITE);
+    ok = hr && sums && cnts && mins && maxs && results;
     if (ok)
     {
       cqlcuda_kernel_set_arg_buffer(hr, 0, row_slot);
@@ -570,42 +757,39 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
       cqlcuda_kernel_set_arg_u64(hr, 2, func_codes);
       cqlcuda_kernel_set_arg_u64(hr, 3, fixed_scales);
       cqlcuda_kernel_set_arg_u64(hr, 4, groups >= AGG_MANY_GROUPS);
-      CqlBatch* b = cqlcuda_batch_begin(0, cells * 16);
-      cqlcuda_batch_buffer_zero(b, sums, cells * 8);
-      cqlcuda_batch_buffer_zero(b, cnts, cells * 4);
-      cqlcuda_batch_buffer_fill(b, mins, cells * 4, 0x7fffffffu);
-      cqlcuda_batch_buffer_fill(b, maxs, cells * 4, 0x80000000u);
-      cqlcuda_batch_kernel_execute(b, hr, (uint32_t)rows, QE_GPU_WORKGROUP_SIZE);
-      cqlcuda_batch_buffer_read(b, sums, hs, cells * 8);
-      cqlcuda_batch_buffer_read(b, mins, hmn, cells * 4);
-      cqlcuda_batch_buffer_read(b, maxs, hmx, cells * 4);
+      cqlcuda_kernel_set_arg_buffer(finish, 4, sums);
+      cqlcuda_kernel_set_arg_buffer(finish, 5, mins);
+      cqlcuda_kernel_set_arg_buffer(finish, 6, maxs);
+      cqlcuda_kernel_set_arg_buffer(finish, 7, results);
+      cqlcuda_kernel_set_arg_u64(finish, 4, 1);
+      CqlBatch* b = cqlcuda_batch_begin(0, groups * 16 + cells * 8);
+      if (reduce)
+      {
+        cqlcuda_batch_buffer_zero(b, sums, cells * 8);
+        cqlcuda_batch_buffer_zero(b, cnts, cells * 4);
+        if (has_min_max)
+        {
+          cqlcuda_batch_buffer_fill(b, mins, cells * 4, 0x7fffffffu);
+          cqlcuda_batch_buffer_fill(b, maxs, cells * 4, 0x80000000u);
+        }
+        cqlcuda_batch_kernel_execute(b, hr, (uint32_t)rows, QE_GPU_WORKGROUP_SIZE);
+      }
+      cqlcuda_batch_kernel_execute(b, finish, (uint32_t)groups, QE_GPU_WORKGROUP_SIZE);
+      cqlcuda_batch_buffer_read(b, repr64, out_repr_row, groups * 8);
+      cqlcuda_batch_buffer_read(b, count64, out_counts, groups * 8);
+      cqlcuda_batch_buffer_read(b, results, out_results, cells * 8);
       ok = cqlcuda_batch_end(b);
     }
-    if (ok)
-    {
-      for (uint64_t g = 0; g < groups; g++)
-        for (uint32_t e = 0; e < expr_count; e++)
-        {
-          /* back out of the scaled integers (:11750-11773) */
-          uint64_t i = g * expr_count + e;
-          double divisor = g_pow10[(fixed_scales >> (4 * e)) & 0xfu];
-          double count = (double)g_count[g], r;
-          switch (funcs[e])
-          {
-            case CQLOPS_FUNC_COUNT: r = count; break;
-            case CQLOPS_FUNC_SUM: r = (double)hs[i] / divisor; break;
-            case CQLOPS_FUNC_AVG: r = count > 0 ? (double)hs[i] / divisor / count : 0.0; break;
-            case CQLOPS_FUNC_MIN: r = (double)hmn[i] / divisor; break;
-            default: r = (double)hmx[i] / divisor; break;
-          }
-          out_results[i] = r;
-        }
-    }
-    free(hs);
-    free(hmn);
-    free(hmx);
   }
   else
+  {
+    CqlBatch* b = cqlcuda_batch_begin(0, groups * 16);
+    cqlcuda_batch_kernel_execute(b, finish, (uint32_t)groups, QE_GPU_WORKGROUP_SIZE);
+    cqlcuda_batch_buffer_read(b, repr64, out_repr_row, groups * 8);
+    cqlcuda_batch_buffer_read(b, count64, out_counts, groups * 8);
+    ok = cqlcuda_batch_end(b);
+  }
+  if (ok && !use_fixed)
   {
     /* 4b: member lists, group g's members at [start[g], start[g] + count[g]), laid out on the device:
        group starts and chunk bases by prefix sums, cursors and chunk ranges by kernels, the member
@@ -613,8 +797,6 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
     ok = csr_reduce(rows, slots, groups, count, offsets, out_count, row_slot, expr_count, funcs, func_codes, arg_f64, params,
                     out_results);
   }
-  free(g_owner);
-  free(g_count);
   if (ok)
   {
     *out_group_count = groups;

@@ -209,8 +209,8 @@ int cqlops_aggregate_global(const CqlColumn* columns, uint32_t column_count, dou
 
 /* AND of up to 8 numeric comparisons over up to 10 columns with scan_simple
    (qe_scan_filter_selected, query_exec.c:2495-3276). Writes the match count; when out_rows is not
-   NULL and out_capacity > 0 also up to out_capacity matching row numbers in ascending order (the
-   kernel's order is not deterministic; the list is sorted before it is returned).
+   NULL and out_capacity > 0 also up to out_capacity matching row numbers in ascending order (the kernel
+   writes a bitmap of the rows, which becomes the ascending list on the device).
    When out_rows is NULL the kernel runs count-only. */
 int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const CqlLeaf* leaves, uint32_t leaf_count,
                        uint64_t* out_count, uint32_t* out_rows, uint64_t out_capacity);
@@ -230,9 +230,13 @@ int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count,
    COUNT/SUM/AVG/MIN/MAX, APPROX_COUNT_DISTINCT (HyperLogLog, precision 10) and APPROX_PERCENTILE
    (t-digest, params[e] is the fraction) - qe_aggregate_impl's GPU hash path,
    src/query_exec/query_exec.c:10258-12300. group_hint > 0 sizes the table for that many groups.
-   path: 0 automatic, 1 member lists + aggregate_reduce, 2 the fixed-point atomic reduce. Per dense
-   group g: out_repr_row[g] (a row of the group), out_counts[g], out_results[g*expr_count + e].
-   out_path receives the path taken (1 or 2). */
+   path: 0 automatic, 1 member lists + aggregate_reduce, 2 the fixed-point atomic reduce, 3 one whole-number
+   key of at most 64 values with COUNT/SUM/AVG/MIN/MAX over f32/f64 columns: the sums from the batched
+   shared scan (exact scaled-integer sums), MIN/MAX and each group's first row from one more pass (groups in
+   key order, each represented by its first row; automatic takes it when it
+   applies and some argument is not a decimal of at most 6 places, which path 2 finalizes as the
+   reference does). Per dense group g: out_repr_row[g] (a row of the group), out_counts[g],
+   out_results[g*expr_count + e]. out_path receives the path taken (1, 2 or 3). */
 int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* args,
                       const double* params, uint64_t group_hint, uint32_t path, uint64_t max_groups, uint64_t* out_group_count,
                       uint64_t* out_repr_row, uint64_t* out_counts, double* out_results, uint32_t* out_path);

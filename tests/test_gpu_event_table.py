@@ -1,9 +1,8 @@
 """The wide-table configuration's nine queries (10M-row, 30-column event table) against the oracle.
 
 The table is the seeded event table at 1M rows (the generator is the same at 10M; the 1M-group query keeps
-its 1M possible user ids). Counts, integer aggregates, group keys, filter rows and the sort order are
-compared exactly; f64 sums within 1e-12 relative of a compensated host sum; the distinct count equals the
-oracle's HyperLogLog estimate from its own registers.
+its 1M possible user ids). Counts, integer aggregates, group keys, MIN/MAX, filter rows and the sort order
+are compared exactly; f64 sums and averages within 1e-12 relative of a compensated host sum.
 """
 import numpy as np
 import pytest
@@ -37,46 +36,58 @@ def test_generator_matches_the_oracle_stream(suite):
 
 def test_group_by_dict_string(suite):
     _, _, h, _, res, _ = suite
-    min_key, counts, _, _, _ = res["group_by_dict_string"]
+    min_key, counts, sums, _, _ = res["group_by_dict_string"]
     assert min_key == 0
     np.testing.assert_array_equal(counts, np.bincount(h["s0"], minlength=200))
+    np.testing.assert_array_equal(sums[:, 1], np.bincount(h["s0"], weights=h["u0"].astype(np.float64), minlength=200).astype(np.int64))
 
 
-def test_group_by_status_f64_sums(suite):
+def _close(got, exact):
+    return abs(got - exact) <= 1e-12 * abs(exact)
+
+
+def test_group_by_status_f64(suite):
     _, _, h, _, res, _ = suite
     r = res["group_by_status_f64"]
     assert r["groups"] == 5
     for g in range(5):
         status = h["status"][int(r["repr_row"][g])]
         sel = h["status"] == status
+        assert r["repr_row"][g] == np.argmax(sel)
         assert r["counts"][g] == sel.sum()
-        for e, m in enumerate(("m0", "m1", "m2")):
-            exact = oracle.compensated_sum(h[m][sel])
-            assert abs(r["results"][g, e] - exact) <= 1e-12 * abs(exact)
+        total, m1 = oracle.compensated_sum(h["m0"][sel]), h["m1"][sel]
+        assert _close(r["results"][g, 0], total)
+        assert _close(r["results"][g, 1], oracle.compensated_sum(m1) / sel.sum())
+        assert (r["results"][g, 2], r["results"][g, 3]) == (m1.min(), m1.max())
 
 
-@pytest.mark.parametrize("name,program", [("dict_string_eq_filter", "eq"), ("three_predicate_filter", "triple")])
-def test_filters(suite, name, program):
-    cols, _, h, _, res, progs = suite
-    count, rows, _ = res[name]
-    arrays = {k: v for k, v in h.items()}
-    want = np.nonzero(oracle_mask(progs[program], arrays))[0]
-    assert count == len(want) and len(want) > 0
-    np.testing.assert_array_equal(rows, want)
+def test_dict_string_eq_count(suite):
+    _, _, h, _, res, progs = suite
+    count, rows, _ = res["dict_string_eq_filter"]
+    assert rows is None
+    assert count == oracle_mask(progs["eq"], dict(h)).sum() > 0
 
 
 def test_group_by_region_five_aggregates(suite):
     _, _, h, _, res, _ = suite
-    min_key, counts, sums, mins, maxs = res["group_by_region_5_aggs"]
-    assert min_key == 0 and len(counts) == 50
+    r = res["group_by_region_5_aggs"]
     key = h["region"]
-    np.testing.assert_array_equal(counts, np.bincount(key, minlength=50))
+    assert r["groups"] == 50
     for g in range(50):
         sel = key == g
-        assert sums[g, 1] == h["u0"][sel].astype(np.int64).sum()
-        assert mins[g, 2] == h["u1"][sel].min()
-        assert maxs[g, 3] == h["u2"][sel].max()
-        assert sums[g, 4] == h["u3"][sel].astype(np.int64).sum()      # AVG's sum; the average is sum / count
+        assert key[int(r["repr_row"][g])] == g and r["counts"][g] == sel.sum()
+        assert r["results"][g, 0] == sel.sum()
+        assert r["results"][g, 1] == float(h["u0"][sel].astype(np.int64).sum())
+        assert _close(r["results"][g, 2], oracle.compensated_sum(h["m0"][sel]) / sel.sum())
+        assert (r["results"][g, 3], r["results"][g, 4]) == (h["m1"][sel].min(), h["m1"][sel].max())
+
+
+def test_three_predicate_count_and_sum(suite):
+    _, _, h, _, res, progs = suite
+    count, sums, _, _ = res["three_predicate_filter"]
+    mask = oracle_mask(progs["triple"], dict(h)).astype(bool)
+    assert count == mask.sum() > 0
+    assert sums[0] == float(h["u5"][mask].astype(np.int64).sum())
 
 
 def test_join_users_group_by_segment(suite):
@@ -93,31 +104,26 @@ def test_group_by_user_id(suite):
     _, _, h, _, res, _ = suite
     r = res["group_by_user_id"]
     uid = h["user_id"]
-    present = np.unique(uid)
-    assert r["groups"] == len(present)
+    assert r["groups"] == len(np.unique(uid))
     keys = uid[r["repr_row"].astype(np.int64)]
     assert len(np.unique(keys)) == r["groups"]
-    order = np.argsort(uid, kind="stable")
-    starts = np.searchsorted(uid[order], keys)
-    ends = np.searchsorted(uid[order], keys, side="right")
-    np.testing.assert_array_equal(r["counts"], ends - starts)
-    m0 = h["m0"][order]
-    for g in np.random.default_rng(1).choice(r["groups"], 2000, replace=False):
-        exact = oracle.compensated_sum(m0[starts[g]:ends[g]])
-        assert abs(r["results"][g, 1] - exact) <= 1e-12 * abs(exact)
+    np.testing.assert_array_equal(r["counts"], np.bincount(uid, minlength=1_000_000)[keys])
+    sums = np.bincount(uid, weights=h["u0"].astype(np.float64), minlength=1_000_000)
+    np.testing.assert_array_equal(r["results"][:, 1], sums[keys])
 
 
-def test_approx_distinct_session(suite):
+def test_distinct_sessions(suite):
     _, _, h, _, res, _ = suite
-    r = res["approx_distinct_session"]
-    want = round(oracle.hll_estimate(oracle.hll_registers(h["session"].astype(np.float64))))
-    assert r["results"][0, 0] == want
+    r = res["distinct_sessions"]
+    assert r["groups"] == len(np.unique(h["session"]))
+    assert int(r["counts"].sum()) == len(h["session"])
 
 
-def test_order_by_f64_filtered(suite):
+def test_sort_200k(suite):
     _, _, h, _, res, _ = suite
-    rows, order = res["order_by_f64_filtered"]
-    want_rows = np.nonzero((h["region"] < 5) & (h["status"] == 1))[0]
+    from computeql_gb300 import eventbench
+    rows, order = res["sort_200k"]
+    want_rows = np.nonzero(h["region"] == eventbench.SORT_REGION)[0]
     np.testing.assert_array_equal(rows, want_rows)
     perm = oracle.sort_rows([h["m4"][want_rows]])
     np.testing.assert_array_equal(order, want_rows[perm.astype(np.int64)])

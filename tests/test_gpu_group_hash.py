@@ -228,7 +228,7 @@ def test_few_groups_many_rows(ops, groups):
     kc, vc, dc = ops.Column.from_numpy(key), ops.Column.from_numpy(v), ops.Column.from_numpy(d)
     fixed = ops.group_hash([kc], [COUNT, SUM, MIN, MAX], [None, vc, vc, vc])
     assert fixed["path"] == 2
-    csr = ops.group_hash([kc], [COUNT, SUM], [None, dc])
+    csr = ops.group_hash([kc], [COUNT, SUM], [None, dc], path=1)
     assert csr["path"] == 1
     for g in range(fixed["groups"]):
         k = key[int(fixed["repr_row"][g])]
@@ -238,3 +238,16 @@ def test_few_groups_many_rows(ops, groups):
         k = key[int(csr["repr_row"][g])]
         exact = math.fsum(d[key == k])
         assert abs(csr["results"][g, 1] - exact) <= 1e-12 * exact
+    # automatic: a key of few values with f64 sums goes through the shared scan (path 3), groups in key
+    # order, each represented by its first row
+    small = ops.group_hash([kc], [COUNT, SUM, AVG], [None, dc, dc])
+    assert small["path"] == 3
+    present = np.unique(key)
+    assert small["groups"] == len(present)
+    for g, k in enumerate(present):
+        m = key == k
+        assert small["repr_row"][g] == np.argmax(m)
+        exact = math.fsum(d[m])
+        assert small["counts"][g] == m.sum() and small["results"][g, 0] == m.sum()
+        assert abs(small["results"][g, 1] - exact) <= 1e-12 * exact
+        assert abs(small["results"][g, 2] - exact / m.sum()) <= 1e-12 * exact / m.sum()
