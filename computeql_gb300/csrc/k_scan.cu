@@ -218,10 +218,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_simple(CqlLaunch a, uint6
   bool skip_on = cql_word(a, 8) != 0;
   uint32_t chunk_start = cql_word(a, 10);
   uint32_t row_offset = cql_word(a, 12);   // added to every row written (a dispatch over one range of the table)
-  // word 14: 1 = the matches as a bitmap of the table's rows (binding 3, one bit a row, each 32-row word
-  // written by the four lanes that own it; the dispatch's first row is a multiple of 32)
+  // word 14: 1 = the matches as a bitmap of the table's rows from row word 2 on (binding 3, one bit a row,
+  // each 32-row word written by the four lanes that own it; the dispatch's first row is a multiple of 32)
   const bool bitmap_mode = !COUNT_ONLY && cql_word(a, 14) != 0;
   const uint64_t bitmap_words = a.bytes[3] / 4;
+  const uint32_t bitmap_first = cql_word(a, 2);   // the table row of the bitmap's first bit (a multiple of 32)
   uint32_t leaf_count = s_leaf_count;
 
   uint64_t groups = (rows + ROWS_PER_THREAD - 1) / ROWS_PER_THREAD;
@@ -288,7 +289,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_simple(CqlLaunch a, uint6
       uint32_t m = live << (8u * (lane & 3u));
       m |= __shfl_xor_sync(0xffffffffu, m, 1);
       m |= __shfl_xor_sync(0xffffffffu, m, 2);
-      uint64_t word = ((uint64_t)row_offset >> 5) + (g >> 2);
+      uint64_t word = ((uint64_t)(row_offset - bitmap_first) >> 5) + (g >> 2);
       if ((lane & 3u) == 0u && word < bitmap_words) out[word] = m;
       private_count += n;
       continue;
@@ -662,34 +663,70 @@ static int launch_scan_filter(const CqlLaunch& a, uint32_t gws, uint32_t lws, cu
 
 // ---------------------------------------------------------------------------------------------
 // A selection bitmap (one bit a row, as the scans write it in bitmap mode) to its rows in ascending
-// order: cql_bitmap_popc counts each word's rows (binding 0 bitmap, 1 counts; word 0 words), the
-// prefix_sum kernel turns the counts into offsets, and cql_bitmap_emit writes each word's rows from its
-// offset (binding 0 bitmap, 1 offsets, 2 rows; word 0 words). No atomics and no sort: the order is the
-// bitmap's.
+// order, in blocks of 256 words (8192 rows): cql_bitmap_popc counts each block's rows (binding 0 bitmap,
+// 1 counts per block; word 0 words), the prefix_sum kernel turns the block counts into offsets, and
+// cql_bitmap_emit ranks each block's words in shared memory and writes their rows from the block's
+// offset (binding 0 bitmap, 1 block offsets, 2 rows; word 0 words, word 2 the row of the first bit). No
+// atomics and no sort: the order is the bitmap's; the scan in between is over words / 256 counts.
+
+__device__ __forceinline__ uint32_t bitmap_block_exclusive(uint32_t v, uint32_t* s_warp, uint32_t* total)
+{
+  uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= (uint32_t)o) incl += y;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  uint32_t before = 0, all = 0;
+  for (uint32_t w = 0; w < SCAN_THREADS / 32; w++)
+  {
+    uint32_t t = s_warp[w];
+    if (w < warp) before += t;
+    all += t;
+  }
+  __syncthreads();
+  *total = all;
+  return before + incl - v;
+}
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_bitmap_popc(CqlLaunch a, uint64_t words)
 {
+  __shared__ uint32_t s_warp[SCAN_THREADS / 32];
   const uint32_t* bits = (const uint32_t*)a.buf[0];
   uint32_t* counts = (uint32_t*)a.buf[1];
-  for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += (uint64_t)gridDim.x * blockDim.x)
-    counts[w] = __popc(bits[w]);
+  uint64_t blocks = (words + SCAN_THREADS - 1) / SCAN_THREADS;
+  for (uint64_t b = blockIdx.x; b < blocks; b += gridDim.x)
+  {
+    uint64_t w = b * SCAN_THREADS + threadIdx.x;
+    uint32_t total;
+    bitmap_block_exclusive(w < words ? __popc(bits[w]) : 0u, s_warp, &total);
+    if (threadIdx.x == 0) counts[b] = total;
+  }
 }
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_bitmap_emit(CqlLaunch a, uint64_t words)
 {
+  __shared__ uint32_t s_warp[SCAN_THREADS / 32];
   const uint32_t* bits = (const uint32_t*)a.buf[0];
   const uint32_t* offsets = (const uint32_t*)a.buf[1];
   uint32_t* rows = (uint32_t*)a.buf[2];
+  uint32_t first = cql_word(a, 2);
   uint64_t cap = a.bytes[2] / 4;
-  for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += (uint64_t)gridDim.x * blockDim.x)
+  uint64_t blocks = (words + SCAN_THREADS - 1) / SCAN_THREADS;
+  for (uint64_t b = blockIdx.x; b < blocks; b += gridDim.x)
   {
-    uint32_t m = bits[w];
-    uint64_t pos = offsets[w];
+    uint64_t w = b * SCAN_THREADS + threadIdx.x;
+    uint32_t m = w < words ? bits[w] : 0u, total;
+    uint64_t pos = (uint64_t)offsets[b] + bitmap_block_exclusive(__popc(m), s_warp, &total);
     while (m)
     {
-      uint32_t b = (uint32_t)(__ffs(m) - 1);
+      uint32_t bit = (uint32_t)(__ffs(m) - 1);
       m &= m - 1u;
-      if (pos < cap) rows[pos] = (uint32_t)(w * 32 + b);
+      if (pos < cap) rows[pos] = first + (uint32_t)(w * 32 + bit);
       pos++;
     }
   }
@@ -701,8 +738,9 @@ static int launch_bitmap_popc(const CqlLaunch& a, uint32_t gws, uint32_t lws, cu
   (void)lws;
   uint64_t words = cql_word(a, 0);
   if (words == 0) return 0;
-  if (a.bytes[0] < words * 4 || a.bytes[1] < words * 4) return (int)cudaErrorInvalidValue;
-  k_bitmap_popc<<<cql_stream_grid((words + SCAN_THREADS - 1) / SCAN_THREADS, 8), SCAN_THREADS, 0, stream>>>(a, words);
+  uint64_t blocks = (words + SCAN_THREADS - 1) / SCAN_THREADS;
+  if (a.bytes[0] < words * 4 || a.bytes[1] < blocks * 4) return (int)cudaErrorInvalidValue;
+  k_bitmap_popc<<<cql_stream_grid(blocks, 8), SCAN_THREADS, 0, stream>>>(a, words);
   CQL_LAUNCH_CHECK();
   return 0;
 }
@@ -713,8 +751,9 @@ static int launch_bitmap_emit(const CqlLaunch& a, uint32_t gws, uint32_t lws, cu
   (void)lws;
   uint64_t words = cql_word(a, 0);
   if (words == 0) return 0;
-  if (a.bytes[0] < words * 4 || a.bytes[1] < words * 4) return (int)cudaErrorInvalidValue;
-  k_bitmap_emit<<<cql_stream_grid((words + SCAN_THREADS - 1) / SCAN_THREADS, 8), SCAN_THREADS, 0, stream>>>(a, words);
+  uint64_t blocks = (words + SCAN_THREADS - 1) / SCAN_THREADS;
+  if (a.bytes[0] < words * 4 || a.bytes[1] < blocks * 4) return (int)cudaErrorInvalidValue;
+  k_bitmap_emit<<<cql_stream_grid(blocks, 8), SCAN_THREADS, 0, stream>>>(a, words);
   CQL_LAUNCH_CHECK();
   return 0;
 }

@@ -284,18 +284,19 @@ static int simple_leaf_words(uint32_t* words, uint32_t slot, const CqlColumn* co
   return 1;
 }
 
-/* The rows of a selection bitmap (one bit a row, as the scans write it in bitmap mode) in ascending
-   order, on the device: each word's population, an exclusive scan of them, then every word's rows written
-   from its offset. The first min(count, cap) rows land in out_rows; count is the bitmap's population. */
-int cqlops_bitmap_rows(CqlBuffer* bitmap, uint64_t rows, uint64_t count, uint32_t* out_rows, uint64_t cap)
+/* The rows of a selection bitmap (one bit a row, as the scans write it in bitmap mode; its first bit is
+   table row first_row, a multiple of 32) in ascending order, on the device: each 256-word block's
+   population, an exclusive scan over the blocks, then every block's rows written from its offset. The
+   first min(count, cap) rows land in out_rows; count is the bitmap's population. */
+int cqlops_bitmap_rows(CqlBuffer* bitmap, uint64_t first_row, uint64_t rows, uint64_t count, uint32_t* out_rows, uint64_t cap)
 {
   if (!count || !cap || !out_rows) return 1;
-  uint64_t words = (rows + 31) / 32, blocks = (words + 255) / 256;
+  uint64_t words = (rows + 31) / 32, blocks = (words + 255) / 256, scan_blocks = (blocks + 255) / 256;
   uint64_t n = count < cap ? count : cap;
-  CqlBuffer* counts = pooled("bitmap_word_counts", words * 4, CQLCUDA_BUFFER_READ_WRITE);
-  CqlBuffer* offsets = pooled("bitmap_word_offsets", (words + 1) * 4, CQLCUDA_BUFFER_READ_WRITE);
-  CqlBuffer* cursor = pooled("bitmap_word_cursor", words * 4, CQLCUDA_BUFFER_READ_WRITE);
-  CqlBuffer* block_sums = pooled("bitmap_block_sums", blocks * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* counts = pooled("bitmap_block_counts", blocks * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* offsets = pooled("bitmap_block_offsets", (blocks + 1) * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* cursor = pooled("bitmap_block_cursor", blocks * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* block_sums = pooled("bitmap_scan_sums", scan_blocks * 4, CQLCUDA_BUFFER_READ_WRITE);
   CqlBuffer* list = pooled("bitmap_rows", count * 4, CQLCUDA_BUFFER_READ_WRITE);
   CqlKernel* popc = kernel_named("cql_bitmap_popc");
   CqlKernel* scan = kernel_named("prefix_sum");
@@ -308,19 +309,24 @@ int cqlops_bitmap_rows(CqlBuffer* bitmap, uint64_t rows, uint64_t count, uint32_
   cqlcuda_kernel_set_arg_buffer(scan, 1, offsets);
   cqlcuda_kernel_set_arg_buffer(scan, 2, cursor);
   cqlcuda_kernel_set_arg_buffer(scan, 3, block_sums);
-  cqlcuda_kernel_set_arg_u64(scan, 0, words);
+  cqlcuda_kernel_set_arg_u64(scan, 0, blocks);
   cqlcuda_kernel_set_arg_buffer(emit, 0, bitmap);
   cqlcuda_kernel_set_arg_buffer(emit, 1, offsets);
   cqlcuda_kernel_set_arg_buffer(emit, 2, list);
   cqlcuda_kernel_set_arg_u64(emit, 0, words);
+  cqlcuda_kernel_set_arg_u64(emit, 1, first_row);
   CqlBatch* b = cqlcuda_batch_begin(0, n * 4);
-  cqlcuda_batch_kernel_execute(b, popc, (uint32_t)words, QE_GPU_WORKGROUP_SIZE);
-  for (uint32_t mode = 0; mode < 3; mode++)
+  if (blocks == 1) cqlcuda_batch_buffer_zero(b, offsets, 4);   /* one block: its rows start at 0 */
+  else
   {
-    cqlcuda_kernel_set_arg_u64(scan, 1, mode);
-    cqlcuda_batch_kernel_execute(b, scan, mode == 1 ? 256u : (uint32_t)(blocks * 256), 256);
+    cqlcuda_batch_kernel_execute(b, popc, (uint32_t)(blocks * 256), QE_GPU_WORKGROUP_SIZE);
+    for (uint32_t mode = 0; mode < 3; mode++)
+    {
+      cqlcuda_kernel_set_arg_u64(scan, 1, mode);
+      cqlcuda_batch_kernel_execute(b, scan, mode == 1 ? 256u : (uint32_t)(scan_blocks * 256), 256);
+    }
   }
-  cqlcuda_batch_kernel_execute(b, emit, (uint32_t)words, QE_GPU_WORKGROUP_SIZE);
+  cqlcuda_batch_kernel_execute(b, emit, (uint32_t)(blocks * 256), QE_GPU_WORKGROUP_SIZE);
   cqlcuda_batch_buffer_read(b, list, out_rows, n * 4);
   return cqlcuda_batch_end(b);
 }
@@ -393,9 +399,11 @@ int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const Cq
   cqlcuda_kernel_set_arg_buffer(k, 5, skip_buf);
   cqlcuda_kernel_set_arg_u64(k, 3, use_skip ? 13 : 0);
   cqlcuda_kernel_set_arg_u64(k, 4, use_skip ? 1 : 0);
-  /* the matches as a bitmap of the table's rows (word 14), turned into ascending rows on the device */
-  uint64_t bitmap_words = (rows + 31) / 32;
-  CqlBuffer* output = want_rows ? pooled("scan_bitmap", bitmap_words * 4, CQLCUDA_BUFFER_READ_WRITE)
+  /* the matches as a bitmap of the rows from the first range's start to the last range's end (word 14;
+     word 2 its first row), turned into ascending rows on the device */
+  uint64_t bitmap_first = range_count ? ranges[0] : 0, bitmap_end = range_count ? ranges[2 * range_count - 1] : 0;
+  uint64_t bitmap_words = (bitmap_end - bitmap_first + 31) / 32;
+  CqlBuffer* output = want_rows ? pooled("scan_bitmap", (bitmap_words ? bitmap_words : 1) * 4, CQLCUDA_BUFFER_READ_WRITE)
                                 : pooled("cqlops_scan_no_output", 0, CQLCUDA_BUFFER_READ);   /* count only */
   if (!output)
   {
@@ -404,14 +412,14 @@ int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const Cq
   }
   cqlcuda_kernel_set_arg_buffer(k, 3, output);
   cqlcuda_kernel_set_arg_u64(k, 7, want_rows ? 1 : 0);
+  cqlcuda_kernel_set_arg_u64(k, 1, bitmap_first);
   uint32_t count32[2] = { 0, 0 };
   CqlBatch* batch = cqlcuda_batch_begin(sizeof(words) + (use_skip ? ((chunks + 31) / 32) * 4 : 0), sizeof(count32));
   cqlcuda_batch_buffer_write(batch, leaf_buf, words, sizeof(words));
   if (use_skip) cqlcuda_batch_buffer_write(batch, skip_buf, skip_bits, ((chunks + 31) / 32) * sizeof(uint32_t));
   cqlcuda_batch_buffer_zero(batch, counter, sizeof(count32));
-  /* ranges a zone map keeps leave the other words unwritten: they must read as no match */
-  int whole = range_count == 1 && ranges[0] == 0 && ranges[1] == rows;
-  if (want_rows && !whole) cqlcuda_batch_buffer_zero(batch, output, bitmap_words * 4);
+  /* ranges a zone map keeps leave the words between them unwritten: they must read as no match */
+  if (want_rows && range_count > 1) cqlcuda_batch_buffer_zero(batch, output, bitmap_words * 4);
   for (uint64_t r = 0; r < range_count; r++)
   {
     /* one dispatch per range: the columns bound from the range's first row, row numbers written
@@ -444,7 +452,7 @@ int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const Cq
   }
   uint64_t result_count = count32[0];
   free(skip_bits);
-  if (want_rows && !cqlops_bitmap_rows(output, rows, result_count, out_rows, out_capacity)) return 0;
+  if (want_rows && !cqlops_bitmap_rows(output, bitmap_first, bitmap_end - bitmap_first, result_count, out_rows, out_capacity)) return 0;
   if (out_count) *out_count = result_count;
   return 1;
 }

@@ -32,7 +32,7 @@ static uint64_t g_failed[FAILED_CAP];
 static uint32_t g_failed_count = 0;
 static uint64_t g_generated_requests = 0, g_generated_failures = 0;
 void cqlops_note_error(const char* why);
-int cqlops_bitmap_rows(CqlBuffer* bitmap, uint64_t rows, uint64_t count, uint32_t* out_rows, uint64_t cap);
+int cqlops_bitmap_rows(CqlBuffer* bitmap, uint64_t first_row, uint64_t rows, uint64_t count, uint32_t* out_rows, uint64_t cap);
 
 void cqlops_generated_stats(uint64_t* out_requests, uint64_t* out_failures)
 {
@@ -286,7 +286,7 @@ static int scan_filter_run(const CqlProgram* prog, const CqlColumn* columns, uin
     cqlcuda_batch_kernel_execute(batch, k, (uint32_t)(rows < 0xffffffffull ? rows : 0xffffffffull), QE_GPU_WORKGROUP_SIZE);
     cqlcuda_batch_buffer_read(batch, counter, c32, 8);
     if (!cqlcuda_batch_end(batch)) return 0;
-    if (!cqlops_bitmap_rows(bits, rows, c32[0], out_rows, out_capacity)) return 0;
+    if (!cqlops_bitmap_rows(bits, 0, rows, c32[0], out_rows, out_capacity)) return 0;
     if (out_count) *out_count = c32[0];
     if (out_strategy) *out_strategy = ran;
     return 1;
