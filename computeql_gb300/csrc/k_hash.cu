@@ -485,7 +485,9 @@ __device__ __forceinline__ void hll_add(uint32_t* sketch, uint64_t sketch_words,
   int msb = rest ? 31 - __clz(rest) : -1;
   uint32_t rho = msb < 0 ? rest_bits + 1u : rest_bits - (uint32_t)msb;
   uint64_t idx = ((uint64_t)g * nhll + slot) * (1ull << p) + bucket;
-  if (idx < sketch_words) atomicMax(&sketch[idx], rho);
+  // registers only grow: a value read at least as large (even a stale one) makes the atomic redundant,
+  // and after the first rows almost every value is below its register
+  if (idx < sketch_words && __ldcg(&sketch[idx]) < rho) atomicMax(&sketch[idx], rho);
 }
 
 struct ReduceArgs
