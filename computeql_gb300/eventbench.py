@@ -18,6 +18,14 @@ RX 6700 XT (README.md:38-48), where it publishes one.
   group_by_user_id           SELECT user_id, COUNT(*), SUM(u0) GROUP BY user_id (1M groups)
   distinct_sessions          SELECT COUNT(*) FROM (SELECT session GROUP BY session) (4M values)
   sort_200k                  SELECT rows WHERE region = 3 ORDER BY m4 (200k rows, ties by row)
+
+and four more of that benchmark's forms, for which the reference publishes no time:
+
+  wide_projection_1pct       SELECT * WHERE u1 > 1038090 (1 %): the rows, then all 28 stored columns' values
+  window_top3_per_region     SELECT COUNT(*) FROM (SELECT ROW_NUMBER() OVER (PARTITION BY region ORDER BY u2 DESC)
+                             AS rn WHERE u0 > 943718) WHERE rn <= 3 (1M rows ranked)
+  having_1m_groups           SELECT user_id, SUM(u0) GROUP BY user_id HAVING SUM(u0) > 8000000
+  eight_measures_by_region   SELECT region, SUM(m0), ..., SUM(m7) GROUP BY region
 """
 from __future__ import annotations
 
@@ -32,11 +40,14 @@ from . import build, native, ops, workloads
 
 REFERENCE_MS = {"group_by_dict_string": 0.43, "group_by_status_f64": 0.79, "dict_string_eq_filter": 0.31,
                 "group_by_region_5_aggs": 1.0, "three_predicate_filter": 1.1, "join_users_by_segment": 10.5,
-                "group_by_user_id": 56.0, "distinct_sessions": None, "sort_200k": 9.5}
+                "group_by_user_id": 56.0, "distinct_sessions": None, "sort_200k": 9.5, "wide_projection_1pct": None,
+                "window_top3_per_region": None, "having_1m_groups": None, "eight_measures_by_region": None}
 
 EQ_WORD, TRIPLE_WORD = 3, 0          # the dictionary values the string filters compare with
 TRIPLE_REGION, U4_LO, U4_HI = 7, 100_000, 900_000
 SORT_REGION = 3
+WIDE_U1_GT, WINDOW_U0_GT, HAVING_SUM_GT = 1_038_090, 943_718, 8_000_000
+STORED = workloads.EVENT_U32 + workloads.EVENT_I64 + workloads.EVENT_F64 + ["user_id", "region", "status"] + workloads.EVENT_DICT + ["session"]
 
 
 def programs(cols, words):
@@ -52,6 +63,23 @@ def queries(cols, users, words):
     progs = programs(cols, words)
     program_eq, program_triple = progs["eq"], progs["triple"]
     F = ops
+
+    stored = [cols[c] for c in STORED]
+
+    def wide_projection():
+        _, rows = ops.scan_simple([cols["u1"]], [(0, ops.CMP_GT, WIDE_U1_GT)], want_rows=True)
+        return rows, ops.gather_rows(stored, rows=rows)
+
+    def window_top3():
+        _, rows = ops.scan_simple([cols["u0"]], [(0, ops.CMP_GT, WINDOW_U0_GT)], want_rows=True)
+        sel = ops.DeviceBuffer(max(rows.nbytes, 4), rows)
+        w = ops.window_rank([cols["region"], cols["u2"]], desc=[0, 1], partitions=1, selection=sel, count=len(rows))
+        return int((w["row_number"] <= 3).sum())
+
+    def having_1m():
+        r = ops.group_hash([cols["user_id"]], [F.FUNC_SUM], [cols["u0"]], group_hint=1_000_000)
+        keep = ops.having("v0 > lit[0]", [r["results"][:, 0]], [HAVING_SUM_GT])
+        return r, keep
 
     def sort_200k():
         _, rows = ops.scan_simple([cols["region"]], [(0, ops.CMP_EQ, SORT_REGION)], want_rows=True)
@@ -72,6 +100,11 @@ def queries(cols, users, words):
                                                     group_hint=1_000_000)),
         ("distinct_sessions", lambda: ops.group_hash([cols["session"]], [F.FUNC_COUNT], [None], group_hint=4_000_000)),
         ("sort_200k", sort_200k),
+        ("wide_projection_1pct", wide_projection),
+        ("window_top3_per_region", window_top3),
+        ("having_1m_groups", having_1m),
+        ("eight_measures_by_region", lambda: ops.group_hash([cols["region"]], [F.FUNC_SUM] * 8, [cols[m] for m in workloads.EVENT_F64],
+                                                            group_hint=50)),
     ]
 
 

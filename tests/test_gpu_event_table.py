@@ -127,3 +127,41 @@ def test_sort_200k(suite):
     np.testing.assert_array_equal(rows, want_rows)
     perm = oracle.sort_rows([h["m4"][want_rows]])
     np.testing.assert_array_equal(order, want_rows[perm.astype(np.int64)])
+
+
+def test_wide_projection(suite):
+    _, _, h, _, res, _ = suite
+    from computeql_gb300 import eventbench
+    rows, values = res["wide_projection_1pct"]
+    want = np.nonzero(h["u1"] > eventbench.WIDE_U1_GT)[0]
+    np.testing.assert_array_equal(rows, want)
+    for name, got in zip(eventbench.STORED, values):
+        np.testing.assert_array_equal(got, oracle.gather_column(h[name], want), err_msg=name)
+
+
+def test_window_top3_per_region(suite):
+    _, _, h, _, res, _ = suite
+    from computeql_gb300 import eventbench
+    sel = np.nonzero(h["u0"] > eventbench.WINDOW_U0_GT)[0]
+    _, rn, _, _ = oracle.window_rank([h["region"][sel], h["u2"][sel]], desc=[0, 1], partitions=1)
+    assert res["window_top3_per_region"] == int((rn <= 3).sum()) == 3 * len(np.unique(h["region"][sel]))
+
+
+def test_having_over_1m_groups(suite):
+    _, _, h, _, res, _ = suite
+    from computeql_gb300 import eventbench
+    r, keep = res["having_1m_groups"]
+    keys = h["user_id"][r["repr_row"].astype(np.int64)]
+    sums = np.bincount(h["user_id"], weights=h["u0"].astype(np.float64), minlength=1_000_000)
+    np.testing.assert_array_equal(keep, (sums[keys] > eventbench.HAVING_SUM_GT).astype(np.uint32))
+
+
+def test_eight_measures_by_region(suite):
+    _, _, h, _, res, _ = suite
+    from computeql_gb300 import workloads
+    r = res["eight_measures_by_region"]
+    assert r["groups"] == 50 and r["path"] == 3
+    for g in range(50):
+        sel = h["region"] == g
+        for e, m in enumerate(workloads.EVENT_F64):
+            assert _close(r["results"][g, e], oracle.compensated_sum(h[m][sel]))
