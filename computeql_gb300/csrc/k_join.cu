@@ -507,7 +507,10 @@ __global__ void __launch_bounds__(JOIN_THREADS) k_join_lut_first(CqlLaunch a, ui
   {
     if (!((present[k >> 5] >> (k & 31)) & 1u)) continue;
     uint32_t gid = table[k];
-    if (gid < groups) atomicMin(&first[gid], visit_of[k]);
+    // a group's first visit only falls: the atomic only when a plain read shows it larger (many keys
+    // share few groups, and their atomics would serialise on them)
+    uint32_t v = visit_of[k];
+    if (gid < groups && v < __ldcg(&first[gid])) atomicMin(&first[gid], v);
   }
 }
 
