@@ -90,11 +90,52 @@ struct CqlStaging
   std::vector<CqlPendingRead> reads;
 };
 
+// A batch opened for a plan shape (cqlcuda_batch_begin_graph) records its operations instead of issuing
+// them; at its end the record's fingerprint (every operation, buffer address, size and kernel argument,
+// not the bytes written) finds the CUDA graph captured for that shape, which is replayed with the new
+// bytes, or the record is captured into a new graph.
+enum
+{
+  CQL_OP_WRITE,
+  CQL_OP_ZERO,
+  CQL_OP_FILL,
+  CQL_OP_KERNEL,
+  CQL_OP_READ,
+};
+
+struct CqlOp
+{
+  int kind;
+  CqlBuffer* buffer;
+  uint64_t offset, size;
+  uint32_t value;
+  uint64_t at;        // WRITE: the bytes' place in the record; READ: the result's place in the out area
+  void* out;          // READ: the caller's destination
+  CqlKernel* kernel;  // KERNEL: with its arguments as they were when it was recorded
+  CqlLaunch launch;
+  uint32_t gws, lws;
+};
+
+struct CqlGraphEntry
+{
+  cudaGraphExec_t exec;
+  unsigned char* in;    // pinned: the bytes the graph uploads
+  unsigned char* out;   // pinned: the results it downloads
+  uint64_t in_size, out_size;
+  uint32_t kernels;
+  uint64_t last_use;
+};
+
 struct CqlBatch
 {
   int active;
   int failed;
   CqlStaging staging;
+  int recording;
+  uint64_t plan_key;
+  std::vector<CqlOp> ops;
+  std::vector<unsigned char> in_bytes;
+  uint64_t out_bytes;
 };
 
 struct CqlStreamSlot
@@ -134,7 +175,12 @@ struct CqlLane
   std::unordered_map<const CqlKernel*, CqlLaunch> args;
   uint32_t launches;     // kernels this lane launched
   int is_main;
+  std::unordered_map<uint64_t, CqlGraphEntry> graphs;   // plan graphs by fingerprint, this lane's alone
+  uint64_t graph_clock;
 };
+
+static std::atomic<uint64_t> g_graph_captures{0}, g_graph_replays{0}, g_graph_fallbacks{0};
+static std::atomic<int> g_graphs_on{1};
 
 struct CqlState
 {
@@ -1032,7 +1078,14 @@ extern "C" void cqlcuda_kernel_set_arg_u64(CqlKernel* k, uint32_t index, uint64_
 }
 
 // Enqueues one dispatch on `stream`, bracketed by events when the profile is on.
+static int dispatch_args(CqlKernel* k, const CqlLaunch& args, uint32_t gws, uint32_t lws, cudaStream_t stream, std::vector<CqlTiming>* timings);
+
 static int dispatch(CqlKernel* k, uint32_t gws, uint32_t lws, cudaStream_t stream, std::vector<CqlTiming>* timings)
+{
+  return dispatch_args(k, L().args[k], gws, lws, stream, timings);
+}
+
+static int dispatch_args(CqlKernel* k, const CqlLaunch& args, uint32_t gws, uint32_t lws, cudaStream_t stream, std::vector<CqlTiming>* timings)
 {
   CqlState& s = S();
   if (s.device_lost)
@@ -1052,14 +1105,14 @@ static int dispatch(CqlKernel* k, uint32_t gws, uint32_t lws, cudaStream_t strea
   int rc = 0;
   if (k->builtin)
   {
-    rc = k->builtin(L().args[k], gws, lws, stream);
+    rc = k->builtin(args, gws, lws, stream);
   }
   else if (k->generated)
   {
     uint32_t block = k->gen_block;
     uint64_t want = lws ? ((uint64_t)gws + lws - 1) / lws : 1;
     uint32_t grid = cql_stream_grid(want ? want : 1, (int)k->gen_per_sm);
-    CqlLaunch a = L().args[k];
+    CqlLaunch a = args;
     void* params[] = { &a };
     cudaError_t e = cudaLaunchKernel((const void*)k->generated, dim3(grid), dim3(block), params, k->gen_smem, stream);
     rc = (int)e;
@@ -1188,8 +1241,34 @@ extern "C" CqlBatch* cqlcuda_batch_begin(uint64_t upload_bytes_needed, uint64_t 
   CqlBatch* b = &l.batch;
   b->active = 1;
   b->failed = 0;
+  b->recording = 0;
+  b->ops.clear();
+  b->in_bytes.clear();
+  b->out_bytes = 0;
   staging_prepare(b->staging, download_bytes_needed);
   return b;
+}
+
+extern "C" CqlBatch* cqlcuda_batch_begin_graph(uint64_t upload_bytes_needed, uint64_t download_bytes_needed, uint64_t plan_key)
+{
+  CqlBatch* b = cqlcuda_batch_begin(upload_bytes_needed, download_bytes_needed);
+  if (b)
+  {
+    b->recording = 1;
+    b->plan_key = plan_key;
+  }
+  return b;
+}
+
+static CqlOp op_of(int kind, CqlBuffer* buffer, uint64_t offset, uint64_t size)
+{
+  CqlOp o;
+  memset(&o, 0, sizeof(o));
+  o.kind = kind;
+  o.buffer = buffer;
+  o.offset = offset;
+  o.size = size;
+  return o;
 }
 
 extern "C" void cqlcuda_batch_buffer_write(CqlBatch* batch, CqlBuffer* buffer, const void* data, uint64_t size)
@@ -1201,12 +1280,26 @@ extern "C" void cqlcuda_batch_buffer_write(CqlBatch* batch, CqlBuffer* buffer, c
     batch->failed = 1;
     return;
   }
+  if (batch->recording)
+  {
+    CqlOp o = op_of(CQL_OP_WRITE, buffer, 0, size);
+    o.at = (batch->in_bytes.size() + 15) & ~15ull;
+    batch->in_bytes.resize(o.at + size);
+    memcpy(batch->in_bytes.data() + o.at, data, size);
+    batch->ops.push_back(o);
+    return;
+  }
   if (!note_cuda(cudaMemcpyAsync(buffer->dptr, data, size, cudaMemcpyHostToDevice, L().stream), "batch write")) batch->failed = 1;
 }
 
 extern "C" void cqlcuda_batch_buffer_zero(CqlBatch* batch, CqlBuffer* buffer, uint64_t size)
 {
   if (!batch || !buffer) return;
+  if (batch->recording)
+  {
+    batch->ops.push_back(op_of(CQL_OP_ZERO, buffer, 0, std::min(size, buffer->size)));
+    return;
+  }
   if (!note_cuda(cudaMemsetAsync(buffer->dptr, 0, std::min(size, buffer->size), L().stream), "batch zero")) batch->failed = 1;
 }
 
@@ -1237,12 +1330,26 @@ static int fill_words(CqlBuffer* buffer, uint64_t offset, uint64_t size, uint32_
 extern "C" void cqlcuda_batch_buffer_fill(CqlBatch* batch, CqlBuffer* buffer, uint64_t size, uint32_t value)
 {
   if (!batch || !buffer) return;
+  if (batch->recording)
+  {
+    CqlOp o = op_of(CQL_OP_FILL, buffer, 0, size);
+    o.value = value;
+    batch->ops.push_back(o);
+    return;
+  }
   if (!fill_words(buffer, 0, size, value, L().stream)) batch->failed = 1;
 }
 
 extern "C" void cqlcuda_batch_fill_range(CqlBatch* batch, CqlBuffer* buffer, uint64_t offset, uint64_t size, uint32_t value)
 {
   if (!batch || !buffer) return;
+  if (batch->recording)
+  {
+    CqlOp o = op_of(CQL_OP_FILL, buffer, offset, size);
+    o.value = value;
+    batch->ops.push_back(o);
+    return;
+  }
   if (!fill_words(buffer, offset, size, value, L().stream))
   {
     set_error("cqlcuda_batch_fill_range: offset %llu of a %llu byte buffer", (unsigned long long)offset, (unsigned long long)buffer->size);
@@ -1253,6 +1360,16 @@ extern "C" void cqlcuda_batch_fill_range(CqlBatch* batch, CqlBuffer* buffer, uin
 extern "C" void cqlcuda_batch_kernel_execute(CqlBatch* batch, CqlKernel* kernel, uint32_t gws, uint32_t lws)
 {
   if (!batch || !kernel) return;
+  if (batch->recording)
+  {
+    CqlOp o = op_of(CQL_OP_KERNEL, nullptr, 0, 0);
+    o.kernel = kernel;
+    o.launch = L().args[kernel];
+    o.gws = gws;
+    o.lws = lws;
+    batch->ops.push_back(o);
+    return;
+  }
   if (!dispatch(kernel, gws, lws, L().stream, &L().timings)) batch->failed = 1;
 }
 
@@ -1264,7 +1381,7 @@ extern "C" void cqlcuda_batch_buffer_read(CqlBatch* batch, CqlBuffer* buffer, vo
     if (out_data) memset(out_data, 0, size);
     return;
   }
-  if (!enqueue_read(batch->staging, buffer, 0, out_data, size, L().stream)) batch->failed = 1;
+  cqlcuda_batch_buffer_read_at(batch, buffer, 0, out_data, size);
 }
 
 extern "C" void cqlcuda_batch_buffer_read_at(CqlBatch* batch, CqlBuffer* buffer, uint64_t offset, void* out_data, uint64_t size)
@@ -1275,7 +1392,195 @@ extern "C" void cqlcuda_batch_buffer_read_at(CqlBatch* batch, CqlBuffer* buffer,
     if (out_data) memset(out_data, 0, size);
     return;
   }
+  if (batch->recording)
+  {
+    if (!out_data || offset > buffer->size || size > buffer->size - offset)
+    {
+      set_error("cqlcuda: read of %llu bytes at %llu from a %llu byte buffer", (unsigned long long)size, (unsigned long long)offset,
+                (unsigned long long)buffer->size);
+      batch->failed = 1;
+      return;
+    }
+    CqlOp o = op_of(CQL_OP_READ, buffer, offset, size);
+    o.out = out_data;
+    o.at = (batch->out_bytes + 15) & ~15ull;
+    batch->out_bytes = o.at + size;
+    batch->ops.push_back(o);
+    return;
+  }
   if (!enqueue_read(batch->staging, buffer, offset, out_data, size, L().stream)) batch->failed = 1;
+}
+
+// ---------------------------------------------------------------------------------------------
+// plan graphs
+
+#define CQL_GRAPHS_PER_LANE 32
+
+static uint64_t fnv_bytes(uint64_t h, const void* p, size_t n)
+{
+  const unsigned char* c = (const unsigned char*)p;
+  for (size_t i = 0; i < n; i++) h = (h ^ c[i]) * 1099511628211ull;
+  return h;
+}
+
+// what a replay must match: every operation with its buffer addresses, sizes, fill values and kernel
+// arguments, and where its bytes sit in the record (the bytes themselves are the replay's new input)
+static uint64_t record_fingerprint(const CqlBatch* b)
+{
+  uint64_t h = fnv_bytes(1469598103934665603ull, &b->plan_key, 8);
+  h = fnv_bytes(h, &b->out_bytes, 8);
+  uint64_t in = b->in_bytes.size();
+  h = fnv_bytes(h, &in, 8);
+  for (const CqlOp& o : b->ops)
+  {
+    h = fnv_bytes(h, &o.kind, sizeof(o.kind));
+    void* dptr = o.buffer ? o.buffer->dptr : nullptr;
+    h = fnv_bytes(h, &dptr, sizeof(dptr));
+    h = fnv_bytes(h, &o.offset, 8);
+    h = fnv_bytes(h, &o.size, 8);
+    h = fnv_bytes(h, &o.value, 4);
+    h = fnv_bytes(h, &o.at, 8);
+    if (o.kind == CQL_OP_KERNEL)
+    {
+      h = fnv_bytes(h, &o.kernel, sizeof(o.kernel));
+      h = fnv_bytes(h, &o.launch, sizeof(o.launch));
+      h = fnv_bytes(h, &o.gws, 4);
+      h = fnv_bytes(h, &o.lws, 4);
+    }
+  }
+  return h;
+}
+
+// the record's operations on the stream; `in`/`out` are the graph's pinned areas, or null for an eager
+// run (bytes from the record, results through the batch's staging)
+static int issue_ops(CqlBatch* b, cudaStream_t stream, const unsigned char* in, unsigned char* out, uint32_t* kernels)
+{
+  for (const CqlOp& o : b->ops)
+  {
+    int ok = 1;
+    switch (o.kind)
+    {
+      case CQL_OP_WRITE:
+        ok = note_cuda(cudaMemcpyAsync(o.buffer->dptr, (in ? in : b->in_bytes.data()) + o.at, o.size, cudaMemcpyHostToDevice, stream), "graph write");
+        break;
+      case CQL_OP_ZERO: ok = note_cuda(cudaMemsetAsync(o.buffer->dptr, 0, o.size, stream), "graph zero"); break;
+      case CQL_OP_FILL: ok = fill_words(o.buffer, o.offset, o.size, o.value, stream); break;
+      case CQL_OP_KERNEL:
+        ok = dispatch_args(o.kernel, o.launch, o.gws, o.lws, stream, out ? nullptr : &L().timings);
+        if (kernels) *kernels += 1;
+        break;
+      default:
+        if (out) ok = note_cuda(cudaMemcpyAsync(out + o.at, (const char*)o.buffer->dptr + o.offset, o.size, cudaMemcpyDeviceToHost, stream), "graph read");
+        else ok = enqueue_read(b->staging, o.buffer, o.offset, o.out, o.size, stream);
+        break;
+    }
+    if (!ok) return 0;
+  }
+  return 1;
+}
+
+static void graph_entry_free(CqlGraphEntry& e)
+{
+  if (e.exec) cudaGraphExecDestroy(e.exec);
+  if (e.in) cudaFreeHost(e.in);
+  if (e.out) cudaFreeHost(e.out);
+  e.exec = nullptr;
+  e.in = e.out = nullptr;
+}
+
+static void graph_copy_out(CqlBatch* b, const CqlGraphEntry& e)
+{
+  for (const CqlOp& o : b->ops)
+    if (o.kind == CQL_OP_READ) memcpy(o.out, e.out + o.at, o.size);
+}
+
+// Replays the graph of the record's shape, or captures one; falls back to issuing the record eagerly
+// when a capture does not take. The results reach the callers' arrays before it returns.
+static void graph_end(CqlBatch* b, CqlLane& l)
+{
+  if (S().profile_enabled || !g_graphs_on.load())
+  {
+    // a profiled batch times every kernel with events of its own: it runs eagerly
+    if (!issue_ops(b, l.stream, nullptr, nullptr, nullptr)) b->failed = 1;
+    b->recording = 0;
+    return;
+  }
+  uint64_t fp = record_fingerprint(b);
+  auto it = l.graphs.find(fp);
+  if (it != l.graphs.end())
+  {
+    CqlGraphEntry& e = it->second;
+    if (!b->in_bytes.empty()) memcpy(e.in, b->in_bytes.data(), b->in_bytes.size());
+    if (!note_cuda(cudaGraphLaunch(e.exec, l.stream), "cudaGraphLaunch") || !wait_stream(l.stream, "graph replay"))
+    {
+      b->failed = 1;
+      return;
+    }
+    for (uint32_t i = 0; i < e.kernels; i++) cql_note_launch();
+    e.last_use = ++l.graph_clock;
+    g_graph_replays.fetch_add(1, std::memory_order_relaxed);
+    graph_copy_out(b, e);
+    return;
+  }
+  CqlGraphEntry e;
+  memset(&e, 0, sizeof(e));
+  e.in_size = b->in_bytes.size();
+  e.out_size = b->out_bytes;
+  bool pinned = cudaHostAlloc((void**)&e.in, std::max<uint64_t>(e.in_size, 16), cudaHostAllocDefault) == cudaSuccess &&
+                cudaHostAlloc((void**)&e.out, std::max<uint64_t>(e.out_size, 16), cudaHostAllocDefault) == cudaSuccess;
+  cudaGraph_t graph = nullptr;
+  bool captured = false;
+  if (pinned)
+  {
+    if (e.in_size) memcpy(e.in, b->in_bytes.data(), e.in_size);
+    if (cudaStreamBeginCapture(l.stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess)
+    {
+      bool issued = issue_ops(b, l.stream, e.in, e.out, &e.kernels) != 0;
+      cudaError_t end = cudaStreamEndCapture(l.stream, &graph);
+      captured = issued && end == cudaSuccess && graph &&
+                 cudaGraphInstantiate(&e.exec, graph, 0) == cudaSuccess;
+      if (graph) cudaGraphDestroy(graph);
+    }
+  }
+  cudaGetLastError();
+  if (!captured)
+  {
+    // the record runs as an ordinary batch
+    graph_entry_free(e);
+    g_graph_fallbacks.fetch_add(1, std::memory_order_relaxed);
+    set_error("");
+    if (!issue_ops(b, l.stream, nullptr, nullptr, nullptr)) b->failed = 1;
+    // eager reads wait in the batch's staging: hand the record's reads over to it
+    b->recording = 0;
+    return;
+  }
+  if (!note_cuda(cudaGraphLaunch(e.exec, l.stream), "cudaGraphLaunch") || !wait_stream(l.stream, "graph launch"))
+  {
+    graph_entry_free(e);
+    b->failed = 1;
+    return;
+  }
+  g_graph_captures.fetch_add(1, std::memory_order_relaxed);
+  graph_copy_out(b, e);
+  if (l.graphs.size() >= CQL_GRAPHS_PER_LANE)
+  {
+    auto oldest = l.graphs.begin();
+    for (auto j = l.graphs.begin(); j != l.graphs.end(); ++j)
+      if (j->second.last_use < oldest->second.last_use) oldest = j;
+    graph_entry_free(oldest->second);
+    l.graphs.erase(oldest);
+  }
+  e.last_use = ++l.graph_clock;
+  l.graphs[fp] = e;
+}
+
+extern "C" void cqlcuda_graph_enable(int on) { g_graphs_on.store(on ? 1 : 0); }
+
+extern "C" void cqlcuda_graph_stats(uint64_t* out_captures, uint64_t* out_replays, uint64_t* out_fallbacks)
+{
+  if (out_captures) *out_captures = g_graph_captures.load();
+  if (out_replays) *out_replays = g_graph_replays.load();
+  if (out_fallbacks) *out_fallbacks = g_graph_fallbacks.load();
 }
 
 extern "C" int cqlcuda_batch_end(CqlBatch* batch)
@@ -1286,7 +1591,15 @@ extern "C" int cqlcuda_batch_end(CqlBatch* batch)
     return 0;
   }
   CqlLane& l = L();
+  if (batch->recording && !batch->failed) graph_end(batch, l);
   int ok = !batch->failed && wait_stream(l.stream, "batch_end");
+  if (batch->recording)
+  {
+    // the results of a recorded batch were copied from its graph's out area (or its staging, eagerly)
+    for (const CqlOp& o : batch->ops)
+      if (o.kind == CQL_OP_READ && !ok) memset(o.out, 0, o.size);
+    batch->recording = 0;
+  }
   staging_finish(batch->staging, ok);
   if (ok) timings_collect(l.timings);
   else
@@ -1625,6 +1938,8 @@ extern "C" void cqlcuda_thread_lane_end(void)
   CqlLane* l = tl_lane;
   if (!l) return;
   wait_stream(l->stream, "lane end");
+  for (auto& g : l->graphs) graph_entry_free(g.second);
+  l->graphs.clear();
   staging_release(l->batch.staging);
   cudaStreamDestroy(l->stream);
   tl_lane = nullptr;

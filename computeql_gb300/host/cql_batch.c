@@ -1805,10 +1805,12 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     kernels[sl] = k;
   }
 #undef SLICE_SHAPES
-  /* one batch: the upload, the cube pass and answers, every slice's scan and fold, the read-backs; one wait */
+  /* one batch: the upload, the cube pass and answers, every slice's scan and fold, the read-backs; one wait.
+     It runs as the CUDA graph of its plan shape: a batch of the same shapes, query count and buffers
+     replays the graph captured for it, with this batch's thresholds as the uploaded bytes. */
   if (launch && ok)
   {
-    CqlBatch* b = cqlcuda_batch_begin(param_bytes, (uint64_t)scan_n * 24 + (cube_n ? cube_out_bytes : 0));
+    CqlBatch* b = cqlcuda_batch_begin_graph(param_bytes, (uint64_t)scan_n * 24 + (cube_n ? cube_out_bytes : 0), 0x62617463685f7363ull);
     cqlcuda_batch_buffer_write(b, param_buf, params, param_bytes);
     if (cube_n)
     {

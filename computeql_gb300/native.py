@@ -127,6 +127,9 @@ CUDA_API = [
     ("cqlcuda_kernel_set_arg_u64", None, [P, u32, u64]),
     ("cqlcuda_kernel_set_arg_buffer_range", None, [P, u32, P, u64, u64]),
     ("cqlcuda_batch_begin", P, [u64, u64]),
+    ("cqlcuda_batch_begin_graph", P, [u64, u64, u64]),
+    ("cqlcuda_graph_stats", None, [P, P, P]),
+    ("cqlcuda_graph_enable", None, [C.c_int]),
     ("cqlcuda_batch_buffer_write", None, [P, P, P, u64]),
     ("cqlcuda_batch_buffer_zero", None, [P, P, u64]),
     ("cqlcuda_batch_buffer_fill", None, [P, P, u64, u32]),

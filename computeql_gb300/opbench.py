@@ -205,11 +205,44 @@ def run_batch(rows, reps):
         if best is None or wall < best[1]:
             best = (rpt, wall, kernel_ms, kernels)
     one_wall, one_kernel, _ = _time(lambda: [ops.fused_aggregate(p, [s]) for p, s in zip(progs, sums)], max(1, reps // 2))
+    graphs = _graph_ab(reps)
     nbytes = rows * (4 * 4 + 4 * 8)
     return {"op": "batch", "rows": rows, "queries": len(qs), "shapes": 29, "reps": reps, "rows_per_thread": best[0], "tuning_wall_ms": tuning,
             "wall_ms": best[1], "kernel_ms": best[2], "rows_per_s": len(qs) * rows / (best[1] / 1e3),
             "kernel_GBps": nbytes / (best[2] / 1e3) / 1e9, "bytes": nbytes, "kernels": best[3],
-            "one_at_a_time_wall_ms": one_wall, "one_at_a_time_kernel_ms": one_kernel, "speedup_wall": one_wall / best[1]}
+            "one_at_a_time_wall_ms": one_wall, "one_at_a_time_kernel_ms": one_kernel, "speedup_wall": one_wall / best[1],
+            "plan_graphs": graphs}
+
+
+def _graph_ab(reps):
+    """Plan graphs on and off: batches of 8 queries of the batched workload's shapes over a 1M-row table
+    (where the launches, not the scan, are most of a batch), wall time without profiling."""
+    lib = native.load_cuda()
+    rng = np.random.default_rng(5)
+    n = 1_000_000
+    cols = {f"u{i}": ops.Column.splitmix(n, 5, 8, i, 1 << 16) for i in range(4)}
+    cols.update({f"d{i}": ops.Column.from_numpy(rng.random(n)) for i in range(4)})
+    qs = _batch_queries(8, 4, 13)
+    progs = [ops.Program(w, cols) for w, _ in qs]
+    sums = [s for _, s in qs]
+
+    def wall(count):
+        fn = lambda: ops.batch_aggregate(progs, sums, 8)
+        fn()
+        fn()
+        walls = []
+        for _ in range(count):
+            t0 = time.perf_counter()
+            fn()
+            walls.append((time.perf_counter() - t0) * 1e3)
+        return statistics.median(walls)
+
+    count = max(20, reps * 10)
+    on = wall(count)
+    lib.cqlcuda_graph_enable(0)
+    off = wall(count)
+    lib.cqlcuda_graph_enable(1)
+    return {"rows": n, "queries": len(qs), "graph_wall_ms": round(on, 4), "eager_wall_ms": round(off, 4)}
 
 
 def main(argv=None):

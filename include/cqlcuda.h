@@ -134,6 +134,17 @@ void      cqlcuda_batch_buffer_read_at(CqlBatch* batch, CqlBuffer* buffer, uint6
    several output arrays of one operator kept in one buffer). */
 void      cqlcuda_batch_fill_range(CqlBatch* batch, CqlBuffer* buffer, uint64_t offset, uint64_t size, uint32_t value);
 int       cqlcuda_batch_end(CqlBatch* batch);                                                            /* :217, 0 on failure (reads zero-filled) */
+/* A batch for a plan shape (no reference counterpart): its writes, fills, dispatches and reads are
+   recorded, and at cqlcuda_batch_end the record runs as a CUDA graph - the one captured the first time a
+   batch of the same shape ended (the same operations on the same buffers with the same kernel arguments;
+   only the bytes written may differ), replayed with the new bytes in one launch. A lane keeps up to 32
+   graphs. A record that cannot be captured, and any record while kernel profiling is on (its kernels are
+   timed one by one), runs as an ordinary batch. plan_key tells shapes apart. */
+CqlBatch* cqlcuda_batch_begin_graph(uint64_t upload_bytes_needed, uint64_t download_bytes_needed, uint64_t plan_key);
+/* On (the default) or off: with graphs off, plan-shape batches run as ordinary batches. */
+void      cqlcuda_graph_enable(int on);
+/* Graphs captured, replayed, and records that ran without one, since start. */
+void      cqlcuda_graph_stats(uint64_t* out_captures, uint64_t* out_replays, uint64_t* out_fallbacks);
 
 /* ---- streams (gpu_backend.h:219-229) ---- */
 CqlStream* cqlcuda_stream_alloc(uint32_t slot_count);                                                    /* :219, 1..8 slots */

@@ -115,3 +115,29 @@ def test_tile_and_register_forms_agree(ops):
     for i, (w, scol) in enumerate(qs):
         if scol:
             assert abs(s0[i] - s8[i]) <= 1e-12 * max(abs(s8[i]), 1e-300), w
+
+
+def test_plan_graph_replays_a_repeated_shape(ops):
+    """Batches of the same shapes and query count run as one CUDA graph: the first captures it, the next
+    replay it with their own literals (the uploaded thresholds); every batch's results equal the oracle's."""
+    import ctypes as C
+    from computeql_gb300 import native
+    from tests.batch_workload import shapes
+    arrays = table(1_000_003, 5)
+    cols = _columns(ops, arrays)
+    gens = shapes(6, 21)
+    lib = native.load_cuda()
+
+    def stats():
+        c, r, f = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        lib.cqlcuda_graph_stats(C.byref(c), C.byref(r), C.byref(f))
+        return c.value, r.value, f.value
+
+    before = stats()
+    for seed in (100, 101, 102):
+        rng = np.random.default_rng(seed)
+        qs = [(gens[q % 6](rng), F64[q % 4]) for q in range(24)]
+        _check(ops, arrays, cols, qs)
+    after = stats()
+    assert after[1] - before[1] >= 1      # a later batch replayed the graph of the first
+    assert after[2] == before[2]          # and no record fell back to an eager run
