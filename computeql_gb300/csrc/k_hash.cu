@@ -39,7 +39,8 @@ __device__ __forceinline__ uint32_t hash_u32(uint32_t x)
 // ---------------------------------------------------------------------------------------------
 // aggregate_assign: binding 0 owner row per slot, 1 rows per slot, 2 slot per row, 3 overflow count,
 // 4 + 2c / 5 + 2c key column c (f64 values, or string bytes + u64 offsets);
-// words 0 rows, 2 buckets, 4 K, 6 key columns, 8 string mask, 10 1 = count atomics per lane (many groups)
+// words 0 rows, 2 buckets, 4 K, 6 key columns, 8 string mask, 10 1 = count atomics per lane (many groups),
+// 12 1 = linear probing over the whole table (slots a power of two)
 
 struct KeyCols
 {
@@ -110,6 +111,9 @@ __global__ void __launch_bounds__(HASH_THREADS) k_aggregate_assign(CqlLaunch a, 
   uint32_t* overflow = (uint32_t*)a.buf[3];
   uint32_t buckets = cql_word(a, 2), K = cql_word(a, 4), ncols = cql_word(a, 6), string_mask = cql_word(a, 8);
   bool alone = cql_word(a, 10) != 0;
+  // word 12: 1 = linear probing over the whole table (a power of two of slots): K probes from slot
+  // hash mod slots, wrapping, instead of the K slots of the hash's bucket
+  bool linear = cql_word(a, 12) != 0;
   if (ncols > 4) ncols = 4;
   KeyCols k;
   for (int c = 0; c < 4; c++)
@@ -124,11 +128,11 @@ __global__ void __launch_bounds__(HASH_THREADS) k_aggregate_assign(CqlLaunch a, 
   {
     bool valid = row < rows;
     uint32_t h = (valid && ncols) ? key_hash(k, ncols, string_mask, row) : 0u;
-    uint64_t start = (uint64_t)(h % (buckets ? buckets : 1u)) * K;
+    uint64_t start = linear ? (uint64_t)h & (slots - 1) : (uint64_t)(h % (buckets ? buckets : 1u)) * K;
     uint32_t claimed = EMPTY_SLOT;
     for (uint32_t p = 0; valid && p < K; p++)
     {
-      uint64_t slot = start + p;
+      uint64_t slot = linear ? (start + p) & (slots - 1) : start + p;
       if (slot >= slots) break;
       // a slot's owner only ever goes from empty to a row: read it first, claim it only when empty
       uint32_t prev = *((volatile uint32_t*)&owner[slot]);

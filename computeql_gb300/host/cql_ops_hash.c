@@ -627,13 +627,26 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
   else
     while (buckets < rows / 64 && buckets < max_buckets) buckets <<= 1;
   uint64_t K = key_count ? 8 : 1;
+  /* GB300 layout: with keys, linear probing over a power-of-two table of about twice the expected groups
+     (K = the probe limit), which for a million groups stays in L2; the reference's buckets of K slots
+     (buckets 1.25 x the groups) would be 16 slots a group, larger than L2 and read whole by compaction */
+  int linear = key_count > 0;
+  if (linear)
+  {
+    uint64_t want = group_hint > 0 ? 2 * group_hint : rows / 32;
+    max_buckets = 1024;
+    while (max_buckets < 2 * rows) max_buckets <<= 1;
+    buckets = 1024;
+    while (buckets < want && buckets < max_buckets) buckets <<= 1;
+    K = 64;
+  }
   CqlKernel* assign = kernel("aggregate_assign");
   if (!assign) return 0;
   CqlBuffer *owner = NULL, *count = NULL, *row_slot = NULL, *overflow = NULL;
   uint64_t slots = 0;
   for (int attempt = 0; attempt < 16; attempt++)
   {
-    slots = buckets * K;
+    slots = linear ? buckets : buckets * K;
     owner = pooled("agg_owner_buf", slots * 4, CQLCUDA_BUFFER_READ_WRITE);
     count = pooled("agg_count_buf", slots * 4, CQLCUDA_BUFFER_READ_WRITE);
     row_slot = pooled("agg_row_slot_buf", rows * 4, CQLCUDA_BUFFER_READ_WRITE);
@@ -655,6 +668,7 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
     cqlcuda_kernel_set_arg_u64(assign, 3, key_count);
     cqlcuda_kernel_set_arg_u64(assign, 4, string_mask);
     cqlcuda_kernel_set_arg_u64(assign, 5, group_hint >= AGG_MANY_GROUPS);
+    cqlcuda_kernel_set_arg_u64(assign, 6, linear);
     uint32_t over = 0;
     CqlBatch* b = cqlcuda_batch_begin(0, 4);
     cqlcuda_batch_buffer_fill(b, owner, slots * 4, EMPTY);
