@@ -177,6 +177,7 @@ struct CqlLane
   int is_main;
   std::unordered_map<uint64_t, CqlGraphEntry> graphs;   // plan graphs by fingerprint, this lane's alone
   uint64_t graph_clock;
+  std::unordered_map<uint64_t, uint32_t> graph_seen;    // fingerprints met once: captured when met again
 };
 
 static std::atomic<uint64_t> g_graph_captures{0}, g_graph_replays{0}, g_graph_fallbacks{0};
@@ -1252,7 +1253,8 @@ extern "C" CqlBatch* cqlcuda_batch_begin(uint64_t upload_bytes_needed, uint64_t 
 extern "C" CqlBatch* cqlcuda_batch_begin_graph(uint64_t upload_bytes_needed, uint64_t download_bytes_needed, uint64_t plan_key)
 {
   CqlBatch* b = cqlcuda_batch_begin(upload_bytes_needed, download_bytes_needed);
-  if (b)
+  // plan graphs are kept to the main lane: a thread's own lane (a serving worker) runs ordinary batches
+  if (b && L().is_main)
   {
     b->recording = 1;
     b->plan_key = plan_key;
@@ -1520,6 +1522,16 @@ static void graph_end(CqlBatch* b, CqlLane& l)
     e.last_use = ++l.graph_clock;
     g_graph_replays.fetch_add(1, std::memory_order_relaxed);
     graph_copy_out(b, e);
+    return;
+  }
+  // a shape is captured the second time it is met: a capture and its instantiation cost more than the
+  // launches a graph saves, so shapes met once (a serving loop's odd batch sizes) run eagerly
+  if (l.graph_seen.find(fp) == l.graph_seen.end())
+  {
+    if (l.graph_seen.size() >= 4096) l.graph_seen.clear();
+    l.graph_seen[fp] = 1;
+    if (!issue_ops(b, l.stream, nullptr, nullptr, nullptr)) b->failed = 1;
+    b->recording = 0;
     return;
   }
   CqlGraphEntry e;

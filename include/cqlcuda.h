@@ -135,10 +135,11 @@ void      cqlcuda_batch_buffer_read_at(CqlBatch* batch, CqlBuffer* buffer, uint6
 void      cqlcuda_batch_fill_range(CqlBatch* batch, CqlBuffer* buffer, uint64_t offset, uint64_t size, uint32_t value);
 int       cqlcuda_batch_end(CqlBatch* batch);                                                            /* :217, 0 on failure (reads zero-filled) */
 /* A batch for a plan shape (no reference counterpart): its writes, fills, dispatches and reads are
-   recorded, and at cqlcuda_batch_end the record runs as a CUDA graph - the one captured the first time a
+   recorded, and at cqlcuda_batch_end the record runs as a CUDA graph - the one captured the second time a
    batch of the same shape ended (the same operations on the same buffers with the same kernel arguments;
-   only the bytes written may differ), replayed with the new bytes in one launch. A lane keeps up to 32
-   graphs. A record that cannot be captured, and any record while kernel profiling is on (its kernels are
+   only the bytes written may differ), replayed with the new bytes in one launch; a shape met once runs as
+   an ordinary batch. Only the main lane keeps graphs (up to 32); on a thread's own lane this opens an
+   ordinary batch. A record that cannot be captured, and any record while kernel profiling is on (its kernels are
    timed one by one), runs as an ordinary batch. plan_key tells shapes apart. */
 CqlBatch* cqlcuda_batch_begin_graph(uint64_t upload_bytes_needed, uint64_t download_bytes_needed, uint64_t plan_key);
 /* On (the default) or off: with graphs off, plan-shape batches run as ordinary batches. */
