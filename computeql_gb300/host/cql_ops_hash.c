@@ -16,6 +16,7 @@
 
 #include <math.h>
 #include <stdio.h>
+#include <stddef.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -343,6 +344,34 @@ static double order_key_to_double(uint64_t k)
   return v;
 }
 
+/* program `dst` = `src` with the one constant holding `from` replaced by `to`: the used words, constants
+   and strings and the bindings are copied, not the whole (84 KB) struct; 0 when `from` is not exactly one
+   constant (the caller then builds the program) */
+static int program_with_literal(CqlProgram* dst, const CqlProgram* src, double from, double to)
+{
+  uint32_t hits = 0, at = 0;
+  for (uint32_t i = 0; i < src->const_count; i++)
+  {
+    double c;
+    memcpy(&c, &src->consts[2 * i], 8);
+    if (c == from)
+    {
+      hits++;
+      at = i;
+    }
+  }
+  if (hits != 1 || src->word_count > CQLOPS_MAX_WORDS || src->str_pool_size > CQLOPS_MAX_STR_POOL) return 0;
+  memcpy(dst->words, src->words, (size_t)src->word_count * 4);
+  dst->word_count = src->word_count;
+  memcpy(dst->consts, src->consts, (size_t)src->const_count * 8);
+  dst->const_count = src->const_count;
+  memcpy(dst->str_pool, src->str_pool, src->str_pool_size);
+  /* everything from str_pool_size to the end: the bindings, flags and error text */
+  memcpy(&dst->str_pool_size, &src->str_pool_size, sizeof(CqlProgram) - offsetof(CqlProgram, str_pool_size));
+  memcpy(&dst->consts[2 * at], &to, 8);
+  return 1;
+}
+
 static int numeric_full(const CqlColumn* c, uint64_t rows)
 {
   return c && c->rows == rows && c->width == 0 && c->buffer &&
@@ -421,9 +450,12 @@ static int group_small_key(const CqlColumn* key, uint32_t expr_count, const uint
   int result = progs && qp && sum_cols && counts && sums && first && ext ? 1 : 0;
   for (uint32_t v = 0; result == 1 && v < values; v++)
   {
+    /* the programs differ in their literal alone: the first is built, the others copied with it replaced */
     char where[64];
     snprintf(where, sizeof(where), "(= k %lld)", (long long)(kmin + v));
-    if (!cqlops_program_build(where, cols, names, ncols, &progs[v])) result = -1;
+    if (!(v > 0 && program_with_literal(&progs[v], &progs[0], (double)kmin, (double)(kmin + v))) &&
+        !cqlops_program_build(where, cols, names, ncols, &progs[v]))
+      result = -1;
     for (uint32_t s = 0; s < sums_per_value; s++)
     {
       qp[v * sums_per_value + s] = &progs[v];
