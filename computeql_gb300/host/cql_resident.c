@@ -356,3 +356,56 @@ CqlResidentStats cqlops_resident_stats(CqlResident* r)
   pthread_mutex_unlock(&r->lock);
   return s;
 }
+
+void cqlops_note_error(const char* why);
+
+static int refuse(const char* why)
+{
+  cqlops_note_error(why);
+  return 0;
+}
+
+/* ---- a streamed operator over the cache ----
+   SUM/MIN/MAX of a host column in chunks through the cache (qe_aggregate_global_streamed,
+   src/query_exec/query_exec.c:8842-9112): each chunk's device copy comes from the cache, or is uploaded
+   into it, and cqlops_aggregate_global reduces it; the chunks' partials are folded in chunk order. A
+   column larger than device memory passes through the cache's budget chunk by chunk, and a column
+   queried again is read from HBM without an upload. */
+int cqlops_aggregate_global_streamed(CqlResident* r, uint64_t column_uid, uint64_t generation, const void* host_values, uint32_t type,
+                                     uint64_t rows, uint64_t chunk_rows, double* out_sum, double* out_min, double* out_max,
+                                     uint64_t* out_uploaded_bytes)
+{
+  cqlops_note_error("");
+  if (out_uploaded_bytes) *out_uploaded_bytes = 0;
+  if (!r || r->ops.alloc != dev_alloc) return refuse("the streamed aggregate takes a cache of backend buffers (created with ops NULL)");
+  uint32_t width = type == CQLOPS_TYPE_F64 ? 8 : (type == CQLOPS_TYPE_U32 || type == CQLOPS_TYPE_I32 || type == CQLOPS_TYPE_F32) ? 4 : 0;
+  if (!width || !host_values || !out_sum || !out_min || !out_max) return refuse("a U32/I32/F32/F64 host column and its outputs");
+  if (chunk_rows == 0) chunk_rows = 1u << 24;
+  double sum = 0.0, mn = 0.0, mx = 0.0;
+  int seen = 0;
+  for (uint64_t start = 0; start < rows; start += chunk_rows)
+  {
+    uint64_t n = rows - start < chunk_rows ? rows - start : chunk_rows;
+    int hit = 0;
+    CqlBuffer* b = (CqlBuffer*)cqlops_resident_acquire(r, column_uid, generation, (const char*)host_values + start * width, start, n, width, &hit);
+    if (!b) return refuse("a chunk could not be held in the cache");
+    if (!hit && out_uploaded_bytes) *out_uploaded_bytes += n * width;
+    CqlColumn col;
+    memset(&col, 0, sizeof(col));
+    col.type = type;
+    col.rows = n;
+    col.buffer = b;
+    double s = 0.0, lo = 0.0, hi = 0.0;
+    int ok = cqlops_aggregate_global(&col, 1, &s, &lo, &hi);
+    cqlops_resident_release(r, b);
+    if (!ok) return 0;
+    sum += s;
+    if (!seen || lo < mn) mn = lo;
+    if (!seen || hi > mx) mx = hi;
+    seen = 1;
+  }
+  *out_sum = sum;
+  *out_min = mn;
+  *out_max = mx;
+  return 1;
+}

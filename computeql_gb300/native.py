@@ -212,6 +212,7 @@ OPS_API = [
     ("cqlops_resident_evict", u64, [P, u64]),
     ("cqlops_resident_clear", None, [P]),
     ("cqlops_resident_stats", CqlResidentStats, [P]),
+    ("cqlops_aggregate_global_streamed", C.c_int, [P, u64, u64, P, u32, u64, u64, P, P, P, P]),
     ("cqlserve_create", P, [P]),
     ("cqlserve_destroy", None, [P]),
     ("cqlserve_add_table", C.c_int, [P, P, u32]),

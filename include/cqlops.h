@@ -453,6 +453,16 @@ uint64_t cqlops_resident_evict(CqlResident* cache, uint64_t bytes_wanted);
 void cqlops_resident_clear(CqlResident* cache);
 CqlResidentStats cqlops_resident_stats(CqlResident* cache);
 
+/* SUM/MIN/MAX of a host column (U32/I32/F32/F64, rows values at host_values) streamed through the
+   cache in chunks of chunk_rows (0: 16M) - qe_aggregate_global_streamed, src/query_exec/query_exec.c:
+   8842-9112: each chunk's device copy comes from the cache (keyed by column_uid, generation and the
+   chunk's rows) or is uploaded into it, is reduced by cqlops_aggregate_global, and the partials are folded
+   in chunk order. The cache must hold backend buffers (created with ops NULL). *out_uploaded_bytes
+   (optional) receives the bytes copied to the device: 0 when every chunk was cached. */
+int cqlops_aggregate_global_streamed(CqlResident* cache, uint64_t column_uid, uint64_t generation, const void* host_values, uint32_t type,
+                                     uint64_t rows, uint64_t chunk_rows, double* out_sum, double* out_min, double* out_max,
+                                     uint64_t* out_uploaded_bytes);
+
 /* Why the last operator call returned 0 when it refused the request itself ("" otherwise; GPU
    failures are in cqlcuda_last_error()). */
 const char* cqlops_last_error(void);

@@ -49,3 +49,38 @@ def test_chunks_are_kept_between_queries(gpu):
     assert np.array_equal(out, host2[:chunk])
     lib.cqlops_resident_release(cache, buf)
     lib.cqlops_resident_destroy(cache)
+
+
+@pytest.mark.parametrize("dtype", [np.uint32, np.int32, np.float64])
+def test_streamed_aggregate_over_the_cache(gpu, dtype):
+    """SUM/MIN/MAX of a host column streamed through the cache: the first pass uploads every chunk, the
+    second uploads nothing and gives the same answer; a written column (a new generation) is uploaded again.
+    Integer sums exact; f64 within 1e-12 of a compensated sum."""
+    import oracle
+    from computeql_gb300 import native, ops
+    lib = native.load_ops()
+    cache = lib.cqlops_resident_create(0, None)
+    rng = np.random.default_rng(3)
+    n, chunk = 3_000_001, 1 << 20
+    if dtype == np.float64:
+        host = rng.lognormal(3.0, 1.0, n)
+    else:
+        host = rng.integers(-2**30 if dtype == np.int32 else 0, 2**30, n).astype(dtype)
+    ctype = {np.uint32: ops.TYPE_U32, np.int32: ops.TYPE_I32, np.float64: ops.TYPE_F64}[dtype]
+    width = host.itemsize
+    results = []
+    for generation in (1, 1, 2):
+        s, mn, mx, up = C.c_double(), C.c_double(), C.c_double(), C.c_uint64()
+        assert lib.cqlops_aggregate_global_streamed(cache, 9, generation, host.ctypes.data, ctype, n, chunk, C.byref(s), C.byref(mn),
+                                                    C.byref(mx), C.byref(up)), native.last_error()
+        results.append((s.value, mn.value, mx.value, up.value))
+    assert [r[3] for r in results] == [n * width, 0, n * width]
+    assert results[0][:3] == results[1][:3] == results[2][:3]
+    s, mn, mx, _ = results[0]
+    assert (mn, mx) == (float(host.min()), float(host.max()))
+    if dtype == np.float64:
+        exact = oracle.compensated_sum(host)
+        assert abs(s - exact) <= 1e-12 * abs(exact)
+    else:
+        assert s == float(host.astype(np.int64).sum())
+    lib.cqlops_resident_destroy(cache)
