@@ -51,6 +51,14 @@ extern int g_cql_max_smem_optin;
 // Counts launches of this library's kernels (the figure a bench reports as gpu_launches).
 void cql_note_launch(void);
 
+// Sets the calling thread's cqlcuda_last_error() text (printf format).
+void cql_set_error_text(const char* fmt, ...);
+
+// Resolves the no-allocation slot compaction's static scratch for the current device and loads its
+// kernel, so that the entry point's later calls allocate nothing even under lazy module loading.
+// Returns 1 on success. cqlcuda_init calls it for the device it opens.
+int cql_noalloc_prepare(void);
+
 #define CQL_LAUNCH_CHECK() do { cudaError_t e__ = cudaGetLastError(); if (e__ != cudaSuccess) return (int)e__; cql_note_launch(); } while (0)
 
 // Grid for a streaming kernel: `per_sm` resident CTAs on every SM, never more CTAs than `work_ctas`.

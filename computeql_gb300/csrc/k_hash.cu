@@ -281,11 +281,12 @@ static int launch_aggregate_compact(const CqlLaunch& a, uint32_t gws, uint32_t l
 // array. Every GPU that loads this library holds that array until the process exits.
 //
 // Limit: CQL_NOALLOC_COMPACT_MAX_SLOTS slots (2^24, i.e. 65536 blocks of 256; 256 KB of scratch).
-// The first call on a device looks up the array's device address with cudaGetSymbolAddress, with
-// that device current, and keeps it for later calls. Make that first call before any stream capture.
-// All calls share the array. Calls whose work overlaps on the GPU race on it: serialise them, for
-// example by issuing them on one stream. Nothing in the array has to start at zero: every block
-// total is written before it is read, and so is the group total.
+// The array's device address is looked up with cudaGetSymbolAddress, with the device current, once
+// per device: by cqlcuda_init for the device it opens (which also loads the kernel, so that under
+// lazy module loading no later call loads a module), else by the first call on a device. Make that
+// first call before any stream capture. All calls share the array. Calls whose work overlaps on the
+// GPU race on it: serialise them, for example by issuing them on one stream. Nothing in the array has
+// to start at zero: every block total is written before it is read, and so is the group total.
 
 #define CQL_NOALLOC_COMPACT_MAX_SLOTS (1u << 24)
 #define CQL_NOALLOC_COMPACT_BLOCKS (CQL_NOALLOC_COMPACT_MAX_SLOTS / 256u)
@@ -295,19 +296,43 @@ static __device__ __align__(256) uint32_t g_noalloc_compact_scratch[CQL_NOALLOC_
 
 static uint32_t* g_noalloc_scratch_ptr[CQL_NOALLOC_MAX_DEVICES];
 
+static int noalloc_resolve(int device)
+{
+  if (g_noalloc_scratch_ptr[device]) return 1;
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_compact_scratch) != cudaSuccess || !p) return 0;
+  cudaFuncAttributes attr;
+  if (cudaFuncGetAttributes(&attr, k_aggregate_compact) != cudaSuccess) return 0;
+  g_noalloc_scratch_ptr[device] = (uint32_t*)p;
+  return 1;
+}
+
+int cql_noalloc_prepare(void)
+{
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= CQL_NOALLOC_MAX_DEVICES) return 0;
+  return noalloc_resolve(device);
+}
+
 extern "C" int cqlcuda_compact_slots_noalloc(const uint32_t* slot_counts, const uint32_t* slot_owner, uint32_t slot_count,
                                              uint32_t* slot_group, uint32_t* group_owner, uint32_t* group_count, uint32_t* out_group_total,
                                              void* stream)
 {
-  if (slot_count == 0 || slot_count > CQL_NOALLOC_COMPACT_MAX_SLOTS) return -1;
-  if (!slot_counts || !slot_owner || !slot_group || !group_owner || !group_count || !out_group_total) return -2;
-  int device = 0;
-  if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= CQL_NOALLOC_MAX_DEVICES) return -3;
-  if (!g_noalloc_scratch_ptr[device])
+  if (slot_count == 0 || slot_count > CQL_NOALLOC_COMPACT_MAX_SLOTS)
   {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_compact_scratch) != cudaSuccess || !p) return -3;
-    g_noalloc_scratch_ptr[device] = (uint32_t*)p;
+    cql_set_error_text("cqlcuda_compact_slots_noalloc: %u slots; it takes 1 to %u", slot_count, CQL_NOALLOC_COMPACT_MAX_SLOTS);
+    return -1;
+  }
+  if (!slot_counts || !slot_owner || !slot_group || !group_owner || !group_count || !out_group_total)
+  {
+    cql_set_error_text("cqlcuda_compact_slots_noalloc: a NULL pointer argument");
+    return -2;
+  }
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= CQL_NOALLOC_MAX_DEVICES || !noalloc_resolve(device))
+  {
+    cql_set_error_text("cqlcuda_compact_slots_noalloc: no usable device (its static scratch could not be resolved)");
+    return -3;
   }
   uint32_t* scratch = g_noalloc_scratch_ptr[device];
   cudaStream_t s = (cudaStream_t)stream;
@@ -329,15 +354,28 @@ extern "C" int cqlcuda_compact_slots_noalloc(const uint32_t* slot_counts, const 
   a.buf[6] = scratch + CQL_NOALLOC_COMPACT_BLOCKS;     // group total
   a.bytes[6] = 4;
   a.push[0] = slot_count;
+  // an earlier, unrelated launch error still pending on this thread is not this call's failure
+  (void)cudaGetLastError();
   for (uint32_t mode = 0; mode < 3; mode++)
   {
     a.push[1] = mode;
     if (mode == 1) k_aggregate_compact<<<1, HASH_THREADS, 0, s>>>(a, mode, slot_count);
     else k_aggregate_compact<<<cql_stream_grid(blocks, 8), HASH_THREADS, 0, s>>>(a, mode, slot_count);
-    if (cudaGetLastError() != cudaSuccess) return -4;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+    {
+      cql_set_error_text("cqlcuda_compact_slots_noalloc: launch of pass %u failed: %s", mode, cudaGetErrorString(e));
+      return -4;
+    }
+    cql_note_launch();
   }
-  if (cudaMemcpyAsync(out_group_total, scratch + CQL_NOALLOC_COMPACT_BLOCKS, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return -4;
-  if (cudaStreamSynchronize(s) != cudaSuccess) return -4;
+  cudaError_t e = cudaMemcpyAsync(out_group_total, scratch + CQL_NOALLOC_COMPACT_BLOCKS, 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess)
+  {
+    cql_set_error_text("cqlcuda_compact_slots_noalloc: %s", cudaGetErrorString(e));
+    return -4;
+  }
   return 1;
 }
 

@@ -3,7 +3,7 @@
 // streams, kernel profile, failure injection.
 //
 // It replaces the Vulkan backend (src/gpu/vulkan/gpu_vulkan.c) behind the same vtable
-// (src/gpu/gpu_backend.h:179-233). Design differences, GB300-first:
+// (src/gpu/gpu_backend.h:17-71). Design differences, GB300-first:
 //  - device memory is plain cudaMalloc, one allocation per buffer (no sub-allocated blocks, no
 //    ReBAR heap): 280 GB of HBM makes block sub-allocation unnecessary;
 //  - a batch is the runtime's stream plus a pinned staging area for reads, finished by one
@@ -283,6 +283,16 @@ static void set_error(const char* fmt, ...)
   tl_error = buf;
 }
 
+void cql_set_error_text(const char* fmt, ...)
+{
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  tl_error = buf;
+}
+
 // A CUDA error that leaves the context unusable makes device_lost sticky, as
 // gpu_vulkan_note_result does for VK_ERROR_DEVICE_LOST (gpu_vulkan.c:1523-1535).
 static int note_cuda(cudaError_t e, const char* what)
@@ -452,6 +462,8 @@ extern "C" int cqlcuda_init(void)
   cudaEventCreate(&s.exec_stop);
   cudaEventCreate(&s.timer_start);
   cudaEventCreate(&s.timer_stop);
+  // the no-allocation compaction's scratch address and kernel, resolved now rather than mid-query
+  cql_noalloc_prepare();
   s.initialized = 1;
   return 1;
 }
@@ -1858,6 +1870,17 @@ __global__ void k_fill_sequence(uint32_t* out, uint64_t rows, uint32_t first)
   for (; i < rows; i += stride) out[i] = first + (uint32_t)i;
 }
 
+__global__ void k_fill_affine(uint32_t* out, uint64_t rows, uint64_t mul, uint64_t add, uint64_t modulus)
+{
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (; i < rows; i += stride)
+  {
+    uint64_t v = i * mul + add;
+    out[i] = (uint32_t)(modulus ? v % modulus : v);
+  }
+}
+
 extern "C" int cqlcuda_fill_splitmix_u32(CqlBuffer* b, uint64_t rows, uint64_t seed, uint32_t per_row, uint32_t index, uint64_t range)
 {
   if (!b || rows * 4 > b->size || b->imported) return 0;
@@ -1876,6 +1899,16 @@ extern "C" int cqlcuda_fill_sequence_u32(CqlBuffer* b, uint64_t rows, uint32_t f
   k_fill_sequence<<<grid, 256, 0, s.stream>>>((uint32_t*)b->dptr, rows, first);
   if (!note_cuda(cudaGetLastError(), "fill_sequence")) return 0;
   return wait_stream(s.stream, "fill_sequence");
+}
+
+extern "C" int cqlcuda_fill_affine_u32(CqlBuffer* b, uint64_t rows, uint64_t mul, uint64_t add, uint64_t modulus)
+{
+  if (!b || rows * 4 > b->size || b->imported) return 0;
+  CqlState& s = S();
+  uint32_t grid = cql_stream_grid((rows + 255) / 256, 8);
+  k_fill_affine<<<grid, 256, 0, s.stream>>>((uint32_t*)b->dptr, rows, mul, add, modulus);
+  if (!note_cuda(cudaGetLastError(), "fill_affine")) return 0;
+  return wait_stream(s.stream, "fill_affine");
 }
 
 extern "C" int cqlcuda_flush_l2(uint64_t bytes)

@@ -41,6 +41,8 @@
 
 void cqlops_note_error(const char* why);
 
+int cqlops_rows_fit(uint64_t rows);
+
 static int refuse(const char* why)
 {
   cqlops_note_error(why);
@@ -1329,6 +1331,7 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
   uint32_t cube_pass = rows_per_thread;
   if (rows_per_thread != 0 && rows_per_thread != 4 && rows_per_thread != 8 && rows_per_thread != 16) rows_per_thread = 8;
   uint64_t rows = columns[0].rows;
+  if (!cqlops_rows_fit(rows)) return 0;
   for (uint32_t c = 0; c < column_count; c++)
   {
     const CqlColumn* col = &columns[c];

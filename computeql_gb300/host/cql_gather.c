@@ -19,6 +19,8 @@
 
 void cqlops_note_error(const char* why);
 
+int cqlops_rows_fit(uint64_t rows);
+
 static int refuse(const char* why)
 {
   cqlops_note_error(why);
@@ -103,7 +105,7 @@ int cqlops_gather_rows(const CqlColumn* columns, uint32_t column_count, const ui
   cqlops_note_error("");
   if (column_count == 0 || count == 0) return 1;
   if (!columns || !out_values) return refuse("columns and outputs are required");
-  if (count >= 0xffffffffull) return refuse("row count out of range");
+  if (!cqlops_rows_fit(count)) return 0;
   uint32_t* params = (uint32_t*)calloc((size_t)column_count * 4, sizeof(uint32_t));
   uint64_t* section = (uint64_t*)malloc((size_t)column_count * sizeof(uint64_t));
   uint32_t* sizes = (uint32_t*)malloc((size_t)column_count * sizeof(uint32_t));

@@ -52,6 +52,19 @@ static int refuse(const char* why)
   return 0;
 }
 
+/* Row numbers and row counts reach the kernels as 32-bit push-constant words (the reference's shaders
+   take them the same way; its operators never pass more than a 16M-row chunk). A column of more
+   rows is refused before any device work rather than truncated. */
+int cqlops_rows_fit(uint64_t rows)
+{
+  if (rows <= CQLOPS_MAX_ROWS) return 1;
+  char why[200];
+  snprintf(why, sizeof(why), "%llu rows: an operator takes at most %llu rows (32-bit row numbers); run it over slices of the table",
+           (unsigned long long)rows, (unsigned long long)CQLOPS_MAX_ROWS);
+  cqlops_note_error(why);
+  return 0;
+}
+
 uint32_t cqlops_last_launches(void)
 {
   return cqlcuda_kernel_launch_count() - g_launch_mark;
@@ -90,6 +103,8 @@ int cqlops_aggregate_global(const CqlColumn* columns, uint32_t column_count, dou
     return 0;
   }
   uint64_t rows = columns[0].rows;
+  for (uint32_t c = 0; c < column_count; c++)
+    if (!cqlops_rows_fit(columns[c].rows)) return 0;
   double sum[QE_AGG_STREAM_MAX_COLUMNS], mn[QE_AGG_STREAM_MAX_COLUMNS], mx[QE_AGG_STREAM_MAX_COLUMNS];
   const CqlColumn* gpu_cols[QE_AGG_STREAM_MAX_COLUMNS];
   uint32_t gpu_to_col[QE_AGG_STREAM_MAX_COLUMNS];
@@ -340,6 +355,8 @@ int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const Cq
     return 0;
   }
   uint64_t rows = columns[0].rows;
+  for (uint32_t c = 0; c < column_count; c++)
+    if (!cqlops_rows_fit(columns[c].rows)) return 0;
   uint32_t words[1 + QE_SIMPLE_SCAN_MAX_LEAVES * 6];
   memset(words, 0, sizeof(words));
   words[0] = leaf_count;
@@ -465,6 +482,7 @@ int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count,
                        int64_t* out_mins, int64_t* out_maxs)
 {
   launches_begin();
+  if (!cqlops_rows_fit(rows)) return 0;
   /* a dictionary string column groups by its codes, as the reference's dictionary GROUP BY does */
   int dict_key = key && key->type == CQLOPS_TYPE_STRING8 && key->dict && key->width == 0;
   if (!key || !key->has_range || !(key->type == CQLOPS_TYPE_U32 || key->type == CQLOPS_TYPE_I32 || dict_key) || key->rows != rows || !key->buffer ||

@@ -42,6 +42,17 @@ void cqlops_generated_stats(uint64_t* out_requests, uint64_t* out_failures)
   pthread_mutex_unlock(&g_failed_lock);
 }
 
+int cqlops_rows_fit(uint64_t rows);
+
+/* every column the program binds fits the kernels' 32-bit row numbers */
+static int program_rows_fit(const CqlProgram* prog, const CqlColumn* columns)
+{
+  if (!prog->binding_count) return cqlops_rows_fit(columns[0].rows);
+  for (uint32_t i = 0; i < prog->binding_count; i++)
+    if (!cqlops_rows_fit(columns[prog->binding_column[i]].rows)) return 0;
+  return 1;
+}
+
 static int refuse(const char* why)
 {
   cqlops_note_error(why);
@@ -217,6 +228,7 @@ static int scan_filter_run(const CqlProgram* prog, const CqlColumn* columns, uin
 {
   cqlops_note_error("");
   if (prog->requires_cpu_scan) return refuse("the program needs the CPU scan, which this backend does not have");
+  if (!program_rows_fit(prog, columns)) return 0;
   /* a fuzzy comparison runs on the interpreter only (qe_scan_filter_selected, :2532, :2641) */
   uint32_t score_flags = prog->has_score_output ? (1u | (prog->has_score_output == 2u ? 2u : 0u)) : 0u;
   if (score_flags)
@@ -360,6 +372,7 @@ int cqlops_fused_filter_aggregate(const CqlProgram* prog_in, const CqlColumn* co
   cqlops_note_error("");
   if (agg_count > 4) return refuse("at most 4 aggregate columns");
   if (prog_in->requires_cpu_scan || prog_in->has_score_output) return refuse("the program needs the CPU scan");
+  if (!program_rows_fit(prog_in, columns)) return 0;
   CqlProgram* prog = (CqlProgram*)malloc(sizeof(CqlProgram));
   if (!prog) return 0;
   memcpy(prog, prog_in, sizeof(CqlProgram));
@@ -457,6 +470,7 @@ int cqlops_fused_filter_group(const CqlProgram* prog_in, const CqlColumn* column
   cqlops_note_error("");
   if (key_count == 0 || key_count > 3 || agg_count > 4) return refuse("1 to 3 keys and at most 4 aggregate columns");
   if (prog_in->requires_cpu_scan || prog_in->has_score_output) return refuse("the program needs the CPU scan");
+  if (!program_rows_fit(prog_in, columns)) return 0;
   CqlProgram* prog = (CqlProgram*)malloc(sizeof(CqlProgram));
   if (!prog) return 0;
   memcpy(prog, prog_in, sizeof(CqlProgram));

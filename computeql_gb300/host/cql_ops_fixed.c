@@ -25,6 +25,8 @@ static const double g_pow10[QE_FIXED_MAX_SCALE + 1] = { 1.0, 10.0, 100.0, 1000.0
 
 void cqlops_note_error(const char* why);
 
+int cqlops_rows_fit(uint64_t rows);
+
 static int refuse(const char* why)
 {
   cqlops_note_error(why);
@@ -73,6 +75,7 @@ int cqlops_fixed_scale(const CqlColumn* column, CqlBuffer* selection, uint64_t s
   *out_largest = 0.0;
   if (!column || !column->buffer || column->width != 0) return refuse("a full-width numeric column");
   uint64_t n = selection ? selection_count : column->rows;
+  if (!cqlops_rows_fit(column->rows) || !cqlops_rows_fit(n)) return 0;
   if (selection && cqlcuda_buffer_size(selection) < n * 4) return refuse("selection buffer smaller than its count");
   if (n == 0)
   {
@@ -130,7 +133,7 @@ int cqlops_group_dense_fixed(const CqlColumn* key, uint32_t expr_count, const ui
   if (expr_count == 0 || expr_count > 8) return refuse("1 to 8 aggregates");
   uint64_t rows = key->rows;
   uint64_t n = selection ? selection_count : rows;
-  if (rows >= 0xffffffffull) return refuse("row count out of range");
+  if (!cqlops_rows_fit(rows)) return 0;
   if (selection && cqlcuda_buffer_size(selection) < n * 4) return refuse("selection buffer smaller than its count");
   uint32_t func_codes = 0, scales = 0, arg_f32 = 0;
   int32_t scale_of[8];

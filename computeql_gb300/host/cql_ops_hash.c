@@ -32,6 +32,25 @@
 
 void cqlops_note_error(const char* why);
 
+/* The HyperLogLog registers of the calling thread's last hash GROUP BY, [group][hll expression][2^p] */
+static __thread uint32_t* tl_hll_regs = NULL;
+static __thread uint64_t tl_hll_words = 0;
+
+uint64_t cqlops_group_hash_registers(uint32_t* out, uint64_t capacity)
+{
+  if (out && tl_hll_regs) memcpy(out, tl_hll_regs, (capacity < tl_hll_words ? capacity : tl_hll_words) * 4);
+  return tl_hll_words;
+}
+
+static void keep_hll_registers(uint32_t* regs, uint64_t words)
+{
+  free(tl_hll_regs);
+  tl_hll_regs = regs;
+  tl_hll_words = regs ? words : 0;
+}
+
+int cqlops_rows_fit(uint64_t rows);
+
 static int refuse(const char* why)
 {
   cqlops_note_error(why);
@@ -320,6 +339,11 @@ static int csr_reduce(uint64_t rows, uint64_t slots, uint64_t groups, CqlBuffer*
     free(cm);
     free(cw);
   }
+  if (ok && sketch)
+  {
+    keep_hll_registers(sketch, sketch_bytes / 4);
+    sketch = NULL;
+  }
   free(sketch);
   free(dmean);
   free(dweight);
@@ -543,12 +567,13 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
                       uint64_t* out_repr_row, uint64_t* out_counts, double* out_results, uint32_t* out_path)
 {
   cqlops_note_error("");
+  keep_hll_registers(NULL, 0);
   if (key_count > 4 || expr_count == 0 || expr_count > 8) return refuse("0 to 4 keys and 1 to 8 aggregates");
   /* no GROUP BY: one bucket of one slot takes every row (:10796-10801) */
   uint64_t rows = key_count ? keys[0].rows : 0;
   for (uint32_t e = 0; e < expr_count && !key_count; e++)
     if (args[e]) rows = args[e]->rows;
-  if (rows >= 0xffffffffull) return refuse("row count out of range");
+  if (!cqlops_rows_fit(rows)) return 0;
   if (rows == 0)
   {
     /* no rows, no groups: an aggregate over nothing is the caller's empty result */

@@ -24,6 +24,8 @@
 
 void cqlops_note_error(const char* why);
 
+int cqlops_rows_fit(uint64_t rows);
+
 static int refuse(const char* why)
 {
   cqlops_note_error(why);
@@ -82,7 +84,7 @@ int cqlops_hash_join(const CqlColumn* build_key, const CqlColumn* probe_key, int
 {
   cqlops_note_error("");
   uint64_t brows = build_key->rows, prows = probe_key->rows;
-  if (brows >= 0xffffffffull || prows >= 0xffffffffull) return refuse("row count out of range");
+  if (!cqlops_rows_fit(brows) || !cqlops_rows_fit(prows)) return 0;
   CqlBuffer *bd, *bo, *pd, *po;
   int bstr, pstr;
   if (!join_key(build_key, "hj_build_f64", &bd, &bo, &bstr) || !join_key(probe_key, "hj_probe_f64", &pd, &po, &pstr)) return 0;
@@ -771,6 +773,9 @@ int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* ou
   const CqlColumn* fk = q->fact_key;
   if (!fk || !(fk->type == CQLOPS_TYPE_U32 || fk->type == CQLOPS_TYPE_I32) || !q->dim_keys || q->expr_count == 0 || q->expr_count > 8)
     return refuse("a U32/I32 fact key, the dim keys and 1 to 8 aggregates");
+  if (!cqlops_rows_fit(fk->rows)) return 0;
+  for (uint32_t e = 0; e < q->expr_count; e++)
+    if (q->fact_args && q->fact_args[e] && !cqlops_rows_fit(q->fact_args[e]->rows)) return 0;
   /* the fact-side totals each expression needs: AVG is a SUM and the count (:8558-8583) */
   uint32_t core_funcs[8];
   const CqlColumn* core_cols[8];

@@ -14,6 +14,8 @@
 
 void cqlops_note_error(const char* why);
 
+int cqlops_rows_fit(uint64_t rows);
+
 static int refuse(const char* why)
 {
   cqlops_note_error(why);
@@ -41,7 +43,7 @@ static int sort_check(const CqlColumn* keys, uint32_t key_count, CqlBuffer* sele
   if (key_count == 0 || key_count > 4) return refuse("1 to 4 sort keys");
   uint64_t rows = keys[0].rows;
   uint64_t n = selection ? selection_count : rows;
-  if (rows >= 0xffffffffull || n >= 0xffffffffull) return refuse("row count out of range");
+  if (!cqlops_rows_fit(rows) || !cqlops_rows_fit(n)) return 0;
   for (uint32_t k = 0; k < key_count; k++)
   {
     int narrow_ok = keys[k].width == 0 || (keys[k].width <= 3 && key_bytes(keys[k].type) == 4 && keys[k].type != CQLOPS_TYPE_F32);

@@ -23,6 +23,8 @@
 
 void cqlops_note_error(const char* why);
 
+int cqlops_rows_fit(uint64_t rows);
+
 static int refuse(const char* why)
 {
   cqlops_note_error(why);
@@ -49,6 +51,7 @@ int cqlops_zone_map_build(const CqlColumn* column, double* out_zone_map, uint64_
 {
   cqlops_note_error("");
   uint64_t rows = column->rows;
+  if (!cqlops_rows_fit(rows)) return 0;
   uint64_t chunks = (rows + CQLOPS_ZONEMAP_CHUNK_ROWS - 1) / CQLOPS_ZONEMAP_CHUNK_ROWS;
   if (out_chunks < chunks + 1) return refuse("the zone map needs one entry per chunk and one for the summary");
   if (rows == 0) return 1;

@@ -167,6 +167,7 @@ CUDA_API = [
     ("cqlcuda_thread_lane_end", None, []),
     ("cqlcuda_fill_splitmix_u32", C.c_int, [P, u64, u64, u32, u32, u64]),
     ("cqlcuda_fill_sequence_u32", C.c_int, [P, u64, u32]),
+    ("cqlcuda_fill_affine_u32", C.c_int, [P, u64, u64, u64, u64]),
     ("cqlcuda_flush_l2", C.c_int, [u64]),
     ("cqlcuda_timer_begin", None, []),
     ("cqlcuda_timer_end_ms", dbl, []),
@@ -224,6 +225,7 @@ OPS_API = [
     ("cqlops_scan_ranges", u64, [P, u32, P, u32, P, u64, P, P, P]),
     ("cqlops_group_dense_fixed", C.c_int, [P, u32, P, P, P, u64, u64, P, P, P, P, P, P]),
     ("cqlops_hll_estimate", dbl, [P, u64]),
+    ("cqlops_group_hash_registers", u64, [P, u64]),
     ("cqlops_tdigest_percentile", dbl, [P, P, u64, dbl]),
 ]
 

@@ -114,6 +114,14 @@ class Column:
         return cls(ctype, rows, None, width=3, base=first & 0xFFFFFFFF, zone=(float(first), float(first + rows - 1)))
 
     @classmethod
+    def affine(cls, rows, mul, add=0, modulus=0):
+        """u32 column (r * mul + add) % modulus (no reduction for modulus 0), generated on the device."""
+        buf = DeviceBuffer(rows * 4)
+        _check(N.load_cuda().cqlcuda_fill_affine_u32(buf.handle, rows, mul, add, modulus), "fill_affine")
+        zone = (0.0, float(modulus - 1)) if modulus and modulus <= (1 << 32) else (0.0, 4294967295.0)
+        return cls(TYPE_U32, rows, buf, zone=zone)
+
+    @classmethod
     def splitmix(cls, rows, seed, per_row, index, rng):
         """u32 column draw(r*per_row+index) % rng, generated on the device."""
         buf = DeviceBuffer(rows * 4)
@@ -445,6 +453,15 @@ def group_hash(keys, funcs, args, params=None, group_hint=0, path=0, max_groups=
                                           N.ptr(counts), N.ptr(results), C.byref(used)), "cqlops_group_hash")
     G = g.value
     return {"groups": G, "repr_row": repr_row[:G], "counts": counts[:G], "results": results[: G * e].reshape(G, e), "path": used.value}
+
+
+def group_hash_registers():
+    """The HyperLogLog registers of this thread's last group_hash as a (groups * hll exprs, 1024) u32 array."""
+    lib = N.load_ops()
+    words = lib.cqlops_group_hash_registers(None, 0)
+    out = np.empty(words, dtype=np.uint32)
+    lib.cqlops_group_hash_registers(N.ptr(out), words)
+    return out.reshape(-1, 1024)
 
 
 def hash_join(build_key, probe_key, left=False, hint_pairs=0, want_pairs=True):

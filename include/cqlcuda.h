@@ -2,10 +2,11 @@
  * cqlcuda.h - C ABI of the GB300 (sm_103a) execution backend for ComputeQL's GPU operators.
  *
  * Every entry point here replaces one function pointer of the reference's backend vtable
- * `GPU_Backend` (src/gpu/gpu_backend.h:179-233) or one forwarder of the backend-neutral API
+ * `GPU_Backend` (src/gpu/gpu_backend.h:17-71) or one forwarder of the backend-neutral API
  * (src/gpu/gpu.h:95-159). The reference's operator layer (src/query_exec) keeps calling
- * gpu_* functions; a C99 adapter (gpu_cuda.c, listed in INTEGRATION.md) fills the vtable with
- * these functions. Types are plain C: opaque handles, pointers and sizes, no CUDA or torch types.
+ * gpu_* functions; a C99 adapter, computeql_gb300/adapter/gpu_cuda.c (src/gpu/cuda/gpu_cuda.c in
+ * the reference's tree), fills the vtable with these functions. Types are plain C: opaque handles,
+ * pointers and sizes, no CUDA or torch types.
  *
  * Kernels are looked up by the names of the reference's shaders (src/gpu/vulkan/shaders/<name>.comp)
  * and honour the same binding contract: up to 16 buffer bindings and 8 U64 push-constant slots,
@@ -78,62 +79,62 @@ typedef struct CqlStreamStats
    pooled buffers were evicted; returns the bytes it freed. */
 typedef uint64_t (*CqlEvictHook)(uint64_t bytes_wanted);
 
-/* ---- device (GPU_Backend init/release/wait/... gpu_backend.h:183-192) ---- */
-int      cqlcuda_init(void);                                   /* gpu_backend.h:183 init; returns 1 on success */
-void     cqlcuda_release(void);                                /* gpu_backend.h:184 release */
-void     cqlcuda_wait(void);                                   /* gpu_backend.h:185 wait */
-uint64_t cqlcuda_get_executed_kernel_time_microseconds(void);  /* gpu_backend.h:186 */
-uint64_t cqlcuda_device_total_memory(void);                    /* gpu_backend.h:187 */
-uint64_t cqlcuda_device_free_memory(void);                     /* gpu_backend.h:188 */
-uint64_t cqlcuda_device_max_storage_buffer_range(void);        /* gpu_backend.h:189 */
-int      cqlcuda_device_lost(void);                            /* gpu_backend.h:190 */
-void     cqlcuda_pool_begin_epoch(void);                       /* gpu_backend.h:191 */
-CqlMemoryStats cqlcuda_memory_stats(void);                     /* gpu_backend.h:192 */
+/* ---- device (GPU_Backend init/release/wait/... gpu_backend.h:21-30) ---- */
+int      cqlcuda_init(void);                                   /* gpu_backend.h:21 init; returns 1 on success */
+void     cqlcuda_release(void);                                /* gpu_backend.h:22 release */
+void     cqlcuda_wait(void);                                   /* gpu_backend.h:23 wait */
+uint64_t cqlcuda_get_executed_kernel_time_microseconds(void);  /* gpu_backend.h:24 */
+uint64_t cqlcuda_device_total_memory(void);                    /* gpu_backend.h:25 */
+uint64_t cqlcuda_device_free_memory(void);                     /* gpu_backend.h:26 */
+uint64_t cqlcuda_device_max_storage_buffer_range(void);        /* gpu_backend.h:27 */
+int      cqlcuda_device_lost(void);                            /* gpu_backend.h:28 */
+void     cqlcuda_pool_begin_epoch(void);                       /* gpu_backend.h:29 */
+CqlMemoryStats cqlcuda_memory_stats(void);                     /* gpu_backend.h:30 */
 uint32_t cqlcuda_sm_count(void);                               /* device property the kernels size grids by */
 
-/* ---- buffers (gpu_backend.h:194-200) ---- */
-CqlBuffer* cqlcuda_buffer_alloc(uint64_t size, uint32_t flags, const void* data);                       /* :194 */
+/* ---- buffers (gpu_backend.h:32-38) ---- */
+CqlBuffer* cqlcuda_buffer_alloc(uint64_t size, uint32_t flags, const void* data);                       /* :32 */
 CqlBuffer* cqlcuda_buffer_alloc_pooled(const char* name, uint64_t name_len, uint64_t size,
-                                       uint32_t flags, const void* data);                             /* :195 */
-CqlBuffer* cqlcuda_buffer_import_host_readonly(const void* host_ptr, uint64_t size);                   /* :196 */
+                                       uint32_t flags, const void* data);                             /* :33 */
+CqlBuffer* cqlcuda_buffer_import_host_readonly(const void* host_ptr, uint64_t size);                   /* :34 */
 CqlBuffer* cqlcuda_buffer_import_host_readonly_pooled(const char* name, uint64_t name_len,
-                                                      const void* host_ptr, uint64_t size);           /* :197 */
-void       cqlcuda_buffer_release(CqlBuffer* buffer);                                                  /* :198 */
-void       cqlcuda_buffer_write(CqlBuffer* buffer, const void* data, uint64_t size);                   /* :199 */
-void       cqlcuda_buffer_read(CqlBuffer* buffer, void* data, uint64_t size);                          /* :200 */
+                                                      const void* host_ptr, uint64_t size);           /* :35 */
+void       cqlcuda_buffer_release(CqlBuffer* buffer);                                                  /* :36 */
+void       cqlcuda_buffer_write(CqlBuffer* buffer, const void* data, uint64_t size);                   /* :37 */
+void       cqlcuda_buffer_read(CqlBuffer* buffer, void* data, uint64_t size);                          /* :38 */
 uint64_t   cqlcuda_buffer_size(const CqlBuffer* buffer);       /* the bound range a kernel sees (VkDescriptorBufferInfo.range, gpu_vulkan.c:2797) */
 void*      cqlcuda_buffer_device_pointer(const CqlBuffer* buffer); /* for zero-copy interop (DLPack/torch) by host code */
 
-/* ---- kernels (gpu_backend.h:202-209) ---- */
-CqlKernel* cqlcuda_kernel_alloc(const char* name, uint64_t name_len);                                  /* :202, by shader name */
-/* :203 kernel_alloc_from_spirv. The reference hands over SPIR-V; here `image` is CUDA C++ source
+/* ---- kernels (gpu_backend.h:40-47) ---- */
+CqlKernel* cqlcuda_kernel_alloc(const char* name, uint64_t name_len);                                  /* :40, by shader name */
+/* :41 kernel_alloc_from_spirv. The reference hands over SPIR-V; here `image` is CUDA C++ source
    (compiled with NVRTC for sm_103a) or a cubin. An empty image only looks the name up. */
 CqlKernel* cqlcuda_kernel_alloc_from_image(const char* name, uint64_t name_len, const void* image, uint64_t image_len);
 CqlKernel* cqlcuda_kernel_alloc_from_image_spec(const char* name, uint64_t name_len, const void* image, uint64_t image_len,
-                                                const uint32_t* spec_values, uint32_t spec_count);    /* :204 */
-void       cqlcuda_generated_kernel_stats(uint64_t* out_compiles, uint64_t* out_evictions);            /* :205 */
-void       cqlcuda_kernel_release(CqlKernel* kernel);                                                  /* :206, kernels are cached: no-op */
-void       cqlcuda_kernel_execute(CqlKernel* kernel, uint32_t global_work_size, uint32_t local_work_size); /* :207, synchronous */
-void       cqlcuda_kernel_set_arg_buffer(CqlKernel* kernel, uint32_t index, CqlBuffer* buffer);        /* :208 */
-void       cqlcuda_kernel_set_arg_u64(CqlKernel* kernel, uint32_t index, uint64_t value);              /* :209 */
+                                                const uint32_t* spec_values, uint32_t spec_count);    /* :42 */
+void       cqlcuda_generated_kernel_stats(uint64_t* out_compiles, uint64_t* out_evictions);            /* :43 */
+void       cqlcuda_kernel_release(CqlKernel* kernel);                                                  /* :44, kernels are cached: no-op */
+void       cqlcuda_kernel_execute(CqlKernel* kernel, uint32_t global_work_size, uint32_t local_work_size); /* :45, synchronous */
+void       cqlcuda_kernel_set_arg_buffer(CqlKernel* kernel, uint32_t index, CqlBuffer* buffer);        /* :46 */
+void       cqlcuda_kernel_set_arg_u64(CqlKernel* kernel, uint32_t index, uint64_t value);              /* :47 */
 /* Binding at a byte offset into a buffer: a chunk of a resident column without a copy. Not in the
    reference vtable; the adapter uses offset 0. */
 void       cqlcuda_kernel_set_arg_buffer_range(CqlKernel* kernel, uint32_t index, CqlBuffer* buffer, uint64_t offset, uint64_t size);
 
-/* ---- batches (gpu_backend.h:211-217) ---- */
-CqlBatch* cqlcuda_batch_begin(uint64_t upload_bytes_needed, uint64_t download_bytes_needed);           /* :211 */
-void      cqlcuda_batch_buffer_write(CqlBatch* batch, CqlBuffer* buffer, const void* data, uint64_t size); /* :212 */
-void      cqlcuda_batch_buffer_zero(CqlBatch* batch, CqlBuffer* buffer, uint64_t size);                 /* :213 */
-void      cqlcuda_batch_buffer_fill(CqlBatch* batch, CqlBuffer* buffer, uint64_t size, uint32_t value);  /* :214 */
-void      cqlcuda_batch_kernel_execute(CqlBatch* batch, CqlKernel* kernel, uint32_t global_work_size, uint32_t local_work_size); /* :215 */
-void      cqlcuda_batch_buffer_read(CqlBatch* batch, CqlBuffer* buffer, void* out_data, uint64_t size);  /* :216 */
+/* ---- batches (gpu_backend.h:49-55) ---- */
+CqlBatch* cqlcuda_batch_begin(uint64_t upload_bytes_needed, uint64_t download_bytes_needed);           /* :49 */
+void      cqlcuda_batch_buffer_write(CqlBatch* batch, CqlBuffer* buffer, const void* data, uint64_t size); /* :50 */
+void      cqlcuda_batch_buffer_zero(CqlBatch* batch, CqlBuffer* buffer, uint64_t size);                 /* :51 */
+void      cqlcuda_batch_buffer_fill(CqlBatch* batch, CqlBuffer* buffer, uint64_t size, uint32_t value);  /* :52 */
+void      cqlcuda_batch_kernel_execute(CqlBatch* batch, CqlKernel* kernel, uint32_t global_work_size, uint32_t local_work_size); /* :53 */
+void      cqlcuda_batch_buffer_read(CqlBatch* batch, CqlBuffer* buffer, void* out_data, uint64_t size);  /* :54 */
 /* The same from byte `offset` of the buffer (no reference counterpart: a read of one word of a device
    array, such as the total a prefix sum leaves after its last element). */
 void      cqlcuda_batch_buffer_read_at(CqlBatch* batch, CqlBuffer* buffer, uint64_t offset, void* out_data, uint64_t size);
 /* cqlcuda_batch_buffer_fill from byte `offset` (a multiple of 4) of the buffer (no reference counterpart:
    several output arrays of one operator kept in one buffer). */
 void      cqlcuda_batch_fill_range(CqlBatch* batch, CqlBuffer* buffer, uint64_t offset, uint64_t size, uint32_t value);
-int       cqlcuda_batch_end(CqlBatch* batch);                                                            /* :217, 0 on failure (reads zero-filled) */
+int       cqlcuda_batch_end(CqlBatch* batch);                                                            /* :55, 0 on failure (reads zero-filled) */
 /* A batch for a plan shape (no reference counterpart): its writes, fills, dispatches and reads are
    recorded, and at cqlcuda_batch_end the record runs as a CUDA graph - the one captured the second time a
    batch of the same shape ended (the same operations on the same buffers with the same kernel arguments;
@@ -147,18 +148,18 @@ void      cqlcuda_graph_enable(int on);
 /* Graphs captured, replayed, and records that ran without one, since start. */
 void      cqlcuda_graph_stats(uint64_t* out_captures, uint64_t* out_replays, uint64_t* out_fallbacks);
 
-/* ---- streams (gpu_backend.h:219-229) ---- */
-CqlStream* cqlcuda_stream_alloc(uint32_t slot_count);                                                    /* :219, 1..8 slots */
-void       cqlcuda_stream_release(CqlStream* stream);                                                    /* :220 */
-int        cqlcuda_stream_slot_begin(CqlStream* stream, uint32_t slot, uint64_t upload_bytes, uint64_t readback_bytes); /* :221 */
-int        cqlcuda_stream_copy(CqlStream* stream, uint32_t slot, CqlBuffer* destination, const void* host_ptr, uint64_t size); /* :222 */
-void       cqlcuda_stream_zero(CqlStream* stream, uint32_t slot, CqlBuffer* buffer, uint64_t size);      /* :223 */
-void       cqlcuda_stream_fill(CqlStream* stream, uint32_t slot, CqlBuffer* buffer, uint64_t size, uint32_t value); /* :224 */
-void       cqlcuda_stream_dispatch(CqlStream* stream, uint32_t slot, CqlKernel* kernel, uint32_t global_work_size, uint32_t local_work_size); /* :225 */
-void       cqlcuda_stream_read(CqlStream* stream, uint32_t slot, CqlBuffer* buffer, void* out_data, uint64_t size); /* :226 */
-int        cqlcuda_stream_submit(CqlStream* stream, uint32_t slot);                                      /* :227 */
-int        cqlcuda_stream_wait(CqlStream* stream, uint32_t slot);                                        /* :228, bounded wait */
-CqlStreamStats cqlcuda_stream_get_stats(CqlStream* stream);                                              /* :229 */
+/* ---- streams (gpu_backend.h:57-67) ---- */
+CqlStream* cqlcuda_stream_alloc(uint32_t slot_count);                                                    /* :57, 1..8 slots */
+void       cqlcuda_stream_release(CqlStream* stream);                                                    /* :58 */
+int        cqlcuda_stream_slot_begin(CqlStream* stream, uint32_t slot, uint64_t upload_bytes, uint64_t readback_bytes); /* :59 */
+int        cqlcuda_stream_copy(CqlStream* stream, uint32_t slot, CqlBuffer* destination, const void* host_ptr, uint64_t size); /* :60 */
+void       cqlcuda_stream_zero(CqlStream* stream, uint32_t slot, CqlBuffer* buffer, uint64_t size);      /* :61 */
+void       cqlcuda_stream_fill(CqlStream* stream, uint32_t slot, CqlBuffer* buffer, uint64_t size, uint32_t value); /* :62 */
+void       cqlcuda_stream_dispatch(CqlStream* stream, uint32_t slot, CqlKernel* kernel, uint32_t global_work_size, uint32_t local_work_size); /* :63 */
+void       cqlcuda_stream_read(CqlStream* stream, uint32_t slot, CqlBuffer* buffer, void* out_data, uint64_t size); /* :64 */
+int        cqlcuda_stream_submit(CqlStream* stream, uint32_t slot);                                      /* :65 */
+int        cqlcuda_stream_wait(CqlStream* stream, uint32_t slot);                                        /* :66, bounded wait */
+CqlStreamStats cqlcuda_stream_get_stats(CqlStream* stream);                                              /* :67 */
 
 /* ---- failure injection, eviction hook, kernel log and profile (src/gpu/gpu.h:38-113) ---- */
 void     cqlcuda_set_fault_alloc_at(uint64_t call_index);     /* g_gpu_fault_alloc_at (gpu.h:68): the k-th allocation call fails, 0 = off */
@@ -194,11 +195,12 @@ int      cqlcuda_compile_check(const char* source, uint64_t source_len);
    entries: the dense group id of every occupied slot, the group total last), group_owner and
    group_count (up to slot_count entries), and *out_group_total on the host.
    Limit: slot_count <= 2^24 (256 KB of scratch, held by every GPU that loads the library until exit).
-   The first call on a device looks the scratch address up with that device current: make it
-   before any stream capture. All calls share the scratch; calls whose work overlaps on the GPU race.
+   cqlcuda_init looks the scratch address up and loads the kernel for the device it opens; on any other
+   device the first call does that set-up, with that device current: make it before any stream capture.
+   All calls share the scratch; calls whose work overlaps on the GPU race.
    `stream` is a cudaStream_t (NULL = the legacy default stream); the call returns once it is done.
    Returns 1, or -1 slot_count is 0 or over the limit, -2 a NULL pointer, -3 no usable device,
-   -4 a launch or copy failed. */
+   -4 a launch or copy failed; cqlcuda_last_error() then says which. */
 int      cqlcuda_compact_slots_noalloc(const uint32_t* slot_counts, const uint32_t* slot_owner, uint32_t slot_count,
                                        uint32_t* slot_group, uint32_t* group_owner, uint32_t* group_count, uint32_t* out_group_total,
                                        void* stream);
@@ -207,14 +209,19 @@ int      cqlcuda_compact_slots_noalloc(const uint32_t* slot_counts, const uint32
 /* Fills `rows` rows of a u32 column from the splitmix64 stream seeded `seed`: row r takes draw
    r*draws_per_row + draw_index (0-based) and stores draw % range (range 0 = the full 32 bits). */
 int      cqlcuda_fill_splitmix_u32(CqlBuffer* buffer, uint64_t rows, uint64_t seed, uint32_t draws_per_row, uint32_t draw_index, uint64_t range);
-/* Fills value[r] = first + r for r < rows. */
 /* Lanes (no reference counterpart): the calling thread gets its own stream, batch, kernel arguments and
    pooled-buffer namespace (pool_tag), so several threads can run operators on the device at once.
    Without a lane a thread uses the main lane: one batch at a time, as the reference's single queue.
    Pooled buffers are not evicted while any lane is open. */
 int      cqlcuda_thread_lane_begin(const char* pool_tag);
 void     cqlcuda_thread_lane_end(void);
+/* Fills value[r] = first + r for r < rows. */
 int      cqlcuda_fill_sequence_u32(CqlBuffer* buffer, uint64_t rows, uint32_t first);
+/* Fills value[r] = (r * mul + add) % modulus for r < rows, in 64-bit arithmetic, truncated to 32 bits
+   (modulus 0: no reduction). The closed-form columns of the reference's scale test
+   (src/tests/scale/bench_select_scale.c:38-56: region = r % 50, amount = r % 10000,
+   needle_key = r * 2654435761 mod 2^32) are such fills. */
+int      cqlcuda_fill_affine_u32(CqlBuffer* buffer, uint64_t rows, uint64_t mul, uint64_t add, uint64_t modulus);
 /* Writes `bytes` bytes of a scratch buffer, to evict the L2 between timed runs. */
 int      cqlcuda_flush_l2(uint64_t bytes);
 /* CUDA-event timing of everything the library enqueues between begin and end, on its own stream. */

@@ -75,6 +75,11 @@ typedef struct CqlDict
    and the smallest chunk max (cqlops_zone_map_build fills it); scans prune chunks with it. A
    sequence column needs none. */
 #define CQLOPS_ZONEMAP_CHUNK_ROWS 8192
+/* The most rows one operator call takes: row numbers and counts are 32-bit words in the kernels'
+   push constants. Every cqlops_* operator refuses a larger column (returns 0, cqlops_last_error()
+   says why) before any device work. */
+#define CQLOPS_MAX_ROWS 0xfffffffeull
+
 typedef struct CqlColumn
 {
   uint32_t type;
@@ -240,6 +245,12 @@ int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count,
 int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* args,
                       const double* params, uint64_t group_hint, uint32_t path, uint64_t max_groups, uint64_t* out_group_count,
                       uint64_t* out_repr_row, uint64_t* out_counts, double* out_results, uint32_t* out_path);
+/* The HyperLogLog registers behind the calling thread's last cqlops_group_hash: per dense group g, per
+   APPROX_COUNT_DISTINCT expression h (in expression order), 2^10 registers at ((g * hll_exprs + h) << 10),
+   each the largest rho seen (hll_add, aggregate_reduce.comp:66-92). Copies up to `capacity` words into
+   `out` (may be NULL) and returns the word count (0 when that call had no APPROX_COUNT_DISTINCT or
+   failed). */
+uint64_t cqlops_group_hash_registers(uint32_t* out, uint64_t capacity);
 /* qe_hll_estimate_cardinality (query_exec.c:6711-6737) over m registers. */
 double cqlops_hll_estimate(const uint32_t* registers, uint64_t m);
 /* qe_tdigest_estimate_percentile (query_exec.c:6748-6790); sorts the centroids in place. */

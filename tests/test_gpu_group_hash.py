@@ -104,9 +104,12 @@ def test_hll_global_matches_oracle_registers(ops, distinct):
     session = rng.integers(0, distinct, n).astype(np.uint32)
     res = ops.group_hash([], [ACD], [ops.Column.from_numpy(session)])
     assert res["groups"] == 1
+    regs = ops.group_hash_registers()
+    want_regs = oracle.hll_registers(session.astype(np.float64))
+    assert regs.shape == (1, 1024)
+    assert np.array_equal(regs[0], want_regs)          # registers bit for bit, not just the estimate
     est = res["results"][0, 0]
-    want = round(oracle.hll_estimate(oracle.hll_registers(session.astype(np.float64))))
-    assert est == want
+    assert est == round(oracle.hll_estimate(want_regs))
     true = len(np.unique(session))
     assert abs(est - true) <= HLL_BOUND * true
 
@@ -117,11 +120,32 @@ def test_hll_per_group_matches_oracle(ops):
     key = rng.integers(0, 10, n).astype(np.uint32)
     val = rng.integers(0, 50_000, n).astype(np.uint32)
     res = ops.group_hash([ops.Column.from_numpy(key)], [ACD, COUNT], [ops.Column.from_numpy(val), None])
+    regs = ops.group_hash_registers()
+    assert regs.shape == (res["groups"], 1024)
     for g in range(res["groups"]):
         k = key[int(res["repr_row"][g])]
         sel = val[key == k].astype(np.float64)
-        assert res["results"][g, 0] == round(oracle.hll_estimate(oracle.hll_registers(sel)))
+        want_regs = oracle.hll_registers(sel)
+        assert np.array_equal(regs[g], want_regs)
+        assert res["results"][g, 0] == round(oracle.hll_estimate(want_regs))
         assert res["results"][g, 1] == len(sel)
+
+
+def test_hll_two_sketches_per_group_registers(ops):
+    """Two APPROX_COUNT_DISTINCT expressions over different columns: registers laid out [group][expr][1024]."""
+    n = 500_000
+    rng = np.random.default_rng(91)
+    key = rng.integers(0, 4, n).astype(np.uint32)
+    a = rng.integers(0, 300_000, n).astype(np.uint32)
+    b = rng.normal(0.0, 1e6, n)
+    res = ops.group_hash([ops.Column.from_numpy(key)], [ACD, COUNT, ACD],
+                         [ops.Column.from_numpy(a), None, ops.Column.from_numpy(b)])
+    regs = ops.group_hash_registers()
+    assert regs.shape == (2 * res["groups"], 1024)
+    for g in range(res["groups"]):
+        sel = key == key[int(res["repr_row"][g])]
+        assert np.array_equal(regs[2 * g], oracle.hll_registers(a[sel].astype(np.float64)))
+        assert np.array_equal(regs[2 * g + 1], oracle.hll_registers(b[sel]))
 
 
 def test_hll_exact_edge_cases(ops):

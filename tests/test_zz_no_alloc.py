@@ -52,22 +52,39 @@ def reference_compact(lib, counts, owner):
     return offsets, g_owner, g_count, int(total[0])
 
 
+class NoallocCase:
+    """Inputs and outputs of one slot table in device buffers the caller owns."""
+
+    def __init__(self, lib, counts, owner):
+        self.lib, self.n = lib, len(counts)
+        n = self.n
+        self.ins = [device_buffer(lib, n * 4, counts), device_buffer(lib, n * 4, owner)]
+        self.outs = [device_buffer(lib, (n + 1) * 4), device_buffer(lib, n * 4), device_buffer(lib, n * 4)]
+
+    def run(self):
+        lib, n, ptr = self.lib, self.n, self.lib.cqlcuda_buffer_device_pointer
+        total = C.c_uint32(0)
+        rc = lib.cqlcuda_compact_slots_noalloc(ptr(self.ins[0]), ptr(self.ins[1]), n, ptr(self.outs[0]), ptr(self.outs[1]),
+                                               ptr(self.outs[2]), C.byref(total), None)
+        assert rc == 1, (rc, lib.cqlcuda_last_error())
+        offsets = np.zeros(n + 1, dtype=np.uint32)
+        g_owner = np.zeros(n, dtype=np.uint32)
+        g_count = np.zeros(n, dtype=np.uint32)
+        for b, arr in zip(self.outs, (offsets, g_owner, g_count)):
+            lib.cqlcuda_buffer_read(b, C.c_void_p(arr.ctypes.data), arr.nbytes)
+        return offsets, g_owner, g_count, total.value
+
+    def release(self):
+        for b in self.ins + self.outs:
+            self.lib.cqlcuda_buffer_release(b)
+
+
 def noalloc_compact(lib, counts, owner):
-    n = len(counts)
-    ins = [device_buffer(lib, n * 4, counts), device_buffer(lib, n * 4, owner)]
-    outs = [device_buffer(lib, (n + 1) * 4), device_buffer(lib, n * 4), device_buffer(lib, n * 4)]
-    ptr = lib.cqlcuda_buffer_device_pointer
-    total = C.c_uint32(0)
-    rc = lib.cqlcuda_compact_slots_noalloc(ptr(ins[0]), ptr(ins[1]), n, ptr(outs[0]), ptr(outs[1]), ptr(outs[2]), C.byref(total), None)
-    assert rc == 1, rc
-    offsets = np.zeros(n + 1, dtype=np.uint32)
-    g_owner = np.zeros(n, dtype=np.uint32)
-    g_count = np.zeros(n, dtype=np.uint32)
-    for b, arr in zip(outs, (offsets, g_owner, g_count)):
-        lib.cqlcuda_buffer_read(b, C.c_void_p(arr.ctypes.data), arr.nbytes)
-    for b in ins + outs:
-        lib.cqlcuda_buffer_release(b)
-    return offsets, g_owner, g_count, total.value
+    case = NoallocCase(lib, counts, owner)
+    try:
+        return case.run()
+    finally:
+        case.release()
 
 
 def slot_table(n, occupancy, seed):
@@ -92,9 +109,28 @@ def test_two_calls_in_a_row_match_the_existing_entry_point(lib):
         assert np.array_equal(got[2][:total], counts[occupied])
 
 
+def test_device_memory_does_not_move_across_calls(lib):
+    """With its buffers in place, calls after the first leave the device's free memory where it was:
+    the entry point allocates nothing and loads no module (the library's init resolved its scratch)."""
+    counts, owner = slot_table(1 << 20, 0.5, 3)
+    case = NoallocCase(lib, counts, owner)
+    try:
+        first = case.run()
+        free0 = lib.cqlcuda_device_free_memory()
+        for _ in range(3):
+            got = case.run()
+            assert got[3] == first[3]
+            assert np.array_equal(got[1][: got[3]], first[1][: first[3]])
+        assert lib.cqlcuda_device_free_memory() == free0
+    finally:
+        case.release()
+
+
 def test_rejects_sizes_past_its_limit_and_null_pointers(lib):
     dummy = C.c_void_p(1)
     total = C.c_uint32(0)
     assert lib.cqlcuda_compact_slots_noalloc(dummy, dummy, (1 << 24) + 1, dummy, dummy, dummy, C.byref(total), None) == -1
+    assert b"it takes 1 to 16777216" in lib.cqlcuda_last_error()
     assert lib.cqlcuda_compact_slots_noalloc(dummy, dummy, 0, dummy, dummy, dummy, C.byref(total), None) == -1
     assert lib.cqlcuda_compact_slots_noalloc(None, dummy, 16, dummy, dummy, dummy, C.byref(total), None) == -2
+    assert b"NULL pointer" in lib.cqlcuda_last_error()
