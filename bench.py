@@ -136,6 +136,100 @@ def make_queries(ops, t, rng_key, dims):
             ("join_dim1m_group_by_seg", 4 * n, q7)]
 
 
+def parity_checks(ops, t, queries, dims, key):
+    """The suite's answers, checked once outside the timed region; returns (status, checks run).
+
+    1. Seed-0 table: every query's result against another kernel path over the same columns - the
+       dense group-bys' totals against the global aggregate, the filter count against a dense
+       GROUP BY flag, the dim50 join against GROUP BY region's groups of the kept regions, the dim1M
+       join grouped by seg against GROUP BY amount folded through dim1M's seg, and the point lookup's
+       row against its key.
+    2. The reference's closed-form scale table at the same size (src/tests/scale/bench_select_scale.c:
+       38-56, filled on the device) against the reference's own known answers (:97-167, cases
+       :1085-1170): SUM/MIN/MAX, the 0.1 % and 2 % filters, the id lookup, GROUP BY region, GROUP BY
+       amount, the filtered join to its 50-row table and the join to its 10k-row table grouped by
+       category.
+    """
+    import numpy as np
+    from tests import closed_form as cf
+    n = t.rows
+    d50, d1m = dims
+    got = {name: q() for name, _, q in queries}
+    checks = []
+
+    def check(name, ok):
+        checks.append(name)
+        if not ok:
+            raise AssertionError(name)
+
+    try:
+        s, mn, mx = got["sum_min_max_amount"]
+        mk3, c3, s3, _, _ = got["group_by_region"]
+        check("group_by_region counts total rows", int(c3.sum()) == n)
+        check("group_by_region sums total SUM(amount)", float(s3[:, 0].sum()) == s[0])
+        mk4, c4, s4, _, _ = got["group_by_amount_10k"]
+        rs, _, _ = ops.aggregate_global([t.region])
+        check("group_by_amount counts total rows", int(c4.sum()) == n)
+        check("group_by_amount sums total SUM(region)", float(s4[:, 1].sum()) == rs[0])
+        present = np.nonzero(c4)[0]
+        check("MIN/MAX(amount) are the extreme amount groups", (mn[0], mx[0]) == (float(mk4 + present[0]), float(mk4 + present[-1])))
+        check("amount groups are their values x counts", float((c4.astype(np.float64) * (mk4 + np.arange(len(c4)))).sum()) == s[0])
+        mkf, cf_, _, _, _ = ops.group_dense(t.flag, [ops.FUNC_COUNT], [None])
+        check("count flag < 2 equals GROUP BY flag's groups 0 and 1", got["count_flag_lt_2"][0] == int(cf_[: 2 - int(mkf)].sum()))
+        cnt, rows = got["point_lookup_id"]
+        check("point lookup finds its one row", cnt == 1 and list(rows) == [key])
+        kept = np.nonzero(d50["name_id"] == 3)[0]
+        r6 = got["join_dim50_filtered"]["results"]
+        check("dim50 join equals GROUP BY region over the kept regions",
+              (r6[0, 0], r6[0, 1]) == (float(c3[kept - mk3].sum()), float(s3[kept - mk3, 0].sum())))
+        r7 = got["join_dim1m_group_by_seg"]
+        amounts = mk4 + np.arange(len(c4))
+        seg_of = d1m["seg"][amounts % 1_000_000]
+        for g in range(r7["groups"]):
+            seg = d1m["seg"][int(r7["dim_row"][g])]
+            sel = seg_of == seg
+            want = (float((c4[sel].astype(np.float64) * amounts[sel]).sum()), float(c4[sel].sum()))
+            check(f"dim1M join seg {seg} equals GROUP BY amount folded by seg", (r7["results"][g, 0], r7["results"][g, 1]) == want)
+
+        # the reference's closed-form table and known answers at the same row count
+        cols = {"id": ops.Column.sequence(n, 1), "region": ops.Column.affine(n, 1, 0, cf.REGIONS),
+                "amount": ops.Column.affine(n, 1, 0, cf.AMOUNT_RANGE)}
+        try:
+            e = cf.expected(n)
+            s, mn, mx = ops.aggregate_global([cols["amount"]])
+            check("closed form SUM/MIN/MAX(amount)", [s[0], mn[0], mx[0]] == e["sum_min_max_amount"])
+            check("closed form COUNT amount > 9990", ops.scan_simple([cols["amount"]], [(0, ops.CMP_GT, cf.HIGH_AMOUNT)])[0] == e["count_amount_gt_9990"])
+            check("closed form COUNT region = 7", ops.scan_simple([cols["region"]], [(0, ops.CMP_EQ, 7)])[0] == e["count_region_eq_7"])
+            row = cf.needle_row(n)
+            cnt, rows = ops.scan_simple([cols["id"]], [(0, ops.CMP_EQ, row + 1)], want_rows=True, max_rows=16)
+            check("closed form id lookup", cnt == 1 and list(rows) == [row])
+            mk, c, sm, _, _ = ops.group_dense(cols["region"], [ops.FUNC_COUNT, ops.FUNC_SUM], [None, cols["amount"]])
+            want = np.array(e["group_region"], dtype=np.float64)
+            check("closed form GROUP BY region", mk == 0 and np.array_equal(c.astype(np.float64), want[:, 1]) and np.array_equal(sm[:, 1].astype(np.float64), want[:, 2]))
+            mk, c, sm, _, _ = ops.group_dense(cols["amount"], [ops.FUNC_COUNT, ops.FUNC_SUM], [None, cols["region"]])
+            want = np.array(e["group_amount"], dtype=np.int64)
+            check("closed form GROUP BY amount", mk == 0 and np.array_equal(c.astype(np.int64), want[:, 1]) and np.array_equal(sm[:, 1], want[:, 2]))
+            regions_k = np.arange(50, dtype=np.uint32)
+            r = ops.join_aggregate(cols["region"], [ops.FUNC_COUNT, ops.FUNC_SUM], [None, cols["amount"]], regions_k,
+                                   dim_rows=np.nonzero(regions_k // 10 == 2)[0])
+            check("closed form join regions zone 2", [r["results"][0, 0], r["results"][0, 1]] == [float(x) for x in e["join_zone2"]])
+            products_k = np.arange(cf.AMOUNT_RANGE, dtype=np.uint32)
+            category = (products_k % 20).astype(np.float64)
+            r = ops.join_aggregate(cols["amount"], [ops.FUNC_COUNT], [None], products_k, group_values=[category])
+            ok = r["groups"] == 20
+            for g in range(r["groups"]):
+                cat = int(category[int(r["dim_row"][g])])
+                ok = ok and r["results"][g, 0] == sum(cf.amount_rows(n, a) for a in range(cat, cf.AMOUNT_RANGE, 20))
+            check("closed form join products GROUP BY category", ok)
+        finally:
+            for c in cols.values():
+                if c.buffer is not None:
+                    c.buffer.close()
+    except AssertionError as err:
+        return f"failed: {err}", len(checks)
+    return "ok", len(checks)
+
+
 def measured_traffic(kernel, rows):
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary (bytes per row, captured
     at 100M rows), scaled to `rows`; None when no capture covers the kernel."""
@@ -248,7 +342,8 @@ def main():
     t = workloads.fact_table(args.rows)
     import numpy as np
     key = np.random.default_rng(1234 + rank).integers(0, args.rows)
-    queries = make_queries(ops, t, key, workloads.dim_tables())
+    dims = workloads.dim_tables()
+    queries = make_queries(ops, t, key, dims)
 
     for _ in range(args.warmup):
         for _, _, q in queries:
@@ -338,6 +433,8 @@ def main():
                         "main_kernel": main_kernel.get(name)}
     kernels = {k: {"ms_avg": ns / c / 1e6, "launches": c} for k, (ns, c) in prof.items()}
 
+    parity, parity_checks_run = parity_checks(ops, t, queries, dims, key)
+
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(args, native, ops, t, queries, lib)
@@ -354,6 +451,7 @@ def main():
                                        f"{len(queries)}-query suite",
                            "rows": args.rows, "queries": [q[0] for q in queries], "l2": "inputs larger than L2 (4 GB columns)",
                            "parallelism": f"replicas x{world}"},
+                "parity": parity, "parity_checks": parity_checks_run,
                 "gpu_launches": launches, "queries": qstats, "kernels": kernels, "roofline": roofline, "clocks": clk,
                 "e2e": e2e, "cpu_baseline": cpu}
         print(json.dumps(line))
