@@ -69,6 +69,29 @@ static int condition_ok(const char* c, uint32_t column_count)
   return 1;
 }
 
+int cqlops_having_source(const char* condition, uint32_t column_count, char* out, uint64_t cap, uint64_t* out_len)
+{
+  if (!condition || column_count > HAVING_MAX_COLUMNS) return refuse("HAVING takes up to 8 result columns");
+  if (!condition_ok(condition, column_count))
+    return refuse("the HAVING condition may use only v0..v7, lit[i], numbers, operators and fabs/fmin/fmax/floor/ceil/sqrt/isnan");
+  /* the kernel: one group per thread over a persistent grid; binding 0 keep, 1 literals, 2 + c column c */
+  uint64_t need = strlen(condition) + 1024 + 64 * column_count;
+  if (cap < need) return refuse("the HAVING source buffer is too small");
+  int len = snprintf(out, cap,
+                     "// cql: block=256 smem=0 per_sm=8\n"
+                     "typedef unsigned int u32;\ntypedef unsigned long long u64;\n"
+                     "struct CqlLaunch { void* buf[16]; u64 bytes[16]; u64 push[8]; };\n"
+                     "extern \"C\" __global__ void __launch_bounds__(256) cql_main(CqlLaunch a)\n{\n"
+                     "  u32* keep = (u32*)a.buf[0]; const double* lit = (const double*)a.buf[1]; (void)lit;\n"
+                     "  const u64 n = a.push[0];\n"
+                     "  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x)\n  {\n");
+  for (uint32_t c = 0; c < column_count; c++)
+    len += snprintf(out + len, cap - (uint64_t)len, "    const double v%u = ((const double*)a.buf[%u])[i];\n", c, 2 + c);
+  len += snprintf(out + len, cap - (uint64_t)len, "    keep[i] = (%s) ? 1u : 0u;\n  }\n}\n", condition);
+  if (out_len) *out_len = (uint64_t)len;
+  return 1;
+}
+
 int cqlops_having(const char* condition, const double* literals, uint32_t literal_count, const double* const* columns, uint32_t column_count,
                   uint64_t group_count, uint32_t* out_keep)
 {
@@ -79,19 +102,14 @@ int cqlops_having(const char* condition, const double* literals, uint32_t litera
     return refuse("the HAVING condition may use only v0..v7, lit[i], numbers, operators and fabs/fmin/fmax/floor/ceil/sqrt/isnan");
   if (group_count == 0) return 1;
   if (group_count >= 0xffffffffull) return refuse("too many groups");
-  /* the kernel: one group per thread over a persistent grid */
   char* src = (char*)malloc(strlen(condition) + 2048);
   if (!src) return 0;
-  int len = sprintf(src,
-                    "// cql: block=256 smem=0 per_sm=8\n"
-                    "typedef unsigned int u32;\ntypedef unsigned long long u64;\n"
-                    "struct CqlLaunch { void* buf[16]; u64 bytes[16]; u64 push[8]; };\n"
-                    "extern \"C\" __global__ void __launch_bounds__(256) cql_main(CqlLaunch a)\n{\n"
-                    "  u32* keep = (u32*)a.buf[0]; const double* lit = (const double*)a.buf[1]; (void)lit;\n"
-                    "  const u64 n = a.push[0];\n"
-                    "  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x)\n  {\n");
-  for (uint32_t c = 0; c < column_count; c++) len += sprintf(src + len, "    const double v%u = ((const double*)a.buf[%u])[i];\n", c, 2 + c);
-  sprintf(src + len, "    keep[i] = (%s) ? 1u : 0u;\n  }\n}\n", condition);
+  uint64_t src_len = 0;
+  if (!cqlops_having_source(condition, column_count, src, strlen(condition) + 2048, &src_len))
+  {
+    free(src);
+    return 0;
+  }
   uint64_t h = 1469598103934665603ull;
   for (const char* p = src; *p; p++) h = (h ^ (unsigned char)*p) * 1099511628211ull;
   char name[48];

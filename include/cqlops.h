@@ -362,6 +362,11 @@ int cqlops_gather_strings(const CqlColumn* column, const uint32_t* rows, CqlBuff
    the result columns, as doubles) and lit[0..15] (the literals), in C syntax (&&, ||, !, comparisons,
    arithmetic, fabs/fmin/fmax/floor/ceil/sqrt/isnan); out_keep[i] = 1 when group i passes. Conditions that
    differ only in their literals share one compiled kernel. Refuses a condition with anything else. */
+/* The CUDA C++ source of the HAVING kernel for a condition over v0..v(column_count-1) and lit[]
+   (qk_having_kernel, query_kernel.c:2530-2575): binding 0 keep (u32 per group), 1 the literals (f64),
+   2 + c result column c (f64), push slot 0 the group count. Returns 0 when the condition uses anything
+   but v0..v7, lit[i], numbers, operators and fabs/fmin/fmax/floor/ceil/sqrt/isnan, or cap is short. */
+int cqlops_having_source(const char* condition, uint32_t column_count, char* out, uint64_t cap, uint64_t* out_len);
 int cqlops_having(const char* condition, const double* literals, uint32_t literal_count, const double* const* columns, uint32_t column_count,
                   uint64_t group_count, uint32_t* out_keep);
 
