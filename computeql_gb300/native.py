@@ -194,6 +194,7 @@ OPS_API = [
     ("cqlops_sort_rows", C.c_int, [P, u32, P, P, u64, P, u64]),
     ("cqlops_window_rank", C.c_int, [P, u32, P, u32, P, u64, P, P, P, P, u64]),
     ("cqlops_having", C.c_int, [cstr, P, u32, P, u32, u64, P]),
+    ("cqlops_having_source", C.c_int, [cstr, u32, P, u64, P]),
     ("cqlops_gather_rows", C.c_int, [P, u32, P, P, u64, P]),
     ("cqlops_gather_strings", C.c_int, [P, P, P, u64, P, P, u64, P]),
     ("cqlops_fixed_scale", C.c_int, [P, P, u64, P, P]),
