@@ -106,6 +106,7 @@ CUDA_API = [
     ("cqlcuda_device_max_storage_buffer_range", u64, []),
     ("cqlcuda_device_lost", C.c_int, []),
     ("cqlcuda_pool_begin_epoch", None, []),
+    ("cqlcuda_pool_evict", u64, [u64]),
     ("cqlcuda_memory_stats", CqlMemoryStats, []),
     ("cqlcuda_sm_count", u32, []),
     ("cqlcuda_buffer_alloc", P, [u64, u32, P]),

@@ -89,6 +89,11 @@ uint64_t cqlcuda_device_free_memory(void);                     /* gpu_backend.h:
 uint64_t cqlcuda_device_max_storage_buffer_range(void);        /* gpu_backend.h:27 */
 int      cqlcuda_device_lost(void);                            /* gpu_backend.h:28 */
 void     cqlcuda_pool_begin_epoch(void);                       /* gpu_backend.h:29 */
+/* Frees pooled buffers not used in the current epoch, least recently used first, until `bytes_wanted`
+   are freed (UINT64_MAX: all of them); returns the bytes freed. gpu_vulkan_pool_evict
+   (src/gpu/vulkan/gpu_vulkan.c:1577-1617), which the reference's failure tests call to start each run
+   cold (src/tests/bench_alloc_fault.c:236-241). Does nothing while a batch is open or a lane is open. */
+uint64_t cqlcuda_pool_evict(uint64_t bytes_wanted);
 CqlMemoryStats cqlcuda_memory_stats(void);                     /* gpu_backend.h:30 */
 uint32_t cqlcuda_sm_count(void);                               /* device property the kernels size grids by */
 

@@ -242,6 +242,39 @@ def gather_column(stored, rows, width=0, base=0):
     return v
 
 
+NO_ROW = 0xFFFFFFFF
+
+
+def selection_gather(mode, rows, source, positions, count, stride=1, row_offset=0, map_stride=1, word_offset=0, map_offset=0):
+    """selection_gather.comp:28-78 for `count` invocations, in 32-bit arithmetic. Modes: 0 an f64 (two
+    words) per row, 1 a 32-bit word per row, 2 rows through positions, 3 resolve through a map, 4 resolve
+    with an offset. rows/source/positions are u32 word arrays; returns the destination words."""
+    rows = np.asarray(rows, dtype=np.uint32)
+    src = np.asarray(source, dtype=np.uint32) if source is not None else None
+    out = np.zeros(count * (2 if mode == 0 else 1), dtype=np.uint32)
+    add = lambda a, b: np.uint32((int(a) + int(b)) & 0xFFFFFFFF)
+    for i in range(count):
+        if mode == 2:
+            index = rows[int(positions[i]) * stride + word_offset]
+            out[i] = NO_ROW if index == NO_ROW else add(index, row_offset)
+            continue
+        index = rows[i * stride + word_offset]
+        if mode == 4:
+            out[i] = NO_ROW if index == NO_ROW else add(index, row_offset)
+        elif mode == 3:
+            mapped = NO_ROW if index == NO_ROW else src[int(index) * map_stride]
+            out[i] = NO_ROW if mapped == NO_ROW else add(mapped, map_offset)
+        else:
+            has = index != NO_ROW
+            row = int(add(index, row_offset))
+            if mode == 0:
+                out[2 * i] = src[2 * row] if has else 0
+                out[2 * i + 1] = src[2 * row + 1] if has else 0
+            else:
+                out[i] = src[row] if has else 0
+    return out
+
+
 def gather_strings(values, rows):
     """The selected rows of a string column, as bytes."""
     return [values[int(i)] for i in rows]
