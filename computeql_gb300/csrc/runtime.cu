@@ -534,15 +534,6 @@ extern "C" uint64_t cqlcuda_device_free_memory(void)
 extern "C" uint64_t cqlcuda_device_max_storage_buffer_range(void) { return cqlcuda_device_total_memory(); }
 extern "C" int cqlcuda_device_lost(void) { return S().device_lost; }
 extern "C" void cqlcuda_pool_begin_epoch(void) { S().pool_epoch += 1; }
-
-extern "C" uint64_t cqlcuda_pool_evict(uint64_t bytes_wanted)
-{
-  CqlState& s = S();
-  std::lock_guard<std::recursive_mutex> g(s.lock);
-  if (!s.initialized) return 0;
-  cudaStreamSynchronize(s.stream);
-  return pool_evict(bytes_wanted);
-}
 extern "C" CqlMemoryStats cqlcuda_memory_stats(void) { return S().mem; }
 extern "C" uint32_t cqlcuda_sm_count(void) { ensure_init(); return (uint32_t)g_cql_sm_count; }
 
@@ -576,6 +567,15 @@ static uint64_t pool_evict(uint64_t bytes_wanted)
     s.mem.pool_evicted_bytes += charge;
   }
   return freed;
+}
+
+extern "C" uint64_t cqlcuda_pool_evict(uint64_t bytes_wanted)
+{
+  CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
+  if (!s.initialized) return 0;
+  cudaStreamSynchronize(s.stream);
+  return pool_evict(bytes_wanted);
 }
 
 // The k-th allocation call fails when fault_alloc_at == k (gpu_vulkan_fault_injected, gpu_vulkan.c:1619-1631).
