@@ -480,39 +480,76 @@ def main():
 
 
 def run_e2e(args, native, ops, t, queries, lib):
-    """The suite from pinned host buffers: upload region/amount/flag, run, read results, every step."""
+    """The suite from page-locked HOST buffers, every step: region, amount and flag uploaded, the seven
+    queries run, their results read back. Uploads go through the backend's stream slots (the reference's
+    GPU_Stream, one copy a slot) and overlap the queries: the upload of the next column runs while the
+    queries that need only the columns already on the device run on the main lane."""
     import ctypes as C
-    import torch
     n = args.rows
     host = {}
     for name in ("region", "amount", "flag"):
         col = getattr(t, name)
-        h = torch.empty(n, dtype=torch.int32, pin_memory=True)
-        lib.cqlcuda_buffer_read(col.buffer.handle, C.c_void_p(h.data_ptr()), n * 4)
+        # the host copy of the column: page-locked memory from the backend (on the GPU's host node)
+        h = lib.cqlcuda_host_alloc(n * 4)
+        if not h:
+            raise RuntimeError("e2e: cqlcuda_host_alloc failed: " + native.last_error())
+        lib.cqlcuda_buffer_read(col.buffer.handle, C.c_void_p(h), n * 4)
         host[name] = h
+    by_name = {name: q for name, _, q in queries}
+    # columns in upload order, each with the queries that can run once it (and those before it) arrived
+    plan = [("amount", ["sum_min_max_amount", "join_dim1m_group_by_seg"]),
+            ("region", ["group_by_region", "group_by_amount_10k", "join_dim50_filtered", "point_lookup_id"]),
+            ("flag", ["count_flag_lt_2"])]
+    assert sorted(q for _, qs in plan for q in qs) == sorted(by_name)
+    stream = lib.cqlcuda_stream_alloc(len(plan))
+    if not stream:
+        raise RuntimeError("e2e: cqlcuda_stream_alloc failed: " + native.last_error())
+
+    def upload(slot):
+        name = plan[slot][0]
+        ok = lib.cqlcuda_stream_slot_begin(stream, slot, n * 4, 0)
+        ok = ok and lib.cqlcuda_stream_copy(stream, slot, getattr(t, name).buffer.handle, C.c_void_p(host[name]), n * 4)
+        ok = ok and lib.cqlcuda_stream_submit(stream, slot)
+        if not ok:
+            raise RuntimeError("e2e upload failed: " + native.last_error())
+
     h2d = 3 * n * 4
-    times, uploads = [], []
+    times = []
     for i in range(args.warmup + max(2, args.steps // 2)):
         t0 = time.perf_counter()
-        batch = lib.cqlcuda_batch_begin(h2d, 0)
-        for name in ("region", "amount", "flag"):
-            lib.cqlcuda_batch_buffer_write(batch, getattr(t, name).buffer.handle, C.c_void_p(host[name].data_ptr()), n * 4)
-        if not lib.cqlcuda_batch_end(batch):
-            raise RuntimeError("e2e upload failed: " + native.last_error())
-        t1 = time.perf_counter()
-        for _, _, q in queries:
-            q()
+        upload(0)
+        for slot, (_, names) in enumerate(plan):
+            if not lib.cqlcuda_stream_wait(stream, slot):
+                raise RuntimeError("e2e upload failed: " + native.last_error())
+            if slot + 1 < len(plan):
+                upload(slot + 1)
+            for q in names:
+                by_name[q]()
         dt = time.perf_counter() - t0
         if i >= args.warmup:
             times.append(dt)
-            uploads.append(t1 - t0)
+    lib.cqlcuda_stream_release(stream)
+    # the uploads alone, one after another, for the link rate
+    uploads = []
+    stream = lib.cqlcuda_stream_alloc(1)
+    for i in range(2):
+        t0 = time.perf_counter()
+        for name, _ in plan:
+            lib.cqlcuda_stream_slot_begin(stream, 0, n * 4, 0)
+            lib.cqlcuda_stream_copy(stream, 0, getattr(t, name).buffer.handle, C.c_void_p(host[name]), n * 4)
+        lib.cqlcuda_stream_submit(stream, 0)
+        lib.cqlcuda_stream_wait(stream, 0)
+        uploads.append(time.perf_counter() - t0)
+    lib.cqlcuda_stream_release(stream)
+    for h in host.values():
+        lib.cqlcuda_host_free(C.c_void_p(h))
     ms = statistics.median(times) * 1e3
-    upload_ms = statistics.median(uploads) * 1e3
+    upload_ms = min(uploads) * 1e3
     # results read back per step: partials/counters/group arrays of the queries (a few hundred KB)
     d2h = 2048 * 3 * 8 + 8 + 50 * 4 * 8 + 10000 * 4 * 8 + 8 + 2 * 8 + 20 * 2 * 8
     return {"value": len(queries) * n / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "upload_ms": upload_ms, "h2d_GBps": h2d / (upload_ms / 1e3) / 1e9}
-
+            "d2h_bytes_per_step": d2h, "upload_ms": upload_ms, "h2d_GBps": h2d / (upload_ms / 1e3) / 1e9,
+            "overlap": "each column's upload overlaps the queries over the columns already uploaded"}
 
 if __name__ == "__main__":
     sys.exit(main())

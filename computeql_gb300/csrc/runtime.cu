@@ -27,6 +27,9 @@
 #include <thread>
 #include <unordered_map>
 #include <vector>
+#include <sys/mman.h>
+#include <sys/syscall.h>
+#include <unistd.h>
 
 int g_cql_sm_count = 152;
 int g_cql_max_smem_optin = 227 * 1024;
@@ -59,6 +62,8 @@ struct CqlKernel
   std::string name;
   CqlLauncher builtin;        // precompiled kernel family
   cudaKernel_t generated;     // NVRTC-built kernel, launched with CqlLaunch by value
+  cudaLibrary_t library;      // the module a generated kernel lives in (unloaded when it is evicted)
+  uint64_t last_use;          // tick of its last lookup, for the generated-kernel cap
   uint32_t gen_block;         // block size a generated kernel declares (256 unless its source says otherwise)
   uint32_t gen_smem;          // dynamic shared memory a generated kernel asks for
   uint32_t gen_per_sm;        // resident CTAs per SM the grid is sized for
@@ -124,6 +129,8 @@ struct CqlGraphEntry
   uint64_t in_size, out_size;
   uint32_t kernels;
   uint64_t last_use;
+  uint64_t plan_key;
+  std::vector<CqlOp> ops;   // the record it was captured from: a fingerprint hit must equal it
 };
 
 struct CqlBatch
@@ -202,6 +209,9 @@ struct CqlState
   std::unordered_map<std::string, CqlKernel*> kernels;
   uint64_t generated_compiles;
   uint64_t generated_evictions;
+  uint32_t generated_cap;                // generated kernels kept loaded (GPU_VULKAN_MAX_GENERATED_KERNELS)
+  uint64_t kernel_tick;
+  std::vector<CqlKernel*> retired;       // evicted kernels: their objects stay valid, their modules are gone
   std::string cache_dir;
   uint32_t fail_compile_every;
   uint64_t compile_attempts;
@@ -224,6 +234,13 @@ struct CqlState
   std::recursive_mutex lock;
 };
 
+// Generated kernels kept loaded, as the reference's GPU_VULKAN_MAX_GENERATED_KERNELS (default 64, at least
+// 8, src/gpu/vulkan/gpu_vulkan.c:75); the least recently looked-up one is evicted past the cap
+// (:2721-2737). The 8 most recently looked-up kernels are never evicted: an operator looks up the few
+// kernels it launches just before it launches them.
+#define CQL_GENERATED_KERNEL_CAP 64
+#define CQL_GENERATED_KERNEL_MIN_CAP 8
+
 static CqlState* g_state = nullptr;
 
 static CqlState& S()
@@ -238,6 +255,8 @@ static CqlState& S()
     g_state->fault_alloc_at = 0;
     g_state->generated_compiles = 0;
     g_state->generated_evictions = 0;
+    g_state->generated_cap = CQL_GENERATED_KERNEL_CAP;
+    g_state->kernel_tick = 0;
     g_state->fail_compile_every = 0;
     g_state->compile_attempts = 0;
     g_state->profile_enabled = 0;
@@ -496,7 +515,13 @@ extern "C" void cqlcuda_release(void)
   }
   s.pool.clear();
   s.pool_index.clear();
-  for (auto& kv : s.kernels) delete kv.second;
+  for (auto& kv : s.kernels)
+  {
+    if (kv.second->library) cudaLibraryUnload(kv.second->library);
+    delete kv.second;
+  }
+  for (CqlKernel* k : s.retired) delete k;
+  s.retired.clear();
   s.kernels.clear();
   staging_release(s.main_lane.batch.staging);
   if (s.flush_buf) cudaFree(s.flush_buf);
@@ -839,6 +864,8 @@ static CqlKernel* kernel_new(const std::string& name)
   k->name = name;
   k->builtin = nullptr;
   k->generated = nullptr;
+  k->library = nullptr;
+  k->last_use = 0;
   k->gen_block = 256;
   k->gen_smem = 0;
   k->gen_per_sm = 4;
@@ -856,7 +883,11 @@ extern "C" CqlKernel* cqlcuda_kernel_alloc(const char* name, uint64_t name_len)
   if (!ensure_init()) return nullptr;
   std::string key(name, name_len);
   auto it = s.kernels.find(key);
-  if (it != s.kernels.end()) return it->second;
+  if (it != s.kernels.end())
+  {
+    if (it->second->generated) it->second->last_use = ++s.kernel_tick;
+    return it->second;
+  }
   const CqlKernelDesc* d = find_builtin(key);
   if (!d)
   {
@@ -976,6 +1007,50 @@ static std::vector<char> compile_nvrtc(const std::string& src, const std::string
   return cubin;
 }
 
+static void graphs_drop_kernel(const CqlKernel* k);
+
+// Evicts the least recently looked-up generated kernels until at most generated_cap stay loaded. Not
+// while the main lane's batch is open (its dispatches may name any kernel; the next compile outside a
+// batch catches up), and never one of the 8 most recently looked-up. The GPU is drained first, every
+// plan graph that launches the kernel is dropped, and its module is unloaded; the kernel object stays
+// valid (a stale handle fails its dispatch with an error instead of launching freed code).
+static void generated_evict_over_cap(void)
+{
+  CqlState& s = S();
+  if (s.main_lane.batch.active) return;
+  for (;;)
+  {
+    uint32_t loaded = 0;
+    CqlKernel* victim = nullptr;
+    for (auto& kv : s.kernels)
+    {
+      CqlKernel* k = kv.second;
+      if (!k->generated) continue;
+      loaded += 1;
+      if (k->last_use + CQL_GENERATED_KERNEL_MIN_CAP > s.kernel_tick) continue;
+      if (!victim || k->last_use < victim->last_use) victim = k;
+    }
+    if (loaded <= s.generated_cap || !victim) return;
+    cudaDeviceSynchronize();
+    graphs_drop_kernel(victim);
+    if (victim->library) cudaLibraryUnload(victim->library);
+    cudaGetLastError();
+    victim->library = nullptr;
+    victim->generated = nullptr;
+    s.kernels.erase(victim->name);
+    s.retired.push_back(victim);
+    s.generated_evictions += 1;
+  }
+}
+
+extern "C" void cqlcuda_set_generated_kernel_cap(uint32_t cap)
+{
+  CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
+  s.generated_cap = cap < CQL_GENERATED_KERNEL_MIN_CAP ? CQL_GENERATED_KERNEL_MIN_CAP : cap;
+  if (s.initialized) generated_evict_over_cap();
+}
+
 extern "C" CqlKernel* cqlcuda_kernel_alloc_from_image_spec(const char* name, uint64_t name_len, const void* image, uint64_t image_len,
                                                           const uint32_t* spec_values, uint32_t spec_count)
 {
@@ -994,7 +1069,11 @@ extern "C" CqlKernel* cqlcuda_kernel_alloc_from_image_spec(const char* name, uin
     }
   }
   auto it = s.kernels.find(key);
-  if (it != s.kernels.end()) return it->second;
+  if (it != s.kernels.end())
+  {
+    if (it->second->generated) it->second->last_use = ++s.kernel_tick;
+    return it->second;
+  }
   if (!image || image_len == 0)
   {
     return nullptr;  // lookup only (src/gpu/gpu.h:129-130)
@@ -1026,9 +1105,15 @@ extern "C" CqlKernel* cqlcuda_kernel_alloc_from_image_spec(const char* name, uin
   cudaLibrary_t lib = nullptr;
   if (!note_cuda(cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0), "cudaLibraryLoadData")) return nullptr;
   cudaKernel_t kfn = nullptr;
-  if (!note_cuda(cudaLibraryGetKernel(&kfn, lib, "cql_main"), "cudaLibraryGetKernel(cql_main)")) return nullptr;
+  if (!note_cuda(cudaLibraryGetKernel(&kfn, lib, "cql_main"), "cudaLibraryGetKernel(cql_main)"))
+  {
+    cudaLibraryUnload(lib);
+    return nullptr;
+  }
   CqlKernel* k = kernel_new(key);
   k->generated = kfn;
+  k->library = lib;
+  k->last_use = ++s.kernel_tick;
   if (!src.empty()) parse_generated_policy(src, k);
   if (k->gen_smem > 48 * 1024)
   {
@@ -1040,6 +1125,7 @@ extern "C" CqlKernel* cqlcuda_kernel_alloc_from_image_spec(const char* name, uin
     k->spec_count = spec_count;
   }
   s.kernels[key] = k;
+  generated_evict_over_cap();
   return k;
 }
 
@@ -1125,6 +1211,11 @@ static int dispatch_args(CqlKernel* k, const CqlLaunch& args, uint32_t gws, uint
     cudaEventRecord(t.start, stream);
   }
   int rc = 0;
+  if (!k->builtin && !k->generated)
+  {
+    set_error("cqlcuda: kernel '%s' was evicted from the generated-kernel cache; look it up again", k->name.c_str());
+    return 0;
+  }
   if (k->builtin)
   {
     rc = k->builtin(args, gws, lws, stream);
@@ -1509,6 +1600,44 @@ static void graph_entry_free(CqlGraphEntry& e)
   if (e.out) cudaFreeHost(e.out);
   e.exec = nullptr;
   e.in = e.out = nullptr;
+  e.ops.clear();
+}
+
+// a fingerprint hit replays only when the record is the captured one, field by field (everything the
+// fingerprint covers; the callers' destinations and the bytes written may differ)
+static bool record_equals(const CqlBatch* b, const CqlGraphEntry& e)
+{
+  if (b->plan_key != e.plan_key || b->out_bytes != e.out_size || b->in_bytes.size() != e.in_size || b->ops.size() != e.ops.size()) return false;
+  for (size_t i = 0; i < b->ops.size(); i++)
+  {
+    const CqlOp& x = b->ops[i];
+    const CqlOp& y = e.ops[i];
+    void* dx = x.buffer ? x.buffer->dptr : nullptr;
+    void* dy = y.buffer ? y.buffer->dptr : nullptr;
+    if (x.kind != y.kind || dx != dy || x.offset != y.offset || x.size != y.size || x.value != y.value || x.at != y.at) return false;
+    if (x.kind == CQL_OP_KERNEL &&
+        (x.kernel != y.kernel || x.gws != y.gws || x.lws != y.lws || memcmp(&x.launch, &y.launch, sizeof(CqlLaunch)) != 0))
+      return false;
+  }
+  return true;
+}
+
+// plan graphs that launch an evicted kernel go with it (graphs live on the main lane only)
+static void graphs_drop_kernel(const CqlKernel* k)
+{
+  CqlLane& l = S().main_lane;
+  for (auto it = l.graphs.begin(); it != l.graphs.end();)
+  {
+    bool uses = false;
+    for (const CqlOp& o : it->second.ops)
+      if (o.kind == CQL_OP_KERNEL && o.kernel == k) uses = true;
+    if (uses)
+    {
+      graph_entry_free(it->second);
+      it = l.graphs.erase(it);
+    }
+    else ++it;
+  }
 }
 
 static void graph_copy_out(CqlBatch* b, const CqlGraphEntry& e)
@@ -1530,6 +1659,13 @@ static void graph_end(CqlBatch* b, CqlLane& l)
   }
   uint64_t fp = record_fingerprint(b);
   auto it = l.graphs.find(fp);
+  if (it != l.graphs.end() && !record_equals(b, it->second))
+  {
+    // two shapes with one fingerprint: the newcomer runs eagerly, the captured graph stays
+    if (!issue_ops(b, l.stream, nullptr, nullptr, nullptr)) b->failed = 1;
+    b->recording = 0;
+    return;
+  }
   if (it != l.graphs.end())
   {
     CqlGraphEntry& e = it->second;
@@ -1555,10 +1691,11 @@ static void graph_end(CqlBatch* b, CqlLane& l)
     b->recording = 0;
     return;
   }
-  CqlGraphEntry e;
-  memset(&e, 0, sizeof(e));
+  CqlGraphEntry e{};
   e.in_size = b->in_bytes.size();
   e.out_size = b->out_bytes;
+  e.plan_key = b->plan_key;
+  e.ops = b->ops;
   bool pinned = cudaHostAlloc((void**)&e.in, std::max<uint64_t>(e.in_size, 16), cudaHostAllocDefault) == cudaSuccess &&
                 cudaHostAlloc((void**)&e.out, std::max<uint64_t>(e.out_size, 16), cudaHostAllocDefault) == cudaSuccess;
   cudaGraph_t graph = nullptr;
@@ -1918,6 +2055,62 @@ extern "C" int cqlcuda_fill_affine_u32(CqlBuffer* b, uint64_t rows, uint64_t mul
   k_fill_affine<<<grid, 256, 0, s.stream>>>((uint32_t*)b->dptr, rows, mul, add, modulus);
   if (!note_cuda(cudaGetLastError(), "fill_affine")) return 0;
   return wait_stream(s.stream, "fill_affine");
+}
+
+// ---------------------------------------------------------------------------------------------
+// page-locked host memory for uploads
+
+static std::mutex g_host_lock;
+static std::unordered_map<void*, uint64_t> g_host_blocks;
+
+extern "C" void* cqlcuda_host_alloc(uint64_t bytes)
+{
+  if (!ensure_init() || bytes == 0) return nullptr;
+  long page = sysconf(_SC_PAGESIZE);
+  uint64_t size = (bytes + (uint64_t)page - 1) / (uint64_t)page * (uint64_t)page;
+  void* p = mmap(nullptr, size, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+  if (p == MAP_FAILED)
+  {
+    set_error("cqlcuda_host_alloc: mmap of %llu bytes failed", (unsigned long long)size);
+    return nullptr;
+  }
+  // large pages where the kernel offers them, and the pages on the host node nearest the GPU
+  madvise(p, size, MADV_HUGEPAGE);
+  int node = -1;
+  cudaDeviceGetAttribute(&node, cudaDevAttrHostNumaId, S().device);
+  if (node >= 0 && node < 1024)
+  {
+    unsigned long mask[1024 / (8 * sizeof(unsigned long))];
+    memset(mask, 0, sizeof(mask));
+    mask[node / (8 * sizeof(unsigned long))] |= 1ul << (node % (8 * sizeof(unsigned long)));
+    syscall(SYS_mbind, p, size, 1 /* MPOL_PREFERRED */, mask, 1024ul, 0u);
+  }
+  cudaError_t e = cudaHostRegister(p, size, cudaHostRegisterDefault);
+  if (e != cudaSuccess)
+  {
+    cudaGetLastError();
+    munmap(p, size);
+    set_error("cqlcuda_host_alloc: cudaHostRegister of %llu bytes failed: %s", (unsigned long long)size, cudaGetErrorString(e));
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> g(g_host_lock);
+  g_host_blocks[p] = size;
+  return p;
+}
+
+extern "C" void cqlcuda_host_free(void* p)
+{
+  if (!p) return;
+  uint64_t size = 0;
+  {
+    std::lock_guard<std::mutex> g(g_host_lock);
+    auto it = g_host_blocks.find(p);
+    if (it == g_host_blocks.end()) return;
+    size = it->second;
+    g_host_blocks.erase(it);
+  }
+  cudaHostUnregister(p);
+  munmap(p, size);
 }
 
 extern "C" int cqlcuda_flush_l2(uint64_t bytes)

@@ -122,6 +122,7 @@ CUDA_API = [
     ("cqlcuda_kernel_alloc_from_image", P, [cstr, u64, P, u64]),
     ("cqlcuda_kernel_alloc_from_image_spec", P, [cstr, u64, P, u64, P, u32]),
     ("cqlcuda_generated_kernel_stats", None, [P, P]),
+    ("cqlcuda_set_generated_kernel_cap", None, [u32]),
     ("cqlcuda_kernel_release", None, [P]),
     ("cqlcuda_kernel_execute", None, [P, u32, u32]),
     ("cqlcuda_kernel_set_arg_buffer", None, [P, u32, P]),
@@ -169,6 +170,8 @@ CUDA_API = [
     ("cqlcuda_fill_splitmix_u32", C.c_int, [P, u64, u64, u32, u32, u64]),
     ("cqlcuda_fill_sequence_u32", C.c_int, [P, u64, u32]),
     ("cqlcuda_fill_affine_u32", C.c_int, [P, u64, u64, u64, u64]),
+    ("cqlcuda_host_alloc", P, [u64]),
+    ("cqlcuda_host_free", None, [P]),
     ("cqlcuda_flush_l2", C.c_int, [u64]),
     ("cqlcuda_timer_begin", None, []),
     ("cqlcuda_timer_end_ms", dbl, []),

@@ -118,6 +118,13 @@ CqlKernel* cqlcuda_kernel_alloc_from_image(const char* name, uint64_t name_len, 
 CqlKernel* cqlcuda_kernel_alloc_from_image_spec(const char* name, uint64_t name_len, const void* image, uint64_t image_len,
                                                 const uint32_t* spec_values, uint32_t spec_count);    /* :42 */
 void       cqlcuda_generated_kernel_stats(uint64_t* out_compiles, uint64_t* out_evictions);            /* :43 */
+/* Generated (NVRTC) kernels kept loaded: the reference's GPU_VULKAN_MAX_GENERATED_KERNELS (default 64, at
+   least 8, src/gpu/vulkan/gpu_vulkan.c:75). Past the cap the least recently looked-up generated kernel is
+   unloaded and counted as an eviction (gpu_vulkan.c:2721-2737), after the GPU drains and with every plan
+   graph that launches it; the 8 most recently looked-up are kept, and nothing is evicted while the main
+   lane's batch is open. A handle to an evicted kernel stays valid: its dispatch fails with an error, and a
+   new lookup by name (with its source) compiles it again. */
+void       cqlcuda_set_generated_kernel_cap(uint32_t cap);
 void       cqlcuda_kernel_release(CqlKernel* kernel);                                                  /* :44, kernels are cached: no-op */
 void       cqlcuda_kernel_execute(CqlKernel* kernel, uint32_t global_work_size, uint32_t local_work_size); /* :45, synchronous */
 void       cqlcuda_kernel_set_arg_buffer(CqlKernel* kernel, uint32_t index, CqlBuffer* buffer);        /* :46 */
@@ -227,6 +234,11 @@ int      cqlcuda_fill_sequence_u32(CqlBuffer* buffer, uint64_t rows, uint32_t fi
    (src/tests/scale/bench_select_scale.c:38-56: region = r % 50, amount = r % 10000,
    needle_key = r * 2654435761 mod 2^32) are such fills. */
 int      cqlcuda_fill_affine_u32(CqlBuffer* buffer, uint64_t rows, uint64_t mul, uint64_t add, uint64_t modulus);
+/* Page-locked host memory for uploads (the reference's host-visible staging, GPU_BufferFlag_HostVisible):
+   large pages where offered, on the host NUMA node nearest the GPU, registered with the device so copies
+   from it run at the link's rate. NULL on failure; free with cqlcuda_host_free. */
+void*    cqlcuda_host_alloc(uint64_t bytes);
+void     cqlcuda_host_free(void* host_ptr);
 /* Writes `bytes` bytes of a scratch buffer, to evict the L2 between timed runs. */
 int      cqlcuda_flush_l2(uint64_t bytes);
 /* CUDA-event timing of everything the library enqueues between begin and end, on its own stream. */

@@ -24,22 +24,30 @@ def env(gpu):
     t = workloads.fact_table(N)
     h = workloads.fact_numpy(N, gen=oracle.splitmix_u32)
     rng = np.random.default_rng(11)
-    key = ops.Column.from_numpy(rng.integers(0, 200_000, N).astype(np.uint32))
-    val = ops.Column.from_numpy(rng.normal(0, 100, N))
+    hkey = rng.integers(0, 200_000, N).astype(np.uint32)
+    key = ops.Column.from_numpy(hkey)
+    val = ops.Column.from_numpy(rng.integers(0, 1_000_000, N).astype(np.uint32))
     dk = np.arange(1_000_000, dtype=np.uint32)
     seg = oracle.splitmix_u32(1_000_000, workloads.DIM1M_SEED, 1, 0, 20).astype(np.float64)
     prog = ops.Program("(or (< flag 3) (and (> amount 9000) (= region 7)))", {"flag": t.flag, "amount": t.amount, "region": t.region})
-    return ops, gpu.load_cuda(), t, h, key, val, dk, seg, prog
+    return ops, gpu.load_cuda(), t, h, key, val, dk, seg, prog, hkey
+
+
+def by_key(res, hkey):
+    """a hash GROUP BY's groups keyed by their key value: the order of its groups and the row that
+    represents each are whichever slot claim won, in the reference too"""
+    keys = hkey[res["repr_row"].astype(np.int64)]
+    return sorted(zip(keys.tolist(), res["counts"].tolist(), res["results"].tolist()))
 
 
 def queries(env):
-    ops, _, t, _, key, val, dk, seg, prog = env
+    ops, _, t, _, key, val, dk, seg, prog, hkey = env
     return {
         "aggregate_global": lambda: ops.aggregate_global([t.amount]),
         "scan_simple_rows": lambda: ops.scan_simple([t.flag], [(0, ops.CMP_LT, 2)], want_rows=True),
         "scan_filter_generated": lambda: ops.scan_filter(prog, strategy=ops.SCAN_GENERATED, want_rows=True),
         "group_dense": lambda: ops.group_dense(t.region, [SUM, COUNT, MIN, MAX], [t.amount, None, t.amount, t.amount]),
-        "group_hash": lambda: ops.group_hash([key], [COUNT, SUM], [None, val]),
+        "group_hash": lambda: by_key(ops.group_hash([key], [COUNT, SUM], [None, val]), hkey),
         "join_aggregate": lambda: ops.join_aggregate(t.amount, [SUM, COUNT], [t.amount, None], dk, group_values=[seg]),
         "sort_rows": lambda: ops.sort_rows([key]),
     }
@@ -54,6 +62,12 @@ def canon(x):
     if isinstance(x, np.ndarray):
         return x.tolist()
     return x
+
+
+def drop_caches(lib):
+    """af_drop_caches (bench_alloc_fault.c:236-241): a new pool epoch, then every pooled buffer evicted"""
+    lib.cqlcuda_pool_begin_epoch()
+    lib.cqlcuda_pool_evict(2 ** 64 - 1)
 
 
 def run(fn):
@@ -71,7 +85,7 @@ def test_every_allocation_fails_cleanly(env, name):
     fn = queries(env)[name]
     status, reference = run(fn)
     assert status == "ok", reference
-    lib.cqlcuda_pool_evict(2 ** 64 - 1)
+    drop_caches(lib)
     before = lib.cqlcuda_memory_stats().alloc_calls
     status, cold = run(fn)
     allocations = lib.cqlcuda_memory_stats().alloc_calls - before
@@ -79,7 +93,7 @@ def test_every_allocation_fails_cleanly(env, name):
     assert allocations > 0, "a cold run allocates"
     tally = {"correct": 0, "error": 0, "unreached": 0}
     for k in range(1, allocations + 1):
-        lib.cqlcuda_pool_evict(2 ** 64 - 1)
+        drop_caches(lib)
         target = lib.cqlcuda_memory_stats().alloc_calls + k
         lib.cqlcuda_set_fault_alloc_at(target)
         try:

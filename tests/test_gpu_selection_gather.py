@@ -75,7 +75,7 @@ def test_strided_pairs_pick_one_side(lib):
     rng = np.random.default_rng(5)
     n = 20_000
     pairs = np.stack([np.arange(n, dtype=np.uint32), with_holes(rng, n, 9_000, 0.2)], axis=1).ravel()
-    src = rng.integers(0, 1 << 31, 10_000).astype(np.uint32)
+    src = rng.integers(0, 1 << 31, n).astype(np.uint32)          # probe rows reach n - 1
     for word_offset in (0, 1):
         got = run(lib, 1, pairs, src, None, n, stride=2, word_offset=word_offset)
         assert np.array_equal(got, oracle.selection_gather(1, pairs, src, None, n, stride=2, word_offset=word_offset))
