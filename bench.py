@@ -479,6 +479,18 @@ def main():
     return 0
 
 
+def _canon(x):
+    """a query result as nested plain values, comparable with =="""
+    import numpy as np
+    if isinstance(x, dict):
+        return {k: _canon(v) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [_canon(v) for v in x]
+    if isinstance(x, np.ndarray):
+        return x.tolist()
+    return x
+
+
 def run_e2e(args, native, ops, t, queries, lib):
     """The suite from page-locked HOST buffers, every step: region, amount and flag uploaded, the seven
     queries run, their results read back. Uploads go through the backend's stream slots (the reference's
@@ -514,7 +526,9 @@ def run_e2e(args, native, ops, t, queries, lib):
             raise RuntimeError("e2e upload failed: " + native.last_error())
 
     h2d = 3 * n * 4
+    resident = {name: _canon(q()) for name, q in by_name.items()}
     times = []
+    last = {}
     for i in range(args.warmup + max(2, args.steps // 2)):
         t0 = time.perf_counter()
         upload(0)
@@ -524,10 +538,13 @@ def run_e2e(args, native, ops, t, queries, lib):
             if slot + 1 < len(plan):
                 upload(slot + 1)
             for q in names:
-                by_name[q]()
+                last[q] = by_name[q]()
         dt = time.perf_counter() - t0
         if i >= args.warmup:
             times.append(dt)
+    # the uploaded columns are the resident ones' bytes: every answer of the last step equals its resident run
+    e2e_parity = "ok" if all(_canon(last[q]) == resident[q] for q in by_name) else \
+        "failed: " + ", ".join(q for q in by_name if _canon(last[q]) != resident[q])
     lib.cqlcuda_stream_release(stream)
     # the uploads alone, one after another, for the link rate
     uploads = []
@@ -548,7 +565,7 @@ def run_e2e(args, native, ops, t, queries, lib):
     # results read back per step: partials/counters/group arrays of the queries (a few hundred KB)
     d2h = 2048 * 3 * 8 + 8 + 50 * 4 * 8 + 10000 * 4 * 8 + 8 + 2 * 8 + 20 * 2 * 8
     return {"value": len(queries) * n / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "upload_ms": upload_ms, "h2d_GBps": h2d / (upload_ms / 1e3) / 1e9,
+            "d2h_bytes_per_step": d2h, "upload_ms": upload_ms, "h2d_GBps": h2d / (upload_ms / 1e3) / 1e9, "parity": e2e_parity,
             "overlap": "each column's upload overlaps the queries over the columns already uploaded"}
 
 if __name__ == "__main__":

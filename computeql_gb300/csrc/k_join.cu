@@ -414,6 +414,203 @@ __global__ void __launch_bounds__(JOIN_THREADS) k_join_probe_native(CqlLaunch a,
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// join_probe_native over a small build side: the table (keys and rows) and the Bloom words are staged
+// into shared memory once per CTA by bulk copies (cp.async.bulk, completion counted on an mbarrier), and
+// the per-dim-row totals are kept per table slot in shared memory, flushed to the dim-row arrays once per
+// CTA. Binding 12 is an error word (bit 0: the staging did not complete within a second; the CTA then
+// waits, again bounded, for its copies and returns without probing). Taken when the error word is bound
+// and the shared arrays fit JOIN_SMEM_MAX_BYTES; the same results as k_join_probe_native.
+
+#define JOIN_SMEM_THREADS 512
+#define JOIN_SMEM_MAX_BYTES (100u * 1024u)
+#define JOIN_WAIT_NS 1000000000ull
+
+struct JoinSmemLayout
+{
+  uint32_t size, bloom_words, exprs;
+  uint32_t keys, trows, bloom, cnt, sums, mins, maxs, total;   // byte offsets in dynamic shared memory
+};
+
+__host__ __device__ inline JoinSmemLayout join_smem_layout(uint32_t size, uint32_t bloom_words, uint32_t exprs)
+{
+  JoinSmemLayout l;
+  l.size = size;
+  l.bloom_words = bloom_words;
+  l.exprs = exprs;
+  l.keys = 16;                                  // the mbarrier sits in the first 8 bytes
+  l.trows = l.keys + 4 * size;
+  l.bloom = l.trows + 4 * size;
+  l.cnt = l.bloom + 4 * bloom_words;
+  l.sums = (l.cnt + 4 * size + 7u) & ~7u;
+  l.mins = l.sums + 8 * size * exprs;
+  l.maxs = l.mins + 4 * size * exprs;
+  l.total = l.maxs + 4 * size * exprs;
+  return l;
+}
+
+__device__ __forceinline__ uint64_t join_globaltimer()
+{
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// waits for phase 0 of the mbarrier for at most JOIN_WAIT_NS; 1 when it completed
+__device__ __forceinline__ int join_mbar_wait(uint32_t bar)
+{
+  uint64_t t0 = join_globaltimer();
+  for (;;)
+  {
+    uint32_t done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done) : "r"(bar), "r"(0u) : "memory");
+    if (done) return 1;
+    if (join_globaltimer() - t0 > JOIN_WAIT_NS) return 0;
+  }
+}
+
+__global__ void __launch_bounds__(JOIN_SMEM_THREADS) k_join_probe_native_smem(CqlLaunch a, uint64_t rows, JoinSmemLayout L)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  JoinDecode d;
+  uint32_t widths = cql_word(a, 1);
+  uint32_t arg_base[4] = { cql_word(a, 3), cql_word(a, 5), cql_word(a, 9), cql_word(a, 11) };
+#pragma unroll
+  for (int c = 0; c < 5; c++)
+  {
+    uint32_t w = (widths >> (4 * c)) & 0xfu;
+    d.col[c] = (const uint32_t*)a.buf[c];
+    d.log2w[c] = w == 1 ? 2 : (w == 2 ? 1 : 0);
+    d.bits[c] = w == 1 ? 8 : (w == 2 ? 16 : 32);
+    d.mask[c] = w == 1 ? 0xffu : (w == 2 ? 0xffffu : 0xffffffffu);
+    d.base[c] = (w == 1 || w == 2) ? (c == 0 ? cql_word(a, 10) : arg_base[c - 1]) : 0u;
+  }
+  uint32_t* counts = (uint32_t*)a.buf[7];
+  unsigned long long* sums = (unsigned long long*)a.buf[8];
+  int* mins = (int*)a.buf[9];
+  int* maxs = (int*)a.buf[10];
+  uint32_t* error = (uint32_t*)a.buf[12];
+  const uint32_t exprs = L.exprs, funcs = cql_word(a, 4), arg_index = cql_word(a, 6), arg_signed = cql_word(a, 7);
+  const uint32_t mask = L.size - 1u, log2_size = cql_word(a, 12), bloom_log2 = cql_word(a, 13);
+  const uint64_t count_cap = a.bytes[7] / 4;
+  uint32_t* s_keys = (uint32_t*)(smem + L.keys);
+  uint32_t* s_rows = (uint32_t*)(smem + L.trows);
+  uint32_t* s_bloom = (uint32_t*)(smem + L.bloom);
+  uint32_t* s_cnt = (uint32_t*)(smem + L.cnt);
+  unsigned long long* s_sums = (unsigned long long*)(smem + L.sums);
+  int* s_mins = (int*)(smem + L.mins);
+  int* s_maxs = (int*)(smem + L.maxs);
+  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(smem);
+
+  // stage the table and the Bloom words: one thread arms the barrier with the bytes and issues the copies
+  if (threadIdx.x == 0)
+  {
+    uint32_t table_bytes = 4u * L.size, bloom_bytes = 4u * L.bloom_words;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar) : "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(2u * table_bytes + bloom_bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(bar + L.keys), "l"(a.buf[5]), "r"(table_bytes), "r"(bar) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(bar + L.trows), "l"(a.buf[6]), "r"(table_bytes), "r"(bar) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(bar + L.bloom), "l"(a.buf[11]), "r"(bloom_bytes), "r"(bar) : "memory");
+  }
+  // the accumulators start empty while the copies fly
+  for (uint32_t i = threadIdx.x; i < L.size; i += blockDim.x) s_cnt[i] = 0u;
+  for (uint32_t i = threadIdx.x; i < L.size * exprs; i += blockDim.x)
+  {
+    s_sums[i] = 0ull;
+    s_mins[i] = 0x7fffffff;
+    s_maxs[i] = (int)0x80000000;
+  }
+  __syncthreads();
+  if (!join_mbar_wait(bar))
+  {
+    if (threadIdx.x == 0) atomicOr(error, 1u);
+    join_mbar_wait(bar);      // the copies in flight land before the CTA leaves
+    return;
+  }
+
+  const uint32_t UNROLL = 8;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; base < rows; base += stride * UNROLL)
+  {
+    uint32_t key[UNROLL];
+    bool maybe[UNROLL];
+#pragma unroll
+    for (uint32_t u = 0; u < UNROLL; u++)
+    {
+      uint64_t at = base + u * stride;
+      key[u] = at < rows ? join_read(d, 0, at) : 0u;
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < UNROLL; u++)
+    {
+      uint64_t at = base + u * stride;
+      uint32_t h = key[u] * 0x9E3779B1u, h2 = key[u] * 0x85EBCA6Bu;
+      uint32_t bits = (1u << ((h2 >> 27) & 31u)) | (1u << ((h2 >> 22) & 31u));
+      maybe[u] = at < rows && (s_bloom[h >> (32u - bloom_log2)] & bits) == bits;
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < UNROLL; u++)
+    {
+      if (!maybe[u]) continue;
+      uint64_t row = base + u * stride;
+      uint32_t slot = (key[u] * 0x9E3779B1u) >> (32u - log2_size);
+      bool found = false;
+      for (uint32_t probe = 0; probe < L.size; probe++)
+      {
+        uint32_t r1 = s_rows[slot];
+        if (r1 == 0u) break;
+        if (s_keys[slot] == key[u])
+        {
+          found = true;
+          break;
+        }
+        slot = (slot + 1u) & mask;
+      }
+      if (!found) continue;
+      atomicAdd(&s_cnt[slot], 1u);
+      for (uint32_t e = 0; e < exprs; e++)
+      {
+        uint32_t f = (funcs >> (e * 4)) & 0xfu;
+        if (f == JFUNC_COUNT) continue;
+        uint32_t ai = (arg_index >> (e * 4)) & 0x3u;
+        uint32_t w = join_read(d, 1 + (int)ai, row);
+        uint32_t index = slot * exprs + e;
+        if (f == JFUNC_SUM || f == JFUNC_AVG)
+        {
+          bool sg = ((arg_signed >> ai) & 1u) != 0;
+          atomicAdd(&s_sums[index], sg ? (unsigned long long)(long long)(int)w : (unsigned long long)w);
+        }
+        else if (f == JFUNC_MIN) atomicMin(&s_mins[index], (int)w);
+        else if (f == JFUNC_MAX) atomicMax(&s_maxs[index], (int)w);
+      }
+    }
+  }
+  __syncthreads();
+  // the CTA's totals per slot into the dim-row arrays
+  for (uint32_t slot = threadIdx.x; slot < L.size; slot += blockDim.x)
+  {
+    uint32_t c = s_cnt[slot];
+    if (c == 0u) continue;
+    uint32_t dim_row = s_rows[slot] - 1u;
+    if (dim_row >= count_cap) continue;
+    atomicAdd(&counts[dim_row], c);
+    for (uint32_t e = 0; e < exprs; e++)
+    {
+      uint32_t f = (funcs >> (e * 4)) & 0xfu;
+      uint64_t index = (uint64_t)dim_row * exprs + e;
+      uint32_t si = slot * exprs + e;
+      if (f == JFUNC_SUM || f == JFUNC_AVG) atomicAdd(&sums[index], s_sums[si]);
+      else if (f == JFUNC_MIN) atomicMin(&mins[index], s_mins[si]);
+      else if (f == JFUNC_MAX) atomicMax(&maxs[index], s_maxs[si]);
+    }
+  }
+}
+
 static int launch_join_probe_native(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
 {
   (void)gws;
@@ -423,6 +620,31 @@ static int launch_join_probe_native(const CqlLaunch& a, uint32_t gws, uint32_t l
   if (rows == 0) return 0;
   if (log2_size == 0 || log2_size > 31 || bloom_log2 == 0 || bloom_log2 > 31) return (int)cudaErrorInvalidValue;
   if ((uint64_t)(cql_word(a, 8)) + 1 != (1ull << log2_size)) return (int)cudaErrorInvalidValue;
+  // a small build side: shared-memory table when the error word is bound, the arrays fit and the bulk
+  // copies' sources and sizes are 16-byte multiples (tables of at least 16 slots and 16 Bloom words)
+  uint32_t exprs = min(cql_word(a, 2), 8u);
+  if (log2_size >= 4 && log2_size <= 16 && bloom_log2 >= 4 && bloom_log2 <= 16 && a.buf[12] && a.bytes[12] >= 4 &&
+      ((uintptr_t)a.buf[5] & 15u) == 0 && ((uintptr_t)a.buf[6] & 15u) == 0 && ((uintptr_t)a.buf[11] & 15u) == 0 &&
+      a.bytes[5] >= (4ull << log2_size) && a.bytes[6] >= (4ull << log2_size) && a.bytes[11] >= (4ull << bloom_log2))
+  {
+    JoinSmemLayout L = join_smem_layout(1u << log2_size, 1u << bloom_log2, exprs);
+    if (L.total <= JOIN_SMEM_MAX_BYTES)
+    {
+      static bool attr_set = false;
+      if (!attr_set)
+      {
+        if (cudaFuncSetAttribute(k_join_probe_native_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)JOIN_SMEM_MAX_BYTES) != cudaSuccess)
+          return (int)cudaGetLastError();
+        attr_set = true;
+      }
+      int per_sm = (int)std::max<uint32_t>(1u, std::min<uint32_t>(4u, (uint32_t)(g_cql_max_smem_optin / (L.total + 1024u))));
+      per_sm = std::min(per_sm, 2048 / JOIN_SMEM_THREADS);
+      k_join_probe_native_smem<<<cql_stream_grid((rows + JOIN_SMEM_THREADS * 8 - 1) / (JOIN_SMEM_THREADS * 8), per_sm), JOIN_SMEM_THREADS,
+                                 L.total, stream>>>(a, rows, L);
+      CQL_LAUNCH_CHECK();
+      return 0;
+    }
+  }
   k_join_probe_native<<<cql_stream_grid((rows + JOIN_THREADS * 8 - 1) / (JOIN_THREADS * 8), 8), JOIN_THREADS, 0, stream>>>(a, rows);
   CQL_LAUNCH_CHECK();
   return 0;

@@ -2085,6 +2085,9 @@ extern "C" void* cqlcuda_host_alloc(uint64_t bytes)
     mask[node / (8 * sizeof(unsigned long))] |= 1ul << (node % (8 * sizeof(unsigned long)));
     syscall(SYS_mbind, p, size, 1 /* MPOL_PREFERRED */, mask, 1024ul, 0u);
   }
+  // every page is written before it is registered: an untouched anonymous page is the shared zero page,
+  // and the pinned mapping must be of the page the process will write
+  memset(p, 0, size);
   cudaError_t e = cudaHostRegister(p, size, cudaHostRegisterDefault);
   if (e != cudaSuccess)
   {

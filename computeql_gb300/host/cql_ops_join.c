@@ -260,11 +260,14 @@ static int probe_totals(const CqlJoinAgg* q, uint32_t core_count, const uint32_t
   CqlBuffer* sb = ok ? pooled("jp_sums", D * core_count * 8, CQLCUDA_BUFFER_READ_WRITE) : NULL;
   CqlBuffer* nb = ok ? pooled("jp_mins", D * core_count * 4, CQLCUDA_BUFFER_READ_WRITE) : NULL;
   CqlBuffer* xb = ok ? pooled("jp_maxs", D * core_count * 4, CQLCUDA_BUFFER_READ_WRITE) : NULL;
+  /* the error word of the small-table form (its table staged in shared memory) */
+  CqlBuffer* eb = ok ? pooled("jp_error", 16, CQLCUDA_BUFFER_READ_WRITE) : NULL;
+  uint32_t stage_error = 0;
   CqlKernel* k = ok ? kernel("join_probe_native") : NULL;
   uint32_t* hc = ok ? (uint32_t*)malloc(D * 4) : NULL;
   uint32_t* hn = ok ? (uint32_t*)malloc(D * core_count * 4) : NULL;
   uint32_t* hx = ok ? (uint32_t*)malloc(D * core_count * 4) : NULL;
-  ok = ok && kb && rb && bb && cb && sb && nb && xb && k && hc && hn && hx;
+  ok = ok && kb && rb && bb && cb && sb && nb && xb && eb && k && hc && hn && hx;
   if (ok)
   {
     uint64_t widths = fk->width == 4 ? 0 : fk->width;
@@ -283,6 +286,7 @@ static int probe_totals(const CqlJoinAgg* q, uint32_t core_count, const uint32_t
     cqlcuda_kernel_set_arg_buffer(k, 9, nb);
     cqlcuda_kernel_set_arg_buffer(k, 10, xb);
     cqlcuda_kernel_set_arg_buffer(k, 11, bb);
+    cqlcuda_kernel_set_arg_buffer(k, 12, eb);
     cqlcuda_kernel_set_arg_u64(k, 0, rows | (widths << 32));
     cqlcuda_kernel_set_arg_u64(k, 1, core_count | ((uint64_t)bases[0] << 32));
     cqlcuda_kernel_set_arg_u64(k, 2, func_codes | ((uint64_t)bases[1] << 32));
@@ -298,12 +302,15 @@ static int probe_totals(const CqlJoinAgg* q, uint32_t core_count, const uint32_t
     cqlcuda_batch_buffer_zero(b, sb, D * core_count * 8);
     cqlcuda_batch_buffer_fill(b, nb, D * core_count * 4, 0x7fffffffu);
     cqlcuda_batch_buffer_fill(b, xb, D * core_count * 4, 0x80000000u);
+    cqlcuda_batch_buffer_zero(b, eb, 16);
     cqlcuda_batch_kernel_execute(b, k, (uint32_t)((rows + 8191) / 8192 * 256), QE_GPU_WORKGROUP_SIZE);
     cqlcuda_batch_buffer_read(b, cb, hc, D * 4);
     cqlcuda_batch_buffer_read(b, sb, sums, D * core_count * 8);
     cqlcuda_batch_buffer_read(b, nb, hn, D * core_count * 4);
     cqlcuda_batch_buffer_read(b, xb, hx, D * core_count * 4);
+    cqlcuda_batch_buffer_read(b, eb, &stage_error, 4);
     ok = cqlcuda_batch_end(b);
+    if (ok && stage_error) ok = refuse("the join table's staging into shared memory did not complete");
   }
   if (ok)
   {

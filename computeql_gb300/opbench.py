@@ -14,6 +14,8 @@ like the configurations the operators serve:
   hash_group    GROUP BY user_id (1M groups) with COUNT and SUM of an f64 measure over 10M rows
   hll           APPROX_COUNT_DISTINCT(session) over 10M rows (4M distinct)
   hash_join     a 1M-row build side (unique keys) probed by 10M rows, pairs counted
+  join_small    the join-aggregate probe (join_probe_native) of a 1024-row dim table by `rows` fact rows (random
+                keys), COUNT and SUM(amount) per dim row folded into 20 groups: the small build side
   zone_map      the zone map of one u32 column
   batch         512 COUNT+SUM queries over 29 WHERE shapes on a table of 4 u32 + 4 f64 columns, in one shared
                 scan (cqlops_batch_filter_aggregate) and, for comparison, one generated kernel per query
@@ -29,7 +31,7 @@ import numpy as np
 
 from . import build, native, ops
 
-OPS = ["sort", "sort_f64_2", "sort_subset", "fixed", "hash_group", "hll", "hash_join", "zone_map", "batch", "materialize"]
+OPS = ["sort", "sort_f64_2", "sort_subset", "fixed", "hash_group", "hll", "hash_join", "join_small", "zone_map", "batch", "materialize"]
 
 
 def _profile():
@@ -113,6 +115,13 @@ def run(op, rows, reps):
         pk = ops.Column.splitmix(probe_rows, 0, 1, 0, 1_000_000)
         fn = lambda: ops.hash_join(bk, pk, want_pairs=False)
         n, nbytes = probe_rows, (build_rows + probe_rows) * 4
+    elif op == "join_small":
+        fk = ops.Column.splitmix(rows, 6, 2, 0, 1024)
+        amount = ops.Column.splitmix(rows, 6, 2, 1, 10_000)
+        dk = np.arange(1024, dtype=np.uint32)
+        seg = (dk % 20).astype(np.float64)
+        fn = lambda: ops.join_aggregate(fk, [0, 1], [None, amount], dk, group_values=[seg], strategy=2)
+        n, nbytes = rows, rows * 8
     elif op == "materialize":
         # 30 columns of a 10M-row table (20 u32, 10 f64) for the rows of a 1 % filter, read back to the host
         total = 10_000_000

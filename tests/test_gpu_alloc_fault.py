@@ -48,7 +48,9 @@ def queries(env):
         "scan_filter_generated": lambda: ops.scan_filter(prog, strategy=ops.SCAN_GENERATED, want_rows=True),
         "group_dense": lambda: ops.group_dense(t.region, [SUM, COUNT, MIN, MAX], [t.amount, None, t.amount, t.amount]),
         "group_hash": lambda: by_key(ops.group_hash([key], [COUNT, SUM], [None, val]), hkey),
-        "join_aggregate": lambda: ops.join_aggregate(t.amount, [SUM, COUNT], [t.amount, None], dk, group_values=[seg]),
+        # a failed allocation may move the join to another strategy (dense core to probe); the answer must hold
+        "join_aggregate": lambda: {k: v for k, v in ops.join_aggregate(t.amount, [SUM, COUNT], [t.amount, None], dk,
+                                                                      group_values=[seg]).items() if k != "strategy"},
         "sort_rows": lambda: ops.sort_rows([key]),
     }
 

@@ -222,3 +222,39 @@ def test_lookup_table_gives_way_to_repeated_dim_keys(ops):
     for g, row in enumerate(r["dim_row"]):
         want = sum(int(per_key[k]) for k in dk[sg == sg[row]])
         assert r["results"][g, 0] == want
+
+
+@pytest.mark.parametrize("dim, funcs", [(50, "sum_min_max"), (1000, "count_sum"), (1000, "sum_min_max"), (3000, "count_sum"),
+                                        (16, "count_sum")])
+def test_small_build_side_probe(ops, dim, funcs):
+    """The probe (strategy 2) with a small dim table: tables that fit take the shared-memory form (the table
+    and Bloom words staged by bulk copies, per-slot totals in shared memory), larger ones the global form;
+    per dim row COUNT/SUM/MIN/MAX equal numpy's over the fact rows whose key is that row's key, with misses,
+    a dim-side filter and signed arguments."""
+    rng = np.random.default_rng(100 + dim)
+    n = 2_000_000
+    dim_keys = rng.choice(1 << 31, dim, replace=False).astype(np.uint32) * 2 + 1
+    miss = rng.integers(0, 1 << 31, n).astype(np.uint32) * 2          # even: never a dim key
+    key = np.where(rng.random(n) < 0.8, dim_keys[rng.integers(0, dim, n)], miss).astype(np.uint32)
+    v = rng.integers(-50_000, 50_000, n).astype(np.int32)
+    kept = np.sort(rng.choice(dim, max(1, dim * 3 // 4), replace=False)).astype(np.uint64)
+    row_id = np.arange(dim, dtype=np.float64)                           # one group per dim row
+    kc, vc = ops.Column.from_numpy(key), ops.Column.from_numpy(v)
+    if funcs == "count_sum":
+        fs, args = [COUNT, SUM], [None, vc]
+    else:
+        fs, args = [SUM, MIN, MAX], [vc, vc, vc]
+    r = ops.join_aggregate(kc, fs, args, dim_keys, dim_rows=kept, group_values=[row_id], strategy=2)
+    assert r["strategy"] == 2
+    got = {int(row): r["results"][g] for g, row in enumerate(r["dim_row"])}
+    order = np.argsort(key, kind="stable")
+    sk = key[order]
+    for d in kept.astype(np.int64):
+        lo, hi = np.searchsorted(sk, dim_keys[d]), np.searchsorted(sk, dim_keys[d], side="right")
+        vals = v[order[lo:hi]].astype(np.int64)
+        if len(vals) == 0:
+            assert d not in got
+            continue
+        want = [float(len(vals)), float(vals.sum())] if funcs == "count_sum" else [float(vals.sum()), float(vals.min()), float(vals.max())]
+        assert list(got[int(d)]) == want, d
+    assert list(r["dim_row"]) == sorted(got)                                # groups in dim-row order
