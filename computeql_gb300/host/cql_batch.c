@@ -21,6 +21,7 @@
  *     atomics); a CTA folds its warps into 128-bit sums, a second kernel folds the CTAs in order. At
  *     most CQL_BATCH_LAUNCH_QUERIES queries go into one launch.
  */
+#define _POSIX_C_SOURCE 200809L
 #include "cqlops.h"
 #include "cql_codegen.h"
 
@@ -30,6 +31,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #define QE_GPU_WORKGROUP_SIZE 256
 #define BATCH_MAX_SITES 16
@@ -355,17 +357,24 @@ static const char* BATCH_PRELUDE =
   "  return (bits >> 63) ? -(long long)mag : (long long)mag;\n"
   "}\n";
 
+/* CTAs per SM of the register form at a block size: its shared accumulators are (block / 32) x 384 x 12
+   bytes, 6 CTAs of 256 threads an SM */
+static uint32_t register_ctas_per_sm(uint32_t block)
+{
+  return BATCH_CTAS_PER_SM * 256u / block;
+}
+
 /* the source of one launch: `shape_exprs` over `shapes` shapes, the register blocks of slot_type */
 static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint32_t shapes, const int* slot_type, const int* sum_cols,
-                          uint32_t sum_col_count, uint32_t rows_per_thread)
+                          uint32_t sum_col_count, uint32_t rows_per_thread, uint32_t block)
 {
   Buf b;
   memset(&b, 0, sizeof(b));
-  bput(&b, "// cql: block=256 smem=%u per_sm=%u\n", 8u * CQL_BATCH_LAUNCH_QUERIES * 12u, BATCH_CTAS_PER_SM);
+  bput(&b, "// cql: block=%u smem=%u per_sm=%u\n", block, (block / 32u) * CQL_BATCH_LAUNCH_QUERIES * 12u, register_ctas_per_sm(block));
   bput(&b, "%s", BATCH_PRELUDE);
   for (uint32_t s = 0; s < shapes; s++) bput(&b, "#define CQL_SHAPE_%u(k) (%s)\n", s, shape_exprs[s]);
   bput(&b,
-       "extern \"C\" __global__ void __launch_bounds__(256) cql_main(CqlLaunch a)\n{\n"
+       "extern \"C\" __global__ void __launch_bounds__(%u) cql_main(CqlLaunch a)\n{\n"
        "  const u64 rows = cql_word(a, 0); const u32 nq = cql_word(a, 2); const u32 q0 = cql_word(a, 4);\n"
        "  const u32 need = cql_word(a, 6), need_sum = cql_word(a, 7);   /* the columns this launch reads and sums */\n"
        "  (void)need_sum;\n"
@@ -388,7 +397,7 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
        "    const u64 row0 = (g0 + threadIdx.x) * RPT;\n"
        "    const u32 valid = row0 < rows ? (u32)min((u64)RPT, rows - row0) : 0u;\n"
        "    const u32 valid_mask = valid >= 32u ? 0xffffffffu : ((1u << valid) - 1u);\n",
-       rows_per_thread);
+       block, rows_per_thread);
   /* the register blocks */
   for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++)
   {
@@ -1165,10 +1174,10 @@ static char* cube_answer_source(const CubePlan* P, char** shape_exprs, const uin
 
 /* the source of one launch in the form rows_per_thread asks for */
 static char* launch_source(char** shape_exprs, const uint32_t* shape_sites, uint32_t shapes, const int* slot_type, const int* sum_cols,
-                           uint32_t sum_col_count, uint32_t rows_per_thread)
+                           uint32_t sum_col_count, uint32_t rows_per_thread, uint32_t block)
 {
   if (!rows_per_thread) return batch_source_tiled(shape_exprs, shape_sites, shapes, slot_type, sum_cols, sum_col_count);
-  return batch_source(shape_exprs, shape_sites, shapes, slot_type, sum_cols, sum_col_count, rows_per_thread);
+  return batch_source(shape_exprs, shape_sites, shapes, slot_type, sum_cols, sum_col_count, rows_per_thread, block);
 }
 
 /* ---- the shape catalog ---- */
@@ -1329,6 +1338,9 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
   /* 0: the shared-memory tile form; 4, 8 or 16: the register form with that many rows per thread (the
      cube-source modes carry the table pass here instead) */
   uint32_t cube_pass = rows_per_thread;
+  /* the form: rows per thread in the low byte, the register form's block size / 256 in the next (1 or 2) */
+  uint32_t block = ((rows_per_thread >> 8) & 0xffu) == 2u ? 512u : 256u;
+  rows_per_thread &= 0xffu;
   if (rows_per_thread != 0 && rows_per_thread != 4 && rows_per_thread != 8 && rows_per_thread != 16) rows_per_thread = 8;
   uint64_t rows = columns[0].rows;
   if (!cqlops_rows_fit(rows)) return 0;
@@ -1469,20 +1481,19 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     double m = fabs(col->zone_min) > fabs(col->zone_max) ? fabs(col->zone_min) : fabs(col->zone_max);
     int e = 0;
     if (m > 0.0) frexp(m, &e);   /* m < 2^e */
-    /* the rows one accumulator takes: in the register form a warp's passes over the grid (32 lanes x
-       rows_per_thread each), in the tile form a CTA's tiles (at most one SM's share of the rows and two
-       tiles, whatever the CTAs per SM) */
-    /* (the cube form adds each row's summand to 128-bit cell totals, so any of these bounds serves it:
-       a query's sum is the same integer whether the cube or the register form answers it) */
-    uint64_t warp_rows;
-    if (rows_per_thread)
+    /* the rows one accumulator takes, the most any form takes: in the register form a warp's passes over
+       the grid (32 lanes x rows per thread each), in the tile form a CTA's tiles (at most one SM's share
+       of the rows and two tiles, whatever the CTAs per SM). One bound for every form gives every form the
+       same scale, so a query's sum is the same integer whichever form (or the autotuner's choice) runs
+       it - and the cube form, which adds the same summands to 128-bit cell totals. */
+    uint64_t per_pass = (uint64_t)(sm_count ? sm_count : 152) * BATCH_CTAS_PER_SM * QE_GPU_WORKGROUP_SIZE;
+    uint64_t warp_rows = rows / (sm_count ? sm_count : 152) + 2048;
+    for (uint32_t rpt = 4; rpt <= 16; rpt *= 2)
     {
-      uint64_t groups = (rows + rows_per_thread - 1) / rows_per_thread;
-      uint64_t per_pass = (uint64_t)(sm_count ? sm_count : 152) * BATCH_CTAS_PER_SM * QE_GPU_WORKGROUP_SIZE;
-      warp_rows = ((groups + per_pass - 1) / per_pass) * 32 * rows_per_thread;
+      uint64_t groups = (rows + rpt - 1) / rpt;
+      uint64_t w = ((groups + per_pass - 1) / per_pass) * 32 * rpt;
+      if (w > warp_rows) warp_rows = w;
     }
-    else
-      warp_rows = rows / (sm_count ? sm_count : 152) + 2048;
     int wr = 0;
     frexp((double)warp_rows, &wr);   /* warp_rows < 2^wr */
     col_scale[c] = ldexp(1.0, 62 - e - wr);
@@ -1700,7 +1711,7 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     uint32_t nq = scan_n < CQL_BATCH_LAUNCH_QUERIES ? scan_n : CQL_BATCH_LAUNCH_QUERIES;
     uint32_t ns;
     SLICE_SHAPES(0, nq, ns);
-    char* src = launch_source(slice_exprs, slice_sites, ns, launch_types, sum_cols, sum_col_count, rows_per_thread);
+    char* src = launch_source(slice_exprs, slice_sites, ns, launch_types, sum_cols, sum_col_count, rows_per_thread, block);
     ok = src != NULL;
     if (ok && mode == BATCH_SOURCE)
     {
@@ -1755,7 +1766,7 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
       memcpy(params + off_cmeta + (uint64_t)i * 4, &meta, 4);
     }
   }
-  uint32_t per_sm = rows_per_thread ? BATCH_CTAS_PER_SM : tiled_layout(launch_types, sum_col_count).per_sm;
+  uint32_t per_sm = rows_per_thread ? register_ctas_per_sm(block) : tiled_layout(launch_types, sum_col_count).per_sm;
   uint64_t ctas = (uint64_t)(sm_count ? sm_count : 152) * per_sm;
   uint32_t widest = scan_n < CQL_BATCH_LAUNCH_QUERIES ? scan_n : CQL_BATCH_LAUNCH_QUERIES;
   const uint64_t cube_out_bytes = 16 + (uint64_t)cube_n * 24;   /* the error word, then (count, lo, hi) per cube query */
@@ -1786,7 +1797,7 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     CqlKernel* k = shared_k;
     if (!k)
     {
-      char* src = launch_source(slice_exprs, slice_sites, ns, launch_types, sum_cols, sum_col_count, rows_per_thread);
+      char* src = launch_source(slice_exprs, slice_sites, ns, launch_types, sum_cols, sum_col_count, rows_per_thread, block);
       if (!src)
       {
         ok = 0;
@@ -1964,10 +1975,164 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
   return ok;
 }
 
+/* ---- the autotuner ----
+   With rows_per_thread = CQLOPS_BATCH_AUTOTUNE the form of the shared scan is picked per plan shape from
+   timed runs: the first batches of a shape run once in each candidate form (the register form with 4, 8
+   or 16 rows a thread and 256 or 512 threads a CTA, and the shared-memory tile form), each compiled before
+   its run is timed; later batches of the shape run in the fastest. Every form gives the same answers (one
+   summand scale for all forms), so the trial runs are ordinary batches. A plan shape is the queries'
+   bytecode (literals apart) and summed columns, the column types, the query count and the table's rows,
+   each of the last two to a power of two; with a catalog, the catalog and the shapes it holds. The
+   reference builds its shared scans from spec-constant modules chosen by fixed rules
+   (src/query_exec/query_kernel.c:1782-2041); here the choice is measured on the device that runs it. */
+
+#define BATCH_TUNE_ENTRIES 256
+static const uint32_t g_tune_forms[] = { 4u | (1u << 8), 8u | (1u << 8), 16u | (1u << 8), 8u | (2u << 8), 16u | (2u << 8), 0u };
+#define BATCH_TUNE_FORMS (sizeof(g_tune_forms) / sizeof(g_tune_forms[0]))
+#define BATCH_DEFAULT_FORM (4u | (1u << 8))
+
+typedef struct
+{
+  uint64_t key;
+  uint32_t next;       /* the candidate to time next; BATCH_TUNE_FORMS once tuned */
+  uint32_t busy;       /* a thread is timing a candidate */
+  uint32_t best;
+  double ms[BATCH_TUNE_FORMS];
+  uint64_t last_use;
+} TuneEntry;
+
+static TuneEntry g_tune[BATCH_TUNE_ENTRIES];
+static uint32_t g_tune_count;
+static uint64_t g_tune_clock;
+static pthread_mutex_t g_tune_lock = PTHREAD_MUTEX_INITIALIZER;
+static __thread uint32_t tl_last_form;
+
+static uint64_t tune_mix(uint64_t h, uint64_t v)
+{
+  for (int i = 0; i < 8; i++) h = (h ^ ((v >> (8 * i)) & 0xffu)) * 1099511628211ull;
+  return h;
+}
+
+static uint32_t log2_floor(uint64_t v)
+{
+  uint32_t r = 0;
+  while (v >>= 1) r++;
+  return r;
+}
+
+static uint64_t tune_key(CqlBatchCatalog* catalog, const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns,
+                         uint32_t column_count, const int32_t* sum_columns)
+{
+  uint64_t h = 1469598103934665603ull;
+  h = tune_mix(h, log2_floor(query_count));
+  h = tune_mix(h, log2_floor(columns[0].rows ? columns[0].rows : 1));
+  for (uint32_t c = 0; c < column_count; c++) h = tune_mix(h, columns[c].type);
+  if (catalog)
+  {
+    h = tune_mix(h, (uint64_t)(uintptr_t)catalog);
+    h = tune_mix(h, cqlops_batch_catalog_shapes(catalog));
+    return h;
+  }
+  for (uint32_t q = 0; q < query_count; q++)
+  {
+    const CqlProgram* p = programs[q];
+    h = tune_mix(h, p->word_count);
+    for (uint32_t w = 0; w < p->word_count; w++) h = tune_mix(h, p->words[w]);
+    h = tune_mix(h, (uint64_t)(int64_t)(sum_columns ? sum_columns[q] : -1));
+  }
+  return h;
+}
+
+static double now_ms(void)
+{
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec * 1e3 + (double)ts.tv_nsec * 1e-6;
+}
+
+static int batch_autotuned(CqlBatchCatalog* catalog, const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns,
+                           uint32_t column_count, const int32_t* sum_columns, uint64_t* out_counts, double* out_sums, uint32_t* out_shapes)
+{
+  uint64_t key = tune_key(catalog, programs, query_count, columns, column_count, sum_columns);
+  pthread_mutex_lock(&g_tune_lock);
+  TuneEntry* e = NULL;
+  for (uint32_t i = 0; i < g_tune_count && !e; i++)
+    if (g_tune[i].key == key) e = &g_tune[i];
+  if (!e)
+  {
+    uint32_t slot = g_tune_count;
+    if (slot < BATCH_TUNE_ENTRIES) g_tune_count++;
+    else
+    {
+      slot = 0;
+      for (uint32_t i = 1; i < BATCH_TUNE_ENTRIES; i++)
+        if (!g_tune[i].busy && (g_tune[slot].busy || g_tune[i].last_use < g_tune[slot].last_use)) slot = i;
+    }
+    e = &g_tune[slot];
+    memset(e, 0, sizeof(*e));
+    e->key = key;
+  }
+  e->last_use = ++g_tune_clock;
+  int trial = e->next < BATCH_TUNE_FORMS && !e->busy;
+  uint32_t candidate = e->next;
+  uint32_t form = trial ? g_tune_forms[candidate] : (e->next >= BATCH_TUNE_FORMS ? g_tune_forms[e->best] : BATCH_DEFAULT_FORM);
+  if (trial) e->busy = 1;
+  pthread_mutex_unlock(&g_tune_lock);
+
+  int ok;
+  if (trial)
+  {
+    /* the candidate's kernel is compiled (and the catalog's shapes entered) before the clock starts */
+    ok = batch_run(catalog, programs, query_count, columns, column_count, sum_columns, form, NULL, NULL, NULL, BATCH_PREPARE, NULL, 0,
+                   NULL, 1);
+    double t0 = now_ms();
+    ok = ok && batch_run(catalog, programs, query_count, columns, column_count, sum_columns, form, out_counts, out_sums, out_shapes, BATCH_RUN,
+                         NULL, 0, NULL, 1);
+    double dt = now_ms() - t0;
+    pthread_mutex_lock(&g_tune_lock);
+    /* the entry may have been taken for another shape meanwhile: record only into this shape's */
+    if (e->key == key && e->busy && e->next == candidate)
+    {
+      e->ms[candidate] = ok ? dt : 1e300;
+      e->next = candidate + 1;
+      if (e->next == BATCH_TUNE_FORMS)
+      {
+        uint32_t best = 0;
+        for (uint32_t i = 1; i < BATCH_TUNE_FORMS; i++)
+          if (e->ms[i] < e->ms[best]) best = i;
+        e->best = best;
+      }
+      e->busy = 0;
+    }
+    pthread_mutex_unlock(&g_tune_lock);
+  }
+  else
+    ok = batch_run(catalog, programs, query_count, columns, column_count, sum_columns, form, out_counts, out_sums, out_shapes, BATCH_RUN,
+                   NULL, 0, NULL, 1);
+  tl_last_form = form | (trial ? 1u << 16 : 0u);
+  return ok;
+}
+
+uint32_t cqlops_batch_last_form(void)
+{
+  return tl_last_form;
+}
+
+void cqlops_batch_tuner_reset(void)
+{
+  pthread_mutex_lock(&g_tune_lock);
+  g_tune_count = 0;
+  memset(g_tune, 0, sizeof(g_tune));
+  pthread_mutex_unlock(&g_tune_lock);
+}
+
 int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
                                   const int32_t* sum_columns, uint32_t rows_per_thread, uint64_t* out_counts, double* out_sums,
                                   uint32_t* out_shapes)
 {
+  if (rows_per_thread == CQLOPS_BATCH_AUTOTUNE && query_count)
+    return batch_autotuned(NULL, programs, query_count, columns, column_count, sum_columns, out_counts, out_sums, out_shapes);
+  tl_last_form = rows_per_thread;
   return batch_run(NULL, programs, query_count, columns, column_count, sum_columns, rows_per_thread, out_counts, out_sums, out_shapes,
                    BATCH_RUN, NULL, 0, NULL, 1);
 }
@@ -1976,6 +2141,9 @@ int cqlops_batch_filter_aggregate_cat(CqlBatchCatalog* catalog, const CqlProgram
                                       const CqlColumn* columns, uint32_t column_count, const int32_t* sum_columns, uint32_t rows_per_thread,
                                       uint64_t* out_counts, double* out_sums, uint32_t* out_shapes)
 {
+  if (rows_per_thread == CQLOPS_BATCH_AUTOTUNE && query_count)
+    return batch_autotuned(catalog, programs, query_count, columns, column_count, sum_columns, out_counts, out_sums, out_shapes);
+  tl_last_form = rows_per_thread;
   return batch_run(catalog, programs, query_count, columns, column_count, sum_columns, rows_per_thread, out_counts, out_sums, out_shapes,
                    BATCH_RUN, NULL, 0, NULL, 1);
 }
@@ -1983,6 +2151,7 @@ int cqlops_batch_filter_aggregate_cat(CqlBatchCatalog* catalog, const CqlProgram
 int cqlops_batch_prepare(CqlBatchCatalog* catalog, const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns,
                          uint32_t column_count, const int32_t* sum_columns, uint32_t rows_per_thread)
 {
+  if (rows_per_thread == CQLOPS_BATCH_AUTOTUNE) rows_per_thread = BATCH_DEFAULT_FORM;
   return batch_run(catalog, programs, query_count, columns, column_count, sum_columns, rows_per_thread, NULL, NULL, NULL, BATCH_PREPARE,
                    NULL, 0, NULL, 1);
 }
@@ -1990,6 +2159,7 @@ int cqlops_batch_prepare(CqlBatchCatalog* catalog, const CqlProgram* const* prog
 int cqlops_batch_source(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
                         const int32_t* sum_columns, uint32_t rows_per_thread, char* out, uint64_t cap, uint64_t* out_len, uint32_t* out_shapes)
 {
+  if (rows_per_thread == CQLOPS_BATCH_AUTOTUNE) rows_per_thread = BATCH_DEFAULT_FORM;
   return batch_run(NULL, programs, query_count, columns, column_count, sum_columns, rows_per_thread, NULL, NULL, out_shapes, BATCH_SOURCE, out,
                    cap, out_len, 0);
 }

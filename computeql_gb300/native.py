@@ -203,6 +203,8 @@ OPS_API = [
     ("cqlops_gather_strings", C.c_int, [P, P, P, u64, P, P, u64, P]),
     ("cqlops_fixed_scale", C.c_int, [P, P, u64, P, P]),
     ("cqlops_zone_map_build", C.c_int, [P, P, u64]),
+    ("cqlops_batch_last_form", u32, []),
+    ("cqlops_batch_tuner_reset", None, []),
     ("cqlops_batch_filter_aggregate", C.c_int, [P, u32, P, u32, P, u32, P, P, P]),
     ("cqlops_batch_source", C.c_int, [P, u32, P, u32, P, u32, P, u64, P, P]),
     ("cqlops_batch_cube_source", C.c_int, [P, u32, P, u32, P, u32, P, u64, P, P]),

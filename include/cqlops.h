@@ -389,12 +389,21 @@ int cqlops_window_rank(const CqlColumn* keys, uint32_t key_count, const uint32_t
    a summed column needs its range (has_range). Queries are grouped by shape (the same bytecode up to
    literal values), one generated kernel evaluates each shape for its queries, literals become per-query
    thresholds. Counts are exact; sums are exact 128-bit sums of the values scaled by 2^k (k from the
-   column's range, |value| x 2^k < 2^55), so |error| <= matched rows x 2^-(k+1). rows_per_thread (4, 8
-   or 16) is the tuning knob of the generated kernel. out_shapes (optional) receives the shape count.
+   column's range, |value| x 2^k < 2^55), so |error| <= matched rows x 2^-(k+1); the scale does not
+   depend on the form, so every form gives the same sums. rows_per_thread picks the form of the generated
+   kernel: 4, 8 or 16 rows a thread in registers (plus 1 << 9 for 512-thread CTAs instead of 256), 0 the
+   shared-memory tile form, or CQLOPS_BATCH_AUTOTUNE: the form timed fastest for the batch's plan shape,
+   each candidate timed on the shape's first batches. out_shapes (optional) receives the shape count.
    Refuses programs with string comparisons. */
 int cqlops_batch_filter_aggregate(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
                                   const int32_t* sum_columns, uint32_t rows_per_thread, uint64_t* out_counts, double* out_sums,
                                   uint32_t* out_shapes);
+#define CQLOPS_BATCH_AUTOTUNE 0xffffffffu
+/* The form the calling thread's last batched scan ran in: rows a thread in bits 0-7 (0 the tile form),
+   the block size / 256 in bits 8-15 (0 or 1: 256 threads), bit 16 set when the run was an autotuner trial. */
+uint32_t cqlops_batch_last_form(void);
+/* Forgets every tuned plan shape (each is timed again from its next batch). */
+void cqlops_batch_tuner_reset(void);
 
 /* A shape catalog for a stream of batches over one table: the WHERE shapes, column types and summed
    columns its batches have met, in the order met (at most 64 shapes). A batch run with a catalog
