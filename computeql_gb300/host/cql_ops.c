@@ -95,7 +95,22 @@ static uint32_t shader_width(const CqlColumn* c)
 /* ------------------------------------------------------------------------------------------------
  * SUM / MIN / MAX of whole columns: qe_aggregate_global_streamed (query_exec.c:8842-9112) */
 
+/* The workgroup partials folded, in workgroup order, into running totals that start at io_* (reset: at
+   0, +F64_MAX and -F64_MAX, qe_agg_stream_begin) */
+static int aggregate_global_fold(const CqlColumn* columns, uint32_t column_count, double* io_sum, double* io_min, double* io_max, int reset);
+
 int cqlops_aggregate_global(const CqlColumn* columns, uint32_t column_count, double* out_sum, double* out_min, double* out_max)
+{
+  return aggregate_global_fold(columns, column_count, out_sum, out_min, out_max, 1);
+}
+
+int cqlops_aggregate_global_accumulate(const CqlColumn* columns, uint32_t column_count, double* io_sum, double* io_min, double* io_max)
+{
+  if (!io_sum || !io_min || !io_max) return refuse("the running totals are required");
+  return aggregate_global_fold(columns, column_count, io_sum, io_min, io_max, 0);
+}
+
+static int aggregate_global_fold(const CqlColumn* columns, uint32_t column_count, double* out_sum, double* out_min, double* out_max, int reset)
 {
   launches_begin();
   if (column_count == 0 || column_count > QE_AGG_STREAM_MAX_COLUMNS)
@@ -117,9 +132,9 @@ int cqlops_aggregate_global(const CqlColumn* columns, uint32_t column_count, dou
     {
       return 0;
     }
-    sum[c] = 0.0;
-    mn[c] = QE_F64_MAX;
-    mx[c] = -QE_F64_MAX;
+    sum[c] = reset ? 0.0 : out_sum[c];
+    mn[c] = reset ? QE_F64_MAX : out_min[c];
+    mx[c] = reset ? -QE_F64_MAX : out_max[c];
     if (col->width == 3)
     {
       /* base + row number: n * first + n * (n - 1) / 2 in 64-bit whole numbers, rounded once (:8906-8916) */
@@ -128,9 +143,9 @@ int cqlops_aggregate_global(const CqlColumn* columns, uint32_t column_count, dou
       if (n > 0)
       {
         int64_t total = first * (int64_t)n + (int64_t)(n * (n - 1) / 2);
-        sum[c] = (double)total;
-        mn[c] = (double)first;
-        mx[c] = (double)first + (double)(n - 1);
+        sum[c] += (double)total;
+        mn[c] = (double)first < mn[c] ? (double)first : mn[c];
+        mx[c] = (double)first + (double)(n - 1) > mx[c] ? (double)first + (double)(n - 1) : mx[c];
       }
     }
     else

@@ -773,103 +773,74 @@ static int lut_join_aggregate(const CqlJoinAgg* q, uint32_t core_count, const ui
   return result;
 }
 
-int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* out_groups, uint64_t* out_group_dim_row, double* out_results,
-                          uint32_t* out_strategy)
+typedef struct
 {
-  cqlops_note_error("");
+  int by_dim_row;          /* totals per dim row (the probe), else per key value from min_key (dense) */
+  uint64_t total_groups;
+  int64_t min_key;
+  uint64_t* counts;
+  int64_t *sums, *mins, *maxs;
+} JoinTotals;
+
+static void join_totals_free(JoinTotals* t)
+{
+  free(t->counts);
+  free(t->sums);
+  free(t->mins);
+  free(t->maxs);
+  memset(t, 0, sizeof(*t));
+}
+
+/* The fact-side totals: dense over the fact key's range (strategy 1, or 0 with a range of at most 65536
+   values), else per dim row by probing a table of the dim keys (:8607-8617) */
+static int join_totals(const CqlJoinAgg* q, uint32_t core_count, const uint32_t* core_funcs, const CqlColumn* const* core_cols, JoinTotals* t)
+{
   const CqlColumn* fk = q->fact_key;
-  if (!fk || !(fk->type == CQLOPS_TYPE_U32 || fk->type == CQLOPS_TYPE_I32) || !q->dim_keys || q->expr_count == 0 || q->expr_count > 8)
-    return refuse("a U32/I32 fact key, the dim keys and 1 to 8 aggregates");
-  if (!cqlops_rows_fit(fk->rows)) return 0;
-  for (uint32_t e = 0; e < q->expr_count; e++)
-    if (q->fact_args && q->fact_args[e] && !cqlops_rows_fit(q->fact_args[e]->rows)) return 0;
-  /* the fact-side totals each expression needs: AVG is a SUM and the count (:8558-8583) */
-  uint32_t core_funcs[8];
-  const CqlColumn* core_cols[8];
-  uint32_t core_count = 0, core_of_expr[8];
-  for (uint32_t e = 0; e < q->expr_count; e++)
-  {
-    uint32_t f = q->funcs[e];
-    if (f > CQLOPS_FUNC_MAX) return refuse("unsupported aggregate function");
-    core_of_expr[e] = 0;
-    if (f == CQLOPS_FUNC_COUNT || (q->dim_args && q->dim_args[e])) continue;
-    uint32_t cf = f == CQLOPS_FUNC_AVG ? CQLOPS_FUNC_SUM : f;
-    const CqlColumn* col = q->fact_args[e];
-    uint32_t i = 0;
-    while (i < core_count && !(core_funcs[i] == cf && core_cols[i] == col)) i++;
-    if (i == core_count)
-    {
-      core_funcs[core_count] = cf;
-      core_cols[core_count] = col;
-      core_count++;
-    }
-    core_of_expr[e] = i;
-  }
-  if (core_count == 0)
-  {
-    core_funcs[0] = CQLOPS_FUNC_COUNT;
-    core_cols[0] = NULL;
-    core_count = 1;
-  }
   uint64_t rows = fk->rows;
-  /* totals per key: dense over a small key range, else per dim row by probing (:8607-8617) */
   uint64_t groups_cap = fk->has_range ? (uint64_t)(fk->zone_max - fk->zone_min) + 1 : 0;
-  /* a mid-sized key range: through a lookup table on the device when the dim side allows it */
-  if (q->strategy == 3 || (q->strategy == 0 && fk->has_range && groups_cap > 65536))
-  {
-    int r = lut_join_aggregate(q, core_count, core_funcs, core_cols, core_of_expr, max_groups, out_groups, out_group_dim_row, out_results);
-    if (r >= 0)
-    {
-      if (r == 1 && out_strategy) *out_strategy = 3u;
-      return r;
-    }
-    if (q->strategy == 3) return refuse("the lookup-table join needs unique dim keys, one small whole-number GROUP BY value and no dim-side aggregates");
-    cqlops_note_error("");
-  }
-  int by_dim_row = 0;
-  uint64_t total_groups = 0;
-  int64_t min_key = 0;
-  uint64_t* counts = NULL;
-  int64_t *sums = NULL, *mins = NULL, *maxs = NULL;
+  memset(t, 0, sizeof(*t));
   int ok = 0;
   if (q->strategy != 2 && fk->has_range && groups_cap <= 65536)
   {
-    counts = (uint64_t*)malloc(groups_cap * 8);
-    sums = (int64_t*)malloc(groups_cap * core_count * 8);
-    mins = (int64_t*)malloc(groups_cap * core_count * 8);
-    maxs = (int64_t*)malloc(groups_cap * core_count * 8);
-    ok = counts && sums && mins && maxs &&
-         cqlops_group_dense(fk, rows, core_count, core_funcs, core_cols, groups_cap, &total_groups, &min_key, counts, sums, mins, maxs);
-    if (!ok)
-    {
-      free(counts);
-      free(sums);
-      free(mins);
-      free(maxs);
-      counts = NULL;
-      sums = mins = maxs = NULL;
-    }
+    t->counts = (uint64_t*)malloc(groups_cap * 8);
+    t->sums = (int64_t*)malloc(groups_cap * core_count * 8);
+    t->mins = (int64_t*)malloc(groups_cap * core_count * 8);
+    t->maxs = (int64_t*)malloc(groups_cap * core_count * 8);
+    ok = t->counts && t->sums && t->mins && t->maxs &&
+         cqlops_group_dense(fk, rows, core_count, core_funcs, core_cols, groups_cap, &t->total_groups, &t->min_key, t->counts, t->sums, t->mins,
+                            t->maxs);
+    if (!ok) join_totals_free(t);
   }
   if (!ok)
   {
     if (q->strategy == 1) return refuse("the fact key's range is not small enough for the dense path");
-    by_dim_row = 1;
+    t->by_dim_row = 1;
     uint64_t D = q->dim_table_rows;
-    counts = (uint64_t*)malloc(D * 8);
-    sums = (int64_t*)malloc(D * core_count * 8);
-    mins = (int64_t*)malloc(D * core_count * 8);
-    maxs = (int64_t*)malloc(D * core_count * 8);
-    ok = counts && sums && mins && maxs && probe_totals(q, core_count, core_funcs, core_cols, counts, sums, mins, maxs);
-    total_groups = D;
+    t->counts = (uint64_t*)malloc(D * 8);
+    t->sums = (int64_t*)malloc(D * core_count * 8);
+    t->mins = (int64_t*)malloc(D * core_count * 8);
+    t->maxs = (int64_t*)malloc(D * core_count * 8);
+    ok = t->counts && t->sums && t->mins && t->maxs && probe_totals(q, core_count, core_funcs, core_cols, t->counts, t->sums, t->mins, t->maxs);
+    t->total_groups = D;
   }
-  if (!ok)
-  {
-    free(counts);
-    free(sums);
-    free(mins);
-    free(maxs);
-    return 0;
-  }
+  if (!ok) join_totals_free(t);
+  return ok;
+}
+
+/* The dim-row pass over the totals and the outputs (:8619-8776); frees the totals. */
+static int join_finish(const CqlJoinAgg* q, JoinTotals* t, const uint32_t* core_of_expr, uint32_t core_count, uint64_t max_groups,
+                       uint64_t* out_groups, uint64_t* out_group_dim_row, double* out_results, uint32_t* out_strategy)
+{
+  const CqlColumn* fk = q->fact_key;
+  int ok = 1;
+  int by_dim_row = t->by_dim_row;
+  uint64_t total_groups = t->total_groups;
+  int64_t min_key = t->min_key;
+  uint64_t* counts = t->counts;
+  int64_t* sums = t->sums;
+  int64_t* mins = t->mins;
+  int64_t* maxs = t->maxs;
+  memset(t, 0, sizeof(*t));
   /* each (filtered) dim row meets its key's totals and joins the group of its group values (:8619-8720);
      the group tables start small and grow with the groups found */
   uint64_t visits = q->dim_rows ? q->dim_count : q->dim_table_rows;
@@ -984,4 +955,230 @@ int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* ou
   free(mins);
   free(maxs);
   return ok;
+}
+
+/* The fact-side totals each expression needs (:8558-8583): AVG is a SUM and the count, equal
+   (function, column) pairs are one total, COUNT-only queries still count */
+static int join_core_plan(const CqlJoinAgg* q, uint32_t* core_funcs, const CqlColumn** core_cols, uint32_t* out_core_count,
+                          uint32_t* core_of_expr)
+{
+  uint32_t core_count = 0;
+  for (uint32_t e = 0; e < q->expr_count; e++)
+  {
+    uint32_t f = q->funcs[e];
+    if (f > CQLOPS_FUNC_MAX) return refuse("unsupported aggregate function");
+    core_of_expr[e] = 0;
+    if (f == CQLOPS_FUNC_COUNT || (q->dim_args && q->dim_args[e])) continue;
+    uint32_t cf = f == CQLOPS_FUNC_AVG ? CQLOPS_FUNC_SUM : f;
+    const CqlColumn* col = q->fact_args[e];
+    uint32_t i = 0;
+    while (i < core_count && !(core_funcs[i] == cf && core_cols[i] == col)) i++;
+    if (i == core_count)
+    {
+      core_funcs[core_count] = cf;
+      core_cols[core_count] = col;
+      core_count++;
+    }
+    core_of_expr[e] = i;
+  }
+  if (core_count == 0)
+  {
+    core_funcs[0] = CQLOPS_FUNC_COUNT;
+    core_cols[0] = NULL;
+    core_count = 1;
+  }
+  *out_core_count = core_count;
+  return 1;
+}
+
+int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* out_groups, uint64_t* out_group_dim_row, double* out_results,
+                          uint32_t* out_strategy)
+{
+  cqlops_note_error("");
+  const CqlColumn* fk = q->fact_key;
+  if (!fk || !(fk->type == CQLOPS_TYPE_U32 || fk->type == CQLOPS_TYPE_I32) || !q->dim_keys || q->expr_count == 0 || q->expr_count > 8)
+    return refuse("a U32/I32 fact key, the dim keys and 1 to 8 aggregates");
+  if (!cqlops_rows_fit(fk->rows)) return 0;
+  for (uint32_t e = 0; e < q->expr_count; e++)
+    if (q->fact_args && q->fact_args[e] && !cqlops_rows_fit(q->fact_args[e]->rows)) return 0;
+  uint32_t core_funcs[8];
+  const CqlColumn* core_cols[8];
+  uint32_t core_count = 0, core_of_expr[8];
+  if (!join_core_plan(q, core_funcs, core_cols, &core_count, core_of_expr)) return 0;
+  /* totals per key: dense over a small key range, else per dim row by probing (:8607-8617) */
+  uint64_t groups_cap = fk->has_range ? (uint64_t)(fk->zone_max - fk->zone_min) + 1 : 0;
+  /* a mid-sized key range: through a lookup table on the device when the dim side allows it */
+  if (q->strategy == 3 || (q->strategy == 0 && fk->has_range && groups_cap > 65536))
+  {
+    int r = lut_join_aggregate(q, core_count, core_funcs, core_cols, core_of_expr, max_groups, out_groups, out_group_dim_row, out_results);
+    if (r >= 0)
+    {
+      if (r == 1 && out_strategy) *out_strategy = 3u;
+      return r;
+    }
+    if (q->strategy == 3) return refuse("the lookup-table join needs unique dim keys, one small whole-number GROUP BY value and no dim-side aggregates");
+    cqlops_note_error("");
+  }
+  JoinTotals totals;
+  if (!join_totals(q, core_count, core_funcs, core_cols, &totals)) return 0;
+  return join_finish(q, &totals, core_of_expr, core_count, max_groups, out_groups, out_group_dim_row, out_results, out_strategy);
+}
+
+/* ---- the fact side streamed through the resident cache (qe_join_probe_stream_core) ---- */
+
+int cqlops_join_aggregate_streamed(CqlResident* r, const CqlJoinAgg* query, const CqlHostColumn* fact_key, const CqlHostColumn* const* fact_args,
+                                   uint64_t rows, uint64_t chunk_rows, uint64_t max_groups, uint64_t* out_groups, uint64_t* out_group_dim_row,
+                                   double* out_results, uint32_t* out_strategy, uint64_t* out_uploaded_bytes)
+{
+  cqlops_note_error("");
+  if (out_uploaded_bytes) *out_uploaded_bytes = 0;
+  if (!r || !query || !fact_key || !(fact_key->type == CQLOPS_TYPE_U32 || fact_key->type == CQLOPS_TYPE_I32) || !fact_key->values ||
+      !query->dim_keys || query->expr_count == 0 || query->expr_count > 8)
+    return refuse("a U32/I32 host fact key, the dim keys and 1 to 8 aggregates");
+  if (query->strategy == 3) return refuse("the lookup-table join does not stream");
+  if (!cqlops_rows_fit(rows)) return 0;
+  if (chunk_rows == 0) chunk_rows = 1u << 24;
+  /* dense over the key's whole range when it is small, else the probe: the same for every chunk */
+  uint64_t range = fact_key->has_range ? (uint64_t)(fact_key->zone_max - fact_key->zone_min) + 1 : 0;
+  uint32_t strategy = query->strategy ? query->strategy : (fact_key->has_range && range <= 65536 ? 1u : 2u);
+  JoinTotals acc;
+  memset(&acc, 0, sizeof(acc));
+  int have = 0, ok = 1;
+  uint32_t core_funcs[8], core_count = 0, core_of_expr[8];
+  const CqlColumn* core_cols[8];
+  CqlColumn kc;
+  CqlJoinAgg qc;
+  for (uint64_t start = 0; ok && (start < rows || !have); start += chunk_rows)
+  {
+    uint64_t n = rows - start < chunk_rows ? rows - start : chunk_rows;
+    CqlColumn ac[8];
+    const CqlColumn* argp[8] = { NULL };
+    CqlBuffer* held[9];
+    uint32_t nheld = 0;
+    memset(&kc, 0, sizeof(kc));
+    if (n > 0)
+    {
+      /* the chunk's fact columns from the cache; a host column met twice is one device column */
+      int hit = 0;
+      CqlBuffer* b = (CqlBuffer*)cqlops_resident_acquire(r, fact_key->uid, fact_key->generation, (const char*)fact_key->values + start * 4,
+                                                         start, n, 4, &hit);
+      if (!b)
+      {
+        ok = refuse("a chunk could not be held in the cache");
+        break;
+      }
+      if (!hit && out_uploaded_bytes) *out_uploaded_bytes += n * 4;
+      held[nheld++] = b;
+      kc.buffer = b;
+    }
+    kc.type = fact_key->type;
+    kc.rows = n;
+    kc.has_range = fact_key->has_range;
+    kc.zone_min = fact_key->zone_min;
+    kc.zone_max = fact_key->zone_max;
+    for (uint32_t e = 0; ok && e < query->expr_count; e++)
+    {
+      const CqlHostColumn* h = fact_args ? fact_args[e] : NULL;
+      if (!h) continue;
+      if (h == fact_key)
+      {
+        argp[e] = &kc;
+        continue;
+      }
+      uint32_t same = e;
+      for (uint32_t j = 0; j < e; j++)
+        if (fact_args[j] == h && argp[j]) same = j;
+      if (same != e)
+      {
+        argp[e] = argp[same];
+        continue;
+      }
+      if (!(h->type == CQLOPS_TYPE_U32 || h->type == CQLOPS_TYPE_I32) || !h->values)
+      {
+        ok = refuse("fact-side aggregates take U32/I32 host columns");
+        break;
+      }
+      memset(&ac[e], 0, sizeof(ac[e]));
+      if (n > 0)
+      {
+        int hit = 0;
+        CqlBuffer* b = (CqlBuffer*)cqlops_resident_acquire(r, h->uid, h->generation, (const char*)h->values + start * 4, start, n, 4, &hit);
+        if (!b)
+        {
+          ok = refuse("a chunk could not be held in the cache");
+          break;
+        }
+        if (!hit && out_uploaded_bytes) *out_uploaded_bytes += n * 4;
+        held[nheld++] = b;
+        ac[e].buffer = b;
+      }
+      ac[e].type = h->type;
+      ac[e].rows = n;
+      ac[e].has_range = h->has_range;
+      ac[e].zone_min = h->zone_min;
+      ac[e].zone_max = h->zone_max;
+      argp[e] = &ac[e];
+    }
+    qc = *query;
+    qc.fact_key = &kc;
+    qc.fact_args = argp;
+    qc.strategy = strategy;
+    JoinTotals t;
+    memset(&t, 0, sizeof(t));
+    if (ok) ok = join_core_plan(&qc, core_funcs, core_cols, &core_count, core_of_expr);
+    if (ok && n == 0)
+    {
+      /* no fact rows: empty totals of the chosen layout */
+      t.by_dim_row = strategy == 2;
+      t.total_groups = t.by_dim_row ? qc.dim_table_rows : range;
+      t.min_key = (int64_t)fact_key->zone_min;
+      t.counts = (uint64_t*)calloc(t.total_groups ? t.total_groups : 1, 8);
+      t.sums = (int64_t*)calloc((t.total_groups ? t.total_groups : 1) * core_count, 8);
+      t.mins = (int64_t*)malloc((t.total_groups ? t.total_groups : 1) * core_count * 8);
+      t.maxs = (int64_t*)malloc((t.total_groups ? t.total_groups : 1) * core_count * 8);
+      ok = t.counts && t.sums && t.mins && t.maxs;
+      for (uint64_t i = 0; ok && i < t.total_groups * core_count; i++)
+      {
+        t.mins[i] = INT32_MAX;
+        t.maxs[i] = INT32_MIN;
+      }
+      if (!ok) join_totals_free(&t);
+    }
+    else if (ok)
+      ok = join_totals(&qc, core_count, core_funcs, core_cols, &t);
+    for (uint32_t i = 0; i < nheld; i++) cqlops_resident_release(r, held[i]);
+    if (!ok) break;
+    if (!have)
+    {
+      acc = t;
+      have = 1;
+      continue;
+    }
+    if (t.by_dim_row != acc.by_dim_row || t.total_groups != acc.total_groups || t.min_key != acc.min_key)
+    {
+      join_totals_free(&t);
+      ok = refuse("a chunk's totals did not line up with the first chunk's");
+      break;
+    }
+    for (uint64_t g = 0; g < t.total_groups; g++)
+    {
+      acc.counts[g] += t.counts[g];
+      for (uint32_t c = 0; c < core_count; c++)
+      {
+        uint64_t i = g * core_count + c;
+        acc.sums[i] += t.sums[i];
+        if (t.mins[i] < acc.mins[i]) acc.mins[i] = t.mins[i];
+        if (t.maxs[i] > acc.maxs[i]) acc.maxs[i] = t.maxs[i];
+      }
+    }
+    join_totals_free(&t);
+  }
+  if (!ok)
+  {
+    join_totals_free(&acc);
+    return 0;
+  }
+  /* the dim-row pass once, over the chunks' totals */
+  qc.fact_args = NULL;
+  return join_finish(&qc, &acc, core_of_expr, core_count, max_groups, out_groups, out_group_dim_row, out_results, out_strategy);
 }

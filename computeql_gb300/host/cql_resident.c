@@ -358,6 +358,7 @@ CqlResidentStats cqlops_resident_stats(CqlResident* r)
 }
 
 void cqlops_note_error(const char* why);
+int cqlops_rows_fit(uint64_t rows);
 
 static int refuse(const char* why)
 {
@@ -381,8 +382,8 @@ int cqlops_aggregate_global_streamed(CqlResident* r, uint64_t column_uid, uint64
   uint32_t width = type == CQLOPS_TYPE_F64 ? 8 : (type == CQLOPS_TYPE_U32 || type == CQLOPS_TYPE_I32 || type == CQLOPS_TYPE_F32) ? 4 : 0;
   if (!width || !host_values || !out_sum || !out_min || !out_max) return refuse("a U32/I32/F32/F64 host column and its outputs");
   if (chunk_rows == 0) chunk_rows = 1u << 24;
-  double sum = 0.0, mn = 0.0, mx = 0.0;
-  int seen = 0;
+  /* one running total over every workgroup partial of every chunk (qe_agg_stream_begin / _retire) */
+  double sum = 0.0, mn = 1.7976931348623157e308, mx = -1.7976931348623157e308;
   for (uint64_t start = 0; start < rows; start += chunk_rows)
   {
     uint64_t n = rows - start < chunk_rows ? rows - start : chunk_rows;
@@ -395,17 +396,186 @@ int cqlops_aggregate_global_streamed(CqlResident* r, uint64_t column_uid, uint64
     col.type = type;
     col.rows = n;
     col.buffer = b;
-    double s = 0.0, lo = 0.0, hi = 0.0;
-    int ok = cqlops_aggregate_global(&col, 1, &s, &lo, &hi);
+    int ok = cqlops_aggregate_global_accumulate(&col, 1, &sum, &mn, &mx);
     cqlops_resident_release(r, b);
     if (!ok) return 0;
-    sum += s;
-    if (!seen || lo < mn) mn = lo;
-    if (!seen || hi > mx) mx = hi;
-    seen = 1;
   }
   *out_sum = sum;
   *out_min = mn;
   *out_max = mx;
+  return 1;
+}
+
+/* ---- streamed scan and dense group-by over the cache ---- */
+
+static uint32_t host_width(uint32_t type)
+{
+  return type == CQLOPS_TYPE_F64 ? 8u : (type == CQLOPS_TYPE_U32 || type == CQLOPS_TYPE_I32 || type == CQLOPS_TYPE_F32) ? 4u : 0u;
+}
+
+/* a chunk of a host column as a device column: from the cache, or uploaded into it */
+static int chunk_column(CqlResident* r, const CqlHostColumn* h, uint64_t start, uint64_t n, CqlColumn* out, uint64_t* uploaded)
+{
+  uint32_t width = host_width(h->type);
+  if (!width || !h->values) return refuse("streamed columns are U32, I32, F32 or F64 host columns");
+  int hit = 0;
+  CqlBuffer* b = (CqlBuffer*)cqlops_resident_acquire(r, h->uid, h->generation, (const char*)h->values + start * width, start, n, width, &hit);
+  if (!b) return refuse("a chunk could not be held in the cache");
+  if (!hit && uploaded) *uploaded += n * width;
+  memset(out, 0, sizeof(*out));
+  out->type = h->type;
+  out->rows = n;
+  out->buffer = b;
+  out->has_range = h->has_range;
+  out->zone_min = h->zone_min;
+  out->zone_max = h->zone_max;
+  return 1;
+}
+
+int cqlops_scan_simple_streamed(CqlResident* r, const CqlHostColumn* columns, uint32_t column_count, uint64_t rows, const CqlLeaf* leaves,
+                                uint32_t leaf_count, uint64_t chunk_rows, uint64_t* out_count, uint32_t* out_rows, uint64_t out_capacity,
+                                uint64_t* out_uploaded_bytes)
+{
+  cqlops_note_error("");
+  if (out_uploaded_bytes) *out_uploaded_bytes = 0;
+  if (!r || r->ops.alloc != dev_alloc) return refuse("the streamed scan takes a cache of backend buffers (created with ops NULL)");
+  if (!columns || column_count == 0 || column_count > CQLOPS_MAX_BINDINGS || !out_count) return refuse("1 to 10 columns and a count");
+  if (!cqlops_rows_fit(rows)) return 0;
+  if (chunk_rows == 0) chunk_rows = 1u << 24;
+  uint64_t total = 0;
+  for (uint64_t start = 0; start < rows; start += chunk_rows)
+  {
+    uint64_t n = rows - start < chunk_rows ? rows - start : chunk_rows;
+    CqlColumn cols[CQLOPS_MAX_BINDINGS];
+    uint32_t held = 0;
+    int ok = 1;
+    for (uint32_t c = 0; c < column_count && ok; c++)
+    {
+      ok = chunk_column(r, &columns[c], start, n, &cols[c], out_uploaded_bytes);
+      if (ok) held++;
+    }
+    uint64_t got = 0;
+    uint64_t room = out_rows && out_capacity > total ? out_capacity - total : 0;
+    if (ok) ok = cqlops_scan_simple(cols, column_count, leaves, leaf_count, &got, room ? out_rows + total : NULL, room);
+    for (uint32_t c = 0; c < held; c++) cqlops_resident_release(r, cols[c].buffer);
+    if (!ok) return 0;
+    /* the chunk's rows are its own: offset by its first row */
+    uint64_t kept = got < room ? got : room;
+    for (uint64_t i = 0; i < kept; i++) out_rows[total + i] += (uint32_t)start;
+    total += got;
+  }
+  *out_count = total;
+  return 1;
+}
+
+int cqlops_group_dense_streamed(CqlResident* r, const CqlHostColumn* key, uint64_t rows, uint32_t expr_count, const uint32_t* funcs,
+                                const CqlHostColumn* const* args, uint64_t chunk_rows, uint64_t max_groups, uint64_t* out_group_count,
+                                int64_t* out_min_key, uint64_t* out_counts, int64_t* out_sums, int64_t* out_mins, int64_t* out_maxs,
+                                uint64_t* out_uploaded_bytes)
+{
+  cqlops_note_error("");
+  if (out_uploaded_bytes) *out_uploaded_bytes = 0;
+  if (!r || r->ops.alloc != dev_alloc) return refuse("the streamed group-by takes a cache of backend buffers (created with ops NULL)");
+  if (!key || !key->has_range || expr_count == 0 || expr_count > 4) return refuse("a key with its range and 1 to 4 aggregates");
+  if (!out_group_count || !out_min_key || !out_counts || !out_sums || !out_mins || !out_maxs) return refuse("every output array is required");
+  if (!cqlops_rows_fit(rows)) return 0;
+  if (chunk_rows == 0) chunk_rows = 1u << 24;
+  uint64_t groups = (uint64_t)(key->zone_max - key->zone_min) + 1;
+  if (groups > max_groups) return refuse("the output arrays hold fewer groups than the key's range");
+  uint64_t* c_counts = (uint64_t*)malloc(groups * 8);
+  int64_t* c_sums = (int64_t*)malloc(groups * expr_count * 8);
+  int64_t* c_mins = (int64_t*)malloc(groups * expr_count * 8);
+  int64_t* c_maxs = (int64_t*)malloc(groups * expr_count * 8);
+  int ok = c_counts && c_sums && c_mins && c_maxs;
+  int first = 1;
+  uint64_t g_count = 0;
+  int64_t min_key = 0;
+  for (uint64_t start = 0; ok && start < rows; start += chunk_rows)
+  {
+    uint64_t n = rows - start < chunk_rows ? rows - start : chunk_rows;
+    CqlColumn kc, ac[4];
+    const CqlColumn* argp[4] = { NULL, NULL, NULL, NULL };
+    CqlBuffer* held[5];
+    uint32_t nheld = 0;
+    ok = chunk_column(r, key, start, n, &kc, out_uploaded_bytes);
+    if (ok) held[nheld++] = kc.buffer;
+    for (uint32_t e = 0; ok && e < expr_count; e++)
+    {
+      if (!args || !args[e] || funcs[e] == CQLOPS_FUNC_COUNT) continue;
+      if (args[e] == key)
+      {
+        argp[e] = &kc;
+        continue;
+      }
+      uint32_t same = e;
+      for (uint32_t j = 0; j < e; j++)
+        if (args && args[j] == args[e] && argp[j]) same = j;
+      if (same != e)
+      {
+        argp[e] = argp[same];
+        continue;
+      }
+      ok = chunk_column(r, args[e], start, n, &ac[e], out_uploaded_bytes);
+      if (ok)
+      {
+        held[nheld++] = ac[e].buffer;
+        argp[e] = &ac[e];
+      }
+    }
+    /* the first chunk writes straight into the outputs, later chunks into the chunk arrays, folded after */
+    uint64_t gc = 0;
+    int64_t mk = 0;
+    if (ok)
+      ok = first ? cqlops_group_dense(&kc, n, expr_count, funcs, argp, max_groups, &gc, &mk, out_counts, out_sums, out_mins, out_maxs)
+                 : cqlops_group_dense(&kc, n, expr_count, funcs, argp, groups, &gc, &mk, c_counts, c_sums, c_mins, c_maxs);
+    for (uint32_t i = 0; i < nheld; i++) cqlops_resident_release(r, held[i]);
+    if (!ok) break;
+    if (first)
+    {
+      g_count = gc;
+      min_key = mk;
+      first = 0;
+      continue;
+    }
+    if (gc != g_count || mk != min_key)
+    {
+      ok = refuse("a chunk's groups did not line up with the key's range");
+      break;
+    }
+    for (uint64_t g = 0; g < gc; g++)
+    {
+      out_counts[g] += c_counts[g];
+      for (uint32_t e = 0; e < expr_count; e++)
+      {
+        uint64_t i = g * expr_count + e;
+        out_sums[i] += c_sums[i];
+        if (c_mins[i] < out_mins[i]) out_mins[i] = c_mins[i];
+        if (c_maxs[i] > out_maxs[i]) out_maxs[i] = c_maxs[i];
+      }
+    }
+  }
+  free(c_counts);
+  free(c_sums);
+  free(c_mins);
+  free(c_maxs);
+  if (!ok) return 0;
+  if (first)
+  {
+    /* no rows: the groups of the key's range, all empty */
+    g_count = groups;
+    min_key = (int64_t)key->zone_min;
+    for (uint64_t g = 0; g < groups; g++)
+    {
+      out_counts[g] = 0;
+      for (uint32_t e = 0; e < expr_count; e++)
+      {
+        out_sums[g * expr_count + e] = 0;
+        out_mins[g * expr_count + e] = INT32_MAX;
+        out_maxs[g * expr_count + e] = INT32_MIN;
+      }
+    }
+  }
+  *out_group_count = g_count;
+  *out_min_key = min_key;
   return 1;
 }

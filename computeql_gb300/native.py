@@ -37,6 +37,10 @@ class CqlColumn(C.Structure):
                 ("zone_min", dbl), ("zone_max", dbl), ("offsets", P), ("dict", P), ("zone_map", P), ("zone_map_chunks", u64)]
 
 
+class CqlHostColumn(C.Structure):
+    _fields_ = [("uid", u64), ("generation", u64), ("values", P), ("type", u32), ("has_range", u32), ("zone_min", dbl), ("zone_max", dbl)]
+
+
 class CqlServeConfig(C.Structure):
     _fields_ = [("workers", u32), ("fuse", u32), ("max_fuse", u32), ("rows_per_thread", u32), ("memory_budget", u64)]
 
@@ -221,6 +225,10 @@ OPS_API = [
     ("cqlops_resident_clear", None, [P]),
     ("cqlops_resident_stats", CqlResidentStats, [P]),
     ("cqlops_aggregate_global_streamed", C.c_int, [P, u64, u64, P, u32, u64, u64, P, P, P, P]),
+    ("cqlops_aggregate_global_accumulate", C.c_int, [P, u32, P, P, P]),
+    ("cqlops_scan_simple_streamed", C.c_int, [P, P, u32, u64, P, u32, u64, P, P, u64, P]),
+    ("cqlops_group_dense_streamed", C.c_int, [P, P, u64, u32, P, P, u64, u64, P, P, P, P, P, P, P]),
+    ("cqlops_join_aggregate_streamed", C.c_int, [P, P, P, P, u64, u64, u64, P, P, P, P, P]),
     ("cqlserve_create", P, [P]),
     ("cqlserve_destroy", None, [P]),
     ("cqlserve_add_table", C.c_int, [P, P, u32]),

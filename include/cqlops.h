@@ -211,6 +211,10 @@ int cqlops_fused_filter_group(const CqlProgram* prog, const CqlColumn* columns, 
 /* SUM/MIN/MAX of up to 4 whole columns (qe_aggregate_global_streamed, query_exec.c:8842-9112, one
    chunk). Partials are folded in workgroup order. Sequence columns are summed in closed form. */
 int cqlops_aggregate_global(const CqlColumn* columns, uint32_t column_count, double* out_sum, double* out_min, double* out_max);
+/* cqlops_aggregate_global adding every workgroup partial, in workgroup order, into running totals the
+   caller carries from chunk to chunk (qe_agg_stream_retire, query_exec.c:8812-8841: one column_sum over
+   every partial of every chunk; start them at 0, +F64_MAX and -F64_MAX). */
+int cqlops_aggregate_global_accumulate(const CqlColumn* columns, uint32_t column_count, double* io_sum, double* io_min, double* io_max);
 
 /* AND of up to 8 numeric comparisons over up to 10 columns with scan_simple
    (qe_scan_filter_selected, query_exec.c:2495-3276). Writes the match count; when out_rows is not
@@ -478,12 +482,55 @@ uint64_t cqlops_resident_evict(CqlResident* cache, uint64_t bytes_wanted);
 void cqlops_resident_clear(CqlResident* cache);
 CqlResidentStats cqlops_resident_stats(CqlResident* cache);
 
+/* A host column for the streamed operators: its identity in the cache (uid and write generation), its
+   values, and - for a key or a summed column - the whole column's range. */
+typedef struct CqlHostColumn
+{
+  uint64_t uid;
+  uint64_t generation;
+  const void* values;   /* `rows` values of `type` (U32, I32, F32 or F64) */
+  uint32_t type;
+  uint32_t has_range;
+  double zone_min;
+  double zone_max;
+} CqlHostColumn;
+
+/* cqlops_scan_simple over host columns streamed through the cache in chunks of chunk_rows (0: 16M):
+   qe_scan_filter_streamed (src/query_exec/query_exec.c:2242-2494). Each chunk's columns come from the
+   cache or are uploaded into it, the chunk is scanned, its rows are offset by the chunk's first row and
+   appended in order; the count is the chunks' total. The same count and rows as the resident scan. */
+int cqlops_scan_simple_streamed(CqlResident* cache, const CqlHostColumn* columns, uint32_t column_count, uint64_t rows, const CqlLeaf* leaves,
+                                uint32_t leaf_count, uint64_t chunk_rows, uint64_t* out_count, uint32_t* out_rows, uint64_t out_capacity,
+                                uint64_t* out_uploaded_bytes);
+
+/* cqlops_group_dense over host columns streamed through the cache: qe_aggregate_dense_streamed
+   (src/query_exec/query_exec.c:7984-8068). The groups are the key column's whole range (its zone), so
+   every chunk's groups line up; counts and sums are added and minimums and maximums kept chunk by
+   chunk, all in integers: the same results as the resident dense group-by. args[e] is NULL for COUNT. */
+int cqlops_group_dense_streamed(CqlResident* cache, const CqlHostColumn* key, uint64_t rows, uint32_t expr_count, const uint32_t* funcs,
+                                const CqlHostColumn* const* args, uint64_t chunk_rows, uint64_t max_groups, uint64_t* out_group_count,
+                                int64_t* out_min_key, uint64_t* out_counts, int64_t* out_sums, int64_t* out_mins, int64_t* out_maxs,
+                                uint64_t* out_uploaded_bytes);
+
+/* cqlops_join_aggregate with the fact side (the key and the argument columns) streamed from the host
+   through the cache: qe_join_probe_stream_core (src/query_exec/query_exec.c:8080-8420). Each chunk's
+   fact-side totals - per key value over the key's whole range (dense, a range of at most 65536 values)
+   or per dim row (the probe) - are added into running totals; the dim-row pass runs once at the end.
+   query->fact_key and query->fact_args are not read; fact_args[e] is NULL where query->funcs[e] takes no
+   fact column. The lookup-table strategy does not stream: strategy 3 is refused, 0 picks dense or probe. */
+int cqlops_join_aggregate_streamed(CqlResident* cache, const CqlJoinAgg* query, const CqlHostColumn* fact_key,
+                                   const CqlHostColumn* const* fact_args, uint64_t rows, uint64_t chunk_rows, uint64_t max_groups,
+                                   uint64_t* out_groups, uint64_t* out_group_dim_row, double* out_results, uint32_t* out_strategy,
+                                   uint64_t* out_uploaded_bytes);
+
 /* SUM/MIN/MAX of a host column (U32/I32/F32/F64, rows values at host_values) streamed through the
    cache in chunks of chunk_rows (0: 16M) - qe_aggregate_global_streamed, src/query_exec/query_exec.c:
    8842-9112: each chunk's device copy comes from the cache (keyed by column_uid, generation and the
-   chunk's rows) or is uploaded into it, is reduced by cqlops_aggregate_global, and the partials are folded
-   in chunk order. The cache must hold backend buffers (created with ops NULL). *out_uploaded_bytes
-   (optional) receives the bytes copied to the device: 0 when every chunk was cached. */
+   chunk's rows) or is uploaded into it, and every workgroup partial of every chunk is added, in chunk
+   then workgroup order, into one running sum, minimum and maximum that start at 0, +F64_MAX and
+   -F64_MAX (qe_agg_stream_retire, :8812-8841; an empty column gives those sentinels). The cache must
+   hold backend buffers (created with ops NULL). *out_uploaded_bytes (optional) receives the bytes copied
+   to the device: 0 when every chunk was cached. */
 int cqlops_aggregate_global_streamed(CqlResident* cache, uint64_t column_uid, uint64_t generation, const void* host_values, uint32_t type,
                                      uint64_t rows, uint64_t chunk_rows, double* out_sum, double* out_min, double* out_max,
                                      uint64_t* out_uploaded_bytes);
