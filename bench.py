@@ -549,7 +549,7 @@ def run_e2e(args, native, ops, t, queries, lib):
     # the uploads alone, one after another, for the link rate
     uploads = []
     stream = lib.cqlcuda_stream_alloc(1)
-    for i in range(2):
+    for i in range(3):
         t0 = time.perf_counter()
         for name, _ in plan:
             lib.cqlcuda_stream_slot_begin(stream, 0, n * 4, 0)

@@ -34,8 +34,11 @@ def stats(lib):
 
 def shape(k):
     """a distinct WHERE shape per k: an OR chain of k equalities, AND a range on amount"""
-    terms = " ".join(f"(= flag {3 * j})" for j in range(k))
-    return f"(and (or {terms}) (< amount {5000 + k}))"
+    terms = [f"(= flag {3 * j})" for j in range(k)]
+    chain = terms[0]
+    for t in terms[1:]:
+        chain = f"(or {chain} {t})"
+    return f"(and {chain} (< amount {5000 + k}))"
 
 
 def expected(k, flag, amount):
