@@ -327,7 +327,7 @@ __device__ __forceinline__ uint32_t join_read(const JoinDecode& d, int c, uint64
   return d.base[c] + ((w >> sh) & d.mask[c]);
 }
 
-__global__ void __launch_bounds__(JOIN_THREADS) k_join_probe_native(CqlLaunch a, uint64_t rows)
+__global__ void __launch_bounds__(JOIN_THREADS, 3) k_join_probe_native(CqlLaunch a, uint64_t rows)
 {
   JoinDecode d;
   uint32_t widths = cql_word(a, 1);
@@ -351,6 +351,9 @@ __global__ void __launch_bounds__(JOIN_THREADS) k_join_probe_native(CqlLaunch a,
   const uint32_t* bloom = (const uint32_t*)a.buf[11];
   uint32_t exprs = min(cql_word(a, 2), 8u), funcs = cql_word(a, 4), arg_index = cql_word(a, 6), arg_signed = cql_word(a, 7);
   uint32_t mask = cql_word(a, 8), log2_size = cql_word(a, 12), bloom_log2 = cql_word(a, 13);
+  uint32_t used_args = 0;   // the argument columns some aggregate reads
+  for (uint32_t e = 0; e < exprs; e++)
+    if (((funcs >> (e * 4)) & 0xfu) != JFUNC_COUNT) used_args |= 1u << ((arg_index >> (e * 4)) & 0x3u);
   uint32_t table_size = mask + 1;
   uint64_t count_cap = a.bytes[7] / 4;
   const uint32_t UNROLL = 8;
@@ -373,23 +376,39 @@ __global__ void __launch_bounds__(JOIN_THREADS) k_join_probe_native(CqlLaunch a,
       uint32_t bits = (1u << ((h2 >> 27) & 31u)) | (1u << ((h2 >> 22) & 31u));
       maybe[u] = at < rows && (bloom[h >> (32u - bloom_log2)] & bits) == bits;
     }
+    // every candidate's first table slot and argument words are loaded before any is used: the loads of
+    // the eight rows are in flight together instead of one probe's latency after another's
+    uint32_t slot0[UNROLL], key0[UNROLL], row0[UNROLL], argv[UNROLL][4];
+#pragma unroll
+    for (uint32_t u = 0; u < UNROLL; u++)
+    {
+      slot0[u] = (key[u] * 0x9E3779B1u) >> (32u - log2_size);
+      key0[u] = maybe[u] ? tkeys[slot0[u]] : 0u;
+      row0[u] = maybe[u] ? trows[slot0[u]] : 0u;
+#pragma unroll
+      for (uint32_t c = 0; c < 4; c++) argv[u][c] = (maybe[u] && ((used_args >> c) & 1u)) ? join_read(d, 1 + (int)c, base + u * stride) : 0u;
+    }
 #pragma unroll
     for (uint32_t u = 0; u < UNROLL; u++)
     {
       if (!maybe[u]) continue;
-      uint64_t row = base + u * stride;
-      uint32_t slot = (key[u] * 0x9E3779B1u) >> (32u - log2_size);
+      uint32_t slot = slot0[u];
       uint32_t found = 0;
-      for (uint32_t probe = 0; probe < table_size; probe++)
+      if (row0[u] != 0u && key0[u] == key[u]) found = row0[u];
+      else if (row0[u] != 0u)
       {
-        uint32_t r1 = trows[slot];
-        if (r1 == 0u) break;
-        if (tkeys[slot] == key[u])
-        {
-          found = r1;
-          break;
-        }
         slot = (slot + 1u) & mask;
+        for (uint32_t probe = 1; probe < table_size; probe++)
+        {
+          uint32_t r1 = trows[slot];
+          if (r1 == 0u) break;
+          if (tkeys[slot] == key[u])
+          {
+            found = r1;
+            break;
+          }
+          slot = (slot + 1u) & mask;
+        }
       }
       if (!found) continue;
       uint32_t dim_row = found - 1u;
@@ -400,7 +419,7 @@ __global__ void __launch_bounds__(JOIN_THREADS) k_join_probe_native(CqlLaunch a,
         uint32_t f = (funcs >> (e * 4)) & 0xfu;
         if (f == JFUNC_COUNT) continue;
         uint32_t ai = (arg_index >> (e * 4)) & 0x3u;
-        uint32_t w = join_read(d, 1 + (int)ai, row);
+        uint32_t w = ai == 0u ? argv[u][0] : ai == 1u ? argv[u][1] : ai == 2u ? argv[u][2] : argv[u][3];
         uint64_t index = (uint64_t)dim_row * exprs + e;
         if (f == JFUNC_SUM || f == JFUNC_AVG)
         {
@@ -470,7 +489,7 @@ __device__ __forceinline__ int join_mbar_wait(uint32_t bar)
   }
 }
 
-__global__ void __launch_bounds__(JOIN_SMEM_THREADS) k_join_probe_native_smem(CqlLaunch a, uint64_t rows, JoinSmemLayout L)
+__global__ void __launch_bounds__(JOIN_SMEM_THREADS, 2) k_join_probe_native_smem(CqlLaunch a, uint64_t rows, JoinSmemLayout L)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   JoinDecode d;
@@ -493,6 +512,9 @@ __global__ void __launch_bounds__(JOIN_SMEM_THREADS) k_join_probe_native_smem(Cq
   uint32_t* error = (uint32_t*)a.buf[12];
   const uint32_t exprs = L.exprs, funcs = cql_word(a, 4), arg_index = cql_word(a, 6), arg_signed = cql_word(a, 7);
   const uint32_t mask = L.size - 1u, log2_size = cql_word(a, 12), bloom_log2 = cql_word(a, 13);
+  uint32_t used_args = 0;   // the argument columns some aggregate reads
+  for (uint32_t e = 0; e < exprs; e++)
+    if (((funcs >> (e * 4)) & 0xfu) != JFUNC_COUNT) used_args |= 1u << ((arg_index >> (e * 4)) & 0x3u);
   const uint64_t count_cap = a.bytes[7] / 4;
   uint32_t* s_keys = (uint32_t*)(smem + L.keys);
   uint32_t* s_rows = (uint32_t*)(smem + L.trows);
@@ -553,11 +575,17 @@ __global__ void __launch_bounds__(JOIN_SMEM_THREADS) k_join_probe_native_smem(Cq
       uint32_t bits = (1u << ((h2 >> 27) & 31u)) | (1u << ((h2 >> 22) & 31u));
       maybe[u] = at < rows && (s_bloom[h >> (32u - bloom_log2)] & bits) == bits;
     }
+    // the argument words of every candidate row are loaded before the probes: their loads are in flight
+    // together, and the probes and totals that follow touch shared memory only
+    uint32_t argv[UNROLL][4];
+#pragma unroll
+    for (uint32_t u = 0; u < UNROLL; u++)
+#pragma unroll
+      for (uint32_t c = 0; c < 4; c++) argv[u][c] = (maybe[u] && ((used_args >> c) & 1u)) ? join_read(d, 1 + (int)c, base + u * stride) : 0u;
 #pragma unroll
     for (uint32_t u = 0; u < UNROLL; u++)
     {
       if (!maybe[u]) continue;
-      uint64_t row = base + u * stride;
       uint32_t slot = (key[u] * 0x9E3779B1u) >> (32u - log2_size);
       bool found = false;
       for (uint32_t probe = 0; probe < L.size; probe++)
@@ -578,7 +606,7 @@ __global__ void __launch_bounds__(JOIN_SMEM_THREADS) k_join_probe_native_smem(Cq
         uint32_t f = (funcs >> (e * 4)) & 0xfu;
         if (f == JFUNC_COUNT) continue;
         uint32_t ai = (arg_index >> (e * 4)) & 0x3u;
-        uint32_t w = join_read(d, 1 + (int)ai, row);
+        uint32_t w = ai == 0u ? argv[u][0] : ai == 1u ? argv[u][1] : ai == 2u ? argv[u][2] : argv[u][3];
         uint32_t index = slot * exprs + e;
         if (f == JFUNC_SUM || f == JFUNC_AVG)
         {
@@ -637,15 +665,15 @@ static int launch_join_probe_native(const CqlLaunch& a, uint32_t gws, uint32_t l
           return (int)cudaGetLastError();
         attr_set = true;
       }
-      int per_sm = (int)std::max<uint32_t>(1u, std::min<uint32_t>(4u, (uint32_t)(g_cql_max_smem_optin / (L.total + 1024u))));
-      per_sm = std::min(per_sm, 2048 / JOIN_SMEM_THREADS);
+      // two CTAs an SM where their shared arrays fit (the register budget is set for two)
+      int per_sm = (int)std::max<uint32_t>(1u, std::min<uint32_t>(2u, (uint32_t)(g_cql_max_smem_optin / (L.total + 1024u))));
       k_join_probe_native_smem<<<cql_stream_grid((rows + JOIN_SMEM_THREADS * 8 - 1) / (JOIN_SMEM_THREADS * 8), per_sm), JOIN_SMEM_THREADS,
                                  L.total, stream>>>(a, rows, L);
       CQL_LAUNCH_CHECK();
       return 0;
     }
   }
-  k_join_probe_native<<<cql_stream_grid((rows + JOIN_THREADS * 8 - 1) / (JOIN_THREADS * 8), 8), JOIN_THREADS, 0, stream>>>(a, rows);
+  k_join_probe_native<<<cql_stream_grid((rows + JOIN_THREADS * 8 - 1) / (JOIN_THREADS * 8), 3), JOIN_THREADS, 0, stream>>>(a, rows);
   CQL_LAUNCH_CHECK();
   return 0;
 }
