@@ -120,14 +120,16 @@ def make_queries(ops, t, rng_key, dims):
     def q5():
         return ops.scan_simple([t.id], [(0, ops.CMP_EQ, k)], want_rows=True, max_rows=16)
 
+    # the dimension tables are resident on the device too: the joins' dim-row passes run there
     def q6():
         kept = np.nonzero(d50["name_id"] == 3)[0]          # the dimension filter (50 rows)
-        return ops.join_aggregate(t.region, [ops.FUNC_COUNT, ops.FUNC_SUM], [None, t.amount], d50["k"], dim_rows=kept)
+        return ops.join_aggregate(t.region, [ops.FUNC_COUNT, ops.FUNC_SUM], [None, t.amount], d50["k"], dim_rows=kept,
+                                  dim_key_col=d50.get("k_col"))
 
     def q7():
         # amount < 10000, so amount % 1000000 is amount itself
         return ops.join_aggregate(t.amount, [ops.FUNC_SUM, ops.FUNC_COUNT], [t.amount, None], d1m["k"],
-                                  group_values=[seg_values])
+                                  group_values=[seg_values], dim_key_col=d1m.get("k_col"), dim_group_col=d1m.get("seg_col"))
 
     # algorithmic bytes: the distinct stored columns a query reads x rows x 4 B. The id lookup reads
     # none: id is a sequence (never stored) and its zone map keeps one 8192-row chunk, latency-bound.
@@ -455,7 +457,7 @@ def main():
 
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(args, native, ops, t, queries, lib)
+        e2e = run_e2e(args, native, ops, t, queries, lib, dims)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -491,41 +493,46 @@ def _canon(x):
     return x
 
 
-def run_e2e(args, native, ops, t, queries, lib):
-    """The suite from page-locked HOST buffers, every step: region, amount and flag uploaded, the seven
-    queries run, their results read back. Uploads go through the backend's stream slots (the reference's
-    GPU_Stream, one copy a slot) and overlap the queries: the upload of the next column runs while the
-    queries that need only the columns already on the device run on the main lane."""
+def run_e2e(args, native, ops, t, queries, lib, dims):
+    """The suite from page-locked HOST buffers, every step: the fact columns region, amount and flag and
+    the dimension tables' device columns uploaded, the seven queries run, their results read back. Uploads
+    go through the backend's stream slots (the reference's GPU_Stream) and overlap the queries: the upload
+    of the next column runs while the queries that need only the columns already on the device run on the
+    main lane."""
     import ctypes as C
     n = args.rows
-    host = {}
-    for name in ("region", "amount", "flag"):
-        col = getattr(t, name)
+    d50, d1m = dims
+    device = {"region": t.region, "amount": t.amount, "flag": t.flag, "dim1m_k": d1m["k_col"], "dim1m_seg": d1m["seg_col"],
+              "dim50_k": d50["k_col"]}
+    host, nbytes = {}, {}
+    for name, col in device.items():
         # the host copy of the column: page-locked memory from the backend (on the GPU's host node)
-        h = lib.cqlcuda_host_alloc(n * 4)
+        nbytes[name] = col.rows * 4
+        h = lib.cqlcuda_host_alloc(nbytes[name])
         if not h:
             raise RuntimeError("e2e: cqlcuda_host_alloc failed: " + native.last_error())
-        lib.cqlcuda_buffer_read(col.buffer.handle, C.c_void_p(h), n * 4)
+        lib.cqlcuda_buffer_read(col.buffer.handle, C.c_void_p(h), nbytes[name])
         host[name] = h
     by_name = {name: q for name, _, q in queries}
-    # columns in upload order, each with the queries that can run once it (and those before it) arrived
-    plan = [("amount", ["sum_min_max_amount", "join_dim1m_group_by_seg"]),
-            ("region", ["group_by_region", "group_by_amount_10k", "join_dim50_filtered", "point_lookup_id"]),
-            ("flag", ["count_flag_lt_2"])]
+    # columns in upload order, each slot with the queries that can run once it (and those before it) arrived
+    plan = [(["amount", "dim1m_k", "dim1m_seg"], ["sum_min_max_amount", "join_dim1m_group_by_seg"]),
+            (["region", "dim50_k"], ["group_by_region", "group_by_amount_10k", "join_dim50_filtered", "point_lookup_id"]),
+            (["flag"], ["count_flag_lt_2"])]
     assert sorted(q for _, qs in plan for q in qs) == sorted(by_name)
     stream = lib.cqlcuda_stream_alloc(len(plan))
     if not stream:
         raise RuntimeError("e2e: cqlcuda_stream_alloc failed: " + native.last_error())
 
     def upload(slot):
-        name = plan[slot][0]
-        ok = lib.cqlcuda_stream_slot_begin(stream, slot, n * 4, 0)
-        ok = ok and lib.cqlcuda_stream_copy(stream, slot, getattr(t, name).buffer.handle, C.c_void_p(host[name]), n * 4)
+        names = plan[slot][0]
+        ok = lib.cqlcuda_stream_slot_begin(stream, slot, sum(nbytes[c] for c in names), 0)
+        for c in names:
+            ok = ok and lib.cqlcuda_stream_copy(stream, slot, device[c].buffer.handle, C.c_void_p(host[c]), nbytes[c])
         ok = ok and lib.cqlcuda_stream_submit(stream, slot)
         if not ok:
             raise RuntimeError("e2e upload failed: " + native.last_error())
 
-    h2d = 3 * n * 4
+    h2d = sum(nbytes.values())
     resident = {name: _canon(q()) for name, q in by_name.items()}
     times = []
     last = {}
@@ -551,9 +558,10 @@ def run_e2e(args, native, ops, t, queries, lib):
     stream = lib.cqlcuda_stream_alloc(1)
     for i in range(3):
         t0 = time.perf_counter()
-        for name, _ in plan:
-            lib.cqlcuda_stream_slot_begin(stream, 0, n * 4, 0)
-            lib.cqlcuda_stream_copy(stream, 0, getattr(t, name).buffer.handle, C.c_void_p(host[name]), n * 4)
+        lib.cqlcuda_stream_slot_begin(stream, 0, h2d, 0)
+        for names, _ in plan:
+            for c in names:
+                lib.cqlcuda_stream_copy(stream, 0, device[c].buffer.handle, C.c_void_p(host[c]), nbytes[c])
         lib.cqlcuda_stream_submit(stream, 0)
         lib.cqlcuda_stream_wait(stream, 0)
         uploads.append(time.perf_counter() - t0)

@@ -804,6 +804,74 @@ static int launch_join_lut_first(const CqlLaunch& a, uint32_t gws, uint32_t lws,
   return 0;
 }
 
+// ---------------------------------------------------------------------------------------------
+// cql_join_dim_fold: the join-aggregate's dim-row pass on the device (not a reference kernel: the
+// reference visits the dim rows on the host, qe_aggregate_join_pushdown query_exec.c:8619-8720). Each
+// kept dim row whose key has fact rows adds its key's dense totals into its group's slot (the group value
+// minus the smallest, or slot 0 without a GROUP BY) and leaves its visit number as the slot's first visit
+// when it is the smallest: the host then orders the groups by first visit, as the host pass does.
+//  binding 0 visits (u32 dim rows; unbound: rows 0..visits-1), 1 dim keys (u32), 2 dim group values (u32 or
+//  i32 bits; unbound: no GROUP BY), 3 dense info (u32 pairs, word 1 the count), 4 dense sums (u32 lo/hi per
+//  key and expression), 5 dense MIN, 6 dense MAX (i32 per key and expression), 7 slot counts (u64), 8 slot
+//  sums (u64), 9 slot MIN, 10 slot MAX (i32), 11 slot first visit (u32, all 0xffffffff before)
+//  words 0 visits, 2 1 = visit list given, 4 min key bits, 6 key range, 8 expressions, 10 smallest group value
+//  bits, 12 slots, 14 bit 0 grouped, bit 1 MIN/MAX wanted
+
+__global__ void __launch_bounds__(JOIN_THREADS) k_join_dim_fold(CqlLaunch a, uint64_t visits)
+{
+  const uint32_t* visit_rows = (const uint32_t*)a.buf[0];
+  const uint32_t* dim_keys = (const uint32_t*)a.buf[1];
+  const uint32_t* group_values = (const uint32_t*)a.buf[2];
+  const uint32_t* info = (const uint32_t*)a.buf[3];
+  const uint32_t* dsums = (const uint32_t*)a.buf[4];
+  const int* dmins = (const int*)a.buf[5];
+  const int* dmaxs = (const int*)a.buf[6];
+  unsigned long long* counts = (unsigned long long*)a.buf[7];
+  unsigned long long* sums = (unsigned long long*)a.buf[8];
+  int* mins = (int*)a.buf[9];
+  int* maxs = (int*)a.buf[10];
+  uint32_t* first = (uint32_t*)a.buf[11];
+  bool listed = cql_word(a, 2) != 0;
+  uint32_t min_key = cql_word(a, 4), range = cql_word(a, 6), exprs = min(cql_word(a, 8), 8u), group_min = cql_word(a, 10);
+  uint32_t slots = cql_word(a, 12), flags = cql_word(a, 14);
+  bool grouped = (flags & 1u) != 0, want_mm = (flags & 2u) != 0;
+  uint64_t dim_rows = a.bytes[1] / 4, value_rows = a.bytes[2] / 4;
+  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < visits; v += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint64_t row = listed ? visit_rows[v] : v;
+    if (row >= dim_rows || (grouped && row >= value_rows)) continue;
+    uint32_t id = dim_keys[row] - min_key;
+    if (id >= range) continue;
+    uint32_t n = info[2ull * id + 1];
+    if (n == 0u) continue;
+    uint32_t slot = grouped ? group_values[row] - group_min : 0u;
+    if (slot >= slots) continue;
+    atomicAdd(&counts[slot], (unsigned long long)n);
+    for (uint32_t e = 0; e < exprs; e++)
+    {
+      uint64_t k = (uint64_t)id * exprs + e, s = (uint64_t)slot * exprs + e;
+      atomicAdd(&sums[s], ((unsigned long long)dsums[2 * k + 1] << 32) | dsums[2 * k]);
+      if (want_mm)
+      {
+        atomicMin(&mins[s], dmins[k]);
+        atomicMax(&maxs[s], dmaxs[k]);
+      }
+    }
+    atomicMin(&first[slot], (uint32_t)v);
+  }
+}
+
+static int launch_join_dim_fold(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t visits = cql_word(a, 0);
+  if (visits == 0) return 0;
+  k_join_dim_fold<<<cql_stream_grid((visits + JOIN_THREADS - 1) / JOIN_THREADS, 8), JOIN_THREADS, 0, stream>>>(a, visits);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
 const CqlKernelDesc cql_kernels_join[] = {
   { "hash_join_build_count", launch_join_build_count },
   { "prefix_sum", launch_prefix_sum },
@@ -814,5 +882,6 @@ const CqlKernelDesc cql_kernels_join[] = {
   { "cql_join_lut_build", launch_join_lut_build },
   { "cql_join_lut_map", launch_join_lut_map },
   { "cql_join_lut_first", launch_join_lut_first },
+  { "cql_join_dim_fold", launch_join_dim_fold },
   { nullptr, nullptr },
 };

@@ -492,9 +492,39 @@ int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const Cq
 /* ------------------------------------------------------------------------------------------------
  * Dense GROUP BY: qe_dense_stream_core (query_exec.c:7632-7983) on one chunk */
 
+/* The dense group-by's totals left on the device: info (u32 pairs, word 1 the count) at 0, sums (u32 lo/hi
+   pairs per group and expression) at sum_at, MIN and MAX (i32 per group and expression) at min_at / max_at
+   (filled with INT32_MAX / INT32_MIN when no expression is MIN/MAX). */
+typedef struct
+{
+  CqlBuffer* buffer;
+  uint64_t sum_at, min_at, max_at;
+  uint64_t group_count;
+  int64_t min_key;
+} CqlDenseTotals;
+
+static int group_dense_run(const CqlColumn* key, uint64_t rows, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* arg_cols,
+                           uint64_t max_groups, uint64_t* out_group_count, int64_t* out_min_key, uint64_t* out_counts, int64_t* out_sums,
+                           int64_t* out_mins, int64_t* out_maxs, CqlDenseTotals* device_out);
+
 int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* arg_cols,
                        uint64_t max_groups, uint64_t* out_group_count, int64_t* out_min_key, uint64_t* out_counts, int64_t* out_sums,
                        int64_t* out_mins, int64_t* out_maxs)
+{
+  return group_dense_run(key, rows, expr_count, funcs, arg_cols, max_groups, out_group_count, out_min_key, out_counts, out_sums, out_mins,
+                         out_maxs, NULL);
+}
+
+/* the dense group-by with its totals kept in its pooled device buffer (the join's device dim-row pass) */
+int cql_group_dense_device(const CqlColumn* key, uint64_t rows, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* arg_cols,
+                           uint64_t max_groups, CqlDenseTotals* out)
+{
+  return group_dense_run(key, rows, expr_count, funcs, arg_cols, max_groups, NULL, NULL, NULL, NULL, NULL, NULL, out);
+}
+
+static int group_dense_run(const CqlColumn* key, uint64_t rows, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* arg_cols,
+                           uint64_t max_groups, uint64_t* out_group_count, int64_t* out_min_key, uint64_t* out_counts, int64_t* out_sums,
+                           int64_t* out_mins, int64_t* out_maxs, CqlDenseTotals* device_out)
 {
   launches_begin();
   if (!cqlops_rows_fit(rows)) return 0;
@@ -623,15 +653,29 @@ int cqlops_group_dense(const CqlColumn* key, uint64_t rows, uint32_t expr_count,
     /* the kernel touches the MIN/MAX arrays only for MIN/MAX expressions: without any, their initial
        values are the results and neither array crosses the bus */
     uint64_t counted = has_min_max ? out_bytes : min_at;
-    CqlBatch* batch = cqlcuda_batch_begin(0, counted);
+    CqlBatch* batch = cqlcuda_batch_begin(0, device_out ? 0 : counted);
     cqlcuda_batch_buffer_zero(batch, out_buf, min_at);
-    if (has_min_max)
+    if (has_min_max || device_out)
     {
       cqlcuda_batch_fill_range(batch, out_buf, min_at, mm_bytes, 0x7fffffffu);
       cqlcuda_batch_fill_range(batch, out_buf, max_at, mm_bytes, 0x80000000u);
     }
     uint64_t workgroups = (rows + slice_rows - 1) / slice_rows;
     cqlcuda_batch_kernel_execute(batch, k, (uint32_t)(workgroups * QE_GPU_WORKGROUP_SIZE), QE_GPU_WORKGROUP_SIZE);
+    if (device_out)
+    {
+      /* the totals stay on the device for the caller's next batch */
+      ok = cqlcuda_batch_end(batch);
+      free(host_out);
+      if (!ok) return 0;
+      device_out->buffer = out_buf;
+      device_out->sum_at = sum_at;
+      device_out->min_at = min_at;
+      device_out->max_at = max_at;
+      device_out->group_count = group_count;
+      device_out->min_key = min_key;
+      return 1;
+    }
     cqlcuda_batch_buffer_read(batch, out_buf, host_out, counted);
     if (!has_min_max)
     {

@@ -957,6 +957,153 @@ static int join_finish(const CqlJoinAgg* q, JoinTotals* t, const uint32_t* core_
   return ok;
 }
 
+/* ---- the dim-row pass on the device, for a dense join over a dim table resident on the device ---- */
+
+typedef struct
+{
+  CqlBuffer* buffer;
+  uint64_t sum_at, min_at, max_at;
+  uint64_t group_count;
+  int64_t min_key;
+} CqlDenseTotals;
+
+int cql_group_dense_device(const CqlColumn* key, uint64_t rows, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* arg_cols,
+                           uint64_t max_groups, CqlDenseTotals* out);
+
+typedef struct
+{
+  uint32_t first, slot;
+} SlotFirst;
+
+static int slot_by_first(const void* a, const void* b)
+{
+  uint32_t x = ((const SlotFirst*)a)->first, y = ((const SlotFirst*)b)->first;
+  return x < y ? -1 : (x > y);
+}
+
+/* -1 when the query does not take this path (the host pass then runs), else 0 / 1 */
+static int join_device_pass(const CqlJoinAgg* q, uint32_t core_count, const uint32_t* core_funcs, const CqlColumn* const* core_cols,
+                            const uint32_t* core_of_expr, uint64_t max_groups, uint64_t* out_groups, uint64_t* out_group_dim_row,
+                            double* out_results, uint32_t* out_strategy)
+{
+  const CqlColumn* fk = q->fact_key;
+  const CqlColumn* dk = q->dim_key_column;
+  const CqlColumn* dg = q->group_count ? q->dim_group_column : NULL;
+  if (!dk || !dk->buffer || dk->width != 0 || dk->rows != q->dim_table_rows || !(dk->type == CQLOPS_TYPE_U32 || dk->type == CQLOPS_TYPE_I32))
+    return -1;
+  if (q->strategy == 2 || !fk->has_range || fk->zone_max - fk->zone_min + 1.0 > 65536.0 || q->group_count > 1) return -1;
+  for (uint32_t e = 0; q->dim_args && e < q->expr_count; e++)
+    if (q->dim_args[e]) return -1;
+  uint64_t slots = 1;
+  int64_t group_min = 0;
+  if (q->group_count)
+  {
+    if (!dg || !dg->buffer || dg->width != 0 || dg->rows != q->dim_table_rows || !(dg->type == CQLOPS_TYPE_U32 || dg->type == CQLOPS_TYPE_I32) ||
+        !dg->has_range || dg->zone_max - dg->zone_min + 1.0 > 65536.0)
+      return -1;
+    slots = (uint64_t)(dg->zone_max - dg->zone_min) + 1;
+    group_min = (int64_t)dg->zone_min;
+  }
+  uint64_t visits = q->dim_rows ? q->dim_count : q->dim_table_rows;
+  if (visits > 0xffffffffull) return -1;
+  CqlDenseTotals t;
+  uint64_t groups_cap = (uint64_t)(fk->zone_max - fk->zone_min) + 1;
+  if (!cql_group_dense_device(fk, fk->rows, core_count, core_funcs, core_cols, groups_cap, &t)) return 0;
+  uint64_t E = core_count;
+  int want_mm = 0;
+  for (uint32_t c = 0; c < core_count; c++) want_mm |= core_funcs[c] == CQLOPS_FUNC_MIN || core_funcs[c] == CQLOPS_FUNC_MAX;
+  uint64_t counts_at = 0, sums_at = slots * 8, mins_at = sums_at + slots * E * 8, maxs_at = mins_at + slots * E * 4,
+           first_at = maxs_at + slots * E * 4, bytes = first_at + slots * 4;
+  CqlBuffer* out = pooled("jdim_slots", bytes, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* vb = q->dim_rows ? pooled("jdim_visits", visits * 4, CQLCUDA_BUFFER_WRITE) : NULL;
+  CqlKernel* k = kernel("cql_join_dim_fold");
+  unsigned char* host = (unsigned char*)malloc(bytes);
+  uint32_t* vl = q->dim_rows ? (uint32_t*)malloc(visits * 4) : NULL;
+  int ok = out && k && host && (!q->dim_rows || (vb && vl));
+  for (uint64_t v = 0; ok && vl && v < visits; v++)
+  {
+    if (q->dim_rows[v] >= q->dim_table_rows) ok = refuse("a dim row past the dim table");
+    else vl[v] = (uint32_t)q->dim_rows[v];
+  }
+  if (ok)
+  {
+    cqlcuda_kernel_set_arg_buffer(k, 0, vb ? vb : dk->buffer);
+    cqlcuda_kernel_set_arg_buffer(k, 1, dk->buffer);
+    cqlcuda_kernel_set_arg_buffer(k, 2, dg ? dg->buffer : dk->buffer);
+    cqlcuda_kernel_set_arg_buffer_range(k, 3, t.buffer, 0, t.group_count * 8);
+    cqlcuda_kernel_set_arg_buffer_range(k, 4, t.buffer, t.sum_at, t.group_count * E * 8);
+    cqlcuda_kernel_set_arg_buffer_range(k, 5, t.buffer, t.min_at, t.group_count * E * 4);
+    cqlcuda_kernel_set_arg_buffer_range(k, 6, t.buffer, t.max_at, t.group_count * E * 4);
+    cqlcuda_kernel_set_arg_buffer_range(k, 7, out, counts_at, slots * 8);
+    cqlcuda_kernel_set_arg_buffer_range(k, 8, out, sums_at, slots * E * 8);
+    cqlcuda_kernel_set_arg_buffer_range(k, 9, out, mins_at, slots * E * 4);
+    cqlcuda_kernel_set_arg_buffer_range(k, 10, out, maxs_at, slots * E * 4);
+    cqlcuda_kernel_set_arg_buffer_range(k, 11, out, first_at, slots * 4);
+    cqlcuda_kernel_set_arg_u64(k, 0, visits | ((uint64_t)(vb ? 1u : 0u) << 32));
+    cqlcuda_kernel_set_arg_u64(k, 1, ((uint64_t)(uint32_t)t.min_key) | ((uint64_t)t.group_count << 32));
+    cqlcuda_kernel_set_arg_u64(k, 2, E | ((uint64_t)(uint32_t)group_min << 32));
+    cqlcuda_kernel_set_arg_u64(k, 3, slots | ((uint64_t)((dg ? 1u : 0u) | (want_mm ? 2u : 0u)) << 32));
+    CqlBatch* b = cqlcuda_batch_begin(vl ? visits * 4 : 0, bytes);
+    if (vl) cqlcuda_batch_buffer_write(b, vb, vl, visits * 4);
+    cqlcuda_batch_buffer_zero(b, out, mins_at);
+    cqlcuda_batch_fill_range(b, out, mins_at, slots * E * 4, 0x7fffffffu);
+    cqlcuda_batch_fill_range(b, out, maxs_at, slots * E * 4, 0x80000000u);
+    cqlcuda_batch_fill_range(b, out, first_at, slots * 4, 0xffffffffu);
+    cqlcuda_batch_kernel_execute(b, k, (uint32_t)(visits < 0x7fffff00ull ? visits : 0x7fffff00ull), QE_GPU_WORKGROUP_SIZE);
+    cqlcuda_batch_buffer_read(b, out, host, bytes);
+    ok = cqlcuda_batch_end(b);
+  }
+  if (ok)
+  {
+    const uint64_t* counts = (const uint64_t*)(host + counts_at);
+    const int64_t* sums = (const int64_t*)(host + sums_at);
+    const int32_t* mins = (const int32_t*)(host + mins_at);
+    const int32_t* maxs = (const int32_t*)(host + maxs_at);
+    const uint32_t* first = (const uint32_t*)(host + first_at);
+    SlotFirst* order = (SlotFirst*)malloc(slots * sizeof(SlotFirst));
+    uint64_t groups = 0;
+    ok = order != NULL;
+    for (uint64_t s2 = 0; ok && s2 < slots; s2++)
+      if (first[s2] != 0xffffffffu)
+      {
+        order[groups].first = first[s2];
+        order[groups].slot = (uint32_t)s2;
+        groups++;
+      }
+    if (ok && groups > max_groups) ok = refuse("more groups than the output arrays hold");
+    if (ok)
+    {
+      /* groups in the order of their first kept dim row, as the host pass meets them */
+      qsort(order, groups, sizeof(SlotFirst), slot_by_first);
+      for (uint64_t g = 0; g < groups; g++)
+      {
+        uint64_t s2 = order[g].slot;
+        out_group_dim_row[g] = q->dim_rows ? q->dim_rows[order[g].first] : order[g].first;
+        for (uint32_t e = 0; e < q->expr_count; e++)
+        {
+          uint64_t c = s2 * E + core_of_expr[e];
+          double r;
+          switch (q->funcs[e])
+          {
+            case CQLOPS_FUNC_COUNT: r = (double)counts[s2]; break;
+            case CQLOPS_FUNC_SUM: r = (double)sums[c]; break;
+            case CQLOPS_FUNC_AVG: r = counts[s2] ? (double)sums[c] / (double)counts[s2] : 0.0; break;
+            case CQLOPS_FUNC_MIN: r = (double)mins[c]; break;
+            default: r = (double)maxs[c]; break;
+          }
+          out_results[g * q->expr_count + e] = r;
+        }
+      }
+      *out_groups = groups;
+      if (out_strategy) *out_strategy = 1u;
+    }
+    free(order);
+  }
+  free(host);
+  free(vl);
+  return ok;
+}
+
 /* The fact-side totals each expression needs (:8558-8583): AVG is a SUM and the count, equal
    (function, column) pairs are one total, COUNT-only queries still count */
 static int join_core_plan(const CqlJoinAgg* q, uint32_t* core_funcs, const CqlColumn** core_cols, uint32_t* out_core_count,
@@ -1018,6 +1165,13 @@ int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* ou
     }
     if (q->strategy == 3) return refuse("the lookup-table join needs unique dim keys, one small whole-number GROUP BY value and no dim-side aggregates");
     cqlops_note_error("");
+  }
+  /* a dim table resident on the device: the dim-row pass runs there */
+  if (q->dim_key_column)
+  {
+    int r = join_device_pass(q, core_count, core_funcs, core_cols, core_of_expr, max_groups, out_groups, out_group_dim_row, out_results,
+                             out_strategy);
+    if (r >= 0) return r;
   }
   JoinTotals totals;
   if (!join_totals(q, core_count, core_funcs, core_cols, &totals)) return 0;

@@ -91,7 +91,7 @@ class CqlProgram(C.Structure):
 class CqlJoinAgg(C.Structure):
     _fields_ = [("fact_key", P), ("expr_count", u32), ("funcs", P), ("fact_args", P), ("dim_args", P), ("dim_keys", P),
                 ("dim_table_rows", u64), ("dim_rows", P), ("dim_count", u64), ("group_count", u32), ("dim_group_values", P),
-                ("strategy", u32)]
+                ("strategy", u32), ("dim_key_column", P), ("dim_group_column", P)]
 
 
 class CqlFusedAgg(C.Structure):

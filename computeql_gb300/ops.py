@@ -480,8 +480,11 @@ def hash_join(build_key, probe_key, left=False, hint_pairs=0, want_pairs=True):
     return n, (out[: 2 * n].reshape(-1, 2) if want_pairs else None)
 
 
-def join_aggregate(fact_key, funcs, fact_args, dim_keys, dim_rows=None, group_values=(), dim_args=None, strategy=0):
-    """Join-aggregate pushdown -> dict(groups, dim_row[G], results[G, E], strategy)."""
+def join_aggregate(fact_key, funcs, fact_args, dim_keys, dim_rows=None, group_values=(), dim_args=None, strategy=0, dim_key_col=None,
+                   dim_group_col=None):
+    """Join-aggregate pushdown -> dict(groups, dim_row[G], results[G, E], strategy). dim_key_col / dim_group_col
+    are the dim table's key and GROUP BY columns resident on the device (the same values as dim_keys and
+    group_values[0]): a dense join then runs its dim-row pass on the device."""
     e = len(funcs)
     fk = fact_key.c()
     structs = {}
@@ -496,9 +499,12 @@ def join_aggregate(fact_key, funcs, fact_args, dim_keys, dim_rows=None, group_va
     gv_keep = [np.ascontiguousarray(g, dtype=np.float64) for g in group_values]
     gv = (C.c_void_p * max(len(gv_keep), 1))(*[g.ctypes.data for g in gv_keep])
     fa = np.array(funcs, dtype=np.uint32)
+    dkc = dim_key_col.c() if dim_key_col is not None else None
+    dgc = dim_group_col.c() if dim_group_col is not None else None
     q = N.CqlJoinAgg(C.addressof(fk), e, fa.ctypes.data, C.addressof(fargs), C.addressof(dargs), dk.ctypes.data, len(dk),
                      dr.ctypes.data if dr is not None else None, len(dr) if dr is not None else 0, len(gv_keep),
-                     C.addressof(gv) if gv_keep else None, strategy)
+                     C.addressof(gv) if gv_keep else None, strategy, C.addressof(dkc) if dkc is not None else None,
+                     C.addressof(dgc) if dgc is not None else None)
     visits = len(dr) if dr is not None else len(dk)
     mg = max(visits, 1)
     dim_row = np.empty(mg, dtype=np.uint64)

@@ -44,14 +44,19 @@ def fact_numpy(rows, seed=FACT_SEED, gen=None):
 
 
 def dim_tables():
-    """dim50 (k, name_id, val) and dim1M (k, seg) as host arrays, drawn on the device like the fact table."""
+    """dim50 (k, name_id, val) and dim1M (k, seg), drawn on the device like the fact table: host arrays under
+    the column names, and the device columns (kept resident, as the fact table is) under "<name>_col"."""
     import numpy as np
     from .ops import Column
     n50, n1m = 50, 1_000_000
-    d50 = {name: Column.splitmix(n50, DIM50_SEED, len(DIM50_DRAWN), idx, rng).buffer.read(np.uint32) for name, idx, rng in DIM50_DRAWN}
-    d1m = {name: Column.splitmix(n1m, DIM1M_SEED, len(DIM1M_DRAWN), idx, rng).buffer.read(np.uint32) for name, idx, rng in DIM1M_DRAWN}
-    d50["k"] = np.arange(n50, dtype=np.uint32)
-    d1m["k"] = np.arange(n1m, dtype=np.uint32)
+    d50, d1m = {}, {}
+    for table, rows, seed, drawn in ((d50, n50, DIM50_SEED, DIM50_DRAWN), (d1m, n1m, DIM1M_SEED, DIM1M_DRAWN)):
+        for name, idx, rng in drawn:
+            col = Column.splitmix(rows, seed, len(drawn), idx, rng)
+            table[name + "_col"] = col
+            table[name] = col.buffer.read(np.uint32)
+        table["k_col"] = Column.affine(rows, 1, 0, 0)
+        table["k"] = np.arange(rows, dtype=np.uint32)
     return d50, d1m
 
 

@@ -288,6 +288,11 @@ typedef struct CqlJoinAgg
                                          3 a lookup table over the fact key's range (unique dim keys, at most one
                                          whole-number GROUP BY value spanning < 65536, no dim-side aggregates, a key
                                          range up to 2^24; automatic picks it for ranges above 65536 when it applies) */
+  /* Optional: the dim table resident on the device - its key column (dim_table_rows rows, the keys of
+     dim_keys) and its one GROUP BY column (whole numbers spanning at most 65536 values, the values of
+     dim_group_values). With them, a dense join's dim-row pass runs on the device instead of the host. */
+  const CqlColumn* dim_key_column;
+  const CqlColumn* dim_group_column;
 } CqlJoinAgg;
 
 /* Groups come out in the order their first dim row is met; out_group_dim_row[g] is that row,

@@ -258,3 +258,44 @@ def test_small_build_side_probe(ops, dim, funcs):
         want = [float(len(vals)), float(vals.sum())] if funcs == "count_sum" else [float(vals.sum()), float(vals.min()), float(vals.max())]
         assert list(got[int(d)]) == want, d
     assert list(r["dim_row"]) == sorted(got)                                # groups in dim-row order
+
+
+@pytest.mark.parametrize("case", ["dim1m_by_seg", "dim50_filtered", "signed_all_funcs", "no_match_rows"])
+def test_device_dim_pass_equals_the_host_pass(ops, case):
+    """A dense join over a dim table resident on the device runs its dim-row pass on the device
+    (cql_join_dim_fold): the same groups, in the same order (first kept dim row), the same results as the
+    host pass over the host arrays of the same dim table."""
+    rng = np.random.default_rng({"dim1m_by_seg": 1, "dim50_filtered": 2, "signed_all_funcs": 3, "no_match_rows": 4}[case])
+    n = 3_000_000
+    if case == "dim1m_by_seg":
+        key = rng.integers(0, 10_000, n).astype(np.uint32)
+        dk = np.arange(1_000_000, dtype=np.uint32)
+        seg = rng.integers(0, 20, len(dk)).astype(np.uint32)
+        funcs, fargs, dim_rows = [SUM, COUNT], ["v", None], None
+    elif case == "dim50_filtered":
+        key = rng.integers(0, 50, n).astype(np.uint32)
+        dk = np.arange(50, dtype=np.uint32)
+        seg = None
+        funcs, fargs, dim_rows = [COUNT, SUM], [None, "v"], np.nonzero(rng.integers(0, 10, 50) == 3)[0]
+    elif case == "signed_all_funcs":
+        key = rng.integers(-3000, 3000, n).astype(np.int32)
+        dk = rng.permutation(np.arange(-4000, 4000, dtype=np.int32)).view(np.uint32)
+        seg = rng.integers(-7, 7, len(dk)).astype(np.int32)
+        funcs, fargs, dim_rows = [COUNT, SUM, AVG, MIN, MAX], [None, "v", "v", "v", "v"], np.sort(rng.choice(len(dk), 5000, replace=False))
+    else:
+        key = rng.integers(0, 1000, n).astype(np.uint32)
+        dk = np.arange(5000, 7000, dtype=np.uint32)          # no dim key meets a fact key
+        seg = rng.integers(0, 3, len(dk)).astype(np.uint32)
+        funcs, fargs, dim_rows = [COUNT, SUM], [None, "v"], None
+    v = rng.integers(-100_000, 100_000, n).astype(np.int32)
+    kc, vc = ops.Column.from_numpy(key), ops.Column.from_numpy(v)
+    args = [vc if a == "v" else None for a in fargs]
+    gvals = [seg.astype(np.float64)] if seg is not None else []
+    host = ops.join_aggregate(kc, funcs, args, dk, dim_rows=dim_rows, group_values=gvals)
+    dkc = ops.Column.from_numpy(dk.view(key.dtype))
+    dgc = ops.Column.from_numpy(seg) if seg is not None else None
+    dev = ops.join_aggregate(kc, funcs, args, dk, dim_rows=dim_rows, group_values=gvals, dim_key_col=dkc, dim_group_col=dgc)
+    assert host["strategy"] == dev["strategy"] == 1
+    assert dev["groups"] == host["groups"]
+    assert np.array_equal(dev["dim_row"], host["dim_row"])
+    assert np.array_equal(dev["results"], host["results"])
