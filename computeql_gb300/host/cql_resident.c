@@ -476,7 +476,7 @@ int cqlops_group_dense_streamed(CqlResident* r, const CqlHostColumn* key, uint64
   cqlops_note_error("");
   if (out_uploaded_bytes) *out_uploaded_bytes = 0;
   if (!r || r->ops.alloc != dev_alloc) return refuse("the streamed group-by takes a cache of backend buffers (created with ops NULL)");
-  if (!key || !key->has_range || expr_count == 0 || expr_count > 4) return refuse("a key with its range and 1 to 4 aggregates");
+  if (!key || !key->has_range || expr_count == 0 || expr_count > 8) return refuse("a key with its range and 1 to 8 aggregates");
   if (!out_group_count || !out_min_key || !out_counts || !out_sums || !out_mins || !out_maxs) return refuse("every output array is required");
   if (!cqlops_rows_fit(rows)) return 0;
   if (chunk_rows == 0) chunk_rows = 1u << 24;
@@ -493,9 +493,9 @@ int cqlops_group_dense_streamed(CqlResident* r, const CqlHostColumn* key, uint64
   for (uint64_t start = 0; ok && start < rows; start += chunk_rows)
   {
     uint64_t n = rows - start < chunk_rows ? rows - start : chunk_rows;
-    CqlColumn kc, ac[4];
-    const CqlColumn* argp[4] = { NULL, NULL, NULL, NULL };
-    CqlBuffer* held[5];
+    CqlColumn kc, ac[8];
+    const CqlColumn* argp[8] = { NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL };
+    CqlBuffer* held[9];
     uint32_t nheld = 0;
     ok = chunk_column(r, key, start, n, &kc, out_uploaded_bytes);
     if (ok) held[nheld++] = kc.buffer;

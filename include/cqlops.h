@@ -511,7 +511,8 @@ int cqlops_scan_simple_streamed(CqlResident* cache, const CqlHostColumn* columns
 /* cqlops_group_dense over host columns streamed through the cache: qe_aggregate_dense_streamed
    (src/query_exec/query_exec.c:7984-8068). The groups are the key column's whole range (its zone), so
    every chunk's groups line up; counts and sums are added and minimums and maximums kept chunk by
-   chunk, all in integers: the same results as the resident dense group-by. args[e] is NULL for COUNT. */
+   chunk, all in integers: the same results as the resident dense group-by. args[e] is NULL for COUNT;
+   at most 8 aggregates over at most 4 distinct argument columns, as cqlops_group_dense. */
 int cqlops_group_dense_streamed(CqlResident* cache, const CqlHostColumn* key, uint64_t rows, uint32_t expr_count, const uint32_t* funcs,
                                 const CqlHostColumn* const* args, uint64_t chunk_rows, uint64_t max_groups, uint64_t* out_group_count,
                                 int64_t* out_min_key, uint64_t* out_counts, int64_t* out_sums, int64_t* out_mins, int64_t* out_maxs,
