@@ -564,3 +564,49 @@ CqlServeStats cqlserve_stats(CqlServer* sv)
   pthread_mutex_unlock(&sv->lock);
   return s;
 }
+
+/* ---- ready-made call requests ---- */
+
+void cqlops_note_error(const char* why);
+
+int cqlserve_join_call(void* ctx)
+{
+  CqlServeJoin* j = (CqlServeJoin*)ctx;
+  if (!j) return 0;
+  return cqlops_join_aggregate(&j->query, j->max_groups, &j->groups, j->out_group_dim_row, j->out_results, &j->strategy);
+}
+
+int cqlserve_sort_call(void* ctx)
+{
+  CqlServeSort* q = (CqlServeSort*)ctx;
+  if (!q || !q->columns || q->sort_column >= q->column_count || !q->out_rows) return 0;
+  uint64_t cap = q->max_rows ? q->max_rows : 1;
+  uint32_t* rows = (uint32_t*)malloc(cap * 4);
+  uint32_t* sorted = (uint32_t*)malloc(cap * 4);
+  uint64_t n = 0;
+  int ok = rows && sorted && cqlops_scan_simple(q->columns, q->column_count, q->leaves, q->leaf_count, &n, rows, cap);
+  if (ok && n > cap)
+  {
+    cqlops_note_error("ORDER BY: more rows passed the WHERE than max_rows");
+    ok = 0;
+  }
+  q->count = ok ? n : 0;
+  if (ok && n > 0)
+  {
+    /* the kept rows as a device selection (a pooled buffer of the worker's lane), sorted there */
+    CqlBuffer* sel = cqlcuda_buffer_alloc_pooled("serve_sort_rows", 15, n * 4, CQLCUDA_BUFFER_WRITE, NULL);
+    ok = sel != NULL;
+    if (ok)
+    {
+      CqlBatch* b = cqlcuda_batch_begin(n * 4, 0);
+      cqlcuda_batch_buffer_write(b, sel, rows, n * 4);
+      ok = cqlcuda_batch_end(b);
+    }
+    ok = ok && cqlops_sort_rows(&q->columns[q->sort_column], 1, &q->desc, sel, n, sorted, n);
+    uint64_t k = q->limit < n ? q->limit : n;
+    if (ok) memcpy(q->out_rows, sorted, k * 4);
+  }
+  free(rows);
+  free(sorted);
+  return ok;
+}

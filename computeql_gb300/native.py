@@ -94,6 +94,16 @@ class CqlJoinAgg(C.Structure):
                 ("strategy", u32), ("dim_key_column", P), ("dim_group_column", P)]
 
 
+class CqlServeJoin(C.Structure):
+    _fields_ = [("query", CqlJoinAgg), ("max_groups", u64), ("out_group_dim_row", P), ("out_results", P), ("groups", u64),
+                ("strategy", u32)]
+
+
+class CqlServeSort(C.Structure):
+    _fields_ = [("columns", P), ("column_count", u32), ("leaves", P), ("leaf_count", u32), ("sort_column", u32), ("desc", u32),
+                ("max_rows", u64), ("limit", u64), ("out_rows", P), ("count", u64)]
+
+
 class CqlFusedAgg(C.Structure):
     _fields_ = [("column_count", u32), ("slots", u32 * 4), ("coltypes", u32 * 4), ("grouped", u32), ("key_count", u32),
                 ("key_slots", u32 * 3), ("key_types", u32 * 3), ("key_ranges", u32 * 3), ("group_count", u32)]
@@ -237,6 +247,8 @@ OPS_API = [
     ("cqlserve_wait", C.c_int, [P, P, u32]),
     ("cqlserve_drain", None, [P]),
     ("cqlserve_stats", CqlServeStats, [P]),
+    ("cqlserve_join_call", C.c_int, [P]),
+    ("cqlserve_sort_call", C.c_int, [P]),
     ("cqlops_scan_ranges", u64, [P, u32, P, u32, P, u64, P, P, P]),
     ("cqlops_group_dense_fixed", C.c_int, [P, u32, P, P, P, u64, u64, P, P, P, P, P, P]),
     ("cqlops_hll_estimate", dbl, [P, u64]),

@@ -124,6 +124,38 @@ int cqlserve_wait(CqlServer* server, CqlServeRequest* request, uint32_t timeout_
 void cqlserve_drain(CqlServer* server);
 CqlServeStats cqlserve_stats(CqlServer* server);
 
+/* Ready-made CALL requests for the join and ORDER BY templates of a served mix: set request.call to the
+   function and request.ctx to its struct; they run on the worker's own lane with no callback into the
+   caller's runtime. */
+typedef struct CqlServeJoin
+{
+  CqlJoinAgg query;               /* cqlops_join_aggregate's query (its arrays stay valid while it runs) */
+  uint64_t max_groups;
+  uint64_t* out_group_dim_row;    /* max_groups entries */
+  double* out_results;            /* max_groups x query.expr_count */
+  uint64_t groups;                /* out */
+  uint32_t strategy;              /* out */
+} CqlServeJoin;
+int cqlserve_join_call(void* join);
+
+/* SELECT ... WHERE <an AND of comparisons> ORDER BY columns[sort_column] [DESC] LIMIT limit: the WHERE by
+   cqlops_scan_simple (up to max_rows matching rows, else the request fails), the kept rows sorted on the
+   device (cqlops_sort_rows over them as a selection), the first `limit` row numbers written. */
+typedef struct CqlServeSort
+{
+  const CqlColumn* columns;
+  uint32_t column_count;
+  const CqlLeaf* leaves;
+  uint32_t leaf_count;
+  uint32_t sort_column;
+  uint32_t desc;
+  uint64_t max_rows;
+  uint64_t limit;
+  uint32_t* out_rows;             /* limit entries */
+  uint64_t count;                 /* out: the rows the WHERE kept */
+} CqlServeSort;
+int cqlserve_sort_call(void* sort);
+
 #ifdef __cplusplus
 }
 #endif

@@ -54,12 +54,15 @@ def test_python_bindings_cover_the_headers():
 
 
 def test_serve_structs_match_the_header(tmp_path):
-    """The ctypes mirrors of the server's structs have the C layout: every field's offset and the size."""
+    """The ctypes mirrors of the operator layer's and the server's structs have the C layout: every field's
+    offset and the size."""
     import ctypes as C
     from computeql_gb300 import native
     checks = []
     for name, cls in (("CqlServeConfig", native.CqlServeConfig), ("CqlServeRequest", native.CqlServeRequest),
-                      ("CqlServeStats", native.CqlServeStats)):
+                      ("CqlServeStats", native.CqlServeStats), ("CqlServeJoin", native.CqlServeJoin),
+                      ("CqlServeSort", native.CqlServeSort), ("CqlJoinAgg", native.CqlJoinAgg), ("CqlColumn", native.CqlColumn),
+                      ("CqlHostColumn", native.CqlHostColumn), ("CqlLeaf", native.CqlLeaf)):
         checks.append((f"sizeof({name})", C.sizeof(cls)))
         for field, _ in cls._fields_:
             checks.append((f"offsetof({name}, {field})", getattr(cls, field).offset))
