@@ -854,6 +854,56 @@ class Server:
         req.footprint = footprint
         return self._submit(req, (cb,))
 
+    def join(self, fact_key, funcs, fact_args, dim_keys, dim_rows=None, group_values=(), dim_key_col=None, dim_group_col=None,
+             footprint=1 << 20, submit=True):
+        """A join-aggregate (cqlops_join_aggregate) as a native call request: no Python runs on the worker.
+        The result is in .req.ctx's CqlServeJoin (see join_result)."""
+        e = len(funcs)
+        keep = {"fk": fact_key.c()}
+        structs = {}
+        for a in fact_args:
+            if a is not None and id(a) not in structs:
+                structs[id(a)] = a.c()
+        keep["structs"] = structs
+        keep["fargs"] = (C.c_void_p * e)(*[C.addressof(structs[id(a)]) if a is not None else None for a in fact_args])
+        keep["dk"] = np.ascontiguousarray(dim_keys, dtype=np.uint32)
+        keep["dr"] = np.ascontiguousarray(dim_rows, dtype=np.uint64) if dim_rows is not None else None
+        keep["gv"] = [np.ascontiguousarray(g, dtype=np.float64) for g in group_values]
+        keep["gvp"] = (C.c_void_p * max(len(keep["gv"]), 1))(*[g.ctypes.data for g in keep["gv"]])
+        keep["fa"] = np.array(funcs, dtype=np.uint32)
+        keep["dkc"] = dim_key_col.c() if dim_key_col is not None else None
+        keep["dgc"] = dim_group_col.c() if dim_group_col is not None else None
+        visits = len(keep["dr"]) if keep["dr"] is not None else len(keep["dk"])
+        keep["rows"] = np.empty(max(visits, 1), dtype=np.uint64)
+        keep["res"] = np.empty(max(visits, 1) * e, dtype=np.float64)
+        q = N.CqlJoinAgg(C.addressof(keep["fk"]), e, keep["fa"].ctypes.data, C.addressof(keep["fargs"]), None, keep["dk"].ctypes.data,
+                         len(keep["dk"]), keep["dr"].ctypes.data if keep["dr"] is not None else None,
+                         len(keep["dr"]) if keep["dr"] is not None else 0, len(keep["gv"]),
+                         C.addressof(keep["gvp"]) if keep["gv"] else None, 0,
+                         C.addressof(keep["dkc"]) if keep["dkc"] is not None else None,
+                         C.addressof(keep["dgc"]) if keep["dgc"] is not None else None)
+        ctx = N.CqlServeJoin(q, max(visits, 1), keep["rows"].ctypes.data, keep["res"].ctypes.data, 0, 0)
+        keep["ctx"] = ctx
+        return self._native_call("cqlserve_join_call", ctx, footprint, keep, submit)
+
+    def sort(self, columns, leaves, sort_column, desc, limit, max_rows, footprint=0, submit=True):
+        """SELECT ... WHERE <leaves> ORDER BY columns[sort_column] [DESC] LIMIT limit as a native call request."""
+        keep = {"cols": (N.CqlColumn * len(columns))(*[c.c() for c in columns]),
+                "leaves": (N.CqlLeaf * len(leaves))(*[N.CqlLeaf(ci, op, float(t)) for ci, op, t in leaves]),
+                "out": np.zeros(max(limit, 1), dtype=np.uint32)}
+        ctx = N.CqlServeSort(C.addressof(keep["cols"]), len(columns), C.addressof(keep["leaves"]), len(leaves), sort_column,
+                             1 if desc else 0, max_rows, limit, keep["out"].ctypes.data, 0)
+        keep["ctx"] = ctx
+        return self._native_call("cqlserve_sort_call", ctx, footprint or max_rows * 32, keep, submit)
+
+    def _native_call(self, fn_name, ctx, footprint, keep, submit):
+        req = N.CqlServeRequest()
+        req.kind = SERVE_CALL
+        req.call = C.cast(getattr(N.load_ops(), fn_name), C.c_void_p)
+        req.ctx = C.addressof(ctx)
+        req.footprint = footprint
+        return self._submit(req, keep, submit)
+
     def drain(self):
         N.load_ops().cqlserve_drain(self.h)
 

@@ -279,3 +279,44 @@ def test_identical_requests_share_one_run(env):
         assert (list(r.req.sum[:2]), list(r.req.min[:2]), list(r.req.max[:2])) == g_ref and r.fused == 3
     assert other.fused == 1 and other.req.sum[0] == ops.aggregate_global([cols["u3"]])[0][0]
     assert stats["merged_requests"] == 4 + 2
+
+
+def test_join_and_sort_requests_equal_their_operators(gpu):
+    """The served mix's join and ORDER BY templates run as native call requests on the workers' lanes; in a
+    mix with filter/aggregate and group-by requests each answers what its operator answers alone."""
+    from computeql_gb300 import ops, workloads
+    import numpy as np
+    n = 2_000_003
+    f = workloads.fact_table(n, seed=5)
+    cols = {"region": f.region, "amount": f.amount, "flag": f.flag}
+    d50, d1m = workloads.dim_tables()
+    seg = d1m["seg"].astype(np.float64)
+    kept = np.nonzero(d50["name_id"] == 4)[0]
+    want_j50 = ops.join_aggregate(f.region, [ops.FUNC_COUNT, ops.FUNC_SUM], [None, f.amount], d50["k"], dim_rows=kept)
+    want_j1m = ops.join_aggregate(f.amount, [ops.FUNC_SUM, ops.FUNC_COUNT], [f.amount, None], d1m["k"], group_values=[seg])
+    cnt, sel = ops.scan_simple([f.flag], [(0, ops.CMP_EQ, 7)], want_rows=True)
+    sel_buf = ops.DeviceBuffer(len(sel) * 4, sel)
+    want_sort = ops.sort_rows([f.amount], [1], selection=sel_buf, count=len(sel))[:100]
+    with ops.Server(workers=3, fuse=True) as sv:
+        table = sv.add_table(cols)
+        reqs = []
+        for i in range(6):
+            reqs.append(("j50", sv.join(f.region, [ops.FUNC_COUNT, ops.FUNC_SUM], [None, f.amount], d50["k"], dim_rows=kept,
+                                        dim_key_col=d50["k_col"])))
+            reqs.append(("j1m", sv.join(f.amount, [ops.FUNC_SUM, ops.FUNC_COUNT], [f.amount, None], d1m["k"], group_values=[seg],
+                                        dim_key_col=d1m["k_col"], dim_group_col=d1m["seg_col"])))
+            reqs.append(("sort", sv.sort([f.flag, f.amount], [(0, ops.CMP_EQ, 7)], 1, True, 100, n // 50)))
+            reqs.append(("filter", sv.filter_agg(table, table.program(f"(< flag {10 + i})"), "amount")))
+            reqs.append(("group", sv.group_dense(table, "region", [ops.FUNC_COUNT], [None])))
+        for kind, r in reqs:
+            assert r.wait(60_000) and r.ok, (kind, r.error)
+            if kind in ("j50", "j1m"):
+                ctx = r._keep["ctx"]
+                want = want_j50 if kind == "j50" else want_j1m
+                g = ctx.groups
+                assert g == want["groups"]
+                assert np.array_equal(r._keep["rows"][:g], want["dim_row"])
+                assert np.array_equal(r._keep["res"][: g * 2].reshape(g, 2), want["results"])
+            elif kind == "sort":
+                assert r._keep["ctx"].count == cnt
+                assert np.array_equal(r._keep["out"], want_sort)
