@@ -229,6 +229,8 @@ def parity_checks(ops, t, queries, dims, key):
                     c.buffer.close()
     except AssertionError as err:
         return f"failed: {err}", len(checks)
+    except Exception as err:   # a malformed answer (a missing group, a short array) is a failed check too
+        return f"failed: {type(err).__name__}: {err}", len(checks)
     return "ok", len(checks)
 
 

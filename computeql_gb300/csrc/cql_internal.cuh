@@ -70,6 +70,21 @@ static inline uint32_t cql_stream_grid(uint64_t work_ctas, int per_sm)
   return (uint32_t)g;
 }
 
+// A full-width numeric value as the f64 the reference widens it to on the host (query_exec.c:10454-10690):
+// type is the CQL column type (1 U32, 2 U64, 3 F32, 4 F64, 7 I32, 8 I64).
+__device__ __forceinline__ double cql_value_as_f64(const void* p, uint32_t type, uint64_t row)
+{
+  switch (type)
+  {
+    case 1: return (double)((const uint32_t*)p)[row];
+    case 7: return (double)((const int*)p)[row];
+    case 3: return (double)__uint_as_float(((const uint32_t*)p)[row]);
+    case 2: return (double)((const unsigned long long*)p)[row];
+    case 8: return (double)((const long long*)p)[row];
+    default: return ((const double*)p)[row];
+  }
+}
+
 // Order-preserving maps used by kernels that keep f64 min/max in integer registers.
 __device__ __forceinline__ unsigned long long cql_f64_order_key(double x)
 {

@@ -40,13 +40,24 @@ __device__ __forceinline__ uint32_t hash_u32(uint32_t x)
 // aggregate_assign: binding 0 owner row per slot, 1 rows per slot, 2 slot per row, 3 overflow count,
 // 4 + 2c / 5 + 2c key column c (f64 values, or string bytes + u64 offsets);
 // words 0 rows, 2 buckets, 4 K, 6 key columns, 8 string mask, 10 1 = count atomics per lane (many groups),
-// 12 1 = linear probing over the whole table (slots a power of two)
+// 12 1 = linear probing over the whole table (slots a power of two), 14 per key column 4 bits: its CQL type
+// when it is bound at its stored width (U32, I32, F32), widened to f64 in registers; 0 = f64 values (the
+// reference's layout)
 
 struct KeyCols
 {
   const uint32_t* data[4];
   const uint32_t* off[4];
+  uint32_t types;
 };
+
+// a numeric key's f64 value and its bits, from the f64 pairs or the stored width
+__device__ __forceinline__ double key_value(const KeyCols& k, uint32_t c, uint64_t row)
+{
+  uint32_t t = (k.types >> (4 * c)) & 0xfu;
+  if (t == 0u) return __hiloint2double((int)k.data[c][row * 2 + 1], (int)k.data[c][row * 2]);
+  return cql_value_as_f64(k.data[c], t, row);
+}
 
 __device__ __forceinline__ uint32_t key_str_off(const KeyCols& k, uint32_t c, uint64_t row) { return k.off[c][row * 2]; }
 __device__ __forceinline__ uint32_t key_byte(const KeyCols& k, uint32_t c, uint64_t i) { return ((const unsigned char*)k.data[c])[i]; }
@@ -65,7 +76,8 @@ __device__ uint32_t key_hash(const KeyCols& k, uint32_t ncols, uint32_t string_m
     }
     else
     {
-      uint32_t lo = k.data[c][row * 2], hi = k.data[c][row * 2 + 1];
+      unsigned long long bits = (unsigned long long)__double_as_longlong(key_value(k, c, row));
+      uint32_t lo = (uint32_t)bits, hi = (uint32_t)(bits >> 32);
       hh = hash_u32(lo ^ hash_u32(hi));
     }
     h = hash_u32(h ^ hh);
@@ -87,8 +99,7 @@ __device__ bool keys_equal(const KeyCols& k, uint32_t ncols, uint32_t string_mas
     }
     else
     {
-      double x = __hiloint2double((int)k.data[c][a * 2 + 1], (int)k.data[c][a * 2]);
-      double y = __hiloint2double((int)k.data[c][b * 2 + 1], (int)k.data[c][b * 2]);
+      double x = key_value(k, c, a), y = key_value(k, c, b);
       if (!(x == y)) return false;
     }
   }
@@ -121,6 +132,7 @@ __global__ void __launch_bounds__(HASH_THREADS) k_aggregate_assign(CqlLaunch a, 
     k.data[c] = (const uint32_t*)a.buf[4 + 2 * c];
     k.off[c] = (const uint32_t*)a.buf[5 + 2 * c];
   }
+  k.types = cql_word(a, 14);
   uint64_t slots = a.bytes[0] / 4;
   uint32_t lane = threadIdx.x & 31u;
   // the loop runs while the warp's first row is in range, so whole warps take every iteration together

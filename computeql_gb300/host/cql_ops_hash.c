@@ -138,10 +138,11 @@ double cqlops_tdigest_percentile(float* means, float* weights, uint64_t count, d
   return result;
 }
 
-/* a numeric device column widened to a dense f64 buffer */
+/* a numeric device column widened to a dense f64 buffer (a full-width f64 column is its own) */
 static CqlBuffer* widen(const CqlColumn* col, const char* name)
 {
   if (col->width != 0 || !col->buffer) return NULL;
+  if (col->type == CQLOPS_TYPE_F64) return col->buffer;
   CqlBuffer* out = pooled(name, col->rows * 8, CQLCUDA_BUFFER_READ_WRITE);
   CqlKernel* k = kernel("cql_widen_f64");
   if (!out || !k) return NULL;
@@ -592,6 +593,7 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
     if (path == 3) return refuse("path 3 takes one whole-number key of at most 64 values with COUNT/SUM/AVG/MIN/MAX over f32/f64 columns");
     cqlops_note_error("");
   }
+  uint32_t key_types = 0;   /* per key: its CQL type when bound at its stored width, 0 = widened to f64 */
   uint32_t string_mask = 0;
   CqlBuffer* key_data[4] = { 0 };
   CqlBuffer* key_off[4] = { 0 };
@@ -605,6 +607,14 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
       string_mask |= 1u << c;
       key_data[c] = keys[c].buffer;
       key_off[c] = keys[c].offsets;
+    }
+    else if (keys[c].width == 0 && keys[c].buffer &&
+             (keys[c].type == CQLOPS_TYPE_U32 || keys[c].type == CQLOPS_TYPE_I32 || keys[c].type == CQLOPS_TYPE_F32))
+    {
+      /* read at its stored width and widened to f64 in the assign kernel's registers */
+      key_data[c] = keys[c].buffer;
+      key_off[c] = keys[c].buffer;
+      key_types |= keys[c].type << (4 * c);
     }
     else
     {
@@ -726,6 +736,7 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
     cqlcuda_kernel_set_arg_u64(assign, 4, string_mask);
     cqlcuda_kernel_set_arg_u64(assign, 5, group_hint >= AGG_MANY_GROUPS);
     cqlcuda_kernel_set_arg_u64(assign, 6, linear);
+    cqlcuda_kernel_set_arg_u64(assign, 7, key_types);
     uint32_t over = 0;
     CqlBatch* b = cqlcuda_batch_begin(0, 4);
     cqlcuda_batch_buffer_fill(b, owner, slots * 4, EMPTY);

@@ -1039,10 +1039,15 @@ static int join_device_pass(const CqlJoinAgg* q, uint32_t core_count, const uint
     cqlcuda_kernel_set_arg_buffer_range(k, 9, out, mins_at, slots * E * 4);
     cqlcuda_kernel_set_arg_buffer_range(k, 10, out, maxs_at, slots * E * 4);
     cqlcuda_kernel_set_arg_buffer_range(k, 11, out, first_at, slots * 4);
-    cqlcuda_kernel_set_arg_u64(k, 0, visits | ((uint64_t)(vb ? 1u : 0u) << 32));
-    cqlcuda_kernel_set_arg_u64(k, 1, ((uint64_t)(uint32_t)t.min_key) | ((uint64_t)t.group_count << 32));
-    cqlcuda_kernel_set_arg_u64(k, 2, E | ((uint64_t)(uint32_t)group_min << 32));
-    cqlcuda_kernel_set_arg_u64(k, 3, slots | ((uint64_t)((dg ? 1u : 0u) | (want_mm ? 2u : 0u)) << 32));
+    /* the kernel reads the low word of each slot (words 0, 2, ..., 14) */
+    cqlcuda_kernel_set_arg_u64(k, 0, visits);
+    cqlcuda_kernel_set_arg_u64(k, 1, vb ? 1u : 0u);
+    cqlcuda_kernel_set_arg_u64(k, 2, (uint32_t)t.min_key);
+    cqlcuda_kernel_set_arg_u64(k, 3, t.group_count);
+    cqlcuda_kernel_set_arg_u64(k, 4, E);
+    cqlcuda_kernel_set_arg_u64(k, 5, (uint32_t)group_min);
+    cqlcuda_kernel_set_arg_u64(k, 6, slots);
+    cqlcuda_kernel_set_arg_u64(k, 7, (dg ? 1u : 0u) | (want_mm ? 2u : 0u));
     CqlBatch* b = cqlcuda_batch_begin(vl ? visits * 4 : 0, bytes);
     if (vl) cqlcuda_batch_buffer_write(b, vb, vl, visits * 4);
     cqlcuda_batch_buffer_zero(b, out, mins_at);
