@@ -319,6 +319,17 @@ struct JoinDecode
   uint32_t log2w[5], bits[5], mask[5], base[5];
 };
 
+// PLAIN: every column bound at its full 32-bit width (no narrow codes to unpack)
+template <bool PLAIN>
+__device__ __forceinline__ uint32_t join_read_t(const JoinDecode& d, int c, uint64_t row)
+{
+  if (PLAIN) return d.col[c][row];
+  uint32_t l = d.log2w[c];
+  uint32_t w = d.col[c][row >> l];
+  uint32_t sh = (uint32_t)((row & ((1u << l) - 1u)) * d.bits[c]) & 31u;
+  return d.base[c] + ((w >> sh) & d.mask[c]);
+}
+
 __device__ __forceinline__ uint32_t join_read(const JoinDecode& d, int c, uint64_t row)
 {
   uint32_t l = d.log2w[c];
@@ -489,6 +500,7 @@ __device__ __forceinline__ int join_mbar_wait(uint32_t bar)
   }
 }
 
+template <bool PLAIN>
 __global__ void __launch_bounds__(JOIN_SMEM_THREADS, 2) k_join_probe_native_smem(CqlLaunch a, uint64_t rows, JoinSmemLayout L)
 {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -565,7 +577,7 @@ __global__ void __launch_bounds__(JOIN_SMEM_THREADS, 2) k_join_probe_native_smem
     for (uint32_t u = 0; u < UNROLL; u++)
     {
       uint64_t at = base + u * stride;
-      key[u] = at < rows ? join_read(d, 0, at) : 0u;
+      key[u] = at < rows ? join_read_t<PLAIN>(d, 0, at) : 0u;
     }
 #pragma unroll
     for (uint32_t u = 0; u < UNROLL; u++)
@@ -581,7 +593,7 @@ __global__ void __launch_bounds__(JOIN_SMEM_THREADS, 2) k_join_probe_native_smem
 #pragma unroll
     for (uint32_t u = 0; u < UNROLL; u++)
 #pragma unroll
-      for (uint32_t c = 0; c < 4; c++) argv[u][c] = (maybe[u] && ((used_args >> c) & 1u)) ? join_read(d, 1 + (int)c, base + u * stride) : 0u;
+      for (uint32_t c = 0; c < 4; c++) argv[u][c] = (maybe[u] && ((used_args >> c) & 1u)) ? join_read_t<PLAIN>(d, 1 + (int)c, base + u * stride) : 0u;
 #pragma unroll
     for (uint32_t u = 0; u < UNROLL; u++)
     {
@@ -661,14 +673,19 @@ static int launch_join_probe_native(const CqlLaunch& a, uint32_t gws, uint32_t l
       static bool attr_set = false;
       if (!attr_set)
       {
-        if (cudaFuncSetAttribute(k_join_probe_native_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)JOIN_SMEM_MAX_BYTES) != cudaSuccess)
+        if (cudaFuncSetAttribute(k_join_probe_native_smem<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)JOIN_SMEM_MAX_BYTES) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(k_join_probe_native_smem<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)JOIN_SMEM_MAX_BYTES) !=
+                cudaSuccess)
           return (int)cudaGetLastError();
         attr_set = true;
       }
+      bool plain = (cql_word(a, 1) & 0xfffffu) == 0u;   // key and every argument at full width
       // two CTAs an SM where their shared arrays fit (the register budget is set for two)
       int per_sm = (int)std::max<uint32_t>(1u, std::min<uint32_t>(2u, (uint32_t)(g_cql_max_smem_optin / (L.total + 1024u))));
-      k_join_probe_native_smem<<<cql_stream_grid((rows + JOIN_SMEM_THREADS * 8 - 1) / (JOIN_SMEM_THREADS * 8), per_sm), JOIN_SMEM_THREADS,
-                                 L.total, stream>>>(a, rows, L);
+      dim3 grid(cql_stream_grid((rows + JOIN_SMEM_THREADS * 8 - 1) / (JOIN_SMEM_THREADS * 8), per_sm));
+      if (plain) k_join_probe_native_smem<true><<<grid, JOIN_SMEM_THREADS, L.total, stream>>>(a, rows, L);
+      else k_join_probe_native_smem<false><<<grid, JOIN_SMEM_THREADS, L.total, stream>>>(a, rows, L);
       CQL_LAUNCH_CHECK();
       return 0;
     }
