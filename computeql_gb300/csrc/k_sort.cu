@@ -17,6 +17,10 @@
 //  cql_radix_scatter  binding 0 keys in, 1 positions in, 2 keys out, 3 positions out, 4 scanned histogram,
 //                     5 selection; word 0 n, word 2 bit shift, word 4 key bytes, word 6 1 = write the
 //                     selection's row instead of the position, word 8 1 = write no keys (the last pass)
+//  cql_pairs_unpack   binding 0 records (u32 words), 1 first out, 2 second out; word 0 n, word 2 words per
+//                     record, word 4 the first's word offset, word 6 the second's
+//  cql_pairs_pack     binding 0 sorted positions, 1 first, 2 second, 3 pairs out (first, second); word 0 n
+//                     (result pairs - join or scan output - put in order on the device by the sort above)
 //
 // A tile is 8 warps x 16 rounds x 32 rows = 4096 rows. The scatter ranks a row within its tile in input
 // order: eight ballots find the lanes of a round with the same digit, per-warp digit counters carry
@@ -355,7 +359,60 @@ static int launch_radix_scatter(const CqlLaunch& a, uint32_t gws, uint32_t lws, 
   return 0;
 }
 
+__global__ void k_pairs_unpack(CqlLaunch a, uint64_t n, uint32_t stride, uint32_t fa, uint32_t fb)
+{
+  const uint32_t* rec = (const uint32_t*)a.buf[0];
+  uint32_t* first = (uint32_t*)a.buf[1];
+  uint32_t* second = (uint32_t*)a.buf[2];
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+  {
+    first[i] = rec[i * stride + fa];
+    second[i] = rec[i * stride + fb];
+  }
+}
+
+__global__ void k_pairs_pack(CqlLaunch a, uint64_t n)
+{
+  const uint32_t* order = (const uint32_t*)a.buf[0];
+  const uint32_t* first = (const uint32_t*)a.buf[1];
+  const uint32_t* second = (const uint32_t*)a.buf[2];
+  uint2* out = (uint2*)a.buf[3];
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint32_t p = order[i];
+    out[i] = make_uint2(first[p], second[p]);
+  }
+}
+
+static int launch_pairs_unpack(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t n = cql_word(a, 0);
+  uint32_t stride = cql_word(a, 2), fa = cql_word(a, 4), fb = cql_word(a, 6);
+  if (n == 0) return 0;
+  if (stride == 0 || fa >= stride || fb >= stride || a.bytes[0] < n * stride * 4 || a.bytes[1] < n * 4 || a.bytes[2] < n * 4)
+    return (int)cudaErrorInvalidValue;
+  k_pairs_unpack<<<cql_stream_grid((n + SORT_THREADS - 1) / SORT_THREADS, 8), SORT_THREADS, 0, stream>>>(a, n, stride, fa, fb);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+static int launch_pairs_pack(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t n = cql_word(a, 0);
+  if (n == 0) return 0;
+  if (a.bytes[0] < n * 4 || a.bytes[1] < n * 4 || a.bytes[2] < n * 4 || a.bytes[3] < n * 8) return (int)cudaErrorInvalidValue;
+  k_pairs_pack<<<cql_stream_grid((n + SORT_THREADS - 1) / SORT_THREADS, 8), SORT_THREADS, 0, stream>>>(a, n);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
 const CqlKernelDesc cql_kernels_sort[] = {
+  { "cql_pairs_unpack", launch_pairs_unpack },
+  { "cql_pairs_pack", launch_pairs_pack },
   { "cql_sort_keys", launch_sort_keys },
   { "cql_radix_count", launch_radix_count },
   { "cql_radix_scatter", launch_radix_scatter },

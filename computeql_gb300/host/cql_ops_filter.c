@@ -43,6 +43,8 @@ void cqlops_generated_stats(uint64_t* out_requests, uint64_t* out_failures)
 }
 
 int cqlops_rows_fit(uint64_t rows);
+int cqlops_sort_pairs(CqlBuffer* records, uint64_t n, uint32_t stride_words, uint32_t first_word, uint32_t second_word, int by_second,
+                      uint32_t* out, uint64_t out_capacity);
 
 /* every column the program binds fits the kernels' 32-bit row numbers */
 static int program_rows_fit(const CqlProgram* prog, const CqlColumn* columns)
@@ -217,12 +219,6 @@ static int run_simple(const CqlProgram* prog, const CqlColumn* columns, const Cq
   return cqlops_scan_simple(cols, used, local, n, out_count, out_rows, cap);
 }
 
-static int pair_by_row(const void* a, const void* b)
-{
-  uint32_t x = ((const uint32_t*)a)[0], y = ((const uint32_t*)b)[0];
-  return x < y ? -1 : (x > y ? 1 : 0);
-}
-
 static int scan_filter_run(const CqlProgram* prog, const CqlColumn* columns, uint32_t strategy, uint64_t* out_count, uint32_t* out_rows,
                            double* out_scores, uint64_t out_capacity, uint32_t* out_strategy)
 {
@@ -330,12 +326,15 @@ static int scan_filter_run(const CqlProgram* prog, const CqlColumn* columns, uin
   if (want_rows && result > cap_rows) return 0;
   if (want_rows && result && out_capacity)
   {
-    uint32_t* pairs = (uint32_t*)malloc(result * 8);
-    if (!pairs) return 0;
-    cqlcuda_buffer_read(output, pairs, result * 8);
-    /* the kernel's order is not deterministic: rows ascending, each with its score */
-    qsort(pairs, result, 8, pair_by_row);
+    /* the kernel's order is not deterministic: (row, score) pairs sorted by row on the device */
     uint64_t m = result < out_capacity ? result : out_capacity;
+    uint32_t* pairs = (uint32_t*)malloc(m * 8);
+    if (!pairs) return 0;
+    if (!cqlops_sort_pairs(output, result, 2, 0, 1, 0, pairs, out_capacity))
+    {
+      free(pairs);
+      return 0;
+    }
     for (uint64_t i = 0; i < m; i++)
     {
       if (out_rows) out_rows[i] = pairs[2 * i];

@@ -25,6 +25,8 @@
 void cqlops_note_error(const char* why);
 
 int cqlops_rows_fit(uint64_t rows);
+int cqlops_sort_pairs(CqlBuffer* records, uint64_t n, uint32_t stride_words, uint32_t first_word, uint32_t second_word, int by_second,
+                      uint32_t* out, uint64_t out_capacity);
 
 static int refuse(const char* why)
 {
@@ -68,15 +70,6 @@ static int join_key(const CqlColumn* col, const char* name, CqlBuffer** data, Cq
   *off = out;
   *is_str = 0;
   return 1;
-}
-
-static int pair_cmp(const void* a, const void* b)
-{
-  const uint32_t* x = (const uint32_t*)a;
-  const uint32_t* y = (const uint32_t*)b;
-  if (x[0] != y[0]) return x[0] < y[0] ? -1 : 1;
-  if (x[1] != y[1]) return x[1] < y[1] ? -1 : 1;
-  return 0;
 }
 
 int cqlops_hash_join(const CqlColumn* build_key, const CqlColumn* probe_key, int left_join, uint64_t hint_pairs, uint64_t* out_count,
@@ -169,21 +162,8 @@ int cqlops_hash_join(const CqlColumn* build_key, const CqlColumn* probe_key, int
     capacity = produced;
   }
   if (produced > capacity) return refuse("the join produced more pairs than its output could hold");
-  if (out_pairs && produced)
-  {
-    uint32_t* raw = (uint32_t*)malloc((uint64_t)produced * 16);
-    if (!raw) return 0;
-    cqlcuda_buffer_read(pairs, raw, (uint64_t)produced * 16);
-    for (uint64_t i = 0; i < produced; i++)
-    {
-      raw[i * 2] = raw[i * 4];
-      raw[i * 2 + 1] = raw[i * 4 + 2];
-    }
-    qsort(raw, produced, 8, pair_cmp);
-    uint64_t n = produced < out_capacity ? produced : out_capacity;
-    memcpy(out_pairs, raw, n * 8);
-    free(raw);
-  }
+  /* (probe row, build row) ascending, sorted on the device: words 0 and 2 of each 16-byte record */
+  if (out_pairs && produced && !cqlops_sort_pairs(pairs, produced, 4, 0, 2, 1, out_pairs, out_capacity)) return 0;
   *out_count = produced;
   return 1;
 }

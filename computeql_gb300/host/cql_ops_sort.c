@@ -152,6 +152,55 @@ int cqlops_sort_rows(const CqlColumn* keys, uint32_t key_count, const uint32_t* 
   return cqlcuda_batch_end(b);
 }
 
+/* Result pairs put in order on the device (the join's pair output, the scan's rows with their scores): n
+   records of stride_words u32 words in `records`; the pair (word first_word, word second_word) of each,
+   sorted by the first word then the second (by_second) or by the first alone (ties by position) with the
+   radix sort above, and up to out_capacity sorted pairs (first, second) read into out. */
+int cqlops_sort_pairs(CqlBuffer* records, uint64_t n, uint32_t stride_words, uint32_t first_word, uint32_t second_word, int by_second,
+                      uint32_t* out, uint64_t out_capacity)
+{
+  if (n == 0 || out_capacity == 0) return 1;
+  if (!cqlops_rows_fit(n)) return 0;
+  CqlBuffer* first = pooled("pairs_first", n * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* second = pooled("pairs_second", n * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* packed = pooled("pairs_sorted", n * 8, CQLCUDA_BUFFER_READ_WRITE);
+  CqlKernel* unpack = cqlcuda_kernel_alloc("cql_pairs_unpack", 16);
+  CqlKernel* pack = cqlcuda_kernel_alloc("cql_pairs_pack", 14);
+  if (!first || !second || !packed || !unpack || !pack) return 0;
+  CqlColumn keys[2];
+  memset(keys, 0, sizeof(keys));
+  for (int k = 0; k < 2; k++)
+  {
+    keys[k].type = CQLOPS_TYPE_U32;
+    keys[k].rows = n;
+    keys[k].buffer = k ? second : first;
+  }
+  uint64_t m = n < out_capacity ? n : out_capacity;
+  CqlBatch* b = cqlcuda_batch_begin(0, m * 8);
+  cqlcuda_kernel_set_arg_buffer(unpack, 0, records);
+  cqlcuda_kernel_set_arg_buffer(unpack, 1, first);
+  cqlcuda_kernel_set_arg_buffer(unpack, 2, second);
+  cqlcuda_kernel_set_arg_u64(unpack, 0, n);
+  cqlcuda_kernel_set_arg_u64(unpack, 1, stride_words);
+  cqlcuda_kernel_set_arg_u64(unpack, 2, first_word);
+  cqlcuda_kernel_set_arg_u64(unpack, 3, second_word);
+  cqlcuda_batch_kernel_execute(b, unpack, (uint32_t)n, QE_GPU_WORKGROUP_SIZE);
+  CqlBuffer* sorted = NULL;
+  if (!sort_enqueue(b, keys, by_second ? 2u : 1u, NULL, NULL, n, &sorted))
+  {
+    cqlcuda_batch_end(b);
+    return 0;
+  }
+  cqlcuda_kernel_set_arg_buffer(pack, 0, sorted);
+  cqlcuda_kernel_set_arg_buffer(pack, 1, first);
+  cqlcuda_kernel_set_arg_buffer(pack, 2, second);
+  cqlcuda_kernel_set_arg_buffer(pack, 3, packed);
+  cqlcuda_kernel_set_arg_u64(pack, 0, n);
+  cqlcuda_batch_kernel_execute(b, pack, (uint32_t)n, QE_GPU_WORKGROUP_SIZE);
+  cqlcuda_batch_buffer_read(b, packed, out, m * 8);
+  return cqlcuda_batch_end(b);
+}
+
 /* ROW_NUMBER, RANK and DENSE_RANK (qe_window_rank_gpu, src/query_exec/query_exec.c:6155-6540): the rows
    sorted by (partition keys, order keys) with the sort above, then per sorted position whether it starts a
    partition or a peer group (keys compared as F64 with !=, window_rank_flags.comp), then the three ranks by

@@ -62,6 +62,8 @@ def lib():
         L.orc_eval_program.restype = u64
         L.orc_eval_program_scored.argtypes = [P, u32, P, P, P, P, u64, P, P]
         L.orc_eval_program_scored.restype = u64
+        L.orc_batch_count_sum.argtypes = [u32, P, P, P, P, P, P, P, u64, P, P]
+        L.orc_batch_count_sum.restype = C.c_int
         L.orc_hll_add.argtypes = [P, u64, u32, P]
         L.orc_hll_estimate.argtypes = [P, u64]
         L.orc_hll_estimate.restype = dbl
@@ -185,6 +187,39 @@ def eval_program(words, consts, str_pool, slot_arrays, slot_types, rows, scores=
         return mask[:rows], sc[:rows]
     lib().orc_eval_program(_p(w), len(w), _p(k), _p(sp), ptrs, _p(types), rows, _p(mask))
     return mask[:rows]
+
+
+def batch_count_sum(programs, rows):
+    """COUNT(*) and the compensated SUM of each program of a batch (orc_batch_count_sum). programs: a list
+    of (words, consts, slot_arrays, slot_types, sum_array or None). Returns (counts uint64, sums f64)."""
+    n = len(programs)
+    keep = []
+    words = (C.c_void_p * n)()
+    wcount = np.zeros(n, dtype=np.uint32)
+    consts = (C.c_void_p * n)()
+    slots = (C.c_void_p * (n * 10))()
+    types = np.zeros(n * 10, dtype=np.uint32)
+    sums = (C.c_void_p * n)()
+    stypes = np.zeros(n, dtype=np.uint32)
+    for q, (w, k, arrays, st, sarr) in enumerate(programs):
+        w = np.ascontiguousarray(w, dtype=np.uint32)
+        k = np.ascontiguousarray(k if len(k) else [0, 0], dtype=np.uint32)
+        keep += [w, k]
+        words[q], wcount[q], consts[q] = w.ctypes.data, len(w), k.ctypes.data
+        for s, a in enumerate(arrays[:10]):
+            if a is not None:
+                a = np.ascontiguousarray(a)
+                keep.append(a)
+                slots[q * 10 + s] = a.ctypes.data
+        types[q * 10: q * 10 + len(st)] = st
+        if sarr is not None:
+            keep.append(sarr)
+            sums[q], stypes[q] = sarr.ctypes.data, type_of(sarr)
+    counts = np.zeros(n, dtype=np.uint64)
+    out = np.zeros(n, dtype=np.float64)
+    if not lib().orc_batch_count_sum(n, words, _p(wcount), consts, slots, _p(types), sums, _p(stypes), rows, _p(counts), _p(out)):
+        raise ValueError("a program holds an opcode the batch evaluator does not take")
+    return counts, out
 
 
 def hll_registers(values, p=10):

@@ -692,3 +692,175 @@ uint64_t orc_eval_program_scored(const uint32_t* words, uint32_t word_count, con
 {
   return eval_program(words, word_count, consts, str_pool, slot_data, slot_types, rows, out_match, out_score);
 }
+
+/* ---- a batch of WHERE programs over one table: COUNT(*) and SUM of a column per program ----
+   The same interpreter as eval_program, run a block of rows at a time: every opcode of a program acts on a
+   whole block (a stack of blocks of doubles), so one pass over the table serves every program of the
+   batch while the block is in cache. Threads take ranges of rows; each range keeps a Neumaier
+   compensated sum per program, and the ranges are folded in order the same way. Numeric opcodes only
+   (the batched shared scan takes no string comparisons). Returns 0 on an opcode it does not take. */
+#define BATCH_BLOCK 1024u
+#define BATCH_STACK 24
+typedef struct
+{
+  uint32_t programs;
+  const uint32_t* const* words;
+  const uint32_t* word_counts;
+  const uint32_t* const* consts;
+  const void* const* slot_data;    /* programs x 10 */
+  const uint32_t* slot_types;      /* programs x 10 */
+  const void* const* sum_data;     /* programs: the summed column or NULL */
+  const uint32_t* sum_types;
+  uint64_t rows;
+  uint64_t rows_per_task;
+  uint64_t* counts;                /* tasks x programs */
+  double* sums;                    /* tasks x programs x 2: sum, compensation */
+  int failed;
+} BatchCtx;
+
+static void batch_load(double* out, const void* p, uint32_t type, uint64_t first, uint32_t n)
+{
+  switch (type)
+  {
+    case 1: case 12: for (uint32_t i = 0; i < n; i++) out[i] = (double)((const uint32_t*)p)[first + i]; break;
+    case 3: for (uint32_t i = 0; i < n; i++) out[i] = (double)((const float*)p)[first + i]; break;
+    case 4: for (uint32_t i = 0; i < n; i++) out[i] = ((const double*)p)[first + i]; break;
+    case 6: for (uint32_t i = 0; i < n; i++) out[i] = (double)((const uint8_t*)p)[first + i]; break;
+    case 7: case 9: for (uint32_t i = 0; i < n; i++) out[i] = (double)((const int32_t*)p)[first + i]; break;
+    default:
+    {
+      const void* data[1] = {p};
+      uint32_t types[1] = {type};
+      for (uint32_t i = 0; i < n; i++) out[i] = slot_value(data, types, 0, first + i);
+    }
+  }
+}
+
+static void batch_task(void* arg, uint32_t task)
+{
+  BatchCtx* x = (BatchCtx*)arg;
+  uint64_t lo = (uint64_t)task * x->rows_per_task, hi = lo + x->rows_per_task;
+  if (hi > x->rows) hi = x->rows;
+  double* stack = (double*)malloc(sizeof(double) * BATCH_BLOCK * (BATCH_STACK + 1));
+  double* sumv = stack + (size_t)BATCH_BLOCK * BATCH_STACK;
+  uint64_t* counts = x->counts + (size_t)task * x->programs;
+  double* sums = x->sums + (size_t)task * x->programs * 2;
+  for (uint64_t first = lo; first < hi; first += BATCH_BLOCK)
+  {
+    uint32_t n = (uint32_t)((hi - first) < BATCH_BLOCK ? (hi - first) : BATCH_BLOCK);
+    for (uint32_t q = 0; q < x->programs; q++)
+    {
+      const uint32_t* w = x->words[q];
+      const uint32_t* k = x->consts[q];
+      uint32_t wc = x->word_counts[q], ip = 0;
+      int sp = 0;
+      while (ip < wc)
+      {
+        uint32_t op = w[ip++];
+        if (op == 13) break;
+        if (sp >= BATCH_STACK - 1) { x->failed = 1; break; }
+        double* top = stack + (size_t)sp * BATCH_BLOCK;
+        if (op == 0 || op == 14 || op == 2)
+        {
+          double v = op == 0 ? 1.0 : 0.0;
+          if (op == 2)
+          {
+            uint32_t c = w[ip++];
+            uint64_t bits = ((uint64_t)k[2 * c + 1] << 32) | k[2 * c];
+            memcpy(&v, &bits, sizeof(v));
+          }
+          for (uint32_t i = 0; i < n; i++) top[i] = v;
+          sp++;
+        }
+        else if (op == 1)
+        {
+          uint32_t operand = w[ip++], slot = operand & 0xffu;
+          batch_load(top, x->slot_data[(size_t)q * 10 + slot], (operand >> 8) & 0xffu, first, n);
+          sp++;
+        }
+        else if (op >= 3 && op <= 10 && sp >= 2)
+        {
+          double* b = top - BATCH_BLOCK;
+          double* a = b - BATCH_BLOCK;
+          switch (op)
+          {
+            case 3: for (uint32_t i = 0; i < n; i++) a[i] = a[i] == b[i] ? 1.0 : 0.0; break;
+            case 4: for (uint32_t i = 0; i < n; i++) a[i] = a[i] != b[i] ? 1.0 : 0.0; break;
+            case 5: for (uint32_t i = 0; i < n; i++) a[i] = a[i] < b[i] ? 1.0 : 0.0; break;
+            case 6: for (uint32_t i = 0; i < n; i++) a[i] = a[i] > b[i] ? 1.0 : 0.0; break;
+            case 7: for (uint32_t i = 0; i < n; i++) a[i] = a[i] <= b[i] ? 1.0 : 0.0; break;
+            case 8: for (uint32_t i = 0; i < n; i++) a[i] = a[i] >= b[i] ? 1.0 : 0.0; break;
+            case 9: for (uint32_t i = 0; i < n; i++) a[i] = (a[i] != 0.0 && b[i] != 0.0) ? 1.0 : 0.0; break;
+            default: for (uint32_t i = 0; i < n; i++) a[i] = (a[i] != 0.0 || b[i] != 0.0) ? 1.0 : 0.0; break;
+          }
+          sp--;
+        }
+        else { x->failed = 1; break; }
+      }
+      if (sp <= 0) { x->failed = 1; continue; }
+      const double* m = stack + (size_t)(sp - 1) * BATCH_BLOCK;
+      uint64_t c = 0;
+      for (uint32_t i = 0; i < n; i++) c += m[i] != 0.0;
+      counts[q] += c;
+      if (x->sum_data[q] && c)
+      {
+        batch_load(sumv, x->sum_data[q], x->sum_types[q], first, n);
+        double s = sums[2 * q], comp = sums[2 * q + 1];
+        for (uint32_t i = 0; i < n; i++)
+        {
+          if (m[i] == 0.0) continue;
+          double v = sumv[i], t = s + v;
+          comp += fabs(s) >= fabs(v) ? (s - t) + v : (v - t) + s;
+          s = t;
+        }
+        sums[2 * q] = s;
+        sums[2 * q + 1] = comp;
+      }
+    }
+  }
+  free(stack);
+}
+
+int orc_batch_count_sum(uint32_t programs, const uint32_t* const* words, const uint32_t* word_counts, const uint32_t* const* consts,
+                        const void* const* slot_data, const uint32_t* slot_types, const void* const* sum_data, const uint32_t* sum_types,
+                        uint64_t rows, uint64_t* out_count, double* out_sum)
+{
+  BatchCtx x;
+  x.programs = programs;
+  x.words = words;
+  x.word_counts = word_counts;
+  x.consts = consts;
+  x.slot_data = slot_data;
+  x.slot_types = slot_types;
+  x.sum_data = sum_data;
+  x.sum_types = sum_types;
+  x.rows = rows;
+  x.rows_per_task = 1u << 20;
+  x.failed = 0;
+  uint32_t tasks = (uint32_t)((rows + x.rows_per_task - 1) / x.rows_per_task);
+  if (tasks == 0) tasks = 1;
+  x.counts = (uint64_t*)calloc((size_t)tasks * programs, sizeof(uint64_t));
+  x.sums = (double*)calloc((size_t)tasks * programs * 2, sizeof(double));
+  orc_parallel(tasks, batch_task, &x);
+  for (uint32_t q = 0; q < programs; q++)
+  {
+    uint64_t c = 0;
+    double s = 0.0, comp = 0.0;
+    for (uint32_t t = 0; t < tasks; t++)
+    {
+      c += x.counts[(size_t)t * programs + q];
+      const double* part = x.sums + ((size_t)t * programs + q) * 2;
+      for (int h = 0; h < 2; h++)
+      {
+        double v = part[h], u = s + v;
+        comp += fabs(s) >= fabs(v) ? (s - u) + v : (v - u) + s;
+        s = u;
+      }
+    }
+    out_count[q] = c;
+    out_sum[q] = s + comp;
+  }
+  free(x.counts);
+  free(x.sums);
+  return !x.failed;
+}

@@ -76,6 +76,15 @@ uint64_t orc_eval_program(const uint32_t* words, uint32_t word_count, const uint
 uint64_t orc_eval_program_scored(const uint32_t* words, uint32_t word_count, const uint32_t* consts, const uint8_t* str_pool,
                                  const void* const* slot_data, const uint32_t* slot_types, uint64_t rows, uint8_t* out_match, double* out_score);
 
+/* A batch of programs over one table (the batched shared scan's answers): the interpreter above run a block
+   of rows at a time over every program, threads over row ranges. slot_data / slot_types: programs x 10;
+   sum_data[q]: the column program q sums (NULL: COUNT only) of type sum_types[q]. Writes each program's
+   match count and the Neumaier-compensated sum of its summed column over the matching rows; returns 0 if a
+   program holds an opcode other than the numeric ones. */
+int orc_batch_count_sum(uint32_t programs, const uint32_t* const* words, const uint32_t* word_counts, const uint32_t* const* consts,
+                        const void* const* slot_data, const uint32_t* slot_types, const void* const* sum_data, const uint32_t* sum_types,
+                        uint64_t rows, uint64_t* out_count, double* out_sum);
+
 /* ---- sketches ---- */
 /* HyperLogLog registers of a set of values (hll_add, src/gpu/vulkan/shaders/aggregate_reduce.comp:66-92):
    h = hash_u32(lo ^ hash_u32(hi)) of the value's f64 bits, bucket = top p bits, rho from the leading

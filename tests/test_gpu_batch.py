@@ -141,3 +141,26 @@ def test_plan_graph_replays_a_repeated_shape(ops):
     after = stats()
     assert after[1] - before[1] >= 1      # a later batch replayed the graph of the first
     assert after[2] == before[2]          # and no record fell back to an eager run
+
+
+def test_batched_configuration_100m_rows_512_queries(ops):
+    """The batched configuration at its own size: 100M rows of 4 u32 + 4 f64 columns, 512 queries over 29
+    shapes, the form chosen by the autotuner. Every query's COUNT bit for bit and its SUM within 1e-12 of the
+    oracle's compensated sum over the same rows (the oracle's batch evaluator, all host threads, one pass)."""
+    import oracle
+    from tests.where_shapes import oracle_batch
+    rows = 100_000_000
+    arrays = table(rows, 0)
+    cols = _columns(ops, arrays)
+    qs = queries(512, 29, 1)
+    progs = [ops.Program(w, cols) for w, _ in qs]
+    counts, sums, shapes = ops.batch_aggregate(progs, [s for _, s in qs], 0xFFFFFFFF)
+    assert shapes <= 29
+    for c in cols.values():
+        c.buffer.close()
+    oracle.set_threads(0)
+    want_counts, want_sums = oracle_batch(progs, [s for _, s in qs], arrays, rows)
+    assert np.array_equal(counts, want_counts)
+    for i, (w, _) in enumerate(qs):
+        assert abs(sums[i] - want_sums[i]) <= 1e-12 * max(abs(want_sums[i]), 1e-300), (w, sums[i], want_sums[i])
+    assert 0 < int((counts > 0).sum()) and int(counts.max()) < rows     # the draws give neither all-empty nor all-full batches

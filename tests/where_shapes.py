@@ -59,9 +59,9 @@ def random_shape(rng, columns, literal):
     return chain("or", [chain("and", t) for t in or_terms])
 
 
-def oracle_mask(program, arrays):
-    """The oracle's match mask for a compiled ops.Program, arrays: name -> numpy column (a string
-    column as (bytes uint8, offsets uint64))."""
+def _slots(program, arrays):
+    """the oracle's slot arrays and types for a compiled ops.Program, arrays: name -> numpy column (a
+    string column as (bytes uint8, offsets uint64))"""
     slots = [None] * 10
     types = [0] * 10
     p = program.prog
@@ -76,8 +76,25 @@ def oracle_mask(program, arrays):
             slots[slot], slots[slot + 1] = a
         else:
             slots[slot] = a
+    return slots, types
+
+
+def oracle_mask(program, arrays):
+    """The oracle's match mask for a compiled ops.Program over host arrays."""
+    slots, types = _slots(program, arrays)
+    p = program.prog
     rows = program.columns[0].rows
     return oracle.eval_program(program.words, list(p.consts[: 2 * p.const_count]), bytes(p.str_pool[: p.str_pool_size]), slots, types, rows)
+
+
+def oracle_batch(programs, sum_names, arrays, rows):
+    """The oracle's COUNT(*) and compensated SUM(sum column) of each compiled program over host arrays, all
+    programs in one pass over the table (numeric programs only)."""
+    batch = []
+    for prog, s in zip(programs, sum_names):
+        slots, types = _slots(prog, arrays)
+        batch.append((prog.words, list(prog.prog.consts[: 2 * prog.prog.const_count]), slots, types, arrays[s] if s else None))
+    return oracle.batch_count_sum(batch, rows)
 
 
 def string_arrays(values):
