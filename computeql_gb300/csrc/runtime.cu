@@ -23,6 +23,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <shared_mutex>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -112,6 +113,8 @@ struct CqlOp
 {
   int kind;
   CqlBuffer* buffer;
+  void* dptr;         // the buffer's device address when recorded: a captured graph's entry keeps it, since
+                      // the CqlBuffer itself may be freed while the graph stays cached
   uint64_t offset, size;
   uint32_t value;
   uint64_t at;        // WRITE: the bytes' place in the record; READ: the result's place in the out area
@@ -232,6 +235,7 @@ struct CqlState
   uint64_t flush_bytes;
 
   std::recursive_mutex lock;
+  std::shared_mutex generated_use;   // launches of generated kernels (shared) against their eviction (exclusive)
 };
 
 // Generated kernels kept loaded, as the reference's GPU_VULKAN_MAX_GENERATED_KERNELS (default 64, at least
@@ -1031,6 +1035,7 @@ static void generated_evict_over_cap(void)
       if (!victim || k->last_use < victim->last_use) victim = k;
     }
     if (loaded <= s.generated_cap || !victim) return;
+    std::unique_lock<std::shared_mutex> evict(s.generated_use);
     cudaDeviceSynchronize();
     graphs_drop_kernel(victim);
     if (victim->library) cudaLibraryUnload(victim->library);
@@ -1220,8 +1225,16 @@ static int dispatch_args(CqlKernel* k, const CqlLaunch& args, uint32_t gws, uint
   {
     rc = k->builtin(args, gws, lws, stream);
   }
-  else if (k->generated)
+  else
   {
+    // a lane launches without the state lock: the eviction of this kernel's module waits for the launch,
+    // and a launch after it sees the kernel gone
+    std::shared_lock<std::shared_mutex> use(s.generated_use);
+    if (!k->generated)
+    {
+      set_error("cqlcuda: kernel '%s' was evicted from the generated-kernel cache; look it up again", k->name.c_str());
+      return 0;
+    }
     uint32_t block = k->gen_block;
     uint64_t want = lws ? ((uint64_t)gws + lws - 1) / lws : 1;
     uint32_t grid = cql_stream_grid(want ? want : 1, (int)k->gen_per_sm);
@@ -1380,6 +1393,7 @@ static CqlOp op_of(int kind, CqlBuffer* buffer, uint64_t offset, uint64_t size)
   memset(&o, 0, sizeof(o));
   o.kind = kind;
   o.buffer = buffer;
+  o.dptr = buffer ? buffer->dptr : nullptr;
   o.offset = offset;
   o.size = size;
   return o;
@@ -1548,8 +1562,7 @@ static uint64_t record_fingerprint(const CqlBatch* b)
   for (const CqlOp& o : b->ops)
   {
     h = fnv_bytes(h, &o.kind, sizeof(o.kind));
-    void* dptr = o.buffer ? o.buffer->dptr : nullptr;
-    h = fnv_bytes(h, &dptr, sizeof(dptr));
+    h = fnv_bytes(h, &o.dptr, sizeof(o.dptr));
     h = fnv_bytes(h, &o.offset, 8);
     h = fnv_bytes(h, &o.size, 8);
     h = fnv_bytes(h, &o.value, 4);
@@ -1612,9 +1625,7 @@ static bool record_equals(const CqlBatch* b, const CqlGraphEntry& e)
   {
     const CqlOp& x = b->ops[i];
     const CqlOp& y = e.ops[i];
-    void* dx = x.buffer ? x.buffer->dptr : nullptr;
-    void* dy = y.buffer ? y.buffer->dptr : nullptr;
-    if (x.kind != y.kind || dx != dy || x.offset != y.offset || x.size != y.size || x.value != y.value || x.at != y.at) return false;
+    if (x.kind != y.kind || x.dptr != y.dptr || x.offset != y.offset || x.size != y.size || x.value != y.value || x.at != y.at) return false;
     if (x.kind == CQL_OP_KERNEL &&
         (x.kernel != y.kernel || x.gws != y.gws || x.lws != y.lws || memcmp(&x.launch, &y.launch, sizeof(CqlLaunch)) != 0))
       return false;
