@@ -532,7 +532,10 @@ __global__ void __launch_bounds__(JOIN_SMEM_THREADS, 2) k_join_probe_native_smem
   uint32_t* s_rows = (uint32_t*)(smem + L.trows);
   uint32_t* s_bloom = (uint32_t*)(smem + L.bloom);
   uint32_t* s_cnt = (uint32_t*)(smem + L.cnt);
-  unsigned long long* s_sums = (unsigned long long*)(smem + L.sums);
+  // 64-bit sums as two 32-bit halves: a 32-bit shared atomic add, and a carry into the high half when the
+  // low half wraps (or the value is negative), instead of a 64-bit shared atomic
+  uint32_t* s_lo = (uint32_t*)(smem + L.sums);
+  uint32_t* s_hi = s_lo + L.size * L.exprs;
   int* s_mins = (int*)(smem + L.mins);
   int* s_maxs = (int*)(smem + L.maxs);
   const uint32_t bar = (uint32_t)__cvta_generic_to_shared(smem);
@@ -555,7 +558,8 @@ __global__ void __launch_bounds__(JOIN_SMEM_THREADS, 2) k_join_probe_native_smem
   for (uint32_t i = threadIdx.x; i < L.size; i += blockDim.x) s_cnt[i] = 0u;
   for (uint32_t i = threadIdx.x; i < L.size * exprs; i += blockDim.x)
   {
-    s_sums[i] = 0ull;
+    s_lo[i] = 0u;
+    s_hi[i] = 0u;
     s_mins[i] = 0x7fffffff;
     s_maxs[i] = (int)0x80000000;
   }
@@ -623,7 +627,9 @@ __global__ void __launch_bounds__(JOIN_SMEM_THREADS, 2) k_join_probe_native_smem
         if (f == JFUNC_SUM || f == JFUNC_AVG)
         {
           bool sg = ((arg_signed >> ai) & 1u) != 0;
-          atomicAdd(&s_sums[index], sg ? (unsigned long long)(long long)(int)w : (unsigned long long)w);
+          uint32_t old = atomicAdd(&s_lo[index], w);
+          uint32_t up = ((sg && (int)w < 0) ? 0xffffffffu : 0u) + ((old + w < old) ? 1u : 0u);
+          if (up) atomicAdd(&s_hi[index], up);
         }
         else if (f == JFUNC_MIN) atomicMin(&s_mins[index], (int)w);
         else if (f == JFUNC_MAX) atomicMax(&s_maxs[index], (int)w);
@@ -644,7 +650,7 @@ __global__ void __launch_bounds__(JOIN_SMEM_THREADS, 2) k_join_probe_native_smem
       uint32_t f = (funcs >> (e * 4)) & 0xfu;
       uint64_t index = (uint64_t)dim_row * exprs + e;
       uint32_t si = slot * exprs + e;
-      if (f == JFUNC_SUM || f == JFUNC_AVG) atomicAdd(&sums[index], s_sums[si]);
+      if (f == JFUNC_SUM || f == JFUNC_AVG) atomicAdd(&sums[index], ((unsigned long long)s_hi[si] << 32) | s_lo[si]);
       else if (f == JFUNC_MIN) atomicMin(&mins[index], s_mins[si]);
       else if (f == JFUNC_MAX) atomicMax(&maxs[index], s_maxs[si]);
     }

@@ -140,6 +140,7 @@ struct CqlBatch
 {
   int active;
   int failed;
+  std::chrono::steady_clock::time_point opened;   // for the host-side entries of the kernel profile
   CqlStaging staging;
   int recording;
   uint64_t plan_key;
@@ -222,8 +223,10 @@ struct CqlState
 
   CqlLane main_lane;
   uint32_t lanes_open;   // threads with a lane of their own (pool eviction waits until they close)
+  uint32_t persistent_open;   // persistent kernels created and not destroyed (no generated kernel is evicted meanwhile)
 
   int profile_enabled;
+  std::atomic<uint64_t> host_open_ns, host_wait_ns, host_copy_ns, host_batches;
   std::vector<CqlProfileEntry> profile;
   std::unordered_map<std::string, uint32_t> profile_index;
 
@@ -264,6 +267,10 @@ static CqlState& S()
     g_state->fail_compile_every = 0;
     g_state->compile_attempts = 0;
     g_state->profile_enabled = 0;
+    g_state->host_batches = 0;
+    g_state->host_open_ns = 0;
+    g_state->host_wait_ns = 0;
+    g_state->host_copy_ns = 0;
     g_state->last_kernel_us = 0;
     g_state->launches = 0;
     g_state->wait_timeout_ms = 30000;
@@ -280,6 +287,7 @@ static CqlState& S()
     m.is_main = 1;
     m.launches = 0;
     g_state->lanes_open = 0;
+    g_state->persistent_open = 0;
   }
   return *g_state;
 }
@@ -756,6 +764,36 @@ extern "C" CqlBuffer* cqlcuda_buffer_import_host_readonly(const void* host_ptr, 
   return b;
 }
 
+// page-locked host memory mapped into the device's address space, owned by the buffer: kernels write results
+// there that the host reads without a copy (a persistent kernel's answers)
+extern "C" CqlBuffer* cqlcuda_buffer_alloc_host_mapped(uint64_t size, void** out_host)
+{
+  CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
+  if (out_host) *out_host = nullptr;
+  if (!ensure_init() || size == 0) return nullptr;
+  if (fault_injected("host_mapped", size)) return nullptr;
+  void* h = nullptr;
+  void* d = nullptr;
+  if (!note_cuda(cudaHostAlloc(&h, size, cudaHostAllocMapped), "cudaHostAlloc(mapped)")) return nullptr;
+  memset(h, 0, size);
+  if (!note_cuda(cudaHostGetDevicePointer(&d, h, 0), "cudaHostGetDevicePointer"))
+  {
+    cudaFreeHost(h);
+    return nullptr;
+  }
+  CqlBuffer* b = new CqlBuffer();
+  b->dptr = d;
+  b->size = size;
+  b->capacity = size;
+  b->flags = CQLCUDA_BUFFER_READ_WRITE;
+  b->imported = 3;
+  b->host_ptr = h;
+  b->charge = 0;
+  if (out_host) *out_host = h;
+  return b;
+}
+
 extern "C" CqlBuffer* cqlcuda_buffer_import_host_readonly_pooled(const char* name, uint64_t name_len, const void* host_ptr, uint64_t size)
 {
   CqlState& s = S();
@@ -798,6 +836,7 @@ extern "C" void cqlcuda_buffer_release(CqlBuffer* b)
     }
   }
   if (b->imported == 1) cudaHostUnregister(const_cast<void*>(b->host_ptr));
+  else if (b->imported == 3) cudaFreeHost(const_cast<void*>(b->host_ptr));
   else if (!b->imported && b->dptr)
   {
     // work already queued on the runtime stream may still read the buffer
@@ -1021,7 +1060,8 @@ static void graphs_drop_kernel(const CqlKernel* k);
 static void generated_evict_over_cap(void)
 {
   CqlState& s = S();
-  if (s.main_lane.batch.active) return;
+  // a persistent kernel may run for its idle limit: the device drain below would wait for it
+  if (s.main_lane.batch.active || s.persistent_open) return;
   for (;;)
   {
     uint32_t loaded = 0;
@@ -1367,6 +1407,7 @@ extern "C" CqlBatch* cqlcuda_batch_begin(uint64_t upload_bytes_needed, uint64_t 
   CqlBatch* b = &l.batch;
   b->active = 1;
   b->failed = 0;
+  if (s.profile_enabled) b->opened = std::chrono::steady_clock::now();
   b->recording = 0;
   b->ops.clear();
   b->in_bytes.clear();
@@ -1772,8 +1813,11 @@ extern "C" int cqlcuda_batch_end(CqlBatch* batch)
     return 0;
   }
   CqlLane& l = L();
+  const bool host_timed = s.profile_enabled != 0;
+  auto t_end = host_timed ? std::chrono::steady_clock::now() : std::chrono::steady_clock::time_point();
   if (batch->recording && !batch->failed) graph_end(batch, l);
   int ok = !batch->failed && wait_stream(l.stream, "batch_end");
+  auto t_waited = host_timed ? std::chrono::steady_clock::now() : t_end;
   if (batch->recording)
   {
     // the results of a recorded batch were copied from its graph's out area (or its staging, eagerly)
@@ -1782,6 +1826,17 @@ extern "C" int cqlcuda_batch_end(CqlBatch* batch)
     batch->recording = 0;
   }
   staging_finish(batch->staging, ok);
+  if (host_timed)
+  {
+    // host-side totals beside the kernels' (cqlcuda_host_profile): a batch from its opening to its end, the
+    // wait for its work, and the copies of staged results into the callers' arrays
+    auto t_done = std::chrono::steady_clock::now();
+    auto ns = [](std::chrono::steady_clock::duration d) { return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(d).count(); };
+    s.host_open_ns.fetch_add(ns(t_done - batch->opened));
+    s.host_wait_ns.fetch_add(ns(t_waited - t_end));
+    s.host_copy_ns.fetch_add(ns(t_done - t_waited));
+    s.host_batches.fetch_add(1);
+  }
   if (ok) timings_collect(l.timings);
   else
   {
@@ -1954,13 +2009,29 @@ extern "C" CqlStreamStats cqlcuda_stream_get_stats(CqlStream* st)
 extern "C" void cqlcuda_set_fault_alloc_at(uint64_t call_index) { S().fault_alloc_at = call_index; }
 extern "C" void cqlcuda_set_evict_hook(CqlEvictHook hook) { S().evict_hook = hook; }
 extern "C" void cqlcuda_kernel_profile_enable(int enabled) { S().profile_enabled = enabled; }
+
+// while the kernel profile is on: batches ended, and their host-side time (opening to end, waiting for the
+// device, copying staged results), since the last profile reset
+extern "C" void cqlcuda_host_profile(uint64_t* out_batches, uint64_t* out_open_ns, uint64_t* out_wait_ns, uint64_t* out_copy_ns)
+{
+  CqlState& s = S();
+  if (out_batches) *out_batches = s.host_batches.load();
+  if (out_open_ns) *out_open_ns = s.host_open_ns.load();
+  if (out_wait_ns) *out_wait_ns = s.host_wait_ns.load();
+  if (out_copy_ns) *out_copy_ns = s.host_copy_ns.load();
+}
 extern "C" void cqlcuda_kernel_profile_reset(void)
 {
-  for (auto& p : S().profile)
+  CqlState& s = S();
+  for (auto& p : s.profile)
   {
     p.total_ns = 0;
     p.dispatches = 0;
   }
+  s.host_batches = 0;
+  s.host_open_ns = 0;
+  s.host_wait_ns = 0;
+  s.host_copy_ns = 0;
 }
 extern "C" int cqlcuda_kernel_profile_entry(uint32_t index, const char** out_name, uint64_t* out_total_ns, uint64_t* out_dispatches)
 {
@@ -2208,4 +2279,142 @@ extern "C" void cqlcuda_thread_lane_end(void)
   CqlState& s = S();
   std::lock_guard<std::recursive_mutex> g(s.lock);
   if (s.lanes_open) s.lanes_open -= 1;
+}
+
+// ---------------------------------------------------------------------------------------------
+// persistent kernels: an entry point of a generated kernel's module launched on a stream of its own and left
+// running. It takes its work from device memory that the host fills through copies queued on the
+// persistent's copy stream (they land in the order queued) and returns by itself at its idle limit; the host
+// never waits on it without a time limit.
+
+struct CqlPersistent
+{
+  CqlKernel* kernel;
+  cudaKernel_t fn;
+  cudaStream_t stream, copies;
+  CqlLaunch args;
+  int launched;
+};
+
+extern "C" CqlPersistent* cqlcuda_persistent_create(CqlKernel* k, const char* entry)
+{
+  CqlState& s = S();
+  std::lock_guard<std::recursive_mutex> g(s.lock);
+  if (!ensure_init()) return nullptr;
+  if (!k || !k->generated || !k->library || !entry)
+  {
+    set_error("cqlcuda_persistent_create: a generated kernel and an entry point name are needed");
+    return nullptr;
+  }
+  cudaKernel_t fn = nullptr;
+  if (!note_cuda(cudaLibraryGetKernel(&fn, k->library, entry), "cudaLibraryGetKernel(persistent entry)")) return nullptr;
+  if (k->gen_smem > 48 * 1024) cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k->gen_smem);
+  CqlPersistent* p = new CqlPersistent();
+  p->kernel = k;
+  p->fn = fn;
+  p->launched = 0;
+  memset(&p->args, 0, sizeof(p->args));
+  if (!note_cuda(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking), "cudaStreamCreate(persistent)"))
+  {
+    delete p;
+    return nullptr;
+  }
+  if (!note_cuda(cudaStreamCreateWithFlags(&p->copies, cudaStreamNonBlocking), "cudaStreamCreate(persistent copies)"))
+  {
+    cudaStreamDestroy(p->stream);
+    delete p;
+    return nullptr;
+  }
+  s.persistent_open += 1;
+  return p;
+}
+
+// 1 while the kernel runs, 0 once it has returned (or was never launched), -1 if it returned with an error
+extern "C" int cqlcuda_persistent_running(CqlPersistent* p)
+{
+  if (!p || !p->launched) return 0;
+  cudaError_t e = cudaStreamQuery(p->stream);
+  if (e == cudaErrorNotReady) return 1;
+  p->launched = 0;
+  if (e != cudaSuccess)
+  {
+    note_cuda(e, "persistent kernel");
+    return -1;
+  }
+  return 0;
+}
+
+// launches the entry with the kernel's arguments as this thread set them, `ctas` CTAs of the kernel's block
+// size and shared memory; `zero`/`zero_bytes` (optional) is cleared on the kernel's stream first
+extern "C" int cqlcuda_persistent_launch(CqlPersistent* p, uint32_t ctas, CqlBuffer* zero, uint64_t zero_bytes)
+{
+  if (!p) return 0;
+  if (ctas == 0)
+  {
+    // every CTA resident at once (a CTA left waiting for a slot would hold back every item until the
+    // resident ones reach their idle limit)
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)p->fn, (int)p->kernel->gen_block, p->kernel->gen_smem) != cudaSuccess ||
+        per_sm < 1)
+    {
+      cudaGetLastError();
+      per_sm = 1;
+    }
+    // and one CTA's room an SM left over (where two or more fit), so that other lanes' kernels still find an
+    // SM while this one waits for work
+    if (per_sm >= 2) per_sm -= 1;
+    ctas = (uint32_t)per_sm * (uint32_t)g_cql_sm_count;
+  }
+  if (cqlcuda_persistent_running(p) == 1)
+  {
+    set_error("cqlcuda_persistent_launch: the kernel is still running");
+    return 0;
+  }
+  if (zero && !note_cuda(cudaMemsetAsync(zero->dptr, 0, std::min(zero_bytes, zero->size), p->stream), "persistent zero")) return 0;
+  p->args = L().args[p->kernel];
+  void* params[] = { &p->args };
+  if (!note_cuda(cudaLaunchKernel((const void*)p->fn, dim3(ctas), dim3(p->kernel->gen_block), params, p->kernel->gen_smem, p->stream),
+                 "persistent launch"))
+    return 0;
+  cql_note_launch();
+  p->launched = 1;
+  return 1;
+}
+
+// queues a copy of host bytes into a device buffer on the copy stream; the source must stay unchanged until
+// the work it describes is done
+extern "C" int cqlcuda_persistent_copy(CqlPersistent* p, CqlBuffer* dst, uint64_t offset, const void* src, uint64_t size)
+{
+  if (!p || !dst || !src || offset > dst->size || size > dst->size - offset || dst->imported)
+  {
+    set_error("cqlcuda_persistent_copy: bad destination");
+    return 0;
+  }
+  return note_cuda(cudaMemcpyAsync((char*)dst->dptr + offset, src, size, cudaMemcpyHostToDevice, p->copies), "persistent copy");
+}
+
+// waits at most timeout_ms for the kernel to return, then frees it: 1 done, 0 still running (p is kept)
+extern "C" int cqlcuda_persistent_destroy(CqlPersistent* p, uint32_t timeout_ms)
+{
+  if (!p) return 1;
+  auto t0 = std::chrono::steady_clock::now();
+  while (cqlcuda_persistent_running(p) == 1)
+  {
+    if (std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(timeout_ms))
+    {
+      set_error("cqlcuda_persistent_destroy: the kernel still runs after %u ms", timeout_ms);
+      return 0;
+    }
+    std::this_thread::sleep_for(std::chrono::microseconds(100));
+  }
+  wait_stream(p->copies, "persistent copies");
+  cudaStreamDestroy(p->copies);
+  cudaStreamDestroy(p->stream);
+  CqlState& s = S();
+  {
+    std::lock_guard<std::recursive_mutex> g(s.lock);
+    if (s.persistent_open) s.persistent_open -= 1;
+  }
+  delete p;
+  return 1;
 }

@@ -364,17 +364,100 @@ static uint32_t register_ctas_per_sm(uint32_t block)
   return BATCH_CTAS_PER_SM * 256u / block;
 }
 
-/* the source of one launch: `shape_exprs` over `shapes` shapes, the register blocks of slot_type */
+/* The persistent form's additions: parameter loads that skip L1 (a slot's parameters are rewritten by
+   copies between the kernel's uses of them, and L1 is not coherent with those copies), and the queue loop. */
+static const char* PERSIST_PRELUDE =
+  "__device__ __forceinline__ unsigned long long cql_cg64(const void* p) { unsigned long long v; asm volatile(\"ld.global.cg.u64 %0, [%1];\" : \"=l\"(v) : \"l\"(p)); return v; }\n"
+  "__device__ __forceinline__ u32 cql_cg32(const void* p) { u32 v; asm volatile(\"ld.global.cg.u32 %0, [%1];\" : \"=r\"(v) : \"l\"(p)); return v; }\n"
+  "struct ThrLd { const Thr* p; __device__ __forceinline__ Thr operator[](u32 i) const { const Thr* t = p + i; Thr r;\n"
+  "  r.a = cql_cg64(&t->a); r.b = cql_cg64(&t->b); const u64 cd = cql_cg64(&t->c); r.c = (u32)cd; r.d = (u32)(cd >> 32); r.pad = 0ull; return r; } };\n"
+  "struct QcLd { const double* p; __device__ __forceinline__ double operator[](u32 i) const { return __longlong_as_double((long long)cql_cg64(p + i)); } };\n"
+  "__device__ __forceinline__ u64 cql_now() { u64 t; asm volatile(\"mov.u64 %0, %%globaltimer;\" : \"=l\"(t)); return t; }\n"
+  "__device__ __forceinline__ u64 cql_acquire64(const void* p) { u64 v; asm volatile(\"ld.acquire.gpu.global.u64 %0, [%1];\" : \"=l\"(v) : \"l\"(p) : \"memory\"); return v; }\n"
+  "__device__ __forceinline__ void cql_release_sys64(void* p, u64 v) { asm volatile(\"st.release.sys.global.u64 [%0], %1;\" :: \"l\"(p), \"l\"(v) : \"memory\"); }\n";
+
+/* The persistent entry (cql_persist): every CTA waits for the next sequence number in the ring (thread 0
+   polls, at most the idle limit, then the CTA returns; the stop word ~0 returns at once), builds the slot's launch in shared memory and runs
+   the scan over its share of the table, adding its totals into the slot's accumulators with atomics (exact
+   integer sums, so the order does not matter); the CTA that finishes last copies the answers into host
+   memory, clears the accumulators and its ticket, and publishes the sequence number as done.
+     p.buf[0]  ring: the sequence number of each slot (R u64, device; the host's copy of it lands after the
+               slot's parameters)
+     p.buf[1]  the slots' parameters (R x SB bytes, device): scales (256 B), a header (nq, need | sums << 32),
+               thresholds at 512, literals, summed columns, shape starts - the ordinary launch's layout
+     p.buf[2]  the slots' accumulators (R x NQ x 3 u64: count, low, high of the scaled sum)
+     p.buf[3]  the slots' CTA tickets (R u32)
+     p.buf[4]  answers (R x NQ x 3 u64, page-locked host memory)
+     p.buf[5]  done words (R u64, page-locked host memory)
+     p.buf[6 + c] the columns
+   words: 0 rows, 2 R, 4 NQ, 6 SB, 8 idle limit (microseconds), 10 and 11 the first sequence number */
+static const char* PERSIST_ENTRY =
+  "extern \"C\" __global__ void __launch_bounds__(CQL_BLOCK) cql_persist(CqlLaunch p)\n{\n"
+  "  __shared__ CqlLaunch s_a; __shared__ u32 s_go, s_last;\n"
+  "  const u64 rows = cql_word(p, 0); const u32 R = cql_word(p, 2), NQ = cql_word(p, 4), SB = cql_word(p, 6);\n"
+  "  const u64 idle_ns = (u64)cql_word(p, 8) * 1000ull;\n"
+  "  u64 seq = (u64)cql_word(p, 10) | ((u64)cql_word(p, 11) << 32);\n"
+  "  const u64 off_qc = 512ull + (u64)NQ * 16ull * 32ull, off_qs = off_qc + (u64)NQ * 32ull * 8ull, off_begin = off_qs + (((u64)NQ * 4ull + 15ull) & ~15ull);\n"
+  "  for (;; seq++)\n  {\n"
+  "    const u32 slot = (u32)(seq % R);\n"
+  "    if (threadIdx.x == 0)\n    {\n"
+  "      const u64* ring = (const u64*)p.buf[0] + slot;\n"
+  "      const u64 t0 = cql_now(); u32 go = 0u;\n"
+  "      for (;;) { const u64 v = cql_acquire64(ring); if (v == seq) { go = 1u; break; } if (v == ~0ull || cql_now() - t0 > idle_ns) break; __nanosleep(256); }\n"
+  "      s_go = go;\n"
+  "      if (go)\n      {\n"
+  "        const char* sp = (const char*)p.buf[1] + (u64)slot * SB;\n"
+  "        const u64 nq = cql_cg64(sp + 256), needs = cql_cg64(sp + 264);\n"
+  "        for (int i = 0; i < 16; i++) { s_a.buf[i] = p.buf[i]; s_a.bytes[i] = p.bytes[i]; }\n"
+  "        s_a.buf[0] = (void*)sp; s_a.bytes[0] = 256ull;\n"
+  "        s_a.buf[1] = (void*)(sp + 512); s_a.bytes[1] = off_qc - 512ull;\n"
+  "        s_a.buf[2] = (void*)(sp + off_qc); s_a.bytes[2] = off_qs - off_qc;\n"
+  "        s_a.buf[3] = (void*)(sp + off_qs); s_a.bytes[3] = (u64)NQ * 4ull;\n"
+  "        s_a.buf[4] = (void*)(sp + off_begin); s_a.bytes[4] = (u64)SB - off_begin;\n"
+  "        s_a.buf[5] = (void*)((u64*)p.buf[2] + (u64)slot * NQ * 3ull); s_a.bytes[5] = (u64)NQ * 24ull;\n"
+  "        s_a.push[0] = rows; s_a.push[1] = nq; s_a.push[2] = 0ull; s_a.push[3] = needs;\n"
+  "        for (int i = 4; i < 8; i++) s_a.push[i] = 0ull;\n"
+  "      }\n"
+  "    }\n"
+  "    __syncthreads();\n"
+  "    if (!s_go) return;\n"
+  "    cql_scan(s_a, blockIdx.x, gridDim.x);\n"
+  "    __syncthreads();\n"
+  "    if (threadIdx.x == 0) { __threadfence(); s_last = atomicAdd((u32*)p.buf[3] + slot, 1u) == gridDim.x - 1u; }\n"
+  "    __syncthreads();\n"
+  "    if (s_last)\n    {\n"
+  "      __threadfence();\n"
+  "      const u32 nq = (u32)s_a.push[1];\n"
+  "      u64* acc = (u64*)s_a.buf[5];\n"
+  "      u64* out = (u64*)p.buf[4] + (u64)slot * NQ * 3ull;\n"
+  "      for (u32 i = threadIdx.x; i < nq * 3u; i += blockDim.x) { out[i] = cql_cg64(acc + i); acc[i] = 0ull; }\n"
+  "      __threadfence_system();\n"
+  "      __syncthreads();\n"
+  "      if (threadIdx.x == 0) { ((u32*)p.buf[3])[slot] = 0u; __threadfence_system(); cql_release_sys64((u64*)p.buf[5] + slot, seq); }\n"
+  "    }\n"
+  "    __syncthreads();\n"
+  "  }\n"
+  "}\n";
+
+/* the source of one launch: `shape_exprs` over `shapes` shapes, the register blocks of slot_type. persistent:
+   the scan as a device function adding its totals into accumulators, entered by cql_main (one pass) and by
+   the persistent queue loop cql_persist */
 static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint32_t shapes, const int* slot_type, const int* sum_cols,
-                          uint32_t sum_col_count, uint32_t rows_per_thread, uint32_t block)
+                          uint32_t sum_col_count, uint32_t rows_per_thread, uint32_t block, int persistent)
 {
   Buf b;
   memset(&b, 0, sizeof(b));
   bput(&b, "// cql: block=%u smem=%u per_sm=%u\n", block, (block / 32u) * CQL_BATCH_LAUNCH_QUERIES * 12u, register_ctas_per_sm(block));
   bput(&b, "%s", BATCH_PRELUDE);
+  if (persistent) bput(&b, "#define CQL_BLOCK %u\n%s", block, PERSIST_PRELUDE);
   for (uint32_t s = 0; s < shapes; s++) bput(&b, "#define CQL_SHAPE_%u(k) (%s)\n", s, shape_exprs[s]);
+  if (persistent)
+    bput(&b, "__device__ __forceinline__ void cql_scan(const CqlLaunch& a, const u32 cta, const u32 ctas)\n{\n"
+             "#define CQL_LD32(p) cql_cg32(p)\n#define CQL_LDF(p) __longlong_as_double((long long)cql_cg64(p))\n#define CQL_LDI(p) ((long long)cql_cg64(p))\n");
+  else
+    bput(&b, "extern \"C\" __global__ void __launch_bounds__(%u) cql_main(CqlLaunch a)\n{\n  const u32 cta = blockIdx.x, ctas = gridDim.x;\n"
+             "#define CQL_LD32(p) (*(p))\n#define CQL_LDF(p) (*(p))\n#define CQL_LDI(p) (*(p))\n", block);
   bput(&b,
-       "extern \"C\" __global__ void __launch_bounds__(%u) cql_main(CqlLaunch a)\n{\n"
        "  const u64 rows = cql_word(a, 0); const u32 nq = cql_word(a, 2); const u32 q0 = cql_word(a, 4);\n"
        "  const u32 need = cql_word(a, 6), need_sum = cql_word(a, 7);   /* the columns this launch reads and sums */\n"
        "  (void)need_sum;\n"
@@ -392,12 +475,12 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
        "  __syncthreads();\n"
        "  long long* acc = (long long*)s_acc + (u64)warp * nq; u32* cacc = s_cnt + (u64)warp * nq;\n"
        "  const u32 RPT = %uu;\n"
-       "  const u64 groups = (rows + RPT - 1ull) / RPT; const u64 per_pass = (u64)gridDim.x * blockDim.x;\n"
-       "  for (u64 g0 = (u64)blockIdx.x * blockDim.x; g0 < groups; g0 += per_pass)\n  {\n"
+       "  const u64 groups = (rows + RPT - 1ull) / RPT; const u64 per_pass = (u64)ctas * blockDim.x;\n"
+       "  for (u64 g0 = (u64)cta * blockDim.x; g0 < groups; g0 += per_pass)\n  {\n"
        "    const u64 row0 = (g0 + threadIdx.x) * RPT;\n"
        "    const u32 valid = row0 < rows ? (u32)min((u64)RPT, rows - row0) : 0u;\n"
        "    const u32 valid_mask = valid >= 32u ? 0xffffffffu : ((1u << valid) - 1u);\n",
-       block, rows_per_thread);
+       rows_per_thread);
   /* the register blocks */
   for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++)
   {
@@ -436,7 +519,7 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
     else if (t == CQLOPS_TYPE_I64) snprintf(expr, sizeof(expr), "__double2ll_rn(cql_i64d(r%d[v]) * sc)", c);
     else snprintf(expr, sizeof(expr), "(sh >= 0 ? (long long)((u64)r%d[v] << sh) : __double2ll_rn((double)r%d[v] * sc))", c, c);
     bput(&b, "    long long fx%d[%u];\n    if (!((need_sum >> %d) & 1u)) { for (u32 v = 0; v < RPT; v++) fx%d[v] = 0ll; }\n", c, rows_per_thread, c, c);
-    bput(&b, "    else { const double sc = col_scale[%d]; const int sh = (int)col_shift[%d]; (void)sh; (void)sc;\n", c, c);
+    bput(&b, "    else { const double sc = CQL_LDF(col_scale + %d); const int sh = (int)CQL_LDI(col_shift + %d); (void)sh; (void)sc;\n", c, c);
     bput(&b, "      for (u32 v = 0; v < RPT; v++) fx%d[v] = v < valid ? %s : 0ll; }\n", c, expr);
   }
   for (uint32_t s = 0; s < shapes; s++)
@@ -448,8 +531,8 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
     for (uint32_t i = 0; i < shape_sites[s] && i < BATCH_MAX_SITES; i++)
       dn += (size_t)snprintf(decls + dn, sizeof(decls) - dn, "      const Thr T%u = TH[%u];\n", i, i);
     bput(&b,
-         "    for (u32 q = shape_begin[%u]; q < shape_begin[%u]; q++)\n    {\n"
-         "      const Thr* TH = thr + (u64)(q0 + q) * %uu; const double* QC = qconst + (u64)(q0 + q) * %uu;\n"
+         "    for (u32 q = CQL_LD32(shape_begin + %u); q < CQL_LD32(shape_begin + %u); q++)\n    {\n"
+         "      const %s TH%s thr + (u64)(q0 + q) * %uu%s; const %s QC%s qconst + (u64)(q0 + q) * %uu%s;\n"
          "      (void)TH; (void)QC;\n"
          "%s"
          "      u32 m = 0u;\n"
@@ -457,9 +540,10 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
          "      for (u32 k = 0; k < RPT; k++) m |= ((CQL_SHAPE_%u(k)) ? 1u : 0u) << k;\n"
          "      m &= valid_mask;\n"
          "      const u32 cnt = __reduce_add_sync(0xffffffffu, (u32)__popc(m));\n"
-         "      const u32 sc = qsum[q0 + q];\n"
+         "      const u32 sc = CQL_LD32(qsum + q0 + q);\n"
          "      long long sv = 0ll;\n",
-         s, s + 1, BATCH_MAX_SITES, BATCH_MAX_CONSTS, decls, s);
+         s, s + 1, persistent ? "ThrLd" : "Thr*", persistent ? "{" : " =", BATCH_MAX_SITES, persistent ? "}" : "",
+         persistent ? "QcLd" : "double*", persistent ? "{" : " =", BATCH_MAX_CONSTS, persistent ? "}" : "", decls, s);
     for (uint32_t i = 0; i < sum_col_count; i++)
       bput(&b, "      if (sc == %du && m) {\n#pragma unroll\n        for (u32 k = 0; k < RPT; k++) if ((m >> k) & 1u) sv += fx%d[k];\n      }\n", sum_cols[i],
            sum_cols[i]);
@@ -475,9 +559,17 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
        "    u64 c = 0ull, lo = 0ull, hi = 0ull;\n"
        "    for (u32 w = 0; w < warps; w++) { long long v = (long long)s_acc[(u64)w * nq + q]; c += s_cnt[(u64)w * nq + q];\n"
        "      u64 l2 = lo + (u64)v; hi += (u64)(v < 0 ? -1ll : 0ll) + (l2 < lo ? 1ull : 0ull); lo = l2; }\n"
-       "    const u64 at = (u64)blockIdx.x * nq + q;\n"
-       "    if (at < pcap) { partials[at * 3] = c; partials[at * 3 + 1] = lo; partials[at * 3 + 2] = hi; }\n"
-       "  }\n}\n");
+       "%s"
+       "  }\n"
+       "#undef CQL_LD32\n#undef CQL_LDF\n#undef CQL_LDI\n}\n",
+       persistent ? /* the CTA's 128-bit totals added into the accumulators: the low words with a carry into the high */
+                    "    if (q < pcap && (c | lo | hi)) { if (c) atomicAdd(&partials[q * 3], c); const u64 old = atomicAdd(&partials[q * 3 + 1], lo);\n"
+                    "      const u64 up = hi + ((old + lo < old) ? 1ull : 0ull); if (up) atomicAdd(&partials[q * 3 + 2], up); }\n"
+                  : "    const u64 at = (u64)cta * nq + q;\n"
+                    "    if (at < pcap) { partials[at * 3] = c; partials[at * 3 + 1] = lo; partials[at * 3 + 2] = hi; }\n");
+  if (persistent)
+    bput(&b, "extern \"C\" __global__ void __launch_bounds__(CQL_BLOCK) cql_main(CqlLaunch a) { cql_scan(a, blockIdx.x, gridDim.x); }\n%s",
+         PERSIST_ENTRY);
   if (b.failed)
   {
     free(b.p);
@@ -1174,10 +1266,10 @@ static char* cube_answer_source(const CubePlan* P, char** shape_exprs, const uin
 
 /* the source of one launch in the form rows_per_thread asks for */
 static char* launch_source(char** shape_exprs, const uint32_t* shape_sites, uint32_t shapes, const int* slot_type, const int* sum_cols,
-                           uint32_t sum_col_count, uint32_t rows_per_thread, uint32_t block)
+                           uint32_t sum_col_count, uint32_t rows_per_thread, uint32_t block, int persistent)
 {
   if (!rows_per_thread) return batch_source_tiled(shape_exprs, shape_sites, shapes, slot_type, sum_cols, sum_col_count);
-  return batch_source(shape_exprs, shape_sites, shapes, slot_type, sum_cols, sum_col_count, rows_per_thread, block);
+  return batch_source(shape_exprs, shape_sites, shapes, slot_type, sum_cols, sum_col_count, rows_per_thread, block, persistent);
 }
 
 /* ---- the shape catalog ---- */
@@ -1232,6 +1324,7 @@ typedef struct
   uint32_t sums[CQL_BATCH_CATALOG_SHAPES];
   int slot_type[CQLOPS_MAX_BINDINGS];
   uint32_t sum_mask;
+  uint64_t version;
 } CatalogView;
 
 /* Maps the batch's shapes to catalog entries (adding the new ones) and takes a view of the catalog.
@@ -1317,6 +1410,7 @@ static int catalog_map(CqlBatchCatalog* c, uint32_t shapes, char** exprs, const 
     memcpy(view->sums, c->sums, sizeof(c->sums));
     memcpy(view->slot_type, c->slot_type, sizeof(c->slot_type));
     view->sum_mask = c->sum_mask;
+    view->version = c->version;
   }
   pthread_mutex_unlock(&c->lock);
   return ok;
@@ -1324,7 +1418,27 @@ static int catalog_map(CqlBatchCatalog* c, uint32_t shapes, char** exprs, const 
 
 /* ---- the operator ---- */
 
-enum { BATCH_RUN = 0, BATCH_SOURCE = 1, BATCH_PREPARE = 2, BATCH_CUBE_BUILD_SOURCE = 3, BATCH_CUBE_ANSWER_SOURCE = 4 };
+enum { BATCH_RUN = 0, BATCH_SOURCE = 1, BATCH_PREPARE = 2, BATCH_CUBE_BUILD_SOURCE = 3, BATCH_CUBE_ANSWER_SOURCE = 4, BATCH_PERSIST = 5 };
+
+/* the persistent form's submission of one planned batch (defined with the persistent form below) */
+typedef struct
+{
+  const CatalogView* view;
+  uint32_t scan_n;
+  const uint32_t* order;
+  const uint32_t* shape_of;
+  const Thr* thr;
+  const double* qconst;
+  const uint32_t* qsum_ordered;
+  const uint32_t* qsum;
+  const double* col_scale;
+  const int64_t* col_shift;
+  uint32_t need, sums;
+  const int* sum_cols;
+  uint32_t sum_col_count;
+} PersistJob;
+static __thread CqlBatchPersist* tl_persist;
+static int persist_submit(CqlBatchPersist* P, const PersistJob* j, uint64_t* out_counts, double* out_sums, char* why, size_t why_cap);
 
 /* The operator; with BATCH_SOURCE the source of its first launch, with BATCH_PREPARE its kernel compiled
    and the shapes entered in the catalog (neither does device work on the table). */
@@ -1340,6 +1454,7 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
   uint32_t cube_pass = rows_per_thread;
   /* the form: rows per thread in the low byte, the register form's block size / 256 in the next (1 or 2) */
   uint32_t block = ((rows_per_thread >> 8) & 0xffu) == 2u ? 512u : 256u;
+  int persistent_source = mode == BATCH_SOURCE && ((rows_per_thread >> 16) & 1u);   /* the persistent form's source */
   rows_per_thread &= 0xffu;
   if (rows_per_thread != 0 && rows_per_thread != 4 && rows_per_thread != 8 && rows_per_thread != 16) rows_per_thread = 8;
   uint64_t rows = columns[0].rows;
@@ -1711,7 +1826,7 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     uint32_t nq = scan_n < CQL_BATCH_LAUNCH_QUERIES ? scan_n : CQL_BATCH_LAUNCH_QUERIES;
     uint32_t ns;
     SLICE_SHAPES(0, nq, ns);
-    char* src = launch_source(slice_exprs, slice_sites, ns, launch_types, sum_cols, sum_col_count, rows_per_thread, block);
+    char* src = launch_source(slice_exprs, slice_sites, ns, launch_types, sum_cols, sum_col_count, rows_per_thread, block, persistent_source);
     ok = src != NULL;
     if (ok && mode == BATCH_SOURCE)
     {
@@ -1730,6 +1845,21 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     free(src);
   }
   if (ok && (mode == BATCH_SOURCE || mode == BATCH_PREPARE) && out_shapes) *out_shapes = shapes;
+  if (mode == BATCH_PERSIST)
+  {
+    /* the persistent form: the batch's parameters into a ring slot of the kernel compiled for the catalog */
+    if (ok && (!view || launch_exprs != view->exprs || scan_n != query_count || scan_n > CQL_BATCH_LAUNCH_QUERIES))
+    {
+      snprintf(why, sizeof(why), "the persistent scan takes at most %d queries of catalog shapes", CQL_BATCH_LAUNCH_QUERIES);
+      ok = 0;
+    }
+    if (ok)
+    {
+      PersistJob job = { view, scan_n, order, shape_of, thr_o, qc_o, qs_o, qsum, col_scale, col_shift, need, scan_sums, sum_cols, sum_col_count };
+      ok = persist_submit(tl_persist, &job, out_counts, out_sums, why, sizeof(why));
+      if (ok && out_shapes) *out_shapes = shapes;
+    }
+  }
   int launch = ok && mode == BATCH_RUN;
   /* one upload of every launch parameter: the scales (doubles at 0..), then their exponents (64-bit
      integers at 16..), the scan's thresholds, literals and summed columns in shape order, each slice's shape
@@ -1797,7 +1927,7 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     CqlKernel* k = shared_k;
     if (!k)
     {
-      char* src = launch_source(slice_exprs, slice_sites, ns, launch_types, sum_cols, sum_col_count, rows_per_thread, block);
+      char* src = launch_source(slice_exprs, slice_sites, ns, launch_types, sum_cols, sum_col_count, rows_per_thread, block, 0);
       if (!src)
       {
         ok = 0;
@@ -1973,6 +2103,280 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
   free(qs_o);
   free(folded);
   return ok;
+}
+
+/* ---- the persistent form ---- */
+
+#define PERSIST_SLOTS 4
+#define PERSIST_WAIT_MS 5000
+
+struct CqlBatchPersist
+{
+  pthread_mutex_t lock;
+  CqlBatchCatalog* catalog;
+  CqlColumn columns[CQLOPS_MAX_BINDINGS];
+  uint32_t column_count;
+  uint32_t rows_per_thread;
+  uint32_t idle_us;
+  uint64_t version;             /* the catalog version the kernel was compiled from */
+  int compiled;
+  CqlKernel* kernel;
+  CqlPersistent* run;
+  CqlBuffer* ring;              /* PERSIST_SLOTS sequence words */
+  CqlBuffer* params;            /* PERSIST_SLOTS parameter slots */
+  CqlBuffer* state;             /* tickets (64 bytes), then the accumulators */
+  CqlBuffer* answers_buf;       /* page-locked host: the answers, then the done words */
+  uint64_t* answers;
+  uint64_t* done;
+  uint64_t slot_bytes;
+  unsigned char* staging;       /* each slot's parameters as copied (kept until the batch is done) */
+  uint64_t seq_word[PERSIST_SLOTS + 1];
+  uint64_t next_seq;
+  uint64_t batches, launches, compiles;
+  int broken;
+};
+
+/* a slot's layout: the scales and shifts (256 B), the header (nq, need | sums << 32) at 256, thresholds at
+   512, literals, summed columns, shape starts (the generated entry computes the same offsets from NQ) */
+static uint64_t persist_off_qc(void) { return 512ull + (uint64_t)CQL_BATCH_LAUNCH_QUERIES * BATCH_MAX_SITES * sizeof(Thr); }
+static uint64_t persist_off_qs(void) { return persist_off_qc() + (uint64_t)CQL_BATCH_LAUNCH_QUERIES * BATCH_MAX_CONSTS * 8ull; }
+static uint64_t persist_off_begin(void) { return persist_off_qs() + (((uint64_t)CQL_BATCH_LAUNCH_QUERIES * 4ull + 15ull) & ~15ull); }
+
+static uint64_t persist_state_bytes(void) { return 64ull + (uint64_t)PERSIST_SLOTS * CQL_BATCH_LAUNCH_QUERIES * 24ull; }
+
+CqlBatchPersist* cqlops_batch_persist_create(CqlBatchCatalog* catalog, const CqlColumn* columns, uint32_t column_count,
+                                             uint32_t rows_per_thread, uint32_t idle_us)
+{
+  cqlops_note_error("");
+  if (!catalog || !columns || column_count == 0 || column_count > CQLOPS_MAX_BINDINGS)
+  {
+    refuse("the persistent scan needs a catalog and 1 to 10 columns");
+    return NULL;
+  }
+  if (rows_per_thread != 4 && rows_per_thread != 8 && rows_per_thread != 16)
+  {
+    refuse("the persistent scan takes 4, 8 or 16 rows per thread");
+    return NULL;
+  }
+  if (!cqlops_rows_fit(columns[0].rows)) return NULL;
+  for (uint32_t c = 0; c < column_count; c++)
+    if (!columns[c].buffer || columns[c].rows != columns[0].rows || columns[c].width != 0)
+    {
+      refuse("batched columns are full-width numeric columns of one length");
+      return NULL;
+    }
+  CqlBatchPersist* p = (CqlBatchPersist*)calloc(1, sizeof(CqlBatchPersist));
+  if (!p) return NULL;
+  pthread_mutex_init(&p->lock, NULL);
+  p->catalog = catalog;
+  memcpy(p->columns, columns, column_count * sizeof(CqlColumn));
+  p->column_count = column_count;
+  p->rows_per_thread = rows_per_thread;
+  p->idle_us = idle_us ? idle_us : 2000;
+  p->slot_bytes = (persist_off_begin() + (BATCH_MAX_SHAPES + 1) * 4 + 255) & ~255ull;
+  p->ring = cqlcuda_buffer_alloc(PERSIST_SLOTS * 8, CQLCUDA_BUFFER_READ_WRITE, NULL);
+  p->params = cqlcuda_buffer_alloc(PERSIST_SLOTS * p->slot_bytes, CQLCUDA_BUFFER_READ_WRITE, NULL);
+  p->state = cqlcuda_buffer_alloc(persist_state_bytes(), CQLCUDA_BUFFER_READ_WRITE, NULL);
+  void* host = NULL;
+  p->answers_buf = cqlcuda_buffer_alloc_host_mapped((uint64_t)PERSIST_SLOTS * CQL_BATCH_LAUNCH_QUERIES * 24 + PERSIST_SLOTS * 8, &host);
+  p->staging = (unsigned char*)calloc(PERSIST_SLOTS, p->slot_bytes);
+  if (!p->ring || !p->params || !p->state || !p->answers_buf || !p->staging)
+  {
+    cqlops_batch_persist_destroy(p);
+    return NULL;
+  }
+  p->answers = (uint64_t*)host;
+  p->done = p->answers + (uint64_t)PERSIST_SLOTS * CQL_BATCH_LAUNCH_QUERIES * 3;
+  /* the ring starts at 0 (no sequence number is 0) */
+  uint64_t zero[PERSIST_SLOTS] = { 0 };
+  cqlcuda_buffer_write(p->ring, zero, sizeof(zero));
+  p->next_seq = 1;
+  return p;
+}
+
+/* tells a running kernel to return (the stop word in the slot it waits on) and waits for it */
+static int persist_stop(CqlBatchPersist* P)
+{
+  if (!P->run) return 1;
+  if (cqlcuda_persistent_running(P->run) == 1)
+  {
+    P->seq_word[PERSIST_SLOTS] = ~0ull;
+    cqlcuda_persistent_copy(P->run, P->ring, (P->next_seq % PERSIST_SLOTS) * 8, &P->seq_word[PERSIST_SLOTS], 8);
+  }
+  if (!cqlcuda_persistent_destroy(P->run, PERSIST_WAIT_MS)) return 0;
+  P->run = NULL;
+  /* the stop word must not stay where the next kernel looks */
+  uint64_t ring[PERSIST_SLOTS] = { 0 };
+  cqlcuda_buffer_write(P->ring, ring, sizeof(ring));
+  return 1;
+}
+
+/* the kernel for the catalog as the job's view holds it */
+static int persist_compile(CqlBatchPersist* P, const PersistJob* j)
+{
+  if (!persist_stop(P)) return refuse("the persistent scan did not return");
+  char* src = batch_source((char**)j->view->exprs, j->view->sites, j->view->shapes, j->view->slot_type, j->sum_cols, j->sum_col_count,
+                           P->rows_per_thread, 256, 1);
+  if (!src) return 0;
+  char name[64];
+  snprintf(name, sizeof(name), "qk_persist_%016llx", (unsigned long long)fnv_str(src));
+  size_t nlen = strlen(name);
+  CqlKernel* k = cqlcuda_kernel_alloc(name, nlen);
+  if (!k) k = cqlcuda_kernel_alloc_from_image(name, nlen, src, strlen(src));
+  free(src);
+  if (!k) return 0;
+  P->run = cqlcuda_persistent_create(k, "cql_persist");
+  if (!P->run) return 0;
+  P->kernel = k;
+  P->version = j->view->version;
+  P->compiled = 1;
+  P->compiles++;
+  return 1;
+}
+
+/* launches the kernel (again), starting at sequence number `first`, with the accumulators and tickets clear */
+static int persist_launch(CqlBatchPersist* P, uint64_t first)
+{
+  CqlKernel* k = P->kernel;
+  cqlcuda_kernel_set_arg_buffer(k, 0, P->ring);
+  cqlcuda_kernel_set_arg_buffer(k, 1, P->params);
+  cqlcuda_kernel_set_arg_buffer_range(k, 2, P->state, 64, persist_state_bytes() - 64);
+  cqlcuda_kernel_set_arg_buffer_range(k, 3, P->state, 0, 64);
+  cqlcuda_kernel_set_arg_buffer_range(k, 4, P->answers_buf, 0, (uint64_t)PERSIST_SLOTS * CQL_BATCH_LAUNCH_QUERIES * 24);
+  cqlcuda_kernel_set_arg_buffer_range(k, 5, P->answers_buf, (uint64_t)PERSIST_SLOTS * CQL_BATCH_LAUNCH_QUERIES * 24, PERSIST_SLOTS * 8);
+  for (uint32_t c = 0; c < CQLOPS_MAX_BINDINGS; c++)
+    cqlcuda_kernel_set_arg_buffer(k, 6 + c, P->columns[c < P->column_count ? c : 0].buffer);
+  cqlcuda_kernel_set_arg_u64(k, 0, P->columns[0].rows);
+  cqlcuda_kernel_set_arg_u64(k, 1, PERSIST_SLOTS);
+  cqlcuda_kernel_set_arg_u64(k, 2, CQL_BATCH_LAUNCH_QUERIES);
+  cqlcuda_kernel_set_arg_u64(k, 3, P->slot_bytes);
+  cqlcuda_kernel_set_arg_u64(k, 4, P->idle_us);
+  cqlcuda_kernel_set_arg_u64(k, 5, first);
+  if (!cqlcuda_persistent_launch(P->run, 0, P->state, persist_state_bytes())) return 0;
+  P->launches++;
+  return 1;
+}
+
+static int persist_submit(CqlBatchPersist* P, const PersistJob* j, uint64_t* out_counts, double* out_sums, char* why, size_t why_cap)
+{
+  if (!P || P->broken)
+  {
+    snprintf(why, why_cap, "the persistent scan is not usable");
+    return 0;
+  }
+  if (!P->compiled || P->version != j->view->version)
+    if (!persist_compile(P, j)) return 0;
+  uint64_t seq = P->next_seq;
+  uint32_t slot = (uint32_t)(seq % PERSIST_SLOTS);
+  /* the slot's parameters */
+  unsigned char* sp = P->staging + (uint64_t)slot * P->slot_bytes;
+  memcpy(sp, j->col_scale, CQLOPS_MAX_BINDINGS * sizeof(double));
+  memset(sp + CQLOPS_MAX_BINDINGS * sizeof(double), 0, 128 - CQLOPS_MAX_BINDINGS * sizeof(double));
+  memcpy(sp + 128, j->col_shift, CQLOPS_MAX_BINDINGS * sizeof(int64_t));
+  uint64_t hdr[2] = { j->scan_n, (uint64_t)j->need | (uint64_t)j->sums << 32 };
+  memcpy(sp + 256, hdr, sizeof(hdr));
+  memcpy(sp + 512, j->thr, (size_t)j->scan_n * BATCH_MAX_SITES * sizeof(Thr));
+  memcpy(sp + persist_off_qc(), j->qconst, (size_t)j->scan_n * BATCH_MAX_CONSTS * 8);
+  memcpy(sp + persist_off_qs(), j->qsum_ordered, (size_t)j->scan_n * 4);
+  /* where each catalog shape's queries start in the ordered list */
+  uint32_t* begin = (uint32_t*)(sp + persist_off_begin());
+  uint32_t at = 0;
+  for (uint32_t s = 0; s < j->view->shapes; s++)
+  {
+    while (at < j->scan_n && j->shape_of[j->order[at]] < s) at++;
+    begin[s] = at;
+  }
+  begin[j->view->shapes] = j->scan_n;
+  uint64_t used = persist_off_begin() + (j->view->shapes + 1) * 4;
+  P->seq_word[slot] = seq;
+  if (!cqlcuda_persistent_copy(P->run, P->params, (uint64_t)slot * P->slot_bytes, sp, used) ||
+      !cqlcuda_persistent_copy(P->run, P->ring, (uint64_t)slot * 8, &P->seq_word[slot], 8))
+    return 0;
+  P->next_seq = seq + 1;
+  if (cqlcuda_persistent_running(P->run) != 1 && !persist_launch(P, seq)) return 0;
+  /* the answers: poll the done word; a kernel that returned (its idle limit met just before the batch) is
+     launched again at this batch, its accumulators cleared */
+  struct timespec t0, t;
+  clock_gettime(CLOCK_MONOTONIC, &t0);
+  uint32_t polls = 0;
+  for (;;)
+  {
+    if (__atomic_load_n(&P->done[slot], __ATOMIC_ACQUIRE) == seq) break;
+    if ((++polls & 1023u) == 0)
+    {
+      int r = cqlcuda_persistent_running(P->run);
+      if (__atomic_load_n(&P->done[slot], __ATOMIC_ACQUIRE) == seq) break;
+      if (r < 0)
+      {
+        P->broken = 1;
+        snprintf(why, why_cap, "the persistent scan failed: %s", cqlcuda_last_error());
+        return 0;
+      }
+      if (r == 0 && !persist_launch(P, seq)) return 0;
+      clock_gettime(CLOCK_MONOTONIC, &t);
+      if ((t.tv_sec - t0.tv_sec) * 1000.0 + (t.tv_nsec - t0.tv_nsec) / 1e6 > PERSIST_WAIT_MS)
+      {
+        P->broken = 1;
+        snprintf(why, why_cap, "the persistent scan did not answer batch %llu within %d ms", (unsigned long long)seq, PERSIST_WAIT_MS);
+        return 0;
+      }
+    }
+  }
+  const uint64_t* ans = P->answers + (uint64_t)slot * CQL_BATCH_LAUNCH_QUERIES * 3;
+  for (uint32_t i = 0; i < j->scan_n; i++)
+  {
+    uint32_t q = j->order[i];
+    out_counts[q] = ans[i * 3];
+    if (!out_sums) continue;
+    if (j->qsum[q] == 0xffffffffu)
+    {
+      out_sums[q] = 0.0;
+      continue;
+    }
+    double v = (double)(int64_t)ans[i * 3 + 2] * 18446744073709551616.0 + (double)ans[i * 3 + 1];
+    out_sums[q] = v / j->col_scale[j->qsum[q]];
+  }
+  P->batches++;
+  return 1;
+}
+
+int cqlops_batch_persist_run(CqlBatchPersist* p, const CqlProgram* const* programs, uint32_t query_count, const int32_t* sum_columns,
+                             uint64_t* out_counts, double* out_sums)
+{
+  cqlops_note_error("");
+  if (!p) return refuse("no persistent scan");
+  if (query_count == 0) return 1;
+  pthread_mutex_lock(&p->lock);
+  tl_persist = p;
+  int ok = batch_run(p->catalog, programs, query_count, p->columns, p->column_count, sum_columns, p->rows_per_thread, out_counts, out_sums,
+                     NULL, BATCH_PERSIST, NULL, 0, NULL, 0);
+  tl_persist = NULL;
+  pthread_mutex_unlock(&p->lock);
+  return ok;
+}
+
+void cqlops_batch_persist_stats(CqlBatchPersist* p, uint64_t* out_batches, uint64_t* out_launches, uint64_t* out_compiles)
+{
+  if (out_batches) *out_batches = p ? p->batches : 0;
+  if (out_launches) *out_launches = p ? p->launches : 0;
+  if (out_compiles) *out_compiles = p ? p->compiles : 0;
+}
+
+int cqlops_batch_persist_destroy(CqlBatchPersist* p)
+{
+  if (!p) return 1;
+  pthread_mutex_lock(&p->lock);
+  int ok = persist_stop(p);
+  pthread_mutex_unlock(&p->lock);
+  if (!ok) return 0;   /* still running: nothing is freed under it */
+  cqlcuda_buffer_release(p->ring);
+  cqlcuda_buffer_release(p->params);
+  cqlcuda_buffer_release(p->state);
+  cqlcuda_buffer_release(p->answers_buf);
+  free(p->staging);
+  pthread_mutex_destroy(&p->lock);
+  free(p);
+  return 1;
 }
 
 /* ---- the autotuner ----

@@ -170,6 +170,7 @@ CUDA_API = [
     ("cqlcuda_kernel_profile_enable", None, [C.c_int]),
     ("cqlcuda_kernel_profile_reset", None, []),
     ("cqlcuda_kernel_profile_entry", C.c_int, [u32, P, P, P]),
+    ("cqlcuda_host_profile", None, [P, P, P, P]),
     ("cqlcuda_kernel_launch_count", u32, []),
     ("cqlcuda_last_error", cstr, []),
     ("cqlcuda_clear_error", None, []),
@@ -186,6 +187,12 @@ CUDA_API = [
     ("cqlcuda_fill_affine_u32", C.c_int, [P, u64, u64, u64, u64]),
     ("cqlcuda_host_alloc", P, [u64]),
     ("cqlcuda_host_free", None, [P]),
+    ("cqlcuda_buffer_alloc_host_mapped", P, [u64, P]),
+    ("cqlcuda_persistent_create", P, [P, cstr]),
+    ("cqlcuda_persistent_launch", C.c_int, [P, u32, P, u64]),
+    ("cqlcuda_persistent_running", C.c_int, [P]),
+    ("cqlcuda_persistent_copy", C.c_int, [P, P, u64, P, u64]),
+    ("cqlcuda_persistent_destroy", C.c_int, [P, u32]),
     ("cqlcuda_flush_l2", C.c_int, [u64]),
     ("cqlcuda_timer_begin", None, []),
     ("cqlcuda_timer_end_ms", dbl, []),
@@ -227,6 +234,10 @@ OPS_API = [
     ("cqlops_batch_catalog_shapes", u32, [P]),
     ("cqlops_batch_filter_aggregate_cat", C.c_int, [P, P, u32, P, u32, P, u32, P, P, P]),
     ("cqlops_batch_prepare", C.c_int, [P, P, u32, P, u32, P, u32]),
+    ("cqlops_batch_persist_create", P, [P, P, u32, u32, u32]),
+    ("cqlops_batch_persist_run", C.c_int, [P, P, u32, P, P, P]),
+    ("cqlops_batch_persist_stats", None, [P, P, P, P]),
+    ("cqlops_batch_persist_destroy", C.c_int, [P]),
     ("cqlops_resident_create", P, [u64, P]),
     ("cqlops_resident_destroy", None, [P]),
     ("cqlops_resident_acquire", P, [P, u64, u64, P, u64, u64, u32, P]),

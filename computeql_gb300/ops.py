@@ -696,6 +696,49 @@ class BatchCatalog:
             N.load_ops().cqlops_batch_catalog_destroy(self.h)
             self.h = None
 
+
+class PersistentScan:
+    """The persistent shared scan over one table (cqlops_batch_persist_*): one long-lived kernel that takes
+    batches from a ring of parameter slots in device memory. The catalog must outlive it."""
+
+    def __init__(self, catalog, programs, rows_per_thread=8, idle_us=2000):
+        base = programs[0]
+        self.catalog = catalog
+        self._cols = base._cols
+        self._names = base
+        self.h = N.load_ops().cqlops_batch_persist_create(catalog.h, base._cols, len(base.columns), rows_per_thread, idle_us)
+        if not self.h:
+            raise OpError("cqlops_batch_persist_create: " + N.load_ops().cqlops_last_error().decode())
+
+    def run(self, programs, sum_names):
+        """-> (counts, sums) of the batch, as batch_aggregate's"""
+        q = len(programs)
+        base = programs[0]
+        ptrs = (C.c_void_p * q)(*[C.addressof(p.prog) for p in programs])
+        sc = np.array([base.index(n) if n is not None else -1 for n in sum_names], dtype=np.int32)
+        counts = np.empty(max(q, 1), dtype=np.uint64)
+        sums = np.empty(max(q, 1), dtype=np.float64)
+        _check(N.load_ops().cqlops_batch_persist_run(self.h, ptrs, q, N.ptr(sc), N.ptr(counts), N.ptr(sums)), "cqlops_batch_persist_run")
+        return counts[:q], sums[:q]
+
+    def stats(self):
+        b, l, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        N.load_ops().cqlops_batch_persist_stats(self.h, C.byref(b), C.byref(l), C.byref(c))
+        return {"batches": b.value, "launches": l.value, "compiles": c.value}
+
+    def close(self):
+        if self.h:
+            ok = N.load_ops().cqlops_batch_persist_destroy(self.h)
+            self.h = None
+            return bool(ok)
+        return True
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
     def __del__(self):
         try:
             self.close()

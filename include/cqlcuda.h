@@ -180,6 +180,9 @@ void     cqlcuda_kernel_profile_enable(int enabled);          /* g_gpu_kernel_pr
 void     cqlcuda_kernel_profile_reset(void);                  /* gpu_kernel_profile_reset (gpu.h:61) */
 /* Profile entry i: its kernel name, total GPU nanoseconds and dispatch count. Returns 0 past the end. */
 int      cqlcuda_kernel_profile_entry(uint32_t index, const char** out_name, uint64_t* out_total_ns, uint64_t* out_dispatches);
+/* While the kernel profile is on: batches ended since the last profile reset and their host-side time in
+   nanoseconds - from opening to end, waiting for the device, copying staged results to the callers. */
+void     cqlcuda_host_profile(uint64_t* out_batches, uint64_t* out_open_ns, uint64_t* out_wait_ns, uint64_t* out_copy_ns);
 uint32_t cqlcuda_kernel_launch_count(void);                   /* launches of this library's kernels since init */
 const char* cqlcuda_last_error(void);                         /* text of the last error, "" when none */
 void     cqlcuda_clear_error(void);
@@ -239,6 +242,26 @@ int      cqlcuda_fill_affine_u32(CqlBuffer* buffer, uint64_t rows, uint64_t mul,
    from it run at the link's rate. NULL on failure; free with cqlcuda_host_free. */
 void*    cqlcuda_host_alloc(uint64_t bytes);
 void     cqlcuda_host_free(void* host_ptr);
+/* Page-locked host memory mapped into the device's address space and owned by the buffer (freed with
+   cqlcuda_buffer_release): kernels write answers there that the host reads through *out_host without a copy.
+   Not a source or destination of cqlcuda_buffer_write/read. */
+CqlBuffer* cqlcuda_buffer_alloc_host_mapped(uint64_t size, void** out_host);
+/* Persistent kernels (no reference counterpart; the reference launches every shared scan anew): the entry
+   point `entry` of generated kernel k's module, launched on a stream of its own and left running. It takes
+   its work from device memory that the host fills with cqlcuda_persistent_copy (copies land in the order
+   queued) and returns by itself at its own idle limit; no generated kernel is evicted while one exists.
+   launch: with k's arguments as this thread set them, `ctas` CTAs of k's block size and shared memory (0:
+   as many as are resident at once, less one CTA's room an SM for other kernels),
+   after clearing zero_bytes of `zero` (optional) on the kernel's stream; refused while the kernel runs.
+   running: 1 while it runs, 0 once it has returned, -1 if it returned with an error.
+   copy: the source must stay unchanged until the work it describes is done.
+   destroy: waits at most timeout_ms for the kernel to return; 0 if it still runs (p is kept). */
+typedef struct CqlPersistent CqlPersistent;
+CqlPersistent* cqlcuda_persistent_create(CqlKernel* k, const char* entry);
+int      cqlcuda_persistent_launch(CqlPersistent* p, uint32_t ctas, CqlBuffer* zero, uint64_t zero_bytes);
+int      cqlcuda_persistent_running(CqlPersistent* p);
+int      cqlcuda_persistent_copy(CqlPersistent* p, CqlBuffer* dst, uint64_t offset, const void* src, uint64_t size);
+int      cqlcuda_persistent_destroy(CqlPersistent* p, uint32_t timeout_ms);
 /* Writes `bytes` bytes of a scratch buffer, to evict the L2 between timed runs. */
 int      cqlcuda_flush_l2(uint64_t bytes);
 /* CUDA-event timing of everything the library enqueues between begin and end, on its own stream. */

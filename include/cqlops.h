@@ -446,9 +446,32 @@ int cqlops_batch_cube_source(const CqlProgram* const* programs, uint32_t query_c
                              const int32_t* sum_columns, uint32_t which, char* out, uint64_t cap, uint64_t* out_len, uint32_t* out_cube_queries);
 
 /* The CUDA C++ source cqlops_batch_filter_aggregate would compile for its first launch (no device
-   work), up to cap bytes into out (out_len receives the length). */
+   work), up to cap bytes into out (out_len receives the length). rows_per_thread | CQLOPS_BATCH_PERSISTENT_SOURCE
+   (a register form): the source of the persistent form (cqlops_batch_persist_create) instead. */
+#define CQLOPS_BATCH_PERSISTENT_SOURCE 0x10000u
 int cqlops_batch_source(const CqlProgram* const* programs, uint32_t query_count, const CqlColumn* columns, uint32_t column_count,
                         const int32_t* sum_columns, uint32_t rows_per_thread, char* out, uint64_t cap, uint64_t* out_len, uint32_t* out_shapes);
+
+/* The persistent shared scan: the batched scan for a serving loop over one table, as one long-lived kernel
+   instead of a launch per batch. The kernel (the register form, compiled for every shape of `catalog`)
+   waits on the device for the next batch in a ring of parameter slots in device memory, scans the table
+   for it, adds each CTA's exact integer totals into the slot's accumulators, and the CTA that finishes last
+   writes the answers into page-locked host memory and marks the batch done; the host writes a batch's
+   thresholds and literals with copies and polls its done word. The kernel returns by itself after idle_us
+   microseconds without a batch (0: 2000) and is launched again by the next run; a batch that brings a shape
+   new to the catalog recompiles it. Each wait is bounded: the device's by the idle limit, the host's by 5 s
+   (then the run fails with an error). rows_per_thread: 4, 8 or 16 (the register form's rows per thread,
+   256 threads a CTA). A run takes at most 384 queries of numeric WHERE shapes (no cube answers); its
+   results equal cqlops_batch_filter_aggregate's bit for bit. Runs on one object are serialised. */
+typedef struct CqlBatchPersist CqlBatchPersist;
+CqlBatchPersist* cqlops_batch_persist_create(CqlBatchCatalog* catalog, const CqlColumn* columns, uint32_t column_count,
+                                             uint32_t rows_per_thread, uint32_t idle_us);
+int cqlops_batch_persist_run(CqlBatchPersist* p, const CqlProgram* const* programs, uint32_t query_count, const int32_t* sum_columns,
+                             uint64_t* out_counts, double* out_sums);
+/* batches run, kernel launches (the first and each after an idle return) and compiles so far */
+void cqlops_batch_persist_stats(CqlBatchPersist* p, uint64_t* out_batches, uint64_t* out_launches, uint64_t* out_compiles);
+/* ends the kernel (a stop word in the slot it waits on) and frees everything; 0 if it did not return in 5 s */
+int cqlops_batch_persist_destroy(CqlBatchPersist* p);
 
 /* ---- the resident chunk cache (QE_ResidentCache, src/query_exec/query_exec.c:1679-1970) ----
    Device copies of host column chunks kept between queries, found by (column, write generation, first

@@ -100,3 +100,18 @@ def test_no_cube_for_wide_or_float_columns(ops):
     progs = [ops.Program(w, cols) for w in ("(> v 3.5)", "(< v 1.0)")]
     with pytest.raises(ops.OpError):
         ops.batch_cube_source(progs, [None, None], 0)
+
+
+@pytest.mark.parametrize("rows_per_thread", [4, 8, 16])
+def test_persistent_source_compiles(ops, rows_per_thread):
+    """The persistent form: the scan as a device function adding into accumulators, its one-pass entry and
+    the queue loop, every wait bounded by the idle limit (a time read from the global timer)."""
+    cols = columns(ops)
+    qs = queries(120, 29, 3)
+    progs = [ops.Program(w, cols) for w, _ in qs]
+    src, shapes = ops.batch_source(progs, [s for _, s in qs], rows_per_thread | 0x10000)
+    assert shapes == 29
+    assert "cql_persist(CqlLaunch p)" in src and "cql_main(CqlLaunch a)" in src
+    assert "cql_now() - t0 > idle_ns" in src and "ld.global.cg" in src
+    ok, log = ops.compile_check(src)
+    assert ok, log
