@@ -1363,7 +1363,10 @@ static void staging_finish(CqlStaging& st, int ok)
   st.used = 0;
 }
 
-#define CQL_DIRECT_READ_BYTES (8ull << 20)
+// Reads from this size on go straight to the caller's memory. On GB300 a device-to-host copy into pageable
+// memory runs at 64 GB/s for 1 MB and 154 GB/s for 8 MB (measured), while a read through the staging area
+// also pays a host memcpy of about 14 GB/s.
+#define CQL_DIRECT_READ_BYTES (256ull << 10)
 
 static int enqueue_read(CqlStaging& st, CqlBuffer* b, uint64_t offset, void* out, uint64_t size, cudaStream_t stream, bool allow_direct = true)
 {

@@ -364,14 +364,12 @@ static uint32_t register_ctas_per_sm(uint32_t block)
   return BATCH_CTAS_PER_SM * 256u / block;
 }
 
-/* The persistent form's additions: parameter loads that skip L1 (a slot's parameters are rewritten by
-   copies between the kernel's uses of them, and L1 is not coherent with those copies), and the queue loop. */
+/* The persistent form's additions: the queue loop's helpers. A slot's parameters are rewritten by copies
+   between the kernel's uses of them; every thread passes a gpu-scope acquire fence after its CTA has seen the
+   slot's new sequence number (read with an acquire load), so the scan's ordinary loads that follow do not
+   see lines its SM's L1 kept from the slot's last use. */
 static const char* PERSIST_PRELUDE =
   "__device__ __forceinline__ unsigned long long cql_cg64(const void* p) { unsigned long long v; asm volatile(\"ld.global.cg.u64 %0, [%1];\" : \"=l\"(v) : \"l\"(p)); return v; }\n"
-  "__device__ __forceinline__ u32 cql_cg32(const void* p) { u32 v; asm volatile(\"ld.global.cg.u32 %0, [%1];\" : \"=r\"(v) : \"l\"(p)); return v; }\n"
-  "struct ThrLd { const Thr* p; __device__ __forceinline__ Thr operator[](u32 i) const { const Thr* t = p + i; Thr r;\n"
-  "  r.a = cql_cg64(&t->a); r.b = cql_cg64(&t->b); const u64 cd = cql_cg64(&t->c); r.c = (u32)cd; r.d = (u32)(cd >> 32); r.pad = 0ull; return r; } };\n"
-  "struct QcLd { const double* p; __device__ __forceinline__ double operator[](u32 i) const { return __longlong_as_double((long long)cql_cg64(p + i)); } };\n"
   "__device__ __forceinline__ u64 cql_now() { u64 t; asm volatile(\"mov.u64 %0, %%globaltimer;\" : \"=l\"(t)); return t; }\n"
   "__device__ __forceinline__ u64 cql_acquire64(const void* p) { u64 v; asm volatile(\"ld.acquire.gpu.global.u64 %0, [%1];\" : \"=l\"(v) : \"l\"(p) : \"memory\"); return v; }\n"
   "__device__ __forceinline__ void cql_release_sys64(void* p, u64 v) { asm volatile(\"st.release.sys.global.u64 [%0], %1;\" :: \"l\"(p), \"l\"(v) : \"memory\"); }\n";
@@ -421,6 +419,7 @@ static const char* PERSIST_ENTRY =
   "    }\n"
   "    __syncthreads();\n"
   "    if (!s_go) return;\n"
+  "    asm volatile(\"fence.acq_rel.gpu;\" ::: \"memory\");\n"
   "    cql_scan(s_a, blockIdx.x, gridDim.x);\n"
   "    __syncthreads();\n"
   "    if (threadIdx.x == 0) { __threadfence(); s_last = atomicAdd((u32*)p.buf[3] + slot, 1u) == gridDim.x - 1u; }\n"
@@ -452,11 +451,9 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
   if (persistent) bput(&b, "#define CQL_BLOCK %u\n%s", block, PERSIST_PRELUDE);
   for (uint32_t s = 0; s < shapes; s++) bput(&b, "#define CQL_SHAPE_%u(k) (%s)\n", s, shape_exprs[s]);
   if (persistent)
-    bput(&b, "__device__ __forceinline__ void cql_scan(const CqlLaunch& a, const u32 cta, const u32 ctas)\n{\n"
-             "#define CQL_LD32(p) cql_cg32(p)\n#define CQL_LDF(p) __longlong_as_double((long long)cql_cg64(p))\n#define CQL_LDI(p) ((long long)cql_cg64(p))\n");
+    bput(&b, "__device__ __forceinline__ void cql_scan(const CqlLaunch& a, const u32 cta, const u32 ctas)\n{\n");
   else
-    bput(&b, "extern \"C\" __global__ void __launch_bounds__(%u) cql_main(CqlLaunch a)\n{\n  const u32 cta = blockIdx.x, ctas = gridDim.x;\n"
-             "#define CQL_LD32(p) (*(p))\n#define CQL_LDF(p) (*(p))\n#define CQL_LDI(p) (*(p))\n", block);
+    bput(&b, "extern \"C\" __global__ void __launch_bounds__(%u) cql_main(CqlLaunch a)\n{\n  const u32 cta = blockIdx.x, ctas = gridDim.x;\n", block);
   bput(&b,
        "  const u64 rows = cql_word(a, 0); const u32 nq = cql_word(a, 2); const u32 q0 = cql_word(a, 4);\n"
        "  const u32 need = cql_word(a, 6), need_sum = cql_word(a, 7);   /* the columns this launch reads and sums */\n"
@@ -519,7 +516,7 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
     else if (t == CQLOPS_TYPE_I64) snprintf(expr, sizeof(expr), "__double2ll_rn(cql_i64d(r%d[v]) * sc)", c);
     else snprintf(expr, sizeof(expr), "(sh >= 0 ? (long long)((u64)r%d[v] << sh) : __double2ll_rn((double)r%d[v] * sc))", c, c);
     bput(&b, "    long long fx%d[%u];\n    if (!((need_sum >> %d) & 1u)) { for (u32 v = 0; v < RPT; v++) fx%d[v] = 0ll; }\n", c, rows_per_thread, c, c);
-    bput(&b, "    else { const double sc = CQL_LDF(col_scale + %d); const int sh = (int)CQL_LDI(col_shift + %d); (void)sh; (void)sc;\n", c, c);
+    bput(&b, "    else { const double sc = col_scale[%d]; const int sh = (int)col_shift[%d]; (void)sh; (void)sc;\n", c, c);
     bput(&b, "      for (u32 v = 0; v < RPT; v++) fx%d[v] = v < valid ? %s : 0ll; }\n", c, expr);
   }
   for (uint32_t s = 0; s < shapes; s++)
@@ -531,8 +528,8 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
     for (uint32_t i = 0; i < shape_sites[s] && i < BATCH_MAX_SITES; i++)
       dn += (size_t)snprintf(decls + dn, sizeof(decls) - dn, "      const Thr T%u = TH[%u];\n", i, i);
     bput(&b,
-         "    for (u32 q = CQL_LD32(shape_begin + %u); q < CQL_LD32(shape_begin + %u); q++)\n    {\n"
-         "      const %s TH%s thr + (u64)(q0 + q) * %uu%s; const %s QC%s qconst + (u64)(q0 + q) * %uu%s;\n"
+         "    for (u32 q = shape_begin[%u]; q < shape_begin[%u]; q++)\n    {\n"
+         "      const Thr* TH = thr + (u64)(q0 + q) * %uu; const double* QC = qconst + (u64)(q0 + q) * %uu;\n"
          "      (void)TH; (void)QC;\n"
          "%s"
          "      u32 m = 0u;\n"
@@ -540,10 +537,9 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
          "      for (u32 k = 0; k < RPT; k++) m |= ((CQL_SHAPE_%u(k)) ? 1u : 0u) << k;\n"
          "      m &= valid_mask;\n"
          "      const u32 cnt = __reduce_add_sync(0xffffffffu, (u32)__popc(m));\n"
-         "      const u32 sc = CQL_LD32(qsum + q0 + q);\n"
+         "      const u32 sc = qsum[q0 + q];\n"
          "      long long sv = 0ll;\n",
-         s, s + 1, persistent ? "ThrLd" : "Thr*", persistent ? "{" : " =", BATCH_MAX_SITES, persistent ? "}" : "",
-         persistent ? "QcLd" : "double*", persistent ? "{" : " =", BATCH_MAX_CONSTS, persistent ? "}" : "", decls, s);
+         s, s + 1, BATCH_MAX_SITES, BATCH_MAX_CONSTS, decls, s);
     for (uint32_t i = 0; i < sum_col_count; i++)
       bput(&b, "      if (sc == %du && m) {\n#pragma unroll\n        for (u32 k = 0; k < RPT; k++) if ((m >> k) & 1u) sv += fx%d[k];\n      }\n", sum_cols[i],
            sum_cols[i]);
@@ -561,7 +557,7 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
        "      u64 l2 = lo + (u64)v; hi += (u64)(v < 0 ? -1ll : 0ll) + (l2 < lo ? 1ull : 0ull); lo = l2; }\n"
        "%s"
        "  }\n"
-       "#undef CQL_LD32\n#undef CQL_LDF\n#undef CQL_LDI\n}\n",
+       "}\n",
        persistent ? /* the CTA's 128-bit totals added into the accumulators: the low words with a carry into the high */
                     "    if (q < pcap && (c | lo | hi)) { if (c) atomicAdd(&partials[q * 3], c); const u64 old = atomicAdd(&partials[q * 3 + 1], lo);\n"
                     "      const u64 up = hi + ((old + lo < old) ? 1ull : 0ull); if (up) atomicAdd(&partials[q * 3 + 2], up); }\n"

@@ -214,13 +214,52 @@ def run_batch(rows, reps):
         if best is None or wall < best[1]:
             best = (rpt, wall, kernel_ms, kernels)
     one_wall, one_kernel, _ = _time(lambda: [ops.fused_aggregate(p, [s]) for p, s in zip(progs, sums)], max(1, reps // 2))
+    # the autotuner: its trial runs (one per candidate form) first, then its pick
+    auto = ops.CQLOPS_BATCH_AUTOTUNE
+    for _ in range(8):
+        ops.batch_aggregate(progs, sums, auto)
+    auto_wall, auto_kernel, _ = _time(lambda: ops.batch_aggregate(progs, sums, auto), reps)
+    auto_form = native.load_ops().cqlops_batch_last_form()
+    persistent = _persistent_ab(progs, sums, best[0] if best[0] else 8, reps)
     graphs = _graph_ab(reps)
     nbytes = rows * (4 * 4 + 4 * 8)
     return {"op": "batch", "rows": rows, "queries": len(qs), "shapes": 29, "reps": reps, "rows_per_thread": best[0], "tuning_wall_ms": tuning,
             "wall_ms": best[1], "kernel_ms": best[2], "rows_per_s": len(qs) * rows / (best[1] / 1e3),
             "kernel_GBps": nbytes / (best[2] / 1e3) / 1e9, "bytes": nbytes, "kernels": best[3],
             "one_at_a_time_wall_ms": one_wall, "one_at_a_time_kernel_ms": one_kernel, "speedup_wall": one_wall / best[1],
-            "plan_graphs": graphs}
+            "autotuned_wall_ms": auto_wall, "autotuned_kernel_ms": auto_kernel,
+            "autotuned_form": {"rows_per_thread": auto_form & 0xff, "block": 256 * max(1, (auto_form >> 8) & 0xff)} if auto_form & 0xff
+            else {"form": "tile"}, "persistent": persistent, "plan_graphs": graphs}
+
+
+def _persistent_ab(progs, sums, rows_per_thread, reps):
+    """The 512 queries as a catalog batch launched (two launches: 384 + 128 queries) and through the persistent
+    scan (two runs), wall time; the launched ones first - an allocation elsewhere waits for a running
+    persistent kernel."""
+    cat = ops.BatchCatalog()
+    halves = [(progs[:384], sums[:384]), (progs[384:], sums[384:])]
+    for p, s in halves:
+        cat.aggregate(p, s, rows_per_thread)
+    walls = []
+    want = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        want = [cat.aggregate(p, s, rows_per_thread)[:2] for p, s in halves]
+        walls.append((time.perf_counter() - t0) * 1e3)
+    with ops.PersistentScan(cat, progs, rows_per_thread=rows_per_thread, idle_us=500_000) as ps:
+        for p, s in halves:
+            ps.run(p, s)
+        pwalls = []
+        same = True
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            got = [ps.run(p, s) for p, s in halves]
+            pwalls.append((time.perf_counter() - t0) * 1e3)
+            same = same and all(np.array_equal(g[0], w[0]) and np.array_equal(g[1].view(np.uint64), w[1].view(np.uint64))
+                                for g, w in zip(got, want))
+        st = ps.stats()
+    return {"rows_per_thread": rows_per_thread, "launched_wall_ms": statistics.median(walls), "persistent_wall_ms": statistics.median(pwalls),
+            "identical": bool(same), **st}
 
 
 def _graph_ab(reps):

@@ -68,6 +68,9 @@ class DeviceBuffer:
             pass
 
 
+CQLOPS_BATCH_AUTOTUNE = 0xFFFFFFFF   # rows_per_thread: the form picked per plan shape by timed trials (include/cqlops.h)
+
+
 class Column:
     """A device-resident column: its buffer, CQL type, encoding and zone range."""
 

@@ -112,6 +112,6 @@ def test_persistent_source_compiles(ops, rows_per_thread):
     src, shapes = ops.batch_source(progs, [s for _, s in qs], rows_per_thread | 0x10000)
     assert shapes == 29
     assert "cql_persist(CqlLaunch p)" in src and "cql_main(CqlLaunch a)" in src
-    assert "cql_now() - t0 > idle_ns" in src and "ld.global.cg" in src
+    assert "cql_now() - t0 > idle_ns" in src and "fence.acq_rel.gpu" in src
     ok, log = ops.compile_check(src)
     assert ok, log

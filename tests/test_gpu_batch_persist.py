@@ -35,18 +35,20 @@ def batch(ops, cols, gens, seed, count):
 
 
 def test_persistent_batches_equal_launched_batches(env):
+    """The launched batches run first: a device allocation or free elsewhere in the process waits for a
+    running persistent kernel (until its idle limit), so the two are not interleaved here."""
     ops, arrays, cols = env
     gens = shapes(12, 77)
     cat = ops.BatchCatalog()
     progs, sums, qs = batch(ops, cols, gens, 1, 96)
     cat.aggregate(progs, sums)                     # every shape in the catalog
+    batches = [batch(ops, cols, gens, seed, 40 + 13 * seed) for seed in range(2, 14)]
+    want = [cat.aggregate(p, s)[:2] for p, s, _ in batches]
     with ops.PersistentScan(cat, progs, rows_per_thread=8, idle_us=200_000) as ps:
-        for seed in range(2, 14):                  # 12 batches: the 4-slot ring wraps three times
-            progs, sums, qs = batch(ops, cols, gens, seed, 40 + 13 * seed)
+        for (progs, sums, qs), (want_c, want_s) in zip(batches, want):   # 12 batches: the 4-slot ring wraps three times
             got_c, got_s = ps.run(progs, sums)
-            want_c, want_s, _ = cat.aggregate(progs, sums)
-            assert np.array_equal(got_c, want_c), seed
-            assert np.array_equal(got_s.view(np.uint64), want_s.view(np.uint64)), seed
+            assert np.array_equal(got_c, want_c), qs[0][0]
+            assert np.array_equal(got_s.view(np.uint64), want_s.view(np.uint64)), qs[0][0]
             for i in (0, len(qs) // 2, len(qs) - 1):
                 assert got_c[i] == oracle_mask(progs[i], arrays).sum(), qs[i][0]
         st = ps.stats()
