@@ -445,37 +445,65 @@ __global__ void __launch_bounds__(JOIN_THREADS, 3) k_join_probe_native(CqlLaunch
 }
 
 // ---------------------------------------------------------------------------------------------
-// join_probe_native over a small build side: the table (keys and rows) and the Bloom words are staged
-// into shared memory once per CTA by bulk copies (cp.async.bulk, completion counted on an mbarrier), and
-// the per-dim-row totals are kept per table slot in shared memory, flushed to the dim-row arrays once per
-// CTA. Binding 12 is an error word (bit 0: the staging did not complete within a second; the CTA then
-// waits, again bounded, for its copies and returns without probing). Taken when the error word is bound
-// and the shared arrays fit JOIN_SMEM_MAX_BYTES; the same results as k_join_probe_native.
+// join_probe_native over a small build side: the per-dim-row totals are kept per table slot in shared
+// memory and flushed to the dim-row arrays once per CTA, instead of a global atomic per matched row. With
+// TSMEM the table (keys and rows) and the Bloom words are staged into shared memory too, once per CTA, by
+// bulk copies (cp.async.bulk, completion counted on an mbarrier); without it (a table too large to stage
+// beside the totals) they are read from global memory, where they stay in L2. The shared arrays hold only
+// what the aggregates need: a count per slot, a 64-bit sum (two 32-bit halves) per SUM/AVG, an extremum
+// per MIN or MAX. Binding 12 is an error word (bit 0: the staging did not complete within a second; the CTA
+// then waits, again bounded, for its copies and returns without probing). Taken when the error word is
+// bound and the shared arrays fit; the same results as k_join_probe_native.
 
 #define JOIN_SMEM_THREADS 512
-#define JOIN_SMEM_MAX_BYTES (100u * 1024u)
+#define JOIN_SMEM_TWO_CTAS (100u * 1024u)    // two CTAs an SM up to this size, one beyond it
+#define JOIN_SMEM_MAX_BYTES (200u * 1024u)
 #define JOIN_WAIT_NS 1000000000ull
 
 struct JoinSmemLayout
 {
-  uint32_t size, bloom_words, exprs;
-  uint32_t keys, trows, bloom, cnt, sums, mins, maxs, total;   // byte offsets in dynamic shared memory
+  uint32_t size, bloom_words, exprs, staged;
+  uint32_t nsum, nmin, nmax;
+  uint32_t slot_of;                               // per expression (4 bits each): its index among its kind
+  uint32_t keys, trows, bloom, cnt, lo, hi, mins, maxs, total;   // byte offsets in dynamic shared memory
 };
 
-__host__ __device__ inline JoinSmemLayout join_smem_layout(uint32_t size, uint32_t bloom_words, uint32_t exprs)
+__host__ __device__ inline JoinSmemLayout join_smem_layout(uint32_t size, uint32_t bloom_words, uint32_t exprs, uint32_t funcs,
+                                                           bool staged)
 {
   JoinSmemLayout l;
   l.size = size;
   l.bloom_words = bloom_words;
   l.exprs = exprs;
-  l.keys = 16;                                  // the mbarrier sits in the first 8 bytes
-  l.trows = l.keys + 4 * size;
-  l.bloom = l.trows + 4 * size;
-  l.cnt = l.bloom + 4 * bloom_words;
-  l.sums = (l.cnt + 4 * size + 7u) & ~7u;
-  l.mins = l.sums + 8 * size * exprs;
-  l.maxs = l.mins + 4 * size * exprs;
-  l.total = l.maxs + 4 * size * exprs;
+  l.staged = staged ? 1u : 0u;
+  l.nsum = l.nmin = l.nmax = 0;
+  l.slot_of = 0;
+  for (uint32_t e = 0; e < exprs; e++)
+  {
+    uint32_t f = (funcs >> (4 * e)) & 0xfu, k = 0;
+    if (f == 1u || f == 2u) k = l.nsum++;          // SUM, AVG
+    else if (f == 3u) k = l.nmin++;               // MIN
+    else if (f == 4u) k = l.nmax++;               // MAX
+    l.slot_of |= k << (4 * e);
+  }
+  uint32_t off = 16;                              // the mbarrier sits in the first 8 bytes
+  l.keys = off;
+  if (staged) off += 4 * size;
+  l.trows = off;
+  if (staged) off += 4 * size;
+  l.bloom = off;
+  if (staged) off += 4 * bloom_words;
+  l.cnt = off;
+  off += 4 * size;
+  l.lo = off;
+  off += 4 * size * l.nsum;
+  l.hi = off;
+  off += 4 * size * l.nsum;
+  l.mins = off;
+  off += 4 * size * l.nmin;
+  l.maxs = off;
+  off += 4 * size * l.nmax;
+  l.total = off;
   return l;
 }
 
@@ -500,7 +528,7 @@ __device__ __forceinline__ int join_mbar_wait(uint32_t bar)
   }
 }
 
-template <bool PLAIN>
+template <bool PLAIN, bool TSMEM>
 __global__ void __launch_bounds__(JOIN_SMEM_THREADS, 2) k_join_probe_native_smem(CqlLaunch a, uint64_t rows, JoinSmemLayout L)
 {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -528,20 +556,20 @@ __global__ void __launch_bounds__(JOIN_SMEM_THREADS, 2) k_join_probe_native_smem
   for (uint32_t e = 0; e < exprs; e++)
     if (((funcs >> (e * 4)) & 0xfu) != JFUNC_COUNT) used_args |= 1u << ((arg_index >> (e * 4)) & 0x3u);
   const uint64_t count_cap = a.bytes[7] / 4;
-  uint32_t* s_keys = (uint32_t*)(smem + L.keys);
-  uint32_t* s_rows = (uint32_t*)(smem + L.trows);
-  uint32_t* s_bloom = (uint32_t*)(smem + L.bloom);
+  const uint32_t* s_keys = TSMEM ? (const uint32_t*)(smem + L.keys) : (const uint32_t*)a.buf[5];
+  const uint32_t* s_rows = TSMEM ? (const uint32_t*)(smem + L.trows) : (const uint32_t*)a.buf[6];
+  const uint32_t* s_bloom = TSMEM ? (const uint32_t*)(smem + L.bloom) : (const uint32_t*)a.buf[11];
   uint32_t* s_cnt = (uint32_t*)(smem + L.cnt);
   // 64-bit sums as two 32-bit halves: a 32-bit shared atomic add, and a carry into the high half when the
   // low half wraps (or the value is negative), instead of a 64-bit shared atomic
-  uint32_t* s_lo = (uint32_t*)(smem + L.sums);
-  uint32_t* s_hi = s_lo + L.size * L.exprs;
+  uint32_t* s_lo = (uint32_t*)(smem + L.lo);
+  uint32_t* s_hi = (uint32_t*)(smem + L.hi);
   int* s_mins = (int*)(smem + L.mins);
   int* s_maxs = (int*)(smem + L.maxs);
   const uint32_t bar = (uint32_t)__cvta_generic_to_shared(smem);
 
   // stage the table and the Bloom words: one thread arms the barrier with the bytes and issues the copies
-  if (threadIdx.x == 0)
+  if (TSMEM && threadIdx.x == 0)
   {
     uint32_t table_bytes = 4u * L.size, bloom_bytes = 4u * L.bloom_words;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar) : "memory");
@@ -554,17 +582,17 @@ __global__ void __launch_bounds__(JOIN_SMEM_THREADS, 2) k_join_probe_native_smem
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                  :: "r"(bar + L.bloom), "l"(a.buf[11]), "r"(bloom_bytes), "r"(bar) : "memory");
   }
-  // the accumulators start empty while the copies fly
+  // the totals start empty while the copies fly
   for (uint32_t i = threadIdx.x; i < L.size; i += blockDim.x) s_cnt[i] = 0u;
-  for (uint32_t i = threadIdx.x; i < L.size * exprs; i += blockDim.x)
+  for (uint32_t i = threadIdx.x; i < L.size * L.nsum; i += blockDim.x)
   {
     s_lo[i] = 0u;
     s_hi[i] = 0u;
-    s_mins[i] = 0x7fffffff;
-    s_maxs[i] = (int)0x80000000;
   }
+  for (uint32_t i = threadIdx.x; i < L.size * L.nmin; i += blockDim.x) s_mins[i] = 0x7fffffff;
+  for (uint32_t i = threadIdx.x; i < L.size * L.nmax; i += blockDim.x) s_maxs[i] = (int)0x80000000;
   __syncthreads();
-  if (!join_mbar_wait(bar))
+  if (TSMEM && !join_mbar_wait(bar))
   {
     if (threadIdx.x == 0) atomicOr(error, 1u);
     join_mbar_wait(bar);      // the copies in flight land before the CTA leaves
@@ -592,7 +620,7 @@ __global__ void __launch_bounds__(JOIN_SMEM_THREADS, 2) k_join_probe_native_smem
       maybe[u] = at < rows && (s_bloom[h >> (32u - bloom_log2)] & bits) == bits;
     }
     // the argument words of every candidate row are loaded before the probes: their loads are in flight
-    // together, and the probes and totals that follow touch shared memory only
+    // together, and the probes and totals that follow touch shared memory (or L2) only
     uint32_t argv[UNROLL][4];
 #pragma unroll
     for (uint32_t u = 0; u < UNROLL; u++)
@@ -623,7 +651,7 @@ __global__ void __launch_bounds__(JOIN_SMEM_THREADS, 2) k_join_probe_native_smem
         if (f == JFUNC_COUNT) continue;
         uint32_t ai = (arg_index >> (e * 4)) & 0x3u;
         uint32_t w = ai == 0u ? argv[u][0] : ai == 1u ? argv[u][1] : ai == 2u ? argv[u][2] : argv[u][3];
-        uint32_t index = slot * exprs + e;
+        uint32_t index = ((L.slot_of >> (4 * e)) & 0xfu) * L.size + slot;
         if (f == JFUNC_SUM || f == JFUNC_AVG)
         {
           bool sg = ((arg_signed >> ai) & 1u) != 0;
@@ -649,7 +677,7 @@ __global__ void __launch_bounds__(JOIN_SMEM_THREADS, 2) k_join_probe_native_smem
     {
       uint32_t f = (funcs >> (e * 4)) & 0xfu;
       uint64_t index = (uint64_t)dim_row * exprs + e;
-      uint32_t si = slot * exprs + e;
+      uint32_t si = ((L.slot_of >> (4 * e)) & 0xfu) * L.size + slot;
       if (f == JFUNC_SUM || f == JFUNC_AVG) atomicAdd(&sums[index], ((unsigned long long)s_hi[si] << 32) | s_lo[si]);
       else if (f == JFUNC_MIN) atomicMin(&mins[index], s_mins[si]);
       else if (f == JFUNC_MAX) atomicMax(&maxs[index], s_maxs[si]);
@@ -666,32 +694,43 @@ static int launch_join_probe_native(const CqlLaunch& a, uint32_t gws, uint32_t l
   if (rows == 0) return 0;
   if (log2_size == 0 || log2_size > 31 || bloom_log2 == 0 || bloom_log2 > 31) return (int)cudaErrorInvalidValue;
   if ((uint64_t)(cql_word(a, 8)) + 1 != (1ull << log2_size)) return (int)cudaErrorInvalidValue;
-  // a small build side: shared-memory table when the error word is bound, the arrays fit and the bulk
-  // copies' sources and sizes are 16-byte multiples (tables of at least 16 slots and 16 Bloom words)
+  // a small build side: the totals per slot in shared memory, and the table with them when it fits (the bulk
+  // copies' sources and sizes are 16-byte multiples: tables of at least 16 slots and 16 Bloom words)
   uint32_t exprs = min(cql_word(a, 2), 8u);
   if (log2_size >= 4 && log2_size <= 16 && bloom_log2 >= 4 && bloom_log2 <= 16 && a.buf[12] && a.bytes[12] >= 4 &&
       ((uintptr_t)a.buf[5] & 15u) == 0 && ((uintptr_t)a.buf[6] & 15u) == 0 && ((uintptr_t)a.buf[11] & 15u) == 0 &&
       a.bytes[5] >= (4ull << log2_size) && a.bytes[6] >= (4ull << log2_size) && a.bytes[11] >= (4ull << bloom_log2))
   {
-    JoinSmemLayout L = join_smem_layout(1u << log2_size, 1u << bloom_log2, exprs);
-    if (L.total <= JOIN_SMEM_MAX_BYTES)
+    uint32_t funcs = cql_word(a, 4);
+    JoinSmemLayout L = join_smem_layout(1u << log2_size, 1u << bloom_log2, exprs, funcs, true);
+    if (L.total > JOIN_SMEM_MAX_BYTES) L = join_smem_layout(1u << log2_size, 1u << bloom_log2, exprs, funcs, false);
+    if (L.total <= JOIN_SMEM_MAX_BYTES && L.total <= (uint32_t)g_cql_max_smem_optin)
     {
       static bool attr_set = false;
       if (!attr_set)
       {
-        if (cudaFuncSetAttribute(k_join_probe_native_smem<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)JOIN_SMEM_MAX_BYTES) !=
-                cudaSuccess ||
-            cudaFuncSetAttribute(k_join_probe_native_smem<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)JOIN_SMEM_MAX_BYTES) !=
-                cudaSuccess)
-          return (int)cudaGetLastError();
+        const void* fns[4] = { (const void*)k_join_probe_native_smem<true, true>, (const void*)k_join_probe_native_smem<false, true>,
+                               (const void*)k_join_probe_native_smem<true, false>, (const void*)k_join_probe_native_smem<false, false> };
+        for (const void* fn : fns)
+          if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<uint32_t>(JOIN_SMEM_MAX_BYTES, (uint32_t)g_cql_max_smem_optin)) !=
+              cudaSuccess)
+            return (int)cudaGetLastError();
         attr_set = true;
       }
       bool plain = (cql_word(a, 1) & 0xfffffu) == 0u;   // key and every argument at full width
-      // two CTAs an SM where their shared arrays fit (the register budget is set for two)
-      int per_sm = (int)std::max<uint32_t>(1u, std::min<uint32_t>(2u, (uint32_t)(g_cql_max_smem_optin / (L.total + 1024u))));
+      // two CTAs an SM where their shared arrays fit (the register budget is set for two), else one
+      int per_sm = L.total <= JOIN_SMEM_TWO_CTAS ? 2 : 1;
       dim3 grid(cql_stream_grid((rows + JOIN_SMEM_THREADS * 8 - 1) / (JOIN_SMEM_THREADS * 8), per_sm));
-      if (plain) k_join_probe_native_smem<true><<<grid, JOIN_SMEM_THREADS, L.total, stream>>>(a, rows, L);
-      else k_join_probe_native_smem<false><<<grid, JOIN_SMEM_THREADS, L.total, stream>>>(a, rows, L);
+      if (L.staged)
+      {
+        if (plain) k_join_probe_native_smem<true, true><<<grid, JOIN_SMEM_THREADS, L.total, stream>>>(a, rows, L);
+        else k_join_probe_native_smem<false, true><<<grid, JOIN_SMEM_THREADS, L.total, stream>>>(a, rows, L);
+      }
+      else
+      {
+        if (plain) k_join_probe_native_smem<true, false><<<grid, JOIN_SMEM_THREADS, L.total, stream>>>(a, rows, L);
+        else k_join_probe_native_smem<false, false><<<grid, JOIN_SMEM_THREADS, L.total, stream>>>(a, rows, L);
+      }
       CQL_LAUNCH_CHECK();
       return 0;
     }

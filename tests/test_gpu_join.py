@@ -225,10 +225,12 @@ def test_lookup_table_gives_way_to_repeated_dim_keys(ops):
 
 
 @pytest.mark.parametrize("dim, funcs", [(50, "sum_min_max"), (1000, "count_sum"), (1000, "sum_min_max"), (3000, "count_sum"),
-                                        (16, "count_sum")])
+                                        (16, "count_sum"), (4096, "count_sum"), (4096, "sum_min_max"), (8000, "count_sum"),
+                                        (40000, "count_sum")])
 def test_small_build_side_probe(ops, dim, funcs):
     """The probe (strategy 2) with a small dim table: tables that fit take the shared-memory form (the table
-    and Bloom words staged by bulk copies, per-slot totals in shared memory), larger ones the global form;
+    and Bloom words staged by bulk copies, per-slot totals in shared memory), tables up to 16384 slots whose
+    totals alone fit keep the totals there and read the table from L2, larger ones the global form;
     per dim row COUNT/SUM/MIN/MAX equal numpy's over the fact rows whose key is that row's key, with misses,
     a dim-side filter and signed arguments."""
     rng = np.random.default_rng(100 + dim)
