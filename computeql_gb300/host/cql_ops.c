@@ -501,6 +501,8 @@ typedef struct
   uint64_t sum_at, min_at, max_at;
   uint64_t group_count;
   int64_t min_key;
+  int keep_open;      /* in: leave the batch open for the caller's next operations */
+  CqlBatch* batch;    /* out (keep_open): that batch, which the caller ends */
 } CqlDenseTotals;
 
 static int group_dense_run(const CqlColumn* key, uint64_t rows, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* arg_cols,
@@ -664,8 +666,11 @@ static int group_dense_run(const CqlColumn* key, uint64_t rows, uint32_t expr_co
     cqlcuda_batch_kernel_execute(batch, k, (uint32_t)(workgroups * QE_GPU_WORKGROUP_SIZE), QE_GPU_WORKGROUP_SIZE);
     if (device_out)
     {
-      /* the totals stay on the device for the caller's next batch */
-      ok = cqlcuda_batch_end(batch);
+      /* the totals stay on the device for the caller's next operations: in this batch, left open (no wait
+         between the two), or in a batch of its own */
+      device_out->batch = NULL;
+      if (device_out->keep_open) device_out->batch = batch;
+      else ok = cqlcuda_batch_end(batch);
       free(host_out);
       if (!ok) return 0;
       device_out->buffer = out_buf;

@@ -945,6 +945,8 @@ typedef struct
   uint64_t sum_at, min_at, max_at;
   uint64_t group_count;
   int64_t min_key;
+  int keep_open;      /* in: leave the batch open for the caller's next operations */
+  CqlBatch* batch;    /* out (keep_open): that batch, which the caller ends */
 } CqlDenseTotals;
 
 int cql_group_dense_device(const CqlColumn* key, uint64_t rows, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* arg_cols,
@@ -987,6 +989,8 @@ static int join_device_pass(const CqlJoinAgg* q, uint32_t core_count, const uint
   uint64_t visits = q->dim_rows ? q->dim_count : q->dim_table_rows;
   if (visits > 0xffffffffull) return -1;
   CqlDenseTotals t;
+  memset(&t, 0, sizeof(t));
+  t.keep_open = 1;   /* the dense pass and the dim-row pass in one batch: one wait */
   uint64_t groups_cap = (uint64_t)(fk->zone_max - fk->zone_min) + 1;
   if (!cql_group_dense_device(fk, fk->rows, core_count, core_funcs, core_cols, groups_cap, &t)) return 0;
   uint64_t E = core_count;
@@ -1028,7 +1032,8 @@ static int join_device_pass(const CqlJoinAgg* q, uint32_t core_count, const uint
     cqlcuda_kernel_set_arg_u64(k, 5, (uint32_t)group_min);
     cqlcuda_kernel_set_arg_u64(k, 6, slots);
     cqlcuda_kernel_set_arg_u64(k, 7, (dg ? 1u : 0u) | (want_mm ? 2u : 0u));
-    CqlBatch* b = cqlcuda_batch_begin(vl ? visits * 4 : 0, bytes);
+    CqlBatch* b = t.batch;
+    t.batch = NULL;
     if (vl) cqlcuda_batch_buffer_write(b, vb, vl, visits * 4);
     cqlcuda_batch_buffer_zero(b, out, mins_at);
     cqlcuda_batch_fill_range(b, out, mins_at, slots * E * 4, 0x7fffffffu);
@@ -1038,6 +1043,7 @@ static int join_device_pass(const CqlJoinAgg* q, uint32_t core_count, const uint
     cqlcuda_batch_buffer_read(b, out, host, bytes);
     ok = cqlcuda_batch_end(b);
   }
+  if (t.batch) cqlcuda_batch_end(t.batch);   /* a refusal above: the dense pass's batch still ends */
   if (ok)
   {
     const uint64_t* counts = (const uint64_t*)(host + counts_at);
