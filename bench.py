@@ -336,6 +336,7 @@ def main():
     ap.add_argument("--cpu-rows", type=int, default=CPU_SAMPLE_ROWS)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the batched and served configurations' figures")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -465,6 +466,11 @@ def main():
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(args.cpu_rows, single_core_rows=args.cpu_rows // 10)
 
+    batched = served = None
+    if rank == 0 and not args.no_extra and world == 1:
+        batched = run_batched(native, ops, lib)
+        served = run_served(ops, workloads, t, dims)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
@@ -476,11 +482,90 @@ def main():
                 "value_without_point_lookup": value_without_lookup,
                 "parity": parity, "parity_checks": parity_checks_run,
                 "gpu_launches": launches, "queries": qstats, "kernels": kernels, "roofline": roofline, "clocks": clk,
-                "e2e": e2e, "cpu_baseline": cpu}
+                "e2e": e2e, "cpu_baseline": cpu, "batched": batched, "served": served}
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def run_batched(native, ops, lib):
+    """The batched configuration, outside the suite's timed region: 100M rows of 4 u32 (uniform [0, 2^16)) and
+    4 f64 (uniform [0, 1)) columns, 512 COUNT + SUM queries over 29 WHERE shapes drawn like the reference's
+    per-query kernel benchmark. Wall times of one shared scan picked by the autotuner, of the queries one at a
+    time through their own generated kernels, and of the persistent scan; the three paths' answers compared."""
+    import numpy as np
+    from computeql_gb300 import opbench
+    rows = 100_000_000
+    rng = np.random.default_rng(4)
+    cols = {f"u{i}": ops.Column.splitmix(rows, 4, 8, i, 1 << 16) for i in range(4)}
+    cols.update({f"d{i}": ops.Column.from_numpy(rng.random(rows)) for i in range(4)})
+    qs = opbench._batch_queries(512, 29, 9)
+    progs = [ops.Program(w, cols) for w, _ in qs]
+    sums = [s for _, s in qs]
+    auto = ops.CQLOPS_BATCH_AUTOTUNE
+    for _ in range(8):                      # the autotuner's trial runs, one per candidate form, then its pick
+        ops.batch_aggregate(progs, sums, auto)
+
+    def timed(fn, reps):
+        walls, out = [], None
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            out = fn()
+            walls.append((time.perf_counter() - t0) * 1e3)
+        return statistics.median(walls), out
+    auto_ms, (c_auto, s_auto, _) = timed(lambda: ops.batch_aggregate(progs, sums, auto), 3)
+    form = native.load_ops().cqlops_batch_last_form()
+    one_ms, one = timed(lambda: [ops.fused_aggregate(p, [s]) for p, s in zip(progs, sums)], 1)
+    c_one = np.array([r[0] for r in one], dtype=np.uint64)
+    s_one = np.array([r[1][0] for r in one], dtype=np.float64)
+    cat = ops.BatchCatalog()
+    halves = [(progs[:384], sums[:384]), (progs[384:], sums[384:])]
+    for p_, s_ in halves:
+        cat.aggregate(p_, s_, 8)
+    with ops.PersistentScan(cat, progs, rows_per_thread=8, idle_us=500_000) as ps:
+        for p_, s_ in halves:
+            ps.run(p_, s_)
+        pers_ms, got = timed(lambda: [ps.run(p_, s_) for p_, s_ in halves], 3)
+    c_pers = np.concatenate([g[0] for g in got])
+    s_pers = np.concatenate([g[1] for g in got])
+    rel = np.abs(s_auto - s_one) / np.maximum(np.abs(s_one), 1e-300)
+    for c in cols.values():
+        c.buffer.close()
+    return {"workload": "100M rows x (4 u32 + 4 f64), 512 COUNT + SUM queries over 29 WHERE shapes", "unit": "ms per batch of 512",
+            "shared_scan_autotuned_ms": auto_ms, "autotuned_form": {"rows_per_thread": form & 0xff, "block": 256 * max(1, (form >> 8) & 0xff)}
+            if form & 0xff else {"form": "tile"},
+            "one_at_a_time_ms": one_ms, "persistent_ms": pers_ms, "speedup_vs_one_at_a_time": one_ms / auto_ms,
+            "parity": "ok" if (np.array_equal(c_auto, c_one) and np.array_equal(c_auto, c_pers) and float(rel.max()) <= 1e-12
+                               and np.array_equal(s_auto.view(np.uint64), s_pers.view(np.uint64))) else "failed",
+            "parity_checks": "counts equal across the three paths; shared-scan sums within 1e-12 of the per-query kernels' and equal "
+                             "to the persistent scan's bit for bit"}
+
+
+def run_served(ops, workloads, t, dims):
+    """The served configuration's mix (computeql_gb300/servebench.py) over resident tables of 1M and 100M rows
+    and the suite's own 1B-row table, 1 s at each offered rate, the plain one-query-at-a-time server against the
+    served one."""
+    import contextlib
+    import io
+    from computeql_gb300 import servebench
+    tables = [{"region": f.region, "amount": f.amount, "flag": f.flag} for f in (workloads.fact_table(1_000_000, seed=1),
+                                                                                 workloads.fact_table(100_000_000, seed=2))]
+    tables.append({"region": t.region, "amount": t.amount, "flag": t.flag})
+    d50, d1m = dims
+    d1m = dict(d1m)
+    d1m["seg_f64"] = d1m["seg"].astype("float64")
+    out = {"workload": "60/25/15 filter-aggregate / group-by / join-sort templates over resident 1M, 100M and 1B-row tables, "
+                       "Poisson arrivals, 160 GB admission budget, 1 s a rate", "slo_p99_ms": 50.0}
+    for mode in ("plain", "served"):
+        with contextlib.redirect_stdout(io.StringIO()):
+            lines, summary = servebench.run_mode(mode, tables, (d50, d1m), [2000.0, 5000.0], 1.0, 3, 50.0, 160 << 30)
+        out[mode] = {"max_qps_within_slo": summary["max_qps_within_slo"],
+                     "rates": [{k: r[k] for k in ("offered_qps", "completed_qps", "p50_ms", "p95_ms", "p99_ms", "failed")} for r in lines]}
+    for tab in tables[:2]:
+        for c in tab.values():
+            c.buffer.close()
+    return out
 
 
 def _canon(x):
