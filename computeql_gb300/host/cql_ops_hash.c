@@ -708,9 +708,12 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
     K = 64;
   }
   CqlKernel* assign = kernel("aggregate_assign");
-  if (!assign) return 0;
+  CqlKernel* compact = kernel("aggregate_compact");
+  if (!assign || !compact) return 0;
   CqlBuffer *owner = NULL, *count = NULL, *row_slot = NULL, *overflow = NULL;
+  CqlBuffer *offsets = NULL, *out_owner = NULL, *out_count = NULL;
   uint64_t slots = 0;
+  uint32_t groups32 = 0;
   for (int attempt = 0; attempt < 16; attempt++)
   {
     slots = linear ? buckets : buckets * K;
@@ -718,7 +721,15 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
     count = pooled("agg_count_buf", slots * 4, CQLCUDA_BUFFER_READ_WRITE);
     row_slot = pooled("agg_row_slot_buf", rows * 4, CQLCUDA_BUFFER_READ_WRITE);
     overflow = pooled("agg_overflow_buf", 4, CQLCUDA_BUFFER_READ_WRITE);
-    if (!owner || !count || !row_slot || !overflow) return 0;
+    /* compaction: offsets[slot] becomes the dense group id of an occupied slot */
+    uint64_t blocks = (slots + 255) / 256;
+    uint64_t max_g = slots < rows ? slots : rows;
+    offsets = pooled("agg_compact_offsets_buf", (slots + 1) * 4, CQLCUDA_BUFFER_READ_WRITE);
+    CqlBuffer* block_sums = pooled("agg_compact_block_sum_buf", blocks * 4, CQLCUDA_BUFFER_READ_WRITE);
+    out_owner = pooled("agg_compact_owner_buf", max_g * 4, CQLCUDA_BUFFER_READ_WRITE);
+    out_count = pooled("agg_compact_count_buf", max_g * 4, CQLCUDA_BUFFER_READ_WRITE);
+    CqlBuffer* total_buf = pooled("agg_compact_total_buf", 4, CQLCUDA_BUFFER_READ_WRITE);
+    if (!owner || !count || !row_slot || !overflow || !offsets || !block_sums || !out_owner || !out_count || !total_buf) return 0;
     for (uint32_t c = 0; c < 4; c++)
     {
       /* key bindings past the key count are never read: bound to the row-slot buffer */
@@ -737,14 +748,31 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
     cqlcuda_kernel_set_arg_u64(assign, 5, group_hint >= AGG_MANY_GROUPS);
     cqlcuda_kernel_set_arg_u64(assign, 6, linear);
     cqlcuda_kernel_set_arg_u64(assign, 7, key_types);
+    cqlcuda_kernel_set_arg_buffer(compact, 0, count);
+    cqlcuda_kernel_set_arg_buffer(compact, 1, owner);
+    cqlcuda_kernel_set_arg_buffer(compact, 2, offsets);
+    cqlcuda_kernel_set_arg_buffer(compact, 3, block_sums);
+    cqlcuda_kernel_set_arg_buffer(compact, 4, out_owner);
+    cqlcuda_kernel_set_arg_buffer(compact, 5, out_count);
+    cqlcuda_kernel_set_arg_buffer(compact, 6, total_buf);
+    cqlcuda_kernel_set_arg_u64(compact, 0, slots);
+    /* the assignment and its compaction in one batch, one wait: an overflowing table (rare) is compacted for
+       nothing and assigned again with more room */
     uint32_t over = 0;
-    CqlBatch* b = cqlcuda_batch_begin(0, 4);
+    CqlBatch* b = cqlcuda_batch_begin(0, 8);
     cqlcuda_batch_buffer_fill(b, owner, slots * 4, EMPTY);
     cqlcuda_batch_buffer_zero(b, count, slots * 4);
     cqlcuda_batch_buffer_fill(b, row_slot, rows * 4, EMPTY);
     cqlcuda_batch_buffer_zero(b, overflow, 4);
     cqlcuda_batch_kernel_execute(b, assign, (uint32_t)rows, QE_GPU_WORKGROUP_SIZE);
+    cqlcuda_kernel_set_arg_u64(compact, 1, 0);
+    cqlcuda_batch_kernel_execute(b, compact, (uint32_t)(blocks * 256), 256);
+    cqlcuda_kernel_set_arg_u64(compact, 1, 1);
+    cqlcuda_batch_kernel_execute(b, compact, 256, 256);
+    cqlcuda_kernel_set_arg_u64(compact, 1, 2);
+    cqlcuda_batch_kernel_execute(b, compact, (uint32_t)(blocks * 256), 256);
     cqlcuda_batch_buffer_read(b, overflow, &over, 4);
+    cqlcuda_batch_buffer_read(b, total_buf, &groups32, 4);
     if (!cqlcuda_batch_end(b)) return 0;
     if (over == 0 || key_count == 0) break;
     /* grow the buckets by how badly they missed, then K (:11226-11243) */
@@ -756,37 +784,6 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
     }
     else K *= 2;
     if (attempt == 15) return refuse("the group-by hash table kept overflowing");
-  }
-
-  /* compaction: offsets[slot] becomes the dense group id of an occupied slot */
-  uint64_t blocks = (slots + 255) / 256;
-  uint64_t max_g = slots < rows ? slots : rows;
-  CqlBuffer* offsets = pooled("agg_compact_offsets_buf", (slots + 1) * 4, CQLCUDA_BUFFER_READ_WRITE);
-  CqlBuffer* block_sums = pooled("agg_compact_block_sum_buf", blocks * 4, CQLCUDA_BUFFER_READ_WRITE);
-  CqlBuffer* out_owner = pooled("agg_compact_owner_buf", max_g * 4, CQLCUDA_BUFFER_READ_WRITE);
-  CqlBuffer* out_count = pooled("agg_compact_count_buf", max_g * 4, CQLCUDA_BUFFER_READ_WRITE);
-  CqlBuffer* total_buf = pooled("agg_compact_total_buf", 4, CQLCUDA_BUFFER_READ_WRITE);
-  CqlKernel* compact = kernel("aggregate_compact");
-  if (!offsets || !block_sums || !out_owner || !out_count || !total_buf || !compact) return 0;
-  cqlcuda_kernel_set_arg_buffer(compact, 0, count);
-  cqlcuda_kernel_set_arg_buffer(compact, 1, owner);
-  cqlcuda_kernel_set_arg_buffer(compact, 2, offsets);
-  cqlcuda_kernel_set_arg_buffer(compact, 3, block_sums);
-  cqlcuda_kernel_set_arg_buffer(compact, 4, out_owner);
-  cqlcuda_kernel_set_arg_buffer(compact, 5, out_count);
-  cqlcuda_kernel_set_arg_buffer(compact, 6, total_buf);
-  cqlcuda_kernel_set_arg_u64(compact, 0, slots);
-  uint32_t groups32 = 0;
-  {
-    CqlBatch* b = cqlcuda_batch_begin(0, 4);
-    cqlcuda_kernel_set_arg_u64(compact, 1, 0);
-    cqlcuda_batch_kernel_execute(b, compact, (uint32_t)(blocks * 256), 256);
-    cqlcuda_kernel_set_arg_u64(compact, 1, 1);
-    cqlcuda_batch_kernel_execute(b, compact, 256, 256);
-    cqlcuda_kernel_set_arg_u64(compact, 1, 2);
-    cqlcuda_batch_kernel_execute(b, compact, (uint32_t)(blocks * 256), 256);
-    cqlcuda_batch_buffer_read(b, total_buf, &groups32, 4);
-    if (!cqlcuda_batch_end(b)) return 0;
   }
   uint64_t groups = groups32;
   if (groups > max_groups) return refuse("more groups than the output arrays hold");
