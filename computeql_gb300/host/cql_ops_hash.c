@@ -164,9 +164,19 @@ static int whole_number_arg(const CqlColumn* col)
 /* The CSR member reduce of the groups found by assign/compact: slot_counts/slot_group (compact
    offsets) per slot, group_counts per group, row_slot per row. Writes out_results[g * exprs + e].
    With row_slot NULL there is one group of every row in order (no key). */
+typedef struct
+{
+  CqlBuffer* buffer;
+  void* dst;
+  uint64_t bytes;
+} PendingRead;
+
+/* `open` (optional): a batch the caller began, which the chunk pass joins and ends after the caller's
+   `reads` - one wait for both */
 static int csr_reduce(uint64_t rows, uint64_t slots, uint64_t groups, CqlBuffer* slot_counts, CqlBuffer* slot_group,
                       CqlBuffer* group_counts, CqlBuffer* row_slot, uint32_t expr_count, const uint32_t* funcs, uint32_t func_codes,
-                      CqlBuffer* const* arg_f64, const double* params, double* out_results)
+                      CqlBuffer* const* arg_f64, const double* params, double* out_results, CqlBatch* open, const PendingRead* reads,
+                      uint32_t read_count)
 {
   uint64_t gb = (groups + 255) / 256;
   CqlBuffer* g_start = pooled("agg_group_start_buf", (groups + 1) * 4, CQLCUDA_BUFFER_READ_WRITE);
@@ -176,10 +186,14 @@ static int csr_reduce(uint64_t rows, uint64_t slots, uint64_t groups, CqlBuffer*
   CqlBuffer* block_sums = pooled("agg_scan_block_buf", gb * 4, CQLCUDA_BUFFER_READ_WRITE);
   CqlKernel* kchunks = kernel("cql_group_chunks");
   CqlKernel* scan = kernel("prefix_sum");
-  if (!g_start || !g_chunks || !c_base || !scratch || !block_sums || !kchunks || !scan) return 0;
+  if (!g_start || !g_chunks || !c_base || !scratch || !block_sums || !kchunks || !scan)
+  {
+    if (open) cqlcuda_batch_end(open);
+    return 0;
+  }
   uint32_t total_chunks32 = 0;
   {
-    CqlBatch* b = cqlcuda_batch_begin(0, 4);
+    CqlBatch* b = open ? open : cqlcuda_batch_begin(0, 4);
     cqlcuda_kernel_set_arg_buffer(kchunks, 0, group_counts);
     cqlcuda_kernel_set_arg_buffer(kchunks, 1, g_chunks);
     cqlcuda_kernel_set_arg_u64(kchunks, 0, groups);
@@ -198,7 +212,8 @@ static int csr_reduce(uint64_t rows, uint64_t slots, uint64_t groups, CqlBuffer*
         cqlcuda_batch_kernel_execute(b, scan, mode == 1 ? 256u : (uint32_t)(gb * 256), 256);
       }
     }
-    /* the chunk count: the scan's total, after the last chunk base */
+    /* the caller's reads, then the chunk count: the scan's total, after the last chunk base */
+    for (uint32_t r = 0; r < read_count; r++) cqlcuda_batch_buffer_read(b, reads[r].buffer, reads[r].dst, reads[r].bytes);
     cqlcuda_batch_buffer_read_at(b, c_base, groups * 4, &total_chunks32, 4);
     if (!cqlcuda_batch_end(b)) return 0;
   }
@@ -671,7 +686,7 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
     if (!cqlcuda_batch_end(b)) return 0;
     out_repr_row[0] = 0;
     out_counts[0] = rows;
-    if (!csr_reduce(rows, 1, 1, NULL, NULL, one, NULL, expr_count, funcs, func_codes, arg_f64, params, out_results)) return 0;
+    if (!csr_reduce(rows, 1, 1, NULL, NULL, one, NULL, expr_count, funcs, func_codes, arg_f64, params, out_results, NULL, NULL, 0)) return 0;
     *out_group_count = 1;
     if (out_path) *out_path = 1u;
     return 1;
@@ -862,19 +877,15 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
   }
   else
   {
-    CqlBatch* b = cqlcuda_batch_begin(0, groups * 16);
-    cqlcuda_batch_kernel_execute(b, finish, (uint32_t)groups, QE_GPU_WORKGROUP_SIZE);
-    cqlcuda_batch_buffer_read(b, repr64, out_repr_row, groups * 8);
-    cqlcuda_batch_buffer_read(b, count64, out_counts, groups * 8);
-    ok = cqlcuda_batch_end(b);
-  }
-  if (ok && !use_fixed)
-  {
     /* 4b: member lists, group g's members at [start[g], start[g] + count[g]), laid out on the device:
        group starts and chunk bases by prefix sums, cursors and chunk ranges by kernels, the member
-       reduce per 4096-row chunk, and each group's chunks folded in chunk order (:11826-12215) */
+       reduce per 4096-row chunk, and each group's chunks folded in chunk order (:11826-12215). The
+       representative rows and counts are finished in the batch of the chunk pass. */
+    CqlBatch* b = cqlcuda_batch_begin(0, groups * 16 + 16);
+    cqlcuda_batch_kernel_execute(b, finish, (uint32_t)groups, QE_GPU_WORKGROUP_SIZE);
+    PendingRead reads[2] = { { repr64, out_repr_row, groups * 8 }, { count64, out_counts, groups * 8 } };
     ok = csr_reduce(rows, slots, groups, count, offsets, out_count, row_slot, expr_count, funcs, func_codes, arg_f64, params,
-                    out_results);
+                    out_results, b, reads, 2);
   }
   if (ok)
   {
