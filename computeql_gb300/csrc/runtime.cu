@@ -2297,6 +2297,7 @@ struct CqlPersistent
   cudaStream_t stream, copies;
   CqlLaunch args;
   int launched;
+  uint32_t ctas;     // the grid of the last launch
 };
 
 extern "C" CqlPersistent* cqlcuda_persistent_create(CqlKernel* k, const char* entry)
@@ -2316,6 +2317,7 @@ extern "C" CqlPersistent* cqlcuda_persistent_create(CqlKernel* k, const char* en
   p->kernel = k;
   p->fn = fn;
   p->launched = 0;
+  p->ctas = 0;
   memset(&p->args, 0, sizeof(p->args));
   if (!note_cuda(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking), "cudaStreamCreate(persistent)"))
   {
@@ -2363,9 +2365,9 @@ extern "C" int cqlcuda_persistent_launch(CqlPersistent* p, uint32_t ctas, CqlBuf
       cudaGetLastError();
       per_sm = 1;
     }
-    // and one CTA's room an SM left over (where two or more fit), so that other lanes' kernels still find an
-    // SM while this one waits for work
-    if (per_sm >= 2) per_sm -= 1;
+    // and one CTA's room an SM left over where four or more fit, so that other lanes' kernels still find an
+    // SM while this one waits for work (with fewer, the room would cost the scan a third of its warps or more)
+    if (per_sm >= 4) per_sm -= 1;
     ctas = (uint32_t)per_sm * (uint32_t)g_cql_sm_count;
   }
   if (cqlcuda_persistent_running(p) == 1)
@@ -2381,8 +2383,11 @@ extern "C" int cqlcuda_persistent_launch(CqlPersistent* p, uint32_t ctas, CqlBuf
     return 0;
   cql_note_launch();
   p->launched = 1;
+  p->ctas = ctas;
   return 1;
 }
+
+extern "C" uint32_t cqlcuda_persistent_ctas(CqlPersistent* p) { return p ? p->ctas : 0; }
 
 // queues a copy of host bytes into a device buffer on the copy stream; the source must stay unchanged until
 // the work it describes is done

@@ -76,8 +76,15 @@ def queries(cols, users, words):
         w = ops.window_rank([cols["region"], cols["u2"]], desc=[0, 1], partitions=1, selection=sel, count=len(rows))
         return int((w["row_number"] <= 3).sum())
 
+    # each hash group-by of many groups writes into its own result area, kept between calls as an engine keeps
+    # its result buffers (fresh arrays would cost their page faults in every call)
+    rows = cols["user_id"].rows
+    out_users = ops.HashOutputs(min(rows, 2_000_000), 2)
+    out_sessions = ops.HashOutputs(min(rows, 8_000_000), 1)
+    out_having = ops.HashOutputs(min(rows, 2_000_000), 1)
+
     def having_1m():
-        r = ops.group_hash([cols["user_id"]], [F.FUNC_SUM], [cols["u0"]], group_hint=1_000_000)
+        r = ops.group_hash([cols["user_id"]], [F.FUNC_SUM], [cols["u0"]], group_hint=1_000_000, out=out_having)
         keep = ops.having("v0 > lit[0]", [r["results"][:, 0]], [HAVING_SUM_GT])
         return r, keep
 
@@ -97,8 +104,8 @@ def queries(cols, users, words):
         ("join_users_by_segment", lambda: ops.join_aggregate(cols["user_id"], [F.FUNC_COUNT, F.FUNC_SUM], [None, cols["u5"]],
                                                              users["user_id"], group_values=[seg])),
         ("group_by_user_id", lambda: ops.group_hash([cols["user_id"]], [F.FUNC_COUNT, F.FUNC_SUM], [None, cols["u0"]],
-                                                    group_hint=1_000_000)),
-        ("distinct_sessions", lambda: ops.group_hash([cols["session"]], [F.FUNC_COUNT], [None], group_hint=4_000_000)),
+                                                    group_hint=1_000_000, out=out_users)),
+        ("distinct_sessions", lambda: ops.group_hash([cols["session"]], [F.FUNC_COUNT], [None], group_hint=4_000_000, out=out_sessions)),
         ("sort_200k", sort_200k),
         ("wide_projection_1pct", wide_projection),
         ("window_top3_per_region", window_top3),

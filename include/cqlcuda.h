@@ -251,7 +251,7 @@ CqlBuffer* cqlcuda_buffer_alloc_host_mapped(uint64_t size, void** out_host);
    its work from device memory that the host fills with cqlcuda_persistent_copy (copies land in the order
    queued) and returns by itself at its own idle limit; no generated kernel is evicted while one exists.
    launch: with k's arguments as this thread set them, `ctas` CTAs of k's block size and shared memory (0:
-   as many as are resident at once, less one CTA's room an SM for other kernels),
+   as many as are resident at once, less one CTA's room an SM for other kernels where four or more fit),
    after clearing zero_bytes of `zero` (optional) on the kernel's stream; refused while the kernel runs.
    running: 1 while it runs, 0 once it has returned, -1 if it returned with an error.
    copy: the source must stay unchanged until the work it describes is done.
@@ -262,6 +262,7 @@ int      cqlcuda_persistent_launch(CqlPersistent* p, uint32_t ctas, CqlBuffer* z
 int      cqlcuda_persistent_running(CqlPersistent* p);
 int      cqlcuda_persistent_copy(CqlPersistent* p, CqlBuffer* dst, uint64_t offset, const void* src, uint64_t size);
 int      cqlcuda_persistent_destroy(CqlPersistent* p, uint32_t timeout_ms);
+uint32_t cqlcuda_persistent_ctas(CqlPersistent* p);    /* the grid of the last launch */
 /* Writes `bytes` bytes of a scratch buffer, to evict the L2 between timed runs. */
 int      cqlcuda_flush_l2(uint64_t bytes);
 /* CUDA-event timing of everything the library enqueues between begin and end, on its own stream. */

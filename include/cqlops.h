@@ -470,6 +470,8 @@ int cqlops_batch_persist_run(CqlBatchPersist* p, const CqlProgram* const* progra
                              uint64_t* out_counts, double* out_sums);
 /* batches run, kernel launches (the first and each after an idle return) and compiles so far */
 void cqlops_batch_persist_stats(CqlBatchPersist* p, uint64_t* out_batches, uint64_t* out_launches, uint64_t* out_compiles);
+/* the CTAs of the kernel's last launch (0 before the first) */
+uint32_t cqlops_batch_persist_ctas(CqlBatchPersist* p);
 /* ends the kernel (a stop word in the slot it waits on) and frees everything; 0 if it did not return in 5 s */
 int cqlops_batch_persist_destroy(CqlBatchPersist* p);
 
