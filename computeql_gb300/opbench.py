@@ -14,6 +14,7 @@ like the configurations the operators serve:
   hash_group    GROUP BY user_id (1M groups) with COUNT and SUM of an f64 measure over 10M rows
   hll           APPROX_COUNT_DISTINCT(session) over 10M rows (4M distinct)
   hash_join     a 1M-row build side (unique keys) probed by 10M rows, pairs counted
+  dense_10k     GROUP BY amount (10k groups) COUNT, SUM(region) over `rows` rows of the seed-0 fact table
   join_small    the join-aggregate probe (join_probe_native) of a 1024-row dim table by `rows` fact rows (random
                 keys), COUNT and SUM(amount) per dim row folded into 20 groups: the small build side
   zone_map      the zone map of one u32 column
@@ -29,9 +30,10 @@ import time
 
 import numpy as np
 
-from . import build, native, ops
+from . import build, native, ops, workloads
 
-OPS = ["sort", "sort_f64_2", "sort_subset", "fixed", "hash_group", "hll", "hash_join", "join_small", "zone_map", "batch", "materialize"]
+OPS = ["sort", "sort_f64_2", "sort_subset", "fixed", "hash_group", "hll", "hash_join", "join_small", "zone_map", "batch", "materialize",
+       "dense_10k"]
 
 
 def _profile():
@@ -116,6 +118,11 @@ def run(op, rows, reps):
         pk = ops.Column.splitmix(probe_rows, 0, 1, 0, 1_000_000)
         fn = lambda: ops.hash_join(bk, pk, want_pairs=False)
         n, nbytes = probe_rows, (build_rows + probe_rows) * 4
+    elif op == "dense_10k":
+        # GROUP BY amount (10k groups) COUNT, SUM(region) over the seed-0 fact table's first `rows` rows
+        t = workloads.fact_table(rows)
+        fn = lambda: ops.group_dense(t.amount, [ops.FUNC_COUNT, ops.FUNC_SUM], [None, t.region])
+        n, nbytes = rows, rows * 8
     elif op == "join_small":
         fk = ops.Column.splitmix(rows, 6, 2, 0, 1024)
         amount = ops.Column.splitmix(rows, 6, 2, 1, 10_000)
