@@ -516,7 +516,13 @@ def run_batched(native, ops, lib):
         return statistics.median(walls), out
     auto_ms, (c_auto, s_auto, _) = timed(lambda: ops.batch_aggregate(progs, sums, auto), 3)
     form = native.load_ops().cqlops_batch_last_form()
+    # one generated kernel per (shape, summed column): 116 here, past the default cap of 64 loaded kernels, which
+    # would evict and recompile them in turn; the cap is raised for this path, its kernels compiled first
+    lib.cqlcuda_set_generated_kernel_cap(256)
+    for p_, s_ in zip(progs, sums):
+        ops.fused_aggregate(p_, [s_])
     one_ms, one = timed(lambda: [ops.fused_aggregate(p, [s]) for p, s in zip(progs, sums)], 1)
+    lib.cqlcuda_set_generated_kernel_cap(64)
     c_one = np.array([r[0] for r in one], dtype=np.uint64)
     s_one = np.array([r[1][0] for r in one], dtype=np.float64)
     cat = ops.BatchCatalog()

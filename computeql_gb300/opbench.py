@@ -221,7 +221,12 @@ def run_batch(rows, reps):
         tuning["tile" if rpt == 0 else f"rows_per_thread_{rpt}"] = round(wall, 3)
         if best is None or wall < best[1]:
             best = (rpt, wall, kernel_ms, kernels)
+    # one generated kernel per (shape, summed column), 116 here: past the default cap of 64 they would be evicted
+    # and compiled again in turn, so the cap is raised for this path
+    lib = native.load_cuda()
+    lib.cqlcuda_set_generated_kernel_cap(256)
     one_wall, one_kernel, _ = _time(lambda: [ops.fused_aggregate(p, [s]) for p, s in zip(progs, sums)], max(1, reps // 2))
+    lib.cqlcuda_set_generated_kernel_cap(64)
     # the autotuner: its trial runs (one per candidate form) first, then its pick
     auto = ops.CQLOPS_BATCH_AUTOTUNE
     for _ in range(8):
