@@ -750,10 +750,11 @@ static int launch_join_probe_native(const CqlLaunch& a, uint32_t gws, uint32_t l
 // right for U32 and I32 keys alike; a key outside [min, min + range) matches nothing.
 //
 //  cql_join_lut_build  binding 0 visits (u32 dim rows; unbound: rows 0..visits-1), 1 dim keys (u32), 2 dim
-//                      group values (f64), 3 table (u32 group id per key value, all EMPTY before),
+//                      group values (word 12's type), 3 table (u32 group id per key value, all EMPTY before),
 //                      4 visit per key value (u32), 5 error word; word 0 visits, word 2 1 = visit list
 //                      given, word 4 min key bits, word 6 range, word 8/9 the smallest group value (f64
-//                      bits), word 10 group values given (else every row is group 0).
+//                      bits), word 10 group values given (else every row is group 0), word 12 the group
+//                      values' type (4 f64, 1 u32, 7 i32; 0 taken as f64).
 //                      Error bit 0: a key met twice (the table cannot stand for the join).
 //  cql_join_lut_map    binding 0 fact keys, 1 table, 2 group ids out (u32), 3 key-present bitmap (all 0
 //                      before); word 0 rows, word 4 min key bits, word 6 range, word 8 the id of no group
@@ -767,20 +768,24 @@ __global__ void __launch_bounds__(JOIN_THREADS) k_join_lut_build(CqlLaunch a, ui
   const uint32_t* visit_rows = (const uint32_t*)a.buf[0];
   const uint32_t* dim_keys = (const uint32_t*)a.buf[1];
   const double* group_values = (const double*)a.buf[2];
+  const uint32_t* group_words = (const uint32_t*)a.buf[2];
   uint32_t* table = (uint32_t*)a.buf[3];
   uint32_t* visit_of = (uint32_t*)a.buf[4];
   uint32_t* error = (uint32_t*)a.buf[5];
   bool listed = cql_word(a, 2) != 0, grouped = cql_word(a, 10) != 0;
   uint32_t min_key = cql_word(a, 4), range = cql_word(a, 6);
+  uint32_t group_type = cql_word(a, 12);    // 4 f64 (or 0), 1 u32, 7 i32
+  bool group_f64 = group_type != 1u && group_type != 7u;
   double group_min = __longlong_as_double((long long)a.push[4]);
-  uint64_t dim_rows = a.bytes[1] / 4, value_rows = a.bytes[2] / 8;
+  uint64_t dim_rows = a.bytes[1] / 4, value_rows = a.bytes[2] / (group_f64 ? 8 : 4);
   for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < visits; v += (uint64_t)gridDim.x * blockDim.x)
   {
     uint64_t row = listed ? visit_rows[v] : v;
     if (row >= dim_rows || (grouped && row >= value_rows)) continue;
     uint32_t k = dim_keys[row] - min_key;
     if (k >= range) continue;
-    uint32_t gid = grouped ? (uint32_t)(group_values[row] - group_min) : 0u;
+    double value = !grouped ? 0.0 : group_f64 ? group_values[row] : group_type == 7u ? (double)(int)group_words[row] : (double)group_words[row];
+    uint32_t gid = grouped ? (uint32_t)(value - group_min) : 0u;
     uint32_t prev = atomicCAS(&table[k], LUT_EMPTY, gid);
     if (prev != LUT_EMPTY) atomicOr(error, 1u);
     else visit_of[k] = (uint32_t)v;

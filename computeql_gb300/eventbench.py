@@ -102,7 +102,8 @@ def queries(cols, users, words):
                                                           [None, cols["u0"], cols["m0"], cols["m1"], cols["m1"]], group_hint=50)),
         ("three_predicate_filter", lambda: ops.fused_aggregate(program_triple, ["u5"])),
         ("join_users_by_segment", lambda: ops.join_aggregate(cols["user_id"], [F.FUNC_COUNT, F.FUNC_SUM], [None, cols["u5"]],
-                                                             users["user_id"], group_values=[seg])),
+                                                             users["user_id"], group_values=[seg], dim_key_col=users.get("user_id_col"),
+                                                             dim_group_col=users.get("segment_col"))),
         ("group_by_user_id", lambda: ops.group_hash([cols["user_id"]], [F.FUNC_COUNT, F.FUNC_SUM], [None, cols["u0"]],
                                                     group_hint=1_000_000, out=out_users)),
         ("distinct_sessions", lambda: ops.group_hash([cols["session"]], [F.FUNC_COUNT], [None], group_hint=4_000_000, out=out_sessions)),

@@ -588,10 +588,24 @@ static int lut_join_aggregate(const CqlJoinAgg* q, uint32_t core_count, const ui
   uint64_t visits = q->dim_rows ? q->dim_count : q->dim_table_rows;
   uint64_t D = q->dim_table_rows;
   if (visits == 0 || D == 0 || D >= 0xffffffffull || visits >= 0xffffffffull) return -1;
+  /* device copies of the dim table's key and group columns, when the caller has them resident: nothing is
+     uploaded, and the group values' range is the column's zone (a superset of the visited rows' range, which
+     only adds empty group ids) */
+  const CqlColumn* dkc = q->dim_key_column;
+  const CqlColumn* dgc = q->group_count ? q->dim_group_column : NULL;
+  int dev_keys = dkc && dkc->buffer && dkc->width == 0 && dkc->rows == D && (dkc->type == CQLOPS_TYPE_U32 || dkc->type == CQLOPS_TYPE_I32);
+  int dev_groups = dev_keys && dgc && dgc->buffer && dgc->width == 0 && dgc->rows == D && dgc->has_range &&
+                   (dgc->type == CQLOPS_TYPE_U32 || dgc->type == CQLOPS_TYPE_I32);
   /* the group values of the visited rows: whole numbers within LUT_MAX_GROUPS of each other */
   const double* gv = q->group_count ? q->dim_group_values[0] : NULL;
   double vmin = 0.0, vmax = 0.0;
-  if (gv)
+  if (gv && dev_groups)
+  {
+    vmin = dgc->zone_min;
+    vmax = dgc->zone_max;
+    if (vmax - vmin > (double)(LUT_MAX_GROUPS - 1)) return -1;
+  }
+  else if (gv)
   {
     vmin = HUGE_VAL;
     vmax = -HUGE_VAL;
@@ -624,8 +638,8 @@ static int lut_join_aggregate(const CqlJoinAgg* q, uint32_t core_count, const ui
     }
   }
   CqlBuffer* vbuf = pooled("join_lut_visits", visit_list ? visits * 4 : 4, CQLCUDA_BUFFER_WRITE);
-  CqlBuffer* kbuf = pooled("join_lut_dim_keys", D * 4, CQLCUDA_BUFFER_WRITE);
-  CqlBuffer* gbuf = pooled("join_lut_group_values", gv ? D * 8 : 8, CQLCUDA_BUFFER_WRITE);
+  CqlBuffer* kbuf = dev_keys ? dkc->buffer : pooled("join_lut_dim_keys", D * 4, CQLCUDA_BUFFER_WRITE);
+  CqlBuffer* gbuf = dev_groups ? dgc->buffer : pooled("join_lut_group_values", gv ? D * 8 : 8, CQLCUDA_BUFFER_WRITE);
   CqlBuffer* table = pooled("join_lut_table", range * 4, CQLCUDA_BUFFER_READ_WRITE);
   CqlBuffer* visit_of = pooled("join_lut_visit_of", range * 4, CQLCUDA_BUFFER_READ_WRITE);
   CqlBuffer* err = pooled("join_lut_error", 4, CQLCUDA_BUFFER_READ_WRITE);
@@ -656,6 +670,7 @@ static int lut_join_aggregate(const CqlJoinAgg* q, uint32_t core_count, const ui
   cqlcuda_kernel_set_arg_u64(kb, 3, range);
   cqlcuda_kernel_set_arg_u64(kb, 4, group_min_bits);
   cqlcuda_kernel_set_arg_u64(kb, 5, gv ? 1 : 0);
+  cqlcuda_kernel_set_arg_u64(kb, 6, dev_groups ? dgc->type : CQLOPS_TYPE_F64);   /* the group values' type */
   cqlcuda_kernel_set_arg_buffer(km, 0, fk->buffer);
   cqlcuda_kernel_set_arg_buffer(km, 1, table);
   cqlcuda_kernel_set_arg_buffer(km, 2, ids);
@@ -672,8 +687,8 @@ static int lut_join_aggregate(const CqlJoinAgg* q, uint32_t core_count, const ui
   uint32_t error = 0;
   CqlBatch* b = cqlcuda_batch_begin((visit_list ? visits * 4 : 0) + D * 4 + (gv ? D * 8 : 0), 4 + (uint64_t)ngroups * 4);
   if (visit_list) cqlcuda_batch_buffer_write(b, vbuf, visit_list, visits * 4);
-  cqlcuda_batch_buffer_write(b, kbuf, q->dim_keys, D * 4);
-  if (gv) cqlcuda_batch_buffer_write(b, gbuf, gv, D * 8);
+  if (!dev_keys) cqlcuda_batch_buffer_write(b, kbuf, q->dim_keys, D * 4);
+  if (gv && !dev_groups) cqlcuda_batch_buffer_write(b, gbuf, gv, D * 8);
   cqlcuda_batch_buffer_fill(b, table, range * 4, 0xffffffffu);
   cqlcuda_batch_buffer_fill(b, first, (uint64_t)ngroups * 4, 0xffffffffu);
   cqlcuda_batch_buffer_zero(b, present, ((range + 31) / 32) * 4);

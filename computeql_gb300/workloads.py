@@ -137,9 +137,13 @@ def event_numpy(rows, seed=EVENT_SEED):
 
 def event_table(rows, seed=EVENT_SEED):
     """The event table resident on the device: a dict of columns (dictionary strings as coded string
-    columns over the shared dictionary), the users table as host arrays, and the host arrays."""
+    columns over the shared dictionary), the users table as host arrays (and its two columns resident under
+    "<name>_col"), and the host arrays."""
     from .ops import Column, StringColumn
     h, users, words = event_numpy(rows, seed)
+    # the users table is resident too (the join's dim-side pass reads it on the device)
+    users["user_id_col"] = Column.from_numpy(users["user_id"])
+    users["segment_col"] = Column.from_numpy(users["segment"])
     cols = {}
     for name, arr in h.items():
         if name in EVENT_DICT:

@@ -200,6 +200,31 @@ def test_lookup_table_join_with_a_dim_filter_and_no_group(ops):
     np.testing.assert_array_equal(a["results"], b["results"])
 
 
+@pytest.mark.parametrize("signed", [False, True])
+def test_lookup_table_reads_resident_dim_columns(ops, signed):
+    """The lookup-table join with the dim table's key and group columns resident (dim_key_col, dim_group_col):
+    nothing uploaded, the group range from the group column's zone (a superset of the kept rows' range); the
+    same groups in the same order and the same totals as with host arrays, with and without a dim filter."""
+    rng = np.random.default_rng(55 + signed)
+    n, d = 2_000_000, 600_000
+    key = rng.integers(0, d, n).astype(np.uint32)
+    v = rng.integers(-3000, 3000, n).astype(np.int32)
+    dim_keys = rng.permutation(d).astype(np.uint32)
+    seg_i = (rng.integers(-7, 13, d) if signed else rng.integers(0, 20, d)).astype(np.int32 if signed else np.uint32)
+    seg = seg_i.astype(np.float64)
+    kept = np.sort(rng.choice(d, d // 2, replace=False)).astype(np.uint64)
+    kc, vc = ops.Column.from_numpy(key), ops.Column.from_numpy(v)
+    dk_col, seg_col = ops.Column.from_numpy(dim_keys), ops.Column.from_numpy(seg_i)
+    funcs, args = [COUNT, SUM, MIN, MAX], [None, vc, vc, vc]
+    for rows in (None, kept):
+        host = ops.join_aggregate(kc, funcs, args, dim_keys, dim_rows=rows, group_values=[seg], strategy=3)
+        dev = ops.join_aggregate(kc, funcs, args, dim_keys, dim_rows=rows, group_values=[seg], strategy=3, dim_key_col=dk_col,
+                                 dim_group_col=seg_col)
+        assert host["strategy"] == dev["strategy"] == 3
+        assert list(dev["dim_row"]) == list(host["dim_row"])
+        np.testing.assert_array_equal(dev["results"], host["results"])
+
+
 def test_lookup_table_gives_way_to_repeated_dim_keys(ops):
     """Repeated dim keys: the lookup table gives way; past the dense range the probe path refuses them as
     it did before (each key must name one dim row), and a forced lookup table refuses too."""
