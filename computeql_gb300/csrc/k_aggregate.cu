@@ -629,7 +629,10 @@ __global__ void __launch_bounds__(1024) k_aggregate_dense(CqlLaunch a, DenseLayo
 // shared atomics with a carry into the high word as aggregate_dense_native.comp:184-200 does, one
 // private table per warp when the groups are few. KEYARG: the one argument column is the key column
 // itself (GROUP BY amount ... SUM(amount)), read once.
-template <int NE, int NA, bool KEYARG = false>
+// DEPTH: key vectors (and vectors of every argument column) in flight per thread. 2 where several CTAs share an
+// SM; 4 for the one-CTA-an-SM tables (1024 threads, a table of thousands of groups), whose warps alone must keep
+// enough loads in flight.
+template <int NE, int NA, bool KEYARG = false, int DEPTH = 2>
 __global__ void __launch_bounds__(1024) k_aggregate_dense_wide(CqlLaunch a, uint32_t G, uint32_t group_base, uint64_t rows,
                                                                uint32_t copies, uint32_t copy_words, uint32_t nsum)
 {
@@ -704,55 +707,39 @@ __global__ void __launch_bounds__(1024) k_aggregate_dense_wide(CqlLaunch a, uint
   uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   constexpr int NC = NA > 0 ? NA : 1;
   uint64_t i = t;
-  // two key vectors and two vectors of every argument column in flight per thread
-  for (; i + stride < vec_count; i += 2 * stride)
+  // DEPTH key vectors and DEPTH vectors of every argument column in flight per thread
+  for (; i + (uint64_t)(DEPTH - 1) * stride < vec_count; i += DEPTH * stride)
   {
-    uint4 k0 = __ldcs(kv + i), k1 = __ldcs(kv + i + stride);
-    uint4 q0[NC], q1[NC];
+    uint4 kk[DEPTH], qq[DEPTH][NC];
 #pragma unroll
-    for (int c = 0; c < NC; c++)
+    for (int dd = 0; dd < DEPTH; dd++)
     {
-      if (KEYARG)
+      kk[dd] = __ldcs(kv + i + dd * stride);
+#pragma unroll
+      for (int c = 0; c < NC; c++)
       {
-        q0[c] = k0;
-        q1[c] = k1;
-      }
-      else if (c < NA)
-      {
-        q0[c] = __ldcs((const uint4*)a.buf[1 + c] + i);
-        q1[c] = __ldcs((const uint4*)a.buf[1 + c] + i + stride);
-      }
-      else
-      {
-        q0[c] = make_uint4(0, 0, 0, 0);
-        q1[c] = q0[c];
+        if (KEYARG) qq[dd][c] = kk[dd];
+        else if (c < NA) qq[dd][c] = __ldcs((const uint4*)a.buf[1 + c] + i + dd * stride);
+        else qq[dd][c] = make_uint4(0, 0, 0, 0);
       }
     }
-    uint32_t v[NC];
 #pragma unroll
-    for (int c = 0; c < NC; c++) v[c] = q0[c].x;
-    row(k0.x, v);
+    for (int dd = 0; dd < DEPTH; dd++)
+    {
+      uint32_t v[NC];
 #pragma unroll
-    for (int c = 0; c < NC; c++) v[c] = q0[c].y;
-    row(k0.y, v);
+      for (int c = 0; c < NC; c++) v[c] = qq[dd][c].x;
+      row(kk[dd].x, v);
 #pragma unroll
-    for (int c = 0; c < NC; c++) v[c] = q0[c].z;
-    row(k0.z, v);
+      for (int c = 0; c < NC; c++) v[c] = qq[dd][c].y;
+      row(kk[dd].y, v);
 #pragma unroll
-    for (int c = 0; c < NC; c++) v[c] = q0[c].w;
-    row(k0.w, v);
+      for (int c = 0; c < NC; c++) v[c] = qq[dd][c].z;
+      row(kk[dd].z, v);
 #pragma unroll
-    for (int c = 0; c < NC; c++) v[c] = q1[c].x;
-    row(k1.x, v);
-#pragma unroll
-    for (int c = 0; c < NC; c++) v[c] = q1[c].y;
-    row(k1.y, v);
-#pragma unroll
-    for (int c = 0; c < NC; c++) v[c] = q1[c].z;
-    row(k1.z, v);
-#pragma unroll
-    for (int c = 0; c < NC; c++) v[c] = q1[c].w;
-    row(k1.w, v);
+      for (int c = 0; c < NC; c++) v[c] = qq[dd][c].w;
+      row(kk[dd].w, v);
+    }
   }
   for (; i < vec_count; i += stride)
   {
@@ -836,6 +823,11 @@ __global__ void __launch_bounds__(1024) k_aggregate_dense_wide(CqlLaunch a, uint
 }
 
 typedef void (*DenseWideFn)(CqlLaunch, uint32_t, uint32_t, uint64_t, uint32_t, uint32_t, uint32_t);
+// four vectors in flight for the one-CTA-an-SM tables of the common shapes (up to 4 aggregates over up to 2
+// argument columns, and the key-is-the-argument form with up to 2 aggregates)
+#define DW4_ROW(NE) { k_aggregate_dense_wide<NE, 0, false, 4>, k_aggregate_dense_wide<NE, 1, false, 4>, k_aggregate_dense_wide<NE, 2, false, 4> }
+static const DenseWideFn k_dense_wide_deep[4][3] = { DW4_ROW(1), DW4_ROW(2), DW4_ROW(3), DW4_ROW(4) };
+static const DenseWideFn k_dense_keyarg_deep[2] = { k_aggregate_dense_wide<1, 1, true, 4>, k_aggregate_dense_wide<2, 1, true, 4> };
 #define DW_ROW(NE) { k_aggregate_dense_wide<NE, 0>, k_aggregate_dense_wide<NE, 1>, k_aggregate_dense_wide<NE, 2>, k_aggregate_dense_wide<NE, 4> }
 static const DenseWideFn k_dense_wide_table[8][4] = { DW_ROW(1), DW_ROW(2), DW_ROW(3), DW_ROW(4), DW_ROW(5), DW_ROW(6), DW_ROW(7), DW_ROW(8) };
 static const DenseWideFn k_dense_keyarg_table[8] = { k_aggregate_dense_wide<1, 1, true>, k_aggregate_dense_wide<2, 1, true>,
@@ -858,13 +850,15 @@ static int launch_dense_wide(const CqlLaunch& a, uint64_t rows, uint32_t exprs, 
     uint32_t f = (funcs >> (4 * e)) & 0xfu;
     if (f != FUNC_COUNT) na = std::max(na, ((arg_index >> (4 * e)) & 0x3u) + 1);
   }
-  DenseWideFn fn = k_dense_wide_table[exprs - 1][na <= 2 ? na : 3];
-  if (na == 1 && a.buf[1] == a.buf[0]) fn = k_dense_keyarg_table[exprs - 1];
+  bool keyarg = na == 1 && a.buf[1] == a.buf[0];
   for (uint32_t base = 0; base < groups; base += tile)
   {
     uint32_t G = std::min(tile, groups - base);
     uint32_t copy_words = (G * per_group + 3) & ~3u;
     uint32_t threads = copy_words * 4 > 48 * 1024 ? 1024 : 512;
+    DenseWideFn fn = keyarg ? k_dense_keyarg_table[exprs - 1] : k_dense_wide_table[exprs - 1][na <= 2 ? na : 3];
+    if (threads == 1024 && keyarg && exprs <= 2) fn = k_dense_keyarg_deep[exprs - 1];
+    else if (threads == 1024 && !keyarg && exprs <= 4 && na <= 2) fn = k_dense_wide_deep[exprs - 1][na];
     uint32_t copies = 1;
     while (copies < threads / 32 && (uint64_t)copy_words * 4 * copies * 2 <= 32 * 1024) copies *= 2;
     size_t smem = (size_t)copy_words * 4 * copies;

@@ -2362,8 +2362,21 @@ extern "C" int cqlcuda_persistent_launch(CqlPersistent* p, uint32_t ctas, CqlBuf
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)p->fn, (int)p->kernel->gen_block, p->kernel->gen_smem) != cudaSuccess ||
         per_sm < 1)
     {
+      // the occupancy query may not take a library kernel handle: the same count from the kernel's registers
+      // and shared memory against one SM's 64K registers, 228 KB of shared memory and 2048 threads
       cudaGetLastError();
       per_sm = 1;
+      cudaFuncAttributes fa;
+      if (cudaFuncGetAttributes(&fa, (const void*)p->fn) == cudaSuccess && fa.numRegs > 0)
+      {
+        int block = (int)p->kernel->gen_block;
+        int warp_regs = ((fa.numRegs * 32 + 255) / 256) * 256;              // registers go to a warp in 256s
+        int by_regs = 65536 / (warp_regs * ((block + 31) / 32));
+        int by_smem = (228 * 1024) / (int)(p->kernel->gen_smem + fa.sharedSizeBytes + 1024);
+        int by_threads = 2048 / block;
+        per_sm = std::max(1, std::min(std::min(by_regs, by_smem), std::min(by_threads, 32)));
+      }
+      else cudaGetLastError();
     }
     // and one CTA's room an SM left over where four or more fit, so that other lanes' kernels still find an
     // SM while this one waits for work (with fewer, the room would cost the scan a third of its warps or more)
