@@ -1,8 +1,8 @@
 """Hash GROUP BY, HyperLogLog and t-digest through the C ABI against the oracle.
 
 Counts, whole-number sums, minimums, maximums and group membership are bit-exact; f64 sums within
-1e-12 relative; HyperLogLog estimates equal the oracle's estimate from its own registers (so the
-registers agree) and stay within the reference's 3 x 1.04 / sqrt(2^10) bound
+1e-12 relative; HyperLogLog registers equal the oracle's bit for bit (per group and global, p = 10, up to
+4M distinct values), and the estimates stay within the reference's 3 x 1.04 / sqrt(2^10) bound
 (src/tests/bench_query_approx_agg.c:174-179); t-digest percentiles within the reference's 5 %
 (:265-270); the exact edge cases 1 row -> 1 and all-identical -> 1 (:428-478).
 """
