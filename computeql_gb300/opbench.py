@@ -80,12 +80,14 @@ def run(op, rows, reps):
     rng = np.random.default_rng(0)
     if op == "sort":
         key = ops.Column.splitmix(rows, 0, 1, 0, 0)
-        fn = lambda: ops.sort_rows([key])
+        perm = np.zeros(rows, dtype=np.uint32)     # the result area kept between calls, as an engine keeps it
+        fn = lambda: ops.sort_rows([key], out=perm)
         n, nbytes = rows, rows * 4
     elif op == "sort_f64_2":
         m = ops.Column.from_numpy(_lognormal_f64(rows, 1))
         k = ops.Column.splitmix(rows, 0, 1, 0, 1000)
-        fn = lambda: ops.sort_rows([m, k], [1, 0])
+        perm = np.zeros(rows, dtype=np.uint32)
+        fn = lambda: ops.sort_rows([m, k], [1, 0], out=perm)
         n, nbytes = rows, rows * 12
     elif op == "sort_subset":
         total = 10_000_000

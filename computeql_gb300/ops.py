@@ -536,11 +536,12 @@ def join_aggregate(fact_key, funcs, fact_args, dim_keys, dim_rows=None, group_va
     return {"groups": G, "dim_row": dim_row[:G], "results": results[: G * e].reshape(G, e), "strategy": used.value}
 
 
-def sort_rows(keys, desc=None, selection=None, count=None):
+def sort_rows(keys, desc=None, selection=None, count=None, out=None):
     """ORDER BY -> row numbers in sorted order (keys compared as F64, ties by input position).
 
     `selection` is an optional DeviceBuffer of u32 row numbers (a filter's row set, `count` of them, all
-    by default); the sort then orders those rows and returns their row numbers.
+    by default); the sort then orders those rows and returns their row numbers. `out` (optional): a u32
+    array kept by the caller between calls to receive them (the result is a view of it).
     """
     kc = len(keys)
     arr = (N.CqlColumn * kc)(*[k.c() for k in keys])
@@ -550,7 +551,8 @@ def sort_rows(keys, desc=None, selection=None, count=None):
         sel = selection.handle
     else:
         n, sel = keys[0].rows, None
-    out = np.empty(max(n, 1), dtype=np.uint32)
+    if out is None or len(out) < n:
+        out = np.empty(max(n, 1), dtype=np.uint32)
     _check(N.load_ops().cqlops_sort_rows(arr, kc, N.ptr(d), sel, n, N.ptr(out), n), "cqlops_sort_rows")
     return out[:n]
 
