@@ -390,7 +390,7 @@ static const char* PERSIST_PRELUDE =
      p.buf[6 + c] the columns
    words: 0 rows, 2 R, 4 NQ, 6 SB, 8 idle limit (microseconds), 10 and 11 the first sequence number */
 static const char* PERSIST_ENTRY =
-  "extern \"C\" __global__ void __launch_bounds__(CQL_BLOCK) cql_persist(CqlLaunch p)\n{\n"
+  "extern \"C\" __global__ void __launch_bounds__(CQL_BLOCK, CQL_MIN_BLOCKS) cql_persist(CqlLaunch p)\n{\n"
   "  __shared__ CqlLaunch s_a; __shared__ u32 s_go, s_last;\n"
   "  const u64 rows = cql_word(p, 0); const u32 R = cql_word(p, 2), NQ = cql_word(p, 4), SB = cql_word(p, 6);\n"
   "  const u64 idle_ns = (u64)cql_word(p, 8) * 1000ull;\n"
@@ -448,7 +448,9 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
   memset(&b, 0, sizeof(b));
   bput(&b, "// cql: block=%u smem=%u per_sm=%u\n", block, (block / 32u) * CQL_BATCH_LAUNCH_QUERIES * 12u, register_ctas_per_sm(block));
   bput(&b, "%s", BATCH_PRELUDE);
-  if (persistent) bput(&b, "#define CQL_BLOCK %u\n%s", block, PERSIST_PRELUDE);
+  /* the persistent kernel's CTAs are all resident at once: at 4 rows a thread two of them an SM (the scan's
+     registers fit 128 a thread), which the register bound keeps */
+  if (persistent) bput(&b, "#define CQL_BLOCK %u\n#define CQL_MIN_BLOCKS %u\n%s", block, rows_per_thread <= 4 ? 2u : 1u, PERSIST_PRELUDE);
   for (uint32_t s = 0; s < shapes; s++) bput(&b, "#define CQL_SHAPE_%u(k) (%s)\n", s, shape_exprs[s]);
   if (persistent)
     bput(&b, "__device__ __forceinline__ void cql_scan(const CqlLaunch& a, const u32 cta, const u32 ctas)\n{\n");
