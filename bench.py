@@ -629,16 +629,26 @@ def run_e2e(args, native, ops, t, queries, lib, dims):
     resident = {name: _canon(q()) for name, q in by_name.items()}
     times = []
     last = {}
+    phases = {}      # per step: the wait for each slot's upload and each query, on the host clock
+
+    def phase(name, t):
+        if record:
+            phases.setdefault(name, []).append((time.perf_counter() - t) * 1e3)
     for i in range(args.warmup + max(2, args.steps // 2)):
+        record = i >= args.warmup
         t0 = time.perf_counter()
         upload(0)
         for slot, (_, names) in enumerate(plan):
+            tw = time.perf_counter()
             if not lib.cqlcuda_stream_wait(stream, slot):
                 raise RuntimeError("e2e upload failed: " + native.last_error())
+            phase(f"wait_upload_{slot}", tw)
             if slot + 1 < len(plan):
                 upload(slot + 1)
             for q in names:
+                tq = time.perf_counter()
                 last[q] = by_name[q]()
+                phase(q, tq)
         dt = time.perf_counter() - t0
         if i >= args.warmup:
             times.append(dt)
@@ -667,6 +677,7 @@ def run_e2e(args, native, ops, t, queries, lib, dims):
     d2h = 2048 * 3 * 8 + 8 + 50 * 4 * 8 + 10000 * 4 * 8 + 8 + 2 * 8 + 20 * 2 * 8
     return {"value": len(queries) * n / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "upload_ms": upload_ms, "h2d_GBps": h2d / (upload_ms / 1e3) / 1e9, "parity": e2e_parity,
+            "phases_ms": {k: round(statistics.median(v), 3) for k, v in phases.items()}, "steps_ms": [round(x * 1e3, 2) for x in times],
             "overlap": "each column's upload overlaps the queries over the columns already uploaded"}
 
 if __name__ == "__main__":
