@@ -472,7 +472,11 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
        "  u32* s_cnt = (u32*)(s_acc + (u64)warps * nq);\n"
        "  for (u32 i = threadIdx.x; i < warps * nq; i += blockDim.x) { s_acc[i] = 0ull; s_cnt[i] = 0u; }\n"
        "  __syncthreads();\n"
-       "  long long* acc = (long long*)s_acc + (u64)warp * nq; u32* cacc = s_cnt + (u64)warp * nq;\n"
+       "  long long* acc = (long long*)s_acc + (u64)warp * nq; u32* cacc = s_cnt + (u64)warp * nq;\n");
+  /* the columns' addresses in registers before the row loop (the persistent form's launch lives in shared memory) */
+  for (int sl = 0; sl < CQLOPS_MAX_BINDINGS; sl++)
+    if (slot_type[sl]) bput(&b, "  const void* const colp%d = a.buf[%d];\n", sl, 6 + sl);
+  bput(&b,
        "  const u32 RPT = %uu;\n"
        "  const u64 groups = (rows + RPT - 1ull) / RPT; const u64 per_pass = (u64)ctas * blockDim.x;\n"
        "  for (u64 g0 = (u64)cta * blockDim.x; g0 < groups; g0 += per_pass)\n  {\n"
@@ -490,14 +494,14 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
     bput(&b, "    %s r%d[%u];\n    if (!((need >> %d) & 1u)) { for (u32 v = 0; v < RPT; v++) r%d[v] = 0u; }\n", w == 8 ? "u64" : "u32", s,
          rows_per_thread, s, s);
     if (w == 8)
-      bput(&b, "    else { for (u32 v = 0; v < RPT; v++) r%d[v] = v < valid ? ((const u64*)a.buf[%d])[row0 + v] : 0ull; }\n", s, 6 + s);
+      bput(&b, "    else { for (u32 v = 0; v < RPT; v++) r%d[v] = v < valid ? ((const u64*)colp%d)[row0 + v] : 0ull; }\n", s, s);
     else if (w == 1)
-      bput(&b, "    else { for (u32 v = 0; v < RPT; v++) r%d[v] = v < valid ? (u32)((const unsigned char*)a.buf[%d])[row0 + v] : 0u; }\n", s, 6 + s);
+      bput(&b, "    else { for (u32 v = 0; v < RPT; v++) r%d[v] = v < valid ? (u32)((const unsigned char*)colp%d)[row0 + v] : 0u; }\n", s, s);
     else
       bput(&b,
-           "    else if (valid == RPT && (RPT & 3u) == 0u) { for (u32 v = 0; v < RPT; v += 4) { uint4 q = cql_ld4((const u32*)a.buf[%d] + row0 + v); r%d[v] = q.x; r%d[v + 1] = q.y; r%d[v + 2] = q.z; r%d[v + 3] = q.w; } }\n"
-           "    else { for (u32 v = 0; v < RPT; v++) r%d[v] = v < valid ? ((const u32*)a.buf[%d])[row0 + v] : 0u; }\n",
-           6 + s, s, s, s, s, s, 6 + s);
+           "    else if (valid == RPT && (RPT & 3u) == 0u) { for (u32 v = 0; v < RPT; v += 4) { uint4 q = cql_ld4((const u32*)colp%d + row0 + v); r%d[v] = q.x; r%d[v + 1] = q.y; r%d[v + 2] = q.z; r%d[v + 3] = q.w; } }\n"
+           "    else { for (u32 v = 0; v < RPT; v++) r%d[v] = v < valid ? ((const u32*)colp%d)[row0 + v] : 0u; }\n",
+           s, s, s, s, s, s, s);
   }
   /* the order keys of the f64 columns, once per row (every query's comparisons read them) */
   for (int s = 0; s < CQLOPS_MAX_BINDINGS; s++)
