@@ -1467,6 +1467,17 @@ static int batch_run(CqlBatchCatalog* catalog, const CqlProgram* const* programs
     if (col->rows != rows || (!col->buffer && mode == BATCH_RUN) || col->width != 0 || col->type == CQLOPS_TYPE_STRING8)
       return refuse("batched columns are full-width numeric columns of one length");
   }
+  if (rows == 0 && (mode == BATCH_RUN || mode == BATCH_PERSIST))
+  {
+    /* an empty table: every query counts 0 rows and sums nothing (no device work) */
+    for (uint32_t q = 0; q < query_count; q++)
+    {
+      out_counts[q] = 0;
+      if (out_sums) out_sums[q] = 0.0;
+    }
+    if (out_shapes) *out_shapes = 0;
+    return 1;
+  }
   /* per query: rebound program, shape, thresholds, literals */
   CqlProgram* rb = (CqlProgram*)malloc(sizeof(CqlProgram));
   uint32_t* shape_of = (uint32_t*)malloc(query_count * 4);

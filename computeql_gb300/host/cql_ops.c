@@ -392,6 +392,12 @@ int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const Cq
       return 0;
     }
   }
+  if (rows == 0)
+  {
+    /* an empty table matches nothing: no device work */
+    if (out_count) *out_count = 0;
+    return 1;
+  }
   CqlKernel* k = kernel_named("scan_simple");
   if (!k)
   {
@@ -530,6 +536,13 @@ static int group_dense_run(const CqlColumn* key, uint64_t rows, uint32_t expr_co
 {
   launches_begin();
   if (!cqlops_rows_fit(rows)) return 0;
+  if (rows == 0 && !device_out && key && key->rows == 0)
+  {
+    /* an empty table has no groups (no device work) */
+    if (out_group_count) *out_group_count = 0;
+    if (out_min_key) *out_min_key = 0;
+    return 1;
+  }
   /* a dictionary string column groups by its codes, as the reference's dictionary GROUP BY does */
   int dict_key = key && key->type == CQLOPS_TYPE_STRING8 && key->dict && key->width == 0;
   if (!key || !key->has_range || !(key->type == CQLOPS_TYPE_U32 || key->type == CQLOPS_TYPE_I32 || dict_key) || key->rows != rows || !key->buffer ||

@@ -233,6 +233,13 @@ static int scan_filter_run(const CqlProgram* prog, const CqlColumn* columns, uin
     strategy = CQLOPS_SCAN_INTERPRETER;
   }
   uint64_t rows = program_rows(prog, columns, 0);
+  if (rows == 0)
+  {
+    /* an empty table matches nothing: no device work */
+    if (out_count) *out_count = 0;
+    if (out_strategy) *out_strategy = strategy == CQLOPS_SCAN_AUTO ? CQLOPS_SCAN_INTERPRETER : strategy;
+    return 1;
+  }
 
   if (strategy == CQLOPS_SCAN_AUTO || strategy == CQLOPS_SCAN_SIMPLE)
   {
@@ -394,6 +401,19 @@ int cqlops_fused_filter_aggregate(const CqlProgram* prog_in, const CqlColumn* co
     }
   }
 
+  if (ok && program_rows(prog, columns, 0) == 0)
+  {
+    /* an empty table: no matched rows, sums 0 and the fold's starting extremes (no device work) */
+    if (out_count) *out_count = 0.0;
+    for (uint32_t c = 0; c < agg_count; c++)
+    {
+      if (out_sum) out_sum[c] = 0.0;
+      if (out_min) out_min[c] = 1.7976931348623157e308;
+      if (out_max) out_max[c] = -1.7976931348623157e308;
+    }
+    free(prog);
+    return 1;
+  }
   CqlKernel* k = ok ? generated_kernel(prog, CQLOPS_KERNEL_FUSED_AGG, &fuse) : NULL;
   CqlBuffer *code = NULL, *consts = NULL, *strs = NULL;
   if (k) ok = upload_program(prog, &code, &consts, &strs);
@@ -470,6 +490,17 @@ int cqlops_fused_filter_group(const CqlProgram* prog_in, const CqlColumn* column
   if (key_count == 0 || key_count > 3 || agg_count > 4) return refuse("1 to 3 keys and at most 4 aggregate columns");
   if (prog_in->requires_cpu_scan || prog_in->has_score_output) return refuse("the program needs the CPU scan");
   if (!program_rows_fit(prog_in, columns)) return 0;
+  if (columns[key_columns[0]].rows == 0)
+  {
+    /* an empty table has no groups (no device work) */
+    if (out_group_total) *out_group_total = 0;
+    for (uint32_t k = 0; k < key_count; k++)
+    {
+      if (out_key_min) out_key_min[k] = 0;
+      if (out_key_range) out_key_range[k] = 0;
+    }
+    return 1;
+  }
   CqlProgram* prog = (CqlProgram*)malloc(sizeof(CqlProgram));
   if (!prog) return 0;
   memcpy(prog, prog_in, sizeof(CqlProgram));

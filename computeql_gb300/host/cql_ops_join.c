@@ -78,6 +78,18 @@ int cqlops_hash_join(const CqlColumn* build_key, const CqlColumn* probe_key, int
   cqlops_note_error("");
   uint64_t brows = build_key->rows, prows = probe_key->rows;
   if (!cqlops_rows_fit(brows) || !cqlops_rows_fit(prows)) return 0;
+  if (prows == 0 || brows == 0)
+  {
+    /* an empty side, no device work: no pairs, or under LEFT every probe row unmatched (build row EMPTY) */
+    uint64_t produced = (brows == 0 && left_join) ? prows : 0;
+    for (uint64_t r = 0; out_pairs && r < produced && r < out_capacity; r++)
+    {
+      out_pairs[2 * r] = (uint32_t)r;
+      out_pairs[2 * r + 1] = 0xffffffffu;
+    }
+    *out_count = produced;
+    return 1;
+  }
   CqlBuffer *bd, *bo, *pd, *po;
   int bstr, pstr;
   if (!join_key(build_key, "hj_build_f64", &bd, &bo, &bstr) || !join_key(probe_key, "hj_probe_f64", &pd, &po, &pstr)) return 0;
@@ -1158,6 +1170,13 @@ int cqlops_join_aggregate(const CqlJoinAgg* q, uint64_t max_groups, uint64_t* ou
   const CqlColumn* core_cols[8];
   uint32_t core_count = 0, core_of_expr[8];
   if (!join_core_plan(q, core_funcs, core_cols, &core_count, core_of_expr)) return 0;
+  if (fk->rows == 0 || (q->dim_rows && q->dim_count == 0) || q->dim_table_rows == 0)
+  {
+    /* no fact rows, or no dim rows kept: the join has no rows and so no groups (no device work) */
+    *out_groups = 0;
+    if (out_strategy) *out_strategy = 0;
+    return 1;
+  }
   /* totals per key: dense over a small key range, else per dim row by probing (:8607-8617) */
   uint64_t groups_cap = fk->has_range ? (uint64_t)(fk->zone_max - fk->zone_min) + 1 : 0;
   /* a mid-sized key range: through a lookup table on the device when the dim side allows it */
