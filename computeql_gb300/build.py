@@ -70,7 +70,7 @@ def _compile_c(src):
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     if not _stale(obj, [src] + _headers()):
         return obj
-    _run(["gcc", "-std=c99", "-O2", "-ffp-contract=off", "-fPIC", "-Wall", "-Wno-unused-function", "-I", INCLUDE, "-I", HOST, "-c", src, "-o", obj])
+    _run(["gcc", "-std=c99", "-O2", "-ffp-contract=off", "-fPIC", "-Wall", "-Wno-unused-function", "-Werror=implicit-function-declaration", "-I", INCLUDE, "-I", HOST, "-c", src, "-o", obj])
     return obj
 
 

@@ -23,6 +23,7 @@
  */
 #define _POSIX_C_SOURCE 200809L
 #include "cqlops.h"
+#include "cql_ops_internal.h"
 #include "cql_codegen.h"
 
 #include <math.h>
@@ -40,10 +41,6 @@
 #define BATCH_CTAS_PER_SM 6
 #define BATCH_MAX_SHAPES 256
 #define CQL_BATCH_CATALOG_SHAPES 64
-
-void cqlops_note_error(const char* why);
-
-int cqlops_rows_fit(uint64_t rows);
 
 static int refuse(const char* why)
 {

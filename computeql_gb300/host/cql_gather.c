@@ -9,6 +9,7 @@
  * then a warp per row copies the bytes.
  */
 #include "cqlops.h"
+#include "cql_ops_internal.h"
 
 #include <stdio.h>
 #include <stdlib.h>
@@ -16,10 +17,6 @@
 
 #define GATHER_COLUMNS 13
 #define QE_GPU_WORKGROUP_SIZE 256
-
-void cqlops_note_error(const char* why);
-
-int cqlops_rows_fit(uint64_t rows);
 
 static int refuse(const char* why)
 {

@@ -9,6 +9,7 @@
  * checked first: only those names, numbers, operators and a few math functions may appear.
  */
 #include "cqlops.h"
+#include "cql_ops_internal.h"
 
 #include <ctype.h>
 #include <stdio.h>
@@ -17,8 +18,6 @@
 
 #define HAVING_MAX_COLUMNS 8
 #define HAVING_MAX_LITERALS 16
-
-void cqlops_note_error(const char* why);
 
 static int refuse(const char* why)
 {

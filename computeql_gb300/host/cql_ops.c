@@ -4,6 +4,7 @@
  * device-resident columns.
  */
 #include "cqlops.h"
+#include "cql_ops_internal.h"
 
 #include <math.h>
 #include <stdio.h>
@@ -497,19 +498,6 @@ int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const Cq
 
 /* ------------------------------------------------------------------------------------------------
  * Dense GROUP BY: qe_dense_stream_core (query_exec.c:7632-7983) on one chunk */
-
-/* The dense group-by's totals left on the device: info (u32 pairs, word 1 the count) at 0, sums (u32 lo/hi
-   pairs per group and expression) at sum_at, MIN and MAX (i32 per group and expression) at min_at / max_at
-   (filled with INT32_MAX / INT32_MIN when no expression is MIN/MAX). */
-typedef struct
-{
-  CqlBuffer* buffer;
-  uint64_t sum_at, min_at, max_at;
-  uint64_t group_count;
-  int64_t min_key;
-  int keep_open;      /* in: leave the batch open for the caller's next operations */
-  CqlBatch* batch;    /* out (keep_open): that batch, which the caller ends */
-} CqlDenseTotals;
 
 static int group_dense_run(const CqlColumn* key, uint64_t rows, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* arg_cols,
                            uint64_t max_groups, uint64_t* out_group_count, int64_t* out_min_key, uint64_t* out_counts, int64_t* out_sums,

@@ -12,6 +12,7 @@
  * :1683-1726): the scan then runs on the interpreter.
  */
 #include "cqlops.h"
+#include "cql_ops_internal.h"
 
 #include <pthread.h>
 #include <stdio.h>
@@ -31,7 +32,6 @@ static pthread_mutex_t g_failed_lock = PTHREAD_MUTEX_INITIALIZER;
 static uint64_t g_failed[FAILED_CAP];
 static uint32_t g_failed_count = 0;
 static uint64_t g_generated_requests = 0, g_generated_failures = 0;
-void cqlops_note_error(const char* why);
 int cqlops_bitmap_rows(CqlBuffer* bitmap, uint64_t first_row, uint64_t rows, uint64_t count, uint32_t* out_rows, uint64_t cap);
 
 void cqlops_generated_stats(uint64_t* out_requests, uint64_t* out_failures)
@@ -41,10 +41,6 @@ void cqlops_generated_stats(uint64_t* out_requests, uint64_t* out_failures)
   if (out_failures) *out_failures = g_generated_failures;
   pthread_mutex_unlock(&g_failed_lock);
 }
-
-int cqlops_rows_fit(uint64_t rows);
-int cqlops_sort_pairs(CqlBuffer* records, uint64_t n, uint32_t stride_words, uint32_t first_word, uint32_t second_word, int by_second,
-                      uint32_t* out, uint64_t out_capacity);
 
 /* every column the program binds fits the kernels' 32-bit row numbers */
 static int program_rows_fit(const CqlProgram* prog, const CqlColumn* columns)

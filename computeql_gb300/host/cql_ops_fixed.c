@@ -11,6 +11,7 @@
  * f64/f32 arguments) and the key range and the scales come from two small reduction kernels.
  */
 #include "cqlops.h"
+#include "cql_ops_internal.h"
 
 #include <stdio.h>
 #include <stdlib.h>
@@ -22,10 +23,6 @@
 #define DENSE_FIXED_MAX_WORDS 51200u
 
 static const double g_pow10[QE_FIXED_MAX_SCALE + 1] = { 1.0, 10.0, 100.0, 1000.0, 10000.0, 100000.0, 1000000.0 };
-
-void cqlops_note_error(const char* why);
-
-int cqlops_rows_fit(uint64_t rows);
 
 static int refuse(const char* why)
 {

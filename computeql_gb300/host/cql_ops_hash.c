@@ -13,6 +13,7 @@
  *      qe_tdigest_estimate_percentile (:6748-6790)
  */
 #include "cqlops.h"
+#include "cql_ops_internal.h"
 
 #include <math.h>
 #include <stdio.h>
@@ -28,9 +29,6 @@
 #define AGG_MANY_GROUPS 4096
 #define HLL_PRECISION 10
 #define HLL_SKETCH_MAX_BYTES (64ull << 20)
-
-
-void cqlops_note_error(const char* why);
 
 /* The HyperLogLog registers of the calling thread's last hash GROUP BY, [group][hll expression][2^p] */
 static __thread uint32_t* tl_hll_regs = NULL;
@@ -48,8 +46,6 @@ static void keep_hll_registers(uint32_t* regs, uint64_t words)
   tl_hll_regs = regs;
   tl_hll_words = regs ? words : 0;
 }
-
-int cqlops_rows_fit(uint64_t rows);
 
 static int refuse(const char* why)
 {

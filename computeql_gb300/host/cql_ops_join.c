@@ -12,6 +12,7 @@
  *                         meets its key's totals and is folded into a group of its group columns on the host
  */
 #include "cqlops.h"
+#include "cql_ops_internal.h"
 #include "cql_pool.h"
 
 #include <math.h>
@@ -21,12 +22,6 @@
 
 #define QE_GPU_WORKGROUP_SIZE 256
 #define PROBE_STREAM_MAX_DIM_ROWS (1ull << 26)
-
-void cqlops_note_error(const char* why);
-
-int cqlops_rows_fit(uint64_t rows);
-int cqlops_sort_pairs(CqlBuffer* records, uint64_t n, uint32_t stride_words, uint32_t first_word, uint32_t second_word, int by_second,
-                      uint32_t* out, uint64_t out_capacity);
 
 static int refuse(const char* why)
 {
@@ -965,19 +960,6 @@ static int join_finish(const CqlJoinAgg* q, JoinTotals* t, const uint32_t* core_
 }
 
 /* ---- the dim-row pass on the device, for a dense join over a dim table resident on the device ---- */
-
-typedef struct
-{
-  CqlBuffer* buffer;
-  uint64_t sum_at, min_at, max_at;
-  uint64_t group_count;
-  int64_t min_key;
-  int keep_open;      /* in: leave the batch open for the caller's next operations */
-  CqlBatch* batch;    /* out (keep_open): that batch, which the caller ends */
-} CqlDenseTotals;
-
-int cql_group_dense_device(const CqlColumn* key, uint64_t rows, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* arg_cols,
-                           uint64_t max_groups, CqlDenseTotals* out);
 
 typedef struct
 {

@@ -4,6 +4,7 @@
  * as a stable LSD radix sort on the GPU: the last key first, each key 8 bits per pass.
  */
 #include "cqlops.h"
+#include "cql_ops_internal.h"
 
 #include <stdio.h>
 #include <stdlib.h>
@@ -11,10 +12,6 @@
 
 #define SORT_TILE 4096
 #define QE_GPU_WORKGROUP_SIZE 256
-
-void cqlops_note_error(const char* why);
-
-int cqlops_rows_fit(uint64_t rows);
 
 static int refuse(const char* why)
 {

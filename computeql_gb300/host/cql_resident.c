@@ -16,6 +16,7 @@
  * backend's and never the other way round; freed buffers are collected under the lock and released after.
  */
 #include "cqlops.h"
+#include "cql_ops_internal.h"
 
 #include <pthread.h>
 #include <stdlib.h>
@@ -356,9 +357,6 @@ CqlResidentStats cqlops_resident_stats(CqlResident* r)
   pthread_mutex_unlock(&r->lock);
   return s;
 }
-
-void cqlops_note_error(const char* why);
-int cqlops_rows_fit(uint64_t rows);
 
 static int refuse(const char* why)
 {

@@ -18,6 +18,7 @@
  */
 #define _GNU_SOURCE
 #include "cqlserve.h"
+#include "cql_ops_internal.h"
 
 #include <pthread.h>
 #include <stdio.h>
@@ -566,8 +567,6 @@ CqlServeStats cqlserve_stats(CqlServer* sv)
 }
 
 /* ---- ready-made call requests ---- */
-
-void cqlops_note_error(const char* why);
 
 int cqlserve_join_call(void* ctx)
 {

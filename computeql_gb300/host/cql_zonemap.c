@@ -10,6 +10,7 @@
  * rows z*8192 .. z*8192+8191, so `id = k` keeps the one chunk holding row k.
  */
 #include "cqlops.h"
+#include "cql_ops_internal.h"
 
 #include <math.h>
 #include <stdlib.h>
@@ -20,10 +21,6 @@
 #define QE_SCAN_MIN_PRUNE_GAP_ROWS 1048576ull
 #define QE_SCAN_MIN_PRUNE_PERCENT 10ull
 #define QE_SCAN_RANGE_COST_ROWS 4194304ull
-
-void cqlops_note_error(const char* why);
-
-int cqlops_rows_fit(uint64_t rows);
 
 static int refuse(const char* why)
 {
