@@ -65,52 +65,58 @@ static int sort_enqueue(CqlBatch* b, const CqlColumn* keys, uint32_t key_count, 
   CqlBuffer* perm[2] = { pooled("sort_perm_a", n * 4, CQLCUDA_BUFFER_READ_WRITE), pooled("sort_perm_b", n * 4, CQLCUDA_BUFFER_READ_WRITE) };
   CqlBuffer* kbuf[2] = { pooled("sort_keys_a", n * widest, CQLCUDA_BUFFER_READ_WRITE), pooled("sort_keys_b", n * widest, CQLCUDA_BUFFER_READ_WRITE) };
   CqlBuffer* hist = pooled("sort_hist", hist_n * 4, CQLCUDA_BUFFER_READ_WRITE);
-  CqlBuffer* offsets = pooled("sort_offsets", (hist_n + 1) * 4, CQLCUDA_BUFFER_READ_WRITE);
-  CqlBuffer* cursor = pooled("sort_cursor", hist_n * 4, CQLCUDA_BUFFER_READ_WRITE);
-  CqlBuffer* block_sums = pooled("sort_block_sums", ((hist_n + 255) / 256) * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* offsets = pooled("sort_offsets", hist_n * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* totals = pooled("sort_digit_totals", 8 * 256 * 4, CQLCUDA_BUFFER_READ_WRITE);
   CqlKernel* kkeys = cqlcuda_kernel_alloc("cql_sort_keys", 13);
   CqlKernel* kcount = cqlcuda_kernel_alloc("cql_radix_count", 15);
-  CqlKernel* kscan = cqlcuda_kernel_alloc("prefix_sum", 10);
+  CqlKernel* koffsets = cqlcuda_kernel_alloc("cql_radix_offsets", 17);
   CqlKernel* kscatter = cqlcuda_kernel_alloc("cql_radix_scatter", 17);
-  if (!perm[0] || !perm[1] || !kbuf[0] || !kbuf[1] || !hist || !offsets || !cursor || !block_sums || !kkeys || !kcount || !kscan || !kscatter)
+  if (!perm[0] || !perm[1] || !kbuf[0] || !kbuf[1] || !hist || !offsets || !totals || !kkeys || !kcount || !koffsets || !kscatter)
     return 0;
   CqlBuffer* sel = selection ? selection : perm[0];
   int cur = 0;
   for (int k = (int)key_count - 1; k >= 0; k--)
   {
     int kb = key_bytes(keys[k].type);
-    /* the key in the current order (the first key sorted builds the identity permutation) */
+    int first_key = k == (int)key_count - 1;
+    /* each pass's digit totals start at zero: the key pass counts the first digit, the count kernels the rest */
+    cqlcuda_batch_fill_range(b, totals, 0, (uint64_t)kb * 256 * 4, 0);
+    /* the key in the current order, with its first digit counted (the first key sorted starts from the
+       identity permutation, which the first scatter takes as row numbers) */
     cqlcuda_kernel_set_arg_buffer(kkeys, 0, keys[k].buffer ? keys[k].buffer : perm[cur]);
     cqlcuda_kernel_set_arg_buffer(kkeys, 1, perm[cur]);
     cqlcuda_kernel_set_arg_buffer(kkeys, 2, kbuf[cur]);
     cqlcuda_kernel_set_arg_buffer(kkeys, 3, sel);
+    cqlcuda_kernel_set_arg_buffer(kkeys, 4, hist);
+    cqlcuda_kernel_set_arg_buffer(kkeys, 5, totals);
     cqlcuda_kernel_set_arg_u64(kkeys, 0, n);
     cqlcuda_kernel_set_arg_u64(kkeys, 1, keys[k].type);
     cqlcuda_kernel_set_arg_u64(kkeys, 2, desc && desc[k] ? 1 : 0);
-    cqlcuda_kernel_set_arg_u64(kkeys, 3, k == (int)key_count - 1 ? 0 : 1);
+    cqlcuda_kernel_set_arg_u64(kkeys, 3, first_key ? 0 : 1);
     cqlcuda_kernel_set_arg_u64(kkeys, 4, selection ? 1 : 0);
     cqlcuda_kernel_set_arg_u64(kkeys, 5, keys[k].width);
     cqlcuda_kernel_set_arg_u64(kkeys, 6, keys[k].base);
+    cqlcuda_kernel_set_arg_u64(kkeys, 7, first_key ? 3 : 1);
     cqlcuda_batch_kernel_execute(b, kkeys, (uint32_t)n, QE_GPU_WORKGROUP_SIZE);
     for (int p = 0; p < kb; p++)
     {
       int last = k == 0 && p == kb - 1;
-      cqlcuda_kernel_set_arg_buffer(kcount, 0, kbuf[cur]);
-      cqlcuda_kernel_set_arg_buffer(kcount, 1, hist);
-      cqlcuda_kernel_set_arg_u64(kcount, 0, n);
-      cqlcuda_kernel_set_arg_u64(kcount, 1, (uint64_t)(8 * p));
-      cqlcuda_kernel_set_arg_u64(kcount, 2, (uint64_t)kb);
-      cqlcuda_batch_kernel_execute(b, kcount, (uint32_t)(tiles * 256), 256);
-      cqlcuda_kernel_set_arg_buffer(kscan, 0, hist);
-      cqlcuda_kernel_set_arg_buffer(kscan, 1, offsets);
-      cqlcuda_kernel_set_arg_buffer(kscan, 2, cursor);
-      cqlcuda_kernel_set_arg_buffer(kscan, 3, block_sums);
-      cqlcuda_kernel_set_arg_u64(kscan, 0, hist_n);
-      for (uint32_t mode = 0; mode < 3; mode++)
+      uint64_t pass_totals = (uint64_t)p * 256 * 4;
+      if (p > 0)
       {
-        cqlcuda_kernel_set_arg_u64(kscan, 1, mode);
-        cqlcuda_batch_kernel_execute(b, kscan, mode == 1 ? 256u : (uint32_t)(((hist_n + 255) / 256) * 256), 256);
+        cqlcuda_kernel_set_arg_buffer(kcount, 0, kbuf[cur]);
+        cqlcuda_kernel_set_arg_buffer(kcount, 1, hist);
+        cqlcuda_kernel_set_arg_buffer_range(kcount, 2, totals, pass_totals, 256 * 4);
+        cqlcuda_kernel_set_arg_u64(kcount, 0, n);
+        cqlcuda_kernel_set_arg_u64(kcount, 1, (uint64_t)(8 * p));
+        cqlcuda_kernel_set_arg_u64(kcount, 2, (uint64_t)kb);
+        cqlcuda_batch_kernel_execute(b, kcount, (uint32_t)(tiles * 256), 256);
       }
+      cqlcuda_kernel_set_arg_buffer(koffsets, 0, hist);
+      cqlcuda_kernel_set_arg_buffer_range(koffsets, 1, totals, pass_totals, 256 * 4);
+      cqlcuda_kernel_set_arg_buffer(koffsets, 2, offsets);
+      cqlcuda_kernel_set_arg_u64(koffsets, 0, n);
+      cqlcuda_batch_kernel_execute(b, koffsets, 256u * 512u, 512);
       cqlcuda_kernel_set_arg_buffer(kscatter, 0, kbuf[cur]);
       cqlcuda_kernel_set_arg_buffer(kscatter, 1, perm[cur]);
       cqlcuda_kernel_set_arg_buffer(kscatter, 2, kbuf[cur ^ 1]);
@@ -122,6 +128,7 @@ static int sort_enqueue(CqlBatch* b, const CqlColumn* keys, uint32_t key_count, 
       cqlcuda_kernel_set_arg_u64(kscatter, 2, (uint64_t)kb);
       cqlcuda_kernel_set_arg_u64(kscatter, 3, last && selection ? 1 : 0);
       cqlcuda_kernel_set_arg_u64(kscatter, 4, last ? 1 : 0);
+      cqlcuda_kernel_set_arg_u64(kscatter, 5, first_key && p == 0 ? 1 : 0);
       cqlcuda_batch_kernel_execute(b, kscatter, (uint32_t)(tiles * 256), 256);
       cur ^= 1;
     }
