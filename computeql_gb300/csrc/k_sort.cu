@@ -22,7 +22,8 @@
 //  cql_radix_scatter  binding 0 keys in, 1 positions in, 2 keys out, 3 positions out, 4 offsets,
 //                     5 selection; word 0 n, word 2 bit shift, word 4 key bytes, word 6 1 = write the
 //                     selection's row instead of the position, word 8 1 = write no keys (the last pass),
-//                     word 10 1 = the positions in are the row numbers (binding 1 is not read)
+//                     word 10 1 = the positions in are the row numbers (binding 1 is not read); binding 6
+//                     (optional) the pass's digit totals: one digit holding all n rows makes the pass a copy
 //  cql_pairs_unpack   binding 0 records (u32 words), 1 first out, 2 second out; word 0 n, word 2 words per
 //                     record, word 4 the first's word offset, word 6 the second's
 //  cql_pairs_pack     binding 0 sorted positions, 1 first, 2 second, 3 pairs out (first, second); word 0 n
@@ -461,15 +462,50 @@ __device__ __forceinline__ void scatter_tile(const CqlLaunch& a, ScatterShared& 
   __syncthreads();
 }
 
+// A pass whose digit is the same for every row (a byte that does not vary) leaves the order as it is: the
+// keys and positions are copied through, with no ranking.
+template <typename K>
+__device__ __forceinline__ void pass_copy(const CqlLaunch& a, uint64_t n, bool map_rows, bool write_keys, bool identity)
+{
+  const K* keys_in = (const K*)a.buf[0];
+  const uint32_t* pos_in = (const uint32_t*)a.buf[1];
+  K* keys_out = (K*)a.buf[2];
+  uint32_t* pos_out = (uint32_t*)a.buf[3];
+  const uint32_t* sel = (const uint32_t*)a.buf[5];
+  uint64_t stride = (uint64_t)gridDim.x * SORT_THREADS;
+#pragma unroll 4
+  for (uint64_t i = (uint64_t)blockIdx.x * SORT_THREADS + threadIdx.x; i < n; i += stride)
+  {
+    if (write_keys) keys_out[i] = keys_in[i];
+    uint32_t p = identity ? (uint32_t)i : pos_in[i];
+    pos_out[i] = map_rows ? sel[p] : p;
+  }
+}
+
 template <typename K, int FORM>
-__global__ void __launch_bounds__(SORT_THREADS, SORT_SCATTER_CTAS(K)) k_radix_scatter(CqlLaunch a, uint64_t n, uint32_t tiles)
+__global__ void __launch_bounds__(SORT_THREADS, SORT_SCATTER_CTAS(K)) k_radix_scatter(CqlLaunch a, uint64_t n, uint32_t tiles, bool has_totals)
 {
   __shared__ ScatterShared sh;
+  __shared__ uint32_t s_one_digit;
   extern __shared__ __align__(16) unsigned char s_tile[];
   K* s_key = (K*)s_tile;
   uint32_t* s_pos = (uint32_t*)(s_tile + sizeof(K) * SORT_TILE);
   uint32_t shift = cql_word(a, 2);
   bool map_rows = cql_word(a, 6) != 0, write_keys = cql_word(a, 8) == 0, identity = cql_word(a, 10) != 0;
+  if (has_totals)
+  {
+    // the pass's digit totals: one digit holding every row makes the pass a copy
+    const uint32_t* totals = (const uint32_t*)a.buf[6];
+    if (threadIdx.x == 0) s_one_digit = 0;
+    __syncthreads();
+    if (totals[threadIdx.x] == (uint32_t)n) s_one_digit = 1;  // RADIX == SORT_THREADS; n < 2^32
+    __syncthreads();
+    if (s_one_digit)
+    {
+      pass_copy<K>(a, n, map_rows, write_keys, identity);
+      return;
+    }
+  }
   uint32_t full_tiles = (uint32_t)(n / SORT_TILE);
   for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x)
   {
@@ -588,8 +624,9 @@ static int launch_radix_scatter(const CqlLaunch& a, uint32_t gws, uint32_t lws, 
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   uint32_t grid = cql_stream_grid(tiles, resident_ctas(fn, smem));
-  if (kb == 4) k_radix_scatter<uint32_t, SORT_RANK_FORM><<<grid, SORT_THREADS, smem, stream>>>(a, n, tiles);
-  else k_radix_scatter<unsigned long long, SORT_RANK_FORM><<<grid, SORT_THREADS, smem, stream>>>(a, n, tiles);
+  bool has_totals = a.buf[6] != nullptr && a.bytes[6] >= RADIX * 4;
+  if (kb == 4) k_radix_scatter<uint32_t, SORT_RANK_FORM><<<grid, SORT_THREADS, smem, stream>>>(a, n, tiles, has_totals);
+  else k_radix_scatter<unsigned long long, SORT_RANK_FORM><<<grid, SORT_THREADS, smem, stream>>>(a, n, tiles, has_totals);
   CQL_LAUNCH_CHECK();
   return 0;
 }

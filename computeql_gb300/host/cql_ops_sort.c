@@ -123,6 +123,7 @@ static int sort_enqueue(CqlBatch* b, const CqlColumn* keys, uint32_t key_count, 
       cqlcuda_kernel_set_arg_buffer(kscatter, 3, perm[cur ^ 1]);
       cqlcuda_kernel_set_arg_buffer(kscatter, 4, offsets);
       cqlcuda_kernel_set_arg_buffer(kscatter, 5, sel);
+      cqlcuda_kernel_set_arg_buffer_range(kscatter, 6, totals, pass_totals, 256 * 4);
       cqlcuda_kernel_set_arg_u64(kscatter, 0, n);
       cqlcuda_kernel_set_arg_u64(kscatter, 1, (uint64_t)(8 * p));
       cqlcuda_kernel_set_arg_u64(kscatter, 2, (uint64_t)kb);

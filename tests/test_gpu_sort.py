@@ -105,6 +105,24 @@ def test_all_equal_keys_keep_input_order(ops):
     assert np.array_equal(ops.sort_rows([ops.Column.from_numpy(v)], [1]), np.arange(100000))
 
 
+@pytest.mark.parametrize("desc", [0, 1])
+def test_passes_whose_digit_does_not_vary(ops, desc):
+    # u32 keys below 2^24 (the high byte's pass is a copy), whole-number f64 keys (the low mantissa bytes'
+    # passes are copies), and both under a row selection, whose last pass maps positions to its rows
+    rng = np.random.default_rng(31 + desc)
+    n = 300001
+    small = rng.integers(0, 1 << 24, n).astype(np.uint32)
+    whole = rng.integers(-5000, 5000, n).astype(np.float64)
+    for v in (small, whole):
+        got = ops.sort_rows([ops.Column.from_numpy(v)], [desc])
+        assert np.array_equal(got, oracle.sort_rows([v], [desc]))
+    sel = np.sort(rng.choice(n, 70001, replace=False)).astype(np.uint32)
+    buf = ops.DeviceBuffer(sel.nbytes, sel)
+    got = ops.sort_rows([ops.Column.from_numpy(whole), ops.Column.from_numpy(small)], [desc, 0], selection=buf)
+    want = sel[oracle.sort_rows([whole[sel], small[sel]], [desc, 0])]
+    assert np.array_equal(got, want)
+
+
 def test_filtered_subset_f64_measure(ops):
     # a 10M-row table with a lognormal f64 measure; ORDER BY it over the ~200k rows a filter keeps
     rng = np.random.default_rng(9)
