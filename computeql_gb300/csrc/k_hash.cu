@@ -957,92 +957,335 @@ static int launch_group_finish(const CqlLaunch& a, uint32_t gws, uint32_t lws, c
 }
 
 // ---------------------------------------------------------------------------------------------
-// cql_small_key_extrema: for each value of a small-range whole-number key (at most 64 values), its first
-// row and the MIN and MAX of up to 4 columns: binding 0 the key column (u32 words, full width), 1 first
-// row per value (u32, all 0xffffffff before), 2 per value and column the (min, max) as f64 order keys
-// (u64 pairs, min all ones and max all zeros before), 3..6 the columns; word 0 rows, word 2 the smallest
-// key (bits), word 4 the range, word 6 the columns, word 8 their CQL types (4 bits each: U32, I32, F32,
-// F64). NaN values are skipped, as `v < min` skips them. Each CTA keeps its extrema in shared memory and
-// takes an atomic only when a value beats the one held, which after the first rows is seldom.
+// cql_group_small: GROUP BY a small-range whole-number key (at most 64 values) in one pass over the key
+// and up to 8 argument columns: per value of the key its row count, first row, and per column the exact
+// SUM and the MIN and MAX.
+//
+// A SUM is exact in fixed point: each value x of a column becomes the whole number q = round(x * 2^s),
+// with s chosen from the column's range so that |q| < 2^61 (s = 0 for whole-number columns, which are then
+// exact), and the q are added as 96-bit two's-complement numbers in three 32-bit limbs (shared atomics
+// with the carries passed up, as the dense group-by's 64-bit sums do), then as 128-bit numbers in the
+// output. The host turns the total back into a double, rounding once: the f64 SUM is the exact sum of the
+// values rounded to 2^-s, whose error is below rows * 2^(E-62) for values below 2^E - far inside the
+// 1e-12 the sum is held to, and independent of the order the rows are met in. NaN and infinite values are
+// kept out of the sum and flagged (NaN 1, +inf 2, -inf 4), so that the host gives the IEEE result.
+//
+// binding 0 the key (u32 words), 1..8 the argument columns, 9 the output (u32 words, for V key values):
+//   [0, 2V)           the counts (u64)
+//   [2V, 3V)          the first rows (u32; all 0xffffffff before)
+//   S = 3V + (V & 1)  per (value, column) 4 words: the sum as a 128-bit two's-complement number
+//   S + 32V           per (value, column) the flags
+//   S + 40V           per (value, column) the (min, max) as f64 order keys (u64 pairs; min all ones and max
+//                     zero before)
+// words: 0 rows, 2 the smallest key (bits), 4 V, 6 the columns, 8 their CQL types (4 bits each: U32, I32,
+// F32, F64), 10 per column 1 = SUM (bits 0-7) and 1 = MIN/MAX (bits 8-15), slots 6 and 7 the columns'
+// scales s (signed 16 bits each, columns 0-3 then 4-7). Dynamic shared memory: `copies` private tables of V counts and 3 limbs per
+// summed column and value; with one table a thread (OWN) they are updated without atomics.
 
-#define EXTREMA_VALUES 64
-#define EXTREMA_COLUMNS 4
+#define SMALL_VALUES 64
+#define SMALL_COLUMNS 8
+#define SMALL_ROWS 4
 
-__device__ __forceinline__ unsigned long long extrema_key(const void* col, uint32_t type, uint64_t r, bool* ok)
+// The per-row work is integer work on the values' IEEE bits (GB300's FP64 pipe is a small fraction of its
+// integer and FP32 rate): a value becomes the bits of its double, then a fixed-point whole number or an
+// order key.
+
+// the double bits of a 32-bit float (exact: subnormals normalized, infinities and NaN kept)
+__device__ __forceinline__ unsigned long long small_f32_bits(uint32_t b)
 {
-  double v;
-  switch (type)
+  unsigned long long sign = (unsigned long long)(b >> 31) << 63;
+  uint32_t e = (b >> 23) & 0xffu, m = b & 0x7fffffu;
+  if (e == 0xffu) return sign | 0x7ff0000000000000ull | ((unsigned long long)m << 29);
+  if (e == 0)
   {
-    case 1: v = (double)((const uint32_t*)col)[r]; break;
-    case 7: v = (double)((const int*)col)[r]; break;
-    case 3: v = (double)((const float*)col)[r]; break;
-    default: v = ((const double*)col)[r]; break;
+    if (m == 0) return sign;
+    uint32_t shift = __clz(m) - 8;   // bring the leading one to bit 23
+    m = (m << shift) & 0x7fffffu;
+    return sign | ((unsigned long long)(1023 - 126 - shift) << 52) | ((unsigned long long)m << 29);
   }
-  *ok = v == v;
-  unsigned long long b = (unsigned long long)__double_as_longlong(v);
-  if ((b << 1) == 0) b = 0;   // -0.0 compares equal to +0.0
-  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+  return sign | ((unsigned long long)(e - 127 + 1023) << 52) | ((unsigned long long)m << 29);
 }
 
-__global__ void __launch_bounds__(HASH_THREADS) k_small_key_extrema(CqlLaunch a, uint64_t rows)
+// the double bits of a whole number below 2^53 in magnitude (exact)
+__device__ __forceinline__ unsigned long long small_int_bits(long long v)
 {
-  __shared__ uint32_t s_first[EXTREMA_VALUES];
-  __shared__ unsigned long long s_ext[EXTREMA_VALUES * EXTREMA_COLUMNS * 2];
+  if (v == 0) return 0;
+  unsigned long long sign = v < 0 ? 0x8000000000000000ull : 0ull, a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  int p = 63 - __clzll(a);
+  return sign | ((unsigned long long)(1023 + p) << 52) | ((a << (52 - p)) & 0xfffffffffffffull);
+}
+
+// round-half-even(x * 2^s) of a finite double x given by its bits; |x * 2^s| < 2^62 by the choice of s
+__device__ __forceinline__ long long small_fixed(unsigned long long b, int s)
+{
+  int e = (int)((b >> 52) & 0x7ffu);
+  unsigned long long m = b & 0xfffffffffffffull;
+  if (e) m |= 1ull << 52;
+  else e = 1;
+  int sh = e - 1075 + s;   // x * 2^s = m * 2^sh
+  unsigned long long q;
+  if (sh >= 0) q = sh > 10 ? (1ull << 62) : m << sh;   // past 2^62 only for a value outside the column's range
+  else if (sh <= -54) q = 0;   // below a half
+  else
+  {
+    uint32_t r = (uint32_t)(-sh);
+    unsigned long long whole = m >> r, rem = m & ((1ull << r) - 1ull), half = 1ull << (r - 1);
+    q = whole + ((rem > half || (rem == half && (whole & 1ull))) ? 1ull : 0ull);
+  }
+  return (b >> 63) ? -(long long)q : (long long)q;
+}
+
+template <bool OWN>
+__device__ __forceinline__ void add96(uint32_t* l0, uint32_t* l1, uint32_t* l2, long long q)
+{
+  uint32_t lo = (uint32_t)q, hi = (uint32_t)((unsigned long long)q >> 32), top = q < 0 ? 0xffffffffu : 0u;
+  uint32_t old0;
+  if (OWN)
+  {
+    old0 = *l0;
+    *l0 = old0 + lo;
+  }
+  else
+    old0 = atomicAdd(l0, lo);
+  uint32_t mid = hi + ((old0 + lo < old0) ? 1u : 0u);
+  top += mid < hi ? 1u : 0u;   // hi + carry passed 2^32
+  if (mid)
+  {
+    uint32_t old1;
+    if (OWN)
+    {
+      old1 = *l1;
+      *l1 = old1 + mid;
+    }
+    else
+      old1 = atomicAdd(l1, mid);
+    top += (old1 + mid < old1) ? 1u : 0u;
+  }
+  if (top)
+  {
+    if (OWN) *l2 += top;
+    else atomicAdd(l2, top);
+  }
+}
+
+template <bool OWN>
+__global__ void __launch_bounds__(HASH_THREADS) k_group_small(CqlLaunch a, uint64_t rows, uint32_t copies)
+{
+  extern __shared__ __align__(16) uint32_t smem[];
+  __shared__ unsigned long long s_ext[SMALL_VALUES * SMALL_COLUMNS * 2];
+  __shared__ uint32_t s_first[SMALL_VALUES], s_flags[SMALL_VALUES * SMALL_COLUMNS];
   const uint32_t* key = (const uint32_t*)a.buf[0];
-  uint32_t* first = (uint32_t*)a.buf[1];
-  unsigned long long* ext = (unsigned long long*)a.buf[2];
-  uint32_t min_key = cql_word(a, 2), range = min(cql_word(a, 4), (uint32_t)EXTREMA_VALUES);
-  uint32_t ncols = min(cql_word(a, 6), (uint32_t)EXTREMA_COLUMNS), types = cql_word(a, 8);
-  uint64_t ext_words = a.bytes[2] / 8;
-  for (uint32_t i = threadIdx.x; i < EXTREMA_VALUES; i += blockDim.x) s_first[i] = 0xffffffffu;
-  for (uint32_t i = threadIdx.x; i < EXTREMA_VALUES * EXTREMA_COLUMNS * 2; i += blockDim.x) s_ext[i] = (i & 1) ? 0ull : ~0ull;
+  uint32_t* out = (uint32_t*)a.buf[1 + SMALL_COLUMNS];
+  uint32_t min_key = cql_word(a, 2), V = cql_word(a, 4), ncols = cql_word(a, 6), types = cql_word(a, 8), need = cql_word(a, 10);
+  // per column: its type, whether summed (and its limb slot), whether its extrema are kept, 2^s
+  uint32_t ctype[SMALL_COLUMNS], cslot[SMALL_COLUMNS], nsum = 0;
+  bool csum[SMALL_COLUMNS], cext[SMALL_COLUMNS], cwhole[SMALL_COLUMNS];
+  int cscale[SMALL_COLUMNS];
+#pragma unroll
+  for (uint32_t c = 0; c < SMALL_COLUMNS; c++)
+  {
+    ctype[c] = (types >> (4 * c)) & 0xfu;
+    csum[c] = c < ncols && ((need >> c) & 1u);
+    cext[c] = c < ncols && ((need >> (SMALL_COLUMNS + c)) & 1u);
+    int sc = (int)(short)(unsigned short)(a.push[6 + c / 4] >> (16 * (c % 4)));
+    cwhole[c] = ctype[c] == 1 || ctype[c] == 7;
+    cscale[c] = sc;
+    cslot[c] = nsum;
+    nsum += csum[c] ? 1u : 0u;
+  }
+  uint32_t words = V * (1 + 3 * nsum);   // one table: V counts, then per summed column 3 limbs of V
+  for (uint32_t i = threadIdx.x; i < copies * words; i += blockDim.x) smem[i] = 0;
+  for (uint32_t i = threadIdx.x; i < SMALL_VALUES * SMALL_COLUMNS * 2; i += blockDim.x) s_ext[i] = (i & 1) ? 0ull : ~0ull;
+  for (uint32_t i = threadIdx.x; i < SMALL_VALUES; i += blockDim.x) s_first[i] = 0xffffffffu;
+  for (uint32_t i = threadIdx.x; i < SMALL_VALUES * SMALL_COLUMNS; i += blockDim.x) s_flags[i] = 0;
   __syncthreads();
+  uint32_t* table = smem + (threadIdx.x % copies) * words;
+  // SMALL_ROWS rows a thread a step, a grid stride apart (each coalesced across the warp): the keys read
+  // together, then each column's values together, so that a thread keeps several loads in flight
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t r0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r0 < rows; r0 += step * SMALL_ROWS)
+  {
+    uint32_t g[SMALL_ROWS];
+#pragma unroll
+    for (uint32_t i = 0; i < SMALL_ROWS; i++)
+    {
+      uint64_t r = r0 + i * step;
+      g[i] = r < rows ? key[r] - min_key : 0xffffffffu;
+    }
+#pragma unroll
+    for (uint32_t i = 0; i < SMALL_ROWS; i++)
+    {
+      if (g[i] >= V) continue;
+      uint32_t r = (uint32_t)(r0 + i * step);
+      if (OWN) table[g[i]] += 1;
+      else atomicAdd(&table[g[i]], 1u);
+      if (r < s_first[g[i]]) atomicMin(&s_first[g[i]], r);
+    }
+#pragma unroll
+    for (uint32_t c = 0; c < SMALL_COLUMNS; c++)
+    {
+      if (!csum[c] && !cext[c]) continue;
+      const void* col = a.buf[1 + c];
+      unsigned long long raw[SMALL_ROWS];
+#pragma unroll
+      for (uint32_t i = 0; i < SMALL_ROWS; i++)
+      {
+        uint64_t r = r0 + i * step;
+        raw[i] = 0;
+        if (r < rows) raw[i] = ctype[c] == 4 ? ((const unsigned long long*)col)[r] : ((const uint32_t*)col)[r];
+      }
+#pragma unroll
+      for (uint32_t i = 0; i < SMALL_ROWS; i++)
+      {
+        if (g[i] >= V) continue;
+        // the value as a whole number (whole-number columns, exact) and as the bits of its double
+        long long whole = ctype[c] == 7 ? (long long)(int)(uint32_t)raw[i] : (long long)raw[i];
+        unsigned long long b = cwhole[c] ? small_int_bits(whole) : ctype[c] == 3 ? small_f32_bits((uint32_t)raw[i]) : raw[i];
+        bool finite = ((b >> 52) & 0x7ffu) != 0x7ffu;
+        if (csum[c])
+        {
+          if (finite)
+          {
+            long long q = cwhole[c] ? whole : small_fixed(b, cscale[c]);
+            uint32_t* l = table + V * (1 + 3 * cslot[c]) + g[i];
+            add96<OWN>(l, l + V, l + 2 * V, q);
+          }
+          else
+            atomicOr(&s_flags[g[i] * SMALL_COLUMNS + c], (b & 0xfffffffffffffull) ? 1u : (b >> 63) ? 4u : 2u);
+        }
+        if (cext[c] && (finite || !(b & 0xfffffffffffffull)))   // NaN is left out
+        {
+          if ((b << 1) == 0) b = 0;   // -0.0 compares equal to +0.0
+          unsigned long long o = (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+          unsigned long long* e = s_ext + (g[i] * SMALL_COLUMNS + c) * 2;
+          if (o < e[0]) atomicMin(&e[0], o);
+          if (o > e[1]) atomicMax(&e[1], o);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // this CTA's tables folded and added to the output: counts (u64), sums (128-bit), first rows, extrema, flags
+  unsigned long long* counts = (unsigned long long*)out;
+  uint32_t sums_at = 3 * V + (V & 1u);
+  unsigned long long* sums = (unsigned long long*)(out + sums_at);
+  uint32_t* flags = out + sums_at + 4 * SMALL_COLUMNS * V;
+  unsigned long long* ext = (unsigned long long*)(out + sums_at + 5 * SMALL_COLUMNS * V);
+  for (uint32_t t = threadIdx.x; t < V * (1 + nsum); t += blockDim.x)
+  {
+    uint32_t g = t % V, part = t / V;
+    if (part == 0)
+    {
+      unsigned long long n = 0;
+      for (uint32_t k = 0; k < copies; k++) n += smem[k * words + g];
+      if (n) atomicAdd(&counts[g], n);
+    }
+    else
+    {
+      __int128 total = 0;
+      uint32_t base = V * (1 + 3 * (part - 1)) + g;
+      for (uint32_t k = 0; k < copies; k++)
+      {
+        const uint32_t* l = smem + k * words + base;
+        unsigned long long low = (unsigned long long)l[0] | ((unsigned long long)l[V] << 32);
+        total += (__int128)(((unsigned __int128)(unsigned long long)(long long)(int)l[2 * V] << 64) | low);
+      }
+      if (total != 0)
+      {
+        // the summed column whose limb slot this is
+        uint32_t c = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < SMALL_COLUMNS; j++)
+          if (csum[j] && cslot[j] == part - 1) c = j;
+        unsigned long long lo = (unsigned long long)total, hi = (unsigned long long)((unsigned __int128)total >> 64);
+        unsigned long long* at = sums + (g * SMALL_COLUMNS + c) * 2;
+        unsigned long long old = atomicAdd(&at[0], lo);
+        hi += (old + lo < old) ? 1ull : 0ull;
+        if (hi) atomicAdd(&at[1], hi);
+      }
+    }
+  }
+  for (uint32_t t = threadIdx.x; t < V * SMALL_COLUMNS; t += blockDim.x)
+  {
+    uint32_t g = t / SMALL_COLUMNS;
+    if (t % SMALL_COLUMNS == 0 && s_first[g] != 0xffffffffu) atomicMin(&out[2 * V + g], s_first[g]);
+    if (s_flags[t]) atomicOr(&flags[t], s_flags[t]);
+    if (s_ext[2 * t] != ~0ull) atomicMin(&ext[2 * t], s_ext[2 * t]);
+    if (s_ext[2 * t + 1] != 0ull) atomicMax(&ext[2 * t + 1], s_ext[2 * t + 1]);
+  }
+}
+
+// cql_finite_magnitude: the largest finite |x| of an f32/f64 column, as the bits of a non-negative double
+// (whose order is the bits' order): binding 0 the column, 1 the result (u64, zero before); word 0 rows,
+// word 2 the CQL type (F32 or F64). The small-key GROUP BY's scale for a column with no finite range.
+__global__ void __launch_bounds__(HASH_THREADS) k_finite_magnitude(CqlLaunch a, uint64_t rows, bool f32)
+{
+  unsigned long long best = 0;
   for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (uint64_t)gridDim.x * blockDim.x)
   {
-    uint32_t k = key[r] - min_key;
-    if (k >= range) continue;
-    if ((uint32_t)r < s_first[k]) atomicMin(&s_first[k], (uint32_t)r);
-    for (uint32_t c = 0; c < ncols; c++)
-    {
-      bool ok;
-      unsigned long long o = extrema_key(a.buf[3 + c], (types >> (4 * c)) & 0xfu, r, &ok);
-      if (!ok) continue;
-      unsigned long long* e = s_ext + (k * EXTREMA_COLUMNS + c) * 2;
-      if (o < e[0]) atomicMin(&e[0], o);
-      if (o > e[1]) atomicMax(&e[1], o);
-    }
+    double x = f32 ? (double)((const float*)a.buf[0])[r] : ((const double*)a.buf[0])[r];
+    if (isfinite(x)) best = max(best, (unsigned long long)__double_as_longlong(fabs(x)));
   }
-  __syncthreads();
-  for (uint32_t i = threadIdx.x; i < range; i += blockDim.x)
-  {
-    if (s_first[i] == 0xffffffffu) continue;
-    if ((uint64_t)(i + 1) * 4 <= a.bytes[1]) atomicMin(&first[i], s_first[i]);
-    for (uint32_t c = 0; c < ncols; c++)
-    {
-      uint64_t at = ((uint64_t)i * EXTREMA_COLUMNS + c) * 2;
-      if (at + 1 >= ext_words) continue;
-      const unsigned long long* e = s_ext + (i * EXTREMA_COLUMNS + c) * 2;
-      atomicMin(&ext[at], e[0]);
-      atomicMax(&ext[at + 1], e[1]);
-    }
-  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if ((threadIdx.x & 31u) == 0 && best) atomicMax((unsigned long long*)a.buf[1], best);
 }
 
-static int launch_small_key_extrema(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+static int launch_finite_magnitude(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
 {
   (void)gws;
   (void)lws;
-  uint64_t rows = cql_word(a, 0);
+  uint64_t rows = a.push[0];
+  uint32_t type = cql_word(a, 2);
   if (rows == 0) return 0;
-  uint32_t ncols = cql_word(a, 6), types = cql_word(a, 8);
-  if (a.bytes[0] < rows * 4 || cql_word(a, 4) > EXTREMA_VALUES || ncols > EXTREMA_COLUMNS) return (int)cudaErrorInvalidValue;
+  if (!(type == 3 || type == 4) || a.bytes[0] < rows * (type == 4 ? 8 : 4) || a.bytes[1] < 8) return (int)cudaErrorInvalidValue;
+  k_finite_magnitude<<<cql_stream_grid((rows + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, rows, type == 3);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+// the output's size in u32 words for V key values
+static uint64_t group_small_words(uint32_t V)
+{
+  return 3ull * V + (V & 1u) + 9ull * SMALL_COLUMNS * V;
+}
+
+static int launch_group_small(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t rows = a.push[0];
+  if (rows == 0) return 0;
+  uint32_t V = cql_word(a, 4), ncols = cql_word(a, 6), types = cql_word(a, 8), need = cql_word(a, 10);
+  if (V == 0 || V > SMALL_VALUES || ncols > SMALL_COLUMNS || rows > 0xffffffffull || a.bytes[0] < rows * 4 ||
+      a.bytes[1 + SMALL_COLUMNS] < group_small_words(V) * 4)
+    return (int)cudaErrorInvalidValue;
+  uint32_t nsum = 0;
   for (uint32_t c = 0; c < ncols; c++)
   {
     uint32_t t = (types >> (4 * c)) & 0xfu;
     uint64_t width = t == 4 ? 8 : 4;
-    if (!(t == 1 || t == 7 || t == 3 || t == 4) || a.bytes[3 + c] < rows * width) return (int)cudaErrorInvalidValue;
+    if (!(t == 1 || t == 7 || t == 3 || t == 4) || a.bytes[1 + c] < rows * width) return (int)cudaErrorInvalidValue;
+    nsum += (need >> c) & 1u;
   }
-  k_small_key_extrema<<<cql_stream_grid((rows + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, rows);
+  // private tables: one a thread when they fit in 48 KB, else as many as fit (a power of two, at least one a warp)
+  uint32_t table_bytes = V * (1 + 3 * nsum) * 4;
+  uint32_t copies = HASH_THREADS;
+  while (copies > 8 && (uint64_t)copies * table_bytes > 48u * 1024u) copies >>= 1;
+  size_t smem = (size_t)copies * table_bytes;
+  bool own = copies == HASH_THREADS;
+  const void* fn = own ? (const void*)k_group_small<true> : (const void*)k_group_small<false>;
+  // with the static tables (extrema, flags, first rows) the CTA passes the default 48 KB: opt in
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, HASH_THREADS, smem) != cudaSuccess || per_sm < 1)
+  {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  uint32_t grid = cql_stream_grid((rows + HASH_THREADS - 1) / HASH_THREADS, per_sm);
+  if (own) k_group_small<true><<<grid, HASH_THREADS, smem, stream>>>(a, rows, copies);
+  else k_group_small<false><<<grid, HASH_THREADS, smem, stream>>>(a, rows, copies);
   CQL_LAUNCH_CHECK();
   return 0;
 }
@@ -1298,7 +1541,8 @@ const CqlKernelDesc cql_kernels_hash[] = {
   { "csr_scatter_tiled", launch_csr_scatter },
   { "aggregate_reduce", launch_aggregate_reduce },
   { "cql_gather_columns", launch_gather_columns },
-  { "cql_small_key_extrema", launch_small_key_extrema },
+  { "cql_finite_magnitude", launch_finite_magnitude },
+  { "cql_group_small", launch_group_small },
   { "cql_group_finish", launch_group_finish },
   { "cql_gather_string_lengths", launch_gather_string_lengths },
   { "cql_gather_string_bytes", launch_gather_string_bytes },

@@ -319,20 +319,20 @@ static int simple_leaf_words(uint32_t* words, uint32_t slot, const CqlColumn* co
    table row first_row, a multiple of 32) in ascending order, on the device: each 256-word block's
    population, an exclusive scan over the blocks, then every block's rows written from its offset. The
    first min(count, cap) rows land in out_rows; count is the bitmap's population. */
-int cqlops_bitmap_rows(CqlBuffer* bitmap, uint64_t first_row, uint64_t rows, uint64_t count, uint32_t* out_rows, uint64_t cap)
+/* Enqueues into batch b the rows of a selection bitmap of `rows` rows, ascending, into `list` (at most its
+   size / 4 of them; the emit kernel stops there). */
+static int bitmap_rows_enqueue(CqlBatch* b, CqlBuffer* bitmap, uint64_t first_row, uint64_t rows, CqlBuffer* list)
 {
-  if (!count || !cap || !out_rows) return 1;
   uint64_t words = (rows + 31) / 32, blocks = (words + 255) / 256, scan_blocks = (blocks + 255) / 256;
-  uint64_t n = count < cap ? count : cap;
+  if (words == 0) return 1;
   CqlBuffer* counts = pooled("bitmap_block_counts", blocks * 4, CQLCUDA_BUFFER_READ_WRITE);
   CqlBuffer* offsets = pooled("bitmap_block_offsets", (blocks + 1) * 4, CQLCUDA_BUFFER_READ_WRITE);
   CqlBuffer* cursor = pooled("bitmap_block_cursor", blocks * 4, CQLCUDA_BUFFER_READ_WRITE);
   CqlBuffer* block_sums = pooled("bitmap_scan_sums", scan_blocks * 4, CQLCUDA_BUFFER_READ_WRITE);
-  CqlBuffer* list = pooled("bitmap_rows", count * 4, CQLCUDA_BUFFER_READ_WRITE);
   CqlKernel* popc = kernel_named("cql_bitmap_popc");
   CqlKernel* scan = kernel_named("prefix_sum");
   CqlKernel* emit = kernel_named("cql_bitmap_emit");
-  if (!counts || !offsets || !cursor || !block_sums || !list || !popc || !scan || !emit) return 0;
+  if (!counts || !offsets || !cursor || !block_sums || !popc || !scan || !emit) return 0;
   cqlcuda_kernel_set_arg_buffer(popc, 0, bitmap);
   cqlcuda_kernel_set_arg_buffer(popc, 1, counts);
   cqlcuda_kernel_set_arg_u64(popc, 0, words);
@@ -346,7 +346,6 @@ int cqlops_bitmap_rows(CqlBuffer* bitmap, uint64_t first_row, uint64_t rows, uin
   cqlcuda_kernel_set_arg_buffer(emit, 2, list);
   cqlcuda_kernel_set_arg_u64(emit, 0, words);
   cqlcuda_kernel_set_arg_u64(emit, 1, first_row);
-  CqlBatch* b = cqlcuda_batch_begin(0, n * 4);
   if (blocks == 1) cqlcuda_batch_buffer_zero(b, offsets, 4);   /* one block: its rows start at 0 */
   else
   {
@@ -358,12 +357,31 @@ int cqlops_bitmap_rows(CqlBuffer* bitmap, uint64_t first_row, uint64_t rows, uin
     }
   }
   cqlcuda_batch_kernel_execute(b, emit, (uint32_t)(blocks * 256), QE_GPU_WORKGROUP_SIZE);
+  return 1;
+}
+
+/* The rows of a selection bitmap (one bit a row, as the scans write it in bitmap mode; its first bit is
+   table row first_row, a multiple of 32) in ascending order, on the device: each 256-word block's
+   population, an exclusive scan over the blocks, then every block's rows written from its offset. The
+   first min(count, cap) rows land in out_rows; count is the bitmap's population. */
+int cqlops_bitmap_rows(CqlBuffer* bitmap, uint64_t first_row, uint64_t rows, uint64_t count, uint32_t* out_rows, uint64_t cap)
+{
+  if (!count || !cap || !out_rows) return 1;
+  uint64_t n = count < cap ? count : cap;
+  CqlBuffer* list = pooled("bitmap_rows", n * 4, CQLCUDA_BUFFER_READ_WRITE);
+  if (!list) return 0;
+  CqlBatch* b = cqlcuda_batch_begin(0, n * 4);
+  if (!bitmap_rows_enqueue(b, bitmap, first_row, rows, list))
+  {
+    cqlcuda_batch_end(b);
+    return 0;
+  }
   cqlcuda_batch_buffer_read(b, list, out_rows, n * 4);
   return cqlcuda_batch_end(b);
 }
 
-int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const CqlLeaf* leaves, uint32_t leaf_count, uint64_t* out_count,
-                       uint32_t* out_rows, uint64_t out_capacity)
+static int scan_simple_run(const CqlColumn* columns, uint32_t column_count, const CqlLeaf* leaves, uint32_t leaf_count, uint64_t* out_count,
+                           uint32_t* out_rows, uint64_t out_capacity, CqlBuffer* out_selection)
 {
   launches_begin();
   if (leaf_count == 0 || leaf_count > QE_SIMPLE_SCAN_MAX_LEAVES || column_count == 0 || column_count > QE_MAX_COLUMN_BINDINGS)
@@ -412,7 +430,7 @@ int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const Cq
   }
   /* the output: none for a count, else a bitmap of the rows (no capacity to outgrow, unlike the
      reference's list sized at :3084-3090) */
-  int want_rows = out_rows != NULL;
+  int want_rows = out_rows != NULL || out_selection != NULL;
   /* zone-map pruning: the ranges of the table the leaves can match, or one pass with a skip bitmap
      (qe_scan_build_dispatch_ranges, :13307-13540) */
   uint64_t chunks = (rows + CQLOPS_ZONEMAP_CHUNK_ROWS - 1) / CQLOPS_ZONEMAP_CHUNK_ROWS;
@@ -483,6 +501,13 @@ int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const Cq
     uint64_t threads = (end - start + QE_SIMPLE_SCAN_ROWS_PER_THREAD - 1) / QE_SIMPLE_SCAN_ROWS_PER_THREAD;
     cqlcuda_batch_kernel_execute(batch, k, (uint32_t)threads, QE_GPU_WORKGROUP_SIZE);
   }
+  /* a device selection: the rows are listed in the same batch (the list stops at the buffer's size) */
+  if (out_selection && !bitmap_rows_enqueue(batch, output, bitmap_first, bitmap_end - bitmap_first, out_selection))
+  {
+    cqlcuda_batch_end(batch);
+    free(skip_bits);
+    return 0;
+  }
   cqlcuda_batch_buffer_read(batch, counter, count32, sizeof(count32));
   if (!cqlcuda_batch_end(batch))
   {
@@ -491,9 +516,22 @@ int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const Cq
   }
   uint64_t result_count = count32[0];
   free(skip_bits);
-  if (want_rows && !cqlops_bitmap_rows(output, bitmap_first, bitmap_end - bitmap_first, result_count, out_rows, out_capacity)) return 0;
+  if (out_rows && !cqlops_bitmap_rows(output, bitmap_first, bitmap_end - bitmap_first, result_count, out_rows, out_capacity)) return 0;
   if (out_count) *out_count = result_count;
   return 1;
+}
+
+int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const CqlLeaf* leaves, uint32_t leaf_count, uint64_t* out_count,
+                       uint32_t* out_rows, uint64_t out_capacity)
+{
+  return scan_simple_run(columns, column_count, leaves, leaf_count, out_count, out_rows, out_capacity, NULL);
+}
+
+int cqlops_scan_simple_select(const CqlColumn* columns, uint32_t column_count, const CqlLeaf* leaves, uint32_t leaf_count,
+                              CqlBuffer* out_selection, uint64_t* out_count)
+{
+  if (!out_selection) return refuse("a device buffer for the selection");
+  return scan_simple_run(columns, column_count, leaves, leaf_count, out_count, NULL, 0, out_selection);
 }
 
 /* ------------------------------------------------------------------------------------------------

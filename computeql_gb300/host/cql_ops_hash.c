@@ -363,12 +363,10 @@ static int csr_reduce(uint64_t rows, uint64_t slots, uint64_t groups, CqlBuffer*
   return ok;
 }
 
-/* ---- path 3: a small-range key with COUNT/SUM/AVG/MIN/MAX of f32/f64 columns, through the shared scan ----
-   Each key value v and summed column s is the query COUNT(*), SUM(s) WHERE key = v; the batched shared scan
-   (cqlops_batch_filter_aggregate) answers them all in one pass over the columns, its sums exact 128-bit
-   sums of the values scaled by 2^k, so the result does not depend on the order of the rows. The first row
-   of each value and the MIN/MAX of up to 4 columns come from one more pass (cql_small_key_extrema). A key
-   of at most 64 values. Gives way (-1) when the query does not fit, and to the fixed-point path when every
+/* ---- path 3: a small-range key with COUNT/SUM/AVG/MIN/MAX of f32/f64 columns, in one pass ----
+   A key of at most 64 values: one pass over the key and the argument columns (cql_group_small) gives per
+   value its count, first row, exact fixed-point SUMs (so the result does not depend on the order of the
+   rows) and MIN/MAX. Gives way (-1) when the query does not fit, and to the fixed-point path when every
    f32/f64 argument is a decimal of at most 6 places (that path finalizes them as the reference does). */
 #define SMALL_KEY_VALUES 64
 
@@ -380,38 +378,159 @@ static double order_key_to_double(uint64_t k)
   return v;
 }
 
-/* program `dst` = `src` with the one constant holding `from` replaced by `to`: the used words, constants
-   and strings and the bindings are copied, not the whole (84 KB) struct; 0 when `from` is not exactly one
-   constant (the caller then builds the program) */
-static int program_with_literal(CqlProgram* dst, const CqlProgram* src, double from, double to)
-{
-  uint32_t hits = 0, at = 0;
-  for (uint32_t i = 0; i < src->const_count; i++)
-  {
-    double c;
-    memcpy(&c, &src->consts[2 * i], 8);
-    if (c == from)
-    {
-      hits++;
-      at = i;
-    }
-  }
-  if (hits != 1 || src->word_count > CQLOPS_MAX_WORDS || src->str_pool_size > CQLOPS_MAX_STR_POOL) return 0;
-  memcpy(dst->words, src->words, (size_t)src->word_count * 4);
-  dst->word_count = src->word_count;
-  memcpy(dst->consts, src->consts, (size_t)src->const_count * 8);
-  dst->const_count = src->const_count;
-  memcpy(dst->str_pool, src->str_pool, src->str_pool_size);
-  /* everything from str_pool_size to the end: the bindings, flags and error text */
-  memcpy(&dst->str_pool_size, &src->str_pool_size, sizeof(CqlProgram) - offsetof(CqlProgram, str_pool_size));
-  memcpy(&dst->consts[2 * at], &to, 8);
-  return 1;
-}
-
 static int numeric_full(const CqlColumn* c, uint64_t rows)
 {
   return c && c->rows == rows && c->width == 0 && c->buffer &&
          (c->type == CQLOPS_TYPE_U32 || c->type == CQLOPS_TYPE_I32 || c->type == CQLOPS_TYPE_F32 || c->type == CQLOPS_TYPE_F64);
+}
+
+/* The one-pass form of the small-key GROUP BY (cql_group_small): the key and up to 8 distinct argument
+   columns read once, each SUM exact in fixed point at a binary scale chosen from the column's range (a
+   whole-number column at scale 0), MIN and MAX as order keys. 1 done, 0 failed. */
+#define GROUP_SMALL_COLUMNS 8
+static int group_small_fused(const CqlColumn* key, uint32_t values, int64_t kmin, uint32_t expr_count, const uint32_t* funcs,
+                             const CqlColumn* const* args, uint64_t max_groups, uint64_t* out_group_count, uint64_t* out_repr_row,
+                             uint64_t* out_counts, double* out_results)
+{
+  uint64_t rows = key->rows;
+  const CqlColumn* cols[GROUP_SMALL_COLUMNS];
+  uint32_t ncols = 0, need = 0, types = 0, col_of[8] = { 0 };
+  int scale[GROUP_SMALL_COLUMNS] = { 0, 0, 0, 0, 0, 0, 0, 0 };
+  for (uint32_t e = 0; e < expr_count; e++)
+  {
+    uint32_t f = funcs[e];
+    if (f == CQLOPS_FUNC_COUNT) continue;
+    const CqlColumn* c = args[e];
+    uint32_t i = 0;
+    while (i < ncols && cols[i]->buffer != c->buffer) i++;
+    if (i == ncols)
+    {
+      cols[ncols++] = c;
+      types |= (c->type & 0xfu) << (4 * i);
+    }
+    col_of[e] = i;
+    need |= (f == CQLOPS_FUNC_SUM || f == CQLOPS_FUNC_AVG) ? (1u << i) : (1u << (GROUP_SMALL_COLUMNS + i));
+  }
+  /* each summed f32/f64 column's largest finite magnitude: from its zone range, or (no range, or an infinite
+     one) from one pass over it */
+  double largest[GROUP_SMALL_COLUMNS] = { 0 };
+  uint64_t measured[GROUP_SMALL_COLUMNS] = { 0 };
+  uint32_t measure_mask = 0;
+  for (uint32_t i = 0; i < ncols; i++)
+  {
+    const CqlColumn* c = cols[i];
+    if (!((need >> i) & 1u) || c->type == CQLOPS_TYPE_U32 || c->type == CQLOPS_TYPE_I32) continue;
+    if (c->has_range && isfinite(c->zone_min) && isfinite(c->zone_max))
+      largest[i] = fabs(c->zone_min) > fabs(c->zone_max) ? fabs(c->zone_min) : fabs(c->zone_max);
+    else
+      measure_mask |= 1u << i;
+  }
+  if (measure_mask)
+  {
+    CqlBuffer* mb = pooled("group_small_magnitude", GROUP_SMALL_COLUMNS * 8, CQLCUDA_BUFFER_READ_WRITE);
+    CqlKernel* mk = kernel("cql_finite_magnitude");
+    if (!mb || !mk) return 0;
+    CqlBatch* b = cqlcuda_batch_begin(0, GROUP_SMALL_COLUMNS * 8);
+    cqlcuda_batch_buffer_zero(b, mb, GROUP_SMALL_COLUMNS * 8);
+    for (uint32_t i = 0; i < ncols; i++)
+    {
+      if (!((measure_mask >> i) & 1u)) continue;
+      cqlcuda_kernel_set_arg_buffer(mk, 0, cols[i]->buffer);
+      cqlcuda_kernel_set_arg_buffer_range(mk, 1, mb, (uint64_t)i * 8, 8);
+      cqlcuda_kernel_set_arg_u64(mk, 0, rows);
+      cqlcuda_kernel_set_arg_u64(mk, 1, cols[i]->type);
+      cqlcuda_batch_kernel_execute(b, mk, (uint32_t)rows, QE_GPU_WORKGROUP_SIZE);
+    }
+    cqlcuda_batch_buffer_read(b, mb, measured, GROUP_SMALL_COLUMNS * 8);
+    if (!cqlcuda_batch_end(b)) return 0;
+    for (uint32_t i = 0; i < ncols; i++)
+      if ((measure_mask >> i) & 1u) memcpy(&largest[i], &measured[i], 8);
+  }
+  for (uint32_t i = 0; i < ncols; i++)
+  {
+    const CqlColumn* c = cols[i];
+    if (!((need >> i) & 1u) || c->type == CQLOPS_TYPE_U32 || c->type == CQLOPS_TYPE_I32) continue;   /* scale 0: exact */
+    int e2 = 0;
+    if (largest[i] > 0.0) frexp(largest[i], &e2);   /* largest < 2^e2 */
+    int sc = 61 - e2;                                /* |x| * 2^sc < 2^61 */
+    scale[i] = sc > 1023 ? 1023 : sc < -1022 ? -1022 : sc;
+  }
+  uint64_t words = 3ull * values + (values & 1u) + 9ull * GROUP_SMALL_COLUMNS * values;
+  uint32_t sums_at = 3u * values + (values & 1u);
+  CqlBuffer* ob = pooled("group_small_out", words * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlKernel* k = kernel("cql_group_small");
+  uint32_t* host = (uint32_t*)calloc(words, 4);
+  if (!ob || !k || !host)
+  {
+    free(host);
+    return 0;
+  }
+  for (uint32_t v = 0; v < values; v++) host[2 * values + v] = 0xffffffffu;
+  uint64_t* ext = (uint64_t*)(host + sums_at + 5u * GROUP_SMALL_COLUMNS * values);
+  for (uint32_t i = 0; i < values * GROUP_SMALL_COLUMNS; i++) ext[2 * i] = ~0ull;
+  uint64_t packed_scales[2] = { 0, 0 };
+  for (uint32_t i = 0; i < GROUP_SMALL_COLUMNS; i++) packed_scales[i / 4] |= (uint64_t)(uint16_t)(int16_t)scale[i] << (16 * (i % 4));
+  cqlcuda_kernel_set_arg_buffer(k, 0, key->buffer);
+  for (uint32_t i = 0; i < GROUP_SMALL_COLUMNS; i++) cqlcuda_kernel_set_arg_buffer(k, 1 + i, i < ncols ? cols[i]->buffer : key->buffer);
+  cqlcuda_kernel_set_arg_buffer(k, 1 + GROUP_SMALL_COLUMNS, ob);
+  cqlcuda_kernel_set_arg_u64(k, 0, rows);
+  cqlcuda_kernel_set_arg_u64(k, 1, (uint32_t)kmin);
+  cqlcuda_kernel_set_arg_u64(k, 2, values);
+  cqlcuda_kernel_set_arg_u64(k, 3, ncols);
+  cqlcuda_kernel_set_arg_u64(k, 4, types);
+  cqlcuda_kernel_set_arg_u64(k, 5, need);
+  cqlcuda_kernel_set_arg_u64(k, 6, packed_scales[0]);
+  cqlcuda_kernel_set_arg_u64(k, 7, packed_scales[1]);
+  CqlBatch* b = cqlcuda_batch_begin(words * 4, words * 4);
+  cqlcuda_batch_buffer_write(b, ob, host, words * 4);
+  cqlcuda_batch_kernel_execute(b, k, (uint32_t)rows, QE_GPU_WORKGROUP_SIZE);
+  cqlcuda_batch_buffer_read(b, ob, host, words * 4);
+  int result = cqlcuda_batch_end(b) ? 1 : 0;
+  const uint64_t* counts = (const uint64_t*)host;
+  const uint32_t* first = host + 2 * values;
+  const uint64_t* sums = (const uint64_t*)(host + sums_at);
+  const uint32_t* flags = host + sums_at + 4u * GROUP_SMALL_COLUMNS * values;
+  uint64_t g = 0;
+  for (uint32_t v = 0; v < values && result == 1; v++)
+  {
+    uint64_t count = counts[v];
+    if (count == 0) continue;
+    if (g >= max_groups)
+    {
+      result = refuse("more groups than the output arrays hold");
+      break;
+    }
+    out_repr_row[g] = first[v];
+    out_counts[g] = count;
+    for (uint32_t e = 0; e < expr_count; e++)
+    {
+      uint32_t f = funcs[e], i = col_of[e], at = v * GROUP_SMALL_COLUMNS + i;
+      double r = (double)count;
+      if (f == CQLOPS_FUNC_SUM || f == CQLOPS_FUNC_AVG)
+      {
+        /* the 128-bit total, rounded once to a double and scaled back by 2^-s; NaN and infinities as IEEE sums give them */
+        __int128 total = (__int128)(((unsigned __int128)sums[2 * at + 1] << 64) | sums[2 * at]);
+        uint32_t fl = flags[at];
+        double sum = ldexp((double)total, -scale[i]);
+        if ((fl & 1u) || (fl & 6u) == 6u) sum = NAN;
+        else if (fl & 2u) sum = INFINITY;
+        else if (fl & 4u) sum = -INFINITY;
+        r = f == CQLOPS_FUNC_AVG ? sum / (double)count : sum;
+      }
+      else if (f == CQLOPS_FUNC_MIN || f == CQLOPS_FUNC_MAX)
+      {
+        /* a group whose values are all NaN keeps the member reduce's starting values */
+        uint64_t o = ext[2 * at + (f == CQLOPS_FUNC_MAX)];
+        int empty = f == CQLOPS_FUNC_MIN ? o == ~0ull : o == 0ull;
+        r = empty ? (f == CQLOPS_FUNC_MIN ? 1.0e300 : -1.0e300) : order_key_to_double(o);
+      }
+      out_results[g * expr_count + e] = r;
+    }
+    g++;
+  }
+  if (result == 1) *out_group_count = g;
+  free(host);
+  return result;
 }
 
 static int group_small_key(const CqlColumn* key, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* args, uint64_t max_groups,
@@ -423,12 +542,7 @@ static int group_small_key(const CqlColumn* key, uint32_t expr_count, const uint
   uint32_t values = (uint32_t)span + 1u;
   int64_t kmin = (int64_t)key->zone_min;
   uint64_t rows = key->rows;
-  /* the table the programs are built over: the key, then each distinct summed column; the extrema columns */
-  CqlColumn cols[9];
-  const char* names[9] = { "k", "a0", "a1", "a2", "a3", "a4", "a5", "a6", "a7" };
-  const CqlColumn* ext_cols[4];
-  uint32_t ncols = 1, next = 0, slot_of_expr[8] = { 0 }, fractional = 0;
-  cols[0] = *key;
+  uint32_t fractional = 0;
   for (uint32_t e = 0; e < expr_count; e++)
   {
     uint32_t f = funcs[e];
@@ -436,29 +550,6 @@ static int group_small_key(const CqlColumn* key, uint32_t expr_count, const uint
     const CqlColumn* c = args[e];
     if (f > CQLOPS_FUNC_MAX || !numeric_full(c, rows)) return -1;
     if (c->type == CQLOPS_TYPE_F32 || c->type == CQLOPS_TYPE_F64) fractional = 1;
-    if (f == CQLOPS_FUNC_SUM || f == CQLOPS_FUNC_AVG)
-    {
-      if (!c->has_range) return -1;
-      uint32_t i = 1;
-      while (i < ncols && cols[i].buffer != c->buffer) i++;
-      if (i == ncols)
-      {
-        if (ncols == 9) return -1;
-        cols[ncols++] = *c;
-      }
-      slot_of_expr[e] = i;
-    }
-    else
-    {
-      uint32_t i = 0;
-      while (i < next && ext_cols[i]->buffer != c->buffer) i++;
-      if (i == next)
-      {
-        if (next == 4) return -1;
-        ext_cols[next++] = c;
-      }
-      slot_of_expr[e] = i;
-    }
   }
   if (!fractional) return -1;   /* whole numbers: the fixed-point hash reduce is exact already */
   /* decimals of at most 6 places take the fixed-point reduce, which finalizes them as the reference does */
@@ -473,105 +564,7 @@ static int group_small_key(const CqlColumn* key, uint32_t expr_count, const uint
   }
   cqlops_note_error("");
   if (all_decimal) return -1;
-  uint32_t sums_per_value = ncols > 1 ? ncols - 1 : 1;
-  uint32_t queries = values * sums_per_value;
-  CqlProgram* progs = (CqlProgram*)malloc((uint64_t)values * sizeof(CqlProgram));
-  const CqlProgram** qp = (const CqlProgram**)malloc((uint64_t)queries * sizeof(CqlProgram*));
-  int32_t* sum_cols = (int32_t*)malloc((uint64_t)queries * 4);
-  uint64_t* counts = (uint64_t*)malloc((uint64_t)queries * 8);
-  double* sums = (double*)malloc((uint64_t)queries * 8);
-  uint32_t* first = (uint32_t*)malloc((uint64_t)values * 4);
-  uint64_t ext_words = (uint64_t)values * 4 * 2;
-  uint64_t* ext = (uint64_t*)malloc(ext_words * 8);
-  int result = progs && qp && sum_cols && counts && sums && first && ext ? 1 : 0;
-  for (uint32_t v = 0; result == 1 && v < values; v++)
-  {
-    /* the programs differ in their literal alone: the first is built, the others copied with it replaced */
-    char where[64];
-    snprintf(where, sizeof(where), "(= k %lld)", (long long)(kmin + v));
-    if (!(v > 0 && program_with_literal(&progs[v], &progs[0], (double)kmin, (double)(kmin + v))) &&
-        !cqlops_program_build(where, cols, names, ncols, &progs[v]))
-      result = -1;
-    for (uint32_t s = 0; s < sums_per_value; s++)
-    {
-      qp[v * sums_per_value + s] = &progs[v];
-      sum_cols[v * sums_per_value + s] = ncols > 1 ? (int32_t)(1 + s) : -1;
-    }
-  }
-  if (result == 1 && !cqlops_batch_filter_aggregate(qp, queries, cols, ncols, sum_cols, 8, counts, sums, NULL)) result = -1;
-  if (result == 1)
-  {
-    CqlBuffer* fb = pooled("agg_small_key_first", (uint64_t)values * 4, CQLCUDA_BUFFER_READ_WRITE);
-    CqlBuffer* eb = pooled("agg_small_key_extrema", ext_words * 8, CQLCUDA_BUFFER_READ_WRITE);
-    CqlKernel* k = kernel("cql_small_key_extrema");
-    if (!fb || !eb || !k) result = 0;
-    else
-    {
-      uint32_t types = 0;
-      for (uint32_t c = 0; c < next; c++) types |= (ext_cols[c]->type & 0xfu) << (4 * c);
-      cqlcuda_kernel_set_arg_buffer(k, 0, key->buffer);
-      cqlcuda_kernel_set_arg_buffer(k, 1, fb);
-      cqlcuda_kernel_set_arg_buffer(k, 2, eb);
-      for (uint32_t c = 0; c < 4; c++) cqlcuda_kernel_set_arg_buffer(k, 3 + c, c < next ? ext_cols[c]->buffer : key->buffer);
-      cqlcuda_kernel_set_arg_u64(k, 0, rows);
-      cqlcuda_kernel_set_arg_u64(k, 1, (uint32_t)kmin);
-      cqlcuda_kernel_set_arg_u64(k, 2, values);
-      cqlcuda_kernel_set_arg_u64(k, 3, next);
-      cqlcuda_kernel_set_arg_u64(k, 4, types);
-      CqlBatch* b = cqlcuda_batch_begin(0, (uint64_t)values * 4 + ext_words * 8);
-      cqlcuda_batch_buffer_fill(b, fb, (uint64_t)values * 4, 0xffffffffu);
-      for (uint64_t i = 0; i < ext_words; i++) ext[i] = (i & 1) ? 0ull : ~0ull;
-      cqlcuda_batch_buffer_write(b, eb, ext, ext_words * 8);
-      cqlcuda_batch_kernel_execute(b, k, (uint32_t)rows, QE_GPU_WORKGROUP_SIZE);
-      cqlcuda_batch_buffer_read(b, fb, first, (uint64_t)values * 4);
-      cqlcuda_batch_buffer_read(b, eb, ext, ext_words * 8);
-      if (!cqlcuda_batch_end(b)) result = 0;
-    }
-  }
-  if (result == 1)
-  {
-    uint64_t g = 0;
-    for (uint32_t v = 0; v < values && result == 1; v++)
-    {
-      uint64_t count = counts[v * sums_per_value];
-      if (count == 0) continue;
-      if (g >= max_groups)
-      {
-        result = refuse("more groups than the output arrays hold");
-        break;
-      }
-      out_repr_row[g] = first[v];
-      out_counts[g] = count;
-      for (uint32_t e = 0; e < expr_count; e++)
-      {
-        uint32_t f = funcs[e];
-        double r = (double)count;
-        if (f == CQLOPS_FUNC_SUM || f == CQLOPS_FUNC_AVG)
-        {
-          double sum = sums[v * sums_per_value + (slot_of_expr[e] - 1)];
-          r = f == CQLOPS_FUNC_AVG ? sum / (double)count : sum;
-        }
-        else if (f == CQLOPS_FUNC_MIN || f == CQLOPS_FUNC_MAX)
-        {
-          /* a group whose values are all NaN keeps the member reduce's starting values */
-          uint64_t o = ext[((uint64_t)v * 4 + slot_of_expr[e]) * 2 + (f == CQLOPS_FUNC_MAX)];
-          int empty = f == CQLOPS_FUNC_MIN ? o == ~0ull : o == 0ull;
-          r = empty ? (f == CQLOPS_FUNC_MIN ? 1.0e300 : -1.0e300) : order_key_to_double(o);
-        }
-        out_results[g * expr_count + e] = r;
-      }
-      g++;
-    }
-    if (result == 1) *out_group_count = g;
-  }
-  free(progs);
-  free(qp);
-  free(sum_cols);
-  free(counts);
-  free(sums);
-  free(first);
-  free(ext);
-  return result;
+  return group_small_fused(key, values, kmin, expr_count, funcs, args, max_groups, out_group_count, out_repr_row, out_counts, out_results);
 }
 
 int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* args,

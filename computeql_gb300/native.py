@@ -202,6 +202,7 @@ CUDA_API = [
 OPS_API = [
     ("cqlops_aggregate_global", C.c_int, [P, u32, P, P, P]),
     ("cqlops_scan_simple", C.c_int, [P, u32, P, u32, P, P, u64]),
+    ("cqlops_scan_simple_select", C.c_int, [P, u32, P, u32, P, P]),
     ("cqlops_group_dense", C.c_int, [P, u64, u32, P, P, u64, P, P, P, P, P, P]),
     ("cqlops_last_launches", u32, []),
     ("cqlops_last_error", cstr, []),

@@ -178,6 +178,16 @@ def scan_simple(columns, leaves, want_rows=False, max_rows=None):
     return count.value, rows
 
 
+def scan_select(columns, leaves, out):
+    """scan_simple with the matching rows kept on the device: up to out.nbytes // 4 of them, ascending, in the
+    DeviceBuffer `out` (a selection for sort_rows, window_rank, gather_rows). -> the match count."""
+    arr = (N.CqlColumn * len(columns))(*[c.c() for c in columns])
+    lv = (N.CqlLeaf * len(leaves))(*[N.CqlLeaf(ci, op, float(t)) for ci, op, t in leaves])
+    count = C.c_uint64()
+    _check(N.load_ops().cqlops_scan_simple_select(arr, len(columns), lv, len(leaves), out.handle, C.byref(count)), "cqlops_scan_simple_select")
+    return count.value
+
+
 def group_dense(key, funcs, args):
     """Dense GROUP BY -> (min_key, counts[G], sums[G,E], mins[G,E], maxs[G,E])."""
     e = len(funcs)

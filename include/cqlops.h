@@ -224,6 +224,13 @@ int cqlops_aggregate_global_accumulate(const CqlColumn* columns, uint32_t column
 int cqlops_scan_simple(const CqlColumn* columns, uint32_t column_count, const CqlLeaf* leaves, uint32_t leaf_count,
                        uint64_t* out_count, uint32_t* out_rows, uint64_t out_capacity);
 
+/* cqlops_scan_simple with the matching rows kept on the device: up to size / 4 of them, ascending, written
+   into out_selection (a device buffer) in the same batch as the scan, for the operators that take a
+   selection (sort, window, gather, fixed-point GROUP BY) - the selection qe_scan_filter_selected keeps on
+   the device for the next operator (keep_on_device, query_exec.c:2793, 3156-3164). Writes the match count. */
+int cqlops_scan_simple_select(const CqlColumn* columns, uint32_t column_count, const CqlLeaf* leaves, uint32_t leaf_count,
+                              CqlBuffer* out_selection, uint64_t* out_count);
+
 /* GROUP BY one small-range whole-number key (or a dictionary string column, by its codes) with
    COUNT/SUM/AVG/MIN/MAX over whole-number columns (qe_dense_stream_core, query_exec.c:7632-7983, one
    chunk). funcs[e]/arg_cols[e] describe

@@ -122,9 +122,9 @@ def test_distinct_sessions(suite):
 def test_sort_200k(suite):
     _, _, h, _, res, _ = suite
     from computeql_gb300 import eventbench
-    rows, order = res["sort_200k"]
+    order = res["sort_200k"]
     want_rows = np.nonzero(h["region"] == eventbench.SORT_REGION)[0]
-    np.testing.assert_array_equal(rows, want_rows)
+    assert len(order) == len(want_rows)
     perm = oracle.sort_rows([h["m4"][want_rows]])
     np.testing.assert_array_equal(order, want_rows[perm.astype(np.int64)])
 

@@ -176,3 +176,30 @@ def test_pruning_on_a_clustered_column(ops):
     cnt, rows = ops.scan_simple([c2], [(0, LE, 7)], want_rows=True)
     m = ts2 <= 7
     assert cnt == m.sum() and np.array_equal(rows, np.nonzero(m)[0].astype(np.uint32))
+
+
+@pytest.mark.parametrize("case", ["random", "clustered", "none", "small_buffer"])
+def test_selection_kept_on_the_device(ops, case):
+    # scan_select lists the matching rows into a device buffer in the scan's own batch: the same rows, in the
+    # same order, as scan_simple's host list; a zone-pruned scan, one with no match, and a buffer smaller than
+    # the match count (the first rows, and the full count)
+    rng = np.random.default_rng(17)
+    n = 2_000_003
+    if case == "clustered":
+        v = np.sort(rng.integers(0, 1_000_000, n)).astype(np.uint32)
+        leaves = [(0, GE, 400_000), (0, LT, 400_900)]
+    else:
+        v = rng.integers(0, 1_000_000, n).astype(np.uint32)
+        leaves = [(0, GT, 2_000_000)] if case == "none" else [(0, LT, 30_000)]
+    col = ops.Column.from_numpy(v)
+    want_count, want_rows = ops.scan_simple([col], leaves, want_rows=True)
+    cap = max(want_count // 3, 1) if case == "small_buffer" else n
+    out = ops.DeviceBuffer(cap * 4)
+    count = ops.scan_select([col], leaves, out)
+    assert count == want_count
+    m = min(count, cap)
+    assert np.array_equal(out.read(np.uint32, m), want_rows[:m])
+    if case == "clustered":
+        # the selection feeds an operator that takes one: ORDER BY the values over the selected rows
+        got = ops.sort_rows([col], [1], selection=out, count=count)
+        assert np.array_equal(got, want_rows[oracle.sort_rows([v[want_rows]], [1])])
