@@ -1015,7 +1015,8 @@ __device__ __forceinline__ unsigned long long small_int_bits(long long v)
   return sign | ((unsigned long long)(1023 + p) << 52) | ((a << (52 - p)) & 0xfffffffffffffull);
 }
 
-// round-half-even(x * 2^s) of a finite double x given by its bits; |x * 2^s| < 2^62 by the choice of s
+// x * 2^s rounded to the nearest whole number (ties away from zero), for a finite double x given by its
+// bits; |x * 2^s| < 2^62 by the choice of s
 __device__ __forceinline__ long long small_fixed(unsigned long long b, int s)
 {
   int e = (int)((b >> 52) & 0x7ffu);
@@ -1025,49 +1026,35 @@ __device__ __forceinline__ long long small_fixed(unsigned long long b, int s)
   int sh = e - 1075 + s;   // x * 2^s = m * 2^sh
   unsigned long long q;
   if (sh >= 0) q = sh > 10 ? (1ull << 62) : m << sh;   // past 2^62 only for a value outside the column's range
-  else if (sh <= -54) q = 0;   // below a half
   else
   {
-    uint32_t r = (uint32_t)(-sh);
-    unsigned long long whole = m >> r, rem = m & ((1ull << r) - 1ull), half = 1ull << (r - 1);
-    q = whole + ((rem > half || (rem == half && (whole & 1ull))) ? 1ull : 0ull);
+    // to nearest, ties away from zero: add half a unit of the last place kept, then shift (0 from 54 places down)
+    uint32_t r = (uint32_t)min(-sh, 63);
+    q = (m + (1ull << (r - 1))) >> r;
   }
   return (b >> 63) ? -(long long)q : (long long)q;
 }
 
-template <bool OWN>
-__device__ __forceinline__ void add96(uint32_t* l0, uint32_t* l1, uint32_t* l2, long long q)
+// Adds a 64-bit signed q into a 96-bit two's-complement number held as three 32-bit limbs shared by
+// several threads: shared atomics, each carry passed up once.
+__device__ __forceinline__ void add96_atomic(uint32_t* l0, uint32_t* l1, uint32_t* l2, long long q)
 {
   uint32_t lo = (uint32_t)q, hi = (uint32_t)((unsigned long long)q >> 32), top = q < 0 ? 0xffffffffu : 0u;
-  uint32_t old0;
-  if (OWN)
-  {
-    old0 = *l0;
-    *l0 = old0 + lo;
-  }
-  else
-    old0 = atomicAdd(l0, lo);
+  uint32_t old0 = atomicAdd(l0, lo);
   uint32_t mid = hi + ((old0 + lo < old0) ? 1u : 0u);
   top += mid < hi ? 1u : 0u;   // hi + carry passed 2^32
   if (mid)
   {
-    uint32_t old1;
-    if (OWN)
-    {
-      old1 = *l1;
-      *l1 = old1 + mid;
-    }
-    else
-      old1 = atomicAdd(l1, mid);
+    uint32_t old1 = atomicAdd(l1, mid);
     top += (old1 + mid < old1) ? 1u : 0u;
   }
-  if (top)
-  {
-    if (OWN) *l2 += top;
-    else atomicAdd(l2, top);
-  }
+  if (top) atomicAdd(l2, top);
 }
 
+// The tables in dynamic shared memory, word-major (word w of table k at w * copies + k), so that the lanes
+// of a warp, each on its own table, meet no bank conflict. With a table a thread (OWN) a sum is a u64
+// low part and a u32 high part, updated without atomics; with tables shared by threads, three u32 limbs
+// updated with atomics.
 template <bool OWN>
 __global__ void __launch_bounds__(HASH_THREADS) k_group_small(CqlLaunch a, uint64_t rows, uint32_t copies)
 {
@@ -1077,7 +1064,7 @@ __global__ void __launch_bounds__(HASH_THREADS) k_group_small(CqlLaunch a, uint6
   const uint32_t* key = (const uint32_t*)a.buf[0];
   uint32_t* out = (uint32_t*)a.buf[1 + SMALL_COLUMNS];
   uint32_t min_key = cql_word(a, 2), V = cql_word(a, 4), ncols = cql_word(a, 6), types = cql_word(a, 8), need = cql_word(a, 10);
-  // per column: its type, whether summed (and its limb slot), whether its extrema are kept, 2^s
+  // per column: its type, whether summed (and its sum slot), whether its extrema are kept, its scale
   uint32_t ctype[SMALL_COLUMNS], cslot[SMALL_COLUMNS], nsum = 0;
   bool csum[SMALL_COLUMNS], cext[SMALL_COLUMNS], cwhole[SMALL_COLUMNS];
   int cscale[SMALL_COLUMNS];
@@ -1087,19 +1074,25 @@ __global__ void __launch_bounds__(HASH_THREADS) k_group_small(CqlLaunch a, uint6
     ctype[c] = (types >> (4 * c)) & 0xfu;
     csum[c] = c < ncols && ((need >> c) & 1u);
     cext[c] = c < ncols && ((need >> (SMALL_COLUMNS + c)) & 1u);
-    int sc = (int)(short)(unsigned short)(a.push[6 + c / 4] >> (16 * (c % 4)));
+    cscale[c] = (int)(short)(unsigned short)(a.push[6 + c / 4] >> (16 * (c % 4)));
     cwhole[c] = ctype[c] == 1 || ctype[c] == 7;
-    cscale[c] = sc;
     cslot[c] = nsum;
     nsum += csum[c] ? 1u : 0u;
   }
-  uint32_t words = V * (1 + 3 * nsum);   // one table: V counts, then per summed column 3 limbs of V
-  for (uint32_t i = threadIdx.x; i < copies * words; i += blockDim.x) smem[i] = 0;
+  // counts [V][copies] (u32); OWN: sum lows [nsum][V][copies] (u64) then highs (u32); else limbs
+  // [nsum][3][V][copies] (u32)
+  // (copies is a power of two of at least 8, so the u64 lows start 8-byte aligned)
+  uint32_t* cnt = smem;
+  unsigned long long* sum_lo = (unsigned long long*)(smem + V * copies);
+  uint32_t* sum_hi = (uint32_t*)(sum_lo + nsum * V * copies);
+  uint32_t* limbs = smem + V * copies;
+  uint32_t total_words = V * copies * (1 + 3 * nsum);
+  for (uint32_t i = threadIdx.x; i < total_words; i += blockDim.x) smem[i] = 0;
   for (uint32_t i = threadIdx.x; i < SMALL_VALUES * SMALL_COLUMNS * 2; i += blockDim.x) s_ext[i] = (i & 1) ? 0ull : ~0ull;
   for (uint32_t i = threadIdx.x; i < SMALL_VALUES; i += blockDim.x) s_first[i] = 0xffffffffu;
   for (uint32_t i = threadIdx.x; i < SMALL_VALUES * SMALL_COLUMNS; i += blockDim.x) s_flags[i] = 0;
   __syncthreads();
-  uint32_t* table = smem + (threadIdx.x % copies) * words;
+  uint32_t copy = threadIdx.x % copies;
   // SMALL_ROWS rows a thread a step, a grid stride apart (each coalesced across the warp): the keys read
   // together, then each column's values together, so that a thread keeps several loads in flight
   const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
@@ -1117,8 +1110,8 @@ __global__ void __launch_bounds__(HASH_THREADS) k_group_small(CqlLaunch a, uint6
     {
       if (g[i] >= V) continue;
       uint32_t r = (uint32_t)(r0 + i * step);
-      if (OWN) table[g[i]] += 1;
-      else atomicAdd(&table[g[i]], 1u);
+      if (OWN) cnt[g[i] * copies + copy] += 1;
+      else atomicAdd(&cnt[g[i] * copies + copy], 1u);
       if (r < s_first[g[i]]) atomicMin(&s_first[g[i]], r);
     }
 #pragma unroll
@@ -1138,28 +1131,44 @@ __global__ void __launch_bounds__(HASH_THREADS) k_group_small(CqlLaunch a, uint6
       for (uint32_t i = 0; i < SMALL_ROWS; i++)
       {
         if (g[i] >= V) continue;
-        // the value as a whole number (whole-number columns, exact) and as the bits of its double
+        // the value as a whole number (whole-number columns, exact) and, where needed, as its double's bits
         long long whole = ctype[c] == 7 ? (long long)(int)(uint32_t)raw[i] : (long long)raw[i];
-        unsigned long long b = cwhole[c] ? small_int_bits(whole) : ctype[c] == 3 ? small_f32_bits((uint32_t)raw[i]) : raw[i];
-        bool finite = ((b >> 52) & 0x7ffu) != 0x7ffu;
+        unsigned long long b = 0;
+        if (!cwhole[c]) b = ctype[c] == 3 ? small_f32_bits((uint32_t)raw[i]) : raw[i];
+        bool finite = cwhole[c] || ((b >> 52) & 0x7ffu) != 0x7ffu;
         if (csum[c])
         {
           if (finite)
           {
             long long q = cwhole[c] ? whole : small_fixed(b, cscale[c]);
-            uint32_t* l = table + V * (1 + 3 * cslot[c]) + g[i];
-            add96<OWN>(l, l + V, l + 2 * V, q);
+            uint32_t at = (cslot[c] * V + g[i]) * copies + copy;
+            if (OWN)
+            {
+              unsigned long long old = sum_lo[at], now = old + (unsigned long long)q;
+              sum_lo[at] = now;
+              uint32_t top = (q < 0 ? 0xffffffffu : 0u) + (now < old ? 1u : 0u);
+              if (top) sum_hi[at] += top;
+            }
+            else
+            {
+              uint32_t at3 = ((cslot[c] * 3) * V + g[i]) * copies + copy, stride = V * copies;
+              add96_atomic(limbs + at3, limbs + at3 + stride, limbs + at3 + 2 * stride, q);
+            }
           }
           else
             atomicOr(&s_flags[g[i] * SMALL_COLUMNS + c], (b & 0xfffffffffffffull) ? 1u : (b >> 63) ? 4u : 2u);
         }
-        if (cext[c] && (finite || !(b & 0xfffffffffffffull)))   // NaN is left out
+        if (cext[c])
         {
-          if ((b << 1) == 0) b = 0;   // -0.0 compares equal to +0.0
-          unsigned long long o = (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
-          unsigned long long* e = s_ext + (g[i] * SMALL_COLUMNS + c) * 2;
-          if (o < e[0]) atomicMin(&e[0], o);
-          if (o > e[1]) atomicMax(&e[1], o);
+          if (cwhole[c]) b = small_int_bits(whole);
+          if (finite || !(b & 0xfffffffffffffull))   // NaN is left out
+          {
+            if ((b << 1) == 0) b = 0;   // -0.0 compares equal to +0.0
+            unsigned long long o = (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+            unsigned long long* e = s_ext + (g[i] * SMALL_COLUMNS + c) * 2;
+            if (o < e[0]) atomicMin(&e[0], o);
+            if (o > e[1]) atomicMax(&e[1], o);
+          }
         }
       }
     }
@@ -1177,33 +1186,37 @@ __global__ void __launch_bounds__(HASH_THREADS) k_group_small(CqlLaunch a, uint6
     if (part == 0)
     {
       unsigned long long n = 0;
-      for (uint32_t k = 0; k < copies; k++) n += smem[k * words + g];
+      for (uint32_t k = 0; k < copies; k++) n += cnt[g * copies + k];
       if (n) atomicAdd(&counts[g], n);
+      continue;
     }
-    else
+    uint32_t slot = part - 1;
+    __int128 total = 0;
+    for (uint32_t k = 0; k < copies; k++)
     {
-      __int128 total = 0;
-      uint32_t base = V * (1 + 3 * (part - 1)) + g;
-      for (uint32_t k = 0; k < copies; k++)
+      if (OWN)
       {
-        const uint32_t* l = smem + k * words + base;
-        unsigned long long low = (unsigned long long)l[0] | ((unsigned long long)l[V] << 32);
-        total += (__int128)(((unsigned __int128)(unsigned long long)(long long)(int)l[2 * V] << 64) | low);
+        uint32_t at = (slot * V + g) * copies + k;
+        total += (__int128)(((unsigned __int128)(unsigned long long)(long long)(int)sum_hi[at] << 64) | sum_lo[at]);
       }
-      if (total != 0)
+      else
       {
-        // the summed column whose limb slot this is
-        uint32_t c = 0;
-#pragma unroll
-        for (uint32_t j = 0; j < SMALL_COLUMNS; j++)
-          if (csum[j] && cslot[j] == part - 1) c = j;
-        unsigned long long lo = (unsigned long long)total, hi = (unsigned long long)((unsigned __int128)total >> 64);
-        unsigned long long* at = sums + (g * SMALL_COLUMNS + c) * 2;
-        unsigned long long old = atomicAdd(&at[0], lo);
-        hi += (old + lo < old) ? 1ull : 0ull;
-        if (hi) atomicAdd(&at[1], hi);
+        uint32_t at3 = ((slot * 3) * V + g) * copies + k, stride = V * copies;
+        unsigned long long low = (unsigned long long)limbs[at3] | ((unsigned long long)limbs[at3 + stride] << 32);
+        total += (__int128)(((unsigned __int128)(unsigned long long)(long long)(int)limbs[at3 + 2 * stride] << 64) | low);
       }
     }
+    if (total == 0) continue;
+    // the summed column whose slot this is
+    uint32_t c = 0;
+#pragma unroll
+    for (uint32_t j = 0; j < SMALL_COLUMNS; j++)
+      if (csum[j] && cslot[j] == slot) c = j;
+    unsigned long long lo = (unsigned long long)total, hi = (unsigned long long)((unsigned __int128)total >> 64);
+    unsigned long long* at = sums + (g * SMALL_COLUMNS + c) * 2;
+    unsigned long long old = atomicAdd(&at[0], lo);
+    hi += (old + lo < old) ? 1ull : 0ull;
+    if (hi) atomicAdd(&at[1], hi);
   }
   for (uint32_t t = threadIdx.x; t < V * SMALL_COLUMNS; t += blockDim.x)
   {
