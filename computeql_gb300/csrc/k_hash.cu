@@ -1059,38 +1059,38 @@ template <bool OWN>
 __global__ void __launch_bounds__(HASH_THREADS) k_group_small(CqlLaunch a, uint64_t rows, uint32_t copies)
 {
   extern __shared__ __align__(16) uint32_t smem[];
-  __shared__ unsigned long long s_ext[SMALL_VALUES * SMALL_COLUMNS * 2];
-  __shared__ uint32_t s_first[SMALL_VALUES], s_flags[SMALL_VALUES * SMALL_COLUMNS];
+  // extrema [column][min | max][value] and flags [column][value]: a warp's lanes on different key values
+  // meet different banks
+  __shared__ unsigned long long s_ext[SMALL_COLUMNS * 2 * SMALL_VALUES];
+  __shared__ uint32_t s_first[SMALL_VALUES], s_flags[SMALL_COLUMNS * SMALL_VALUES];
+  // per column: type, sum slot, scale and what is kept (1 SUM, 2 MIN/MAX, 4 a whole-number column)
+  __shared__ uint32_t s_type[SMALL_COLUMNS], s_slot[SMALL_COLUMNS], s_what[SMALL_COLUMNS];
+  __shared__ int s_scale[SMALL_COLUMNS];
   const uint32_t* key = (const uint32_t*)a.buf[0];
   uint32_t* out = (uint32_t*)a.buf[1 + SMALL_COLUMNS];
   uint32_t min_key = cql_word(a, 2), V = cql_word(a, 4), ncols = cql_word(a, 6), types = cql_word(a, 8), need = cql_word(a, 10);
-  // per column: its type, whether summed (and its sum slot), whether its extrema are kept, its scale
-  uint32_t ctype[SMALL_COLUMNS], cslot[SMALL_COLUMNS], nsum = 0;
-  bool csum[SMALL_COLUMNS], cext[SMALL_COLUMNS], cwhole[SMALL_COLUMNS];
-  int cscale[SMALL_COLUMNS];
-#pragma unroll
-  for (uint32_t c = 0; c < SMALL_COLUMNS; c++)
+  uint32_t nsum = 0;
+  for (uint32_t c = 0; c < ncols; c++) nsum += (need >> c) & 1u;
+  if (threadIdx.x < SMALL_COLUMNS)
   {
-    ctype[c] = (types >> (4 * c)) & 0xfu;
-    csum[c] = c < ncols && ((need >> c) & 1u);
-    cext[c] = c < ncols && ((need >> (SMALL_COLUMNS + c)) & 1u);
-    cscale[c] = (int)(short)(unsigned short)(a.push[6 + c / 4] >> (16 * (c % 4)));
-    cwhole[c] = ctype[c] == 1 || ctype[c] == 7;
-    cslot[c] = nsum;
-    nsum += csum[c] ? 1u : 0u;
+    uint32_t c = threadIdx.x, t = (types >> (4 * c)) & 0xfu;
+    s_type[c] = t;
+    s_slot[c] = __popc(need & ((1u << c) - 1u) & 0xffu);
+    s_what[c] = c < ncols ? (((need >> c) & 1u) | (((need >> (SMALL_COLUMNS + c)) & 1u) << 1) | ((t == 1 || t == 7) ? 4u : 0u)) : 0u;
+    s_scale[c] = (int)(short)(unsigned short)(a.push[6 + c / 4] >> (16 * (c % 4)));
   }
   // counts [V][copies] (u32); OWN: sum lows [nsum][V][copies] (u64) then highs (u32); else limbs
-  // [nsum][3][V][copies] (u32)
-  // (copies is a power of two of at least 8, so the u64 lows start 8-byte aligned)
+  // [nsum][3][V][copies] (u32) (copies is a power of two of at least 8, so the u64 lows start 8-byte aligned)
   uint32_t* cnt = smem;
   unsigned long long* sum_lo = (unsigned long long*)(smem + V * copies);
   uint32_t* sum_hi = (uint32_t*)(sum_lo + nsum * V * copies);
   uint32_t* limbs = smem + V * copies;
   uint32_t total_words = V * copies * (1 + 3 * nsum);
   for (uint32_t i = threadIdx.x; i < total_words; i += blockDim.x) smem[i] = 0;
-  for (uint32_t i = threadIdx.x; i < SMALL_VALUES * SMALL_COLUMNS * 2; i += blockDim.x) s_ext[i] = (i & 1) ? 0ull : ~0ull;
+  for (uint32_t i = threadIdx.x; i < SMALL_COLUMNS * 2 * SMALL_VALUES; i += blockDim.x)
+    s_ext[i] = ((i / SMALL_VALUES) & 1u) ? 0ull : ~0ull;
   for (uint32_t i = threadIdx.x; i < SMALL_VALUES; i += blockDim.x) s_first[i] = 0xffffffffu;
-  for (uint32_t i = threadIdx.x; i < SMALL_VALUES * SMALL_COLUMNS; i += blockDim.x) s_flags[i] = 0;
+  for (uint32_t i = threadIdx.x; i < SMALL_COLUMNS * SMALL_VALUES; i += blockDim.x) s_flags[i] = 0;
   __syncthreads();
   uint32_t copy = threadIdx.x % copies;
   // SMALL_ROWS rows a thread a step, a grid stride apart (each coalesced across the warp): the keys read
@@ -1114,10 +1114,12 @@ __global__ void __launch_bounds__(HASH_THREADS) k_group_small(CqlLaunch a, uint6
       else atomicAdd(&cnt[g[i] * copies + copy], 1u);
       if (r < s_first[g[i]]) atomicMin(&s_first[g[i]], r);
     }
-#pragma unroll
-    for (uint32_t c = 0; c < SMALL_COLUMNS; c++)
+#pragma unroll 1
+    for (uint32_t c = 0; c < ncols; c++)
     {
-      if (!csum[c] && !cext[c]) continue;
+      uint32_t type = s_type[c], what = s_what[c], slot = s_slot[c];
+      int scale = s_scale[c];
+      bool whole_col = (what & 4u) != 0;
       const void* col = a.buf[1 + c];
       unsigned long long raw[SMALL_ROWS];
 #pragma unroll
@@ -1125,25 +1127,25 @@ __global__ void __launch_bounds__(HASH_THREADS) k_group_small(CqlLaunch a, uint6
       {
         uint64_t r = r0 + i * step;
         raw[i] = 0;
-        if (r < rows) raw[i] = ctype[c] == 4 ? ((const unsigned long long*)col)[r] : ((const uint32_t*)col)[r];
+        if (r < rows) raw[i] = type == 4 ? ((const unsigned long long*)col)[r] : ((const uint32_t*)col)[r];
       }
 #pragma unroll
       for (uint32_t i = 0; i < SMALL_ROWS; i++)
       {
         if (g[i] >= V) continue;
         // the value as a whole number (whole-number columns, exact) and, where needed, as its double's bits
-        long long whole = ctype[c] == 7 ? (long long)(int)(uint32_t)raw[i] : (long long)raw[i];
+        long long whole = type == 7 ? (long long)(int)(uint32_t)raw[i] : (long long)raw[i];
         unsigned long long b = 0;
-        if (!cwhole[c]) b = ctype[c] == 3 ? small_f32_bits((uint32_t)raw[i]) : raw[i];
-        bool finite = cwhole[c] || ((b >> 52) & 0x7ffu) != 0x7ffu;
-        if (csum[c])
+        if (!whole_col) b = type == 3 ? small_f32_bits((uint32_t)raw[i]) : raw[i];
+        bool finite = whole_col || ((b >> 52) & 0x7ffu) != 0x7ffu;
+        if (what & 1u)
         {
           if (finite)
           {
-            long long q = cwhole[c] ? whole : small_fixed(b, cscale[c]);
-            uint32_t at = (cslot[c] * V + g[i]) * copies + copy;
+            long long q = whole_col ? whole : small_fixed(b, scale);
             if (OWN)
             {
+              uint32_t at = (slot * V + g[i]) * copies + copy;
               unsigned long long old = sum_lo[at], now = old + (unsigned long long)q;
               sum_lo[at] = now;
               uint32_t top = (q < 0 ? 0xffffffffu : 0u) + (now < old ? 1u : 0u);
@@ -1151,23 +1153,23 @@ __global__ void __launch_bounds__(HASH_THREADS) k_group_small(CqlLaunch a, uint6
             }
             else
             {
-              uint32_t at3 = ((cslot[c] * 3) * V + g[i]) * copies + copy, stride = V * copies;
+              uint32_t at3 = ((slot * 3) * V + g[i]) * copies + copy, stride = V * copies;
               add96_atomic(limbs + at3, limbs + at3 + stride, limbs + at3 + 2 * stride, q);
             }
           }
           else
-            atomicOr(&s_flags[g[i] * SMALL_COLUMNS + c], (b & 0xfffffffffffffull) ? 1u : (b >> 63) ? 4u : 2u);
+            atomicOr(&s_flags[c * SMALL_VALUES + g[i]], (b & 0xfffffffffffffull) ? 1u : (b >> 63) ? 4u : 2u);
         }
-        if (cext[c])
+        if (what & 2u)
         {
-          if (cwhole[c]) b = small_int_bits(whole);
+          if (whole_col) b = small_int_bits(whole);
           if (finite || !(b & 0xfffffffffffffull))   // NaN is left out
           {
             if ((b << 1) == 0) b = 0;   // -0.0 compares equal to +0.0
             unsigned long long o = (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
-            unsigned long long* e = s_ext + (g[i] * SMALL_COLUMNS + c) * 2;
+            unsigned long long* e = s_ext + c * 2 * SMALL_VALUES + g[i];
             if (o < e[0]) atomicMin(&e[0], o);
-            if (o > e[1]) atomicMax(&e[1], o);
+            if (o > e[SMALL_VALUES]) atomicMax(&e[SMALL_VALUES], o);
           }
         }
       }
@@ -1209,9 +1211,8 @@ __global__ void __launch_bounds__(HASH_THREADS) k_group_small(CqlLaunch a, uint6
     if (total == 0) continue;
     // the summed column whose slot this is
     uint32_t c = 0;
-#pragma unroll
-    for (uint32_t j = 0; j < SMALL_COLUMNS; j++)
-      if (csum[j] && cslot[j] == slot) c = j;
+    for (uint32_t j = 0; j < ncols; j++)
+      if ((s_what[j] & 1u) && s_slot[j] == slot) c = j;
     unsigned long long lo = (unsigned long long)total, hi = (unsigned long long)((unsigned __int128)total >> 64);
     unsigned long long* at = sums + (g * SMALL_COLUMNS + c) * 2;
     unsigned long long old = atomicAdd(&at[0], lo);
@@ -1220,11 +1221,14 @@ __global__ void __launch_bounds__(HASH_THREADS) k_group_small(CqlLaunch a, uint6
   }
   for (uint32_t t = threadIdx.x; t < V * SMALL_COLUMNS; t += blockDim.x)
   {
-    uint32_t g = t / SMALL_COLUMNS;
-    if (t % SMALL_COLUMNS == 0 && s_first[g] != 0xffffffffu) atomicMin(&out[2 * V + g], s_first[g]);
-    if (s_flags[t]) atomicOr(&flags[t], s_flags[t]);
-    if (s_ext[2 * t] != ~0ull) atomicMin(&ext[2 * t], s_ext[2 * t]);
-    if (s_ext[2 * t + 1] != 0ull) atomicMax(&ext[2 * t + 1], s_ext[2 * t + 1]);
+    // t = g * SMALL_COLUMNS + c in the output's order
+    uint32_t g = t / SMALL_COLUMNS, c = t % SMALL_COLUMNS;
+    if (c == 0 && s_first[g] != 0xffffffffu) atomicMin(&out[2 * V + g], s_first[g]);
+    uint32_t f = s_flags[c * SMALL_VALUES + g];
+    if (f) atomicOr(&flags[t], f);
+    unsigned long long lo = s_ext[c * 2 * SMALL_VALUES + g], hi = s_ext[c * 2 * SMALL_VALUES + SMALL_VALUES + g];
+    if (lo != ~0ull) atomicMin(&ext[2 * t], lo);
+    if (hi != 0ull) atomicMax(&ext[2 * t + 1], hi);
   }
 }
 

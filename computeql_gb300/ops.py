@@ -455,6 +455,17 @@ class HashOutputs:
         self.results = np.zeros(max(max_groups, 1) * max(exprs, 1), dtype=np.float64)
 
 
+def _key_values_bound(keys):
+    """How many distinct key tuples the keys can form, from the whole-number keys' zone ranges (no bound
+    for other keys): the most groups a GROUP BY over them can have."""
+    bound = 1
+    for k in keys:
+        if k.ctype not in (TYPE_U32, TYPE_I32) or k.zone is None:
+            return 1 << 62
+        bound *= int(k.zone[1]) - int(k.zone[0]) + 1
+    return bound
+
+
 def group_hash(keys, funcs, args, params=None, group_hint=0, path=0, max_groups=None, out=None):
     """Hash GROUP BY -> dict(groups, repr_row[G], counts[G], results[G, E], path). With `out` (a HashOutputs)
     the results are views of its arrays, valid until its next use."""
@@ -472,7 +483,7 @@ def group_hash(keys, funcs, args, params=None, group_hint=0, path=0, max_groups=
         mg = min(out.max_groups, max_groups if max_groups is not None else out.max_groups)
         repr_row, counts, results = out.repr_row, out.counts, out.results
     else:
-        mg = max_groups if max_groups is not None else rows
+        mg = max_groups if max_groups is not None else min(rows, _key_values_bound(keys))
         repr_row = np.empty(max(mg, 1), dtype=np.uint64)
         counts = np.empty(max(mg, 1), dtype=np.uint64)
         results = np.empty(max(mg, 1) * e, dtype=np.float64)
