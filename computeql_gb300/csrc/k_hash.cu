@@ -1232,6 +1232,194 @@ __global__ void __launch_bounds__(HASH_THREADS) k_group_small(CqlLaunch a, uint6
   }
 }
 
+// cql_group_direct: GROUP BY one whole-number key of a dense range too large for shared memory (R values
+// from the smallest, R <= 2^24) over whole-number arguments, straight into tables in device memory indexed
+// by key - min (a few MB: they stay in L2), with atomics whose results are not read. Binding 0 the key (u32
+// words), 1..8 the argument columns (u32/i32 words, values inside the i32 range), 9 the tables (u32
+// words): counts [R] at 0, first rows [R] at R (all 0xffffffff before), then expression e's table at word
+// offset slot 4 + e/2 (half e%2): SUM/AVG an i64 [R] (8-byte aligned), MIN/MAX an i32 [R] (INT32_MAX /
+// INT32_MIN before). Words: 0 rows, 2 the smallest key (bits), 3 R, 4 expressions, 5 their functions (4
+// bits each), 6 per expression 1 = an I32 argument.
+#define DIRECT_ROWS 4
+
+__global__ void __launch_bounds__(HASH_THREADS) k_group_direct(CqlLaunch a, uint64_t rows)
+{
+  const uint32_t* key = (const uint32_t*)a.buf[0];
+  uint32_t* tab = (uint32_t*)a.buf[9];
+  uint32_t kmin = cql_word(a, 2), R = cql_word(a, 3), exprs = min(cql_word(a, 4), 8u), funcs = cql_word(a, 5), sgn = cql_word(a, 6);
+  uint32_t* cnt = tab;
+  uint32_t* first = tab + R;
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t r0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r0 < rows; r0 += step * DIRECT_ROWS)
+  {
+    uint32_t k[DIRECT_ROWS];
+#pragma unroll
+    for (uint32_t i = 0; i < DIRECT_ROWS; i++)
+    {
+      uint64_t r = r0 + i * step;
+      k[i] = r < rows ? key[r] - kmin : 0xffffffffu;
+    }
+#pragma unroll
+    for (uint32_t i = 0; i < DIRECT_ROWS; i++)
+    {
+      if (k[i] >= R) continue;
+      atomicAdd(&cnt[k[i]], 1u);
+      atomicMin(&first[k[i]], (uint32_t)(r0 + i * step));
+    }
+#pragma unroll 1
+    for (uint32_t e = 0; e < exprs; e++)
+    {
+      uint32_t f = (funcs >> (4 * e)) & 0xfu;
+      if (f == FUNC_COUNT) continue;
+      const uint32_t* col = (const uint32_t*)a.buf[1 + e];
+      bool is_signed = (sgn >> e) & 1u;
+      uint32_t off = cql_word(a, 8 + e);
+      uint32_t v[DIRECT_ROWS];
+#pragma unroll
+      for (uint32_t i = 0; i < DIRECT_ROWS; i++)
+      {
+        uint64_t r = r0 + i * step;
+        v[i] = (r < rows && k[i] < R) ? col[r] : 0u;
+      }
+#pragma unroll
+      for (uint32_t i = 0; i < DIRECT_ROWS; i++)
+      {
+        if (k[i] >= R) continue;
+        if (f == FUNC_SUM || f == FUNC_AVG)
+        {
+          long long x = is_signed ? (long long)(int)v[i] : (long long)v[i];
+          atomicAdd((unsigned long long*)(tab + off) + k[i], (unsigned long long)x);
+        }
+        else if (f == FUNC_MIN)
+          atomicMin((int*)(tab + off) + k[i], (int)v[i]);
+        else
+          atomicMax((int*)(tab + off) + k[i], (int)v[i]);
+      }
+    }
+  }
+}
+
+// cql_group_direct_bits: binding 0 the counts [R], 1 a bitmap of the present keys out (bit k = count > 0),
+// 2 the number of present keys (u32, zero before); word 0 R.
+__global__ void __launch_bounds__(HASH_THREADS) k_group_direct_bits(CqlLaunch a, uint32_t R)
+{
+  const uint32_t* cnt = (const uint32_t*)a.buf[0];
+  uint32_t* bits = (uint32_t*)a.buf[1];
+  uint32_t* present = (uint32_t*)a.buf[2];
+  uint32_t words = (R + 31) / 32;
+  for (uint64_t w0 = (uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x / 32); w0 < words; w0 += (uint64_t)gridDim.x * (blockDim.x / 32))
+  {
+    uint64_t k = w0 * 32 + (threadIdx.x & 31);
+    uint32_t m = __ballot_sync(0xffffffffu, k < R && cnt[k] != 0);
+    if ((threadIdx.x & 31) == 0)
+    {
+      bits[w0] = m;
+      if (m) atomicAdd(present, (uint32_t)__popc(m));
+    }
+  }
+}
+
+// cql_group_direct_emit: the groups in key order in the caller's layout: binding 0 the tables, 1 the present
+// keys (ascending offsets from the smallest key), 2 the number of them, 3 representative (first) rows out
+// (u64), 4 counts out (u64), 5 results out (f64 [group][expr]); words as cql_group_direct's (0 rows unused,
+// 3 R, 4 expressions, 5 functions, 8.. the table offsets). The results are those of the fixed-point
+// reduce at scale 0: the double of the sum, AVG that divided by the count, MIN/MAX the double of the value.
+__global__ void __launch_bounds__(HASH_THREADS) k_group_direct_emit(CqlLaunch a, uint64_t cap)
+{
+  const uint32_t* tab = (const uint32_t*)a.buf[0];
+  const uint32_t* list = (const uint32_t*)a.buf[1];
+  uint32_t groups = *(const uint32_t*)a.buf[2];
+  unsigned long long* repr = (unsigned long long*)a.buf[3];
+  unsigned long long* counts = (unsigned long long*)a.buf[4];
+  double* results = (double*)a.buf[5];
+  uint32_t R = cql_word(a, 3), exprs = min(cql_word(a, 4), 8u), funcs = cql_word(a, 5);
+  uint64_t n = min((uint64_t)groups, cap);
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (uint64_t)gridDim.x * blockDim.x)
+  {
+    uint32_t k = list[g];
+    if (k >= R) continue;
+    uint32_t c = tab[k];
+    repr[g] = tab[R + k];
+    counts[g] = c;
+    for (uint32_t e = 0; e < exprs; e++)
+    {
+      uint32_t f = (funcs >> (4 * e)) & 0xfu, off = cql_word(a, 8 + e);
+      double r;
+      if (f == FUNC_COUNT) r = (double)c;
+      else if (f == FUNC_SUM || f == FUNC_AVG)
+      {
+        double sum = (double)((const long long*)(tab + off))[k];
+        r = f == FUNC_AVG ? (c > 0 ? sum / (double)c : 0.0) : sum;
+      }
+      else r = (double)((const int*)(tab + off))[k];
+      results[g * exprs + e] = r;
+    }
+  }
+}
+
+static int launch_group_direct(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint64_t rows = a.push[0];
+  uint32_t R = cql_word(a, 3), exprs = cql_word(a, 4), funcs = cql_word(a, 5);
+  if (rows == 0) return 0;
+  if (R == 0 || R > (1u << 24) || exprs == 0 || exprs > 8 || rows > 0xffffffffull || a.bytes[0] < rows * 4) return (int)cudaErrorInvalidValue;
+  uint64_t words = a.bytes[9] / 4;
+  if (words < 2ull * R) return (int)cudaErrorInvalidValue;
+  for (uint32_t e = 0; e < exprs; e++)
+  {
+    uint32_t f = (funcs >> (4 * e)) & 0xfu;
+    if (f == FUNC_COUNT) continue;
+    if (f > FUNC_MAX || a.bytes[1 + e] < rows * 4) return (int)cudaErrorInvalidValue;
+    uint64_t off = cql_word(a, 8 + e), need = (f == FUNC_SUM || f == FUNC_AVG) ? 2ull * R : R;
+    if (off < 2ull * R || off + need > words || ((f == FUNC_SUM || f == FUNC_AVG) && (off & 1))) return (int)cudaErrorInvalidValue;
+  }
+  k_group_direct<<<cql_stream_grid((rows + HASH_THREADS * DIRECT_ROWS - 1) / (HASH_THREADS * DIRECT_ROWS), 8), HASH_THREADS, 0, stream>>>(a, rows);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+static int launch_group_direct_bits(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint32_t R = cql_word(a, 0);
+  if (R == 0) return 0;
+  if (a.bytes[0] < (uint64_t)R * 4 || a.bytes[1] < (uint64_t)((R + 31) / 32) * 4 || a.bytes[2] < 4) return (int)cudaErrorInvalidValue;
+  uint64_t warps = (R + 31) / 32;
+  k_group_direct_bits<<<cql_stream_grid((warps + HASH_THREADS / 32 - 1) / (HASH_THREADS / 32), 8), HASH_THREADS, 0, stream>>>(a, R);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
+static int launch_group_direct_emit(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)
+{
+  (void)gws;
+  (void)lws;
+  uint32_t R = cql_word(a, 3), exprs = cql_word(a, 4), funcs = cql_word(a, 5);
+  if (R == 0 || exprs == 0 || exprs > 8 || a.bytes[2] < 4) return (int)cudaErrorInvalidValue;
+  uint64_t words = a.bytes[0] / 4;
+  if (words < 2ull * R) return (int)cudaErrorInvalidValue;
+  for (uint32_t e = 0; e < exprs; e++)
+  {
+    uint32_t f = (funcs >> (4 * e)) & 0xfu;
+    if (f == FUNC_COUNT) continue;
+    uint64_t off = cql_word(a, 8 + e), need = (f == FUNC_SUM || f == FUNC_AVG) ? 2ull * R : R;
+    if (f > FUNC_MAX || off + need > words) return (int)cudaErrorInvalidValue;
+  }
+  // the most groups each output holds
+  uint64_t cap = a.bytes[1] / 4;
+  cap = std::min<uint64_t>(cap, a.bytes[3] / 8);
+  cap = std::min<uint64_t>(cap, a.bytes[4] / 8);
+  cap = std::min<uint64_t>(cap, a.bytes[5] / (8ull * exprs));
+  if (cap == 0) return 0;
+  uint64_t most = std::min<uint64_t>(cap, R);
+  k_group_direct_emit<<<cql_stream_grid((most + HASH_THREADS - 1) / HASH_THREADS, 8), HASH_THREADS, 0, stream>>>(a, cap);
+  CQL_LAUNCH_CHECK();
+  return 0;
+}
+
 // cql_finite_magnitude: the largest finite |x| of an f32/f64 column, as the bits of a non-negative double
 // (whose order is the bits' order): binding 0 the column, 1 the result (u64, zero before); word 0 rows,
 // word 2 the CQL type (F32 or F64). The small-key GROUP BY's scale for a column with no finite range.
@@ -1560,6 +1748,9 @@ const CqlKernelDesc cql_kernels_hash[] = {
   { "cql_gather_columns", launch_gather_columns },
   { "cql_finite_magnitude", launch_finite_magnitude },
   { "cql_group_small", launch_group_small },
+  { "cql_group_direct", launch_group_direct },
+  { "cql_group_direct_bits", launch_group_direct_bits },
+  { "cql_group_direct_emit", launch_group_direct_emit },
   { "cql_group_finish", launch_group_finish },
   { "cql_gather_string_lengths", launch_gather_string_lengths },
   { "cql_gather_string_bytes", launch_gather_string_bytes },

@@ -161,7 +161,15 @@ int cqlops_gather_rows(const CqlColumn* columns, uint32_t column_count, const ui
         cqlcuda_kernel_set_arg_u64(k, 2, n);
         cqlcuda_batch_kernel_execute(b, k, (uint32_t)count, QE_GPU_WORKGROUP_SIZE);
       }
-      for (uint32_t c = 0; c < column_count; c++) cqlcuda_batch_buffer_read_at(b, dest, section[c], out_values[c], count * sizes[c]);
+      /* outputs laid out as the device sections are (one host block, each column at its section's offset):
+         one read of the whole block; else a read a column */
+      int contiguous = 1;
+      for (uint32_t c = 1; c < column_count && contiguous; c++)
+        contiguous = (const char*)out_values[c] == (const char*)out_values[0] + section[c];
+      if (contiguous)
+        cqlcuda_batch_buffer_read_at(b, dest, 0, out_values[0], section[column_count - 1] + count * sizes[column_count - 1]);
+      else
+        for (uint32_t c = 0; c < column_count; c++) cqlcuda_batch_buffer_read_at(b, dest, section[c], out_values[c], count * sizes[c]);
     }
     int ended = cqlcuda_batch_end(b);
     ok = ok && ended;

@@ -321,7 +321,7 @@ static int simple_leaf_words(uint32_t* words, uint32_t slot, const CqlColumn* co
    first min(count, cap) rows land in out_rows; count is the bitmap's population. */
 /* Enqueues into batch b the rows of a selection bitmap of `rows` rows, ascending, into `list` (at most its
    size / 4 of them; the emit kernel stops there). */
-static int bitmap_rows_enqueue(CqlBatch* b, CqlBuffer* bitmap, uint64_t first_row, uint64_t rows, CqlBuffer* list)
+int cqlops_bitmap_rows_enqueue(CqlBatch* b, CqlBuffer* bitmap, uint64_t first_row, uint64_t rows, CqlBuffer* list)
 {
   uint64_t words = (rows + 31) / 32, blocks = (words + 255) / 256, scan_blocks = (blocks + 255) / 256;
   if (words == 0) return 1;
@@ -371,7 +371,7 @@ int cqlops_bitmap_rows(CqlBuffer* bitmap, uint64_t first_row, uint64_t rows, uin
   CqlBuffer* list = pooled("bitmap_rows", n * 4, CQLCUDA_BUFFER_READ_WRITE);
   if (!list) return 0;
   CqlBatch* b = cqlcuda_batch_begin(0, n * 4);
-  if (!bitmap_rows_enqueue(b, bitmap, first_row, rows, list))
+  if (!cqlops_bitmap_rows_enqueue(b, bitmap, first_row, rows, list))
   {
     cqlcuda_batch_end(b);
     return 0;
@@ -502,7 +502,7 @@ static int scan_simple_run(const CqlColumn* columns, uint32_t column_count, cons
     cqlcuda_batch_kernel_execute(batch, k, (uint32_t)threads, QE_GPU_WORKGROUP_SIZE);
   }
   /* a device selection: the rows are listed in the same batch (the list stops at the buffer's size) */
-  if (out_selection && !bitmap_rows_enqueue(batch, output, bitmap_first, bitmap_end - bitmap_first, out_selection))
+  if (out_selection && !cqlops_bitmap_rows_enqueue(batch, output, bitmap_first, bitmap_end - bitmap_first, out_selection))
   {
     cqlcuda_batch_end(batch);
     free(skip_bits);

@@ -567,6 +567,122 @@ static int group_small_key(const CqlColumn* key, uint32_t expr_count, const uint
   return group_small_fused(key, values, kmin, expr_count, funcs, args, max_groups, out_group_count, out_repr_row, out_counts, out_results);
 }
 
+/* ---- path 4: one whole-number key of a dense range too large for shared memory, in tables indexed by key ----
+   A key whose zone range holds 65537 to 2^24 values (past the dense group-by's 65536 and at most 8 times the
+   rows) with whole-number COUNT/SUM/AVG/MIN/MAX: counts, first rows, sums (i64), minimums and maximums (i32)
+   in device tables indexed by key - min (cql_group_direct: a few MB, which stay in L2), then the present keys
+   listed in key order and the groups written in the caller's layout on the device. No hashing, no member
+   pass; the results are those of the fixed-point reduce at scale 0. Gives way (-1) when the query does not
+   fit. */
+#define DIRECT_MIN_VALUES 65537ull
+#define DIRECT_MAX_VALUES (1ull << 24)
+
+static int group_direct(const CqlColumn* key, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* args, uint64_t max_groups,
+                        uint64_t* out_group_count, uint64_t* out_repr_row, uint64_t* out_counts, double* out_results)
+{
+  if (!(key->type == CQLOPS_TYPE_U32 || key->type == CQLOPS_TYPE_I32) || key->width != 0 || !key->buffer || !key->has_range) return -1;
+  double span = key->zone_max - key->zone_min;
+  uint64_t rows = key->rows;
+  if (!(span >= 0.0) || span + 1.0 > (double)DIRECT_MAX_VALUES || span + 1.0 < (double)DIRECT_MIN_VALUES || span + 1.0 > 8.0 * (double)rows)
+    return -1;
+  uint32_t R = (uint32_t)span + 1u;
+  uint32_t func_codes = 0, signed_args = 0, offsets[8] = { 0 };
+  uint64_t words = 2ull * R;
+  for (uint32_t e = 0; e < expr_count; e++)
+  {
+    uint32_t f = funcs[e];
+    if (f > CQLOPS_FUNC_MAX) return -1;
+    func_codes |= f << (4 * e);
+    if (f == CQLOPS_FUNC_COUNT) continue;
+    const CqlColumn* c = args[e];
+    if (!c || c->rows != rows || c->width != 0 || !c->buffer || !whole_number_arg(c)) return -1;
+    if (c->type == CQLOPS_TYPE_I32) signed_args |= 1u << e;
+    if (f == CQLOPS_FUNC_SUM || f == CQLOPS_FUNC_AVG)
+    {
+      words = (words + 1) & ~1ull;   /* i64 tables start 8-byte aligned */
+      offsets[e] = (uint32_t)words;
+      words += 2ull * R;
+    }
+    else
+    {
+      offsets[e] = (uint32_t)words;
+      words += R;
+    }
+  }
+  if (words > 0xffffffffull) return -1;
+  uint64_t most = R < rows ? R : rows;
+  uint64_t out_cap = most < max_groups ? most : max_groups;
+  if (out_cap == 0) out_cap = 1;
+  CqlBuffer* tab = pooled("group_direct_tables", words * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* bits = pooled("group_direct_bits", ((R + 31ull) / 32) * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* present = pooled("group_direct_present", 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* list = pooled("group_direct_list", most * 4, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* repr = pooled("group_direct_repr", out_cap * 8, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* cnts = pooled("group_direct_counts", out_cap * 8, CQLCUDA_BUFFER_READ_WRITE);
+  CqlBuffer* res = pooled("group_direct_results", out_cap * 8 * expr_count, CQLCUDA_BUFFER_READ_WRITE);
+  CqlKernel* k = kernel("cql_group_direct");
+  CqlKernel* kb = kernel("cql_group_direct_bits");
+  CqlKernel* ke = kernel("cql_group_direct_emit");
+  if (!tab || !bits || !present || !list || !repr || !cnts || !res || !k || !kb || !ke) return 0;
+  cqlcuda_kernel_set_arg_buffer(k, 0, key->buffer);
+  for (uint32_t e = 0; e < 8; e++)
+    cqlcuda_kernel_set_arg_buffer(k, 1 + e, e < expr_count && funcs[e] != CQLOPS_FUNC_COUNT ? args[e]->buffer : key->buffer);
+  cqlcuda_kernel_set_arg_buffer(k, 9, tab);
+  cqlcuda_kernel_set_arg_u64(k, 0, rows);
+  cqlcuda_kernel_set_arg_u64(k, 1, (uint64_t)(uint32_t)(int64_t)key->zone_min | ((uint64_t)R << 32));
+  cqlcuda_kernel_set_arg_u64(k, 2, (uint64_t)expr_count | ((uint64_t)func_codes << 32));
+  cqlcuda_kernel_set_arg_u64(k, 3, signed_args);
+  for (uint32_t i = 0; i < 4; i++) cqlcuda_kernel_set_arg_u64(k, 4 + i, (uint64_t)offsets[2 * i] | ((uint64_t)offsets[2 * i + 1] << 32));
+  cqlcuda_kernel_set_arg_buffer(kb, 0, tab);
+  cqlcuda_kernel_set_arg_buffer(kb, 1, bits);
+  cqlcuda_kernel_set_arg_buffer(kb, 2, present);
+  cqlcuda_kernel_set_arg_u64(kb, 0, R);
+  cqlcuda_kernel_set_arg_buffer(ke, 0, tab);
+  cqlcuda_kernel_set_arg_buffer(ke, 1, list);
+  cqlcuda_kernel_set_arg_buffer(ke, 2, present);
+  cqlcuda_kernel_set_arg_buffer(ke, 3, repr);
+  cqlcuda_kernel_set_arg_buffer(ke, 4, cnts);
+  cqlcuda_kernel_set_arg_buffer(ke, 5, res);
+  for (uint32_t i = 0; i < 8; i++) cqlcuda_kernel_set_arg_u64(ke, i, 0);
+  cqlcuda_kernel_set_arg_u64(ke, 1, (uint64_t)R << 32);
+  cqlcuda_kernel_set_arg_u64(ke, 2, (uint64_t)expr_count | ((uint64_t)func_codes << 32));
+  for (uint32_t i = 0; i < 4; i++) cqlcuda_kernel_set_arg_u64(ke, 4 + i, (uint64_t)offsets[2 * i] | ((uint64_t)offsets[2 * i + 1] << 32));
+  uint32_t groups = 0;
+  CqlBatch* b = cqlcuda_batch_begin(0, 4);
+  cqlcuda_batch_fill_range(b, tab, 0, (uint64_t)R * 4, 0);
+  cqlcuda_batch_fill_range(b, tab, (uint64_t)R * 4, (uint64_t)R * 4, 0xffffffffu);
+  for (uint32_t e = 0; e < expr_count; e++)
+  {
+    uint32_t f = funcs[e];
+    if (f == CQLOPS_FUNC_COUNT) continue;
+    uint64_t at = (uint64_t)offsets[e] * 4;
+    if (f == CQLOPS_FUNC_SUM || f == CQLOPS_FUNC_AVG) cqlcuda_batch_fill_range(b, tab, at, (uint64_t)R * 8, 0);
+    else cqlcuda_batch_fill_range(b, tab, at, (uint64_t)R * 4, f == CQLOPS_FUNC_MIN ? 0x7fffffffu : 0x80000000u);
+  }
+  cqlcuda_batch_buffer_zero(b, present, 4);
+  cqlcuda_batch_kernel_execute(b, k, (uint32_t)rows, QE_GPU_WORKGROUP_SIZE);
+  cqlcuda_batch_kernel_execute(b, kb, R, QE_GPU_WORKGROUP_SIZE);
+  if (!cqlops_bitmap_rows_enqueue(b, bits, 0, R, list))
+  {
+    cqlcuda_batch_end(b);
+    return 0;
+  }
+  cqlcuda_batch_kernel_execute(b, ke, (uint32_t)most, QE_GPU_WORKGROUP_SIZE);
+  cqlcuda_batch_buffer_read(b, present, &groups, 4);
+  if (!cqlcuda_batch_end(b)) return 0;
+  if (groups > max_groups) return refuse("more groups than the output arrays hold");
+  if (groups)
+  {
+    b = cqlcuda_batch_begin(0, (uint64_t)groups * (16 + 8ull * expr_count));
+    cqlcuda_batch_buffer_read(b, repr, out_repr_row, (uint64_t)groups * 8);
+    cqlcuda_batch_buffer_read(b, cnts, out_counts, (uint64_t)groups * 8);
+    cqlcuda_batch_buffer_read(b, res, out_results, (uint64_t)groups * 8 * expr_count);
+    if (!cqlcuda_batch_end(b)) return 0;
+  }
+  *out_group_count = groups;
+  return 1;
+}
+
 int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_count, const uint32_t* funcs, const CqlColumn* const* args,
                       const double* params, uint64_t group_hint, uint32_t path, uint64_t max_groups, uint64_t* out_group_count,
                       uint64_t* out_repr_row, uint64_t* out_counts, double* out_results, uint32_t* out_path)
@@ -595,6 +711,18 @@ int cqlops_group_hash(const CqlColumn* keys, uint32_t key_count, uint32_t expr_c
       return r;
     }
     if (path == 3) return refuse("path 3 takes one whole-number key of at most 64 values with COUNT/SUM/AVG/MIN/MAX over f32/f64 columns");
+    cqlops_note_error("");
+  }
+  if ((path == 0 || path == 4) && key_count == 1)
+  {
+    int r = group_direct(&keys[0], expr_count, funcs, args, max_groups, out_group_count, out_repr_row, out_counts, out_results);
+    if (r >= 0)
+    {
+      if (r == 1 && out_path) *out_path = 4;
+      return r;
+    }
+    if (path == 4)
+      return refuse("path 4 takes one whole-number key of 65537 to 2^24 values (at most 8 per row) with whole-number COUNT/SUM/AVG/MIN/MAX");
     cqlops_note_error("");
   }
   uint32_t key_types = 0;   /* per key: its CQL type when bound at its stored width, 0 = widened to f64 */

@@ -12,6 +12,10 @@ void cqlops_note_error(const char* why);
 /* 1 when a row count fits the kernels' 32-bit row numbers; else 0 with the reason noted */
 int cqlops_rows_fit(uint64_t rows);
 
+/* enqueues into batch b the rows of a selection bitmap of `rows` bits (bit i = row first_row + i), ascending,
+   into `list` (at most its size / 4 of them) - cql_ops.c */
+int cqlops_bitmap_rows_enqueue(CqlBatch* b, CqlBuffer* bitmap, uint64_t first_row, uint64_t rows, CqlBuffer* list);
+
 /* result pairs put in order on the device by the radix sort (cql_ops_sort.c) */
 int cqlops_sort_pairs(CqlBuffer* records, uint64_t n, uint32_t stride_words, uint32_t first_word, uint32_t second_word, int by_second,
                       uint32_t* out, uint64_t out_capacity);

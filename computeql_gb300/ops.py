@@ -626,7 +626,14 @@ def gather_rows(columns, rows=None, selection=None, count=None):
     `rows` (host row numbers), else the device buffer `selection`, else rows 0..count-1."""
     k = len(columns)
     r, sel, n = _gather_selection(rows, selection, count, min((c.rows for c in columns), default=0))
-    outs = [np.empty(max(n, 1), dtype=_GATHER_DTYPES[c.ctype]) for c in columns]
+    # one host block, each column at its offset in the device's gather area, so that it comes back in one read
+    dtypes = [np.dtype(_GATHER_DTYPES[c.ctype]) for c in columns]
+    offsets, total = [], 0
+    for dt in dtypes:
+        offsets.append(total)
+        total += (max(n, 1) * dt.itemsize + 15) & ~15
+    block = np.empty(max(total, 16), dtype=np.uint8)
+    outs = [block[o:o + max(n, 1) * dt.itemsize].view(dt) for o, dt in zip(offsets, dtypes)]
     structs = (N.CqlColumn * k)(*[c.c() for c in columns])
     ptrs = (C.c_void_p * k)(*[o.ctypes.data for o in outs])
     _check(N.load_ops().cqlops_gather_rows(structs, k, N.ptr(r) if r is not None else None, sel.handle if sel is not None else None, n, ptrs),

@@ -362,7 +362,9 @@ int cqlops_sort_rows(const CqlColumn* keys, uint32_t key_count, const uint32_t* 
    count values of column c: 4 bytes each for U32/I32/F32/DATE/ENUM columns, for narrow and sequence
    encodings (the value base + code or base + row) and for dictionary strings (the code); 8 bytes for
    U64/I64/F64/TIMESTAMP/DECIMAL; 1 byte for BOOL. Raw strings go through cqlops_gather_strings. Host rows
-   are checked against the columns' length; a device selection's rows past a column read as zero. */
+   are checked against the columns' length; a device selection's rows past a column read as zero. Outputs
+   laid out as one block - column c at the byte offset that sums, over the columns before it, count x width
+   rounded up to a multiple of 16 - come back in one read. */
 int cqlops_gather_rows(const CqlColumn* columns, uint32_t column_count, const uint32_t* rows, CqlBuffer* selection, uint64_t count,
                        void* const* out_values);
 

@@ -43,7 +43,8 @@ def test_integer_aggregates_per_group(ops, path, groups):
     w = rng.integers(-(1 << 20), 1 << 20, n).astype(np.int32)
     kc, vc, wc = ops.Column.from_numpy(key), ops.Column.from_numpy(v), ops.Column.from_numpy(w)
     res = ops.group_hash([kc], [COUNT, SUM, MIN, MAX, SUM, AVG], [None, vc, vc, vc, wc, wc], path=path)
-    assert res["path"] == (2 if path == 0 else 1)
+    # path 0 picks the direct tables for a key range past 65536 values, else the fixed-point reduce
+    assert res["path"] == ((4 if groups > 65536 else 2) if path == 0 else 1)
     got = by_key(res, [key])
     uniq = np.unique(key)
     assert len(got) == len(uniq)
@@ -275,3 +276,39 @@ def test_few_groups_many_rows(ops, groups):
         assert small["counts"][g] == m.sum() and small["results"][g, 0] == m.sum()
         assert abs(small["results"][g, 1] - exact) <= 1e-12 * exact
         assert abs(small["results"][g, 2] - exact / m.sum()) <= 1e-12 * exact / m.sum()
+
+
+@pytest.mark.parametrize("span", [70_000, 1_000_000])
+def test_direct_tables_for_a_dense_key_range(ops, span):
+    # one i32 key over a range past the dense group-by's 65536 values, not every value present, negative keys
+    # and arguments: groups in key order, each represented by its first row
+    n = 2_000_003
+    rng = np.random.default_rng(span)
+    key = (rng.integers(0, span, n) - span // 3).astype(np.int32)
+    key[:2] = [-(span // 3), span - 1 - span // 3]          # the range's ends present
+    v = rng.integers(-(1 << 30), 1 << 30, n).astype(np.int32)
+    u = rng.integers(0, 1 << 20, n).astype(np.uint32)
+    kc, vc, uc = ops.Column.from_numpy(key), ops.Column.from_numpy(v), ops.Column.from_numpy(u)
+    funcs = [COUNT, SUM, AVG, MIN, MAX, SUM]
+    res = ops.group_hash([kc], funcs, [None, vc, vc, vc, vc, uc])
+    assert res["path"] == 4
+    uniq, first, counts = np.unique(key, return_index=True, return_counts=True)
+    assert res["groups"] == len(uniq)
+    np.testing.assert_array_equal(res["repr_row"], first)
+    np.testing.assert_array_equal(res["counts"], counts)
+    order = np.argsort(key, kind="stable")
+    bounds = np.concatenate([[0], np.cumsum(counts)])
+    vsum = np.add.reduceat(v[order].astype(np.int64), bounds[:-1])
+    usum = np.add.reduceat(u[order].astype(np.int64), bounds[:-1])
+    np.testing.assert_array_equal(res["results"][:, 0], counts.astype(np.float64))
+    np.testing.assert_array_equal(res["results"][:, 1], vsum.astype(np.float64))
+    np.testing.assert_array_equal(res["results"][:, 2], vsum.astype(np.float64) / counts)
+    np.testing.assert_array_equal(res["results"][:, 3], np.minimum.reduceat(v[order], bounds[:-1]).astype(np.float64))
+    np.testing.assert_array_equal(res["results"][:, 4], np.maximum.reduceat(v[order], bounds[:-1]).astype(np.float64))
+    np.testing.assert_array_equal(res["results"][:, 5], usum.astype(np.float64))
+    # too small a result area is refused, not overrun; a range this path does not take is refused when asked for
+    with pytest.raises(ops.OpError):
+        ops.group_hash([kc], funcs, [None, vc, vc, vc, vc, uc], max_groups=len(uniq) - 1)
+    small = ops.Column.from_numpy(rng.integers(0, 1000, n).astype(np.uint32))
+    with pytest.raises(ops.OpError):
+        ops.group_hash([small], [COUNT], [None], path=4)
