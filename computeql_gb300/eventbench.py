@@ -78,10 +78,13 @@ def queries(cols, users, words):
         values = ops.gather_rows(stored + [row_numbers], selection=selection, count=n)
         return values[-1], values[:-1]
 
+    window_out = {}
+
     def window_top3():
         n = ops.scan_select([cols["u0"]], [(0, ops.CMP_GT, WINDOW_U0_GT)], selection)
-        w = ops.window_rank([cols["region"], cols["u2"]], desc=[0, 1], partitions=1, selection=selection, count=n)
-        return int((w["row_number"] <= 3).sum())
+        w = ops.window_rank([cols["region"], cols["u2"]], desc=[0, 1], partitions=1, selection=selection, count=n,
+                            want=("row_number",), out=window_out)
+        return int(np.count_nonzero(w["row_number"] <= 3))
 
     # each hash group-by of many groups writes into its own result area, kept between calls as an engine keeps
     # its result buffers (fresh arrays would cost their page faults in every call)

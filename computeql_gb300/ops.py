@@ -590,9 +590,14 @@ def having(condition, columns, literals=()):
     return keep[:g]
 
 
-def window_rank(keys, desc=None, partitions=0, selection=None, count=None):
+WINDOW_OUTPUTS = ("rows", "row_number", "rank", "dense_rank")
+
+
+def window_rank(keys, desc=None, partitions=0, selection=None, count=None, want=WINDOW_OUTPUTS, out=None):
     """ROW_NUMBER / RANK / DENSE_RANK over (PARTITION BY keys[:partitions] ORDER BY keys[partitions:])
-    -> dict of u32 arrays in window order: rows, row_number, rank, dense_rank."""
+    -> dict of u32 arrays in window order: rows, row_number, rank, dense_rank (those named in `want`; the
+    others are not read back). `out` (optional): a dict of u32 arrays kept by the caller between calls to
+    receive them (the results are views of them)."""
     k = len(keys)
     structs = (N.CqlColumn * k)(*[c.c() for c in keys])
     d = np.array(desc if desc is not None else [0] * k, dtype=np.uint32)
@@ -600,11 +605,19 @@ def window_rank(keys, desc=None, partitions=0, selection=None, count=None):
         n = selection.nbytes // 4 if count is None else count
     else:
         n = keys[0].rows
-    out = {name: np.empty(max(n, 1), dtype=np.uint32) for name in ("rows", "row_number", "rank", "dense_rank")}
+    arrays = {}
+    for name in want:
+        a = out.get(name) if out is not None else None
+        if a is None or len(a) < max(n, 1):
+            a = np.empty(max(n, 1), dtype=np.uint32)
+            if out is not None:
+                out[name] = a
+        arrays[name] = a
+    ptr = lambda name: N.ptr(arrays[name]) if name in arrays else None
     _check(N.load_ops().cqlops_window_rank(structs, k, N.ptr(d), partitions, selection.handle if selection is not None else None, n,
-                                           N.ptr(out["rows"]), N.ptr(out["row_number"]), N.ptr(out["rank"]), N.ptr(out["dense_rank"]),
-                                           max(n, 1)), "cqlops_window_rank")
-    return {name: a[:n] for name, a in out.items()}
+                                           ptr("rows"), ptr("row_number"), ptr("rank"), ptr("dense_rank"), max(n, 1)),
+           "cqlops_window_rank")
+    return {name: a[:n] for name, a in arrays.items()}
 
 
 _GATHER_DTYPES = {TYPE_U32: np.uint32, 12: np.uint32, TYPE_I32: np.int32, 9: np.int32, TYPE_F32: np.float32, TYPE_U64: np.uint64,
