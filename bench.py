@@ -563,9 +563,11 @@ def run_served(ops, workloads, t, dims):
     d1m["seg_f64"] = d1m["seg"].astype("float64")
     out = {"workload": "60/25/15 filter-aggregate / group-by / join-sort templates over resident 1M, 100M and 1B-row tables, "
                        "Poisson arrivals, 160 GB admission budget, 1 s a rate", "slo_p99_ms": 50.0}
+    # the plain server already falls behind at 5000 QPS; the served one is also offered 16000
+    rates = {"plain": [2000.0, 5000.0], "served": [2000.0, 5000.0, 16000.0]}
     for mode in ("plain", "served"):
         with contextlib.redirect_stdout(io.StringIO()):
-            lines, summary = servebench.run_mode(mode, tables, (d50, d1m), [2000.0, 5000.0], 1.0, 3, 50.0, 160 << 30)
+            lines, summary = servebench.run_mode(mode, tables, (d50, d1m), rates[mode], 1.0, 3, 50.0, 160 << 30)
         out[mode] = {"max_qps_within_slo": summary["max_qps_within_slo"],
                      "rates": [{k: r[k] for k in ("offered_qps", "completed_qps", "p50_ms", "p95_ms", "p99_ms", "failed")} for r in lines]}
     for tab in tables[:2]:
