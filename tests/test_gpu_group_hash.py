@@ -312,3 +312,37 @@ def test_direct_tables_for_a_dense_key_range(ops, span):
     small = ops.Column.from_numpy(rng.integers(0, 1000, n).astype(np.uint32))
     with pytest.raises(ops.OpError):
         ops.group_hash([small], [COUNT], [None], path=4)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_direct_tables_random_shapes(ops, seed):
+    # random dense key ranges past 65536 values, sparse use of them, and random aggregate mixes
+    rng = np.random.default_rng(200 + seed)
+    span = int(rng.integers(65_537, 3_000_000))
+    n = int(rng.integers(span // 8 + 1, 3_000_000))
+    low = int(rng.integers(-2**30, 2**30))
+    key = (rng.integers(0, span, n) + low).astype(np.int32)
+    key[0], key[-1] = low, low + span - 1
+    arrs = [rng.integers(-2**31, 2**31 - 1, n).astype(np.int32), rng.integers(0, 2**31 - 1, n).astype(np.uint32)]
+    cols = [ops.Column.from_numpy(a) for a in arrs]
+    funcs = [int(f) for f in rng.integers(0, 5, int(rng.integers(1, 9)))]
+    which = [int(w) for w in rng.integers(0, 2, len(funcs))]
+    res = ops.group_hash([ops.Column.from_numpy(key)], funcs, [None if f == COUNT else cols[w] for f, w in zip(funcs, which)])
+    assert res["path"] == 4
+    uniq, first, counts = np.unique(key, return_index=True, return_counts=True)
+    np.testing.assert_array_equal(res["repr_row"], first)
+    np.testing.assert_array_equal(res["counts"], counts)
+    order = np.argsort(key, kind="stable")
+    starts = np.concatenate([[0], np.cumsum(counts)])[:-1]
+    for e, (f, w) in enumerate(zip(funcs, which)):
+        got = res["results"][:, e]
+        if f == COUNT:
+            np.testing.assert_array_equal(got, counts.astype(np.float64))
+            continue
+        v = arrs[w][order]
+        if f in (SUM, AVG):
+            s = np.add.reduceat(v.astype(np.int64), starts).astype(np.float64)
+            np.testing.assert_array_equal(got, s if f == SUM else s / counts)
+        else:
+            m = (np.minimum if f == MIN else np.maximum).reduceat(v, starts)
+            np.testing.assert_array_equal(got, m.astype(np.float64))

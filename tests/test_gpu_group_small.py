@@ -139,3 +139,46 @@ def test_column_without_a_finite_range(ops, zone):
     res = ops.group_hash([ops.Column.from_numpy(key)], funcs, [None, xc, xc])
     assert res["path"] == 3
     check(res, key, funcs, [None, x, x], 0)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_shapes(ops, seed):
+    # random key ranges (1 to 64 values, negative keys too), column types and aggregate mixes
+    rng = np.random.default_rng(100 + seed)
+    n = int(rng.integers(1, 400_000))
+    values = int(rng.integers(1, 65))
+    low = int(rng.integers(-1000, 1000))
+    key = (rng.integers(0, values, n) + low).astype(np.int32)
+    cols, arrs = [], []
+    for c in range(int(rng.integers(1, 5))):
+        kind = rng.integers(0, 4)
+        if kind == 0:
+            a = rng.normal(size=n) * 10.0 ** int(rng.integers(-5, 8))
+        elif kind == 1:
+            a = (rng.normal(size=n) * 1000).astype(np.float32)
+        elif kind == 2:
+            a = rng.integers(-2**31, 2**31 - 1, n).astype(np.int32)
+        else:
+            a = rng.integers(0, 2**31 - 1, n).astype(np.uint32)
+        arrs.append(a)
+        cols.append(column(ops, a))
+    funcs, args, dev = [], [], []
+    for e in range(int(rng.integers(1, 9))):
+        f = int(rng.integers(0, 5))
+        c = int(rng.integers(0, len(cols)))
+        funcs.append(f)
+        args.append(None if f == COUNT else arrs[c])
+        dev.append(None if f == COUNT else cols[c])
+    if all(f == COUNT for f in funcs) or all(a is None or a.dtype.kind != "f" for a in args):
+        funcs.append(SUM)                      # one f32/f64 argument makes it this path's
+        fa = next((i for i, a in enumerate(arrs) if a.dtype.kind == "f"), None)
+        if fa is None:
+            arrs.append(rng.normal(size=n))
+            cols.append(column(ops, arrs[-1]))
+            fa = len(arrs) - 1
+        args.append(arrs[fa])
+        dev.append(cols[fa])
+        funcs, args, dev = funcs[-8:], args[-8:], dev[-8:]
+    res = ops.group_hash([ops.Column.from_numpy(key)], funcs, dev)
+    assert res["path"] == 3
+    check(res, key, funcs, args, low)
