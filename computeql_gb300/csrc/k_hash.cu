@@ -1264,7 +1264,10 @@ __global__ void __launch_bounds__(HASH_THREADS) k_group_direct(CqlLaunch a, uint
     {
       if (k[i] >= R) continue;
       atomicAdd(&cnt[k[i]], 1u);
-      atomicMin(&first[k[i]], (uint32_t)(r0 + i * step));
+      // the first row: an atomic only when a read (from L2; it can only be larger than the true value, which
+      // only falls) shows a later row, so after a key's first rows it is seldom taken
+      uint32_t r = (uint32_t)(r0 + i * step);
+      if (r < __ldcg(&first[k[i]])) atomicMin(&first[k[i]], r);
     }
 #pragma unroll 1
     for (uint32_t e = 0; e < exprs; e++)
@@ -1303,10 +1306,13 @@ __global__ void __launch_bounds__(HASH_THREADS) k_group_direct(CqlLaunch a, uint
 // 2 the number of present keys (u32, zero before); word 0 R.
 __global__ void __launch_bounds__(HASH_THREADS) k_group_direct_bits(CqlLaunch a, uint32_t R)
 {
+  __shared__ uint32_t s_present;
   const uint32_t* cnt = (const uint32_t*)a.buf[0];
   uint32_t* bits = (uint32_t*)a.buf[1];
   uint32_t* present = (uint32_t*)a.buf[2];
-  uint32_t words = (R + 31) / 32;
+  uint32_t words = (R + 31) / 32, mine = 0;
+  if (threadIdx.x == 0) s_present = 0;
+  __syncthreads();
   for (uint64_t w0 = (uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x / 32); w0 < words; w0 += (uint64_t)gridDim.x * (blockDim.x / 32))
   {
     uint64_t k = w0 * 32 + (threadIdx.x & 31);
@@ -1314,9 +1320,13 @@ __global__ void __launch_bounds__(HASH_THREADS) k_group_direct_bits(CqlLaunch a,
     if ((threadIdx.x & 31) == 0)
     {
       bits[w0] = m;
-      if (m) atomicAdd(present, (uint32_t)__popc(m));
+      mine += (uint32_t)__popc(m);
     }
   }
+  // one atomic a CTA on the shared count (a global atomic a warp word would all meet on one address)
+  if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&s_present, mine);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_present) atomicAdd(present, s_present);
 }
 
 // cql_group_direct_emit: the groups in key order in the caller's layout: binding 0 the tables, 1 the present
