@@ -1263,11 +1263,10 @@ __global__ void __launch_bounds__(HASH_THREADS) k_group_direct(CqlLaunch a, uint
     for (uint32_t i = 0; i < DIRECT_ROWS; i++)
     {
       if (k[i] >= R) continue;
+      // atomics whose results are not read: the L2 performs them, the thread does not wait (a read of the
+      // first row before its atomic would cost the same L2 operation plus the wait)
       atomicAdd(&cnt[k[i]], 1u);
-      // the first row: an atomic only when a read (from L2; it can only be larger than the true value, which
-      // only falls) shows a later row, so after a key's first rows it is seldom taken
-      uint32_t r = (uint32_t)(r0 + i * step);
-      if (r < __ldcg(&first[k[i]])) atomicMin(&first[k[i]], r);
+      atomicMin(&first[k[i]], (uint32_t)(r0 + i * step));
     }
 #pragma unroll 1
     for (uint32_t e = 0; e < exprs; e++)
