@@ -80,16 +80,33 @@ __global__ void __launch_bounds__(FIX_THREADS) k_fixed_scale(CqlLaunch a, uint64
     scale = max(scale, s);
     largest = max(largest, f.mag_bits);
   }
-  // one atomic of each kind per warp
+  // reduced over the warp, then the CTA, then one atomic of each kind a CTA (atomics a warp would all meet on
+  // the same three words)
+  __shared__ uint32_t s_failed, s_scale;
+  __shared__ unsigned long long s_largest;
+  if (threadIdx.x == 0)
+  {
+    s_failed = 0;
+    s_scale = 0;
+    s_largest = 0;
+  }
+  __syncthreads();
   uint32_t any_failed = __any_sync(0xffffffffu, failed);
   int wscale = __reduce_max_sync(0xffffffffu, (unsigned)scale);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) largest = max(largest, __shfl_xor_sync(0xffffffffu, largest, o));
   if ((threadIdx.x & 31u) == 0)
   {
-    if (any_failed) atomicOr(&result[1], 1u);
-    atomicMax(&result[0], (unsigned)wscale);
-    atomicMax((unsigned long long*)(result + 2), largest);
+    if (any_failed) s_failed = 1u;
+    if (wscale) atomicMax(&s_scale, (unsigned)wscale);
+    if (largest) atomicMax(&s_largest, largest);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    if (s_failed) atomicOr(&result[1], 1u);
+    if (s_scale) atomicMax(&result[0], s_scale);
+    if (s_largest) atomicMax((unsigned long long*)(result + 2), s_largest);
   }
 }
 
@@ -171,11 +188,28 @@ __global__ void __launch_bounds__(FIX_THREADS) k_key_range(CqlLaunch a, uint64_t
     hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
   }
   bool any_bad = __any_sync(0xffffffffu, bad);
+  // over the CTA first, then one atomic of each kind a CTA
+  __shared__ long long s_lo, s_hi;
+  __shared__ uint32_t s_bad;
+  if (threadIdx.x == 0)
+  {
+    s_lo = LLONG_MAX;
+    s_hi = LLONG_MIN;
+    s_bad = 0;
+  }
+  __syncthreads();
   if ((threadIdx.x & 31u) == 0)
   {
-    atomicMin(&result[0], lo);
-    atomicMax(&result[1], hi);
-    if (any_bad) atomicOr((unsigned*)&result[2], 1u);
+    atomicMin(&s_lo, lo);
+    atomicMax(&s_hi, hi);
+    if (any_bad) s_bad = 1u;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    atomicMin(&result[0], s_lo);
+    atomicMax(&result[1], s_hi);
+    if (s_bad) atomicOr((unsigned*)&result[2], 1u);
   }
 }
 

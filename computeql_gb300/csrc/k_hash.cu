@@ -1442,7 +1442,12 @@ __global__ void __launch_bounds__(HASH_THREADS) k_finite_magnitude(CqlLaunch a, 
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
-  if ((threadIdx.x & 31u) == 0 && best) atomicMax((unsigned long long*)a.buf[1], best);
+  __shared__ unsigned long long s_best;
+  if (threadIdx.x == 0) s_best = 0;
+  __syncthreads();
+  if ((threadIdx.x & 31u) == 0 && best) atomicMax(&s_best, best);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_best) atomicMax((unsigned long long*)a.buf[1], s_best);
 }
 
 static int launch_finite_magnitude(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)

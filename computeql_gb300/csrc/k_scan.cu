@@ -646,7 +646,16 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_filter(CqlLaunch a, uint6
     }
     __syncthreads();
   }
-  if (bitmap_mode && lane == 0 && bitmap_count) atomicAdd(out_count, bitmap_count);
+  // one atomic a CTA (a warp's would all meet on the one count word)
+  if (bitmap_mode)
+  {
+    __shared__ uint32_t s_count;
+    if (threadIdx.x == 0) s_count = 0;
+    __syncthreads();
+    if (lane == 0 && bitmap_count) atomicAdd(&s_count, bitmap_count);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_count) atomicAdd(out_count, s_count);
+  }
 }
 
 static int launch_scan_filter(const CqlLaunch& a, uint32_t gws, uint32_t lws, cudaStream_t stream)

@@ -12,6 +12,10 @@ like the configurations the operators serve:
   sort_subset   ORDER BY an f64 measure over the ~200k rows a filter keeps of a 10M-row table
   fixed         GROUP BY region (50) with SUM/MIN/MAX of a 2-place decimal f64 column
   hash_group    GROUP BY user_id (1M groups) with COUNT and SUM of an f64 measure over 10M rows
+  group_small   GROUP BY a key of 5 values with SUM(m0), AVG(m1), MIN(m1), MAX(m1) of two lognormal f64 measures over
+                `rows` rows (the one-pass small-key form)
+  group_direct  GROUP BY a key of 1M values with COUNT and SUM of a u32 column over `rows` rows (the tables indexed
+                by key)
   hll           APPROX_COUNT_DISTINCT(session) over 10M rows (4M distinct)
   hash_join     a 1M-row build side (unique keys) probed by 10M rows, pairs counted
   dense_10k     GROUP BY amount (10k groups) COUNT, SUM(region) over `rows` rows of the seed-0 fact table
@@ -32,8 +36,8 @@ import numpy as np
 
 from . import build, native, ops, workloads
 
-OPS = ["sort", "sort_f64_2", "sort_subset", "fixed", "hash_group", "hll", "hash_join", "join_small", "zone_map", "batch", "materialize",
-       "dense_10k"]
+OPS = ["sort", "sort_f64_2", "sort_subset", "fixed", "hash_group", "group_small", "group_direct", "hll", "hash_join", "join_small",
+       "zone_map", "batch", "materialize", "dense_10k"]
 
 
 def _profile():
@@ -109,6 +113,18 @@ def run(op, rows, reps):
         out = ops.HashOutputs(2_000_000, 2)      # the result area kept between calls, as an engine keeps it
         fn = lambda: ops.group_hash([user], [0, 1], [None, measure], group_hint=1_000_000, out=out)
         n, nbytes = total, total * 12
+    elif op == "group_small":
+        key = ops.Column.splitmix(rows, 7, 1, 0, 5)
+        m0 = ops.Column.from_numpy(_lognormal_f64(rows, 4))
+        m1 = ops.Column.from_numpy(_lognormal_f64(rows, 5))
+        fn = lambda: ops.group_hash([key], [1, 2, 3, 4], [m0, m1, m1, m1], group_hint=5)
+        n, nbytes = rows, rows * 20
+    elif op == "group_direct":
+        key = ops.Column.splitmix(rows, 8, 2, 0, 1_000_000)
+        u = ops.Column.splitmix(rows, 8, 2, 1, 1 << 20)
+        out = ops.HashOutputs(2_000_000, 2)
+        fn = lambda: ops.group_hash([key], [0, 1], [None, u], group_hint=1_000_000, out=out)
+        n, nbytes = rows, rows * 8
     elif op == "hll":
         total = 10_000_000
         session = ops.Column.splitmix(total, 0, 2, 1, 4_000_000)
