@@ -14,7 +14,7 @@ import pytest
 import oracle
 
 pytestmark = pytest.mark.gpu
-COUNT, SUM, MIN, MAX = 0, 1, 3, 4
+COUNT, SUM, AVG, MIN, MAX = 0, 1, 2, 3, 4
 N = 1_000_003
 
 
@@ -30,7 +30,8 @@ def env(gpu):
     dk = np.arange(1_000_000, dtype=np.uint32)
     seg = oracle.splitmix_u32(1_000_000, workloads.DIM1M_SEED, 1, 0, 20).astype(np.float64)
     prog = ops.Program("(or (< flag 3) (and (> amount 9000) (= region 7)))", {"flag": t.flag, "amount": t.amount, "region": t.region})
-    return ops, gpu.load_cuda(), t, h, key, val, dk, seg, prog, hkey
+    measure = ops.Column.from_numpy(rng.lognormal(3.0, 1.0, N))
+    return ops, gpu.load_cuda(), t, h, key, val, dk, seg, prog, hkey, measure
 
 
 def by_key(res, hkey):
@@ -41,7 +42,13 @@ def by_key(res, hkey):
 
 
 def queries(env):
-    ops, _, t, _, key, val, dk, seg, prog, hkey = env
+    ops, _, t, _, key, val, dk, seg, prog, hkey, measure = env
+
+    def select_then_sort():
+        sel = ops.DeviceBuffer(N * 4)
+        n = ops.scan_select([t.flag], [(0, ops.CMP_LT, 2)], sel)
+        return n, ops.sort_rows([t.amount], selection=sel, count=n)
+
     return {
         "aggregate_global": lambda: ops.aggregate_global([t.amount]),
         "scan_simple_rows": lambda: ops.scan_simple([t.flag], [(0, ops.CMP_LT, 2)], want_rows=True),
@@ -52,6 +59,9 @@ def queries(env):
         "join_aggregate": lambda: {k: v for k, v in ops.join_aggregate(t.amount, [SUM, COUNT], [t.amount, None], dk,
                                                                       group_values=[seg]).items() if k != "strategy"},
         "sort_rows": lambda: ops.sort_rows([key]),
+        # the one-pass small-key GROUP BY over an f64 measure, and a filter's rows kept on the device for a sort
+        "group_small": lambda: ops.group_hash([t.region], [SUM, AVG, MIN, MAX], [measure] * 4),
+        "scan_select_sort": select_then_sort,
     }
 
 
@@ -81,7 +91,7 @@ def run(fn):
 
 
 @pytest.mark.parametrize("name", ["aggregate_global", "scan_simple_rows", "scan_filter_generated", "group_dense", "group_hash",
-                                  "join_aggregate", "sort_rows"])
+                                  "join_aggregate", "sort_rows", "group_small", "scan_select_sort"])
 def test_every_allocation_fails_cleanly(env, name):
     ops, lib = env[0], env[1]
     fn = queries(env)[name]
