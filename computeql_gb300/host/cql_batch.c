@@ -334,6 +334,12 @@ static const char* BATCH_PRELUDE =
   "__device__ __forceinline__ bool cql_bf(const Thr* t, float v) { float x = __uint_as_float((u32)t->a); u32 op = t->c; bool s = t->d != 0u;\n"
   "  if (op == 5u) return s ? v < x : v <= x; if (op == 7u) return v <= x; if (op == 6u) return s ? v > x : v >= x; if (op == 8u) return v >= x;\n"
   "  if (op == 3u) return v == x; return v != x; }\n"
+  /* the warp's sum of a 64-bit value, mod 2^64: four independent warp reductions of its 16-bit slices (a
+     32-lane sum of 16-bit values fits in 21 bits), instead of a chain of five 64-bit shuffles and adds */
+  "__device__ __forceinline__ long long cql_wsum64(long long v) { const u64 u = (u64)v;\n"
+  "  const u64 s0 = __reduce_add_sync(0xffffffffu, (u32)(u & 0xffffu)), s1 = __reduce_add_sync(0xffffffffu, (u32)((u >> 16) & 0xffffu));\n"
+  "  const u64 s2 = __reduce_add_sync(0xffffffffu, (u32)((u >> 32) & 0xffffu)), s3 = __reduce_add_sync(0xffffffffu, (u32)(u >> 48));\n"
+  "  return (long long)(s0 + (s1 << 16) + (s2 << 32) + (s3 << 48)); }\n"
   "__device__ __forceinline__ double cql_i64d(u64 x) { double u = (double)(u32)(x >> 32) * 4294967296.0 + (double)(u32)x; return (x >> 63) ? u - 18446744073709551616.0 : u; }\n"
   /* x * 2^sh rounded to the nearest integer (ties to even), from the bits of x in integer arithmetic:
      x = m * 2^e, so x * 2^sh = m * 2^(e + sh). Exact, as the product of x by the power of two is; a
@@ -547,7 +553,7 @@ static char* batch_source(char** shape_exprs, const uint32_t* shape_sites, uint3
       bput(&b, "      if (sc == %du && m) {\n#pragma unroll\n        for (u32 k = 0; k < RPT; k++) if ((m >> k) & 1u) sv += fx%d[k];\n      }\n", sum_cols[i],
            sum_cols[i]);
     bput(&b,
-         "      if (sc != 0xffffffffu) { for (int o = 16; o > 0; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o); }\n"
+         "      if (sc != 0xffffffffu) sv = cql_wsum64(sv);\n"
          "      if (lane == 0u) { cacc[q] += cnt; acc[q] += sv; }\n"
          "    }\n");
   }
@@ -798,7 +804,7 @@ static char* batch_source_tiled(char** shape_exprs, const uint32_t* shape_sites,
        "      default: break;\n"
        "      }\n"
        "      cnt = __reduce_add_sync(0xffffffffu, cnt);\n"
-       "      if (fxp) { for (int o = 16; o > 0; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o); }\n"
+       "      if (fxp) sv = cql_wsum64(sv);\n"
        "      if (lane == 0u) { atomicAdd(&s_cnt[q], (u64)cnt); if (sv) atomicAdd(&s_sum[q], (u64)sv); }\n"
        "    }\n"
        "    __syncthreads();\n"
