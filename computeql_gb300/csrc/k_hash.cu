@@ -963,9 +963,9 @@ static int launch_group_finish(const CqlLaunch& a, uint32_t gws, uint32_t lws, c
 //
 // A SUM is exact in fixed point: each value x of a column becomes the whole number q = round(x * 2^s),
 // with s chosen from the column's range so that |q| < 2^61 (s = 0 for whole-number columns, which are then
-// exact), and the q are added as 96-bit two's-complement numbers in three 32-bit limbs (shared atomics
-// with the carries passed up, as the dense group-by's 64-bit sums do), then as 128-bit numbers in the
-// output. The host turns the total back into a double, rounding once: the f64 SUM is the exact sum of the
+// exact), and the q are added as 96-bit two's-complement numbers (a thread's own table: a u64 low part and
+// a u32 high part; tables shared by threads: three 32-bit limbs, shared atomics with the carries passed up,
+// as the dense group-by's 64-bit sums do), then as 128-bit numbers in the output. The host turns the total back into a double, rounding once: the f64 SUM is the exact sum of the
 // values rounded to 2^-s, whose error is below rows * 2^(E-62) for values below 2^E - far inside the
 // 1e-12 the sum is held to, and independent of the order the rows are met in. NaN and infinite values are
 // kept out of the sum and flagged (NaN 1, +inf 2, -inf 4), so that the host gives the IEEE result.
@@ -979,8 +979,9 @@ static int launch_group_finish(const CqlLaunch& a, uint32_t gws, uint32_t lws, c
 //                     zero before)
 // words: 0 rows, 2 the smallest key (bits), 4 V, 6 the columns, 8 their CQL types (4 bits each: U32, I32,
 // F32, F64), 10 per column 1 = SUM (bits 0-7) and 1 = MIN/MAX (bits 8-15), slots 6 and 7 the columns'
-// scales s (signed 16 bits each, columns 0-3 then 4-7). Dynamic shared memory: `copies` private tables of V counts and 3 limbs per
-// summed column and value; with one table a thread (OWN) they are updated without atomics.
+// scales s (signed 16 bits each, columns 0-3 then 4-7). Dynamic shared memory: `copies` private tables of
+// V counts and one sum per summed column and value (laid out below the kernel's head); with one table a
+// thread (OWN) they are updated without atomics.
 
 #define SMALL_VALUES 64
 #define SMALL_COLUMNS 8
