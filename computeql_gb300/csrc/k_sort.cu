@@ -30,9 +30,9 @@
 //                     (result pairs - join or scan output - put in order on the device by the sort above)
 //
 // A tile is 8 warps x 16 rounds x 32 rows = 4096 rows. The scatter ranks a row within its tile in input
-// order: eight ballots find the lanes of a round with the same digit, per-warp digit counters carry
-// the rounds, and a prefix over the warps orders the warps; the global base of (digit, tile) comes from
-// the offsets kernel: the digit's place in the pass's output (the totals of the digits below it, counted
+// order: eight ballots or the match instruction (alternate rounds) find the lanes of a round with the same
+// digit, per-warp digit counters carry the rounds, and a prefix over the warps orders the warps; the global
+// base of (digit, tile) comes from the offsets kernel: the digit's place in the pass's output (the totals of the digits below it, counted
 // while the histogram is made) plus the digit's counts in the tiles before.
 #include "cql_internal.cuh"
 #include <algorithm>
